@@ -1,0 +1,229 @@
+"""cryoim_gb300 — GB300 (sm_103a) implementation of cryoIM's icosahedral
+projection-matching refinement loop (icosprocess modes 4/5/1 and proc_icos).
+
+The compute lives in libcryoim_gb300.so behind the C ABI of include/cryoim.h; this
+package is the host-side mirror of the reference's drivers for Python callers (tests,
+bench).  Every call goes to the CUDA library; nothing here computes on the CPU.
+"""
+from __future__ import annotations
+
+import ctypes as C
+
+import numpy as np
+
+from . import _abi
+from ._abi import (PARTICLE_DTYPE, TEMPLATE_DTYPE, CryoimError, Params, call, load, ptr)
+
+__all__ = ["Context", "Params", "PARTICLE_DTYPE", "TEMPLATE_DTYPE", "CryoimError", "default_params",
+           "icos_ops", "asu_fold", "equalort", "transform_ort", "load"]
+
+
+def default_params(fftsize: int, **kw) -> Params:
+    """Reference defaults for a stack of nx=fftsize (0initialvalue.f90), with keyword
+    overrides by icosprocess key name (apix, minRes, maxRes, searchstep, ...), then
+    the derived values of 0calc_initialvalues.f90."""
+    p = Params()
+    call("cryoim_params_default", C.byref(p), int(fftsize))
+    alias = {"minRes": "min_res", "maxRes": "max_res", "applyCTF": "apply_ctf", "Cs": "cs",
+             "PR_threshold": "pr_threshold", "boundX": "boundx", "Ncycle": "ncycle",
+             "Bfactor": "bfactor"}
+    for k, v in kw.items():
+        k = alias.get(k, k)
+        if not hasattr(p, k):
+            raise KeyError(k)
+        setattr(p, k, v)
+    call("cryoim_params_derive", C.byref(p))
+    return p
+
+
+def particles(n: int) -> np.ndarray:
+    return np.zeros(n, dtype=PARTICLE_DTYPE)
+
+
+def templates(n: int) -> np.ndarray:
+    return np.zeros(n, dtype=TEMPLATE_DTYPE)
+
+
+class Context:
+    """One device context (cryoim_ctx): params, resident templates, scratch, stream."""
+
+    def __init__(self, device: int = 0, params: Params | None = None):
+        load()
+        h = C.c_void_p()
+        call("cryoim_ctx_create", int(device), C.byref(h))
+        self._h = h
+        self.params: Params | None = None
+        if params is not None:
+            self.set_params(params)
+
+    # -- lifetime -------------------------------------------------------------
+    def close(self) -> None:
+        if getattr(self, "_h", None) is not None and self._h.value:
+            call("cryoim_ctx_destroy", self._h)
+            self._h = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    # -- configuration --------------------------------------------------------
+    def set_params(self, p: Params) -> None:
+        call("cryoim_set_params", self._h, C.byref(p))
+        self.params = p
+
+    def set_stream(self, stream_handle: int | None) -> None:
+        call("cryoim_ctx_set_stream", self._h, C.c_void_p(stream_handle) if stream_handle else None)
+
+    def set_batch(self, b: int) -> None:
+        call("cryoim_ctx_set_batch", self._h, int(b))
+
+    def set_profiling(self, on: bool) -> None:
+        call("cryoim_ctx_set_profiling", self._h, int(bool(on)))
+
+    def kernel_time(self) -> tuple[float, int]:
+        """(total ms, launches) of the hot search kernel since the last call."""
+        ms, n = C.c_double(), C.c_int64()
+        call("cryoim_ctx_kernel_time", self._h, C.byref(ms), C.byref(n))
+        return ms.value, n.value
+
+    def search_terms(self) -> float:
+        t = C.c_double()
+        call("cryoim_search_terms", self._h, C.byref(t))
+        return t.value
+
+    # -- templates ------------------------------------------------------------
+    def project_templates(self, map3d: np.ndarray, tmpl: np.ndarray) -> np.ndarray:
+        n = self.params.fftsize
+        m = np.ascontiguousarray(map3d, dtype=np.float32)
+        t = np.ascontiguousarray(tmpl, dtype=TEMPLATE_DTYPE)
+        out = np.zeros((len(t), n, n), np.float32)
+        call("cryoim_project_templates", self._h, ptr(m), ptr(t), len(t), ptr(out))
+        return out
+
+    def load_templates(self, imgs: np.ndarray, tmpl: np.ndarray) -> None:
+        im = np.ascontiguousarray(imgs, dtype=np.float32)
+        t = np.ascontiguousarray(tmpl, dtype=TEMPLATE_DTYPE)
+        call("cryoim_load_templates", self._h, ptr(im), ptr(t), len(t))
+
+    # -- mode 4 ---------------------------------------------------------------
+    def search_grid(self) -> tuple[int, int, int, int]:
+        a = [C.c_int32() for _ in range(4)]
+        call("cryoim_search_grid", self._h, *[C.byref(x) for x in a])
+        return tuple(x.value for x in a)
+
+    def globesearch(self, imgs, parts: np.ndarray, want_pr_array: bool = False):
+        """Global search; parts (PARTICLE_DTYPE) is updated in place.  imgs may be a
+        host array (P, nx, nx) or a device pointer (int) for the _device entry point."""
+        assert parts.dtype == PARTICLE_DTYPE and parts.flags["C_CONTIGUOUS"]
+        pra = None
+        if want_pr_array:
+            nth, nph, nom, _ = self.search_grid()
+            pra = np.zeros((len(parts), nth + 1, 2 * nph + 1, nom), np.float32)
+        if isinstance(imgs, int):
+            call("cryoim_globesearch_device", self._h, C.c_void_p(imgs), ptr(parts), len(parts), ptr(pra))
+        else:
+            im = np.ascontiguousarray(imgs, dtype=np.float32)
+            call("cryoim_globesearch", self._h, ptr(im), ptr(parts), len(parts), ptr(pra))
+        return pra
+
+    def prscore_omega(self, ft_a, ft_b, fcut0, ctf, theta: float, phi: float) -> np.ndarray:
+        nom = int(360.0 / np.float32(self.params.searchstep))
+        out = np.zeros(nom, np.float32)
+        a = np.ascontiguousarray(ft_a, np.float32)
+        b = np.ascontiguousarray(ft_b, np.float32)
+        f = np.ascontiguousarray(fcut0, np.float32)
+        c = None if ctf is None else np.ascontiguousarray(ctf, np.float32)
+        call("cryoim_prscore_omega", self._h, ptr(a), ptr(b), ptr(f), ptr(c), float(theta), float(phi), ptr(out))
+        return out
+
+    # -- mode 5 ---------------------------------------------------------------
+    def refine(self, imgs, parts: np.ndarray) -> None:
+        assert parts.dtype == PARTICLE_DTYPE and parts.flags["C_CONTIGUOUS"]
+        if isinstance(imgs, int):
+            call("cryoim_refine_device", self._h, C.c_void_p(imgs), ptr(parts), len(parts))
+        else:
+            im = np.ascontiguousarray(imgs, dtype=np.float32)
+            call("cryoim_refine", self._h, ptr(im), ptr(parts), len(parts))
+
+    def prscore(self, ft_a, ft_b, fcut0, ctf, theta, phi, omega, x, y) -> float:
+        out = C.c_float()
+        a = np.ascontiguousarray(ft_a, np.float32)
+        b = np.ascontiguousarray(ft_b, np.float32)
+        f = np.ascontiguousarray(fcut0, np.float32)
+        c = None if ctf is None else np.ascontiguousarray(ctf, np.float32)
+        call("cryoim_prscore", self._h, ptr(a), ptr(b), ptr(f), ptr(c), float(theta), float(phi),
+             float(omega), float(x), float(y), C.byref(out))
+        return out.value
+
+    # -- mode 1 ---------------------------------------------------------------
+    def rec_begin(self) -> None:
+        call("cryoim_rec_begin", self._h)
+
+    def rec_insert(self, imgs, parts: np.ndarray) -> int:
+        used = C.c_int32()
+        p = np.ascontiguousarray(parts, dtype=PARTICLE_DTYPE)
+        if isinstance(imgs, int):
+            call("cryoim_rec_insert_device", self._h, C.c_void_p(imgs), ptr(p), len(p), C.byref(used))
+        else:
+            im = np.ascontiguousarray(imgs, dtype=np.float32)
+            call("cryoim_rec_insert", self._h, ptr(im), ptr(p), len(p), C.byref(used))
+        return used.value
+
+    def rec_finish(self) -> np.ndarray:
+        n = self.params.fftsize
+        out = np.zeros((n, n, n), np.float32)
+        call("cryoim_rec_finish", self._h, ptr(out))
+        return out
+
+    def rec_get_partial(self):
+        R = self.params.max_r
+        t = 2 * R + 1
+        fa, fb, wg = (np.zeros((R + 1, t, t), np.float32) for _ in range(3))
+        call("cryoim_rec_get_partial", self._h, ptr(fa), ptr(fb), ptr(wg))
+        return fa, fb, wg
+
+    # -- central sections ----------------------------------------------------
+    def central_sections(self, ft_re, ft_im, eulers) -> tuple[np.ndarray, np.ndarray]:
+        n = self.params.fftsize
+        e = np.ascontiguousarray(eulers, np.float32).reshape(-1, 3)
+        re = np.ascontiguousarray(ft_re, np.float32)
+        im = np.ascontiguousarray(ft_im, np.float32)
+        ore = np.zeros((len(e), n, n), np.float32)
+        oim = np.zeros((len(e), n, n), np.float32)
+        call("cryoim_central_sections", self._h, ptr(re), ptr(im), ptr(e), len(e), ptr(ore), ptr(oim))
+        return ore, oim
+
+
+# -- proc_icos (host geometry in the library) ----------------------------------
+def icos_ops() -> np.ndarray:
+    out = np.zeros((60, 3, 3), np.float32)
+    call("cryoim_icos_ops", ptr(out))
+    return out
+
+
+def asu_fold(theta: float, phi: float, omega: float) -> tuple[float, float, float]:
+    t, p, o = C.c_float(theta), C.c_float(phi), C.c_float(omega)
+    call("cryoim_asu_fold", C.byref(t), C.byref(p), C.byref(o))
+    return t.value, p.value, o.value
+
+
+def equalort(theta: float, phi: float, omega: float) -> np.ndarray:
+    out = np.zeros((60, 3), np.float32)
+    call("cryoim_equalort", float(theta), float(phi), float(omega), ptr(out))
+    return out
+
+
+def transform_ort(to: int, theta, phi, omega):
+    t = np.ascontiguousarray(theta, np.float32).copy()
+    p = np.ascontiguousarray(phi, np.float32).copy()
+    o = np.ascontiguousarray(omega, np.float32).copy()
+    call("cryoim_transform_ort", int(to), ptr(t), ptr(p), ptr(o), len(t))
+    return t, p, o

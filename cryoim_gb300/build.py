@@ -1,0 +1,83 @@
+"""Build libcryoim_gb300.so (sm_103a) and the CPU oracle, in-tree.
+
+The CUDA library is compiled with nvcc directly (no torch extension: the C ABI in
+include/cryoim.h carries no torch types).  Translation units:
+
+* prep.cu  -- -fmad=false: FP32 expressions round where the Fortran reference rounds;
+* score.cu -- hot scoring kernels, multiply-add contraction allowed;
+* api.cu   -- context, drivers, C ABI (host code built with -ffp-contract=off).
+"""
+from __future__ import annotations
+
+import os
+import shutil
+import subprocess
+import sys
+from concurrent.futures import ThreadPoolExecutor
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(HERE)
+CSRC = os.path.join(HERE, "csrc")
+OUT = os.path.join(HERE, "_lib")
+LIBNAME = "libcryoim_gb300.so"
+ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
+
+
+def nvcc() -> str:
+    for cand in (os.environ.get("NVCC"), "/usr/local/cuda/bin/nvcc", shutil.which("nvcc")):
+        if cand and os.path.exists(cand):
+            return cand
+    raise RuntimeError("nvcc not found")
+
+
+def _run(cmd: list[str]) -> None:
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError("command failed:\n  " + " ".join(cmd) + "\n" + r.stdout + r.stderr)
+    if r.stderr.strip():
+        sys.stderr.write(r.stderr)
+
+
+UNITS = {
+    "prep.cu": ["-fmad=false"],
+    "score.cu": [],
+    "api.cu": [],
+}
+
+
+def build_library(verbose: bool = False, extra: list[str] | None = None) -> str:
+    os.makedirs(OUT, exist_ok=True)
+    common = ARCH + ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC,-ffp-contract=off",
+                     "-I", os.path.join(ROOT, "include")] + (extra or [])
+    objs = []
+    cmds = []
+    for src, flags in UNITS.items():
+        obj = os.path.join(OUT, src.replace(".cu", ".o"))
+        objs.append(obj)
+        cmds.append([nvcc(), "-c", os.path.join(CSRC, src), "-o", obj] + common + flags)
+    with ThreadPoolExecutor(max_workers=len(cmds)) as ex:
+        list(ex.map(_run, cmds))
+    lib = os.path.join(OUT, LIBNAME)
+    _run([nvcc(), "-shared", "-o", lib] + objs + ARCH + ["-lcufft", "-lcudart"])
+    if verbose:
+        print("built", lib)
+    return lib
+
+
+def build_oracle() -> str:
+    """The CPU oracle (test infrastructure; never linked into the library)."""
+    odir = os.path.join(ROOT, "oracle")
+    _run(["make", "-s", "-C", odir])
+    return os.path.join(odir, "_build", "libcryoim_oracle.so")
+
+
+def build_all(verbose: bool = False) -> None:
+    with ThreadPoolExecutor(max_workers=2) as ex:
+        f1 = ex.submit(build_library, verbose)
+        f2 = ex.submit(build_oracle)
+        f1.result()
+        f2.result()
+
+
+if __name__ == "__main__":
+    build_all(verbose=True)

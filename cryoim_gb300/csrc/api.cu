@@ -1,0 +1,1186 @@
+// api.cu — context, drivers and the C ABI of libcryoim_gb300.so (include/cryoim.h).
+//
+// Host-side logic mirrors the reference drivers: ort_globesearch.f90 (mode 4),
+// ort_refinement.f90 (mode 5), reconstruct.f90 / reconstruct_substep.f90 (mode 1),
+// load_template.f90, and proc_icos's orientation transforms.  Device work runs on one
+// CUDA stream per context; particles are processed in batches of `batch` images.
+#include <cuda_runtime.h>
+#include <cufft.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <map>
+#include <string>
+#include <vector>
+
+#include "../../include/cryoim.h"
+#include "geom.cuh"
+#include "kernels.h"
+
+using namespace cryoim;
+
+namespace {
+
+thread_local std::string g_err = "";
+
+int fail(int code, const char* fmt, ...) {
+    char buf[512];
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(buf, sizeof(buf), fmt, ap);
+    va_end(ap);
+    g_err = buf;
+    return code;
+}
+
+#define CK(x)                                                                                   \
+    do {                                                                                        \
+        cudaError_t e__ = (x);                                                                  \
+        if (e__ != cudaSuccess)                                                                 \
+            return fail(CRYOIM_ERR_CUDA, "%s failed: %s (%s:%d)", #x, cudaGetErrorString(e__), \
+                        __FILE__, __LINE__);                                                    \
+    } while (0)
+#define CKF(x)                                                                                \
+    do {                                                                                      \
+        cufftResult r__ = (x);                                                                \
+        if (r__ != CUFFT_SUCCESS)                                                             \
+            return fail(CRYOIM_ERR_CUDA, "%s failed: cufft %d (%s:%d)", #x, (int)r__, __FILE__, \
+                        __LINE__);                                                            \
+    } while (0)
+
+// ---------------------------------------------------------------------------
+// host geometry
+// ---------------------------------------------------------------------------
+
+// The 60 operators, generated from the group generators of
+// proc_icos/SRC/icos2f_operation_matrix.f90:13-55 (in R), generator order.
+template <class R> void gen_ops(R* r) {
+    const R d2r = R(4) * std::atan2(R(1), R(1)) / R(180);
+    R a5 = R(72) * d2r;
+    R v = std::acos(std::cos(R(60) * d2r) / std::sin(R(36) * d2r));
+    R rz5[9] = {std::cos(a5), -std::sin(a5), 0, std::sin(a5), std::cos(a5), 0, 0, 0, 1};
+    R ryv[9] = {std::cos(v), 0, std::sin(v), 0, 1, 0, -std::sin(v), 0, std::cos(v)};
+    R ryvt[9] = {ryv[0], ryv[3], ryv[6], ryv[1], ryv[4], ryv[7], ryv[2], ryv[5], ryv[8]};
+    auto mm = [](const R* a, const R* b, R* c) {
+        R t[9];
+        for (int i = 0; i < 3; ++i)
+            for (int j = 0; j < 3; ++j) {
+                R s = a[i * 3] * b[j];
+                s = s + a[i * 3 + 1] * b[3 + j];
+                s = s + a[i * 3 + 2] * b[6 + j];
+                t[i * 3 + j] = s;
+            }
+        std::memcpy(c, t, sizeof(t));
+    };
+    R t[9];
+    mm(rz5, ryvt, t);
+    mm(ryv, t, rz5);
+    const R rx2[9] = {1, 0, 0, 0, -1, 0, 0, 0, -1};
+    const R ry2[9] = {-1, 0, 0, 0, 1, 0, 0, 0, -1};
+    const R r3[9] = {0, 0, 1, 1, 0, 0, 0, 1, 0};
+    for (int k = 0; k < 9; ++k) r[k] = (k % 4 == 0) ? R(1) : R(0);
+    for (int i = 1; i < 5; ++i) mm(r + (i - 1) * 9, rz5, r + i * 9);
+    for (int i = 5; i < 10; ++i) mm(rx2, r + (i - 5) * 9, r + i * 9);
+    for (int i = 10; i < 20; ++i) mm(ry2, r + (i - 10) * 9, r + i * 9);
+    for (int i = 20; i < 60; ++i) mm(r3, r + (i - 20) * 9, r + i * 9);
+}
+
+// icosprocess/SRC/icos2f_sym_mat.f90:5-243 holds the same 60 matrices in another order;
+// entry k of that table is generator element TABLE_FROM_GEN[k].
+const int TABLE_FROM_GEN[60] = {
+    0, 26, 34, 48, 42, 24, 56, 28, 17, 23, 6, 52, 49, 41, 58, 9, 37, 18, 32, 54,
+    36, 1, 2, 3, 4, 8, 29, 35, 45, 40, 20, 31, 7, 38, 22, 55, 30, 59, 51, 25,
+    50, 19, 47, 43, 16, 27, 13, 12, 33, 15, 44, 14, 5, 11, 46, 57, 53, 21, 10, 39};
+
+const float* table_ops() {
+    static float tab[540];
+    static bool init = false;
+    if (!init) {
+        double g[540];
+        gen_ops<double>(g);
+        const double cand[5] = {0.0, 0.5, 1.0, 0.80901699437494742, 0.30901699437494742};
+        for (int k = 0; k < 60; ++k)
+            for (int e = 0; e < 9; ++e) {
+                double x = g[TABLE_FROM_GEN[k] * 9 + e], ax = std::fabs(x), best = 0.0;
+                for (double c : cand)
+                    if (std::fabs(ax - c) < std::fabs(ax - best)) best = c;
+                tab[k * 9 + e] = (float)(x < 0 ? -best : best);
+            }
+        init = true;
+    }
+    return tab;
+}
+
+// proc_icos/SRC/Eularmatrix.f90:1-15
+void eular_matrix(float theta0, float phi0, float omega0, float* r) {
+    const float d2r = 4.0f * std::atan2(1.0f, 1.0f) / 180.0f;
+    float theta = theta0 * d2r, phi = phi0 * d2r, omega = omega0 * d2r;
+    r[0] = cosf(phi) * cosf(theta) * cosf(omega) - sinf(phi) * sinf(omega);
+    r[1] = -cosf(phi) * cosf(theta) * sinf(omega) - sinf(phi) * cosf(omega);
+    r[2] = cosf(phi) * sinf(theta);
+    r[3] = sinf(phi) * cosf(theta) * cosf(omega) + cosf(phi) * sinf(omega);
+    r[4] = -sinf(phi) * cosf(theta) * sinf(omega) + cosf(phi) * cosf(omega);
+    r[5] = sinf(phi) * sinf(theta);
+    r[6] = -sinf(theta) * cosf(omega);
+    r[7] = sinf(theta) * sinf(omega);
+    r[8] = cosf(theta);
+}
+
+// equalort.f90:13-21 / transform_ort_2fTo5f.f90:19-27
+void euler_from(const float* r, float* th, float* ph, float* om) {
+    const float r2d = 45.0f / std::atan2(1.0f, 1.0f);
+    if (r[8] >= 1.0f) *th = 0.0f;
+    else if (r[8] < -1.0f) *th = 180.0f;
+    else *th = acosf(r[8]) * r2d;
+    *ph = atan2f(r[5], r[2]) * r2d;
+    *om = atan2f(r[7], -r[6]) * r2d;
+}
+
+// ---------------------------------------------------------------------------
+// context
+// ---------------------------------------------------------------------------
+template <class T> struct DBuf {
+    T* p = nullptr;
+    size_t n = 0;
+    int ensure(size_t want) {
+        if (want <= n) return 0;
+        if (p) cudaFree(p);
+        p = nullptr;
+        n = 0;
+        cudaError_t e = cudaMalloc(&p, want * sizeof(T));
+        if (e != cudaSuccess) {
+            p = nullptr;
+            return fail(CRYOIM_ERR_NOMEM, "cudaMalloc(%zu bytes): %s", want * sizeof(T),
+                        cudaGetErrorString(e));
+        }
+        n = want;
+        return 0;
+    }
+    void release() {
+        if (p) cudaFree(p);
+        p = nullptr;
+        n = 0;
+    }
+};
+
+struct Ctx {
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    bool own_stream = false;
+    // CUDA-event timing of the hot kernel launches (off by default)
+    bool prof = false;
+    cudaEvent_t pe0 = nullptr, pe1 = nullptr;
+    double prof_ms = 0.0;
+    long long prof_launches = 0;
+    cryoim_params p{};
+    bool have_params = false;
+    Band bd{};
+    int batch = 64;
+    DBuf<float> ops;  // 540, table order
+    // templates
+    int T = 0;
+    std::vector<cryoim_template> tmpl;
+    DBuf<float2> tband;
+    DBuf<float> tfcut0, tort;
+    // search grid
+    bool grid_ready = false;
+    int nth = 0, nph = 0, nom = 0, V = 0;
+    std::vector<float> views;  // V x 4
+    DBuf<float> d_views;
+    DBuf<float2> alpha;
+    // per-batch scratch
+    DBuf<float> imgs, par, fcut0, ctf, tfcut, state, cand, rpr, rot, prbuf;
+    DBuf<float2> fft, band, ralpha;
+    DBuf<unsigned long long> best;
+    DBuf<int> flag, sel;
+    std::map<int, cufftHandle> plans;
+    // reconstruction
+    DBuf<float4> acc;
+    DBuf<int2> samples;
+    DBuf<float2> vol;
+    bool rec_active = false;
+    int nsamples = 0, rec_used = 0, rec_img_id0 = -100;
+    float rec_src_df[3] = {0, 0, 0};
+    bool rec_have_first = false;
+    float rec_ox = 0, rec_oy = 0;
+    float rec_off_xy = 0, rec_off_z = 0;
+    int rec_base_xy = 0, rec_base_z = 0;
+
+    ~Ctx() {
+        cudaSetDevice(device);
+        for (auto& kv : plans) cufftDestroy(kv.second);
+        ops.release(); tband.release(); tfcut0.release(); tort.release(); d_views.release();
+        alpha.release(); imgs.release(); par.release(); fcut0.release(); ctf.release();
+        tfcut.release(); state.release(); cand.release(); rpr.release(); rot.release();
+        prbuf.release(); fft.release(); band.release(); ralpha.release(); best.release();
+        flag.release(); sel.release(); acc.release(); samples.release(); vol.release();
+        if (pe0) cudaEventDestroy(pe0);
+        if (pe1) cudaEventDestroy(pe1);
+        if (own_stream && stream) cudaStreamDestroy(stream);
+    }
+};
+
+Ctx* as_ctx(void* c) { return reinterpret_cast<Ctx*>(c); }
+
+int plan2d(Ctx* c, int nb, cufftHandle* out) {
+    auto it = c->plans.find(nb);
+    if (it != c->plans.end()) {
+        *out = it->second;
+        return CRYOIM_OK;
+    }
+    cufftHandle h;
+    int n[2] = {c->p.fftsize, c->p.fftsize};
+    CKF(cufftPlanMany(&h, 2, n, nullptr, 1, 0, nullptr, 1, 0, CUFFT_C2C, nb));
+    CKF(cufftSetStream(h, c->stream));
+    c->plans[nb] = h;
+    *out = h;
+    return CRYOIM_OK;
+}
+
+int check_ready(Ctx* c, bool need_templates) {
+    if (!c) return fail(CRYOIM_ERR_ARG, "null context");
+    if (!c->have_params) return fail(CRYOIM_ERR_STATE, "cryoim_set_params has not been called");
+    if (need_templates && c->T <= 0)
+        return fail(CRYOIM_ERR_STATE, "cryoim_load_templates has not been called");
+    CK(cudaSetDevice(c->device));
+    return CRYOIM_OK;
+}
+
+int ensure_batch(Ctx* c, int B) {
+    const long nn = (long)c->p.fftsize * c->p.fftsize;
+    const Band& bd = c->bd;
+    const long w2 = (long)bd.W * bd.W;
+    int r;
+    if ((r = c->imgs.ensure((size_t)B * nn))) return r;
+    if ((r = c->fft.ensure((size_t)B * nn))) return r;
+    if ((r = c->band.ensure((size_t)B * w2))) return r;
+    if ((r = c->fcut0.ensure((size_t)B * bd.nr))) return r;
+    if ((r = c->ctf.ensure((size_t)B * w2))) return r;
+    if ((r = c->par.ensure((size_t)B * 8))) return r;
+    if ((r = c->best.ensure((size_t)B))) return r;
+    if ((r = c->flag.ensure(4))) return r;
+    if ((r = c->sel.ensure((size_t)B))) return r;
+    if ((r = c->rot.ensure((size_t)B * 9))) return r;
+    if (c->T > 0 && (r = c->tfcut.ensure((size_t)B * c->T * bd.nr))) return r;
+    return CRYOIM_OK;
+}
+
+// Per-image parameter block on the device: [ox | oy | sx | sy | df(3) ...] of B each.
+struct ParView {
+    float *ox, *oy, *sx, *sy, *dfs;
+};
+ParView par_view(Ctx* c, int B) {
+    float* b = c->par.p;
+    return ParView{b, b + B, b + 2 * B, b + 3 * B, b + 4 * B};
+}
+
+// Mask / checkerboard / FFT / band of nb images already on the device.
+int transform_batch(Ctx* c, const float* d_src, int nb, int B, const std::vector<float>& hpar,
+                    int use_mask, int normalize, bool shift) {
+    ParView pv = par_view(c, B);
+    CK(cudaMemcpyAsync(c->par.p, hpar.data(), sizeof(float) * 8 * B, cudaMemcpyHostToDevice,
+                       c->stream));
+    CK(cudaMemsetAsync(c->flag.p, 0, sizeof(int), c->stream));
+    launch_prep_images(d_src, nb, c->p.fftsize, pv.ox, pv.oy, use_mask, c->p.imgmask_px, normalize,
+                       c->fft.p, c->flag.p, c->stream);
+    CK(cudaGetLastError());
+    cufftHandle h;
+    int r = plan2d(c, nb, &h);
+    if (r) return r;
+    CKF(cufftExecC2C(h, (cufftComplex*)c->fft.p, (cufftComplex*)c->fft.p, CUFFT_FORWARD));
+    launch_post_fft(c->fft.p, nb, c->bd, shift ? pv.sx : nullptr, shift ? pv.sy : nullptr,
+                    c->band.p, c->fcut0.p, c->stream);
+    CK(cudaGetLastError());
+    return CRYOIM_OK;
+}
+
+int check_flag(Ctx* c) {
+    int f = 0;
+    CK(cudaMemcpyAsync(&f, c->flag.p, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
+    CK(cudaStreamSynchronize(c->stream));
+    if (f) return fail(CRYOIM_ERR_INPUT, "non-finite pixel (NaN/Inf) in an input image");
+    return CRYOIM_OK;
+}
+
+// Views of ort_globesearch.f90:68-101.  For iphi = 0 the reference evaluates (theta, 0)
+// and then (theta, -0) into the same slot; only the second survives, so only it is run.
+int ensure_grid(Ctx* c) {
+    if (c->grid_ready) return CRYOIM_OK;
+    const float step = c->p.searchstep;
+    c->nth = (int)(21.0f / step);
+    c->nph = (int)(32.0f / step);
+    c->nom = (int)(360.0f / step);
+    if (c->nom < 1 || c->nom > 768)
+        return fail(CRYOIM_ERR_SIZE, "searchstep %g gives Nomega=%d (supported 1..768)", step, c->nom);
+    Angles an = host_angles();
+    const float d2r = an.deg2rad;
+    AsuPlanes pl = asu_planes(d2r);
+    c->views.clear();
+    for (int it = 0; it <= c->nth; ++it) {
+        float theta = 69.0f + step * (float)it;
+        float tmp = theta * d2r;
+        float z = cosf(tmp), z0 = sinf(tmp);
+        for (int iph = 0; iph <= c->nph; ++iph) {
+            float phi = step * (float)iph;
+            tmp = phi * d2r;
+            float x = z0 * cosf(tmp), y = z0 * sinf(tmp);
+            if (!asu_inside(pl, x, y, z)) continue;
+            for (int sgn = (iph == 0 ? -1 : 1); sgn >= -1; sgn -= 2) {
+                int slot = (it * (2 * c->nph + 1) + (sgn * iph + c->nph)) * c->nom;
+                float v[4];
+                v[0] = theta;
+                v[1] = (sgn > 0) ? phi : -phi;
+                std::memcpy(&v[2], &slot, 4);
+                v[3] = 0.0f;
+                c->views.insert(c->views.end(), v, v + 4);
+            }
+        }
+    }
+    c->V = (int)(c->views.size() / 4);
+    int r;
+    if ((r = c->d_views.ensure(c->views.size() + 4))) return r;
+    CK(cudaMemcpyAsync(c->d_views.p, c->views.data(), sizeof(float) * c->views.size(),
+                       cudaMemcpyHostToDevice, c->stream));
+    if (c->V > 0) {
+        std::vector<float> v2(2 * c->V);
+        for (int v = 0; v < c->V; ++v) { v2[2 * v] = c->views[4 * v]; v2[2 * v + 1] = c->views[4 * v + 1]; }
+        DBuf<float> tmp;
+        if ((r = tmp.ensure(v2.size()))) return r;
+        CK(cudaMemcpyAsync(tmp.p, v2.data(), sizeof(float) * v2.size(), cudaMemcpyHostToDevice,
+                           c->stream));
+        if ((r = c->alpha.ensure((size_t)c->V * c->T * 60))) return r;
+        launch_alpha_table(tmp.p, c->V, c->tort.p, c->T, c->ops.p, c->alpha.p, c->stream);
+        CK(cudaGetLastError());
+        CK(cudaStreamSynchronize(c->stream));
+        tmp.release();
+    }
+    c->grid_ready = true;
+    return CRYOIM_OK;
+}
+
+unsigned long long key_of(float pr, unsigned idx) {
+    unsigned bits;
+    std::memcpy(&bits, &pr, 4);
+    return ((unsigned long long)bits << 32) | idx;
+}
+
+int globesearch_impl(Ctx* c, const float* imgs, bool on_device, cryoim_particle* parts, int P,
+                     float* pr_array) {
+    int r = check_ready(c, true);
+    if (r) return r;
+    if (!imgs || !parts || P < 0) return fail(CRYOIM_ERR_ARG, "null input or negative count");
+    if (P == 0) return CRYOIM_OK;
+    if ((r = ensure_grid(c))) return r;
+    const int B = c->batch, nx = c->p.fftsize;
+    const long nn = (long)nx * nx;
+    if ((r = ensure_batch(c, B))) return r;
+    const long per = (long)c->nom * (2 * c->nph + 1) * (c->nth + 1);
+    if (pr_array && (r = c->prbuf.ensure((size_t)B * per))) return r;
+    // CTF cache of ort_globesearch.f90:60-66
+    std::vector<int> src(P);
+    {
+        int id0 = -100, cur = -1;
+        for (int i = 0; i < P; ++i) {
+            if (parts[i].img_id != id0) { cur = i; id0 = parts[i].img_id; }
+            src[i] = cur;
+        }
+    }
+    std::vector<float> hpar(8 * B);
+    std::vector<unsigned long long> hbest(B);
+    for (int b0 = 0; b0 < P; b0 += B) {
+        const int nb = std::min(B, P - b0);
+        const float* d_src;
+        if (on_device) {
+            d_src = imgs + b0 * nn;
+        } else {
+            CK(cudaMemcpyAsync(c->imgs.p, imgs + b0 * nn, sizeof(float) * nb * nn,
+                               cudaMemcpyHostToDevice, c->stream));
+            d_src = c->imgs.p;
+        }
+        std::fill(hpar.begin(), hpar.end(), 0.0f);
+        for (int i = 0; i < nb; ++i) {
+            const cryoim_particle& q = parts[b0 + i];
+            const cryoim_particle& s = parts[src[b0 + i]];
+            hpar[i] = q.x; hpar[B + i] = q.y; hpar[2 * B + i] = q.x; hpar[3 * B + i] = q.y;
+            hpar[4 * B + 3 * i] = s.df1; hpar[4 * B + 3 * i + 1] = s.df2; hpar[4 * B + 3 * i + 2] = s.astigang;
+        }
+        // ort_globesearch.f90:50 masks unconditionally
+        if ((r = transform_batch(c, d_src, nb, B, hpar, 1, 0, true))) return r;
+        ParView pv = par_view(c, B);
+        const float* ctfp = nullptr;
+        const float* tfc = c->tfcut0.p;
+        long tfs = 0;
+        if (c->p.apply_ctf) {
+            launch_ctf_band(nb, c->bd, pv.dfs, c->p.apix, c->p.vol, c->p.cs, c->p.ampwg, c->ctf.p,
+                            c->stream);
+            launch_tmpl_fcut(c->tband.p, c->T, c->ctf.p, nb, c->bd, c->tfcut.p, c->stream);
+            CK(cudaGetLastError());
+            ctfp = c->ctf.p;
+            tfc = c->tfcut.p;
+            tfs = (long)c->T * c->bd.nr;
+        }
+        for (int i = 0; i < nb; ++i) hbest[i] = key_of(1000.0f, 0u);
+        CK(cudaMemcpyAsync(c->best.p, hbest.data(), sizeof(unsigned long long) * nb,
+                           cudaMemcpyHostToDevice, c->stream));
+        if (pr_array) {
+            std::vector<float> init((size_t)nb * per, 1000.0f);
+            CK(cudaMemcpyAsync(c->prbuf.p, init.data(), sizeof(float) * init.size(),
+                               cudaMemcpyHostToDevice, c->stream));
+            CK(cudaStreamSynchronize(c->stream));
+        }
+        if (c->V > 0) {
+            PrOmegaArgs a{};
+            a.band = c->band.p; a.fcut0 = c->fcut0.p; a.tband = c->tband.p;
+            a.tfcut = tfc; a.tfcut_pstride = tfs; a.ctf = ctfp; a.alpha = c->alpha.p;
+            a.views = c->d_views.p; a.V = c->V; a.T = c->T; a.nomega = c->nom;
+            a.step = c->p.searchstep; a.bd = c->bd; a.best = c->best.p;
+            a.pr_array = pr_array ? c->prbuf.p : nullptr; a.per = per;
+            if (c->prof) CK(cudaEventRecord(c->pe0, c->stream));
+            CK(launch_pr_omega(a, nb, c->stream));
+            if (c->prof) CK(cudaEventRecord(c->pe1, c->stream));
+        }
+        CK(cudaMemcpyAsync(hbest.data(), c->best.p, sizeof(unsigned long long) * nb,
+                           cudaMemcpyDeviceToHost, c->stream));
+        if (pr_array)
+            CK(cudaMemcpyAsync(pr_array + (long)b0 * per, c->prbuf.p, sizeof(float) * nb * per,
+                               cudaMemcpyDeviceToHost, c->stream));
+        if ((r = check_flag(c))) return r;
+        if (c->prof && c->V > 0) {
+            float ms = 0.f;
+            CK(cudaEventElapsedTime(&ms, c->pe0, c->pe1));
+            c->prof_ms += ms;
+            c->prof_launches += 1;
+        }
+        for (int i = 0; i < nb; ++i) {
+            cryoim_particle& q = parts[b0 + i];
+            unsigned idx = (unsigned)(hbest[i] & 0xffffffffu);
+            unsigned bits = (unsigned)(hbest[i] >> 32);
+            float pr;
+            std::memcpy(&pr, &bits, 4);
+            int iom = (int)(idx % c->nom);
+            int iph = (int)((idx / c->nom) % (2 * c->nph + 1));
+            int it = (int)(idx / ((unsigned)c->nom * (2 * c->nph + 1)));
+            // ort_globesearch.f90:102-126
+            q.theta0 = q.theta; q.phi0 = q.phi; q.omega0 = q.omega; q.x0 = q.x; q.y0 = q.y;
+            q.pr0 = q.pr;
+            q.theta = 69.0f + c->p.searchstep * (float)it;
+            q.phi = c->p.searchstep * (float)(iph - c->nph);
+            q.omega = c->p.searchstep * (float)iom;
+            q.pr = pr;
+            q.dtheta = q.theta - q.theta0; q.dphi = q.phi - q.phi0; q.domega = q.omega - q.omega0;
+            q.dx = q.x - q.x0; q.dy = q.y - q.y0; q.dpr = q.pr - q.pr0;
+        }
+    }
+    return CRYOIM_OK;
+}
+
+int refine_impl(Ctx* c, const float* imgs, bool on_device, cryoim_particle* parts, int P) {
+    int r = check_ready(c, true);
+    if (r) return r;
+    if (!imgs || !parts || P < 0) return fail(CRYOIM_ERR_ARG, "null input or negative count");
+    if (P == 0) return CRYOIM_OK;
+    const int B = c->batch, nx = c->p.fftsize, T = c->T;
+    const long nn = (long)nx * nx;
+    if ((r = ensure_batch(c, B))) return r;
+    if ((r = c->state.ensure((size_t)B * 6))) return r;
+    if ((r = c->cand.ensure((size_t)B * 55))) return r;
+    if ((r = c->rpr.ensure((size_t)B * 11))) return r;
+    if ((r = c->ralpha.ensure((size_t)B * 11 * T * 60))) return r;
+    std::vector<float> hpar(8 * B), hstate(6 * B);
+    for (int b0 = 0; b0 < P; b0 += B) {
+        const int nb = std::min(B, P - b0);
+        const float* d_src;
+        if (on_device) {
+            d_src = imgs + b0 * nn;
+        } else {
+            CK(cudaMemcpyAsync(c->imgs.p, imgs + b0 * nn, sizeof(float) * nb * nn,
+                               cudaMemcpyHostToDevice, c->stream));
+            d_src = c->imgs.p;
+        }
+        std::fill(hpar.begin(), hpar.end(), 0.0f);
+        for (int i = 0; i < nb; ++i) {
+            const cryoim_particle& q = parts[b0 + i];
+            hpar[i] = q.x; hpar[B + i] = q.y;
+            // ort_refinement.f90:61-67: CTF per particle (no imgID cache)
+            hpar[4 * B + 3 * i] = q.df1; hpar[4 * B + 3 * i + 1] = q.df2; hpar[4 * B + 3 * i + 2] = q.astigang;
+            hstate[6 * i] = q.theta; hstate[6 * i + 1] = q.phi; hstate[6 * i + 2] = q.omega;
+            hstate[6 * i + 3] = q.x; hstate[6 * i + 4] = q.y; hstate[6 * i + 5] = q.pr;
+        }
+        // ort_refinement.f90:46-54: no origin shift at this point
+        if ((r = transform_batch(c, d_src, nb, B, hpar, c->p.use_imgmask, 0, false))) return r;
+        ParView pv = par_view(c, B);
+        const float* ctfp = nullptr;
+        const float* tfc = c->tfcut0.p;
+        long tfs = 0;
+        if (c->p.apply_ctf) {
+            launch_ctf_band(nb, c->bd, pv.dfs, c->p.apix, c->p.vol, c->p.cs, c->p.ampwg, c->ctf.p,
+                            c->stream);
+            launch_tmpl_fcut(c->tband.p, T, c->ctf.p, nb, c->bd, c->tfcut.p, c->stream);
+            ctfp = c->ctf.p;
+            tfc = c->tfcut.p;
+            tfs = (long)T * c->bd.nr;
+        }
+        CK(cudaMemcpyAsync(c->state.p, hstate.data(), sizeof(float) * 6 * nb, cudaMemcpyHostToDevice,
+                           c->stream));
+        float fac = 1.0f;
+        for (int cyc = 1; cyc <= c->p.ncycle; ++cyc) {
+            float dang = c->p.delta_angle * fac, dtran = c->p.delta_trans * fac;
+            fac = fac * 0.8f;
+            launch_refine_candidates(c->state.p, nb, dang, dtran, c->ops.p, c->cand.p, c->stream);
+            launch_refine_alpha(c->cand.p, nb, c->tort.p, T, c->ops.p, c->ralpha.p, c->stream);
+            PrSingleArgs a{};
+            a.band = c->band.p; a.fcut0 = c->fcut0.p; a.tband = c->tband.p; a.tfcut = tfc;
+            a.tfcut_pstride = tfs; a.ctf = ctfp; a.cand = c->cand.p; a.alpha = c->ralpha.p;
+            a.T = T; a.bd = c->bd; a.pr = c->rpr.p;
+            CK(launch_pr_single(a, nb, c->stream));
+            launch_refine_select(c->cand.p, c->rpr.p, nb, c->state.p, c->stream);
+            CK(cudaGetLastError());
+        }
+        CK(cudaMemcpyAsync(hstate.data(), c->state.p, sizeof(float) * 6 * nb, cudaMemcpyDeviceToHost,
+                           c->stream));
+        if ((r = check_flag(c))) return r;
+        for (int i = 0; i < nb; ++i) {
+            cryoim_particle& q = parts[b0 + i];
+            const float* st = &hstate[6 * i];
+            q.theta0 = q.theta; q.phi0 = q.phi; q.omega0 = q.omega; q.x0 = q.x; q.y0 = q.y;
+            q.pr0 = q.pr;
+            q.theta = st[0]; q.phi = st[1]; q.omega = st[2]; q.x = st[3]; q.y = st[4]; q.pr = st[5];
+            q.dtheta = q.theta - q.theta0; q.dphi = q.phi - q.phi0; q.domega = q.omega - q.omega0;
+            q.dx = q.x - q.x0; q.dy = q.y - q.y0; q.dpr = q.pr - q.pr0;
+        }
+    }
+    return CRYOIM_OK;
+}
+
+int rec_insert_impl(Ctx* c, const float* imgs, bool on_device, const cryoim_particle* parts, int P,
+                    int32_t* used) {
+    int r = check_ready(c, false);
+    if (r) return r;
+    if (!c->rec_active) return fail(CRYOIM_ERR_STATE, "cryoim_rec_begin has not been called");
+    if (!imgs || !parts || P < 0) return fail(CRYOIM_ERR_ARG, "null input or negative count");
+    const int B = c->batch, nx = c->p.fftsize;
+    const long nn = (long)nx * nx;
+    if ((r = ensure_batch(c, B))) return r;
+    const float boundx = c->p.subrec ? (float)nx / 4.0f : c->p.boundx;  // reconstruct_substep.f90:22
+    const Angles an = host_angles();
+    std::vector<float> hpar(8 * B), hrot(9 * B);
+    std::vector<int> hsel(B);
+    int nused = 0;
+    for (int b0 = 0; b0 < P; b0 += B) {
+        const int nb = std::min(B, P - b0);
+        std::fill(hpar.begin(), hpar.end(), 0.0f);
+        for (int i = 0; i < nb; ++i) {
+            const cryoim_particle& q = parts[b0 + i];
+            if (!c->rec_have_first) {  // reconstruct.f90:92 masks every image at particle(first)'s origin
+                c->rec_ox = q.x; c->rec_oy = q.y; c->rec_have_first = true;
+            }
+            int s = (q.pr <= c->p.pr_threshold && std::fabs(q.x) <= boundx && std::fabs(q.y) <= boundx);
+            hsel[i] = s;
+            hpar[i] = c->rec_ox; hpar[B + i] = c->rec_oy;
+            hpar[2 * B + i] = q.x; hpar[3 * B + i] = q.y;
+            if (s) {
+                ++nused;
+                // reconstruct.f90:80-91: CTF per particle for imgstck, else cached per imgID
+                if (c->p.imgstck || q.img_id != c->rec_img_id0) {
+                    c->rec_src_df[0] = q.df1; c->rec_src_df[1] = q.df2; c->rec_src_df[2] = q.astigang;
+                    if (!c->p.imgstck) c->rec_img_id0 = q.img_id;
+                }
+                hpar[4 * B + 3 * i] = c->rec_src_df[0];
+                hpar[4 * B + 3 * i + 1] = c->rec_src_df[1];
+                hpar[4 * B + 3 * i + 2] = c->rec_src_df[2];
+                euler_mat(q.theta, q.phi, q.omega, an.deg2rad, &hrot[9 * i]);
+            }
+        }
+        const float* d_src;
+        if (on_device) {
+            d_src = imgs + b0 * nn;
+        } else {
+            CK(cudaMemcpyAsync(c->imgs.p, imgs + b0 * nn, sizeof(float) * nb * nn,
+                               cudaMemcpyHostToDevice, c->stream));
+            d_src = c->imgs.p;
+        }
+        if ((r = transform_batch(c, d_src, nb, B, hpar, c->p.use_imgmask, 1, true))) return r;
+        ParView pv = par_view(c, B);
+        const float* ctfp = nullptr;
+        if (c->p.apply_ctf || c->p.imgstck) {
+            launch_ctf_band(nb, c->bd, pv.dfs, c->p.apix, c->p.vol, c->p.cs, c->p.ampwg, c->ctf.p,
+                            c->stream);
+            ctfp = c->ctf.p;
+        }
+        CK(cudaMemcpyAsync(c->rot.p, hrot.data(), sizeof(float) * 9 * nb, cudaMemcpyHostToDevice,
+                           c->stream));
+        CK(cudaMemcpyAsync(c->sel.p, hsel.data(), sizeof(int) * nb, cudaMemcpyHostToDevice,
+                           c->stream));
+        InsertArgs a{};
+        a.band = c->band.p; a.ctf = ctfp; a.rot = c->rot.p; a.ops = c->ops.p;
+        a.samples = c->samples.p; a.nsamples = c->nsamples; a.nsym = c->p.nsym; a.sel = c->sel.p;
+        a.off_xy = c->rec_off_xy; a.off_z = c->rec_off_z; a.base_xy = c->rec_base_xy;
+        a.base_z = c->rec_base_z; a.bd = c->bd; a.acc = c->acc.p;
+        if (c->nsamples > 0) CK(launch_insert(a, nb, c->stream));
+        if ((r = check_flag(c))) return r;
+    }
+    c->rec_used += nused;
+    if (used) *used = nused;
+    return CRYOIM_OK;
+}
+
+}  // namespace
+
+// ===========================================================================
+// C ABI
+// ===========================================================================
+extern "C" {
+
+int32_t cryoim_version(void) { return 100; }
+
+const char* cryoim_last_error(void) { return g_err.c_str(); }
+
+int cryoim_params_default(cryoim_params* p, int32_t fftsize) {
+    if (!p) return fail(CRYOIM_ERR_ARG, "null params");
+    if (fftsize < 8 || (fftsize & 1)) return fail(CRYOIM_ERR_SIZE, "fftsize %d must be even and >= 8", fftsize);
+    std::memset(p, 0, sizeof(*p));
+    p->fftsize = fftsize;
+    p->mode = 0;
+    p->first = 1;
+    p->last = 0;
+    p->ncycle = 6;
+    p->apply_ctf = 1;
+    p->use_imgmask = 1;
+    p->apix = 1.0f;
+    p->min_res = 300.0f;
+    p->max_res = 8.0f;
+    p->imgmask = (float)(fftsize / 2 - 2);
+    p->vol = 300.0f;
+    p->cs = 2.7f;
+    p->ampwg = 0.1f;
+    p->bfactor = 0.0f;
+    p->pr_threshold = 90.0f;
+    p->searchstep = 2.0f;
+    p->maxcentshift = 100.0f;
+    p->boundx = (float)(fftsize / 2 - 2);
+    p->nsym = 60;
+    p->nlin = 60;
+    return CRYOIM_OK;
+}
+
+int cryoim_params_derive(cryoim_params* p) {
+    if (!p) return fail(CRYOIM_ERR_ARG, "null params");
+    if (!(p->apix > 0) || !(p->min_res > 0) || !(p->max_res > 0))
+        return fail(CRYOIM_ERR_ARG, "apix, minRes and maxRes must be positive");
+    // 0calc_initialvalues.f90:6-21 (mode != 6)
+    float minres = p->apix * (float)p->fftsize / p->min_res;
+    float maxres = p->apix * (float)p->fftsize / p->max_res;
+    p->min_r = (int)minres;
+    p->max_r = (int)maxres;
+    if (p->max_r % 2 != 0) p->max_r = p->max_r + 1;
+    p->imgmask_px = p->use_imgmask ? p->imgmask / p->apix : p->imgmask;
+    p->delta_angle = 360.0f / (maxres * sqrtf(5.0f) * 3.14159f);
+    p->delta_trans = (float)p->fftsize / (maxres * sqrtf(5.0f));
+    p->nsym = 60;
+    p->nlin = 60;
+    return CRYOIM_OK;
+}
+
+int cryoim_ctx_create(int32_t device, void** out) {
+    if (!out) return fail(CRYOIM_ERR_ARG, "null output pointer");
+    *out = nullptr;
+    int ndev = 0;
+    CK(cudaGetDeviceCount(&ndev));
+    if (device < 0 || device >= ndev) return fail(CRYOIM_ERR_ARG, "device %d of %d", device, ndev);
+    CK(cudaSetDevice(device));
+    Ctx* c = new Ctx();
+    c->device = device;
+    cudaError_t e = cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking);
+    if (e != cudaSuccess) {
+        delete c;
+        return fail(CRYOIM_ERR_CUDA, "cudaStreamCreate: %s", cudaGetErrorString(e));
+    }
+    c->own_stream = true;
+    int r = c->ops.ensure(540);
+    if (r) { delete c; return r; }
+    e = cudaMemcpy(c->ops.p, table_ops(), sizeof(float) * 540, cudaMemcpyHostToDevice);
+    if (e != cudaSuccess) {
+        delete c;
+        return fail(CRYOIM_ERR_CUDA, "cudaMemcpy: %s", cudaGetErrorString(e));
+    }
+    *out = c;
+    return CRYOIM_OK;
+}
+
+int cryoim_ctx_destroy(void* ctx) {
+    if (!ctx) return CRYOIM_OK;
+    delete as_ctx(ctx);
+    return CRYOIM_OK;
+}
+
+int cryoim_ctx_set_stream(void* ctx, void* stream) {
+    Ctx* c = as_ctx(ctx);
+    if (!c) return fail(CRYOIM_ERR_ARG, "null context");
+    CK(cudaSetDevice(c->device));
+    CK(cudaStreamSynchronize(c->stream));
+    if (c->own_stream && c->stream) cudaStreamDestroy(c->stream);
+    if (stream) {
+        c->stream = (cudaStream_t)stream;
+        c->own_stream = false;
+    } else {
+        CK(cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking));
+        c->own_stream = true;
+    }
+    for (auto& kv : c->plans) CKF(cufftSetStream(kv.second, c->stream));
+    return CRYOIM_OK;
+}
+
+int cryoim_ctx_set_batch(void* ctx, int32_t batch) {
+    Ctx* c = as_ctx(ctx);
+    if (!c) return fail(CRYOIM_ERR_ARG, "null context");
+    if (batch < 1 || batch > 65535) return fail(CRYOIM_ERR_ARG, "batch %d out of range", batch);
+    c->batch = batch;
+    return CRYOIM_OK;
+}
+
+int cryoim_ctx_set_profiling(void* ctx, int32_t on) {
+    Ctx* c = as_ctx(ctx);
+    if (!c) return fail(CRYOIM_ERR_ARG, "null context");
+    CK(cudaSetDevice(c->device));
+    if (on && !c->pe0) {
+        CK(cudaEventCreate(&c->pe0));
+        CK(cudaEventCreate(&c->pe1));
+    }
+    c->prof = on != 0;
+    c->prof_ms = 0.0;
+    c->prof_launches = 0;
+    return CRYOIM_OK;
+}
+
+int cryoim_ctx_kernel_time(void* ctx, double* ms, int64_t* launches) {
+    Ctx* c = as_ctx(ctx);
+    if (!c || !ms || !launches) return fail(CRYOIM_ERR_ARG, "null argument");
+    *ms = c->prof_ms;
+    *launches = c->prof_launches;
+    c->prof_ms = 0.0;
+    c->prof_launches = 0;
+    return CRYOIM_OK;
+}
+
+int cryoim_set_params(void* ctx, const cryoim_params* p) {
+    Ctx* c = as_ctx(ctx);
+    if (!c || !p) return fail(CRYOIM_ERR_ARG, "null argument");
+    if (p->fftsize < 8 || (p->fftsize & 1) || p->fftsize > 2048)
+        return fail(CRYOIM_ERR_SIZE, "fftsize %d unsupported (even, 8..2048)", p->fftsize);
+    if (p->min_r < 0 || p->max_r < p->min_r)
+        return fail(CRYOIM_ERR_ARG, "minR=%d maxR=%d (derive the parameters first)", p->min_r, p->max_r);
+    if (p->max_r > p->fftsize / 2 - 2)
+        return fail(CRYOIM_ERR_SIZE, "maxR=%d exceeds FFTsize/2-2=%d", p->max_r, p->fftsize / 2 - 2);
+    if (!(p->searchstep > 0)) return fail(CRYOIM_ERR_ARG, "searchstep must be positive");
+    if (p->nsym != 60) return fail(CRYOIM_ERR_ARG, "only sym=icos (nsym=60) is on this path");
+    CK(cudaSetDevice(c->device));
+    CK(cudaStreamSynchronize(c->stream));
+    bool geom_changed = !c->have_params || c->p.fftsize != p->fftsize || c->p.min_r != p->min_r ||
+                        c->p.max_r != p->max_r;
+    bool step_changed = !c->have_params || c->p.searchstep != p->searchstep;
+    c->p = *p;
+    c->bd = make_band(p->fftsize, p->min_r, p->max_r);
+    c->have_params = true;
+    if (geom_changed) {
+        for (auto& kv : c->plans) cufftDestroy(kv.second);
+        c->plans.clear();
+        c->T = 0;  // templates depend on the band geometry
+        c->grid_ready = false;
+        c->rec_active = false;
+    }
+    if (step_changed) c->grid_ready = false;
+    long nn = (long)p->fftsize * p->fftsize;
+    c->batch = (int)std::max(1L, std::min(64L, (long)(16L * 1024 * 1024) / nn));
+    return CRYOIM_OK;
+}
+
+int cryoim_load_templates(void* ctx, const float* tmpl_real, const cryoim_template* t, int32_t T) {
+    Ctx* c = as_ctx(ctx);
+    int r = check_ready(c, false);
+    if (r) return r;
+    if (!tmpl_real || !t || T < 1) return fail(CRYOIM_ERR_ARG, "templates: null input or T < 1");
+    const int nx = c->p.fftsize;
+    const long nn = (long)nx * nx, w2 = (long)c->bd.W * c->bd.W;
+    c->T = 0;
+    c->grid_ready = false;
+    c->tmpl.assign(t, t + T);
+    if ((r = c->tband.ensure((size_t)T * w2))) return r;
+    if ((r = c->tfcut0.ensure((size_t)T * c->bd.nr))) return r;
+    if ((r = c->tort.ensure((size_t)T * 3))) return r;
+    std::vector<float> tort(3 * T);
+    for (int i = 0; i < T; ++i) { tort[3 * i] = t[i].theta; tort[3 * i + 1] = t[i].phi; tort[3 * i + 2] = t[i].omega; }
+    CK(cudaMemcpyAsync(c->tort.p, tort.data(), sizeof(float) * 3 * T, cudaMemcpyHostToDevice, c->stream));
+    const int B = c->batch;
+    if ((r = ensure_batch(c, B))) return r;
+    std::vector<float> hpar(8 * B);
+    for (int b0 = 0; b0 < T; b0 += B) {
+        const int nb = std::min(B, T - b0);
+        CK(cudaMemcpyAsync(c->imgs.p, tmpl_real + b0 * nn, sizeof(float) * nb * nn,
+                           cudaMemcpyHostToDevice, c->stream));
+        std::fill(hpar.begin(), hpar.end(), 0.0f);
+        for (int i = 0; i < nb; ++i) {
+            hpar[i] = t[b0 + i].x; hpar[B + i] = t[b0 + i].y;
+            hpar[2 * B + i] = t[b0 + i].x; hpar[3 * B + i] = t[b0 + i].y;
+        }
+        // load_template.f90:36-47
+        if ((r = transform_batch(c, c->imgs.p, nb, B, hpar, c->p.use_imgmask, 0, true))) return r;
+        CK(cudaMemcpyAsync(c->tband.p + b0 * w2, c->band.p, sizeof(float2) * nb * w2,
+                           cudaMemcpyDeviceToDevice, c->stream));
+        CK(cudaMemcpyAsync(c->tfcut0.p + (long)b0 * c->bd.nr, c->fcut0.p,
+                           sizeof(float) * nb * c->bd.nr, cudaMemcpyDeviceToDevice, c->stream));
+        if ((r = check_flag(c))) return r;
+    }
+    c->T = T;
+    if ((r = ensure_batch(c, B))) return r;  // tfcut sized for T
+    return CRYOIM_OK;
+}
+
+int cryoim_project_templates(void* ctx, const float* map3d, const cryoim_template* t, int32_t T,
+                             float* out) {
+    Ctx* c = as_ctx(ctx);
+    int r = check_ready(c, false);
+    if (r) return r;
+    if (!map3d || !t || !out || T < 1) return fail(CRYOIM_ERR_ARG, "null input or T < 1");
+    const int nx = c->p.fftsize;
+    const long nn = (long)nx * nx, n3 = nn * nx;
+    DBuf<float> dmap, deul, dout;
+    if ((r = dmap.ensure(n3)) || (r = deul.ensure(3 * T)) || (r = dout.ensure((size_t)T * nn))) return r;
+    std::vector<float> eul(3 * T);
+    for (int i = 0; i < T; ++i) { eul[3 * i] = t[i].theta; eul[3 * i + 1] = t[i].phi; eul[3 * i + 2] = t[i].omega; }
+    CK(cudaMemcpyAsync(dmap.p, map3d, sizeof(float) * n3, cudaMemcpyHostToDevice, c->stream));
+    CK(cudaMemcpyAsync(deul.p, eul.data(), sizeof(float) * 3 * T, cudaMemcpyHostToDevice, c->stream));
+    launch_project(dmap.p, nx, deul.p, T, dout.p, c->stream);
+    CK(cudaGetLastError());
+    CK(cudaMemcpyAsync(out, dout.p, sizeof(float) * T * nn, cudaMemcpyDeviceToHost, c->stream));
+    CK(cudaStreamSynchronize(c->stream));
+    return CRYOIM_OK;
+}
+
+int cryoim_search_grid(void* ctx, int32_t* ntheta, int32_t* nphi, int32_t* nomega, int32_t* nviews) {
+    Ctx* c = as_ctx(ctx);
+    int r = check_ready(c, true);
+    if (r) return r;
+    if ((r = ensure_grid(c))) return r;
+    if (ntheta) *ntheta = c->nth;
+    if (nphi) *nphi = c->nph;
+    if (nomega) *nomega = c->nom;
+    if (nviews) *nviews = c->V;
+    return CRYOIM_OK;
+}
+
+int cryoim_search_terms(void* ctx, double* terms) {
+    Ctx* c = as_ctx(ctx);
+    int r = check_ready(c, true);
+    if (r) return r;
+    if (!terms) return fail(CRYOIM_ERR_ARG, "null output");
+    if ((r = ensure_grid(c))) return r;
+    std::vector<float2> al((size_t)c->V * c->T * 60);
+    if (!al.empty()) {
+        CK(cudaMemcpyAsync(al.data(), c->alpha.p, sizeof(float2) * al.size(), cudaMemcpyDeviceToHost,
+                           c->stream));
+        CK(cudaStreamSynchronize(c->stream));
+    }
+    long long lines = 0;
+    for (const float2& a : al) lines += (a.x < 999.0f && a.y < 999.0f);
+    *terms = (double)lines * c->bd.nr * c->nom;
+    return CRYOIM_OK;
+}
+
+int cryoim_globesearch(void* ctx, const float* imgs, cryoim_particle* parts, int32_t P,
+                       float* pr_array) {
+    return globesearch_impl(as_ctx(ctx), imgs, false, parts, P, pr_array);
+}
+
+int cryoim_globesearch_device(void* ctx, const float* d_imgs, cryoim_particle* parts, int32_t P,
+                              float* pr_array) {
+    return globesearch_impl(as_ctx(ctx), d_imgs, true, parts, P, pr_array);
+}
+
+int cryoim_prscore_omega(void* ctx, const float* ft_a, const float* ft_b, const float* fcut0,
+                         const float* ctf, float theta, float phi, float* pr_omega) {
+    Ctx* c = as_ctx(ctx);
+    int r = check_ready(c, true);
+    if (r) return r;
+    if (!ft_a || !ft_b || !fcut0 || !pr_omega) return fail(CRYOIM_ERR_ARG, "null argument");
+    const int nx = c->p.fftsize, W = c->bd.W, off = c->bd.off, nr = c->bd.nr, T = c->T;
+    const float step = c->p.searchstep;
+    const int nom = (int)(360.0f / step);
+    if (nom < 1 || nom > 768) return fail(CRYOIM_ERR_SIZE, "Nomega=%d unsupported", nom);
+    if ((r = ensure_batch(c, c->batch))) return r;
+    std::vector<float2> band((size_t)W * W);
+    std::vector<float> cband(ctf ? (size_t)W * W : 0);
+    for (int y = 0; y < W; ++y)
+        for (int x = 0; x < W; ++x) {
+            long i = (long)(off + y) * nx + (off + x);
+            band[(size_t)y * W + x] = make_float2(ft_a[i], ft_b[i]);
+            if (ctf) cband[(size_t)y * W + x] = ctf[i];
+        }
+    CK(cudaMemcpyAsync(c->band.p, band.data(), sizeof(float2) * W * W, cudaMemcpyHostToDevice, c->stream));
+    CK(cudaMemcpyAsync(c->fcut0.p, fcut0, sizeof(float) * nr, cudaMemcpyHostToDevice, c->stream));
+    float hv[4] = {theta, phi, 0.f, 0.f};
+    int zero = 0;
+    std::memcpy(&hv[2], &zero, 4);
+    DBuf<float> dv;
+    DBuf<float2> dal;
+    DBuf<float> dprs;
+    if ((r = dv.ensure(4)) || (r = dal.ensure((size_t)T * 60)) || (r = dprs.ensure(nom))) return r;
+    CK(cudaMemcpyAsync(dv.p, hv, sizeof(hv), cudaMemcpyHostToDevice, c->stream));
+    launch_alpha_table(dv.p, 1, c->tort.p, T, c->ops.p, dal.p, c->stream);
+    // the view array of launch_alpha_table is (theta, phi) pairs: pass hv's first two
+    const float* tfc = c->tfcut0.p;
+    long tfs = 0;
+    const float* ctfp = nullptr;
+    if (ctf) {
+        CK(cudaMemcpyAsync(c->ctf.p, cband.data(), sizeof(float) * W * W, cudaMemcpyHostToDevice, c->stream));
+        launch_tmpl_fcut(c->tband.p, T, c->ctf.p, 1, c->bd, c->tfcut.p, c->stream);
+        ctfp = c->ctf.p;
+        tfc = c->tfcut.p;
+        tfs = (long)T * nr;
+    }
+    unsigned long long k0 = key_of(1000.0f, 0u);
+    CK(cudaMemcpyAsync(c->best.p, &k0, sizeof(k0), cudaMemcpyHostToDevice, c->stream));
+    PrOmegaArgs a{};
+    a.band = c->band.p; a.fcut0 = c->fcut0.p; a.tband = c->tband.p; a.tfcut = tfc;
+    a.tfcut_pstride = tfs; a.ctf = ctfp; a.alpha = dal.p; a.views = dv.p; a.V = 1; a.T = T;
+    a.nomega = nom; a.step = step; a.bd = c->bd; a.best = c->best.p; a.pr_array = dprs.p; a.per = nom;
+    CK(launch_pr_omega(a, 1, c->stream));
+    CK(cudaMemcpyAsync(pr_omega, dprs.p, sizeof(float) * nom, cudaMemcpyDeviceToHost, c->stream));
+    CK(cudaStreamSynchronize(c->stream));
+    return CRYOIM_OK;
+}
+
+int cryoim_refine(void* ctx, const float* imgs, cryoim_particle* parts, int32_t P) {
+    return refine_impl(as_ctx(ctx), imgs, false, parts, P);
+}
+
+int cryoim_refine_device(void* ctx, const float* d_imgs, cryoim_particle* parts, int32_t P) {
+    return refine_impl(as_ctx(ctx), d_imgs, true, parts, P);
+}
+
+int cryoim_prscore(void* ctx, const float* ft_a, const float* ft_b, const float* fcut0,
+                   const float* ctf, float theta, float phi, float omega, float x, float y,
+                   float* pr) {
+    Ctx* c = as_ctx(ctx);
+    int r = check_ready(c, true);
+    if (r) return r;
+    if (!ft_a || !ft_b || !fcut0 || !pr) return fail(CRYOIM_ERR_ARG, "null argument");
+    const int nx = c->p.fftsize, W = c->bd.W, off = c->bd.off, nr = c->bd.nr, T = c->T;
+    if ((r = ensure_batch(c, c->batch))) return r;
+    if ((r = c->cand.ensure(55)) || (r = c->rpr.ensure(11)) || (r = c->ralpha.ensure((size_t)11 * T * 60)))
+        return r;
+    std::vector<float2> band((size_t)W * W);
+    std::vector<float> cband(ctf ? (size_t)W * W : 0);
+    for (int yy = 0; yy < W; ++yy)
+        for (int xx = 0; xx < W; ++xx) {
+            long i = (long)(off + yy) * nx + (off + xx);
+            band[(size_t)yy * W + xx] = make_float2(ft_a[i], ft_b[i]);
+            if (ctf) cband[(size_t)yy * W + xx] = ctf[i];
+        }
+    CK(cudaMemcpyAsync(c->band.p, band.data(), sizeof(float2) * W * W, cudaMemcpyHostToDevice, c->stream));
+    CK(cudaMemcpyAsync(c->fcut0.p, fcut0, sizeof(float) * nr, cudaMemcpyHostToDevice, c->stream));
+    std::vector<float> hc(55);
+    for (int j = 0; j < 11; ++j) { hc[5 * j] = theta; hc[5 * j + 1] = phi; hc[5 * j + 2] = omega; hc[5 * j + 3] = x; hc[5 * j + 4] = y; }
+    CK(cudaMemcpyAsync(c->cand.p, hc.data(), sizeof(float) * 55, cudaMemcpyHostToDevice, c->stream));
+    launch_refine_alpha(c->cand.p, 1, c->tort.p, T, c->ops.p, c->ralpha.p, c->stream);
+    const float* tfc = c->tfcut0.p;
+    long tfs = 0;
+    const float* ctfp = nullptr;
+    if (ctf) {
+        CK(cudaMemcpyAsync(c->ctf.p, cband.data(), sizeof(float) * W * W, cudaMemcpyHostToDevice, c->stream));
+        launch_tmpl_fcut(c->tband.p, T, c->ctf.p, 1, c->bd, c->tfcut.p, c->stream);
+        ctfp = c->ctf.p;
+        tfc = c->tfcut.p;
+        tfs = (long)T * nr;
+    }
+    PrSingleArgs a{};
+    a.band = c->band.p; a.fcut0 = c->fcut0.p; a.tband = c->tband.p; a.tfcut = tfc;
+    a.tfcut_pstride = tfs; a.ctf = ctfp; a.cand = c->cand.p; a.alpha = c->ralpha.p; a.T = T;
+    a.bd = c->bd; a.pr = c->rpr.p;
+    CK(launch_pr_single(a, 1, c->stream));
+    float out[11];
+    CK(cudaMemcpyAsync(out, c->rpr.p, sizeof(float) * 11, cudaMemcpyDeviceToHost, c->stream));
+    CK(cudaStreamSynchronize(c->stream));
+    *pr = out[0];
+    return CRYOIM_OK;
+}
+
+int cryoim_rec_begin(void* ctx) {
+    Ctx* c = as_ctx(ctx);
+    int r = check_ready(c, false);
+    if (r) return r;
+    const Band& bd = c->bd;
+    const int R = bd.max_r, nx = c->p.fftsize;
+    const long nacc = (long)bd.AW * bd.AW * (R + 2);
+    if ((r = c->acc.ensure(nacc))) return r;
+    // reconstruct.f90:26-28 (wg = 0.01) or reconstruct_substep.f90:23-25 (wg = 0)
+    const float wg0 = c->p.subrec ? 0.0f : 0.01f;
+    std::vector<float4> init(nacc, make_float4(0.f, 0.f, wg0, 0.f));
+    CK(cudaMemcpyAsync(c->acc.p, init.data(), sizeof(float4) * nacc, cudaMemcpyHostToDevice, c->stream));
+    // insertion samples: reconstruct.f90:103-106 (r <= maxR) or reconstruct_substep.f90:101-104 (r <= maxR-2)
+    const float lim = c->p.subrec ? (float)(R - 2) : (float)R;
+    std::vector<int2> smp;
+    for (int ky = -R; ky <= R; ++ky)
+        for (int hx = 0; hx <= R; ++hx) {
+            float dr = sqrtf((float)(hx * hx + ky * ky));
+            if (dr <= lim) smp.push_back(make_int2(hx, ky));
+        }
+    c->nsamples = (int)smp.size();
+    if ((r = c->samples.ensure(smp.size() + 1))) return r;
+    CK(cudaMemcpyAsync(c->samples.p, smp.data(), sizeof(int2) * smp.size(), cudaMemcpyHostToDevice, c->stream));
+    if (c->p.subrec) {
+        // reconstruct_substep.f90:121: x0(1:2) += maxR, z unshifted; tnf cell lx -> box lx+1
+        c->rec_off_xy = (float)R; c->rec_off_z = 0.0f; c->rec_base_xy = -1; c->rec_base_z = 0;
+    } else {
+        c->rec_off_xy = (float)(nx / 2); c->rec_off_z = (float)(nx / 2);
+        c->rec_base_xy = nx / 2 - R - 1; c->rec_base_z = nx / 2;
+    }
+    CK(cudaStreamSynchronize(c->stream));
+    c->rec_active = true;
+    c->rec_used = 0;
+    c->rec_img_id0 = -100;
+    c->rec_have_first = false;
+    return CRYOIM_OK;
+}
+
+int cryoim_rec_insert(void* ctx, const float* imgs, const cryoim_particle* parts, int32_t P,
+                      int32_t* used) {
+    return rec_insert_impl(as_ctx(ctx), imgs, false, parts, P, used);
+}
+
+int cryoim_rec_insert_device(void* ctx, const float* d_imgs, const cryoim_particle* parts,
+                             int32_t P, int32_t* used) {
+    return rec_insert_impl(as_ctx(ctx), d_imgs, true, parts, P, used);
+}
+
+int cryoim_rec_finish(void* ctx, float* map) {
+    Ctx* c = as_ctx(ctx);
+    int r = check_ready(c, false);
+    if (r) return r;
+    if (!c->rec_active) return fail(CRYOIM_ERR_STATE, "cryoim_rec_begin has not been called");
+    if (!map) return fail(CRYOIM_ERR_ARG, "null map");
+    if (c->p.subrec)
+        return fail(CRYOIM_ERR_STATE, "subrec accumulation has no map: use cryoim_rec_get_partial");
+    const int nx = c->p.fftsize;
+    const long n3 = (long)nx * nx * nx;
+    if ((r = c->vol.ensure(n3))) return r;
+    CK(cudaMemsetAsync(c->vol.p, 0, sizeof(float2) * n3, c->stream));
+    launch_rec_fold(c->acc.p, c->bd, c->vol.p, c->stream);
+    CK(cudaGetLastError());
+    cufftHandle h;
+    CKF(cufftPlan3d(&h, nx, nx, nx, CUFFT_C2C));
+    cufftResult fr = cufftSetStream(h, c->stream);
+    if (fr == CUFFT_SUCCESS)
+        fr = cufftExecC2C(h, (cufftComplex*)c->vol.p, (cufftComplex*)c->vol.p, CUFFT_INVERSE);
+    if (fr != CUFFT_SUCCESS) {
+        cufftDestroy(h);
+        return fail(CRYOIM_ERR_CUDA, "3D inverse FFT failed: cufft %d", (int)fr);
+    }
+    DBuf<float> dmap;
+    if ((r = dmap.ensure(n3))) { cufftDestroy(h); return r; }
+    launch_rec_real(c->vol.p, nx, dmap.p, c->stream);
+    cudaError_t e = cudaMemcpyAsync(map, dmap.p, sizeof(float) * n3, cudaMemcpyDeviceToHost, c->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+    cufftDestroy(h);
+    if (e != cudaSuccess) return fail(CRYOIM_ERR_CUDA, "finish: %s", cudaGetErrorString(e));
+    return CRYOIM_OK;
+}
+
+int cryoim_rec_get_partial(void* ctx, float* fa, float* fb, float* wg) {
+    Ctx* c = as_ctx(ctx);
+    int r = check_ready(c, false);
+    if (r) return r;
+    if (!c->rec_active) return fail(CRYOIM_ERR_STATE, "cryoim_rec_begin has not been called");
+    if (!fa || !fb || !wg) return fail(CRYOIM_ERR_ARG, "null output");
+    const Band& bd = c->bd;
+    const int R = bd.max_r, AW = bd.AW, t = 2 * R + 1;
+    const long nacc = (long)AW * AW * (R + 2);
+    std::vector<float4> h(nacc);
+    CK(cudaMemcpyAsync(h.data(), c->acc.p, sizeof(float4) * nacc, cudaMemcpyDeviceToHost, c->stream));
+    CK(cudaStreamSynchronize(c->stream));
+    // tnf cell (x, y, z), x = hx + maxR, is box cell (hx, ky, lz) = acc_cell(x - R, y - R, z)
+    for (int z = 0; z <= R; ++z)
+        for (int y = 0; y < t; ++y)
+            for (int x = 0; x < t; ++x) {
+                const float4& v = h[acc_cell(bd, x - R, y - R, z)];
+                long o = ((long)z * t + y) * t + x;
+                fa[o] = v.x; fb[o] = v.y; wg[o] = v.z;
+            }
+    return CRYOIM_OK;
+}
+
+int cryoim_central_sections(void* ctx, const float* ft_re, const float* ft_im, const float* eulers,
+                            int32_t n, float* out_re, float* out_im) {
+    Ctx* c = as_ctx(ctx);
+    int r = check_ready(c, false);
+    if (r) return r;
+    if (!ft_re || !ft_im || !eulers || !out_re || !out_im || n < 1)
+        return fail(CRYOIM_ERR_ARG, "null input or n < 1");
+    const int nx = c->p.fftsize;
+    const long nn = (long)nx * nx, n3 = nn * nx;
+    DBuf<float> dre, dim, deul, ore, oim;
+    if ((r = dre.ensure(n3)) || (r = dim.ensure(n3)) || (r = deul.ensure(3 * n)) ||
+        (r = ore.ensure((size_t)n * nn)) || (r = oim.ensure((size_t)n * nn)))
+        return r;
+    CK(cudaMemcpyAsync(dre.p, ft_re, sizeof(float) * n3, cudaMemcpyHostToDevice, c->stream));
+    CK(cudaMemcpyAsync(dim.p, ft_im, sizeof(float) * n3, cudaMemcpyHostToDevice, c->stream));
+    CK(cudaMemcpyAsync(deul.p, eulers, sizeof(float) * 3 * n, cudaMemcpyHostToDevice, c->stream));
+    launch_sections(dre.p, dim.p, nx, deul.p, n, ore.p, oim.p, c->stream);
+    CK(cudaGetLastError());
+    CK(cudaMemcpyAsync(out_re, ore.p, sizeof(float) * n * nn, cudaMemcpyDeviceToHost, c->stream));
+    CK(cudaMemcpyAsync(out_im, oim.p, sizeof(float) * n * nn, cudaMemcpyDeviceToHost, c->stream));
+    CK(cudaStreamSynchronize(c->stream));
+    return CRYOIM_OK;
+}
+
+int cryoim_icos_ops(float* rot) {
+    if (!rot) return fail(CRYOIM_ERR_ARG, "null output");
+    std::memcpy(rot, table_ops(), sizeof(float) * 540);
+    return CRYOIM_OK;
+}
+
+int cryoim_asu_fold(float* theta, float* phi, float* omega) {
+    if (!theta || !phi || !omega) return fail(CRYOIM_ERR_ARG, "null argument");
+    asu_fold(theta, phi, omega, table_ops(), host_angles().deg2rad);
+    return CRYOIM_OK;
+}
+
+int cryoim_equalort(float theta, float phi, float omega, float* out) {
+    if (!out) return fail(CRYOIM_ERR_ARG, "null output");
+    float e[9], g[540];
+    eular_matrix(theta, phi, omega, e);
+    gen_ops<float>(g);
+    for (int i = 0; i < 60; ++i) {
+        float r[9];
+        mm3(g + i * 9, e, r);
+        euler_from(r, out + 3 * i, out + 3 * i + 1, out + 3 * i + 2);
+    }
+    return CRYOIM_OK;
+}
+
+int cryoim_transform_ort(int32_t to, float* theta, float* phi, float* omega, int32_t n) {
+    if (!theta || !phi || !omega || n < 0) return fail(CRYOIM_ERR_ARG, "null argument");
+    if (to != 5 && to != 3) return fail(CRYOIM_ERR_ARG, "to must be 5 or 3");
+    const float d2r = 4.0f * std::atan2(1.0f, 1.0f) / 180.0f;
+    float rot0[9];
+    if (to == 5) {
+        float v = acosf(cosf(60.0f * d2r) / sinf(36.0f * d2r));
+        float t[9] = {cosf(v), 0, sinf(v), 0, 1, 0, -sinf(v), 0, cosf(v)};
+        std::memcpy(rot0, t, sizeof(t));
+    } else {
+        float w = acosf(cosf(36.0f * d2r) / sinf(60.0f * d2r));
+        float t[9] = {1, 0, 0, 0, cosf(-w), sinf(-w), 0, -sinf(-w), cosf(-w)};
+        std::memcpy(rot0, t, sizeof(t));
+    }
+    for (int i = 0; i < n; ++i) {
+        float e[9], r[9];
+        eular_matrix(theta[i], phi[i], omega[i], e);
+        mm3(rot0, e, r);
+        euler_from(r, theta + i, phi + i, omega + i);
+    }
+    return CRYOIM_OK;
+}
+
+}  // extern "C"

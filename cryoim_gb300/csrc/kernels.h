@@ -1,0 +1,118 @@
+// kernels.h — launchers shared by the translation units of libcryoim_gb300.so.
+//
+// Device data layout (all buffers live in HBM, owned by the context):
+//   * particle / template Fourier "band": the (W x W) window of the centred nx*nx
+//     transform that the common-line sampler can touch, W = 2*maxR + 2, window
+//     origin at pixel (off, off), off = nx/2 - maxR.  float2 = (a, b) with b = -Im.
+//   * amplitude cuts (Fcut): nr = maxR - minR + 1 floats per image.
+//   * reconstruction accumulator: float4 (fa, fb, wg, 0) over a half box of
+//     AW x AW x (maxR + 2) voxels, AW = 2*maxR + 3, covering frequencies
+//     -maxR-1 .. maxR+1 in x and y and 0 .. maxR+1 in z (z >= 0 after the Friedel
+//     fold).  The extra low cell absorbs FP32 rotations that put a radius-maxR
+//     sample a hair beyond -maxR (the reference writes that cell in its full grid).
+#pragma once
+#include <cuda_runtime.h>
+#include <cstdint>
+
+namespace cryoim {
+
+struct Band {
+    int nx, min_r, max_r, nr, W, off, AW;
+};
+inline Band make_band(int nx, int min_r, int max_r) {
+    Band b;
+    b.nx = nx; b.min_r = min_r; b.max_r = max_r; b.nr = max_r - min_r + 1;
+    b.W = 2 * max_r + 2; b.off = nx / 2 - max_r;
+    b.AW = 2 * max_r + 3;
+    return b;
+}
+// accumulator index of frequency (hx, ky, lz)
+__host__ __device__ inline long acc_cell(const Band& b, int hx, int ky, int lz) {
+    return ((long)lz * b.AW + (ky + b.max_r + 1)) * b.AW + (hx + b.max_r + 1);
+}
+
+// ---- prep.cu (FP32 in the reference's operation order, -fmad=false) -------
+// mask (+ optional img2d_norm), checkerboard, real -> complex; nonfinite -> *flag |= 1
+void launch_prep_images(const float* imgs, int B, int nx, const float* ox, const float* oy,
+                        int use_mask, float mask_px, int normalize, float2* fft, int* flag,
+                        cudaStream_t st);
+// scale 1/nx^2, b = -Im, Fcut fit, optional origin shift (sx/sy per image, may be null),
+// band extraction.
+void launch_post_fft(const float2* fft, int B, Band bd, const float* sx, const float* sy,
+                     float2* band, float* fcut, cudaStream_t st);
+// getCTF2d over the band for B images (per-image defocus triples in dfs: df1, df2, astig)
+void launch_ctf_band(int B, Band bd, const float* dfs, float apix, float vol, float cs,
+                     float ampwg, float* ctf, cudaStream_t st);
+// Fcut of template x CTF for every (image, template)
+void launch_tmpl_fcut(const float2* tband, int T, const float* ctf, int B, Band bd, float* tfcut,
+                      cudaStream_t st);
+// common-line angle pairs for every (view, template, operator); views: V x 2 (theta, phi)
+void launch_alpha_table(const float* views, int V, const float* tort, int T, const float* ops,
+                        float2* alpha, cudaStream_t st);
+// refinement: the 11 candidates of every image (ort_cent_11) and their angle pairs
+void launch_refine_candidates(float* state, int B, float dang, float dtran, const float* ops,
+                              float* cand, cudaStream_t st);
+void launch_refine_alpha(const float* cand, int B, const float* tort, int T, const float* ops,
+                         float2* alpha, cudaStream_t st);
+void launch_refine_select(const float* cand, const float* pr, int B, float* state,
+                          cudaStream_t st);
+// reconstruction finish: fold / divide / sign into the full complex grid
+void launch_rec_fold(const float4* acc, Band bd, float2* vol, cudaStream_t st);
+void launch_rec_real(const float2* vol, int nx, float* map, cudaStream_t st);
+// real-space template projection and central sections
+void launch_project(const float* map, int nx, const float* eul, int n, float* out,
+                    cudaStream_t st);
+void launch_sections(const float* fre, const float* fim, int nx, const float* eul, int n,
+                     float* ore, float* oim, cudaStream_t st);
+
+// ---- score.cu (phase-residual scoring and insertion) ------------------------
+struct PrOmegaArgs {
+    const float2* band;      // [B][W*W]
+    const float* fcut0;      // [B][nr]
+    const float2* tband;     // [T][W*W]
+    const float* tfcut;      // [B][T][nr] (CTF) or [T][nr] (no CTF, tfcut_pstride = 0)
+    long tfcut_pstride;
+    const float* ctf;        // [B][W*W] or nullptr
+    const float2* alpha;     // [V][T][60]
+    const float* views;      // [V][4]: theta, phi, slot base (int bits), pad
+    int V, T, nomega;
+    float step;
+    Band bd;
+    unsigned long long* best;  // [B]
+    float* pr_array;           // [B][per] or nullptr
+    long per;
+};
+int pr_omega_smem_bytes(const Band& bd, int nomega, int* threads);
+cudaError_t launch_pr_omega(const PrOmegaArgs& a, int B, cudaStream_t st);
+
+struct PrSingleArgs {
+    const float2* band;      // [B][W*W] unshifted particle FT
+    const float* fcut0;      // [B][nr]
+    const float2* tband;     // [T][W*W]
+    const float* tfcut;
+    long tfcut_pstride;
+    const float* ctf;        // [B][W*W] or nullptr
+    const float* cand;       // [B][11][5]
+    const float2* alpha;     // [B][11][T][60]
+    int T;
+    Band bd;
+    float* pr;               // [B][11]
+};
+cudaError_t launch_pr_single(const PrSingleArgs& a, int B, cudaStream_t st);
+
+struct InsertArgs {
+    const float2* band;      // [B][W*W] shifted particle FT
+    const float* ctf;        // [B][W*W] or nullptr (CTF = 1)
+    const float* rot;        // [B][9] particle rotation matrices
+    const float* ops;        // [60][9]
+    const int2* samples;     // (hx, ky) insertion samples
+    int nsamples, nsym;
+    const int* sel;          // [B] 1 = insert
+    float off_xy, off_z;     // coordinate offsets added before int()
+    int base_xy, base_z;     // accumulator index origin
+    Band bd;
+    float4* acc;             // half box
+};
+cudaError_t launch_insert(const InsertArgs& a, int B, cudaStream_t st);
+
+}  // namespace cryoim

@@ -1,0 +1,565 @@
+// prep.cu — per-image preprocessing, CTF, amplitude-cut fit, orientation tables,
+// reconstruction fold and projections.
+//
+// Compiled with -fmad=false: every FP32 expression rounds where the Fortran's does
+// (icosprocess is built without fused multiply-add), so these kernels reproduce the
+// reference's preprocessing to the last bit of its expression order.  Reductions the
+// reference does sequentially in FP32 are done here in FP64 (then rounded), which is
+// closer to the exact value than the reference and independent of thread order.
+#include <cstdio>
+
+#include "geom.cuh"
+#include "kernels.h"
+
+namespace cryoim {
+namespace {
+
+struct HostAngles {
+    float pi, d2r, r2d;
+};
+HostAngles angles() {
+    Angles a = host_angles();
+    return HostAngles{a.pi, a.deg2rad, a.rad2deg};
+}
+
+__device__ double block_sum_d(double v, double* sh) {
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    int w = threadIdx.x >> 5, l = threadIdx.x & 31;
+    __syncthreads();
+    if (l == 0) sh[w] = v;
+    __syncthreads();
+    int nw = (blockDim.x + 31) >> 5;
+    double r = 0;
+    if (threadIdx.x < 32) {
+        r = (l < nw) ? sh[l] : 0.0;
+        for (int o = 16; o > 0; o >>= 1) r += __shfl_xor_sync(0xffffffffu, r, o);
+        if (l == 0) sh[0] = r;
+    }
+    __syncthreads();
+    r = sh[0];
+    __syncthreads();
+    return r;
+}
+
+// ---------------------------------------------------------------------------
+// mask / normalise / checkerboard: img2d_norm.f90:1-22, img2d_mask.f90:2-49,
+// and the (-1)^(hx+ky) multiply of ort_globesearch.f90:51
+// ---------------------------------------------------------------------------
+__global__ void k_prep_images(const float* __restrict__ imgs, int nx,
+                              const float* __restrict__ ox, const float* __restrict__ oy,
+                              int use_mask, float mask, int normalize, float pi,
+                              float2* __restrict__ out, int* flag) {
+    __shared__ double sh[32];
+    const int p = blockIdx.x;
+    const long nn = (long)nx * nx;
+    const float* img = imgs + p * nn;
+    float2* o = out + p * nn;
+    int bad = 0;
+    float avg = 0.f, nd = 1.f;
+    if (normalize) {
+        double s = 0;
+        for (long i = threadIdx.x; i < nn; i += blockDim.x) s += (double)img[i];
+        s = block_sum_d(s, sh);
+        avg = (float)s / (float)nn;
+        double s2 = 0;
+        for (long i = threadIdx.x; i < nn; i += blockDim.x) {
+            float d = img[i] - avg;
+            s2 += (double)(d * d);
+        }
+        s2 = block_sum_d(s2, sh);
+        nd = sqrtf((float)s2 / (float)nn);
+    }
+    const int h = nx / 2;
+    float R1 = mask - 3.0f;
+    if (R1 <= 0.0f) R1 = 0.0f;
+    float R2 = mask + 3.0f;
+    if (R2 > (float)h) R2 = (float)h;
+    const float x0 = ox[p] + (float)h, y0 = oy[p] + (float)h;
+    double summ = 0;
+    if (use_mask) {
+        double s = 0, c = 0;
+        for (long i = threadIdx.x; i < nn; i += blockDim.x) {
+            int iy = (int)(i / nx), ix = (int)(i % nx);
+            float yy = (-y0 + (float)iy) * (-y0 + (float)iy);
+            float xx = (-x0 + (float)ix) * (-x0 + (float)ix);
+            float ra = sqrtf(yy + xx);
+            if (ra > R1 && ra <= R2) {
+                float v = img[i];
+                if (normalize) v = (v - avg) / nd;
+                s += (double)v;
+                c += 1.0;
+            }
+        }
+        s = block_sum_d(s, sh);
+        c = block_sum_d(c, sh);
+        summ = s;
+        if (c != 0.0) summ = summ / (double)(float)c;
+    }
+    for (long i = threadIdx.x; i < nn; i += blockDim.x) {
+        int iy = (int)(i / nx), ix = (int)(i % nx);
+        float v = img[i];
+        if (!isfinite(v)) bad = 1;
+        if (normalize) v = (v - avg) / nd;
+        if (use_mask) {
+            float yy = (-y0 + (float)iy) * (-y0 + (float)iy);
+            float xx = (-x0 + (float)ix) * (-x0 + (float)ix);
+            float ra = sqrtf(yy + xx);
+            if (ra > R1 && ra <= R2) {
+                float edge = (1.0f + cosf(pi * (ra - R1) / 6.0f)) / 2.0f;
+                v = (float)((double)(v * edge) + (double)(1.0f - edge) * summ);
+            }
+            if (ra > R2) v = (float)summ;
+        }
+        if ((ix + iy) & 1) v = -v;
+        o[i] = make_float2(v, 0.0f);
+    }
+    if (bad) atomicOr(flag, 1);
+}
+
+// FT_amp_expfit.f90:27-46: per-ring means, log, 2x2 least squares, Fcut.
+__device__ void expfit_finish(const double* sfav, const double* sres, const int* snum, int nr,
+                              float* out) {
+    float aa11 = 0.f, aa12 = 0.f, aa22 = 0.f, bb1 = 0.f, bb2 = 0.f;
+    for (int k = 0; k < nr; ++k) {
+        float fa = (float)sfav[k], rl = (float)sres[k];
+        int num = snum[k];
+        float fl;
+        if (num > 0 && fa > 0.0f) {
+            rl = rl / (float)num;
+            fl = logf(fa / (float)num);
+        } else {
+            fl = 0.0f;
+        }
+        aa11 = aa11 + rl * rl;
+        aa12 = aa12 + rl * 1.0f;
+        aa22 = aa22 + 1.0f * 1.0f;
+        bb1 = bb1 + rl * fl;
+        bb2 = bb2 + 1.0f * fl;
+    }
+    float aa21 = aa12;
+    float x2 = (bb2 - bb1 * aa21 / aa11) / (aa22 - aa12 * aa21 / aa11);
+    float x1 = (bb1 - aa12 * x2) / aa11;
+    for (int k = 0; k < nr; ++k) {
+        float rl = (float)sres[k];
+        int num = snum[k];
+        if (num > 0 && (float)sfav[k] > 0.0f) rl = rl / (float)num;
+        out[k] = expf(rl * x1 + x2) * 0.8f;
+    }
+}
+
+// ---------------------------------------------------------------------------
+// after the forward FFT: 1/nx^2, b = -Im (img2d_FFT.f90:18-19, FFTW.f90:185),
+// Fcut fit (FT_amp_expfit.f90:13-25), optional origin shift (img2d_FT_centshift.f90:8-16)
+// and extraction of the band window.
+// ---------------------------------------------------------------------------
+__global__ void k_post_fft(const float2* __restrict__ fft, Band bd, const float* __restrict__ sx,
+                           const float* __restrict__ sy, float pi, float2* __restrict__ band,
+                           float* __restrict__ fcut) {
+    extern __shared__ double dsm[];
+    const int nr = bd.nr, R = bd.max_r, nx = bd.nx, h = nx / 2;
+    double* sfav = dsm;
+    double* sres = dsm + nr;
+    int* snum = (int*)(dsm + 2 * nr);
+    const int p = blockIdx.x;
+    const long nn = (long)nx * nx;
+    const float2* f = fft + p * nn;
+    for (int k = threadIdx.x; k < nr; k += blockDim.x) { sfav[k] = 0; sres[k] = 0; snum[k] = 0; }
+    __syncthreads();
+    const float s = (float)nn;
+    const int span = 2 * R + 1, cnt = (R + 1) * span;
+    for (int q = threadIdx.x; q < cnt; q += blockDim.x) {
+        int ky = q / span, hx = q % span - R;
+        float rad = sqrtf((float)(hx * hx + ky * ky));
+        int ir = (int)(rad + 0.5f);
+        if (ir >= bd.min_r && ir <= R) {
+            float2 v = f[(long)(ky + h) * nx + (hx + h)];
+            float a = v.x / s, b = -(v.y / s);
+            float amp = sqrtf(a * a + b * b);
+            atomicAdd(&sfav[ir - bd.min_r], (double)amp);
+            atomicAdd(&sres[ir - bd.min_r], (double)rad);
+            atomicAdd(&snum[ir - bd.min_r], 1);
+        }
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) expfit_finish(sfav, sres, snum, nr, fcut + (long)p * nr);
+    const int W = bd.W;
+    const bool shift = (sx != nullptr);
+    const float xs = shift ? sx[p] + (float)h : 0.f, ys = shift ? sy[p] + (float)h : 0.f;
+    float2* ob = band + (long)p * W * W;
+    for (int q = threadIdx.x; q < W * W; q += blockDim.x) {
+        int by = q / W, bx = q % W;
+        int hi = bd.off + bx, ki = bd.off + by;
+        float2 v = f[(long)ki * nx + hi];
+        float a = v.x / s, b = -(v.y / s);
+        if (shift) {
+            int hx = hi - h, ky = ki - h;
+            float phase = 2.0f * pi * (xs * (float)hx + ys * (float)ky) / (float)nx;
+            float c = cosf(phase), sn = sinf(phase);
+            float fr = (a * c + b * sn);
+            float fi = (-a * sn + b * c);
+            a = fr;
+            b = fi;
+        }
+        ob[q] = make_float2(a, b);
+    }
+}
+
+// getCTF2d.f90:2-29 evaluated over the band window.
+__global__ void k_ctf_band(Band bd, const float* __restrict__ dfs, float apix, float vol, float cs0,
+                           float ampwg, float pi, float* __restrict__ ctf) {
+    const int p = blockIdx.y;
+    const int W = bd.W, R = bd.max_r;
+    const int q = blockIdx.x * blockDim.x + threadIdx.x;
+    if (q >= W * W) return;
+    const float d2r = pi / 180.0f;
+    float lam = 0.387818f / sqrtf(1.0f * vol * (1.0f + 0.978459E-3f * vol));
+    float cs = cs0 * 1.0e7f, df1 = dfs[p * 3] * 1.0e4f, df2 = dfs[p * 3 + 1] * 1.0e4f;
+    float astig = dfs[p * 3 + 2] * d2r;
+    int ky = q / W - R, hx = q % W - R;
+    float phi = atan2f((float)ky, (float)hx);
+    if (phi < 0.0f) phi = phi + 2.0f * pi;
+    phi = phi - astig;
+    float c = cosf(phi), s = sinf(phi);
+    float df = df1 * (c * c) + df2 * (s * s);
+    float res = sqrtf((float)(hx * hx + ky * ky)) / (float)bd.nx / apix;
+    float r2 = res * res, r4 = r2 * r2, lam3 = lam * lam * lam;
+    float phase = 2.0f * pi * (-(cs * lam3 * r4 / 4.0f) + df * lam * r2 / 2.0f);
+    float sq = sqrtf(1.0f - ampwg * ampwg);
+    ctf[(long)p * W * W + q] = -(sq * sinf(phase) + ampwg * cosf(phase));
+}
+
+// Fcut of (template x CTF): cal_crosslin_PR_omega.f90:34-38, hoisted per particle.
+__global__ void k_tmpl_fcut(const float2* __restrict__ tband, int T, const float* __restrict__ ctf,
+                            Band bd, float* __restrict__ tfcut) {
+    extern __shared__ double dsm[];
+    const int nr = bd.nr, R = bd.max_r, W = bd.W;
+    double* sfav = dsm;
+    double* sres = dsm + nr;
+    int* snum = (int*)(dsm + 2 * nr);
+    const int i = blockIdx.x, p = blockIdx.y;
+    for (int k = threadIdx.x; k < nr; k += blockDim.x) { sfav[k] = 0; sres[k] = 0; snum[k] = 0; }
+    __syncthreads();
+    const float2* tb = tband + (long)i * W * W;
+    const float* cb = ctf + (long)p * W * W;
+    const int span = 2 * R + 1, cnt = (R + 1) * span;
+    for (int q = threadIdx.x; q < cnt; q += blockDim.x) {
+        int ky = q / span, hx = q % span - R;
+        float rad = sqrtf((float)(hx * hx + ky * ky));
+        int ir = (int)(rad + 0.5f);
+        if (ir >= bd.min_r && ir <= R) {
+            int b = (ky + R) * W + (hx + R);
+            float c = cb[b];
+            float2 t = tb[b];
+            float a2 = t.x * c, b2 = t.y * c;
+            float amp = sqrtf(a2 * a2 + b2 * b2);
+            atomicAdd(&sfav[ir - bd.min_r], (double)amp);
+            atomicAdd(&sres[ir - bd.min_r], (double)rad);
+            atomicAdd(&snum[ir - bd.min_r], 1);
+        }
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) expfit_finish(sfav, sres, snum, nr, tfcut + ((long)p * T + i) * nr);
+}
+
+// icos_crosslin_angle.f90 for every (view, template, operator).
+__global__ void k_alpha_table(const float* __restrict__ views, int V, const float* __restrict__ tort,
+                              int T, const float* __restrict__ ops, float d2r, float r2d,
+                              float2* __restrict__ alpha) {
+    long q = (long)blockIdx.x * blockDim.x + threadIdx.x;
+    long total = (long)V * T * 60;
+    if (q >= total) return;
+    int j = (int)(q % 60);
+    int i = (int)((q / 60) % T);
+    int v = (int)(q / (60L * T));
+    float e1[9], e2[9];
+    euler_mat(views[v * 2], views[v * 2 + 1], 0.0f, d2r, e1);
+    euler_mat(tort[i * 3], tort[i * 3 + 1], tort[i * 3 + 2], d2r, e2);
+    float a1, a2;
+    crosslin_pair(e1, e2, ops + j * 9, r2d, &a1, &a2);
+    alpha[q] = make_float2(a1, a2);
+}
+
+// ort_cent_11.f90:1-94 (state = theta, phi, omega, x, y, pr per image).
+__global__ void k_refine_candidates(float* __restrict__ state, int B, float dang, float dtran,
+                                    const float* __restrict__ ops, float d2r,
+                                    float* __restrict__ cand) {
+    int p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= B) return;
+    float* st = state + p * 6;
+    float th0 = st[0], ph0 = st[1], om0 = st[2], x0 = st[3], y0 = st[4];
+    asu_fold(&th0, &ph0, &om0, ops, d2r);
+    st[0] = th0; st[1] = ph0; st[2] = om0;
+    for (int jj = 0; jj <= 10; ++jj) {
+        float th = th0, ph = ph0, om = om0, x = x0, y = y0;
+        switch (jj) {
+            case 1: th = th0 - dang; break;
+            case 2: th = th0 + dang; break;
+            case 3: ph = ph0 - dang; break;
+            case 4: ph = ph0 + dang; break;
+            case 5: om = om0 - dang; break;
+            case 6: om = om0 + dang; break;
+            case 7: x = x0 - dtran; break;
+            case 8: x = x0 + dtran; break;
+            case 9: y = y0 - dtran; break;
+            case 10: y = y0 + dtran; break;
+            default: break;
+        }
+        asu_fold(&th, &ph, &om, ops, d2r);
+        float* o = cand + ((long)p * 11 + jj) * 5;
+        o[0] = th; o[1] = ph; o[2] = om; o[3] = x; o[4] = y;
+    }
+}
+
+__global__ void k_refine_alpha(const float* __restrict__ cand, int B, const float* __restrict__ tort,
+                               int T, const float* __restrict__ ops, float d2r, float r2d,
+                               float2* __restrict__ alpha) {
+    long q = (long)blockIdx.x * blockDim.x + threadIdx.x;
+    long total = (long)B * 11 * T * 60;
+    if (q >= total) return;
+    int j = (int)(q % 60);
+    int i = (int)((q / 60) % T);
+    long pc = q / (60L * T);  // p*11 + c
+    const float* c = cand + pc * 5;
+    float e1[9], e2[9];
+    euler_mat(c[0], c[1], c[2], d2r, e1);
+    euler_mat(tort[i * 3], tort[i * 3 + 1], tort[i * 3 + 2], d2r, e2);
+    float a1, a2;
+    crosslin_pair(e1, e2, ops + j * 9, r2d, &a1, &a2);
+    alpha[q] = make_float2(a1, a2);
+}
+
+// ort_refinement.f90:85-91: first minimum of the 11 scores.
+__global__ void k_refine_select(const float* __restrict__ cand, const float* __restrict__ pr, int B,
+                                float* __restrict__ state) {
+    int p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= B) return;
+    const float* v = pr + p * 11;
+    int mn = 0;
+    for (int jj = 1; jj <= 10; ++jj)
+        if (v[jj] < v[mn]) mn = jj;
+    const float* c = cand + ((long)p * 11 + mn) * 5;
+    float* st = state + p * 6;
+    st[0] = c[0]; st[1] = c[1]; st[2] = c[2]; st[3] = c[3]; st[4] = c[4]; st[5] = v[mn];
+}
+
+// ---------------------------------------------------------------------------
+// reconstruction finish: reconstruct.f90:151-241 (Friedel completion, divide by the
+// CTF^2 weights in FP64, (-1)^(h+k+l) sign) into FFT3d = cmplx(fa, -fb).
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ long acc_index(const Band& bd, int hx, int ky, int lz) {
+    return acc_cell(bd, hx, ky, lz);
+}
+__device__ __forceinline__ long vol_index(int nx, int hx, int ky, int lz) {
+    int h = nx / 2;
+    return ((long)(lz + h) * nx + (ky + h)) * nx + (hx + h);
+}
+__device__ __forceinline__ float qdiv(float a, float w) { return (float)((double)a / (double)w); }
+
+__global__ void k_rec_fold_plane0(const float4* __restrict__ acc, Band bd, float2* __restrict__ vol) {
+    const int R = bd.max_r, span = 2 * R + 1;
+    int q = blockIdx.x * blockDim.x + threadIdx.x;
+    int n_a = R * span, n_b = R;
+    if (q > n_a + n_b) return;
+    if (q == n_a + n_b) {  // origin: reconstruct.f90:205-208
+        float4 v = acc[acc_index(bd, 0, 0, 0)];
+        vol[vol_index(bd.nx, 0, 0, 0)] = make_float2(qdiv(v.x, v.z), -0.0f);
+        return;
+    }
+    int hx, ky;
+    if (q < n_a) { ky = 1 + q / span; hx = q % span - R; }
+    else { ky = 0; hx = 1 + (q - n_a); }
+    float4 v1 = acc[acc_index(bd, hx, ky, 0)];
+    float4 v2 = acc[acc_index(bd, -hx, -ky, 0)];
+    float dr = sqrtf((float)(hx * hx + ky * ky));
+    float fa1 = 0.f, fb1 = 0.f, fa2 = 0.f, fb2 = 0.f;
+    if (dr <= (float)R) {
+        float w = v1.z + v2.z;
+        fa1 = qdiv(v1.x + v2.x, w);
+        fb1 = qdiv(v1.y - v2.y, w);
+        if (((hx + ky) & 1) == 0) { fa2 = fa1; fb2 = -fb1; }
+        else { fa1 = -fa1; fb1 = -fb1; fa2 = fa1; fb2 = -fb1; }
+    }
+    vol[vol_index(bd.nx, hx, ky, 0)] = make_float2(fa1, -fb1);
+    vol[vol_index(bd.nx, -hx, -ky, 0)] = make_float2(fa2, -fb2);
+}
+
+__global__ void k_rec_fold_upper(const float4* __restrict__ acc, Band bd, float2* __restrict__ vol) {
+    const int R = bd.max_r, span = 2 * R + 1;
+    long q = (long)blockIdx.x * blockDim.x + threadIdx.x;
+    long total = (long)R * span * span;
+    if (q >= total) return;
+    int hx = (int)(q % span) - R;
+    int ky = (int)((q / span) % span) - R;
+    int lz = 1 + (int)(q / ((long)span * span));
+    float dr = sqrtf((float)(hx * hx + ky * ky + lz * lz));
+    float fa1 = 0.f, fb1 = 0.f;
+    if (dr <= (float)R) {
+        float4 v = acc[acc_index(bd, hx, ky, lz)];
+        fa1 = qdiv(v.x, v.z);
+        fb1 = qdiv(v.y, v.z);
+        if ((hx + ky + lz) & 1) { fa1 = -fa1; fb1 = -fb1; }
+    }
+    vol[vol_index(bd.nx, hx, ky, lz)] = make_float2(fa1, -fb1);
+    vol[vol_index(bd.nx, -hx, -ky, -lz)] = make_float2(fa1, fb1);
+}
+
+// shift3dComplex (FFTW.f90:304-321) and the real part (reconstruct.f90:246-247)
+__global__ void k_rec_real(const float2* __restrict__ vol, int nx, float* __restrict__ map) {
+    long q = (long)blockIdx.x * blockDim.x + threadIdx.x;
+    long n3 = (long)nx * nx * nx;
+    if (q >= n3) return;
+    int hx = (int)(q % nx), ky = (int)((q / nx) % nx), lz = (int)(q / ((long)nx * nx));
+    float v = vol[q].x;
+    map[q] = ((hx + ky + lz) & 1) ? -v : v;
+}
+
+// project_template2d.f90:33-73: one thread per output pixel, z summed in order.
+__global__ void k_project(const float* __restrict__ map, int nx, const float* __restrict__ eul,
+                          float d2r, float* __restrict__ out) {
+    __shared__ float rot[9];
+    const int o = blockIdx.y;
+    if (threadIdx.x == 0) euler_mat(eul[o * 3], eul[o * 3 + 1], eul[o * 3 + 2], d2r, rot);
+    __syncthreads();
+    const long nn = (long)nx * nx;
+    long i2 = (long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i2 >= nn) return;
+    const int h = nx / 2;
+    const int ix = (int)(i2 % nx), iy = (int)(i2 / nx);
+    float acc = 0.0f;
+    for (int iz = 0; iz < nx; ++iz) {
+        float xp[3] = {(float)ix - (float)h, (float)iy - (float)h, (float)iz - (float)h};
+        if (sqrtf(xp[0] * xp[0] + xp[1] * xp[1] + xp[2] * xp[2]) >= (float)(h - 1)) continue;
+        float x[3];
+        mv3(rot, xp, x);
+        x[0] = x[0] + (float)h; x[1] = x[1] + (float)h; x[2] = x[2] + (float)h;
+        int jx = (int)x[0], jy = (int)x[1], jz = (int)x[2];
+        float xb = x[0] - (float)jx, yb = x[1] - (float)jy, zb = x[2] - (float)jz;
+        long n1 = (long)jz * nn + (long)jy * nx + jx;
+        acc = acc + (1.f - xb) * (1.f - yb) * (1.f - zb) * map[n1];
+        acc = acc + xb * (1.f - yb) * (1.f - zb) * map[n1 + 1];
+        acc = acc + (1.f - xb) * yb * (1.f - zb) * map[n1 + nx];
+        acc = acc + xb * yb * (1.f - zb) * map[n1 + nx + 1];
+        acc = acc + (1.f - xb) * (1.f - yb) * zb * map[n1 + nn];
+        acc = acc + xb * (1.f - yb) * zb * map[n1 + nn + 1];
+        acc = acc + (1.f - xb) * yb * zb * map[n1 + nn + nx];
+        acc = acc + xb * yb * zb * map[n1 + nn + nx + 1];
+    }
+    out[(long)o * nn + i2] = acc;
+}
+
+// project2d_FT3dTo2d.f90:27-84: trilinear central section of a centred 3D FT.
+__global__ void k_sections(const float* __restrict__ fre, const float* __restrict__ fim, int nx,
+                           const float* __restrict__ eul, float d2r, float* __restrict__ ore,
+                           float* __restrict__ oim) {
+    __shared__ float rot[9];
+    const int o = blockIdx.y;
+    if (threadIdx.x == 0) euler_mat(eul[o * 3], eul[o * 3 + 1], eul[o * 3 + 2], d2r, rot);
+    __syncthreads();
+    const long nn = (long)nx * nx;
+    long n = (long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (n >= nn) return;
+    const int h = nx / 2;
+    const int ix = (int)(n % nx) - h, iy = (int)(n / nx) - h;
+    float xp[3] = {(float)ix, (float)iy, 0.0f}, xx[3];
+    mv3(rot, xp, xx);
+    float vr = 0.f, vi = 0.f;
+    if (!(sqrtf(xx[0] * xx[0] + xx[1] * xx[1] + xx[2] * xx[2]) > (float)(h - 2))) {
+        xx[0] = xx[0] + (float)h; xx[1] = xx[1] + (float)h; xx[2] = xx[2] + (float)h;
+        int hx = (int)xx[0], ky = (int)xx[1], lz = (int)xx[2];
+        float xb = xx[0] - (float)hx, yb = xx[1] - (float)ky, zb = xx[2] - (float)lz;
+        long b0 = (long)lz * nn + (long)ky * nx + hx;
+        const float w1 = (1.f - xb) * (1.f - yb) * (1.f - zb), w2 = xb * (1.f - yb) * (1.f - zb);
+        const float w3 = (1.f - xb) * yb * (1.f - zb), w4 = xb * yb * (1.f - zb);
+        const float w5 = (1.f - xb) * (1.f - yb) * zb, w6 = xb * (1.f - yb) * zb;
+        const float w7 = (1.f - xb) * yb * zb, w8 = xb * yb * zb;
+        vr = w1 * fre[b0] + w2 * fre[b0 + 1] + w3 * fre[b0 + nx] + w4 * fre[b0 + nx + 1] +
+             w5 * fre[b0 + nn] + w6 * fre[b0 + nn + 1] + w7 * fre[b0 + nn + nx] +
+             w8 * fre[b0 + nn + nx + 1];
+        vi = w1 * fim[b0] + w2 * fim[b0 + 1] + w3 * fim[b0 + nx] + w4 * fim[b0 + nx + 1] +
+             w5 * fim[b0 + nn] + w6 * fim[b0 + nn + 1] + w7 * fim[b0 + nn + nx] +
+             w8 * fim[b0 + nn + nx + 1];
+    }
+    ore[(long)o * nn + n] = vr;
+    oim[(long)o * nn + n] = vi;
+}
+
+inline int cdiv(long a, long b) { return (int)((a + b - 1) / b); }
+
+}  // namespace
+
+void launch_prep_images(const float* imgs, int B, int nx, const float* ox, const float* oy,
+                        int use_mask, float mask_px, int normalize, float2* fft, int* flag,
+                        cudaStream_t st) {
+    k_prep_images<<<B, 1024, 0, st>>>(imgs, nx, ox, oy, use_mask, mask_px, normalize, angles().pi,
+                                      fft, flag);
+}
+
+void launch_post_fft(const float2* fft, int B, Band bd, const float* sx, const float* sy,
+                     float2* band, float* fcut, cudaStream_t st) {
+    size_t sm = (size_t)bd.nr * (2 * sizeof(double) + sizeof(int)) + 16;
+    k_post_fft<<<B, 1024, sm, st>>>(fft, bd, sx, sy, angles().pi, band, fcut);
+}
+
+void launch_ctf_band(int B, Band bd, const float* dfs, float apix, float vol, float cs,
+                     float ampwg, float* ctf, cudaStream_t st) {
+    dim3 g(cdiv((long)bd.W * bd.W, 256), B);
+    k_ctf_band<<<g, 256, 0, st>>>(bd, dfs, apix, vol, cs, ampwg, angles().pi, ctf);
+}
+
+void launch_tmpl_fcut(const float2* tband, int T, const float* ctf, int B, Band bd, float* tfcut,
+                      cudaStream_t st) {
+    size_t sm = (size_t)bd.nr * (2 * sizeof(double) + sizeof(int)) + 16;
+    dim3 g(T, B);
+    k_tmpl_fcut<<<g, 512, sm, st>>>(tband, T, ctf, bd, tfcut);
+}
+
+void launch_alpha_table(const float* views, int V, const float* tort, int T, const float* ops,
+                        float2* alpha, cudaStream_t st) {
+    long total = (long)V * T * 60;
+    HostAngles a = angles();
+    k_alpha_table<<<cdiv(total, 128), 128, 0, st>>>(views, V, tort, T, ops, a.d2r, a.r2d, alpha);
+}
+
+void launch_refine_candidates(float* state, int B, float dang, float dtran, const float* ops,
+                              float* cand, cudaStream_t st) {
+    k_refine_candidates<<<cdiv(B, 64), 64, 0, st>>>(state, B, dang, dtran, ops, angles().d2r, cand);
+}
+
+void launch_refine_alpha(const float* cand, int B, const float* tort, int T, const float* ops,
+                         float2* alpha, cudaStream_t st) {
+    long total = (long)B * 11 * T * 60;
+    HostAngles a = angles();
+    k_refine_alpha<<<cdiv(total, 128), 128, 0, st>>>(cand, B, tort, T, ops, a.d2r, a.r2d, alpha);
+}
+
+void launch_refine_select(const float* cand, const float* pr, int B, float* state,
+                          cudaStream_t st) {
+    k_refine_select<<<cdiv(B, 64), 64, 0, st>>>(cand, pr, B, state);
+}
+
+void launch_rec_fold(const float4* acc, Band bd, float2* vol, cudaStream_t st) {
+    const int R = bd.max_r, span = 2 * R + 1;
+    int n0 = R * span + R + 1;
+    k_rec_fold_plane0<<<cdiv(n0, 256), 256, 0, st>>>(acc, bd, vol);
+    long n1 = (long)R * span * span;
+    k_rec_fold_upper<<<cdiv(n1, 256), 256, 0, st>>>(acc, bd, vol);
+}
+
+void launch_rec_real(const float2* vol, int nx, float* map, cudaStream_t st) {
+    long n3 = (long)nx * nx * nx;
+    k_rec_real<<<cdiv(n3, 256), 256, 0, st>>>(vol, nx, map);
+}
+
+void launch_project(const float* map, int nx, const float* eul, int n, float* out,
+                    cudaStream_t st) {
+    dim3 g(cdiv((long)nx * nx, 128), n);
+    k_project<<<g, 128, 0, st>>>(map, nx, eul, angles().d2r, out);
+}
+
+void launch_sections(const float* fre, const float* fim, int nx, const float* eul, int n,
+                     float* ore, float* oim, cudaStream_t st) {
+    dim3 g(cdiv((long)nx * nx, 256), n);
+    k_sections<<<g, 256, 0, st>>>(fre, fim, nx, eul, angles().d2r, ore, oim);
+}
+
+}  // namespace cryoim

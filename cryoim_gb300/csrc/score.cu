@@ -1,0 +1,371 @@
+// score.cu — cross-common-line phase-residual scoring and symmetrised insertion.
+//
+// k_pr_omega is the hot kernel of the global search (cal_crosslin_PR_omega.f90 for
+// every asymmetric-unit view of every particle).  One CTA owns one (particle, view):
+//   * the particle's band-limited Fourier window (W x W float2) sits in shared memory
+//     for the whole CTA, so every bilinear tap is a shared-memory load;
+//   * thread (g, k) owns omega index k and accumulates PR1(k), PR2(k) in registers over
+//     the lines j = g, g+G, ... of every template (no cross-thread reduction until the
+//     end of the view), with per-line FP32 partial sums folded into Kahan-compensated
+//     running sums;
+//   * per template, the 60 x nR template line samples (template x CTF, bilinear) are
+//     staged once into shared memory as (amplitude or -1 if below Fcut, phase);
+//   * the per-view argmin over omega is folded into a per-particle 64-bit key
+//     (PR bits << 32 | column-major index) with atomicMin, which reproduces Fortran
+//     minloc's first-occurrence rule.
+// The sampling positions x = FR*cos + nx/2 are rounded exactly as the reference
+// rounds them (separate multiply and add), so the bilinear taps and weights match it.
+#include <cstdio>
+
+#include "geom.cuh"
+#include "kernels.h"
+
+namespace cryoim {
+namespace {
+
+__device__ __forceinline__ void kahan_add(float& s, float& c, float x) {
+    float y = x - c;
+    float t = s + y;
+    c = (t - s) - y;
+    s = t;
+}
+
+__device__ __forceinline__ float bilerp(float ax, float ay, float v00, float v10, float v01,
+                                        float v11) {
+    float bx = 1.0f - ax, by = 1.0f - ay;
+    return bx * by * v00 + ax * by * v10 + bx * ay * v01 + ax * ay * v11;
+}
+
+struct Consts {
+    float d2r, r2d, pi, tpi;
+};
+
+// Template line sample (template x CTF, bilinear) at angle alpha2, radius fr.
+__device__ __forceinline__ void tmpl_sample(const float2* __restrict__ tb, const float* __restrict__ cb,
+                                            int W, int offW, float nxh, float alpha2, float fr,
+                                            float d2r, float* re, float* im) {
+    float ang = __fmul_rn(alpha2, d2r);
+    float cs = cosf(ang), sn = sinf(ang);
+    float x = __fadd_rn(__fmul_rn(fr, cs), nxh), y = __fadd_rn(__fmul_rn(fr, sn), nxh);
+    int lx = (int)x, ly = (int)y;
+    float ax = __fsub_rn(x, (float)lx), ay = __fsub_rn(y, (float)ly);
+    int b0 = ly * W + lx - offW;
+    float2 t00 = tb[b0], t10 = tb[b0 + 1], t01 = tb[b0 + W], t11 = tb[b0 + W + 1];
+    if (cb) {
+        float c00 = cb[b0], c10 = cb[b0 + 1], c01 = cb[b0 + W], c11 = cb[b0 + W + 1];
+        t00.x = __fmul_rn(t00.x, c00); t00.y = __fmul_rn(t00.y, c00);
+        t10.x = __fmul_rn(t10.x, c10); t10.y = __fmul_rn(t10.y, c10);
+        t01.x = __fmul_rn(t01.x, c01); t01.y = __fmul_rn(t01.y, c01);
+        t11.x = __fmul_rn(t11.x, c11); t11.y = __fmul_rn(t11.y, c11);
+    }
+    *re = bilerp(ax, ay, t00.x, t10.x, t01.x, t11.x);
+    *im = bilerp(ax, ay, t00.y, t10.y, t01.y, t11.y);
+}
+
+__global__ void __launch_bounds__(768, 1) k_pr_omega(PrOmegaArgs a, int nomp, Consts K) {
+    extern __shared__ __align__(16) unsigned char smraw[];
+    const Band bd = a.bd;
+    const int W = bd.W, nr = bd.nr, minR = bd.min_r;
+    float2* sband = reinterpret_cast<float2*>(smraw);
+    float2* sline = sband + W * W;
+    float* sfc0 = reinterpret_cast<float*>(sline + 60 * nr);
+    float* salpha = sfc0 + ((nr + 3) & ~3);
+    float* sred = salpha + 64;
+    unsigned long long* skey = reinterpret_cast<unsigned long long*>(sred + 2 * blockDim.x);
+
+    const int p = blockIdx.y, t = threadIdx.x;
+    const int G = blockDim.x / nomp, g = t / nomp, k = t - g * nomp;
+    {
+        const float4* gb = reinterpret_cast<const float4*>(a.band + (long)p * W * W);
+        float4* sb4 = reinterpret_cast<float4*>(sband);
+        for (int q = t; q < (W * W) / 2; q += blockDim.x) sb4[q] = gb[q];
+        for (int q = t; q < nr; q += blockDim.x) sfc0[q] = a.fcut0[(long)p * nr + q];
+    }
+    const float nxh = (float)(bd.nx / 2);
+    const int offW = bd.off * W + bd.off;
+    const float* ctfp = a.ctf ? a.ctf + (long)p * W * W : nullptr;
+    const float* tfc = a.tfcut + (long)p * a.tfcut_pstride;
+    const float womega = __fmul_rn(a.step, (float)k);
+    const int nwarps = blockDim.x >> 5;
+
+    for (int v = blockIdx.x; v < a.V; v += gridDim.x) {
+        float pr1 = 0.f, pr2 = 0.f, c1 = 0.f, c2 = 0.f;
+        for (int i = 0; i < a.T; ++i) {
+            __syncthreads();
+            const float2* al = a.alpha + ((long)v * a.T + i) * 60;
+            if (t < 60) {
+                float2 aa = al[t];
+                salpha[t] = (aa.x < 999.0f && aa.y < 999.0f) ? aa.x : 1000.0f;
+            }
+            const float2* tb = a.tband + (long)i * W * W;
+            const float* fct = tfc + (long)i * nr;
+            for (int q = t; q < 60 * nr; q += blockDim.x) {
+                int j = q / nr, iq = q - j * nr;
+                float2 aa = al[j];
+                float amp2 = -1.0f, ph2 = 0.0f;
+                if (aa.x < 999.0f && aa.y < 999.0f) {
+                    float re, im;
+                    tmpl_sample(tb, ctfp, W, offW, nxh, aa.y, (float)(minR + iq), K.d2r, &re, &im);
+                    float amp = sqrtf(re * re + im * im);
+                    if (amp >= fct[iq]) { amp2 = amp; ph2 = atan2f(im, re); }
+                }
+                sline[q] = make_float2(amp2, ph2);
+            }
+            __syncthreads();
+            if (k < a.nomega) {
+                for (int j = g; j < 60; j += G) {
+                    const float al1 = salpha[j];
+                    if (!(al1 < 999.0f)) continue;
+                    const float ang = __fmul_rn(__fsub_rn(al1, womega), K.d2r);
+                    float sn, cs;
+                    sincosf(ang, &sn, &cs);
+                    const float2* sl = sline + j * nr;
+                    float l1 = 0.f, l2 = 0.f;
+#pragma unroll 2
+                    for (int iq = 0; iq < nr; ++iq) {
+                        const float2 tl = sl[iq];
+                        if (tl.x < 0.0f) continue;
+                        const float fr = (float)(minR + iq);
+                        const float x = __fadd_rn(__fmul_rn(fr, cs), nxh);
+                        const float y = __fadd_rn(__fmul_rn(fr, sn), nxh);
+                        const int lx = (int)x, ly = (int)y;
+                        const float ax = x - (float)lx, ay = y - (float)ly;
+                        const int b0 = ly * W + lx - offW;
+                        const float2 t00 = sband[b0], t10 = sband[b0 + 1];
+                        const float2 t01 = sband[b0 + W], t11 = sband[b0 + W + 1];
+                        const float re = bilerp(ax, ay, t00.x, t10.x, t01.x, t11.x);
+                        const float im = bilerp(ax, ay, t00.y, t10.y, t01.y, t11.y);
+                        const float amp1 = sqrtf(re * re + im * im);
+                        if (amp1 >= sfc0[iq]) {
+                            const float ph1 = atan2f(im, re);
+                            float d = fabsf(tl.y - ph1);
+                            d = fminf(d, K.tpi - d);
+                            const float w = 0.5f * (amp1 + tl.x);
+                            l1 = fmaf(d, w, l1);
+                            l2 = l2 + w;
+                        }
+                    }
+                    kahan_add(pr1, c1, l1);
+                    kahan_add(pr2, c2, l2);
+                }
+            }
+        }
+        sred[2 * t] = pr1;
+        sred[2 * t + 1] = pr2;
+        __syncthreads();
+        unsigned long long key = ~0ull;
+        if (g == 0 && k < a.nomega) {
+            float s1 = 0.f, s2 = 0.f;
+            for (int gg = 0; gg < G; ++gg) {
+                s1 += sred[2 * (gg * nomp + k)];
+                s2 += sred[2 * (gg * nomp + k) + 1];
+            }
+            const float pr = (s2 > 1.0e-10f) ? s1 / s2 * K.r2d : 999.0f;
+            const int base = __float_as_int(a.views[(long)v * 4 + 2]);
+            if (a.pr_array) a.pr_array[(long)p * a.per + base + k] = pr;
+            key = ((unsigned long long)__float_as_uint(pr) << 32) | (unsigned)(base + k);
+        }
+        for (int o = 16; o > 0; o >>= 1) {
+            unsigned long long other = __shfl_xor_sync(0xffffffffu, key, o);
+            key = other < key ? other : key;
+        }
+        if ((t & 31) == 0) skey[t >> 5] = key;
+        __syncthreads();
+        if (t < 32) {
+            key = (t < nwarps) ? skey[t] : ~0ull;
+            for (int o = 16; o > 0; o >>= 1) {
+                unsigned long long other = __shfl_xor_sync(0xffffffffu, key, o);
+                key = other < key ? other : key;
+            }
+            if (t == 0) atomicMin(a.best + p, key);
+        }
+    }
+}
+
+// cal_crosslin_PR.f90:2-71 for the 11 candidates of each particle; the candidate
+// origin shift (img2d_FT_centshift.f90) is applied to each bilinear tap, which is the
+// same per-pixel arithmetic as shifting the whole transform first.
+__global__ void __launch_bounds__(512) k_pr_single(PrSingleArgs a, Consts K) {
+    __shared__ double sh[2][32];
+    const Band bd = a.bd;
+    const int W = bd.W, nr = bd.nr, minR = bd.min_r, nx = bd.nx;
+    const int c = blockIdx.x, p = blockIdx.y;
+    const float* cd = a.cand + ((long)p * 11 + c) * 5;
+    const float nxh = (float)(nx / 2);
+    const float xs = __fadd_rn(cd[3], nxh), ys = __fadd_rn(cd[4], nxh);
+    const int offW = bd.off * W + bd.off;
+    const float2* pb = a.band + (long)p * W * W;
+    const float* ctfp = a.ctf ? a.ctf + (long)p * W * W : nullptr;
+    const float* fc0 = a.fcut0 + (long)p * nr;
+    const float* tfc = a.tfcut + (long)p * a.tfcut_pstride;
+    const float twopi = __fmul_rn(2.0f, K.pi);
+    double p1 = 0.0, p2 = 0.0;
+    for (int i = 0; i < a.T; ++i) {
+        const float2* al = a.alpha + (((long)p * 11 + c) * a.T + i) * 60;
+        const float2* tb = a.tband + (long)i * W * W;
+        const float* fct = tfc + (long)i * nr;
+        for (int q = threadIdx.x; q < 60 * nr; q += blockDim.x) {
+            int j = q / nr, iq = q - j * nr;
+            float2 aa = al[j];
+            if (!(aa.x < 999.0f && aa.y < 999.0f)) continue;
+            const float fr = (float)(minR + iq);
+            // particle sample with the candidate origin shift on each tap
+            float ang = __fmul_rn(aa.x, K.d2r);
+            float cs = cosf(ang), sn = sinf(ang);
+            float x = __fadd_rn(__fmul_rn(fr, cs), nxh), y = __fadd_rn(__fmul_rn(fr, sn), nxh);
+            int lx = (int)x, ly = (int)y;
+            float ax = __fsub_rn(x, (float)lx), ay = __fsub_rn(y, (float)ly);
+            float tr[4], ti[4];
+#pragma unroll
+            for (int u = 0; u < 4; ++u) {
+                int tx = lx + (u & 1), ty = ly + (u >> 1);
+                float2 vv = pb[ty * W + tx - offW];
+                int hx = tx - nx / 2, ky = ty - nx / 2;
+                float ph = __fdiv_rn(__fmul_rn(twopi, __fadd_rn(__fmul_rn(xs, (float)hx),
+                                                                 __fmul_rn(ys, (float)ky))),
+                                     (float)nx);
+                float s, co;
+                sincosf(ph, &s, &co);
+                tr[u] = __fadd_rn(__fmul_rn(vv.x, co), __fmul_rn(vv.y, s));
+                ti[u] = __fadd_rn(__fmul_rn(-vv.x, s), __fmul_rn(vv.y, co));
+            }
+            float re1 = bilerp(ax, ay, tr[0], tr[1], tr[2], tr[3]);
+            float im1 = bilerp(ax, ay, ti[0], ti[1], ti[2], ti[3]);
+            float re2, im2;
+            tmpl_sample(tb, ctfp, W, offW, nxh, aa.y, fr, K.d2r, &re2, &im2);
+            float amp1 = sqrtf(re1 * re1 + im1 * im1);
+            float amp2 = sqrtf(re2 * re2 + im2 * im2);
+            if (amp1 >= fc0[iq] && amp2 >= fct[iq]) {
+                float ph1 = atan2f(im1, re1), ph2 = atan2f(im2, re2);
+                float d = fabsf(ph2 - ph1);
+                d = fminf(d, K.tpi - d);
+                float w = 0.5f * (amp1 + amp2);
+                p1 += (double)(d * w);
+                p2 += (double)w;
+            }
+        }
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+        p1 += __shfl_xor_sync(0xffffffffu, p1, o);
+        p2 += __shfl_xor_sync(0xffffffffu, p2, o);
+    }
+    const int w = threadIdx.x >> 5, l = threadIdx.x & 31, nw = blockDim.x >> 5;
+    if (l == 0) { sh[0][w] = p1; sh[1][w] = p2; }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double s1 = 0, s2 = 0;
+        for (int q = 0; q < nw; ++q) { s1 += sh[0][q]; s2 += sh[1][q]; }
+        float f1 = (float)s1, f2 = (float)s2;
+        a.pr[(long)p * 11 + c] = (f2 > 1.0e-10f) ? f1 / f2 * 180.0f / K.pi : 1000.0f;
+    }
+}
+
+// reconstruct.f90:103-145: rotate each half-plane sample, apply the 60 operators,
+// fold to z >= 0 and splat (a*ctf, b*ctf*signz, ctf^2) trilinearly.  One thread per
+// (sample, operator); the three sums of a voxel are one float4 vector atomic.
+__device__ __forceinline__ void mv3_rn(const float* m, const float* v, float* o) {
+    float t0 = __fmul_rn(m[0], v[0]); t0 = __fadd_rn(t0, __fmul_rn(m[1], v[1])); t0 = __fadd_rn(t0, __fmul_rn(m[2], v[2]));
+    float t1 = __fmul_rn(m[3], v[0]); t1 = __fadd_rn(t1, __fmul_rn(m[4], v[1])); t1 = __fadd_rn(t1, __fmul_rn(m[5], v[2]));
+    float t2 = __fmul_rn(m[6], v[0]); t2 = __fadd_rn(t2, __fmul_rn(m[7], v[1])); t2 = __fadd_rn(t2, __fmul_rn(m[8], v[2]));
+    o[0] = t0; o[1] = t1; o[2] = t2;
+}
+
+__global__ void __launch_bounds__(256) k_insert(InsertArgs a) {
+    const int p = blockIdx.y;
+    if (!a.sel[p]) return;
+    const long q = (long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (q >= (long)a.nsamples * a.nsym) return;
+    const int s = (int)(q / a.nsym), k = (int)(q - (long)s * a.nsym);
+    const Band bd = a.bd;
+    const int W = bd.W, R = bd.max_r;
+    const int2 hk = a.samples[s];
+    const float* rot = a.rot + p * 9;
+    float xv[3] = {(float)hk.x, (float)hk.y, 0.0f}, x00[3], x0[3];
+    mv3_rn(rot, xv, x00);
+    mv3_rn(a.ops + k * 9, x00, x0);
+    float signz = 1.0f;
+    if (x0[2] < 0.0f) { x0[0] = -x0[0]; x0[1] = -x0[1]; x0[2] = -x0[2]; signz = -1.0f; }
+    x0[0] = __fadd_rn(x0[0], a.off_xy);
+    x0[1] = __fadd_rn(x0[1], a.off_xy);
+    x0[2] = __fadd_rn(x0[2], a.off_z);
+    const int lx = (int)x0[0], ly = (int)x0[1], lz = (int)x0[2];
+    const float ax = x0[0] - (float)lx, ay = x0[1] - (float)ly, az = x0[2] - (float)lz;
+    const float bx = 1.0f - ax, by = 1.0f - ay, bz = 1.0f - az;
+    float dx[8];
+    dx[0] = __fmul_rn(__fmul_rn(bx, by), bz);
+    dx[1] = __fmul_rn(__fmul_rn(ax, by), bz);
+    dx[2] = __fmul_rn(__fmul_rn(bx, ay), bz);
+    dx[3] = __fmul_rn(__fmul_rn(ax, ay), bz);
+    dx[4] = __fmul_rn(__fmul_rn(bx, by), az);
+    dx[5] = __fmul_rn(__fmul_rn(ax, by), az);
+    dx[6] = __fmul_rn(__fmul_rn(bx, ay), az);
+    dx[7] = __fmul_rn(__fmul_rn(ax, ay), az);
+    const int bidx = (hk.y + R) * W + (hk.x + R);
+    const float2 fv = a.band[(long)p * W * W + bidx];
+    const float c = a.ctf ? a.ctf[(long)p * W * W + bidx] : 1.0f;
+    const float c2 = __fmul_rn(c, c);
+    const int AW = bd.AW;
+    const int ix = lx - a.base_xy, iy = ly - a.base_xy, iz = lz - a.base_z;
+    if (ix < 0 || iy < 0 || iz < 0 || ix > AW - 2 || iy > AW - 2 || iz > R) return;  // never taken
+    const long base = ((long)iz * AW + iy) * AW + ix;
+    const long offs[8] = {0, 1, AW, AW + 1, (long)AW * AW, (long)AW * AW + 1, (long)AW * AW + AW,
+                          (long)AW * AW + AW + 1};
+#pragma unroll
+    for (int j = 0; j < 8; ++j) {
+        float va = __fmul_rn(__fmul_rn(fv.x, dx[j]), c);
+        float vb = __fmul_rn(__fmul_rn(__fmul_rn(fv.y, dx[j]), c), signz);
+        float vw = __fmul_rn(dx[j], c2);
+        atomicAdd(a.acc + base + offs[j], make_float4(va, vb, vw, 0.0f));
+    }
+}
+
+Consts consts() {
+    Angles an = host_angles();
+    Consts K;
+    K.d2r = an.deg2rad;
+    K.pi = an.pi;
+    K.tpi = an.tpi;
+    K.r2d = 180.0f / an.pi;
+    return K;
+}
+
+}  // namespace
+
+int pr_omega_smem_bytes(const Band& bd, int nomega, int* threads) {
+    int nomp = (nomega + 31) / 32 * 32;
+    if (nomp > 768) return -1;
+    int G = 768 / nomp;
+    if (G < 1) G = 1;
+    int nt = G * nomp;
+    if (threads) *threads = nt;
+    size_t b = (size_t)bd.W * bd.W * 8 + (size_t)60 * bd.nr * 8 + (size_t)((bd.nr + 3) & ~3) * 4 +
+               64 * 4 + (size_t)2 * nt * 4 + 32 * 8;
+    return (int)b;
+}
+
+cudaError_t launch_pr_omega(const PrOmegaArgs& a, int B, cudaStream_t st) {
+    int nt = 0;
+    int sm = pr_omega_smem_bytes(a.bd, a.nomega, &nt);
+    if (sm < 0) return cudaErrorInvalidValue;
+    int nomp = (a.nomega + 31) / 32 * 32;
+    cudaError_t e = cudaFuncSetAttribute(k_pr_omega, cudaFuncAttributeMaxDynamicSharedMemorySize, sm);
+    if (e != cudaSuccess) return e;
+    dim3 grid(a.V, B);
+    k_pr_omega<<<grid, nt, sm, st>>>(a, nomp, consts());
+    return cudaGetLastError();
+}
+
+cudaError_t launch_pr_single(const PrSingleArgs& a, int B, cudaStream_t st) {
+    dim3 grid(11, B);
+    k_pr_single<<<grid, 512, 0, st>>>(a, consts());
+    return cudaGetLastError();
+}
+
+cudaError_t launch_insert(const InsertArgs& a, int B, cudaStream_t st) {
+    long total = (long)a.nsamples * a.nsym;
+    dim3 grid((unsigned)((total + 255) / 256), B);
+    k_insert<<<grid, 256, 0, st>>>(a);
+    return cudaGetLastError();
+}
+
+}  // namespace cryoim

@@ -1,0 +1,219 @@
+/*
+ * cryoim.h — C ABI of libcryoim_gb300.so, the GB300 (sm_103a) implementation of
+ * cryoIM's icosahedral projection-matching refinement loop.
+ *
+ * The reference (chenwenyuan2009/cryoIM) is Fortran 90 with all state in module
+ * globals (icosprocess/SRC/0common_icosproc.f90:2-115) and no library API.  Every
+ * entry point below replaces one Fortran subroutine (or driver loop) of that path
+ * and is callable from Fortran through ISO_C_BINDING: plain pointers, int32/float
+ * by value, no C++ or torch types, every function returns an int status
+ * (CRYOIM_OK = 0, negative = error; nothing calls exit()).
+ *
+ * Ownership: the caller owns every host array.  Device memory lives inside an
+ * opaque cryoim_ctx (one per host thread; a context is not thread safe).  Calls are
+ * synchronous at the API edge unless the name ends in _async.  Entry points whose
+ * name ends in _device take device pointers (resident in HBM) for their bulk
+ * inputs; all others take host pointers and do the host<->device copies.
+ *
+ * Array conventions follow the reference: images are nx*nx float32 with x fastest
+ * (MRC order); a Fourier image is two real arrays (a = Re, b = -Im, the
+ * icosprocess/SRC/img2d_FFT.f90:18-19 convention) centred at (nx/2, nx/2).
+ */
+#ifndef CRYOIM_H
+#define CRYOIM_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes ------------------------------------------------------ */
+#define CRYOIM_OK            0
+#define CRYOIM_ERR_ARG      -1  /* null pointer, non-positive size, bad enum      */
+#define CRYOIM_ERR_CUDA     -2  /* a CUDA / cuFFT call failed                      */
+#define CRYOIM_ERR_NOMEM    -3  /* device allocation failed                        */
+#define CRYOIM_ERR_STATE    -4  /* call order: params / templates not set          */
+#define CRYOIM_ERR_SIZE     -5  /* a size is beyond what the kernels support       */
+#define CRYOIM_ERR_INPUT    -6  /* NaN/Inf in an input array, bad ort value        */
+#define CRYOIM_ERR_IO       -7  /* file missing / short / malformed (host I/O)     */
+#define CRYOIM_ERR_MISMATCH -8  /* ort file and stack disagree (checkstckfile)     */
+
+/* ---- records ----------------------------------------------------------- */
+
+/* One particle record, the `particles` type of icosprocess/SRC/0common_icosproc.f90:28-34
+ * without its stckfile name (kept by the host I/O layer).  *0 fields hold the values
+ * before a search/refinement, d* fields the change, as the reference writes them. */
+typedef struct cryoim_particle {
+    int32_t particle_id, img_id, img_particle_id;
+    float theta0, phi0, omega0, x0, y0, pr0, df1, df2, astigang;
+    float theta, phi, omega, x, y, pr;
+    float dtheta, dphi, domega, dx, dy, dpr;
+} cryoim_particle;
+
+/* One template orientation, the `templates` type of 0common_icosproc.f90:37-40. */
+typedef struct cryoim_template {
+    int32_t particle_id;
+    float theta, phi, omega, x, y;
+} cryoim_template;
+
+/* Run parameters: the 32 `key=value` keys of icosprocess/SRC/0input_parameters.f90:6-37
+ * that act on this path, their code defaults (0initialvalue.f90:26-45,
+ * 0input_parameters.f90:40-51) and the values derived from them
+ * (0calc_initialvalues.f90:5-61).  Flags are 0/1 (the reference's 'y'/'n'). */
+typedef struct cryoim_params {
+    /* inputs */
+    int32_t fftsize;        /* FFTsize = nx of the particle stack                  */
+    int32_t mode;           /* 1 reconstruct, 4 global search, 5 refinement        */
+    int32_t first, last;    /* 1-based particle range                              */
+    int32_t ncycle;         /* Ncycle (6)                                          */
+    int32_t apply_ctf;      /* applyCTF (y)                                        */
+    int32_t use_imgmask;    /* proc2d%imgmask (y)                                  */
+    int32_t realspaceavg;   /* realspaceavg (n)                                    */
+    int32_t subrec;         /* subrec (n)                                          */
+    int32_t fsc;            /* FSC (n)                                             */
+    int32_t imgstck;        /* imgstck given (CTF not cached per imgID)            */
+    float apix;             /* apix (1.0)                                          */
+    float min_res, max_res; /* minRes (300), maxRes (8.0), Angstrom                */
+    float imgmask;          /* imgmask, Angstrom ((FFTsize/2-2) before /apix)      */
+    float vol, cs, ampwg, bfactor; /* CTF: 300 kV, 2.7 mm, 0.1, 0                  */
+    float pr_threshold;     /* PR_threshold (90)                                   */
+    float searchstep;       /* searchstep (2.0 degrees)                            */
+    float maxcentshift;     /* maxcentshift (100)                                  */
+    float boundx;           /* boundX (FFTsize/2-2)                                */
+    /* derived by cryoim_params_derive */
+    int32_t min_r, max_r;   /* minR=int(apix*N/minRes), maxR=int(apix*N/maxRes) even */
+    int32_t nsym, nlin;     /* 60/60 for icos                                      */
+    float imgmask_px;       /* mask radius in pixels                               */
+    float delta_angle;      /* 360/(maxRes*sqrt(5)*3.14159)                        */
+    float delta_trans;      /* FFTsize/(maxRes*sqrt(5))                            */
+} cryoim_params;
+
+/* ---- library / context ------------------------------------------------- */
+
+int32_t cryoim_version(void);
+/* Text of the last error on this host thread (never NULL). */
+const char* cryoim_last_error(void);
+
+/* Fill *p with the reference's code defaults for a stack of nx = fftsize.
+ * Replaces icosprocess/SRC/0initialvalue.f90:26-45 and 0input_parameters.f90:40-51. */
+int cryoim_params_default(cryoim_params* p, int32_t fftsize);
+/* Derive min_r, max_r, imgmask_px, delta_angle, delta_trans, nsym, nlin.
+ * Replaces icosprocess/SRC/0calc_initialvalues.f90:4-25 (mode != 6 branch). */
+int cryoim_params_derive(cryoim_params* p);
+
+int cryoim_ctx_create(int32_t device, void** ctx_out);
+int cryoim_ctx_destroy(void* ctx);
+/* Run all device work of this context on `stream` (a cudaStream_t); NULL = own stream. */
+int cryoim_ctx_set_stream(void* ctx, void* stream);
+/* CUDA-event timing of every launch of the hot kernel (the phase-residual search
+ * kernel); off by default.  No reference counterpart (the reference has no timers). */
+int cryoim_ctx_set_profiling(void* ctx, int32_t on);
+/* Total milliseconds and number of timed launches since the last call (then reset). */
+int cryoim_ctx_kernel_time(void* ctx, double* ms, int64_t* launches);
+/* Copy and validate parameters (derived fields must be set).  Resets the batch size. */
+int cryoim_set_params(void* ctx, const cryoim_params* p);
+/* Images processed per device batch (default: min(64, 16M / nx^2)).  No reference
+ * counterpart: the reference processes one particle at a time. */
+int cryoim_ctx_set_batch(void* ctx, int32_t batch);
+
+/* ---- templates (icosprocess mode 4/5 set-up) ------------------------------ */
+
+/* Real-space projection of a 3D map (nx^3 float32) along each template orientation
+ * by trilinear line integral: replaces icosprocess/SRC/project_template2d.f90:25-76.
+ * out: T*nx*nx float32. */
+int cryoim_project_templates(void* ctx, const float* map3d, const cryoim_template* t,
+                             int32_t T, float* out);
+/* Mask, checkerboard, 2D FFT, origin shift and amplitude-cut fit of T template
+ * images (T*nx*nx float32); keeps their Fourier transforms resident on the device.
+ * Replaces icosprocess/SRC/load_template.f90:35-48. */
+int cryoim_load_templates(void* ctx, const float* tmpl_real, const cryoim_template* t,
+                          int32_t T);
+
+/* ---- global orientation search (icosprocess mode 4) ------------------------ */
+
+/* Exhaustive search over the icosahedral asymmetric unit scored by the cross-common-
+ * line phase residual, for P particles whose images are imgs (P*nx*nx float32, host).
+ * parts[] is read (origin, CTF, imgID) and updated in place exactly as
+ * icosprocess/SRC/ort_globesearch.f90:34-133 updates particle(i).
+ * pr_array (optional, may be NULL): P * Nomega*(2*Nphi+1)*(Ntheta+1) floats, the
+ * reference's PR_array(0:Nomega-1,-Nphi:Nphi,0:Ntheta) per particle. */
+int cryoim_globesearch(void* ctx, const float* imgs, cryoim_particle* parts, int32_t P,
+                       float* pr_array);
+/* Same with the images already in device memory (d_imgs, P*nx*nx float32). */
+int cryoim_globesearch_device(void* ctx, const float* d_imgs, cryoim_particle* parts,
+                              int32_t P, float* pr_array);
+/* Grid sizes of the search (ort_globesearch.f90:19-21): Ntheta, Nphi, Nomega and the
+ * number of distinct asymmetric-unit views evaluated. */
+int cryoim_search_grid(void* ctx, int32_t* ntheta, int32_t* nphi, int32_t* nomega,
+                       int32_t* nviews);
+
+/* Phase-residual terms evaluated per particle by the search: sum over views and templates
+ * of the valid common lines, times (maxR-minR+1) radii, times Nomega. */
+int cryoim_search_terms(void* ctx, double* terms_per_particle);
+
+/* Kernel-level hook: PR(omega) of one particle Fourier image against the loaded
+ * templates at view (theta, phi, 0): replaces icosprocess/SRC/cal_crosslin_PR_omega.f90:3-82.
+ * ft_a, ft_b: nx*nx (shifted particle FT), fcut0: maxR-minR+1 amplitude cuts of the
+ * particle, ctf: nx*nx or NULL (no CTF), pr_omega: Nomega outputs. */
+int cryoim_prscore_omega(void* ctx, const float* ft_a, const float* ft_b,
+                         const float* fcut0, const float* ctf, float theta, float phi,
+                         float* pr_omega);
+
+/* ---- local refinement (icosprocess mode 5) -------------------------------- */
+
+/* Ncycle rounds of the 11-point descent over (theta, phi, omega, x, y) scored by
+ * cross-common-line PR.  Replaces icosprocess/SRC/ort_refinement.f90:31-124 with
+ * ort_cent_11.f90, return_icos_asymmetry_unit.f90 and cal_crosslin_PR.f90. */
+int cryoim_refine(void* ctx, const float* imgs, cryoim_particle* parts, int32_t P);
+int cryoim_refine_device(void* ctx, const float* d_imgs, cryoim_particle* parts, int32_t P);
+/* Kernel-level hook: PR of one candidate (cal_crosslin_PR.f90:2-71).  ft_a/ft_b is the
+ * unshifted particle FT; the candidate origin (x, y) is applied inside. */
+int cryoim_prscore(void* ctx, const float* ft_a, const float* ft_b, const float* fcut0,
+                   const float* ctf, float theta, float phi, float omega, float x,
+                   float y, float* pr);
+
+/* ---- reconstruction (icosprocess mode 1) --------------------------------- */
+
+/* Start a symmetrised direct-Fourier reconstruction (reconstruct.f90:22-34). */
+int cryoim_rec_begin(void* ctx);
+/* Insert P particles (host images) whose PR/origin pass the reference's selection
+ * (reconstruct.f90:77); returns the number used in *used (may be NULL).
+ * Replaces icosprocess/SRC/reconstruct.f90:53-149. */
+int cryoim_rec_insert(void* ctx, const float* imgs, const cryoim_particle* parts,
+                      int32_t P, int32_t* used);
+int cryoim_rec_insert_device(void* ctx, const float* d_imgs, const cryoim_particle* parts,
+                             int32_t P, int32_t* used);
+/* Friedel completion, divide by the CTF^2 weights, inverse 3D FFT and origin shift
+ * into map (nx^3 float32).  Replaces icosprocess/SRC/reconstruct.f90:151-247. */
+int cryoim_rec_finish(void* ctx, float* map);
+/* Partial accumulators in the tnf half-box layout of reconstruct_substep.f90:18-19,152-155:
+ * fa, fb, wg each (2*maxR+1)^2*(maxR+1) floats (x fastest, then y, then z >= 0). */
+int cryoim_rec_get_partial(void* ctx, float* fa, float* fb, float* wg);
+
+/* ---- central sections (projection-matching form, spec step a/b) ------ */
+
+/* Trilinear central sections of a 3D Fourier map: replaces
+ * icosprocess/SRC/project2d_FT3dTo2d.f90:19-84 (the section before its inverse FFT).
+ * ft_re/ft_im: nx^3 float32 (x fastest, centred at nx/2); eulers: n*3 (theta,phi,omega)
+ * degrees; out_re/out_im: n*nx*nx float32. */
+int cryoim_central_sections(void* ctx, const float* ft_re, const float* ft_im,
+                            const float* eulers, int32_t n, float* out_re, float* out_im);
+
+/* ---- orientation bookkeeping (proc_icos) --------------------------------- */
+
+/* The 60 icosahedral rotations in the 2-fold frame, in the order of
+ * icosprocess/SRC/icos2f_sym_mat.f90:5-243 (rot[k*9 + r*3 + c]). */
+int cryoim_icos_ops(float* rot);
+/* Fold an orientation into the asymmetric unit (return_icos_asymmetry_unit.f90:1-33). */
+int cryoim_asu_fold(float* theta, float* phi, float* omega);
+/* The 60 symmetry-equivalent orientations (proc_icos/SRC/equalort.f90:1-24): out 60*3. */
+int cryoim_equalort(float theta, float phi, float omega, float* out);
+/* 2-fold -> 5-fold (to=5) or 2-fold -> 3-fold (to=3) frame, in place on n orientations
+ * (proc_icos/SRC/transform_ort_2fTo5f.f90:11-30, transform_ort_2fTo3f.f90:11-32). */
+int cryoim_transform_ort(int32_t to, float* theta, float* phi, float* omega, int32_t n);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* CRYOIM_H */

@@ -1,0 +1,295 @@
+"""ctypes wrapper of the CPU oracle (oracle/cryoim_oracle.cpp).
+
+TEST INFRASTRUCTURE ONLY: used by tests/, __graft_entry__.smoke() and the CPU-baseline
+legs of bench.py as the checker.  The product (libcryoim_gb300.so and the
+cryoim_gb300 package) never imports this module.
+
+Every function takes an `fp` argument: "f32" (FP32 in the Fortran's operation order)
+or "f64" (the same algorithm in FP64).
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import subprocess
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB = os.path.join(HERE, "_build", "libcryoim_oracle.so")
+_lib = None
+
+
+def build() -> None:
+    subprocess.run(["make", "-s", "-C", HERE], check=True)
+
+
+def lib() -> C.CDLL:
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB):
+            build()
+        _lib = C.CDLL(LIB)
+        for s, R in (("f32", C.c_float), ("f64", C.c_double)):
+            getattr(_lib, f"orc_pr_single_{s}").restype = R
+    return _lib
+
+
+def _dt(fp):
+    return np.float32 if fp == "f32" else np.float64
+
+
+def _R(fp):
+    return C.c_float if fp == "f32" else C.c_double
+
+
+def _p(a):
+    return None if a is None else a.ctypes.data_as(C.c_void_p)
+
+
+def _fn(name, fp):
+    f = getattr(lib(), f"orc_{name}_{fp}")
+    return f
+
+
+# --- single routines ---------------------------------------------------------
+def ctf2d(nx, df1, df2, astig, apix, vol, cs, ampwg, fp="f32"):
+    R = _R(fp)
+    out = np.zeros(nx * nx, _dt(fp))
+    _fn("ctf2d", fp)(C.c_int(nx), R(df1), R(df2), R(astig), R(apix), R(vol), R(cs), R(ampwg), _p(out))
+    return out.reshape(nx, nx)
+
+
+def mask(img, radius, ox, oy, fp="f32"):
+    a = np.ascontiguousarray(img, _dt(fp)).copy()
+    R = _R(fp)
+    _fn("mask", fp)(_p(a), C.c_int(a.shape[-1]), R(radius), R(ox), R(oy))
+    return a
+
+
+def fft2d(a, b, nbit=1, fp="f32"):
+    a = np.ascontiguousarray(a, _dt(fp)).copy()
+    b = np.ascontiguousarray(b, _dt(fp)).copy()
+    _fn("fft2d", fp)(_p(a), _p(b), C.c_int(a.shape[-1]), C.c_int(a.shape[-2]), C.c_int(nbit))
+    return a, b
+
+
+def fft3d(re, im, sign, fp="f64"):
+    re = np.ascontiguousarray(re, _dt(fp)).copy()
+    im = np.ascontiguousarray(im, _dt(fp)).copy()
+    _fn("fft3d", fp)(_p(re), _p(im), C.c_int(re.shape[-1]), C.c_int(sign))
+    return re, im
+
+
+def expfit(a, b, min_r, max_r, fp="f32"):
+    a = np.ascontiguousarray(a, _dt(fp))
+    b = np.ascontiguousarray(b, _dt(fp))
+    out = np.zeros(max_r - min_r + 1, _dt(fp))
+    _fn("expfit", fp)(_p(a), _p(b), C.c_int(a.shape[-1]), C.c_int(min_r), C.c_int(max_r), _p(out))
+    return out
+
+
+def centshift(a, b, x0, y0, fp="f32"):
+    a = np.ascontiguousarray(a, _dt(fp)).copy()
+    b = np.ascontiguousarray(b, _dt(fp)).copy()
+    R = _R(fp)
+    _fn("centshift", fp)(_p(a), _p(b), C.c_int(a.shape[-1]), R(x0), R(y0))
+    return a, b
+
+
+def norm(img, fp="f32"):
+    a = np.ascontiguousarray(img, _dt(fp)).copy()
+    _fn("norm", fp)(_p(a), C.c_int(a.shape[-1]))
+    return a
+
+
+def euler(theta, phi, omega, fp="f32"):
+    m = np.zeros(9, _dt(fp))
+    R = _R(fp)
+    _fn("euler", fp)(R(theta), R(phi), R(omega), _p(m))
+    return m.reshape(3, 3)
+
+
+def icos_ops(fp="f64"):
+    m = np.zeros(540, _dt(fp))
+    _fn("icos_ops", fp)(_p(m))
+    return m.reshape(60, 3, 3)
+
+
+def icos_gen(fp="f64"):
+    m = np.zeros(540, _dt(fp))
+    _fn("icos_gen", fp)(_p(m))
+    return m.reshape(60, 3, 3)
+
+
+def crosslin(o1, o2, fp="f32"):
+    a1 = np.zeros(60, _dt(fp))
+    a2 = np.zeros(60, _dt(fp))
+    R = _R(fp)
+    _fn("crosslin", fp)(*(R(v) for v in (*o1, *o2)), _p(a1), _p(a2))
+    return a1, a2
+
+
+def asu_fold(theta, phi, omega, fp="f32"):
+    R = _R(fp)
+    t, p, o = R(theta), R(phi), R(omega)
+    _fn("asu_fold", fp)(C.byref(t), C.byref(p), C.byref(o))
+    return t.value, p.value, o.value
+
+
+def fill_lin(a, b, min_r, max_r, alpha, fp="f32"):
+    a = np.ascontiguousarray(a, _dt(fp))
+    b = np.ascontiguousarray(b, _dt(fp))
+    al = np.ascontiguousarray(alpha, _dt(fp))
+    nr = max_r - min_r + 1
+    out = np.zeros((len(al), nr, 2), _dt(fp))
+    _fn("fill_lin", fp)(C.c_int(len(al)), _p(a), _p(b), C.c_int(a.shape[-1]), C.c_int(min_r),
+                        C.c_int(max_r), _p(al), _p(out))
+    return out
+
+
+def pr_omega(pa, pb, fcut0, tmpl, tort, tfcut, ctf, min_r, max_r, step, theta, phi, omega=0.0,
+             fp="f64"):
+    dt = _dt(fp)
+    R = _R(fp)
+    nx = pa.shape[-1]
+    nom = int(np.float32(360.0) / np.float32(step))
+    out = np.zeros(nom, dt)
+    args = [np.ascontiguousarray(x, dt) if x is not None else None
+            for x in (pa, pb, fcut0, tmpl, tort, tfcut, ctf)]
+    _fn("pr_omega", fp)(*[_p(x) for x in args], C.c_int(len(tort)), C.c_int(nx), C.c_int(min_r),
+                        C.c_int(max_r), R(step), C.c_int(nom), R(theta), R(phi), R(omega), _p(out))
+    return out
+
+
+def pr_single(pa, pb, fcut0, tmpl, tort, tfcut, ctf, min_r, max_r, theta, phi, omega, x, y,
+              fp="f64"):
+    dt = _dt(fp)
+    R = _R(fp)
+    args = [np.ascontiguousarray(v, dt) if v is not None else None
+            for v in (pa, pb, fcut0, tmpl, tort, tfcut, ctf)]
+    return _fn("pr_single", fp)(*[_p(v) for v in args], C.c_int(len(tort)), C.c_int(pa.shape[-1]),
+                                C.c_int(min_r), C.c_int(max_r), R(theta), R(phi), R(omega), R(x), R(y))
+
+
+def prep_particle(img, use_mask, mask_px, x, y, shift, min_r, max_r, fp="f64"):
+    dt = _dt(fp)
+    R = _R(fp)
+    im = np.ascontiguousarray(img, np.float32)
+    nx = im.shape[-1]
+    a = np.zeros((nx, nx), dt)
+    b = np.zeros((nx, nx), dt)
+    f = np.zeros(max_r - min_r + 1, dt)
+    _fn("prep_particle", fp)(_p(im), C.c_int(nx), C.c_int(int(use_mask)), R(mask_px), R(x), R(y),
+                             C.c_int(int(shift)), C.c_int(min_r), C.c_int(max_r), _p(a), _p(b), _p(f))
+    return a, b, f
+
+
+def load_templates(imgs, tmpl, params, fp="f64"):
+    dt = _dt(fp)
+    im = np.ascontiguousarray(imgs, np.float32)
+    t = np.ascontiguousarray(tmpl)
+    T, nx = len(t), params.fftsize
+    nr = params.max_r - params.min_r + 1
+    tm = np.zeros((T, 2, nx, nx), dt)
+    tf = np.zeros((T, nr), dt)
+    _fn("load_templates", fp)(_p(im), _p(t), C.c_int(T), C.byref(params), _p(tm), _p(tf))
+    return tm, tf
+
+
+def globesearch(params, tm, tf, tmpl, imgs, parts, want_pr_array=False, nthreads=0, fp="f64"):
+    dt = _dt(fp)
+    nth, nph, nom = grid_sizes(params.searchstep)
+    pra = None
+    if want_pr_array:
+        pra = np.zeros((len(parts), nth + 1, 2 * nph + 1, nom), np.float32)
+    im = np.ascontiguousarray(imgs, np.float32)
+    r = _fn("globesearch", fp)(C.byref(params), _p(np.ascontiguousarray(tm, dt)),
+                               _p(np.ascontiguousarray(tf, dt)), _p(np.ascontiguousarray(tmpl)),
+                               C.c_int(len(tmpl)), _p(im), _p(parts), C.c_int(len(parts)), _p(pra),
+                               C.c_int(nthreads))
+    assert r == 0
+    return pra
+
+
+def refine(params, tm, tf, tmpl, imgs, parts, nthreads=0, fp="f64"):
+    dt = _dt(fp)
+    im = np.ascontiguousarray(imgs, np.float32)
+    r = _fn("refine", fp)(C.byref(params), _p(np.ascontiguousarray(tm, dt)),
+                          _p(np.ascontiguousarray(tf, dt)), _p(np.ascontiguousarray(tmpl)),
+                          C.c_int(len(tmpl)), _p(im), _p(parts), C.c_int(len(parts)), C.c_int(nthreads))
+    assert r == 0
+
+
+def search_views(params, tm, tf, tmpl, img, part, views, nthreads=0, fp="f32"):
+    """PR(omega) of one particle at the listed (theta, phi) views (CPU baseline sample)."""
+    dt = _dt(fp)
+    nth, nph, nom = grid_sizes(params.searchstep)
+    v = np.ascontiguousarray(views, np.float32).reshape(-1, 2)
+    out = np.zeros((len(v), nom), np.float32)
+    q = np.ascontiguousarray(part).reshape(1)
+    r = _fn("search_views", fp)(C.byref(params), _p(np.ascontiguousarray(tm, dt)),
+                                _p(np.ascontiguousarray(tf, dt)), _p(np.ascontiguousarray(tmpl)),
+                                C.c_int(len(tmpl)), _p(np.ascontiguousarray(img, np.float32)), _p(q),
+                                _p(v), C.c_int(len(v)), C.c_int(nthreads), _p(out))
+    assert r == 0
+    return out
+
+
+def project_template2d(map3d, theta, phi, omega, fp="f32"):
+    m = np.ascontiguousarray(map3d, np.float32)
+    nx = m.shape[-1]
+    out = np.zeros((nx, nx), _dt(fp))
+    R = _R(fp)
+    _fn("project_template2d", fp)(_p(m), C.c_int(nx), R(theta), R(phi), R(omega), _p(out))
+    return out
+
+
+def central_section(fre, fim, theta, phi, omega, fp="f32"):
+    dt = _dt(fp)
+    fre = np.ascontiguousarray(fre, dt)
+    fim = np.ascontiguousarray(fim, dt)
+    nx = fre.shape[-1]
+    ore = np.zeros((nx, nx), dt)
+    oim = np.zeros((nx, nx), dt)
+    R = _R(fp)
+    _fn("central_section", fp)(_p(fre), _p(fim), C.c_int(nx), R(theta), R(phi), R(omega), _p(ore), _p(oim))
+    return ore, oim
+
+
+def reconstruct(params, imgs, parts, want_acc=False, fp="f64"):
+    dt = _dt(fp)
+    nx = params.fftsize
+    im = np.ascontiguousarray(imgs, np.float32)
+    out = np.zeros((nx, nx, nx), np.float32)
+    acc = np.zeros((3, nx, nx, nx), dt) if want_acc else None
+    r = _fn("reconstruct", fp)(C.byref(params), _p(im), _p(np.ascontiguousarray(parts)),
+                               C.c_int(len(parts)), _p(out), _p(acc))
+    assert r == 0
+    return (out, acc) if want_acc else out
+
+
+def equalort(theta, phi, omega, fp="f32"):
+    out = np.zeros((60, 3), _dt(fp))
+    R = _R(fp)
+    _fn("equalort", fp)(R(theta), R(phi), R(omega), _p(out))
+    return out
+
+
+def transform_ort(to, theta, phi, omega, fp="f32"):
+    dt = _dt(fp)
+    t = np.array(theta, dt).ravel().copy()
+    p = np.array(phi, dt).ravel().copy()
+    o = np.array(omega, dt).ravel().copy()
+    _fn("transform_ort", fp)(C.c_int(to), _p(t), _p(p), _p(o), C.c_int(len(t)))
+    return t, p, o
+
+
+def grid_sizes(step):
+    a, b, c = C.c_int(), C.c_int(), C.c_int()
+    lib().orc_grid_sizes(C.c_float(step), C.byref(a), C.byref(b), C.byref(c))
+    return a.value, b.value, c.value
+
+
+def num_threads():
+    return lib().orc_num_threads()

@@ -1,0 +1,211 @@
+"""Parity of the CUDA path (through the C ABI) with the FP64 oracle.
+
+Tolerances (FP32 drop-in form): phase-residual scores within 1e-4 relative; orientation
+identical wherever the oracle's best-two score gap exceeds that tolerance; maps within
+1e-4 relative L2 with FSC >= 0.9999.  The FP32 oracle is compared where the reference's
+own FP32 evaluation order matters.
+"""
+import numpy as np
+import pytest
+
+from _data import small_case
+
+pytestmark = pytest.mark.gpu
+RTOL = 1e-4
+
+
+@pytest.fixture(scope="module")
+def case():
+    return small_case()
+
+
+@pytest.fixture(scope="module")
+def ctx(built, case):
+    import cryoim_gb300 as ci
+    p, vol, tmpl, timgs, imgs, parts, truth = case
+    c = ci.Context(0, p)
+    c.load_templates(timgs, tmpl)
+    yield c
+    c.close()
+
+
+@pytest.fixture(scope="module")
+def otmpl(orc, case):
+    p, vol, tmpl, timgs, imgs, parts, truth = case
+    return orc.load_templates(timgs, tmpl, p, "f64")
+
+
+def _tort(tmpl):
+    return np.stack([tmpl["theta"], tmpl["phi"], tmpl["omega"]], 1)
+
+
+def test_prscore_omega_matches_oracle(ctx, orc, case, otmpl):
+    """cal_crosslin_PR_omega on prepared inputs (kernel-level hook)."""
+    p, vol, tmpl, timgs, imgs, parts, truth = case
+    tm, tf = otmpl
+    for i in range(len(parts)):
+        a, b, f = orc.prep_particle(imgs[i], 1, p.imgmask_px, parts["x"][i], parts["y"][i], 1,
+                                    p.min_r, p.max_r, "f64")
+        ctf = orc.ctf2d(p.fftsize, parts["df1"][i], parts["df2"][i], parts["astigang"][i], p.apix,
+                        p.vol, p.cs, p.ampwg, "f64")
+        for th, ph in [(81.0, 8.0), (73.0, -12.0), (89.0, 0.0)]:
+            want = orc.pr_omega(a, b, f, tm, _tort(tmpl), tf, ctf, p.min_r, p.max_r, p.searchstep,
+                                th, ph, fp="f64")
+            got = ctx.prscore_omega(a, b, f, ctf, th, ph)
+            assert got.shape == want.shape
+            assert np.array_equal(got >= 999, want >= 999)
+            ok = want < 999
+            rel = np.abs(got[ok] - want[ok]) / want[ok]
+            assert rel.max() < RTOL, (i, th, ph, rel.max())
+
+
+def test_globesearch_matches_oracle(ctx, orc, case, otmpl):
+    p, vol, tmpl, timgs, imgs, parts, truth = case
+    tm, tf = otmpl
+    q_gpu = parts.copy()
+    pra_gpu = ctx.globesearch(imgs, q_gpu, want_pr_array=True)
+    q_orc = parts.copy()
+    pra_orc = orc.globesearch(p, tm, tf, tmpl, imgs, q_orc, want_pr_array=True, fp="f64")
+    assert pra_gpu.shape == pra_orc.shape
+    assert np.array_equal(pra_gpu == 1000, pra_orc == 1000)
+    assert np.array_equal(pra_gpu == 999, pra_orc == 999)
+    ok = pra_orc < 999
+    rel = np.abs(pra_gpu[ok] - pra_orc[ok]) / pra_orc[ok]
+    assert rel.max() < RTOL, rel.max()
+    for i in range(len(parts)):
+        v = np.sort(pra_orc[i].ravel())
+        gap = (v[1] - v[0]) / v[0]
+        assert np.isclose(q_gpu["pr"][i], q_orc["pr"][i], rtol=RTOL)
+        if gap > RTOL:
+            for k in ("theta", "phi", "omega"):
+                assert q_gpu[k][i] == q_orc[k][i], (i, k, q_gpu[k][i], q_orc[k][i])
+        for k in ("theta0", "phi0", "omega0", "x", "y", "df1"):
+            assert q_gpu[k][i] == q_orc[k][i]
+
+
+def test_globesearch_without_ctf(built, orc):
+    import cryoim_gb300 as ci
+    p, vol, tmpl, timgs, imgs, parts, truth = small_case(apply_ctf=0, P=2, T=3)
+    tm, tf = orc.load_templates(timgs, tmpl, p, "f64")
+    with ci.Context(0, p) as c:
+        c.load_templates(timgs, tmpl)
+        q = parts.copy()
+        pg = c.globesearch(imgs, q, want_pr_array=True)
+    po = orc.globesearch(p, tm, tf, tmpl, imgs, parts.copy(), want_pr_array=True, fp="f64")
+    ok = po < 999
+    assert np.abs(pg[ok] - po[ok]).max() / po[ok].min() < RTOL
+
+
+def test_prscore_single_matches_oracle(ctx, orc, case, otmpl):
+    """cal_crosslin_PR with the candidate origin shift (refinement scorer)."""
+    p, vol, tmpl, timgs, imgs, parts, truth = case
+    tm, tf = otmpl
+    rng = np.random.default_rng(11)
+    for i in range(len(parts)):
+        a, b, f = orc.prep_particle(imgs[i], 1, p.imgmask_px, parts["x"][i], parts["y"][i], 0,
+                                    p.min_r, p.max_r, "f64")
+        ctf = orc.ctf2d(p.fftsize, parts["df1"][i], parts["df2"][i], parts["astigang"][i], p.apix,
+                        p.vol, p.cs, p.ampwg, "f64")
+        for _ in range(4):
+            th, ph, om = rng.uniform(69, 90), rng.uniform(-30, 30), rng.uniform(0, 360)
+            x, y = rng.uniform(-3, 3, size=2)
+            want = orc.pr_single(a, b, f, tm, _tort(tmpl), tf, ctf, p.min_r, p.max_r, th, ph, om, x, y, fp="f64")
+            got = ctx.prscore(a, b, f, ctf, th, ph, om, x, y)
+            assert abs(got - want) / want < RTOL, (got, want)
+
+
+def test_refine_matches_oracle(ctx, orc, case, otmpl):
+    p, vol, tmpl, timgs, imgs, parts, truth = case
+    tm, tf = otmpl
+    q = parts.copy()
+    q["theta"], q["phi"], q["omega"] = truth[:, 0], truth[:, 1], truth[:, 2]
+    q_gpu, q_orc = q.copy(), q.copy()
+    ctx.refine(imgs, q_gpu)
+    orc.refine(p, tm, tf, tmpl, imgs, q_orc, fp="f64")
+    for i in range(len(q)):
+        assert abs(q_gpu["pr"][i] - q_orc["pr"][i]) / q_orc["pr"][i] < RTOL
+        for k in ("theta", "phi", "omega", "x", "y"):
+            assert abs(q_gpu[k][i] - q_orc[k][i]) < 1e-3, (i, k, q_gpu[k][i], q_orc[k][i])
+        assert q_gpu["pr0"][i] == q["pr"][i]
+
+
+def fsc(a, b):
+    A = np.fft.fftn(a)
+    B = np.fft.fftn(b)
+    return np.real(np.vdot(A, B)) / np.sqrt(np.vdot(A, A).real * np.vdot(B, B).real)
+
+
+def test_reconstruction_matches_oracle(ctx, orc, case):
+    p, vol, tmpl, timgs, imgs, parts, truth = case
+    q = parts.copy()
+    q["pr"] = 10.0
+    q["pr"][1] = 95.0  # above PR_threshold: not inserted
+    ctx.rec_begin()
+    used = ctx.rec_insert(imgs, q)
+    assert used == len(q) - 1
+    m_gpu = ctx.rec_finish()
+    m_orc = orc.reconstruct(p, imgs, q, fp="f64")
+    rel = np.linalg.norm(m_gpu - m_orc) / np.linalg.norm(m_orc)
+    assert rel < RTOL, rel
+    assert fsc(m_gpu, m_orc) > 0.9999
+
+
+def test_reconstruction_in_two_calls_equals_one(ctx, case):
+    """Insertion accumulates across calls (particle ranges are independent)."""
+    p, vol, tmpl, timgs, imgs, parts, truth = case
+    q = parts.copy()
+    q["pr"] = 0.0
+    ctx.rec_begin()
+    ctx.rec_insert(imgs, q)
+    m1 = ctx.rec_finish()
+    ctx.rec_begin()
+    ctx.rec_insert(imgs[:1], q[:1])
+    ctx.rec_insert(imgs[1:], q[1:])
+    m2 = ctx.rec_finish()
+    assert np.linalg.norm(m1 - m2) / np.linalg.norm(m1) < 1e-5
+
+
+def test_central_sections_match_oracle(ctx, orc, case):
+    p, vol, *_ = case
+    n = p.fftsize
+    F = np.fft.fftshift(np.fft.fftn(np.fft.ifftshift(vol)))
+    fre, fim = F.real.astype(np.float32), F.imag.astype(np.float32)
+    eul = np.array([[30.0, 40.0, 50.0], [88.0, -10.0, 300.0], [0.0, 0.0, 0.0]], np.float32)
+    gr, gi = ctx.central_sections(fre, fim, eul)
+    for k, e in enumerate(eul):
+        orr, ori = orc.central_section(fre, fim, *e, fp="f32")
+        scale = np.abs(orr).max()
+        assert np.abs(gr[k] - orr).max() < 1e-5 * scale and np.abs(gi[k] - ori).max() < 1e-5 * scale
+
+
+def test_project_templates_match_oracle(ctx, orc, case):
+    p, vol, tmpl, *_ = case
+    out = ctx.project_templates(vol, tmpl)
+    for k in range(len(tmpl)):
+        want = orc.project_template2d(vol, tmpl["theta"][k], tmpl["phi"][k], tmpl["omega"][k], fp="f32")
+        assert np.abs(out[k] - want).max() <= 1e-5 * np.abs(want).max()
+
+
+def test_nonfinite_image_is_rejected(ctx, case):
+    import cryoim_gb300 as ci
+    from cryoim_gb300._abi import ERR_INPUT
+    p, vol, tmpl, timgs, imgs, parts, truth = case
+    bad = imgs[:1].copy()
+    bad[0, 3, 5] = np.nan
+    with pytest.raises(ci.CryoimError) as e:
+        ctx.globesearch(bad, parts[:1].copy())
+    assert e.value.code == ERR_INPUT
+
+
+def test_call_order_errors(built, case):
+    import cryoim_gb300 as ci
+    from cryoim_gb300._abi import ERR_STATE
+    p, vol, tmpl, timgs, imgs, parts, truth = case
+    with ci.Context(0) as c:
+        with pytest.raises(ci.CryoimError) as e:
+            c.set_params(p)
+            c.globesearch(imgs, parts.copy())
+        assert e.value.code == ERR_STATE
+        with pytest.raises(ci.CryoimError) as e:
+            c.rec_finish()
+        assert e.value.code == ERR_STATE
