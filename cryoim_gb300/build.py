@@ -42,6 +42,7 @@ UNITS = {
     "prep.cu": ["-fmad=false"],
     "score.cu": [],
     "api.cu": [],
+    "noalloc.cu": [],
 }
 
 

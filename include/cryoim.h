@@ -173,6 +173,38 @@ int cryoim_prscore(void* ctx, const float* ft_a, const float* ft_b, const float*
                    const float* ctf, float theta, float phi, float omega, float x,
                    float y, float* pr);
 
+/* Allocation-free scoring of refinement candidates.  No counterpart in the
+ * reference: it exists for callers that cannot allocate device memory when they
+ * score (a fixed memory budget owned by another allocator, or a host loop that must
+ * not enter the CUDA allocator between steps).  Everything is a caller-owned device
+ * pointer and the call runs asynchronously on `stream`; it calls no cudaMalloc,
+ * cudaFree or allocating library routine.
+ *
+ * Computes what cryoim_prscore computes (cal_crosslin_PR.f90) for K <= 11 candidates
+ * (theta, phi, omega, x, y) of one particle, from band windows instead of full
+ * transforms: a band is the (2*max_r+2)^2 float2 (a, b = -Im) window of a centred
+ * nx*nx transform starting at pixel (nx/2-max_r, nx/2-max_r).  d_band: unshifted
+ * particle FT; d_fcut0: its max_r-min_r+1 amplitude cuts; d_ctf_band: the particle
+ * CTF over the window (NULL = no CTF, then d_tmpl_fcut gives the template cuts);
+ * d_tmpl_band: T template windows; d_tmpl_ort: T x (theta, phi, omega); d_pr: K scores.
+ *
+ * Its intermediate results live in one file-scope device array of about 0.4 MB that
+ * every GPU loading the library keeps until the process exits.  Limits: T <=
+ * CRYOIM_NOALLOC_MAX_TEMPLATES, K <= CRYOIM_NOALLOC_MAX_CANDIDATES, max_r-min_r+1 <=
+ * CRYOIM_NOALLOC_MAX_RADII; larger sizes return CRYOIM_ERR_SIZE.  The first call on a
+ * device (with that device current) looks the array up and fills its operator table,
+ * a synchronous step: make that first call before any stream capture.  All calls
+ * share the one array, so calls that overlap on the GPU (other streams, other host
+ * threads) race; serialise them. */
+#define CRYOIM_NOALLOC_MAX_TEMPLATES 64
+#define CRYOIM_NOALLOC_MAX_CANDIDATES 11
+#define CRYOIM_NOALLOC_MAX_RADII 256
+int cryoim_prscore_noalloc(int32_t nx, int32_t min_r, int32_t max_r, const float* d_band,
+                           const float* d_fcut0, const float* d_ctf_band,
+                           const float* d_tmpl_band, const float* d_tmpl_fcut,
+                           const float* d_tmpl_ort, int32_t T, const float* d_cand, int32_t K,
+                           float* d_pr, void* stream);
+
 /* ---- reconstruction (icosprocess mode 1) --------------------------------- */
 
 /* Start a symmetrised direct-Fourier reconstruction (reconstruct.f90:22-34). */
