@@ -73,6 +73,7 @@ SIGNATURES = {
     "cryoim_prscore": [_vp, _vp, _vp, _vp, _vp, _f32, _f32, _f32, _f32, _f32, _fp],
     "cryoim_prscore_noalloc": [_i32, _i32, _i32, _vp, _vp, _vp, _vp, _vp, _vp, _i32, _vp, _i32,
                                _vp, _vp],
+    "cryoim_gemm_bf16_argmax": [_vp, _vp, _i32, _i32, _i32, _vp, _vp, _vp, _vp, _vp],
     "cryoim_rec_begin": [_vp],
     "cryoim_rec_insert": [_vp, _vp, _vp, _i32, _ip],
     "cryoim_rec_insert_device": [_vp, _vp, _vp, _i32, _ip],

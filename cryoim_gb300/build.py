@@ -43,6 +43,7 @@ UNITS = {
     "score.cu": [],
     "api.cu": [],
     "noalloc.cu": [],
+    "gemm_tc.cu": [],
 }
 
 

@@ -1,0 +1,349 @@
+// gemm_tc.cu — BF16 x BF16 -> FP32 contraction on the 5th-generation tensor cores
+// (tcgen05.mma, accumulators in TMEM, operands staged by TMA), with a fused
+// per-tile argmax epilogue.  This is the dense cross-correlation of the projection-
+// matching form: C[m, n] = sum_k A[m, k] B[n, k] with both operands K-major, where a
+// row of A is one (particle, origin) and a row of B one orientation's central section.
+// The full C is never stored: each (row, 256-column tile) reduces to (max, argmax).
+//
+// Persistent kernel, one CTA per SM, 192 threads:
+//   warp 0    : TMA producer (one lane) filling a 4-stage ring of 128x64 A and
+//               256x64 B tiles (128-byte swizzle), mbarrier full/empty handshakes;
+//   warp 1    : MMA issuer (one lane): 4 x tcgen05.mma (M128 N256 K16) per stage into
+//               one of two TMEM accumulators (2 x 256 columns), tcgen05.commit frees
+//               the stage and, at the end of a tile, signals the epilogue;
+//   warps 2-5 : epilogue, one TMEM lane (= output row) per thread: tcgen05.ld 32
+//               columns at a time, running max/argmax, then release the accumulator.
+// Tiles are visited m-fastest so consecutive CTAs share a B tile through L2.
+// Every wait is bounded (2 s of %globaltimer); a timeout sets *err, the issuer drains
+// its MMAs, the producer waits for its copies, and TMEM is freed before exit.
+#include <cuda.h>
+#include <cudaTypedefs.h>
+#include <cuda_runtime.h>
+
+#include <cstdint>
+#include <cstring>
+
+#include "../../include/cryoim.h"
+#include "kernels.h"
+
+namespace cryoim {
+namespace {
+
+constexpr int GM = 128, GN = 256, GK = 64, NSTAGE = 4;
+constexpr int A_BYTES = GM * GK * 2, B_BYTES = GN * GK * 2;
+constexpr int STAGE_BYTES = A_BYTES + B_BYTES;
+constexpr int TMEM_COLS = 512;
+constexpr int NTHREADS = 192;
+constexpr unsigned long long WAIT_NS = 2000000000ull;
+constexpr int SMEM_BYTES = NSTAGE * STAGE_BYTES + 1024 + 256;
+
+// instruction descriptor, kind::f16: D=F32 (bits 4-5), A=BF16 (7-9), B=BF16 (10-12),
+// both K-major (bits 15, 16 = 0), N>>3 at bits 17-22, M>>4 at bits 24-28
+constexpr uint32_t IDESC = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(GN >> 3) << 17) |
+                           ((uint32_t)(GM >> 4) << 24);
+
+__device__ __forceinline__ uint32_t su32(const void* p) {
+    return (uint32_t)__cvta_generic_to_shared(p);
+}
+__device__ __forceinline__ uint64_t gtimer() {
+    uint64_t t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
+}
+__device__ __forceinline__ void mbar_init(uint64_t* b, uint32_t n) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(su32(b)), "r"(n) : "memory");
+}
+__device__ __forceinline__ bool mbar_try(uint64_t* b, uint32_t par) {
+    uint32_t ok;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+        "selp.u32 %0, 1, 0, p;\n}"
+        : "=r"(ok)
+        : "r"(su32(b)), "r"(par)
+        : "memory");
+    return ok != 0;
+}
+// Bounded wait.  abort_on_err: also give up as soon as another role has failed.
+__device__ __forceinline__ bool mbar_wait(uint64_t* b, uint32_t par, int* err, bool abort_on_err) {
+    if (mbar_try(b, par)) return true;
+    const uint64_t t0 = gtimer();
+    while (true) {
+        if (mbar_try(b, par)) return true;
+        if (abort_on_err && *(volatile int*)err) return false;
+        if (gtimer() - t0 > WAIT_NS) {
+            atomicExch(err, 1);
+            return false;
+        }
+    }
+}
+__device__ __forceinline__ void mbar_expect_tx(uint64_t* b, uint32_t bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(su32(b)), "r"(bytes)
+                 : "memory");
+}
+__device__ __forceinline__ void mbar_arrive(uint64_t* b) {
+    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(su32(b)) : "memory");
+}
+__device__ __forceinline__ void tma_load_2d(void* dst, const CUtensorMap* tm, int c0, int c1,
+                                            uint64_t* b) {
+    asm volatile(
+        "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes"
+        " [%0], [%1, {%2, %3}], [%4];" ::"r"(su32(dst)),
+        "l"((uint64_t)tm), "r"(c0), "r"(c1), "r"(su32(b))
+        : "memory");
+}
+__device__ __forceinline__ void tc_fence_before() {
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+}
+__device__ __forceinline__ void tc_fence_after() {
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+}
+__device__ __forceinline__ void tc_commit(uint64_t* b) {
+    asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
+                     su32(b))
+                 : "memory");
+}
+__device__ __forceinline__ void tc_mma(uint32_t d, uint64_t a, uint64_t bdesc, uint32_t acc) {
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "setp.ne.b32 p, %4, 0;\n\t"
+        "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}" ::"r"(d),
+        "l"(a), "l"(bdesc), "r"(IDESC), "r"(acc)
+        : "memory");
+}
+// shared-memory matrix descriptor: K-major, 128-byte swizzle, 8-row atoms 1024 B apart
+__device__ __forceinline__ uint64_t sdesc(uint32_t saddr) {
+    uint64_t d = 0;
+    d |= (uint64_t)((saddr & 0x3FFFFu) >> 4);
+    d |= (uint64_t)1 << 16;          // leading byte offset (unused for swizzled K-major)
+    d |= (uint64_t)(1024 >> 4) << 32;  // stride byte offset
+    d |= (uint64_t)1 << 46;          // descriptor version for tcgen05
+    d |= (uint64_t)2 << 61;          // SWIZZLE_128B
+    return d;
+}
+__device__ __forceinline__ void tmem_ld32(uint32_t taddr, float* v) {
+    uint32_t r[32];
+    asm volatile(
+        "tcgen05.ld.sync.aligned.32x32b.x32.b32 "
+        "{%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,"
+        "%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];"
+        : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]),
+          "=r"(r[7]), "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]),
+          "=r"(r[14]), "=r"(r[15]), "=r"(r[16]), "=r"(r[17]), "=r"(r[18]), "=r"(r[19]),
+          "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]), "=r"(r[24]), "=r"(r[25]),
+          "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
+        : "r"(taddr));
+    asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+    for (int i = 0; i < 32; ++i) v[i] = __uint_as_float(r[i]);
+}
+
+__global__ void __launch_bounds__(NTHREADS, 1)
+    k_gemm_bf16_argmax(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB,
+                       GemmArgmaxArgs g) {
+    extern __shared__ unsigned char smem_raw[];
+    unsigned char* sm = (unsigned char*)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
+    unsigned char* sA = sm;
+    unsigned char* sB = sm + NSTAGE * A_BYTES;
+    uint64_t* bars = (uint64_t*)(sB + NSTAGE * B_BYTES);
+    uint64_t* full = bars;
+    uint64_t* empty = bars + NSTAGE;
+    uint64_t* accf = bars + 2 * NSTAGE;
+    uint64_t* acce = accf + 2;
+    uint64_t* drain = acce + 2;
+    uint32_t* tmem_slot = (uint32_t*)(drain + 1);
+
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    if (threadIdx.x == 0) {
+        for (int s = 0; s < NSTAGE; ++s) { mbar_init(full + s, 1); mbar_init(empty + s, 1); }
+        for (int b = 0; b < 2; ++b) { mbar_init(accf + b, 1); mbar_init(acce + b, 128); }
+        mbar_init(drain, 1);
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+        asm volatile("prefetch.tensormap [%0];" ::"l"((uint64_t)&tmA) : "memory");
+        asm volatile("prefetch.tensormap [%0];" ::"l"((uint64_t)&tmB) : "memory");
+    }
+    if (warp == 0) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(
+                         su32(tmem_slot)),
+                     "r"(TMEM_COLS)
+                     : "memory");
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+    }
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    const uint32_t tmem = *tmem_slot;
+    const int total = g.m_tiles * g.n_tiles;
+
+    if (warp == 0) {
+        if (lane == 0) {
+            int s = 0;
+            uint32_t ph = 0;
+            uint32_t last_par[NSTAGE];
+            bool used[NSTAGE];
+            for (int i = 0; i < NSTAGE; ++i) { used[i] = false; last_par[i] = 0; }
+            bool ok = true;
+            for (int t = blockIdx.x; t < total && ok; t += gridDim.x) {
+                const int mt = t % g.m_tiles, nt = t / g.m_tiles;
+                for (int kb = 0; kb < g.kblocks; ++kb) {
+                    if (!mbar_wait(empty + s, ph ^ 1u, g.err, true)) { ok = false; break; }
+                    mbar_expect_tx(full + s, STAGE_BYTES);
+                    tma_load_2d(sA + s * A_BYTES, &tmA, kb * GK, mt * GM, full + s);
+                    tma_load_2d(sB + s * B_BYTES, &tmB, kb * GK, nt * GN, full + s);
+                    used[s] = true;
+                    last_par[s] = ph;
+                    if (++s == NSTAGE) { s = 0; ph ^= 1u; }
+                }
+            }
+            // every issued copy lands before the CTA can exit
+            for (int i = 0; i < NSTAGE; ++i)
+                if (used[i]) mbar_wait(full + i, last_par[i], g.err, false);
+        }
+    } else if (warp == 1) {
+        if (lane == 0) {
+            int s = 0, lt = 0;
+            uint32_t ph = 0;
+            bool ok = true;
+            for (int t = blockIdx.x; t < total && ok; t += gridDim.x, ++lt) {
+                const int b = lt & 1;
+                const uint32_t aph = (uint32_t)(lt >> 1) & 1u;
+                if (!mbar_wait(acce + b, aph ^ 1u, g.err, true)) break;
+                tc_fence_after();
+                const uint32_t d = tmem + (uint32_t)(b * GN);
+                for (int kb = 0; kb < g.kblocks; ++kb) {
+                    if (!mbar_wait(full + s, ph, g.err, true)) { ok = false; break; }
+                    tc_fence_after();
+                    const uint32_t a0 = su32(sA + s * A_BYTES), b0 = su32(sB + s * B_BYTES);
+#pragma unroll
+                    for (int kk = 0; kk < GK / 16; ++kk)
+                        tc_mma(d, sdesc(a0 + kk * 32), sdesc(b0 + kk * 32), (kb | kk) != 0);
+                    tc_commit(empty + s);
+                    if (++s == NSTAGE) { s = 0; ph ^= 1u; }
+                }
+                if (ok) tc_commit(accf + b);
+            }
+            // all issued MMAs complete before TMEM is released
+            tc_commit(drain);
+            mbar_wait(drain, 0, g.err, false);
+        }
+    } else {
+        const int q = warp & 3;
+        const int row_in_tile = 32 * q + lane;
+        int lt = 0;
+        for (int t = blockIdx.x; t < total; t += gridDim.x, ++lt) {
+            const int b = lt & 1;
+            const uint32_t aph = (uint32_t)(lt >> 1) & 1u;
+            if (!mbar_wait(accf + b, aph, g.err, true)) break;
+            tc_fence_after();
+            const int mt = t % g.m_tiles, nt = t / g.m_tiles;
+            const long row = (long)mt * GM + row_in_tile;
+            float best = -3.0e38f;
+            int bi = -1;
+            for (int c = 0; c < GN / 32; ++c) {
+                float v[32];
+                tmem_ld32(tmem + ((uint32_t)(32 * q) << 16) + (uint32_t)(b * GN + c * 32), v);
+                const int col0 = nt * GN + c * 32;
+#pragma unroll
+                for (int j = 0; j < 32; ++j) {
+                    const int col = col0 + j;
+                    if (col < g.n_valid && v[j] > best) { best = v[j]; bi = col; }
+                }
+                if (g.cfull && row < g.m_valid) {
+                    for (int j = 0; j < 32; ++j)
+                        if (col0 + j < g.n_valid) g.cfull[row * g.ldc + col0 + j] = v[j];
+                }
+            }
+            tc_fence_before();
+            mbar_arrive(acce + b);
+            if (row < g.m_valid) {
+                g.topv[row * g.n_tiles + nt] = best;
+                g.topi[row * g.n_tiles + nt] = bi;
+            }
+        }
+    }
+    tc_fence_before();
+    __syncthreads();
+    if (warp == 0) {
+        tc_fence_after();
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(TMEM_COLS)
+                     : "memory");
+    }
+}
+
+PFN_cuTensorMapEncodeTiled_v12000 encode_fn() {
+    static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
+    if (!fn) {
+        void* p = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) ==
+                cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            fn = (PFN_cuTensorMapEncodeTiled_v12000)p;
+    }
+    return fn;
+}
+
+// rows x k BF16, row-major (k contiguous), box = (GK, box_rows), 128-byte swizzle
+bool make_map(CUtensorMap* m, const void* base, long rows, int k, int box_rows) {
+    auto fn = encode_fn();
+    if (!fn) return false;
+    cuuint64_t dims[2] = {(cuuint64_t)k, (cuuint64_t)rows};
+    cuuint64_t strides[1] = {(cuuint64_t)k * 2};
+    cuuint32_t box[2] = {(cuuint32_t)GK, (cuuint32_t)box_rows};
+    cuuint32_t es[2] = {1, 1};
+    CUresult r = fn(m, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, const_cast<void*>(base), dims, strides, box,
+                    es, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B,
+                    CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    return r == CUDA_SUCCESS;
+}
+
+}  // namespace
+
+int gemm_tile_n() { return GN; }
+int gemm_tile_m() { return GM; }
+
+cudaError_t launch_gemm_bf16_argmax(const void* a, const void* b, int M, int N, int K,
+                                    const GemmArgmaxArgs& in, int num_sms, cudaStream_t st) {
+    if (K % GK != 0 || M < 1 || N < 1) return cudaErrorInvalidValue;
+    if (((uintptr_t)a & 15) || ((uintptr_t)b & 15)) return cudaErrorInvalidValue;
+    CUtensorMap ta, tb;
+    if (!make_map(&ta, a, M, K, GM) || !make_map(&tb, b, N, K, GN)) return cudaErrorInvalidValue;
+    GemmArgmaxArgs g = in;
+    g.m_tiles = (M + GM - 1) / GM;
+    g.n_tiles = (N + GN - 1) / GN;
+    g.kblocks = K / GK;
+    g.m_valid = M;
+    g.n_valid = N;
+    cudaError_t e = cudaFuncSetAttribute(k_gemm_bf16_argmax, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         SMEM_BYTES);
+    if (e != cudaSuccess) return e;
+    int total = g.m_tiles * g.n_tiles;
+    int grid = total < num_sms ? total : num_sms;
+    k_gemm_bf16_argmax<<<grid, NTHREADS, SMEM_BYTES, st>>>(ta, tb, g);
+    return cudaGetLastError();
+}
+
+}  // namespace cryoim
+
+// Kernel-level test hook (device pointers): C = A B^T with per-(row, 256-column tile)
+// max/argmax, optional full C.  d_err receives 1 if a pipeline wait timed out.
+extern "C" int cryoim_gemm_bf16_argmax(const void* d_a, const void* d_b, int32_t M, int32_t N,
+                                       int32_t K, float* d_topv, int32_t* d_topi, float* d_c,
+                                       int32_t* d_err, void* stream) {
+    if (!d_a || !d_b || !d_topv || !d_topi || !d_err) return CRYOIM_ERR_ARG;
+    if (M < 1 || N < 1 || K < 64 || K % 64) return CRYOIM_ERR_SIZE;
+    int dev = 0, sms = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess ||
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess)
+        return CRYOIM_ERR_CUDA;
+    cryoim::GemmArgmaxArgs g{};
+    g.topv = d_topv;
+    g.topi = d_topi;
+    g.cfull = d_c;
+    g.ldc = N;
+    g.err = d_err;
+    cudaStream_t st = (cudaStream_t)stream;
+    if (cudaMemsetAsync(d_err, 0, sizeof(int), st) != cudaSuccess) return CRYOIM_ERR_CUDA;
+    cudaError_t e = cryoim::launch_gemm_bf16_argmax(d_a, d_b, M, N, K, g, sms, st);
+    return e == cudaSuccess ? CRYOIM_OK : CRYOIM_ERR_CUDA;
+}

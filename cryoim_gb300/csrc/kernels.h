@@ -115,4 +115,19 @@ struct InsertArgs {
 };
 cudaError_t launch_insert(const InsertArgs& a, int B, cudaStream_t st);
 
+// ---- gemm_tc.cu (tcgen05 BF16 contraction with fused per-tile argmax) --------
+struct GemmArgmaxArgs {
+    int m_tiles, n_tiles, kblocks, m_valid, n_valid;  // set by the launcher
+    float* topv;   // [M][n_tiles] max of each row over each 256-column tile
+    int* topi;     // [M][n_tiles] its column
+    float* cfull;  // optional full C [M][ldc] (tests)
+    long ldc;
+    int* err;      // set to 1 when a wait times out (zero it before the launch)
+};
+int gemm_tile_n();
+int gemm_tile_m();
+// A: M x K, B: N x K, BF16 row-major (K contiguous, K % 64 == 0, 16-byte aligned)
+cudaError_t launch_gemm_bf16_argmax(const void* a, const void* b, int M, int N, int K,
+                                    const GemmArgmaxArgs& g, int num_sms, cudaStream_t st);
+
 }  // namespace cryoim

@@ -232,6 +232,15 @@ int cryoim_rec_get_partial(void* ctx, float* fa, float* fb, float* wg);
 int cryoim_central_sections(void* ctx, const float* ft_re, const float* ft_im,
                             const float* eulers, int32_t n, float* out_re, float* out_im);
 
+/* Kernel-level hook of the tensor-core contraction (no reference counterpart: the
+ * reference has no cross-correlation search).  Device pointers: A (M x K) and B (N x K)
+ * BF16 row-major with K % 64 == 0; C = A B^T in FP32 is reduced to the max and argmax
+ * of every (row, 256-column tile): d_topv / d_topi are M x ceil(N/256); d_c (optional)
+ * receives the full M x N C.  *d_err = 1 if a pipeline wait timed out. */
+int cryoim_gemm_bf16_argmax(const void* d_a, const void* d_b, int32_t M, int32_t N, int32_t K,
+                            float* d_topv, int32_t* d_topi, float* d_c, int32_t* d_err,
+                            void* stream);
+
 /* ---- orientation bookkeeping (proc_icos) --------------------------------- */
 
 /* The 60 icosahedral rotations in the 2-fold frame, in the order of
