@@ -144,6 +144,34 @@ class Context:
         call("cryoim_prscore_omega", self._h, ptr(a), ptr(b), ptr(f), ptr(c), float(theta), float(phi), ptr(out))
         return out
 
+    # -- contraction form ------------------------------------------------------
+    def set_reference_map(self, map3d: np.ndarray) -> None:
+        m = np.ascontiguousarray(map3d, dtype=np.float32)
+        call("cryoim_set_reference_map", self._h, ptr(m))
+
+    def contract_search(self, imgs, parts: np.ndarray, origin_max: float = 6.0,
+                        origin_step: float = 0.5, topk: int = 16, pick: int = 0,
+                        want_cands: bool = False):
+        """Tensor-core cross-correlation search with FP64 / phase-residual rescoring of
+        the top-k; parts is updated in place.  Returns (P, topk, 8) candidates if asked:
+        theta, phi, omega, x, y, CC (BF16 contraction), CC (FP64), PR."""
+        assert parts.dtype == PARTICLE_DTYPE and parts.flags["C_CONTIGUOUS"]
+        o = _abi.ContractOpts(float(origin_max), float(origin_step), int(topk), int(pick))
+        out = np.zeros((len(parts), topk, 8), np.float32) if want_cands else None
+        if isinstance(imgs, int):
+            call("cryoim_contract_search_device", self._h, C.c_void_p(imgs), ptr(parts), len(parts),
+                 C.byref(o), ptr(out))
+        else:
+            im = np.ascontiguousarray(imgs, dtype=np.float32)
+            call("cryoim_contract_search", self._h, ptr(im), ptr(parts), len(parts), C.byref(o), ptr(out))
+        return out
+
+    def contract_stats(self) -> dict:
+        v = np.zeros(6, np.float64)
+        call("cryoim_contract_stats", self._h, ptr(v))
+        return {"slice_ms": v[0], "gemm_ms": v[1], "gemm_launches": int(v[2]), "gemm_flops": v[3],
+                "orientations": int(v[4]), "kpad": int(v[5])}
+
     # -- mode 5 ---------------------------------------------------------------
     def refine(self, imgs, parts: np.ndarray) -> None:
         assert parts.dtype == PARTICLE_DTYPE and parts.flags["C_CONTIGUOUS"]

@@ -45,8 +45,15 @@ class Params(C.Structure):
         return {k: getattr(self, k) for k, _ in self._fields_}
 
 
+class ContractOpts(C.Structure):
+    """cryoim_contract_opts (include/cryoim.h)."""
+    _fields_ = [("origin_max", C.c_float), ("origin_step", C.c_float), ("topk", C.c_int32),
+                ("pick", C.c_int32)]
+
+
 _vp, _fp, _ip, _i32, _f32 = C.c_void_p, C.POINTER(C.c_float), C.POINTER(C.c_int32), C.c_int32, C.c_float
 _pp = C.POINTER(Params)
+_op = C.POINTER(ContractOpts)
 
 # name -> argtypes (every function returns int status unless listed in _RESTYPES)
 SIGNATURES = {
@@ -74,6 +81,10 @@ SIGNATURES = {
     "cryoim_prscore_noalloc": [_i32, _i32, _i32, _vp, _vp, _vp, _vp, _vp, _vp, _i32, _vp, _i32,
                                _vp, _vp],
     "cryoim_gemm_bf16_argmax": [_vp, _vp, _i32, _i32, _i32, _vp, _vp, _vp, _vp, _vp],
+    "cryoim_set_reference_map": [_vp, _vp],
+    "cryoim_contract_search": [_vp, _vp, _vp, _i32, _op, _vp],
+    "cryoim_contract_search_device": [_vp, _vp, _vp, _i32, _op, _vp],
+    "cryoim_contract_stats": [_vp, _vp],
     "cryoim_rec_begin": [_vp],
     "cryoim_rec_insert": [_vp, _vp, _vp, _i32, _ip],
     "cryoim_rec_insert_device": [_vp, _vp, _vp, _i32, _ip],

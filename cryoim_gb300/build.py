@@ -44,6 +44,7 @@ UNITS = {
     "api.cu": [],
     "noalloc.cu": [],
     "gemm_tc.cu": [],
+    "contract.cu": [],
 }
 
 

@@ -208,6 +208,27 @@ struct Ctx {
     float rec_ox = 0, rec_oy = 0;
     float rec_off_xy = 0, rec_off_z = 0;
     int rec_base_xy = 0, rec_base_z = 0;
+    // contraction form: map band cube, samples, orientation sections (operand B)
+    DBuf<float2> mapcube;
+    bool map_ready = false;
+    DBuf<int2> csamples;
+    int cS = 0, cKpad = 0;
+    DBuf<uint16_t> bmat;
+    long n_orient = 0;
+    bool bmat_ready = false;
+    double bmat_ms = 0.0;
+    DBuf<uint16_t> amat;
+    DBuf<float> corigins, topv, kcc, kcand, kpr;
+    DBuf<int> topi, gerr, kor, korig;
+    DBuf<double> pnorm, kcc64;
+    DBuf<float2> kalpha;
+    int n_origin = 0;
+    float orig_max = -1.0f, orig_step = -1.0f;
+    int num_sms = 0;
+    // CUDA-event timing of the contraction launches (with prof)
+    double prof_gemm_ms = 0.0;
+    long long prof_gemm_launches = 0;
+    double prof_gemm_flops = 0.0;
 
     ~Ctx() {
         cudaSetDevice(device);
@@ -217,6 +238,9 @@ struct Ctx {
         tfcut.release(); state.release(); cand.release(); rpr.release(); rot.release();
         prbuf.release(); fft.release(); band.release(); ralpha.release(); best.release();
         flag.release(); sel.release(); acc.release(); samples.release(); vol.release();
+        mapcube.release(); csamples.release(); bmat.release(); amat.release(); corigins.release();
+        topv.release(); kcc.release(); kcand.release(); kpr.release(); topi.release(); gerr.release();
+        kor.release(); korig.release(); pnorm.release(); kcc64.release(); kalpha.release();
         if (pe0) cudaEventDestroy(pe0);
         if (pe1) cudaEventDestroy(pe1);
         if (own_stream && stream) cudaStreamDestroy(stream);
@@ -627,6 +651,241 @@ int rec_insert_impl(Ctx* c, const float* imgs, bool on_device, const cryoim_part
     return CRYOIM_OK;
 }
 
+// ---------------------------------------------------------------------------
+// contraction form
+// ---------------------------------------------------------------------------
+
+// Half-plane band samples (hx > 0, or hx == 0 and ky > 0) with minR <= |h| <= maxR.
+int ensure_samples(Ctx* c) {
+    if (c->cS > 0) return CRYOIM_OK;
+    const int R = c->p.max_r, r0 = c->p.min_r;
+    std::vector<int2> s;
+    for (int ky = -R; ky <= R; ++ky)
+        for (int hx = 0; hx <= R; ++hx) {
+            if (hx == 0 && ky <= 0) continue;
+            const int d2 = hx * hx + ky * ky;
+            if (d2 >= r0 * r0 && d2 <= R * R) s.push_back(make_int2(hx, ky));
+        }
+    int r;
+    if ((r = c->csamples.ensure(s.size()))) return r;
+    CK(cudaMemcpyAsync(c->csamples.p, s.data(), sizeof(int2) * s.size(), cudaMemcpyHostToDevice, c->stream));
+    c->cS = (int)s.size();
+    c->cKpad = (2 * c->cS + 63) / 64 * 64;
+    return CRYOIM_OK;
+}
+
+int ensure_bmat(Ctx* c) {
+    int r;
+    if ((r = ensure_grid(c))) return r;
+    if ((r = ensure_samples(c))) return r;
+    const long n = (long)c->V * c->nom;
+    if (c->bmat_ready && c->n_orient == n) return CRYOIM_OK;
+    if ((r = c->bmat.ensure((size_t)n * c->cKpad))) return r;
+    std::vector<float> v2(2 * (size_t)c->V);
+    for (int v = 0; v < c->V; ++v) { v2[2 * v] = c->views[4 * v]; v2[2 * v + 1] = c->views[4 * v + 1]; }
+    DBuf<float> dv;
+    if ((r = dv.ensure(v2.size() + 2))) return r;
+    CK(cudaMemcpyAsync(dv.p, v2.data(), sizeof(float) * v2.size(), cudaMemcpyHostToDevice, c->stream));
+    cudaEvent_t e0, e1;
+    CK(cudaEventCreate(&e0));
+    CK(cudaEventCreate(&e1));
+    CK(cudaEventRecord(e0, c->stream));
+    CK(launch_slice_bf16(c->mapcube.p, c->p.max_r, c->csamples.p, c->cS, c->cKpad, dv.p, c->nom,
+                         c->p.searchstep, 0, n, c->bmat.p, c->stream));
+    CK(cudaEventRecord(e1, c->stream));
+    CK(cudaEventSynchronize(e1));
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, e0, e1);
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    c->bmat_ms = ms;
+    c->n_orient = n;
+    c->bmat_ready = true;
+    return CRYOIM_OK;
+}
+
+int contract_impl(Ctx* c, const float* imgs, bool on_device, cryoim_particle* parts, int P,
+                  const cryoim_contract_opts* opts, float* cands) {
+    int r = check_ready(c, false);
+    if (r) return r;
+    if (!imgs || !parts || !opts || P < 0) return fail(CRYOIM_ERR_ARG, "null input or negative count");
+    if (!c->map_ready) return fail(CRYOIM_ERR_STATE, "cryoim_set_reference_map has not been called");
+    const int k = opts->topk;
+    if (k < 1 || k > 64) return fail(CRYOIM_ERR_ARG, "topk must be 1..64");
+    if (!(opts->origin_step > 0) || opts->origin_max < 0) return fail(CRYOIM_ERR_ARG, "bad origin grid");
+    if (opts->pick == 0 && c->T <= 0)
+        return fail(CRYOIM_ERR_STATE, "PR rescoring needs cryoim_load_templates");
+    if (P == 0) return CRYOIM_OK;
+    if ((r = ensure_bmat(c))) return r;
+    if (c->n_orient > 0x7fffffffL) return fail(CRYOIM_ERR_SIZE, "too many orientations");
+    // origin grid
+    if (opts->origin_max != c->orig_max || opts->origin_step != c->orig_step) {
+        const int n1 = (int)(2.0f * opts->origin_max / opts->origin_step + 0.5f) + 1;
+        std::vector<float> og;
+        for (int iy = 0; iy < n1; ++iy)
+            for (int ix = 0; ix < n1; ++ix) {
+                og.push_back(-opts->origin_max + opts->origin_step * (float)ix);
+                og.push_back(-opts->origin_max + opts->origin_step * (float)iy);
+            }
+        if ((r = c->corigins.ensure(og.size()))) return r;
+        CK(cudaMemcpyAsync(c->corigins.p, og.data(), sizeof(float) * og.size(), cudaMemcpyHostToDevice,
+                           c->stream));
+        c->n_origin = n1 * n1;
+        c->orig_max = opts->origin_max;
+        c->orig_step = opts->origin_step;
+    }
+    const int O = c->n_origin, T = c->T, nx = c->p.fftsize;
+    const long nn = (long)nx * nx;
+    // particles per contraction launch: keep operand A (about 2400 rows) L2-resident
+    const int pb = std::max(1, std::min(c->batch, 2400 / std::max(O, 1)));
+    const int ntiles = (int)((c->n_orient + gemm_tile_n() - 1) / gemm_tile_n());
+    if ((r = ensure_batch(c, pb))) return r;
+    if ((r = c->amat.ensure((size_t)pb * O * c->cKpad))) return r;
+    if ((r = c->topv.ensure((size_t)pb * O * ntiles)) || (r = c->topi.ensure((size_t)pb * O * ntiles))) return r;
+    if ((r = c->gerr.ensure(1)) || (r = c->pnorm.ensure(pb)) || (r = c->kor.ensure((size_t)pb * k)) ||
+        (r = c->korig.ensure((size_t)pb * k)) || (r = c->kcc.ensure((size_t)pb * k)) ||
+        (r = c->kcand.ensure((size_t)pb * k * 5)) || (r = c->kcc64.ensure((size_t)pb * k)) ||
+        (r = c->kpr.ensure((size_t)pb * k)))
+        return r;
+    if (T > 0 && (r = c->kalpha.ensure((size_t)pb * k * T * 60))) return r;
+    if (c->num_sms == 0) CK(cudaDeviceGetAttribute(&c->num_sms, cudaDevAttrMultiProcessorCount, c->device));
+    std::vector<int> src(P);
+    {
+        int id0 = -100, cur = -1;
+        for (int i = 0; i < P; ++i) {
+            if (parts[i].img_id != id0) { cur = i; id0 = parts[i].img_id; }
+            src[i] = cur;
+        }
+    }
+    std::vector<float> hpar(8 * pb), hcand((size_t)pb * k * 5), hcc((size_t)pb * k), hpr((size_t)pb * k);
+    std::vector<int> hor((size_t)pb * k), horig((size_t)pb * k);
+    std::vector<double> hcc64((size_t)pb * k);
+    std::vector<float> ohost(2 * (size_t)O);
+    CK(cudaMemcpyAsync(ohost.data(), c->corigins.p, sizeof(float) * 2 * O, cudaMemcpyDeviceToHost, c->stream));
+    cudaEvent_t g0 = nullptr, g1 = nullptr;
+    if (c->prof) {
+        CK(cudaEventCreate(&g0));
+        CK(cudaEventCreate(&g1));
+    }
+    for (int b0 = 0; b0 < P; b0 += pb) {
+        const int nb = std::min(pb, P - b0);
+        const float* d_src;
+        if (on_device) {
+            d_src = imgs + b0 * nn;
+        } else {
+            CK(cudaMemcpyAsync(c->imgs.p, imgs + b0 * nn, sizeof(float) * nb * nn, cudaMemcpyHostToDevice,
+                               c->stream));
+            d_src = c->imgs.p;
+        }
+        std::fill(hpar.begin(), hpar.end(), 0.0f);
+        for (int i = 0; i < nb; ++i) {
+            const cryoim_particle& q = parts[b0 + i];
+            const cryoim_particle& s = parts[src[b0 + i]];
+            hpar[i] = q.x; hpar[pb + i] = q.y;
+            hpar[4 * pb + 3 * i] = s.df1; hpar[4 * pb + 3 * i + 1] = s.df2; hpar[4 * pb + 3 * i + 2] = s.astigang;
+        }
+        // mask at the input origin as ort_globesearch.f90:50 does; the transform stays unshifted
+        if ((r = transform_batch(c, d_src, nb, pb, hpar, 1, 0, false))) return r;
+        ParView pv = par_view(c, pb);
+        const float* ctfp = nullptr;
+        const float* tfc = c->tfcut0.p;
+        long tfs = 0;
+        if (c->p.apply_ctf) {
+            launch_ctf_band(nb, c->bd, pv.dfs, c->p.apix, c->p.vol, c->p.cs, c->p.ampwg, c->ctf.p, c->stream);
+            ctfp = c->ctf.p;
+            if (T > 0) {
+                launch_tmpl_fcut(c->tband.p, T, c->ctf.p, nb, c->bd, c->tfcut.p, c->stream);
+                tfc = c->tfcut.p;
+                tfs = (long)T * c->bd.nr;
+            }
+        }
+        launch_particle_norm(c->band.p, ctfp, c->bd, c->csamples.p, c->cS, nb, c->pnorm.p, c->stream);
+        launch_build_a(c->band.p, ctfp, c->bd, c->csamples.p, c->cS, c->cKpad, c->corigins.p, O, c->pnorm.p,
+                       nb, c->amat.p, c->stream);
+        CK(cudaGetLastError());
+        GemmArgmaxArgs g{};
+        g.topv = c->topv.p;
+        g.topi = c->topi.p;
+        g.cfull = nullptr;
+        g.err = c->gerr.p;
+        CK(cudaMemsetAsync(c->gerr.p, 0, sizeof(int), c->stream));
+        if (c->prof) CK(cudaEventRecord(g0, c->stream));
+        CK(launch_gemm_bf16_argmax(c->amat.p, c->bmat.p, nb * O, (int)c->n_orient, c->cKpad, g, c->num_sms,
+                                   c->stream));
+        if (c->prof) CK(cudaEventRecord(g1, c->stream));
+        launch_select_topk(c->topv.p, c->topi.p, O, ntiles, k, nb, c->kor.p, c->korig.p, c->kcc.p, c->stream);
+        CK(cudaGetLastError());
+        int gerr = 0;
+        CK(cudaMemcpyAsync(&gerr, c->gerr.p, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
+        CK(cudaMemcpyAsync(hor.data(), c->kor.p, sizeof(int) * nb * k, cudaMemcpyDeviceToHost, c->stream));
+        CK(cudaMemcpyAsync(horig.data(), c->korig.p, sizeof(int) * nb * k, cudaMemcpyDeviceToHost, c->stream));
+        CK(cudaMemcpyAsync(hcc.data(), c->kcc.p, sizeof(float) * nb * k, cudaMemcpyDeviceToHost, c->stream));
+        if ((r = check_flag(c))) return r;
+        if (gerr) return fail(CRYOIM_ERR_CUDA, "contraction pipeline wait timed out");
+        if (c->prof) {
+            float ms = 0.f;
+            CK(cudaEventElapsedTime(&ms, g0, g1));
+            c->prof_gemm_ms += ms;
+            c->prof_gemm_launches += 1;
+            c->prof_gemm_flops += 2.0 * (double)nb * O * (double)c->n_orient * (double)c->cKpad;
+        }
+        // candidates (theta, phi, omega, x, y) of the selected (orientation, origin) pairs
+        for (int i = 0; i < nb * k; ++i) {
+            int n = hor[i] < 0 ? 0 : hor[i];
+            int v = n / c->nom, io = n % c->nom;
+            int o = horig[i];
+            hcand[5 * i] = c->views[4 * v];
+            hcand[5 * i + 1] = c->views[4 * v + 1];
+            hcand[5 * i + 2] = c->p.searchstep * (float)io;
+            hcand[5 * i + 3] = ohost[2 * o];
+            hcand[5 * i + 4] = ohost[2 * o + 1];
+        }
+        CK(cudaMemcpyAsync(c->kcand.p, hcand.data(), sizeof(float) * nb * k * 5, cudaMemcpyHostToDevice,
+                           c->stream));
+        launch_cc_fp64(c->mapcube.p, c->band.p, ctfp, c->bd, c->csamples.p, c->cS, c->kcand.p, k, nb,
+                       c->kcc64.p, c->stream);
+        if (T > 0) {
+            launch_refine_alpha(c->kcand.p, nb, c->tort.p, T, c->ops.p, c->kalpha.p, c->stream, k);
+            PrSingleArgs a{};
+            a.band = c->band.p; a.fcut0 = c->fcut0.p; a.tband = c->tband.p; a.tfcut = tfc;
+            a.tfcut_pstride = tfs; a.ctf = ctfp; a.cand = c->kcand.p; a.alpha = c->kalpha.p; a.T = T;
+            a.bd = c->bd; a.pr = c->kpr.p; a.ncand = k;
+            CK(launch_pr_single(a, nb, c->stream));
+            CK(cudaMemcpyAsync(hpr.data(), c->kpr.p, sizeof(float) * nb * k, cudaMemcpyDeviceToHost, c->stream));
+        }
+        CK(cudaMemcpyAsync(hcc64.data(), c->kcc64.p, sizeof(double) * nb * k, cudaMemcpyDeviceToHost,
+                           c->stream));
+        CK(cudaStreamSynchronize(c->stream));
+        for (int i = 0; i < nb; ++i) {
+            int best = 0;
+            for (int j = 1; j < k; ++j) {
+                const int a = i * k + j, bsel = i * k + best;
+                if (opts->pick == 0 ? (hpr[a] < hpr[bsel]) : (hcc64[a] > hcc64[bsel])) best = j;
+            }
+            const int sidx = i * k + best;
+            cryoim_particle& q = parts[b0 + i];
+            q.theta0 = q.theta; q.phi0 = q.phi; q.omega0 = q.omega; q.x0 = q.x; q.y0 = q.y; q.pr0 = q.pr;
+            q.theta = hcand[5 * sidx]; q.phi = hcand[5 * sidx + 1]; q.omega = hcand[5 * sidx + 2];
+            q.x = hcand[5 * sidx + 3]; q.y = hcand[5 * sidx + 4];
+            q.pr = T > 0 ? hpr[sidx] : (float)hcc64[sidx];
+            q.dtheta = q.theta - q.theta0; q.dphi = q.phi - q.phi0; q.domega = q.omega - q.omega0;
+            q.dx = q.x - q.x0; q.dy = q.y - q.y0; q.dpr = q.pr - q.pr0;
+            if (cands)
+                for (int j = 0; j < k; ++j) {
+                    const int a = i * k + j;
+                    float* o = cands + ((size_t)(b0 + i) * k + j) * 8;
+                    for (int e = 0; e < 5; ++e) o[e] = hcand[5 * a + e];
+                    o[5] = hcc[a];
+                    o[6] = (float)hcc64[a];
+                    o[7] = T > 0 ? hpr[a] : 0.0f;
+                }
+        }
+    }
+    if (g0) cudaEventDestroy(g0);
+    if (g1) cudaEventDestroy(g1);
+    return CRYOIM_OK;
+}
+
 }  // namespace
 
 // ===========================================================================
@@ -790,8 +1049,14 @@ int cryoim_set_params(void* ctx, const cryoim_params* p) {
         c->T = 0;  // templates depend on the band geometry
         c->grid_ready = false;
         c->rec_active = false;
+        c->map_ready = false;
+        c->cS = 0;
+        c->bmat_ready = false;
     }
-    if (step_changed) c->grid_ready = false;
+    if (step_changed) {
+        c->grid_ready = false;
+        c->bmat_ready = false;
+    }
     long nn = (long)p->fftsize * p->fftsize;
     c->batch = (int)std::max(1L, std::min(64L, (long)(16L * 1024 * 1024) / nn));
     return CRYOIM_OK;
@@ -1132,6 +1397,65 @@ int cryoim_central_sections(void* ctx, const float* ft_re, const float* ft_im, c
     CK(cudaMemcpyAsync(out_re, ore.p, sizeof(float) * n * nn, cudaMemcpyDeviceToHost, c->stream));
     CK(cudaMemcpyAsync(out_im, oim.p, sizeof(float) * n * nn, cudaMemcpyDeviceToHost, c->stream));
     CK(cudaStreamSynchronize(c->stream));
+    return CRYOIM_OK;
+}
+
+int cryoim_set_reference_map(void* ctx, const float* map3d) {
+    Ctx* c = as_ctx(ctx);
+    int r = check_ready(c, false);
+    if (r) return r;
+    if (!map3d) return fail(CRYOIM_ERR_ARG, "null map");
+    const int nx = c->p.fftsize, R = c->p.max_r;
+    const long n3 = (long)nx * nx * nx, c3 = (long)(2 * R + 3) * (2 * R + 3) * (2 * R + 3);
+    DBuf<float> dmap;
+    DBuf<float2> work;
+    if ((r = dmap.ensure(n3)) || (r = work.ensure(n3)) || (r = c->mapcube.ensure(c3))) return r;
+    CK(cudaMemcpyAsync(dmap.p, map3d, sizeof(float) * n3, cudaMemcpyHostToDevice, c->stream));
+    launch_map_checker(dmap.p, nx, work.p, c->stream);
+    CK(cudaGetLastError());
+    cufftHandle h;
+    CKF(cufftPlan3d(&h, nx, nx, nx, CUFFT_C2C));
+    cufftResult fr = cufftSetStream(h, c->stream);
+    if (fr == CUFFT_SUCCESS) fr = cufftExecC2C(h, (cufftComplex*)work.p, (cufftComplex*)work.p, CUFFT_FORWARD);
+    if (fr != CUFFT_SUCCESS) {
+        cufftDestroy(h);
+        return fail(CRYOIM_ERR_CUDA, "3D forward FFT failed: cufft %d", (int)fr);
+    }
+    launch_map_band(work.p, nx, R, c->mapcube.p, c->stream);
+    cudaError_t e = cudaStreamSynchronize(c->stream);
+    cufftDestroy(h);
+    if (e != cudaSuccess) return fail(CRYOIM_ERR_CUDA, "reference map: %s", cudaGetErrorString(e));
+    c->map_ready = true;
+    c->bmat_ready = false;
+    return CRYOIM_OK;
+}
+
+int cryoim_contract_search(void* ctx, const float* imgs, cryoim_particle* parts, int32_t P,
+                           const cryoim_contract_opts* opts, float* cands) {
+    return contract_impl(as_ctx(ctx), imgs, false, parts, P, opts, cands);
+}
+
+int cryoim_contract_search_device(void* ctx, const float* d_imgs, cryoim_particle* parts, int32_t P,
+                                  const cryoim_contract_opts* opts, float* cands) {
+    return contract_impl(as_ctx(ctx), d_imgs, true, parts, P, opts, cands);
+}
+
+int cryoim_contract_stats(void* ctx, double* out /* 6 */) {
+    Ctx* c = as_ctx(ctx);
+    if (!c || !out) return fail(CRYOIM_ERR_ARG, "null argument");
+    int r;
+    if (c->map_ready && c->have_params && c->T >= 0) {
+        if ((r = ensure_grid(c)) || (r = ensure_samples(c))) return r;
+    }
+    out[0] = c->bmat_ms;
+    out[1] = c->prof_gemm_ms;
+    out[2] = (double)c->prof_gemm_launches;
+    out[3] = c->prof_gemm_flops;
+    out[4] = (double)((long)c->V * c->nom);
+    out[5] = (double)c->cKpad;
+    c->prof_gemm_ms = 0.0;
+    c->prof_gemm_launches = 0;
+    c->prof_gemm_flops = 0.0;
     return CRYOIM_OK;
 }
 

@@ -1,0 +1,320 @@
+// contract.cu — the projection-matching contraction form of the global search.
+//
+// Score: for particle p, origin s and orientation R,
+//     CC(p, s, R) = Re sum_h  A_ps(h) conj(B_R(h)) / (|A_p| |B_R|)
+// over the half-plane band samples h (minR <= |h| <= maxR), with
+//     A_ps(h) = CTF_p(h) P_p(h) exp(2 pi i h.(s + nx/2)/nx)     (the particle, its CTF and
+//               the origin shift of img2d_FT_centshift.f90, so the reference's CTF
+//               multiply and origin ramps sit on the particle side of the product)
+//     B_R(h)  = M(R (hx, ky, 0))                                (trilinear central section
+//               of the centred 3D Fourier map, project2d_FT3dTo2d.f90:30-83)
+// Stacking (Re, Im) along K turns it into one real contraction
+//     C[(p,s), R] = sum_k A[(p,s), k] B[R, k],   K = 2 x samples,
+// which gemm_tc.cu runs on the tensor cores in BF16 with FP32 accumulation.  The
+// normalisation sums are FP64; the best candidates are rescored in FP64 here and with
+// the reference's phase residual (k_pr_single) by the driver.
+#include <cuda_bf16.h>
+#include <cuda_runtime.h>
+
+#include "geom.cuh"
+#include "kernels.h"
+
+namespace cryoim {
+namespace {
+
+__device__ double block_sum_double(double v, double* sh) {
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    const int w = threadIdx.x >> 5, l = threadIdx.x & 31, nw = (blockDim.x + 31) >> 5;
+    __syncthreads();
+    if (l == 0) sh[w] = v;
+    __syncthreads();
+    double r = 0;
+    if (threadIdx.x < 32) {
+        r = (l < nw) ? sh[l] : 0.0;
+        for (int o = 16; o > 0; o >>= 1) r += __shfl_xor_sync(0xffffffffu, r, o);
+        if (l == 0) sh[0] = r;
+    }
+    __syncthreads();
+    r = sh[0];
+    __syncthreads();
+    return r;
+}
+
+// map * (-1)^(x+y+z) as complex, so the forward FFT is centred at nx/2
+__global__ void k_map_checker(const float* __restrict__ map, int nx, float2* __restrict__ out) {
+    const long n3 = (long)nx * nx * nx;
+    for (long q = (long)blockIdx.x * blockDim.x + threadIdx.x; q < n3; q += (long)gridDim.x * blockDim.x) {
+        int x = (int)(q % nx), y = (int)((q / nx) % nx), z = (int)(q / ((long)nx * nx));
+        float v = map[q];
+        out[q] = make_float2(((x + y + z) & 1) ? -v : v, 0.0f);
+    }
+}
+
+// Band cube of the transform: frequencies -(R+1) .. R+1 per axis, phase referenced to
+// the map centre ((-1)^(kx+ky+kz)), standard complex convention, scaled by 1/nx^3.
+__global__ void k_map_band(const float2* __restrict__ ft, int nx, int R, float2* __restrict__ cube) {
+    const int C = 2 * R + 3, h = nx / 2;
+    const long total = (long)C * C * C;
+    const float s = 1.0f / ((float)nx * (float)nx * (float)nx);
+    for (long q = (long)blockIdx.x * blockDim.x + threadIdx.x; q < total; q += (long)gridDim.x * blockDim.x) {
+        int x = (int)(q % C), y = (int)((q / C) % C), z = (int)(q / ((long)C * C));
+        int kx = x - (R + 1), ky = y - (R + 1), kz = z - (R + 1);
+        float2 v = ft[((long)(kz + h) * nx + (ky + h)) * nx + (kx + h)];
+        float sg = ((kx + ky + kz) & 1) ? -s : s;
+        cube[q] = make_float2(v.x * sg, v.y * sg);
+    }
+}
+
+__device__ __forceinline__ float2 cube_trilinear(const float2* __restrict__ cube, int C, int off,
+                                                 float x, float y, float z) {
+    const float fx = floorf(x), fy = floorf(y), fz = floorf(z);
+    const int ix = (int)fx + off, iy = (int)fy + off, iz = (int)fz + off;
+    const float ax = x - fx, ay = y - fy, az = z - fz;
+    const long b0 = ((long)iz * C + iy) * C + ix;
+    const long CC = (long)C * C;
+    float2 c000 = cube[b0], c100 = cube[b0 + 1], c010 = cube[b0 + C], c110 = cube[b0 + C + 1];
+    float2 c001 = cube[b0 + CC], c101 = cube[b0 + CC + 1], c011 = cube[b0 + CC + C], c111 = cube[b0 + CC + C + 1];
+    const float bx = 1.f - ax, by = 1.f - ay, bz = 1.f - az;
+    float2 r;
+    r.x = bz * (by * (bx * c000.x + ax * c100.x) + ay * (bx * c010.x + ax * c110.x)) +
+          az * (by * (bx * c001.x + ax * c101.x) + ay * (bx * c011.x + ax * c111.x));
+    r.y = bz * (by * (bx * c000.y + ax * c100.y) + ay * (bx * c010.y + ax * c110.y)) +
+          az * (by * (bx * c001.y + ax * c101.y) + ay * (bx * c011.y + ax * c111.y));
+    return r;
+}
+
+// One CTA per orientation n = view * nomega + iomega: section samples in shared
+// memory, FP64 norm, then the unit-norm row in BF16 (Re, Im interleaved, zero pad).
+__global__ void __launch_bounds__(256) k_slice_bf16(const float2* __restrict__ cube, int R,
+                                                    const int2* __restrict__ samples, int S, int Kpad,
+                                                    const float* __restrict__ views, int nom, float step,
+                                                    float d2r, long n0, __nv_bfloat162* __restrict__ B) {
+    extern __shared__ float2 ssec[];
+    __shared__ double sh[32];
+    __shared__ float rot[9];
+    const long n = n0 + blockIdx.x;
+    const int v = (int)(n / nom), io = (int)(n % nom);
+    if (threadIdx.x == 0) euler_mat(views[2 * v], views[2 * v + 1], step * (float)io, d2r, rot);
+    __syncthreads();
+    const int C = 2 * R + 3, off = R + 1;
+    double nrm = 0.0;
+    for (int i = threadIdx.x; i < S; i += blockDim.x) {
+        const int2 hk = samples[i];
+        const float hx = (float)hk.x, ky = (float)hk.y;
+        const float x = rot[0] * hx + rot[1] * ky, y = rot[3] * hx + rot[4] * ky, z = rot[6] * hx + rot[7] * ky;
+        float2 val = cube_trilinear(cube, C, off, x, y, z);
+        ssec[i] = val;
+        nrm += (double)val.x * val.x + (double)val.y * val.y;
+    }
+    nrm = block_sum_double(nrm, sh);
+    const float inv = nrm > 0.0 ? (float)(1.0 / sqrt(nrm)) : 0.0f;
+    __nv_bfloat162* row = B + (long)blockIdx.x * (Kpad / 2);
+    for (int i = threadIdx.x; i < Kpad / 2; i += blockDim.x) {
+        float2 val = i < S ? ssec[i] : make_float2(0.f, 0.f);
+        row[i] = __floats2bfloat162_rn(val.x * inv, val.y * inv);
+    }
+}
+
+// FP64 sum over samples of |CTF * P|^2 per particle (the origin shift keeps it).
+__global__ void k_particle_norm(const float2* __restrict__ band, const float* __restrict__ ctf, Band bd,
+                                const int2* __restrict__ samples, int S, double* __restrict__ norm) {
+    __shared__ double sh[32];
+    const int p = blockIdx.x, W = bd.W, R = bd.max_r;
+    const float2* b = band + (long)p * W * W;
+    const float* c = ctf ? ctf + (long)p * W * W : nullptr;
+    double acc = 0.0;
+    for (int i = threadIdx.x; i < S; i += blockDim.x) {
+        const int2 hk = samples[i];
+        const int q = (hk.y + R) * W + (hk.x + R);
+        const double cv = c ? (double)c[q] : 1.0;
+        const double re = b[q].x * cv, im = b[q].y * cv;
+        acc += re * re + im * im;
+    }
+    acc = block_sum_double(acc, sh);
+    if (threadIdx.x == 0) norm[p] = acc;
+}
+
+// Row (p, o) of A: CTF x particle x origin phase ramp, unit norm, BF16.
+__global__ void __launch_bounds__(256) k_build_a(const float2* __restrict__ band, const float* __restrict__ ctf,
+                                                 Band bd, const int2* __restrict__ samples, int S, int Kpad,
+                                                 const float* __restrict__ origins, int O,
+                                                 const double* __restrict__ norm, float two_pi_over_n,
+                                                 __nv_bfloat162* __restrict__ A) {
+    const int o = blockIdx.x, p = blockIdx.y, W = bd.W, R = bd.max_r;
+    const float2* b = band + (long)p * W * W;
+    const float* c = ctf ? ctf + (long)p * W * W : nullptr;
+    const float h = (float)(bd.nx / 2);
+    const float sx = origins[2 * o] + h, sy = origins[2 * o + 1] + h;
+    const float inv = norm[p] > 0.0 ? (float)(1.0 / sqrt(norm[p])) : 0.0f;
+    __nv_bfloat162* row = A + ((long)p * O + o) * (Kpad / 2);
+    for (int i = threadIdx.x; i < Kpad / 2; i += blockDim.x) {
+        float re = 0.f, im = 0.f;
+        if (i < S) {
+            const int2 hk = samples[i];
+            const int q = (hk.y + R) * W + (hk.x + R);
+            const float2 ab = b[q];  // (a, b) = (Re F, -Im F) referenced to pixel 0
+            float sn, cs;
+            sincosf(two_pi_over_n * (sx * (float)hk.x + sy * (float)hk.y), &sn, &cs);
+            // centshift: (a', b') = (a cos + b sin, -a sin + b cos); P = a' - i b'
+            const float a2 = ab.x * cs + ab.y * sn, b2 = -ab.x * sn + ab.y * cs;
+            const float cv = (c ? c[q] : 1.0f) * inv;
+            re = a2 * cv;
+            im = -b2 * cv;
+        }
+        row[i] = __floats2bfloat162_rn(re, im);
+    }
+}
+
+// Per particle: the k best (row, tile) maxima over its O origin rows, by repeated
+// block argmax (selected entries are set to -inf in topv, a scratch array).
+__global__ void k_select_topk(float* __restrict__ topv, const int* __restrict__ topi, int O, int ntiles,
+                              int k, int* __restrict__ out_orient, int* __restrict__ out_origin,
+                              float* __restrict__ out_cc) {
+    __shared__ float sv[32];
+    __shared__ long si[32];
+    const int p = blockIdx.x;
+    const long base = (long)p * O * ntiles, cnt = (long)O * ntiles;
+    for (int r = 0; r < k; ++r) {
+        float bv = -3.0e38f;
+        long bi = -1;
+        for (long q = threadIdx.x; q < cnt; q += blockDim.x) {
+            float v = topv[base + q];
+            if (v > bv) { bv = v; bi = q; }
+        }
+        for (int off = 16; off > 0; off >>= 1) {
+            float ov = __shfl_xor_sync(0xffffffffu, bv, off);
+            long oi = __shfl_xor_sync(0xffffffffu, bi, off);
+            if (ov > bv || (ov == bv && oi < bi && oi >= 0)) { bv = ov; bi = oi; }
+        }
+        const int w = threadIdx.x >> 5, l = threadIdx.x & 31, nw = blockDim.x >> 5;
+        if (l == 0) { sv[w] = bv; si[w] = bi; }
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            float v0 = sv[0];
+            long i0 = si[0];
+            for (int q = 1; q < nw; ++q)
+                if (sv[q] > v0 || (sv[q] == v0 && si[q] < i0 && si[q] >= 0)) { v0 = sv[q]; i0 = si[q]; }
+            if (i0 >= 0) {
+                out_orient[p * k + r] = topi[base + i0];
+                out_origin[p * k + r] = (int)(i0 / ntiles);
+                out_cc[p * k + r] = v0;
+                topv[base + i0] = -3.0e38f;
+            } else {
+                out_orient[p * k + r] = -1;
+                out_origin[p * k + r] = 0;
+                out_cc[p * k + r] = -3.0e38f;
+            }
+        }
+        __syncthreads();
+    }
+}
+
+// FP64 rescoring of one (particle, candidate): the same CC with every product,
+// interpolation and sum in double precision.
+__global__ void k_cc_fp64(const float2* __restrict__ cube, const float2* __restrict__ band,
+                          const float* __restrict__ ctf, Band bd, const int2* __restrict__ samples, int S,
+                          const float* __restrict__ cand, int k, double* __restrict__ out) {
+    __shared__ double sh[32];
+    __shared__ double rot[9];
+    const int c = blockIdx.x, p = blockIdx.y, W = bd.W, R = bd.max_r, C = 2 * R + 3, off = R + 1;
+    const float* cd = cand + ((long)p * k + c) * 5;
+    if (threadIdx.x == 0) {
+        const double d2r = 3.14159265358979323846 / 180.0;
+        double t = cd[0] * d2r, ph = cd[1] * d2r, om = cd[2] * d2r;
+        double c1 = cos(ph), c2 = cos(t), c3 = cos(om), s1 = sin(ph), s2 = sin(t), s3 = sin(om);
+        rot[0] = c1 * c2 * c3 - s1 * s3; rot[1] = -c1 * c2 * s3 - c3 * s1; rot[2] = c1 * s2;
+        rot[3] = c2 * c3 * s1 + c1 * s3; rot[4] = -c2 * s1 * s3 + c1 * c3; rot[5] = s1 * s2;
+        rot[6] = -c3 * s2;               rot[7] = s2 * s3;                 rot[8] = c2;
+    }
+    __syncthreads();
+    const float2* b = band + (long)p * W * W;
+    const float* cb = ctf ? ctf + (long)p * W * W : nullptr;
+    const double h = (double)(bd.nx / 2), sx = cd[3] + h, sy = cd[4] + h;
+    const double tpn = 2.0 * 3.14159265358979323846 / (double)bd.nx;
+    double dot = 0, na = 0, nb = 0;
+    for (int i = threadIdx.x; i < S; i += blockDim.x) {
+        const int2 hk = samples[i];
+        const double x = rot[0] * hk.x + rot[1] * hk.y, y = rot[3] * hk.x + rot[4] * hk.y,
+                     z = rot[6] * hk.x + rot[7] * hk.y;
+        const double fx = floor(x), fy = floor(y), fz = floor(z);
+        const int ix = (int)fx + off, iy = (int)fy + off, iz = (int)fz + off;
+        const double ax = x - fx, ay = y - fy, az = z - fz;
+        double sr = 0, si = 0;
+        for (int dz = 0; dz < 2; ++dz)
+            for (int dy = 0; dy < 2; ++dy)
+                for (int dx = 0; dx < 2; ++dx) {
+                    const double w = (dx ? ax : 1 - ax) * (dy ? ay : 1 - ay) * (dz ? az : 1 - az);
+                    const float2 v = cube[((long)(iz + dz) * C + (iy + dy)) * C + (ix + dx)];
+                    sr += w * v.x;
+                    si += w * v.y;
+                }
+        const int q = (hk.y + R) * W + (hk.x + R);
+        const double th = tpn * (sx * hk.x + sy * hk.y);
+        const double cs = cos(th), sn = sin(th);
+        const double a2 = b[q].x * cs + b[q].y * sn, b2 = -b[q].x * sn + b[q].y * cs;
+        const double cv = cb ? (double)cb[q] : 1.0;
+        const double pr = a2 * cv, pi = -b2 * cv;
+        dot += pr * sr + pi * si;
+        na += pr * pr + pi * pi;
+        nb += sr * sr + si * si;
+    }
+    dot = block_sum_double(dot, sh);
+    na = block_sum_double(na, sh);
+    nb = block_sum_double(nb, sh);
+    if (threadIdx.x == 0) out[(long)p * k + c] = (na > 0 && nb > 0) ? dot / sqrt(na * nb) : 0.0;
+}
+
+inline int cdiv(long a, long b) { return (int)((a + b - 1) / b); }
+
+}  // namespace
+
+void launch_map_checker(const float* map, int nx, float2* work, cudaStream_t st) {
+    const long n3 = (long)nx * nx * nx;
+    k_map_checker<<<cdiv(n3, 256) < 65535 ? cdiv(n3, 256) : 65535, 256, 0, st>>>(map, nx, work);
+}
+
+void launch_map_band(const float2* ft, int nx, int R, float2* cube, cudaStream_t st) {
+    const long c3 = (long)(2 * R + 3) * (2 * R + 3) * (2 * R + 3);
+    k_map_band<<<cdiv(c3, 256) < 65535 ? cdiv(c3, 256) : 65535, 256, 0, st>>>(ft, nx, R, cube);
+}
+
+cudaError_t launch_slice_bf16(const float2* cube, int R, const int2* samples, int S, int Kpad,
+                              const float* views, int nom, float step, long n0, long count, void* B,
+                              cudaStream_t st) {
+    size_t sm = (size_t)S * sizeof(float2);
+    cudaError_t e = cudaFuncSetAttribute(k_slice_bf16, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+    if (e != cudaSuccess) return e;
+    for (long c0 = 0; c0 < count; c0 += 65535) {
+        long nb = count - c0 < 65535 ? count - c0 : 65535;
+        k_slice_bf16<<<(unsigned)nb, 256, sm, st>>>(cube, R, samples, S, Kpad, views, nom, step,
+                                                   host_angles().deg2rad, n0 + c0,
+                                                   (__nv_bfloat162*)B + c0 * (Kpad / 2));
+    }
+    return cudaGetLastError();
+}
+
+void launch_particle_norm(const float2* band, const float* ctf, Band bd, const int2* samples, int S,
+                          int B, double* norm, cudaStream_t st) {
+    k_particle_norm<<<B, 256, 0, st>>>(band, ctf, bd, samples, S, norm);
+}
+
+void launch_build_a(const float2* band, const float* ctf, Band bd, const int2* samples, int S, int Kpad,
+                    const float* origins, int O, const double* norm, int B, void* A, cudaStream_t st) {
+    dim3 g(O, B);
+    const float tpn = 2.0f * host_angles().pi / (float)bd.nx;
+    k_build_a<<<g, 256, 0, st>>>(band, ctf, bd, samples, S, Kpad, origins, O, norm, tpn,
+                                 (__nv_bfloat162*)A);
+}
+
+void launch_select_topk(float* topv, const int* topi, int O, int ntiles, int k, int B, int* orient,
+                        int* origin, float* cc, cudaStream_t st) {
+    k_select_topk<<<B, 512, 0, st>>>(topv, topi, O, ntiles, k, orient, origin, cc);
+}
+
+void launch_cc_fp64(const float2* cube, const float2* band, const float* ctf, Band bd, const int2* samples,
+                    int S, const float* cand, int k, int B, double* out, cudaStream_t st) {
+    dim3 g(k, B);
+    k_cc_fp64<<<g, 256, 0, st>>>(cube, band, ctf, bd, samples, S, cand, k, out);
+}
+
+}  // namespace cryoim

@@ -53,7 +53,7 @@ void launch_alpha_table(const float* views, int V, const float* tort, int T, con
 void launch_refine_candidates(float* state, int B, float dang, float dtran, const float* ops,
                               float* cand, cudaStream_t st);
 void launch_refine_alpha(const float* cand, int B, const float* tort, int T, const float* ops,
-                         float2* alpha, cudaStream_t st);
+                         float2* alpha, cudaStream_t st, int ncand = 11);
 void launch_refine_select(const float* cand, const float* pr, int B, float* state,
                           cudaStream_t st);
 // reconstruction finish: fold / divide / sign into the full complex grid
@@ -92,11 +92,12 @@ struct PrSingleArgs {
     const float* tfcut;
     long tfcut_pstride;
     const float* ctf;        // [B][W*W] or nullptr
-    const float* cand;       // [B][11][5]
-    const float2* alpha;     // [B][11][T][60]
+    const float* cand;       // [B][ncand][5]
+    const float2* alpha;     // [B][ncand][T][60]
     int T;
     Band bd;
-    float* pr;               // [B][11]
+    float* pr;               // [B][ncand]
+    int ncand = 11;          // 11 for the refinement step (ort_cent_11.f90)
 };
 cudaError_t launch_pr_single(const PrSingleArgs& a, int B, cudaStream_t st);
 
@@ -129,5 +130,24 @@ int gemm_tile_m();
 // A: M x K, B: N x K, BF16 row-major (K contiguous, K % 64 == 0, 16-byte aligned)
 cudaError_t launch_gemm_bf16_argmax(const void* a, const void* b, int M, int N, int K,
                                     const GemmArgmaxArgs& g, int num_sms, cudaStream_t st);
+
+// ---- contract.cu (operands of the contraction, selection, FP64 rescoring) ------
+// Fourier band cube of the reference map: (2R+3)^3 float2, frequencies -(R+1)..R+1.
+void launch_map_checker(const float* map, int nx, float2* work, cudaStream_t st);
+void launch_map_band(const float2* ft, int nx, int R, float2* cube, cudaStream_t st);
+// Rows n0 .. n0+count-1 of B (orientation n = view * nom + iomega), unit norm, BF16.
+cudaError_t launch_slice_bf16(const float2* cube, int R, const int2* samples, int S, int Kpad,
+                              const float* views, int nom, float step, long n0, long count, void* B,
+                              cudaStream_t st);
+void launch_particle_norm(const float2* band, const float* ctf, Band bd, const int2* samples, int S,
+                          int B, double* norm, cudaStream_t st);
+// Rows (p, o) of A, p < B, o < O; origins: O x 2 (x, y) pixels.
+void launch_build_a(const float2* band, const float* ctf, Band bd, const int2* samples, int S, int Kpad,
+                    const float* origins, int O, const double* norm, int B, void* A, cudaStream_t st);
+void launch_select_topk(float* topv, const int* topi, int O, int ntiles, int k, int B, int* orient,
+                        int* origin, float* cc, cudaStream_t st);
+// cand: B x k x (theta, phi, omega, x, y); out: B x k FP64 cross-correlations
+void launch_cc_fp64(const float2* cube, const float2* band, const float* ctf, Band bd, const int2* samples,
+                    int S, const float* cand, int k, int B, double* out, cudaStream_t st);
 
 }  // namespace cryoim

@@ -310,11 +310,11 @@ __global__ void k_refine_candidates(float* __restrict__ state, int B, float dang
     }
 }
 
-__global__ void k_refine_alpha(const float* __restrict__ cand, int B, const float* __restrict__ tort,
-                               int T, const float* __restrict__ ops, float d2r, float r2d,
-                               float2* __restrict__ alpha) {
+__global__ void k_refine_alpha(const float* __restrict__ cand, long ncand_rows,
+                               const float* __restrict__ tort, int T, const float* __restrict__ ops,
+                               float d2r, float r2d, float2* __restrict__ alpha) {
     long q = (long)blockIdx.x * blockDim.x + threadIdx.x;
-    long total = (long)B * 11 * T * 60;
+    long total = ncand_rows * T * 60;
     if (q >= total) return;
     int j = (int)(q % 60);
     int i = (int)((q / 60) % T);
@@ -526,10 +526,11 @@ void launch_refine_candidates(float* state, int B, float dang, float dtran, cons
 }
 
 void launch_refine_alpha(const float* cand, int B, const float* tort, int T, const float* ops,
-                         float2* alpha, cudaStream_t st) {
-    long total = (long)B * 11 * T * 60;
+                         float2* alpha, cudaStream_t st, int ncand) {
+    long rows = (long)B * ncand;
+    long total = rows * T * 60;
     HostAngles a = angles();
-    k_refine_alpha<<<cdiv(total, 128), 128, 0, st>>>(cand, B, tort, T, ops, a.d2r, a.r2d, alpha);
+    k_refine_alpha<<<cdiv(total, 128), 128, 0, st>>>(cand, rows, tort, T, ops, a.d2r, a.r2d, alpha);
 }
 
 void launch_refine_select(const float* cand, const float* pr, int B, float* state,

@@ -190,7 +190,7 @@ __global__ void __launch_bounds__(512) k_pr_single(PrSingleArgs a, Consts K) {
     const Band bd = a.bd;
     const int W = bd.W, nr = bd.nr, minR = bd.min_r, nx = bd.nx;
     const int c = blockIdx.x, p = blockIdx.y;
-    const float* cd = a.cand + ((long)p * 11 + c) * 5;
+    const float* cd = a.cand + ((long)p * a.ncand + c) * 5;
     const float nxh = (float)(nx / 2);
     const float xs = __fadd_rn(cd[3], nxh), ys = __fadd_rn(cd[4], nxh);
     const int offW = bd.off * W + bd.off;
@@ -201,7 +201,7 @@ __global__ void __launch_bounds__(512) k_pr_single(PrSingleArgs a, Consts K) {
     const float twopi = __fmul_rn(2.0f, K.pi);
     double p1 = 0.0, p2 = 0.0;
     for (int i = 0; i < a.T; ++i) {
-        const float2* al = a.alpha + (((long)p * 11 + c) * a.T + i) * 60;
+        const float2* al = a.alpha + (((long)p * a.ncand + c) * a.T + i) * 60;
         const float2* tb = a.tband + (long)i * W * W;
         const float* fct = tfc + (long)i * nr;
         for (int q = threadIdx.x; q < 60 * nr; q += blockDim.x) {
@@ -256,7 +256,7 @@ __global__ void __launch_bounds__(512) k_pr_single(PrSingleArgs a, Consts K) {
         double s1 = 0, s2 = 0;
         for (int q = 0; q < nw; ++q) { s1 += sh[0][q]; s2 += sh[1][q]; }
         float f1 = (float)s1, f2 = (float)s2;
-        a.pr[(long)p * 11 + c] = (f2 > 1.0e-10f) ? f1 / f2 * 180.0f / K.pi : 1000.0f;
+        a.pr[(long)p * a.ncand + c] = (f2 > 1.0e-10f) ? f1 / f2 * 180.0f / K.pi : 1000.0f;
     }
 }
 
@@ -356,7 +356,7 @@ cudaError_t launch_pr_omega(const PrOmegaArgs& a, int B, cudaStream_t st) {
 }
 
 cudaError_t launch_pr_single(const PrSingleArgs& a, int B, cudaStream_t st) {
-    dim3 grid(11, B);
+    dim3 grid(a.ncand, B);
     k_pr_single<<<grid, 512, 0, st>>>(a, consts());
     return cudaGetLastError();
 }

@@ -232,6 +232,31 @@ int cryoim_rec_get_partial(void* ctx, float* fa, float* fb, float* wg);
 int cryoim_central_sections(void* ctx, const float* ft_re, const float* ft_im,
                             const float* eulers, int32_t n, float* out_re, float* out_im);
 
+/* ---- projection-matching contraction form -------------------------------- */
+/* No counterpart in the reference, which scores by phase residual only.  A second
+ * search beside cryoim_globesearch: the cross-correlation of every (particle, origin)
+ * with every grid orientation's central section, run as one dense BF16 contraction on
+ * the tensor cores (FP32 accumulation), its top-k candidates per particle rescored in
+ * FP64 and with the reference's phase residual (cal_crosslin_PR.f90), the particle
+ * updated with the best by PR (pick = 0) or by FP64 cross-correlation (pick = 1). */
+typedef struct cryoim_contract_opts {
+    float origin_max;   /* origins searched on [-origin_max, origin_max]^2 pixels   */
+    float origin_step;  /* origin grid step, pixels                                 */
+    int32_t topk;       /* candidates rescored per particle (1..64)                 */
+    int32_t pick;       /* 0: minimum phase residual, 1: maximum FP64 correlation  */
+} cryoim_contract_opts;
+/* The 3D map (nx^3 float32) whose central sections are correlated: its centred Fourier
+ * transform is kept as a band cube of (2 maxR + 3)^3 complex values. */
+int cryoim_set_reference_map(void* ctx, const float* map3d);
+/* cands (optional): P x topk x 8 floats (theta, phi, omega, x, y, CC bf16, CC fp64, PR). */
+int cryoim_contract_search(void* ctx, const float* imgs, cryoim_particle* parts, int32_t P,
+                           const cryoim_contract_opts* opts, float* cands);
+int cryoim_contract_search_device(void* ctx, const float* d_imgs, cryoim_particle* parts, int32_t P,
+                                  const cryoim_contract_opts* opts, float* cands);
+/* out[6]: section build ms, contraction ms and launches since the last call (timed when
+ * profiling is on), contraction FLOP, orientations, padded K. Resets the counters. */
+int cryoim_contract_stats(void* ctx, double* out);
+
 /* Kernel-level hook of the tensor-core contraction (no reference counterpart: the
  * reference has no cross-correlation search).  Device pointers: A (M x K) and B (N x K)
  * BF16 row-major with K % 64 == 0; C = A B^T in FP32 is reduced to the max and argmax

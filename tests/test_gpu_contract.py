@@ -1,0 +1,102 @@
+"""The projection-matching contraction form (cryoim_contract_search): every returned
+candidate's FP64 cross-correlation equals an independent FP64 restatement (oracle
+central section of the map's centred transform x oracle-prepared particle, CTF and
+origin shift), the BF16 tensor-core score tracks it, the phase-residual rescoring
+matches the oracle's cal_crosslin_PR, and noise-free particles land on their true
+orientation (up to symmetry)."""
+import numpy as np
+import pytest
+
+from _data import small_case
+
+pytestmark = pytest.mark.gpu
+
+
+def map_cube_full(vol):
+    """Centred FT of the map (phase at the map centre), standard complex, / n^3."""
+    n = vol.shape[-1]
+    z, y, x = np.indices(vol.shape)
+    chk = np.where((x + y + z) % 2 == 1, -1.0, 1.0)
+    ft = np.fft.fftn(vol.astype(np.float64) * chk) / n ** 3
+    k = np.arange(n) - n // 2
+    sg = np.where((k[:, None, None] + k[None, :, None] + k[None, None, :]) % 2 == 1, -1.0, 1.0)
+    return ft * sg
+
+
+def cc_fp64(orc, p, vol_ft, img, part, cand):
+    n, R, r0 = p.fftsize, p.max_r, p.min_r
+    h = n // 2
+    sre, sim = orc.central_section(vol_ft.real, vol_ft.imag, *cand[:3], fp="f64")
+    a, b, _ = orc.prep_particle(img, 1, p.imgmask_px, part["x"], part["y"], 0, r0, R, "f64")
+    a, b = orc.centshift(a, b, cand[3], cand[4], "f64")
+    ctf = orc.ctf2d(n, part["df1"], part["df2"], part["astigang"], p.apix, p.vol, p.cs, p.ampwg, "f64")
+    ky, hx = np.meshgrid(np.arange(n) - h, np.arange(n) - h, indexing="ij")
+    d2 = hx ** 2 + ky ** 2
+    half = ((hx > 0) | ((hx == 0) & (ky > 0))) & (d2 >= r0 * r0) & (d2 <= R * R)
+    pr, pi = (a * ctf)[half], (-b * ctf)[half]
+    qr, qi = sre[half], sim[half]
+    return float(np.sum(pr * qr + pi * qi) / np.sqrt(np.sum(pr * pr + pi * pi) * np.sum(qr * qr + qi * qi)))
+
+
+@pytest.fixture(scope="module")
+def run(built, orc):
+    import cryoim_gb300 as ci
+    case = small_case(P=3, T=4, step=4.0)
+    p, vol, tmpl, timgs, imgs, parts, truth = case
+    with ci.Context(0, p) as ctx:
+        ctx.load_templates(timgs, tmpl)
+        ctx.set_reference_map(vol)
+        q = parts.copy()
+        cands = ctx.contract_search(imgs, q, origin_max=2.0, origin_step=0.5, topk=8, want_cands=True)
+        stats = ctx.contract_stats()
+    return case, q, cands, stats
+
+
+def test_fp64_rescoring_matches_independent_cc(run, orc):
+    (p, vol, tmpl, timgs, imgs, parts, truth), q, cands, stats = run
+    vol_ft = map_cube_full(vol)
+    for i in range(len(parts)):
+        for j in range(3):
+            c = cands[i, j]
+            want = cc_fp64(orc, p, vol_ft, imgs[i], parts[i], c[:5].astype(np.float64))
+            assert abs(c[6] - want) < 2e-5, (i, j, c[6], want)
+            # BF16 operands, FP32 accumulation
+            assert abs(c[5] - c[6]) < 2e-2, (i, j, c[5], c[6])
+
+
+def test_candidates_are_sorted_and_distinct(run):
+    (p, *_), q, cands, stats = run
+    for i in range(cands.shape[0]):
+        cc = cands[i, :, 5]
+        assert np.all(np.diff(cc) <= 1e-6)
+        keys = {tuple(np.round(c[:5], 4)) for c in cands[i]}
+        assert len(keys) == cands.shape[1]
+    assert stats["orientations"] > 0 and stats["kpad"] % 64 == 0
+
+
+def test_pr_rescoring_matches_oracle(run, orc):
+    (p, vol, tmpl, timgs, imgs, parts, truth), q, cands, stats = run
+    tm, tf = orc.load_templates(timgs, tmpl, p, "f64")
+    tort = np.stack([tmpl["theta"], tmpl["phi"], tmpl["omega"]], 1)
+    for i in range(len(parts)):
+        a, b, f = orc.prep_particle(imgs[i], 1, p.imgmask_px, parts["x"][i], parts["y"][i], 0,
+                                    p.min_r, p.max_r, "f64")
+        ctf = orc.ctf2d(p.fftsize, parts["df1"][i], parts["df2"][i], parts["astigang"][i], p.apix,
+                        p.vol, p.cs, p.ampwg, "f64")
+        for j in range(cands.shape[1]):
+            c = cands[i, j]
+            want = orc.pr_single(a, b, f, tm, tort, tf, ctf, p.min_r, p.max_r, *c[:5], fp="f64")
+            assert abs(c[7] - want) / want < 5e-3
+        best = int(np.argmin(cands[i, :, 7]))
+        assert q["pr"][i] == cands[i, best, 7]
+        assert q["theta"][i] == cands[i, best, 0] and q["x"][i] == cands[i, best, 3]
+
+
+def test_noise_free_particles_find_their_orientation(run):
+    from cryoim_gb300 import synth
+    (p, vol, tmpl, timgs, imgs, parts, truth), q, cands, stats = run
+    for i in range(len(parts)):
+        top = cands[i, 0]
+        err = synth.orientation_error(tuple(top[:3]), truth[i])
+        assert err < 1.5 * p.searchstep, (i, err)
+        assert abs(top[3] - parts["x"][i]) <= 0.5 and abs(top[4] - parts["y"][i]) <= 0.5
