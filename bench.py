@@ -1,22 +1,30 @@
 #!/usr/bin/env python3
-"""Throughput of the icosahedral global orientation search at box 256.
+"""Global orientation search throughput at box 256: the BF16 tensor-core contraction
+form against the plain FP32 (reference-parity) form.
 
-Workload (the production-size plain-method configuration): 256x256 particles at
-1.5 A/px, band 1/50 - 1/6 A^-1 (minR 7, maxR 64), 1-degree asymmetric-unit grid
-(Nomega 360), 20 templates, CTF 300 kV / 2.7 mm / 0.07 with defocus 0.8-3.5 um and
-astigmatism up to 0.1 um, SNR 0.05, origins within +-6 px.  Synthetic, seeded
-(phantom: Gaussian blobs placed by the 60 icosahedral rotations plus a shell; random-
-init inputs with the workload's shapes and value distributions).
+Workload (the production-size configuration): 256x256 particles at 1.5 A/px, band
+1/50 - 1/6 A^-1 (minR 7, maxR 64), 1-degree asymmetric-unit grid (664 views x 360
+omega = 239,040 orientations), origins +-6 px at 0.5 px (625), 20 templates, CTF 300 kV
+/ 2.7 mm / 0.07 with defocus 0.8-3.5 um and astigmatism up to 0.1 um, SNR 0.05.
+Synthetic and seeded: a phantom of Gaussian blobs placed by the 60 icosahedral
+rotations plus a shell (the reference map), projected at random orientations; the
+reference names no public dataset.
 
-A step is one call of the reference-facing search (cryoim_globesearch*, the
-replacement of ort_globesearch.f90) over one batch of particles.  `value` is
-particles/s with the images already resident in HBM; `e2e` is the same call with host
-(pinned) images, host->device copies inside the timed region.  The L2 is flushed
-(256 MiB write) before every timed step.
+A step is one call of cryoim_contract_search_device over one batch of particles:
+particle transforms, CTF and origin ramps, the BF16 contraction against every
+orientation's central section with a fused argmax, top-16 selection, FP64 and
+phase-residual rescoring.  The central sections (operand B) are built once per map and
+reused by every particle of a refinement cycle; each step is charged its pro-rata share
+of that build for a 10,000-particle cycle.  `value` = particles/s with images resident
+in HBM; `e2e` = the same call with pinned host images, host->device copies in the timed
+region.  The L2 is flushed (256 MiB write) before every timed step.  The FP32 form
+(cryoim_globesearch_device, the drop-in replacement of ort_globesearch.f90) is timed
+on the first 16 particles of the same set, and the two forms' chosen orientations are
+compared.
 
---impl reference times the reference algorithm's CPU restatement (the oracle port,
-FP32 in the Fortran's operation order) on all host cores over a bounded sample of
-views of the same workload.
+--impl reference times the reference algorithm's CPU restatement (the oracle port of
+the phase-residual search, FP32 in the Fortran's operation order) on all host cores
+over a bounded sample of views of one particle, extrapolated to the full grid.
 """
 from __future__ import annotations
 
@@ -34,17 +42,24 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
 WORKLOAD = dict(nx=256, apix=1.5, min_res=50.0, max_res=6.0, searchstep=1.0, ntemplates=20,
-                df=(0.8, 3.5), astig=0.1, snr=0.05, origin=6.0, ampwg=0.07, seed=20261205)
-METRIC = "particles/s (box 256), FP32 cross-common-line PR global search, 1-deg ASU grid"
+                df=(0.8, 3.5), astig=0.1, snr=0.05, origin=6.0, origin_step=0.5, topk=16,
+                ampwg=0.07, seed=20261205, cycle_particles=10000)
+METRIC = "particles/s (box 256), BF16+learned vs plain FP32 GPU at >=99% same orientation"
 FP32_PEAK_TFLOPS_NOMINAL = 152 * 128 * 2 * 2.07e9 / 1e12  # FMA lanes x 2 flop x max SM clock
 FLOPS_PER_TERM = 30.0
 
 
 def rank_env():
-    r = int(os.environ.get("RANK", "0"))
-    w = int(os.environ.get("WORLD_SIZE", "1"))
-    lr = int(os.environ.get("LOCAL_RANK", "0"))
-    return r, w, lr
+    return (int(os.environ.get("RANK", "0")), int(os.environ.get("WORLD_SIZE", "1")),
+            int(os.environ.get("LOCAL_RANK", "0")))
+
+
+def measured_peaks():
+    try:
+        d = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
+        return float(d["bf16_tflops_sustained"]), float(d["bf16_tflops"]), float(d["hbm_gbs"]), "measured"
+    except Exception:
+        return 1700.0, 1900.0, 6800.0, "fallback"
 
 
 def make_params(ci):
@@ -54,27 +69,26 @@ def make_params(ci):
                              imgmask=(w["nx"] // 2 - 2) * w["apix"])
 
 
-def make_data(ci, ctx, params, nparticles: int, projector):
+def _as_tmpl(ci, e):
+    t = ci.templates(len(e))
+    t["theta"], t["phi"], t["omega"] = e[:, 0], e[:, 1], e[:, 2]
+    return t
+
+
+def make_data(ci, nparticles: int, projector):
+    """projector(map, template_records) -> images."""
     from cryoim_gb300 import synth
     w = WORKLOAD
     rng = np.random.default_rng(w["seed"])
     vol = synth.phantom(w["nx"], w["seed"])
     te = synth.random_asu_orientations(w["ntemplates"], rng)
-    tmpl = ci.templates(w["ntemplates"])
+    tmpl = _as_tmpl(ci, te)
     tmpl["particle_id"] = np.arange(1, w["ntemplates"] + 1)
-    tmpl["theta"], tmpl["phi"], tmpl["omega"] = te[:, 0], te[:, 1], te[:, 2]
     timgs = projector(vol, tmpl)
     imgs, parts, truth = synth.make_particles(
-        vol, nparticles, w["seed"] + 1,
-        lambda v, e: projector(v, _as_tmpl(ci, e)), w["apix"], df_range=w["df"],
-        astig_max=w["astig"], origin_max=w["origin"], snr=w["snr"], ampwg=w["ampwg"])
-    return tmpl, timgs, imgs, parts, truth
-
-
-def _as_tmpl(ci, e):
-    t = ci.templates(len(e))
-    t["theta"], t["phi"], t["omega"] = e[:, 0], e[:, 1], e[:, 2]
-    return t
+        vol, nparticles, w["seed"] + 1, lambda v, e: projector(v, _as_tmpl(ci, e)), w["apix"],
+        df_range=w["df"], astig_max=w["astig"], origin_max=w["origin"], snr=w["snr"], ampwg=w["ampwg"])
+    return vol, tmpl, timgs, imgs, parts, truth
 
 
 class ClockSampler:
@@ -116,13 +130,13 @@ class ClockSampler:
     def summary(self):
         if not self.rows:
             return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unavailable"]}
-        sm = [float(r[0]) for r in self.rows if r[0].replace(".", "").isdigit()]
-        mx = [float(r[1]) for r in self.rows if r[1].replace(".", "").isdigit()]
+        num = lambda s: s.replace(".", "", 1).isdigit()
+        sm = [float(r[0]) for r in self.rows if num(r[0])]
+        mx = [float(r[1]) for r in self.rows if num(r[1])]
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
         reasons = sorted({names[k] for r in self.rows for k in range(4) if r[3 + k].lower() == "active"})
-        return {"sm_mhz": float(np.median(sm)) if sm else None,
-                "sm_max_mhz": max(mx) if mx else None, "reasons": reasons,
-                "samples": len(self.rows)}
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(self.rows)}
 
 
 def asu_views(step: float):
@@ -147,7 +161,7 @@ def asu_views(step: float):
     return np.array(out, np.float32)
 
 
-def cpu_sample(ci, params, tmpl, timgs, img, part, seconds: float = 15.0):
+def cpu_sample(params, tmpl, timgs, img, part, seconds: float = 15.0):
     """Time the oracle port (FP32) on all host cores over a bounded sample of views of
     one particle; return particles/s extrapolated to the full view set."""
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
@@ -165,8 +179,21 @@ def cpu_sample(ci, params, tmpl, timgs, img, part, seconds: float = 15.0):
     pps = (nv / len(views)) / dt
     return pps, {"cores": nthr, "kind": "port", "views": nv, "views_total": len(views), "seconds": dt,
                  "sample": f"1 particle x {nv}/{len(views)} ASU views (x {len(tmpl)} templates, "
-                           f"Nomega {int(360 / params.searchstep)}), oracle FP32 port, OpenMP over views, "
-                           f"extrapolated to the full grid"}
+                           f"Nomega {int(360 / params.searchstep)}) of the phase-residual search, oracle "
+                           f"FP32 port, OpenMP over views on all host cores, extrapolated to the full grid"}
+
+
+def config_dict(params, batch):
+    w = WORKLOAD
+    return {"workload": "icos global search, box 256, 1-deg ASU grid x 625 origins (10k-particle "
+                        "production configuration shapes)",
+            "box": w["nx"], "apix": w["apix"], "band_A": [w["min_res"], w["max_res"]],
+            "minR": params.min_r, "maxR": params.max_r, "searchstep_deg": w["searchstep"],
+            "origins": f"+-{w['origin']} px @ {w['origin_step']} px", "topk_rescored": w["topk"],
+            "templates": w["ntemplates"], "particles_per_step": batch, "snr": w["snr"],
+            "section_build": f"per map, charged pro rata per particle of a {w['cycle_particles']}-particle cycle",
+            "learned_proposer": "not built: exhaustive contraction over the full grid",
+            "l2": "flushed (256 MiB write) before every timed step"}
 
 
 def run_reference(args):
@@ -176,12 +203,11 @@ def run_reference(args):
     import cryoim_gb300 as ci
     from cryoim_gb300 import synth
     params = make_params(ci)
-    tmpl, timgs, imgs, parts, truth = make_data(ci, None, params, 1, lambda v, t: synth.project_numpy(
-        v, np.stack([t["theta"], t["phi"], t["omega"]], 1)))
-    vals = []
-    info = None
+    proj = lambda v, t: synth.project_fourier(v, np.stack([t["theta"], t["phi"], t["omega"]], 1))
+    vol, tmpl, timgs, imgs, parts, truth = make_data(ci, 1, proj)
+    vals, info = [], None
     for k in range(args.warmup + args.steps):
-        pps, info = cpu_sample(ci, params, tmpl, timgs, imgs[0], parts[0], seconds=args.ref_seconds)
+        pps, info = cpu_sample(params, tmpl, timgs, imgs[0], parts[0], seconds=args.ref_seconds)
         if k >= args.warmup:
             vals.append(pps)
     v = float(np.mean(vals))
@@ -196,51 +222,42 @@ def run_reference(args):
     return 0
 
 
-def config_dict(params, batch):
-    w = WORKLOAD
-    return {"workload": "icos global search, box 256 (10k-particle production config shapes)",
-            "box": w["nx"], "apix": w["apix"], "band_A": [w["min_res"], w["max_res"]],
-            "minR": params.min_r, "maxR": params.max_r, "searchstep_deg": w["searchstep"],
-            "templates": w["ntemplates"], "particles_per_step": batch, "snr": w["snr"],
-            "l2": "flushed (256 MiB write) before every timed step"}
-
-
 def run_ours(args):
     import torch
     import cryoim_gb300 as ci
+    from cryoim_gb300 import synth
     r, world, lr = rank_env()
     dev = lr if torch.cuda.device_count() > 1 else 0
     torch.cuda.set_device(dev)
     if world > 1:
         import torch.distributed as dist
         dist.init_process_group("nccl", device_id=torch.device("cuda", dev))
+    w = WORKLOAD
     params = make_params(ci)
     ctx = ci.Context(dev, params)
     B = args.batch
-    ctx.set_batch(B)
-    proj = lambda v, t: ctx.project_templates(v, t)
-    tmpl, timgs, imgs, parts, truth = make_data(ci, ctx, params, B, proj)
+    npr = min(args.pr_particles, B)
+    vol, tmpl, timgs, imgs, parts, truth = make_data(ci, B, lambda v, t: ctx.project_templates(v, t))
     ctx.load_templates(timgs, tmpl)
+    ctx.set_reference_map(vol)
     stream = torch.cuda.Stream(device=dev)
     ctx.set_stream(stream.cuda_stream)
     d_imgs = torch.from_numpy(imgs).to(f"cuda:{dev}")
     h_imgs = torch.from_numpy(imgs).pin_memory()
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=f"cuda:{dev}")
-    terms = ctx.search_terms()
-    nth, nph, nom, nviews = ctx.search_grid()
+    copts = dict(origin_max=w["origin"], origin_step=w["origin_step"], topk=w["topk"], pick=0)
 
-    def step(dev_ptr=True):
+    def contract_step(dev_ptr=True):
         q = parts.copy()
         with torch.cuda.stream(stream):
             flush.zero_()
-        if dev_ptr:
-            ctx.globesearch(d_imgs.data_ptr(), q)
-        else:
-            ctx.globesearch(h_imgs.numpy(), q)
+        ctx.contract_search(d_imgs.data_ptr() if dev_ptr else h_imgs.numpy(), q, **copts)
         return q
 
+    # ---- BF16 contraction form (headline) ----
     for _ in range(args.warmup):
-        q = step()
+        q = contract_step()
+    st0 = ctx.contract_stats()  # section build time (first call) and reset
     ctx.set_profiling(True)
     torch.cuda.synchronize()
     if world > 1:
@@ -249,54 +266,98 @@ def run_ours(args):
     with ClockSampler(dev) as clk:
         e0.record(stream)
         for _ in range(args.steps):
-            q = step()
+            q = contract_step()
         e1.record(stream)
         torch.cuda.synchronize()
     ms = e0.elapsed_time(e1)
-    kms, klaunch = ctx.kernel_time()
+    gst = ctx.contract_stats()
     ctx.set_profiling(False)
+    slice_share_ms = st0["slice_ms"] * B * args.steps / w["cycle_particles"]
+    ms_eff = ms + slice_share_ms
     if world > 1:
-        t = torch.tensor([ms], device=f"cuda:{dev}")
+        t = torch.tensor([ms_eff], device=f"cuda:{dev}")
         torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        ms = float(t.item())
-    value = world * B * args.steps / (ms / 1000.0)
-    # end to end: host images through the same call
+        ms_eff = float(t.item())
+    value = world * B * args.steps / (ms_eff / 1000.0)
+    q_bf16 = q
+    # end to end through the host-pointer entry point
     torch.cuda.synchronize()
     e2, e3 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     k2 = max(1, args.steps // 2)
     e2.record(stream)
     for _ in range(k2):
-        q = step(dev_ptr=False)
+        contract_step(dev_ptr=False)
     e3.record(stream)
     torch.cuda.synchronize()
-    e2e = world * B * k2 / (e2.elapsed_time(e3) / 1000.0)
-    # accuracy against the generating orientations (informational)
-    from cryoim_gb300 import synth
-    errs = [synth.orientation_error((q["theta"][i], q["phi"][i], q["omega"][i]), truth[i]) for i in range(B)]
+    e2e_ms = e2.elapsed_time(e3) + st0["slice_ms"] * B * k2 / w["cycle_particles"]
+    e2e = world * B * k2 / (e2e_ms / 1000.0)
+
+    # ---- FP32 exhaustive phase-residual form (drop-in) on the first npr particles ----
+    def pr_step():
+        qq = parts[:npr].copy()
+        with torch.cuda.stream(stream):
+            flush.zero_()
+        ctx.globesearch(d_imgs.data_ptr(), qq)
+        return qq
+    pr_step()
+    ctx.set_profiling(True)
+    e4, e5 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e4.record(stream)
+    for _ in range(2):
+        q_pr = pr_step()
+    e5.record(stream)
+    torch.cuda.synchronize()
+    pr_ms = e4.elapsed_time(e5)
+    kms, klaunch = ctx.kernel_time()
+    ctx.set_profiling(False)
+    fp32_pps = world * npr * 2 / (pr_ms / 1000.0)
+    terms = ctx.search_terms()
+
+    # ---- agreement and accuracy ----
+    same = same1 = 0
+    e_b, e_p = [], []
+    for i in range(npr):
+        ob = (q_bf16["theta"][i], q_bf16["phi"][i], q_bf16["omega"][i])
+        op = (q_pr["theta"][i], q_pr["phi"][i], q_pr["omega"][i])
+        same += int(np.allclose(ob, op, atol=1e-3))
+        same1 += int(synth.orientation_error(ob, op) <= 1.5 * w["searchstep"])
+        e_b.append(synth.orientation_error(ob, truth[i]))
+        e_p.append(synth.orientation_error(op, truth[i]))
     if r != 0:
         return 0
-    avg_launch_ms = kms / max(klaunch, 1)
-    achieved = terms * B * FLOPS_PER_TERM / (avg_launch_ms / 1000.0) / 1e12
+    peak_s, peak_b, hbm, src = measured_peaks()
+    gemm_ms = gst["gemm_ms"] / max(gst["gemm_launches"], 1)
+    achieved = gst["gemm_flops"] / max(gst["gemm_ms"], 1e-9) / 1e9  # TFLOP/s
+    pr_avg = kms / max(klaunch, 1)
+    pr_achieved = terms * npr * FLOPS_PER_TERM / (pr_avg / 1000.0) / 1e12
     line = {"metric": METRIC, "value": value, "unit": "particles/s", "n_gpus": world,
-            "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms / args.steps,
-            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_eff / args.steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "bf16",
             "data": "synthetic (seeded phantom, CTF, noise; see bench.py docstring)",
             "config": config_dict(params, B),
-            "e2e": {"value": e2e, "unit": "particles/s", "h2d_bytes_per_step": int(imgs.nbytes + B * 8 * 4),
-                    "d2h_bytes_per_step": int(B * 8)},
-            "gpu_launches": 5 * args.steps,
-            "roofline": {"bound": "fp32", "kernel": "k_pr_omega", "achieved": achieved,
-                         "peak": FP32_PEAK_TFLOPS_NOMINAL, "unit": "TFLOP/s", "frac": achieved / FP32_PEAK_TFLOPS_NOMINAL,
-                         "traffic": None, "terms_per_particle": terms, "flops_per_term": FLOPS_PER_TERM,
-                         "terms_per_s": terms * B / (avg_launch_ms / 1000.0),
-                         "avg_launch_ms": avg_launch_ms, "launches": klaunch,
-                         "peak_source": "nominal FP32 FMA rate at 2.07 GHz (MEASURED_PEAKS.json has no "
-                                        "non-tensor FP32 figure); the kernel is ALU/SFU-bound, not HBM or tensor"},
-            "clocks": clk.summary(),
-            "grid": {"ntheta": nth, "nphi": nph, "nomega": nom, "views": nviews},
-            "orientation_error_deg_median": float(np.median(errs))}
+            "e2e": {"value": e2e, "unit": "particles/s", "h2d_bytes_per_step": int(imgs.nbytes + B * 32),
+                    "d2h_bytes_per_step": int(B * (w["topk"] * 16 + 8))},
+            "gpu_launches": 11 * ((B + 2) // 3) * args.steps,
+            "roofline": {"bound": "tensor", "kernel": "k_gemm_bf16_argmax", "achieved": achieved,
+                         "peak": peak_s, "unit": "TFLOP/s", "frac": achieved / peak_s, "traffic": None,
+                         "peak_source": f"{src} bf16_tflops_sustained (kernel runs inside multi-second steps)",
+                         "flops_per_particle": gst["gemm_flops"] / max(B * args.steps, 1),
+                         "avg_launch_ms": gemm_ms, "launches": gst["gemm_launches"],
+                         "orientations": gst["orientations"], "kpad": gst["kpad"]},
+            "section_build_ms": st0["slice_ms"],
+            "fp32_form": {"value": fp32_pps, "unit": "particles/s", "particles": npr,
+                          "speedup_of_bf16_form": value / fp32_pps,
+                          "roofline": {"bound": "fp32", "kernel": "k_pr_omega", "achieved": pr_achieved,
+                                       "peak": FP32_PEAK_TFLOPS_NOMINAL, "unit": "TFLOP/s",
+                                       "frac": pr_achieved / FP32_PEAK_TFLOPS_NOMINAL,
+                                       "terms_per_particle": terms, "avg_launch_ms": pr_avg,
+                                       "peak_source": "nominal FP32 FMA rate (no measured non-tensor FP32 peak)"}},
+            "agreement": {"identical_orientation": same / npr, "within_1_step": same1 / npr, "particles": npr,
+                          "median_error_vs_truth_deg": {"bf16_form": float(np.median(e_b)),
+                                                        "fp32_form": float(np.median(e_p))}},
+            "clocks": clk.summary()}
     if not args.no_cpu_baseline:
-        pps, info = cpu_sample(ci, params, tmpl, timgs, imgs[0], parts[0], seconds=args.ref_seconds)
+        pps, info = cpu_sample(params, tmpl, timgs, imgs[0], parts[0], seconds=args.ref_seconds)
         line["cpu_baseline"] = {"value": pps, "unit": "particles/s", "cores": info["cores"],
                                 "kind": info["kind"], "sample": info["sample"]}
     print(json.dumps(line))
@@ -309,7 +370,8 @@ def main():
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=4)
     ap.add_argument("--warmup", type=int, default=3)
-    ap.add_argument("--batch", type=int, default=64)
+    ap.add_argument("--batch", type=int, default=48)
+    ap.add_argument("--pr-particles", type=int, default=16)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--ref-seconds", type=float, default=15.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")

@@ -224,6 +224,11 @@ struct Ctx {
     DBuf<float2> kalpha;
     int n_origin = 0;
     float orig_max = -1.0f, orig_step = -1.0f;
+    DBuf<float> tilev, xcand, xpr;
+    DBuf<int> tileo, tileorig;
+    DBuf<float2> xalpha;
+    // view <-> grid slot (itheta * (2 Nphi + 1) + iphi + Nphi) maps for neighbours
+    std::vector<int> view_slot, slot_view;
     int num_sms = 0;
     // CUDA-event timing of the contraction launches (with prof)
     double prof_gemm_ms = 0.0;
@@ -241,6 +246,8 @@ struct Ctx {
         mapcube.release(); csamples.release(); bmat.release(); amat.release(); corigins.release();
         topv.release(); kcc.release(); kcand.release(); kpr.release(); topi.release(); gerr.release();
         kor.release(); korig.release(); pnorm.release(); kcc64.release(); kalpha.release();
+        tilev.release(); xcand.release(); xpr.release(); tileo.release(); tileorig.release();
+        xalpha.release();
         if (pe0) cudaEventDestroy(pe0);
         if (pe1) cudaEventDestroy(pe1);
         if (own_stream && stream) cudaStreamDestroy(stream);
@@ -364,6 +371,14 @@ int ensure_grid(Ctx* c) {
         }
     }
     c->V = (int)(c->views.size() / 4);
+    c->view_slot.assign(c->V, -1);
+    c->slot_view.assign((size_t)(c->nth + 1) * (2 * c->nph + 1), -1);
+    for (int v = 0; v < c->V; ++v) {
+        int base;
+        std::memcpy(&base, &c->views[4 * v + 2], 4);
+        c->view_slot[v] = base / c->nom;
+        c->slot_view[base / c->nom] = v;
+    }
     int r;
     if ((r = c->d_views.ensure(c->views.size() + 4))) return r;
     CK(cudaMemcpyAsync(c->d_views.p, c->views.data(), sizeof(float) * c->views.size(),
@@ -748,6 +763,13 @@ int contract_impl(Ctx* c, const float* imgs, bool on_device, cryoim_particle* pa
         (r = c->kpr.ensure((size_t)pb * k)))
         return r;
     if (T > 0 && (r = c->kalpha.ensure((size_t)pb * k * T * 60))) return r;
+    // rescoring set: each selected orientation and its 26 grid neighbours
+    const int maxx = 27 * k;
+    if ((r = c->tilev.ensure((size_t)pb * ntiles)) || (r = c->tileo.ensure((size_t)pb * ntiles)) ||
+        (r = c->tileorig.ensure((size_t)pb * ntiles)) || (r = c->xcand.ensure((size_t)pb * maxx * 5)) ||
+        (r = c->xpr.ensure((size_t)pb * maxx)))
+        return r;
+    if (T > 0 && (r = c->xalpha.ensure((size_t)pb * maxx * T * 60))) return r;
     if (c->num_sms == 0) CK(cudaDeviceGetAttribute(&c->num_sms, cudaDevAttrMultiProcessorCount, c->device));
     std::vector<int> src(P);
     {
@@ -813,7 +835,8 @@ int contract_impl(Ctx* c, const float* imgs, bool on_device, cryoim_particle* pa
         CK(launch_gemm_bf16_argmax(c->amat.p, c->bmat.p, nb * O, (int)c->n_orient, c->cKpad, g, c->num_sms,
                                    c->stream));
         if (c->prof) CK(cudaEventRecord(g1, c->stream));
-        launch_select_topk(c->topv.p, c->topi.p, O, ntiles, k, nb, c->kor.p, c->korig.p, c->kcc.p, c->stream);
+        launch_select_topk(c->topv.p, c->topi.p, O, ntiles, k, nb, c->tilev.p, c->tileo.p, c->tileorig.p,
+                           c->kor.p, c->korig.p, c->kcc.p, c->stream);
         CK(cudaGetLastError());
         int gerr = 0;
         CK(cudaMemcpyAsync(&gerr, c->gerr.p, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
@@ -844,30 +867,82 @@ int contract_impl(Ctx* c, const float* imgs, bool on_device, cryoim_particle* pa
                            c->stream));
         launch_cc_fp64(c->mapcube.p, c->band.p, ctfp, c->bd, c->csamples.p, c->cS, c->kcand.p, k, nb,
                        c->kcc64.p, c->stream);
+        // Phase-residual rescoring at the particle's own origin (ort_globesearch.f90 scores
+        // every view at particle(i)%x, %y) over each selected orientation and its 26 grid
+        // neighbours; the result equals the exhaustive search wherever its minimum lies there.
+        std::vector<std::vector<int>> xs(nb);
+        int maxc = 1;
+        const int span = 2 * c->nph + 1;
         if (T > 0) {
-            launch_refine_alpha(c->kcand.p, nb, c->tort.p, T, c->ops.p, c->kalpha.p, c->stream, k);
+            for (int i = 0; i < nb; ++i) {
+                std::vector<int>& lst = xs[i];
+                for (int rr = 0; rr < k; ++rr) {
+                    const int n = hor[i * k + rr];
+                    if (n < 0) continue;
+                    const int v = n / c->nom, io = n % c->nom, slot = c->view_slot[v];
+                    const int it = slot / span, ips = slot % span - c->nph;
+                    for (int dt = -1; dt <= 1; ++dt)
+                        for (int dp = -1; dp <= 1; ++dp) {
+                            const int it2 = it + dt, ips2 = ips + dp;
+                            if (it2 < 0 || it2 > c->nth || ips2 < -c->nph || ips2 > c->nph) continue;
+                            const int v2 = c->slot_view[(size_t)it2 * span + ips2 + c->nph];
+                            if (v2 < 0) continue;
+                            for (int dw = -1; dw <= 1; ++dw) {
+                                const int n2 = v2 * c->nom + (io + dw + c->nom) % c->nom;
+                                if (std::find(lst.begin(), lst.end(), n2) == lst.end()) lst.push_back(n2);
+                            }
+                        }
+                }
+                if (lst.empty()) lst.push_back(0);
+                maxc = std::max(maxc, (int)lst.size());
+            }
+            std::vector<float> hx((size_t)nb * maxc * 5);
+            for (int i = 0; i < nb; ++i)
+                for (int j = 0; j < maxc; ++j) {
+                    const int n = xs[i][std::min<size_t>(j, xs[i].size() - 1)];
+                    float* o = &hx[((size_t)i * maxc + j) * 5];
+                    o[0] = c->views[4 * (n / c->nom)];
+                    o[1] = c->views[4 * (n / c->nom) + 1];
+                    o[2] = c->p.searchstep * (float)(n % c->nom);
+                    o[3] = parts[b0 + i].x;
+                    o[4] = parts[b0 + i].y;
+                }
+            CK(cudaMemcpyAsync(c->xcand.p, hx.data(), sizeof(float) * hx.size(), cudaMemcpyHostToDevice,
+                               c->stream));
+            launch_refine_alpha(c->xcand.p, nb, c->tort.p, T, c->ops.p, c->xalpha.p, c->stream, maxc);
             PrSingleArgs a{};
             a.band = c->band.p; a.fcut0 = c->fcut0.p; a.tband = c->tband.p; a.tfcut = tfc;
-            a.tfcut_pstride = tfs; a.ctf = ctfp; a.cand = c->kcand.p; a.alpha = c->kalpha.p; a.T = T;
-            a.bd = c->bd; a.pr = c->kpr.p; a.ncand = k;
+            a.tfcut_pstride = tfs; a.ctf = ctfp; a.cand = c->xcand.p; a.alpha = c->xalpha.p; a.T = T;
+            a.bd = c->bd; a.pr = c->xpr.p; a.ncand = maxc;
             CK(launch_pr_single(a, nb, c->stream));
-            CK(cudaMemcpyAsync(hpr.data(), c->kpr.p, sizeof(float) * nb * k, cudaMemcpyDeviceToHost, c->stream));
+            hpr.resize((size_t)nb * maxc);
+            CK(cudaMemcpyAsync(hpr.data(), c->xpr.p, sizeof(float) * nb * maxc, cudaMemcpyDeviceToHost,
+                               c->stream));
         }
         CK(cudaMemcpyAsync(hcc64.data(), c->kcc64.p, sizeof(double) * nb * k, cudaMemcpyDeviceToHost,
                            c->stream));
         CK(cudaStreamSynchronize(c->stream));
         for (int i = 0; i < nb; ++i) {
-            int best = 0;
-            for (int j = 1; j < k; ++j) {
-                const int a = i * k + j, bsel = i * k + best;
-                if (opts->pick == 0 ? (hpr[a] < hpr[bsel]) : (hcc64[a] > hcc64[bsel])) best = j;
-            }
-            const int sidx = i * k + best;
             cryoim_particle& q = parts[b0 + i];
             q.theta0 = q.theta; q.phi0 = q.phi; q.omega0 = q.omega; q.x0 = q.x; q.y0 = q.y; q.pr0 = q.pr;
-            q.theta = hcand[5 * sidx]; q.phi = hcand[5 * sidx + 1]; q.omega = hcand[5 * sidx + 2];
-            q.x = hcand[5 * sidx + 3]; q.y = hcand[5 * sidx + 4];
-            q.pr = T > 0 ? hpr[sidx] : (float)hcc64[sidx];
+            if (opts->pick == 0) {
+                int best = 0;
+                for (int j = 1; j < (int)xs[i].size(); ++j)
+                    if (hpr[(size_t)i * maxc + j] < hpr[(size_t)i * maxc + best]) best = j;
+                const int n = xs[i][best];
+                q.theta = c->views[4 * (n / c->nom)];
+                q.phi = c->views[4 * (n / c->nom) + 1];
+                q.omega = c->p.searchstep * (float)(n % c->nom);
+                q.pr = hpr[(size_t)i * maxc + best];
+            } else {
+                int best = 0;
+                for (int j = 1; j < k; ++j)
+                    if (hcc64[i * k + j] > hcc64[i * k + best]) best = j;
+                const int sidx = i * k + best;
+                q.theta = hcand[5 * sidx]; q.phi = hcand[5 * sidx + 1]; q.omega = hcand[5 * sidx + 2];
+                q.x = hcand[5 * sidx + 3]; q.y = hcand[5 * sidx + 4];
+                q.pr = (float)hcc64[sidx];
+            }
             q.dtheta = q.theta - q.theta0; q.dphi = q.phi - q.phi0; q.domega = q.omega - q.omega0;
             q.dx = q.x - q.x0; q.dy = q.y - q.y0; q.dpr = q.pr - q.pr0;
             if (cands)
@@ -877,7 +952,10 @@ int contract_impl(Ctx* c, const float* imgs, bool on_device, cryoim_particle* pa
                     for (int e = 0; e < 5; ++e) o[e] = hcand[5 * a + e];
                     o[5] = hcc[a];
                     o[6] = (float)hcc64[a];
-                    o[7] = T > 0 ? hpr[a] : 0.0f;
+                    o[7] = 0.0f;
+                    if (T > 0)
+                        for (size_t m = 0; m < xs[i].size(); ++m)
+                            if (xs[i][m] == hor[a]) { o[7] = hpr[(size_t)i * maxc + m]; break; }
                 }
         }
     }

@@ -165,15 +165,49 @@ __global__ void __launch_bounds__(256) k_build_a(const float2* __restrict__ band
     }
 }
 
-// Per particle: the k best (row, tile) maxima over its O origin rows, by repeated
-// block argmax (selected entries are set to -inf in topv, a scratch array).
-__global__ void k_select_topk(float* __restrict__ topv, const int* __restrict__ topi, int O, int ntiles,
-                              int k, int* __restrict__ out_orient, int* __restrict__ out_origin,
+// Per (particle, column tile): the best of its O origin rows -> (cc, orientation,
+// origin).  Distinct tiles hold distinct orientations.
+__global__ void k_tile_best(const float* __restrict__ topv, const int* __restrict__ topi, int O,
+                            int ntiles, float* __restrict__ bv_out, int* __restrict__ bo_out,
+                            int* __restrict__ borig_out) {
+    __shared__ float sv[32];
+    __shared__ int si[32];
+    const int t = blockIdx.x, p = blockIdx.y;
+    float bv = -3.0e38f;
+    int bi = -1;
+    for (int o = threadIdx.x; o < O; o += blockDim.x) {
+        const float v = topv[((long)p * O + o) * ntiles + t];
+        if (v > bv) { bv = v; bi = o; }
+    }
+    for (int off = 16; off > 0; off >>= 1) {
+        float ov = __shfl_xor_sync(0xffffffffu, bv, off);
+        int oi = __shfl_xor_sync(0xffffffffu, bi, off);
+        if (ov > bv || (ov == bv && oi >= 0 && oi < bi)) { bv = ov; bi = oi; }
+    }
+    const int w = threadIdx.x >> 5, l = threadIdx.x & 31, nw = blockDim.x >> 5;
+    if (l == 0) { sv[w] = bv; si[w] = bi; }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        for (int q = 1; q < nw; ++q)
+            if (sv[q] > sv[0] || (sv[q] == sv[0] && si[q] >= 0 && si[q] < si[0])) { sv[0] = sv[q]; si[0] = si[q]; }
+        const long o = (long)p * ntiles + t;
+        bv_out[o] = sv[0];
+        borig_out[o] = si[0] < 0 ? 0 : si[0];
+        bo_out[o] = si[0] < 0 ? -1 : topi[((long)p * O + si[0]) * ntiles + t];
+    }
+}
+
+// Per particle: the k best entries of cnt (value, orientation, origin) triples, by
+// repeated block argmax (selected values are set to -inf in v, a scratch array).
+__global__ void k_select_topk(float* __restrict__ v, const int* __restrict__ orient,
+                              const int* __restrict__ origin, int cnt_per_particle, int k,
+                              int* __restrict__ out_orient, int* __restrict__ out_origin,
                               float* __restrict__ out_cc) {
     __shared__ float sv[32];
     __shared__ long si[32];
     const int p = blockIdx.x;
-    const long base = (long)p * O * ntiles, cnt = (long)O * ntiles;
+    const long base = (long)p * cnt_per_particle, cnt = cnt_per_particle;
+    float* topv = v;
     for (int r = 0; r < k; ++r) {
         float bv = -3.0e38f;
         long bi = -1;
@@ -194,9 +228,9 @@ __global__ void k_select_topk(float* __restrict__ topv, const int* __restrict__ 
             long i0 = si[0];
             for (int q = 1; q < nw; ++q)
                 if (sv[q] > v0 || (sv[q] == v0 && si[q] < i0 && si[q] >= 0)) { v0 = sv[q]; i0 = si[q]; }
-            if (i0 >= 0) {
-                out_orient[p * k + r] = topi[base + i0];
-                out_origin[p * k + r] = (int)(i0 / ntiles);
+            if (i0 >= 0 && v0 > -3.0e38f) {
+                out_orient[p * k + r] = orient[base + i0];
+                out_origin[p * k + r] = origin[base + i0];
                 out_cc[p * k + r] = v0;
                 topv[base + i0] = -3.0e38f;
             } else {
@@ -306,9 +340,12 @@ void launch_build_a(const float2* band, const float* ctf, Band bd, const int2* s
                                  (__nv_bfloat162*)A);
 }
 
-void launch_select_topk(float* topv, const int* topi, int O, int ntiles, int k, int B, int* orient,
-                        int* origin, float* cc, cudaStream_t st) {
-    k_select_topk<<<B, 512, 0, st>>>(topv, topi, O, ntiles, k, orient, origin, cc);
+void launch_select_topk(const float* topv, const int* topi, int O, int ntiles, int k, int B,
+                        float* tile_v, int* tile_o, int* tile_orig, int* orient, int* origin, float* cc,
+                        cudaStream_t st) {
+    dim3 g(ntiles, B);
+    k_tile_best<<<g, 256, 0, st>>>(topv, topi, O, ntiles, tile_v, tile_o, tile_orig);
+    k_select_topk<<<B, 512, 0, st>>>(tile_v, tile_o, tile_orig, ntiles, k, orient, origin, cc);
 }
 
 void launch_cc_fp64(const float2* cube, const float2* band, const float* ctf, Band bd, const int2* samples,

@@ -144,8 +144,11 @@ void launch_particle_norm(const float2* band, const float* ctf, Band bd, const i
 // Rows (p, o) of A, p < B, o < O; origins: O x 2 (x, y) pixels.
 void launch_build_a(const float2* band, const float* ctf, Band bd, const int2* samples, int S, int Kpad,
                     const float* origins, int O, const double* norm, int B, void* A, cudaStream_t st);
-void launch_select_topk(float* topv, const int* topi, int O, int ntiles, int k, int B, int* orient,
-                        int* origin, float* cc, cudaStream_t st);
+// Best origin per (particle, tile) (tile_*: B x ntiles scratch), then the k best tiles
+// per particle: distinct orientations with their best origin and CC.
+void launch_select_topk(const float* topv, const int* topi, int O, int ntiles, int k, int B,
+                        float* tile_v, int* tile_o, int* tile_orig, int* orient, int* origin, float* cc,
+                        cudaStream_t st);
 // cand: B x k x (theta, phi, omega, x, y); out: B x k FP64 cross-correlations
 void launch_cc_fp64(const float2* cube, const float2* band, const float* ctf, Band bd, const int2* samples,
                     int S, const float* cand, int k, int B, double* out, cudaStream_t st);

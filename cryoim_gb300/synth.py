@@ -139,6 +139,26 @@ def project_numpy(map3d: np.ndarray, eulers: np.ndarray) -> np.ndarray:
     return out
 
 
+def project_fourier(map3d: np.ndarray, eulers: np.ndarray) -> np.ndarray:
+    """Projections by the projection-slice theorem (one 3D FFT, trilinear central
+    sections, 2D inverse FFTs): same geometry as project_numpy, for large boxes where
+    only the inputs' statistics matter (CPU-side input generation)."""
+    from scipy.ndimage import map_coordinates
+    n = map3d.shape[-1]
+    h = n // 2
+    F = np.fft.fftshift(np.fft.fftn(np.fft.ifftshift(map3d.astype(np.float32)))).astype(np.complex64)
+    iy, ix = np.meshgrid(np.arange(n) - h, np.arange(n) - h, indexing="ij")
+    pts = np.stack([ix.ravel(), iy.ravel(), np.zeros(n * n)]).astype(np.float64)
+    out = np.empty((len(eulers), n, n), np.float32)
+    for k, e in enumerate(np.asarray(eulers, np.float64)):
+        x = euler_mat(*e) @ pts + h
+        coords = np.stack([x[2], x[1], x[0]])
+        s = (map_coordinates(F.real, coords, order=1, mode="constant") +
+             1j * map_coordinates(F.imag, coords, order=1, mode="constant")).reshape(n, n)
+        out[k] = np.fft.fftshift(np.fft.ifft2(np.fft.ifftshift(s))).real
+    return out
+
+
 def ctf2d(n, df1, df2, astig, apix, vol=300.0, cs=2.7, ampwg=0.1) -> np.ndarray:
     """getCTF2d.f90 in FP64 on the centred grid (defocus um, Cs mm)."""
     lam = 0.387818 / np.sqrt(vol * (1 + 0.978459e-3 * vol))

@@ -236,9 +236,13 @@ int cryoim_central_sections(void* ctx, const float* ft_re, const float* ft_im,
 /* No counterpart in the reference, which scores by phase residual only.  A second
  * search beside cryoim_globesearch: the cross-correlation of every (particle, origin)
  * with every grid orientation's central section, run as one dense BF16 contraction on
- * the tensor cores (FP32 accumulation), its top-k candidates per particle rescored in
- * FP64 and with the reference's phase residual (cal_crosslin_PR.f90), the particle
- * updated with the best by PR (pick = 0) or by FP64 cross-correlation (pick = 1). */
+ * the tensor cores (FP32 accumulation); per particle the best origin of every block of
+ * 256 orientations is kept and the top-k of those (distinct orientations) are rescored
+ * in FP64.  pick = 0 (drop-in for mode 4): each candidate orientation and its 26 grid
+ * neighbours are scored with the reference's phase residual (cal_crosslin_PR.f90) at
+ * the particle's own origin, as ort_globesearch.f90 scores every view, and the minimum
+ * is taken; the origin is left unchanged.  pick = 1: the candidate with the largest FP64
+ * cross-correlation, orientation and origin. */
 typedef struct cryoim_contract_opts {
     float origin_max;   /* origins searched on [-origin_max, origin_max]^2 pixels   */
     float origin_step;  /* origin grid step, pixels                                 */
@@ -248,7 +252,8 @@ typedef struct cryoim_contract_opts {
 /* The 3D map (nx^3 float32) whose central sections are correlated: its centred Fourier
  * transform is kept as a band cube of (2 maxR + 3)^3 complex values. */
 int cryoim_set_reference_map(void* ctx, const float* map3d);
-/* cands (optional): P x topk x 8 floats (theta, phi, omega, x, y, CC bf16, CC fp64, PR). */
+/* cands (optional): P x topk x 8 floats: theta, phi, omega, x, y (the candidate's best
+ * origin), CC from the BF16 contraction, CC in FP64, PR at the particle's origin. */
 int cryoim_contract_search(void* ctx, const float* imgs, cryoim_particle* parts, int32_t P,
                            const cryoim_contract_opts* opts, float* cands);
 int cryoim_contract_search_device(void* ctx, const float* d_imgs, cryoim_particle* parts, int32_t P,

@@ -85,11 +85,30 @@ def test_pr_rescoring_matches_oracle(run, orc):
                         p.vol, p.cs, p.ampwg, "f64")
         for j in range(cands.shape[1]):
             c = cands[i, j]
-            want = orc.pr_single(a, b, f, tm, tort, tf, ctf, p.min_r, p.max_r, *c[:5], fp="f64")
+            # scored at the particle's own origin, as ort_globesearch does
+            want = orc.pr_single(a, b, f, tm, tort, tf, ctf, p.min_r, p.max_r, *c[:3],
+                                 parts["x"][i], parts["y"][i], fp="f64")
             assert abs(c[7] - want) / want < 5e-3
-        best = int(np.argmin(cands[i, :, 7]))
-        assert q["pr"][i] == cands[i, best, 7]
-        assert q["theta"][i] == cands[i, best, 0] and q["x"][i] == cands[i, best, 3]
+        # the pick is the minimum over the candidates and their grid neighbours
+        assert q["pr"][i] <= cands[i, :, 7].min() + 1e-6
+        want = orc.pr_single(a, b, f, tm, tort, tf, ctf, p.min_r, p.max_r, q["theta"][i], q["phi"][i],
+                             q["omega"][i], parts["x"][i], parts["y"][i], fp="f64")
+        assert abs(q["pr"][i] - want) / want < 5e-3
+        assert q["x"][i] == parts["x"][i] and q["y"][i] == parts["y"][i]
+
+
+def test_pick_matches_exhaustive_pr_search(run, built):
+    """On noise-free particles the exhaustive FP32 search's minimum lies next to a
+    contraction candidate, so the two forms return the same grid orientation."""
+    import cryoim_gb300 as ci
+    (p, vol, tmpl, timgs, imgs, parts, truth), q, cands, stats = run
+    with ci.Context(0, p) as ctx:
+        ctx.load_templates(timgs, tmpl)
+        qe = parts.copy()
+        ctx.globesearch(imgs, qe)
+    for i in range(len(parts)):
+        assert (q["theta"][i], q["phi"][i], q["omega"][i]) == (qe["theta"][i], qe["phi"][i], qe["omega"][i])
+        assert abs(q["pr"][i] - qe["pr"][i]) / qe["pr"][i] < 1e-3
 
 
 def test_noise_free_particles_find_their_orientation(run):
