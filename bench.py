@@ -47,6 +47,10 @@ WORKLOAD = dict(nx=256, apix=1.5, min_res=50.0, max_res=6.0, searchstep=1.0, nte
 METRIC = "particles/s (box 256), BF16+learned vs plain FP32 GPU at >=99% same orientation"
 FP32_PEAK_TFLOPS_NOMINAL = 152 * 128 * 2 * 2.07e9 / 1e12  # FMA lanes x 2 flop x max SM clock
 FLOPS_PER_TERM = 30.0
+# DRAM bytes (read + write) of one GEMM launch (3 particles x 625 origins) from an ncu
+# capture at the 2-degree grid (1.483 GB for 31,320 orientations), scaled to the
+# orientation count: operand B streams once per launch.
+GEMM_TRAFFIC_PER_ORIENT = 1.483e9 / 31320
 
 
 def rank_env():
@@ -339,7 +343,11 @@ def run_ours(args):
                     "d2h_bytes_per_step": int(B * (w["topk"] * 16 + 8))},
             "gpu_launches": 11 * ((B + 2) // 3) * args.steps,
             "roofline": {"bound": "tensor", "kernel": "k_gemm_bf16_argmax", "achieved": achieved,
-                         "peak": peak_s, "unit": "TFLOP/s", "frac": achieved / peak_s, "traffic": None,
+                         "peak": peak_s, "unit": "TFLOP/s", "frac": achieved / peak_s,
+                         "traffic": GEMM_TRAFFIC_PER_ORIENT * gst["orientations"],
+                         "traffic_note": "bytes per launch, ncu capture at the 2-degree grid scaled by "
+                                         "orientations; algorithmic bytes per launch (A + B once): "
+                                         f"{2.0 * gst['kpad'] * (gst['orientations'] + 1875):.4g}",
                          "peak_source": f"{src} bf16_tflops_sustained (kernel runs inside multi-second steps)",
                          "flops_per_particle": gst["gemm_flops"] / max(B * args.steps, 1),
                          "avg_launch_ms": gemm_ms, "launches": gst["gemm_launches"],
@@ -370,12 +378,20 @@ def main():
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=4)
     ap.add_argument("--warmup", type=int, default=3)
-    ap.add_argument("--batch", type=int, default=48)
-    ap.add_argument("--pr-particles", type=int, default=16)
+    ap.add_argument("--batch", type=int, default=64)
+    ap.add_argument("--pr-particles", type=int, default=64)
+    ap.add_argument("--searchstep", type=float, default=None,
+                    help="override the 1-degree grid (small cases for profiler captures only)")
+    ap.add_argument("--origin-step", type=float, default=None,
+                    help="override the 0.5 px origin step (small cases for profiler captures only)")
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--ref-seconds", type=float, default=15.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     args = ap.parse_args()
+    if args.searchstep:
+        WORKLOAD["searchstep"] = args.searchstep
+    if args.origin_step:
+        WORKLOAD["origin_step"] = args.origin_step
     if args.impl == "reference":
         return run_reference(args)
     return run_ours(args)
