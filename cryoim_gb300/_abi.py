@@ -85,6 +85,17 @@ SIGNATURES = {
     "cryoim_contract_search": [_vp, _vp, _vp, _i32, _op, _vp],
     "cryoim_contract_search_device": [_vp, _vp, _vp, _i32, _op, _vp],
     "cryoim_contract_stats": [_vp, _vp],
+    "cryoim_rec_add_partial": [_vp, _vp, _vp, _vp],
+    "cryoim_mrc_read_header": [C.c_char_p, _vp],
+    "cryoim_mrc_read_sections": [C.c_char_p, _i32, _i32, _vp],
+    "cryoim_map_header": [_vp, _i32, _i32, _i32, _f32],
+    "cryoim_mrc_write": [C.c_char_p, _vp, _vp, C.c_int64],
+    "cryoim_ort_count": [C.c_char_p, _ip],
+    "cryoim_ort_read": [C.c_char_p, _i32, _i32, _vp, _vp, _i32],
+    "cryoim_ort_write": [C.c_char_p, _vp, _vp, _i32, _i32, _i32, _i32],
+    "cryoim_template_ort_read": [C.c_char_p, _vp, _i32, _ip],
+    "cryoim_tnf_write": [C.c_char_p, _i32, _i32, _f32, _f32, _i32, _i32, _vp, _vp, _vp],
+    "cryoim_tnf_read": [C.c_char_p, _vp, _vp, _vp, _vp, _vp],
     "cryoim_rec_begin": [_vp],
     "cryoim_rec_insert": [_vp, _vp, _vp, _i32, _ip],
     "cryoim_rec_insert_device": [_vp, _vp, _vp, _i32, _ip],

@@ -58,13 +58,45 @@ def build_library(verbose: bool = False, extra: list[str] | None = None) -> str:
         obj = os.path.join(OUT, src.replace(".cu", ".o"))
         objs.append(obj)
         cmds.append([nvcc(), "-c", os.path.join(CSRC, src), "-o", obj] + common + flags)
+    for src in HOST_UNITS:
+        obj = os.path.join(OUT, src.replace(".cpp", ".o"))
+        objs.append(obj)
+        cmds.append([cxx(), "-c", os.path.join(CSRC, src), "-o", obj, "-O2", "-std=c++17", "-fPIC",
+                     "-ffp-contract=off", "-Wall", "-I", os.path.join(ROOT, "include")])
     with ThreadPoolExecutor(max_workers=len(cmds)) as ex:
         list(ex.map(_run, cmds))
     lib = os.path.join(OUT, LIBNAME)
     _run([nvcc(), "-shared", "-o", lib] + objs + ARCH + ["-lcufft", "-lcudart"])
     if verbose:
         print("built", lib)
+    build_tools(lib)
     return lib
+
+
+HOST_UNITS = ["io.cpp"]
+TOOLS = {"icosprocess": "icosprocess.cpp", "proc_icos": "proc_icos.cpp",
+         "merge_icosprocess_subrec": "merge_subrec.cpp"}
+BIN = os.path.join(HERE, "bin")
+
+
+def cxx() -> str:
+    return os.environ.get("CXX") or shutil.which("g++") or "g++"
+
+
+def build_tools(lib: str) -> None:
+    """The drop-in executables (C++ hosts over the C ABI), rpath to the in-tree library."""
+    os.makedirs(BIN, exist_ok=True)
+    cuda_inc = os.path.join(os.path.dirname(os.path.dirname(nvcc())), "include")
+    cmds = []
+    for name, src in TOOLS.items():
+        path = os.path.join(CSRC, "host", src)
+        if not os.path.exists(path):
+            continue
+        cmds.append([cxx(), "-O2", "-std=c++17", "-ffp-contract=off", "-Wall", path, "-o",
+                     os.path.join(BIN, name), "-I", os.path.join(ROOT, "include"), "-I", cuda_inc,
+                     "-L", OUT, "-lcryoim_gb300", "-Wl,-rpath,$ORIGIN/../_lib"])
+    with ThreadPoolExecutor(max_workers=max(1, len(cmds))) as ex:
+        list(ex.map(_run, cmds))
 
 
 def build_oracle() -> str:

@@ -1454,6 +1454,32 @@ int cryoim_rec_get_partial(void* ctx, float* fa, float* fb, float* wg) {
     return CRYOIM_OK;
 }
 
+int cryoim_rec_add_partial(void* ctx, const float* fa, const float* fb, const float* wg) {
+    Ctx* c = as_ctx(ctx);
+    int r = check_ready(c, false);
+    if (r) return r;
+    if (!c->rec_active) return fail(CRYOIM_ERR_STATE, "cryoim_rec_begin has not been called");
+    if (!fa || !fb || !wg) return fail(CRYOIM_ERR_ARG, "null input");
+    const Band& bd = c->bd;
+    const int R = bd.max_r, t = 2 * R + 1;
+    const long nacc = (long)bd.AW * bd.AW * (R + 2);
+    std::vector<float4> h(nacc);
+    CK(cudaMemcpyAsync(h.data(), c->acc.p, sizeof(float4) * nacc, cudaMemcpyDeviceToHost, c->stream));
+    CK(cudaStreamSynchronize(c->stream));
+    for (int z = 0; z <= R; ++z)
+        for (int y = 0; y < t; ++y)
+            for (int x = 0; x < t; ++x) {
+                const long i = ((long)z * t + y) * t + x;
+                float4& v = h[acc_cell(bd, x - R, y - R, z)];
+                v.x += fa[i];
+                v.y += fb[i];
+                v.z += wg[i];
+            }
+    CK(cudaMemcpyAsync(c->acc.p, h.data(), sizeof(float4) * nacc, cudaMemcpyHostToDevice, c->stream));
+    CK(cudaStreamSynchronize(c->stream));
+    return CRYOIM_OK;
+}
+
 int cryoim_central_sections(void* ctx, const float* ft_re, const float* ft_im, const float* eulers,
                             int32_t n, float* out_re, float* out_im) {
     Ctx* c = as_ctx(ctx);

@@ -223,6 +223,51 @@ int cryoim_rec_finish(void* ctx, float* map);
  * fa, fb, wg each (2*maxR+1)^2*(maxR+1) floats (x fastest, then y, then z >= 0). */
 int cryoim_rec_get_partial(void* ctx, float* fa, float* fb, float* wg);
 
+/* Add a tnf partial (the layout above) into the running accumulator: the summation of
+ * merge_icosprocess_subrec/SRC/merge_reconstruct.f90:20-34.  With subrec off, a
+ * rec_begin, one add per partial and rec_finish give the merged map. */
+int cryoim_rec_add_partial(void* ctx, const float* fa, const float* fb, const float* wg);
+
+/* ---- files (host only; byte-compatible with the reference) ---------------- */
+
+/* The `mrchead` type of icosprocess/SRC/0common_icosproc.f90:61-112: 1024 bytes. */
+typedef struct cryoim_mrc_header {
+    int32_t nx, ny, nz, mode, nxstart, nystart, nzstart, mx, my, mz;
+    float a, b, c, alpha, beta, gamma;
+    int32_t mapc, mapr, maps;
+    float amin, amax, amean;
+    int32_t ispg, nsymbt, extra[25];
+    float xorigin, yorigin, zorigin;
+    char map[4], machinestamp[4];
+    float arms;
+    int32_t nlabl;
+    char label[800];
+} cryoim_mrc_header;
+int cryoim_mrc_read_header(const char* path, cryoim_mrc_header* h);
+/* count images (sections) starting at the 1-based index first, float32 (mode 2) only */
+int cryoim_mrc_read_sections(const char* path, int32_t first, int32_t count, float* out);
+/* mrchead.f90:2-58 (maphead) for an nx x ny x nz float map */
+int cryoim_map_header(cryoim_mrc_header* h, int32_t nx, int32_t ny, int32_t nz, float apix);
+int cryoim_mrc_write(const char* path, const cryoim_mrc_header* h, const float* data, int64_t n);
+/* non-blank rows of an orientation file */
+int cryoim_ort_count(const char* path, int32_t* n);
+/* rows first..last (1-based) of a 13-column orientation file (load_original_ortcent.f90);
+ * stck (optional): (last-first+1) x stck_len bytes of stack names */
+int cryoim_ort_read(const char* path, int32_t first, int32_t last, cryoim_particle* parts,
+                    char* stck, int32_t stck_len);
+/* name_width 54: the 19-column row of format 900 (ort_globesearch.f90:139);
+ * name_width 64: proc_icos's 13-column row (transform_ort_2fTo5f.f90:36) */
+int cryoim_ort_write(const char* path, const cryoim_particle* parts, const char* stck,
+                     int32_t stck_len, int32_t n, int32_t name_width, int32_t append);
+/* template orientation rows `id theta phi omega x y` (load_template.f90:18-21); *n = rows */
+int cryoim_template_ort_read(const char* path, cryoim_template* t, int32_t maxn, int32_t* n);
+/* tnf partial (reconstruct_substep.f90:152-155) */
+int cryoim_tnf_write(const char* path, int32_t fftsize, int32_t max_r, float apix, float imgmask,
+                     int32_t flag_fsc, int32_t flag_avg, const float* fa, const float* fb,
+                     const float* wg);
+/* ihdr[4] = fftsize, max_r, flag_fsc, flag_avg; fhdr[2] = apix, imgmask; arrays optional */
+int cryoim_tnf_read(const char* path, int32_t* ihdr, float* fhdr, float* fa, float* fb, float* wg);
+
 /* ---- central sections (projection-matching form, spec step a/b) ------ */
 
 /* Trilinear central sections of a 3D Fourier map: replaces
