@@ -62,12 +62,33 @@ __device__ __forceinline__ void tmpl_sample(const float2* __restrict__ tb, const
     *im = bilerp(ax, ay, t00.y, t10.y, t01.y, t11.y);
 }
 
+// Angle between two complex numbers z1, z2 from their cross and dot products, in [0, pi]:
+// |arg(z2 conj z1)| = the reference's |phase2 - phase1| folded into [0, pi]
+// (cal_crosslin_PR_omega.f90:53-60).  atan on [0, 1] is a 6-term odd polynomial fitted
+// to atan(t)/t by reweighted least squares on [0, 1] (max error 1.7e-6 rad in FP32).
+__device__ __forceinline__ float angle_between(float cross, float dot, float pi) {
+    const float a = fabsf(cross), b = fabsf(dot);
+    const float mx = fmaxf(a, b), mn = fminf(a, b);
+    const float t = mn * __frcp_rn(mx);
+    const float s = t * t;
+    float p = fmaf(s, -0.011719364672899246f, 0.05264794081449509f);
+    p = fmaf(p, s, -0.11642702668905258f);
+    p = fmaf(p, s, 0.19354058802127838f);
+    p = fmaf(p, s, -0.33262285590171814f);
+    p = fmaf(p, s, 0.9999772310256958f);
+    float r = t * p;
+    r = (a > b) ? 0.5f * pi - r : r;
+    return (dot < 0.0f) ? pi - r : r;
+}
+
 __global__ void __launch_bounds__(768, 1) k_pr_omega(PrOmegaArgs a, int nomp, Consts K) {
     extern __shared__ __align__(16) unsigned char smraw[];
     const Band bd = a.bd;
     const int W = bd.W, nr = bd.nr, minR = bd.min_r;
     float2* sband = reinterpret_cast<float2*>(smraw);
-    float2* sline = sband + W * W;
+    // per (line, radius): template sample (a2, b2), half amplitude (-1 below its cut),
+    // particle cut at that radius
+    float4* sline = reinterpret_cast<float4*>(sband + W * W);
     float* sfc0 = reinterpret_cast<float*>(sline + 60 * nr);
     float* salpha = sfc0 + ((nr + 3) & ~3);
     float* sred = salpha + 64;
@@ -102,14 +123,14 @@ __global__ void __launch_bounds__(768, 1) k_pr_omega(PrOmegaArgs a, int nomp, Co
             for (int q = t; q < 60 * nr; q += blockDim.x) {
                 int j = q / nr, iq = q - j * nr;
                 float2 aa = al[j];
-                float amp2 = -1.0f, ph2 = 0.0f;
+                float4 e = make_float4(0.f, 0.f, -1.0f, sfc0[iq]);
                 if (aa.x < 999.0f && aa.y < 999.0f) {
                     float re, im;
                     tmpl_sample(tb, ctfp, W, offW, nxh, aa.y, (float)(minR + iq), K.d2r, &re, &im);
                     float amp = sqrtf(re * re + im * im);
-                    if (amp >= fct[iq]) { amp2 = amp; ph2 = atan2f(im, re); }
+                    if (amp >= fct[iq]) { e.x = re; e.y = im; e.z = 0.5f * amp; }
                 }
-                sline[q] = make_float2(amp2, ph2);
+                sline[q] = e;
             }
             __syncthreads();
             if (k < a.nomega) {
@@ -119,34 +140,40 @@ __global__ void __launch_bounds__(768, 1) k_pr_omega(PrOmegaArgs a, int nomp, Co
                     const float ang = __fmul_rn(__fsub_rn(al1, womega), K.d2r);
                     float sn, cs;
                     sincosf(ang, &sn, &cs);
-                    const float2* sl = sline + j * nr;
-                    float l1 = 0.f, l2 = 0.f;
+                    const float2 csn = make_float2(cs, sn), half2c = make_float2(nxh, nxh);
+                    const float4* sl = sline + j * nr;
+                    float2 acc = make_float2(0.f, 0.f);  // (sum diff*w, sum w) of this line
 #pragma unroll 2
                     for (int iq = 0; iq < nr; ++iq) {
-                        const float2 tl = sl[iq];
-                        if (tl.x < 0.0f) continue;
+                        const float4 e = sl[iq];
+                        if (e.z < 0.0f) continue;
                         const float fr = (float)(minR + iq);
-                        const float x = __fadd_rn(__fmul_rn(fr, cs), nxh);
-                        const float y = __fadd_rn(__fmul_rn(fr, sn), nxh);
-                        const int lx = (int)x, ly = (int)y;
-                        const float ax = x - (float)lx, ay = y - (float)ly;
+                        // sample position (x, y) = FR (cos, sin) + nx/2, then its cell
+                        const float2 xy = __ffma2_rn(make_float2(fr, fr), csn, half2c);
+                        const int lx = (int)xy.x, ly = (int)xy.y;
+                        const float2 f = __fadd2_rn(xy, make_float2(-(float)lx, -(float)ly));
                         const int b0 = ly * W + lx - offW;
                         const float2 t00 = sband[b0], t10 = sband[b0 + 1];
                         const float2 t01 = sband[b0 + W], t11 = sband[b0 + W + 1];
-                        const float re = bilerp(ax, ay, t00.x, t10.x, t01.x, t11.x);
-                        const float im = bilerp(ax, ay, t00.y, t10.y, t01.y, t11.y);
-                        const float amp1 = sqrtf(re * re + im * im);
-                        if (amp1 >= sfc0[iq]) {
-                            const float ph1 = atan2f(im, re);
-                            float d = fabsf(tl.y - ph1);
-                            d = fminf(d, K.tpi - d);
-                            const float w = 0.5f * (amp1 + tl.x);
-                            l1 = fmaf(d, w, l1);
-                            l2 = l2 + w;
+                        // bilinear on (re, im) pairs: lerp in x on both rows, then in y
+                        const float2 ax2 = make_float2(f.x, f.x), ay2 = make_float2(f.y, f.y);
+                        const float2 m1 = make_float2(-1.f, -1.f);
+                        const float2 v0 = __ffma2_rn(ax2, __ffma2_rn(t00, m1, t10), t00);
+                        const float2 v1 = __ffma2_rn(ax2, __ffma2_rn(t01, m1, t11), t01);
+                        const float2 z = __ffma2_rn(ay2, __ffma2_rn(v0, m1, v1), v0);
+                        const float2 zz = __fmul2_rn(z, z);
+                        const float sq = zz.x + zz.y;
+                        const float amp1 = sq * rsqrtf(sq);  // NaN for 0: fails the cut
+                        if (amp1 >= e.w) {
+                            const float2 pd = __fmul2_rn(z, make_float2(e.x, e.y));
+                            const float2 pc = __fmul2_rn(z, make_float2(e.y, -e.x));
+                            const float d = angle_between(pc.x + pc.y, pd.x + pd.y, K.pi);
+                            const float w = fmaf(0.5f, amp1, e.z);
+                            acc = __ffma2_rn(make_float2(d, 1.0f), make_float2(w, w), acc);
                         }
                     }
-                    kahan_add(pr1, c1, l1);
-                    kahan_add(pr2, c2, l2);
+                    kahan_add(pr1, c1, acc.x);
+                    kahan_add(pr2, c2, acc.y);
                 }
             }
         }
@@ -338,7 +365,7 @@ int pr_omega_smem_bytes(const Band& bd, int nomega, int* threads) {
     if (G < 1) G = 1;
     int nt = G * nomp;
     if (threads) *threads = nt;
-    size_t b = (size_t)bd.W * bd.W * 8 + (size_t)60 * bd.nr * 8 + (size_t)((bd.nr + 3) & ~3) * 4 +
+    size_t b = (size_t)bd.W * bd.W * 8 + (size_t)60 * bd.nr * 16 + (size_t)((bd.nr + 3) & ~3) * 4 +
                64 * 4 + (size_t)2 * nt * 4 + 32 * 8;
     return (int)b;
 }
