@@ -218,6 +218,38 @@ class Context:
         call("cryoim_rec_get_partial", self._h, ptr(fa), ptr(fb), ptr(wg))
         return fa, fb, wg
 
+    def rec_begin_half(self, mask_x: float, mask_y: float) -> None:
+        """One half map of a gold-standard pair (reconstruct_half.f90); images are masked
+        at (mask_x, mask_y), particle(first)'s origin in the reference."""
+        call("cryoim_rec_begin_half", self._h, float(mask_x), float(mask_y))
+
+    def half_maps(self, imgs, parts: np.ndarray):
+        """Odd and even tnf half maps of `parts` (particles 0, 2, ... and 1, 3, ...), both
+        masked at parts[0]'s origin, as icosprocess FSC=y builds them."""
+        p = np.ascontiguousarray(parts, dtype=PARTICLE_DTYPE)
+        im = np.ascontiguousarray(imgs, dtype=np.float32)
+        out = []
+        for parity in (0, 1):
+            self.rec_begin_half(p["x"][0], p["y"][0])
+            if parity < len(p):
+                self.rec_insert(im[parity::2], p[parity::2])
+            out.append(self.rec_get_partial())
+        return out
+
+    def fsc_combine(self, odd, even, want_map: bool = True):
+        """(FSC per shell 0..maxR, FSC-weighted map or None) from two tnf half maps."""
+        n, R = self.params.fftsize, self.params.max_r
+        a = [np.ascontiguousarray(x, np.float32) for x in (*odd, *even)]
+        t = 2 * R + 1
+        for x in a:
+            if x.size != (R + 1) * t * t:
+                raise ValueError("tnf arrays must hold (maxR+1)(2maxR+1)^2 floats")
+        fsc = np.zeros(R + 1, np.float32)
+        out = np.zeros((n, n, n), np.float32) if want_map else None
+        call("cryoim_fsc_combine", self._h, *[ptr(x) for x in a], ptr(fsc),
+             ptr(out) if want_map else None)
+        return fsc, out
+
     # -- central sections ----------------------------------------------------
     def central_sections(self, ft_re, ft_im, eulers) -> tuple[np.ndarray, np.ndarray]:
         n = self.params.fftsize

@@ -5,7 +5,8 @@ include/cryoim.h carries no torch types).  Translation units:
 
 * prep.cu  -- -fmad=false: FP32 expressions round where the Fortran reference rounds;
 * score.cu -- hot scoring kernels, multiply-add contraction allowed;
-* api.cu   -- context, drivers, C ABI (host code built with -ffp-contract=off).
+* api.cu   -- context, drivers, C ABI (host code built with -ffp-contract=off);
+* fsc.cu   -- -fmad=false: half-map FSC and the FSC-weighted map.
 """
 from __future__ import annotations
 
@@ -45,6 +46,7 @@ UNITS = {
     "noalloc.cu": [],
     "gemm_tc.cu": [],
     "contract.cu": [],
+    "fsc.cu": ["-fmad=false"],
 }
 
 

@@ -166,6 +166,10 @@ template <class T> struct DBuf {
     }
 };
 
+// accumulation kinds: full box (reconstruct.f90), tnf partial (reconstruct_substep.f90),
+// tnf half map (reconstruct_half.f90)
+enum { REC_FULL = 0, REC_SUBSTEP = 1, REC_HALF = 2 };
+
 struct Ctx {
     int device = 0;
     cudaStream_t stream = nullptr;
@@ -202,6 +206,7 @@ struct Ctx {
     DBuf<int2> samples;
     DBuf<float2> vol;
     bool rec_active = false;
+    int rec_kind = 0;  // REC_FULL, REC_SUBSTEP or REC_HALF
     int nsamples = 0, rec_used = 0, rec_img_id0 = -100;
     float rec_src_df[3] = {0, 0, 0};
     bool rec_have_first = false;
@@ -603,7 +608,8 @@ int rec_insert_impl(Ctx* c, const float* imgs, bool on_device, const cryoim_part
     const int B = c->batch, nx = c->p.fftsize;
     const long nn = (long)nx * nx;
     if ((r = ensure_batch(c, B))) return r;
-    const float boundx = c->p.subrec ? (float)nx / 4.0f : c->p.boundx;  // reconstruct_substep.f90:22
+    // reconstruct_substep.f90:22 sets boundX = FFTsize/4; reconstruct_half.f90:17 keeps it
+    const float boundx = c->rec_kind == REC_SUBSTEP ? (float)nx / 4.0f : c->p.boundx;
     const Angles an = host_angles();
     std::vector<float> hpar(8 * B), hrot(9 * B);
     std::vector<int> hsel(B);
@@ -1350,20 +1356,23 @@ int cryoim_prscore(void* ctx, const float* ft_a, const float* ft_b, const float*
     return CRYOIM_OK;
 }
 
-int cryoim_rec_begin(void* ctx) {
-    Ctx* c = as_ctx(ctx);
+// kind: REC_FULL (reconstruct.f90), REC_SUBSTEP (reconstruct_substep.f90) or REC_HALF
+// (reconstruct_half.f90, mask origin given by the caller).
+static int rec_begin_impl(Ctx* c, int kind, const float* mask_origin) {
     int r = check_ready(c, false);
     if (r) return r;
     const Band& bd = c->bd;
     const int R = bd.max_r, nx = c->p.fftsize;
     const long nacc = (long)bd.AW * bd.AW * (R + 2);
     if ((r = c->acc.ensure(nacc))) return r;
-    // reconstruct.f90:26-28 (wg = 0.01) or reconstruct_substep.f90:23-25 (wg = 0)
-    const float wg0 = c->p.subrec ? 0.0f : 0.01f;
+    // reconstruct.f90:26-28 (wg = 0.01), reconstruct_substep.f90:23-25 and
+    // reconstruct_half.f90:17 (wg = 0)
+    const float wg0 = kind == REC_FULL ? 0.01f : 0.0f;
     std::vector<float4> init(nacc, make_float4(0.f, 0.f, wg0, 0.f));
     CK(cudaMemcpyAsync(c->acc.p, init.data(), sizeof(float4) * nacc, cudaMemcpyHostToDevice, c->stream));
-    // insertion samples: reconstruct.f90:103-106 (r <= maxR) or reconstruct_substep.f90:101-104 (r <= maxR-2)
-    const float lim = c->p.subrec ? (float)(R - 2) : (float)R;
+    // insertion samples: reconstruct.f90:103-106 and reconstruct_half.f90:95-96 (r <= maxR),
+    // reconstruct_substep.f90:101-104 (r <= maxR-2)
+    const float lim = kind == REC_SUBSTEP ? (float)(R - 2) : (float)R;
     std::vector<int2> smp;
     for (int ky = -R; ky <= R; ++ky)
         for (int hx = 0; hx <= R; ++hx) {
@@ -1373,19 +1382,32 @@ int cryoim_rec_begin(void* ctx) {
     c->nsamples = (int)smp.size();
     if ((r = c->samples.ensure(smp.size() + 1))) return r;
     CK(cudaMemcpyAsync(c->samples.p, smp.data(), sizeof(int2) * smp.size(), cudaMemcpyHostToDevice, c->stream));
-    if (c->p.subrec) {
-        // reconstruct_substep.f90:121: x0(1:2) += maxR, z unshifted; tnf cell lx -> box lx+1
+    if (kind != REC_FULL) {
+        // reconstruct_substep.f90:121, reconstruct_half.f90:114: x0(1:2) += maxR, z
+        // unshifted; tnf cell lx -> box lx+1
         c->rec_off_xy = (float)R; c->rec_off_z = 0.0f; c->rec_base_xy = -1; c->rec_base_z = 0;
     } else {
         c->rec_off_xy = (float)(nx / 2); c->rec_off_z = (float)(nx / 2);
         c->rec_base_xy = nx / 2 - R - 1; c->rec_base_z = nx / 2;
     }
     CK(cudaStreamSynchronize(c->stream));
+    c->rec_kind = kind;
     c->rec_active = true;
     c->rec_used = 0;
     c->rec_img_id0 = -100;
-    c->rec_have_first = false;
+    c->rec_have_first = mask_origin != nullptr;
+    if (mask_origin) { c->rec_ox = mask_origin[0]; c->rec_oy = mask_origin[1]; }
     return CRYOIM_OK;
+}
+
+int cryoim_rec_begin(void* ctx) {
+    Ctx* c = as_ctx(ctx);
+    return rec_begin_impl(c, c->p.subrec ? REC_SUBSTEP : REC_FULL, nullptr);
+}
+
+int cryoim_rec_begin_half(void* ctx, float mask_x, float mask_y) {
+    const float o[2] = {mask_x, mask_y};
+    return rec_begin_impl(as_ctx(ctx), REC_HALF, o);
 }
 
 int cryoim_rec_insert(void* ctx, const float* imgs, const cryoim_particle* parts, int32_t P,
@@ -1404,8 +1426,9 @@ int cryoim_rec_finish(void* ctx, float* map) {
     if (r) return r;
     if (!c->rec_active) return fail(CRYOIM_ERR_STATE, "cryoim_rec_begin has not been called");
     if (!map) return fail(CRYOIM_ERR_ARG, "null map");
-    if (c->p.subrec)
-        return fail(CRYOIM_ERR_STATE, "subrec accumulation has no map: use cryoim_rec_get_partial");
+    if (c->rec_kind != REC_FULL)
+        return fail(CRYOIM_ERR_STATE, "tnf accumulation (subrec or half map) has no map: use "
+                                      "cryoim_rec_get_partial (and cryoim_fsc_combine for half maps)");
     const int nx = c->p.fftsize;
     const long n3 = (long)nx * nx * nx;
     if ((r = c->vol.ensure(n3))) return r;
@@ -1451,6 +1474,75 @@ int cryoim_rec_get_partial(void* ctx, float* fa, float* fb, float* wg) {
                 long o = ((long)z * t + y) * t + x;
                 fa[o] = v.x; fb[o] = v.y; wg[o] = v.z;
             }
+    if (c->rec_kind != REC_FULL) {
+        // The reference indexes its tnf box linearly (cubID = lz t^2 + ly t + lx + 1,
+        // reconstruct_half.f90:127-130): a trilinear corner at x = t (or y = t) lands on
+        // the next row (plane).  Corners at z = maxR+1 fall past its array: dropped.
+        const long tnf = (long)(R + 1) * t * t;
+        for (int z = 0; z <= R + 1; ++z)
+            for (int y = 0; y <= t; ++y)
+                for (int x = 0; x <= t; ++x) {
+                    if (x < t && y < t && z <= R) continue;
+                    const long o = ((long)z * t + y) * t + x;
+                    if (o >= tnf) continue;
+                    const float4& v = h[acc_cell(bd, x - R, y - R, z)];
+                    fa[o] += v.x; fb[o] += v.y; wg[o] += v.z;
+                }
+    }
+    return CRYOIM_OK;
+}
+
+int cryoim_fsc_combine(void* ctx, const float* fa1, const float* fb1, const float* wg1, const float* fa2,
+                       const float* fb2, const float* wg2, float* fsc, float* map) {
+    Ctx* c = as_ctx(ctx);
+    int r = check_ready(c, false);
+    if (r) return r;
+    if (!fa1 || !fb1 || !wg1 || !fa2 || !fb2 || !wg2) return fail(CRYOIM_ERR_ARG, "null tnf input");
+    const int nx = c->p.fftsize, R = c->p.max_r, t = 2 * R + 1, ns = R + 1;
+    const long tnf = (long)ns * t * t, n3 = (long)nx * nx * nx;
+    DBuf<float> d;
+    DBuf<double> sums;
+    DBuf<float> wt;
+    if ((r = d.ensure(6 * tnf)) || (r = sums.ensure(3 * ns)) || (r = wt.ensure(ns))) return r;
+    const float* src[6] = {fa1, fb1, wg1, fa2, fb2, wg2};
+    for (int i = 0; i < 6; ++i)
+        CK(cudaMemcpyAsync(d.p + i * tnf, src[i], sizeof(float) * tnf, cudaMemcpyHostToDevice, c->stream));
+    FscArgs a{};
+    a.fa1 = d.p; a.fb1 = d.p + tnf; a.wg1 = d.p + 2 * tnf;
+    a.fa2 = d.p + 3 * tnf; a.fb2 = d.p + 4 * tnf; a.wg2 = d.p + 5 * tnf;
+    a.nx = nx; a.max_r = R;
+    if (c->num_sms == 0) CK(cudaDeviceGetAttribute(&c->num_sms, cudaDevAttrMultiProcessorCount, c->device));
+    CK(launch_fsc_shells(a, sums.p, c->num_sms, c->stream));
+    std::vector<double> hs(3 * ns);
+    CK(cudaMemcpyAsync(hs.data(), sums.p, sizeof(double) * 3 * ns, cudaMemcpyDeviceToHost, c->stream));
+    CK(cudaStreamSynchronize(c->stream));
+    // reconstruct_FSC.f90:43-62: FSC1 = FSC2 = 1e-10 at start; weight sqrt(2F/(1+F)), 0 if F <= 0
+    std::vector<float> hw(ns);
+    for (int i = 0; i < ns; ++i) {
+        const float F = (float)(hs[i] / std::sqrt((1e-10 + hs[ns + i]) * (1e-10 + hs[2 * ns + i])));
+        if (fsc) fsc[i] = F;
+        hw[i] = F <= 0.0f ? 0.0f : std::sqrt(2.0f * F / (1.0f + F));
+    }
+    if (!map) return CRYOIM_OK;
+    CK(cudaMemcpyAsync(wt.p, hw.data(), sizeof(float) * ns, cudaMemcpyHostToDevice, c->stream));
+    if ((r = c->vol.ensure(n3))) return r;
+    CK(launch_fsc_fold(a, wt.p, c->vol.p, c->stream));
+    cufftHandle h;
+    CKF(cufftPlan3d(&h, nx, nx, nx, CUFFT_C2C));
+    cufftResult fr = cufftSetStream(h, c->stream);
+    if (fr == CUFFT_SUCCESS)
+        fr = cufftExecC2C(h, (cufftComplex*)c->vol.p, (cufftComplex*)c->vol.p, CUFFT_INVERSE);
+    if (fr != CUFFT_SUCCESS) {
+        cufftDestroy(h);
+        return fail(CRYOIM_ERR_CUDA, "3D inverse FFT failed: cufft %d", (int)fr);
+    }
+    DBuf<float> dmap;
+    if ((r = dmap.ensure(n3))) { cufftDestroy(h); return r; }
+    launch_rec_real(c->vol.p, nx, dmap.p, c->stream);
+    cudaError_t e = cudaMemcpyAsync(map, dmap.p, sizeof(float) * n3, cudaMemcpyDeviceToHost, c->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+    cufftDestroy(h);
+    if (e != cudaSuccess) return fail(CRYOIM_ERR_CUDA, "fsc combine: %s", cudaGetErrorString(e));
     return CRYOIM_OK;
 }
 

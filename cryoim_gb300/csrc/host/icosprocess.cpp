@@ -6,13 +6,16 @@
 // MRC, orientation files read as 13 list-directed columns and written as the 19-column
 // row of format 900, tnf partial reconstructions.  Modes:
 //   0  project the model along every template orientation into templatestck
-//   1  symmetrised reconstruction into result3d (map, or tnf partial with subrec=y)
+//   1  symmetrised reconstruction into result3d (map, or tnf partial with subrec=y;
+//      FSC=y: gold-standard half maps, FSC.txt and the FSC-weighted map)
 //   4  global orientation search (ort_globesearch.f90) -> newortfile
 //   5  local refinement (ort_refinement.f90) -> newortfile
 // Extension keys without a reference counterpart: device, batch (particles per device
 // call), contract=y (mode 4 through the tensor-core contraction), originmax,
 // originstep, topk.  Output rows are appended after every chunk, so a run can resume
 // with first=k as with the reference's per-particle writes.
+#include <algorithm>
+#include <cmath>
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
@@ -38,7 +41,8 @@ void usage() {
         "icosprocess (cryoim_gb300): icosahedral projection matching on a GB300 GPU\n"
         "usage: icosprocess mode=<0|1|4|5> ortfile=<ort> key=value ...\n"
         "  mode=0 project model3d along templateort into templatestck\n"
-        "  mode=1 reconstruct into result3d      (PR_threshold, boundX, subrec, applyCTF)\n"
+        "  mode=1 reconstruct into result3d      (PR_threshold, boundX, subrec, applyCTF;\n"
+        "         FSC=y: odd/even half maps oddtnf, evetnf, FSC.txt, FSC-weighted result3d)\n"
         "  mode=4 global search into newortfile  (templateort + templatestck or model3d,\n"
         "         searchstep, minRes, maxRes, applyCTF, vol, Cs, ampwg)\n"
         "  mode=5 local refinement into newortfile (Ncycle, templateort, ...)\n"
@@ -179,7 +183,7 @@ int main(int argc, char** argv) {
     if (sval("sym", "icos") != "icos") return die("only sym=icos is on this path", 2);
     if (has("corrCTF") || has("recISAF") || has("loc_box"))
         return die("corrCTF / recISAF / loc_box modes are not on this path", 2);
-    if (p.fsc && mode == 1) return die("FSC=y (half-map reconstruction) is not on this path", 2);
+    if (p.realspaceavg && mode == 1) return die("realspaceavg=y is not on this path", 2);
     if (cryoim_params_derive(&p)) return die("parameters", 2);
     if (p.first < 1 || p.last < p.first || p.last > nrows) return die("first/last out of range", 2);
 
@@ -262,6 +266,62 @@ int main(int argc, char** argv) {
             }
             if (cryoim_ort_write(out.c_str(), &parts[i0], &names[(size_t)i0 * 256], 256, n, 54, 1))
                 return die("cannot write newortfile", 2);
+        }
+    } else if (mode == 1 && p.fsc) {
+        // 0main.f90:207-222: odd half (first, first+2, ...) into oddtnf, even half
+        // (first+1, ...) into evetnf, both masked at particle(first)'s origin; without
+        // subrec, reconstruct_FSC combines them into FSC.txt and result3d.
+        const std::string res = sval("result3d", "map3d.mrc");
+        const size_t t = (size_t)(2 * p.max_r + 1), tnf = t * t * (p.max_r + 1);
+        std::vector<float> half[2][3];
+        std::string last_stack = imgstck;
+        for (int parity = 0; parity < 2; ++parity) {
+            std::vector<cryoim_particle> hp;
+            std::vector<std::string> hs;
+            for (int i = parity; i < P; i += 2) { hp.push_back(parts[i]); hs.push_back(stck[i]); }
+            if (cryoim_rec_begin_half(ctx, parts[0].x, parts[0].y)) return die("half map", 2);
+            const int H = (int)hp.size();
+            int used = 0;
+            for (int i0 = 0; i0 < H; i0 += chunk) {
+                const int n = std::min(chunk, H - i0);
+                // with imgstck the reference reads the stack in sequence from image first
+                // of the half, one image per step of two particles (reconstruct_half.f90:
+                // 32-36, 53): particle first+2k meets image first+k
+                if (gather(hp, hs, i0, n, nx, imgstck, p.first + parity, imgs)) return die("particle stack read", 2);
+                int u = 0;
+                if (cryoim_rec_insert(ctx, imgs.data(), &hp[i0], n, &u)) return die("insertion", 2);
+                used += u;
+            }
+            if (H > 0 && imgstck.empty()) last_stack = hs[H - 1];
+            std::printf(" half %s: used particles: %d of %d\n", parity ? "even" : "odd", used, H);
+            for (auto& v : half[parity]) v.resize(tnf);
+            if (cryoim_rec_get_partial(ctx, half[parity][0].data(), half[parity][1].data(), half[parity][2].data()))
+                return die("partial", 2);
+            const std::string name = (p.subrec ? res : std::string()) + (parity ? "evetnf" : "oddtnf");
+            // reconstruct_half.f90:140-144: the header flag is subrec
+            if (cryoim_tnf_write(name.c_str(), nx, p.max_r, p.apix, p.imgmask_px, p.subrec, p.realspaceavg,
+                                 half[parity][0].data(), half[parity][1].data(), half[parity][2].data()))
+                return die("cannot write the half-map tnf", 2);
+        }
+        if (!p.subrec) {
+            std::vector<float> fsc(p.max_r + 1), map((size_t)nx * nx * nx);
+            if (cryoim_fsc_combine(ctx, half[0][0].data(), half[0][1].data(), half[0][2].data(), half[1][0].data(),
+                                   half[1][1].data(), half[1][2].data(), fsc.data(), map.data()))
+                return die("FSC", 2);
+            std::FILE* f = std::fopen("FSC.txt", "w");  // reconstruct_FSC.f90:14, 56
+            if (!f) return die("cannot write FSC.txt", 2);
+            for (int ir = 0; ir <= p.max_r; ++ir) {
+                const float F = fsc[ir], w = std::sqrt(2.0f * F / (1.0f + F));
+                std::fprintf(f, "%12d %15.7f ", ir, F);
+                if (w == w) std::fprintf(f, "%15.7f\n", w);
+                else std::fprintf(f, "%15s\n", "NaN");
+            }
+            std::fclose(f);
+            // reconstruct_FSC.f90:181-182 writes the header it last read: that of the
+            // particle stack the even half read last
+            cryoim_mrc_header oh;
+            if (cryoim_mrc_read_header(last_stack.c_str(), &oh)) cryoim_map_header(&oh, nx, nx, nx, p.apix);
+            if (cryoim_mrc_write(res.c_str(), &oh, map.data(), (int64_t)map.size())) return die("cannot write result3d", 2);
         }
     } else if (mode == 1) {
         if (cryoim_rec_begin(ctx)) return die("reconstruction", 2);

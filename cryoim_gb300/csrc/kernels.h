@@ -153,4 +153,15 @@ void launch_select_topk(const float* topv, const int* topi, int O, int ntiles, i
 void launch_cc_fp64(const float2* cube, const float2* band, const float* ctf, Band bd, const int2* samples,
                     int S, const float* cand, int k, int B, double* out, cudaStream_t st);
 
+// ---- fsc.cu: half-map FSC and the FSC-weighted map ---------------------------
+struct FscArgs {
+    const float *fa1, *fb1, *wg1;  // odd tnf partial, (maxR+1)(2maxR+1)^2 each
+    const float *fa2, *fb2, *wg2;  // even tnf partial
+    int nx, max_r;
+};
+// sums: 3 x (maxR+1) FP64 (cross, |odd|^2, |even|^2 per shell)
+cudaError_t launch_fsc_shells(const FscArgs& a, double* sums, int sms, cudaStream_t st);
+// wt: maxR+1 shell weights; vol: nx^3 complex, zeroed and filled with cmplx(fa, fb)
+cudaError_t launch_fsc_fold(const FscArgs& a, const float* wt, float2* vol, cudaStream_t st);
+
 }  // namespace cryoim

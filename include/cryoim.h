@@ -228,6 +228,26 @@ int cryoim_rec_get_partial(void* ctx, float* fa, float* fb, float* wg);
  * rec_begin, one add per partial and rec_finish give the merged map. */
 int cryoim_rec_add_partial(void* ctx, const float* fa, const float* fb, const float* wg);
 
+/* Start one half map of a gold-standard pair (reconstruct_half.f90:4-151): tnf
+ * accumulation with wg starting at 0, samples r <= maxR, boundX from the parameters.
+ * The caller inserts the half's particles (first, first+2, ... for the odd half;
+ * first+1, first+3, ... for the even half) with cryoim_rec_insert and reads the tnf with
+ * cryoim_rec_get_partial.  (mask_x, mask_y): the origin every image is masked at, which
+ * in the reference is particle(first) of the whole range for both halves
+ * (reconstruct_half.f90:83 passes particle%x).  Replaces the two `call reconstruct_half`
+ * of icosprocess/SRC/0main.f90:207-221. */
+int cryoim_rec_begin_half(void* ctx, float mask_x, float mask_y);
+
+/* Fourier shell correlation of the odd (fa1, fb1, wg1) and even (fa2, fb2, wg2) tnf half
+ * maps and their FSC-weighted sum as a map (reconstruct_FSC.f90:25-178): fsc (maxR+1
+ * floats, may be NULL) gets FSC(ir) of the integer shells ir = 0..maxR, as written to
+ * FSC.txt; map (nx^3, may be NULL) gets the weighted, Friedel-completed, inverse-FFT map
+ * (FFT3d = cmplx(fa, fb) as reconstruct_FSC.f90:173 has it: the point inversion of what
+ * reconstruct.f90:241 gives).  Replaces `call reconstruct_fsc` (0main.f90:222). */
+int cryoim_fsc_combine(void* ctx, const float* fa1, const float* fb1, const float* wg1,
+                       const float* fa2, const float* fb2, const float* wg2, float* fsc,
+                       float* map);
+
 /* ---- files (host only; byte-compatible with the reference) ---------------- */
 
 /* The `mrchead` type of icosprocess/SRC/0common_icosproc.f90:61-112: 1024 bytes. */

@@ -1043,6 +1043,172 @@ int reconstruct(const cryoim_params* p, const float* imgs, const cryoim_particle
     return 0;
 }
 
+/* icosprocess/SRC/reconstruct_half.f90:4-151: particles parity, parity+2, ... of the
+ * range, accumulated into the tnf half box (R+1)(2R+1)^2 (fa, fb, wg start at 0).  Masks
+ * every image at parts[0]'s origin (the reference passes particle%x, whose first element
+ * is particle(first) of the whole range for both halves), samples r <= maxR, x0(1:2) +=
+ * maxR.  A trilinear corner past the box's row/plane end lands, as in the reference's
+ * linear cubID, on the next row/plane; one past the last plane is dropped. */
+template <class R>
+int reconstruct_half(const cryoim_params* p, const float* imgs, const cryoim_particle* parts, int P,
+                     int parity, R* fa, R* fb, R* wg) {
+    int nx = p->fftsize, maxR = p->max_r, h = nx / 2, t = 2 * maxR + 1;
+    long nn = (long)nx * nx, tnf = (long)(maxR + 1) * t * t;
+    std::fill(fa, fa + tnf, R(0));
+    std::fill(fb, fb + tnf, R(0));
+    std::fill(wg, wg + tnf, R(0));
+    if (P < 1) return 0;
+    const R* sym = icos_ops<R>();
+    std::vector<R> a(nn), b(nn), ctf(nn, R(1));
+    const R ox = (R)parts[0].x, oy = (R)parts[0].y;
+    int id0 = -100;
+    for (int ip = parity; ip < P; ip += 2) {
+        const cryoim_particle& q = parts[ip];
+        if (!(q.pr <= p->pr_threshold && std::fabs(q.x) <= p->boundx && std::fabs(q.y) <= p->boundx))
+            continue;
+        for (long k = 0; k < nn; ++k) a[k] = (R)imgs[(long)ip * nn + k];
+        img2d_norm(a.data(), nx);
+        /* reconstruct_half.f90:71-81: every particle's CTF for imgstck, else cached per imgID */
+        if (p->imgstck || (p->apply_ctf && q.img_id != id0)) {
+            get_ctf2d(nx, (R)q.df1, (R)q.df2, (R)q.astigang, (R)p->apix, (R)p->vol, (R)p->cs,
+                      (R)p->ampwg, ctf.data());
+            if (!p->imgstck) id0 = q.img_id;
+        }
+        if (p->use_imgmask) img2d_mask(a.data(), nx, (R)p->imgmask_px, ox, oy);
+        for (long k = 0; k < nn; ++k) {
+            int ky = (int)(k / nx), hx = (int)(k % nx);
+            if ((hx + ky) & 1) a[k] = -a[k];
+            b[k] = R(0);
+        }
+        img2d_fft(a.data(), b.data(), nx, nx, 1);
+        centshift(a.data(), b.data(), nx, (R)q.x, (R)q.y);
+        R rot[9];
+        euler_mat((R)q.theta, (R)q.phi, (R)q.omega, rot);
+        for (int ky = -maxR; ky <= maxR; ++ky)
+            for (int hx = 0; hx <= maxR; ++hx) {
+                R dr = std::sqrt((R)(hx * hx + ky * ky));
+                if (!(dr <= (R)maxR)) continue;
+                long i2 = (long)(ky + h) * nx + (hx + h);
+                R xv[3] = {(R)hx, (R)ky, R(0)}, x00[3];
+                mv3(rot, xv, x00);
+                for (int is = 0; is < p->nsym; ++is) {
+                    R x0[3];
+                    mv3(sym + is * 9, x00, x0);
+                    R signz = R(1);
+                    if (x0[2] < R(0)) { x0[0] = -x0[0]; x0[1] = -x0[1]; x0[2] = -x0[2]; signz = R(-1); }
+                    x0[0] = x0[0] + (R)maxR; x0[1] = x0[1] + (R)maxR;
+                    int lx[3] = {fint(x0[0]), fint(x0[1]), fint(x0[2])};
+                    R ax[3] = {x0[0] - (R)lx[0], x0[1] - (R)lx[1], x0[2] - (R)lx[2]};
+                    R dx[8];
+                    dx[0] = (R(1) - ax[0]) * (R(1) - ax[1]) * (R(1) - ax[2]);
+                    dx[1] = (ax[0]) * (R(1) - ax[1]) * (R(1) - ax[2]);
+                    dx[2] = (R(1) - ax[0]) * (ax[1]) * (R(1) - ax[2]);
+                    dx[3] = (ax[0]) * (ax[1]) * (R(1) - ax[2]);
+                    dx[4] = (R(1) - ax[0]) * (R(1) - ax[1]) * (ax[2]);
+                    dx[5] = (ax[0]) * (R(1) - ax[1]) * (ax[2]);
+                    dx[6] = (R(1) - ax[0]) * (ax[1]) * (ax[2]);
+                    dx[7] = (ax[0]) * (ax[1]) * (ax[2]);
+                    long c1 = ((long)lx[2] * t + lx[1]) * t + lx[0];
+                    long tt = (long)t * t;
+                    long cub[8] = {c1, c1 + 1, c1 + t, c1 + t + 1, c1 + tt, c1 + tt + 1, c1 + tt + t, c1 + tt + t + 1};
+                    R c = ctf[i2];
+                    for (int j = 0; j < 8; ++j) {
+                        if (cub[j] < 0 || cub[j] >= tnf) continue;
+                        fa[cub[j]] = fa[cub[j]] + a[i2] * dx[j] * c;
+                        fb[cub[j]] = fb[cub[j]] + b[i2] * dx[j] * c * signz;
+                        wg[cub[j]] = wg[cub[j]] + dx[j] * (c * c);
+                    }
+                }
+            }
+    }
+    return 0;
+}
+
+/* icosprocess/SRC/reconstruct_FSC.f90:25-178: FSC per integer shell of the odd (1) and
+ * even (2) tnf partials, FSC weighting sqrt(2F/(1+F)) of their sum, Friedel fold to the
+ * full cube, FFT3d = cmplx(fa, fb), backward 3D FFT, shift3dComplex, real part.
+ * fsc_out: R+1 raw FSC values (as written to FSC.txt); map_out: nx^3. */
+template <class R>
+int fsc_combine(int nx, int maxR, const float* fa1, const float* fb1, const float* wg1,
+                const float* fa2, const float* fb2, const float* wg2, R* fsc_out, float* map_out) {
+    int t = 2 * maxR + 1, h = nx / 2;
+    long tnf = (long)(maxR + 1) * t * t, nn = (long)nx * nx, n3 = nn * nx;
+    std::vector<R> a1(tnf), b1(tnf), w1(tnf), a2(tnf), b2(tnf), w2(tnf);
+    for (long i = 0; i < tnf; ++i) {
+        w1[i] = (R)wg1[i] + R(1); w2[i] = (R)wg2[i] + R(1);
+        a1[i] = (R)fa1[i] / w1[i]; b1[i] = (R)fb1[i] / w1[i];
+        a2[i] = (R)fa2[i] / w2[i]; b2[i] = (R)fb2[i] / w2[i];
+    }
+    std::vector<R> F(maxR + 1, R(0)), F1(maxR + 1, R(1e-10)), F2(maxR + 1, R(1e-10));
+    auto tidx = [&](int hx, int ky, int lz) { return ((long)lz * t + (ky + maxR)) * t + (hx + maxR); };
+    auto shell = [&](int hx, int ky, int lz) { return fint(std::sqrt((float)(hx * hx + ky * ky + lz * lz))); };
+    for (int lz = 0; lz <= maxR; ++lz)
+        for (int ky = -maxR; ky <= maxR; ++ky)
+            for (int hx = -maxR; hx <= maxR; ++hx) {
+                int ir = shell(hx, ky, lz);
+                if (ir > maxR) continue;
+                long i3 = tidx(hx, ky, lz);
+                F[ir] = F[ir] + (a1[i3] * a2[i3] + b1[i3] * b2[i3]);
+                F1[ir] = F1[ir] + (a1[i3] * a1[i3] + b1[i3] * b1[i3]);
+                F2[ir] = F2[ir] + (a2[i3] * a2[i3] + b2[i3] * b2[i3]);
+            }
+    for (int ir = 0; ir <= maxR; ++ir) {
+        F[ir] = F[ir] / std::sqrt(F1[ir] * F2[ir]);
+        fsc_out[ir] = F[ir];
+        F[ir] = F[ir] <= R(0) ? R(0) : std::sqrt(R(2) * F[ir] / (R(1) + F[ir]));
+    }
+    for (long i = 0; i < tnf; ++i) {
+        a1[i] = a1[i] * w1[i] + a2[i] * w2[i];
+        b1[i] = b1[i] * w1[i] + b2[i] * w2[i];
+        w1[i] = w1[i] + w2[i] - R(2);
+    }
+    for (int lz = 0; lz <= maxR; ++lz)
+        for (int ky = -maxR; ky <= maxR; ++ky)
+            for (int hx = -maxR; hx <= maxR; ++hx) {
+                int ir = shell(hx, ky, lz);
+                long i3 = tidx(hx, ky, lz);
+                if (ir <= maxR) { a1[i3] = a1[i3] * F[ir]; b1[i3] = b1[i3] * F[ir]; w1[i3] = w1[i3] * F[ir]; }
+                else { a1[i3] = R(0); b1[i3] = R(0); }
+            }
+    for (long i = 0; i < tnf; ++i) w1[i] = w1[i] + R(1);
+    std::vector<R> fa(n3, R(0)), fb(n3, R(0));
+    auto vidx = [&](int hx, int ky, int lz) { return (long)(lz + h) * nn + (long)(ky + h) * nx + (hx + h); };
+    auto pair0 = [&](int hx, int ky) {
+        if (shell(hx, ky, 0) > maxR) return;
+        long ia = tidx(hx, ky, 0), ib = tidx(-hx, -ky, 0), n1 = vidx(hx, ky, 0), n2 = vidx(-hx, -ky, 0);
+        w1[ia] = w1[ia] + w1[ib];
+        fa[n1] = (a1[ia] + a1[ib]) / w1[ia];
+        fb[n1] = (b1[ia] - b1[ib]) / w1[ia];
+        if (((hx + ky) % 2 + 2) % 2 == 0) { fa[n2] = fa[n1]; fb[n2] = -fb[n1]; }
+        else { fa[n1] = -fa[n1]; fb[n1] = -fb[n1]; fa[n2] = fa[n1]; fb[n2] = -fb[n1]; }
+    };
+    for (int ky = 1; ky <= maxR; ++ky)
+        for (int hx = -maxR; hx <= maxR; ++hx) pair0(hx, ky);
+    for (int hx = 1; hx <= maxR; ++hx) pair0(hx, 0);
+    fa[vidx(0, 0, 0)] = a1[tidx(0, 0, 0)] / w1[tidx(0, 0, 0)];
+    fb[vidx(0, 0, 0)] = R(0);
+    for (int lz = 1; lz <= maxR; ++lz)
+        for (int ky = -maxR; ky <= maxR; ++ky)
+            for (int hx = -maxR; hx <= maxR; ++hx) {
+                if (shell(hx, ky, lz) > maxR) continue;
+                long i3 = tidx(hx, ky, lz), n1 = vidx(hx, ky, lz), n2 = vidx(-hx, -ky, -lz);
+                R s = (((hx + ky + lz) % 2 + 2) % 2 == 0) ? R(1) : R(-1);
+                fa[n1] = a1[i3] / w1[i3] * s;
+                fb[n1] = b1[i3] / w1[i3] * s;
+                fa[n2] = fa[n1];
+                fb[n2] = -fb[n1];
+            }
+    /* FFT3d = cmplx(fa, fb) (reconstruct_FSC.f90:173; reconstruct.f90:241 conjugates) */
+    fft3d(fa.data(), fb.data(), nx, +1);
+    for (long k = 0; k < n3; ++k) {
+        int lz = (int)(k / nn), ky = (int)((k / nx) % nx), hx = (int)(k % nx);
+        R v = fa[k];
+        if ((hx + ky + lz) & 1) v = -v;
+        map_out[k] = (float)v;
+    }
+    return 0;
+}
+
 /* ------------------------------------------------------------------------ */
 /* proc_icos                                                                   */
 /* ------------------------------------------------------------------------ */
@@ -1165,6 +1331,16 @@ template <class R> void transform_ort(int to, R* th, R* ph, R* om, int n) {
     extern "C" int orc_reconstruct_##S(const cryoim_params* p, const float* im,                      \
                                         const cryoim_particle* pa, int P, float* map, R* acc) {       \
         return reconstruct<R>(p, im, pa, P, map, acc);                                                 \
+    }                                                                                                  \
+    extern "C" int orc_reconstruct_half_##S(const cryoim_params* p, const float* im,                 \
+                                             const cryoim_particle* pa, int P, int parity, R* fa,      \
+                                             R* fb, R* wg) {                                           \
+        return reconstruct_half<R>(p, im, pa, P, parity, fa, fb, wg);                                  \
+    }                                                                                                  \
+    extern "C" int orc_fsc_combine_##S(int nx, int maxR, const float* a1, const float* b1,           \
+                                        const float* w1, const float* a2, const float* b2,             \
+                                        const float* w2, R* fsc, float* map) {                         \
+        return fsc_combine<R>(nx, maxR, a1, b1, w1, a2, b2, w2, fsc, map);                             \
     }                                                                                                  \
     extern "C" void orc_equalort_##S(R th, R ph, R om, R* out) { equalort<R>(th, ph, om, out); }      \
     extern "C" void orc_transform_ort_##S(int to, R* th, R* ph, R* om, int n) {                      \

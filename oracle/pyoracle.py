@@ -269,6 +269,31 @@ def reconstruct(params, imgs, parts, want_acc=False, fp="f64"):
     return (out, acc) if want_acc else out
 
 
+def reconstruct_half(params, imgs, parts, parity, fp="f64"):
+    """reconstruct_half.f90: tnf partial (fa, fb, wg), each (R+1, 2R+1, 2R+1), of the
+    particles parity, parity+2, ... of `parts`."""
+    dt = _dt(fp)
+    R = params.max_r
+    t = 2 * R + 1
+    im = np.ascontiguousarray(imgs, np.float32)
+    fa, fb, wg = (np.zeros((R + 1, t, t), dt) for _ in range(3))
+    r = _fn("reconstruct_half", fp)(C.byref(params), _p(im), _p(np.ascontiguousarray(parts)),
+                                    C.c_int(len(parts)), C.c_int(parity), _p(fa), _p(fb), _p(wg))
+    assert r == 0
+    return fa, fb, wg
+
+
+def fsc_combine(nx, max_r, odd, even, fp="f64"):
+    """reconstruct_FSC.f90: (FSC per shell 0..R, FSC-weighted map nx^3) from the odd and
+    even tnf partials (each a (fa, fb, wg) triple, float32)."""
+    a = [np.ascontiguousarray(x, np.float32) for x in (*odd, *even)]
+    fsc = np.zeros(max_r + 1, _dt(fp))
+    out = np.zeros((nx, nx, nx), np.float32)
+    r = _fn("fsc_combine", fp)(C.c_int(nx), C.c_int(max_r), *[_p(x) for x in a], _p(fsc), _p(out))
+    assert r == 0
+    return fsc, out
+
+
 def equalort(theta, phi, omega, fp="f32"):
     out = np.zeros((60, 3), _dt(fp))
     R = _R(fp)

@@ -48,10 +48,23 @@ def files(built, tmp_path_factory):
     return d, common, (p, vol, tmpl, timgs, imgs, parts, truth)
 
 
-def run(args):
-    r = subprocess.run([os.path.join(BIN, args[0])] + args[1:], capture_output=True, text=True)
+def run(args, cwd=None):
+    r = subprocess.run([os.path.join(BIN, args[0])] + args[1:], capture_output=True, text=True, cwd=cwd)
     assert r.returncode == 0, r.stdout + r.stderr
     return r
+
+
+def read_tnf(path):
+    import ctypes as C
+    L = lib()
+    ih, fh = np.zeros(4, np.int32), np.zeros(2, np.float32)
+    assert L.cryoim_tnf_read(str(path).encode(), ih.ctypes.data, fh.ctypes.data, None, None, None) == 0
+    R = int(ih[1])
+    t = 2 * R + 1
+    a, b, w = (np.zeros((R + 1, t, t), np.float32) for _ in range(3))
+    assert L.cryoim_tnf_read(str(path).encode(), ih.ctypes.data, fh.ctypes.data, a.ctypes.data,
+                             b.ctypes.data, w.ctypes.data) == 0
+    return ih, fh, (a, b, w)
 
 
 def library_parts(d, case):
@@ -135,6 +148,37 @@ def test_mode1_and_subrec_merge(files):
     run(["merge_icosprocess_subrec", str(d / "all.tnf"), str(d / "m1.mrc")])
     m1, m2 = read_map(d / "m1.mrc", n), read_map(d / "m2.mrc", n)
     assert np.linalg.norm(m1 - m2) / np.linalg.norm(m1) < 1e-4
+
+
+def test_mode1_fsc_half_maps(files):
+    """FSC=y (0main.f90:216-222): oddtnf, evetnf, FSC.txt and the FSC-weighted map in
+    result3d; with subrec=y only the two tnf files, named result3d//'oddtnf' etc."""
+    import cryoim_gb300 as ci
+    d, common, case = files
+    p, vol, tmpl, timgs, imgs, parts, truth = case
+    n = p.fftsize
+    run(["icosprocess", "mode=1", *common, "FSC=y", f"result3d={d / 'fsc.mrc'}"], cwd=d)
+    q = library_parts(d, case)
+    with ci.Context(0, p) as ctx:
+        odd, even = ctx.half_maps(imgs, q)
+        fsc, want = ctx.fsc_combine(odd, even)
+    for name, ref in (("oddtnf", odd), ("evetnf", even)):
+        ih, fh, got = read_tnf(d / name)
+        assert ih[0] == n and ih[1] == p.max_r and ih[2] == 0  # header flag: subrec
+        for k in range(3):
+            assert np.linalg.norm(got[k] - ref[k]) <= 1e-5 * np.linalg.norm(ref[k])
+    rows = np.array([[float(v) for v in line.split()[:2]] for line in open(d / "FSC.txt")])
+    assert np.array_equal(rows[:, 0], np.arange(p.max_r + 1))
+    assert np.abs(rows[:, 1] - fsc).max() < 1e-5
+    m = read_map(d / "fsc.mrc", n)
+    assert np.linalg.norm(m - want) / np.linalg.norm(want) < 1e-5
+    # the header is the particle stack's, as reconstruct_FSC.f90:181 writes it
+    nz = np.frombuffer(open(d / "fsc.mrc", "rb").read(12), np.int32)[2]
+    assert nz == len(imgs)
+    run(["icosprocess", "mode=1", *common, "FSC=y", "subrec=y", f"result3d={d / 'h'}"], cwd=d)
+    ih, fh, got = read_tnf(d / "hevetnf")
+    assert ih[2] == 1
+    assert np.linalg.norm(got[2] - even[2]) <= 1e-5 * np.linalg.norm(even[2])
 
 
 def test_mode0_projections(files):

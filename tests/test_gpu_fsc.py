@@ -1,0 +1,107 @@
+"""Gold-standard half maps and FSC on the GPU (cryoim_rec_begin_half + cryoim_rec_insert +
+cryoim_rec_get_partial, cryoim_fsc_combine) against the oracle's reconstruct_half and
+reconstruct_FSC restatements.
+
+Tolerances: half-map accumulators within 1e-4 relative L2 (FP32 transforms and FP32
+atomics against the FP64 oracle, as for the full reconstruction); from identical tnf
+inputs, FSC within 1e-5 absolute and the weighted map within 1e-5 relative L2.
+"""
+import numpy as np
+import pytest
+
+from _data import small_case
+
+pytestmark = pytest.mark.gpu
+RTOL = 1e-4
+
+
+def _rel(a, b):
+    return float(np.linalg.norm(np.asarray(a, np.float64) - b) / max(np.linalg.norm(b), 1e-30))
+
+
+@pytest.fixture(scope="module")
+def case():
+    return small_case()
+
+
+def test_half_maps_match_oracle(built, orc, case):
+    import cryoim_gb300 as ci
+    p, vol, tmpl, timgs, imgs, parts, truth = case
+    q = parts.copy()
+    q["pr"] = 10.0
+    q["pr"][2] = 95.0  # above PR_threshold: left out of the odd half
+    with ci.Context(0, p) as ctx:
+        odd, even = ctx.half_maps(imgs, q)
+    for parity, got in ((0, odd), (1, even)):
+        want = orc.reconstruct_half(p, imgs, q, parity, "f64")
+        for k in range(3):
+            assert _rel(got[k], want[k]) < RTOL, (parity, k, _rel(got[k], want[k]))
+
+
+def test_half_map_masks_at_the_range_origin(built, orc, case):
+    """Both halves mask at particle(first)'s origin, not at their own first particle."""
+    import cryoim_gb300 as ci
+    p, vol, tmpl, timgs, imgs, parts, truth = case
+    q = parts.copy()
+    q["pr"] = 10.0
+    q["x"][0], q["y"][0] = 9.0, -7.0  # far from particle 2's origin: the mask moves
+    with ci.Context(0, p) as ctx:
+        _, even = ctx.half_maps(imgs, q)
+        ctx.rec_begin_half(q["x"][1], q["y"][1])
+        ctx.rec_insert(imgs[1::2], q[1::2])
+        own = ctx.rec_get_partial()
+    want = orc.reconstruct_half(p, imgs, q, 1, "f64")
+    assert _rel(even[0], want[0]) < RTOL
+    assert _rel(own[0], want[0]) > 10 * RTOL
+
+
+def test_fsc_combine_matches_oracle(built, orc, case):
+    import cryoim_gb300 as ci
+    p, vol, tmpl, timgs, imgs, parts, truth = case
+    q = parts.copy()
+    q["pr"] = 10.0
+    odd = [x.astype(np.float32) for x in orc.reconstruct_half(p, imgs, q, 0, "f64")]
+    even = [x.astype(np.float32) for x in orc.reconstruct_half(p, imgs, q, 1, "f64")]
+    f_orc, m_orc = orc.fsc_combine(p.fftsize, p.max_r, odd, even, "f64")
+    with ci.Context(0, p) as ctx:
+        f_gpu, m_gpu = ctx.fsc_combine(odd, even)
+        f_only, none = ctx.fsc_combine(odd, even, want_map=False)
+    assert none is None and np.array_equal(f_only, f_gpu)
+    assert np.abs(f_gpu - f_orc).max() < 1e-5, np.abs(f_gpu - f_orc).max()
+    assert _rel(m_gpu, m_orc) < 1e-5, _rel(m_gpu, m_orc)
+
+
+def test_fsc_of_identical_halves_is_one_on_gpu(built, case):
+    import cryoim_gb300 as ci
+    p, vol, tmpl, timgs, imgs, parts, truth = case
+    q = parts.copy()
+    q["pr"] = 10.0
+    with ci.Context(0, p) as ctx:
+        odd, _ = ctx.half_maps(imgs, q)
+        f, _ = ctx.fsc_combine(odd, odd, want_map=False)
+    assert np.all(np.abs(f - 1.0) < 1e-6), f
+
+
+def test_half_map_pipeline_end_to_end(built, orc, case):
+    """GPU half maps -> GPU FSC and map against the oracle chain on the same particles."""
+    import cryoim_gb300 as ci
+    p, vol, tmpl, timgs, imgs, parts, truth = case
+    q = parts.copy()
+    q["pr"] = 10.0
+    with ci.Context(0, p) as ctx:
+        odd, even = ctx.half_maps(imgs, q)
+        f_gpu, m_gpu = ctx.fsc_combine(odd, even)
+    o = [x.astype(np.float32) for x in orc.reconstruct_half(p, imgs, q, 0, "f64")]
+    e = [x.astype(np.float32) for x in orc.reconstruct_half(p, imgs, q, 1, "f64")]
+    f_orc, m_orc = orc.fsc_combine(p.fftsize, p.max_r, o, e, "f64")
+    assert np.abs(f_gpu - f_orc).max() < 1e-3
+    assert _rel(m_gpu, m_orc) < RTOL
+
+
+def test_finish_refuses_half_maps(built, case):
+    import cryoim_gb300 as ci
+    p, *_ = case
+    with ci.Context(0, p) as ctx:
+        ctx.rec_begin_half(0.0, 0.0)
+        with pytest.raises(ci.CryoimError):
+            ctx.rec_finish()
