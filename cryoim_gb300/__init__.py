@@ -236,8 +236,9 @@ class Context:
             out.append(self.rec_get_partial())
         return out
 
-    def fsc_combine(self, odd, even, want_map: bool = True):
-        """(FSC per shell 0..maxR, FSC-weighted map or None) from two tnf half maps."""
+    def fsc_combine(self, odd, even, want_map: bool = True, merge: bool = False):
+        """(FSC per shell 0..maxR, FSC-weighted map or None) from two tnf half maps;
+        merge=True follows merge_reconstruct_FSC.f90 instead of reconstruct_FSC.f90."""
         n, R = self.params.fftsize, self.params.max_r
         a = [np.ascontiguousarray(x, np.float32) for x in (*odd, *even)]
         t = 2 * R + 1
@@ -246,9 +247,32 @@ class Context:
                 raise ValueError("tnf arrays must hold (maxR+1)(2maxR+1)^2 floats")
         fsc = np.zeros(R + 1, np.float32)
         out = np.zeros((n, n, n), np.float32) if want_map else None
-        call("cryoim_fsc_combine", self._h, *[ptr(x) for x in a], ptr(fsc),
-             ptr(out) if want_map else None)
+        call("cryoim_merge_fsc_combine" if merge else "cryoim_fsc_combine", self._h,
+             *[ptr(x) for x in a], ptr(fsc), ptr(out) if want_map else None)
         return fsc, out
+
+    def rec_add_partial(self, fa, fb, wg) -> None:
+        """Add a tnf partial (each (maxR+1, 2maxR+1, 2maxR+1)) into the accumulation."""
+        a = [np.ascontiguousarray(x, np.float32) for x in (fa, fb, wg)]
+        R = self.params.max_r
+        if any(x.size != (R + 1) * (2 * R + 1) ** 2 for x in a):
+            raise ValueError("tnf arrays must hold (maxR+1)(2maxR+1)^2 floats")
+        call("cryoim_rec_add_partial", self._h, *[ptr(x) for x in a])
+
+    def rec_finish_merge(self) -> np.ndarray:
+        n = self.params.fftsize
+        out = np.zeros((n, n, n), np.float32)
+        call("cryoim_rec_finish_merge", self._h, ptr(out))
+        return out
+
+    def icosavg(self, map3d, r0: float) -> np.ndarray:
+        """Real-space icosahedral average (img3d_icosavg.f90) of a cubic map."""
+        m = np.array(map3d, np.float32, copy=True, order="C")
+        n = m.shape[0]
+        if m.shape != (n, n, n):
+            raise ValueError("map must be cubic")
+        call("cryoim_icosavg", self._h, ptr(m), n, float(r0))
+        return m
 
     # -- central sections ----------------------------------------------------
     def central_sections(self, ft_re, ft_im, eulers) -> tuple[np.ndarray, np.ndarray]:

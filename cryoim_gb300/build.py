@@ -6,7 +6,8 @@ include/cryoim.h carries no torch types).  Translation units:
 * prep.cu  -- -fmad=false: FP32 expressions round where the Fortran reference rounds;
 * score.cu -- hot scoring kernels, multiply-add contraction allowed;
 * api.cu   -- context, drivers, C ABI (host code built with -ffp-contract=off);
-* fsc.cu   -- -fmad=false: half-map FSC and the FSC-weighted map.
+* fsc.cu   -- -fmad=false: half-map FSC and the FSC-weighted map;
+* mapops.cu -- -fmad=false: real-space icosahedral average, merge output step.
 """
 from __future__ import annotations
 
@@ -47,6 +48,7 @@ UNITS = {
     "gemm_tc.cu": [],
     "contract.cu": [],
     "fsc.cu": ["-fmad=false"],
+    "mapops.cu": ["-fmad=false"],
 }
 
 

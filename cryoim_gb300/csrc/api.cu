@@ -1356,6 +1356,36 @@ int cryoim_prscore(void* ctx, const float* ft_a, const float* ft_b, const float*
     return CRYOIM_OK;
 }
 
+// The end of every map-producing routine, on c->vol (nx^3 complex, filled by a fold):
+// 3D FFT in direction dir (cuFFT unnormalised, as FFTW's backward and Singleton's
+// isn = -1 transforms are), then either shift3dComplex + real part (reconstruct.f90:
+// 246-247) or the masked real part of merge_reconstruct_FSC.f90:190-198 (merge_mask),
+// then the real-space icosahedral average at imgmask when avg is set, into host map.
+static int finish_volume(Ctx* c, int dir, bool merge_mask, bool avg, float* map) {
+    const int nx = c->p.fftsize;
+    const long n3 = (long)nx * nx * nx;
+    cufftHandle h;
+    CKF(cufftPlan3d(&h, nx, nx, nx, CUFFT_C2C));
+    cufftResult fr = cufftSetStream(h, c->stream);
+    if (fr == CUFFT_SUCCESS) fr = cufftExecC2C(h, (cufftComplex*)c->vol.p, (cufftComplex*)c->vol.p, dir);
+    if (fr != CUFFT_SUCCESS) {
+        cufftDestroy(h);
+        return fail(CRYOIM_ERR_CUDA, "3D FFT failed: cufft %d", (int)fr);
+    }
+    DBuf<float> dmap, davg;
+    int r;
+    if ((r = dmap.ensure(n3)) || (avg && (r = davg.ensure(n3)))) { cufftDestroy(h); return r; }
+    cudaError_t e = merge_mask ? launch_merge_real(c->vol.p, nx, c->p.imgmask_px, dmap.p, c->stream)
+                               : (launch_rec_real(c->vol.p, nx, dmap.p, c->stream), cudaGetLastError());
+    if (e == cudaSuccess && avg) e = launch_icosavg(dmap.p, nx, c->p.imgmask_px, c->ops.p, 60, davg.p, c->stream);
+    if (e == cudaSuccess)
+        e = cudaMemcpyAsync(map, avg ? davg.p : dmap.p, sizeof(float) * n3, cudaMemcpyDeviceToHost, c->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+    cufftDestroy(h);
+    if (e != cudaSuccess) return fail(CRYOIM_ERR_CUDA, "map finish: %s", cudaGetErrorString(e));
+    return CRYOIM_OK;
+}
+
 // kind: REC_FULL (reconstruct.f90), REC_SUBSTEP (reconstruct_substep.f90) or REC_HALF
 // (reconstruct_half.f90, mask origin given by the caller).
 static int rec_begin_impl(Ctx* c, int kind, const float* mask_origin) {
@@ -1433,24 +1463,40 @@ int cryoim_rec_finish(void* ctx, float* map) {
     const long n3 = (long)nx * nx * nx;
     if ((r = c->vol.ensure(n3))) return r;
     CK(cudaMemsetAsync(c->vol.p, 0, sizeof(float2) * n3, c->stream));
-    launch_rec_fold(c->acc.p, c->bd, c->vol.p, c->stream);
+    launch_rec_fold(c->acc.p, c->bd, 0, c->vol.p, c->stream);
     CK(cudaGetLastError());
-    cufftHandle h;
-    CKF(cufftPlan3d(&h, nx, nx, nx, CUFFT_C2C));
-    cufftResult fr = cufftSetStream(h, c->stream);
-    if (fr == CUFFT_SUCCESS)
-        fr = cufftExecC2C(h, (cufftComplex*)c->vol.p, (cufftComplex*)c->vol.p, CUFFT_INVERSE);
-    if (fr != CUFFT_SUCCESS) {
-        cufftDestroy(h);
-        return fail(CRYOIM_ERR_CUDA, "3D inverse FFT failed: cufft %d", (int)fr);
-    }
-    DBuf<float> dmap;
-    if ((r = dmap.ensure(n3))) { cufftDestroy(h); return r; }
-    launch_rec_real(c->vol.p, nx, dmap.p, c->stream);
-    cudaError_t e = cudaMemcpyAsync(map, dmap.p, sizeof(float) * n3, cudaMemcpyDeviceToHost, c->stream);
-    if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
-    cufftDestroy(h);
-    if (e != cudaSuccess) return fail(CRYOIM_ERR_CUDA, "finish: %s", cudaGetErrorString(e));
+    // reconstruct.f90:243-255: backward FFT, shift, real part, icosavg if realspaceavg
+    return finish_volume(c, CUFFT_INVERSE, false, c->p.realspaceavg != 0, map);
+}
+
+int cryoim_rec_finish_merge(void* ctx, float* map) {
+    Ctx* c = as_ctx(ctx);
+    int r = check_ready(c, false);
+    if (r) return r;
+    if (!c->rec_active) return fail(CRYOIM_ERR_STATE, "cryoim_rec_begin has not been called");
+    if (!map) return fail(CRYOIM_ERR_ARG, "null map");
+    if (c->rec_kind != REC_FULL) return fail(CRYOIM_ERR_STATE, "merge sums into a full accumulation");
+    const int nx = c->p.fftsize;
+    const long n3 = (long)nx * nx * nx;
+    if ((r = c->vol.ensure(n3))) return r;
+    CK(cudaMemsetAsync(c->vol.p, 0, sizeof(float2) * n3, c->stream));
+    launch_rec_fold(c->acc.p, c->bd, 1, c->vol.p, c->stream);
+    CK(cudaGetLastError());
+    return finish_volume(c, CUFFT_INVERSE, false, false, map);
+}
+
+int cryoim_icosavg(void* ctx, float* map, int32_t n, float r0) {
+    Ctx* c = as_ctx(ctx);
+    int r = check_ready(c, false);
+    if (r) return r;
+    if (!map || n < 2) return fail(CRYOIM_ERR_ARG, "null map or n < 2");
+    const long n3 = (long)n * n * n;
+    DBuf<float> a, b;
+    if ((r = a.ensure(n3)) || (r = b.ensure(n3))) return r;
+    CK(cudaMemcpyAsync(a.p, map, sizeof(float) * n3, cudaMemcpyHostToDevice, c->stream));
+    CK(launch_icosavg(a.p, n, r0, c->ops.p, 60, b.p, c->stream));
+    CK(cudaMemcpyAsync(map, b.p, sizeof(float) * n3, cudaMemcpyDeviceToHost, c->stream));
+    CK(cudaStreamSynchronize(c->stream));
     return CRYOIM_OK;
 }
 
@@ -1492,19 +1538,19 @@ int cryoim_rec_get_partial(void* ctx, float* fa, float* fb, float* wg) {
     return CRYOIM_OK;
 }
 
-int cryoim_fsc_combine(void* ctx, const float* fa1, const float* fb1, const float* wg1, const float* fa2,
-                       const float* fb2, const float* wg2, float* fsc, float* map) {
-    Ctx* c = as_ctx(ctx);
+// reconstruct_FSC.f90:25-187 (merge = false) or merge_reconstruct_FSC.f90:37-198 (merge =
+// true; the same FSC, weighting and fold, a different transform and output step).
+static int fsc_impl(Ctx* c, const float* const src[6], float* fsc, float* map, bool merge) {
     int r = check_ready(c, false);
     if (r) return r;
-    if (!fa1 || !fb1 || !wg1 || !fa2 || !fb2 || !wg2) return fail(CRYOIM_ERR_ARG, "null tnf input");
+    for (int i = 0; i < 6; ++i)
+        if (!src[i]) return fail(CRYOIM_ERR_ARG, "null tnf input");
     const int nx = c->p.fftsize, R = c->p.max_r, t = 2 * R + 1, ns = R + 1;
     const long tnf = (long)ns * t * t, n3 = (long)nx * nx * nx;
     DBuf<float> d;
     DBuf<double> sums;
     DBuf<float> wt;
     if ((r = d.ensure(6 * tnf)) || (r = sums.ensure(3 * ns)) || (r = wt.ensure(ns))) return r;
-    const float* src[6] = {fa1, fb1, wg1, fa2, fb2, wg2};
     for (int i = 0; i < 6; ++i)
         CK(cudaMemcpyAsync(d.p + i * tnf, src[i], sizeof(float) * tnf, cudaMemcpyHostToDevice, c->stream));
     FscArgs a{};
@@ -1527,23 +1573,22 @@ int cryoim_fsc_combine(void* ctx, const float* fa1, const float* fb1, const floa
     CK(cudaMemcpyAsync(wt.p, hw.data(), sizeof(float) * ns, cudaMemcpyHostToDevice, c->stream));
     if ((r = c->vol.ensure(n3))) return r;
     CK(launch_fsc_fold(a, wt.p, c->vol.p, c->stream));
-    cufftHandle h;
-    CKF(cufftPlan3d(&h, nx, nx, nx, CUFFT_C2C));
-    cufftResult fr = cufftSetStream(h, c->stream);
-    if (fr == CUFFT_SUCCESS)
-        fr = cufftExecC2C(h, (cufftComplex*)c->vol.p, (cufftComplex*)c->vol.p, CUFFT_INVERSE);
-    if (fr != CUFFT_SUCCESS) {
-        cufftDestroy(h);
-        return fail(CRYOIM_ERR_CUDA, "3D inverse FFT failed: cufft %d", (int)fr);
-    }
-    DBuf<float> dmap;
-    if ((r = dmap.ensure(n3))) { cufftDestroy(h); return r; }
-    launch_rec_real(c->vol.p, nx, dmap.p, c->stream);
-    cudaError_t e = cudaMemcpyAsync(map, dmap.p, sizeof(float) * n3, cudaMemcpyDeviceToHost, c->stream);
-    if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
-    cufftDestroy(h);
-    if (e != cudaSuccess) return fail(CRYOIM_ERR_CUDA, "fsc combine: %s", cudaGetErrorString(e));
-    return CRYOIM_OK;
+    if (merge)  // merge_reconstruct_FSC.f90:184-198: Singleton isn = -1 transform, masked real part
+        return finish_volume(c, CUFFT_FORWARD, true, false, map);
+    // reconstruct_FSC.f90:177-187: backward FFT, shift, real part, icosavg if realspaceavg
+    return finish_volume(c, CUFFT_INVERSE, false, c->p.realspaceavg != 0, map);
+}
+
+int cryoim_fsc_combine(void* ctx, const float* fa1, const float* fb1, const float* wg1, const float* fa2,
+                       const float* fb2, const float* wg2, float* fsc, float* map) {
+    const float* in[6] = {fa1, fb1, wg1, fa2, fb2, wg2};
+    return fsc_impl(as_ctx(ctx), in, fsc, map, false);
+}
+
+int cryoim_merge_fsc_combine(void* ctx, const float* fa1, const float* fb1, const float* wg1,
+                             const float* fa2, const float* fb2, const float* wg2, float* fsc, float* map) {
+    const float* in[6] = {fa1, fb1, wg1, fa2, fb2, wg2};
+    return fsc_impl(as_ctx(ctx), in, fsc, map, true);
 }
 
 int cryoim_rec_add_partial(void* ctx, const float* fa, const float* fb, const float* wg) {

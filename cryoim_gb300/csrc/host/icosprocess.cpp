@@ -183,7 +183,6 @@ int main(int argc, char** argv) {
     if (sval("sym", "icos") != "icos") return die("only sym=icos is on this path", 2);
     if (has("corrCTF") || has("recISAF") || has("loc_box"))
         return die("corrCTF / recISAF / loc_box modes are not on this path", 2);
-    if (p.realspaceavg && mode == 1) return die("realspaceavg=y is not on this path", 2);
     if (cryoim_params_derive(&p)) return die("parameters", 2);
     if (p.first < 1 || p.last < p.first || p.last > nrows) return die("first/last out of range", 2);
 

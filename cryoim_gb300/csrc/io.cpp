@@ -131,7 +131,11 @@ int cryoim_map_header(cryoim_mrc_header* h, int32_t nx, int32_t ny, int32_t nz, 
     h->alpha = 90; h->beta = 90; h->gamma = 90;
     h->mapc = 1; h->mapr = 2; h->maps = 3;
     h->xorigin = -1.0f * (float)nx; h->yorigin = -1.0f * (float)ny; h->zorigin = -1.0f * (float)nz;
-    std::memcpy(h->map, "MAP ", 4);
+    // mrchead.f90:60-66 assigns 'map ', 'lhr' and 'Hongrong Liu' to arrays of single
+    // characters (0common_icosproc.f90:104-111): every element takes the first letter.
+    std::memset(h->map, 'm', 4);
+    std::memset(h->machinestamp, 'l', 4);
+    std::memset(h->label, 'H', sizeof(h->label));
     return CRYOIM_OK;
 }
 

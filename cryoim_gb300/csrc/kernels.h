@@ -57,7 +57,9 @@ void launch_refine_alpha(const float* cand, int B, const float* tort, int T, con
 void launch_refine_select(const float* cand, const float* pr, int B, float* state,
                           cudaStream_t st);
 // reconstruction finish: fold / divide / sign into the full complex grid
-void launch_rec_fold(const float4* acc, Band bd, float2* vol, cudaStream_t st);
+// int_shell: 0 keeps |h| <= maxR (reconstruct.f90), 1 keeps int(|h|) <= maxR
+// (merge_reconstruct.f90)
+void launch_rec_fold(const float4* acc, Band bd, int int_shell, float2* vol, cudaStream_t st);
 void launch_rec_real(const float2* vol, int nx, float* map, cudaStream_t st);
 // real-space template projection and central sections
 void launch_project(const float* map, int nx, const float* eul, int n, float* out,
@@ -163,5 +165,12 @@ struct FscArgs {
 cudaError_t launch_fsc_shells(const FscArgs& a, double* sums, int sms, cudaStream_t st);
 // wt: maxR+1 shell weights; vol: nx^3 complex, zeroed and filled with cmplx(fa, fb)
 cudaError_t launch_fsc_fold(const FscArgs& a, const float* wt, float2* vol, cudaStream_t st);
+
+// ---- mapops.cu: whole-map real-space operations ------------------------------
+// real-space icosahedral average of an nx^3 map (in != out), radius r0 pixels
+cudaError_t launch_icosavg(const float* in, int nx, float r0, const float* ops, int nsym, float* out,
+                           cudaStream_t st);
+// real part with the (-1)^(x+y+z) origin shift, zero beyond r0 (merge_reconstruct_FSC.f90)
+cudaError_t launch_merge_real(const float2* vol, int nx, float r0, float* map, cudaStream_t st);
 
 }  // namespace cryoim

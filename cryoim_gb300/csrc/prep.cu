@@ -355,7 +355,15 @@ __device__ __forceinline__ long vol_index(int nx, int hx, int ky, int lz) {
 }
 __device__ __forceinline__ float qdiv(float a, float w) { return (float)((double)a / (double)w); }
 
-__global__ void k_rec_fold_plane0(const float4* __restrict__ acc, Band bd, float2* __restrict__ vol) {
+// reconstruct.f90:156-157 keeps |h| <= maxR with a real radius; merge_reconstruct.f90:10,
+// 42 stores the radius in an integer, which keeps int(|h|) <= maxR.
+__device__ __forceinline__ bool in_fold(int d2, int R, int int_shell) {
+    const float dr = sqrtf((float)d2);
+    return int_shell ? (int)dr <= R : dr <= (float)R;
+}
+
+__global__ void k_rec_fold_plane0(const float4* __restrict__ acc, Band bd, int int_shell,
+                                  float2* __restrict__ vol) {
     const int R = bd.max_r, span = 2 * R + 1;
     int q = blockIdx.x * blockDim.x + threadIdx.x;
     int n_a = R * span, n_b = R;
@@ -370,9 +378,8 @@ __global__ void k_rec_fold_plane0(const float4* __restrict__ acc, Band bd, float
     else { ky = 0; hx = 1 + (q - n_a); }
     float4 v1 = acc[acc_index(bd, hx, ky, 0)];
     float4 v2 = acc[acc_index(bd, -hx, -ky, 0)];
-    float dr = sqrtf((float)(hx * hx + ky * ky));
     float fa1 = 0.f, fb1 = 0.f, fa2 = 0.f, fb2 = 0.f;
-    if (dr <= (float)R) {
+    if (in_fold(hx * hx + ky * ky, R, int_shell)) {
         float w = v1.z + v2.z;
         fa1 = qdiv(v1.x + v2.x, w);
         fb1 = qdiv(v1.y - v2.y, w);
@@ -383,7 +390,8 @@ __global__ void k_rec_fold_plane0(const float4* __restrict__ acc, Band bd, float
     vol[vol_index(bd.nx, -hx, -ky, 0)] = make_float2(fa2, -fb2);
 }
 
-__global__ void k_rec_fold_upper(const float4* __restrict__ acc, Band bd, float2* __restrict__ vol) {
+__global__ void k_rec_fold_upper(const float4* __restrict__ acc, Band bd, int int_shell,
+                                 float2* __restrict__ vol) {
     const int R = bd.max_r, span = 2 * R + 1;
     long q = (long)blockIdx.x * blockDim.x + threadIdx.x;
     long total = (long)R * span * span;
@@ -391,9 +399,8 @@ __global__ void k_rec_fold_upper(const float4* __restrict__ acc, Band bd, float2
     int hx = (int)(q % span) - R;
     int ky = (int)((q / span) % span) - R;
     int lz = 1 + (int)(q / ((long)span * span));
-    float dr = sqrtf((float)(hx * hx + ky * ky + lz * lz));
     float fa1 = 0.f, fb1 = 0.f;
-    if (dr <= (float)R) {
+    if (in_fold(hx * hx + ky * ky + lz * lz, R, int_shell)) {
         float4 v = acc[acc_index(bd, hx, ky, lz)];
         fa1 = qdiv(v.x, v.z);
         fb1 = qdiv(v.y, v.z);
@@ -538,12 +545,12 @@ void launch_refine_select(const float* cand, const float* pr, int B, float* stat
     k_refine_select<<<cdiv(B, 64), 64, 0, st>>>(cand, pr, B, state);
 }
 
-void launch_rec_fold(const float4* acc, Band bd, float2* vol, cudaStream_t st) {
+void launch_rec_fold(const float4* acc, Band bd, int int_shell, float2* vol, cudaStream_t st) {
     const int R = bd.max_r, span = 2 * R + 1;
     int n0 = R * span + R + 1;
-    k_rec_fold_plane0<<<cdiv(n0, 256), 256, 0, st>>>(acc, bd, vol);
+    k_rec_fold_plane0<<<cdiv(n0, 256), 256, 0, st>>>(acc, bd, int_shell, vol);
     long n1 = (long)R * span * span;
-    k_rec_fold_upper<<<cdiv(n1, 256), 256, 0, st>>>(acc, bd, vol);
+    k_rec_fold_upper<<<cdiv(n1, 256), 256, 0, st>>>(acc, bd, int_shell, vol);
 }
 
 void launch_rec_real(const float2* vol, int nx, float* map, cudaStream_t st) {

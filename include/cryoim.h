@@ -248,6 +248,26 @@ int cryoim_fsc_combine(void* ctx, const float* fa1, const float* fb1, const floa
                        const float* fa2, const float* fb2, const float* wg2, float* fsc,
                        float* map);
 
+/* The FSC merge of merge_icosprocess_subrec (merge_reconstruct_FSC.f90:37-198): the same
+ * FSC, weighting and fold as cryoim_fsc_combine on the summed odd and even partials, then
+ * the forward-signed transform of that program (Singleton FFT, isn = -1), the
+ * (-1)^(x+y+z) shift and a spherical cut at the imgmask radius (params imgmask_px).
+ * map: nx^3, before that program's output quirks (which its executable applies). */
+int cryoim_merge_fsc_combine(void* ctx, const float* fa1, const float* fb1, const float* wg1,
+                             const float* fa2, const float* fb2, const float* wg2, float* fsc,
+                             float* map);
+
+/* Finish a summed accumulation (cryoim_rec_add_partial) as merge_reconstruct.f90:37-140
+ * does: the Friedel fold keeps int(|h|) <= maxR (its radius is an integer), then the
+ * backward transform and origin shift into map (nx^3). */
+int cryoim_rec_finish_merge(void* ctx, float* map);
+
+/* Real-space icosahedral average (img3d_icosavg.f90:45-123) of the n^3 host map, in place:
+ * voxels with radius > r0 pixels become 0, the others the mean of the map's trilinear
+ * samples at the 60 operators' images.  Also applied by cryoim_rec_finish and
+ * cryoim_fsc_combine when the parameters ask for realspaceavg (r0 = imgmask_px). */
+int cryoim_icosavg(void* ctx, float* map, int32_t n, float r0);
+
 /* ---- files (host only; byte-compatible with the reference) ---------------- */
 
 /* The `mrchead` type of icosprocess/SRC/0common_icosproc.f90:61-112: 1024 bytes. */

@@ -1130,7 +1130,8 @@ int reconstruct_half(const cryoim_params* p, const float* imgs, const cryoim_par
  * fsc_out: R+1 raw FSC values (as written to FSC.txt); map_out: nx^3. */
 template <class R>
 int fsc_combine(int nx, int maxR, const float* fa1, const float* fb1, const float* wg1,
-                const float* fa2, const float* fb2, const float* wg2, R* fsc_out, float* map_out) {
+                const float* fa2, const float* fb2, const float* wg2, R* fsc_out, float* map_out,
+                bool merge = false, R imgmask = R(0)) {
     int t = 2 * maxR + 1, h = nx / 2;
     long tnf = (long)(maxR + 1) * t * t, nn = (long)nx * nx, n3 = nn * nx;
     std::vector<R> a1(tnf), b1(tnf), w1(tnf), a2(tnf), b2(tnf), w2(tnf);
@@ -1198,6 +1199,19 @@ int fsc_combine(int nx, int maxR, const float* fa1, const float* fb1, const floa
                 fa[n2] = fa[n1];
                 fb[n2] = -fb[n1];
             }
+    if (merge) {
+        /* merge_reconstruct_FSC.f90:184-198: Singleton FFT with isn = -1 (exponent sign
+         * negative) along each axis, then (-1)^(x+y+z) inside radius imgmask, 0 outside */
+        fft3d(fa.data(), fb.data(), nx, -1);
+        for (long k = 0; k < n3; ++k) {
+            int lz = (int)(k / nn), ky = (int)((k / nx) % nx), hx = (int)(k % nx);
+            float r = std::sqrt((float)((hx - h) * (hx - h) + (ky - h) * (ky - h) + (lz - h) * (lz - h)));
+            R v = R(0);
+            if (r <= (float)imgmask) v = ((hx + ky + lz) & 1) ? -fa[k] : fa[k];
+            map_out[k] = (float)v;
+        }
+        return 0;
+    }
     /* FFT3d = cmplx(fa, fb) (reconstruct_FSC.f90:173; reconstruct.f90:241 conjugates) */
     fft3d(fa.data(), fb.data(), nx, +1);
     for (long k = 0; k < n3; ++k) {
@@ -1207,6 +1221,108 @@ int fsc_combine(int nx, int maxR, const float* fa1, const float* fb1, const floa
         map_out[k] = (float)v;
     }
     return 0;
+}
+
+/* merge_icosprocess_subrec/SRC/merge_reconstruct.f90:20-140 on the summed tnf partials
+ * (fa, fb, wg in the tnf layout): a (2maxR+1)^3 box with wg = 0.01, the partials in its
+ * lz >= 0 half, the Friedel fold keeping int(|h|) <= maxR (the radius is an integer
+ * there), cmplx(fa, -fb) in the nx^3 cube, backward FFT, shift3dComplex, real part. */
+template <class R>
+int merge_finish(int nx, int maxR, const float* fa0, const float* fb0, const float* wg0, float* map_out) {
+    const int t = 2 * maxR + 1, h = nx / 2;
+    const long tt = (long)t * t, box = tt * t, nn = (long)nx * nx, n3 = nn * nx;
+    std::vector<R> fa(box, R(0)), fb(box, R(0)), wg(box, R(0.01));
+    for (long i = 0; i < tt * (maxR + 1); ++i) {
+        fa[tt * maxR + i] += (R)fa0[i];
+        fb[tt * maxR + i] += (R)fb0[i];
+        wg[tt * maxR + i] += (R)wg0[i];
+    }
+    auto bidx = [&](int hx, int ky, int lz) { return ((long)(lz + maxR) * t + (ky + maxR)) * t + (hx + maxR); };
+    auto inside = [&](int d2) { return fint(std::sqrt((float)d2)) <= maxR; };
+    auto pair0 = [&](int hx, int ky) {
+        long n1 = bidx(hx, ky, 0), n2 = bidx(-hx, -ky, 0);
+        if (inside(hx * hx + ky * ky)) {
+            wg[n1] = wg[n1] + wg[n2];
+            R s = (((hx + ky) % 2 + 2) % 2 == 0) ? R(1) : R(-1);
+            fa[n1] = (fa[n1] + fa[n2]) / wg[n1] * s;
+            fb[n1] = (fb[n1] - fb[n2]) / wg[n1] * s;
+            fa[n2] = fa[n1];
+            fb[n2] = -fb[n1];
+        } else {
+            fa[n1] = fb[n1] = fa[n2] = fb[n2] = R(0);
+        }
+    };
+    for (int ky = 1; ky <= maxR; ++ky)
+        for (int hx = -maxR; hx <= maxR; ++hx) pair0(hx, ky);
+    for (int hx = 1; hx <= maxR; ++hx) pair0(hx, 0);
+    fa[bidx(0, 0, 0)] = fa[bidx(0, 0, 0)] / wg[bidx(0, 0, 0)];
+    fb[bidx(0, 0, 0)] = R(0);
+    for (int lz = 1; lz <= maxR; ++lz)
+        for (int ky = -maxR; ky <= maxR; ++ky)
+            for (int hx = -maxR; hx <= maxR; ++hx) {
+                long n1 = bidx(hx, ky, lz), n2 = bidx(-hx, -ky, -lz);
+                if (inside(hx * hx + ky * ky + lz * lz)) {
+                    R s = (((hx + ky + lz) % 2 + 2) % 2 == 0) ? R(1) : R(-1);
+                    fa[n1] = fa[n1] * s / wg[n1];
+                    fb[n1] = fb[n1] * s / wg[n1];
+                    fa[n2] = fa[n1];
+                    fb[n2] = -fb[n1];
+                } else {
+                    fa[n1] = fb[n1] = fa[n2] = fb[n2] = R(0);
+                }
+            }
+    std::vector<R> va(n3, R(0)), vb(n3, R(0));
+    for (int lz = -maxR; lz <= maxR; ++lz)
+        for (int ky = -maxR; ky <= maxR; ++ky)
+            for (int hx = -maxR; hx <= maxR; ++hx) {
+                long n = (long)(lz + h) * nn + (long)(ky + h) * nx + (hx + h);
+                va[n] = fa[bidx(hx, ky, lz)];
+                vb[n] = -fb[bidx(hx, ky, lz)];
+            }
+    fft3d(va.data(), vb.data(), nx, +1);
+    for (long k = 0; k < n3; ++k) {
+        int lz = (int)(k / nn), ky = (int)((k / nx) % nx), hx = (int)(k % nx);
+        R v = va[k];
+        if ((hx + ky + lz) & 1) v = -v;
+        map_out[k] = (float)v;
+    }
+    return 0;
+}
+
+/* icosprocess/SRC/img3d_icosavg.f90:45-123 (sym = icos): voxels beyond r0 become 0, the
+ * others the mean over the 60 operators of the trilinear sample at S x + nx/2.  Corners
+ * outside the array (r0 beyond nx/2 - 2) count as 0. */
+template <class R> void icosavg(const float* in, int nx, R r0, float* out) {
+    const R* sym = icos_ops<R>();
+    const long nn = (long)nx * nx, n3 = nn * nx;
+    const int h = nx / 2;
+#pragma omp parallel for schedule(static)
+    for (long q = 0; q < n3; ++q) {
+        int hx = (int)(q % nx) - h, ky = (int)((q / nx) % nx) - h, lz = (int)(q / nn) - h;
+        R r = std::sqrt((R)(hx * hx + ky * ky + lz * lz));
+        if (r > r0) { out[q] = 0.0f; continue; }
+        R x0[3] = {(R)hx, (R)ky, (R)lz}, acc = R(0);
+        for (int s = 0; s < 60; ++s) {
+            R x[3];
+            mv3(sym + 9 * s, x0, x);
+            for (int i = 0; i < 3; ++i) x[i] = x[i] + (R)h;
+            int ix = fint(x[0]), iy = fint(x[1]), iz = fint(x[2]);
+            R ax = x[0] - (R)ix, ay = x[1] - (R)iy, az = x[2] - (R)iz;
+            long n1 = (long)iz * nn + (long)iy * nx + ix;
+            long nb[8] = {n1, n1 + 1, n1 + nx, n1 + nx + 1, n1 + nn, n1 + nn + 1, n1 + nn + nx, n1 + nn + nx + 1};
+            R v[8];
+            for (int j = 0; j < 8; ++j) v[j] = (nb[j] >= 0 && nb[j] < n3) ? (R)in[nb[j]] : R(0);
+            acc = acc + (R(1) - ax) * (R(1) - ay) * (R(1) - az) * v[0];
+            acc = acc + (ax) * (R(1) - ay) * (R(1) - az) * v[1];
+            acc = acc + (R(1) - ax) * (ay) * (R(1) - az) * v[2];
+            acc = acc + (ax) * (ay) * (R(1) - az) * v[3];
+            acc = acc + (R(1) - ax) * (R(1) - ay) * (az) * v[4];
+            acc = acc + (ax) * (R(1) - ay) * (az) * v[5];
+            acc = acc + (R(1) - ax) * (ay) * (az) * v[6];
+            acc = acc + (ax) * (ay) * (az) * v[7];
+        }
+        out[q] = (float)(acc / R(60));
+    }
 }
 
 /* ------------------------------------------------------------------------ */
@@ -1341,6 +1457,18 @@ template <class R> void transform_ort(int to, R* th, R* ph, R* om, int n) {
                                         const float* w1, const float* a2, const float* b2,             \
                                         const float* w2, R* fsc, float* map) {                         \
         return fsc_combine<R>(nx, maxR, a1, b1, w1, a2, b2, w2, fsc, map);                             \
+    }                                                                                                  \
+    extern "C" int orc_merge_fsc_##S(int nx, int maxR, const float* a1, const float* b1,             \
+                                      const float* w1, const float* a2, const float* b2,               \
+                                      const float* w2, R imgmask, R* fsc, float* map) {                \
+        return fsc_combine<R>(nx, maxR, a1, b1, w1, a2, b2, w2, fsc, map, true, imgmask);              \
+    }                                                                                                  \
+    extern "C" int orc_merge_finish_##S(int nx, int maxR, const float* a, const float* b,            \
+                                         const float* w, float* map) {                                 \
+        return merge_finish<R>(nx, maxR, a, b, w, map);                                                \
+    }                                                                                                  \
+    extern "C" void orc_icosavg_##S(const float* in, int nx, R r0, float* out) {                     \
+        icosavg<R>(in, nx, r0, out);                                                                   \
     }                                                                                                  \
     extern "C" void orc_equalort_##S(R th, R ph, R om, R* out) { equalort<R>(th, ph, om, out); }      \
     extern "C" void orc_transform_ort_##S(int to, R* th, R* ph, R* om, int n) {                      \

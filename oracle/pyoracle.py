@@ -294,6 +294,33 @@ def fsc_combine(nx, max_r, odd, even, fp="f64"):
     return fsc, out
 
 
+def merge_fsc(nx, max_r, odd, even, imgmask, fp="f64"):
+    """merge_reconstruct_FSC.f90: (FSC per shell, nx^3 map before the output quirks)."""
+    a = [np.ascontiguousarray(x, np.float32) for x in (*odd, *even)]
+    fsc = np.zeros(max_r + 1, _dt(fp))
+    out = np.zeros((nx, nx, nx), np.float32)
+    r = _fn("merge_fsc", fp)(C.c_int(nx), C.c_int(max_r), *[_p(x) for x in a], _R(fp)(imgmask),
+                             _p(fsc), _p(out))
+    assert r == 0
+    return fsc, out
+
+
+def merge_finish(nx, max_r, part, fp="f64"):
+    """merge_reconstruct.f90:20-140 on a summed tnf partial (fa, fb, wg): the nx^3 map."""
+    a = [np.ascontiguousarray(x, np.float32) for x in part]
+    out = np.zeros((nx, nx, nx), np.float32)
+    assert _fn("merge_finish", fp)(C.c_int(nx), C.c_int(max_r), *[_p(x) for x in a], _p(out)) == 0
+    return out
+
+
+def icosavg(map3d, r0, fp="f64"):
+    """img3d_icosavg.f90: real-space icosahedral average of a cubic map."""
+    m = np.ascontiguousarray(map3d, np.float32)
+    out = np.zeros_like(m)
+    _fn("icosavg", fp)(_p(m), C.c_int(m.shape[0]), _R(fp)(r0), _p(out))
+    return out
+
+
 def equalort(theta, phi, omega, fp="f32"):
     out = np.zeros((60, 3), _dt(fp))
     R = _R(fp)

@@ -146,8 +146,21 @@ def test_mode1_and_subrec_merge(files):
     run(["icosprocess", "mode=1", *c0, "subrec=y", f"result3d={d / 'all.tnf'}"])
     run(["merge_icosprocess_subrec", str(d / "a.tnf"), str(d / "b.tnf"), str(d / "m2.mrc")])
     run(["merge_icosprocess_subrec", str(d / "all.tnf"), str(d / "m1.mrc")])
-    m1, m2 = read_map(d / "m1.mrc", n), read_map(d / "m2.mrc", n)
+    # merge_reconstruct.f90 writes the central (n-8)^3 box under an (n-8) header
+    m1, m2 = read_map(d / "m1.mrc", n - 8), read_map(d / "m2.mrc", n - 8)
     assert np.linalg.norm(m1 - m2) / np.linalg.norm(m1) < 1e-4
+    assert tuple(np.frombuffer(open(d / "m1.mrc", "rb").read(12), np.int32)) == (n - 8,) * 3
+    # the crop, with its index: voxel i (1-based) from section i // (n-8)^2 + 4
+    ih, fh, part = read_tnf(d / "all.tnf")
+    with ci.Context(0, p) as ctx:
+        ctx.rec_begin()
+        ctx.rec_add_partial(*part)
+        full = ctx.rec_finish_merge()
+    m = n - 8
+    i = np.arange(1, m ** 3 + 1)
+    lz, ky, hx = i // (m * m) + 4, (i - 1) % (m * m) // m + 4, (i - 1) % (m * m) % m + 4
+    want = full[lz, ky, hx].reshape(m, m, m)
+    assert np.linalg.norm(m1 - want) <= 1e-5 * np.linalg.norm(want)
 
 
 def test_mode1_fsc_half_maps(files):
@@ -179,6 +192,19 @@ def test_mode1_fsc_half_maps(files):
     ih, fh, got = read_tnf(d / "hevetnf")
     assert ih[2] == 1
     assert np.linalg.norm(got[2] - even[2]) <= 1e-5 * np.linalg.norm(even[2])
+    # merge_icosprocess_subrec on the prefix: header flag 1 -> merge_reconstruct_FSC.f90
+    os.remove(d / "FSC.txt")
+    run(["merge_icosprocess_subrec", "h", "mfsc.mrc"], cwd=d)
+    rows = np.array([[float(v) for v in line.split()[:2]] for line in open(d / "FSC.txt")])
+    assert np.abs(rows[:, 1] - fsc).max() < 1e-5
+    with ci.Context(0, p) as ctx:
+        fm, full = ctx.fsc_combine(odd, even, merge=True)
+    m = n - 8
+    raw = open(d / "mfsc.mrc", "rb").read()
+    assert tuple(np.frombuffer(raw[:12], np.int32)) == (m, m, m)
+    got = np.frombuffer(raw[1024:], np.float32)
+    want = full.ravel()[:m ** 3]  # the routine writes the first (n-8)^3 values of its n^3 array
+    assert np.linalg.norm(got - want) <= 1e-5 * np.linalg.norm(want)
 
 
 def test_mode0_projections(files):

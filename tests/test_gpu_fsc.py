@@ -105,3 +105,57 @@ def test_finish_refuses_half_maps(built, case):
         ctx.rec_begin_half(0.0, 0.0)
         with pytest.raises(ci.CryoimError):
             ctx.rec_finish()
+
+
+def test_icosavg_matches_oracle(built, orc, case):
+    import cryoim_gb300 as ci
+    p, vol, *_ = case
+    r0 = p.imgmask_px
+    with ci.Context(0, p) as ctx:
+        got = ctx.icosavg(vol, r0)
+    want = orc.icosavg(vol, r0, "f64")
+    assert _rel(got, want) < 1e-5, _rel(got, want)
+    assert np.all(got[np.abs(want) == 0] == 0)
+
+
+def test_finish_applies_realspaceavg(built, orc, case):
+    """realspaceavg=y: reconstruct.f90:253-255 and reconstruct_FSC.f90:185-187 average the
+    map in real space before writing it."""
+    import cryoim_gb300 as ci
+    p, vol, tmpl, timgs, imgs, parts, truth = case
+    q = parts.copy()
+    q["pr"] = 10.0
+    pa = ci.Params.from_buffer_copy(p)
+    pa.realspaceavg = 1
+    with ci.Context(0, pa) as ctx:
+        ctx.rec_begin()
+        ctx.rec_insert(imgs, q)
+        m = ctx.rec_finish()
+        odd, even = ctx.half_maps(imgs, q)
+        _, mf = ctx.fsc_combine(odd, even)
+    want = orc.icosavg(orc.reconstruct(p, imgs, q, fp="f64"), p.imgmask_px, "f64")
+    assert _rel(m, want) < RTOL, _rel(m, want)
+    with ci.Context(0, p) as ctx:
+        _, plain = ctx.fsc_combine(odd, even)
+    assert _rel(mf, orc.icosavg(plain, p.imgmask_px, "f64")) < 1e-5
+
+
+def test_merge_finish_and_merge_fsc_match_oracle(built, orc, case):
+    import cryoim_gb300 as ci
+    p, vol, tmpl, timgs, imgs, parts, truth = case
+    q = parts.copy()
+    q["pr"] = 10.0
+    odd = [x.astype(np.float32) for x in orc.reconstruct_half(p, imgs, q, 0, "f64")]
+    even = [x.astype(np.float32) for x in orc.reconstruct_half(p, imgs, q, 1, "f64")]
+    total = [a + b for a, b in zip(odd, even)]
+    with ci.Context(0, p) as ctx:
+        ctx.rec_begin()
+        ctx.rec_add_partial(*odd)
+        ctx.rec_add_partial(*even)
+        m = ctx.rec_finish_merge()
+        f, mf = ctx.fsc_combine(odd, even, merge=True)
+    want = orc.merge_finish(p.fftsize, p.max_r, total, "f64")
+    assert _rel(m, want) < 1e-5, _rel(m, want)
+    f_orc, mf_orc = orc.merge_fsc(p.fftsize, p.max_r, odd, even, p.imgmask_px, "f64")
+    assert np.abs(f - f_orc).max() < 1e-5
+    assert _rel(mf, mf_orc) < 1e-5, _rel(mf, mf_orc)

@@ -53,6 +53,10 @@ def test_mrc_round_trip_and_header_layout(built, tmp_path):
     assert (nx, ny, nz, mode) == (12, 16, 3, 2)
     assert struct.unpack("<3i", raw[16:28]) == (-6, -8, -1)          # n*start = -n/2 (mrchead.f90:17-19)
     assert struct.unpack("<f", raw[28 + 12:28 + 16])[0] == np.float32(11 * 1.5)  # a = mx * apix
+    # map(4), machinestamp(4), label(10,80) are arrays of single characters: the strings
+    # assigned in mrchead.f90:60-66 leave their first letter in every element
+    assert raw[208:216] == b"mmmmllll" and raw[224:1024] == b"H" * 800
+    assert struct.unpack("<3f", raw[196:208]) == (-12.0, -16.0, -3.0)  # x/y/zorigin = -n
     out = np.zeros((2, 16, 12), np.float32)
     assert L.cryoim_mrc_read_sections(str(p).encode(), 2, 2, out.ctypes.data) == 0
     assert np.array_equal(out, data[1:])

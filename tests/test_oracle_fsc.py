@@ -1,6 +1,8 @@
-"""Oracle restatement of the gold-standard half maps and FSC (reconstruct_half.f90,
-reconstruct_FSC.f90), checked against the full reconstruction and an independent numpy
-restatement of the FSC weighting, Friedel fold and inverse transform."""
+"""Oracle restatements of the map-side routines: gold-standard half maps and FSC
+(reconstruct_half.f90, reconstruct_FSC.f90), the merges of merge_icosprocess_subrec
+(merge_reconstruct.f90, merge_reconstruct_FSC.f90) and the real-space icosahedral average
+(img3d_icosavg.f90), checked against the full reconstruction, independent numpy
+restatements and symmetry properties."""
 import numpy as np
 import pytest
 
@@ -134,3 +136,88 @@ def test_half_map_fsc_of_noiseless_projections(orc):
     fsc, m = orc.fsc_combine(p.fftsize, p.max_r, odd, even, "f64")
     assert fsc[1:4].min() > 0.8, fsc
     assert np.isfinite(m).all()
+
+
+def icosavg_numpy(m, r0, ops):
+    """img3d_icosavg.f90:45-123 with whole-array numpy operations (FP64)."""
+    n = m.shape[0]
+    h = n // 2
+    flat = m.astype(np.float64).ravel()
+    lz, ky, hx = np.meshgrid(*(np.arange(n) - h,) * 3, indexing="ij")
+    x0 = np.stack([hx, ky, lz], -1).reshape(-1, 3).astype(np.float64)
+    inside = np.sqrt((x0 ** 2).sum(1)) <= r0
+    acc = np.zeros(len(x0))
+    nn = n * n
+    for S in ops.astype(np.float64):
+        x = x0 @ S.T + h
+        i = np.trunc(x).astype(np.int64)
+        a = x - i
+        base = i[:, 2] * nn + i[:, 1] * n + i[:, 0]
+        for dz in (0, 1):
+            for dy in (0, 1):
+                for dx in (0, 1):
+                    idx = base + dz * nn + dy * n + dx
+                    ok = (idx >= 0) & (idx < flat.size)
+                    v = np.where(ok, flat[np.clip(idx, 0, flat.size - 1)], 0.0)
+                    w = ((a[:, 0] if dx else 1 - a[:, 0]) * (a[:, 1] if dy else 1 - a[:, 1])
+                         * (a[:, 2] if dz else 1 - a[:, 2]))
+                    acc += w * v
+    return np.where(inside, acc / 60.0, 0.0).reshape(n, n, n)
+
+
+def test_icosavg_matches_numpy_and_is_symmetric(orc, golden_ops):
+    rng = np.random.default_rng(11)
+    n = 16
+    m = rng.normal(size=(n, n, n)).astype(np.float32)
+    r0 = n / 2 - 2
+    out = orc.icosavg(m, r0, "f64")
+    ref = icosavg_numpy(m, r0, golden_ops)
+    assert np.abs(out - ref).max() < 1e-6 * np.abs(ref).max()
+    out32 = orc.icosavg(m, r0, "f32")
+    assert np.abs(out32 - out).max() < 1e-5 * np.abs(out).max()
+    # the 2-fold frame has 2-fold axes on x, y and z: (x, y, z) -> (-x, -y, z) maps grid
+    # points to grid points, so the average is invariant under it (up to summation order)
+    h = n // 2
+    a = out[:, 1:, 1:]
+    b = out[:, 1:, 1:][:, ::-1, ::-1]
+    assert np.abs(a - b).max() < 1e-6 * np.abs(out).max()
+    # a constant map stays constant where no sample leaves the map
+    c = orc.icosavg(np.full((n, n, n), 2.5, np.float32), r0, "f64")
+    lz, ky, hx = np.meshgrid(*(np.arange(n) - h,) * 3, indexing="ij")
+    r = np.sqrt(hx ** 2 + ky ** 2 + lz ** 2)
+    assert np.abs(c[r <= r0] - 2.5).max() < 1e-6 and np.all(c[r > r0] == 0)
+
+
+def test_merge_finish_equals_reconstruct_for_band_limited_partials(orc):
+    """merge_reconstruct.f90 on the tnf view of reconstruct.f90's accumulator (weights less
+    the 0.01 start, nothing beyond maxR) gives reconstruct.f90's map."""
+    p, vol, tmpl, timgs, imgs, parts, truth = small_case(n=32, P=3, min_res=40.0, max_res=10.0, apix=4.0)
+    q = parts.copy()
+    q["pr"] = 10.0
+    R, h = p.max_r, p.fftsize // 2
+    m_rec, acc = orc.reconstruct(p, imgs, q, want_acc=True, fp="f64")
+    box = acc[:, h:h + R + 1, h - R:h + R + 1, h - R:h + R + 1].copy()
+    box[2] -= 0.01
+    lz, ky, hx = np.meshgrid(np.arange(R + 1), np.arange(-R, R + 1), np.arange(-R, R + 1), indexing="ij")
+    far = np.sqrt(hx ** 2 + ky ** 2 + lz ** 2) > R
+    box[:, far] = 0.0
+    m = orc.merge_finish(p.fftsize, R, [x.astype(np.float32) for x in box], "f64")
+    assert np.linalg.norm(m - m_rec) < 1e-5 * np.linalg.norm(m_rec)
+
+
+def test_merge_fsc_is_the_uninverted_masked_fsc_map(orc):
+    """merge_reconstruct_FSC.f90 transforms with the opposite exponent sign to
+    reconstruct_FSC.f90 (its map is not point-inverted) and cuts at imgmask."""
+    rng = np.random.default_rng(4)
+    R, nx, r0 = 5, 16, 5.5
+    odd = _random_tnf(rng, R)
+    even = _random_tnf(rng, R)
+    f1, m1 = orc.fsc_combine(nx, R, odd, even, "f64")
+    f2, m2 = orc.merge_fsc(nx, R, odd, even, r0, "f64")
+    assert np.array_equal(f1, f2)
+    inv = np.roll(m1[::-1, ::-1, ::-1], 1, axis=(0, 1, 2))
+    h = nx // 2
+    lz, ky, hx = np.meshgrid(*(np.arange(nx) - h,) * 3, indexing="ij")
+    inside = np.sqrt((hx ** 2 + ky ** 2 + lz ** 2).astype(np.float32)) <= r0
+    assert np.abs(m2[inside] - inv[inside]).max() < 1e-9 * np.abs(inv).max()
+    assert np.all(m2[~inside] == 0)
