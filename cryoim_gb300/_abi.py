@@ -48,7 +48,7 @@ class Params(C.Structure):
 class ContractOpts(C.Structure):
     """cryoim_contract_opts (include/cryoim.h)."""
     _fields_ = [("origin_max", C.c_float), ("origin_step", C.c_float), ("topk", C.c_int32),
-                ("pick", C.c_int32)]
+                ("pick", C.c_int32), ("precision", C.c_int32)]
 
 
 _vp, _fp, _ip, _i32, _f32 = C.c_void_p, C.POINTER(C.c_float), C.POINTER(C.c_int32), C.c_int32, C.c_float
@@ -81,6 +81,7 @@ SIGNATURES = {
     "cryoim_prscore_noalloc": [_i32, _i32, _i32, _vp, _vp, _vp, _vp, _vp, _vp, _i32, _vp, _i32,
                                _vp, _vp],
     "cryoim_gemm_bf16_argmax": [_vp, _vp, _i32, _i32, _i32, _vp, _vp, _vp, _vp, _vp],
+    "cryoim_gemm_e4m3_argmax": [_vp, _vp, _i32, _i32, _i32, _vp, _vp, _vp, _vp, _vp],
     "cryoim_set_reference_map": [_vp, _vp],
     "cryoim_contract_search": [_vp, _vp, _vp, _i32, _op, _vp],
     "cryoim_contract_search_device": [_vp, _vp, _vp, _i32, _op, _vp],

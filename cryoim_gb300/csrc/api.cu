@@ -223,6 +223,15 @@ struct Ctx {
     bool bmat_ready = false;
     double bmat_ms = 0.0;
     DBuf<uint16_t> amat;
+    // FP8-e4m3 operands: B8 (n_orient x cKpad8 bytes), per-sample band scales, A8
+    DBuf<uint8_t> bmat8, amat8;
+    bool bmat8_ready = false;
+    double bmat8_ms = 0.0;
+    int cKpad8 = 0, last_kpad = 0;
+    double last_slice_ms = 0.0;
+    DBuf<float> mulA, mulB;
+    DBuf<unsigned> bandmax;
+    DBuf<int> fexp;
     DBuf<float> corigins, topv, kcc, kcand, kpr;
     DBuf<int> topi, gerr, kor, korig;
     DBuf<double> pnorm, kcc64;
@@ -252,7 +261,8 @@ struct Ctx {
         topv.release(); kcc.release(); kcand.release(); kpr.release(); topi.release(); gerr.release();
         kor.release(); korig.release(); pnorm.release(); kcc64.release(); kalpha.release();
         tilev.release(); xcand.release(); xpr.release(); tileo.release(); tileorig.release();
-        xalpha.release();
+        xalpha.release(); bmat8.release(); amat8.release(); mulA.release(); mulB.release();
+        bandmax.release(); fexp.release();
         if (pe0) cudaEventDestroy(pe0);
         if (pe1) cudaEventDestroy(pe1);
         if (own_stream && stream) cudaStreamDestroy(stream);
@@ -692,6 +702,7 @@ int ensure_samples(Ctx* c) {
     CK(cudaMemcpyAsync(c->csamples.p, s.data(), sizeof(int2) * s.size(), cudaMemcpyHostToDevice, c->stream));
     c->cS = (int)s.size();
     c->cKpad = (2 * c->cS + 63) / 64 * 64;
+    c->cKpad8 = (2 * c->cS + 127) / 128 * 128;
     return CRYOIM_OK;
 }
 
@@ -725,6 +736,56 @@ int ensure_bmat(Ctx* c) {
     return CRYOIM_OK;
 }
 
+// FP8-e4m3 copy of operand B with per-band power-of-two scales (contract.cu explains the
+// scaling): band maxima of the BF16 rows (every 4th orientation), e_b = floor(log2(224 /
+// max_b)), mulB = 2^e_b and mulA = 2^-e_b per sample, then the conversion.
+int ensure_bmat8(Ctx* c) {
+    int r;
+    if ((r = ensure_bmat(c))) return r;
+    if (c->bmat8_ready) return CRYOIM_OK;
+    const int S = c->cS, nband = c->p.max_r + 2;
+    const long n = c->n_orient;
+    if ((r = c->bmat8.ensure((size_t)n * c->cKpad8)) || (r = c->bandmax.ensure(nband)) ||
+        (r = c->mulA.ensure(S)) || (r = c->mulB.ensure(S)))
+        return r;
+    if (c->num_sms == 0) CK(cudaDeviceGetAttribute(&c->num_sms, cudaDevAttrMultiProcessorCount, c->device));
+    cudaEvent_t e0, e1;
+    CK(cudaEventCreate(&e0));
+    CK(cudaEventCreate(&e1));
+    CK(cudaEventRecord(e0, c->stream));
+    CK(launch_band_absmax(c->bmat.p, n, c->cKpad, c->csamples.p, S, nband, 4, c->bandmax.p, c->num_sms,
+                          c->stream));
+    std::vector<unsigned> hm(nband);
+    std::vector<int2> hs(S);
+    CK(cudaMemcpyAsync(hm.data(), c->bandmax.p, sizeof(unsigned) * nband, cudaMemcpyDeviceToHost, c->stream));
+    CK(cudaMemcpyAsync(hs.data(), c->csamples.p, sizeof(int2) * S, cudaMemcpyDeviceToHost, c->stream));
+    CK(cudaStreamSynchronize(c->stream));
+    std::vector<int> eb(nband, 0);
+    for (int b = 0; b < nband; ++b) {
+        float m;
+        std::memcpy(&m, &hm[b], 4);
+        if (m > 0.0f) eb[b] = std::max(-30, std::min(30, (int)std::floor(std::log2(224.0f / m))));
+    }
+    std::vector<float> ma(S), mb(S);
+    for (int i = 0; i < S; ++i) {
+        const int b = std::min(nband - 1, (int)std::sqrt((float)(hs[i].x * hs[i].x + hs[i].y * hs[i].y)));
+        mb[i] = std::ldexp(1.0f, eb[b]);
+        ma[i] = std::ldexp(1.0f, -eb[b]);
+    }
+    CK(cudaMemcpyAsync(c->mulA.p, ma.data(), sizeof(float) * S, cudaMemcpyHostToDevice, c->stream));
+    CK(cudaMemcpyAsync(c->mulB.p, mb.data(), sizeof(float) * S, cudaMemcpyHostToDevice, c->stream));
+    CK(launch_b_to_e4m3(c->bmat.p, n, c->cKpad, S, c->mulB.p, c->cKpad8, c->bmat8.p, c->stream));
+    CK(cudaEventRecord(e1, c->stream));
+    CK(cudaEventSynchronize(e1));
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, e0, e1);
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    c->bmat8_ms = ms;
+    c->bmat8_ready = true;
+    return CRYOIM_OK;
+}
+
 int contract_impl(Ctx* c, const float* imgs, bool on_device, cryoim_particle* parts, int P,
                   const cryoim_contract_opts* opts, float* cands) {
     int r = check_ready(c, false);
@@ -736,8 +797,13 @@ int contract_impl(Ctx* c, const float* imgs, bool on_device, cryoim_particle* pa
     if (!(opts->origin_step > 0) || opts->origin_max < 0) return fail(CRYOIM_ERR_ARG, "bad origin grid");
     if (opts->pick == 0 && c->T <= 0)
         return fail(CRYOIM_ERR_STATE, "PR rescoring needs cryoim_load_templates");
+    if (opts->precision != 0 && opts->precision != 1) return fail(CRYOIM_ERR_ARG, "precision must be 0 or 1");
+    const bool f8 = opts->precision == 1;
     if (P == 0) return CRYOIM_OK;
-    if ((r = ensure_bmat(c))) return r;
+    if ((r = f8 ? ensure_bmat8(c) : ensure_bmat(c))) return r;
+    const int kpad = f8 ? c->cKpad8 : c->cKpad;
+    c->last_kpad = kpad;
+    c->last_slice_ms = c->bmat_ms + (f8 ? c->bmat8_ms : 0.0);
     if (c->n_orient > 0x7fffffffL) return fail(CRYOIM_ERR_SIZE, "too many orientations");
     // origin grid
     if (opts->origin_max != c->orig_max || opts->origin_step != c->orig_step) {
@@ -761,7 +827,9 @@ int contract_impl(Ctx* c, const float* imgs, bool on_device, cryoim_particle* pa
     const int pb = std::max(1, std::min(c->batch, 2400 / std::max(O, 1)));
     const int ntiles = (int)((c->n_orient + gemm_tile_n() - 1) / gemm_tile_n());
     if ((r = ensure_batch(c, pb))) return r;
-    if ((r = c->amat.ensure((size_t)pb * O * c->cKpad))) return r;
+    if (f8 ? ((r = c->amat8.ensure((size_t)pb * O * c->cKpad8)) || (r = c->fexp.ensure(pb)))
+           : (r = c->amat.ensure((size_t)pb * O * c->cKpad)))
+        return r;
     if ((r = c->topv.ensure((size_t)pb * O * ntiles)) || (r = c->topi.ensure((size_t)pb * O * ntiles))) return r;
     if ((r = c->gerr.ensure(1)) || (r = c->pnorm.ensure(pb)) || (r = c->kor.ensure((size_t)pb * k)) ||
         (r = c->korig.ensure((size_t)pb * k)) || (r = c->kcc.ensure((size_t)pb * k)) ||
@@ -828,8 +896,12 @@ int contract_impl(Ctx* c, const float* imgs, bool on_device, cryoim_particle* pa
             }
         }
         launch_particle_norm(c->band.p, ctfp, c->bd, c->csamples.p, c->cS, nb, c->pnorm.p, c->stream);
-        launch_build_a(c->band.p, ctfp, c->bd, c->csamples.p, c->cS, c->cKpad, c->corigins.p, O, c->pnorm.p,
-                       nb, c->amat.p, c->stream);
+        if (f8)
+            launch_build_a8(c->band.p, ctfp, c->bd, c->csamples.p, c->cS, c->cKpad8, c->corigins.p, O,
+                            c->pnorm.p, c->mulA.p, c->fexp.p, nb, c->amat8.p, c->stream);
+        else
+            launch_build_a(c->band.p, ctfp, c->bd, c->csamples.p, c->cS, c->cKpad, c->corigins.p, O, c->pnorm.p,
+                           nb, c->amat.p, c->stream);
         CK(cudaGetLastError());
         GemmArgmaxArgs g{};
         g.topv = c->topv.p;
@@ -838,8 +910,12 @@ int contract_impl(Ctx* c, const float* imgs, bool on_device, cryoim_particle* pa
         g.err = c->gerr.p;
         CK(cudaMemsetAsync(c->gerr.p, 0, sizeof(int), c->stream));
         if (c->prof) CK(cudaEventRecord(g0, c->stream));
-        CK(launch_gemm_bf16_argmax(c->amat.p, c->bmat.p, nb * O, (int)c->n_orient, c->cKpad, g, c->num_sms,
-                                   c->stream));
+        if (f8)
+            CK(launch_gemm_argmax(c->amat8.p, c->bmat8.p, nb * O, (int)c->n_orient, kpad, true, g, c->num_sms,
+                                  c->stream));
+        else
+            CK(launch_gemm_argmax(c->amat.p, c->bmat.p, nb * O, (int)c->n_orient, kpad, false, g, c->num_sms,
+                                  c->stream));
         if (c->prof) CK(cudaEventRecord(g1, c->stream));
         launch_select_topk(c->topv.p, c->topi.p, O, ntiles, k, nb, c->tilev.p, c->tileo.p, c->tileorig.p,
                            c->kor.p, c->korig.p, c->kcc.p, c->stream);
@@ -849,14 +925,18 @@ int contract_impl(Ctx* c, const float* imgs, bool on_device, cryoim_particle* pa
         CK(cudaMemcpyAsync(hor.data(), c->kor.p, sizeof(int) * nb * k, cudaMemcpyDeviceToHost, c->stream));
         CK(cudaMemcpyAsync(horig.data(), c->korig.p, sizeof(int) * nb * k, cudaMemcpyDeviceToHost, c->stream));
         CK(cudaMemcpyAsync(hcc.data(), c->kcc.p, sizeof(float) * nb * k, cudaMemcpyDeviceToHost, c->stream));
+        std::vector<int> hfe(nb, 0);
+        if (f8) CK(cudaMemcpyAsync(hfe.data(), c->fexp.p, sizeof(int) * nb, cudaMemcpyDeviceToHost, c->stream));
         if ((r = check_flag(c))) return r;
         if (gerr) return fail(CRYOIM_ERR_CUDA, "contraction pipeline wait timed out");
+        if (f8)  // remove the per-particle exponent: the CC of the unit-norm rows
+            for (int i = 0; i < nb * k; ++i) hcc[i] = std::ldexp(hcc[i], -hfe[i / k]);
         if (c->prof) {
             float ms = 0.f;
             CK(cudaEventElapsedTime(&ms, g0, g1));
             c->prof_gemm_ms += ms;
             c->prof_gemm_launches += 1;
-            c->prof_gemm_flops += 2.0 * (double)nb * O * (double)c->n_orient * (double)c->cKpad;
+            c->prof_gemm_flops += 2.0 * (double)nb * O * (double)c->n_orient * (double)kpad;
         }
         // candidates (theta, phi, omega, x, y) of the selected (orientation, origin) pairs
         for (int i = 0; i < nb * k; ++i) {
@@ -1136,10 +1216,12 @@ int cryoim_set_params(void* ctx, const cryoim_params* p) {
         c->map_ready = false;
         c->cS = 0;
         c->bmat_ready = false;
+        c->bmat8_ready = false;
     }
     if (step_changed) {
         c->grid_ready = false;
         c->bmat_ready = false;
+        c->bmat8_ready = false;
     }
     long nn = (long)p->fftsize * p->fftsize;
     c->batch = (int)std::max(1L, std::min(64L, (long)(16L * 1024 * 1024) / nn));
@@ -1668,6 +1750,7 @@ int cryoim_set_reference_map(void* ctx, const float* map3d) {
     if (e != cudaSuccess) return fail(CRYOIM_ERR_CUDA, "reference map: %s", cudaGetErrorString(e));
     c->map_ready = true;
     c->bmat_ready = false;
+    c->bmat8_ready = false;
     return CRYOIM_OK;
 }
 
@@ -1688,12 +1771,12 @@ int cryoim_contract_stats(void* ctx, double* out /* 6 */) {
     if (c->map_ready && c->have_params && c->T >= 0) {
         if ((r = ensure_grid(c)) || (r = ensure_samples(c))) return r;
     }
-    out[0] = c->bmat_ms;
+    out[0] = c->last_slice_ms > 0.0 ? c->last_slice_ms : c->bmat_ms;
     out[1] = c->prof_gemm_ms;
     out[2] = (double)c->prof_gemm_launches;
     out[3] = c->prof_gemm_flops;
     out[4] = (double)((long)c->V * c->nom);
-    out[5] = (double)c->cKpad;
+    out[5] = (double)(c->last_kpad > 0 ? c->last_kpad : c->cKpad);
     c->prof_gemm_ms = 0.0;
     c->prof_gemm_launches = 0;
     c->prof_gemm_flops = 0.0;

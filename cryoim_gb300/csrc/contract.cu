@@ -14,6 +14,7 @@
 // normalisation sums are FP64; the best candidates are rescored in FP64 here and with
 // the reference's phase residual (k_pr_single) by the driver.
 #include <cuda_bf16.h>
+#include <cuda_fp8.h>
 #include <cuda_runtime.h>
 
 #include "geom.cuh"
@@ -298,9 +299,148 @@ __global__ void k_cc_fp64(const float2* __restrict__ cube, const float2* __restr
     if (threadIdx.x == 0) out[(long)p * k + c] = (na > 0 && nb > 0) ? dot / sqrt(na * nb) : 0.0;
 }
 
+// ---- FP8-e4m3 operands ---------------------------------------------------------
+// Both operands are unit-norm rows whose elements span a wide range: low-frequency
+// samples carry most of the norm, high-frequency ones little.  Each radial band b =
+// int(|h|) of the samples gets a power-of-two scale 2^e_b on the B side (the sections)
+// and 2^-e_b on the A side (the particles), so every product, hence every score, is
+// unchanged, while each band of B uses the top of the e4m3 range (max 448).  A whole A
+// row is further scaled by 2^f_p per particle (its origins share it), which scales all
+// of that particle's scores alike and is removed from the reported CC.
+
+__device__ __forceinline__ int sample_band(int2 hk) {
+    return (int)sqrtf((float)(hk.x * hk.x + hk.y * hk.y));
+}
+
+// Largest |Re| or |Im| of B per band over every stride-th row (float bits, non-negative,
+// so unsigned order is float order).
+__global__ void k_band_absmax(const __nv_bfloat162* __restrict__ B, long n, int Kpad, const int2* __restrict__ samples,
+                              int S, int nband, int stride, unsigned* __restrict__ out) {
+    extern __shared__ unsigned smax[];
+    for (int b = threadIdx.x; b < nband; b += blockDim.x) smax[b] = 0u;
+    __syncthreads();
+    for (long r = (long)blockIdx.x * stride; r < n; r += (long)gridDim.x * stride) {
+        const __nv_bfloat162* row = B + r * (Kpad / 2);
+        for (int i = threadIdx.x; i < S; i += blockDim.x) {
+            const float2 v = __bfloat1622float2(row[i]);
+            const float m = fmaxf(fabsf(v.x), fabsf(v.y));
+            atomicMax(&smax[sample_band(samples[i])], __float_as_uint(m));
+        }
+    }
+    __syncthreads();
+    for (int b = threadIdx.x; b < nband; b += blockDim.x)
+        if (smax[b]) atomicMax(&out[b], smax[b]);
+}
+
+// One CTA per row: B8[r] = e4m3(B[r] * mulB[sample]), zero padded to Kpad8 bytes.
+__global__ void k_b_to_e4m3(const __nv_bfloat162* __restrict__ B, int Kpad, int S, const float* __restrict__ mulB,
+                            int Kpad8, unsigned short* __restrict__ B8) {
+    const long r = blockIdx.x;
+    const __nv_bfloat162* row = B + r * (Kpad / 2);
+    unsigned short* out = B8 + r * (Kpad8 / 2);
+    for (int i = threadIdx.x; i < Kpad8 / 2; i += blockDim.x) {
+        float2 v = make_float2(0.f, 0.f);
+        if (i < S) {
+            v = __bfloat1622float2(row[i]);
+            v.x *= mulB[i];
+            v.y *= mulB[i];
+        }
+        out[i] = __nv_cvt_float2_to_fp8x2(v, __NV_SATFINITE, __NV_E4M3);
+    }
+}
+
+// Per particle: f_p = floor(log2(224 / max_i |A_i| mulA_i)) with |A_i| = |CTF P| / |A|.
+__global__ void k_particle_exp8(const float2* __restrict__ band, const float* __restrict__ ctf, Band bd,
+                                const int2* __restrict__ samples, int S, const double* __restrict__ norm,
+                                const float* __restrict__ mulA, int* __restrict__ fexp) {
+    __shared__ float sm[32];
+    const int p = blockIdx.x, W = bd.W, R = bd.max_r;
+    const float2* b = band + (long)p * W * W;
+    const float* c = ctf ? ctf + (long)p * W * W : nullptr;
+    const float inv = norm[p] > 0.0 ? (float)(1.0 / sqrt(norm[p])) : 0.0f;
+    float m = 0.0f;
+    for (int i = threadIdx.x; i < S; i += blockDim.x) {
+        const int2 hk = samples[i];
+        const int q = (hk.y + R) * W + (hk.x + R);
+        const float a = sqrtf(b[q].x * b[q].x + b[q].y * b[q].y) * fabsf(c ? c[q] : 1.0f);
+        m = fmaxf(m, a * inv * mulA[i]);
+    }
+    for (int o = 16; o > 0; o >>= 1) m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, o));
+    if ((threadIdx.x & 31) == 0) sm[threadIdx.x >> 5] = m;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        for (int w = 1; w < (int)(blockDim.x >> 5); ++w) m = fmaxf(m, sm[w]);
+        m = fmaxf(m, sm[0]);
+        fexp[p] = m > 0.0f ? (int)floorf(log2f(224.0f / m)) : 0;
+    }
+}
+
+// Row (p, o) of A in e4m3: k_build_a's value x mulA[sample] x 2^f_p.
+__global__ void __launch_bounds__(256) k_build_a8(const float2* __restrict__ band, const float* __restrict__ ctf,
+                                                  Band bd, const int2* __restrict__ samples, int S, int Kpad8,
+                                                  const float* __restrict__ origins, int O,
+                                                  const double* __restrict__ norm, const float* __restrict__ mulA,
+                                                  const int* __restrict__ fexp, float two_pi_over_n,
+                                                  unsigned short* __restrict__ A8) {
+    const int o = blockIdx.x, p = blockIdx.y, W = bd.W, R = bd.max_r;
+    const float2* b = band + (long)p * W * W;
+    const float* c = ctf ? ctf + (long)p * W * W : nullptr;
+    const float h = (float)(bd.nx / 2);
+    const float sx = origins[2 * o] + h, sy = origins[2 * o + 1] + h;
+    const float inv = norm[p] > 0.0 ? (float)(1.0 / sqrt(norm[p])) : 0.0f;
+    const float pscale = ldexpf(1.0f, fexp[p]);
+    unsigned short* row = A8 + ((long)p * O + o) * (Kpad8 / 2);
+    for (int i = threadIdx.x; i < Kpad8 / 2; i += blockDim.x) {
+        float re = 0.f, im = 0.f;
+        if (i < S) {
+            const int2 hk = samples[i];
+            const int q = (hk.y + R) * W + (hk.x + R);
+            const float2 ab = b[q];
+            float sn, cs;
+            sincosf(two_pi_over_n * (sx * (float)hk.x + sy * (float)hk.y), &sn, &cs);
+            const float a2 = ab.x * cs + ab.y * sn, b2 = -ab.x * sn + ab.y * cs;
+            const float cv = (c ? c[q] : 1.0f) * inv * mulA[i] * pscale;
+            re = a2 * cv;
+            im = -b2 * cv;
+        }
+        row[i] = __nv_cvt_float2_to_fp8x2(make_float2(re, im), __NV_SATFINITE, __NV_E4M3);
+    }
+}
+
 inline int cdiv(long a, long b) { return (int)((a + b - 1) / b); }
 
 }  // namespace
+
+cudaError_t launch_band_absmax(const void* B, long n, int Kpad, const int2* samples, int S, int nband, int stride,
+                               unsigned* out, int sms, cudaStream_t st) {
+    cudaError_t e = cudaMemsetAsync(out, 0, sizeof(unsigned) * nband, st);
+    if (e != cudaSuccess) return e;
+    long rows = (n + stride - 1) / stride;
+    int grid = (int)(rows < 4L * sms ? rows : 4L * sms);
+    k_band_absmax<<<grid, 256, sizeof(unsigned) * nband, st>>>((const __nv_bfloat162*)B, n, Kpad, samples, S, nband,
+                                                               stride, out);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_b_to_e4m3(const void* B, long n, int Kpad, int S, const float* mulB, int Kpad8, void* B8,
+                             cudaStream_t st) {
+    for (long r0 = 0; r0 < n; r0 += 1L << 30) {
+        long nb = n - r0 < (1L << 30) ? n - r0 : (1L << 30);
+        k_b_to_e4m3<<<(unsigned)nb, 256, 0, st>>>((const __nv_bfloat162*)B + r0 * (Kpad / 2), Kpad, S, mulB, Kpad8,
+                                                  (unsigned short*)B8 + r0 * (Kpad8 / 2));
+    }
+    return cudaGetLastError();
+}
+
+void launch_build_a8(const float2* band, const float* ctf, Band bd, const int2* samples, int S, int Kpad8,
+                     const float* origins, int O, const double* norm, const float* mulA, int* fexp, int B, void* A8,
+                     cudaStream_t st) {
+    k_particle_exp8<<<B, 256, 0, st>>>(band, ctf, bd, samples, S, norm, mulA, fexp);
+    dim3 g(O, B);
+    const float tpn = 2.0f * host_angles().pi / (float)bd.nx;
+    k_build_a8<<<g, 256, 0, st>>>(band, ctf, bd, samples, S, Kpad8, origins, O, norm, mulA, fexp, tpn,
+                                  (unsigned short*)A8);
+}
 
 void launch_map_checker(const float* map, int nx, float2* work, cudaStream_t st) {
     const long n3 = (long)nx * nx * nx;

@@ -1,16 +1,19 @@
-// gemm_tc.cu — BF16 x BF16 -> FP32 contraction on the 5th-generation tensor cores
-// (tcgen05.mma, accumulators in TMEM, operands staged by TMA), with a fused
-// per-tile argmax epilogue.  This is the dense cross-correlation of the projection-
-// matching form: C[m, n] = sum_k A[m, k] B[n, k] with both operands K-major, where a
-// row of A is one (particle, origin) and a row of B one orientation's central section.
-// The full C is never stored: each (row, 256-column tile) reduces to (max, argmax).
+// gemm_tc.cu — BF16 x BF16 (or FP8-e4m3 x FP8-e4m3) -> FP32 contraction on the
+// 5th-generation tensor cores (tcgen05.mma, accumulators in TMEM, operands staged by
+// TMA), with a fused per-tile argmax epilogue.  This is the dense cross-correlation of the
+// projection-matching form: C[m, n] = sum_k A[m, k] B[n, k] with both operands K-major,
+// where a row of A is one (particle, origin) and a row of B one orientation's central
+// section.  The full C is never stored: each (row, 256-column tile) reduces to
+// (max, argmax).
 //
 // Persistent kernel, one CTA per SM, 192 threads:
-//   warp 0    : TMA producer (one lane) filling a 4-stage ring of 128x64 A and
-//               256x64 B tiles (128-byte swizzle), mbarrier full/empty handshakes;
-//   warp 1    : MMA issuer (one lane): 4 x tcgen05.mma (M128 N256 K16) per stage into
-//               one of two TMEM accumulators (2 x 256 columns), tcgen05.commit frees
-//               the stage and, at the end of a tile, signals the epilogue;
+//   warp 0    : TMA producer (one lane) filling a 4-stage ring of 128-row A and 256-row
+//               B tiles of 128 bytes per row (64 BF16 or 128 FP8 elements, 128-byte
+//               swizzle), mbarrier full/empty handshakes;
+//   warp 1    : MMA issuer (one lane): 4 x tcgen05.mma (M128 N256, K16 BF16 / K32 FP8,
+//               32 bytes of K each) per stage into one of two TMEM accumulators
+//               (2 x 256 columns), tcgen05.commit frees the stage and, at the end of a
+//               tile, signals the epilogue;
 //   warps 2-5 : epilogue, one TMEM lane (= output row) per thread: tcgen05.ld 32
 //               columns at a time, running max/argmax, then release the accumulator.
 // Tiles are visited m-fastest so consecutive CTAs share a B tile through L2.
@@ -29,18 +32,20 @@
 namespace cryoim {
 namespace {
 
-constexpr int GM = 128, GN = 256, GK = 64, NSTAGE = 4;
-constexpr int A_BYTES = GM * GK * 2, B_BYTES = GN * GK * 2;
+constexpr int GM = 128, GN = 256, GKB = 128, NSTAGE = 4;  // GKB: bytes of K per stage
+constexpr int A_BYTES = GM * GKB, B_BYTES = GN * GKB;
 constexpr int STAGE_BYTES = A_BYTES + B_BYTES;
 constexpr int TMEM_COLS = 512;
 constexpr int NTHREADS = 192;
 constexpr unsigned long long WAIT_NS = 2000000000ull;
 constexpr int SMEM_BYTES = NSTAGE * STAGE_BYTES + 1024 + 256;
 
-// instruction descriptor, kind::f16: D=F32 (bits 4-5), A=BF16 (7-9), B=BF16 (10-12),
-// both K-major (bits 15, 16 = 0), N>>3 at bits 17-22, M>>4 at bits 24-28
-constexpr uint32_t IDESC = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(GN >> 3) << 17) |
-                           ((uint32_t)(GM >> 4) << 24);
+// instruction descriptors: D=F32 (bits 4-5), A and B formats at bits 7-9 and 10-12
+// (kind::f16: BF16 = 1; kind::f8f6f4: E4M3 = 0), both K-major (bits 15, 16 = 0),
+// N>>3 at bits 17-22, M>>4 at bits 24-28
+constexpr uint32_t IDESC_BF16 = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(GN >> 3) << 17) |
+                                ((uint32_t)(GM >> 4) << 24);
+constexpr uint32_t IDESC_E4M3 = (1u << 4) | ((uint32_t)(GN >> 3) << 17) | ((uint32_t)(GM >> 4) << 24);
 
 __device__ __forceinline__ uint32_t su32(const void* p) {
     return (uint32_t)__cvta_generic_to_shared(p);
@@ -103,13 +108,23 @@ __device__ __forceinline__ void tc_commit(uint64_t* b) {
                      su32(b))
                  : "memory");
 }
+template <bool F8>
 __device__ __forceinline__ void tc_mma(uint32_t d, uint64_t a, uint64_t bdesc, uint32_t acc) {
-    asm volatile(
-        "{\n\t.reg .pred p;\n\t"
-        "setp.ne.b32 p, %4, 0;\n\t"
-        "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}" ::"r"(d),
-        "l"(a), "l"(bdesc), "r"(IDESC), "r"(acc)
-        : "memory");
+    if constexpr (F8) {
+        asm volatile(
+            "{\n\t.reg .pred p;\n\t"
+            "setp.ne.b32 p, %4, 0;\n\t"
+            "tcgen05.mma.cta_group::1.kind::f8f6f4 [%0], %1, %2, %3, p;\n}" ::"r"(d),
+            "l"(a), "l"(bdesc), "r"(IDESC_E4M3), "r"(acc)
+            : "memory");
+    } else {
+        asm volatile(
+            "{\n\t.reg .pred p;\n\t"
+            "setp.ne.b32 p, %4, 0;\n\t"
+            "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}" ::"r"(d),
+            "l"(a), "l"(bdesc), "r"(IDESC_BF16), "r"(acc)
+            : "memory");
+    }
 }
 // shared-memory matrix descriptor: K-major, 128-byte swizzle, 8-row atoms 1024 B apart
 __device__ __forceinline__ uint64_t sdesc(uint32_t saddr) {
@@ -138,9 +153,12 @@ __device__ __forceinline__ void tmem_ld32(uint32_t taddr, float* v) {
     for (int i = 0; i < 32; ++i) v[i] = __uint_as_float(r[i]);
 }
 
+// F8 = false: BF16 operands, 64 elements of K per stage; true: FP8-e4m3, 128 elements.
+template <bool F8>
 __global__ void __launch_bounds__(NTHREADS, 1)
-    k_gemm_bf16_argmax(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB,
-                       GemmArgmaxArgs g) {
+    k_gemm_argmax(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB,
+                  GemmArgmaxArgs g) {
+    constexpr int GK = F8 ? GKB : GKB / 2;  // K elements per stage
     extern __shared__ unsigned char smem_raw[];
     unsigned char* sm = (unsigned char*)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
     unsigned char* sA = sm;
@@ -215,8 +233,8 @@ __global__ void __launch_bounds__(NTHREADS, 1)
                     tc_fence_after();
                     const uint32_t a0 = su32(sA + s * A_BYTES), b0 = su32(sB + s * B_BYTES);
 #pragma unroll
-                    for (int kk = 0; kk < GK / 16; ++kk)
-                        tc_mma(d, sdesc(a0 + kk * 32), sdesc(b0 + kk * 32), (kb | kk) != 0);
+                    for (int kk = 0; kk < GKB / 32; ++kk)
+                        tc_mma<F8>(d, sdesc(a0 + kk * 32), sdesc(b0 + kk * 32), (kb | kk) != 0);
                     tc_commit(empty + s);
                     if (++s == NSTAGE) { s = 0; ph ^= 1u; }
                 }
@@ -283,15 +301,18 @@ PFN_cuTensorMapEncodeTiled_v12000 encode_fn() {
     return fn;
 }
 
-// rows x k BF16, row-major (k contiguous), box = (GK, box_rows), 128-byte swizzle
-bool make_map(CUtensorMap* m, const void* base, long rows, int k, int box_rows) {
+// rows x k elements (BF16, or FP8 as bytes), row-major (k contiguous), box = 128 bytes
+// of k x box_rows, 128-byte swizzle
+bool make_map(CUtensorMap* m, const void* base, long rows, int k, int box_rows, bool f8) {
     auto fn = encode_fn();
     if (!fn) return false;
+    const int esz = f8 ? 1 : 2;
     cuuint64_t dims[2] = {(cuuint64_t)k, (cuuint64_t)rows};
-    cuuint64_t strides[1] = {(cuuint64_t)k * 2};
-    cuuint32_t box[2] = {(cuuint32_t)GK, (cuuint32_t)box_rows};
+    cuuint64_t strides[1] = {(cuuint64_t)k * esz};
+    cuuint32_t box[2] = {(cuuint32_t)(GKB / esz), (cuuint32_t)box_rows};
     cuuint32_t es[2] = {1, 1};
-    CUresult r = fn(m, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, const_cast<void*>(base), dims, strides, box,
+    CUresult r = fn(m, f8 ? CU_TENSOR_MAP_DATA_TYPE_UINT8 : CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2,
+                    const_cast<void*>(base), dims, strides, box,
                     es, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B,
                     CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
     return r == CUDA_SUCCESS;
@@ -302,36 +323,42 @@ bool make_map(CUtensorMap* m, const void* base, long rows, int k, int box_rows) 
 int gemm_tile_n() { return GN; }
 int gemm_tile_m() { return GM; }
 
-cudaError_t launch_gemm_bf16_argmax(const void* a, const void* b, int M, int N, int K,
-                                    const GemmArgmaxArgs& in, int num_sms, cudaStream_t st) {
-    if (K % GK != 0 || M < 1 || N < 1) return cudaErrorInvalidValue;
+cudaError_t launch_gemm_argmax(const void* a, const void* b, int M, int N, int K, bool f8,
+                               const GemmArgmaxArgs& in, int num_sms, cudaStream_t st) {
+    const int gk = f8 ? GKB : GKB / 2;
+    if (K % gk != 0 || M < 1 || N < 1) return cudaErrorInvalidValue;
     if (((uintptr_t)a & 15) || ((uintptr_t)b & 15)) return cudaErrorInvalidValue;
     CUtensorMap ta, tb;
-    if (!make_map(&ta, a, M, K, GM) || !make_map(&tb, b, N, K, GN)) return cudaErrorInvalidValue;
+    if (!make_map(&ta, a, M, K, GM, f8) || !make_map(&tb, b, N, K, GN, f8)) return cudaErrorInvalidValue;
     GemmArgmaxArgs g = in;
     g.m_tiles = (M + GM - 1) / GM;
     g.n_tiles = (N + GN - 1) / GN;
-    g.kblocks = K / GK;
+    g.kblocks = K / gk;
     g.m_valid = M;
     g.n_valid = N;
-    cudaError_t e = cudaFuncSetAttribute(k_gemm_bf16_argmax, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                         SMEM_BYTES);
+    auto kern = f8 ? k_gemm_argmax<true> : k_gemm_argmax<false>;
+    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM_BYTES);
     if (e != cudaSuccess) return e;
     int total = g.m_tiles * g.n_tiles;
     int grid = total < num_sms ? total : num_sms;
-    k_gemm_bf16_argmax<<<grid, NTHREADS, SMEM_BYTES, st>>>(ta, tb, g);
+    kern<<<grid, NTHREADS, SMEM_BYTES, st>>>(ta, tb, g);
     return cudaGetLastError();
+}
+
+cudaError_t launch_gemm_bf16_argmax(const void* a, const void* b, int M, int N, int K,
+                                    const GemmArgmaxArgs& in, int num_sms, cudaStream_t st) {
+    return launch_gemm_argmax(a, b, M, N, K, false, in, num_sms, st);
 }
 
 }  // namespace cryoim
 
 // Kernel-level test hook (device pointers): C = A B^T with per-(row, 256-column tile)
 // max/argmax, optional full C.  d_err receives 1 if a pipeline wait timed out.
-extern "C" int cryoim_gemm_bf16_argmax(const void* d_a, const void* d_b, int32_t M, int32_t N,
-                                       int32_t K, float* d_topv, int32_t* d_topi, float* d_c,
-                                       int32_t* d_err, void* stream) {
+static int gemm_hook(const void* d_a, const void* d_b, int32_t M, int32_t N, int32_t K, float* d_topv,
+                     int32_t* d_topi, float* d_c, int32_t* d_err, void* stream, bool f8) {
+    const int kq = f8 ? 128 : 64;
     if (!d_a || !d_b || !d_topv || !d_topi || !d_err) return CRYOIM_ERR_ARG;
-    if (M < 1 || N < 1 || K < 64 || K % 64) return CRYOIM_ERR_SIZE;
+    if (M < 1 || N < 1 || K < kq || K % kq) return CRYOIM_ERR_SIZE;
     int dev = 0, sms = 0;
     if (cudaGetDevice(&dev) != cudaSuccess ||
         cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess)
@@ -344,6 +371,18 @@ extern "C" int cryoim_gemm_bf16_argmax(const void* d_a, const void* d_b, int32_t
     g.err = d_err;
     cudaStream_t st = (cudaStream_t)stream;
     if (cudaMemsetAsync(d_err, 0, sizeof(int), st) != cudaSuccess) return CRYOIM_ERR_CUDA;
-    cudaError_t e = cryoim::launch_gemm_bf16_argmax(d_a, d_b, M, N, K, g, sms, st);
+    cudaError_t e = cryoim::launch_gemm_argmax(d_a, d_b, M, N, K, f8, g, sms, st);
     return e == cudaSuccess ? CRYOIM_OK : CRYOIM_ERR_CUDA;
+}
+
+extern "C" int cryoim_gemm_bf16_argmax(const void* d_a, const void* d_b, int32_t M, int32_t N,
+                                       int32_t K, float* d_topv, int32_t* d_topi, float* d_c,
+                                       int32_t* d_err, void* stream) {
+    return gemm_hook(d_a, d_b, M, N, K, d_topv, d_topi, d_c, d_err, stream, false);
+}
+
+extern "C" int cryoim_gemm_e4m3_argmax(const void* d_a, const void* d_b, int32_t M, int32_t N,
+                                       int32_t K, float* d_topv, int32_t* d_topi, float* d_c,
+                                       int32_t* d_err, void* stream) {
+    return gemm_hook(d_a, d_b, M, N, K, d_topv, d_topi, d_c, d_err, stream, true);
 }

@@ -12,7 +12,7 @@
 //   5  local refinement (ort_refinement.f90) -> newortfile
 // Extension keys without a reference counterpart: device, batch (particles per device
 // call), contract=y (mode 4 through the tensor-core contraction), originmax,
-// originstep, topk.  Output rows are appended after every chunk, so a run can resume
+// originstep, topk, precision=bf16|fp8 (contraction operands).  Output rows are appended after every chunk, so a run can resume
 // with first=k as with the reference's per-particle writes.
 #include <algorithm>
 #include <cmath>
@@ -34,7 +34,7 @@ const char* kKeys[] = {"apix",         "minRes",       "maxRes",     "imgmask", 
                        "realspaceavg", "ortfile",      "recISAF",    "subrec",     "FSC",
                        "imgstck",      "sym",          "maxcentshift", "corrCTF",  "boundX",
                        "loc_box",      "check"};
-const char* kExt[] = {"device", "batch", "contract", "originmax", "originstep", "topk"};
+const char* kExt[] = {"device", "batch", "contract", "originmax", "originstep", "topk", "precision"};
 
 void usage() {
     std::puts(
@@ -47,7 +47,7 @@ void usage() {
         "         searchstep, minRes, maxRes, applyCTF, vol, Cs, ampwg)\n"
         "  mode=5 local refinement into newortfile (Ncycle, templateort, ...)\n"
         "  common: apix imgmask first last imgstck\n"
-        "  GPU extensions: device batch contract=y originmax originstep topk");
+        "  GPU extensions: device batch contract=y originmax originstep topk precision=bf16|fp8");
 }
 
 bool yes(const std::string& v) { return !v.empty() && (v[0] == 'y' || v[0] == 'Y'); }
@@ -242,7 +242,8 @@ int main(int argc, char** argv) {
         }
         if (cryoim_load_templates(ctx, timg.data(), t.data(), T)) return die("templates", 2);
         const bool contract = mode == 4 && yes(sval("contract", "n"));
-        cryoim_contract_opts co{fval("originmax", 6.0f), fval("originstep", 0.5f), ival("topk", 16), 0};
+        cryoim_contract_opts co{fval("originmax", 6.0f), fval("originstep", 0.5f), ival("topk", 16), 0,
+                                sval("precision", "bf16") == "fp8" ? 1 : 0};
         if (contract) {
             if (map.empty()) return die("contract=y needs model3d", 2);
             if (cryoim_set_reference_map(ctx, map.data())) return die("reference map", 2);

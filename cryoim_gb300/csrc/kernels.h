@@ -132,6 +132,9 @@ int gemm_tile_m();
 // A: M x K, B: N x K, BF16 row-major (K contiguous, K % 64 == 0, 16-byte aligned)
 cudaError_t launch_gemm_bf16_argmax(const void* a, const void* b, int M, int N, int K,
                                     const GemmArgmaxArgs& g, int num_sms, cudaStream_t st);
+// f8: both operands FP8-e4m3 bytes (K % 128 == 0), else BF16
+cudaError_t launch_gemm_argmax(const void* a, const void* b, int M, int N, int K, bool f8,
+                               const GemmArgmaxArgs& g, int num_sms, cudaStream_t st);
 
 // ---- contract.cu (operands of the contraction, selection, FP64 rescoring) ------
 // Fourier band cube of the reference map: (2R+3)^3 float2, frequencies -(R+1)..R+1.
@@ -154,6 +157,17 @@ void launch_select_topk(const float* topv, const int* topi, int O, int ntiles, i
 // cand: B x k x (theta, phi, omega, x, y); out: B x k FP64 cross-correlations
 void launch_cc_fp64(const float2* cube, const float2* band, const float* ctf, Band bd, const int2* samples,
                     int S, const float* cand, int k, int B, double* out, cudaStream_t st);
+
+// FP8-e4m3 operands (contract.cu): per-band max |B| (R+1 bands, float bits) over every
+// stride-th row; B8 = e4m3(B x mulB) with rows of Kpad8 bytes; A8 rows with mulA and the
+// per-particle exponent fexp (written by launch_build_a8).
+cudaError_t launch_band_absmax(const void* B, long n, int Kpad, const int2* samples, int S, int nband, int stride,
+                               unsigned* out, int sms, cudaStream_t st);
+cudaError_t launch_b_to_e4m3(const void* B, long n, int Kpad, int S, const float* mulB, int Kpad8, void* B8,
+                             cudaStream_t st);
+void launch_build_a8(const float2* band, const float* ctf, Band bd, const int2* samples, int S, int Kpad8,
+                     const float* origins, int O, const double* norm, const float* mulA, int* fexp, int B, void* A8,
+                     cudaStream_t st);
 
 // ---- fsc.cu: half-map FSC and the FSC-weighted map ---------------------------
 struct FscArgs {

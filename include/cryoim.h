@@ -333,12 +333,14 @@ typedef struct cryoim_contract_opts {
     float origin_step;  /* origin grid step, pixels                                 */
     int32_t topk;       /* candidates rescored per particle (1..64)                 */
     int32_t pick;       /* 0: minimum phase residual, 1: maximum FP64 correlation  */
+    int32_t precision;  /* operands: 0 BF16, 1 FP8-e4m3 with per-band power-of-two
+                           scales (both with FP32 accumulation)                    */
 } cryoim_contract_opts;
 /* The 3D map (nx^3 float32) whose central sections are correlated: its centred Fourier
  * transform is kept as a band cube of (2 maxR + 3)^3 complex values. */
 int cryoim_set_reference_map(void* ctx, const float* map3d);
 /* cands (optional): P x topk x 8 floats: theta, phi, omega, x, y (the candidate's best
- * origin), CC from the BF16 contraction, CC in FP64, PR at the particle's origin. */
+ * origin), CC from the contraction (BF16 or FP8), CC in FP64, PR at the particle's origin. */
 int cryoim_contract_search(void* ctx, const float* imgs, cryoim_particle* parts, int32_t P,
                            const cryoim_contract_opts* opts, float* cands);
 int cryoim_contract_search_device(void* ctx, const float* d_imgs, cryoim_particle* parts, int32_t P,
@@ -353,6 +355,11 @@ int cryoim_contract_stats(void* ctx, double* out);
  * of every (row, 256-column tile): d_topv / d_topi are M x ceil(N/256); d_c (optional)
  * receives the full M x N C.  *d_err = 1 if a pipeline wait timed out. */
 int cryoim_gemm_bf16_argmax(const void* d_a, const void* d_b, int32_t M, int32_t N, int32_t K,
+                            float* d_topv, int32_t* d_topi, float* d_c, int32_t* d_err,
+                            void* stream);
+/* The same with FP8-e4m3 operands (one byte per element, K % 128 == 0), FP32 accumulation
+ * (tcgen05.mma kind::f8f6f4). */
+int cryoim_gemm_e4m3_argmax(const void* d_a, const void* d_b, int32_t M, int32_t N, int32_t K,
                             float* d_topv, int32_t* d_topi, float* d_c, int32_t* d_err,
                             void* stream);
 

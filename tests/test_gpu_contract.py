@@ -119,3 +119,25 @@ def test_noise_free_particles_find_their_orientation(run):
         err = synth.orientation_error(tuple(top[:3]), truth[i])
         assert err < 1.5 * p.searchstep, (i, err)
         assert abs(top[3] - parts["x"][i]) <= 0.5 and abs(top[4] - parts["y"][i]) <= 0.5
+
+
+def test_fp8_form_tracks_fp64_and_picks_the_same_orientation(run, built):
+    """FP8-e4m3 operands with per-band power-of-two scales: the descaled tensor-core CC of
+    every candidate tracks its FP64 CC, the candidates carry the same FP64 rescoring, and
+    the pick equals the BF16 form's."""
+    import cryoim_gb300 as ci
+    (p, vol, tmpl, timgs, imgs, parts, truth), q, cands, stats = run
+    with ci.Context(0, p) as ctx:
+        ctx.load_templates(timgs, tmpl)
+        ctx.set_reference_map(vol)
+        q8 = parts.copy()
+        c8 = ctx.contract_search(imgs, q8, origin_max=2.0, origin_step=0.5, topk=8, want_cands=True,
+                                 precision="fp8")
+        st8 = ctx.contract_stats()
+    assert st8["kpad"] % 128 == 0
+    for i in range(len(parts)):
+        for j in range(c8.shape[1]):
+            assert abs(c8[i, j, 5] - c8[i, j, 6]) < 5e-2, (i, j, c8[i, j, 5], c8[i, j, 6])
+        assert (q8["theta"][i], q8["phi"][i], q8["omega"][i]) == (q["theta"][i], q["phi"][i], q["omega"][i])
+        # the BF16 form's best candidate is among the FP8 form's best three
+        assert any(np.allclose(c8[i, j, :3], cands[i, 0, :3]) for j in range(3))

@@ -1,5 +1,6 @@
-"""The tcgen05 BF16 contraction with fused per-tile argmax against an FP32 matmul of
-the same BF16 operands (ragged M and N exercise the TMA zero fill)."""
+"""The tcgen05 contraction with fused per-tile argmax (BF16 x BF16 and FP8-e4m3 x
+FP8-e4m3, FP32 accumulation) against an FP32 matmul of the same operands (ragged M and
+N exercise the TMA zero fill)."""
 import ctypes as C
 
 import numpy as np
@@ -8,21 +9,24 @@ import pytest
 pytestmark = pytest.mark.gpu
 
 
-@pytest.mark.parametrize("M,N,K", [(128, 256, 64), (300, 1000, 448), (1000, 3000, 1280)])
-def test_gemm_argmax_matches_fp32_matmul(built, M, N, K):
+@pytest.mark.parametrize("kind,M,N,K", [("bf16", 128, 256, 64), ("bf16", 300, 1000, 448),
+                                        ("bf16", 1000, 3000, 1280), ("e4m3", 128, 256, 128),
+                                        ("e4m3", 300, 1000, 512), ("e4m3", 1000, 3000, 1280)])
+def test_gemm_argmax_matches_fp32_matmul(built, kind, M, N, K):
     import torch
     from cryoim_gb300._abi import call
     torch.manual_seed(M + N + K)
     dev = torch.device("cuda", 0)
-    a = torch.randn(M, K, device=dev).to(torch.bfloat16)
-    b = torch.randn(N, K, device=dev).to(torch.bfloat16)
+    dt = torch.bfloat16 if kind == "bf16" else torch.float8_e4m3fn
+    a = torch.randn(M, K, device=dev).to(dt)
+    b = torch.randn(N, K, device=dev).to(dt)
     nt = (N + 255) // 256
     topv = torch.empty(M, nt, device=dev)
     topi = torch.empty(M, nt, dtype=torch.int32, device=dev)
     cfull = torch.zeros(M, N, device=dev)
     err = torch.zeros(1, dtype=torch.int32, device=dev)
     s = torch.cuda.current_stream().cuda_stream
-    call("cryoim_gemm_bf16_argmax", C.c_void_p(a.data_ptr()), C.c_void_p(b.data_ptr()), M, N, K,
+    call(f"cryoim_gemm_{kind}_argmax", C.c_void_p(a.data_ptr()), C.c_void_p(b.data_ptr()), M, N, K,
          C.c_void_p(topv.data_ptr()), C.c_void_p(topi.data_ptr()), C.c_void_p(cfull.data_ptr()),
          C.c_void_p(err.data_ptr()), C.c_void_p(s))
     torch.cuda.synchronize()
