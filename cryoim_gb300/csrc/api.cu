@@ -721,11 +721,17 @@ int ensure_bmat(Ctx* c) {
     cudaEvent_t e0, e1;
     CK(cudaEventCreate(&e0));
     CK(cudaEventCreate(&e1));
-    CK(cudaEventRecord(e0, c->stream));
-    CK(launch_slice_bf16(c->mapcube.p, c->p.max_r, c->csamples.p, c->cS, c->cKpad, dv.p, c->nom,
-                         c->p.searchstep, 0, n, c->bmat.p, c->stream));
-    CK(cudaEventRecord(e1, c->stream));
-    CK(cudaEventSynchronize(e1));
+    cudaArray_t arr = nullptr;
+    cudaTextureObject_t tex = 0;
+    cudaError_t te = make_cube_texture(c->mapcube.p, c->p.max_r, c->stream, &arr, &tex);
+    if (te == cudaSuccess) te = cudaEventRecord(e0, c->stream);
+    if (te == cudaSuccess)
+        te = launch_slice_bf16(tex, c->p.max_r, c->csamples.p, c->cS, c->cKpad, dv.p, c->nom, c->p.searchstep, 0,
+                               n, c->bmat.p, c->stream);
+    if (te == cudaSuccess) te = cudaEventRecord(e1, c->stream);
+    if (te == cudaSuccess) te = cudaEventSynchronize(e1);
+    free_cube_texture(arr, tex);
+    if (te != cudaSuccess) return fail(CRYOIM_ERR_CUDA, "section build: %s", cudaGetErrorString(te));
     float ms = 0.f;
     cudaEventElapsedTime(&ms, e0, e1);
     cudaEventDestroy(e0);

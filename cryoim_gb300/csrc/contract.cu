@@ -66,27 +66,13 @@ __global__ void k_map_band(const float2* __restrict__ ft, int nx, int R, float2*
     }
 }
 
-__device__ __forceinline__ float2 cube_trilinear(const float2* __restrict__ cube, int C, int off,
-                                                 float x, float y, float z) {
-    const float fx = floorf(x), fy = floorf(y), fz = floorf(z);
-    const int ix = (int)fx + off, iy = (int)fy + off, iz = (int)fz + off;
-    const float ax = x - fx, ay = y - fy, az = z - fz;
-    const long b0 = ((long)iz * C + iy) * C + ix;
-    const long CC = (long)C * C;
-    float2 c000 = cube[b0], c100 = cube[b0 + 1], c010 = cube[b0 + C], c110 = cube[b0 + C + 1];
-    float2 c001 = cube[b0 + CC], c101 = cube[b0 + CC + 1], c011 = cube[b0 + CC + C], c111 = cube[b0 + CC + C + 1];
-    const float bx = 1.f - ax, by = 1.f - ay, bz = 1.f - az;
-    float2 r;
-    r.x = bz * (by * (bx * c000.x + ax * c100.x) + ay * (bx * c010.x + ax * c110.x)) +
-          az * (by * (bx * c001.x + ax * c101.x) + ay * (bx * c011.x + ax * c111.x));
-    r.y = bz * (by * (bx * c000.y + ax * c100.y) + ay * (bx * c010.y + ax * c110.y)) +
-          az * (by * (bx * c001.y + ax * c101.y) + ay * (bx * c011.y + ax * c111.y));
-    return r;
-}
-
 // One CTA per orientation n = view * nomega + iomega: section samples in shared
-// memory, FP64 norm, then the unit-norm row in BF16 (Re, Im interleaved, zero pad).
-__global__ void __launch_bounds__(256) k_slice_bf16(const float2* __restrict__ cube, int R,
+// memory, norm (FP32 per thread, FP64 across the block), then the unit-norm row in BF16
+// (Re, Im interleaved, zero pad).  The trilinear interpolation runs on the texture
+// units: the band cube is a float2 3D array with linear filtering (hardware weights in
+// 1/256 steps, well inside the BF16 rounding of the row), texel centres at +0.5, zero
+// outside the cube.
+__global__ void __launch_bounds__(512) k_slice_bf16(cudaTextureObject_t cube, int R,
                                                     const int2* __restrict__ samples, int S, int Kpad,
                                                     const float* __restrict__ views, int nom, float step,
                                                     float d2r, long n0, __nv_bfloat162* __restrict__ B) {
@@ -97,17 +83,17 @@ __global__ void __launch_bounds__(256) k_slice_bf16(const float2* __restrict__ c
     const int v = (int)(n / nom), io = (int)(n % nom);
     if (threadIdx.x == 0) euler_mat(views[2 * v], views[2 * v + 1], step * (float)io, d2r, rot);
     __syncthreads();
-    const int C = 2 * R + 3, off = R + 1;
-    double nrm = 0.0;
+    const float off = (float)(R + 1) + 0.5f;
+    float part = 0.0f;
     for (int i = threadIdx.x; i < S; i += blockDim.x) {
         const int2 hk = samples[i];
         const float hx = (float)hk.x, ky = (float)hk.y;
         const float x = rot[0] * hx + rot[1] * ky, y = rot[3] * hx + rot[4] * ky, z = rot[6] * hx + rot[7] * ky;
-        float2 val = cube_trilinear(cube, C, off, x, y, z);
+        const float2 val = tex3D<float2>(cube, x + off, y + off, z + off);
         ssec[i] = val;
-        nrm += (double)val.x * val.x + (double)val.y * val.y;
+        part += val.x * val.x + val.y * val.y;
     }
-    nrm = block_sum_double(nrm, sh);
+    const double nrm = block_sum_double((double)part, sh);
     const float inv = nrm > 0.0 ? (float)(1.0 / sqrt(nrm)) : 0.0f;
     __nv_bfloat162* row = B + (long)blockIdx.x * (Kpad / 2);
     for (int i = threadIdx.x; i < Kpad / 2; i += blockDim.x) {
@@ -452,7 +438,37 @@ void launch_map_band(const float2* ft, int nx, int R, float2* cube, cudaStream_t
     k_map_band<<<cdiv(c3, 256) < 65535 ? cdiv(c3, 256) : 65535, 256, 0, st>>>(ft, nx, R, cube);
 }
 
-cudaError_t launch_slice_bf16(const float2* cube, int R, const int2* samples, int S, int Kpad,
+// The band cube ((2R+3)^3 float2, x fastest) as a 3D array behind a linear-filtering
+// texture (unnormalised coordinates, zero border).  Release with free_cube_texture.
+cudaError_t make_cube_texture(const float2* cube, int R, cudaStream_t st, cudaArray_t* arr,
+                              cudaTextureObject_t* tex) {
+    const int C = 2 * R + 3;
+    cudaChannelFormatDesc fd = cudaCreateChannelDesc<float2>();
+    cudaError_t e = cudaMalloc3DArray(arr, &fd, make_cudaExtent(C, C, C));
+    if (e != cudaSuccess) return e;
+    cudaMemcpy3DParms cp{};
+    cp.srcPtr = make_cudaPitchedPtr(const_cast<float2*>(cube), (size_t)C * sizeof(float2), C, C);
+    cp.dstArray = *arr;
+    cp.extent = make_cudaExtent(C, C, C);
+    cp.kind = cudaMemcpyDeviceToDevice;
+    if ((e = cudaMemcpy3DAsync(&cp, st)) != cudaSuccess) return e;
+    cudaResourceDesc rd{};
+    rd.resType = cudaResourceTypeArray;
+    rd.res.array.array = *arr;
+    cudaTextureDesc td{};
+    td.addressMode[0] = td.addressMode[1] = td.addressMode[2] = cudaAddressModeBorder;
+    td.filterMode = cudaFilterModeLinear;
+    td.readMode = cudaReadModeElementType;
+    td.normalizedCoords = 0;
+    return cudaCreateTextureObject(tex, &rd, &td, nullptr);
+}
+
+void free_cube_texture(cudaArray_t arr, cudaTextureObject_t tex) {
+    if (tex) cudaDestroyTextureObject(tex);
+    if (arr) cudaFreeArray(arr);
+}
+
+cudaError_t launch_slice_bf16(cudaTextureObject_t cube, int R, const int2* samples, int S, int Kpad,
                               const float* views, int nom, float step, long n0, long count, void* B,
                               cudaStream_t st) {
     size_t sm = (size_t)S * sizeof(float2);
@@ -460,7 +476,7 @@ cudaError_t launch_slice_bf16(const float2* cube, int R, const int2* samples, in
     if (e != cudaSuccess) return e;
     for (long c0 = 0; c0 < count; c0 += 65535) {
         long nb = count - c0 < 65535 ? count - c0 : 65535;
-        k_slice_bf16<<<(unsigned)nb, 256, sm, st>>>(cube, R, samples, S, Kpad, views, nom, step,
+        k_slice_bf16<<<(unsigned)nb, 512, sm, st>>>(cube, R, samples, S, Kpad, views, nom, step,
                                                    host_angles().deg2rad, n0 + c0,
                                                    (__nv_bfloat162*)B + c0 * (Kpad / 2));
     }

@@ -140,8 +140,12 @@ cudaError_t launch_gemm_argmax(const void* a, const void* b, int M, int N, int K
 // Fourier band cube of the reference map: (2R+3)^3 float2, frequencies -(R+1)..R+1.
 void launch_map_checker(const float* map, int nx, float2* work, cudaStream_t st);
 void launch_map_band(const float2* ft, int nx, int R, float2* cube, cudaStream_t st);
+// The band cube as a linear-filtering 3D texture (for the section build).
+cudaError_t make_cube_texture(const float2* cube, int R, cudaStream_t st, cudaArray_t* arr,
+                              cudaTextureObject_t* tex);
+void free_cube_texture(cudaArray_t arr, cudaTextureObject_t tex);
 // Rows n0 .. n0+count-1 of B (orientation n = view * nom + iomega), unit norm, BF16.
-cudaError_t launch_slice_bf16(const float2* cube, int R, const int2* samples, int S, int Kpad,
+cudaError_t launch_slice_bf16(cudaTextureObject_t cube, int R, const int2* samples, int S, int Kpad,
                               const float* views, int nom, float step, long n0, long count, void* B,
                               cudaStream_t st);
 void launch_particle_norm(const float2* band, const float* ctf, Band bd, const int2* samples, int S,
