@@ -461,8 +461,8 @@ def run_ours(args):
                                      "frac": slice_bytes / (st0["slice_ms"] / 1000.0) / 1e9 / hbm,
                                      "traffic_algorithmic": slice_bytes,
                                      "note": "BF16 rows written + band cube read once; the kernel is bound by "
-                                             "its 8-tap trilinear gathers from the L2-resident cube, and runs "
-                                             "once per map (0.2 % of a 10k-particle cycle)"}},
+                                             "its trilinear texture fetches (one per sample, hardware "
+                                             "filtering of the cube), and runs once per map"}},
             "agreement": {"identical_orientation": same / npr, "within_1_step": same1 / npr, "particles": npr,
                           "map_fsc_min": float(fsc_forms[1:].min()),
                           "map_fsc_note": "FSC (shells 1..maxR) between the maps reconstructed from the "
