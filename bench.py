@@ -482,6 +482,90 @@ def run_ours(args):
     return 0
 
 
+def run_precision_report(args):
+    """Precision form on the CPU-runnable configuration's data: box 128, 2.0 A/px, band
+    1/60-1/10 A^-1, defocus 1.0-3.0 um without astigmatism, SNR 0.1, origins within
+    +-3 px; global 0.5-degree grid with origins +-6 px at 0.5 px; the contraction in BF16
+    and in FP8-e4m3 (per-band scales, FP32 accumulation, FP64 rescoring of the top 16).
+    Reports, per form, the contraction score error against the FP64 CC of the same
+    candidates, orientation agreement with the exhaustive FP32 phase-residual search (the
+    drop-in form, itself held to the FP64 oracle by the parity tests) and throughput."""
+    import torch
+    import cryoim_gb300 as ci
+    from cryoim_gb300 import synth
+    r, world, lr = rank_env()
+    if r != 0:
+        return 0
+    n, P = 128, args.precision_report
+    seed = 20261204
+    params = ci.default_params(n, apix=2.0, minRes=60.0, maxRes=10.0, searchstep=0.5, ampwg=0.07,
+                               imgmask=(n // 2 - 2) * 2.0)
+    ctx = ci.Context(0, params)
+    rng = np.random.default_rng(seed)
+    vol = synth.phantom(n, seed)
+    te = synth.random_asu_orientations(20, rng)
+    tmpl = _as_tmpl(ci, te)
+    tmpl["particle_id"] = np.arange(1, 21)
+    timgs = ctx.project_templates(vol, tmpl)
+    imgs, parts, truth = synth.make_particles(
+        vol, P, seed + 1, lambda v, e: ctx.project_templates(v, _as_tmpl(ci, e)), 2.0, df_range=(1.0, 3.0),
+        astig_max=0.0, origin_max=3.0, snr=0.1, ampwg=0.07)
+    ctx.load_templates(timgs, tmpl)
+    ctx.set_reference_map(vol)
+    d_imgs = torch.from_numpy(imgs).to("cuda:0")
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    q_pr = parts.copy()
+    ctx.globesearch(d_imgs.data_ptr(), q_pr)
+    torch.cuda.synchronize()
+    t_pr = time.perf_counter() - t0
+    out = {"report": "precision form", "config": {"box": n, "apix": 2.0, "band_A": [60.0, 10.0],
+                                                  "minR": params.min_r, "maxR": params.max_r,
+                                                  "searchstep_deg": 0.5, "origins": "+-6 px @ 0.5 px",
+                                                  "particles": P, "snr": 0.1, "topk_rescored": 16,
+                                                  "data": "synthetic, seeded"},
+           "fp32_form": {"particles_per_s": P / t_pr}}
+    for form, topk, nbr in ((f, k, b) for f in ("bf16", "fp8") for k, b in ((16, 1), (16, 2), (32, 2))):
+        q = parts.copy()
+        ctx.contract_search(d_imgs.data_ptr(), q[:1].copy(), origin_max=6.0, origin_step=0.5, topk=topk,
+                            precision=form, nbr=nbr)  # section build outside the timing
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        c = ctx.contract_search(d_imgs.data_ptr(), q, origin_max=6.0, origin_step=0.5, topk=topk,
+                                want_cands=True, precision=form, nbr=nbr)
+        torch.cuda.synchronize()
+        dt = time.perf_counter() - t0
+        err = np.abs(c[:, :, 5].astype(np.float64) - c[:, :, 6])
+        rel = err / np.maximum(np.abs(c[:, :, 6]), 1e-12)
+        same = np.array([np.allclose((q["theta"][i], q["phi"][i], q["omega"][i]),
+                                     (q_pr["theta"][i], q_pr["phi"][i], q_pr["omega"][i]), atol=1e-3)
+                         for i in range(P)])
+        errs = [synth.orientation_error((q["theta"][i], q["phi"][i], q["omega"][i]), truth[i]) for i in range(P)]
+        apart = [synth.orientation_error((q["theta"][i], q["phi"][i], q["omega"][i]),
+                                         (q_pr["theta"][i], q_pr["phi"][i], q_pr["omega"][i]))
+                 for i in range(P) if not same[i]]
+        out[f"{form}_form_top{topk}_nbr{nbr}"] = {
+            "particles_per_s": P / dt,
+            "disagreement_angle_deg": {"median": float(np.median(apart)) if apart else 0.0,
+                                       "max": float(np.max(apart)) if apart else 0.0},
+            "exhaustive_pick_closer_to_truth": float(np.mean(
+                [synth.orientation_error((q_pr["theta"][i], q_pr["phi"][i], q_pr["omega"][i]), truth[i]) <
+                 synth.orientation_error((q["theta"][i], q["phi"][i], q["omega"][i]), truth[i])
+                 for i in range(P) if not same[i]])) if apart else 0.0,
+            "cc_abs_error_vs_fp64": {"median": float(np.median(err)), "p99": float(np.quantile(err, 0.99)),
+                                     "max": float(err.max())},
+            "cc_rel_error_vs_fp64": {"median": float(np.median(rel)), "p99": float(np.quantile(rel, 0.99))},
+            "identical_orientation_vs_fp32_form": float(same.mean()),
+            "pr_gap_on_disagreement": float(np.max(np.abs(q["pr"][~same] - q_pr["pr"][~same]) /
+                                                   q_pr["pr"][~same])) if (~same).any() else 0.0,
+            "median_error_vs_truth_deg": float(np.median(errs))}
+    out["fp32_form"]["median_error_vs_truth_deg"] = float(np.median(
+        [synth.orientation_error((q_pr["theta"][i], q_pr["phi"][i], q_pr["omega"][i]), truth[i]) for i in range(P)]))
+    print(json.dumps(out))
+    ctx.close()
+    return 0
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -496,7 +580,12 @@ def main():
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--ref-seconds", type=float, default=15.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--precision-report", type=int, default=0, metavar="P",
+                    help="instead of the bench line: BF16 and FP8 contraction against FP64 scores and the "
+                         "exhaustive FP32 search on P particles of the box-128 configuration (0.5-degree grid)")
     args = ap.parse_args()
+    if args.precision_report:
+        return run_precision_report(args)
     if args.searchstep:
         WORKLOAD["searchstep"] = args.searchstep
     if args.origin_step:

@@ -805,6 +805,9 @@ int contract_impl(Ctx* c, const float* imgs, bool on_device, cryoim_particle* pa
         return fail(CRYOIM_ERR_STATE, "PR rescoring needs cryoim_load_templates");
     if (opts->precision != 0 && opts->precision != 1) return fail(CRYOIM_ERR_ARG, "precision must be 0 or 1");
     const bool f8 = opts->precision == 1;
+    const int nbr = opts->nbr <= 0 ? 1 : opts->nbr;
+    const int nbox = (2 * nbr + 1) * (2 * nbr + 1) * (2 * nbr + 1);
+    if (nbr > 3 || (long)nbox * k > 4096) return fail(CRYOIM_ERR_ARG, "(2 nbr + 1)^3 x topk must be <= 4096");
     if (P == 0) return CRYOIM_OK;
     if ((r = f8 ? ensure_bmat8(c) : ensure_bmat(c))) return r;
     const int kpad = f8 ? c->cKpad8 : c->cKpad;
@@ -843,8 +846,8 @@ int contract_impl(Ctx* c, const float* imgs, bool on_device, cryoim_particle* pa
         (r = c->kpr.ensure((size_t)pb * k)))
         return r;
     if (T > 0 && (r = c->kalpha.ensure((size_t)pb * k * T * 60))) return r;
-    // rescoring set: each selected orientation and its 26 grid neighbours
-    const int maxx = 27 * k;
+    // rescoring set: each selected orientation and its grid neighbours within nbr steps
+    const int maxx = nbox * k;
     if ((r = c->tilev.ensure((size_t)pb * ntiles)) || (r = c->tileo.ensure((size_t)pb * ntiles)) ||
         (r = c->tileorig.ensure((size_t)pb * ntiles)) || (r = c->xcand.ensure((size_t)pb * maxx * 5)) ||
         (r = c->xpr.ensure((size_t)pb * maxx)))
@@ -960,8 +963,9 @@ int contract_impl(Ctx* c, const float* imgs, bool on_device, cryoim_particle* pa
         launch_cc_fp64(c->mapcube.p, c->band.p, ctfp, c->bd, c->csamples.p, c->cS, c->kcand.p, k, nb,
                        c->kcc64.p, c->stream);
         // Phase-residual rescoring at the particle's own origin (ort_globesearch.f90 scores
-        // every view at particle(i)%x, %y) over each selected orientation and its 26 grid
-        // neighbours; the result equals the exhaustive search wherever its minimum lies there.
+        // every view at particle(i)%x, %y) over each selected orientation and its grid
+        // neighbours within nbr steps; the result equals the exhaustive search wherever its
+        // minimum lies there.  The set is sorted by orientation index, without repeats.
         std::vector<std::vector<int>> xs(nb);
         int maxc = 1;
         const int span = 2 * c->nph + 1;
@@ -973,18 +977,18 @@ int contract_impl(Ctx* c, const float* imgs, bool on_device, cryoim_particle* pa
                     if (n < 0) continue;
                     const int v = n / c->nom, io = n % c->nom, slot = c->view_slot[v];
                     const int it = slot / span, ips = slot % span - c->nph;
-                    for (int dt = -1; dt <= 1; ++dt)
-                        for (int dp = -1; dp <= 1; ++dp) {
+                    for (int dt = -nbr; dt <= nbr; ++dt)
+                        for (int dp = -nbr; dp <= nbr; ++dp) {
                             const int it2 = it + dt, ips2 = ips + dp;
                             if (it2 < 0 || it2 > c->nth || ips2 < -c->nph || ips2 > c->nph) continue;
                             const int v2 = c->slot_view[(size_t)it2 * span + ips2 + c->nph];
                             if (v2 < 0) continue;
-                            for (int dw = -1; dw <= 1; ++dw) {
-                                const int n2 = v2 * c->nom + (io + dw + c->nom) % c->nom;
-                                if (std::find(lst.begin(), lst.end(), n2) == lst.end()) lst.push_back(n2);
-                            }
+                            for (int dw = -nbr; dw <= nbr; ++dw)
+                                lst.push_back(v2 * c->nom + ((io + dw) % c->nom + c->nom) % c->nom);
                         }
                 }
+                std::sort(lst.begin(), lst.end());
+                lst.erase(std::unique(lst.begin(), lst.end()), lst.end());
                 if (lst.empty()) lst.push_back(0);
                 maxc = std::max(maxc, (int)lst.size());
             }

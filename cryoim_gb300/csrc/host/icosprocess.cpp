@@ -12,8 +12,9 @@
 //   5  local refinement (ort_refinement.f90) -> newortfile
 // Extension keys without a reference counterpart: device, batch (particles per device
 // call), contract=y (mode 4 through the tensor-core contraction), originmax,
-// originstep, topk, precision=bf16|fp8 (contraction operands).  Output rows are appended after every chunk, so a run can resume
-// with first=k as with the reference's per-particle writes.
+// originstep, topk, precision=bf16|fp8 (contraction operands), nbr (rescoring
+// neighbourhood in grid steps).  Output rows are appended after every chunk, so a run
+// can resume with first=k as with the reference's per-particle writes.
 #include <algorithm>
 #include <cmath>
 #include <cstdio>
@@ -34,7 +35,7 @@ const char* kKeys[] = {"apix",         "minRes",       "maxRes",     "imgmask", 
                        "realspaceavg", "ortfile",      "recISAF",    "subrec",     "FSC",
                        "imgstck",      "sym",          "maxcentshift", "corrCTF",  "boundX",
                        "loc_box",      "check"};
-const char* kExt[] = {"device", "batch", "contract", "originmax", "originstep", "topk", "precision"};
+const char* kExt[] = {"device", "batch", "contract", "originmax", "originstep", "topk", "precision", "nbr"};
 
 void usage() {
     std::puts(
@@ -47,7 +48,7 @@ void usage() {
         "         searchstep, minRes, maxRes, applyCTF, vol, Cs, ampwg)\n"
         "  mode=5 local refinement into newortfile (Ncycle, templateort, ...)\n"
         "  common: apix imgmask first last imgstck\n"
-        "  GPU extensions: device batch contract=y originmax originstep topk precision=bf16|fp8");
+        "  GPU extensions: device batch contract=y originmax originstep topk precision=bf16|fp8 nbr");
 }
 
 bool yes(const std::string& v) { return !v.empty() && (v[0] == 'y' || v[0] == 'Y'); }
@@ -243,7 +244,7 @@ int main(int argc, char** argv) {
         if (cryoim_load_templates(ctx, timg.data(), t.data(), T)) return die("templates", 2);
         const bool contract = mode == 4 && yes(sval("contract", "n"));
         cryoim_contract_opts co{fval("originmax", 6.0f), fval("originstep", 0.5f), ival("topk", 16), 0,
-                                sval("precision", "bf16") == "fp8" ? 1 : 0};
+                                sval("precision", "bf16") == "fp8" ? 1 : 0, ival("nbr", 1)};
         if (contract) {
             if (map.empty()) return die("contract=y needs model3d", 2);
             if (cryoim_set_reference_map(ctx, map.data())) return die("reference map", 2);

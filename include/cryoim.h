@@ -335,6 +335,9 @@ typedef struct cryoim_contract_opts {
     int32_t pick;       /* 0: minimum phase residual, 1: maximum FP64 correlation  */
     int32_t precision;  /* operands: 0 BF16, 1 FP8-e4m3 with per-band power-of-two
                            scales (both with FP32 accumulation)                    */
+    int32_t nbr;        /* PR rescoring of each candidate's grid neighbours within
+                           nbr steps in theta, phi and omega (1: 26 neighbours; 0 is
+                           taken as 1); (2 nbr + 1)^3 x topk <= 4096                 */
 } cryoim_contract_opts;
 /* The 3D map (nx^3 float32) whose central sections are correlated: its centred Fourier
  * transform is kept as a band cube of (2 maxR + 3)^3 complex values. */
