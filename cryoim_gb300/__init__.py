@@ -256,6 +256,15 @@ class Context:
              *[ptr(x) for x in a], ptr(fsc), ptr(out) if want_map else None)
         return fsc, out
 
+    # -- mode 3 ---------------------------------------------------------------
+    def center(self, imgs, parts: np.ndarray, map3d=None) -> None:
+        """Origin centring (calc_center.f90 against map3d, or calc_center_selfrot180.f90
+        without); parts is updated in place."""
+        assert parts.dtype == PARTICLE_DTYPE and parts.flags["C_CONTIGUOUS"]
+        im = np.ascontiguousarray(imgs, dtype=np.float32)
+        m = None if map3d is None else np.ascontiguousarray(map3d, dtype=np.float32)
+        call("cryoim_center", self._h, ptr(m), ptr(im), ptr(parts), len(parts))
+
     def rec_add_partial(self, fa, fb, wg) -> None:
         """Add a tnf partial (each (maxR+1, 2maxR+1, 2maxR+1)) into the accumulation."""
         a = [np.ascontiguousarray(x, np.float32) for x in (fa, fb, wg)]

@@ -107,6 +107,7 @@ SIGNATURES = {
     "cryoim_merge_fsc_combine": [_vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp],
     "cryoim_rec_finish_merge": [_vp, _vp],
     "cryoim_icosavg": [_vp, _vp, _i32, _f32],
+    "cryoim_center": [_vp, _vp, _vp, _vp, _i32],
     "cryoim_central_sections": [_vp, _vp, _vp, _vp, _i32, _vp, _vp],
     "cryoim_icos_ops": [_vp],
     "cryoim_asu_fold": [_fp, _fp, _fp],

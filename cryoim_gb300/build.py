@@ -7,7 +7,8 @@ include/cryoim.h carries no torch types).  Translation units:
 * score.cu -- hot scoring kernels, multiply-add contraction allowed;
 * api.cu   -- context, drivers, C ABI (host code built with -ffp-contract=off);
 * fsc.cu   -- -fmad=false: half-map FSC and the FSC-weighted map;
-* mapops.cu -- -fmad=false: real-space icosahedral average, merge output step.
+* mapops.cu -- -fmad=false: real-space icosahedral average, merge output step;
+* center.cu -- -fmad=false: origin centring of icosprocess mode 3.
 """
 from __future__ import annotations
 
@@ -49,6 +50,7 @@ UNITS = {
     "contract.cu": [],
     "fsc.cu": ["-fmad=false"],
     "mapops.cu": ["-fmad=false"],
+    "center.cu": ["-fmad=false"],
 }
 
 

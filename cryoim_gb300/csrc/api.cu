@@ -1709,6 +1709,147 @@ int cryoim_rec_add_partial(void* ctx, const float* fa, const float* fb, const fl
     return CRYOIM_OK;
 }
 
+// icosprocess mode 3.  With map3d: calc_center.f90:22-105 (the map masked by img3d_mask
+// and transformed once; per particle the image masked at its origin and low-passed, the
+// model's projection at its orientation with the CTF, masked at the centre and
+// low-passed, both normalised, cross-correlated, Gaussian fit of the peak).  Without:
+// calc_center_selfrot180.f90:22-86 (the image against itself rotated by 180 degrees,
+// half the peak offset).
+int cryoim_center(void* ctx, const float* map3d, const float* imgs, cryoim_particle* parts, int32_t P) {
+    Ctx* c = as_ctx(ctx);
+    int r = check_ready(c, false);
+    if (r) return r;
+    if (!imgs || !parts || P < 0) return fail(CRYOIM_ERR_ARG, "null input or negative count");
+    if (P == 0) return CRYOIM_OK;
+    const int nx = c->p.fftsize, B = c->batch, R = c->p.max_r;
+    const long nn = (long)nx * nx, n3 = nn * nx;
+    const bool model = map3d != nullptr, mask = c->p.use_imgmask != 0;
+    if ((r = ensure_batch(c, B))) return r;
+    DBuf<float2> f2;
+    DBuf<float> a1, a2, ore, oim, ctfb, eul, out, fr, fi;
+    DBuf<double> acc2;
+    if ((r = f2.ensure((size_t)B * nn)) || (r = a1.ensure((size_t)B * nn)) || (r = a2.ensure((size_t)B * nn)) ||
+        (r = out.ensure((size_t)3 * B)) || (r = acc2.ensure(2)))
+        return r;
+    if (model && ((r = ore.ensure((size_t)B * nn)) || (r = oim.ensure((size_t)B * nn)) ||
+                  (r = ctfb.ensure((size_t)B * nn)) || (r = eul.ensure((size_t)3 * B)) || (r = fr.ensure(n3)) ||
+                  (r = fi.ensure(n3))))
+        return r;
+    if (model) {  // calc_center.f90:24-38
+        DBuf<float> dmap;
+        DBuf<float2> work;
+        if ((r = dmap.ensure(n3)) || (r = work.ensure(n3))) return r;
+        CK(cudaMemcpyAsync(dmap.p, map3d, sizeof(float) * n3, cudaMemcpyHostToDevice, c->stream));
+        if (mask) CK(launch_mask3d(dmap.p, nx, c->p.imgmask_px, acc2.p, c->stream));
+        launch_map_checker(dmap.p, nx, work.p, c->stream);
+        cufftHandle h3;
+        CKF(cufftPlan3d(&h3, nx, nx, nx, CUFFT_C2C));
+        cufftResult fr3 = cufftSetStream(h3, c->stream);
+        if (fr3 == CUFFT_SUCCESS) fr3 = cufftExecC2C(h3, (cufftComplex*)work.p, (cufftComplex*)work.p, CUFFT_FORWARD);
+        cudaError_t e = fr3 == CUFFT_SUCCESS ? launch_center_ft(work.p, nx, fr.p, fi.p, c->stream) : cudaSuccess;
+        if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+        cufftDestroy(h3);
+        if (fr3 != CUFFT_SUCCESS) return fail(CRYOIM_ERR_CUDA, "3D forward FFT failed: cufft %d", (int)fr3);
+        if (e != cudaSuccess) return fail(CRYOIM_ERR_CUDA, "centring map: %s", cudaGetErrorString(e));
+    }
+    // a forward or backward transform of the first nb images of buf, img2d_FFT-style
+    auto xform = [&](float2* buf, int nb, bool fwd) -> int {
+        cufftHandle h;
+        if ((r = plan2d(c, nb, &h))) return r;
+        CKF(cufftExecC2C(h, (cufftComplex*)buf, (cufftComplex*)buf, fwd ? CUFFT_FORWARD : CUFFT_INVERSE));
+        launch_ref_post(buf, (long)nb * nn, fwd ? (float)nn : 1.0f, c->stream);
+        return CRYOIM_OK;
+    };
+    // img2d_lowpass of the shifted complex images in buf (from prep or pack), into real dst
+    auto lowpass = [&](float2* buf, int nb, float* dst) -> int {
+        if ((r = xform(buf, nb, true))) return r;
+        launch_lowpass(buf, nx, (long)nb * nn, R, c->stream);
+        if ((r = xform(buf, nb, false))) return r;
+        launch_real_shift(buf, nx, (long)nb * nn, dst, c->stream);
+        return CRYOIM_OK;
+    };
+    Band bf{};  // the full nx x nx CTF through the band kernel: window = whole image
+    bf.nx = nx; bf.max_r = nx / 2; bf.W = nx;
+    const ParView pv = par_view(c, B);
+    std::vector<float> hpar(8 * B), heul(3 * B), hout(3 * B);
+    int id0 = -100;
+    float sdf[3] = {0, 0, 0};
+    for (int b0 = 0; b0 < P; b0 += B) {
+        const int nb = std::min(B, P - b0);
+        const long m = (long)nb * nn;
+        CK(cudaMemcpyAsync(c->imgs.p, imgs + b0 * nn, sizeof(float) * m, cudaMemcpyHostToDevice, c->stream));
+        std::fill(hpar.begin(), hpar.end(), 0.0f);
+        for (int i = 0; i < nb; ++i) {
+            const cryoim_particle& q = parts[b0 + i];
+            if (model) { hpar[i] = q.x; hpar[B + i] = q.y; }
+            if (q.img_id != id0) { sdf[0] = q.df1; sdf[1] = q.df2; sdf[2] = q.astigang; id0 = q.img_id; }
+            hpar[4 * B + 3 * i] = sdf[0]; hpar[4 * B + 3 * i + 1] = sdf[1]; hpar[4 * B + 3 * i + 2] = sdf[2];
+            heul[3 * i] = q.theta; heul[3 * i + 1] = q.phi; heul[3 * i + 2] = q.omega;
+        }
+        CK(cudaMemcpyAsync(c->par.p, hpar.data(), sizeof(float) * 8 * B, cudaMemcpyHostToDevice, c->stream));
+        CK(cudaMemsetAsync(c->flag.p, 0, sizeof(int), c->stream));
+        if (model) {
+            // a1: mask at the particle's origin, low pass (calc_center.f90:55-56)
+            if (mask) launch_prep_images(c->imgs.p, nb, nx, pv.ox, pv.oy, 1, c->p.imgmask_px, 0, c->fft.p, c->flag.p,
+                                         c->stream);
+            else launch_pack_shift(c->imgs.p, nullptr, nx, m, c->fft.p, c->stream);
+            if ((r = lowpass(c->fft.p, nb, a1.p))) return r;
+            // a2: projection of the model (project2d_FT3dTo2d.f90), CTF, mask, low pass (:57-67)
+            CK(cudaMemcpyAsync(eul.p, heul.data(), sizeof(float) * 3 * nb, cudaMemcpyHostToDevice, c->stream));
+            launch_sections(fr.p, fi.p, nx, eul.p, nb, ore.p, oim.p, c->stream);
+            launch_pack_shift(ore.p, oim.p, nx, m, f2.p, c->stream);
+            if ((r = xform(f2.p, nb, false))) return r;
+            launch_real_shift(f2.p, nx, m, a2.p, c->stream);
+            if (c->p.apply_ctf) {  // img2d_applyCTF.f90
+                launch_ctf_band(nb, bf, pv.dfs, c->p.apix, c->p.vol, c->p.cs, c->p.ampwg, ctfb.p, c->stream);
+                launch_pack_shift(a2.p, nullptr, nx, m, f2.p, c->stream);
+                if ((r = xform(f2.p, nb, true))) return r;
+                launch_ctf_mul(f2.p, ctfb.p, m, c->stream);
+                if ((r = xform(f2.p, nb, false))) return r;
+                launch_real_shift(f2.p, nx, m, a2.p, c->stream);
+            }
+            if (mask) launch_prep_images(a2.p, nb, nx, pv.sx, pv.sy, 1, c->p.imgmask_px, 0, f2.p, c->flag.p,
+                                         c->stream);  // sx, sy are zero here: the centre
+            else launch_pack_shift(a2.p, nullptr, nx, m, f2.p, c->stream);
+            if ((r = lowpass(f2.p, nb, a2.p))) return r;
+            launch_norm(a1.p, nx, nb, c->stream);
+            launch_norm(a2.p, nx, nb, c->stream);
+        } else {
+            // calc_center_selfrot180.f90:39-52: low pass, mask at the centre, norm, rotate
+            launch_pack_shift(c->imgs.p, nullptr, nx, m, c->fft.p, c->stream);
+            if ((r = lowpass(c->fft.p, nb, a1.p))) return r;
+            if (mask) {
+                launch_prep_images(a1.p, nb, nx, pv.ox, pv.oy, 1, c->p.imgmask_px, 0, c->fft.p, c->flag.p, c->stream);
+                launch_real_shift(c->fft.p, nx, m, a1.p, c->stream);
+            }
+            launch_norm(a1.p, nx, nb, c->stream);
+            launch_rot180(a1.p, a2.p, nx, m, c->stream);
+        }
+        // cross_correlation.f90 and the peak (calc_center.f90:71-86)
+        launch_pack(a1.p, m, c->fft.p, c->stream);
+        launch_pack(a2.p, m, f2.p, c->stream);
+        if ((r = xform(c->fft.p, nb, true)) || (r = xform(f2.p, nb, true))) return r;
+        launch_cross_power(c->fft.p, f2.p, nx, m, c->stream);
+        if ((r = xform(c->fft.p, nb, false))) return r;
+        launch_peak(c->fft.p, nx, nb, model ? 0 : 1, out.p, c->stream);
+        CK(cudaGetLastError());
+        CK(cudaMemcpyAsync(hout.data(), out.p, sizeof(float) * 3 * nb, cudaMemcpyDeviceToHost, c->stream));
+        if ((r = check_flag(c))) return r;
+        for (int i = 0; i < nb; ++i) {  // calc_center.f90:87-99
+            cryoim_particle& q = parts[b0 + i];
+            float cc = hout[3 * i + 2];
+            if (cc >= 1.0f) cc = 1.0f;
+            if (cc <= -1.0f) cc = -1.0f;
+            q.x0 = q.x; q.y0 = q.y; q.pr0 = q.pr;
+            q.x = hout[3 * i];
+            q.y = hout[3 * i + 1];
+            q.pr = std::acos(cc) * 45.0f / std::atan2(1.0f, 1.0f);
+            q.dx = q.x - q.x0; q.dy = q.y - q.y0; q.dpr = q.pr - q.pr0;
+        }
+    }
+    return CRYOIM_OK;
+}
+
 int cryoim_central_sections(void* ctx, const float* ft_re, const float* ft_im, const float* eulers,
                             int32_t n, float* out_re, float* out_im) {
     Ctx* c = as_ctx(ctx);

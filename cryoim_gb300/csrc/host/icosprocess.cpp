@@ -8,6 +8,7 @@
 //   0  project the model along every template orientation into templatestck
 //   1  symmetrised reconstruction into result3d (map, or tnf partial with subrec=y;
 //      FSC=y: gold-standard half maps, FSC.txt and the FSC-weighted map)
+//   3  origin centring (calc_center.f90 / calc_center_selfrot180.f90) -> newortfile
 //   4  global orientation search (ort_globesearch.f90) -> newortfile
 //   5  local refinement (ort_refinement.f90) -> newortfile
 // Extension keys without a reference counterpart: device, batch (particles per device
@@ -40,10 +41,11 @@ const char* kExt[] = {"device", "batch", "contract", "originmax", "originstep", 
 void usage() {
     std::puts(
         "icosprocess (cryoim_gb300): icosahedral projection matching on a GB300 GPU\n"
-        "usage: icosprocess mode=<0|1|4|5> ortfile=<ort> key=value ...\n"
+        "usage: icosprocess mode=<0|1|3|4|5> ortfile=<ort> key=value ...\n"
         "  mode=0 project model3d along templateort into templatestck\n"
         "  mode=1 reconstruct into result3d      (PR_threshold, boundX, subrec, applyCTF;\n"
         "         FSC=y: odd/even half maps oddtnf, evetnf, FSC.txt, FSC-weighted result3d)\n"
+        "  mode=3 origin centring into newortfile (against model3d, or the 180-degree self-rotation)\n"
         "  mode=4 global search into newortfile  (templateort + templatestck or model3d,\n"
         "         searchstep, minRes, maxRes, applyCTF, vol, Cs, ampwg)\n"
         "  mode=5 local refinement into newortfile (Ncycle, templateort, ...)\n"
@@ -268,6 +270,29 @@ int main(int argc, char** argv) {
             if (cryoim_ort_write(out.c_str(), &parts[i0], &names[(size_t)i0 * 256], 256, n, 54, 1))
                 return die("cannot write newortfile", 2);
         }
+    } else if (mode == 3) {
+        // 0main.f90:237-241: calc_center with model3d, else calc_center_selfrot180; then
+        // output_ort.f90 writes every particle of first..last to newortfile
+        std::vector<float> map;
+        if (has("model3d")) {
+            map.resize((size_t)nx * nx * nx);
+            if (cryoim_mrc_read_sections(sval("model3d", "").c_str(), 1, nx, map.data())) return die("model3d", 2);
+        }
+        // calc_center.f90:40-53 reads the particles' own stacks even with imgstck
+        const std::string src = map.empty() ? imgstck : std::string();
+        for (int i0 = 0; i0 < P; i0 += chunk) {
+            const int n = std::min(chunk, P - i0);
+            if (gather(parts, stck, i0, n, nx, src, p.first, imgs)) return die("particle stack read", 2);
+            if (cryoim_center(ctx, map.empty() ? nullptr : map.data(), imgs.data(), &parts[i0], n))
+                return die("centring", 2);
+            for (int i = 0; i < n; ++i) {
+                const cryoim_particle& q = parts[i0 + i];
+                std::printf("%12d %14.7f %14.7f %14.7f\n", p.first + i0 + i, q.x, q.y, q.pr);
+            }
+        }
+        const std::string out = sval("newortfile", "newort.dat");
+        if (cryoim_ort_write(out.c_str(), parts.data(), names.data(), 256, P, 54, 0))
+            return die("cannot write newortfile", 2);
     } else if (mode == 1 && p.fsc) {
         // 0main.f90:207-222: odd half (first, first+2, ...) into oddtnf, even half
         // (first+1, ...) into evetnf, both masked at particle(first)'s origin; without
@@ -351,7 +376,7 @@ int main(int argc, char** argv) {
             if (cryoim_mrc_write(out.c_str(), &oh, map.data(), (int64_t)map.size())) return die("cannot write result3d", 2);
         }
     } else {
-        return die("mode must be 0, 1, 4 or 5 on this path", 2);
+        return die("mode must be 0, 1, 3, 4 or 5 on this path", 2);
     }
     cryoim_ctx_destroy(ctx);
     return 0;

@@ -184,6 +184,21 @@ cudaError_t launch_fsc_shells(const FscArgs& a, double* sums, int sms, cudaStrea
 // wt: maxR+1 shell weights; vol: nx^3 complex, zeroed and filled with cmplx(fa, fb)
 cudaError_t launch_fsc_fold(const FscArgs& a, const float* wt, float2* vol, cudaStream_t st);
 
+// ---- center.cu: mode-3 origin centring (buffers of B x nx^2, float2 = (a, b) in the
+// img2d_FFT convention b = -Im) -------------------------------------------------
+cudaError_t launch_mask3d(float* map, int nx, float mask, double* acc2, cudaStream_t st);
+cudaError_t launch_center_ft(const float2* ft, int nx, float* fr, float* fi, cudaStream_t st);
+void launch_ref_post(float2* b, long n, float s, cudaStream_t st);
+void launch_lowpass(float2* b, int nx, long n, int lp, cudaStream_t st);
+void launch_ctf_mul(float2* b, const float* ctf, long n, cudaStream_t st);
+void launch_real_shift(const float2* b, int nx, long n, float* out, cudaStream_t st);
+void launch_pack_shift(const float* re, const float* im, int nx, long n, float2* b, cudaStream_t st);
+void launch_pack(const float* re, long n, float2* b, cudaStream_t st);
+void launch_norm(float* img, int nx, int B, cudaStream_t st);
+void launch_cross_power(float2* f1, const float2* f2, int nx, long n, cudaStream_t st);
+void launch_rot180(float* a1, float* a2, int nx, long n, cudaStream_t st);
+void launch_peak(const float2* cc, int nx, int B, int half, float* out, cudaStream_t st);
+
 // ---- mapops.cu: whole-map real-space operations ------------------------------
 // real-space icosahedral average of an nx^3 map (in != out), radius r0 pixels
 cudaError_t launch_icosavg(const float* in, int nx, float r0, const float* ops, int nsym, float* out,

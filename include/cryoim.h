@@ -268,6 +268,20 @@ int cryoim_rec_finish_merge(void* ctx, float* map);
  * cryoim_fsc_combine when the parameters ask for realspaceavg (r0 = imgmask_px). */
 int cryoim_icosavg(void* ctx, float* map, int32_t n, float r0);
 
+/* ---- origin centring (icosprocess mode 3) -------------------------------- */
+
+/* Re-centre P particles (host images, P x nx^2): with map3d (nx^3, the model) as
+ * calc_center.f90:22-105 — each image masked at its origin and Gaussian low-passed
+ * (1/e^2 at maxR) is cross-correlated with the model's projection at its orientation
+ * (CTF applied when apply_ctf, masked at the centre, low-passed); with map3d NULL as
+ * calc_center_selfrot180.f90:22-86 — the image against itself rotated by 180 degrees.
+ * A Gaussian fit of the correlation peak gives the new origin (set to 0 beyond nx/16)
+ * and PR = acos(peak) in degrees; x0, y0, pr0 keep the old values, dx, dy, dpr the
+ * changes; orientations are not touched.  Replaces the mode-3 branch of
+ * icosprocess/SRC/0main.f90:237-241. */
+int cryoim_center(void* ctx, const float* map3d, const float* imgs, cryoim_particle* parts,
+                  int32_t P);
+
 /* ---- files (host only; byte-compatible with the reference) ---------------- */
 
 /* The `mrchead` type of icosprocess/SRC/0common_icosproc.f90:61-112: 1024 bytes. */

@@ -1326,6 +1326,206 @@ template <class R> void icosavg(const float* in, int nx, R r0, float* out) {
 }
 
 /* ------------------------------------------------------------------------ */
+/* origin centring (icosprocess mode 3)                                        */
+/* ------------------------------------------------------------------------ */
+
+/* icosprocess/SRC/img2d_lowpass.f90:2-33: exp(-r^2 / (2 lp^2)) in Fourier space. */
+template <class R> void img2d_lowpass(R* a, int nx, int lp) {
+    const long nn = (long)nx * nx;
+    std::vector<R> b(nn, R(0));
+    const R lowpass = R(2) * (R)(lp * lp);
+    for (long i = 0; i < nn; ++i)
+        if (((i / nx) + (i % nx)) & 1) a[i] = -a[i];
+    img2d_fft(a, b.data(), nx, nx, 1);
+    for (long i = 0; i < nn; ++i) {
+        int ky = (int)(i / nx), hx = (int)(i % nx);
+        R r2 = (R)((hx - nx / 2) * (hx - nx / 2) + (ky - nx / 2) * (ky - nx / 2));
+        R huv = std::exp(-r2 / lowpass);
+        a[i] = a[i] * huv / (R)(float)nn;
+        b[i] = b[i] * huv / (R)(float)nn;
+    }
+    img2d_fft(a, b.data(), nx, nx, -1);
+    for (long i = 0; i < nn; ++i)
+        if (((i / nx) + (i % nx)) & 1) a[i] = -a[i];
+}
+
+/* icosprocess/SRC/img2d_applyCTF.f90:2-28. */
+template <class R> void img2d_apply_ctf(R* a, int nx, const R* ctf) {
+    const long nn = (long)nx * nx;
+    std::vector<R> b(nn, R(0));
+    for (long i = 0; i < nn; ++i)
+        if (((i / nx) + (i % nx)) & 1) a[i] = -a[i];
+    img2d_fft(a, b.data(), nx, nx, 1);
+    for (long i = 0; i < nn; ++i) { a[i] = a[i] * ctf[i]; b[i] = b[i] * ctf[i]; }
+    img2d_fft(a, b.data(), nx, nx, -1);
+    for (long i = 0; i < nn; ++i)
+        if (((i / nx) + (i % nx)) & 1) a[i] = -a[i];
+}
+
+/* icosprocess/SRC/cross_correlation.f90:1-26: a1 <- the centred cross-correlation map. */
+template <class R> void cross_correlation(R* a1, R* a2, int nx) {
+    const long nn = (long)nx * nx;
+    std::vector<R> b1(nn, R(0)), b2(nn, R(0));
+    img2d_fft(a1, b1.data(), nx, nx, 1);
+    img2d_fft(a2, b2.data(), nx, nx, 1);
+    for (long i = 0; i < nn; ++i) {
+        R x = a1[i] * a2[i] + b1[i] * b2[i];
+        R y = b1[i] * a2[i] - a1[i] * b2[i];
+        if (((i / nx) + (i % nx)) & 1) { x = -x; y = -y; }
+        a1[i] = x; b1[i] = y;
+    }
+    img2d_fft(a1, b1.data(), nx, nx, -1);
+}
+
+/* icosprocess/SRC/guass_regression.f90:1-56; z[j+1][i+1] = z(i, j). */
+template <class R> void gauss_regression(const R z[3][3], R* dx, R* dy, R* cc) {
+    R c10 = 0, c01 = 0, c11 = 0, c20 = 0, c02 = 0, c00 = 0;
+    for (int j = -1; j <= 1; ++j)
+        for (int i = -1; i <= 1; ++i) c10 = c10 + (R)i * std::log(z[j + 1][i + 1]);
+    c10 = c10 / R(6);
+    for (int j = -1; j <= 1; ++j)
+        for (int i = -1; i <= 1; ++i) c01 = c01 + (R)j * std::log(z[j + 1][i + 1]);
+    c01 = c01 / R(6);
+    for (int j = -1; j <= 1; ++j)
+        for (int i = -1; i <= 1; ++i) c11 = c11 + (R)(i * j) * std::log(z[j + 1][i + 1]);
+    c11 = c11 / R(4);
+    for (int j = -1; j <= 1; ++j)
+        for (int i = -1; i <= 1; ++i) c20 = c20 + (R)(3 * i * i - 2) * std::log(z[j + 1][i + 1]);
+    c20 = c20 / R(6);
+    for (int j = -1; j <= 1; ++j)
+        for (int i = -1; i <= 1; ++i) c02 = c02 + (R)(3 * j * j - 2) * std::log(z[j + 1][i + 1]);
+    c02 = c02 / R(6);
+    for (int j = -1; j <= 1; ++j)
+        for (int i = -1; i <= 1; ++i) c00 = c00 + (R)(5 - 3 * i * i - 3 * j * j) * std::log(z[j + 1][i + 1]);
+    c00 = c00 / R(9);
+    R den = R(4) * c20 * c02 - c11 * c11;
+    *dx = (c11 * c01 - R(2) * c10 * c02) / den;
+    *dy = (c11 * c10 - R(2) * c01 * c20) / den;
+    *cc = std::exp(c00 - c20 * (*dx * *dx) - c11 * *dx * *dy - c02 * (*dy * *dy));
+}
+
+/* icosprocess/SRC/img3d_mask.f90:3-56 at the box centre. */
+template <class R> void img3d_mask(R* d, int nx, R mask) {
+    const R pi = C<R>::pi();
+    R R1 = mask - R(3);
+    if (R1 <= R(0)) R1 = R(0);
+    R R2 = mask + R(3);
+    if (R2 > (R)(nx / 2)) R2 = (R)(nx / 2);
+    const R c = (R)(nx / 2);
+    const long n3 = (long)nx * nx * nx;
+    auto radius = [&](long q) {
+        int iz = (int)(q / ((long)nx * nx)), iy = (int)((q / nx) % nx), ix = (int)(q % nx);
+        R yy = (-c + (R)iy) * (-c + (R)iy), xx = (-c + (R)ix) * (-c + (R)ix), zz = (-c + (R)iz) * (-c + (R)iz);
+        return std::sqrt(xx + yy + zz);
+    };
+    double summ = 0;
+    long num = 0;
+    for (long q = 0; q < n3; ++q) {
+        R ra = radius(q);
+        if (ra > R1 && ra <= R2) { summ = summ + (double)d[q]; ++num; }
+    }
+    if (num != 0) summ = summ / (double)(float)num;
+    for (long q = 0; q < n3; ++q) {
+        R ra = radius(q);
+        if (ra > R1 && ra <= R2) {
+            R edge = (R(1) + std::cos(pi * (ra - R1) / R(6))) / R(2);
+            d[q] = (R)((double)(d[q] * edge) + (double)(R(1) - edge) * summ);
+        }
+        if (ra > R2) d[q] = (R)summ;
+    }
+}
+
+/* The peak of calc_center.f90:71-86 (first maximum; 3 x 3 neighbourhood with its linear
+ * index clamped to the image, where the reference reads past it), then the Gaussian fit;
+ * half = 1 halves the offset (calc_center_selfrot180.f90:72-73). */
+template <class R> void cc_peak(const R* a1, int nx, int half, R* cx, R* cy, R* cc) {
+    const long nn = (long)nx * nx;
+    long n0 = 0;
+    for (long i = 1; i < nn; ++i)
+        if (a1[i] > a1[n0]) n0 = i;
+    int iy0 = (int)(n0 / nx), ix0 = (int)(n0 % nx);
+    R z[3][3];
+    for (int ky = -1; ky <= 1; ++ky)
+        for (int hx = -1; hx <= 1; ++hx) {
+            long j = (long)(iy0 + ky) * nx + (ix0 + hx);
+            j = j < 0 ? 0 : (j >= nn ? nn - 1 : j);
+            z[ky + 1][hx + 1] = a1[j];
+        }
+    R dx, dy;
+    gauss_regression(z, &dx, &dy, cc);
+    *cx = (R)(ix0 - nx / 2) + dx;
+    *cy = (R)(iy0 - nx / 2) + dy;
+    if (half) { *cx = *cx / R(2); *cy = *cy / R(2); }
+    if (std::fabs(*cx) >= (R)nx / R(16)) *cx = R(0);
+    if (std::fabs(*cy) >= (R)nx / R(16)) *cy = R(0);
+}
+
+/* icosprocess/SRC/calc_center.f90:22-105 (map given) or calc_center_selfrot180.f90:22-86
+ * (map NULL); out: (centx, centy, cc) per particle before the record update. */
+template <class R>
+int center(const cryoim_params* p, const float* map, const float* imgs, const cryoim_particle* parts, int P,
+           R* out) {
+    const int nx = p->fftsize, maxR = p->max_r;
+    const long nn = (long)nx * nx, n3 = nn * nx;
+    std::vector<R> fr, fi;
+    if (map) {
+        std::vector<R> re(map, map + n3), im(n3, R(0));
+        if (p->use_imgmask) img3d_mask(re.data(), nx, (R)p->imgmask_px);
+        for (long q = 0; q < n3; ++q)
+            if (((q / nn) + (q / nx) % nx + q % nx) & 1) re[q] = -re[q];
+        fft3d(re.data(), im.data(), nx, -1);
+        const R s = (R)(float)n3;
+        fr.resize(n3); fi.resize(n3);
+        for (long q = 0; q < n3; ++q) {
+            R a = re[q] / s, b = im[q] / s;
+            if (((q / nn) + (q / nx) % nx + q % nx) & 1) { a = -a; b = -b; }
+            fr[q] = a; fi[q] = -b;
+        }
+    }
+    std::vector<R> a1(nn), a2(nn), si(nn), ctf(nn, R(1));
+    int id0 = -100;
+    for (int ip = 0; ip < P; ++ip) {
+        const cryoim_particle& q = parts[ip];
+        for (long i = 0; i < nn; ++i) a1[i] = (R)imgs[(long)ip * nn + i];
+        if (map) {
+            if (p->use_imgmask) img2d_mask(a1.data(), nx, (R)p->imgmask_px, (R)q.x, (R)q.y);
+            img2d_lowpass(a1.data(), nx, maxR);
+            central_section(fr.data(), fi.data(), nx, (R)q.theta, (R)q.phi, (R)q.omega, a2.data(), si.data());
+            for (long i = 0; i < nn; ++i)
+                if (((i / nx) + (i % nx)) & 1) { a2[i] = -a2[i]; si[i] = -si[i]; }
+            img2d_fft(a2.data(), si.data(), nx, nx, -1);
+            for (long i = 0; i < nn; ++i)
+                if (((i / nx) + (i % nx)) & 1) a2[i] = -a2[i];
+            if (p->apply_ctf) {
+                if (q.img_id != id0) {
+                    get_ctf2d(nx, (R)q.df1, (R)q.df2, (R)q.astigang, (R)p->apix, (R)p->vol, (R)p->cs, (R)p->ampwg,
+                              ctf.data());
+                    id0 = q.img_id;
+                }
+                img2d_apply_ctf(a2.data(), nx, ctf.data());
+            }
+            if (p->use_imgmask) img2d_mask(a2.data(), nx, (R)p->imgmask_px, R(0), R(0));
+            img2d_lowpass(a2.data(), nx, maxR);
+            img2d_norm(a1.data(), nx);
+            img2d_norm(a2.data(), nx);
+        } else {
+            img2d_lowpass(a1.data(), nx, maxR);
+            if (p->use_imgmask) img2d_mask(a1.data(), nx, (R)p->imgmask_px, R(0), R(0));
+            img2d_norm(a1.data(), nx);
+            std::fill(a2.begin(), a2.end(), R(0));
+            for (long i = 0; i < nn; ++i) {
+                int ky = (int)(i / nx), hx = (int)(i % nx);
+                if (hx == 0 || ky == 0) a1[i] = R(0);
+                else a2[(long)(nx - ky) * nx + (nx - hx)] = a1[i];
+            }
+        }
+        cross_correlation(a1.data(), a2.data(), nx);
+        cc_peak(a1.data(), nx, map ? 0 : 1, &out[3 * ip], &out[3 * ip + 1], &out[3 * ip + 2]);
+    }
+    return 0;
+}
+
+/* ------------------------------------------------------------------------ */
 /* proc_icos                                                                   */
 /* ------------------------------------------------------------------------ */
 
@@ -1469,6 +1669,16 @@ template <class R> void transform_ort(int to, R* th, R* ph, R* om, int n) {
     }                                                                                                  \
     extern "C" void orc_icosavg_##S(const float* in, int nx, R r0, float* out) {                     \
         icosavg<R>(in, nx, r0, out);                                                                   \
+    }                                                                                                  \
+    extern "C" int orc_center_##S(const cryoim_params* p, const float* map, const float* im,         \
+                                   const cryoim_particle* pa, int P, R* out) {                         \
+        return center<R>(p, map, im, pa, P, out);                                                      \
+    }                                                                                                  \
+    extern "C" void orc_lowpass_##S(R* a, int nx, int lp) { img2d_lowpass<R>(a, nx, lp); }          \
+    extern "C" void orc_gauss_regression_##S(const R* z, R* out) {                                   \
+        R zz[3][3];                                                                                    \
+        for (int k = 0; k < 9; ++k) zz[k / 3][k % 3] = z[k];                                           \
+        gauss_regression<R>(zz, &out[0], &out[1], &out[2]);                                            \
     }                                                                                                  \
     extern "C" void orc_equalort_##S(R th, R ph, R om, R* out) { equalort<R>(th, ph, om, out); }      \
     extern "C" void orc_transform_ort_##S(int to, R* th, R* ph, R* om, int n) {                      \

@@ -321,6 +321,33 @@ def icosavg(map3d, r0, fp="f64"):
     return out
 
 
+def center(params, imgs, parts, map3d=None, fp="f64"):
+    """calc_center.f90 (map3d given) / calc_center_selfrot180.f90: (P, 3) of (centx,
+    centy, cc) before the record update."""
+    dt = _dt(fp)
+    im = np.ascontiguousarray(imgs, np.float32)
+    m = None if map3d is None else np.ascontiguousarray(map3d, np.float32)
+    out = np.zeros((len(parts), 3), dt)
+    r = _fn("center", fp)(C.byref(params), _p(m), _p(im), _p(np.ascontiguousarray(parts)),
+                          C.c_int(len(parts)), _p(out))
+    assert r == 0
+    return out
+
+
+def lowpass(img, lp, fp="f64"):
+    a = np.array(img, _dt(fp), copy=True, order="C")
+    _fn("lowpass", fp)(_p(a), C.c_int(a.shape[0]), C.c_int(lp))
+    return a
+
+
+def gauss_regression(z, fp="f64"):
+    """z[j+1][i+1] = z(i, j) of guass_regression.f90; returns (dx, dy, cc)."""
+    zz = np.ascontiguousarray(z, _dt(fp)).reshape(9)
+    out = np.zeros(3, _dt(fp))
+    _fn("gauss_regression", fp)(_p(zz), _p(out))
+    return out
+
+
 def equalort(theta, phi, omega, fp="f32"):
     out = np.zeros((60, 3), _dt(fp))
     R = _R(fp)

@@ -207,6 +207,28 @@ def test_mode1_fsc_half_maps(files):
     assert np.linalg.norm(got - want) <= 1e-5 * np.linalg.norm(want)
 
 
+def test_mode3_centring(files):
+    """mode=3 (0main.f90:237-241): calc_center with model3d, calc_center_selfrot180
+    without; every particle of first..last written to newortfile."""
+    import cryoim_gb300 as ci
+    d, common, case = files
+    p, vol, tmpl, timgs, imgs, parts, truth = case
+    run(["icosprocess", "mode=3", *common, f"model3d={d / 'model.mrc'}", f"newortfile={d / 'c3.dat'}"])
+    rows = read_rows(d / "c3.dat")
+    q = library_parts(d, case)
+    with ci.Context(0, p) as ctx:
+        ctx.center(imgs, q, vol)
+    assert len(rows) == len(parts)
+    assert np.allclose(rows[:, 3], q["x"], atol=2e-4) and np.allclose(rows[:, 4], q["y"], atol=2e-4)
+    assert np.allclose(rows[:, 0], q["theta"], atol=2e-4)
+    run(["icosprocess", "mode=3", *common, f"newortfile={d / 'c3s.dat'}"])
+    rows = read_rows(d / "c3s.dat")
+    q = library_parts(d, case)
+    with ci.Context(0, p) as ctx:
+        ctx.center(imgs, q)
+    assert np.allclose(rows[:, 3], q["x"], atol=2e-4) and np.allclose(rows[:, 5], q["pr"], atol=2e-3)
+
+
 def test_mode0_projections(files):
     import cryoim_gb300 as ci
     d, common, case = files
