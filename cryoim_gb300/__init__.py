@@ -256,6 +256,15 @@ class Context:
              *[ptr(x) for x in a], ptr(fsc), ptr(out) if want_map else None)
         return fsc, out
 
+    # -- local_refine ---------------------------------------------------------
+    def local_refine(self, lp, map3d, imgs, lparts: np.ndarray) -> None:
+        """local_refine's refine_PR on sub-particle records (LOCAL_PARTICLE_DTYPE, updated in
+        place); imgs: one whole-particle image per record (P, fftsize0, fftsize0)."""
+        assert lparts.dtype == _abi.LOCAL_PARTICLE_DTYPE and lparts.flags["C_CONTIGUOUS"]
+        m = np.ascontiguousarray(map3d, np.float32)
+        im = np.ascontiguousarray(imgs, np.float32)
+        call("cryoim_local_refine", self._h, C.byref(lp), ptr(m), ptr(im), ptr(lparts), len(lparts))
+
     # -- mode 3 ---------------------------------------------------------------
     def center(self, imgs, parts: np.ndarray, map3d=None) -> None:
         """Origin centring (calc_center.f90 against map3d, or calc_center_selfrot180.f90
@@ -301,6 +310,44 @@ class Context:
 
 
 # -- proc_icos (host geometry in the library) ----------------------------------
+def local_particles(n: int) -> np.ndarray:
+    return np.zeros(n, dtype=_abi.LOCAL_PARTICLE_DTYPE)
+
+
+def local_params(fftsize: int, fftsize0: int, **kw) -> "_abi.LocalParams":
+    """local_refine defaults (0input_parameters.f90) with keyword overrides by field name
+    (apix, max_res, imgmask, nsym, ncycle, apply_ctf, normalize, vol, cs, ampwg,
+    refine_angle, refine_shift, convf), then the derived values."""
+    p = _abi.LocalParams()
+    call("cryoim_local_params_default", C.byref(p), int(fftsize), int(fftsize0))
+    p.refine_angle = p.refine_shift = 0.0
+    for k, v in kw.items():
+        if not hasattr(p, k):
+            raise KeyError(k)
+        setattr(p, k, v)
+    call("cryoim_local_params_derive", C.byref(p))
+    return p
+
+
+def local_sym_matrices(sym: str) -> np.ndarray:
+    out = np.zeros((60, 3, 3), np.float32)
+    n = C.c_int32()
+    call("cryoim_local_sym_matrices", sym.encode(), ptr(out), C.byref(n))
+    return out[:n.value].copy()
+
+
+def local_box_coordinates(parts: np.ndarray, sym: np.ndarray, loc, apix: float, fftsize: int,
+                          pr_threshold: float = 90.0, boundx: float = 100.0) -> np.ndarray:
+    """local_box's coordinate mode: sub-particle records for the selected particles."""
+    p = np.ascontiguousarray(parts, dtype=PARTICLE_DTYPE)
+    s = np.ascontiguousarray(sym, np.float32).reshape(-1, 3, 3)
+    out = local_particles(len(p) * len(s))
+    n = C.c_int32()
+    call("cryoim_local_box_coordinates", ptr(p), len(p), ptr(s), len(s), float(loc[0]), float(loc[1]),
+         float(loc[2]), float(apix), int(fftsize), float(pr_threshold), float(boundx), ptr(out), C.byref(n))
+    return out[:n.value].copy()
+
+
 def icos_ops() -> np.ndarray:
     out = np.zeros((60, 3, 3), np.float32)
     call("cryoim_icos_ops", ptr(out))

@@ -29,6 +29,21 @@ PARTICLE_DTYPE = np.dtype([("particle_id", "<i4"), ("img_id", "<i4"), ("img_part
 TEMPLATE_DTYPE = np.dtype([("particle_id", "<i4"), ("theta", "<f4"), ("phi", "<f4"),
                            ("omega", "<f4"), ("x", "<f4"), ("y", "<f4")])
 assert PARTICLE_DTYPE.itemsize == 24 * 4 and TEMPLATE_DTYPE.itemsize == 24
+# cryoim_local_particle: the sub-particle rows of local_box / local_refine
+_LI = ["particle_id", "img_id", "img_particle_id", "local_img_id", "local_hx0", "local_ky0"]
+_LF = ["theta", "phi", "omega", "x", "y", "pr", "df1", "df2", "astigang",
+       "local_theta0", "local_phi0", "local_omega0", "local_x0", "local_y0", "local_z0", "local_pr0",
+       "local_theta", "local_phi", "local_omega", "local_x", "local_y", "local_z", "local_pr",
+       "local_dtheta", "local_dphi", "local_domega", "local_dx", "local_dy"]
+LOCAL_PARTICLE_DTYPE = np.dtype([(f, "<i4") for f in _LI] + [(f, "<f4") for f in _LF])
+assert LOCAL_PARTICLE_DTYPE.itemsize == 34 * 4
+
+
+class LocalParams(C.Structure):
+    """cryoim_local_params (include/cryoim.h)."""
+    _fields_ = [(n, C.c_int32) for n in ("fftsize", "fftsize0", "nsym", "ncycle", "apply_ctf", "normalize")] + \
+               [(n, C.c_float) for n in ("apix", "max_res", "imgmask", "vol", "cs", "ampwg", "refine_angle",
+                                         "refine_shift", "convf", "max_r", "imgmask_px")]
 
 
 class Params(C.Structure):
@@ -108,6 +123,13 @@ SIGNATURES = {
     "cryoim_rec_finish_merge": [_vp, _vp],
     "cryoim_icosavg": [_vp, _vp, _i32, _f32],
     "cryoim_center": [_vp, _vp, _vp, _vp, _i32],
+    "cryoim_local_sym_matrices": [C.c_char_p, _vp, _ip],
+    "cryoim_local_box_coordinates": [_vp, _i32, _vp, _i32, _f32, _f32, _f32, _f32, _i32, _f32, _f32, _vp, _ip],
+    "cryoim_local_params_default": [_vp, _i32, _i32],
+    "cryoim_local_params_derive": [_vp],
+    "cryoim_local_refine": [_vp, _vp, _vp, _vp, _vp, _i32],
+    "cryoim_local_ort_read": [C.c_char_p, _i32, _i32, _vp, _vp, _i32],
+    "cryoim_local_ort_write": [C.c_char_p, _vp, _vp, _i32, _i32, _i32, _i32],
     "cryoim_central_sections": [_vp, _vp, _vp, _vp, _i32, _vp, _vp],
     "cryoim_icos_ops": [_vp],
     "cryoim_asu_fold": [_fp, _fp, _fp],

@@ -8,7 +8,10 @@ include/cryoim.h carries no torch types).  Translation units:
 * api.cu   -- context, drivers, C ABI (host code built with -ffp-contract=off);
 * fsc.cu   -- -fmad=false: half-map FSC and the FSC-weighted map;
 * mapops.cu -- -fmad=false: real-space icosahedral average, merge output step;
-* center.cu -- -fmad=false: origin centring of icosprocess mode 3.
+* center.cu -- -fmad=false: origin centring of icosprocess mode 3;
+* local.cu -- -fmad=false: local_refine's sub-particle refinement;
+* io.cpp, local_host.cpp -- host only (g++): MRC / orientation / tnf files, local_box
+  geometry and local_refine parameters.
 """
 from __future__ import annotations
 
@@ -51,6 +54,7 @@ UNITS = {
     "fsc.cu": ["-fmad=false"],
     "mapops.cu": ["-fmad=false"],
     "center.cu": ["-fmad=false"],
+    "local.cu": ["-fmad=false"],
 }
 
 
@@ -79,9 +83,10 @@ def build_library(verbose: bool = False, extra: list[str] | None = None) -> str:
     return lib
 
 
-HOST_UNITS = ["io.cpp"]
+HOST_UNITS = ["io.cpp", "local_host.cpp"]
 TOOLS = {"icosprocess": "icosprocess.cpp", "proc_icos": "proc_icos.cpp",
-         "merge_icosprocess_subrec": "merge_subrec.cpp"}
+         "merge_icosprocess_subrec": "merge_subrec.cpp", "local_box": "local_box.cpp",
+         "local_refine": "local_refine.cpp"}
 BIN = os.path.join(HERE, "bin")
 
 

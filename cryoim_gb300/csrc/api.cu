@@ -1850,6 +1850,188 @@ int cryoim_center(void* ctx, const float* map3d, const float* imgs, cryoim_parti
     return CRYOIM_OK;
 }
 
+// local_refine/SRC/icos_equalort.f90:1-23 with icos2f_sym_matc.f90's C_N rotations: the
+// nsym orientations equivalent to (theta, phi, omega), FP32 as the reference.
+static void local_equalort(float th0, float ph0, float om0, const float* sym, int nsym, float d2r, float* out) {
+    const float r2d = 45.0f / std::atan2(1.0f, 1.0f);
+    float e[9];
+    euler_mat(th0, -ph0, 180.0f - om0, d2r, e);
+    for (int s = 0; s < nsym; ++s) {
+        const float* S = sym + 9 * s;
+        float m[9];
+        for (int i = 0; i < 3; ++i)
+            for (int j = 0; j < 3; ++j) {
+                float t = S[3 * i] * e[j];
+                t = t + S[3 * i + 1] * e[3 + j];
+                t = t + S[3 * i + 2] * e[6 + j];
+                m[3 * i + j] = t;
+            }
+        out[3 * s] = std::acos(m[8]) * r2d;
+        out[3 * s + 1] = -std::atan2(m[5], m[2]) * r2d;
+        out[3 * s + 2] = std::atan2(m[7], m[6]) * r2d;
+    }
+}
+
+// local_refine/SRC/ort_cent_11.f90: centre, -/+ x, -/+ y, then -/+ theta, phi, omega
+static void local_cent11(const float* s, float dang, float dtran, float* c) {
+    for (int j = 0; j < 11; ++j)
+        for (int k = 0; k < 5; ++k) c[5 * j + k] = s[k];
+    c[5 * 1 + 3] = s[3] - dtran; c[5 * 2 + 3] = s[3] + dtran;
+    c[5 * 3 + 4] = s[4] - dtran; c[5 * 4 + 4] = s[4] + dtran;
+    c[5 * 5 + 0] = s[0] - dang;  c[5 * 6 + 0] = s[0] + dang;
+    c[5 * 7 + 1] = s[1] - dang;  c[5 * 8 + 1] = s[1] + dang;
+    c[5 * 9 + 2] = s[2] - dang;  c[5 * 10 + 2] = s[2] + dang;
+}
+
+int cryoim_local_refine(void* ctx, const cryoim_local_params* lp, const float* map3d, const float* imgs,
+                        cryoim_local_particle* parts, int32_t P) {
+    Ctx* c = as_ctx(ctx);
+    if (!c || !lp || !map3d || !imgs || !parts || P < 0) return fail(CRYOIM_ERR_ARG, "null input or negative count");
+    const int nx = lp->fftsize, nx0 = lp->fftsize0, nsym = lp->nsym;
+    if (nx < 8 || (nx & 1) || nx > 1024 || nx0 < nx || nx0 > 4096)
+        return fail(CRYOIM_ERR_SIZE, "fftsize %d / fftsize0 %d unsupported", nx, nx0);
+    if (nsym < 1 || nsym > 360 || lp->ncycle < 0 || !(lp->max_r > 0) || !(lp->imgmask_px >= 0))
+        return fail(CRYOIM_ERR_ARG, "local parameters (derive them first)");
+    if (P == 0) return CRYOIM_OK;
+    CK(cudaSetDevice(c->device));
+    const long nn = (long)nx * nx, nn0 = (long)nx0 * nx0, n3 = nn * nx;
+    const int B = (int)std::max(1L, std::min(64L, (256L << 20) / (nn0 * 4)));
+    const int C = std::max(nsym, 11);
+    DBuf<float> dmap, fr, fi, dimg, boxed, ctf, dfs, cand, prs, oxy;
+    DBuf<float2> work, spec;
+    DBuf<double> acc2;
+    DBuf<int> hk, flag;
+    int r;
+    if ((r = dmap.ensure(n3)) || (r = fr.ensure(n3)) || (r = fi.ensure(n3)) || (r = work.ensure(n3)) ||
+        (r = acc2.ensure(2)) || (r = dimg.ensure((size_t)B * nn0)) || (r = boxed.ensure((size_t)B * nn)) ||
+        (r = spec.ensure((size_t)B * nn)) || (r = ctf.ensure((size_t)B * nn)) || (r = dfs.ensure(3 * B)) ||
+        (r = cand.ensure((size_t)B * C * 5)) || (r = prs.ensure((size_t)B * C)) || (r = oxy.ensure(2 * B)) ||
+        (r = hk.ensure(2 * B)) || (r = flag.ensure(1)))
+        return r;
+    // refine_PR.f90:24-52: the soft-masked local map and its transform
+    CK(cudaMemcpyAsync(dmap.p, map3d, sizeof(float) * n3, cudaMemcpyHostToDevice, c->stream));
+    CK(launch_local_softmask(dmap.p, nx, lp->imgmask_px, acc2.p, c->stream));
+    launch_map_checker(dmap.p, nx, work.p, c->stream);
+    cufftHandle h3;
+    CKF(cufftPlan3d(&h3, nx, nx, nx, CUFFT_C2C));
+    cufftResult fr3 = cufftSetStream(h3, c->stream);
+    if (fr3 == CUFFT_SUCCESS) fr3 = cufftExecC2C(h3, (cufftComplex*)work.p, (cufftComplex*)work.p, CUFFT_FORWARD);
+    cudaError_t e3 = fr3 == CUFFT_SUCCESS ? launch_local_ft(work.p, nx, fr.p, fi.p, c->stream) : cudaSuccess;
+    if (e3 == cudaSuccess) e3 = cudaStreamSynchronize(c->stream);
+    cufftDestroy(h3);
+    if (fr3 != CUFFT_SUCCESS) return fail(CRYOIM_ERR_CUDA, "3D forward FFT failed: cufft %d", (int)fr3);
+    if (e3 != cudaSuccess) return fail(CRYOIM_ERR_CUDA, "local map: %s", cudaGetErrorString(e3));
+    std::vector<float> sym(9 * (size_t)nsym);
+    {
+        const std::string name = "c" + std::to_string(nsym);
+        int32_t ns = 0;
+        if (nsym <= 60) {
+            if (cryoim_local_sym_matrices(name.c_str(), sym.data(), &ns) != CRYOIM_OK || ns != nsym)
+                return fail(CRYOIM_ERR_ARG, "symmetry c%d", nsym);
+        } else {
+            return fail(CRYOIM_ERR_ARG, "sym c%d: at most c60", nsym);
+        }
+    }
+    const Angles an = host_angles();
+    std::vector<float> hcand((size_t)B * C * 5), hpr((size_t)B * C), hdf(3 * B), hxy(2 * B), st(5 * (size_t)B),
+        best(B);
+    std::vector<int> hhk(2 * B);
+    for (int b0 = 0; b0 < P; b0 += B) {
+        const int nb = std::min(B, P - b0);
+        const long m = (long)nb * nn;
+        cufftHandle h2;
+        int dims[2] = {nx, nx};
+        CKF(cufftPlanMany(&h2, 2, dims, nullptr, 1, 0, nullptr, 1, 0, CUFFT_C2C, nb));
+        cufftResult f2 = cufftSetStream(h2, c->stream);
+        for (int i = 0; i < nb; ++i) {
+            const cryoim_local_particle& q = parts[b0 + i];
+            hhk[2 * i] = q.local_hx0; hhk[2 * i + 1] = q.local_ky0;
+            hxy[i] = q.local_x0; hxy[B + i] = q.local_y0;
+            hdf[3 * i] = q.df1; hdf[3 * i + 1] = q.df2; hdf[3 * i + 2] = q.astigang;
+        }
+        CK(cudaMemcpyAsync(dimg.p, imgs + (size_t)b0 * nn0, sizeof(float) * nb * nn0, cudaMemcpyHostToDevice,
+                           c->stream));
+        CK(cudaMemcpyAsync(hk.p, hhk.data(), sizeof(int) * 2 * nb, cudaMemcpyHostToDevice, c->stream));
+        CK(cudaMemcpyAsync(oxy.p, hxy.data(), sizeof(float) * 2 * B, cudaMemcpyHostToDevice, c->stream));
+        CK(cudaMemcpyAsync(dfs.p, hdf.data(), sizeof(float) * 3 * nb, cudaMemcpyHostToDevice, c->stream));
+        CK(cudaMemsetAsync(flag.p, 0, sizeof(int), c->stream));
+        // refine_PR.f90:116-120: window, mask at the local origin, transform, weight
+        launch_local_box(dimg.p, nx0, hk.p, nx, lp->normalize, nb, boxed.p, c->stream);
+        launch_prep_images(boxed.p, nb, nx, oxy.p, oxy.p + B, 1, lp->imgmask_px, 0, spec.p, flag.p, c->stream);
+        if (f2 == CUFFT_SUCCESS) f2 = cufftExecC2C(h2, (cufftComplex*)spec.p, (cufftComplex*)spec.p, CUFFT_FORWARD);
+        if (f2 != CUFFT_SUCCESS) { cufftDestroy(h2); return fail(CRYOIM_ERR_CUDA, "2D FFT failed: cufft %d", (int)f2); }
+        cufftDestroy(h2);
+        launch_ref_post(spec.p, m, (float)nn, c->stream);
+        launch_wlp(spec.p, nx, m, lp->max_r, c->stream);
+        const float* ctfp = nullptr;
+        if (lp->apply_ctf) {
+            launch_local_ctf(dfs.p, nx, lp->apix, lp->vol, lp->cs, lp->ampwg, nb, ctf.p, c->stream);
+            ctfp = ctf.p;
+        }
+        CK(cudaGetLastError());
+        for (int i = 0; i < nb; ++i) {
+            const cryoim_local_particle& q = parts[b0 + i];
+            float* s = &st[5 * i];
+            s[0] = q.local_theta0; s[1] = q.local_phi0; s[2] = q.local_omega0; s[3] = q.local_x0; s[4] = q.local_y0;
+            best[i] = 0.0f;  // refine_PR.f90 leaves maxCC unset when there is nothing to score
+        }
+        // score nc candidates per particle (already in hcand) and move to the first minimum
+        auto score_round = [&](int nc) -> int {
+            CK(cudaMemcpyAsync(cand.p, hcand.data(), sizeof(float) * nb * nc * 5, cudaMemcpyHostToDevice, c->stream));
+            launch_local_pr(cand.p, nc, fr.p, fi.p, nx, spec.p, ctfp, lp->max_r, nb, prs.p, c->stream);
+            CK(cudaGetLastError());
+            CK(cudaMemcpyAsync(hpr.data(), prs.p, sizeof(float) * nb * nc, cudaMemcpyDeviceToHost, c->stream));
+            CK(cudaStreamSynchronize(c->stream));
+            for (int i = 0; i < nb; ++i) {
+                int k = 0;
+                for (int j = 1; j < nc; ++j)
+                    if (hpr[(size_t)i * nc + j] < hpr[(size_t)i * nc + k]) k = j;
+                for (int v = 0; v < 5; ++v) st[5 * i + v] = hcand[((size_t)i * nc + k) * 5 + v];
+                best[i] = hpr[(size_t)i * nc + k];
+            }
+            return CRYOIM_OK;
+        };
+        if (nsym > 1) {  // refine_PR.f90:122-145: the equivalent orientations at the local origin
+            std::vector<float> eq(3 * (size_t)nsym);
+            for (int i = 0; i < nb; ++i) {
+                local_equalort(st[5 * i], st[5 * i + 1], st[5 * i + 2], sym.data(), nsym, an.deg2rad, eq.data());
+                for (int s = 0; s < nsym; ++s) {
+                    float* o = &hcand[((size_t)i * nsym + s) * 5];
+                    o[0] = eq[3 * s]; o[1] = eq[3 * s + 1]; o[2] = eq[3 * s + 2];
+                    o[3] = st[5 * i + 3]; o[4] = st[5 * i + 4];
+                }
+            }
+            if ((r = score_round(nsym))) return r;
+        }
+        // refine_PR.f90:146-168 / 180-202: Ncycle rounds of the 11-candidate descent
+        float fac = 1.0f;
+        for (int cyc = 1; cyc <= lp->ncycle; ++cyc) {
+            const float dang = lp->refine_angle * fac, dtran = lp->refine_shift * fac;
+            fac = fac * lp->convf;
+            for (int i = 0; i < nb; ++i) local_cent11(&st[5 * i], dang, dtran, &hcand[(size_t)i * 11 * 5]);
+            if ((r = score_round(11))) return r;
+        }
+        int bad = 0;
+        CK(cudaMemcpyAsync(&bad, flag.p, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
+        CK(cudaStreamSynchronize(c->stream));
+        if (bad) return fail(CRYOIM_ERR_INPUT, "non-finite pixel (NaN/Inf) in a sub-particle window");
+        for (int i = 0; i < nb; ++i) {  // refine_PR.f90:220-231
+            cryoim_local_particle& q = parts[b0 + i];
+            const float* s = &st[5 * i];
+            q.local_dtheta = s[0] - q.local_theta0;
+            q.local_dphi = s[1] - q.local_phi0;
+            q.local_domega = s[2] - q.local_omega0;
+            q.local_dx = s[3] - q.local_x0;
+            q.local_dy = s[4] - q.local_y0;
+            q.local_theta = s[0]; q.local_phi = s[1]; q.local_omega = s[2];
+            q.local_x = s[3]; q.local_y = s[4];
+            q.local_z = q.local_z0;
+            q.local_pr = best[i];
+        }
+    }
+    return CRYOIM_OK;
+}
+
 int cryoim_central_sections(void* ctx, const float* ft_re, const float* ft_im, const float* eulers,
                             int32_t n, float* out_re, float* out_im) {
     Ctx* c = as_ctx(ctx);

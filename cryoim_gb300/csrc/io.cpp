@@ -227,6 +227,87 @@ int cryoim_ort_write(const char* path, const cryoim_particle* parts, const char*
     return std::fclose(f) == 0 ? CRYOIM_OK : CRYOIM_ERR_IO;
 }
 
+// local_refine/SRC/load_original_ort.f90:12-15: the 23 list-directed columns of rows
+// first..last.
+int cryoim_local_ort_read(const char* path, int32_t first, int32_t last, cryoim_local_particle* parts,
+                          char* stck, int32_t stck_len) {
+    if (!path || !parts || first < 1 || last < first || (stck && stck_len < 1)) return CRYOIM_ERR_ARG;
+    FILE* f = std::fopen(path, "r");
+    if (!f) return CRYOIM_ERR_IO;
+    char line[8192];
+    int32_t row = 0, k = 0;
+    int rc = CRYOIM_OK;
+    while (std::fgets(line, sizeof(line), f)) {
+        std::vector<std::string> t = tokens(line);
+        if (t.empty()) continue;
+        ++row;
+        if (row < first) continue;
+        if (row > last) break;
+        if (t.size() < 23) { rc = CRYOIM_ERR_IO; break; }
+        cryoim_local_particle& q = parts[k];
+        std::memset(&q, 0, sizeof(q));
+        bool ok = to_i(t[1], &q.particle_id) && to_f(t[2], &q.theta) && to_f(t[3], &q.phi) &&
+                  to_f(t[4], &q.omega) && to_f(t[5], &q.x) && to_f(t[6], &q.y) && to_f(t[7], &q.pr) &&
+                  to_i(t[8], &q.img_id) && to_i(t[9], &q.img_particle_id) && to_f(t[10], &q.df1) &&
+                  to_f(t[11], &q.df2) && to_f(t[12], &q.astigang) && to_i(t[13], &q.local_img_id) &&
+                  to_i(t[14], &q.local_hx0) && to_i(t[15], &q.local_ky0) && to_f(t[16], &q.local_theta0) &&
+                  to_f(t[17], &q.local_phi0) && to_f(t[18], &q.local_omega0) && to_f(t[19], &q.local_x0) &&
+                  to_f(t[20], &q.local_y0) && to_f(t[21], &q.local_z0) && to_f(t[22], &q.local_pr0);
+        if (!ok) { rc = CRYOIM_ERR_INPUT; break; }
+        if (stck) {
+            char* dst = stck + (size_t)k * stck_len;
+            std::memset(dst, 0, (size_t)stck_len);
+            std::strncpy(dst, t[0].c_str(), (size_t)stck_len - 1);
+        }
+        ++k;
+    }
+    std::fclose(f);
+    if (rc == CRYOIM_OK && k != last - first + 1) rc = CRYOIM_ERR_IO;
+    return rc;
+}
+
+// format 900 of local_box/SRC/loc_box_coordinate.f90:46 (23 columns) or format 901 of
+// local_refine/SRC/refine_PR.f90:246-253 (28 columns; its PR column is local_PR).
+int cryoim_local_ort_write(const char* path, const cryoim_local_particle* parts, const char* stck,
+                           int32_t stck_len, int32_t n, int32_t columns, int32_t append) {
+    if (!path || (!parts && n > 0) || n < 0 || (stck && stck_len < 1)) return CRYOIM_ERR_ARG;
+    if (columns != 23 && columns != 28) return CRYOIM_ERR_ARG;
+    FILE* f = std::fopen(path, append ? "a" : "w");
+    if (!f) return CRYOIM_ERR_IO;
+    std::string s;
+    const bool box = columns == 23;
+    for (int32_t i = 0; i < n; ++i) {
+        const cryoim_local_particle& q = parts[i];
+        s.clear();
+        put_a(s, stck ? stck + (size_t)i * stck_len : "", 64);
+        put_i(s, q.particle_id, box ? 8 : 9);
+        for (float v : {q.theta, q.phi, q.omega, q.x, q.y}) put_f(s, v, 10, 4);
+        put_f(s, box ? q.pr : q.local_pr, 10, 4);
+        put_i(s, q.img_id, box ? 12 : 11);
+        put_i(s, q.img_particle_id, box ? 6 : 7);
+        put_f(s, q.df1, 15, 4);
+        put_f(s, q.df2, 15, 4);
+        put_f(s, q.astigang, 10, 4);
+        put_i(s, q.local_img_id, 9);
+        put_i(s, q.local_hx0, 6);
+        put_i(s, q.local_ky0, 6);
+        if (box) {
+            for (float v : {q.local_theta0, q.local_phi0, q.local_omega0, q.local_x0, q.local_y0}) put_f(s, v, 10, 4);
+            put_f(s, q.local_z0, 11, 4);
+            put_f(s, q.local_pr0, 11, 4);
+        } else {
+            for (float v : {q.local_theta, q.local_phi, q.local_omega, q.local_x, q.local_y}) put_f(s, v, 10, 4);
+            put_f(s, q.local_z, 11, 4);
+            put_f(s, q.local_pr, 10, 4);
+            for (float v : {q.local_dtheta, q.local_dphi, q.local_domega, q.local_dx, q.local_dy})
+                put_f(s, v, 10, 4);
+        }
+        s += '\n';
+        std::fputs(s.c_str(), f);
+    }
+    return std::fclose(f) == 0 ? CRYOIM_OK : CRYOIM_ERR_IO;
+}
+
 // load_template.f90:18-21 (the file's first rows; 0main.f90:53-58 counts them).
 int cryoim_template_ort_read(const char* path, cryoim_template* t, int32_t maxn, int32_t* n) {
     if (!path || !n || maxn < 0 || (!t && maxn > 0)) return CRYOIM_ERR_ARG;

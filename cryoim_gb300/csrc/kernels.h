@@ -199,6 +199,19 @@ void launch_cross_power(float2* f1, const float2* f2, int nx, long n, cudaStream
 void launch_rot180(float* a1, float* a2, int nx, long n, cudaStream_t st);
 void launch_peak(const float2* cc, int nx, int B, int half, float* out, cudaStream_t st);
 
+// ---- local.cu: local_refine's sub-particle refinement ------------------------
+cudaError_t launch_local_softmask(float* map, int nx, float mask, double* acc2, cudaStream_t st);
+cudaError_t launch_local_ft(const float2* ft, int nx, float* fr, float* fi, cudaStream_t st);
+// hk: B x (hx0, ky0); out: B x nx^2 windows of the B whole images (nx0^2 each)
+void launch_local_box(const float* imgs, int nx0, const int* hk, int nx, int normalize, int B, float* out,
+                      cudaStream_t st);
+// dfs: B x (df1, df2, astig) with defocus in Angstrom; ctf: B x nx^2
+void launch_local_ctf(const float* dfs, int nx, float apix, float vol, float cs, float ampwg, int B, float* ctf,
+                      cudaStream_t st);
+void launch_wlp(float2* b, int nx, long n, float max_r, cudaStream_t st);
+void launch_local_pr(const float* cand, int C, const float* fr, const float* fi, int nx, const float2* part,
+                     const float* ctf, float max_r, int B, float* out, cudaStream_t st);
+
 // ---- mapops.cu: whole-map real-space operations ------------------------------
 // real-space icosahedral average of an nx^3 map (in != out), radius r0 pixels
 cudaError_t launch_icosavg(const float* in, int nx, float r0, const float* ops, int nsym, float* out,

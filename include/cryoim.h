@@ -282,6 +282,79 @@ int cryoim_icosavg(void* ctx, float* map, int32_t n, float r0);
 int cryoim_center(void* ctx, const float* map3d, const float* imgs, cryoim_particle* parts,
                   int32_t P);
 
+/* ---- localized reconstruction inputs: local_box and local_refine --------- */
+
+/* One sub-particle record: the columns of the local orientation files
+ * (local_box/SRC/loc_box_coordinate.f90:35-38 writes the first 23, local_refine reads
+ * them in local_refine/SRC/load_original_ort.f90:12-15 and writes all 28 in
+ * refine_PR.f90:236-244).  df1, df2 are in Angstrom here (local_box multiplies the
+ * micrometre values by 10^4). */
+typedef struct cryoim_local_particle {
+    int32_t particle_id, img_id, img_particle_id, local_img_id, local_hx0, local_ky0;
+    float theta, phi, omega, x, y, pr, df1, df2, astigang;
+    float local_theta0, local_phi0, local_omega0, local_x0, local_y0, local_z0, local_pr0;
+    float local_theta, local_phi, local_omega, local_x, local_y, local_z, local_pr;
+    float local_dtheta, local_dphi, local_domega, local_dx, local_dy;
+} cryoim_local_particle;
+
+/* Symmetry rotations of local_box (row-major 3x3 each, at most 60): "cN" (N = 1..60,
+ * C_matrix.f90), "i2", "i3", "i5" (icos_matrix_i2.f90, icos_matrix_i3.f90,
+ * icos_matrix_i5.f90).  *n receives the count. */
+int cryoim_local_sym_matrices(const char* sym, float* out, int32_t* n);
+
+/* local_box's coordinate mode (loc_box_coordinate.f90:13-40) for P whole-particle
+ * records (the icosprocess ort fields; selected are those with PR <= pr_threshold and
+ * |x|, |y| <= boundx, load_ort.f90:30-34): for every selected particle and every one of
+ * the nsym rotations, the equivalent orientation (equalort.f90), the sub-particle
+ * centre R^T (loc_x, loc_y, loc_z) + fftsize/2 + (x, y) split into the integer box
+ * centre (local_hx0, local_ky0) and the fraction (local_x0, local_y0), and local_z0 =
+ * (z - fftsize/2) * apix.  out holds room for P x nsym records; *nout receives the
+ * count written. */
+int cryoim_local_box_coordinates(const cryoim_particle* parts, int32_t P, const float* sym, int32_t nsym,
+                                 float loc_x, float loc_y, float loc_z, float apix, int32_t fftsize,
+                                 float pr_threshold, float boundx, cryoim_local_particle* out,
+                                 int32_t* nout);
+
+/* local_refine parameters (local_refine/SRC/0input_parameters.f90:25-55 defaults,
+ * 0calc_initialvalue.f90:65-76 derived values). */
+typedef struct cryoim_local_params {
+    int32_t fftsize;       /* local map box (the sub-particle size)                       */
+    int32_t fftsize0;      /* whole-particle image box                                    */
+    int32_t nsym;          /* sym cN: N                                                   */
+    int32_t ncycle;        /* refinement cycles (12)                                      */
+    int32_t apply_ctf;     /* 1 (applyCTF=y)                                              */
+    int32_t normalize;     /* 1: img2d_norm of the whole image (stack files); 0 (imgstck)  */
+    float apix, max_res, imgmask, vol, cs, ampwg, refine_angle, refine_shift, convf;
+    /* derived by cryoim_local_params_derive: */
+    float max_r;           /* apix * fftsize / max_res (pixels, not rounded)              */
+    float imgmask_px;      /* imgmask / apix if imgmask > 0, else fftsize/2 - 2            */
+} cryoim_local_params;
+
+/* The reference defaults (apix 1, maxRes 10, Ncycle 12, convF 0.8, vol 200, Cs 2.7,
+ * ampwg 0.1, sym c1, applyCTF y, refine_angle / refine_shift derived when <= 0). */
+int cryoim_local_params_default(cryoim_local_params* p, int32_t fftsize, int32_t fftsize0);
+int cryoim_local_params_derive(cryoim_local_params* p);
+
+/* local_refine's refine_PR (refine_PR.f90:55-232) for P sub-particles: whole-particle
+ * images (P x fftsize0^2, one per record, in record order), the local map
+ * (fftsize^3).  Each sub-particle is boxed at (local_hx0, local_ky0), masked at its
+ * (local_x0, local_y0), transformed and Gaussian-weighted; with nsym > 1 the nsym
+ * equivalent orientations (icos_equalort) are scored first, then ncycle rounds of the
+ * 11-candidate descent, every candidate scored by cal_PR_FT against the map's central
+ * section (FFT3d_slice) shifted to the candidate origin, times CTF and the weight.  The
+ * local_* output fields are set as refine_PR.f90:220-231 sets them. */
+int cryoim_local_refine(void* ctx, const cryoim_local_params* p, const float* map3d, const float* imgs,
+                        cryoim_local_particle* parts, int32_t P);
+
+/* The local orientation files: 23 list-directed columns in, and out either the 23 of
+ * local_box (format 900 of loc_box_coordinate.f90:46, columns = 23) or the 28 of
+ * local_refine (format 901 of refine_PR.f90:246-253, columns = 28).  stck as in
+ * cryoim_ort_read (stck_len bytes per record, name width 64 on output). */
+int cryoim_local_ort_read(const char* path, int32_t first, int32_t last, cryoim_local_particle* parts,
+                          char* stck, int32_t stck_len);
+int cryoim_local_ort_write(const char* path, const cryoim_local_particle* parts, const char* stck,
+                           int32_t stck_len, int32_t n, int32_t columns, int32_t append);
+
 /* ---- files (host only; byte-compatible with the reference) ---------------- */
 
 /* The `mrchead` type of icosprocess/SRC/0common_icosproc.f90:61-112: 1024 bytes. */

@@ -1526,6 +1526,248 @@ int center(const cryoim_params* p, const float* map, const float* imgs, const cr
 }
 
 /* ------------------------------------------------------------------------ */
+/* local_box (coordinate mode) and local_refine (refine_PR)                   */
+/* ------------------------------------------------------------------------ */
+
+/* local_box/SRC/Eularmatrix.f90 (row-major). */
+template <class R> void eularmatrix(R th0, R ph0, R om0, R* r) {
+    const R d2r = R(4) * std::atan2(R(1), R(1)) / R(180);
+    R th = th0 * d2r, ph = ph0 * d2r, om = om0 * d2r;
+    r[0] = std::cos(ph) * std::cos(th) * std::cos(om) - std::sin(ph) * std::sin(om);
+    r[1] = -std::cos(ph) * std::cos(th) * std::sin(om) - std::sin(ph) * std::cos(om);
+    r[2] = std::cos(ph) * std::sin(th);
+    r[3] = std::sin(ph) * std::cos(th) * std::cos(om) + std::cos(ph) * std::sin(om);
+    r[4] = -std::sin(ph) * std::cos(th) * std::sin(om) + std::cos(ph) * std::cos(om);
+    r[5] = std::sin(ph) * std::sin(th);
+    r[6] = -std::sin(th) * std::cos(om);
+    r[7] = std::sin(th) * std::sin(om);
+    r[8] = std::cos(th);
+}
+
+/* C_matrix.f90 / icos2f_sym_matc.f90: rotations by 2 pi k / n about z, k = 1..n. */
+template <class R> void c_matrix(int n, R* out) {
+    const R pi = R(4) * std::atan2(R(1), R(1));
+    const R phi = R(2) * pi / (R)n;
+    R r1[9] = {std::cos(phi), -std::sin(phi), 0, std::sin(phi), std::cos(phi), 0, 0, 0, 1};
+    std::copy(r1, r1 + 9, out);
+    for (int k = 1; k < n; ++k) {
+        R t[9];
+        for (int i = 0; i < 3; ++i)
+            for (int j = 0; j < 3; ++j)
+                t[3 * i + j] = out[9 * (k - 1) + 3 * i] * r1[j] + out[9 * (k - 1) + 3 * i + 1] * r1[3 + j] +
+                               out[9 * (k - 1) + 3 * i + 2] * r1[6 + j];
+        std::copy(t, t + 9, out + 9 * k);
+    }
+}
+
+/* local_box/SRC/loc_box_coordinate.f90:13-40 with equalort.f90 and load_ort.f90's
+ * selection; sym: nsym row-major rotations. */
+template <class R>
+int local_box_coordinates(const cryoim_particle* parts, int P, const float* sym, int nsym, R lx, R ly, R lz,
+                          R apix, int fftsize, R prthr, R boundx, cryoim_local_particle* out) {
+    const R r2d = R(45) / std::atan2(R(1), R(1));
+    const R h = (R)(fftsize / 2);
+    const R x0[3] = {lx, ly, lz};
+    int k = 0;
+    for (int i = 0; i < P; ++i) {
+        const cryoim_particle& q = parts[i];
+        if (!((R)q.pr <= prthr && std::fabs((R)q.x) <= boundx && std::fabs((R)q.y) <= boundx)) continue;
+        R e[9];
+        eularmatrix((R)q.theta, (R)q.phi, (R)q.omega, e);
+        for (int s = 0; s < nsym; ++s) {
+            R r[9];
+            for (int a = 0; a < 3; ++a)
+                for (int b = 0; b < 3; ++b)
+                    r[3 * a + b] = (R)sym[9 * s + 3 * a] * e[b] + (R)sym[9 * s + 3 * a + 1] * e[3 + b] +
+                                   (R)sym[9 * s + 3 * a + 2] * e[6 + b];
+            R th = r[8] >= R(1) ? R(0) : (r[8] < R(-1) ? R(180) : std::acos(r[8]) * r2d);
+            R ph = std::atan2(r[5], r[2]) * r2d, om = std::atan2(r[7], -r[6]) * r2d;
+            R rot[9];
+            eularmatrix(th, ph, om, rot);
+            R c[3];
+            for (int a = 0; a < 3; ++a) c[a] = rot[a] * x0[0] + rot[3 + a] * x0[1] + rot[6 + a] * x0[2] + h;
+            c[0] = c[0] + (R)q.x;
+            c[1] = c[1] + (R)q.y;
+            int hx0 = fint(c[0]), ky0 = fint(c[1]);
+            cryoim_local_particle& o = out[k++];
+            std::memset(&o, 0, sizeof(o));
+            o.particle_id = q.particle_id; o.img_id = q.img_id; o.img_particle_id = q.img_particle_id;
+            o.theta = q.theta; o.phi = q.phi; o.omega = q.omega; o.x = q.x; o.y = q.y; o.pr = q.pr;
+            o.df1 = (float)((R)q.df1 * R(10000)); o.df2 = (float)((R)q.df2 * R(10000)); o.astigang = q.astigang;
+            o.local_img_id = s + 1; o.local_hx0 = hx0; o.local_ky0 = ky0;
+            o.local_theta0 = (float)th; o.local_phi0 = (float)ph; o.local_omega0 = (float)om;
+            o.local_x0 = (float)(c[0] - (R)hx0); o.local_y0 = (float)(c[1] - (R)ky0);
+            o.local_z0 = (float)((c[2] - h) * apix);
+            o.local_pr0 = q.pr;
+        }
+    }
+    return k;
+}
+
+/* local_refine/SRC/getCTF2d.f90 (defocus already in Angstrom). */
+template <class R> void local_ctf2d(int nx, R df1, R df2, R astig0, R apix, R vol, R cs0, R ampwg, R* ctf) {
+    get_ctf2d(nx, df1 / R(1.0e4), df2 / R(1.0e4), astig0, apix, vol, cs0, ampwg, ctf);
+}
+
+/* refine_PR.f90:128-143 for one candidate: FFT3d_slice, img2d_FTphase, shift x CTF x
+ * weight, cal_PR_FT against the sub-particle's weighted transform (a2, b2). */
+template <class R>
+R local_score(const R* fr, const R* fi, int nx, const R* cand, const R* a2, const R* b2, const R* ctf, const R* w,
+              R maxR) {
+    const long nn = (long)nx * nx;
+    std::vector<R> sa(nn), sb(nn);
+    central_section(fr, fi, nx, cand[0], cand[1], cand[2], sa.data(), sb.data());
+    const R pi = R(4) * std::atan2(R(1), R(1)), tpi = R(2) * pi;
+    R pr1 = 0, pr2 = 0;
+    for (long i = 0; i < nn; ++i) {
+        int ky = (int)(i / nx) - nx / 2, hx = (int)(i % nx) - nx / 2;
+        R ph = R(2) * pi * (cand[3] * (R)hx + cand[4] * (R)ky) / (R)nx;
+        R a1 = sa[i] * std::cos(ph) + sb[i] * std::sin(ph);
+        R b1 = -sa[i] * std::sin(ph) + sb[i] * std::cos(ph);
+        R s = (((i / nx) + (i % nx)) & 1) ? R(-1) : R(1);
+        a1 = a1 * s * ctf[i] * w[i];
+        b1 = b1 * s * ctf[i] * w[i];
+        R dr = std::sqrt((R)(hx * hx + ky * ky));
+        if (!(dr >= R(-1) && dr <= maxR)) continue;
+        R amp1 = std::sqrt(a1 * a1 + b1 * b1), amp2 = std::sqrt(a2[i] * a2[i] + b2[i] * b2[i]);
+        R diff = std::fabs(std::atan2(b2[i], a2[i]) - std::atan2(b1, a1));
+        diff = std::fmod(diff, tpi);
+        if (diff > pi) diff = tpi - diff;
+        amp1 = amp1 + amp2;
+        pr1 = diff * amp1 + pr1;
+        pr2 = amp1 + pr2;
+    }
+    return pr2 > R(1.0e-10) ? pr1 / pr2 * R(180) / pi : R(1000);
+}
+
+/* local_refine/SRC/refine_PR.f90:24-232 (sym cN: nsym = N; the refine_PR path). */
+template <class R>
+int local_refine(const cryoim_local_params* p, const float* map, const float* imgs, cryoim_local_particle* parts,
+                 int P) {
+    const int nx = p->fftsize, nx0 = p->fftsize0, nsym = p->nsym;
+    const long nn = (long)nx * nx, nn0 = (long)nx0 * nx0, n3 = nn * nx;
+    const R pi = R(4) * std::atan2(R(1), R(1));
+    /* img3d_softmask.f90 */
+    std::vector<R> re(map, map + n3), im(n3, R(0));
+    {
+        R inn = (R)p->imgmask_px - R(3);
+        if (inn <= R(0)) inn = R(0);
+        R out = (R)p->imgmask_px + R(3);
+        if (out > (R)(nx / 2)) out = (R)(nx / 2);
+        auto rad = [&](long q) {
+            int iz = (int)(q / nn) - nx / 2, iy = (int)((q / nx) % nx) - nx / 2, ix = (int)(q % nx) - nx / 2;
+            return std::sqrt((R)(ix * ix + iy * iy + iz * iz));
+        };
+        R summ = 0;
+        long num = 0;
+        for (long q = 0; q < n3; ++q) {
+            R r = rad(q);
+            if (r > inn && r <= out) { summ = re[q] + summ; ++num; }
+        }
+        if (num != 0) summ = summ / (R)(float)num;
+        for (long q = 0; q < n3; ++q) {
+            R r = rad(q);
+            if (r > inn && r <= out) {
+                R edge = (R(1) + std::cos(pi * (r - inn) / R(6))) / R(2);
+                re[q] = re[q] * edge + (R(1) - edge) * summ;
+            }
+            if (r > out) re[q] = summ;
+        }
+    }
+    /* refine_PR.f90:48-52 */
+    for (long q = 0; q < n3; ++q)
+        if (((q / nn) + (q / nx) % nx + q % nx) & 1) re[q] = -re[q];
+    fft3d(re.data(), im.data(), nx, -1);
+    const R s3 = (R)(float)n3;
+    for (long q = 0; q < n3; ++q) {
+        re[q] = re[q] / s3; im[q] = im[q] / s3;
+        if (((q / nn) + (q / nx) % nx + q % nx) & 1) { re[q] = -re[q]; im[q] = -im[q]; }
+    }
+    const R maxR = (R)p->max_r;
+    std::vector<R> w(nn);
+    for (long i = 0; i < nn; ++i) {
+        int ky = (int)(i / nx), hx = (int)(i % nx);
+        R r2 = (R)((hx - nx / 2) * (hx - nx / 2) + (ky - nx / 2) * (ky - nx / 2)) / R(2) / (maxR * maxR);
+        w[i] = std::exp(-r2);
+    }
+    std::vector<R> symr(9 * (size_t)nsym);
+    c_matrix<R>(nsym, symr.data());
+    std::vector<R> img(nn0), a2(nn), b2(nn), ctf(nn, R(1));
+    for (int ip = 0; ip < P; ++ip) {
+        cryoim_local_particle& q = parts[ip];
+        for (long i = 0; i < nn0; ++i) img[i] = (R)imgs[(long)ip * nn0 + i];
+        if (p->normalize) img2d_norm(img.data(), nx0);
+        /* img2d_local_box.f90 */
+        for (long i = 0; i < nn; ++i) {
+            int hx = (int)(i % nx) + q.local_hx0 - nx / 2, ky = (int)(i / nx) + q.local_ky0 - nx / 2;
+            if (hx < 0) hx += nx0;
+            if (hx >= nx0) hx -= nx0;
+            if (ky < 0) ky += nx0;
+            if (ky >= nx0) ky -= nx0;
+            long i2 = (long)ky * nx0 + hx;
+            a2[i] = (i2 >= 0 && i2 < nn0) ? img[i2] : R(0);
+        }
+        img2d_mask(a2.data(), nx, (R)p->imgmask_px, (R)q.local_x0, (R)q.local_y0);
+        for (long i = 0; i < nn; ++i) {
+            if (((i / nx) + (i % nx)) & 1) a2[i] = -a2[i];
+            b2[i] = R(0);
+        }
+        img2d_fft(a2.data(), b2.data(), nx, nx, 1);
+        for (long i = 0; i < nn; ++i) { a2[i] = a2[i] * w[i]; b2[i] = b2[i] * w[i]; }
+        if (p->apply_ctf)
+            local_ctf2d(nx, (R)q.df1, (R)q.df2, (R)q.astigang, (R)p->apix, (R)p->vol, (R)p->cs, (R)p->ampwg,
+                        ctf.data());
+        R st[5] = {(R)q.local_theta0, (R)q.local_phi0, (R)q.local_omega0, (R)q.local_x0, (R)q.local_y0};
+        R best = 0;
+        if (nsym > 1) {
+            /* icos_equalort.f90 */
+            const R r2d = R(45) / std::atan2(R(1), R(1));
+            R e[9];
+            euler_mat(st[0], -st[1], R(180) - st[2], e);
+            R bst[5];
+            for (int s = 0; s < nsym; ++s) {
+                R m[9];
+                for (int a = 0; a < 3; ++a)
+                    for (int b = 0; b < 3; ++b)
+                        m[3 * a + b] = symr[9 * s + 3 * a] * e[b] + symr[9 * s + 3 * a + 1] * e[3 + b] +
+                                       symr[9 * s + 3 * a + 2] * e[6 + b];
+                R cand[5] = {std::acos(m[8]) * r2d, -std::atan2(m[5], m[2]) * r2d, std::atan2(m[7], m[6]) * r2d,
+                             st[3], st[4]};
+                R v = local_score(re.data(), im.data(), nx, cand, a2.data(), b2.data(), ctf.data(), w.data(), maxR);
+                if (s == 0 || v < best) { best = v; std::copy(cand, cand + 5, bst); }
+            }
+            std::copy(bst, bst + 5, st);
+        }
+        R fac = 1;
+        for (int cyc = 1; cyc <= p->ncycle; ++cyc) {
+            R dang = (R)p->refine_angle * fac, dtran = (R)p->refine_shift * fac;
+            fac = fac * (R)p->convf;
+            R c11[11][5];
+            for (int j = 0; j < 11; ++j) std::copy(st, st + 5, c11[j]);
+            c11[1][3] -= dtran; c11[2][3] += dtran; c11[3][4] -= dtran; c11[4][4] += dtran;
+            c11[5][0] -= dang; c11[6][0] += dang; c11[7][1] -= dang; c11[8][1] += dang;
+            c11[9][2] -= dang; c11[10][2] += dang;
+            int kb = 0;
+            for (int j = 0; j < 11; ++j) {
+                R v = local_score(re.data(), im.data(), nx, c11[j], a2.data(), b2.data(), ctf.data(), w.data(), maxR);
+                if (j == 0 || v < best) { best = v; kb = j; }
+            }
+            std::copy(c11[kb], c11[kb] + 5, st);
+        }
+        q.local_dtheta = (float)(st[0] - (R)q.local_theta0);
+        q.local_dphi = (float)(st[1] - (R)q.local_phi0);
+        q.local_domega = (float)(st[2] - (R)q.local_omega0);
+        q.local_dx = (float)(st[3] - (R)q.local_x0);
+        q.local_dy = (float)(st[4] - (R)q.local_y0);
+        q.local_theta = (float)st[0]; q.local_phi = (float)st[1]; q.local_omega = (float)st[2];
+        q.local_x = (float)st[3]; q.local_y = (float)st[4];
+        q.local_z = q.local_z0;
+        q.local_pr = (float)best;
+    }
+    return 0;
+}
+
+/* ------------------------------------------------------------------------ */
 /* proc_icos                                                                   */
 /* ------------------------------------------------------------------------ */
 
@@ -1675,6 +1917,15 @@ template <class R> void transform_ort(int to, R* th, R* ph, R* om, int n) {
         return center<R>(p, map, im, pa, P, out);                                                      \
     }                                                                                                  \
     extern "C" void orc_lowpass_##S(R* a, int nx, int lp) { img2d_lowpass<R>(a, nx, lp); }          \
+    extern "C" int orc_local_box_coordinates_##S(const cryoim_particle* pa, int P, const float* sym,   \
+                                                  int nsym, R lx, R ly, R lz, R apix, int nx, R prt,   \
+                                                  R bx, cryoim_local_particle* out) {                  \
+        return local_box_coordinates<R>(pa, P, sym, nsym, lx, ly, lz, apix, nx, prt, bx, out);         \
+    }                                                                                                  \
+    extern "C" int orc_local_refine_##S(const cryoim_local_params* p, const float* map,              \
+                                         const float* im, cryoim_local_particle* pa, int P) {          \
+        return local_refine<R>(p, map, im, pa, P);                                                     \
+    }                                                                                                  \
     extern "C" void orc_gauss_regression_##S(const R* z, R* out) {                                   \
         R zz[3][3];                                                                                    \
         for (int k = 0; k < 9; ++k) zz[k / 3][k % 3] = z[k];                                           \

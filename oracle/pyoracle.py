@@ -348,6 +348,28 @@ def gauss_regression(z, fp="f64"):
     return out
 
 
+def local_box_coordinates(parts, sym, loc, apix, fftsize, pr_threshold=90.0, boundx=100.0, fp="f64"):
+    """loc_box_coordinate.f90: sub-particle records (LOCAL_PARTICLE_DTYPE)."""
+    from cryoim_gb300._abi import LOCAL_PARTICLE_DTYPE
+    p = np.ascontiguousarray(parts)
+    s = np.ascontiguousarray(sym, np.float32).reshape(-1, 3, 3)
+    out = np.zeros(len(p) * len(s), LOCAL_PARTICLE_DTYPE)
+    R = _R(fp)
+    k = _fn("local_box_coordinates", fp)(_p(p), C.c_int(len(p)), _p(s), C.c_int(len(s)), R(loc[0]), R(loc[1]),
+                                         R(loc[2]), R(apix), C.c_int(fftsize), R(pr_threshold), R(boundx), _p(out))
+    return out[:k].copy()
+
+
+def local_refine(lp, map3d, imgs, lparts, fp="f64"):
+    """refine_PR.f90 on sub-particle records (a refined copy is returned)."""
+    q = np.array(lparts, copy=True)
+    m = np.ascontiguousarray(map3d, np.float32)
+    im = np.ascontiguousarray(imgs, np.float32)
+    r = _fn("local_refine", fp)(C.byref(lp), _p(m), _p(im), _p(q), C.c_int(len(q)))
+    assert r == 0
+    return q
+
+
 def equalort(theta, phi, omega, fp="f32"):
     out = np.zeros((60, 3), _dt(fp))
     R = _R(fp)
