@@ -63,7 +63,7 @@ class Params(C.Structure):
 class ContractOpts(C.Structure):
     """cryoim_contract_opts (include/cryoim.h)."""
     _fields_ = [("origin_max", C.c_float), ("origin_step", C.c_float), ("topk", C.c_int32),
-                ("pick", C.c_int32), ("precision", C.c_int32), ("nbr", C.c_int32)]
+                ("pick", C.c_int32), ("precision", C.c_int32), ("nbr", C.c_int32), ("coarse", C.c_int32)]
 
 
 _vp, _fp, _ip, _i32, _f32 = C.c_void_p, C.POINTER(C.c_float), C.POINTER(C.c_int32), C.c_int32, C.c_float

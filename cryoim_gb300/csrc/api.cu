@@ -170,6 +170,50 @@ template <class T> struct DBuf {
 // tnf half map (reconstruct_half.f90)
 enum { REC_FULL = 0, REC_SUBSTEP = 1, REC_HALF = 2 };
 
+// The ASU view grid of ort_globesearch.f90:68-101 at a given step: views (theta, phi,
+// slot bits, 0), with the slot <-> view maps used for grid neighbours.
+struct ViewGrid {
+    float step = 0.0f;
+    int nth = 0, nph = 0, nom = 0, V = 0;
+    std::vector<float> views;
+    std::vector<int> view_slot, slot_view;
+};
+
+static void build_view_grid(float step, ViewGrid* g) {
+    g->step = step;
+    g->nth = (int)(21.0f / step);
+    g->nph = (int)(32.0f / step);
+    g->nom = (int)(360.0f / step);
+    const Angles an = host_angles();
+    const float d2r = an.deg2rad;
+    const AsuPlanes pl = asu_planes(d2r);
+    g->views.clear();
+    for (int it = 0; it <= g->nth; ++it) {
+        const float theta = 69.0f + step * (float)it;
+        const float z = cosf(theta * d2r), z0 = sinf(theta * d2r);
+        for (int iph = 0; iph <= g->nph; ++iph) {
+            const float phi = step * (float)iph;
+            const float x = z0 * cosf(phi * d2r), y = z0 * sinf(phi * d2r);
+            if (!asu_inside(pl, x, y, z)) continue;
+            for (int sgn = (iph == 0 ? -1 : 1); sgn >= -1; sgn -= 2) {
+                const int slot = it * (2 * g->nph + 1) + (sgn * iph + g->nph);
+                float v[4] = {theta, sgn > 0 ? phi : -phi, 0.0f, 0.0f};
+                std::memcpy(&v[2], &slot, 4);
+                g->views.insert(g->views.end(), v, v + 4);
+            }
+        }
+    }
+    g->V = (int)(g->views.size() / 4);
+    g->view_slot.assign(g->V, -1);
+    g->slot_view.assign((size_t)(g->nth + 1) * (2 * g->nph + 1), -1);
+    for (int v = 0; v < g->V; ++v) {
+        int slot;
+        std::memcpy(&slot, &g->views[4 * v + 2], 4);
+        g->view_slot[v] = slot;
+        g->slot_view[slot] = v;
+    }
+}
+
 struct Ctx {
     int device = 0;
     cudaStream_t stream = nullptr;
@@ -232,6 +276,19 @@ struct Ctx {
     DBuf<float> mulA, mulB;
     DBuf<unsigned> bandmax;
     DBuf<int> fexp;
+    // coarse-to-fine proposals: a 2x-step grid, the half-radius band, a 2x-step origin
+    // grid; its BF16 sections; per-particle gathered fine rows
+    ViewGrid cgrid;
+    DBuf<int2> csamples_c;
+    int cS_c = 0, cKpad_c = 0, n_origin_c = 0;
+    float orig_max_c = -1.0f, orig_step_c = -1.0f;
+    DBuf<uint16_t> bmat_c, amat_c;
+    bool bmat_c_ready = false;
+    long n_orient_c = 0;
+    DBuf<float> corigins_c, topv_c, tilev_c, kcc_c;
+    DBuf<int> topi_c, tileo_c, tileorig_c, kor_c, korig_c, gidx;
+    DBuf<double> pnorm_c;
+    DBuf<uint8_t> bgather;
     DBuf<float> corigins, topv, kcc, kcand, kpr;
     DBuf<int> topi, gerr, kor, korig;
     DBuf<double> pnorm, kcc64;
@@ -240,7 +297,8 @@ struct Ctx {
     float orig_max = -1.0f, orig_step = -1.0f;
     DBuf<float> tilev, xcand, xpr;
     DBuf<int> tileo, tileorig;
-    DBuf<float2> xalpha;
+    DBuf<float2> xalpha, sband;
+    DBuf<int> xcount;
     // view <-> grid slot (itheta * (2 Nphi + 1) + iphi + Nphi) maps for neighbours
     std::vector<int> view_slot, slot_view;
     int num_sms = 0;
@@ -263,6 +321,10 @@ struct Ctx {
         tilev.release(); xcand.release(); xpr.release(); tileo.release(); tileorig.release();
         xalpha.release(); bmat8.release(); amat8.release(); mulA.release(); mulB.release();
         bandmax.release(); fexp.release();
+        csamples_c.release(); bmat_c.release(); amat_c.release(); corigins_c.release(); topv_c.release();
+        tilev_c.release(); kcc_c.release(); topi_c.release(); tileo_c.release(); tileorig_c.release();
+        kor_c.release(); korig_c.release(); gidx.release(); pnorm_c.release(); bgather.release();
+        sband.release(); xcount.release();
         if (pe0) cudaEventDestroy(pe0);
         if (pe1) cudaEventDestroy(pe1);
         if (own_stream && stream) cudaStreamDestroy(stream);
@@ -742,6 +804,126 @@ int ensure_bmat(Ctx* c) {
     return CRYOIM_OK;
 }
 
+// The coarse level of the proposal form: views at twice the search step, the band
+// minR <= |h| <= maxR/2, BF16 unit-norm sections (built as the fine ones), origins at
+// twice the origin step over the same range.
+int ensure_coarse(Ctx* c, float omax, float ostep) {
+    int r;
+    if ((r = ensure_grid(c))) return r;
+    if (!c->bmat_c_ready) {
+        build_view_grid(2.0f * c->p.searchstep, &c->cgrid);
+        const ViewGrid& g = c->cgrid;
+        if (g.nom < 1 || g.V < 1) return fail(CRYOIM_ERR_SIZE, "coarse grid is empty");
+        const int R = c->p.max_r, r0 = c->p.min_r, Rc = std::max(r0 + 1, R / 2);
+        std::vector<int2> s;
+        for (int ky = -Rc; ky <= Rc; ++ky)
+            for (int hx = 0; hx <= Rc; ++hx) {
+                if (hx == 0 && ky <= 0) continue;
+                const int d2 = hx * hx + ky * ky;
+                if (d2 >= r0 * r0 && d2 <= Rc * Rc) s.push_back(make_int2(hx, ky));
+            }
+        if ((r = c->csamples_c.ensure(s.size()))) return r;
+        CK(cudaMemcpyAsync(c->csamples_c.p, s.data(), sizeof(int2) * s.size(), cudaMemcpyHostToDevice, c->stream));
+        c->cS_c = (int)s.size();
+        c->cKpad_c = (2 * c->cS_c + 63) / 64 * 64;
+        const long n = (long)g.V * g.nom;
+        if ((r = c->bmat_c.ensure((size_t)n * c->cKpad_c))) return r;
+        std::vector<float> v2(2 * (size_t)g.V);
+        for (int v = 0; v < g.V; ++v) { v2[2 * v] = g.views[4 * v]; v2[2 * v + 1] = g.views[4 * v + 1]; }
+        DBuf<float> dv;
+        if ((r = dv.ensure(v2.size()))) return r;
+        CK(cudaMemcpyAsync(dv.p, v2.data(), sizeof(float) * v2.size(), cudaMemcpyHostToDevice, c->stream));
+        cudaArray_t arr = nullptr;
+        cudaTextureObject_t tex = 0;
+        cudaError_t te = make_cube_texture(c->mapcube.p, R, c->stream, &arr, &tex);
+        if (te == cudaSuccess)
+            te = launch_slice_bf16(tex, R, c->csamples_c.p, c->cS_c, c->cKpad_c, dv.p, g.nom, g.step, 0, n,
+                                   c->bmat_c.p, c->stream);
+        if (te == cudaSuccess) te = cudaStreamSynchronize(c->stream);
+        free_cube_texture(arr, tex);
+        if (te != cudaSuccess) return fail(CRYOIM_ERR_CUDA, "coarse sections: %s", cudaGetErrorString(te));
+        c->n_orient_c = n;
+        c->bmat_c_ready = true;
+    }
+    if (omax != c->orig_max_c || 2.0f * ostep != c->orig_step_c) {
+        const float st = 2.0f * ostep;
+        const int n1 = (int)(2.0f * omax / st + 0.5f) + 1;
+        std::vector<float> og;
+        for (int iy = 0; iy < n1; ++iy)
+            for (int ix = 0; ix < n1; ++ix) {
+                og.push_back(-omax + st * (float)ix);
+                og.push_back(-omax + st * (float)iy);
+            }
+        if ((r = c->corigins_c.ensure(og.size()))) return r;
+        CK(cudaMemcpyAsync(c->corigins_c.p, og.data(), sizeof(float) * og.size(), cudaMemcpyHostToDevice,
+                           c->stream));
+        c->n_origin_c = n1 * n1;
+        c->orig_max_c = omax;
+        c->orig_step_c = st;
+    }
+    return CRYOIM_OK;
+}
+
+// Coarse level for nb prepared particles (c->band, ctfp): the best kc distinct coarse
+// orientations of each, mapped onto the fine grid (twice the coarse indices) with their
+// fine neighbours within nbf steps in theta, phi and omega -> lists[i], sorted.
+int coarse_lists(Ctx* c, int nb, const float* ctfp, int kc, int nbf, std::vector<std::vector<int>>& lists) {
+    const ViewGrid& g = c->cgrid;
+    const int Oc = c->n_origin_c;
+    const int ntc = (int)((c->n_orient_c + gemm_tile_n() - 1) / gemm_tile_n());
+    int r;
+    if ((r = c->amat_c.ensure((size_t)nb * Oc * c->cKpad_c)) || (r = c->topv_c.ensure((size_t)nb * Oc * ntc)) ||
+        (r = c->topi_c.ensure((size_t)nb * Oc * ntc)) || (r = c->tilev_c.ensure((size_t)nb * ntc)) ||
+        (r = c->tileo_c.ensure((size_t)nb * ntc)) || (r = c->tileorig_c.ensure((size_t)nb * ntc)) ||
+        (r = c->kor_c.ensure((size_t)nb * kc)) || (r = c->korig_c.ensure((size_t)nb * kc)) ||
+        (r = c->kcc_c.ensure((size_t)nb * kc)) || (r = c->pnorm_c.ensure(nb)))
+        return r;
+    launch_particle_norm(c->band.p, ctfp, c->bd, c->csamples_c.p, c->cS_c, nb, c->pnorm_c.p, c->stream);
+    launch_build_a(c->band.p, ctfp, c->bd, c->csamples_c.p, c->cS_c, c->cKpad_c, c->corigins_c.p, Oc, c->pnorm_c.p,
+                   nb, c->amat_c.p, c->stream);
+    GemmArgmaxArgs ga{};
+    ga.topv = c->topv_c.p;
+    ga.topi = c->topi_c.p;
+    ga.err = c->gerr.p;
+    CK(cudaMemsetAsync(c->gerr.p, 0, sizeof(int), c->stream));
+    CK(launch_gemm_argmax(c->amat_c.p, c->bmat_c.p, nb * Oc, (int)c->n_orient_c, c->cKpad_c, false, ga, c->num_sms,
+                          c->stream));
+    launch_select_topk(c->topv_c.p, c->topi_c.p, Oc, ntc, kc, nb, c->tilev_c.p, c->tileo_c.p, c->tileorig_c.p,
+                       c->kor_c.p, c->korig_c.p, c->kcc_c.p, c->stream);
+    CK(cudaGetLastError());
+    std::vector<int> kor((size_t)nb * kc);
+    int gerr = 0;
+    CK(cudaMemcpyAsync(&gerr, c->gerr.p, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
+    CK(cudaMemcpyAsync(kor.data(), c->kor_c.p, sizeof(int) * nb * kc, cudaMemcpyDeviceToHost, c->stream));
+    CK(cudaStreamSynchronize(c->stream));
+    if (gerr) return fail(CRYOIM_ERR_CUDA, "coarse contraction wait timed out");
+    if (c->prof) c->prof_gemm_flops += 2.0 * (double)nb * Oc * (double)c->n_orient_c * (double)c->cKpad_c;
+    const int span_c = 2 * g.nph + 1, span = 2 * c->nph + 1;
+    lists.assign(nb, std::vector<int>());
+    for (int i = 0; i < nb; ++i) {
+        std::vector<int>& lst = lists[i];
+        for (int j = 0; j < kc; ++j) {
+            const int n = kor[(size_t)i * kc + j];
+            if (n < 0) continue;
+            const int vc = n / g.nom, ioc = n % g.nom, slot = g.view_slot[vc];
+            const int it = 2 * (slot / span_c), ips = 2 * (slot % span_c - g.nph), io = 2 * ioc;
+            for (int dt = -nbf; dt <= nbf; ++dt)
+                for (int dp = -nbf; dp <= nbf; ++dp) {
+                    const int it2 = it + dt, ips2 = ips + dp;
+                    if (it2 < 0 || it2 > c->nth || ips2 < -c->nph || ips2 > c->nph) continue;
+                    const int v2 = c->slot_view[(size_t)it2 * span + ips2 + c->nph];
+                    if (v2 < 0) continue;
+                    for (int dw = -nbf; dw <= nbf; ++dw)
+                        lst.push_back(v2 * c->nom + ((io + dw) % c->nom + c->nom) % c->nom);
+                }
+        }
+        std::sort(lst.begin(), lst.end());
+        lst.erase(std::unique(lst.begin(), lst.end()), lst.end());
+        if (lst.empty()) lst.push_back(0);
+    }
+    return CRYOIM_OK;
+}
+
 // FP8-e4m3 copy of operand B with per-band power-of-two scales (contract.cu explains the
 // scaling): band maxima of the BF16 rows (every 4th orientation), e_b = floor(log2(224 /
 // max_b)), mulB = 2^e_b and mulA = 2^-e_b per sample, then the conversion.
@@ -808,8 +990,12 @@ int contract_impl(Ctx* c, const float* imgs, bool on_device, cryoim_particle* pa
     const int nbr = opts->nbr <= 0 ? 1 : opts->nbr;
     const int nbox = (2 * nbr + 1) * (2 * nbr + 1) * (2 * nbr + 1);
     if (nbr > 3 || (long)nbox * k > 4096) return fail(CRYOIM_ERR_ARG, "(2 nbr + 1)^3 x topk must be <= 4096");
+    const int kc = opts->coarse;  // 0: exhaustive; else coarse proposals per particle
+    const int nbf = 2;            // fine neighbourhood of a coarse proposal, in fine steps
+    if (kc < 0 || kc > 64) return fail(CRYOIM_ERR_ARG, "coarse must be 0..64");
     if (P == 0) return CRYOIM_OK;
     if ((r = f8 ? ensure_bmat8(c) : ensure_bmat(c))) return r;
+    if (kc > 0 && (r = ensure_coarse(c, opts->origin_max, opts->origin_step))) return r;
     const int kpad = f8 ? c->cKpad8 : c->cKpad;
     c->last_kpad = kpad;
     c->last_slice_ms = c->bmat_ms + (f8 ? c->bmat8_ms : 0.0);
@@ -852,7 +1038,9 @@ int contract_impl(Ctx* c, const float* imgs, bool on_device, cryoim_particle* pa
         (r = c->tileorig.ensure((size_t)pb * ntiles)) || (r = c->xcand.ensure((size_t)pb * maxx * 5)) ||
         (r = c->xpr.ensure((size_t)pb * maxx)))
         return r;
-    if (T > 0 && (r = c->xalpha.ensure((size_t)pb * maxx * T * 60))) return r;
+    if (T > 0 && ((r = c->xalpha.ensure((size_t)pb * maxx * T * 60)) ||
+                  (r = c->sband.ensure((size_t)pb * c->bd.W * c->bd.W)) || (r = c->xcount.ensure(pb))))
+        return r;
     if (c->num_sms == 0) CK(cudaDeviceGetAttribute(&c->num_sms, cudaDevAttrMultiProcessorCount, c->device));
     std::vector<int> src(P);
     {
@@ -918,17 +1106,64 @@ int contract_impl(Ctx* c, const float* imgs, bool on_device, cryoim_particle* pa
         g.cfull = nullptr;
         g.err = c->gerr.p;
         CK(cudaMemsetAsync(c->gerr.p, 0, sizeof(int), c->stream));
-        if (c->prof) CK(cudaEventRecord(g0, c->stream));
-        if (f8)
-            CK(launch_gemm_argmax(c->amat8.p, c->bmat8.p, nb * O, (int)c->n_orient, kpad, true, g, c->num_sms,
-                                  c->stream));
-        else
-            CK(launch_gemm_argmax(c->amat.p, c->bmat.p, nb * O, (int)c->n_orient, kpad, false, g, c->num_sms,
-                                  c->stream));
-        if (c->prof) CK(cudaEventRecord(g1, c->stream));
-        launch_select_topk(c->topv.p, c->topi.p, O, ntiles, k, nb, c->tilev.p, c->tileo.p, c->tileorig.p,
-                           c->kor.p, c->korig.p, c->kcc.p, c->stream);
-        CK(cudaGetLastError());
+        std::vector<std::vector<int>> lists;
+        if (kc > 0) {
+            // proposal form: the coarse level names each particle's candidate orientations,
+            // the fine contraction runs on their gathered sections only
+            if (c->prof) CK(cudaEventRecord(g0, c->stream));
+            if ((r = coarse_lists(c, nb, ctfp, kc, nbf, lists))) return r;
+            const long row_bytes = f8 ? (long)c->cKpad8 : 2L * c->cKpad;
+            const void* bsrc = f8 ? (const void*)c->bmat8.p : (const void*)c->bmat.p;
+            const char* abase = f8 ? (const char*)c->amat8.p : (const char*)c->amat.p;
+            CK(cudaMemsetAsync(c->gerr.p, 0, sizeof(int), c->stream));
+            // particles in groups whose gathered sections stay under 4 GB: one gather per
+            // group, then per particle a contraction over its own rows and a selection of k
+            // distinct orientations, all queued without a host wait
+            for (int i0 = 0; i0 < nb;) {
+                int i1 = i0;
+                long rows = 0;
+                while (i1 < nb && (i1 == i0 || (rows + (long)lists[i1].size()) * row_bytes <= (4L << 30)))
+                    rows += (long)lists[i1++].size();
+                std::vector<int> idx;
+                idx.reserve(rows);
+                for (int i = i0; i < i1; ++i) idx.insert(idx.end(), lists[i].begin(), lists[i].end());
+                if ((r = c->gidx.ensure(rows)) || (r = c->bgather.ensure((size_t)rows * row_bytes))) return r;
+                CK(cudaMemcpyAsync(c->gidx.p, idx.data(), sizeof(int) * rows, cudaMemcpyHostToDevice, c->stream));
+                CK(launch_gather_rows(bsrc, row_bytes, c->gidx.p, (int)rows, c->bgather.p, c->stream));
+                long roff = 0, toff = 0;
+                for (int i = i0; i < i1; ++i) {
+                    const int nl = (int)lists[i].size();
+                    const int ntp = (nl + gemm_tile_n() - 1) / gemm_tile_n();
+                    GemmArgmaxArgs gi = g;
+                    gi.topv = c->topv.p + toff;
+                    gi.topi = c->topi.p + toff;
+                    CK(launch_gemm_argmax(abase + (size_t)i * O * row_bytes, c->bgather.p + roff * row_bytes, O, nl,
+                                          kpad, f8, gi, c->num_sms, c->stream));
+                    launch_select_distinct(gi.topv, gi.topi, O, ntp, k, c->kor.p + (size_t)i * k,
+                                           c->korig.p + (size_t)i * k, c->kcc.p + (size_t)i * k, c->stream);
+                    CK(cudaGetLastError());
+                    roff += nl;
+                    toff += (long)O * ntp;
+                    if (c->prof) c->prof_gemm_flops += 2.0 * (double)O * (double)nl * (double)kpad;
+                }
+                // the gather buffer is reused by the next group
+                if (i1 < nb) CK(cudaStreamSynchronize(c->stream));
+                i0 = i1;
+            }
+            if (c->prof) CK(cudaEventRecord(g1, c->stream));
+        } else {
+            if (c->prof) CK(cudaEventRecord(g0, c->stream));
+            if (f8)
+                CK(launch_gemm_argmax(c->amat8.p, c->bmat8.p, nb * O, (int)c->n_orient, kpad, true, g, c->num_sms,
+                                      c->stream));
+            else
+                CK(launch_gemm_argmax(c->amat.p, c->bmat.p, nb * O, (int)c->n_orient, kpad, false, g, c->num_sms,
+                                      c->stream));
+            if (c->prof) CK(cudaEventRecord(g1, c->stream));
+            launch_select_topk(c->topv.p, c->topi.p, O, ntiles, k, nb, c->tilev.p, c->tileo.p, c->tileorig.p,
+                               c->kor.p, c->korig.p, c->kcc.p, c->stream);
+            CK(cudaGetLastError());
+        }
         int gerr = 0;
         CK(cudaMemcpyAsync(&gerr, c->gerr.p, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
         CK(cudaMemcpyAsync(hor.data(), c->kor.p, sizeof(int) * nb * k, cudaMemcpyDeviceToHost, c->stream));
@@ -940,12 +1175,15 @@ int contract_impl(Ctx* c, const float* imgs, bool on_device, cryoim_particle* pa
         if (gerr) return fail(CRYOIM_ERR_CUDA, "contraction pipeline wait timed out");
         if (f8)  // remove the per-particle exponent: the CC of the unit-norm rows
             for (int i = 0; i < nb * k; ++i) hcc[i] = std::ldexp(hcc[i], -hfe[i / k]);
+        if (kc > 0)  // gathered column -> fine orientation index
+            for (int i = 0; i < nb * k; ++i)
+                if (hor[i] >= 0) hor[i] = lists[i / k][hor[i]];
         if (c->prof) {
             float ms = 0.f;
             CK(cudaEventElapsedTime(&ms, g0, g1));
             c->prof_gemm_ms += ms;
             c->prof_gemm_launches += 1;
-            c->prof_gemm_flops += 2.0 * (double)nb * O * (double)c->n_orient * (double)kpad;
+            if (kc == 0) c->prof_gemm_flops += 2.0 * (double)nb * O * (double)c->n_orient * (double)kpad;
         }
         // candidates (theta, phi, omega, x, y) of the selected (orientation, origin) pairs
         for (int i = 0; i < nb * k; ++i) {
@@ -1005,11 +1243,16 @@ int contract_impl(Ctx* c, const float* imgs, bool on_device, cryoim_particle* pa
                 }
             CK(cudaMemcpyAsync(c->xcand.p, hx.data(), sizeof(float) * hx.size(), cudaMemcpyHostToDevice,
                                c->stream));
+            std::vector<int> hcount(nb);
+            for (int i = 0; i < nb; ++i) hcount[i] = (int)xs[i].size();
+            CK(cudaMemcpyAsync(c->xcount.p, hcount.data(), sizeof(int) * nb, cudaMemcpyHostToDevice, c->stream));
             launch_refine_alpha(c->xcand.p, nb, c->tort.p, T, c->ops.p, c->xalpha.p, c->stream, maxc);
+            // every candidate of a particle sits at the particle's origin: shift its band once
+            CK(launch_shift_band(c->band.p, c->xcand.p, maxc, c->bd, nb, c->sband.p, c->stream));
             PrSingleArgs a{};
             a.band = c->band.p; a.fcut0 = c->fcut0.p; a.tband = c->tband.p; a.tfcut = tfc;
             a.tfcut_pstride = tfs; a.ctf = ctfp; a.cand = c->xcand.p; a.alpha = c->xalpha.p; a.T = T;
-            a.bd = c->bd; a.pr = c->xpr.p; a.ncand = maxc;
+            a.bd = c->bd; a.pr = c->xpr.p; a.ncand = maxc; a.sband = c->sband.p; a.ncount = c->xcount.p;
             CK(launch_pr_single(a, nb, c->stream));
             hpr.resize((size_t)nb * maxc);
             CK(cudaMemcpyAsync(hpr.data(), c->xpr.p, sizeof(float) * nb * maxc, cudaMemcpyDeviceToHost,
@@ -1227,11 +1470,14 @@ int cryoim_set_params(void* ctx, const cryoim_params* p) {
         c->cS = 0;
         c->bmat_ready = false;
         c->bmat8_ready = false;
+        c->cS_c = 0;
+        c->bmat_c_ready = false;
     }
     if (step_changed) {
         c->grid_ready = false;
         c->bmat_ready = false;
         c->bmat8_ready = false;
+        c->bmat_c_ready = false;
     }
     long nn = (long)p->fftsize * p->fftsize;
     c->batch = (int)std::max(1L, std::min(64L, (long)(16L * 1024 * 1024) / nn));
@@ -2084,6 +2330,7 @@ int cryoim_set_reference_map(void* ctx, const float* map3d) {
     c->map_ready = true;
     c->bmat_ready = false;
     c->bmat8_ready = false;
+    c->bmat_c_ready = false;
     return CRYOIM_OK;
 }
 

@@ -230,6 +230,59 @@ __global__ void k_select_topk(float* __restrict__ v, const int* __restrict__ ori
     }
 }
 
+// Proposal form, one particle: the k best (origin row, column tile) maxima with
+// distinct orientations.  v[o * ntiles + t] is the best CC of tile t at origin o and
+// col[...] its column in the gathered list; once a column is taken, every entry that
+// names it is retired, so the candidates are k distinct orientations, each at its best
+// origin.  Columns are remapped to orientations on the host.
+__global__ void k_select_distinct(float* __restrict__ v, const int* __restrict__ col, int O, int ntiles, int k,
+                                  int* __restrict__ out_col, int* __restrict__ out_origin,
+                                  float* __restrict__ out_cc) {
+    __shared__ float sv[32];
+    __shared__ int si[32];
+    __shared__ int taken;
+    const int cnt = O * ntiles;
+    const int w = threadIdx.x >> 5, l = threadIdx.x & 31, nw = blockDim.x >> 5;
+    for (int r = 0; r < k; ++r) {
+        float bv = -3.0e38f;
+        int bi = -1;
+        for (int q = threadIdx.x; q < cnt; q += blockDim.x) {
+            const float x = v[q];
+            if (col[q] >= 0 && x > bv) { bv = x; bi = q; }
+        }
+        for (int off = 16; off > 0; off >>= 1) {
+            float ov = __shfl_xor_sync(0xffffffffu, bv, off);
+            int oi = __shfl_xor_sync(0xffffffffu, bi, off);
+            if (ov > bv || (ov == bv && oi >= 0 && (bi < 0 || oi < bi))) { bv = ov; bi = oi; }
+        }
+        if (l == 0) { sv[w] = bv; si[w] = bi; }
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            float v0 = sv[0];
+            int i0 = si[0];
+            for (int q = 1; q < nw; ++q)
+                if (sv[q] > v0 || (sv[q] == v0 && si[q] >= 0 && (i0 < 0 || si[q] < i0))) { v0 = sv[q]; i0 = si[q]; }
+            if (i0 >= 0 && v0 > -3.0e38f) {
+                out_col[r] = col[i0];
+                out_origin[r] = i0 / ntiles;
+                out_cc[r] = v0;
+                taken = col[i0];
+            } else {
+                out_col[r] = -1;
+                out_origin[r] = 0;
+                out_cc[r] = -3.0e38f;
+                taken = -1;
+            }
+        }
+        __syncthreads();
+        const int t = taken;
+        if (t >= 0)
+            for (int q = threadIdx.x; q < cnt; q += blockDim.x)
+                if (col[q] == t) v[q] = -3.0e38f;
+        __syncthreads();
+    }
+}
+
 // FP64 rescoring of one (particle, candidate): the same CC with every product,
 // interpolation and sum in double precision.
 __global__ void k_cc_fp64(const float2* __restrict__ cube, const float2* __restrict__ band,
@@ -393,9 +446,24 @@ __global__ void __launch_bounds__(256) k_build_a8(const float2* __restrict__ ban
     }
 }
 
+// One CTA per gathered row: dst[r] = src[idx[r]], rows of row_bytes (a multiple of 16).
+__global__ void k_gather_rows(const uint4* __restrict__ src, long row_vec, const int* __restrict__ idx,
+                              uint4* __restrict__ dst) {
+    const long r = blockIdx.x;
+    const uint4* s = src + (long)idx[r] * row_vec;
+    uint4* d = dst + r * row_vec;
+    for (long i = threadIdx.x; i < row_vec; i += blockDim.x) d[i] = s[i];
+}
+
 inline int cdiv(long a, long b) { return (int)((a + b - 1) / b); }
 
 }  // namespace
+
+cudaError_t launch_gather_rows(const void* src, long row_bytes, const int* idx, int n, void* dst, cudaStream_t st) {
+    if (row_bytes % 16 || n < 1) return cudaErrorInvalidValue;
+    k_gather_rows<<<n, 256, 0, st>>>((const uint4*)src, row_bytes / 16, idx, (uint4*)dst);
+    return cudaGetLastError();
+}
 
 cudaError_t launch_band_absmax(const void* B, long n, int Kpad, const int2* samples, int S, int nband, int stride,
                                unsigned* out, int sms, cudaStream_t st) {
@@ -502,6 +570,11 @@ void launch_select_topk(const float* topv, const int* topi, int O, int ntiles, i
     dim3 g(ntiles, B);
     k_tile_best<<<g, 256, 0, st>>>(topv, topi, O, ntiles, tile_v, tile_o, tile_orig);
     k_select_topk<<<B, 512, 0, st>>>(tile_v, tile_o, tile_orig, ntiles, k, orient, origin, cc);
+}
+
+void launch_select_distinct(float* topv, const int* topi, int O, int ntiles, int k, int* col, int* origin,
+                            float* cc, cudaStream_t st) {
+    k_select_distinct<<<1, 512, 0, st>>>(topv, topi, O, ntiles, k, col, origin, cc);
 }
 
 void launch_cc_fp64(const float2* cube, const float2* band, const float* ctf, Band bd, const int2* samples,

@@ -36,7 +36,8 @@ const char* kKeys[] = {"apix",         "minRes",       "maxRes",     "imgmask", 
                        "realspaceavg", "ortfile",      "recISAF",    "subrec",     "FSC",
                        "imgstck",      "sym",          "maxcentshift", "corrCTF",  "boundX",
                        "loc_box",      "check"};
-const char* kExt[] = {"device", "batch", "contract", "originmax", "originstep", "topk", "precision", "nbr"};
+const char* kExt[] = {"device", "batch", "contract", "originmax", "originstep", "topk", "precision", "nbr",
+                      "coarse"};
 
 void usage() {
     std::puts(
@@ -246,7 +247,7 @@ int main(int argc, char** argv) {
         if (cryoim_load_templates(ctx, timg.data(), t.data(), T)) return die("templates", 2);
         const bool contract = mode == 4 && yes(sval("contract", "n"));
         cryoim_contract_opts co{fval("originmax", 6.0f), fval("originstep", 0.5f), ival("topk", 16), 0,
-                                sval("precision", "bf16") == "fp8" ? 1 : 0, ival("nbr", 1)};
+                                sval("precision", "bf16") == "fp8" ? 1 : 0, ival("nbr", 1), ival("coarse", 0)};
         if (contract) {
             if (map.empty()) return die("contract=y needs model3d", 2);
             if (cryoim_set_reference_map(ctx, map.data())) return die("reference map", 2);

@@ -100,8 +100,13 @@ struct PrSingleArgs {
     Band bd;
     float* pr;               // [B][ncand]
     int ncand = 11;          // 11 for the refinement step (ort_cent_11.f90)
+    const float2* sband = nullptr;  // [B][W*W] band shifted to the candidates' common origin, or nullptr
+    const int* ncount = nullptr;    // [B] candidates in use (later slots are skipped), or nullptr
 };
 cudaError_t launch_pr_single(const PrSingleArgs& a, int B, cudaStream_t st);
+// sband for PrSingleArgs: the band of each particle shifted to cand[p][0]'s origin
+cudaError_t launch_shift_band(const float2* band, const float* cand, int ncand, const Band& bd, int B,
+                              float2* out, cudaStream_t st);
 
 struct InsertArgs {
     const float2* band;      // [B][W*W] shifted particle FT
@@ -162,6 +167,10 @@ void launch_select_topk(const float* topv, const int* topi, int O, int ntiles, i
 void launch_cc_fp64(const float2* cube, const float2* band, const float* ctf, Band bd, const int2* samples,
                     int S, const float* cand, int k, int B, double* out, cudaStream_t st);
 
+// dst row r = src row idx[r] (row_bytes a multiple of 16), n rows
+void launch_select_distinct(float* topv, const int* topi, int O, int ntiles, int k, int* col, int* origin,
+                            float* cc, cudaStream_t st);
+cudaError_t launch_gather_rows(const void* src, long row_bytes, const int* idx, int n, void* dst, cudaStream_t st);
 // FP8-e4m3 operands (contract.cu): per-band max |B| (R+1 bands, float bits) over every
 // stride-th row; B8 = e4m3(B x mulB) with rows of Kpad8 bytes; A8 rows with mulA and the
 // per-particle exponent fexp (written by launch_build_a8).

@@ -41,11 +41,9 @@ struct Consts {
 };
 
 // Template line sample (template x CTF, bilinear) at angle alpha2, radius fr.
-__device__ __forceinline__ void tmpl_sample(const float2* __restrict__ tb, const float* __restrict__ cb,
-                                            int W, int offW, float nxh, float alpha2, float fr,
-                                            float d2r, float* re, float* im) {
-    float ang = __fmul_rn(alpha2, d2r);
-    float cs = cosf(ang), sn = sinf(ang);
+__device__ __forceinline__ void tmpl_sample_cs(const float2* __restrict__ tb, const float* __restrict__ cb,
+                                               int W, int offW, float nxh, float cs, float sn, float fr,
+                                               float* re, float* im) {
     float x = __fadd_rn(__fmul_rn(fr, cs), nxh), y = __fadd_rn(__fmul_rn(fr, sn), nxh);
     int lx = (int)x, ly = (int)y;
     float ax = __fsub_rn(x, (float)lx), ay = __fsub_rn(y, (float)ly);
@@ -60,6 +58,13 @@ __device__ __forceinline__ void tmpl_sample(const float2* __restrict__ tb, const
     }
     *re = bilerp(ax, ay, t00.x, t10.x, t01.x, t11.x);
     *im = bilerp(ax, ay, t00.y, t10.y, t01.y, t11.y);
+}
+
+__device__ __forceinline__ void tmpl_sample(const float2* __restrict__ tb, const float* __restrict__ cb,
+                                            int W, int offW, float nxh, float alpha2, float fr,
+                                            float d2r, float* re, float* im) {
+    float ang = __fmul_rn(alpha2, d2r);
+    tmpl_sample_cs(tb, cb, W, offW, nxh, cosf(ang), sinf(ang), fr, re, im);
 }
 
 // Angle between two complex numbers z1, z2 from their cross and dot products, in [0, pi]:
@@ -214,14 +219,17 @@ __global__ void __launch_bounds__(768, 1) k_pr_omega(PrOmegaArgs a, int nomp, Co
 // same per-pixel arithmetic as shifting the whole transform first.
 __global__ void __launch_bounds__(512) k_pr_single(PrSingleArgs a, Consts K) {
     __shared__ double sh[2][32];
+    __shared__ float sline[4][60];  // cos, sin of the particle line; cos, sin of the template line
     const Band bd = a.bd;
     const int W = bd.W, nr = bd.nr, minR = bd.min_r, nx = bd.nx;
     const int c = blockIdx.x, p = blockIdx.y;
+    if (a.ncount && c >= a.ncount[p]) return;  // padding slot (whole block)
     const float* cd = a.cand + ((long)p * a.ncand + c) * 5;
     const float nxh = (float)(nx / 2);
     const float xs = __fadd_rn(cd[3], nxh), ys = __fadd_rn(cd[4], nxh);
     const int offW = bd.off * W + bd.off;
     const float2* pb = a.band + (long)p * W * W;
+    const float2* sb = a.sband ? a.sband + (long)p * W * W : nullptr;
     const float* ctfp = a.ctf ? a.ctf + (long)p * W * W : nullptr;
     const float* fc0 = a.fcut0 + (long)p * nr;
     const float* tfc = a.tfcut + (long)p * a.tfcut_pstride;
@@ -231,35 +239,56 @@ __global__ void __launch_bounds__(512) k_pr_single(PrSingleArgs a, Consts K) {
         const float2* al = a.alpha + (((long)p * a.ncand + c) * a.T + i) * 60;
         const float2* tb = a.tband + (long)i * W * W;
         const float* fct = tfc + (long)i * nr;
+        // the two in-plane directions of each common line, once per line
+        __syncthreads();
+        if (threadIdx.x < 60) {
+            const float2 aa = al[threadIdx.x];
+            if (aa.x < 999.0f && aa.y < 999.0f) {
+                const float a1 = __fmul_rn(aa.x, K.d2r), a2 = __fmul_rn(aa.y, K.d2r);
+                sline[0][threadIdx.x] = cosf(a1);
+                sline[1][threadIdx.x] = sinf(a1);
+                sline[2][threadIdx.x] = cosf(a2);
+                sline[3][threadIdx.x] = sinf(a2);
+            }
+        }
+        __syncthreads();
         for (int q = threadIdx.x; q < 60 * nr; q += blockDim.x) {
             int j = q / nr, iq = q - j * nr;
             float2 aa = al[j];
             if (!(aa.x < 999.0f && aa.y < 999.0f)) continue;
             const float fr = (float)(minR + iq);
             // particle sample with the candidate origin shift on each tap
-            float ang = __fmul_rn(aa.x, K.d2r);
-            float cs = cosf(ang), sn = sinf(ang);
+            float cs = sline[0][j], sn = sline[1][j];
             float x = __fadd_rn(__fmul_rn(fr, cs), nxh), y = __fadd_rn(__fmul_rn(fr, sn), nxh);
             int lx = (int)x, ly = (int)y;
             float ax = __fsub_rn(x, (float)lx), ay = __fsub_rn(y, (float)ly);
             float tr[4], ti[4];
+            if (sb) {
 #pragma unroll
-            for (int u = 0; u < 4; ++u) {
-                int tx = lx + (u & 1), ty = ly + (u >> 1);
-                float2 vv = pb[ty * W + tx - offW];
-                int hx = tx - nx / 2, ky = ty - nx / 2;
-                float ph = __fdiv_rn(__fmul_rn(twopi, __fadd_rn(__fmul_rn(xs, (float)hx),
-                                                                 __fmul_rn(ys, (float)ky))),
-                                     (float)nx);
-                float s, co;
-                sincosf(ph, &s, &co);
-                tr[u] = __fadd_rn(__fmul_rn(vv.x, co), __fmul_rn(vv.y, s));
-                ti[u] = __fadd_rn(__fmul_rn(-vv.x, s), __fmul_rn(vv.y, co));
+                for (int u = 0; u < 4; ++u) {
+                    const float2 vv = sb[(ly + (u >> 1)) * W + lx + (u & 1) - offW];
+                    tr[u] = vv.x;
+                    ti[u] = vv.y;
+                }
+            } else {
+#pragma unroll
+                for (int u = 0; u < 4; ++u) {
+                    int tx = lx + (u & 1), ty = ly + (u >> 1);
+                    float2 vv = pb[ty * W + tx - offW];
+                    int hx = tx - nx / 2, ky = ty - nx / 2;
+                    float ph = __fdiv_rn(__fmul_rn(twopi, __fadd_rn(__fmul_rn(xs, (float)hx),
+                                                                     __fmul_rn(ys, (float)ky))),
+                                         (float)nx);
+                    float s, co;
+                    sincosf(ph, &s, &co);
+                    tr[u] = __fadd_rn(__fmul_rn(vv.x, co), __fmul_rn(vv.y, s));
+                    ti[u] = __fadd_rn(__fmul_rn(-vv.x, s), __fmul_rn(vv.y, co));
+                }
             }
             float re1 = bilerp(ax, ay, tr[0], tr[1], tr[2], tr[3]);
             float im1 = bilerp(ax, ay, ti[0], ti[1], ti[2], ti[3]);
             float re2, im2;
-            tmpl_sample(tb, ctfp, W, offW, nxh, aa.y, fr, K.d2r, &re2, &im2);
+            tmpl_sample_cs(tb, ctfp, W, offW, nxh, sline[2][j], sline[3][j], fr, &re2, &im2);
             float amp1 = sqrtf(re1 * re1 + im1 * im1);
             float amp2 = sqrtf(re2 * re2 + im2 * im2);
             if (amp1 >= fc0[iq] && amp2 >= fct[iq]) {
@@ -285,6 +314,29 @@ __global__ void __launch_bounds__(512) k_pr_single(PrSingleArgs a, Consts K) {
         float f1 = (float)s1, f2 = (float)s2;
         a.pr[(long)p * a.ncand + c] = (f2 > 1.0e-10f) ? f1 / f2 * 180.0f / K.pi : 1000.0f;
     }
+}
+
+// The particle transform shifted to the origin its candidates share (cand[p][0][3..4]):
+// per pixel the same phase rotation k_pr_single applies to each bilinear tap
+// (img2d_FT_centshift.f90), computed once per pixel instead of once per tap.
+__global__ void k_shift_band(const float2* __restrict__ band, const float* __restrict__ cand, int ncand, Band bd,
+                             Consts K, float2* __restrict__ out) {
+    const int W = bd.W, nx = bd.nx, p = blockIdx.y;
+    const int m = blockIdx.x * blockDim.x + threadIdx.x;
+    if (m >= W * W) return;
+    const float* cd = cand + (long)p * ncand * 5;
+    const float nxh = (float)(nx / 2);
+    const float xs = __fadd_rn(cd[3], nxh), ys = __fadd_rn(cd[4], nxh);
+    const float twopi = __fmul_rn(2.0f, K.pi);
+    const int by = m / W, bx = m - by * W;
+    const int hx = bx + bd.off - nx / 2, ky = by + bd.off - nx / 2;
+    const float2 vv = band[(long)p * W * W + m];
+    float ph = __fdiv_rn(__fmul_rn(twopi, __fadd_rn(__fmul_rn(xs, (float)hx), __fmul_rn(ys, (float)ky))),
+                         (float)nx);
+    float s, co;
+    sincosf(ph, &s, &co);
+    out[(long)p * W * W + m] = make_float2(__fadd_rn(__fmul_rn(vv.x, co), __fmul_rn(vv.y, s)),
+                                           __fadd_rn(__fmul_rn(-vv.x, s), __fmul_rn(vv.y, co)));
 }
 
 // reconstruct.f90:103-145: rotate each half-plane sample, apply the 60 operators,
@@ -379,6 +431,14 @@ cudaError_t launch_pr_omega(const PrOmegaArgs& a, int B, cudaStream_t st) {
     if (e != cudaSuccess) return e;
     dim3 grid(a.V, B);
     k_pr_omega<<<grid, nt, sm, st>>>(a, nomp, consts());
+    return cudaGetLastError();
+}
+
+cudaError_t launch_shift_band(const float2* band, const float* cand, int ncand, const Band& bd, int B,
+                              float2* out, cudaStream_t st) {
+    const int n = bd.W * bd.W;
+    dim3 grid((n + 255) / 256, B);
+    k_shift_band<<<grid, 256, 0, st>>>(band, cand, ncand, bd, consts(), out);
     return cudaGetLastError();
 }
 

@@ -425,6 +425,11 @@ typedef struct cryoim_contract_opts {
     int32_t nbr;        /* PR rescoring of each candidate's grid neighbours within
                            nbr steps in theta, phi and omega (1: 26 neighbours; 0 is
                            taken as 1); (2 nbr + 1)^3 x topk <= 4096                 */
+    int32_t coarse;     /* 0: every grid orientation is correlated.  k > 0 (<= 64):
+                           proposal form: a BF16 contraction over half the band, a
+                           grid of twice the step and origins at twice the step names
+                           k orientations; only their fine neighbourhoods (+-2 steps)
+                           are correlated at full band                              */
 } cryoim_contract_opts;
 /* The 3D map (nx^3 float32) whose central sections are correlated: its centred Fourier
  * transform is kept as a band cube of (2 maxR + 3)^3 complex values. */

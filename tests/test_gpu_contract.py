@@ -141,3 +141,26 @@ def test_fp8_form_tracks_fp64_and_picks_the_same_orientation(run, built):
         assert (q8["theta"][i], q8["phi"][i], q8["omega"][i]) == (q["theta"][i], q["phi"][i], q["omega"][i])
         # the BF16 form's best candidate is among the FP8 form's best three
         assert any(np.allclose(c8[i, j, :3], cands[i, 0, :3]) for j in range(3))
+
+
+@pytest.mark.parametrize("precision", ["bf16", "fp8"])
+def test_proposal_form_picks_the_exhaustive_orientation(run, built, precision):
+    """coarse > 0: the coarse level's proposals and their fine neighbourhoods contain the
+    exhaustive contraction's best candidates on these particles, so the pick is the same."""
+    import cryoim_gb300 as ci
+    (p, vol, tmpl, timgs, imgs, parts, truth), q, cands, stats = run
+    with ci.Context(0, p) as ctx:
+        ctx.load_templates(timgs, tmpl)
+        ctx.set_reference_map(vol)
+        qp = parts.copy()
+        cp = ctx.contract_search(imgs, qp, origin_max=2.0, origin_step=0.5, topk=8, want_cands=True,
+                                 precision=precision, coarse=8)
+    for i in range(len(parts)):
+        assert (qp["theta"][i], qp["phi"][i], qp["omega"][i]) == (q["theta"][i], q["phi"][i], q["omega"][i])
+        # k distinct orientations, sorted by the contraction score
+        assert len({tuple(np.round(c[:3], 4)) for c in cp[i]}) == cp.shape[1]
+        assert np.all(np.diff(cp[i, :, 5]) <= 1e-6)
+        # the best FP64 CC among the candidates is no worse than the exhaustive BF16 form's;
+        # FP8 scores may place an orientation at a neighbouring 0.5 px origin
+        tol = 1e-4 if precision == "bf16" else 5e-3
+        assert cp[i, :, 6].max() > cands[i, :, 6].max() - tol, (i, cp[i, :, 6], cands[i, :, 6])
