@@ -289,16 +289,18 @@ struct Ctx {
     DBuf<int> topi_c, tileo_c, tileorig_c, kor_c, korig_c, gidx;
     DBuf<double> pnorm_c;
     DBuf<uint8_t> bgather;
-    DBuf<float> corigins, topv, kcc, kcand, kpr;
+    DBuf<float> corigins, topv, kcc, kcand;
     DBuf<int> topi, gerr, kor, korig;
     DBuf<double> pnorm, kcc64;
-    DBuf<float2> kalpha;
     int n_origin = 0;
     float orig_max = -1.0f, orig_step = -1.0f;
     DBuf<float> tilev, xcand, xpr;
     DBuf<int> tileo, tileorig;
     DBuf<float2> xalpha, sband;
     DBuf<int> xcount;
+    DBuf<double> kpart;
+    DBuf<GemmGroup> ggroups;
+    DBuf<int2> gseg;
     // view <-> grid slot (itheta * (2 Nphi + 1) + iphi + Nphi) maps for neighbours
     std::vector<int> view_slot, slot_view;
     int num_sms = 0;
@@ -316,15 +318,15 @@ struct Ctx {
         prbuf.release(); fft.release(); band.release(); ralpha.release(); best.release();
         flag.release(); sel.release(); acc.release(); samples.release(); vol.release();
         mapcube.release(); csamples.release(); bmat.release(); amat.release(); corigins.release();
-        topv.release(); kcc.release(); kcand.release(); kpr.release(); topi.release(); gerr.release();
-        kor.release(); korig.release(); pnorm.release(); kcc64.release(); kalpha.release();
+        topv.release(); kcc.release(); kcand.release(); topi.release(); gerr.release();
+        kor.release(); korig.release(); pnorm.release(); kcc64.release();
         tilev.release(); xcand.release(); xpr.release(); tileo.release(); tileorig.release();
         xalpha.release(); bmat8.release(); amat8.release(); mulA.release(); mulB.release();
         bandmax.release(); fexp.release();
         csamples_c.release(); bmat_c.release(); amat_c.release(); corigins_c.release(); topv_c.release();
         tilev_c.release(); kcc_c.release(); topi_c.release(); tileo_c.release(); tileorig_c.release();
         kor_c.release(); korig_c.release(); gidx.release(); pnorm_c.release(); bgather.release();
-        sband.release(); xcount.release();
+        sband.release(); xcount.release(); kpart.release(); ggroups.release(); gseg.release();
         if (pe0) cudaEventDestroy(pe0);
         if (pe1) cudaEventDestroy(pe1);
         if (own_stream && stream) cudaStreamDestroy(stream);
@@ -1017,29 +1019,34 @@ int contract_impl(Ctx* c, const float* imgs, bool on_device, cryoim_particle* pa
         c->orig_step = opts->origin_step;
     }
     const int O = c->n_origin, T = c->T, nx = c->p.fftsize;
-    const long nn = (long)nx * nx;
-    // particles per contraction launch: keep operand A (about 2400 rows) L2-resident
-    const int pb = std::max(1, std::min(c->batch, 2400 / std::max(O, 1)));
+    const long nn = (long)nx * nx, w2 = (long)c->bd.W * c->bd.W;
+    // Particles per pass (transform, rescoring: large grids, two host waits per pass) and
+    // per exhaustive contraction launch (operand A of about 2400 rows stays L2-resident
+    // while the sections stream).  The proposal form builds A for the whole pass: its
+    // grouped launch reads each particle's A against that particle's own few tiles.
+    const int PB = std::max(1, c->batch);
+    const int pb = std::max(1, std::min(PB, 2400 / std::max(O, 1)));
+    const int arows = kc > 0 ? PB : pb;
     const int ntiles = (int)((c->n_orient + gemm_tile_n() - 1) / gemm_tile_n());
-    if ((r = ensure_batch(c, pb))) return r;
-    if (f8 ? ((r = c->amat8.ensure((size_t)pb * O * c->cKpad8)) || (r = c->fexp.ensure(pb)))
-           : (r = c->amat.ensure((size_t)pb * O * c->cKpad)))
+    if ((r = ensure_batch(c, PB))) return r;
+    if (f8 ? ((r = c->amat8.ensure((size_t)arows * O * c->cKpad8)) || (r = c->fexp.ensure(PB)))
+           : (r = c->amat.ensure((size_t)arows * O * c->cKpad)))
         return r;
-    if ((r = c->topv.ensure((size_t)pb * O * ntiles)) || (r = c->topi.ensure((size_t)pb * O * ntiles))) return r;
-    if ((r = c->gerr.ensure(1)) || (r = c->pnorm.ensure(pb)) || (r = c->kor.ensure((size_t)pb * k)) ||
-        (r = c->korig.ensure((size_t)pb * k)) || (r = c->kcc.ensure((size_t)pb * k)) ||
-        (r = c->kcand.ensure((size_t)pb * k * 5)) || (r = c->kcc64.ensure((size_t)pb * k)) ||
-        (r = c->kpr.ensure((size_t)pb * k)))
+    if ((r = c->topv.ensure((size_t)arows * O * ntiles)) || (r = c->topi.ensure((size_t)arows * O * ntiles)))
         return r;
-    if (T > 0 && (r = c->kalpha.ensure((size_t)pb * k * T * 60))) return r;
+    if ((r = c->gerr.ensure(1)) || (r = c->pnorm.ensure(PB)) || (r = c->kor.ensure((size_t)PB * k)) ||
+        (r = c->korig.ensure((size_t)PB * k)) || (r = c->kcc.ensure((size_t)PB * k)) ||
+        (r = c->kcand.ensure((size_t)PB * k * 5)) || (r = c->kcc64.ensure((size_t)PB * k)) ||
+        (r = c->kpart.ensure((size_t)cc_fp64_scratch(k, PB))))
+        return r;
     // rescoring set: each selected orientation and its grid neighbours within nbr steps
     const int maxx = nbox * k;
     if ((r = c->tilev.ensure((size_t)pb * ntiles)) || (r = c->tileo.ensure((size_t)pb * ntiles)) ||
-        (r = c->tileorig.ensure((size_t)pb * ntiles)) || (r = c->xcand.ensure((size_t)pb * maxx * 5)) ||
-        (r = c->xpr.ensure((size_t)pb * maxx)))
+        (r = c->tileorig.ensure((size_t)pb * ntiles)) || (r = c->xcand.ensure((size_t)PB * maxx * 5)) ||
+        (r = c->xpr.ensure((size_t)PB * maxx)))
         return r;
-    if (T > 0 && ((r = c->xalpha.ensure((size_t)pb * maxx * T * 60)) ||
-                  (r = c->sband.ensure((size_t)pb * c->bd.W * c->bd.W)) || (r = c->xcount.ensure(pb))))
+    if (T > 0 && ((r = c->xalpha.ensure((size_t)PB * maxx * T * 60)) || (r = c->sband.ensure((size_t)PB * w2)) ||
+                  (r = c->xcount.ensure(PB))))
         return r;
     if (c->num_sms == 0) CK(cudaDeviceGetAttribute(&c->num_sms, cudaDevAttrMultiProcessorCount, c->device));
     std::vector<int> src(P);
@@ -1050,9 +1057,9 @@ int contract_impl(Ctx* c, const float* imgs, bool on_device, cryoim_particle* pa
             src[i] = cur;
         }
     }
-    std::vector<float> hpar(8 * pb), hcand((size_t)pb * k * 5), hcc((size_t)pb * k), hpr((size_t)pb * k);
-    std::vector<int> hor((size_t)pb * k), horig((size_t)pb * k);
-    std::vector<double> hcc64((size_t)pb * k);
+    std::vector<float> hpar(8 * PB), hcand((size_t)PB * k * 5), hcc((size_t)PB * k), hpr;
+    std::vector<int> hor((size_t)PB * k), horig((size_t)PB * k);
+    std::vector<double> hcc64((size_t)PB * k);
     std::vector<float> ohost(2 * (size_t)O);
     CK(cudaMemcpyAsync(ohost.data(), c->corigins.p, sizeof(float) * 2 * O, cudaMemcpyDeviceToHost, c->stream));
     cudaEvent_t g0 = nullptr, g1 = nullptr;
@@ -1060,8 +1067,9 @@ int contract_impl(Ctx* c, const float* imgs, bool on_device, cryoim_particle* pa
         CK(cudaEventCreate(&g0));
         CK(cudaEventCreate(&g1));
     }
-    for (int b0 = 0; b0 < P; b0 += pb) {
-        const int nb = std::min(pb, P - b0);
+    const long row_bytes = f8 ? (long)c->cKpad8 : 2L * c->cKpad;
+    for (int b0 = 0; b0 < P; b0 += PB) {
+        const int nb = std::min(PB, P - b0);
         const float* d_src;
         if (on_device) {
             d_src = imgs + b0 * nn;
@@ -1074,12 +1082,12 @@ int contract_impl(Ctx* c, const float* imgs, bool on_device, cryoim_particle* pa
         for (int i = 0; i < nb; ++i) {
             const cryoim_particle& q = parts[b0 + i];
             const cryoim_particle& s = parts[src[b0 + i]];
-            hpar[i] = q.x; hpar[pb + i] = q.y;
-            hpar[4 * pb + 3 * i] = s.df1; hpar[4 * pb + 3 * i + 1] = s.df2; hpar[4 * pb + 3 * i + 2] = s.astigang;
+            hpar[i] = q.x; hpar[PB + i] = q.y;
+            hpar[4 * PB + 3 * i] = s.df1; hpar[4 * PB + 3 * i + 1] = s.df2; hpar[4 * PB + 3 * i + 2] = s.astigang;
         }
         // mask at the input origin as ort_globesearch.f90:50 does; the transform stays unshifted
-        if ((r = transform_batch(c, d_src, nb, pb, hpar, 1, 0, false))) return r;
-        ParView pv = par_view(c, pb);
+        if ((r = transform_batch(c, d_src, nb, PB, hpar, 1, 0, false))) return r;
+        ParView pv = par_view(c, PB);
         const float* ctfp = nullptr;
         const float* tfc = c->tfcut0.p;
         long tfs = 0;
@@ -1093,13 +1101,18 @@ int contract_impl(Ctx* c, const float* imgs, bool on_device, cryoim_particle* pa
             }
         }
         launch_particle_norm(c->band.p, ctfp, c->bd, c->csamples.p, c->cS, nb, c->pnorm.p, c->stream);
-        if (f8)
-            launch_build_a8(c->band.p, ctfp, c->bd, c->csamples.p, c->cS, c->cKpad8, c->corigins.p, O,
-                            c->pnorm.p, c->mulA.p, c->fexp.p, nb, c->amat8.p, c->stream);
-        else
-            launch_build_a(c->band.p, ctfp, c->bd, c->csamples.p, c->cS, c->cKpad, c->corigins.p, O, c->pnorm.p,
-                           nb, c->amat.p, c->stream);
-        CK(cudaGetLastError());
+        // operand A rows (particle, origin) of particles [s0, s0 + ns) at row (s0 - a0) O
+        auto build_rows = [&](int s0, int ns, int a0) {
+            const float2* bb = c->band.p + (long)s0 * w2;
+            const float* cc = ctfp ? ctfp + (long)s0 * w2 : nullptr;
+            if (f8)
+                launch_build_a8(bb, cc, c->bd, c->csamples.p, c->cS, c->cKpad8, c->corigins.p, O, c->pnorm.p + s0,
+                                c->mulA.p, c->fexp.p + s0, ns, c->amat8.p + (size_t)(s0 - a0) * O * c->cKpad8,
+                                c->stream);
+            else
+                launch_build_a(bb, cc, c->bd, c->csamples.p, c->cS, c->cKpad, c->corigins.p, O, c->pnorm.p + s0, ns,
+                               c->amat.p + (size_t)(s0 - a0) * O * c->cKpad, c->stream);
+        };
         GemmArgmaxArgs g{};
         g.topv = c->topv.p;
         g.topi = c->topi.p;
@@ -1107,22 +1120,23 @@ int contract_impl(Ctx* c, const float* imgs, bool on_device, cryoim_particle* pa
         g.err = c->gerr.p;
         CK(cudaMemsetAsync(c->gerr.p, 0, sizeof(int), c->stream));
         std::vector<std::vector<int>> lists;
+        if (c->prof) CK(cudaEventRecord(g0, c->stream));
         if (kc > 0) {
             // proposal form: the coarse level names each particle's candidate orientations,
             // the fine contraction runs on their gathered sections only
-            if (c->prof) CK(cudaEventRecord(g0, c->stream));
             if ((r = coarse_lists(c, nb, ctfp, kc, nbf, lists))) return r;
-            const long row_bytes = f8 ? (long)c->cKpad8 : 2L * c->cKpad;
+            CK(cudaMemsetAsync(c->gerr.p, 0, sizeof(int), c->stream));
             const void* bsrc = f8 ? (const void*)c->bmat8.p : (const void*)c->bmat.p;
             const char* abase = f8 ? (const char*)c->amat8.p : (const char*)c->amat.p;
-            CK(cudaMemsetAsync(c->gerr.p, 0, sizeof(int), c->stream));
-            // particles in groups whose gathered sections stay under 4 GB: one gather per
-            // group, then per particle a contraction over its own rows and a selection of k
-            // distinct orientations, all queued without a host wait
+            build_rows(0, nb, 0);
+            CK(cudaGetLastError());
+            // particles in groups whose gathered sections stay under 8 GB: one gather and one
+            // grouped contraction (each particle's origin rows against its own sections) per
+            // group, then the k distinct best orientations of each particle
             for (int i0 = 0; i0 < nb;) {
                 int i1 = i0;
                 long rows = 0;
-                while (i1 < nb && (i1 == i0 || (rows + (long)lists[i1].size()) * row_bytes <= (4L << 30)))
+                while (i1 < nb && (i1 == i0 || (rows + (long)lists[i1].size()) * row_bytes <= (8L << 30)))
                     rows += (long)lists[i1++].size();
                 std::vector<int> idx;
                 idx.reserve(rows);
@@ -1130,40 +1144,55 @@ int contract_impl(Ctx* c, const float* imgs, bool on_device, cryoim_particle* pa
                 if ((r = c->gidx.ensure(rows)) || (r = c->bgather.ensure((size_t)rows * row_bytes))) return r;
                 CK(cudaMemcpyAsync(c->gidx.p, idx.data(), sizeof(int) * rows, cudaMemcpyHostToDevice, c->stream));
                 CK(launch_gather_rows(bsrc, row_bytes, c->gidx.p, (int)rows, c->bgather.p, c->stream));
+                std::vector<GemmGroup> hg(i1 - i0);
+                std::vector<int2> seg(i1 - i0);
                 long roff = 0, toff = 0;
                 for (int i = i0; i < i1; ++i) {
                     const int nl = (int)lists[i].size();
                     const int ntp = (nl + gemm_tile_n() - 1) / gemm_tile_n();
-                    GemmArgmaxArgs gi = g;
-                    gi.topv = c->topv.p + toff;
-                    gi.topi = c->topi.p + toff;
-                    CK(launch_gemm_argmax(abase + (size_t)i * O * row_bytes, c->bgather.p + roff * row_bytes, O, nl,
-                                          kpad, f8, gi, c->num_sms, c->stream));
-                    launch_select_distinct(gi.topv, gi.topi, O, ntp, k, c->kor.p + (size_t)i * k,
-                                           c->korig.p + (size_t)i * k, c->kcc.p + (size_t)i * k, c->stream);
-                    CK(cudaGetLastError());
+                    GemmGroup& q = hg[i - i0];
+                    q.a_row0 = i * O;
+                    q.m_valid = O;
+                    q.b_row0 = (int)roff;
+                    q.n_valid = nl;
+                    q.topv_off = (int)toff;
+                    seg[i - i0] = make_int2((int)toff, ntp);
                     roff += nl;
                     toff += (long)O * ntp;
                     if (c->prof) c->prof_gemm_flops += 2.0 * (double)O * (double)nl * (double)kpad;
                 }
+                if ((r = c->ggroups.ensure(i1 - i0)) || (r = c->gseg.ensure(i1 - i0))) return r;
+                CK(launch_gemm_argmax_grouped(abase, (long)nb * O, c->bgather.p, rows, kpad, f8, hg.data(), i1 - i0,
+                                              c->ggroups.p, g, c->num_sms, c->stream));
+                CK(cudaMemcpyAsync(c->gseg.p, seg.data(), sizeof(int2) * seg.size(), cudaMemcpyHostToDevice,
+                                   c->stream));
+                launch_select_distinct(c->topv.p, c->topi.p, O, c->gseg.p, i1 - i0, k, c->kor.p + (size_t)i0 * k,
+                                       c->korig.p + (size_t)i0 * k, c->kcc.p + (size_t)i0 * k, c->stream);
+                CK(cudaGetLastError());
                 // the gather buffer is reused by the next group
                 if (i1 < nb) CK(cudaStreamSynchronize(c->stream));
                 i0 = i1;
             }
-            if (c->prof) CK(cudaEventRecord(g1, c->stream));
         } else {
-            if (c->prof) CK(cudaEventRecord(g0, c->stream));
-            if (f8)
-                CK(launch_gemm_argmax(c->amat8.p, c->bmat8.p, nb * O, (int)c->n_orient, kpad, true, g, c->num_sms,
-                                      c->stream));
-            else
-                CK(launch_gemm_argmax(c->amat.p, c->bmat.p, nb * O, (int)c->n_orient, kpad, false, g, c->num_sms,
-                                      c->stream));
-            if (c->prof) CK(cudaEventRecord(g1, c->stream));
-            launch_select_topk(c->topv.p, c->topi.p, O, ntiles, k, nb, c->tilev.p, c->tileo.p, c->tileorig.p,
-                               c->kor.p, c->korig.p, c->kcc.p, c->stream);
-            CK(cudaGetLastError());
+            // exhaustive: sub-batches of pb particles against every section, queued back to back
+            for (int s0 = 0; s0 < nb; s0 += pb) {
+                const int ns = std::min(pb, nb - s0);
+                build_rows(s0, ns, s0);
+                CK(cudaGetLastError());
+                if (f8)
+                    CK(launch_gemm_argmax(c->amat8.p, c->bmat8.p, ns * O, (int)c->n_orient, kpad, true, g,
+                                          c->num_sms, c->stream));
+                else
+                    CK(launch_gemm_argmax(c->amat.p, c->bmat.p, ns * O, (int)c->n_orient, kpad, false, g,
+                                          c->num_sms, c->stream));
+                launch_select_topk(c->topv.p, c->topi.p, O, ntiles, k, ns, c->tilev.p, c->tileo.p, c->tileorig.p,
+                                   c->kor.p + (size_t)s0 * k, c->korig.p + (size_t)s0 * k,
+                                   c->kcc.p + (size_t)s0 * k, c->stream);
+                CK(cudaGetLastError());
+                if (c->prof) c->prof_gemm_flops += 2.0 * (double)ns * O * (double)c->n_orient * (double)kpad;
+            }
         }
+        if (c->prof) CK(cudaEventRecord(g1, c->stream));
         int gerr = 0;
         CK(cudaMemcpyAsync(&gerr, c->gerr.p, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
         CK(cudaMemcpyAsync(hor.data(), c->kor.p, sizeof(int) * nb * k, cudaMemcpyDeviceToHost, c->stream));
@@ -1183,7 +1212,6 @@ int contract_impl(Ctx* c, const float* imgs, bool on_device, cryoim_particle* pa
             CK(cudaEventElapsedTime(&ms, g0, g1));
             c->prof_gemm_ms += ms;
             c->prof_gemm_launches += 1;
-            if (kc == 0) c->prof_gemm_flops += 2.0 * (double)nb * O * (double)c->n_orient * (double)kpad;
         }
         // candidates (theta, phi, omega, x, y) of the selected (orientation, origin) pairs
         for (int i = 0; i < nb * k; ++i) {
@@ -1198,7 +1226,7 @@ int contract_impl(Ctx* c, const float* imgs, bool on_device, cryoim_particle* pa
         }
         CK(cudaMemcpyAsync(c->kcand.p, hcand.data(), sizeof(float) * nb * k * 5, cudaMemcpyHostToDevice,
                            c->stream));
-        launch_cc_fp64(c->mapcube.p, c->band.p, ctfp, c->bd, c->csamples.p, c->cS, c->kcand.p, k, nb,
+        launch_cc_fp64(c->mapcube.p, c->band.p, ctfp, c->bd, c->csamples.p, c->cS, c->kcand.p, k, nb, c->kpart.p,
                        c->kcc64.p, c->stream);
         // Phase-residual rescoring at the particle's own origin (ort_globesearch.f90 scores
         // every view at particle(i)%x, %y) over each selected orientation and its grid

@@ -230,18 +230,25 @@ __global__ void k_select_topk(float* __restrict__ v, const int* __restrict__ ori
     }
 }
 
-// Proposal form, one particle: the k best (origin row, column tile) maxima with
+// Proposal form, per particle: the k best (origin row, column tile) maxima with
 // distinct orientations.  v[o * ntiles + t] is the best CC of tile t at origin o and
 // col[...] its column in the gathered list; once a column is taken, every entry that
 // names it is retired, so the candidates are k distinct orientations, each at its best
 // origin.  Columns are remapped to orientations on the host.
-__global__ void k_select_distinct(float* __restrict__ v, const int* __restrict__ col, int O, int ntiles, int k,
-                                  int* __restrict__ out_col, int* __restrict__ out_origin,
-                                  float* __restrict__ out_cc) {
+// One block per particle of a group: seg[b] = (offset of its entries, its ntiles).
+__global__ void k_select_distinct(float* __restrict__ v0, const int* __restrict__ col0, int O,
+                                  const int2* __restrict__ seg, int k, int* __restrict__ out_col0,
+                                  int* __restrict__ out_origin0, float* __restrict__ out_cc0) {
     __shared__ float sv[32];
     __shared__ int si[32];
     __shared__ int taken;
-    const int cnt = O * ntiles;
+    const int2 sg = seg[blockIdx.x];
+    const int ntiles = sg.y, cnt = O * ntiles;
+    float* v = v0 + sg.x;
+    const int* col = col0 + sg.x;
+    int* out_col = out_col0 + (long)blockIdx.x * k;
+    int* out_origin = out_origin0 + (long)blockIdx.x * k;
+    float* out_cc = out_cc0 + (long)blockIdx.x * k;
     const int w = threadIdx.x >> 5, l = threadIdx.x & 31, nw = blockDim.x >> 5;
     for (int r = 0; r < k; ++r) {
         float bv = -3.0e38f;
@@ -285,12 +292,19 @@ __global__ void k_select_distinct(float* __restrict__ v, const int* __restrict__
 
 // FP64 rescoring of one (particle, candidate): the same CC with every product,
 // interpolation and sum in double precision.
+// FP64 rescoring, one (candidate, particle, sample chunk) per block: the three sums of
+// the CC (p.q, |p|^2, |q|^2) over samples [S*s/NS, S*(s+1)/NS).  The origin shift
+// exp(-i 2pi (sx hx + sy ky)/n) is separable, so each block tabulates the per-hx and
+// per-ky phasors in double once and multiplies them per sample.
+constexpr int CC_SPLIT = 4;
+
 __global__ void k_cc_fp64(const float2* __restrict__ cube, const float2* __restrict__ band,
                           const float* __restrict__ ctf, Band bd, const int2* __restrict__ samples, int S,
-                          const float* __restrict__ cand, int k, double* __restrict__ out) {
+                          const float* __restrict__ cand, int k, double* __restrict__ part) {
+    extern __shared__ double2 ctab[];  // [R + 1] per hx, then [2R + 1] per ky
     __shared__ double sh[32];
     __shared__ double rot[9];
-    const int c = blockIdx.x, p = blockIdx.y, W = bd.W, R = bd.max_r, C = 2 * R + 3, off = R + 1;
+    const int c = blockIdx.x, p = blockIdx.y, sp = blockIdx.z, W = bd.W, R = bd.max_r, C = 2 * R + 3, off = R + 1;
     const float* cd = cand + ((long)p * k + c) * 5;
     if (threadIdx.x == 0) {
         const double d2r = 3.14159265358979323846 / 180.0;
@@ -300,13 +314,23 @@ __global__ void k_cc_fp64(const float2* __restrict__ cube, const float2* __restr
         rot[3] = c2 * c3 * s1 + c1 * s3; rot[4] = -c2 * s1 * s3 + c1 * c3; rot[5] = s1 * s2;
         rot[6] = -c3 * s2;               rot[7] = s2 * s3;                 rot[8] = c2;
     }
+    const double h = (double)(bd.nx / 2), sx = cd[3] + h, sy = cd[4] + h;
+    const double tpn = 2.0 * 3.14159265358979323846 / (double)bd.nx;
+    double2* tx = ctab;
+    double2* ty = ctab + (R + 1);
+    for (int i = threadIdx.x; i < 3 * R + 2; i += blockDim.x) {
+        double th, sn, cs;
+        if (i <= R) th = tpn * (sx * (double)i);
+        else th = tpn * (sy * (double)(i - (R + 1) - R));
+        sincos(th, &sn, &cs);
+        ctab[i] = make_double2(cs, sn);
+    }
     __syncthreads();
     const float2* b = band + (long)p * W * W;
     const float* cb = ctf ? ctf + (long)p * W * W : nullptr;
-    const double h = (double)(bd.nx / 2), sx = cd[3] + h, sy = cd[4] + h;
-    const double tpn = 2.0 * 3.14159265358979323846 / (double)bd.nx;
     double dot = 0, na = 0, nb = 0;
-    for (int i = threadIdx.x; i < S; i += blockDim.x) {
+    const int i0 = (int)((long)S * sp / gridDim.z), i1 = (int)((long)S * (sp + 1) / gridDim.z);
+    for (int i = i0 + threadIdx.x; i < i1; i += blockDim.x) {
         const int2 hk = samples[i];
         const double x = rot[0] * hk.x + rot[1] * hk.y, y = rot[3] * hk.x + rot[4] * hk.y,
                      z = rot[6] * hk.x + rot[7] * hk.y;
@@ -323,8 +347,9 @@ __global__ void k_cc_fp64(const float2* __restrict__ cube, const float2* __restr
                     si += w * v.y;
                 }
         const int q = (hk.y + R) * W + (hk.x + R);
-        const double th = tpn * (sx * hk.x + sy * hk.y);
-        const double cs = cos(th), sn = sin(th);
+        // cos/sin of tpn (sx hx + sy ky) from the two tabulated phasors
+        const double2 ex = tx[hk.x], ey = ty[hk.y + R];
+        const double cs = ex.x * ey.x - ex.y * ey.y, sn = ex.y * ey.x + ex.x * ey.y;
         const double a2 = b[q].x * cs + b[q].y * sn, b2 = -b[q].x * sn + b[q].y * cs;
         const double cv = cb ? (double)cb[q] : 1.0;
         const double pr = a2 * cv, pi = -b2 * cv;
@@ -335,7 +360,25 @@ __global__ void k_cc_fp64(const float2* __restrict__ cube, const float2* __restr
     dot = block_sum_double(dot, sh);
     na = block_sum_double(na, sh);
     nb = block_sum_double(nb, sh);
-    if (threadIdx.x == 0) out[(long)p * k + c] = (na > 0 && nb > 0) ? dot / sqrt(na * nb) : 0.0;
+    if (threadIdx.x == 0) {
+        double* o = part + (((long)p * k + c) * gridDim.z + sp) * 3;
+        o[0] = dot;
+        o[1] = na;
+        o[2] = nb;
+    }
+}
+
+// CC of each (particle, candidate) from its chunks' sums, in chunk order.
+__global__ void k_cc_fp64_finish(const double* __restrict__ part, int n, int ns, double* __restrict__ out) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    double dot = 0, na = 0, nb = 0;
+    for (int s = 0; s < ns; ++s) {
+        dot += part[((long)i * ns + s) * 3];
+        na += part[((long)i * ns + s) * 3 + 1];
+        nb += part[((long)i * ns + s) * 3 + 2];
+    }
+    out[i] = (na > 0 && nb > 0) ? dot / sqrt(na * nb) : 0.0;
 }
 
 // ---- FP8-e4m3 operands ---------------------------------------------------------
@@ -572,15 +615,19 @@ void launch_select_topk(const float* topv, const int* topi, int O, int ntiles, i
     k_select_topk<<<B, 512, 0, st>>>(tile_v, tile_o, tile_orig, ntiles, k, orient, origin, cc);
 }
 
-void launch_select_distinct(float* topv, const int* topi, int O, int ntiles, int k, int* col, int* origin,
-                            float* cc, cudaStream_t st) {
-    k_select_distinct<<<1, 512, 0, st>>>(topv, topi, O, ntiles, k, col, origin, cc);
+void launch_select_distinct(float* topv, const int* topi, int O, const int2* seg, int B, int k, int* col,
+                            int* origin, float* cc, cudaStream_t st) {
+    k_select_distinct<<<B, 512, 0, st>>>(topv, topi, O, seg, k, col, origin, cc);
 }
 
+long cc_fp64_scratch(int k, int B) { return (long)k * B * CC_SPLIT * 3; }
+
 void launch_cc_fp64(const float2* cube, const float2* band, const float* ctf, Band bd, const int2* samples,
-                    int S, const float* cand, int k, int B, double* out, cudaStream_t st) {
-    dim3 g(k, B);
-    k_cc_fp64<<<g, 256, 0, st>>>(cube, band, ctf, bd, samples, S, cand, k, out);
+                    int S, const float* cand, int k, int B, double* scratch, double* out, cudaStream_t st) {
+    dim3 g(k, B, CC_SPLIT);
+    const size_t sm = sizeof(double2) * (3 * bd.max_r + 2);
+    k_cc_fp64<<<g, 256, sm, st>>>(cube, band, ctf, bd, samples, S, cand, k, scratch);
+    k_cc_fp64_finish<<<(k * B + 127) / 128, 128, 0, st>>>(scratch, k * B, CC_SPLIT, out);
 }
 
 }  // namespace cryoim

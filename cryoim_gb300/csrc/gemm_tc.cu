@@ -153,6 +153,38 @@ __device__ __forceinline__ void tmem_ld32(uint32_t taddr, float* v) {
     for (int i = 0; i < 32; ++i) v[i] = __uint_as_float(r[i]);
 }
 
+// Tile t of the launch -> its product, tile coordinates and operand rows.
+struct TileAt {
+    int mt, nt, a_row, b_row, m_valid, n_valid, n_tiles, topv_off;
+};
+__device__ __forceinline__ TileAt tile_at(const GemmArgmaxArgs& g, int t) {
+    TileAt r;
+    if (!g.groups) {
+        r.mt = t % g.m_tiles;
+        r.nt = t / g.m_tiles;
+        r.a_row = r.mt * GM;
+        r.b_row = r.nt * GN;
+        r.m_valid = g.m_valid;
+        r.n_valid = g.n_valid;
+        r.n_tiles = g.n_tiles;
+        r.topv_off = 0;
+        return r;
+    }
+    int q = 0;
+    while (q + 1 < g.ngroups && __ldg(&g.groups[q + 1].tile_start) <= t) ++q;
+    const GemmGroup* G = g.groups + q;
+    const int local = t - __ldg(&G->tile_start), mtiles = __ldg(&G->m_tiles);
+    r.mt = local % mtiles;
+    r.nt = local / mtiles;
+    r.a_row = __ldg(&G->a_row0) + r.mt * GM;
+    r.b_row = __ldg(&G->b_row0) + r.nt * GN;
+    r.m_valid = __ldg(&G->m_valid);
+    r.n_valid = __ldg(&G->n_valid);
+    r.n_tiles = __ldg(&G->n_tiles);
+    r.topv_off = __ldg(&G->topv_off);
+    return r;
+}
+
 // F8 = false: BF16 operands, 64 elements of K per stage; true: FP8-e4m3, 128 elements.
 template <bool F8>
 __global__ void __launch_bounds__(NTHREADS, 1)
@@ -191,7 +223,7 @@ __global__ void __launch_bounds__(NTHREADS, 1)
     __syncthreads();
     tc_fence_after();
     const uint32_t tmem = *tmem_slot;
-    const int total = g.m_tiles * g.n_tiles;
+    const int total = g.groups ? g.total_tiles : g.m_tiles * g.n_tiles;
 
     if (warp == 0) {
         if (lane == 0) {
@@ -202,12 +234,12 @@ __global__ void __launch_bounds__(NTHREADS, 1)
             for (int i = 0; i < NSTAGE; ++i) { used[i] = false; last_par[i] = 0; }
             bool ok = true;
             for (int t = blockIdx.x; t < total && ok; t += gridDim.x) {
-                const int mt = t % g.m_tiles, nt = t / g.m_tiles;
+                const TileAt ta = tile_at(g, t);
                 for (int kb = 0; kb < g.kblocks; ++kb) {
                     if (!mbar_wait(empty + s, ph ^ 1u, g.err, true)) { ok = false; break; }
                     mbar_expect_tx(full + s, STAGE_BYTES);
-                    tma_load_2d(sA + s * A_BYTES, &tmA, kb * GK, mt * GM, full + s);
-                    tma_load_2d(sB + s * B_BYTES, &tmB, kb * GK, nt * GN, full + s);
+                    tma_load_2d(sA + s * A_BYTES, &tmA, kb * GK, ta.a_row, full + s);
+                    tma_load_2d(sB + s * B_BYTES, &tmB, kb * GK, ta.b_row, full + s);
                     used[s] = true;
                     last_par[s] = ph;
                     if (++s == NSTAGE) { s = 0; ph ^= 1u; }
@@ -253,29 +285,29 @@ __global__ void __launch_bounds__(NTHREADS, 1)
             const uint32_t aph = (uint32_t)(lt >> 1) & 1u;
             if (!mbar_wait(accf + b, aph, g.err, true)) break;
             tc_fence_after();
-            const int mt = t % g.m_tiles, nt = t / g.m_tiles;
-            const long row = (long)mt * GM + row_in_tile;
+            const TileAt ta = tile_at(g, t);
+            const long row = (long)ta.mt * GM + row_in_tile;
             float best = -3.0e38f;
             int bi = -1;
             for (int c = 0; c < GN / 32; ++c) {
                 float v[32];
                 tmem_ld32(tmem + ((uint32_t)(32 * q) << 16) + (uint32_t)(b * GN + c * 32), v);
-                const int col0 = nt * GN + c * 32;
+                const int col0 = ta.nt * GN + c * 32;
 #pragma unroll
                 for (int j = 0; j < 32; ++j) {
                     const int col = col0 + j;
-                    if (col < g.n_valid && v[j] > best) { best = v[j]; bi = col; }
+                    if (col < ta.n_valid && v[j] > best) { best = v[j]; bi = col; }
                 }
-                if (g.cfull && row < g.m_valid) {
+                if (g.cfull && row < ta.m_valid) {
                     for (int j = 0; j < 32; ++j)
-                        if (col0 + j < g.n_valid) g.cfull[row * g.ldc + col0 + j] = v[j];
+                        if (col0 + j < ta.n_valid) g.cfull[row * g.ldc + col0 + j] = v[j];
                 }
             }
             tc_fence_before();
             mbar_arrive(acce + b);
-            if (row < g.m_valid) {
-                g.topv[row * g.n_tiles + nt] = best;
-                g.topi[row * g.n_tiles + nt] = bi;
+            if (row < ta.m_valid) {
+                g.topv[ta.topv_off + row * ta.n_tiles + ta.nt] = best;
+                g.topi[ta.topv_off + row * ta.n_tiles + ta.nt] = bi;
             }
         }
     }
@@ -341,6 +373,41 @@ cudaError_t launch_gemm_argmax(const void* a, const void* b, int M, int N, int K
     if (e != cudaSuccess) return e;
     int total = g.m_tiles * g.n_tiles;
     int grid = total < num_sms ? total : num_sms;
+    kern<<<grid, NTHREADS, SMEM_BYTES, st>>>(ta, tb, g);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_gemm_argmax_grouped(const void* a, long Mtot, const void* b, long Ntot, int K, bool f8,
+                                       GemmGroup* hg, int ngroups, GemmGroup* dg, const GemmArgmaxArgs& in,
+                                       int num_sms, cudaStream_t st) {
+    const int gk = f8 ? GKB : GKB / 2;
+    if (K % gk != 0 || Mtot < 1 || Ntot < 1 || ngroups < 1 || in.cfull) return cudaErrorInvalidValue;
+    if (((uintptr_t)a & 15) || ((uintptr_t)b & 15)) return cudaErrorInvalidValue;
+    long total = 0;
+    for (int i = 0; i < ngroups; ++i) {
+        GemmGroup& q = hg[i];
+        if (q.m_valid < 1 || q.n_valid < 1 || q.a_row0 < 0 || q.b_row0 < 0 ||
+            (long)q.a_row0 + q.m_valid > Mtot || (long)q.b_row0 + q.n_valid > Ntot)
+            return cudaErrorInvalidValue;
+        q.m_tiles = (q.m_valid + GM - 1) / GM;
+        q.n_tiles = (q.n_valid + GN - 1) / GN;
+        q.tile_start = (int)total;
+        total += (long)q.m_tiles * q.n_tiles;
+    }
+    if (total > (1L << 30)) return cudaErrorInvalidValue;
+    CUtensorMap ta, tb;
+    if (!make_map(&ta, a, Mtot, K, GM, f8) || !make_map(&tb, b, Ntot, K, GN, f8)) return cudaErrorInvalidValue;
+    cudaError_t e = cudaMemcpyAsync(dg, hg, sizeof(GemmGroup) * ngroups, cudaMemcpyHostToDevice, st);
+    if (e != cudaSuccess) return e;
+    GemmArgmaxArgs g = in;
+    g.groups = dg;
+    g.ngroups = ngroups;
+    g.total_tiles = (int)total;
+    g.kblocks = K / gk;
+    auto kern = f8 ? k_gemm_argmax<true> : k_gemm_argmax<false>;
+    e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM_BYTES);
+    if (e != cudaSuccess) return e;
+    const int grid = total < num_sms ? (int)total : num_sms;
     kern<<<grid, NTHREADS, SMEM_BYTES, st>>>(ta, tb, g);
     return cudaGetLastError();
 }

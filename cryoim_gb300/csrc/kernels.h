@@ -124,13 +124,21 @@ struct InsertArgs {
 cudaError_t launch_insert(const InsertArgs& a, int B, cudaStream_t st);
 
 // ---- gemm_tc.cu (tcgen05 BF16 contraction with fused per-tile argmax) --------
+// One independent product of a grouped launch: rows [a_row0, a_row0 + m_valid) of A
+// against rows [b_row0, b_row0 + n_valid) of B; its (row, tile) maxima go to
+// topv/topi + topv_off as [m_valid][n_tiles], columns counted from b_row0.
+struct GemmGroup {
+    int tile_start, m_tiles, a_row0, m_valid, b_row0, n_valid, n_tiles, topv_off;
+};
 struct GemmArgmaxArgs {
     int m_tiles, n_tiles, kblocks, m_valid, n_valid;  // set by the launcher
     float* topv;   // [M][n_tiles] max of each row over each 256-column tile
     int* topi;     // [M][n_tiles] its column
-    float* cfull;  // optional full C [M][ldc] (tests)
+    float* cfull;  // optional full C [M][ldc] (tests; not with groups)
     long ldc;
     int* err;      // set to 1 when a wait times out (zero it before the launch)
+    const GemmGroup* groups = nullptr;  // device array, or nullptr for one product
+    int ngroups = 0, total_tiles = 0;   // set by the grouped launcher
 };
 int gemm_tile_n();
 int gemm_tile_m();
@@ -140,6 +148,12 @@ cudaError_t launch_gemm_bf16_argmax(const void* a, const void* b, int M, int N, 
 // f8: both operands FP8-e4m3 bytes (K % 128 == 0), else BF16
 cudaError_t launch_gemm_argmax(const void* a, const void* b, int M, int N, int K, bool f8,
                                const GemmArgmaxArgs& g, int num_sms, cudaStream_t st);
+// Several products in one persistent launch (A: Mtot x K, B: Ntot x K).  hgroups
+// (host, a_row0/m_valid/b_row0/n_valid/topv_off filled) is completed and copied to
+// dgroups (device, ngroups entries) on st; the host array must stay alive until then.
+cudaError_t launch_gemm_argmax_grouped(const void* a, long Mtot, const void* b, long Ntot, int K, bool f8,
+                                       GemmGroup* hgroups, int ngroups, GemmGroup* dgroups,
+                                       const GemmArgmaxArgs& g, int num_sms, cudaStream_t st);
 
 // ---- contract.cu (operands of the contraction, selection, FP64 rescoring) ------
 // Fourier band cube of the reference map: (2R+3)^3 float2, frequencies -(R+1)..R+1.
@@ -164,12 +178,16 @@ void launch_select_topk(const float* topv, const int* topi, int O, int ntiles, i
                         float* tile_v, int* tile_o, int* tile_orig, int* orient, int* origin, float* cc,
                         cudaStream_t st);
 // cand: B x k x (theta, phi, omega, x, y); out: B x k FP64 cross-correlations
+// scratch: cc_fp64_scratch(k, B) doubles
+long cc_fp64_scratch(int k, int B);
 void launch_cc_fp64(const float2* cube, const float2* band, const float* ctf, Band bd, const int2* samples,
-                    int S, const float* cand, int k, int B, double* out, cudaStream_t st);
+                    int S, const float* cand, int k, int B, double* scratch, double* out, cudaStream_t st);
 
 // dst row r = src row idx[r] (row_bytes a multiple of 16), n rows
-void launch_select_distinct(float* topv, const int* topi, int O, int ntiles, int k, int* col, int* origin,
-                            float* cc, cudaStream_t st);
+// per particle b of B: the k best of its O x seg[b].y (value, column) entries at
+// topv/topi + seg[b].x with distinct columns -> col, origin, cc [B][k]
+void launch_select_distinct(float* topv, const int* topi, int O, const int2* seg, int B, int k, int* col,
+                            int* origin, float* cc, cudaStream_t st);
 cudaError_t launch_gather_rows(const void* src, long row_bytes, const int* idx, int n, void* dst, cudaStream_t st);
 // FP8-e4m3 operands (contract.cu): per-band max |B| (R+1 bands, float bits) over every
 // stride-th row; B8 = e4m3(B x mulB) with rows of Kpad8 bytes; A8 rows with mulA and the

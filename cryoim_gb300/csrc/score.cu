@@ -217,6 +217,10 @@ __global__ void __launch_bounds__(768, 1) k_pr_omega(PrOmegaArgs a, int nomp, Co
 // cal_crosslin_PR.f90:2-71 for the 11 candidates of each particle; the candidate
 // origin shift (img2d_FT_centshift.f90) is applied to each bilinear tap, which is the
 // same per-pixel arithmetic as shifting the whole transform first.
+// SHIFTED (the contraction's rescoring: every candidate at the particle's origin, band
+// pre-shifted) also takes the exhaustive scorer's arithmetic for the phase difference
+// (angle_between) and float Kahan sums per thread, so its values match k_pr_omega's.
+template <bool SHIFTED>
 __global__ void __launch_bounds__(512) k_pr_single(PrSingleArgs a, Consts K) {
     __shared__ double sh[2][32];
     __shared__ float sline[4][60];  // cos, sin of the particle line; cos, sin of the template line
@@ -229,12 +233,13 @@ __global__ void __launch_bounds__(512) k_pr_single(PrSingleArgs a, Consts K) {
     const float xs = __fadd_rn(cd[3], nxh), ys = __fadd_rn(cd[4], nxh);
     const int offW = bd.off * W + bd.off;
     const float2* pb = a.band + (long)p * W * W;
-    const float2* sb = a.sband ? a.sband + (long)p * W * W : nullptr;
+    const float2* sb = SHIFTED ? a.sband + (long)p * W * W : nullptr;
     const float* ctfp = a.ctf ? a.ctf + (long)p * W * W : nullptr;
     const float* fc0 = a.fcut0 + (long)p * nr;
     const float* tfc = a.tfcut + (long)p * a.tfcut_pstride;
     const float twopi = __fmul_rn(2.0f, K.pi);
     double p1 = 0.0, p2 = 0.0;
+    float f1 = 0.f, f2 = 0.f, k1 = 0.f, k2 = 0.f;
     for (int i = 0; i < a.T; ++i) {
         const float2* al = a.alpha + (((long)p * a.ncand + c) * a.T + i) * 60;
         const float2* tb = a.tband + (long)i * W * W;
@@ -263,7 +268,7 @@ __global__ void __launch_bounds__(512) k_pr_single(PrSingleArgs a, Consts K) {
             int lx = (int)x, ly = (int)y;
             float ax = __fsub_rn(x, (float)lx), ay = __fsub_rn(y, (float)ly);
             float tr[4], ti[4];
-            if (sb) {
+            if (SHIFTED) {
 #pragma unroll
                 for (int u = 0; u < 4; ++u) {
                     const float2 vv = sb[(ly + (u >> 1)) * W + lx + (u & 1) - offW];
@@ -292,14 +297,25 @@ __global__ void __launch_bounds__(512) k_pr_single(PrSingleArgs a, Consts K) {
             float amp1 = sqrtf(re1 * re1 + im1 * im1);
             float amp2 = sqrtf(re2 * re2 + im2 * im2);
             if (amp1 >= fc0[iq] && amp2 >= fct[iq]) {
-                float ph1 = atan2f(im1, re1), ph2 = atan2f(im2, re2);
-                float d = fabsf(ph2 - ph1);
-                d = fminf(d, K.tpi - d);
-                float w = 0.5f * (amp1 + amp2);
-                p1 += (double)(d * w);
-                p2 += (double)w;
+                if (SHIFTED) {
+                    const float d = angle_between(re1 * im2 - im1 * re2, re1 * re2 + im1 * im2, K.pi);
+                    const float w = 0.5f * (amp1 + amp2);
+                    kahan_add(f1, k1, d * w);
+                    kahan_add(f2, k2, w);
+                } else {
+                    float ph1 = atan2f(im1, re1), ph2 = atan2f(im2, re2);
+                    float d = fabsf(ph2 - ph1);
+                    d = fminf(d, K.tpi - d);
+                    float w = 0.5f * (amp1 + amp2);
+                    p1 += (double)(d * w);
+                    p2 += (double)w;
+                }
             }
         }
+    }
+    if (SHIFTED) {
+        p1 = (double)f1;
+        p2 = (double)f2;
     }
     for (int o = 16; o > 0; o >>= 1) {
         p1 += __shfl_xor_sync(0xffffffffu, p1, o);
@@ -444,7 +460,10 @@ cudaError_t launch_shift_band(const float2* band, const float* cand, int ncand, 
 
 cudaError_t launch_pr_single(const PrSingleArgs& a, int B, cudaStream_t st) {
     dim3 grid(a.ncand, B);
-    k_pr_single<<<grid, 512, 0, st>>>(a, consts());
+    if (a.sband)
+        k_pr_single<true><<<grid, 512, 0, st>>>(a, consts());
+    else
+        k_pr_single<false><<<grid, 512, 0, st>>>(a, consts());
     return cudaGetLastError();
 }
 
