@@ -152,18 +152,19 @@ class Context:
     def contract_search(self, imgs, parts: np.ndarray, origin_max: float = 6.0,
                         origin_step: float = 0.5, topk: int = 16, pick: int = 0,
                         want_cands: bool = False, precision: str = "bf16", nbr: int = 1,
-                        coarse: int = 0):
+                        coarse: int = 0, learned: int = 0):
         """Tensor-core cross-correlation search with FP64 / phase-residual rescoring of
         the top-k and their grid neighbours within nbr steps; parts is updated in place.
         precision: "bf16" or "fp8" (e4m3 operands with per-band scales); coarse > 0: the
         proposal form (a coarse contraction names `coarse` orientations per particle,
-        only their fine neighbourhoods are correlated).  Returns (P, topk, 8) candidates
+        only their fine neighbourhoods are correlated); learned > 0: the same with the
+        trained proposer's `learned` cells (learn_train / learn_load first).  Returns (P, topk, 8) candidates
         if asked: theta, phi, omega, x, y, CC (contraction), CC (FP64), PR."""
         assert parts.dtype == PARTICLE_DTYPE and parts.flags["C_CONTIGUOUS"]
         if precision not in ("bf16", "fp8"):
             raise ValueError("precision must be 'bf16' or 'fp8'")
         o = _abi.ContractOpts(float(origin_max), float(origin_step), int(topk), int(pick),
-                              int(precision == "fp8"), int(nbr), int(coarse))
+                              int(precision == "fp8"), int(nbr), int(coarse), int(learned))
         out = np.zeros((len(parts), topk, 8), np.float32) if want_cands else None
         if isinstance(imgs, int):
             call("cryoim_contract_search_device", self._h, C.c_void_p(imgs), ptr(parts), len(parts),
@@ -171,6 +172,66 @@ class Context:
         else:
             im = np.ascontiguousarray(imgs, dtype=np.float32)
             call("cryoim_contract_search", self._h, ptr(im), ptr(parts), len(parts), C.byref(o), ptr(out))
+        return out
+
+    # -- learned orientation proposer ------------------------------------------
+    def learn_train(self, map3d: np.ndarray, **opts) -> dict:
+        """Trains the proposer on projections of map3d rendered by the library (keys of
+        cryoim_learn_opts: samples, batch, seed, lr, snr, df_min, df_max, astig_max,
+        origin_max).  Returns the mean loss of the last tenth of the steps, the time,
+        the angle sign and the number of views."""
+        o = _abi.LearnOpts()
+        call("cryoim_learn_opts_default", C.byref(o))
+        for k, v in opts.items():
+            if not hasattr(o, k):
+                raise KeyError(k)
+            setattr(o, k, v)
+        m = np.ascontiguousarray(map3d, dtype=np.float32)
+        st = (C.c_float * 4)()
+        call("cryoim_learn_train", self._h, ptr(m), C.byref(o), st)
+        return {"loss": st[0], "seconds": st[1], "sign": int(st[2]), "views": int(st[3])}
+
+    def learn_save(self, path: str) -> None:
+        call("cryoim_learn_save", self._h, str(path).encode())
+
+    def learn_load(self, path: str) -> None:
+        call("cryoim_learn_load", self._h, str(path).encode())
+
+    def learn_params(self, set_to: np.ndarray | None = None) -> np.ndarray:
+        n = C.c_int64()
+        call("cryoim_learn_params", self._h, None, None, C.byref(n))
+        out = np.zeros(n.value, np.float32)
+        s = None if set_to is None else np.ascontiguousarray(set_to, np.float32)
+        if s is not None and s.size != n.value:
+            raise ValueError(f"expected {n.value} parameters")
+        call("cryoim_learn_params", self._h, ptr(out), ptr(s), C.byref(n))
+        return out
+
+    def learn_forward(self, feat: np.ndarray, truth: np.ndarray | None = None, views: int = 0):
+        """Scores (B, views, 128); with truth (B, 4) also the loss (B,) and the
+        parameter gradients."""
+        f = np.ascontiguousarray(feat, np.float32)
+        B = f.shape[0]
+        nparam = self.learn_params().size
+        sc = np.zeros((B, views, 128), np.float32) if views else None
+        loss = np.zeros(B, np.float32) if truth is not None else None
+        gr = np.zeros(nparam, np.float32) if truth is not None else None
+        t = None if truth is None else np.ascontiguousarray(truth, np.float32)
+        call("cryoim_learn_forward", self._h, ptr(f), ptr(t), B, ptr(sc), ptr(loss), ptr(gr))
+        return sc, loss, gr
+
+    def learn_views(self) -> np.ndarray:
+        """(V, 2) theta, phi of the proposer's view classes."""
+        n = C.c_int32()
+        call("cryoim_learn_views", self._h, None, C.byref(n))
+        out = np.zeros((n.value, 2), np.float32)
+        call("cryoim_learn_views", self._h, ptr(out), C.byref(n))
+        return out
+
+    def learn_features(self, imgs: np.ndarray, parts: np.ndarray) -> np.ndarray:
+        im = np.ascontiguousarray(imgs, np.float32)
+        out = np.zeros((len(parts), 64, 128), np.float32)
+        call("cryoim_learn_features", self._h, ptr(im), ptr(parts), len(parts), ptr(out))
         return out
 
     def contract_stats(self) -> dict:

@@ -63,7 +63,14 @@ class Params(C.Structure):
 class ContractOpts(C.Structure):
     """cryoim_contract_opts (include/cryoim.h)."""
     _fields_ = [("origin_max", C.c_float), ("origin_step", C.c_float), ("topk", C.c_int32),
-                ("pick", C.c_int32), ("precision", C.c_int32), ("nbr", C.c_int32), ("coarse", C.c_int32)]
+                ("pick", C.c_int32), ("precision", C.c_int32), ("nbr", C.c_int32), ("coarse", C.c_int32),
+                ("learned", C.c_int32)]
+
+
+class LearnOpts(C.Structure):
+    """cryoim_learn_opts (include/cryoim.h)."""
+    _fields_ = [("samples", C.c_int32), ("batch", C.c_int32), ("seed", C.c_int32)] + \
+               [(n, C.c_float) for n in ("lr", "snr", "df_min", "df_max", "astig_max", "origin_max")]
 
 
 _vp, _fp, _ip, _i32, _f32 = C.c_void_p, C.POINTER(C.c_float), C.POINTER(C.c_int32), C.c_int32, C.c_float
@@ -130,6 +137,14 @@ SIGNATURES = {
     "cryoim_local_refine": [_vp, _vp, _vp, _vp, _vp, _i32],
     "cryoim_local_ort_read": [C.c_char_p, _i32, _i32, _vp, _vp, _i32],
     "cryoim_local_ort_write": [C.c_char_p, _vp, _vp, _i32, _i32, _i32, _i32],
+    "cryoim_learn_opts_default": [_vp],
+    "cryoim_learn_train": [_vp, _vp, _vp, _fp],
+    "cryoim_learn_save": [_vp, C.c_char_p],
+    "cryoim_learn_load": [_vp, C.c_char_p],
+    "cryoim_learn_params": [_vp, _vp, _vp, C.POINTER(C.c_int64)],
+    "cryoim_learn_forward": [_vp, _vp, _vp, _i32, _vp, _vp, _vp],
+    "cryoim_learn_features": [_vp, _vp, _vp, _i32, _vp],
+    "cryoim_learn_views": [_vp, _vp, _ip],
     "cryoim_central_sections": [_vp, _vp, _vp, _vp, _i32, _vp, _vp],
     "cryoim_icos_ops": [_vp],
     "cryoim_asu_fold": [_fp, _fp, _fp],

@@ -10,6 +10,7 @@ include/cryoim.h carries no torch types).  Translation units:
 * mapops.cu -- -fmad=false: real-space icosahedral average, merge output step;
 * center.cu -- -fmad=false: origin centring of icosprocess mode 3;
 * local.cu -- -fmad=false: local_refine's sub-particle refinement;
+* learn.cu -- the learned orientation proposer (features, CNN forward / backward, Adam);
 * io.cpp, local_host.cpp -- host only (g++): MRC / orientation / tnf files, local_box
   geometry and local_refine parameters.
 """
@@ -55,6 +56,7 @@ UNITS = {
     "mapops.cu": ["-fmad=false"],
     "center.cu": ["-fmad=false"],
     "local.cu": ["-fmad=false"],
+    "learn.cu": [],
 }
 
 

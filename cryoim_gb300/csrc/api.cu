@@ -8,11 +8,13 @@
 #include <cufft.h>
 
 #include <algorithm>
+#include <chrono>
 #include <cmath>
 #include <cstdarg>
 #include <cstdio>
 #include <cstring>
 #include <map>
+#include <random>
 #include <string>
 #include <vector>
 
@@ -214,6 +216,30 @@ static void build_view_grid(float step, ViewGrid* g) {
     }
 }
 
+// The learned proposer's weights, Adam state and activations (learn.cu has the layers).
+struct LearnModel {
+    bool ready = false;
+    int V = 0;          // classes: views of the twice-the-step grid
+    int sign = 1;       // +1: an in-plane rotation by w shifts the features by +w
+    float step = 0.0f;  // search step the view grid belongs to
+    long nparam = 0;
+    long oW[5] = {0}, ob[5] = {0}, oT = 0;  // parameter offsets (conv 1-4, mix)
+    int steps = 0;      // Adam steps taken
+    int cap = 0, capV = 0;  // batch capacity of the activations, views they were sized for
+    DBuf<float> w, gr, m, v, vview, wflip;
+    DBuf<float> feat, a1, a2, p2, a3, p3, a4, p4, g, sc, dsc, dg, dp4, da4, dp3, da3, dp2, da2, da1, loss, truth;
+    DBuf<int> cell;
+    DBuf<float> cellv;
+    void release() {
+        for (DBuf<float>* b : {&w, &gr, &m, &v, &vview, &wflip, &feat, &a1, &a2, &p2, &a3, &p3, &a4, &p4, &g, &sc,
+                               &dsc, &dg, &dp4, &da4, &dp3, &da3, &dp2, &da2, &da1, &loss, &truth, &cellv})
+            b->release();
+        cell.release();
+        ready = false;
+        cap = 0;
+    }
+};
+
 struct Ctx {
     int device = 0;
     cudaStream_t stream = nullptr;
@@ -301,6 +327,7 @@ struct Ctx {
     DBuf<double> kpart;
     DBuf<GemmGroup> ggroups;
     DBuf<int2> gseg;
+    LearnModel lm;
     // view <-> grid slot (itheta * (2 Nphi + 1) + iphi + Nphi) maps for neighbours
     std::vector<int> view_slot, slot_view;
     int num_sms = 0;
@@ -327,6 +354,7 @@ struct Ctx {
         tilev_c.release(); kcc_c.release(); topi_c.release(); tileo_c.release(); tileorig_c.release();
         kor_c.release(); korig_c.release(); gidx.release(); pnorm_c.release(); bgather.release();
         sband.release(); xcount.release(); kpart.release(); ggroups.release(); gseg.release();
+        lm.release();
         if (pe0) cudaEventDestroy(pe0);
         if (pe1) cudaEventDestroy(pe1);
         if (own_stream && stream) cudaStreamDestroy(stream);
@@ -462,7 +490,7 @@ int ensure_grid(Ctx* c) {
     if ((r = c->d_views.ensure(c->views.size() + 4))) return r;
     CK(cudaMemcpyAsync(c->d_views.p, c->views.data(), sizeof(float) * c->views.size(),
                        cudaMemcpyHostToDevice, c->stream));
-    if (c->V > 0) {
+    if (c->V > 0 && c->T > 0) {  // common-line angles of the phase-residual search
         std::vector<float> v2(2 * c->V);
         for (int v = 0; v < c->V; ++v) { v2[2 * v] = c->views[4 * v]; v2[2 * v + 1] = c->views[4 * v + 1]; }
         DBuf<float> tmp;
@@ -926,6 +954,344 @@ int coarse_lists(Ctx* c, int nb, const float* ctfp, int kc, int nbf, std::vector
     return CRYOIM_OK;
 }
 
+// ---- learned orientation proposer: host side -------------------------------------
+constexpr int LP_CIN[4] = {1, LP_C1, LP_C2, LP_C3}, LP_COUT[4] = {LP_C1, LP_C2, LP_C3, LP_C4};
+
+int ensure_cgrid(Ctx* c) {
+    if (c->cgrid.V > 0 && c->cgrid.step == 2.0f * c->p.searchstep) return CRYOIM_OK;
+    build_view_grid(2.0f * c->p.searchstep, &c->cgrid);
+    if (c->cgrid.V < 1) return fail(CRYOIM_ERR_SIZE, "coarse view grid is empty");
+    return CRYOIM_OK;
+}
+
+// parameter layout and view vectors for V views; weights not initialised
+int learn_layout(Ctx* c, int V) {
+    LearnModel& L = c->lm;
+    long off = 0;
+    for (int l = 0; l < 4; ++l) {
+        L.oW[l] = off;
+        off += (long)LP_COUT[l] * LP_CIN[l] * 9;
+        L.ob[l] = off;
+        off += LP_COUT[l];
+    }
+    L.oW[4] = off;
+    off += (long)LP_CM * LP_MIXK;
+    L.ob[4] = off;
+    off += LP_CM;
+    L.oT = off;
+    off += (long)V * LP_CM * LP_NT;
+    L.nparam = off;
+    L.V = V;
+    int r;
+    if ((r = L.w.ensure(off)) || (r = L.gr.ensure(off)) || (r = L.m.ensure(off)) || (r = L.v.ensure(off)) ||
+        (r = L.vview.ensure(3 * (size_t)V)) || (r = L.wflip.ensure((size_t)LP_C2 * LP_C3 * 9)))
+        return r;
+    std::vector<float> vv(3 * (size_t)V);
+    const float d2r = host_angles().deg2rad;
+    for (int i = 0; i < V; ++i) {
+        const float th = c->cgrid.views[4 * i] * d2r, ph = c->cgrid.views[4 * i + 1] * d2r;
+        vv[3 * i] = sinf(th) * cosf(ph);
+        vv[3 * i + 1] = sinf(th) * sinf(ph);
+        vv[3 * i + 2] = cosf(th);
+    }
+    CK(cudaMemcpyAsync(L.vview.p, vv.data(), sizeof(float) * vv.size(), cudaMemcpyHostToDevice, c->stream));
+    return CRYOIM_OK;
+}
+
+int learn_activations(Ctx* c, int B) {
+    LearnModel& L = c->lm;
+    if (B <= L.cap && L.V == L.capV) return CRYOIM_OK;
+    B = std::max(B, L.cap);
+    const size_t b = (size_t)B, P = LP_NT;
+    int r;
+    if ((r = L.feat.ensure(b * LP_NR * P)) || (r = L.a1.ensure(b * LP_C1 * LP_NR * P)) ||
+        (r = L.a2.ensure(b * LP_C2 * LP_NR * P)) || (r = L.p2.ensure(b * LP_C2 * (LP_NR / 2) * P)) ||
+        (r = L.a3.ensure(b * LP_C3 * (LP_NR / 2) * P)) || (r = L.p3.ensure(b * LP_C3 * (LP_NR / 4) * P)) ||
+        (r = L.a4.ensure(b * LP_C4 * (LP_NR / 4) * P)) || (r = L.p4.ensure(b * LP_MIXK * P)) ||
+        (r = L.g.ensure(b * LP_CM * P)) || (r = L.sc.ensure(b * L.V * P)) || (r = L.dsc.ensure(b * L.V * P)) ||
+        (r = L.dg.ensure(b * LP_CM * P)) || (r = L.dp4.ensure(b * LP_MIXK * P)) ||
+        (r = L.da4.ensure(b * LP_C4 * (LP_NR / 4) * P)) || (r = L.dp3.ensure(b * LP_C3 * (LP_NR / 4) * P)) ||
+        (r = L.da3.ensure(b * LP_C3 * (LP_NR / 2) * P)) || (r = L.dp2.ensure(b * LP_C2 * (LP_NR / 2) * P)) ||
+        (r = L.da2.ensure(b * LP_C2 * LP_NR * P)) || (r = L.da1.ensure(b * LP_C1 * LP_NR * P)) ||
+        (r = L.loss.ensure(b)) || (r = L.truth.ensure(4 * b)) || (r = L.cell.ensure(b * 64)) ||
+        (r = L.cellv.ensure(b * 64)))
+        return r;
+    L.cap = B;
+    L.capV = L.V;
+    return CRYOIM_OK;
+}
+
+// scores L.sc [B][V][NT] of the features in L.feat
+int learn_forward(Ctx* c, int B) {
+    LearnModel& L = c->lm;
+    const float* w = L.w.p;
+    cudaStream_t st = c->stream;
+    CK(launch_lp_conv3(L.feat.p, B, 1, LP_NR, w + L.oW[0], w + L.ob[0], LP_C1, true, L.a1.p, st));
+    CK(launch_lp_conv3(L.a1.p, B, LP_C1, LP_NR, w + L.oW[1], w + L.ob[1], LP_C2, true, L.a2.p, st));
+    launch_lp_pool(L.a2.p, B, LP_C2, LP_NR / 2, L.p2.p, st);
+    CK(launch_lp_conv3(L.p2.p, B, LP_C2, LP_NR / 2, w + L.oW[2], w + L.ob[2], LP_C3, true, L.a3.p, st));
+    launch_lp_pool(L.a3.p, B, LP_C3, LP_NR / 4, L.p3.p, st);
+    CK(launch_lp_conv3(L.p3.p, B, LP_C3, LP_NR / 4, w + L.oW[3], w + L.ob[3], LP_C4, true, L.a4.p, st));
+    launch_lp_pool(L.a4.p, B, LP_C4, LP_NR / 8, L.p4.p, st);
+    launch_lp_mix(L.p4.p, B, w + L.oW[4], w + L.ob[4], L.g.p, st);
+    CK(launch_lp_head(L.g.p, w + L.oT, B, L.V, L.sc.p, st));
+    return CRYOIM_OK;
+}
+
+// loss (L.loss [B]) and parameter gradients (L.gr) of the last forward, targets in L.truth
+int learn_backward(Ctx* c, int B) {
+    LearnModel& L = c->lm;
+    const float* w = L.w.p;
+    float* gr = L.gr.p;
+    cudaStream_t st = c->stream;
+    const long nt = LP_NT;
+    CK(cudaMemsetAsync(gr, 0, sizeof(float) * L.nparam, st));
+    launch_lp_loss(L.sc.p, B, L.V, L.vview.p, L.truth.p, 2.0f * c->p.searchstep, 1.0f, L.dsc.p, L.loss.p, st);
+    launch_lp_head_grad(L.g.p, w + L.oT, L.dsc.p, B, L.V, L.dg.p, gr + L.oT, st);
+    launch_lp_mix_grad(L.p4.p, L.dg.p, B, w + L.oW[4], L.dp4.p, gr + L.oW[4], gr + L.ob[4], st);
+    // layer 4
+    launch_lp_pool_grad(L.dp4.p, B, LP_C4, LP_NR / 8, L.da4.p, st);
+    launch_lp_relu_grad(L.a4.p, L.da4.p, (long)B * LP_C4 * (LP_NR / 4) * nt, L.da4.p, st);
+    CK(launch_lp_conv3_wgrad(L.p3.p, L.da4.p, B, LP_C3, LP_NR / 4, LP_C4, gr + L.oW[3], gr + L.ob[3], st));
+    launch_lp_flip(w + L.oW[3], LP_C4, LP_C3, L.wflip.p, st);
+    CK(launch_lp_conv3(L.da4.p, B, LP_C4, LP_NR / 4, L.wflip.p, nullptr, LP_C3, false, L.dp3.p, st));
+    // layer 3
+    launch_lp_pool_grad(L.dp3.p, B, LP_C3, LP_NR / 4, L.da3.p, st);
+    launch_lp_relu_grad(L.a3.p, L.da3.p, (long)B * LP_C3 * (LP_NR / 2) * nt, L.da3.p, st);
+    CK(launch_lp_conv3_wgrad(L.p2.p, L.da3.p, B, LP_C2, LP_NR / 2, LP_C3, gr + L.oW[2], gr + L.ob[2], st));
+    launch_lp_flip(w + L.oW[2], LP_C3, LP_C2, L.wflip.p, st);
+    CK(launch_lp_conv3(L.da3.p, B, LP_C3, LP_NR / 2, L.wflip.p, nullptr, LP_C2, false, L.dp2.p, st));
+    // layer 2
+    launch_lp_pool_grad(L.dp2.p, B, LP_C2, LP_NR / 2, L.da2.p, st);
+    launch_lp_relu_grad(L.a2.p, L.da2.p, (long)B * LP_C2 * LP_NR * nt, L.da2.p, st);
+    CK(launch_lp_conv3_wgrad(L.a1.p, L.da2.p, B, LP_C1, LP_NR, LP_C2, gr + L.oW[1], gr + L.ob[1], st));
+    launch_lp_flip(w + L.oW[1], LP_C2, LP_C1, L.wflip.p, st);
+    CK(launch_lp_conv3(L.da2.p, B, LP_C2, LP_NR, L.wflip.p, nullptr, LP_C1, false, L.da1.p, st));
+    // layer 1
+    launch_lp_relu_grad(L.a1.p, L.da1.p, (long)B * LP_C1 * LP_NR * nt, L.da1.p, st);
+    CK(launch_lp_conv3_wgrad(L.feat.p, L.da1.p, B, 1, LP_NR, LP_C1, gr + L.oW[0], gr + L.ob[0], st));
+    return CRYOIM_OK;
+}
+
+// Haar-uniform rotation (unit quaternion) as ZYZ Euler angles in degrees
+template <class RNG> void random_euler(RNG& rng, float* e) {
+    std::normal_distribution<double> nd(0.0, 1.0);
+    double q[4], s = 0.0;
+    for (double& x : q) { x = nd(rng); s += x * x; }
+    s = 1.0 / std::sqrt(s);
+    const double w = q[0] * s, x = q[1] * s, y = q[2] * s, z = q[3] * s;
+    const double r02 = 2 * (x * z + y * w), r12 = 2 * (y * z - x * w), r20 = 2 * (x * z - y * w),
+                 r21 = 2 * (y * z + x * w), r22 = 1 - 2 * (x * x + y * y);
+    const double r2d = 180.0 / 3.14159265358979323846;
+    e[0] = (float)(std::acos(std::min(1.0, std::max(-1.0, r22))) * r2d);
+    e[1] = (float)(std::atan2(r12, r02) * r2d);
+    e[2] = (float)(std::atan2(r21, -r20) * r2d);
+}
+
+// Renders B particles into img (device, B x nx^2): projection of dmap at eul, CTF and
+// origin shift from par (if apply_ctf; otherwise the shift only), white noise at snr.
+int learn_render(Ctx* c, const float* dmap, const float* deul, const float* dpar, int B, float snr,
+                 unsigned long long seed, float* img, float2* ft, float* var) {
+    const int nx = c->p.fftsize;
+    launch_project(dmap, nx, deul, B, img, c->stream);
+    launch_lp_real_to_cplx(img, nx, B, ft, c->stream);
+    cufftHandle h;
+    int r;
+    if ((r = plan2d(c, B, &h))) return r;
+    CKF(cufftExecC2C(h, (cufftComplex*)ft, (cufftComplex*)ft, CUFFT_FORWARD));
+    launch_lp_ctf_shift(ft, nx, B, dpar, c->p.apix, c->p.apply_ctf ? c->p.vol : -1.0f, c->p.cs, c->p.ampwg,
+                        c->stream);
+    CKF(cufftExecC2C(h, (cufftComplex*)ft, (cufftComplex*)ft, CUFFT_INVERSE));
+    launch_lp_cplx_to_real(ft, nx, B, img, var, c->stream);
+    if (snr > 0.0f) launch_lp_add_noise(img, nx, B, var, snr, seed, c->stream);
+    CK(cudaGetLastError());
+    return CRYOIM_OK;
+}
+
+// mask at (x, y), transform, polar features of nb images on the device -> L.feat
+int learn_features_dev(Ctx* c, const float* d_img, int nb, const float* ox, const float* oy) {
+    std::vector<float> hpar(8 * (size_t)nb, 0.0f);
+    for (int i = 0; i < nb; ++i) { hpar[i] = ox[i]; hpar[nb + i] = oy[i]; }
+    int r;
+    if ((r = ensure_batch(c, nb))) return r;
+    if ((r = transform_batch(c, d_img, nb, nb, hpar, 1, 0, false))) return r;
+    launch_lp_features(c->band.p, c->bd, nb, c->lm.feat.p, c->stream);
+    CK(cudaGetLastError());
+    return CRYOIM_OK;
+}
+
+int learn_train_impl(Ctx* c, const float* map3d, const cryoim_learn_opts* o, float* stats) {
+    int r = check_ready(c, false);
+    if (r) return r;
+    if (!map3d || !o) return fail(CRYOIM_ERR_ARG, "null input");
+    if (o->batch < 8 || o->batch > 1024 || o->samples < o->batch || !(o->lr > 0) || o->snr < 0 ||
+        o->df_max < o->df_min || o->origin_max < 0 || o->astig_max < 0)
+        return fail(CRYOIM_ERR_ARG, "bad learn options");
+    const auto t0 = std::chrono::steady_clock::now();
+    if ((r = ensure_cgrid(c))) return r;
+    LearnModel& L = c->lm;
+    L.ready = false;
+    const int V = c->cgrid.V, B = o->batch, nx = c->p.fftsize;
+    const long nn = (long)nx * nx;
+    if ((r = learn_layout(c, V)) || (r = learn_activations(c, B))) return r;
+    // initial weights: He-normal convolutions, 1/sqrt(fan-in) mix, small templates
+    std::mt19937_64 rng((uint64_t)o->seed * 0x9E3779B97F4A7C15ull + 12345u);
+    {
+        std::vector<float> hw(L.nparam, 0.0f);
+        std::normal_distribution<float> nd(0.0f, 1.0f);
+        for (int l = 0; l < 4; ++l) {
+            const float sd = std::sqrt(2.0f / (9.0f * LP_CIN[l]));
+            for (long q = 0; q < (long)LP_COUT[l] * LP_CIN[l] * 9; ++q) hw[L.oW[l] + q] = sd * nd(rng);
+        }
+        for (long q = 0; q < (long)LP_CM * LP_MIXK; ++q) hw[L.oW[4] + q] = nd(rng) / std::sqrt((float)LP_MIXK);
+        for (long q = 0; q < (long)V * LP_CM * LP_NT; ++q) hw[L.oT + q] = 0.01f * nd(rng);
+        CK(cudaMemcpyAsync(L.w.p, hw.data(), sizeof(float) * L.nparam, cudaMemcpyHostToDevice, c->stream));
+        CK(cudaMemsetAsync(L.m.p, 0, sizeof(float) * L.nparam, c->stream));
+        CK(cudaMemsetAsync(L.v.p, 0, sizeof(float) * L.nparam, c->stream));
+        CK(cudaStreamSynchronize(c->stream));
+    }
+    L.steps = 0;
+    DBuf<float> dmap, img, deul, dpar, var;
+    DBuf<float2> ft;
+    if ((r = dmap.ensure(nn * nx)) || (r = img.ensure((size_t)B * nn)) || (r = ft.ensure((size_t)B * nn)) ||
+        (r = deul.ensure(3 * (size_t)B)) || (r = dpar.ensure(5 * (size_t)B)) || (r = var.ensure(B)))
+        return r;
+    CK(cudaMemcpyAsync(dmap.p, map3d, sizeof(float) * nn * nx, cudaMemcpyHostToDevice, c->stream));
+    // direction of the feature shift under an in-plane rotation: two clean projections
+    // 30 degrees apart, features, circular correlation
+    {
+        const float e2[6] = {80.0f, 5.0f, 0.0f, 80.0f, 5.0f, 30.0f};
+        const float p2[10] = {0, 0, 0, 0, 0, 0, 0, 0, 0, 0};
+        CK(cudaMemcpyAsync(deul.p, e2, sizeof(e2), cudaMemcpyHostToDevice, c->stream));
+        CK(cudaMemcpyAsync(dpar.p, p2, sizeof(p2), cudaMemcpyHostToDevice, c->stream));
+        launch_project(dmap.p, nx, deul.p, 2, img.p, c->stream);
+        const float z2[2] = {0.0f, 0.0f};
+        if ((r = learn_features_dev(c, img.p, 2, z2, z2))) return r;
+        std::vector<float> f(2 * LP_NR * LP_NT);
+        CK(cudaMemcpyAsync(f.data(), L.feat.p, sizeof(float) * f.size(), cudaMemcpyDeviceToHost, c->stream));
+        CK(cudaStreamSynchronize(c->stream));
+        int best = 0;
+        double bv = -1e300;
+        for (int s = 0; s < LP_NT; ++s) {
+            double acc = 0.0;
+            for (int ir = 0; ir < LP_NR; ++ir)
+                for (int t = 0; t < LP_NT; ++t)
+                    acc += (double)f[ir * LP_NT + t] * f[LP_NR * LP_NT + ir * LP_NT + (t + s) % LP_NT];
+            if (acc > bv) { bv = acc; best = s; }
+        }
+        // the best s has f1(t + s) ~ f0(t): a rotation by +30 degrees moves the features
+        // by +s bins; the head then peaks at shift sign * omega / (180 / NT)
+        const float dw = 180.0f / LP_NT;
+        const float sdeg = best * dw;
+        L.sign = std::fabs(sdeg - 30.0f) < std::fabs(sdeg - 150.0f) ? 1 : -1;
+    }
+    const int nsteps = o->samples / B;
+    std::uniform_real_distribution<float> U(0.0f, 1.0f);
+    std::vector<float> heul(3 * B), hpar(5 * B), htruth(4 * B), hox(B), hoy(B), hl(B);
+    const float* ops = table_ops();
+    const float d2r = host_angles().deg2rad, dw = 180.0f / LP_NT;
+    double tail = 0.0;
+    int ntail = 0;
+    for (int sidx = 0; sidx < nsteps; ++sidx) {
+        for (int b = 0; b < B; ++b) {
+            float e[3];
+            random_euler(rng, e);
+            heul[3 * b] = e[0]; heul[3 * b + 1] = e[1]; heul[3 * b + 2] = e[2];
+            const float df = o->df_min + (o->df_max - o->df_min) * U(rng);
+            const float da = o->astig_max * U(rng), ang = 180.0f * U(rng);
+            const float ox = o->origin_max * (2.0f * U(rng) - 1.0f), oy = o->origin_max * (2.0f * U(rng) - 1.0f);
+            hpar[5 * b] = df; hpar[5 * b + 1] = df + da; hpar[5 * b + 2] = ang; hpar[5 * b + 3] = ox;
+            hpar[5 * b + 4] = oy;
+            hox[b] = ox;
+            hoy[b] = oy;
+            float th = e[0], ph = e[1], om = e[2];
+            asu_fold(&th, &ph, &om, ops, d2r);
+            htruth[4 * b] = sinf(th * d2r) * cosf(ph * d2r);
+            htruth[4 * b + 1] = sinf(th * d2r) * sinf(ph * d2r);
+            htruth[4 * b + 2] = cosf(th * d2r);
+            float wv = std::fmod((float)L.sign * om, 180.0f);
+            if (wv < 0.0f) wv += 180.0f;
+            htruth[4 * b + 3] = (float)(((int)std::lround(wv / dw)) % LP_NT);
+        }
+        CK(cudaMemcpyAsync(deul.p, heul.data(), sizeof(float) * 3 * B, cudaMemcpyHostToDevice, c->stream));
+        CK(cudaMemcpyAsync(dpar.p, hpar.data(), sizeof(float) * 5 * B, cudaMemcpyHostToDevice, c->stream));
+        CK(cudaMemcpyAsync(L.truth.p, htruth.data(), sizeof(float) * 4 * B, cudaMemcpyHostToDevice, c->stream));
+        if ((r = learn_render(c, dmap.p, deul.p, dpar.p, B, o->snr,
+                              (unsigned long long)o->seed * 1000003ull + (unsigned long long)sidx, img.p, ft.p,
+                              var.p)))
+            return r;
+        if ((r = learn_features_dev(c, img.p, B, hox.data(), hoy.data()))) return r;
+        if ((r = learn_forward(c, B)) || (r = learn_backward(c, B))) return r;
+        launch_lp_adam(L.w.p, L.gr.p, L.m.p, L.v.p, L.nparam, o->lr, ++L.steps, c->stream);
+        CK(cudaGetLastError());
+        if (sidx >= nsteps - std::max(1, nsteps / 10)) {
+            CK(cudaMemcpyAsync(hl.data(), L.loss.p, sizeof(float) * B, cudaMemcpyDeviceToHost, c->stream));
+            CK(cudaStreamSynchronize(c->stream));
+            for (int b = 0; b < B; ++b) tail += hl[b];
+            ntail += B;
+        }
+        if ((r = check_flag(c))) return r;
+    }
+    CK(cudaStreamSynchronize(c->stream));
+    L.step = c->p.searchstep;
+    L.ready = true;
+    if (stats) {
+        stats[0] = ntail ? (float)(tail / ntail) : 0.0f;
+        stats[1] = (float)std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+        stats[2] = (float)L.sign;
+        stats[3] = (float)V;
+    }
+    return CRYOIM_OK;
+}
+
+// Proposals of the trained model for the nb particles whose band is in c->band: the
+// top kl cells, each as two fine-grid seeds (angle, angle + 180 degrees), expanded to
+// their fine neighbourhoods within nbf steps -> lists[i], sorted.
+int learned_lists(Ctx* c, int nb, int kl, int nbf, std::vector<std::vector<int>>& lists) {
+    LearnModel& L = c->lm;
+    int r;
+    if ((r = learn_activations(c, nb))) return r;
+    launch_lp_features(c->band.p, c->bd, nb, L.feat.p, c->stream);
+    if ((r = learn_forward(c, nb))) return r;
+    launch_lp_topk(L.sc.p, nb, L.V, kl, L.cell.p, L.cellv.p, c->stream);
+    CK(cudaGetLastError());
+    std::vector<int> cell((size_t)nb * kl);
+    CK(cudaMemcpyAsync(cell.data(), L.cell.p, sizeof(int) * cell.size(), cudaMemcpyDeviceToHost, c->stream));
+    CK(cudaStreamSynchronize(c->stream));
+    const ViewGrid& g = c->cgrid;
+    const int span_c = 2 * g.nph + 1, span = 2 * c->nph + 1;
+    const float dw = 180.0f / LP_NT, step = c->p.searchstep;
+    lists.assign(nb, std::vector<int>());
+    for (int i = 0; i < nb; ++i) {
+        std::vector<int>& lst = lists[i];
+        for (int j = 0; j < kl; ++j) {
+            const int q = cell[(size_t)i * kl + j];
+            if (q < 0) continue;
+            const int vc = q / LP_NT, s = q % LP_NT, slot = g.view_slot[vc];
+            const int it = 2 * (slot / span_c), ips = 2 * (slot % span_c - g.nph);
+            for (int half = 0; half < 2; ++half) {
+                float om = (float)L.sign * dw * (float)s + 180.0f * (float)half;
+                om = std::fmod(om, 360.0f);
+                if (om < 0.0f) om += 360.0f;
+                const int io = ((int)std::lround(om / step)) % c->nom;
+                for (int dt = -nbf; dt <= nbf; ++dt)
+                    for (int dp = -nbf; dp <= nbf; ++dp) {
+                        const int it2 = it + dt, ips2 = ips + dp;
+                        if (it2 < 0 || it2 > c->nth || ips2 < -c->nph || ips2 > c->nph) continue;
+                        const int v2 = c->slot_view[(size_t)it2 * span + ips2 + c->nph];
+                        if (v2 < 0) continue;
+                        for (int dwi = -nbf; dwi <= nbf; ++dwi)
+                            lst.push_back(v2 * c->nom + ((io + dwi) % c->nom + c->nom) % c->nom);
+                    }
+            }
+        }
+        std::sort(lst.begin(), lst.end());
+        lst.erase(std::unique(lst.begin(), lst.end()), lst.end());
+        if (lst.empty()) lst.push_back(0);
+    }
+    return CRYOIM_OK;
+}
+
 // FP8-e4m3 copy of operand B with per-band power-of-two scales (contract.cu explains the
 // scaling): band maxima of the BF16 rows (every 4th orientation), e_b = floor(log2(224 /
 // max_b)), mulB = 2^e_b and mulA = 2^-e_b per sample, then the conversion.
@@ -995,6 +1361,10 @@ int contract_impl(Ctx* c, const float* imgs, bool on_device, cryoim_particle* pa
     const int kc = opts->coarse;  // 0: exhaustive; else coarse proposals per particle
     const int nbf = 2;            // fine neighbourhood of a coarse proposal, in fine steps
     if (kc < 0 || kc > 64) return fail(CRYOIM_ERR_ARG, "coarse must be 0..64");
+    const int kl = opts->learned;  // 0: off; else learned proposals per particle
+    if (kl < 0 || kl > 64 || (kl > 0 && kc > 0)) return fail(CRYOIM_ERR_ARG, "learned must be 0..64, not with coarse");
+    if (kl > 0 && !(c->lm.ready && c->lm.step == c->p.searchstep && c->cgrid.V == c->lm.V))
+        return fail(CRYOIM_ERR_STATE, "no trained proposer for this search step (cryoim_learn_train / _load)");
     if (P == 0) return CRYOIM_OK;
     if ((r = f8 ? ensure_bmat8(c) : ensure_bmat(c))) return r;
     if (kc > 0 && (r = ensure_coarse(c, opts->origin_max, opts->origin_step))) return r;
@@ -1026,7 +1396,7 @@ int contract_impl(Ctx* c, const float* imgs, bool on_device, cryoim_particle* pa
     // grouped launch reads each particle's A against that particle's own few tiles.
     const int PB = std::max(1, c->batch);
     const int pb = std::max(1, std::min(PB, 2400 / std::max(O, 1)));
-    const int arows = kc > 0 ? PB : pb;
+    const int arows = (kc > 0 || kl > 0) ? PB : pb;
     const int ntiles = (int)((c->n_orient + gemm_tile_n() - 1) / gemm_tile_n());
     if ((r = ensure_batch(c, PB))) return r;
     if (f8 ? ((r = c->amat8.ensure((size_t)arows * O * c->cKpad8)) || (r = c->fexp.ensure(PB)))
@@ -1121,10 +1491,12 @@ int contract_impl(Ctx* c, const float* imgs, bool on_device, cryoim_particle* pa
         CK(cudaMemsetAsync(c->gerr.p, 0, sizeof(int), c->stream));
         std::vector<std::vector<int>> lists;
         if (c->prof) CK(cudaEventRecord(g0, c->stream));
-        if (kc > 0) {
-            // proposal form: the coarse level names each particle's candidate orientations,
-            // the fine contraction runs on their gathered sections only
-            if ((r = coarse_lists(c, nb, ctfp, kc, nbf, lists))) return r;
+        if (kc > 0 || kl > 0) {
+            // proposal forms: the coarse contraction or the learned proposer names each
+            // particle's candidate orientations, the fine contraction runs on their
+            // gathered sections only
+            if ((r = kc > 0 ? coarse_lists(c, nb, ctfp, kc, nbf, lists) : learned_lists(c, nb, kl, nbf, lists)))
+                return r;
             CK(cudaMemsetAsync(c->gerr.p, 0, sizeof(int), c->stream));
             const void* bsrc = f8 ? (const void*)c->bmat8.p : (const void*)c->bmat.p;
             const char* abase = f8 ? (const char*)c->amat8.p : (const char*)c->amat.p;
@@ -1204,7 +1576,7 @@ int contract_impl(Ctx* c, const float* imgs, bool on_device, cryoim_particle* pa
         if (gerr) return fail(CRYOIM_ERR_CUDA, "contraction pipeline wait timed out");
         if (f8)  // remove the per-particle exponent: the CC of the unit-norm rows
             for (int i = 0; i < nb * k; ++i) hcc[i] = std::ldexp(hcc[i], -hfe[i / k]);
-        if (kc > 0)  // gathered column -> fine orientation index
+        if (kc > 0 || kl > 0)  // gathered column -> fine orientation index
             for (int i = 0; i < nb * k; ++i)
                 if (hor[i] >= 0) hor[i] = lists[i / k][hor[i]];
         if (c->prof) {
@@ -2370,6 +2742,169 @@ int cryoim_contract_search(void* ctx, const float* imgs, cryoim_particle* parts,
 int cryoim_contract_search_device(void* ctx, const float* d_imgs, cryoim_particle* parts, int32_t P,
                                   const cryoim_contract_opts* opts, float* cands) {
     return contract_impl(as_ctx(ctx), d_imgs, true, parts, P, opts, cands);
+}
+
+int cryoim_learn_opts_default(cryoim_learn_opts* o) {
+    if (!o) return fail(CRYOIM_ERR_ARG, "null options");
+    o->samples = 200000;
+    o->batch = 256;
+    o->seed = 1;
+    o->lr = 2.0e-3f;
+    o->snr = 0.1f;
+    o->df_min = 1.0f;
+    o->df_max = 3.0f;
+    o->astig_max = 0.0f;
+    o->origin_max = 3.0f;
+    return CRYOIM_OK;
+}
+
+int cryoim_learn_train(void* ctx, const float* map3d, const cryoim_learn_opts* o, float* stats) {
+    return learn_train_impl(as_ctx(ctx), map3d, o, stats);
+}
+
+int cryoim_learn_save(void* ctx, const char* path) {
+    Ctx* c = as_ctx(ctx);
+    int r = check_ready(c, false);
+    if (r) return r;
+    if (!path) return fail(CRYOIM_ERR_ARG, "null path");
+    const LearnModel& L = c->lm;
+    if (!L.ready) return fail(CRYOIM_ERR_STATE, "no trained proposer");
+    std::vector<float> w(L.nparam);
+    CK(cudaMemcpyAsync(w.data(), L.w.p, sizeof(float) * L.nparam, cudaMemcpyDeviceToHost, c->stream));
+    CK(cudaStreamSynchronize(c->stream));
+    FILE* f = std::fopen(path, "wb");
+    if (!f) return fail(CRYOIM_ERR_IO, "cannot write %s", path);
+    const int32_t hdr[3] = {1, L.V, L.sign};
+    const int64_t np = L.nparam;
+    bool ok = std::fwrite("CRYOIMLP", 1, 8, f) == 8 && std::fwrite(hdr, 4, 3, f) == 3 &&
+              std::fwrite(&L.step, 4, 1, f) == 1 && std::fwrite(&np, 8, 1, f) == 1 &&
+              std::fwrite(w.data(), 4, w.size(), f) == w.size();
+    ok = (std::fclose(f) == 0) && ok;
+    return ok ? CRYOIM_OK : fail(CRYOIM_ERR_IO, "short write to %s", path);
+}
+
+int cryoim_learn_load(void* ctx, const char* path) {
+    Ctx* c = as_ctx(ctx);
+    int r = check_ready(c, false);
+    if (r) return r;
+    if (!path) return fail(CRYOIM_ERR_ARG, "null path");
+    FILE* f = std::fopen(path, "rb");
+    if (!f) return fail(CRYOIM_ERR_IO, "cannot read %s", path);
+    char magic[8];
+    int32_t hdr[3];
+    float step = 0.0f;
+    int64_t np = 0;
+    bool ok = std::fread(magic, 1, 8, f) == 8 && std::memcmp(magic, "CRYOIMLP", 8) == 0 &&
+              std::fread(hdr, 4, 3, f) == 3 && std::fread(&step, 4, 1, f) == 1 && std::fread(&np, 8, 1, f) == 1;
+    if (!ok || hdr[0] != 1) {
+        std::fclose(f);
+        return fail(CRYOIM_ERR_INPUT, "%s is not a proposer file", path);
+    }
+    if ((r = ensure_cgrid(c))) { std::fclose(f); return r; }
+    if (step != c->p.searchstep || hdr[1] != c->cgrid.V) {
+        std::fclose(f);
+        return fail(CRYOIM_ERR_MISMATCH, "%s was trained for step %g (%d views), not %g (%d views)", path,
+                    (double)step, hdr[1], (double)c->p.searchstep, c->cgrid.V);
+    }
+    LearnModel& L = c->lm;
+    if ((r = learn_layout(c, hdr[1]))) { std::fclose(f); return r; }
+    if (np != L.nparam) {
+        std::fclose(f);
+        return fail(CRYOIM_ERR_MISMATCH, "%s holds %lld parameters, expected %ld", path, (long long)np, L.nparam);
+    }
+    std::vector<float> w(np);
+    ok = std::fread(w.data(), 4, w.size(), f) == w.size();
+    std::fclose(f);
+    if (!ok) return fail(CRYOIM_ERR_IO, "short read from %s", path);
+    CK(cudaMemcpyAsync(L.w.p, w.data(), sizeof(float) * np, cudaMemcpyHostToDevice, c->stream));
+    CK(cudaStreamSynchronize(c->stream));
+    L.sign = hdr[2];
+    L.step = step;
+    L.steps = 0;
+    L.ready = true;
+    return CRYOIM_OK;
+}
+
+int cryoim_learn_params(void* ctx, float* get, const float* set, int64_t* n) {
+    Ctx* c = as_ctx(ctx);
+    int r = check_ready(c, false);
+    if (r) return r;
+    if ((r = ensure_cgrid(c))) return r;
+    LearnModel& L = c->lm;
+    if (L.nparam == 0 || L.V != c->cgrid.V) {
+        if ((r = learn_layout(c, c->cgrid.V))) return r;
+        CK(cudaMemsetAsync(L.w.p, 0, sizeof(float) * L.nparam, c->stream));
+        L.step = c->p.searchstep;
+    }
+    if (n) *n = L.nparam;
+    if (set) CK(cudaMemcpyAsync(L.w.p, set, sizeof(float) * L.nparam, cudaMemcpyHostToDevice, c->stream));
+    if (get) CK(cudaMemcpyAsync(get, L.w.p, sizeof(float) * L.nparam, cudaMemcpyDeviceToHost, c->stream));
+    CK(cudaStreamSynchronize(c->stream));
+    return CRYOIM_OK;
+}
+
+int cryoim_learn_forward(void* ctx, const float* feat, const float* truth, int32_t B, float* scores, float* loss,
+                         float* grads) {
+    Ctx* c = as_ctx(ctx);
+    int r = check_ready(c, false);
+    if (r) return r;
+    LearnModel& L = c->lm;
+    if (L.nparam == 0) return fail(CRYOIM_ERR_STATE, "no proposer parameters (cryoim_learn_params)");
+    if (!feat || B < 1 || ((loss || grads) && !truth)) return fail(CRYOIM_ERR_ARG, "bad arguments");
+    if ((r = learn_activations(c, B))) return r;
+    CK(cudaMemcpyAsync(L.feat.p, feat, sizeof(float) * B * LP_NR * LP_NT, cudaMemcpyHostToDevice, c->stream));
+    if ((r = learn_forward(c, B))) return r;
+    if (scores)
+        CK(cudaMemcpyAsync(scores, L.sc.p, sizeof(float) * B * L.V * LP_NT, cudaMemcpyDeviceToHost, c->stream));
+    if (truth) {
+        CK(cudaMemcpyAsync(L.truth.p, truth, sizeof(float) * 4 * B, cudaMemcpyHostToDevice, c->stream));
+        if ((r = learn_backward(c, B))) return r;
+        if (loss) CK(cudaMemcpyAsync(loss, L.loss.p, sizeof(float) * B, cudaMemcpyDeviceToHost, c->stream));
+        if (grads) CK(cudaMemcpyAsync(grads, L.gr.p, sizeof(float) * L.nparam, cudaMemcpyDeviceToHost, c->stream));
+    }
+    CK(cudaStreamSynchronize(c->stream));
+    return CRYOIM_OK;
+}
+
+int cryoim_learn_views(void* ctx, float* out, int32_t* V) {
+    Ctx* c = as_ctx(ctx);
+    int r = check_ready(c, false);
+    if (r) return r;
+    if (!V) return fail(CRYOIM_ERR_ARG, "null count");
+    if ((r = ensure_cgrid(c))) return r;
+    *V = c->cgrid.V;
+    if (out)
+        for (int i = 0; i < c->cgrid.V; ++i) {
+            out[2 * i] = c->cgrid.views[4 * i];
+            out[2 * i + 1] = c->cgrid.views[4 * i + 1];
+        }
+    return CRYOIM_OK;
+}
+
+int cryoim_learn_features(void* ctx, const float* imgs, const cryoim_particle* parts, int32_t P, float* feat) {
+    Ctx* c = as_ctx(ctx);
+    int r = check_ready(c, false);
+    if (r) return r;
+    if (!imgs || !parts || !feat || P < 1) return fail(CRYOIM_ERR_ARG, "bad arguments");
+    const long nn = (long)c->p.fftsize * c->p.fftsize;
+    const int B = std::min(P, 64);
+    if ((r = ensure_cgrid(c))) return r;
+    if (c->lm.V == 0) c->lm.V = c->cgrid.V;
+    if ((r = learn_activations(c, B)) || (r = ensure_batch(c, B))) return r;
+    DBuf<float> d;
+    if ((r = d.ensure((size_t)B * nn))) return r;
+    std::vector<float> ox(B), oy(B);
+    for (int b0 = 0; b0 < P; b0 += B) {
+        const int nb = std::min(B, P - b0);
+        for (int i = 0; i < nb; ++i) { ox[i] = parts[b0 + i].x; oy[i] = parts[b0 + i].y; }
+        CK(cudaMemcpyAsync(d.p, imgs + b0 * nn, sizeof(float) * nb * nn, cudaMemcpyHostToDevice, c->stream));
+        if ((r = learn_features_dev(c, d.p, nb, ox.data(), oy.data()))) return r;
+        CK(cudaMemcpyAsync(feat + (long)b0 * LP_NR * LP_NT, c->lm.feat.p, sizeof(float) * nb * LP_NR * LP_NT,
+                           cudaMemcpyDeviceToHost, c->stream));
+        CK(cudaStreamSynchronize(c->stream));
+    }
+    if ((r = check_flag(c))) return r;
+    return CRYOIM_OK;
 }
 
 int cryoim_contract_stats(void* ctx, double* out /* 6 */) {

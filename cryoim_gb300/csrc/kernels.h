@@ -183,6 +183,40 @@ long cc_fp64_scratch(int k, int B);
 void launch_cc_fp64(const float2* cube, const float2* band, const float* ctf, Band bd, const int2* samples,
                     int S, const float* cand, int k, int B, double* scratch, double* out, cudaStream_t st);
 
+// ---- learned orientation proposer (learn.cu) ----
+constexpr int LP_NR = 64, LP_NT = 128;   // polar feature: radii over [minR, maxR] x angles over [0, 180)
+constexpr int LP_C1 = 16, LP_C2 = 32, LP_C3 = 32, LP_C4 = 32, LP_CM = 16;
+constexpr int LP_MIXK = LP_C4 * (LP_NR / 8);  // (channel, radius) inputs of the mix
+void launch_lp_real_to_cplx(const float* img, int nx, int B, float2* out, cudaStream_t st);
+// par[b] = (df1, df2, astig, ox, oy)
+void launch_lp_ctf_shift(float2* ft, int nx, int B, const float* par, float apix, float volt, float cs, float ampwg,
+                         cudaStream_t st);
+void launch_lp_cplx_to_real(const float2* in, int nx, int B, float* out, float* var, cudaStream_t st);
+void launch_lp_add_noise(float* img, int nx, int B, const float* var, float snr, unsigned long long seed,
+                         cudaStream_t st);
+void launch_lp_features(const float2* band, const Band& bd, int B, float* feat, cudaStream_t st);
+cudaError_t launch_lp_conv3(const float* in, int B, int Cin, int H, const float* W, const float* bias, int Cout,
+                            bool relu, float* out, cudaStream_t st);
+// accumulates into dW, db (zero them first)
+cudaError_t launch_lp_conv3_wgrad(const float* in, const float* dpre, int B, int Cin, int H, int Cout, float* dW,
+                                  float* db, cudaStream_t st);
+void launch_lp_relu_grad(const float* out, const float* dout, long n, float* dpre, cudaStream_t st);
+void launch_lp_flip(const float* W, int Cout, int Cin, float* Wf, cudaStream_t st);
+void launch_lp_pool(const float* a, int B, int C, int Hout, float* p, cudaStream_t st);
+void launch_lp_pool_grad(const float* dp, int B, int C, int Hout, float* da, cudaStream_t st);
+void launch_lp_mix(const float* x, int B, const float* W5, const float* b5, float* g, cudaStream_t st);
+void launch_lp_mix_grad(const float* x, const float* dg, int B, const float* W5, float* dx, float* dW5, float* db5,
+                        cudaStream_t st);
+cudaError_t launch_lp_head(const float* g, const float* T, int B, int V, float* sc, cudaStream_t st);
+void launch_lp_head_grad(const float* g, const float* T, const float* dsc, int B, int V, float* dg, float* dT,
+                         cudaStream_t st);
+// truth[b] = (view unit vector x, y, z, shift); sv degrees, ss shifts
+void launch_lp_loss(const float* sc, int B, int V, const float* vview, const float* truth, float sv, float ss,
+                    float* dsc, float* loss, cudaStream_t st);
+void launch_lp_adam(float* w, const float* g, float* m, float* v, long n, float lr, int step, cudaStream_t st);
+// sc is overwritten (taken cells set to -inf)
+void launch_lp_topk(float* sc, int B, int V, int k, int* cell, float* val, cudaStream_t st);
+
 // dst row r = src row idx[r] (row_bytes a multiple of 16), n rows
 // per particle b of B: the k best of its O x seg[b].y (value, column) entries at
 // topv/topi + seg[b].x with distinct columns -> col, origin, cc [B][k]

@@ -1,0 +1,694 @@
+// learn.cu — the learned orientation proposer: a small rotation-equivariant CNN on each
+// particle's polar power spectrum, trained on projections the library itself renders.
+//
+// Input: |F|^2 of the particle's band (the masked, unshifted transform the search uses)
+// on a polar grid of LP_NR radii over [minR, maxR] x LP_NT angles over [0, 180 deg)
+// (a power spectrum is point-symmetric, so half a turn holds all of it); log, then each
+// radius normalised to zero mean and unit variance over angle, which removes the
+// isotropic CTF envelope and the noise level.  An in-plane rotation of the particle is
+// a circular shift along the angle axis, so every layer is circular in angle:
+//   4 x conv 3x3 (circular in angle, zero-padded in radius) + ReLU, average pooling of
+//   radius pairs after layers 2-4 (64 -> 8 radii);
+//   a linear mix of (channel, radius) -> LP_CM channels per angle: g[b][c][t];
+//   the head: one learned template T[v][c][t] per view v of a coarse view grid, scored
+//   at every circular shift s, sc[b][v][s] = sum_{c,t} g[b][c][(t + s) % NT] T[v][c][t].
+// A cell (v, s) names a view and an in-plane angle (and the angle + 180 deg).  Training
+// minimises the cross entropy against a target spread over neighbouring views and
+// shifts.  Everything is FP32 on the CUDA cores: the proposer costs a few ms per batch
+// next to the contraction it feeds.
+#include <cuda_runtime.h>
+
+#include <cstdint>
+
+#include "kernels.h"
+
+namespace cryoim {
+namespace {
+
+constexpr int NR = LP_NR, NT = LP_NT, CM = LP_CM;
+
+__device__ __forceinline__ float warp_sum(float v) {
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    return v;
+}
+__device__ __forceinline__ float warp_max(float v) {
+    for (int o = 16; o > 0; o >>= 1) v = fmaxf(v, __shfl_xor_sync(0xffffffffu, v, o));
+    return v;
+}
+// block-wide sum / max (blockDim a multiple of 32, <= 1024); all threads get the result
+__device__ float block_sum(float v, float* sh) {
+    v = warp_sum(v);
+    const int w = threadIdx.x >> 5, l = threadIdx.x & 31, nw = blockDim.x >> 5;
+    __syncthreads();
+    if (l == 0) sh[w] = v;
+    __syncthreads();
+    float r = (l < nw) ? sh[l] : 0.0f;
+    r = warp_sum(r);
+    return r;
+}
+__device__ float block_max(float v, float* sh) {
+    v = warp_max(v);
+    const int w = threadIdx.x >> 5, l = threadIdx.x & 31, nw = blockDim.x >> 5;
+    __syncthreads();
+    if (l == 0) sh[w] = v;
+    __syncthreads();
+    float r = (l < nw) ? sh[l] : -3.0e38f;
+    r = warp_max(r);
+    return r;
+}
+
+// ---- training data: CTF, origin shift and noise on rendered projections ----------
+
+// img * (-1)^(x+y) as complex (the centred-transform convention of the search)
+__global__ void k_real_to_cplx(const float* __restrict__ img, long total, int nx, float2* __restrict__ out) {
+    for (long q = (long)blockIdx.x * blockDim.x + threadIdx.x; q < total; q += (long)gridDim.x * blockDim.x) {
+        const int x = (int)(q % nx), y = (int)((q / nx) % nx);
+        const float v = img[q];
+        out[q] = make_float2(((x + y) & 1) ? -v : v, 0.0f);
+    }
+}
+
+// Centred transform x CTF (getCTF2d.f90 with defocus in um, Cs in mm, astigmatism angle
+// in degrees) x exp(-2 pi i (hx ox + ky oy) / n), the forward model of a particle at
+// origin (ox, oy).  par[b] = (df1, df2, astig, ox, oy); volt <= 0: no CTF.
+__global__ void k_ctf_shift(float2* __restrict__ ft, int nx, const float* __restrict__ par, float apix, float volt,
+                            float cs, float ampwg) {
+    const int b = blockIdx.y;
+    const long nn = (long)nx * nx;
+    const float* pp = par + 5 * b;
+    const float lam = volt > 0.0f ? 0.387818f / sqrtf(volt * (1.0f + 0.978459e-3f * volt)) : 0.0f;
+    const float pi = 3.14159265358979f;
+    for (long q = (long)blockIdx.x * blockDim.x + threadIdx.x; q < nn; q += (long)gridDim.x * blockDim.x) {
+        const int hx = (int)(q % nx) - nx / 2, ky = (int)(q / nx) - nx / 2;
+        float ph = atan2f((float)ky, (float)hx);
+        if (ph < 0.0f) ph += 2.0f * pi;
+        ph -= pp[2] * pi / 180.0f;
+        const float c = cosf(ph), s = sinf(ph);
+        const float df = (pp[0] * c * c + pp[1] * s * s) * 1.0e4f;
+        const float res2 = (float)(hx * hx + ky * ky) / ((float)nx * apix * (float)nx * apix);
+        const float chi = 2.0f * pi * (-cs * 1.0e7f * lam * lam * lam * res2 * res2 * 0.25f + df * lam * res2 * 0.5f);
+        const float ctf = volt > 0.0f ? -(sqrtf(1.0f - ampwg * ampwg) * sinf(chi) + ampwg * cosf(chi)) : 1.0f;
+        float sn, cn;
+        sincosf(-2.0f * pi * ((float)hx * pp[3] + (float)ky * pp[4]) / (float)nx, &sn, &cn);
+        const float2 v = ft[(long)b * nn + q];
+        ft[(long)b * nn + q] = make_float2(ctf * (v.x * cn - v.y * sn), ctf * (v.x * sn + v.y * cn));
+    }
+}
+
+// Re(inverse) * (-1)^(x+y) / n^2 and its variance inside the disc r <= 0.4 n
+__global__ void k_cplx_to_real(const float2* __restrict__ in, int nx, float* __restrict__ out,
+                               float* __restrict__ var) {
+    __shared__ float sh[32];
+    const int b = blockIdx.x;
+    const long nn = (long)nx * nx;
+    const float inv = 1.0f / (float)nn, rr = 0.4f * (float)nx;
+    float s1 = 0.f, s2 = 0.f, cnt = 0.f;
+    for (long q = threadIdx.x; q < nn; q += blockDim.x) {
+        const int x = (int)(q % nx), y = (int)(q / nx);
+        float v = in[(long)b * nn + q].x * inv;
+        if ((x + y) & 1) v = -v;
+        out[(long)b * nn + q] = v;
+        const float dx = (float)(x - nx / 2), dy = (float)(y - nx / 2);
+        if (dx * dx + dy * dy <= rr * rr) { s1 += v; s2 += v * v; cnt += 1.0f; }
+    }
+    s1 = block_sum(s1, sh);
+    s2 = block_sum(s2, sh);
+    cnt = block_sum(cnt, sh);
+    if (threadIdx.x == 0) {
+        const float m = s1 / fmaxf(cnt, 1.0f);
+        var[b] = fmaxf(s2 / fmaxf(cnt, 1.0f) - m * m, 0.0f);
+    }
+}
+
+// counter-based normal deviates (splitmix64 -> two uniforms -> Box-Muller)
+__device__ __forceinline__ uint64_t mix64(uint64_t z) {
+    z += 0x9E3779B97F4A7C15ull;
+    z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+    z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+    return z ^ (z >> 31);
+}
+__global__ void k_add_noise(float* __restrict__ img, int nx, const float* __restrict__ var, float snr,
+                            unsigned long long seed) {
+    const int b = blockIdx.y;
+    const long nn = (long)nx * nx;
+    const float sd = snr > 0.0f ? sqrtf(var[b] / snr) : 0.0f;
+    if (sd == 0.0f) return;
+    for (long q = (long)blockIdx.x * blockDim.x + threadIdx.x; q < nn; q += (long)gridDim.x * blockDim.x) {
+        const uint64_t h = mix64(seed ^ mix64((uint64_t)b * (uint64_t)nn + (uint64_t)q));
+        const float u1 = ((float)(h >> 40) + 0.5f) * (1.0f / 16777216.0f);
+        const float u2 = (float)((h >> 16) & 0xFFFFFFull) * (1.0f / 16777216.0f);
+        img[(long)b * nn + q] += sd * sqrtf(-2.0f * logf(u1)) * cospif(2.0f * u2);
+    }
+}
+
+// ---- features ------------------------------------------------------------------
+// One block per particle: bilinear |F|^2 of the band at (n/2 + r cos a, n/2 + r sin a),
+// log(P + 1e-6 mean P), then per radius (P - mean) / (std + 1e-6) over the angles.
+__global__ void __launch_bounds__(256) k_features(const float2* __restrict__ band, Band bd,
+                                                  float* __restrict__ feat) {
+    __shared__ float s[NR * NT];
+    __shared__ float sh[32];
+    const int b = blockIdx.x, W = bd.W, nx = bd.nx;
+    const float2* pb = band + (long)b * W * W;
+    const float h = (float)(nx / 2);
+    const float pi = 3.14159265358979f;
+    float part = 0.f;
+    for (int q = threadIdx.x; q < NR * NT; q += blockDim.x) {
+        const int ir = q / NT, it = q - ir * NT;
+        const float r = (float)bd.min_r + (float)(bd.max_r - bd.min_r) * (float)ir / (float)(NR - 1);
+        float sn, cn;
+        sincosf(pi * (float)it / (float)NT, &sn, &cn);
+        const float x = r * cn + h, y = r * sn + h;
+        const int lx = (int)floorf(x), ly = (int)floorf(y);
+        const float ax = x - (float)lx, ay = y - (float)ly;
+        float p[4];
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+            const int tx = lx + (u & 1) - bd.off, ty = ly + (u >> 1) - bd.off;
+            const float2 v = pb[(long)ty * W + tx];
+            p[u] = v.x * v.x + v.y * v.y;
+        }
+        const float v = (1.f - ay) * ((1.f - ax) * p[0] + ax * p[1]) + ay * ((1.f - ax) * p[2] + ax * p[3]);
+        s[q] = v;
+        part += v;
+    }
+    const float mean = block_sum(part, sh) / (float)(NR * NT);
+    __syncthreads();
+    const float eps = 1.0e-6f * mean + 1.0e-30f;
+    for (int q = threadIdx.x; q < NR * NT; q += blockDim.x) s[q] = logf(s[q] + eps);
+    __syncthreads();
+    const int w = threadIdx.x >> 5, l = threadIdx.x & 31, nw = blockDim.x >> 5;
+    for (int ir = w; ir < NR; ir += nw) {
+        float a = 0.f;
+        for (int it = l; it < NT; it += 32) a += s[ir * NT + it];
+        const float m = warp_sum(a) / (float)NT;
+        float d = 0.f;
+        for (int it = l; it < NT; it += 32) {
+            const float e = s[ir * NT + it] - m;
+            d += e * e;
+        }
+        const float inv = 1.0f / (sqrtf(warp_sum(d) / (float)NT) + 1.0e-6f);
+        for (int it = l; it < NT; it += 32) feat[((long)b * NR + ir) * NT + it] = (s[ir * NT + it] - m) * inv;
+    }
+}
+
+// ---- network layers --------------------------------------------------------------
+// 3x3 convolution, circular in angle (NT = 128 = blockDim), zero-padded in radius:
+// out[b][co][h][t] = bias[co] + sum_{ci,dh,dt} in[b][ci][h+dh-1][t+dt-1] W[co][ci][dh][dt],
+// ReLU if relu.  Block (h tile of HT rows, co tile of CT, b).
+template <int CT, int HT>
+__global__ void __launch_bounds__(NT) k_conv3(const float* __restrict__ in, int Cin, int H,
+                                             const float* __restrict__ Wt, const float* __restrict__ bias, int Cout,
+                                             int relu, float* __restrict__ out) {
+    __shared__ float sx[HT + 2][NT + 2];
+    __shared__ float sw[CT * 9];
+    const int t = threadIdx.x, h0 = blockIdx.x * HT, co0 = blockIdx.y * CT, b = blockIdx.z;
+    float acc[CT][HT];
+#pragma unroll
+    for (int c = 0; c < CT; ++c)
+#pragma unroll
+        for (int r = 0; r < HT; ++r) acc[c][r] = 0.f;
+    for (int ci = 0; ci < Cin; ++ci) {
+        const float* ip = in + ((long)b * Cin + ci) * H * NT;
+        __syncthreads();
+#pragma unroll
+        for (int r = 0; r < HT + 2; ++r) {
+            const int hh = h0 + r - 1;
+            const bool ok = hh >= 0 && hh < H;
+            sx[r][t + 1] = ok ? ip[hh * NT + t] : 0.f;
+            if (t == 0) sx[r][0] = ok ? ip[hh * NT + NT - 1] : 0.f;
+            if (t == NT - 1) sx[r][NT + 1] = ok ? ip[hh * NT] : 0.f;
+        }
+        for (int q = t; q < CT * 9; q += NT) sw[q] = Wt[((long)(co0 + q / 9) * Cin + ci) * 9 + q % 9];
+        __syncthreads();
+        float x[HT + 2][3];
+#pragma unroll
+        for (int r = 0; r < HT + 2; ++r)
+#pragma unroll
+            for (int d = 0; d < 3; ++d) x[r][d] = sx[r][t + d];
+#pragma unroll
+        for (int c = 0; c < CT; ++c)
+#pragma unroll
+            for (int k = 0; k < 9; ++k) {
+                const float wv = sw[c * 9 + k];
+#pragma unroll
+                for (int r = 0; r < HT; ++r) acc[c][r] = fmaf(wv, x[r + k / 3][k % 3], acc[c][r]);
+            }
+    }
+#pragma unroll
+    for (int c = 0; c < CT; ++c) {
+        const float bv = bias ? bias[co0 + c] : 0.f;
+#pragma unroll
+        for (int r = 0; r < HT; ++r) {
+            float v = acc[c][r] + bv;
+            if (relu) v = fmaxf(v, 0.f);
+            out[(((long)b * Cout + co0 + c) * H + h0 + r) * NT + t] = v;
+        }
+    }
+}
+
+// Weight and bias gradients of k_conv3 from dpre (the gradient before the ReLU):
+// dW[co][ci][dh][dt] += sum_{b,h,t} dpre[b][co][h][t] in[b][ci][h+dh-1][t+dt-1].
+// Block (co tile, ci, b chunk); the 128 angle threads reduce, then one atomic each.
+template <int CT>
+__global__ void __launch_bounds__(NT) k_conv3_wgrad(const float* __restrict__ in, const float* __restrict__ dpre,
+                                                   int B, int Cin, int H, int Cout, int bchunk,
+                                                   float* __restrict__ dW, float* __restrict__ db) {
+    __shared__ float red[4][CT * 10];
+    const int t = threadIdx.x, co0 = blockIdx.x * CT, ci = blockIdx.y, b0 = blockIdx.z * bchunk;
+    const int tm = (t + NT - 1) % NT, tp = (t + 1) % NT;
+    float acc[CT][10];
+#pragma unroll
+    for (int c = 0; c < CT; ++c)
+#pragma unroll
+        for (int k = 0; k < 10; ++k) acc[c][k] = 0.f;
+    for (int b = b0; b < min(B, b0 + bchunk); ++b) {
+        const float* ip = in + ((long)b * Cin + ci) * H * NT;
+        for (int h = 0; h < H; ++h) {
+            float x[3][3];
+#pragma unroll
+            for (int dh = 0; dh < 3; ++dh) {
+                const int hh = h + dh - 1;
+                const bool ok = hh >= 0 && hh < H;
+                x[dh][0] = ok ? __ldg(ip + hh * NT + tm) : 0.f;
+                x[dh][1] = ok ? __ldg(ip + hh * NT + t) : 0.f;
+                x[dh][2] = ok ? __ldg(ip + hh * NT + tp) : 0.f;
+            }
+#pragma unroll
+            for (int c = 0; c < CT; ++c) {
+                const float g = __ldg(dpre + (((long)b * Cout + co0 + c) * H + h) * NT + t);
+#pragma unroll
+                for (int k = 0; k < 9; ++k) acc[c][k] = fmaf(g, x[k / 3][k % 3], acc[c][k]);
+                acc[c][9] += g;
+            }
+        }
+    }
+    const int w = t >> 5, l = t & 31;
+#pragma unroll
+    for (int c = 0; c < CT; ++c)
+#pragma unroll
+        for (int k = 0; k < 10; ++k) {
+            const float v = warp_sum(acc[c][k]);
+            if (l == 0) red[w][c * 10 + k] = v;
+        }
+    __syncthreads();
+    for (int q = t; q < CT * 10; q += NT) {
+        const float v = red[0][q] + red[1][q] + red[2][q] + red[3][q];
+        const int c = q / 10, k = q % 10;
+        if (k < 9) atomicAdd(dW + ((long)(co0 + c) * Cin + ci) * 9 + k, v);
+        else if (ci == 0) atomicAdd(db + co0 + c, v);
+    }
+}
+
+// dpre = dout where out > 0 (the ReLU gate), else 0
+__global__ void k_relu_grad(const float* __restrict__ out, const float* __restrict__ dout, long n,
+                            float* __restrict__ dpre) {
+    for (long q = (long)blockIdx.x * blockDim.x + threadIdx.x; q < n; q += (long)gridDim.x * blockDim.x)
+        dpre[q] = out[q] > 0.f ? dout[q] : 0.f;
+}
+
+// Wf[ci][co][2-dh][2-dt] = W[co][ci][dh][dt]: the data gradient is a k_conv3 with Wf
+__global__ void k_flip(const float* __restrict__ W, int Cout, int Cin, float* __restrict__ Wf) {
+    const int q = blockIdx.x * blockDim.x + threadIdx.x;
+    if (q >= Cout * Cin * 9) return;
+    const int k = q % 9, ci = (q / 9) % Cin, co = q / (9 * Cin);
+    Wf[((long)ci * Cout + co) * 9 + (8 - k)] = W[q];
+}
+
+// average of radius pairs: p[b][c][h][t] = (a[..][2h][t] + a[..][2h+1][t]) / 2
+__global__ void k_pool(const float* __restrict__ a, long nout, int Hout, float* __restrict__ p) {
+    for (long q = (long)blockIdx.x * blockDim.x + threadIdx.x; q < nout; q += (long)gridDim.x * blockDim.x) {
+        const int t = (int)(q % NT);
+        const long bch = q / NT;  // (b, c, h)
+        const int h = (int)(bch % Hout);
+        const long bc = bch / Hout;
+        const float* src = a + (bc * 2 * Hout + 2 * h) * NT + t;
+        p[q] = 0.5f * (src[0] + src[NT]);
+    }
+}
+__global__ void k_pool_grad(const float* __restrict__ dp, long nout, int Hout, float* __restrict__ da) {
+    for (long q = (long)blockIdx.x * blockDim.x + threadIdx.x; q < nout; q += (long)gridDim.x * blockDim.x) {
+        const int t = (int)(q % NT);
+        const long bch = q / NT;
+        const int h = (int)(bch % Hout);
+        const long bc = bch / Hout;
+        float* dst = da + (bc * 2 * Hout + 2 * h) * NT + t;
+        const float v = 0.5f * dp[q];
+        dst[0] = v;
+        dst[NT] = v;
+    }
+}
+
+// g[b][o][t] = b5[o] + sum_k W5[o][k] x[b][k][t], K = LP_MIXK
+__global__ void __launch_bounds__(NT) k_mix(const float* __restrict__ x, const float* __restrict__ W5,
+                                           const float* __restrict__ b5, float* __restrict__ g) {
+    __shared__ float sw[CM * LP_MIXK];
+    const int b = blockIdx.x, t = threadIdx.x;
+    for (int q = t; q < CM * LP_MIXK; q += NT) sw[q] = W5[q];
+    __syncthreads();
+    float acc[CM];
+#pragma unroll
+    for (int o = 0; o < CM; ++o) acc[o] = b5[o];
+    for (int k = 0; k < LP_MIXK; ++k) {
+        const float v = x[((long)b * LP_MIXK + k) * NT + t];
+#pragma unroll
+        for (int o = 0; o < CM; ++o) acc[o] = fmaf(sw[o * LP_MIXK + k], v, acc[o]);
+    }
+#pragma unroll
+    for (int o = 0; o < CM; ++o) g[((long)b * CM + o) * NT + t] = acc[o];
+}
+// dx[b][k][t] = sum_o W5[o][k] dg[b][o][t]
+__global__ void __launch_bounds__(NT) k_mix_dx(const float* __restrict__ dg, const float* __restrict__ W5,
+                                              float* __restrict__ dx) {
+    __shared__ float sw[CM * LP_MIXK];
+    const int b = blockIdx.x, t = threadIdx.x;
+    for (int q = t; q < CM * LP_MIXK; q += NT) sw[q] = W5[q];
+    __syncthreads();
+    float d[CM];
+#pragma unroll
+    for (int o = 0; o < CM; ++o) d[o] = dg[((long)b * CM + o) * NT + t];
+    for (int k = 0; k < LP_MIXK; ++k) {
+        float a = 0.f;
+#pragma unroll
+        for (int o = 0; o < CM; ++o) a = fmaf(sw[o * LP_MIXK + k], d[o], a);
+        dx[((long)b * LP_MIXK + k) * NT + t] = a;
+    }
+}
+// dW5[o][k] = sum_{b,t} dg[b][o][t] x[b][k][t]; db5[o] = sum dg (block k = 0 adds it)
+__global__ void __launch_bounds__(256) k_mix_dw(const float* __restrict__ x, const float* __restrict__ dg, int B,
+                                               float* __restrict__ dW5, float* __restrict__ db5) {
+    __shared__ float sh[32];
+    const int k = blockIdx.x;
+    float acc[CM], accb[CM];
+#pragma unroll
+    for (int o = 0; o < CM; ++o) { acc[o] = 0.f; accb[o] = 0.f; }
+    for (long q = threadIdx.x; q < (long)B * NT; q += blockDim.x) {
+        const long b = q / NT;
+        const int t = (int)(q % NT);
+        const float v = x[(b * LP_MIXK + k) * NT + t];
+#pragma unroll
+        for (int o = 0; o < CM; ++o) {
+            const float d = dg[(b * CM + o) * NT + t];
+            acc[o] = fmaf(d, v, acc[o]);
+            accb[o] += d;
+        }
+    }
+    for (int o = 0; o < CM; ++o) {
+        const float s = block_sum(acc[o], sh);
+        if (threadIdx.x == 0) dW5[o * LP_MIXK + k] = s;
+        if (k == 0) {
+            const float sb = block_sum(accb[o], sh);
+            if (threadIdx.x == 0) db5[o] = sb;
+        }
+    }
+}
+
+// Head: sc[b][v][s] = sum_{c,t} g[b][c][(t + s) % NT] T[v][c][t].  Block (8 views, b),
+// 64 threads, each two shifts (s, s + 64) x 8 views; g doubled in shared memory so the
+// circular index needs no modulo; the 8 views' templates interleaved [c][t][8].
+constexpr int HV = 8;
+__global__ void __launch_bounds__(64) k_head(const float* __restrict__ g, const float* __restrict__ T, int V,
+                                            float* __restrict__ sc) {
+    extern __shared__ float hsm[];
+    float* sg = hsm;               // [CM][2 NT]
+    float* sT = hsm + CM * 2 * NT;  // [CM][NT][HV]
+    const int b = blockIdx.y, v0 = blockIdx.x * HV, s = threadIdx.x;
+    for (int q = s; q < CM * NT; q += 64) {
+        const float v = g[(long)b * CM * NT + q];
+        const int c = q / NT, t = q % NT;
+        sg[c * 2 * NT + t] = v;
+        sg[c * 2 * NT + t + NT] = v;
+    }
+    for (int q = s; q < HV * CM * NT; q += 64) {
+        const int j = q / (CM * NT), ct = q % (CM * NT);
+        sT[ct * HV + j] = (v0 + j < V) ? T[(long)(v0 + j) * CM * NT + ct] : 0.f;
+    }
+    __syncthreads();
+    float a0[HV], a1[HV];
+#pragma unroll
+    for (int j = 0; j < HV; ++j) { a0[j] = 0.f; a1[j] = 0.f; }
+    for (int c = 0; c < CM; ++c) {
+        const float* gr = sg + c * 2 * NT;
+        const float4* tr = reinterpret_cast<const float4*>(sT + c * NT * HV);
+#pragma unroll 4
+        for (int t = 0; t < NT; ++t) {
+            const float g0 = gr[t + s], g1 = gr[t + s + 64];
+            const float4 ta = tr[2 * t], tb = tr[2 * t + 1];
+            const float tv[HV] = {ta.x, ta.y, ta.z, ta.w, tb.x, tb.y, tb.z, tb.w};
+#pragma unroll
+            for (int j = 0; j < HV; ++j) {
+                a0[j] = fmaf(g0, tv[j], a0[j]);
+                a1[j] = fmaf(g1, tv[j], a1[j]);
+            }
+        }
+    }
+#pragma unroll
+    for (int j = 0; j < HV; ++j)
+        if (v0 + j < V) {
+            sc[((long)b * V + v0 + j) * NT + s] = a0[j];
+            sc[((long)b * V + v0 + j) * NT + s + 64] = a1[j];
+        }
+}
+
+// dT[v][c][t] = sum_b sum_s dsc[b][v][s] g[b][c][(t + s) % NT].  Block per view, thread t.
+__global__ void __launch_bounds__(NT) k_head_dT(const float* __restrict__ g, const float* __restrict__ dsc, int B,
+                                               int V, float* __restrict__ dT) {
+    __shared__ float sg[CM][2 * NT];
+    __shared__ float sd[NT];
+    const int v = blockIdx.x, t = threadIdx.x;
+    float acc[CM];
+#pragma unroll
+    for (int c = 0; c < CM; ++c) acc[c] = 0.f;
+    for (int b = 0; b < B; ++b) {
+        __syncthreads();
+        sd[t] = dsc[((long)b * V + v) * NT + t];
+#pragma unroll
+        for (int c = 0; c < CM; ++c) {
+            const float x = g[((long)b * CM + c) * NT + t];
+            sg[c][t] = x;
+            sg[c][t + NT] = x;
+        }
+        __syncthreads();
+        for (int s = 0; s < NT; ++s) {
+            const float d = sd[s];
+#pragma unroll
+            for (int c = 0; c < CM; ++c) acc[c] = fmaf(d, sg[c][t + s], acc[c]);
+        }
+    }
+#pragma unroll
+    for (int c = 0; c < CM; ++c) dT[((long)v * CM + c) * NT + t] = acc[c];
+}
+
+// dg[b][c][u] = sum_v sum_s dsc[b][v][s] T[v][c][(u - s) % NT].  Block per particle, thread u.
+__global__ void __launch_bounds__(NT) k_head_dg(const float* __restrict__ T, const float* __restrict__ dsc, int V,
+                                               float* __restrict__ dg) {
+    __shared__ float sT[CM][2 * NT];
+    __shared__ float sd[NT];
+    const int b = blockIdx.x, u = threadIdx.x;
+    float acc[CM];
+#pragma unroll
+    for (int c = 0; c < CM; ++c) acc[c] = 0.f;
+    for (int v = 0; v < V; ++v) {
+        __syncthreads();
+        sd[u] = dsc[((long)b * V + v) * NT + u];
+#pragma unroll
+        for (int c = 0; c < CM; ++c) {
+            const float x = T[((long)v * CM + c) * NT + u];
+            sT[c][u] = x;
+            sT[c][u + NT] = x;
+        }
+        __syncthreads();
+        // T[(u - s) mod NT] = sT[u - s + NT]
+        for (int s = 0; s < NT; ++s) {
+            const float d = sd[s];
+#pragma unroll
+            for (int c = 0; c < CM; ++c) acc[c] = fmaf(d, sT[c][u - s + NT], acc[c]);
+        }
+    }
+#pragma unroll
+    for (int c = 0; c < CM; ++c) dg[((long)b * CM + c) * NT + u] = acc[c];
+}
+
+// Soft-target cross entropy over the V x NT cells of each particle.  truth[b] = (view
+// unit vector, shift); target(v, s) = exp(-(angle(v, v*) / sv)^2 - (d(s, s*) / ss)^2),
+// normalised.  dsc = (softmax - target) / B; loss[b] = -sum target log softmax.
+__global__ void __launch_bounds__(256) k_loss(const float* __restrict__ sc, int B, int V,
+                                             const float* __restrict__ vview, const float* __restrict__ truth,
+                                             float sv, float ss, float* __restrict__ dsc, float* __restrict__ loss) {
+    __shared__ float sh[32];
+    const int b = blockIdx.x;
+    const long n = (long)V * NT;
+    const float* x = sc + (long)b * n;
+    const float* tr = truth + 4 * b;
+    const float rad2deg = 57.29577951308232f;
+    float mx = -3.0e38f;
+    for (long q = threadIdx.x; q < n; q += blockDim.x) mx = fmaxf(mx, x[q]);
+    mx = block_max(mx, sh);
+    float se = 0.f, st = 0.f, stx = 0.f;
+    for (long q = threadIdx.x; q < n; q += blockDim.x) {
+        const int v = (int)(q / NT), s = (int)(q % NT);
+        se += expf(x[q] - mx);
+        const float dot = vview[3 * v] * tr[0] + vview[3 * v + 1] * tr[1] + vview[3 * v + 2] * tr[2];
+        const float av = acosf(fminf(fmaxf(dot, -1.f), 1.f)) * rad2deg / sv;
+        int ds = abs(s - (int)tr[3]) % NT;
+        ds = min(ds, NT - ds);
+        const float as = (float)ds / ss;
+        const float tg = expf(-av * av - as * as);
+        st += tg;
+        stx += tg * (x[q] - mx);
+    }
+    se = block_sum(se, sh);
+    st = block_sum(st, sh);
+    stx = block_sum(stx, sh);
+    const float lse = logf(se);
+    if (threadIdx.x == 0) loss[b] = -(stx / st - lse);
+    const float ist = 1.0f / st, ise = 1.0f / se, ib = 1.0f / (float)B;
+    for (long q = threadIdx.x; q < n; q += blockDim.x) {
+        const int v = (int)(q / NT), s = (int)(q % NT);
+        const float dot = vview[3 * v] * tr[0] + vview[3 * v + 1] * tr[1] + vview[3 * v + 2] * tr[2];
+        const float av = acosf(fminf(fmaxf(dot, -1.f), 1.f)) * rad2deg / sv;
+        int ds = abs(s - (int)tr[3]) % NT;
+        ds = min(ds, NT - ds);
+        const float as = (float)ds / ss;
+        const float tg = expf(-av * av - as * as);
+        dsc[(long)b * n + q] = (expf(x[q] - mx) * ise - tg * ist) * ib;
+    }
+}
+
+__global__ void k_adam(float* __restrict__ w, const float* __restrict__ g, float* __restrict__ m,
+                       float* __restrict__ v, long n, float lr, float b1, float b2, float eps, float c1, float c2) {
+    for (long q = (long)blockIdx.x * blockDim.x + threadIdx.x; q < n; q += (long)gridDim.x * blockDim.x) {
+        const float gq = g[q];
+        const float mq = b1 * m[q] + (1.f - b1) * gq, vq = b2 * v[q] + (1.f - b2) * gq * gq;
+        m[q] = mq;
+        v[q] = vq;
+        w[q] -= lr * (mq * c1) / (sqrtf(vq * c2) + eps);
+    }
+}
+
+// The k best cells of each particle's V x NT scores (repeated block argmax; sc is
+// scratch: taken cells are set to -inf).
+__global__ void __launch_bounds__(512) k_topk_cells(float* __restrict__ sc, long n, int k, int* __restrict__ cell,
+                                                   float* __restrict__ val) {
+    __shared__ float sv[32];
+    __shared__ long si[32];
+    const int b = blockIdx.x;
+    float* x = sc + (long)b * n;
+    const int w = threadIdx.x >> 5, l = threadIdx.x & 31, nw = blockDim.x >> 5;
+    for (int r = 0; r < k; ++r) {
+        float bv = -3.0e38f;
+        long bi = -1;
+        for (long q = threadIdx.x; q < n; q += blockDim.x)
+            if (x[q] > bv) { bv = x[q]; bi = q; }
+        for (int o = 16; o > 0; o >>= 1) {
+            const float ov = __shfl_xor_sync(0xffffffffu, bv, o);
+            const long oi = __shfl_xor_sync(0xffffffffu, bi, o);
+            if (ov > bv || (ov == bv && oi >= 0 && (bi < 0 || oi < bi))) { bv = ov; bi = oi; }
+        }
+        if (l == 0) { sv[w] = bv; si[w] = bi; }
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            float v0 = sv[0];
+            long i0 = si[0];
+            for (int q = 1; q < nw; ++q)
+                if (sv[q] > v0 || (sv[q] == v0 && si[q] >= 0 && (i0 < 0 || si[q] < i0))) { v0 = sv[q]; i0 = si[q]; }
+            cell[b * k + r] = (int)i0;
+            val[b * k + r] = v0;
+            if (i0 >= 0) x[i0] = -3.0e38f;
+        }
+        __syncthreads();
+    }
+}
+
+inline int cdiv(long a, long b) { return (int)((a + b - 1) / b); }
+inline int grid_for(long n, int tpb) {
+    const long g = (n + tpb - 1) / tpb;
+    return (int)(g < 65535L * 16 ? g : 65535L * 16);
+}
+
+}  // namespace
+
+void launch_lp_real_to_cplx(const float* img, int nx, int B, float2* out, cudaStream_t st) {
+    const long total = (long)B * nx * nx;
+    k_real_to_cplx<<<grid_for(total, 256), 256, 0, st>>>(img, total, nx, out);
+}
+void launch_lp_ctf_shift(float2* ft, int nx, int B, const float* par, float apix, float volt, float cs, float ampwg,
+                         cudaStream_t st) {
+    dim3 g(cdiv((long)nx * nx, 256 * 4), B);
+    k_ctf_shift<<<g, 256, 0, st>>>(ft, nx, par, apix, volt, cs, ampwg);
+}
+void launch_lp_cplx_to_real(const float2* in, int nx, int B, float* out, float* var, cudaStream_t st) {
+    k_cplx_to_real<<<B, 512, 0, st>>>(in, nx, out, var);
+}
+void launch_lp_add_noise(float* img, int nx, int B, const float* var, float snr, unsigned long long seed,
+                         cudaStream_t st) {
+    dim3 g(cdiv((long)nx * nx, 256 * 4), B);
+    k_add_noise<<<g, 256, 0, st>>>(img, nx, var, snr, seed);
+}
+void launch_lp_features(const float2* band, const Band& bd, int B, float* feat, cudaStream_t st) {
+    k_features<<<B, 256, 0, st>>>(band, bd, feat);
+}
+cudaError_t launch_lp_conv3(const float* in, int B, int Cin, int H, const float* W, const float* bias, int Cout,
+                            bool relu, float* out, cudaStream_t st) {
+    if (Cout % 16 || H % 4) return cudaErrorInvalidValue;
+    dim3 g(H / 4, Cout / 16, B);
+    k_conv3<16, 4><<<g, NT, 0, st>>>(in, Cin, H, W, bias, Cout, relu ? 1 : 0, out);
+    return cudaGetLastError();
+}
+cudaError_t launch_lp_conv3_wgrad(const float* in, const float* dpre, int B, int Cin, int H, int Cout, float* dW,
+                                  float* db, cudaStream_t st) {
+    if (Cout % 8) return cudaErrorInvalidValue;
+    const int bchunk = 8;
+    dim3 g(Cout / 8, Cin, cdiv(B, bchunk));
+    k_conv3_wgrad<8><<<g, NT, 0, st>>>(in, dpre, B, Cin, H, Cout, bchunk, dW, db);
+    return cudaGetLastError();
+}
+void launch_lp_relu_grad(const float* out, const float* dout, long n, float* dpre, cudaStream_t st) {
+    k_relu_grad<<<grid_for(n, 256), 256, 0, st>>>(out, dout, n, dpre);
+}
+void launch_lp_flip(const float* W, int Cout, int Cin, float* Wf, cudaStream_t st) {
+    k_flip<<<cdiv((long)Cout * Cin * 9, 256), 256, 0, st>>>(W, Cout, Cin, Wf);
+}
+void launch_lp_pool(const float* a, int B, int C, int Hout, float* p, cudaStream_t st) {
+    const long n = (long)B * C * Hout * NT;
+    k_pool<<<grid_for(n, 256), 256, 0, st>>>(a, n, Hout, p);
+}
+void launch_lp_pool_grad(const float* dp, int B, int C, int Hout, float* da, cudaStream_t st) {
+    const long n = (long)B * C * Hout * NT;
+    k_pool_grad<<<grid_for(n, 256), 256, 0, st>>>(dp, n, Hout, da);
+}
+void launch_lp_mix(const float* x, int B, const float* W5, const float* b5, float* g, cudaStream_t st) {
+    k_mix<<<B, NT, 0, st>>>(x, W5, b5, g);
+}
+void launch_lp_mix_grad(const float* x, const float* dg, int B, const float* W5, float* dx, float* dW5, float* db5,
+                        cudaStream_t st) {
+    if (dx) k_mix_dx<<<B, NT, 0, st>>>(dg, W5, dx);
+    k_mix_dw<<<LP_MIXK, 256, 0, st>>>(x, dg, B, dW5, db5);
+}
+cudaError_t launch_lp_head(const float* g, const float* T, int B, int V, float* sc, cudaStream_t st) {
+    const int sm = (int)(sizeof(float) * (CM * 2 * NT + HV * CM * NT));
+    cudaError_t e = cudaFuncSetAttribute(k_head, cudaFuncAttributeMaxDynamicSharedMemorySize, sm);
+    if (e != cudaSuccess) return e;
+    dim3 grid(cdiv(V, HV), B);
+    k_head<<<grid, 64, sm, st>>>(g, T, V, sc);
+    return cudaGetLastError();
+}
+void launch_lp_head_grad(const float* g, const float* T, const float* dsc, int B, int V, float* dg, float* dT,
+                         cudaStream_t st) {
+    k_head_dT<<<V, NT, 0, st>>>(g, dsc, B, V, dT);
+    k_head_dg<<<B, NT, 0, st>>>(T, dsc, V, dg);
+}
+void launch_lp_loss(const float* sc, int B, int V, const float* vview, const float* truth, float sv, float ss,
+                    float* dsc, float* loss, cudaStream_t st) {
+    k_loss<<<B, 256, 0, st>>>(sc, B, V, vview, truth, sv, ss, dsc, loss);
+}
+void launch_lp_adam(float* w, const float* g, float* m, float* v, long n, float lr, int step, cudaStream_t st) {
+    const float b1 = 0.9f, b2 = 0.999f;
+    const float c1 = 1.0f / (1.0f - powf(b1, (float)step)), c2 = 1.0f / (1.0f - powf(b2, (float)step));
+    k_adam<<<grid_for(n, 256), 256, 0, st>>>(w, g, m, v, n, lr, b1, b2, 1.0e-8f, c1, c2);
+}
+void launch_lp_topk(float* sc, int B, int V, int k, int* cell, float* val, cudaStream_t st) {
+    k_topk_cells<<<B, 512, 0, st>>>(sc, (long)V * NT, k, cell, val);
+}
+
+}  // namespace cryoim

@@ -430,7 +430,54 @@ typedef struct cryoim_contract_opts {
                            grid of twice the step and origins at twice the step names
                            k orientations; only their fine neighbourhoods (+-2 steps)
                            are correlated at full band                              */
+    int32_t learned;    /* 0: off.  k > 0 (<= 64, not with coarse): the trained
+                           proposer (cryoim_learn_train / _load) names k cells (view
+                           of the twice-the-step grid, in-plane angle and the angle
+                           + 180 degrees) per particle; their fine neighbourhoods
+                           (+-2 steps) are correlated as in the coarse form           */
 } cryoim_contract_opts;
+
+/* ---- learned orientation proposer ------------------------------------------- */
+/* A small rotation-equivariant CNN on each particle's polar power spectrum (64 radii
+ * over [minR, maxR] x 128 angles over half a turn): four 3x3 convolutions circular in
+ * angle, a (channel, radius) mix to 16 channels per angle, and one learned template
+ * per view of the twice-the-search-step grid scored at every circular angle shift.
+ * Trained on projections the library renders from the map (real-space projector, CTF,
+ * origin shift, white noise), labelled with their orientations folded into the
+ * asymmetric unit.  No counterpart in the reference. */
+typedef struct cryoim_learn_opts {
+    int32_t samples;    /* training projections (default 200000)                    */
+    int32_t batch;      /* minibatch (default 256)                                  */
+    int32_t seed;       /* orientations, CTF, origins, noise and initial weights    */
+    float lr;           /* Adam learning rate (default 2e-3)                        */
+    float snr;          /* signal / noise variance inside the 0.4 nx disc (0: none) */
+    float df_min, df_max;   /* defocus range, um                                    */
+    float astig_max;    /* astigmatism up to this (um) at a uniform angle           */
+    float origin_max;   /* origins uniform on [-origin_max, origin_max]^2 px        */
+} cryoim_learn_opts;
+int cryoim_learn_opts_default(cryoim_learn_opts* o);
+/* Trains (or retrains) the proposer of ctx for its parameters' search step.  map3d:
+ * nx^3 real map on the host.  stats (may be NULL) <- [mean loss of the last 10% of
+ * steps, seconds, angle sign (+1 / -1), views]. */
+int cryoim_learn_train(void* ctx, const float* map3d, const cryoim_learn_opts* o, float* stats);
+/* The trained weights to / from a file (little-endian: "CRYOIMLP", version, views,
+ * angle sign, search step, parameter count, FP32 parameters). */
+int cryoim_learn_save(void* ctx, const char* path);
+int cryoim_learn_load(void* ctx, const char* path);
+/* Test hooks: parameters (get and / or set; *n <- count), and one forward (+ backward
+ * with truth) on given features [B][64][128]: scores [B][views][128], loss per
+ * particle [B], parameter gradients (NULL to skip).  truth[b] = (view unit vector,
+ * angle shift). */
+int cryoim_learn_params(void* ctx, float* get, const float* set, int64_t* n);
+int cryoim_learn_forward(void* ctx, const float* feat, const float* truth, int32_t B, float* scores,
+                         float* loss, float* grads);
+/* The proposer's classes: views (theta, phi) of the twice-the-step grid, in order
+ * (out may be NULL; *V <- count). */
+int cryoim_learn_views(void* ctx, float* out, int32_t* V);
+/* The proposer's input features [P][64][128] of P particles (mask at each particle's
+ * origin, transform, polar power spectrum). */
+int cryoim_learn_features(void* ctx, const float* imgs, const cryoim_particle* parts, int32_t P,
+                          float* feat);
 /* The 3D map (nx^3 float32) whose central sections are correlated: its centred Fourier
  * transform is kept as a band cube of (2 maxR + 3)^3 complex values. */
 int cryoim_set_reference_map(void* ctx, const float* map3d);

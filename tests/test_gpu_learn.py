@@ -1,0 +1,195 @@
+"""The learned orientation proposer (cryoim_learn_*): its CUDA forward and backward pass
+against a plain PyTorch FP32 restatement of the same network (same weights, features
+and targets), its input features against a numpy restatement on the oracle's particle
+transform, and a trained proposer whose proposals lead the contraction to the same
+pick as the exhaustive form."""
+import math
+
+import numpy as np
+import pytest
+
+from _data import small_case
+
+pytestmark = pytest.mark.gpu
+
+NR, NT, CM, MIXK = 64, 128, 16, 256
+CONV = [(1, 16), (16, 32), (32, 32), (32, 32)]
+
+
+def torch_reference(w, feat, truth, views, sv):
+    """The network of learn.cu in torch FP32 (CPU): scores, per-particle loss and the
+    gradients of the mean loss, flattened in the library's parameter order."""
+    torch = pytest.importorskip("torch")
+    F = torch.nn.functional
+    wt = torch.tensor(w, dtype=torch.float32, requires_grad=True)
+    x = torch.tensor(feat, dtype=torch.float32)[:, None]
+    B = x.shape[0]
+    off = 0
+
+    def take(n):
+        nonlocal off
+        t = wt[off:off + n]
+        off += n
+        return t
+
+    for layer, (ci, co) in enumerate(CONV):
+        W = take(co * ci * 9).reshape(co, ci, 3, 3)
+        b = take(co)
+        x = F.pad(x, (1, 1, 0, 0), mode="circular")
+        x = F.pad(x, (0, 0, 1, 1))
+        x = F.relu(F.conv2d(x, W, b))
+        if layer >= 1:
+            x = F.avg_pool2d(x, (2, 1))
+    W5 = take(CM * MIXK).reshape(CM, MIXK)
+    b5 = take(CM)
+    g = torch.einsum("ok,bkt->bot", W5, x.reshape(B, MIXK, NT)) + b5[None, :, None]
+    V = len(views)
+    T = take(V * CM * NT).reshape(V, CM, NT)
+    idx = (torch.arange(NT)[:, None] + torch.arange(NT)[None, :]) % NT  # [s, t] -> (t + s) % NT
+    sc = torch.einsum("bcst,vct->bvs", g[:, :, idx], T)
+    d2r = math.pi / 180.0
+    th, ph = torch.tensor(views[:, 0] * d2r), torch.tensor(views[:, 1] * d2r)
+    vv = torch.stack([torch.sin(th) * torch.cos(ph), torch.sin(th) * torch.sin(ph), torch.cos(th)], 1).float()
+    tr = torch.tensor(truth, dtype=torch.float32)
+    dot = torch.clamp(tr[:, None, :3] @ vv.T[None], -1, 1)[:, 0]  # [B, V]
+    av = torch.rad2deg(torch.acos(dot)) / sv
+    s = torch.arange(NT)[None]
+    ds = (s - tr[:, 3:4].long()).abs() % NT
+    ds = torch.minimum(ds, NT - ds).float()
+    tgt = torch.exp(-av[:, :, None] ** 2 - ds[:, None, :] ** 2)
+    tgt = tgt / tgt.sum(dim=(1, 2), keepdim=True)
+    logp = F.log_softmax(sc.reshape(B, -1), dim=1).reshape(sc.shape)
+    loss = -(tgt * logp).sum(dim=(1, 2))
+    loss.mean().backward()
+    return sc.detach().numpy(), loss.detach().numpy(), wt.grad.numpy()
+
+
+@pytest.fixture(scope="module")
+def lctx(built):
+    import cryoim_gb300 as ci
+    p, *_ = small_case()
+    with ci.Context(0, p) as ctx:
+        yield ctx, p
+
+
+def random_weights(n, V, rng):
+    w = np.zeros(n, np.float32)
+    off = 0
+    for ci, co in CONV:
+        w[off:off + co * ci * 9] = rng.normal(0, math.sqrt(2.0 / (9 * ci)), co * ci * 9)
+        off += co * ci * 9
+        w[off:off + co] = rng.normal(0, 0.05, co)
+        off += co
+    w[off:off + CM * MIXK] = rng.normal(0, 1 / math.sqrt(MIXK), CM * MIXK)
+    off += CM * MIXK
+    w[off:off + CM] = rng.normal(0, 0.05, CM)
+    off += CM
+    assert n - off == V * CM * NT
+    w[off:] = rng.normal(0, 0.05, n - off)
+    return w
+
+
+def test_forward_backward_match_torch(lctx):
+    ctx, p = lctx
+    rng = np.random.default_rng(5)
+    views = ctx.learn_views()
+    V = len(views)
+    n = ctx.learn_params().size
+    w = random_weights(n, V, rng)
+    ctx.learn_params(w)
+    B = 6
+    feat = rng.normal(size=(B, NR, NT)).astype(np.float32)
+    d2r = math.pi / 180.0
+    truth = np.zeros((B, 4), np.float32)
+    for b in range(B):
+        th, ph = views[rng.integers(V)] + rng.normal(0, 1.0, 2)
+        truth[b, :3] = [math.sin(th * d2r) * math.cos(ph * d2r), math.sin(th * d2r) * math.sin(ph * d2r),
+                        math.cos(th * d2r)]
+        truth[b, 3] = rng.integers(NT)
+    sc, loss, gr = ctx.learn_forward(feat, truth, views=V)
+    rsc, rloss, rgr = torch_reference(w, feat, truth, views.astype(np.float64), 2.0 * p.searchstep)
+    assert np.abs(sc - rsc).max() < 1e-4 * np.abs(rsc).max() + 1e-6
+    assert np.allclose(loss, rloss, rtol=1e-4, atol=1e-5)
+    # gradients, block by block (conv 1-4 weights and biases, mix, templates)
+    sizes = []
+    for ci, co in CONV:
+        sizes += [co * ci * 9, co]
+    sizes += [CM * MIXK, CM, V * CM * NT]
+    off = 0
+    for k, sz in enumerate(sizes):
+        a, b = gr[off:off + sz], rgr[off:off + sz]
+        assert np.abs(a - b).max() <= 2e-3 * np.abs(b).max() + 1e-7, (k, np.abs(a - b).max(), np.abs(b).max())
+        off += sz
+
+
+def features_numpy(a, b, n, r0, R):
+    P = a.astype(np.float64) ** 2 + b.astype(np.float64) ** 2
+    out = np.zeros((NR, NT))
+    for ir in range(NR):
+        r = r0 + (R - r0) * ir / (NR - 1)
+        for it in range(NT):
+            ang = math.pi * it / NT
+            x, y = r * math.cos(ang) + n // 2, r * math.sin(ang) + n // 2
+            lx, ly = math.floor(x), math.floor(y)
+            ax, ay = x - lx, y - ly
+            out[ir, it] = ((1 - ay) * ((1 - ax) * P[ly, lx] + ax * P[ly, lx + 1]) +
+                           ay * ((1 - ax) * P[ly + 1, lx] + ax * P[ly + 1, lx + 1]))
+    out = np.log(out + 1e-6 * out.mean())
+    out = (out - out.mean(axis=1, keepdims=True)) / (out.std(axis=1, keepdims=True) + 1e-6)
+    return out
+
+
+def test_features_match_numpy(lctx, orc):
+    ctx, p = lctx
+    _, vol, tmpl, timgs, imgs, parts, truth = small_case()
+    got = ctx.learn_features(imgs, parts)
+    for i in range(len(parts)):
+        a, b, _ = orc.prep_particle(imgs[i], 1, p.imgmask_px, parts["x"][i], parts["y"][i], 0,
+                                    p.min_r, p.max_r, "f64")
+        want = features_numpy(a, b, p.fftsize, p.min_r, p.max_r)
+        d = np.abs(got[i] - want)
+        assert np.median(d) < 1e-3 and np.quantile(d, 0.999) < 2e-2, (i, np.median(d), d.max())
+
+
+def test_trained_proposer_leads_to_the_exhaustive_pick(built, tmp_path):
+    """Trained on library-rendered projections of the map (noisy, CTF, shifted), the
+    proposer's 16 cells per particle, expanded to their +-2-step neighbourhoods, contain
+    the exhaustive contraction's pick on noise-free particles; a saved and reloaded
+    proposer proposes the same."""
+    import cryoim_gb300 as ci
+    p, vol, tmpl, timgs, imgs, parts, truth = small_case(P=8)
+    with ci.Context(0, p) as ctx:
+        ctx.load_templates(timgs, tmpl)
+        ctx.set_reference_map(vol)
+        st = ctx.learn_train(vol, samples=24576, batch=128, seed=3, snr=1.0, df_min=1.0, df_max=3.0,
+                             origin_max=2.0)
+        assert st["views"] == len(ctx.learn_views()) and st["sign"] in (1, -1)
+        assert np.isfinite(st["loss"])
+        qe = parts.copy()
+        ctx.contract_search(imgs, qe, origin_max=2.0, origin_step=0.5, topk=8)
+        ql = parts.copy()
+        cl = ctx.contract_search(imgs, ql, origin_max=2.0, origin_step=0.5, topk=8, learned=16, want_cands=True)
+        path = str(tmp_path / "proposer.bin")
+        ctx.learn_save(path)
+    for i in range(len(parts)):
+        assert (ql["theta"][i], ql["phi"][i], ql["omega"][i]) == (qe["theta"][i], qe["phi"][i], qe["omega"][i]), i
+    with ci.Context(0, p) as c2:
+        c2.load_templates(timgs, tmpl)
+        c2.set_reference_map(vol)
+        c2.learn_load(path)
+        q2 = parts.copy()
+        c2b = c2.contract_search(imgs, q2, origin_max=2.0, origin_step=0.5, topk=8, learned=16, want_cands=True)
+    assert np.array_equal(q2, ql)
+    assert np.array_equal(c2b, cl)
+
+
+def test_learned_form_needs_a_trained_proposer(built):
+    import cryoim_gb300 as ci
+    p, vol, tmpl, timgs, imgs, parts, truth = small_case()
+    with ci.Context(0, p) as ctx:
+        ctx.load_templates(timgs, tmpl)
+        ctx.set_reference_map(vol)
+        with pytest.raises(ci.CryoimError):
+            ctx.contract_search(imgs, parts.copy(), learned=8)
+        with pytest.raises(ci.CryoimError):
+            ctx.contract_search(imgs, parts.copy(), learned=8, coarse=8)
