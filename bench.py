@@ -43,10 +43,15 @@ sys.path.insert(0, ROOT)
 
 WORKLOAD = dict(nx=256, apix=1.5, min_res=50.0, max_res=6.0, searchstep=1.0, ntemplates=20,
                 df=(0.8, 3.5), astig=0.1, snr=0.05, origin=6.0, origin_step=0.5, topk=16,
-                ampwg=0.07, seed=20261205, cycle_particles=10000)
+                ampwg=0.07, seed=20261205, cycle_particles=10000, learned=16, nbr_best=4)
 METRIC = "particles/s (box 256), BF16+learned vs plain FP32 GPU at >=99% same orientation"
 FP32_PEAK_TFLOPS_NOMINAL = 152 * 128 * 2 * 2.07e9 / 1e12  # FMA lanes x 2 flop x max SM clock
 FLOPS_PER_TERM = 30.0
+# this library's kernels launched per 64-particle pass of the headline form (ncu launch
+# list): prep, FFT post-processing, CTF, template cuts, norms, features, 4 convolutions,
+# 3 poolings, mix, head, cell top-k, operand A, gather, grouped contraction, distinct
+# selection, FP64 rescoring (2), and two rounds of alpha table, band shift, phase residual
+LAUNCHES_PER_PASS = 29
 # DRAM bytes (read + write) of one GEMM launch (3 particles x 625 origins) from an ncu
 # capture at the 2-degree grid (1.483 GB for 31,320 orientations), scaled to the
 # orientation count: operand B streams once per launch.
@@ -193,7 +198,7 @@ def cpu_sample(params, tmpl, timgs, img, part, seconds: float = 15.0):
                            f"FP32 port, OpenMP over views on all host cores, extrapolated to the full grid"}
 
 
-def config_dict(params, batch):
+def config_dict(params, batch, learn_samples=None):
     w = WORKLOAD
     return {"workload": "icos global search, box 256, 1-deg ASU grid x 625 origins (10k-particle "
                         "production configuration shapes)",
@@ -201,8 +206,12 @@ def config_dict(params, batch):
             "minR": params.min_r, "maxR": params.max_r, "searchstep_deg": w["searchstep"],
             "origins": f"+-{w['origin']} px @ {w['origin_step']} px", "topk_rescored": w["topk"],
             "templates": w["ntemplates"], "particles_per_step": batch, "snr": w["snr"],
+            "form": "BF16 contraction over the neighbourhoods (+-2 steps) of the learned proposer's "
+                    f"{w['learned']} cells per particle",
             "section_build": f"per map, charged pro rata per particle of a {w['cycle_particles']}-particle cycle",
-            "learned_proposer": "not built: exhaustive contraction over the full grid",
+            "learned_proposer": (f"trained on {learn_samples} rendered projections per map, the training time "
+                                 f"charged pro rata per particle of a {w['cycle_particles']}-particle cycle")
+                                if learn_samples else "the reference CPU path has none",
             "l2": "flushed (256 MiB write) before every timed step"}
 
 
@@ -247,144 +256,129 @@ def run_ours(args):
     params = make_params(ci)
     ctx = ci.Context(dev, params)
     B = args.batch
-    npr = min(args.pr_particles, B)
-    vol, tmpl, timgs, imgs, parts, truth = make_data(ci, B, lambda v, t: ctx.project_templates(v, t))
+    npr = args.pr_particles
+    P = max(B, npr)
+    vol, tmpl, timgs, imgs, parts, truth = make_data(ci, P, lambda v, t: ctx.project_templates(v, t))
     ctx.load_templates(timgs, tmpl)
     ctx.set_reference_map(vol)
     stream = torch.cuda.Stream(device=dev)
     ctx.set_stream(stream.cuda_stream)
     d_imgs = torch.from_numpy(imgs).to(f"cuda:{dev}")
-    h_imgs = torch.from_numpy(imgs).pin_memory()
+    h_imgs = torch.from_numpy(imgs[:B]).pin_memory()
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=f"cuda:{dev}")
     copts = dict(origin_max=w["origin"], origin_step=w["origin_step"], topk=w["topk"], pick=0)
+    lopts = dict(copts, learned=w["learned"], nbr_best=w["nbr_best"])
+    cyc = w["cycle_particles"]
 
-    def contract_step(dev_ptr=True):
-        q = parts.copy()
-        with torch.cuda.stream(stream):
-            flush.zero_()
-        ctx.contract_search(d_imgs.data_ptr() if dev_ptr else h_imgs.numpy(), q, **copts)
-        return q
-
-    # ---- BF16 contraction form (headline) ----
-    for _ in range(args.warmup):
-        q = contract_step()
-    st0 = ctx.contract_stats()  # section build time (first call) and reset
-    ctx.set_profiling(True)
-    torch.cuda.synchronize()
-    if world > 1:
-        torch.distributed.barrier()
-    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    with ClockSampler(dev) as clk:
+    def timed_steps(fn, steps, sampler=None):
+        torch.cuda.synchronize()
+        if world > 1:
+            torch.distributed.barrier()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        if sampler is not None:
+            sampler.__enter__()
         e0.record(stream)
-        for _ in range(args.steps):
-            q = contract_step()
+        out = None
+        for _ in range(steps):
+            out = fn()
         e1.record(stream)
         torch.cuda.synchronize()
-    ms = e0.elapsed_time(e1)
+        if sampler is not None:
+            sampler.__exit__(None, None, None)
+        return e0.elapsed_time(e1), out
+
+    def search_step(dev_ptr=True, n=B, **kw):
+        q = parts[:n].copy()
+        with torch.cuda.stream(stream):
+            flush.zero_()
+        ctx.contract_search(d_imgs.data_ptr() if dev_ptr else h_imgs.numpy(), q, **kw)
+        return q
+
+    # ---- the learned proposer, trained on projections the library renders from the map ----
+    lst = ctx.learn_train(vol, samples=args.learn_samples, batch=256, seed=w["seed"], snr=w["snr"],
+                          df_min=w["df"][0], df_max=w["df"][1], astig_max=w["astig"], origin_max=w["origin"])
+    train_ms = lst["seconds"] * 1000.0
+
+    # ---- headline: BF16 contraction on the learned proposer's neighbourhoods ----
+    for _ in range(args.warmup):
+        search_step(**lopts)
+    st0 = ctx.contract_stats()  # section build time (first call) and reset
+    ctx.set_profiling(True)
+    clk = ClockSampler(dev)
+    ms, _ = timed_steps(lambda: search_step(**lopts), args.steps, clk)
     gst = ctx.contract_stats()
     ctx.set_profiling(False)
-    slice_share_ms = st0["slice_ms"] * B * args.steps / w["cycle_particles"]
-    ms_eff = ms + slice_share_ms
+    # per-cycle costs charged pro rata: the section build and the proposer's training
+    share = B * args.steps / cyc
+    ms_eff = ms + (st0["slice_ms"] + train_ms) * share
     if world > 1:
         t = torch.tensor([ms_eff], device=f"cuda:{dev}")
         torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
         ms_eff = float(t.item())
     value = world * B * args.steps / (ms_eff / 1000.0)
-    q_bf16 = q
-    # end to end through the host-pointer entry point
-    torch.cuda.synchronize()
-    e2, e3 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    search_only = world * B * args.steps / (ms / 1000.0)
     k2 = max(1, args.steps // 2)
-    e2.record(stream)
-    for _ in range(k2):
-        contract_step(dev_ptr=False)
-    e3.record(stream)
-    torch.cuda.synchronize()
-    e2e_ms = e2.elapsed_time(e3) + st0["slice_ms"] * B * k2 / w["cycle_particles"]
-    e2e = world * B * k2 / (e2e_ms / 1000.0)
+    e2e_ms, _ = timed_steps(lambda: search_step(dev_ptr=False, **lopts), k2)
+    e2e = world * B * k2 / ((e2e_ms + (st0["slice_ms"] + train_ms) * B * k2 / cyc) / 1000.0)
 
-    # ---- FP32 exhaustive phase-residual form (drop-in) on the first npr particles ----
-    def pr_step():
-        qq = parts[:npr].copy()
-        with torch.cuda.stream(stream):
-            flush.zero_()
-        ctx.globesearch(d_imgs.data_ptr(), qq)
-        return qq
-    pr_step()
+    # ---- the FP32 exhaustive phase-residual form (the drop-in) on npr particles ----
+    ctx.globesearch(d_imgs.data_ptr(), parts[:4].copy())
     ctx.set_profiling(True)
-    e4, e5 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    e4.record(stream)
-    for _ in range(2):
-        q_pr = pr_step()
-    e5.record(stream)
-    torch.cuda.synchronize()
-    pr_ms = e4.elapsed_time(e5)
+    q_pr = parts[:npr].copy()
+    pr_ms, _ = timed_steps(lambda: ctx.globesearch(d_imgs.data_ptr(), q_pr), 1)
     kms, klaunch = ctx.kernel_time()
     ctx.set_profiling(False)
-    fp32_pps = world * npr * 2 / (pr_ms / 1000.0)
+    fp32_pps = world * npr / (pr_ms / 1000.0)
     terms = ctx.search_terms()
 
-    # ---- FP8-e4m3 contraction form (per-band scales) on the same particles ----
-    copts8 = dict(copts, precision="fp8")
+    def agree(qa, n=npr):
+        return sum(int(np.allclose((qa["theta"][i], qa["phi"][i], qa["omega"][i]),
+                                   (q_pr["theta"][i], q_pr["phi"][i], q_pr["omega"][i]), atol=1e-3))
+                   for i in range(n)) / n
 
-    def contract8_step():
-        q = parts.copy()
-        with torch.cuda.stream(stream):
-            flush.zero_()
-        ctx.contract_search(d_imgs.data_ptr(), q, **copts8)
+    def on_npr(**kw):
+        q = parts[:npr].copy()
+        ctx.contract_search(d_imgs.data_ptr(), q, **kw)
         return q
-    for _ in range(args.warmup):
-        contract8_step()
-    st8 = ctx.contract_stats()  # FP8 section build (BF16 sections + conversion) and reset
-    ctx.set_profiling(True)
-    torch.cuda.synchronize()
-    e6, e7 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    e6.record(stream)
-    for _ in range(args.steps):
-        q_fp8 = contract8_step()
-    e7.record(stream)
-    torch.cuda.synchronize()
-    ms8 = e6.elapsed_time(e7) + st8["slice_ms"] * B * args.steps / w["cycle_particles"]
-    g8 = ctx.contract_stats()
-    ctx.set_profiling(False)
-    fp8_value = world * B * args.steps / (ms8 / 1000.0)
+    q_learn = on_npr(**lopts)
 
-    # ---- proposal form: a coarse contraction (half band, 2-degree grid, 1 px origins)
-    # names 32 orientations per particle; their fine neighbourhoods are correlated ----
-    prop = {}
+    # ---- the exhaustive contraction forms (every grid orientation), BF16 and FP8, on
+    # steps of Bs particles ----
+    Bs = min(B, args.side_batch)
+    share_s = Bs * args.steps / cyc
+    forms = {}
     for form in ("bf16", "fp8"):
-        def prop_step():
-            q = parts.copy()
-            with torch.cuda.stream(stream):
-                flush.zero_()
-            ctx.contract_search(d_imgs.data_ptr(), q, precision=form, coarse=32, **copts)
-            return q
+        kw = dict(copts, precision=form)
         for _ in range(args.warmup):
-            prop_step()
-        torch.cuda.synchronize()
-        p0, p1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        p0.record(stream)
-        for _ in range(args.steps):
-            q_prop = prop_step()
-        p1.record(stream)
-        torch.cuda.synchronize()
-        # the fine sections' build is shared per cycle as in the headline
-        prop[form] = (world * B * args.steps / ((p0.elapsed_time(p1) + slice_share_ms) / 1000.0), q_prop)
+            search_step(n=Bs, **kw)
+        stf = ctx.contract_stats()
+        ctx.set_profiling(True)
+        msf, _ = timed_steps(lambda: search_step(n=Bs, **kw), args.steps)
+        gf = ctx.contract_stats()
+        ctx.set_profiling(False)
+        vf = world * Bs * args.steps / ((msf + stf["slice_ms"] * share_s) / 1000.0)
+        forms[form] = (vf, stf, gf, on_npr(**kw))
+
+    # ---- the other proposal forms: learned with FP8 operands, coarse contraction ----
+    extra = {}
+    for name, kw in (("learned_fp8", dict(lopts, precision="fp8")),
+                     ("coarse_bf16", dict(copts, coarse=32, nbr_best=w["nbr_best"])),
+                     ("coarse_fp8", dict(copts, coarse=32, nbr_best=w["nbr_best"], precision="fp8"))):
+        for _ in range(args.warmup):
+            search_step(n=Bs, **kw)
+        mse, _ = timed_steps(lambda: search_step(n=Bs, **kw), args.steps)
+        charge = st0["slice_ms"] + (train_ms if name.startswith("learned") else 0.0)
+        extra[name] = (world * Bs * args.steps / ((mse + charge * share_s) / 1000.0), on_npr(**kw))
 
     # ---- the other stages of a refinement cycle: local refinement and insertion ----
     def timed(fn, reps=2):
         fn()
-        s0, s1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        s0.record(stream)
-        for _ in range(reps):
-            fn()
-        s1.record(stream)
-        torch.cuda.synchronize()
-        return s0.elapsed_time(s1) / reps
+        t_ms, _ = timed_steps(fn, reps)
+        return t_ms / reps
 
-    q_ref = q_bf16.copy()
+    q_ref = q_learn[:Bs].copy()
     ref_ms = timed(lambda: ctx.refine(d_imgs.data_ptr(), q_ref.copy()))
-    q_ins = q_bf16.copy()
+    q_ins = q_learn[:Bs].copy()
     q_ins["pr"] = 0.0
 
     def insert_all():
@@ -421,87 +415,93 @@ def run_ours(args):
         ctx.rec_begin_half(parts["x"][0], parts["y"][0])
         ctx.rec_insert(d_imgs.data_ptr(), qq)
         return ctx.rec_get_partial()
-    fsc_forms, _ = ctx.fsc_combine(tnf_from(q_bf16[:npr]), tnf_from(q_pr), want_map=False)
+    fsc_forms, _ = ctx.fsc_combine(tnf_from(q_learn), tnf_from(q_pr), want_map=False)
 
-    # ---- agreement and accuracy ----
-    same = same1 = 0
-    e_b, e_p = [], []
+    # ---- agreement and accuracy of the headline form ----
+    same1 = 0
+    e_l, e_p = [], []
     for i in range(npr):
-        ob = (q_bf16["theta"][i], q_bf16["phi"][i], q_bf16["omega"][i])
+        ol = (q_learn["theta"][i], q_learn["phi"][i], q_learn["omega"][i])
         op = (q_pr["theta"][i], q_pr["phi"][i], q_pr["omega"][i])
-        same += int(np.allclose(ob, op, atol=1e-3))
-        same1 += int(synth.orientation_error(ob, op) <= 1.5 * w["searchstep"])
-        e_b.append(synth.orientation_error(ob, truth[i]))
+        same1 += int(synth.orientation_error(ol, op) <= 1.5 * w["searchstep"])
+        e_l.append(synth.orientation_error(ol, truth[i]))
         e_p.append(synth.orientation_error(op, truth[i]))
-    def agree(qa):
-        return sum(int(np.allclose((qa["theta"][i], qa["phi"][i], qa["omega"][i]),
-                                   (q_pr["theta"][i], q_pr["phi"][i], q_pr["omega"][i]), atol=1e-3))
-                   for i in range(npr)) / npr
-    same8 = agree(q_fp8) * npr
     if r != 0:
         return 0
     peak_s, peak_b, hbm, src = measured_peaks()
     R = params.max_r
     s_ins = sum(1 for ky in range(-R, R + 1) for hx in range(R + 1) if hx * hx + ky * ky <= R * R)
-    slice_bytes = gst["orientations"] * gst["kpad"] * 2 + (2 * R + 3) ** 3 * 8
-    gemm_ms = gst["gemm_ms"] / max(gst["gemm_launches"], 1)
-    achieved = gst["gemm_flops"] / max(gst["gemm_ms"], 1e-9) / 1e9  # TFLOP/s
+    slice_bytes = st0["orientations"] * st0["kpad"] * 2 + (2 * R + 3) ** 3 * 8 if st0["orientations"] else 0
+    ach = gst["gemm_flops"] / max(gst["gemm_ms"], 1e-9) / 1e9  # TFLOP/s of the grouped fine contraction
     pr_avg = kms / max(klaunch, 1)
     pr_achieved = terms * npr * FLOPS_PER_TERM / (pr_avg / 1000.0) / 1e12
+
+    def gemm_roofline(g, peak, kernel, src_note):
+        a = g["gemm_flops"] / max(g["gemm_ms"], 1e-9) / 1e9
+        return {"bound": "tensor", "kernel": kernel, "achieved": a, "peak": peak, "unit": "TFLOP/s",
+                "frac": a / peak, "avg_launch_ms": g["gemm_ms"] / max(g["gemm_launches"], 1),
+                "launches": g["gemm_launches"], "orientations": g["orientations"], "kpad": g["kpad"],
+                "peak_source": src_note}
+    bf_v, bf_st, bf_g, bf_q = forms["bf16"]
+    f8_v, f8_st, f8_g, f8_q = forms["fp8"]
+    passes = (B + 63) // 64
     line = {"metric": METRIC, "value": value, "unit": "particles/s", "n_gpus": world,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_eff / args.steps,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "bf16",
             "data": "synthetic (seeded phantom, CTF, noise; see bench.py docstring)",
-            "config": config_dict(params, B),
-            "e2e": {"value": e2e, "unit": "particles/s", "h2d_bytes_per_step": int(imgs.nbytes + B * 32),
+            "config": config_dict(params, B, args.learn_samples),
+            "e2e": {"value": e2e, "unit": "particles/s", "h2d_bytes_per_step": int(imgs[:B].nbytes + B * 32),
                     "d2h_bytes_per_step": int(B * (w["topk"] * 16 + 8))},
-            "gpu_launches": 11 * ((B + 2) // 3) * args.steps,
-            "roofline": {"bound": "tensor", "kernel": "k_gemm_bf16_argmax", "achieved": achieved,
-                         "peak": peak_s, "unit": "TFLOP/s", "frac": achieved / peak_s,
-                         "traffic": GEMM_TRAFFIC_PER_ORIENT * gst["orientations"],
-                         "traffic_note": "bytes per launch, ncu capture at the 2-degree grid scaled by "
-                                         "orientations; algorithmic bytes per launch (A + B once): "
-                                         f"{2.0 * gst['kpad'] * (gst['orientations'] + 1875):.4g}",
-                         "peak_source": f"{src} bf16_tflops_sustained (kernel runs inside multi-second steps)",
-                         "flops_per_particle": gst["gemm_flops"] / max(B * args.steps, 1),
-                         "avg_launch_ms": gemm_ms, "launches": gst["gemm_launches"],
-                         "orientations": gst["orientations"], "kpad": gst["kpad"]},
+            "gpu_launches": LAUNCHES_PER_PASS * passes * args.steps,
+            "search_only_value": search_only,
+            "charged_per_cycle_ms": {"proposer_training": train_ms, "section_build": st0["slice_ms"],
+                                     "cycle_particles": cyc},
+            "proposer": {"training_samples": args.learn_samples, "training_s": lst["seconds"],
+                         "final_loss": lst["loss"], "views": lst["views"], "cells_per_particle": w["learned"],
+                         "rescoring": f"top-{w['topk']} distinct orientations (FP64 CC), phase residual of "
+                                      f"those and of the grid neighbours of the best {w['nbr_best']}"},
+            "roofline": dict(gemm_roofline(gst, peak_s, "k_gemm_argmax<bf16> (grouped, gathered sections)",
+                                           f"{src} bf16_tflops_sustained"),
+                             traffic=None,
+                             note="the grouped fine contraction of the headline form; its launches are "
+                                  "small (each particle's 625 origins x its few thousand gathered "
+                                  "orientations), and the step is shared with the rescoring kernels "
+                                  "(profiles/ has the launch list)"),
             "section_build_ms": st0["slice_ms"],
             "fp32_form": {"value": fp32_pps, "unit": "particles/s", "particles": npr,
-                          "speedup_of_bf16_form": value / fp32_pps,
+                          "speedup_of_headline": value / fp32_pps,
                           "roofline": {"bound": "fp32", "kernel": "k_pr_omega", "achieved": pr_achieved,
                                        "peak": FP32_PEAK_TFLOPS_NOMINAL, "unit": "TFLOP/s",
                                        "frac": pr_achieved / FP32_PEAK_TFLOPS_NOMINAL,
                                        "terms_per_particle": terms, "avg_launch_ms": pr_avg,
                                        "peak_source": "nominal FP32 FMA rate (no measured non-tensor FP32 peak)"}},
-            "fp8_form": {"value": fp8_value, "unit": "particles/s", "particles_per_step": B,
-                         "identical_orientation_vs_fp32_form": same8 / npr,
-                         "section_build_ms": st8["slice_ms"], "kpad": g8["kpad"],
-                         "roofline": {"bound": "tensor", "kernel": "k_gemm_argmax<e4m3>",
-                                      "achieved": g8["gemm_flops"] / max(g8["gemm_ms"], 1e-9) / 1e9,
-                                      "peak": 2.0 * peak_s, "unit": "TFLOP/s",
-                                      "frac": g8["gemm_flops"] / max(g8["gemm_ms"], 1e-9) / 1e9 / (2.0 * peak_s),
-                                      "avg_launch_ms": g8["gemm_ms"] / max(g8["gemm_launches"], 1),
-                                      "peak_source": "2 x measured bf16_tflops_sustained (the dense FP8 rate "
-                                                     "is twice BF16; no measured FP8 figure)"}},
-            "proposal_form": {f: {"value": prop[f][0], "unit": "particles/s",
-                                  "identical_orientation_vs_fp32_form": agree(prop[f][1]),
-                                  "speedup_over_fp32_form": prop[f][0] / fp32_pps}
-                              for f in prop} | {
-                "note": "coarse BF16 contraction (band to maxR/2, 2-degree grid, origins at 1 px) names 32 "
-                        "orientations per particle; their fine neighbourhoods (+-2 steps, up to 4,000 "
-                        "orientations) are gathered and correlated at full band, then rescored as the "
-                        "exhaustive forms (FP64 CC, phase residual); not a learned proposer"},
-            "refinement": {"value": B / (ref_ms / 1000.0), "unit": "particles/s",
+            "bf16_exhaustive_form": {"value": bf_v, "unit": "particles/s",
+                                     "identical_orientation_vs_fp32_form": agree(bf_q),
+                                     "section_build_ms": bf_st["slice_ms"],
+                                     "roofline": dict(gemm_roofline(bf_g, peak_s, "k_gemm_argmax<bf16>",
+                                                                    f"{src} bf16_tflops_sustained"),
+                                                      traffic=GEMM_TRAFFIC_PER_ORIENT * bf_g["orientations"],
+                                                      traffic_note="bytes per launch, ncu capture at the 2-degree "
+                                                                   "grid scaled by orientations")},
+            "fp8_exhaustive_form": {"value": f8_v, "unit": "particles/s",
+                                    "identical_orientation_vs_fp32_form": agree(f8_q),
+                                    "section_build_ms": f8_st["slice_ms"],
+                                    "roofline": gemm_roofline(f8_g, 2.0 * peak_s, "k_gemm_argmax<e4m3>",
+                                                              "2 x measured bf16_tflops_sustained (the dense FP8 "
+                                                              "rate is twice BF16; no measured FP8 figure)")},
+            "other_proposal_forms": {k: {"value": v[0], "unit": "particles/s",
+                                         "identical_orientation_vs_fp32_form": agree(v[1])}
+                                     for k, v in extra.items()},
+            "refinement": {"value": Bs / (ref_ms / 1000.0), "unit": "particles/s",
                            "ncycle": int(params.ncycle), "entry": "cryoim_refine_device"},
-            "reconstruction": {"insert_value": B / (ins_ms / 1000.0), "unit": "particles/s",
+            "reconstruction": {"insert_value": Bs / (ins_ms / 1000.0), "unit": "particles/s",
                                "samples_x_operators_per_particle": "r <= maxR half plane x 60",
                                "finish_ms": fin_ms, "entry": "cryoim_rec_insert_device / cryoim_rec_finish",
                                "roofline": {"bound": "l2_atomics", "kernel": "k_insert",
-                                            "atomics_per_s": s_ins * 60 * 8 * B / (ins_ms / 1000.0),
-                                            "achieved": s_ins * 12 * B / (ins_ms / 1000.0) / 1e9,
+                                            "atomics_per_s": s_ins * 60 * 8 * Bs / (ins_ms / 1000.0),
+                                            "achieved": s_ins * 12 * Bs / (ins_ms / 1000.0) / 1e9,
                                             "peak": hbm, "unit": "GB/s",
-                                            "frac": s_ins * 12 * B / (ins_ms / 1000.0) / 1e9 / hbm,
+                                            "frac": s_ins * 12 * Bs / (ins_ms / 1000.0) / 1e9 / hbm,
                                             "note": "algorithmic bytes = insertion samples x (8 B transform + "
                                                     "4 B CTF) per particle; the kernel is bound by its "
                                                     "S_ins x 60 x 8 float4 atomics into the L2-resident "
@@ -512,18 +512,20 @@ def run_ours(args):
                              "entry": "cryoim_local_refine (host images and map: H2D, map transform and "
                                       "soft mask inside the timing)"},
             "slicing": {"kernel": "k_slice_bf16", "ms_per_map": st0["slice_ms"],
-                        "roofline": {"bound": "hbm", "achieved": slice_bytes / (st0["slice_ms"] / 1000.0) / 1e9,
+                        "roofline": {"bound": "hbm",
+                                     "achieved": slice_bytes / (st0["slice_ms"] / 1000.0) / 1e9 if slice_bytes else None,
                                      "peak": hbm, "unit": "GB/s",
-                                     "frac": slice_bytes / (st0["slice_ms"] / 1000.0) / 1e9 / hbm,
+                                     "frac": slice_bytes / (st0["slice_ms"] / 1000.0) / 1e9 / hbm if slice_bytes else None,
                                      "traffic_algorithmic": slice_bytes,
                                      "note": "BF16 rows written + band cube read once; the kernel is bound by "
                                              "its trilinear texture fetches (one per sample, hardware "
                                              "filtering of the cube), and runs once per map"}},
-            "agreement": {"identical_orientation": same / npr, "within_1_step": same1 / npr, "particles": npr,
+            "agreement": {"identical_orientation": agree(q_learn), "within_1_step": same1 / npr, "particles": npr,
+                          "form": "headline (BF16 + learned proposals) against the FP32 form",
                           "map_fsc_min": float(fsc_forms[1:].min()),
                           "map_fsc_note": "FSC (shells 1..maxR) between the maps reconstructed from the "
-                                          "BF16-form and the FP32-form orientations of the same particles",
-                          "median_error_vs_truth_deg": {"bf16_form": float(np.median(e_b)),
+                                          "headline form's and the FP32 form's orientations of the same particles",
+                          "median_error_vs_truth_deg": {"headline_form": float(np.median(e_l)),
                                                         "fp32_form": float(np.median(e_p))}},
             "clocks": clk.summary()}
     if not args.no_cpu_baseline:
@@ -629,8 +631,12 @@ def main():
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=4)
     ap.add_argument("--warmup", type=int, default=3)
-    ap.add_argument("--batch", type=int, default=64)
-    ap.add_argument("--pr-particles", type=int, default=64)
+    ap.add_argument("--batch", type=int, default=1024, help="particles per headline step")
+    ap.add_argument("--side-batch", type=int, default=64, help="particles per step of the other forms")
+    ap.add_argument("--pr-particles", type=int, default=192,
+                    help="particles of the agreement check against the FP32 form")
+    ap.add_argument("--learn-samples", type=int, default=25600,
+                    help="projections the learned proposer is trained on")
     ap.add_argument("--searchstep", type=float, default=None,
                     help="override the 1-degree grid (small cases for profiler captures only)")
     ap.add_argument("--origin-step", type=float, default=None,

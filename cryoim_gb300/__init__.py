@@ -152,19 +152,21 @@ class Context:
     def contract_search(self, imgs, parts: np.ndarray, origin_max: float = 6.0,
                         origin_step: float = 0.5, topk: int = 16, pick: int = 0,
                         want_cands: bool = False, precision: str = "bf16", nbr: int = 1,
-                        coarse: int = 0, learned: int = 0):
+                        coarse: int = 0, learned: int = 0, nbr_best: int = 0):
         """Tensor-core cross-correlation search with FP64 / phase-residual rescoring of
         the top-k and their grid neighbours within nbr steps; parts is updated in place.
         precision: "bf16" or "fp8" (e4m3 operands with per-band scales); coarse > 0: the
         proposal form (a coarse contraction names `coarse` orientations per particle,
         only their fine neighbourhoods are correlated); learned > 0: the same with the
-        trained proposer's `learned` cells (learn_train / learn_load first).  Returns (P, topk, 8) candidates
+        trained proposer's `learned` cells (learn_train / learn_load first); nbr_best > 0:
+        only the neighbourhoods of the nbr_best candidates of least phase residual are
+        rescored.  Returns (P, topk, 8) candidates
         if asked: theta, phi, omega, x, y, CC (contraction), CC (FP64), PR."""
         assert parts.dtype == PARTICLE_DTYPE and parts.flags["C_CONTIGUOUS"]
         if precision not in ("bf16", "fp8"):
             raise ValueError("precision must be 'bf16' or 'fp8'")
         o = _abi.ContractOpts(float(origin_max), float(origin_step), int(topk), int(pick),
-                              int(precision == "fp8"), int(nbr), int(coarse), int(learned))
+                              int(precision == "fp8"), int(nbr), int(coarse), int(learned), int(nbr_best))
         out = np.zeros((len(parts), topk, 8), np.float32) if want_cands else None
         if isinstance(imgs, int):
             call("cryoim_contract_search_device", self._h, C.c_void_p(imgs), ptr(parts), len(parts),
@@ -219,6 +221,18 @@ class Context:
         t = None if truth is None else np.ascontiguousarray(truth, np.float32)
         call("cryoim_learn_forward", self._h, ptr(f), ptr(t), B, ptr(sc), ptr(loss), ptr(gr))
         return sc, loss, gr
+
+    def learn_render(self, map3d: np.ndarray, eulers: np.ndarray, par: np.ndarray, snr: float = 0.0,
+                     seed: int = 0) -> np.ndarray:
+        """Training renderer: (B, nx, nx) particles of map3d at eulers (B, 3) with par
+        (B, 5) = (df1, df2, astig, x, y)."""
+        m = np.ascontiguousarray(map3d, np.float32)
+        e = np.ascontiguousarray(eulers, np.float32).reshape(-1, 3)
+        pr = np.ascontiguousarray(par, np.float32).reshape(-1, 5)
+        n = self.params.fftsize
+        out = np.zeros((len(e), n, n), np.float32)
+        call("cryoim_learn_render", self._h, ptr(m), ptr(e), ptr(pr), len(e), float(snr), int(seed), ptr(out))
+        return out
 
     def learn_views(self) -> np.ndarray:
         """(V, 2) theta, phi of the proposer's view classes."""

@@ -64,7 +64,7 @@ class ContractOpts(C.Structure):
     """cryoim_contract_opts (include/cryoim.h)."""
     _fields_ = [("origin_max", C.c_float), ("origin_step", C.c_float), ("topk", C.c_int32),
                 ("pick", C.c_int32), ("precision", C.c_int32), ("nbr", C.c_int32), ("coarse", C.c_int32),
-                ("learned", C.c_int32)]
+                ("learned", C.c_int32), ("nbr_best", C.c_int32)]
 
 
 class LearnOpts(C.Structure):
@@ -145,6 +145,7 @@ SIGNATURES = {
     "cryoim_learn_forward": [_vp, _vp, _vp, _i32, _vp, _vp, _vp],
     "cryoim_learn_features": [_vp, _vp, _vp, _i32, _vp],
     "cryoim_learn_views": [_vp, _vp, _ip],
+    "cryoim_learn_render": [_vp, _vp, _vp, _vp, _i32, _f32, _i32, _vp],
     "cryoim_central_sections": [_vp, _vp, _vp, _vp, _i32, _vp, _vp],
     "cryoim_icos_ops": [_vp],
     "cryoim_asu_fold": [_fp, _fp, _fp],

@@ -13,6 +13,7 @@
 #include <cstdarg>
 #include <cstdio>
 #include <cstring>
+#include <iterator>
 #include <map>
 #include <random>
 #include <string>
@@ -927,7 +928,6 @@ int coarse_lists(Ctx* c, int nb, const float* ctfp, int kc, int nbf, std::vector
     CK(cudaMemcpyAsync(kor.data(), c->kor_c.p, sizeof(int) * nb * kc, cudaMemcpyDeviceToHost, c->stream));
     CK(cudaStreamSynchronize(c->stream));
     if (gerr) return fail(CRYOIM_ERR_CUDA, "coarse contraction wait timed out");
-    if (c->prof) c->prof_gemm_flops += 2.0 * (double)nb * Oc * (double)c->n_orient_c * (double)c->cKpad_c;
     const int span_c = 2 * g.nph + 1, span = 2 * c->nph + 1;
     lists.assign(nb, std::vector<int>());
     for (int i = 0; i < nb; ++i) {
@@ -1088,23 +1088,58 @@ template <class RNG> void random_euler(RNG& rng, float* e) {
     e[2] = (float)(std::atan2(r21, -r20) * r2d);
 }
 
-// Renders B particles into img (device, B x nx^2): projection of dmap at eul, CTF and
-// origin shift from par (if apply_ctf; otherwise the shift only), white noise at snr.
-int learn_render(Ctx* c, const float* dmap, const float* deul, const float* dpar, int B, float snr,
-                 unsigned long long seed, float* img, float2* ft, float* var) {
+// Renders B particles into img (device, B x nx^2) from the band cube texture: Fourier
+// slice at eul, CTF (if ctf) and origin shift from par, inverse transform, white noise
+// at snr (signal variance inside the 0.4 nx disc / noise variance; 0: none).
+int learn_render(Ctx* c, cudaTextureObject_t tex, const float* deul, const float* dpar, int B, float snr,
+                 unsigned long long seed, bool ctf, float* img, float2* ft, float* var) {
     const int nx = c->p.fftsize;
-    launch_project(dmap, nx, deul, B, img, c->stream);
-    launch_lp_real_to_cplx(img, nx, B, ft, c->stream);
+    launch_lp_render(tex, 2 * c->p.max_r + 3, c->p.max_r + 1, 2, nx, deul, dpar, B, c->p.apix,
+                     ctf ? c->p.vol : -1.0f, c->p.cs, c->p.ampwg, host_angles().deg2rad, ft, c->stream);
     cufftHandle h;
     int r;
     if ((r = plan2d(c, B, &h))) return r;
-    CKF(cufftExecC2C(h, (cufftComplex*)ft, (cufftComplex*)ft, CUFFT_FORWARD));
-    launch_lp_ctf_shift(ft, nx, B, dpar, c->p.apix, c->p.apply_ctf ? c->p.vol : -1.0f, c->p.cs, c->p.ampwg,
-                        c->stream);
     CKF(cufftExecC2C(h, (cufftComplex*)ft, (cufftComplex*)ft, CUFFT_INVERSE));
     launch_lp_cplx_to_real(ft, nx, B, img, var, c->stream);
     if (snr > 0.0f) launch_lp_add_noise(img, nx, B, var, snr, seed, c->stream);
     CK(cudaGetLastError());
+    return CRYOIM_OK;
+}
+
+// the band cube as a texture for the lifetime of a scope
+struct CubeTexture {
+    cudaArray_t arr = nullptr;
+    cudaTextureObject_t tex = 0;
+    ~CubeTexture() { if (arr || tex) free_cube_texture(arr, tex); }
+};
+
+// The renderer's band cube: the map padded to (2n)^3, its transform, frequencies up to
+// 2 (maxR + 1) + 1 of the padded grid (maxR + 1 of the map's, twice oversampled), as a
+// texture.
+int render_cube(Ctx* c, const float* map3d, CubeTexture* ct) {
+    const int n = c->p.fftsize, m = 2 * n, Rc = 2 * c->p.max_r + 3;
+    const long m3 = (long)m * m * m, c3 = (long)(2 * Rc + 3) * (2 * Rc + 3) * (2 * Rc + 3);
+    DBuf<float> dmap;
+    DBuf<float2> work, cube;
+    int r;
+    if ((r = dmap.ensure((size_t)n * n * n)) || (r = work.ensure(m3)) || (r = cube.ensure(c3))) return r;
+    CK(cudaMemcpyAsync(dmap.p, map3d, sizeof(float) * n * n * n, cudaMemcpyHostToDevice, c->stream));
+    launch_lp_pad_checker(dmap.p, n, work.p, c->stream);
+    CK(cudaGetLastError());
+    cufftHandle h;
+    CKF(cufftPlan3d(&h, m, m, m, CUFFT_C2C));
+    cufftResult fr = cufftSetStream(h, c->stream);
+    if (fr == CUFFT_SUCCESS) fr = cufftExecC2C(h, (cufftComplex*)work.p, (cufftComplex*)work.p, CUFFT_FORWARD);
+    if (fr != CUFFT_SUCCESS) {
+        cufftDestroy(h);
+        return fail(CRYOIM_ERR_CUDA, "padded 3D transform failed: cufft %d", (int)fr);
+    }
+    launch_map_band(work.p, m, Rc, cube.p, c->stream);
+    cudaError_t e = cudaStreamSynchronize(c->stream);
+    cufftDestroy(h);
+    if (e != cudaSuccess) return fail(CRYOIM_ERR_CUDA, "render cube: %s", cudaGetErrorString(e));
+    CK(make_cube_texture(cube.p, Rc, c->stream, &ct->arr, &ct->tex));
+    CK(cudaStreamSynchronize(c->stream));
     return CRYOIM_OK;
 }
 
@@ -1151,12 +1186,13 @@ int learn_train_impl(Ctx* c, const float* map3d, const cryoim_learn_opts* o, flo
         CK(cudaStreamSynchronize(c->stream));
     }
     L.steps = 0;
-    DBuf<float> dmap, img, deul, dpar, var;
+    CubeTexture ct;
+    if ((r = render_cube(c, map3d, &ct))) return r;
+    DBuf<float> img, deul, dpar, var;
     DBuf<float2> ft;
-    if ((r = dmap.ensure(nn * nx)) || (r = img.ensure((size_t)B * nn)) || (r = ft.ensure((size_t)B * nn)) ||
-        (r = deul.ensure(3 * (size_t)B)) || (r = dpar.ensure(5 * (size_t)B)) || (r = var.ensure(B)))
+    if ((r = img.ensure((size_t)B * nn)) || (r = ft.ensure((size_t)B * nn)) || (r = deul.ensure(3 * (size_t)B)) ||
+        (r = dpar.ensure(5 * (size_t)B)) || (r = var.ensure(B)))
         return r;
-    CK(cudaMemcpyAsync(dmap.p, map3d, sizeof(float) * nn * nx, cudaMemcpyHostToDevice, c->stream));
     // direction of the feature shift under an in-plane rotation: two clean projections
     // 30 degrees apart, features, circular correlation
     {
@@ -1164,7 +1200,7 @@ int learn_train_impl(Ctx* c, const float* map3d, const cryoim_learn_opts* o, flo
         const float p2[10] = {0, 0, 0, 0, 0, 0, 0, 0, 0, 0};
         CK(cudaMemcpyAsync(deul.p, e2, sizeof(e2), cudaMemcpyHostToDevice, c->stream));
         CK(cudaMemcpyAsync(dpar.p, p2, sizeof(p2), cudaMemcpyHostToDevice, c->stream));
-        launch_project(dmap.p, nx, deul.p, 2, img.p, c->stream);
+        if ((r = learn_render(c, ct.tex, deul.p, dpar.p, 2, 0.0f, 0, false, img.p, ft.p, var.p))) return r;
         const float z2[2] = {0.0f, 0.0f};
         if ((r = learn_features_dev(c, img.p, 2, z2, z2))) return r;
         std::vector<float> f(2 * LP_NR * LP_NT);
@@ -1216,9 +1252,9 @@ int learn_train_impl(Ctx* c, const float* map3d, const cryoim_learn_opts* o, flo
         CK(cudaMemcpyAsync(deul.p, heul.data(), sizeof(float) * 3 * B, cudaMemcpyHostToDevice, c->stream));
         CK(cudaMemcpyAsync(dpar.p, hpar.data(), sizeof(float) * 5 * B, cudaMemcpyHostToDevice, c->stream));
         CK(cudaMemcpyAsync(L.truth.p, htruth.data(), sizeof(float) * 4 * B, cudaMemcpyHostToDevice, c->stream));
-        if ((r = learn_render(c, dmap.p, deul.p, dpar.p, B, o->snr,
-                              (unsigned long long)o->seed * 1000003ull + (unsigned long long)sidx, img.p, ft.p,
-                              var.p)))
+        if ((r = learn_render(c, ct.tex, deul.p, dpar.p, B, o->snr,
+                              (unsigned long long)o->seed * 1000003ull + (unsigned long long)sidx,
+                              c->p.apply_ctf != 0, img.p, ft.p, var.p)))
             return r;
         if ((r = learn_features_dev(c, img.p, B, hox.data(), hoy.data()))) return r;
         if ((r = learn_forward(c, B)) || (r = learn_backward(c, B))) return r;
@@ -1356,6 +1392,8 @@ int contract_impl(Ctx* c, const float* imgs, bool on_device, cryoim_particle* pa
     if (opts->precision != 0 && opts->precision != 1) return fail(CRYOIM_ERR_ARG, "precision must be 0 or 1");
     const bool f8 = opts->precision == 1;
     const int nbr = opts->nbr <= 0 ? 1 : opts->nbr;
+    const int nbest = opts->nbr_best;  // 0: neighbourhoods of every candidate
+    if (nbest < 0) return fail(CRYOIM_ERR_ARG, "nbr_best must be >= 0");
     const int nbox = (2 * nbr + 1) * (2 * nbr + 1) * (2 * nbr + 1);
     if (nbr > 3 || (long)nbox * k > 4096) return fail(CRYOIM_ERR_ARG, "(2 nbr + 1)^3 x topk must be <= 4096");
     const int kc = opts->coarse;  // 0: exhaustive; else coarse proposals per particle
@@ -1427,16 +1465,23 @@ int contract_impl(Ctx* c, const float* imgs, bool on_device, cryoim_particle* pa
             src[i] = cur;
         }
     }
-    std::vector<float> hpar(8 * PB), hcand((size_t)PB * k * 5), hcc((size_t)PB * k), hpr;
+    std::vector<float> hpar(8 * PB), hcand((size_t)PB * k * 5), hcc((size_t)PB * k);
     std::vector<int> hor((size_t)PB * k), horig((size_t)PB * k);
     std::vector<double> hcc64((size_t)PB * k);
     std::vector<float> ohost(2 * (size_t)O);
     CK(cudaMemcpyAsync(ohost.data(), c->corigins.p, sizeof(float) * 2 * O, cudaMemcpyDeviceToHost, c->stream));
-    cudaEvent_t g0 = nullptr, g1 = nullptr;
-    if (c->prof) {
-        CK(cudaEventCreate(&g0));
-        CK(cudaEventCreate(&g1));
-    }
+    // profiling: an event pair around every contraction launch of a pass
+    std::vector<cudaEvent_t> gev;
+    auto gmark = [&](size_t i) -> int {
+        while (gev.size() <= i) {
+            cudaEvent_t e;
+            CK(cudaEventCreate(&e));
+            gev.push_back(e);
+        }
+        CK(cudaEventRecord(gev[i], c->stream));
+        return CRYOIM_OK;
+    };
+    size_t ngev = 0;
     const long row_bytes = f8 ? (long)c->cKpad8 : 2L * c->cKpad;
     for (int b0 = 0; b0 < P; b0 += PB) {
         const int nb = std::min(PB, P - b0);
@@ -1490,7 +1535,7 @@ int contract_impl(Ctx* c, const float* imgs, bool on_device, cryoim_particle* pa
         g.err = c->gerr.p;
         CK(cudaMemsetAsync(c->gerr.p, 0, sizeof(int), c->stream));
         std::vector<std::vector<int>> lists;
-        if (c->prof) CK(cudaEventRecord(g0, c->stream));
+        ngev = 0;
         if (kc > 0 || kl > 0) {
             // proposal forms: the coarse contraction or the learned proposer names each
             // particle's candidate orientations, the fine contraction runs on their
@@ -1534,8 +1579,10 @@ int contract_impl(Ctx* c, const float* imgs, bool on_device, cryoim_particle* pa
                     if (c->prof) c->prof_gemm_flops += 2.0 * (double)O * (double)nl * (double)kpad;
                 }
                 if ((r = c->ggroups.ensure(i1 - i0)) || (r = c->gseg.ensure(i1 - i0))) return r;
+                if (c->prof && (r = gmark(ngev++))) return r;
                 CK(launch_gemm_argmax_grouped(abase, (long)nb * O, c->bgather.p, rows, kpad, f8, hg.data(), i1 - i0,
                                               c->ggroups.p, g, c->num_sms, c->stream));
+                if (c->prof && (r = gmark(ngev++))) return r;
                 CK(cudaMemcpyAsync(c->gseg.p, seg.data(), sizeof(int2) * seg.size(), cudaMemcpyHostToDevice,
                                    c->stream));
                 launch_select_distinct(c->topv.p, c->topi.p, O, c->gseg.p, i1 - i0, k, c->kor.p + (size_t)i0 * k,
@@ -1551,12 +1598,14 @@ int contract_impl(Ctx* c, const float* imgs, bool on_device, cryoim_particle* pa
                 const int ns = std::min(pb, nb - s0);
                 build_rows(s0, ns, s0);
                 CK(cudaGetLastError());
+                if (c->prof && (r = gmark(ngev++))) return r;
                 if (f8)
                     CK(launch_gemm_argmax(c->amat8.p, c->bmat8.p, ns * O, (int)c->n_orient, kpad, true, g,
                                           c->num_sms, c->stream));
                 else
                     CK(launch_gemm_argmax(c->amat.p, c->bmat.p, ns * O, (int)c->n_orient, kpad, false, g,
                                           c->num_sms, c->stream));
+                if (c->prof && (r = gmark(ngev++))) return r;
                 launch_select_topk(c->topv.p, c->topi.p, O, ntiles, k, ns, c->tilev.p, c->tileo.p, c->tileorig.p,
                                    c->kor.p + (size_t)s0 * k, c->korig.p + (size_t)s0 * k,
                                    c->kcc.p + (size_t)s0 * k, c->stream);
@@ -1564,7 +1613,6 @@ int contract_impl(Ctx* c, const float* imgs, bool on_device, cryoim_particle* pa
                 if (c->prof) c->prof_gemm_flops += 2.0 * (double)ns * O * (double)c->n_orient * (double)kpad;
             }
         }
-        if (c->prof) CK(cudaEventRecord(g1, c->stream));
         int gerr = 0;
         CK(cudaMemcpyAsync(&gerr, c->gerr.p, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
         CK(cudaMemcpyAsync(hor.data(), c->kor.p, sizeof(int) * nb * k, cudaMemcpyDeviceToHost, c->stream));
@@ -1579,12 +1627,13 @@ int contract_impl(Ctx* c, const float* imgs, bool on_device, cryoim_particle* pa
         if (kc > 0 || kl > 0)  // gathered column -> fine orientation index
             for (int i = 0; i < nb * k; ++i)
                 if (hor[i] >= 0) hor[i] = lists[i / k][hor[i]];
-        if (c->prof) {
-            float ms = 0.f;
-            CK(cudaEventElapsedTime(&ms, g0, g1));
-            c->prof_gemm_ms += ms;
-            c->prof_gemm_launches += 1;
-        }
+        if (c->prof)
+            for (size_t e = 0; e + 1 < ngev; e += 2) {
+                float ms = 0.f;
+                CK(cudaEventElapsedTime(&ms, gev[e], gev[e + 1]));
+                c->prof_gemm_ms += ms;
+                c->prof_gemm_launches += 1;
+            }
         // candidates (theta, phi, omega, x, y) of the selected (orientation, origin) pairs
         for (int i = 0; i < nb * k; ++i) {
             int n = hor[i] < 0 ? 0 : hor[i];
@@ -1602,38 +1651,37 @@ int contract_impl(Ctx* c, const float* imgs, bool on_device, cryoim_particle* pa
                        c->kcc64.p, c->stream);
         // Phase-residual rescoring at the particle's own origin (ort_globesearch.f90 scores
         // every view at particle(i)%x, %y) over each selected orientation and its grid
-        // neighbours within nbr steps; the result equals the exhaustive search wherever its
-        // minimum lies there.  The set is sorted by orientation index, without repeats.
+        // neighbours within nbr steps (all of them, or, with nbr_best = m, only those of
+        // the m candidates of least phase residual, scored first); the result equals the
+        // exhaustive search wherever its minimum lies in the scored set.  Sets are sorted
+        // by orientation index, without repeats.
         std::vector<std::vector<int>> xs(nb);
-        int maxc = 1;
+        std::vector<std::vector<float>> xp(nb);
         const int span = 2 * c->nph + 1;
-        if (T > 0) {
-            for (int i = 0; i < nb; ++i) {
-                std::vector<int>& lst = xs[i];
-                for (int rr = 0; rr < k; ++rr) {
-                    const int n = hor[i * k + rr];
-                    if (n < 0) continue;
-                    const int v = n / c->nom, io = n % c->nom, slot = c->view_slot[v];
-                    const int it = slot / span, ips = slot % span - c->nph;
-                    for (int dt = -nbr; dt <= nbr; ++dt)
-                        for (int dp = -nbr; dp <= nbr; ++dp) {
-                            const int it2 = it + dt, ips2 = ips + dp;
-                            if (it2 < 0 || it2 > c->nth || ips2 < -c->nph || ips2 > c->nph) continue;
-                            const int v2 = c->slot_view[(size_t)it2 * span + ips2 + c->nph];
-                            if (v2 < 0) continue;
-                            for (int dw = -nbr; dw <= nbr; ++dw)
-                                lst.push_back(v2 * c->nom + ((io + dw) % c->nom + c->nom) % c->nom);
-                        }
+        auto neighbourhood = [&](int n, std::vector<int>& lst) {
+            const int v = n / c->nom, io = n % c->nom, slot = c->view_slot[v];
+            const int it = slot / span, ips = slot % span - c->nph;
+            for (int dt = -nbr; dt <= nbr; ++dt)
+                for (int dp = -nbr; dp <= nbr; ++dp) {
+                    const int it2 = it + dt, ips2 = ips + dp;
+                    if (it2 < 0 || it2 > c->nth || ips2 < -c->nph || ips2 > c->nph) continue;
+                    const int v2 = c->slot_view[(size_t)it2 * span + ips2 + c->nph];
+                    if (v2 < 0) continue;
+                    for (int dw = -nbr; dw <= nbr; ++dw)
+                        lst.push_back(v2 * c->nom + ((io + dw) % c->nom + c->nom) % c->nom);
                 }
-                std::sort(lst.begin(), lst.end());
-                lst.erase(std::unique(lst.begin(), lst.end()), lst.end());
-                if (lst.empty()) lst.push_back(0);
-                maxc = std::max(maxc, (int)lst.size());
-            }
-            std::vector<float> hx((size_t)nb * maxc * 5);
-            for (int i = 0; i < nb; ++i)
+        };
+        // phase residuals of per-particle orientation sets (empty sets score nothing)
+        auto score = [&](const std::vector<std::vector<int>>& sets, std::vector<std::vector<float>>& out) -> int {
+            int maxc = 1;
+            for (int i = 0; i < nb; ++i) maxc = std::max(maxc, (int)sets[i].size());
+            if (maxc > maxx) return fail(CRYOIM_ERR_SIZE, "rescoring set of %d orientations", maxc);
+            std::vector<float> hx((size_t)nb * maxc * 5, 0.0f);
+            std::vector<int> hcount(nb);
+            for (int i = 0; i < nb; ++i) {
+                hcount[i] = (int)sets[i].size();
                 for (int j = 0; j < maxc; ++j) {
-                    const int n = xs[i][std::min<size_t>(j, xs[i].size() - 1)];
+                    const int n = sets[i].empty() ? 0 : sets[i][std::min<size_t>(j, sets[i].size() - 1)];
                     float* o = &hx[((size_t)i * maxc + j) * 5];
                     o[0] = c->views[4 * (n / c->nom)];
                     o[1] = c->views[4 * (n / c->nom) + 1];
@@ -1641,10 +1689,9 @@ int contract_impl(Ctx* c, const float* imgs, bool on_device, cryoim_particle* pa
                     o[3] = parts[b0 + i].x;
                     o[4] = parts[b0 + i].y;
                 }
+            }
             CK(cudaMemcpyAsync(c->xcand.p, hx.data(), sizeof(float) * hx.size(), cudaMemcpyHostToDevice,
                                c->stream));
-            std::vector<int> hcount(nb);
-            for (int i = 0; i < nb; ++i) hcount[i] = (int)xs[i].size();
             CK(cudaMemcpyAsync(c->xcount.p, hcount.data(), sizeof(int) * nb, cudaMemcpyHostToDevice, c->stream));
             launch_refine_alpha(c->xcand.p, nb, c->tort.p, T, c->ops.p, c->xalpha.p, c->stream, maxc);
             // every candidate of a particle sits at the particle's origin: shift its band once
@@ -1654,9 +1701,60 @@ int contract_impl(Ctx* c, const float* imgs, bool on_device, cryoim_particle* pa
             a.tfcut_pstride = tfs; a.ctf = ctfp; a.cand = c->xcand.p; a.alpha = c->xalpha.p; a.T = T;
             a.bd = c->bd; a.pr = c->xpr.p; a.ncand = maxc; a.sband = c->sband.p; a.ncount = c->xcount.p;
             CK(launch_pr_single(a, nb, c->stream));
-            hpr.resize((size_t)nb * maxc);
-            CK(cudaMemcpyAsync(hpr.data(), c->xpr.p, sizeof(float) * nb * maxc, cudaMemcpyDeviceToHost,
-                               c->stream));
+            std::vector<float> h((size_t)nb * maxc);
+            CK(cudaMemcpyAsync(h.data(), c->xpr.p, sizeof(float) * h.size(), cudaMemcpyDeviceToHost, c->stream));
+            CK(cudaStreamSynchronize(c->stream));
+            out.assign(nb, std::vector<float>());
+            for (int i = 0; i < nb; ++i) out[i].assign(h.begin() + (size_t)i * maxc, h.begin() + (size_t)i * maxc + sets[i].size());
+            return CRYOIM_OK;
+        };
+        if (T > 0) {
+            if (nbest <= 0 || nbest >= k) {
+                for (int i = 0; i < nb; ++i) {
+                    for (int rr = 0; rr < k; ++rr)
+                        if (hor[i * k + rr] >= 0) neighbourhood(hor[i * k + rr], xs[i]);
+                    std::sort(xs[i].begin(), xs[i].end());
+                    xs[i].erase(std::unique(xs[i].begin(), xs[i].end()), xs[i].end());
+                    if (xs[i].empty()) xs[i].push_back(0);
+                }
+                if ((r = score(xs, xp))) return r;
+            } else {
+                // the candidates first, then the neighbourhoods of the nbest best of them
+                std::vector<std::vector<int>> xa(nb), xb(nb);
+                std::vector<std::vector<float>> pa, pb;
+                for (int i = 0; i < nb; ++i) {
+                    for (int rr = 0; rr < k; ++rr)
+                        if (hor[i * k + rr] >= 0) xa[i].push_back(hor[i * k + rr]);
+                    std::sort(xa[i].begin(), xa[i].end());
+                    xa[i].erase(std::unique(xa[i].begin(), xa[i].end()), xa[i].end());
+                    if (xa[i].empty()) xa[i].push_back(0);
+                }
+                if ((r = score(xa, pa))) return r;
+                for (int i = 0; i < nb; ++i) {
+                    std::vector<int> ord(xa[i].size());
+                    for (size_t j = 0; j < ord.size(); ++j) ord[j] = (int)j;
+                    std::stable_sort(ord.begin(), ord.end(), [&](int x, int y) { return pa[i][x] < pa[i][y]; });
+                    std::vector<int> nb_set;
+                    for (int j = 0; j < std::min<int>(nbest, (int)ord.size()); ++j) neighbourhood(xa[i][ord[j]], nb_set);
+                    std::sort(nb_set.begin(), nb_set.end());
+                    nb_set.erase(std::unique(nb_set.begin(), nb_set.end()), nb_set.end());
+                    std::set_difference(nb_set.begin(), nb_set.end(), xa[i].begin(), xa[i].end(),
+                                        std::back_inserter(xb[i]));
+                }
+                if ((r = score(xb, pb))) return r;
+                for (int i = 0; i < nb; ++i) {  // merge, sorted by orientation index
+                    size_t ia = 0, ib = 0;
+                    while (ia < xa[i].size() || ib < xb[i].size()) {
+                        if (ib >= xb[i].size() || (ia < xa[i].size() && xa[i][ia] < xb[i][ib])) {
+                            xs[i].push_back(xa[i][ia]);
+                            xp[i].push_back(pa[i][ia++]);
+                        } else {
+                            xs[i].push_back(xb[i][ib]);
+                            xp[i].push_back(pb[i][ib++]);
+                        }
+                    }
+                }
+            }
         }
         CK(cudaMemcpyAsync(hcc64.data(), c->kcc64.p, sizeof(double) * nb * k, cudaMemcpyDeviceToHost,
                            c->stream));
@@ -1667,12 +1765,12 @@ int contract_impl(Ctx* c, const float* imgs, bool on_device, cryoim_particle* pa
             if (opts->pick == 0) {
                 int best = 0;
                 for (int j = 1; j < (int)xs[i].size(); ++j)
-                    if (hpr[(size_t)i * maxc + j] < hpr[(size_t)i * maxc + best]) best = j;
+                    if (xp[i][j] < xp[i][best]) best = j;
                 const int n = xs[i][best];
                 q.theta = c->views[4 * (n / c->nom)];
                 q.phi = c->views[4 * (n / c->nom) + 1];
                 q.omega = c->p.searchstep * (float)(n % c->nom);
-                q.pr = hpr[(size_t)i * maxc + best];
+                q.pr = xp[i][best];
             } else {
                 int best = 0;
                 for (int j = 1; j < k; ++j)
@@ -1694,12 +1792,11 @@ int contract_impl(Ctx* c, const float* imgs, bool on_device, cryoim_particle* pa
                     o[7] = 0.0f;
                     if (T > 0)
                         for (size_t m = 0; m < xs[i].size(); ++m)
-                            if (xs[i][m] == hor[a]) { o[7] = hpr[(size_t)i * maxc + m]; break; }
+                            if (xs[i][m] == hor[a]) { o[7] = xp[i][m]; break; }
                 }
         }
     }
-    if (g0) cudaEventDestroy(g0);
-    if (g1) cudaEventDestroy(g1);
+    for (cudaEvent_t e : gev) cudaEventDestroy(e);
     return CRYOIM_OK;
 }
 
@@ -2862,6 +2959,30 @@ int cryoim_learn_forward(void* ctx, const float* feat, const float* truth, int32
         if (loss) CK(cudaMemcpyAsync(loss, L.loss.p, sizeof(float) * B, cudaMemcpyDeviceToHost, c->stream));
         if (grads) CK(cudaMemcpyAsync(grads, L.gr.p, sizeof(float) * L.nparam, cudaMemcpyDeviceToHost, c->stream));
     }
+    CK(cudaStreamSynchronize(c->stream));
+    return CRYOIM_OK;
+}
+
+int cryoim_learn_render(void* ctx, const float* map3d, const float* eul, const float* par, int32_t B, float snr,
+                        int32_t seed, float* imgs) {
+    Ctx* c = as_ctx(ctx);
+    int r = check_ready(c, false);
+    if (r) return r;
+    if (!map3d || !eul || !par || !imgs || B < 1 || snr < 0) return fail(CRYOIM_ERR_ARG, "bad arguments");
+    const long nn = (long)c->p.fftsize * c->p.fftsize;
+    CubeTexture ct;
+    if ((r = render_cube(c, map3d, &ct))) return r;
+    DBuf<float> img, deul, dpar, var;
+    DBuf<float2> ft;
+    if ((r = img.ensure((size_t)B * nn)) || (r = ft.ensure((size_t)B * nn)) || (r = deul.ensure(3 * (size_t)B)) ||
+        (r = dpar.ensure(5 * (size_t)B)) || (r = var.ensure(B)))
+        return r;
+    CK(cudaMemcpyAsync(deul.p, eul, sizeof(float) * 3 * B, cudaMemcpyHostToDevice, c->stream));
+    CK(cudaMemcpyAsync(dpar.p, par, sizeof(float) * 5 * B, cudaMemcpyHostToDevice, c->stream));
+    if ((r = learn_render(c, ct.tex, deul.p, dpar.p, B, snr, (unsigned long long)seed, c->p.apply_ctf != 0, img.p,
+                          ft.p, var.p)))
+        return r;
+    CK(cudaMemcpyAsync(imgs, img.p, sizeof(float) * B * nn, cudaMemcpyDeviceToHost, c->stream));
     CK(cudaStreamSynchronize(c->stream));
     return CRYOIM_OK;
 }

@@ -187,10 +187,13 @@ void launch_cc_fp64(const float2* cube, const float2* band, const float* ctf, Ba
 constexpr int LP_NR = 64, LP_NT = 128;   // polar feature: radii over [minR, maxR] x angles over [0, 180)
 constexpr int LP_C1 = 16, LP_C2 = 32, LP_C3 = 32, LP_C4 = 32, LP_CM = 16;
 constexpr int LP_MIXK = LP_C4 * (LP_NR / 8);  // (channel, radius) inputs of the mix
-void launch_lp_real_to_cplx(const float* img, int nx, int B, float2* out, cudaStream_t st);
-// par[b] = (df1, df2, astig, ox, oy)
-void launch_lp_ctf_shift(float2* ft, int nx, int B, const float* par, float apix, float volt, float cs, float ampwg,
-                         cudaStream_t st);
+// the n^3 map zero-padded to (2n)^3, checkerboarded, complex
+void launch_lp_pad_checker(const float* map, int n, float2* out, cudaStream_t st);
+// transforms of B rendered particles (Fourier slice of the band cube texture of the
+// map padded scale times, CTF, origin shift) over |h| <= R1; par[b] = (df1, df2,
+// astig, ox, oy), volt <= 0: no CTF
+void launch_lp_render(cudaTextureObject_t cube, int Rc, int R1, int scale, int nx, const float* eul, const float* par,
+                      int B, float apix, float volt, float cs, float ampwg, float d2r, float2* ft, cudaStream_t st);
 void launch_lp_cplx_to_real(const float2* in, int nx, int B, float* out, float* var, cudaStream_t st);
 void launch_lp_add_noise(float* img, int nx, int B, const float* var, float snr, unsigned long long seed,
                          cudaStream_t st);

@@ -20,6 +20,7 @@
 
 #include <cstdint>
 
+#include "geom.cuh"
 #include "kernels.h"
 
 namespace cryoim {
@@ -59,27 +60,15 @@ __device__ float block_max(float v, float* sh) {
 
 // ---- training data: CTF, origin shift and noise on rendered projections ----------
 
-// img * (-1)^(x+y) as complex (the centred-transform convention of the search)
-__global__ void k_real_to_cplx(const float* __restrict__ img, long total, int nx, float2* __restrict__ out) {
-    for (long q = (long)blockIdx.x * blockDim.x + threadIdx.x; q < total; q += (long)gridDim.x * blockDim.x) {
-        const int x = (int)(q % nx), y = (int)((q / nx) % nx);
-        const float v = img[q];
-        out[q] = make_float2(((x + y) & 1) ? -v : v, 0.0f);
-    }
-}
-
-// Centred transform x CTF (getCTF2d.f90 with defocus in um, Cs in mm, astigmatism angle
-// in degrees) x exp(-2 pi i (hx ox + ky oy) / n), the forward model of a particle at
-// origin (ox, oy).  par[b] = (df1, df2, astig, ox, oy); volt <= 0: no CTF.
-__global__ void k_ctf_shift(float2* __restrict__ ft, int nx, const float* __restrict__ par, float apix, float volt,
-                            float cs, float ampwg) {
-    const int b = blockIdx.y;
-    const long nn = (long)nx * nx;
-    const float* pp = par + 5 * b;
-    const float lam = volt > 0.0f ? 0.387818f / sqrtf(volt * (1.0f + 0.978459e-3f * volt)) : 0.0f;
+// CTF (getCTF2d.f90 with defocus in um, Cs in mm, astigmatism angle in degrees) times
+// exp(-2 pi i (hx ox + ky oy) / n) applied to v: the forward model of a particle at
+// origin (ox, oy).  pp = (df1, df2, astig, ox, oy); volt <= 0: no CTF.
+__device__ __forceinline__ float2 ctf_shift(float2 v, int hx, int ky, int nx, const float* pp, float apix,
+                                            float volt, float cs, float ampwg) {
     const float pi = 3.14159265358979f;
-    for (long q = (long)blockIdx.x * blockDim.x + threadIdx.x; q < nn; q += (long)gridDim.x * blockDim.x) {
-        const int hx = (int)(q % nx) - nx / 2, ky = (int)(q / nx) - nx / 2;
+    float ctf = 1.0f;
+    if (volt > 0.0f) {
+        const float lam = 0.387818f / sqrtf(volt * (1.0f + 0.978459e-3f * volt));
         float ph = atan2f((float)ky, (float)hx);
         if (ph < 0.0f) ph += 2.0f * pi;
         ph -= pp[2] * pi / 180.0f;
@@ -87,11 +76,57 @@ __global__ void k_ctf_shift(float2* __restrict__ ft, int nx, const float* __rest
         const float df = (pp[0] * c * c + pp[1] * s * s) * 1.0e4f;
         const float res2 = (float)(hx * hx + ky * ky) / ((float)nx * apix * (float)nx * apix);
         const float chi = 2.0f * pi * (-cs * 1.0e7f * lam * lam * lam * res2 * res2 * 0.25f + df * lam * res2 * 0.5f);
-        const float ctf = volt > 0.0f ? -(sqrtf(1.0f - ampwg * ampwg) * sinf(chi) + ampwg * cosf(chi)) : 1.0f;
-        float sn, cn;
-        sincosf(-2.0f * pi * ((float)hx * pp[3] + (float)ky * pp[4]) / (float)nx, &sn, &cn);
-        const float2 v = ft[(long)b * nn + q];
-        ft[(long)b * nn + q] = make_float2(ctf * (v.x * cn - v.y * sn), ctf * (v.x * sn + v.y * cn));
+        ctf = -(sqrtf(1.0f - ampwg * ampwg) * sinf(chi) + ampwg * cosf(chi));
+    }
+    float sn, cn;
+    sincosf(-2.0f * pi * ((float)hx * pp[3] + (float)ky * pp[4]) / (float)nx, &sn, &cn);
+    return make_float2(ctf * (v.x * cn - v.y * sn), ctf * (v.x * sn + v.y * cn));
+}
+
+// The map zero-padded to (2n)^3 (the map at [n/2, 3n/2) per axis) times (-1)^(x+y+z),
+// as complex: its transform samples the map's at half-integer frequencies, so the
+// trilinear slices below interpolate a twice-oversampled transform.
+__global__ void k_pad_checker(const float* __restrict__ map, int n, float2* __restrict__ out) {
+    const int m = 2 * n;
+    const long total = (long)m * m * m;
+    for (long q = (long)blockIdx.x * blockDim.x + threadIdx.x; q < total; q += (long)gridDim.x * blockDim.x) {
+        const int x = (int)(q % m), y = (int)((q / m) % m), z = (int)(q / ((long)m * m));
+        const int X = x - n / 2, Y = y - n / 2, Z = z - n / 2;
+        float v = 0.0f;
+        if (X >= 0 && X < n && Y >= 0 && Y < n && Z >= 0 && Z < n) v = map[((long)Z * n + Y) * n + X];
+        out[q] = make_float2(((x + y + z) & 1) ? -v : v, 0.0f);
+    }
+}
+
+// Transform of a rendered particle by the Fourier slice theorem: at centred frequency
+// (hx, ky) with |h| <= R1, the band cube (texture, side 2 Rc + 3, phase at the map
+// centre, scaled 1 / (scale n)^3) of the map padded scale times, sampled at
+// scale R_euler (hx, ky, 0), times (scale n)^3 and (-1)^(hx + ky) (the phase moved to
+// pixel 0, the convention of the forward transform of img * (-1)^(x+y)), then CTF and
+// origin shift; zero outside.  Its inverse, times (-1)^(x+y) / n^2, is the real-space
+// projection (k_project's geometry) low-passed at R1.
+__global__ void k_render_section(cudaTextureObject_t cube, int Rc, int R1, int scale, int nx,
+                                 const float* __restrict__ eul, const float* __restrict__ par, float apix, float volt,
+                                 float cs, float ampwg, float d2r, float2* __restrict__ ft) {
+    __shared__ float rot[9];
+    const int b = blockIdx.y;
+    if (threadIdx.x == 0) euler_mat(eul[3 * b], eul[3 * b + 1], eul[3 * b + 2], d2r, rot);
+    __syncthreads();
+    const long nn = (long)nx * nx;
+    const float sn = (float)(scale * nx), n3 = sn * sn * sn, off = (float)(Rc + 1) + 0.5f, sc = (float)scale;
+    for (long q = (long)blockIdx.x * blockDim.x + threadIdx.x; q < nn; q += (long)gridDim.x * blockDim.x) {
+        const int hx = (int)(q % nx) - nx / 2, ky = (int)(q / nx) - nx / 2;
+        float2 out = make_float2(0.f, 0.f);
+        if (hx * hx + ky * ky <= R1 * R1) {
+            const float fx = sc * (float)hx, fy = sc * (float)ky;
+            const float x = rot[0] * fx + rot[1] * fy, y = rot[3] * fx + rot[4] * fy, z = rot[6] * fx + rot[7] * fy;
+            float2 v = tex3D<float2>(cube, x + off, y + off, z + off);
+            const float sg = ((hx + ky) & 1) ? -n3 : n3;
+            v.x *= sg;
+            v.y *= sg;
+            out = ctf_shift(v, hx, ky, nx, par + 5 * b, apix, volt, cs, ampwg);
+        }
+        ft[(long)b * nn + q] = out;
     }
 }
 
@@ -608,14 +643,14 @@ inline int grid_for(long n, int tpb) {
 
 }  // namespace
 
-void launch_lp_real_to_cplx(const float* img, int nx, int B, float2* out, cudaStream_t st) {
-    const long total = (long)B * nx * nx;
-    k_real_to_cplx<<<grid_for(total, 256), 256, 0, st>>>(img, total, nx, out);
+void launch_lp_pad_checker(const float* map, int n, float2* out, cudaStream_t st) {
+    const long total = 8L * n * n * n;
+    k_pad_checker<<<grid_for(total, 256), 256, 0, st>>>(map, n, out);
 }
-void launch_lp_ctf_shift(float2* ft, int nx, int B, const float* par, float apix, float volt, float cs, float ampwg,
-                         cudaStream_t st) {
+void launch_lp_render(cudaTextureObject_t cube, int Rc, int R1, int scale, int nx, const float* eul, const float* par,
+                      int B, float apix, float volt, float cs, float ampwg, float d2r, float2* ft, cudaStream_t st) {
     dim3 g(cdiv((long)nx * nx, 256 * 4), B);
-    k_ctf_shift<<<g, 256, 0, st>>>(ft, nx, par, apix, volt, cs, ampwg);
+    k_render_section<<<g, 256, 0, st>>>(cube, Rc, R1, scale, nx, eul, par, apix, volt, cs, ampwg, d2r, ft);
 }
 void launch_lp_cplx_to_real(const float2* in, int nx, int B, float* out, float* var, cudaStream_t st) {
     k_cplx_to_real<<<B, 512, 0, st>>>(in, nx, out, var);

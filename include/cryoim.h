@@ -435,6 +435,10 @@ typedef struct cryoim_contract_opts {
                            of the twice-the-step grid, in-plane angle and the angle
                            + 180 degrees) per particle; their fine neighbourhoods
                            (+-2 steps) are correlated as in the coarse form           */
+    int32_t nbr_best;   /* 0: the phase-residual rescoring covers the neighbourhoods of
+                           all topk candidates.  m > 0: the candidates are scored
+                           first, then only the neighbourhoods of the m with the least
+                           phase residual                                            */
 } cryoim_contract_opts;
 
 /* ---- learned orientation proposer ------------------------------------------- */
@@ -457,7 +461,8 @@ typedef struct cryoim_learn_opts {
 } cryoim_learn_opts;
 int cryoim_learn_opts_default(cryoim_learn_opts* o);
 /* Trains (or retrains) the proposer of ctx for its parameters' search step.  map3d:
- * nx^3 real map on the host.  stats (may be NULL) <- [mean loss of the last 10% of
+ * nx^3 real map on the host, from which the training particles are rendered
+ * (cryoim_learn_render).  stats (may be NULL) <- [mean loss of the last 10% of
  * steps, seconds, angle sign (+1 / -1), views]. */
 int cryoim_learn_train(void* ctx, const float* map3d, const cryoim_learn_opts* o, float* stats);
 /* The trained weights to / from a file (little-endian: "CRYOIMLP", version, views,
@@ -471,6 +476,12 @@ int cryoim_learn_load(void* ctx, const char* path);
 int cryoim_learn_params(void* ctx, float* get, const float* set, int64_t* n);
 int cryoim_learn_forward(void* ctx, const float* feat, const float* truth, int32_t B, float* scores,
                          float* loss, float* grads);
+/* The proposer's training renderer: B particles of the nx^3 map (host) at eul[b] =
+ * (theta, phi, omega) with par[b] = (df1, df2, astig, x, y) (CTF if apply_ctf), white
+ * noise at snr (0: none) from seed -> imgs [B][nx][nx].  Fourier slices of the twice
+ * zero-padded map's transform, low-passed at maxR + 1. */
+int cryoim_learn_render(void* ctx, const float* map3d, const float* eul, const float* par, int32_t B, float snr,
+                        int32_t seed, float* imgs);
 /* The proposer's classes: views (theta, phi) of the twice-the-step grid, in order
  * (out may be NULL; *V <- count). */
 int cryoim_learn_views(void* ctx, float* out, int32_t* V);

@@ -193,3 +193,33 @@ def test_learned_form_needs_a_trained_proposer(built):
             ctx.contract_search(imgs, parts.copy(), learned=8)
         with pytest.raises(ci.CryoimError):
             ctx.contract_search(imgs, parts.copy(), learned=8, coarse=8)
+
+
+def test_render_matches_real_space_projection(built):
+    """The training renderer (Fourier slice of the twice-padded map's transform, CTF,
+    origin shift) against the numpy real-space projector with the same CTF and shift,
+    over |h| <= maxR."""
+    import cryoim_gb300 as ci
+    from cryoim_gb300 import synth
+    p, vol, *_ = small_case()
+    n, R = p.fftsize, p.max_r
+    rng = np.random.default_rng(9)
+    e = synth.random_rotations(4, rng)
+    par = np.zeros((4, 5), np.float32)
+    par[:, 0] = rng.uniform(1.0, 3.0, 4)
+    par[:, 1] = par[:, 0] + 0.05
+    par[:, 2] = 30.0
+    par[:, 3:] = rng.uniform(-2, 2, (4, 2))
+    with ci.Context(0, p) as ctx:
+        got = ctx.learn_render(vol, e, par)
+    ky, hx = np.meshgrid(np.arange(n) - n // 2, np.arange(n) - n // 2, indexing="ij")
+    disc = hx ** 2 + ky ** 2 <= R * R
+    for i in range(4):
+        proj = synth.project_numpy(vol, e[i:i + 1].astype(np.float32))[0]
+        c = synth.ctf2d(n, par[i, 0], par[i, 1], par[i, 2], p.apix, p.vol, p.cs, p.ampwg)
+        want = synth.apply_ctf_shift(proj.astype(np.float64), c, par[i, 3], par[i, 4])
+        fa = np.fft.fftshift(np.fft.fft2(got[i]))[disc]
+        fb = np.fft.fftshift(np.fft.fft2(want))[disc]
+        cc = np.real(np.vdot(fa, fb)) / np.sqrt(np.vdot(fa, fa).real * np.vdot(fb, fb).real)
+        ratio = np.linalg.norm(fa) / np.linalg.norm(fb)
+        assert cc > 0.99 and 0.95 < ratio < 1.05, (i, cc, ratio)
