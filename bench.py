@@ -71,10 +71,10 @@ def measured_peaks():
         return 1700.0, 1900.0, 6800.0, "fallback"
 
 
-def make_params(ci):
+def make_params(ci, searchstep=None):
     w = WORKLOAD
     return ci.default_params(w["nx"], apix=w["apix"], minRes=w["min_res"], maxRes=w["max_res"],
-                             searchstep=w["searchstep"], ampwg=w["ampwg"],
+                             searchstep=searchstep or w["searchstep"], ampwg=w["ampwg"],
                              imgmask=(w["nx"] // 2 - 2) * w["apix"])
 
 
@@ -295,8 +295,10 @@ def run_ours(args):
         return q
 
     # ---- the learned proposer, trained on projections the library renders from the map ----
+    torch.cuda.nvtx.range_push("training")
     lst = ctx.learn_train(vol, samples=args.learn_samples, batch=256, seed=w["seed"], snr=w["snr"],
                           df_min=w["df"][0], df_max=w["df"][1], astig_max=w["astig"], origin_max=w["origin"])
+    torch.cuda.nvtx.range_pop()
     train_ms = lst["seconds"] * 1000.0
 
     # ---- headline: BF16 contraction on the learned proposer's neighbourhoods ----
@@ -305,7 +307,9 @@ def run_ours(args):
     st0 = ctx.contract_stats()  # section build time (first call) and reset
     ctx.set_profiling(True)
     clk = ClockSampler(dev)
+    torch.cuda.nvtx.range_push("headline")
     ms, _ = timed_steps(lambda: search_step(**lopts), args.steps, clk)
+    torch.cuda.nvtx.range_pop()
     gst = ctx.contract_stats()
     ctx.set_profiling(False)
     # per-cycle costs charged pro rata: the section build and the proposer's training
@@ -540,6 +544,42 @@ def run_ours(args):
     return 0
 
 
+def run_profile_case(args):
+    """Small cases for profiler captures (a few GB on the device, seconds of GPU time):
+    learned: 64 particles of the box-256 workload, the headline form with a proposer
+    trained on 2,560 projections, 2 calls; exhaustive-bf16 / exhaustive-fp8: 12
+    particles at a 2-degree grid (31,320 orientations), 2 calls; fp32: 4 particles of
+    the FP32 phase-residual form, 2 calls."""
+    import torch
+    import cryoim_gb300 as ci
+    w = WORKLOAD
+    case = args.profile_case
+    step = 2.0 if case.startswith("exhaustive") else w["searchstep"]
+    params = make_params(ci, searchstep=step)
+    ctx = ci.Context(0, params)
+    P = {"learned": 64, "exhaustive-bf16": 12, "exhaustive-fp8": 12, "fp32": 4}[case]
+    vol, tmpl, timgs, imgs, parts, truth = make_data(ci, P, lambda v, t: ctx.project_templates(v, t))
+    ctx.load_templates(timgs, tmpl)
+    ctx.set_reference_map(vol)
+    d = torch.from_numpy(imgs).cuda()
+    copts = dict(origin_max=w["origin"], origin_step=w["origin_step"], topk=w["topk"], pick=0)
+    if case == "learned":
+        ctx.learn_train(vol, samples=2560, batch=256, seed=w["seed"], snr=w["snr"], df_min=w["df"][0],
+                        df_max=w["df"][1], astig_max=w["astig"], origin_max=w["origin"])
+        copts.update(learned=w["learned"], nbr_best=w["nbr_best"])
+    elif case == "exhaustive-fp8":
+        copts.update(precision="fp8")
+    for _ in range(2):
+        if case == "fp32":
+            ctx.globesearch(d.data_ptr(), parts.copy())
+        else:
+            ctx.contract_search(d.data_ptr(), parts.copy(), **copts)
+    torch.cuda.synchronize()
+    print(json.dumps({"profile_case": case, "particles": P, "ok": True}))
+    ctx.close()
+    return 0
+
+
 def run_precision_report(args):
     """Precision form on the CPU-runnable configuration's data: box 128, 2.0 A/px, band
     1/60-1/10 A^-1, defocus 1.0-3.0 um without astigmatism, SNR 0.1, origins within
@@ -644,12 +684,16 @@ def main():
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--ref-seconds", type=float, default=15.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--profile-case", choices=["learned", "exhaustive-bf16", "exhaustive-fp8", "fp32"],
+                    default=None, help="instead of the bench line: a small case for profiler captures")
     ap.add_argument("--precision-report", type=int, default=0, metavar="P",
                     help="instead of the bench line: BF16 and FP8 contraction against FP64 scores and the "
                          "exhaustive FP32 search on P particles of the box-128 configuration (0.5-degree grid)")
     args = ap.parse_args()
     if args.precision_report:
         return run_precision_report(args)
+    if args.profile_case:
+        return run_profile_case(args)
     if args.searchstep:
         WORKLOAD["searchstep"] = args.searchstep
     if args.origin_step:

@@ -231,11 +231,13 @@ struct LearnModel {
     DBuf<float> feat, a1, a2, p2, a3, p3, a4, p4, g, sc, dsc, dg, dp4, da4, dp3, da3, dp2, da2, da1, loss, truth;
     DBuf<int> cell;
     DBuf<float> cellv;
+    DBuf<float2> hscr;  // the head's frequency-domain scratch
     void release() {
         for (DBuf<float>* b : {&w, &gr, &m, &v, &vview, &wflip, &feat, &a1, &a2, &p2, &a3, &p3, &a4, &p4, &g, &sc,
                                &dsc, &dg, &dp4, &da4, &dp3, &da3, &dp2, &da2, &da1, &loss, &truth, &cellv})
             b->release();
         cell.release();
+        hscr.release();
         ready = false;
         cap = 0;
     }
@@ -1014,7 +1016,7 @@ int learn_activations(Ctx* c, int B) {
         (r = L.da3.ensure(b * LP_C3 * (LP_NR / 2) * P)) || (r = L.dp2.ensure(b * LP_C2 * (LP_NR / 2) * P)) ||
         (r = L.da2.ensure(b * LP_C2 * LP_NR * P)) || (r = L.da1.ensure(b * LP_C1 * LP_NR * P)) ||
         (r = L.loss.ensure(b)) || (r = L.truth.ensure(4 * b)) || (r = L.cell.ensure(b * 64)) ||
-        (r = L.cellv.ensure(b * 64)))
+        (r = L.cellv.ensure(b * 64)) || (r = L.hscr.ensure((size_t)lp_head_scratch(B, L.V))))
         return r;
     L.cap = B;
     L.capV = L.V;
@@ -1034,7 +1036,7 @@ int learn_forward(Ctx* c, int B) {
     CK(launch_lp_conv3(L.p3.p, B, LP_C3, LP_NR / 4, w + L.oW[3], w + L.ob[3], LP_C4, true, L.a4.p, st));
     launch_lp_pool(L.a4.p, B, LP_C4, LP_NR / 8, L.p4.p, st);
     launch_lp_mix(L.p4.p, B, w + L.oW[4], w + L.ob[4], L.g.p, st);
-    CK(launch_lp_head(L.g.p, w + L.oT, B, L.V, L.sc.p, st));
+    CK(launch_lp_head(L.g.p, w + L.oT, B, L.V, L.sc.p, L.hscr.p, st));
     return CRYOIM_OK;
 }
 
@@ -1047,7 +1049,7 @@ int learn_backward(Ctx* c, int B) {
     const long nt = LP_NT;
     CK(cudaMemsetAsync(gr, 0, sizeof(float) * L.nparam, st));
     launch_lp_loss(L.sc.p, B, L.V, L.vview.p, L.truth.p, 2.0f * c->p.searchstep, 1.0f, L.dsc.p, L.loss.p, st);
-    launch_lp_head_grad(L.g.p, w + L.oT, L.dsc.p, B, L.V, L.dg.p, gr + L.oT, st);
+    launch_lp_head_grad(L.g.p, w + L.oT, L.dsc.p, B, L.V, L.dg.p, gr + L.oT, L.hscr.p, st);
     launch_lp_mix_grad(L.p4.p, L.dg.p, B, w + L.oW[4], L.dp4.p, gr + L.oW[4], gr + L.ob[4], st);
     // layer 4
     launch_lp_pool_grad(L.dp4.p, B, LP_C4, LP_NR / 8, L.da4.p, st);

@@ -121,12 +121,31 @@ __global__ void k_particle_norm(const float2* __restrict__ band, const float* __
     if (threadIdx.x == 0) norm[p] = acc;
 }
 
+// The origin phase exp(i 2pi/n (sx hx + sy ky)) of a row of A is separable: the block
+// tabulates (cos, sin) of 2pi/n sx hx for hx in [0, R] and of 2pi/n sy ky for ky in
+// [-R, R] (3R + 2 entries in shared memory) and multiplies the two per sample.
+__device__ __forceinline__ void origin_phasors(float sx, float sy, int R, float two_pi_over_n, float2* tab) {
+    for (int i = threadIdx.x; i < 3 * R + 2; i += blockDim.x) {
+        const float a = i <= R ? two_pi_over_n * (sx * (float)i) : two_pi_over_n * (sy * (float)(i - 2 * R - 1));
+        float sn, cs;
+        sincosf(a, &sn, &cs);
+        tab[i] = make_float2(cs, sn);
+    }
+    __syncthreads();
+}
+__device__ __forceinline__ void phasor_at(const float2* tab, int R, int2 hk, float* sn, float* cs) {
+    const float2 ex = tab[hk.x], ey = tab[R + 1 + R + hk.y];
+    *cs = ex.x * ey.x - ex.y * ey.y;
+    *sn = ex.y * ey.x + ex.x * ey.y;
+}
+
 // Row (p, o) of A: CTF x particle x origin phase ramp, unit norm, BF16.
 __global__ void __launch_bounds__(256) k_build_a(const float2* __restrict__ band, const float* __restrict__ ctf,
                                                  Band bd, const int2* __restrict__ samples, int S, int Kpad,
                                                  const float* __restrict__ origins, int O,
                                                  const double* __restrict__ norm, float two_pi_over_n,
                                                  __nv_bfloat162* __restrict__ A) {
+    extern __shared__ float2 ptab[];
     const int o = blockIdx.x, p = blockIdx.y, W = bd.W, R = bd.max_r;
     const float2* b = band + (long)p * W * W;
     const float* c = ctf ? ctf + (long)p * W * W : nullptr;
@@ -134,6 +153,7 @@ __global__ void __launch_bounds__(256) k_build_a(const float2* __restrict__ band
     const float sx = origins[2 * o] + h, sy = origins[2 * o + 1] + h;
     const float inv = norm[p] > 0.0 ? (float)(1.0 / sqrt(norm[p])) : 0.0f;
     __nv_bfloat162* row = A + ((long)p * O + o) * (Kpad / 2);
+    origin_phasors(sx, sy, R, two_pi_over_n, ptab);
     for (int i = threadIdx.x; i < Kpad / 2; i += blockDim.x) {
         float re = 0.f, im = 0.f;
         if (i < S) {
@@ -141,7 +161,7 @@ __global__ void __launch_bounds__(256) k_build_a(const float2* __restrict__ band
             const int q = (hk.y + R) * W + (hk.x + R);
             const float2 ab = b[q];  // (a, b) = (Re F, -Im F) referenced to pixel 0
             float sn, cs;
-            sincosf(two_pi_over_n * (sx * (float)hk.x + sy * (float)hk.y), &sn, &cs);
+            phasor_at(ptab, R, hk, &sn, &cs);
             // centshift: (a', b') = (a cos + b sin, -a sin + b cos); P = a' - i b'
             const float a2 = ab.x * cs + ab.y * sn, b2 = -ab.x * sn + ab.y * cs;
             const float cv = (c ? c[q] : 1.0f) * inv;
@@ -464,6 +484,7 @@ __global__ void __launch_bounds__(256) k_build_a8(const float2* __restrict__ ban
                                                   const double* __restrict__ norm, const float* __restrict__ mulA,
                                                   const int* __restrict__ fexp, float two_pi_over_n,
                                                   unsigned short* __restrict__ A8) {
+    extern __shared__ float2 ptab[];
     const int o = blockIdx.x, p = blockIdx.y, W = bd.W, R = bd.max_r;
     const float2* b = band + (long)p * W * W;
     const float* c = ctf ? ctf + (long)p * W * W : nullptr;
@@ -472,6 +493,7 @@ __global__ void __launch_bounds__(256) k_build_a8(const float2* __restrict__ ban
     const float inv = norm[p] > 0.0 ? (float)(1.0 / sqrt(norm[p])) : 0.0f;
     const float pscale = ldexpf(1.0f, fexp[p]);
     unsigned short* row = A8 + ((long)p * O + o) * (Kpad8 / 2);
+    origin_phasors(sx, sy, R, two_pi_over_n, ptab);
     for (int i = threadIdx.x; i < Kpad8 / 2; i += blockDim.x) {
         float re = 0.f, im = 0.f;
         if (i < S) {
@@ -479,7 +501,7 @@ __global__ void __launch_bounds__(256) k_build_a8(const float2* __restrict__ ban
             const int q = (hk.y + R) * W + (hk.x + R);
             const float2 ab = b[q];
             float sn, cs;
-            sincosf(two_pi_over_n * (sx * (float)hk.x + sy * (float)hk.y), &sn, &cs);
+            phasor_at(ptab, R, hk, &sn, &cs);
             const float a2 = ab.x * cs + ab.y * sn, b2 = -ab.x * sn + ab.y * cs;
             const float cv = (c ? c[q] : 1.0f) * inv * mulA[i] * pscale;
             re = a2 * cv;
@@ -535,7 +557,8 @@ void launch_build_a8(const float2* band, const float* ctf, Band bd, const int2* 
     k_particle_exp8<<<B, 256, 0, st>>>(band, ctf, bd, samples, S, norm, mulA, fexp);
     dim3 g(O, B);
     const float tpn = 2.0f * host_angles().pi / (float)bd.nx;
-    k_build_a8<<<g, 256, 0, st>>>(band, ctf, bd, samples, S, Kpad8, origins, O, norm, mulA, fexp, tpn,
+    k_build_a8<<<g, 256, sizeof(float2) * (3 * bd.max_r + 2), st>>>(band, ctf, bd, samples, S, Kpad8, origins, O,
+                                                                     norm, mulA, fexp, tpn,
                                   (unsigned short*)A8);
 }
 
@@ -603,7 +626,8 @@ void launch_build_a(const float2* band, const float* ctf, Band bd, const int2* s
                     const float* origins, int O, const double* norm, int B, void* A, cudaStream_t st) {
     dim3 g(O, B);
     const float tpn = 2.0f * host_angles().pi / (float)bd.nx;
-    k_build_a<<<g, 256, 0, st>>>(band, ctf, bd, samples, S, Kpad, origins, O, norm, tpn,
+    k_build_a<<<g, 256, sizeof(float2) * (3 * bd.max_r + 2), st>>>(band, ctf, bd, samples, S, Kpad, origins, O,
+                                                                    norm, tpn,
                                  (__nv_bfloat162*)A);
 }
 

@@ -210,9 +210,12 @@ void launch_lp_pool_grad(const float* dp, int B, int C, int Hout, float* da, cud
 void launch_lp_mix(const float* x, int B, const float* W5, const float* b5, float* g, cudaStream_t st);
 void launch_lp_mix_grad(const float* x, const float* dg, int B, const float* W5, float* dx, float* dW5, float* db5,
                         cudaStream_t st);
-cudaError_t launch_lp_head(const float* g, const float* T, int B, int V, float* sc, cudaStream_t st);
+// the head through 128-point real transforms; scratch of lp_head_scratch(B, V) float2,
+// kept between a forward and its backward
+long lp_head_scratch(int B, int V);
+cudaError_t launch_lp_head(const float* g, const float* T, int B, int V, float* sc, float2* scratch, cudaStream_t st);
 void launch_lp_head_grad(const float* g, const float* T, const float* dsc, int B, int V, float* dg, float* dT,
-                         cudaStream_t st);
+                         float2* scratch, cudaStream_t st);
 // truth[b] = (view unit vector x, y, z, shift); sv degrees, ss shifts
 void launch_lp_loss(const float* sc, int B, int V, const float* vview, const float* truth, float sv, float ss,
                     float* dsc, float* loss, cudaStream_t st);

@@ -18,6 +18,7 @@
 // next to the contraction it feeds.
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <cstdint>
 
 #include "geom.cuh"
@@ -438,110 +439,121 @@ __global__ void __launch_bounds__(256) k_mix_dw(const float* __restrict__ x, con
     }
 }
 
-// Head: sc[b][v][s] = sum_{c,t} g[b][c][(t + s) % NT] T[v][c][t].  Block (8 views, b),
-// 64 threads, each two shifts (s, s + 64) x 8 views; g doubled in shared memory so the
-// circular index needs no modulo; the 8 views' templates interleaved [c][t][8].
-constexpr int HV = 8;
-__global__ void __launch_bounds__(64) k_head(const float* __restrict__ g, const float* __restrict__ T, int V,
-                                            float* __restrict__ sc) {
-    extern __shared__ float hsm[];
-    float* sg = hsm;               // [CM][2 NT]
-    float* sT = hsm + CM * 2 * NT;  // [CM][NT][HV]
-    const int b = blockIdx.y, v0 = blockIdx.x * HV, s = threadIdx.x;
-    for (int q = s; q < CM * NT; q += 64) {
-        const float v = g[(long)b * CM * NT + q];
-        const int c = q / NT, t = q % NT;
-        sg[c * 2 * NT + t] = v;
-        sg[c * 2 * NT + t + NT] = v;
+// Head in the frequency domain.  With X^(f) = sum_t x(t) e^{-2 pi i f t / NT} (the real
+// transform, f = 0 .. NT/2), the circular correlation sc(s) = sum_t g(t + s) T(t) has
+// the transform G^(f) conj(T^(f)); its gradients are dT(t) <-> sum_b conj(D^(f)) G^(f)
+// and dg(u) <-> sum_v D^(f) T^(f), D = the transform of dsc over s.  Transforms are
+// 128-point sums against a twiddle table (NT^2 / 2 operations each, a few per particle
+// and view), products over the NT / 2 + 1 frequencies.
+constexpr int NF = NT / 2 + 1;
+
+__device__ __forceinline__ void twiddles(float2* tw) {
+    for (int k = threadIdx.x; k < NT; k += blockDim.x) {
+        float sn, cs;
+        sincospif(2.0f * (float)k / (float)NT, &sn, &cs);
+        tw[k] = make_float2(cs, sn);
     }
-    for (int q = s; q < HV * CM * NT; q += 64) {
-        const int j = q / (CM * NT), ct = q % (CM * NT);
-        sT[ct * HV + j] = (v0 + j < V) ? T[(long)(v0 + j) * CM * NT + ct] : 0.f;
-    }
-    __syncthreads();
-    float a0[HV], a1[HV];
-#pragma unroll
-    for (int j = 0; j < HV; ++j) { a0[j] = 0.f; a1[j] = 0.f; }
-    for (int c = 0; c < CM; ++c) {
-        const float* gr = sg + c * 2 * NT;
-        const float4* tr = reinterpret_cast<const float4*>(sT + c * NT * HV);
-#pragma unroll 4
-        for (int t = 0; t < NT; ++t) {
-            const float g0 = gr[t + s], g1 = gr[t + s + 64];
-            const float4 ta = tr[2 * t], tb = tr[2 * t + 1];
-            const float tv[HV] = {ta.x, ta.y, ta.z, ta.w, tb.x, tb.y, tb.z, tb.w};
-#pragma unroll
-            for (int j = 0; j < HV; ++j) {
-                a0[j] = fmaf(g0, tv[j], a0[j]);
-                a1[j] = fmaf(g1, tv[j], a1[j]);
+}
+
+// X[r][f] = sum_t x[r][t] e^{-2 pi i f t / NT} for rows r < n; block of NT threads,
+// rows in a grid-stride loop
+__global__ void __launch_bounds__(NT) k_rdft(const float* __restrict__ x, long n, float2* __restrict__ X) {
+    __shared__ float2 tw[NT];
+    __shared__ float sx[NT];
+    twiddles(tw);
+    for (long r = blockIdx.x; r < n; r += gridDim.x) {
+        __syncthreads();
+        sx[threadIdx.x] = x[r * NT + threadIdx.x];
+        __syncthreads();
+        const int f = threadIdx.x;
+        if (f < NF) {
+            float re = 0.f, im = 0.f;
+            for (int t = 0; t < NT; ++t) {
+                const float2 w = tw[(f * t) & (NT - 1)];
+                re = fmaf(sx[t], w.x, re);
+                im = fmaf(-sx[t], w.y, im);
             }
+            X[r * NF + f] = make_float2(re, im);
         }
     }
-#pragma unroll
-    for (int j = 0; j < HV; ++j)
-        if (v0 + j < V) {
-            sc[((long)b * V + v0 + j) * NT + s] = a0[j];
-            sc[((long)b * V + v0 + j) * NT + s + 64] = a1[j];
-        }
 }
 
-// dT[v][c][t] = sum_b sum_s dsc[b][v][s] g[b][c][(t + s) % NT].  Block per view, thread t.
-__global__ void __launch_bounds__(NT) k_head_dT(const float* __restrict__ g, const float* __restrict__ dsc, int B,
-                                               int V, float* __restrict__ dT) {
-    __shared__ float sg[CM][2 * NT];
-    __shared__ float sd[NT];
-    const int v = blockIdx.x, t = threadIdx.x;
-    float acc[CM];
-#pragma unroll
-    for (int c = 0; c < CM; ++c) acc[c] = 0.f;
-    for (int b = 0; b < B; ++b) {
+// x[r][t] = (1/NT) sum over all f of X e^{+2 pi i f t / NT} for Hermitian spectra given
+// on f = 0 .. NT/2; beta: x = inverse + beta * x (0 or 1)
+__global__ void __launch_bounds__(NT) k_irdft(const float2* __restrict__ X, long n, float* __restrict__ x) {
+    __shared__ float2 tw[NT];
+    __shared__ float2 sX[NF];
+    twiddles(tw);
+    const float inv = 1.0f / (float)NT;
+    for (long r = blockIdx.x; r < n; r += gridDim.x) {
         __syncthreads();
-        sd[t] = dsc[((long)b * V + v) * NT + t];
-#pragma unroll
-        for (int c = 0; c < CM; ++c) {
-            const float x = g[((long)b * CM + c) * NT + t];
-            sg[c][t] = x;
-            sg[c][t + NT] = x;
-        }
+        if (threadIdx.x < NF) sX[threadIdx.x] = X[r * NF + threadIdx.x];
         __syncthreads();
-        for (int s = 0; s < NT; ++s) {
-            const float d = sd[s];
-#pragma unroll
-            for (int c = 0; c < CM; ++c) acc[c] = fmaf(d, sg[c][t + s], acc[c]);
+        const int t = threadIdx.x;
+        float acc = sX[0].x + ((t & 1) ? -sX[NT / 2].x : sX[NT / 2].x);
+        float a2 = 0.f;
+        for (int f = 1; f < NT / 2; ++f) {
+            const float2 w = tw[(f * t) & (NT - 1)];
+            a2 = fmaf(sX[f].x, w.x, a2);
+            a2 = fmaf(-sX[f].y, w.y, a2);
         }
+        x[r * NT + t] = (acc + 2.0f * a2) * inv;
     }
-#pragma unroll
-    for (int c = 0; c < CM; ++c) dT[((long)v * CM + c) * NT + t] = acc[c];
 }
 
-// dg[b][c][u] = sum_v sum_s dsc[b][v][s] T[v][c][(u - s) % NT].  Block per particle, thread u.
-__global__ void __launch_bounds__(NT) k_head_dg(const float* __restrict__ T, const float* __restrict__ dsc, int V,
-                                               float* __restrict__ dg) {
-    __shared__ float sT[CM][2 * NT];
-    __shared__ float sd[NT];
-    const int b = blockIdx.x, u = threadIdx.x;
-    float acc[CM];
-#pragma unroll
-    for (int c = 0; c < CM; ++c) acc[c] = 0.f;
-    for (int v = 0; v < V; ++v) {
-        __syncthreads();
-        sd[u] = dsc[((long)b * V + v) * NT + u];
+// Xs[b][v][f] = sum_c G[b][c][f] conj(TT[v][c][f])
+__global__ void k_head_prod(const float2* __restrict__ G, const float2* __restrict__ TT, int B, int V,
+                            float2* __restrict__ Xs) {
+    const long n = (long)B * V * NF;
+    for (long q = (long)blockIdx.x * blockDim.x + threadIdx.x; q < n; q += (long)gridDim.x * blockDim.x) {
+        const int f = (int)(q % NF);
+        const long bv = q / NF;
+        const int v = (int)(bv % V), b = (int)(bv / V);
+        float re = 0.f, im = 0.f;
 #pragma unroll
         for (int c = 0; c < CM; ++c) {
-            const float x = T[((long)v * CM + c) * NT + u];
-            sT[c][u] = x;
-            sT[c][u + NT] = x;
+            const float2 g = G[((long)b * CM + c) * NF + f], t = TT[((long)v * CM + c) * NF + f];
+            re = fmaf(g.x, t.x, fmaf(g.y, t.y, re));
+            im = fmaf(g.y, t.x, fmaf(-g.x, t.y, im));
         }
-        __syncthreads();
-        // T[(u - s) mod NT] = sT[u - s + NT]
-        for (int s = 0; s < NT; ++s) {
-            const float d = sd[s];
-#pragma unroll
-            for (int c = 0; c < CM; ++c) acc[c] = fmaf(d, sT[c][u - s + NT], acc[c]);
-        }
+        Xs[q] = make_float2(re, im);
     }
-#pragma unroll
-    for (int c = 0; c < CM; ++c) dg[((long)b * CM + c) * NT + u] = acc[c];
+}
+
+// dTT[v][c][f] = sum_b conj(D[b][v][f]) G[b][c][f]
+__global__ void k_head_dTT(const float2* __restrict__ D, const float2* __restrict__ G, int B, int V,
+                           float2* __restrict__ dTT) {
+    const long n = (long)V * CM * NF;
+    for (long q = (long)blockIdx.x * blockDim.x + threadIdx.x; q < n; q += (long)gridDim.x * blockDim.x) {
+        const int f = (int)(q % NF);
+        const long vc = q / NF;
+        const int c = (int)(vc % CM), v = (int)(vc / CM);
+        float re = 0.f, im = 0.f;
+        for (int b = 0; b < B; ++b) {
+            const float2 d = D[((long)b * V + v) * NF + f], g = G[((long)b * CM + c) * NF + f];
+            re = fmaf(d.x, g.x, fmaf(d.y, g.y, re));
+            im = fmaf(d.x, g.y, fmaf(-d.y, g.x, im));
+        }
+        dTT[q] = make_float2(re, im);
+    }
+}
+
+// dG[b][c][f] = sum_v D[b][v][f] TT[v][c][f]
+__global__ void k_head_dG(const float2* __restrict__ D, const float2* __restrict__ TT, int B, int V,
+                          float2* __restrict__ dG) {
+    const long n = (long)B * CM * NF;
+    for (long q = (long)blockIdx.x * blockDim.x + threadIdx.x; q < n; q += (long)gridDim.x * blockDim.x) {
+        const int f = (int)(q % NF);
+        const long bc = q / NF;
+        const int c = (int)(bc % CM), b = (int)(bc / CM);
+        float re = 0.f, im = 0.f;
+        for (int v = 0; v < V; ++v) {
+            const float2 d = D[((long)b * V + v) * NF + f], t = TT[((long)v * CM + c) * NF + f];
+            re = fmaf(d.x, t.x, fmaf(-d.y, t.y, re));
+            im = fmaf(d.x, t.y, fmaf(d.y, t.x, im));
+        }
+        dG[q] = make_float2(re, im);
+    }
 }
 
 // Soft-target cross entropy over the V x NT cells of each particle.  truth[b] = (view
@@ -700,18 +712,35 @@ void launch_lp_mix_grad(const float* x, const float* dg, int B, const float* W5,
     if (dx) k_mix_dx<<<B, NT, 0, st>>>(dg, W5, dx);
     k_mix_dw<<<LP_MIXK, 256, 0, st>>>(x, dg, B, dW5, db5);
 }
-cudaError_t launch_lp_head(const float* g, const float* T, int B, int V, float* sc, cudaStream_t st) {
-    const int sm = (int)(sizeof(float) * (CM * 2 * NT + HV * CM * NT));
-    cudaError_t e = cudaFuncSetAttribute(k_head, cudaFuncAttributeMaxDynamicSharedMemorySize, sm);
-    if (e != cudaSuccess) return e;
-    dim3 grid(cdiv(V, HV), B);
-    k_head<<<grid, 64, sm, st>>>(g, T, V, sc);
+long lp_head_scratch(int B, int V) { return (long)NF * (2L * B * CM + 2L * V * CM + 2L * B * V); }
+
+// scratch (float2): G [B][CM][NF], TT [V][CM][NF], X [B][V][NF], then the backward's
+// D [B][V][NF], dTT [V][CM][NF], dG [B][CM][NF] reuse the same layout
+cudaError_t launch_lp_head(const float* g, const float* T, int B, int V, float* sc, float2* scratch, cudaStream_t st) {
+    float2* G = scratch;
+    float2* TT = G + (long)B * CM * NF;
+    float2* X = TT + (long)V * CM * NF;
+    const int gmax = 152 * 16;
+    k_rdft<<<(int)std::min<long>((long)B * CM, gmax), NT, 0, st>>>(g, (long)B * CM, G);
+    k_rdft<<<(int)std::min<long>((long)V * CM, gmax), NT, 0, st>>>(T, (long)V * CM, TT);
+    k_head_prod<<<grid_for((long)B * V * NF, 256), 256, 0, st>>>(G, TT, B, V, X);
+    k_irdft<<<(int)std::min<long>((long)B * V, gmax), NT, 0, st>>>(X, (long)B * V, sc);
     return cudaGetLastError();
 }
 void launch_lp_head_grad(const float* g, const float* T, const float* dsc, int B, int V, float* dg, float* dT,
-                         cudaStream_t st) {
-    k_head_dT<<<V, NT, 0, st>>>(g, dsc, B, V, dT);
-    k_head_dg<<<B, NT, 0, st>>>(T, dsc, V, dg);
+                         float2* scratch, cudaStream_t st) {
+    // G and TT from the forward are still in the scratch
+    float2* G = scratch;
+    float2* TT = G + (long)B * CM * NF;
+    float2* D = TT + (long)V * CM * NF;  // over X
+    float2* dTT = D + (long)B * V * NF;
+    float2* dG = dTT + (long)V * CM * NF;
+    const int gmax = 152 * 16;
+    k_rdft<<<(int)std::min<long>((long)B * V, gmax), NT, 0, st>>>(dsc, (long)B * V, D);
+    k_head_dTT<<<grid_for((long)V * CM * NF, 128), 128, 0, st>>>(D, G, B, V, dTT);
+    k_head_dG<<<grid_for((long)B * CM * NF, 128), 128, 0, st>>>(D, TT, B, V, dG);
+    k_irdft<<<(int)std::min<long>((long)V * CM, gmax), NT, 0, st>>>(dTT, (long)V * CM, dT);
+    k_irdft<<<(int)std::min<long>((long)B * CM, gmax), NT, 0, st>>>(dG, (long)B * CM, dg);
 }
 void launch_lp_loss(const float* sc, int B, int V, const float* vview, const float* truth, float sv, float ss,
                     float* dsc, float* loss, cudaStream_t st) {
