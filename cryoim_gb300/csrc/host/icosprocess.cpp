@@ -14,8 +14,12 @@
 // Extension keys without a reference counterpart: device, batch (particles per device
 // call), contract=y (mode 4 through the tensor-core contraction), originmax,
 // originstep, topk, precision=bf16|fp8 (contraction operands), nbr (rescoring
-// neighbourhood in grid steps).  Output rows are appended after every chunk, so a run
-// can resume with first=k as with the reference's per-particle writes.
+// neighbourhood in grid steps), nbrbest (rescore only the neighbourhoods of the best k
+// candidates), coarse=k (coarse-contraction proposals), learned=k (proposals of the
+// learned proposer: loaded from learnmodel=file if it exists, else trained on
+// learnsamples projections of model3d and saved there).  Output rows are appended after
+// every chunk, so a run can resume with first=k as with the reference's per-particle
+// writes.
 #include <algorithm>
 #include <cmath>
 #include <cstdio>
@@ -37,7 +41,7 @@ const char* kKeys[] = {"apix",         "minRes",       "maxRes",     "imgmask", 
                        "imgstck",      "sym",          "maxcentshift", "corrCTF",  "boundX",
                        "loc_box",      "check"};
 const char* kExt[] = {"device", "batch", "contract", "originmax", "originstep", "topk", "precision", "nbr",
-                      "coarse"};
+                      "coarse", "nbrbest", "learned", "learnmodel", "learnsamples"};
 
 void usage() {
     std::puts(
@@ -51,7 +55,8 @@ void usage() {
         "         searchstep, minRes, maxRes, applyCTF, vol, Cs, ampwg)\n"
         "  mode=5 local refinement into newortfile (Ncycle, templateort, ...)\n"
         "  common: apix imgmask first last imgstck\n"
-        "  GPU extensions: device batch contract=y originmax originstep topk precision=bf16|fp8 nbr");
+        "  GPU extensions: device batch contract=y originmax originstep topk precision=bf16|fp8 nbr nbrbest\n"
+        "                  coarse learned learnmodel learnsamples");
 }
 
 bool yes(const std::string& v) { return !v.empty() && (v[0] == 'y' || v[0] == 'Y'); }
@@ -247,10 +252,29 @@ int main(int argc, char** argv) {
         if (cryoim_load_templates(ctx, timg.data(), t.data(), T)) return die("templates", 2);
         const bool contract = mode == 4 && yes(sval("contract", "n"));
         cryoim_contract_opts co{fval("originmax", 6.0f), fval("originstep", 0.5f), ival("topk", 16), 0,
-                                sval("precision", "bf16") == "fp8" ? 1 : 0, ival("nbr", 1), ival("coarse", 0)};
+                                sval("precision", "bf16") == "fp8" ? 1 : 0, ival("nbr", 1), ival("coarse", 0),
+                                ival("learned", 0), ival("nbrbest", 0)};
         if (contract) {
             if (map.empty()) return die("contract=y needs model3d", 2);
             if (cryoim_set_reference_map(ctx, map.data())) return die("reference map", 2);
+            if (co.learned > 0) {
+                const std::string model = sval("learnmodel", "proposer.bin");
+                std::FILE* f = std::fopen(model.c_str(), "rb");
+                if (f) {
+                    std::fclose(f);
+                    if (cryoim_learn_load(ctx, model.c_str())) return die("learnmodel", 2);
+                } else {
+                    cryoim_learn_opts lo;
+                    cryoim_learn_opts_default(&lo);
+                    lo.samples = ival("learnsamples", 25600);
+                    lo.origin_max = co.origin_max;
+                    float st[4];
+                    if (cryoim_learn_train(ctx, map.data(), &lo, st)) return die("proposer training", 2);
+                    std::printf("proposer: %d views, trained on %d projections in %.1f s (loss %.3f)\n",
+                                (int)st[3], lo.samples, st[1], st[0]);
+                    if (cryoim_learn_save(ctx, model.c_str())) return die("learnmodel write", 2);
+                }
+            }
         }
         const std::string out = sval("newortfile", "newort.dat");
         std::FILE* trunc = std::fopen(out.c_str(), "w");
