@@ -328,6 +328,7 @@ struct Ctx {
     DBuf<float2> xalpha, sband;
     DBuf<int> xcount;
     DBuf<double> kpart;
+    DBuf<float2> tbandc;
     DBuf<GemmGroup> ggroups;
     DBuf<int2> gseg;
     LearnModel lm;
@@ -356,7 +357,7 @@ struct Ctx {
         csamples_c.release(); bmat_c.release(); amat_c.release(); corigins_c.release(); topv_c.release();
         tilev_c.release(); kcc_c.release(); topi_c.release(); tileo_c.release(); tileorig_c.release();
         kor_c.release(); korig_c.release(); gidx.release(); pnorm_c.release(); bgather.release();
-        sband.release(); xcount.release(); kpart.release(); ggroups.release(); gseg.release();
+        sband.release(); xcount.release(); kpart.release(); ggroups.release(); gseg.release(); tbandc.release();
         lm.release();
         if (pe0) cudaEventDestroy(pe0);
         if (pe1) cudaEventDestroy(pe1);
@@ -1456,7 +1457,7 @@ int contract_impl(Ctx* c, const float* imgs, bool on_device, cryoim_particle* pa
         (r = c->xpr.ensure((size_t)PB * maxx)))
         return r;
     if (T > 0 && ((r = c->xalpha.ensure((size_t)PB * maxx * T * 60)) || (r = c->sband.ensure((size_t)PB * w2)) ||
-                  (r = c->xcount.ensure(PB))))
+                  (r = c->xcount.ensure(PB)) || (c->p.apply_ctf && (r = c->tbandc.ensure((size_t)PB * T * w2)))))
         return r;
     if (c->num_sms == 0) CK(cudaDeviceGetAttribute(&c->num_sms, cudaDevAttrMultiProcessorCount, c->device));
     std::vector<int> src(P);
@@ -1702,6 +1703,7 @@ int contract_impl(Ctx* c, const float* imgs, bool on_device, cryoim_particle* pa
             a.band = c->band.p; a.fcut0 = c->fcut0.p; a.tband = c->tband.p; a.tfcut = tfc;
             a.tfcut_pstride = tfs; a.ctf = ctfp; a.cand = c->xcand.p; a.alpha = c->xalpha.p; a.T = T;
             a.bd = c->bd; a.pr = c->xpr.p; a.ncand = maxc; a.sband = c->sband.p; a.ncount = c->xcount.p;
+            a.tbandc = ctfp ? c->tbandc.p : nullptr;
             CK(launch_pr_single(a, nb, c->stream));
             std::vector<float> h((size_t)nb * maxc);
             CK(cudaMemcpyAsync(h.data(), c->xpr.p, sizeof(float) * h.size(), cudaMemcpyDeviceToHost, c->stream));
@@ -1711,6 +1713,8 @@ int contract_impl(Ctx* c, const float* imgs, bool on_device, cryoim_particle* pa
             return CRYOIM_OK;
         };
         if (T > 0) {
+            // the templates under each particle's CTF, once per pass
+            if (ctfp) CK(launch_tband_ctf(c->tband.p, T, ctfp, c->bd, nb, c->tbandc.p, c->stream));
             if (nbest <= 0 || nbest >= k) {
                 for (int i = 0; i < nb; ++i) {
                     for (int rr = 0; rr < k; ++rr)

@@ -102,8 +102,11 @@ struct PrSingleArgs {
     int ncand = 11;          // 11 for the refinement step (ort_cent_11.f90)
     const float2* sband = nullptr;  // [B][W*W] band shifted to the candidates' common origin, or nullptr
     const int* ncount = nullptr;    // [B] candidates in use (later slots are skipped), or nullptr
+    const float2* tbandc = nullptr; // with sband: [B][T][W*W] templates x CTF (launch_tband_ctf), or nullptr
 };
 cudaError_t launch_pr_single(const PrSingleArgs& a, int B, cudaStream_t st);
+cudaError_t launch_tband_ctf(const float2* tband, int T, const float* ctf, const Band& bd, int B, float2* out,
+                             cudaStream_t st);
 // sband for PrSingleArgs: the band of each particle shifted to cand[p][0]'s origin
 cudaError_t launch_shift_band(const float2* band, const float* cand, int ncand, const Band& bd, int B,
                               float2* out, cudaStream_t st);

@@ -224,6 +224,8 @@ template <bool SHIFTED>
 __global__ void __launch_bounds__(512) k_pr_single(PrSingleArgs a, Consts K) {
     __shared__ double sh[2][32];
     __shared__ float sline[4][60];  // cos, sin of the particle line; cos, sin of the template line
+    __shared__ int svalid[60];
+    __shared__ float sfc[2][256];   // SHIFTED: the particle's and the template's amplitude cuts
     const Band bd = a.bd;
     const int W = bd.W, nr = bd.nr, minR = bd.min_r, nx = bd.nx;
     const int c = blockIdx.x, p = blockIdx.y;
@@ -240,15 +242,21 @@ __global__ void __launch_bounds__(512) k_pr_single(PrSingleArgs a, Consts K) {
     const float twopi = __fmul_rn(2.0f, K.pi);
     double p1 = 0.0, p2 = 0.0;
     float f1 = 0.f, f2 = 0.f, k1 = 0.f, k2 = 0.f;
+    if (SHIFTED)
+        for (int q = threadIdx.x; q < nr; q += blockDim.x) sfc[0][q] = fc0[q];
     for (int i = 0; i < a.T; ++i) {
         const float2* al = a.alpha + (((long)p * a.ncand + c) * a.T + i) * 60;
         const float2* tb = a.tband + (long)i * W * W;
         const float* fct = tfc + (long)i * nr;
+        // SHIFTED: the templates already multiplied by this particle's CTF
+        const float2* tbc = SHIFTED && a.tbandc ? a.tbandc + ((long)p * a.T + i) * W * W : nullptr;
         // the two in-plane directions of each common line, once per line
         __syncthreads();
         if (threadIdx.x < 60) {
             const float2 aa = al[threadIdx.x];
-            if (aa.x < 999.0f && aa.y < 999.0f) {
+            const bool ok = aa.x < 999.0f && aa.y < 999.0f;
+            svalid[threadIdx.x] = ok;
+            if (ok) {
                 const float a1 = __fmul_rn(aa.x, K.d2r), a2 = __fmul_rn(aa.y, K.d2r);
                 sline[0][threadIdx.x] = cosf(a1);
                 sline[1][threadIdx.x] = sinf(a1);
@@ -256,11 +264,12 @@ __global__ void __launch_bounds__(512) k_pr_single(PrSingleArgs a, Consts K) {
                 sline[3][threadIdx.x] = sinf(a2);
             }
         }
+        if (SHIFTED)
+            for (int q = threadIdx.x; q < nr; q += blockDim.x) sfc[1][q] = fct[q];
         __syncthreads();
         for (int q = threadIdx.x; q < 60 * nr; q += blockDim.x) {
             int j = q / nr, iq = q - j * nr;
-            float2 aa = al[j];
-            if (!(aa.x < 999.0f && aa.y < 999.0f)) continue;
+            if (!svalid[j]) continue;
             const float fr = (float)(minR + iq);
             // particle sample with the candidate origin shift on each tap
             float cs = sline[0][j], sn = sline[1][j];
@@ -293,10 +302,14 @@ __global__ void __launch_bounds__(512) k_pr_single(PrSingleArgs a, Consts K) {
             float re1 = bilerp(ax, ay, tr[0], tr[1], tr[2], tr[3]);
             float im1 = bilerp(ax, ay, ti[0], ti[1], ti[2], ti[3]);
             float re2, im2;
-            tmpl_sample_cs(tb, ctfp, W, offW, nxh, sline[2][j], sline[3][j], fr, &re2, &im2);
+            if (tbc)
+                tmpl_sample_cs(tbc, nullptr, W, offW, nxh, sline[2][j], sline[3][j], fr, &re2, &im2);
+            else
+                tmpl_sample_cs(tb, ctfp, W, offW, nxh, sline[2][j], sline[3][j], fr, &re2, &im2);
             float amp1 = sqrtf(re1 * re1 + im1 * im1);
             float amp2 = sqrtf(re2 * re2 + im2 * im2);
-            if (amp1 >= fc0[iq] && amp2 >= fct[iq]) {
+            const float cut1 = SHIFTED ? sfc[0][iq] : fc0[iq], cut2 = SHIFTED ? sfc[1][iq] : fct[iq];
+            if (amp1 >= cut1 && amp2 >= cut2) {
                 if (SHIFTED) {
                     const float d = angle_between(re1 * im2 - im1 * re2, re1 * re2 + im1 * im2, K.pi);
                     const float w = 0.5f * (amp1 + amp2);
@@ -458,7 +471,28 @@ cudaError_t launch_shift_band(const float2* band, const float* cand, int ncand, 
     return cudaGetLastError();
 }
 
+// out[p][i] = tband[i] x ctf[p] per band pixel (the products tmpl_sample forms per tap)
+__global__ void k_tband_ctf(const float2* __restrict__ tband, int T, const float* __restrict__ ctf, long w2,
+                            float2* __restrict__ out) {
+    const int p = blockIdx.y;
+    const long n = (long)T * w2;
+    for (long q = (long)blockIdx.x * blockDim.x + threadIdx.x; q < n; q += (long)gridDim.x * blockDim.x) {
+        const float2 t = tband[q];
+        const float c = ctf[(long)p * w2 + q % w2];
+        out[(long)p * n + q] = make_float2(__fmul_rn(t.x, c), __fmul_rn(t.y, c));
+    }
+}
+
+cudaError_t launch_tband_ctf(const float2* tband, int T, const float* ctf, const Band& bd, int B, float2* out,
+                             cudaStream_t st) {
+    const long w2 = (long)bd.W * bd.W;
+    dim3 grid((int)std::min<long>((T * w2 + 255) / 256, 4096), B);
+    k_tband_ctf<<<grid, 256, 0, st>>>(tband, T, ctf, w2, out);
+    return cudaGetLastError();
+}
+
 cudaError_t launch_pr_single(const PrSingleArgs& a, int B, cudaStream_t st) {
+    if (a.sband && a.bd.nr > 256) return cudaErrorInvalidValue;
     dim3 grid(a.ncand, B);
     if (a.sband)
         k_pr_single<true><<<grid, 512, 0, st>>>(a, consts());
