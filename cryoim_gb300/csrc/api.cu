@@ -334,6 +334,7 @@ struct Ctx {
     LearnModel lm;
     // view <-> grid slot (itheta * (2 Nphi + 1) + iphi + Nphi) maps for neighbours
     std::vector<int> view_slot, slot_view;
+    std::vector<uint8_t> list_mark;  // one byte per fine-grid orientation (expand_seeds)
     int num_sms = 0;
     // CUDA-event timing of the contraction launches (with prof)
     double prof_gemm_ms = 0.0;
@@ -898,9 +899,42 @@ int ensure_coarse(Ctx* c, float omax, float ostep) {
     return CRYOIM_OK;
 }
 
+// The fine-grid orientations within nbf steps (theta, phi, omega) of each seed (fine
+// grid theta index, signed phi index, omega index), each once, in the order first
+// reached: lists[i] for seeds[i].  One byte per grid orientation marks what a list
+// already holds (cleared after each list), so the cost is linear in the seeds.
+void expand_seeds(Ctx* c, const std::vector<std::vector<int3>>& seeds, int nbf,
+                  std::vector<std::vector<int>>& lists) {
+    const int span = 2 * c->nph + 1;
+    std::vector<uint8_t>& mark = c->list_mark;
+    if (mark.size() < (size_t)c->n_orient) mark.assign((size_t)c->n_orient, 0);
+    lists.assign(seeds.size(), std::vector<int>());
+    for (size_t i = 0; i < seeds.size(); ++i) {
+        std::vector<int>& lst = lists[i];
+        lst.reserve(seeds[i].size() * (2 * nbf + 1) * (2 * nbf + 1) * (2 * nbf + 1));
+        for (const int3& sd : seeds[i])
+            for (int dt = -nbf; dt <= nbf; ++dt)
+                for (int dp = -nbf; dp <= nbf; ++dp) {
+                    const int it2 = sd.x + dt, ips2 = sd.y + dp;
+                    if (it2 < 0 || it2 > c->nth || ips2 < -c->nph || ips2 > c->nph) continue;
+                    const int v2 = c->slot_view[(size_t)it2 * span + ips2 + c->nph];
+                    if (v2 < 0) continue;
+                    for (int dw = -nbf; dw <= nbf; ++dw) {
+                        const int n = v2 * c->nom + ((sd.z + dw) % c->nom + c->nom) % c->nom;
+                        if (!mark[n]) {
+                            mark[n] = 1;
+                            lst.push_back(n);
+                        }
+                    }
+                }
+        for (int n : lst) mark[n] = 0;
+        if (lst.empty()) lst.push_back(0);
+    }
+}
+
 // Coarse level for nb prepared particles (c->band, ctfp): the best kc distinct coarse
 // orientations of each, mapped onto the fine grid (twice the coarse indices) with their
-// fine neighbours within nbf steps in theta, phi and omega -> lists[i], sorted.
+// fine neighbours within nbf steps in theta, phi and omega -> lists[i].
 int coarse_lists(Ctx* c, int nb, const float* ctfp, int kc, int nbf, std::vector<std::vector<int>>& lists) {
     const ViewGrid& g = c->cgrid;
     const int Oc = c->n_origin_c;
@@ -931,29 +965,16 @@ int coarse_lists(Ctx* c, int nb, const float* ctfp, int kc, int nbf, std::vector
     CK(cudaMemcpyAsync(kor.data(), c->kor_c.p, sizeof(int) * nb * kc, cudaMemcpyDeviceToHost, c->stream));
     CK(cudaStreamSynchronize(c->stream));
     if (gerr) return fail(CRYOIM_ERR_CUDA, "coarse contraction wait timed out");
-    const int span_c = 2 * g.nph + 1, span = 2 * c->nph + 1;
-    lists.assign(nb, std::vector<int>());
-    for (int i = 0; i < nb; ++i) {
-        std::vector<int>& lst = lists[i];
+    const int span_c = 2 * g.nph + 1;
+    std::vector<std::vector<int3>> seeds(nb);
+    for (int i = 0; i < nb; ++i)
         for (int j = 0; j < kc; ++j) {
             const int n = kor[(size_t)i * kc + j];
             if (n < 0) continue;
             const int vc = n / g.nom, ioc = n % g.nom, slot = g.view_slot[vc];
-            const int it = 2 * (slot / span_c), ips = 2 * (slot % span_c - g.nph), io = 2 * ioc;
-            for (int dt = -nbf; dt <= nbf; ++dt)
-                for (int dp = -nbf; dp <= nbf; ++dp) {
-                    const int it2 = it + dt, ips2 = ips + dp;
-                    if (it2 < 0 || it2 > c->nth || ips2 < -c->nph || ips2 > c->nph) continue;
-                    const int v2 = c->slot_view[(size_t)it2 * span + ips2 + c->nph];
-                    if (v2 < 0) continue;
-                    for (int dw = -nbf; dw <= nbf; ++dw)
-                        lst.push_back(v2 * c->nom + ((io + dw) % c->nom + c->nom) % c->nom);
-                }
+            seeds[i].push_back(make_int3(2 * (slot / span_c), 2 * (slot % span_c - g.nph), 2 * ioc));
         }
-        std::sort(lst.begin(), lst.end());
-        lst.erase(std::unique(lst.begin(), lst.end()), lst.end());
-        if (lst.empty()) lst.push_back(0);
-    }
+    expand_seeds(c, seeds, nbf, lists);
     return CRYOIM_OK;
 }
 
@@ -1285,7 +1306,7 @@ int learn_train_impl(Ctx* c, const float* map3d, const cryoim_learn_opts* o, flo
 
 // Proposals of the trained model for the nb particles whose band is in c->band: the
 // top kl cells, each as two fine-grid seeds (angle, angle + 180 degrees), expanded to
-// their fine neighbourhoods within nbf steps -> lists[i], sorted.
+// their fine neighbourhoods within nbf steps -> lists[i].
 int learned_lists(Ctx* c, int nb, int kl, int nbf, std::vector<std::vector<int>>& lists) {
     LearnModel& L = c->lm;
     int r;
@@ -1298,36 +1319,23 @@ int learned_lists(Ctx* c, int nb, int kl, int nbf, std::vector<std::vector<int>>
     CK(cudaMemcpyAsync(cell.data(), L.cell.p, sizeof(int) * cell.size(), cudaMemcpyDeviceToHost, c->stream));
     CK(cudaStreamSynchronize(c->stream));
     const ViewGrid& g = c->cgrid;
-    const int span_c = 2 * g.nph + 1, span = 2 * c->nph + 1;
+    const int span_c = 2 * g.nph + 1;
     const float dw = 180.0f / LP_NT, step = c->p.searchstep;
-    lists.assign(nb, std::vector<int>());
-    for (int i = 0; i < nb; ++i) {
-        std::vector<int>& lst = lists[i];
+    std::vector<std::vector<int3>> seeds(nb);
+    for (int i = 0; i < nb; ++i)
         for (int j = 0; j < kl; ++j) {
             const int q = cell[(size_t)i * kl + j];
             if (q < 0) continue;
             const int vc = q / LP_NT, s = q % LP_NT, slot = g.view_slot[vc];
-            const int it = 2 * (slot / span_c), ips = 2 * (slot % span_c - g.nph);
             for (int half = 0; half < 2; ++half) {
                 float om = (float)L.sign * dw * (float)s + 180.0f * (float)half;
                 om = std::fmod(om, 360.0f);
                 if (om < 0.0f) om += 360.0f;
                 const int io = ((int)std::lround(om / step)) % c->nom;
-                for (int dt = -nbf; dt <= nbf; ++dt)
-                    for (int dp = -nbf; dp <= nbf; ++dp) {
-                        const int it2 = it + dt, ips2 = ips + dp;
-                        if (it2 < 0 || it2 > c->nth || ips2 < -c->nph || ips2 > c->nph) continue;
-                        const int v2 = c->slot_view[(size_t)it2 * span + ips2 + c->nph];
-                        if (v2 < 0) continue;
-                        for (int dwi = -nbf; dwi <= nbf; ++dwi)
-                            lst.push_back(v2 * c->nom + ((io + dwi) % c->nom + c->nom) % c->nom);
-                    }
+                seeds[i].push_back(make_int3(2 * (slot / span_c), 2 * (slot % span_c - g.nph), io));
             }
         }
-        std::sort(lst.begin(), lst.end());
-        lst.erase(std::unique(lst.begin(), lst.end()), lst.end());
-        if (lst.empty()) lst.push_back(0);
-    }
+    expand_seeds(c, seeds, nbf, lists);
     return CRYOIM_OK;
 }
 
