@@ -43,7 +43,7 @@ sys.path.insert(0, ROOT)
 
 WORKLOAD = dict(nx=256, apix=1.5, min_res=50.0, max_res=6.0, searchstep=1.0, ntemplates=20,
                 df=(0.8, 3.5), astig=0.1, snr=0.05, origin=6.0, origin_step=0.5, topk=16,
-                ampwg=0.07, seed=20261205, cycle_particles=10000, learned=16, nbr_best=4)
+                ampwg=0.07, seed=20261205, cycle_particles=10000, learned=16, nbr_best=4, learn_lr=4e-3)
 METRIC = "particles/s (box 256), BF16+learned vs plain FP32 GPU at >=99% same orientation"
 FP32_PEAK_TFLOPS_NOMINAL = 152 * 128 * 2 * 2.07e9 / 1e12  # FMA lanes x 2 flop x max SM clock
 FLOPS_PER_TERM = 30.0
@@ -296,8 +296,9 @@ def run_ours(args):
 
     # ---- the learned proposer, trained on projections the library renders from the map ----
     torch.cuda.nvtx.range_push("training")
-    lst = ctx.learn_train(vol, samples=args.learn_samples, batch=256, seed=w["seed"], snr=w["snr"],
-                          df_min=w["df"][0], df_max=w["df"][1], astig_max=w["astig"], origin_max=w["origin"])
+    lst = ctx.learn_train(vol, samples=args.learn_samples, batch=256, lr=w["learn_lr"], seed=w["seed"],
+                          snr=w["snr"], df_min=w["df"][0], df_max=w["df"][1], astig_max=w["astig"],
+                          origin_max=w["origin"])
     torch.cuda.nvtx.range_pop()
     train_ms = lst["seconds"] * 1000.0
 
@@ -564,8 +565,8 @@ def run_profile_case(args):
     d = torch.from_numpy(imgs).cuda()
     copts = dict(origin_max=w["origin"], origin_step=w["origin_step"], topk=w["topk"], pick=0)
     if case == "learned":
-        ctx.learn_train(vol, samples=2560, batch=256, seed=w["seed"], snr=w["snr"], df_min=w["df"][0],
-                        df_max=w["df"][1], astig_max=w["astig"], origin_max=w["origin"])
+        ctx.learn_train(vol, samples=2560, batch=256, lr=w["learn_lr"], seed=w["seed"], snr=w["snr"],
+                        df_min=w["df"][0], df_max=w["df"][1], astig_max=w["astig"], origin_max=w["origin"])
         copts.update(learned=w["learned"], nbr_best=w["nbr_best"])
     elif case == "exhaustive-fp8":
         copts.update(precision="fp8")
@@ -675,7 +676,7 @@ def main():
     ap.add_argument("--side-batch", type=int, default=64, help="particles per step of the other forms")
     ap.add_argument("--pr-particles", type=int, default=192,
                     help="particles of the agreement check against the FP32 form")
-    ap.add_argument("--learn-samples", type=int, default=25600,
+    ap.add_argument("--learn-samples", type=int, default=16384,
                     help="projections the learned proposer is trained on")
     ap.add_argument("--searchstep", type=float, default=None,
                     help="override the 1-degree grid (small cases for profiler captures only)")

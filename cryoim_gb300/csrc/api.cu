@@ -1074,20 +1074,17 @@ int learn_backward(Ctx* c, int B) {
     launch_lp_head_grad(L.g.p, w + L.oT, L.dsc.p, B, L.V, L.dg.p, gr + L.oT, L.hscr.p, st);
     launch_lp_mix_grad(L.p4.p, L.dg.p, B, w + L.oW[4], L.dp4.p, gr + L.oW[4], gr + L.ob[4], st);
     // layer 4
-    launch_lp_pool_grad(L.dp4.p, B, LP_C4, LP_NR / 8, L.da4.p, st);
-    launch_lp_relu_grad(L.a4.p, L.da4.p, (long)B * LP_C4 * (LP_NR / 4) * nt, L.da4.p, st);
+    launch_lp_pool_grad(L.dp4.p, B, LP_C4, LP_NR / 8, L.a4.p, L.da4.p, st);
     CK(launch_lp_conv3_wgrad(L.p3.p, L.da4.p, B, LP_C3, LP_NR / 4, LP_C4, gr + L.oW[3], gr + L.ob[3], st));
     launch_lp_flip(w + L.oW[3], LP_C4, LP_C3, L.wflip.p, st);
     CK(launch_lp_conv3(L.da4.p, B, LP_C4, LP_NR / 4, L.wflip.p, nullptr, LP_C3, false, L.dp3.p, st));
     // layer 3
-    launch_lp_pool_grad(L.dp3.p, B, LP_C3, LP_NR / 4, L.da3.p, st);
-    launch_lp_relu_grad(L.a3.p, L.da3.p, (long)B * LP_C3 * (LP_NR / 2) * nt, L.da3.p, st);
+    launch_lp_pool_grad(L.dp3.p, B, LP_C3, LP_NR / 4, L.a3.p, L.da3.p, st);
     CK(launch_lp_conv3_wgrad(L.p2.p, L.da3.p, B, LP_C2, LP_NR / 2, LP_C3, gr + L.oW[2], gr + L.ob[2], st));
     launch_lp_flip(w + L.oW[2], LP_C3, LP_C2, L.wflip.p, st);
     CK(launch_lp_conv3(L.da3.p, B, LP_C3, LP_NR / 2, L.wflip.p, nullptr, LP_C2, false, L.dp2.p, st));
     // layer 2
-    launch_lp_pool_grad(L.dp2.p, B, LP_C2, LP_NR / 2, L.da2.p, st);
-    launch_lp_relu_grad(L.a2.p, L.da2.p, (long)B * LP_C2 * LP_NR * nt, L.da2.p, st);
+    launch_lp_pool_grad(L.dp2.p, B, LP_C2, LP_NR / 2, L.a2.p, L.da2.p, st);
     CK(launch_lp_conv3_wgrad(L.a1.p, L.da2.p, B, LP_C1, LP_NR, LP_C2, gr + L.oW[1], gr + L.ob[1], st));
     launch_lp_flip(w + L.oW[1], LP_C2, LP_C1, L.wflip.p, st);
     CK(launch_lp_conv3(L.da2.p, B, LP_C2, LP_NR, L.wflip.p, nullptr, LP_C1, false, L.da1.p, st));

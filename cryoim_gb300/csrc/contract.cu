@@ -139,36 +139,50 @@ __device__ __forceinline__ void phasor_at(const float2* tab, int R, int2 hk, flo
     *sn = ex.y * ey.x + ex.x * ey.y;
 }
 
-// Row (p, o) of A: CTF x particle x origin phase ramp, unit norm, BF16.
+// Rows (p, o0 .. o0 + AO - 1) of A: CTF x particle x origin phase ramp, unit norm,
+// BF16.  Each thread reads a sample's transform and CTF once and writes it for AO
+// origins (phasor tables of all AO origins in shared memory).
+constexpr int AO = 8;
 __global__ void __launch_bounds__(256) k_build_a(const float2* __restrict__ band, const float* __restrict__ ctf,
                                                  Band bd, const int2* __restrict__ samples, int S, int Kpad,
                                                  const float* __restrict__ origins, int O,
                                                  const double* __restrict__ norm, float two_pi_over_n,
                                                  __nv_bfloat162* __restrict__ A) {
-    extern __shared__ float2 ptab[];
-    const int o = blockIdx.x, p = blockIdx.y, W = bd.W, R = bd.max_r;
+    extern __shared__ float2 ptab[];  // [AO][3 R + 2]
+    const int o0 = blockIdx.x * AO, p = blockIdx.y, W = bd.W, R = bd.max_r, nt = 3 * R + 2;
+    const int no = min(AO, O - o0);
     const float2* b = band + (long)p * W * W;
     const float* c = ctf ? ctf + (long)p * W * W : nullptr;
     const float h = (float)(bd.nx / 2);
-    const float sx = origins[2 * o] + h, sy = origins[2 * o + 1] + h;
     const float inv = norm[p] > 0.0 ? (float)(1.0 / sqrt(norm[p])) : 0.0f;
-    __nv_bfloat162* row = A + ((long)p * O + o) * (Kpad / 2);
-    origin_phasors(sx, sy, R, two_pi_over_n, ptab);
+    for (int j = 0; j < no; ++j) {
+        const float sx = origins[2 * (o0 + j)] + h, sy = origins[2 * (o0 + j) + 1] + h;
+        for (int i = threadIdx.x; i < nt; i += blockDim.x) {
+            const float a = i <= R ? two_pi_over_n * (sx * (float)i)
+                                   : two_pi_over_n * (sy * (float)(i - 2 * R - 1));
+            float sn, cs;
+            sincosf(a, &sn, &cs);
+            ptab[j * nt + i] = make_float2(cs, sn);
+        }
+    }
+    __syncthreads();
     for (int i = threadIdx.x; i < Kpad / 2; i += blockDim.x) {
-        float re = 0.f, im = 0.f;
         if (i < S) {
             const int2 hk = samples[i];
             const int q = (hk.y + R) * W + (hk.x + R);
             const float2 ab = b[q];  // (a, b) = (Re F, -Im F) referenced to pixel 0
-            float sn, cs;
-            phasor_at(ptab, R, hk, &sn, &cs);
-            // centshift: (a', b') = (a cos + b sin, -a sin + b cos); P = a' - i b'
-            const float a2 = ab.x * cs + ab.y * sn, b2 = -ab.x * sn + ab.y * cs;
             const float cv = (c ? c[q] : 1.0f) * inv;
-            re = a2 * cv;
-            im = -b2 * cv;
+            for (int j = 0; j < no; ++j) {
+                float sn, cs;
+                phasor_at(ptab + j * nt, R, hk, &sn, &cs);
+                // centshift: (a', b') = (a cos + b sin, -a sin + b cos); P = a' - i b'
+                const float a2 = ab.x * cs + ab.y * sn, b2 = -ab.x * sn + ab.y * cs;
+                A[((long)p * O + o0 + j) * (Kpad / 2) + i] = __floats2bfloat162_rn(a2 * cv, -b2 * cv);
+            }
+        } else {
+            for (int j = 0; j < no; ++j)
+                A[((long)p * O + o0 + j) * (Kpad / 2) + i] = __floats2bfloat162_rn(0.f, 0.f);
         }
-        row[i] = __floats2bfloat162_rn(re, im);
     }
 }
 
@@ -624,11 +638,11 @@ void launch_particle_norm(const float2* band, const float* ctf, Band bd, const i
 
 void launch_build_a(const float2* band, const float* ctf, Band bd, const int2* samples, int S, int Kpad,
                     const float* origins, int O, const double* norm, int B, void* A, cudaStream_t st) {
-    dim3 g(O, B);
     const float tpn = 2.0f * host_angles().pi / (float)bd.nx;
-    k_build_a<<<g, 256, sizeof(float2) * (3 * bd.max_r + 2), st>>>(band, ctf, bd, samples, S, Kpad, origins, O,
-                                                                    norm, tpn,
-                                 (__nv_bfloat162*)A);
+    dim3 ga((O + AO - 1) / AO, B);
+    const int sm = (int)(sizeof(float2) * AO * (3 * bd.max_r + 2));
+    if (sm > 48 * 1024) cudaFuncSetAttribute(k_build_a, cudaFuncAttributeMaxDynamicSharedMemorySize, sm);
+    k_build_a<<<ga, 256, sm, st>>>(band, ctf, bd, samples, S, Kpad, origins, O, norm, tpn, (__nv_bfloat162*)A);
 }
 
 void launch_select_topk(const float* topv, const int* topi, int O, int ntiles, int k, int B,

@@ -209,7 +209,8 @@ cudaError_t launch_lp_conv3_wgrad(const float* in, const float* dpre, int B, int
 void launch_lp_relu_grad(const float* out, const float* dout, long n, float* dpre, cudaStream_t st);
 void launch_lp_flip(const float* W, int Cout, int Cin, float* Wf, cudaStream_t st);
 void launch_lp_pool(const float* a, int B, int C, int Hout, float* p, cudaStream_t st);
-void launch_lp_pool_grad(const float* dp, int B, int C, int Hout, float* da, cudaStream_t st);
+// with a (the pooled layer's ReLU output, or nullptr): the ReLU gate applied too
+void launch_lp_pool_grad(const float* dp, int B, int C, int Hout, const float* a, float* da, cudaStream_t st);
 void launch_lp_mix(const float* x, int B, const float* W5, const float* b5, float* g, cudaStream_t st);
 void launch_lp_mix_grad(const float* x, const float* dg, int B, const float* W5, float* dx, float* dW5, float* db5,
                         cudaStream_t st);

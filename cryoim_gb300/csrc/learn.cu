@@ -244,19 +244,38 @@ __global__ void __launch_bounds__(NT) k_conv3(const float* __restrict__ in, int 
     for (int c = 0; c < CT; ++c)
 #pragma unroll
         for (int r = 0; r < HT; ++r) acc[c][r] = 0.f;
-    for (int ci = 0; ci < Cin; ++ci) {
+    // the next input channel's rows (and halo) and weights are loaded into registers
+    // while the current one is used from shared memory
+    float px[HT + 2], ph[HT + 2], pw[2];
+    auto fetch = [&](int ci) {
         const float* ip = in + ((long)b * Cin + ci) * H * NT;
-        __syncthreads();
 #pragma unroll
         for (int r = 0; r < HT + 2; ++r) {
             const int hh = h0 + r - 1;
             const bool ok = hh >= 0 && hh < H;
-            sx[r][t + 1] = ok ? ip[hh * NT + t] : 0.f;
-            if (t == 0) sx[r][0] = ok ? ip[hh * NT + NT - 1] : 0.f;
-            if (t == NT - 1) sx[r][NT + 1] = ok ? ip[hh * NT] : 0.f;
+            px[r] = ok ? ip[hh * NT + t] : 0.f;
+            ph[r] = (ok && (t == 0 || t == NT - 1)) ? ip[hh * NT + (t == 0 ? NT - 1 : 0)] : 0.f;
         }
-        for (int q = t; q < CT * 9; q += NT) sw[q] = Wt[((long)(co0 + q / 9) * Cin + ci) * 9 + q % 9];
+#pragma unroll
+        for (int u = 0; u < 2; ++u) {
+            const int q = t + u * NT;
+            pw[u] = q < CT * 9 ? Wt[((long)(co0 + q / 9) * Cin + ci) * 9 + q % 9] : 0.f;
+        }
+    };
+    fetch(0);
+    for (int ci = 0; ci < Cin; ++ci) {
         __syncthreads();
+#pragma unroll
+        for (int r = 0; r < HT + 2; ++r) {
+            sx[r][t + 1] = px[r];
+            if (t == 0) sx[r][0] = ph[r];
+            if (t == NT - 1) sx[r][NT + 1] = ph[r];
+        }
+#pragma unroll
+        for (int u = 0; u < 2; ++u)
+            if (t + u * NT < CT * 9) sw[t + u * NT] = pw[u];
+        __syncthreads();
+        if (ci + 1 < Cin) fetch(ci + 1);
         float x[HT + 2][3];
 #pragma unroll
         for (int r = 0; r < HT + 2; ++r)
@@ -300,16 +319,21 @@ __global__ void __launch_bounds__(NT) k_conv3_wgrad(const float* __restrict__ in
         for (int k = 0; k < 10; ++k) acc[c][k] = 0.f;
     for (int b = b0; b < min(B, b0 + bchunk); ++b) {
         const float* ip = in + ((long)b * Cin + ci) * H * NT;
+        // rows h-1, h, h+1 at t-1, t, t+1, rolled down one row per step
+        float x[3][3] = {{0.f, 0.f, 0.f}, {0.f, 0.f, 0.f}, {0.f, 0.f, 0.f}};
+        x[2][0] = __ldg(ip + tm);
+        x[2][1] = __ldg(ip + t);
+        x[2][2] = __ldg(ip + tp);
         for (int h = 0; h < H; ++h) {
-            float x[3][3];
 #pragma unroll
-            for (int dh = 0; dh < 3; ++dh) {
-                const int hh = h + dh - 1;
-                const bool ok = hh >= 0 && hh < H;
-                x[dh][0] = ok ? __ldg(ip + hh * NT + tm) : 0.f;
-                x[dh][1] = ok ? __ldg(ip + hh * NT + t) : 0.f;
-                x[dh][2] = ok ? __ldg(ip + hh * NT + tp) : 0.f;
+            for (int d = 0; d < 3; ++d) {
+                x[0][d] = x[1][d];
+                x[1][d] = x[2][d];
             }
+            const bool ok = h + 1 < H;
+            x[2][0] = ok ? __ldg(ip + (h + 1) * NT + tm) : 0.f;
+            x[2][1] = ok ? __ldg(ip + (h + 1) * NT + t) : 0.f;
+            x[2][2] = ok ? __ldg(ip + (h + 1) * NT + tp) : 0.f;
 #pragma unroll
             for (int c = 0; c < CT; ++c) {
                 const float g = __ldg(dpre + (((long)b * Cout + co0 + c) * H + h) * NT + t);
@@ -362,16 +386,18 @@ __global__ void k_pool(const float* __restrict__ a, long nout, int Hout, float* 
         p[q] = 0.5f * (src[0] + src[NT]);
     }
 }
-__global__ void k_pool_grad(const float* __restrict__ dp, long nout, int Hout, float* __restrict__ da) {
+// gradient through the pooling and, given the pooled layer's ReLU output a, its gate
+__global__ void k_pool_grad(const float* __restrict__ dp, long nout, int Hout, const float* __restrict__ a,
+                            float* __restrict__ da) {
     for (long q = (long)blockIdx.x * blockDim.x + threadIdx.x; q < nout; q += (long)gridDim.x * blockDim.x) {
         const int t = (int)(q % NT);
         const long bch = q / NT;
         const int h = (int)(bch % Hout);
         const long bc = bch / Hout;
-        float* dst = da + (bc * 2 * Hout + 2 * h) * NT + t;
+        const long o = (bc * 2 * Hout + 2 * h) * NT + t;
         const float v = 0.5f * dp[q];
-        dst[0] = v;
-        dst[NT] = v;
+        da[o] = (!a || a[o] > 0.f) ? v : 0.f;
+        da[o + NT] = (!a || a[o + NT] > 0.f) ? v : 0.f;
     }
 }
 
@@ -700,9 +726,9 @@ void launch_lp_pool(const float* a, int B, int C, int Hout, float* p, cudaStream
     const long n = (long)B * C * Hout * NT;
     k_pool<<<grid_for(n, 256), 256, 0, st>>>(a, n, Hout, p);
 }
-void launch_lp_pool_grad(const float* dp, int B, int C, int Hout, float* da, cudaStream_t st) {
+void launch_lp_pool_grad(const float* dp, int B, int C, int Hout, const float* a, float* da, cudaStream_t st) {
     const long n = (long)B * C * Hout * NT;
-    k_pool_grad<<<grid_for(n, 256), 256, 0, st>>>(dp, n, Hout, da);
+    k_pool_grad<<<grid_for(n, 256), 256, 0, st>>>(dp, n, Hout, a, da);
 }
 void launch_lp_mix(const float* x, int B, const float* W5, const float* b5, float* g, cudaStream_t st) {
     k_mix<<<B, NT, 0, st>>>(x, W5, b5, g);
