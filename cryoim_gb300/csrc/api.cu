@@ -329,6 +329,7 @@ struct Ctx {
     DBuf<int> xcount;
     DBuf<double> kpart;
     DBuf<float2> tbandc;
+    DBuf<int4> xgroups;
     DBuf<GemmGroup> ggroups;
     DBuf<int2> gseg;
     LearnModel lm;
@@ -358,7 +359,7 @@ struct Ctx {
         csamples_c.release(); bmat_c.release(); amat_c.release(); corigins_c.release(); topv_c.release();
         tilev_c.release(); kcc_c.release(); topi_c.release(); tileo_c.release(); tileorig_c.release();
         kor_c.release(); korig_c.release(); gidx.release(); pnorm_c.release(); bgather.release();
-        sband.release(); xcount.release(); kpart.release(); ggroups.release(); gseg.release(); tbandc.release();
+        sband.release(); xcount.release(); kpart.release(); ggroups.release(); gseg.release(); tbandc.release(); xgroups.release();
         lm.release();
         if (pe0) cudaEventDestroy(pe0);
         if (pe1) cudaEventDestroy(pe1);
@@ -1709,7 +1710,23 @@ int contract_impl(Ctx* c, const float* imgs, bool on_device, cryoim_particle* pa
             a.tfcut_pstride = tfs; a.ctf = ctfp; a.cand = c->xcand.p; a.alpha = c->xalpha.p; a.T = T;
             a.bd = c->bd; a.pr = c->xpr.p; a.ncand = maxc; a.sband = c->sband.p; a.ncount = c->xcount.p;
             a.tbandc = ctfp ? c->tbandc.p : nullptr;
-            CK(launch_pr_single(a, nb, c->stream));
+            // candidates of a particle sharing a view, in groups (the sets are sorted by
+            // orientation index, so a view's omegas are adjacent)
+            std::vector<int4> grp;
+            const int rg = pr_rescore_group_size();
+            for (int i = 0; i < nb; ++i)
+                for (size_t j = 0; j < sets[i].size();) {
+                    size_t e = j + 1;
+                    while (e < sets[i].size() && (int)(e - j) < rg && sets[i][e] / c->nom == sets[i][j] / c->nom) ++e;
+                    grp.push_back(make_int4(i, (int)j, (int)(e - j), 0));
+                    j = e;
+                }
+            if (!grp.empty()) {
+                if ((r = c->xgroups.ensure(grp.size()))) return r;
+                CK(cudaMemcpyAsync(c->xgroups.p, grp.data(), sizeof(int4) * grp.size(), cudaMemcpyHostToDevice,
+                                   c->stream));
+                CK(launch_pr_rescore_groups(a, c->xgroups.p, (int)grp.size(), c->stream));
+            }
             std::vector<float> h((size_t)nb * maxc);
             CK(cudaMemcpyAsync(h.data(), c->xpr.p, sizeof(float) * h.size(), cudaMemcpyDeviceToHost, c->stream));
             CK(cudaStreamSynchronize(c->stream));

@@ -105,6 +105,10 @@ struct PrSingleArgs {
     const float2* tbandc = nullptr; // with sband: [B][T][W*W] templates x CTF (launch_tband_ctf), or nullptr
 };
 cudaError_t launch_pr_single(const PrSingleArgs& a, int B, cudaStream_t st);
+// rescoring by groups of candidates sharing a view: groups[g] = (particle, first
+// candidate slot, count <= pr_rescore_group_size(), 0); requires sband
+cudaError_t launch_pr_rescore_groups(const PrSingleArgs& a, const int4* groups, int ngroups, cudaStream_t st);
+int pr_rescore_group_size();
 cudaError_t launch_tband_ctf(const float2* tband, int T, const float* ctf, const Band& bd, int B, float2* out,
                              cudaStream_t st);
 // sband for PrSingleArgs: the band of each particle shifted to cand[p][0]'s origin

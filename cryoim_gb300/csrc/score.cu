@@ -345,6 +345,190 @@ __global__ void __launch_bounds__(512) k_pr_single(PrSingleArgs a, Consts K) {
     }
 }
 
+// Rescoring form of k_pr_single<true> (every candidate at the particle's origin, band
+// pre-shifted, templates pre-multiplied by the CTF): the lines of all templates are set
+// up once (directions, validity, cuts in shared memory), then the block's threads run
+// one flat loop over (template, line, radius) with no barrier inside.  Same per-term
+// arithmetic as the exhaustive scorer (angle_between, Kahan sums per thread).
+__global__ void __launch_bounds__(512) k_pr_rescore(PrSingleArgs a, Consts K) {
+    extern __shared__ float rsm[];
+    __shared__ double sh[2][32];
+    const Band bd = a.bd;
+    const int W = bd.W, nr = bd.nr, minR = bd.min_r, nx = bd.nx, T = a.T;
+    const int c = blockIdx.x, p = blockIdx.y;
+    if (a.ncount && c >= a.ncount[p]) return;  // padding slot (whole block)
+    float* scs = rsm;                          // [T][60][4]: cos, sin particle line; cos, sin template line
+    float* sfc = scs + (long)T * 240;          // [T + 1][nr]: template cuts, then the particle's
+    int* sval = reinterpret_cast<int*>(sfc + (long)(T + 1) * nr);  // [T][60]
+    const float2* al0 = a.alpha + ((long)p * a.ncand + c) * T * 60;
+    for (int q = threadIdx.x; q < T * 60; q += blockDim.x) {
+        const float2 aa = al0[q];
+        const bool ok = aa.x < 999.0f && aa.y < 999.0f;
+        sval[q] = ok;
+        if (ok) {
+            const float a1 = __fmul_rn(aa.x, K.d2r), a2 = __fmul_rn(aa.y, K.d2r);
+            scs[4 * q] = cosf(a1);
+            scs[4 * q + 1] = sinf(a1);
+            scs[4 * q + 2] = cosf(a2);
+            scs[4 * q + 3] = sinf(a2);
+        }
+    }
+    const float* tfc = a.tfcut + (long)p * a.tfcut_pstride;
+    for (int q = threadIdx.x; q < T * nr; q += blockDim.x) sfc[q] = tfc[q];
+    for (int q = threadIdx.x; q < nr; q += blockDim.x) sfc[T * nr + q] = a.fcut0[(long)p * nr + q];
+    __syncthreads();
+    const float nxh = (float)(nx / 2);
+    const int offW = bd.off * W + bd.off;
+    const float2* sb = a.sband + (long)p * W * W;
+    const float2* tbc0 = a.tbandc ? a.tbandc + (long)p * T * W * W : nullptr;
+    const float* ctfp = a.ctf ? a.ctf + (long)p * W * W : nullptr;
+    const int per_t = 60 * nr;
+    float f1 = 0.f, f2 = 0.f, k1 = 0.f, k2 = 0.f;
+    for (int q = threadIdx.x; q < T * per_t; q += blockDim.x) {
+        const int i = q / per_t, rem = q - i * per_t, j = rem / nr, iq = rem - j * nr;
+        const int lj = i * 60 + j;
+        if (!sval[lj]) continue;
+        const float4 cs4 = *reinterpret_cast<const float4*>(scs + 4 * lj);
+        const float fr = (float)(minR + iq);
+        const float x = __fadd_rn(__fmul_rn(fr, cs4.x), nxh), y = __fadd_rn(__fmul_rn(fr, cs4.y), nxh);
+        const int lx = (int)x, ly = (int)y;
+        const float ax = __fsub_rn(x, (float)lx), ay = __fsub_rn(y, (float)ly);
+        const int b0 = ly * W + lx - offW;
+        const float2 t00 = sb[b0], t10 = sb[b0 + 1], t01 = sb[b0 + W], t11 = sb[b0 + W + 1];
+        const float re1 = bilerp(ax, ay, t00.x, t10.x, t01.x, t11.x);
+        const float im1 = bilerp(ax, ay, t00.y, t10.y, t01.y, t11.y);
+        float re2, im2;
+        if (tbc0)
+            tmpl_sample_cs(tbc0 + (long)i * W * W, nullptr, W, offW, nxh, cs4.z, cs4.w, fr, &re2, &im2);
+        else
+            tmpl_sample_cs(a.tband + (long)i * W * W, ctfp, W, offW, nxh, cs4.z, cs4.w, fr, &re2, &im2);
+        const float amp1 = sqrtf(re1 * re1 + im1 * im1);
+        const float amp2 = sqrtf(re2 * re2 + im2 * im2);
+        if (amp1 >= sfc[T * nr + iq] && amp2 >= sfc[i * nr + iq]) {
+            const float d = angle_between(re1 * im2 - im1 * re2, re1 * re2 + im1 * im2, K.pi);
+            const float w = 0.5f * (amp1 + amp2);
+            kahan_add(f1, k1, d * w);
+            kahan_add(f2, k2, w);
+        }
+    }
+    double p1 = (double)f1, p2 = (double)f2;
+    for (int o = 16; o > 0; o >>= 1) {
+        p1 += __shfl_xor_sync(0xffffffffu, p1, o);
+        p2 += __shfl_xor_sync(0xffffffffu, p2, o);
+    }
+    const int w = threadIdx.x >> 5, l = threadIdx.x & 31, nw = blockDim.x >> 5;
+    if (l == 0) { sh[0][w] = p1; sh[1][w] = p2; }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double s1 = 0, s2 = 0;
+        for (int q = 0; q < nw; ++q) { s1 += sh[0][q]; s2 += sh[1][q]; }
+        const float g1 = (float)s1, g2 = (float)s2;
+        a.pr[(long)p * a.ncand + c] = (g2 > 1.0e-10f) ? g1 / g2 * 180.0f / K.pi : 1000.0f;
+    }
+}
+
+// Grouped rescoring: up to RG candidates of one particle that share a view (theta,
+// phi) and differ in omega.  The template side of a term (line direction, taps, cut)
+// does not depend on omega, so each (template, line, radius) sample of the templates
+// is taken once and compared with the RG particle samples.  groups[g] = (particle,
+// first candidate slot, count).  Same per-term arithmetic as k_pr_rescore.
+constexpr int RG = 4;
+__global__ void __launch_bounds__(512) k_pr_rescore_g(PrSingleArgs a, const int4* __restrict__ groups, Consts K) {
+    extern __shared__ float rsm[];
+    __shared__ double sh[2][RG][16];
+    const Band bd = a.bd;
+    const int W = bd.W, nr = bd.nr, minR = bd.min_r, nx = bd.nx, T = a.T;
+    const int4 gr = groups[blockIdx.x];
+    const int p = gr.x, c0 = gr.y, m = gr.z;
+    float* spl = rsm;                          // [RG][T][60][2]: cos, sin of the particle lines
+    float* stl = spl + (long)RG * T * 120;     // [T][60][2]: cos, sin of the template lines
+    float* sfc = stl + (long)T * 120;          // [T + 1][nr]: template cuts, then the particle's
+    int* sval = reinterpret_cast<int*>(sfc + (long)(T + 1) * nr);  // [T][60]
+    for (int q = threadIdx.x; q < T * 60; q += blockDim.x) {
+        const float2 aa = a.alpha[((long)p * a.ncand + c0) * T * 60 + q];
+        const bool ok = aa.x < 999.0f && aa.y < 999.0f;
+        sval[q] = ok;
+        if (ok) {
+            const float a2 = __fmul_rn(aa.y, K.d2r);
+            stl[2 * q] = cosf(a2);
+            stl[2 * q + 1] = sinf(a2);
+        }
+    }
+    for (int q = threadIdx.x; q < m * T * 60; q += blockDim.x) {
+        const int g = q / (T * 60), r = q - g * T * 60;
+        const float2 aa = a.alpha[((long)p * a.ncand + c0 + g) * T * 60 + r];
+        const float a1 = __fmul_rn(aa.x, K.d2r);
+        spl[2 * q] = cosf(a1);
+        spl[2 * q + 1] = sinf(a1);
+    }
+    const float* tfc = a.tfcut + (long)p * a.tfcut_pstride;
+    for (int q = threadIdx.x; q < T * nr; q += blockDim.x) sfc[q] = tfc[q];
+    for (int q = threadIdx.x; q < nr; q += blockDim.x) sfc[T * nr + q] = a.fcut0[(long)p * nr + q];
+    __syncthreads();
+    const float nxh = (float)(nx / 2);
+    const int offW = bd.off * W + bd.off;
+    const float2* sb = a.sband + (long)p * W * W;
+    const float2* tbc0 = a.tbandc ? a.tbandc + (long)p * T * W * W : nullptr;
+    const float* ctfp = a.ctf ? a.ctf + (long)p * W * W : nullptr;
+    const int per_t = 60 * nr;
+    float f1[RG], f2[RG], k1[RG], k2[RG];
+#pragma unroll
+    for (int g = 0; g < RG; ++g) { f1[g] = 0.f; f2[g] = 0.f; k1[g] = 0.f; k2[g] = 0.f; }
+    for (int q = threadIdx.x; q < T * per_t; q += blockDim.x) {
+        const int i = q / per_t, rem = q - i * per_t, j = rem / nr, iq = rem - j * nr;
+        const int lj = i * 60 + j;
+        if (!sval[lj]) continue;
+        const float fr = (float)(minR + iq);
+        float re2, im2;
+        if (tbc0)
+            tmpl_sample_cs(tbc0 + (long)i * W * W, nullptr, W, offW, nxh, stl[2 * lj], stl[2 * lj + 1], fr, &re2,
+                           &im2);
+        else
+            tmpl_sample_cs(a.tband + (long)i * W * W, ctfp, W, offW, nxh, stl[2 * lj], stl[2 * lj + 1], fr, &re2,
+                           &im2);
+        const float amp2 = sqrtf(re2 * re2 + im2 * im2);
+        if (!(amp2 >= sfc[i * nr + iq])) continue;
+        const float cut1 = sfc[T * nr + iq];
+#pragma unroll
+        for (int g = 0; g < RG; ++g) {
+            if (g >= m) break;
+            const float cs = spl[2 * ((long)g * T * 60 + lj)], sn = spl[2 * ((long)g * T * 60 + lj) + 1];
+            const float x = __fadd_rn(__fmul_rn(fr, cs), nxh), y = __fadd_rn(__fmul_rn(fr, sn), nxh);
+            const int lx = (int)x, ly = (int)y;
+            const float ax = __fsub_rn(x, (float)lx), ay = __fsub_rn(y, (float)ly);
+            const int b0 = ly * W + lx - offW;
+            const float2 t00 = sb[b0], t10 = sb[b0 + 1], t01 = sb[b0 + W], t11 = sb[b0 + W + 1];
+            const float re1 = bilerp(ax, ay, t00.x, t10.x, t01.x, t11.x);
+            const float im1 = bilerp(ax, ay, t00.y, t10.y, t01.y, t11.y);
+            const float amp1 = sqrtf(re1 * re1 + im1 * im1);
+            if (amp1 >= cut1) {
+                const float d = angle_between(re1 * im2 - im1 * re2, re1 * re2 + im1 * im2, K.pi);
+                const float w = 0.5f * (amp1 + amp2);
+                kahan_add(f1[g], k1[g], d * w);
+                kahan_add(f2[g], k2[g], w);
+            }
+        }
+    }
+    const int w = threadIdx.x >> 5, l = threadIdx.x & 31, nw = blockDim.x >> 5;
+#pragma unroll
+    for (int g = 0; g < RG; ++g) {
+        double p1 = (double)f1[g], p2 = (double)f2[g];
+        for (int o = 16; o > 0; o >>= 1) {
+            p1 += __shfl_xor_sync(0xffffffffu, p1, o);
+            p2 += __shfl_xor_sync(0xffffffffu, p2, o);
+        }
+        if (l == 0) { sh[0][g][w] = p1; sh[1][g][w] = p2; }
+    }
+    __syncthreads();
+    if (threadIdx.x < m) {
+        const int g = threadIdx.x;
+        double s1 = 0, s2 = 0;
+        for (int q = 0; q < nw; ++q) { s1 += sh[0][g][q]; s2 += sh[1][g][q]; }
+        const float g1 = (float)s1, g2 = (float)s2;
+        a.pr[(long)p * a.ncand + c0 + g] = (g2 > 1.0e-10f) ? g1 / g2 * 180.0f / K.pi : 1000.0f;
+    }
+}
+
 // The particle transform shifted to the origin its candidates share (cand[p][0][3..4]):
 // per pixel the same phase rotation k_pr_single applies to each bilinear tap
 // (img2d_FT_centshift.f90), computed once per pixel instead of once per tap.
@@ -492,14 +676,36 @@ cudaError_t launch_tband_ctf(const float2* tband, int T, const float* ctf, const
 }
 
 cudaError_t launch_pr_single(const PrSingleArgs& a, int B, cudaStream_t st) {
-    if (a.sband && a.bd.nr > 256) return cudaErrorInvalidValue;
     dim3 grid(a.ncand, B);
-    if (a.sband)
+    if (a.sband) {
+        // the flat rescoring kernel when its line tables fit in shared memory
+        const size_t sm = sizeof(float) * ((size_t)a.T * 240 + (size_t)(a.T + 1) * a.bd.nr) + sizeof(int) * a.T * 60;
+        if (sm <= 200 * 1024) {
+            cudaError_t e = cudaFuncSetAttribute(k_pr_rescore, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+            if (e != cudaSuccess) return e;
+            k_pr_rescore<<<grid, 512, sm, st>>>(a, consts());
+            return cudaGetLastError();
+        }
+        if (a.bd.nr > 256) return cudaErrorInvalidValue;
         k_pr_single<true><<<grid, 512, 0, st>>>(a, consts());
-    else
+    } else {
         k_pr_single<false><<<grid, 512, 0, st>>>(a, consts());
+    }
     return cudaGetLastError();
 }
+
+cudaError_t launch_pr_rescore_groups(const PrSingleArgs& a, const int4* groups, int ngroups, cudaStream_t st) {
+    if (!a.sband || ngroups < 1) return cudaErrorInvalidValue;
+    const size_t sm = sizeof(float) * ((size_t)RG * a.T * 120 + (size_t)a.T * 120 + (size_t)(a.T + 1) * a.bd.nr) +
+                      sizeof(int) * a.T * 60;
+    if (sm > 200 * 1024) return cudaErrorInvalidValue;
+    cudaError_t e = cudaFuncSetAttribute(k_pr_rescore_g, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+    if (e != cudaSuccess) return e;
+    k_pr_rescore_g<<<ngroups, 512, sm, st>>>(a, groups, consts());
+    return cudaGetLastError();
+}
+
+int pr_rescore_group_size() { return RG; }
 
 cudaError_t launch_insert(const InsertArgs& a, int B, cudaStream_t st) {
     long total = (long)a.nsamples * a.nsym;
