@@ -327,9 +327,11 @@ __global__ void k_select_distinct(float* __restrict__ v0, const int* __restrict_
 // FP64 rescoring of one (particle, candidate): the same CC with every product,
 // interpolation and sum in double precision.
 // FP64 rescoring, one (candidate, particle, sample chunk) per block: the three sums of
-// the CC (p.q, |p|^2, |q|^2) over samples [S*s/NS, S*(s+1)/NS).  The origin shift
-// exp(-i 2pi (sx hx + sy ky)/n) is separable, so each block tabulates the per-hx and
-// per-ky phasors in double once and multiplies them per sample.
+// the CC (p.q, |p|^2, |q|^2) over samples [S*s/NS, S*(s+1)/NS).  The section sample
+// is interpolated at FP64-rotated coordinates; its trilinear blend of the FP32 cube runs
+// in FP32 (the data's own precision), every product and sum after it in FP64.  The
+// origin shift exp(-i 2pi (sx hx + sy ky)/n) is separable, so each block tabulates the
+// per-hx and per-ky phasors in double once and multiplies them per sample.
 constexpr int CC_SPLIT = 4;
 
 __global__ void k_cc_fp64(const float2* __restrict__ cube, const float2* __restrict__ band,
@@ -370,16 +372,22 @@ __global__ void k_cc_fp64(const float2* __restrict__ cube, const float2* __restr
                      z = rot[6] * hk.x + rot[7] * hk.y;
         const double fx = floor(x), fy = floor(y), fz = floor(z);
         const int ix = (int)fx + off, iy = (int)fy + off, iz = (int)fz + off;
-        const double ax = x - fx, ay = y - fy, az = z - fz;
-        double sr = 0, si = 0;
-        for (int dz = 0; dz < 2; ++dz)
-            for (int dy = 0; dy < 2; ++dy)
-                for (int dx = 0; dx < 2; ++dx) {
-                    const double w = (dx ? ax : 1 - ax) * (dy ? ay : 1 - ay) * (dz ? az : 1 - az);
-                    const float2 v = cube[((long)(iz + dz) * C + (iy + dy)) * C + (ix + dx)];
-                    sr += w * v.x;
-                    si += w * v.y;
-                }
+        // the cube holds FP32 values: its trilinear blend runs in FP32 (exact-geometry
+        // weights rounded once), the products and sums below in FP64
+        const float ax = (float)(x - fx), ay = (float)(y - fy), az = (float)(z - fz);
+        const float2* cb0 = cube + ((long)iz * C + iy) * C + ix;
+        float2 r0, r1;
+        {
+            const float2 v000 = cb0[0], v001 = cb0[1], v010 = cb0[C], v011 = cb0[C + 1];
+            const float2 v100 = cb0[C * C], v101 = cb0[C * C + 1], v110 = cb0[C * C + C], v111 = cb0[C * C + C + 1];
+            const float2 a0 = make_float2(fmaf(ax, v001.x - v000.x, v000.x), fmaf(ax, v001.y - v000.y, v000.y));
+            const float2 a1 = make_float2(fmaf(ax, v011.x - v010.x, v010.x), fmaf(ax, v011.y - v010.y, v010.y));
+            const float2 a2 = make_float2(fmaf(ax, v101.x - v100.x, v100.x), fmaf(ax, v101.y - v100.y, v100.y));
+            const float2 a3 = make_float2(fmaf(ax, v111.x - v110.x, v110.x), fmaf(ax, v111.y - v110.y, v110.y));
+            r0 = make_float2(fmaf(ay, a1.x - a0.x, a0.x), fmaf(ay, a1.y - a0.y, a0.y));
+            r1 = make_float2(fmaf(ay, a3.x - a2.x, a2.x), fmaf(ay, a3.y - a2.y, a2.y));
+        }
+        const double sr = (double)fmaf(az, r1.x - r0.x, r0.x), si = (double)fmaf(az, r1.y - r0.y, r0.y);
         const int q = (hk.y + R) * W + (hk.x + R);
         // cos/sin of tpn (sx hx + sy ky) from the two tabulated phasors
         const double2 ex = tx[hk.x], ey = ty[hk.y + R];
