@@ -56,6 +56,10 @@ LAUNCHES_PER_PASS = 29
 # capture at the 2-degree grid (1.483 GB for 31,320 orientations), scaled to the
 # orientation count: operand B streams once per launch.
 GEMM_TRAFFIC_PER_ORIENT = 1.483e9 / 31320
+# dram__bytes_read.sum + dram__bytes_write.sum of one grouped fine-contraction launch over
+# a 64-particle pass of the box-256 workload (ncu capture of --profile-case learned)
+GROUPED_GEMM_TRAFFIC_PER_PASS = 3.802061e9 + 5.544448e6
+
 
 
 def rank_env():
@@ -467,7 +471,9 @@ def run_ours(args):
                                       f"those and of the grid neighbours of the best {w['nbr_best']}"},
             "roofline": dict(gemm_roofline(gst, peak_s, "k_gemm_argmax<bf16> (grouped, gathered sections)",
                                            f"{src} bf16_tflops_sustained"),
-                             traffic=None,
+                             traffic=GROUPED_GEMM_TRAFFIC_PER_PASS * min(1.0, B / 64.0),
+                             traffic_note="DRAM bytes per launch (64-particle pass), ncu capture of a launch "
+                                          "of the same shape",
                              note="the grouped fine contraction of the headline form; its launches are "
                                   "small (each particle's 625 origins x its few thousand gathered "
                                   "orientations), and the step is shared with the rescoring kernels "
