@@ -209,6 +209,11 @@ class Context:
         call("cryoim_learn_params", self._h, ptr(out), ptr(s), C.byref(n))
         return out
 
+    def learn_set_conv(self, tensor_cores: bool) -> None:
+        """The proposer's convolutions on the tensor cores (TF32 operands, the default)
+        or on the CUDA cores (FP32)."""
+        call("cryoim_learn_set_conv", self._h, 1 if tensor_cores else 0)
+
     def learn_forward(self, feat: np.ndarray, truth: np.ndarray | None = None, views: int = 0):
         """Scores (B, views, 128); with truth (B, 4) also the loss (B,) and the
         parameter gradients."""
@@ -449,3 +454,25 @@ def transform_ort(to: int, theta, phi, omega):
     o = np.ascontiguousarray(omega, np.float32).copy()
     call("cryoim_transform_ort", int(to), ptr(t), ptr(p), ptr(o), len(t))
     return t, p, o
+
+
+def conv3_check(x: np.ndarray, W: np.ndarray, bias: np.ndarray | None = None, relu: bool = False,
+                dpre: np.ndarray | None = None, tensor_cores: bool = True):
+    """Test hook of the proposer's 3x3 convolution kernels (circular in the 128 angles,
+    zero-padded in radius): x (B, Cin, H, 128), W (Cout, Cin, 3, 3) -> out (B, Cout, H,
+    128); with dpre (B, Cout, H, 128) also the weight and bias gradients.  Returns
+    (out, dW, db)."""
+    x = np.ascontiguousarray(x, np.float32)
+    W = np.ascontiguousarray(W, np.float32)
+    B, Cin, H, T = x.shape
+    Cout = W.shape[0]
+    if T != 128 or W.shape != (Cout, Cin, 3, 3):
+        raise ValueError("x must be (B, Cin, H, 128) and W (Cout, Cin, 3, 3)")
+    b = None if bias is None else np.ascontiguousarray(bias, np.float32)
+    g = None if dpre is None else np.ascontiguousarray(dpre, np.float32)
+    out = np.zeros((B, Cout, H, T), np.float32)
+    dW = np.zeros_like(W) if g is not None else None
+    db = np.zeros(Cout, np.float32) if g is not None else None
+    call("cryoim_conv3_check", 1 if tensor_cores else 0, ptr(x), B, Cin, H, ptr(W), ptr(b), Cout,
+         1 if relu else 0, ptr(out), ptr(g), ptr(dW), ptr(db))
+    return out, dW, db

@@ -143,6 +143,8 @@ SIGNATURES = {
     "cryoim_learn_load": [_vp, C.c_char_p],
     "cryoim_learn_params": [_vp, _vp, _vp, C.POINTER(C.c_int64)],
     "cryoim_learn_forward": [_vp, _vp, _vp, _i32, _vp, _vp, _vp],
+    "cryoim_learn_set_conv": [_vp, _i32],
+    "cryoim_conv3_check": [_i32, _vp, _i32, _i32, _i32, _vp, _vp, _i32, _i32, _vp, _vp, _vp, _vp],
     "cryoim_learn_features": [_vp, _vp, _vp, _i32, _vp],
     "cryoim_learn_views": [_vp, _vp, _ip],
     "cryoim_learn_render": [_vp, _vp, _vp, _vp, _i32, _f32, _i32, _vp],

@@ -11,6 +11,7 @@ include/cryoim.h carries no torch types).  Translation units:
 * center.cu -- -fmad=false: origin centring of icosprocess mode 3;
 * local.cu -- -fmad=false: local_refine's sub-particle refinement;
 * learn.cu -- the learned orientation proposer (features, CNN forward / backward, Adam);
+* conv_tc.cu -- the proposer's convolutions on the tcgen05 tensor cores (TF32);
 * io.cpp, local_host.cpp -- host only (g++): MRC / orientation / tnf files, local_box
   geometry and local_refine parameters.
 """
@@ -57,6 +58,7 @@ UNITS = {
     "center.cu": ["-fmad=false"],
     "local.cu": ["-fmad=false"],
     "learn.cu": [],
+    "conv_tc.cu": [],
 }
 
 

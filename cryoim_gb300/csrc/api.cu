@@ -232,12 +232,15 @@ struct LearnModel {
     DBuf<int> cell;
     DBuf<float> cellv;
     DBuf<float2> hscr;  // the head's frequency-domain scratch
+    bool conv_tc = true;  // convolutions on the tensor cores (TF32) or on the CUDA cores (FP32)
+    DBuf<int> cerr;       // set by a tensor-core convolution whose wait timed out
     void release() {
         for (DBuf<float>* b : {&w, &gr, &m, &v, &vview, &wflip, &feat, &a1, &a2, &p2, &a3, &p3, &a4, &p4, &g, &sc,
                                &dsc, &dg, &dp4, &da4, &dp3, &da3, &dp2, &da2, &da1, &loss, &truth, &cellv})
             b->release();
         cell.release();
         hscr.release();
+        cerr.release();
         ready = false;
         cap = 0;
     }
@@ -1009,8 +1012,10 @@ int learn_layout(Ctx* c, int V) {
     L.V = V;
     int r;
     if ((r = L.w.ensure(off)) || (r = L.gr.ensure(off)) || (r = L.m.ensure(off)) || (r = L.v.ensure(off)) ||
-        (r = L.vview.ensure(3 * (size_t)V)) || (r = L.wflip.ensure((size_t)LP_C2 * LP_C3 * 9)))
+        (r = L.vview.ensure(3 * (size_t)V)) || (r = L.wflip.ensure((size_t)LP_C2 * LP_C3 * 9)) ||
+        (r = L.cerr.ensure(1)))
         return r;
+    CK(cudaMemsetAsync(L.cerr.p, 0, sizeof(int), c->stream));
     std::vector<float> vv(3 * (size_t)V);
     const float d2r = host_angles().deg2rad;
     for (int i = 0; i < V; ++i) {
@@ -1046,17 +1051,42 @@ int learn_activations(Ctx* c, int B) {
     return CRYOIM_OK;
 }
 
+// The proposer's 3x3 convolutions: TF32 on the tensor cores (conv_tc.cu, the default) or
+// FP32 on the CUDA cores (learn.cu).
+cudaError_t lp_conv(Ctx* c, const float* in, int B, int Cin, int H, const float* W, const float* bias, int Cout,
+                    bool relu, float* out) {
+    LearnModel& L = c->lm;
+    if (L.conv_tc) return launch_lp_conv3_tc(in, B, Cin, H, W, bias, Cout, relu, out, L.cerr.p, c->stream);
+    return launch_lp_conv3(in, B, Cin, H, W, bias, Cout, relu, out, c->stream);
+}
+cudaError_t lp_wgrad(Ctx* c, const float* in, const float* dpre, int B, int Cin, int H, int Cout, float* dW,
+                     float* db) {
+    LearnModel& L = c->lm;
+    if (L.conv_tc) return launch_lp_conv3_wgrad_tc(in, dpre, B, Cin, H, Cout, dW, db, L.cerr.p, c->stream);
+    return launch_lp_conv3_wgrad(in, dpre, B, Cin, H, Cout, dW, db, c->stream);
+}
+// After the stream has drained: did a tensor-core convolution give up waiting?
+int learn_conv_status(Ctx* c) {
+    LearnModel& L = c->lm;
+    if (!L.cerr.p) return CRYOIM_OK;
+    int e = 0;
+    CK(cudaMemcpyAsync(&e, L.cerr.p, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
+    CK(cudaStreamSynchronize(c->stream));
+    if (e) return fail(CRYOIM_ERR_CUDA, "proposer convolution: tensor-core wait timed out");
+    return CRYOIM_OK;
+}
+
 // scores L.sc [B][V][NT] of the features in L.feat
 int learn_forward(Ctx* c, int B) {
     LearnModel& L = c->lm;
     const float* w = L.w.p;
     cudaStream_t st = c->stream;
-    CK(launch_lp_conv3(L.feat.p, B, 1, LP_NR, w + L.oW[0], w + L.ob[0], LP_C1, true, L.a1.p, st));
-    CK(launch_lp_conv3(L.a1.p, B, LP_C1, LP_NR, w + L.oW[1], w + L.ob[1], LP_C2, true, L.a2.p, st));
+    CK(lp_conv(c, L.feat.p, B, 1, LP_NR, w + L.oW[0], w + L.ob[0], LP_C1, true, L.a1.p));
+    CK(lp_conv(c, L.a1.p, B, LP_C1, LP_NR, w + L.oW[1], w + L.ob[1], LP_C2, true, L.a2.p));
     launch_lp_pool(L.a2.p, B, LP_C2, LP_NR / 2, L.p2.p, st);
-    CK(launch_lp_conv3(L.p2.p, B, LP_C2, LP_NR / 2, w + L.oW[2], w + L.ob[2], LP_C3, true, L.a3.p, st));
+    CK(lp_conv(c, L.p2.p, B, LP_C2, LP_NR / 2, w + L.oW[2], w + L.ob[2], LP_C3, true, L.a3.p));
     launch_lp_pool(L.a3.p, B, LP_C3, LP_NR / 4, L.p3.p, st);
-    CK(launch_lp_conv3(L.p3.p, B, LP_C3, LP_NR / 4, w + L.oW[3], w + L.ob[3], LP_C4, true, L.a4.p, st));
+    CK(lp_conv(c, L.p3.p, B, LP_C3, LP_NR / 4, w + L.oW[3], w + L.ob[3], LP_C4, true, L.a4.p));
     launch_lp_pool(L.a4.p, B, LP_C4, LP_NR / 8, L.p4.p, st);
     launch_lp_mix(L.p4.p, B, w + L.oW[4], w + L.ob[4], L.g.p, st);
     CK(launch_lp_head(L.g.p, w + L.oT, B, L.V, L.sc.p, L.hscr.p, st));
@@ -1076,22 +1106,22 @@ int learn_backward(Ctx* c, int B) {
     launch_lp_mix_grad(L.p4.p, L.dg.p, B, w + L.oW[4], L.dp4.p, gr + L.oW[4], gr + L.ob[4], st);
     // layer 4
     launch_lp_pool_grad(L.dp4.p, B, LP_C4, LP_NR / 8, L.a4.p, L.da4.p, st);
-    CK(launch_lp_conv3_wgrad(L.p3.p, L.da4.p, B, LP_C3, LP_NR / 4, LP_C4, gr + L.oW[3], gr + L.ob[3], st));
+    CK(lp_wgrad(c, L.p3.p, L.da4.p, B, LP_C3, LP_NR / 4, LP_C4, gr + L.oW[3], gr + L.ob[3]));
     launch_lp_flip(w + L.oW[3], LP_C4, LP_C3, L.wflip.p, st);
-    CK(launch_lp_conv3(L.da4.p, B, LP_C4, LP_NR / 4, L.wflip.p, nullptr, LP_C3, false, L.dp3.p, st));
+    CK(lp_conv(c, L.da4.p, B, LP_C4, LP_NR / 4, L.wflip.p, nullptr, LP_C3, false, L.dp3.p));
     // layer 3
     launch_lp_pool_grad(L.dp3.p, B, LP_C3, LP_NR / 4, L.a3.p, L.da3.p, st);
-    CK(launch_lp_conv3_wgrad(L.p2.p, L.da3.p, B, LP_C2, LP_NR / 2, LP_C3, gr + L.oW[2], gr + L.ob[2], st));
+    CK(lp_wgrad(c, L.p2.p, L.da3.p, B, LP_C2, LP_NR / 2, LP_C3, gr + L.oW[2], gr + L.ob[2]));
     launch_lp_flip(w + L.oW[2], LP_C3, LP_C2, L.wflip.p, st);
-    CK(launch_lp_conv3(L.da3.p, B, LP_C3, LP_NR / 2, L.wflip.p, nullptr, LP_C2, false, L.dp2.p, st));
+    CK(lp_conv(c, L.da3.p, B, LP_C3, LP_NR / 2, L.wflip.p, nullptr, LP_C2, false, L.dp2.p));
     // layer 2
     launch_lp_pool_grad(L.dp2.p, B, LP_C2, LP_NR / 2, L.a2.p, L.da2.p, st);
-    CK(launch_lp_conv3_wgrad(L.a1.p, L.da2.p, B, LP_C1, LP_NR, LP_C2, gr + L.oW[1], gr + L.ob[1], st));
+    CK(lp_wgrad(c, L.a1.p, L.da2.p, B, LP_C1, LP_NR, LP_C2, gr + L.oW[1], gr + L.ob[1]));
     launch_lp_flip(w + L.oW[1], LP_C2, LP_C1, L.wflip.p, st);
-    CK(launch_lp_conv3(L.da2.p, B, LP_C2, LP_NR, L.wflip.p, nullptr, LP_C1, false, L.da1.p, st));
+    CK(lp_conv(c, L.da2.p, B, LP_C2, LP_NR, L.wflip.p, nullptr, LP_C1, false, L.da1.p));
     // layer 1
     launch_lp_relu_grad(L.a1.p, L.da1.p, (long)B * LP_C1 * LP_NR * nt, L.da1.p, st);
-    CK(launch_lp_conv3_wgrad(L.feat.p, L.da1.p, B, 1, LP_NR, LP_C1, gr + L.oW[0], gr + L.ob[0], st));
+    CK(lp_wgrad(c, L.feat.p, L.da1.p, B, 1, LP_NR, LP_C1, gr + L.oW[0], gr + L.ob[0]));
     return CRYOIM_OK;
 }
 
@@ -1291,6 +1321,7 @@ int learn_train_impl(Ctx* c, const float* map3d, const cryoim_learn_opts* o, flo
         if ((r = check_flag(c))) return r;
     }
     CK(cudaStreamSynchronize(c->stream));
+    if ((r = learn_conv_status(c))) return r;
     L.step = c->p.searchstep;
     L.ready = true;
     if (stats) {
@@ -1316,6 +1347,7 @@ int learned_lists(Ctx* c, int nb, int kl, int nbf, std::vector<std::vector<int>>
     std::vector<int> cell((size_t)nb * kl);
     CK(cudaMemcpyAsync(cell.data(), L.cell.p, sizeof(int) * cell.size(), cudaMemcpyDeviceToHost, c->stream));
     CK(cudaStreamSynchronize(c->stream));
+    if ((r = learn_conv_status(c))) return r;
     const ViewGrid& g = c->cgrid;
     const int span_c = 2 * g.nph + 1;
     const float dw = 180.0f / LP_NT, step = c->p.searchstep;
@@ -2988,6 +3020,68 @@ int cryoim_learn_forward(void* ctx, const float* feat, const float* truth, int32
         if (grads) CK(cudaMemcpyAsync(grads, L.gr.p, sizeof(float) * L.nparam, cudaMemcpyDeviceToHost, c->stream));
     }
     CK(cudaStreamSynchronize(c->stream));
+    return learn_conv_status(c);
+}
+
+// Test hook of the proposer's convolution kernels on host arrays (current device, its
+// default stream): out = conv(x) (+ bias, ReLU) and, when dpre is given, the weight and
+// bias gradients dW, db of dpre.  tensor_cores: 1 = conv_tc.cu (TF32), 0 = learn.cu (FP32).
+int cryoim_conv3_check(int32_t tensor_cores, const float* x, int32_t B, int32_t Cin, int32_t H, const float* W,
+                       const float* bias, int32_t Cout, int32_t relu, float* out, const float* dpre, float* dW,
+                       float* db) {
+    if (!x || !W || !out || B < 1 || H < 1 || Cin < 1 || Cin > 32 || (Cout != 16 && Cout != 32) ||
+        (dpre && (!dW || !db)))
+        return fail(CRYOIM_ERR_ARG, "bad arguments");
+    const size_t nx = (size_t)B * Cin * H * LP_NT, ny = (size_t)B * Cout * H * LP_NT, nw = (size_t)Cout * Cin * 9;
+    DBuf<float> dx, dy, dwt, dbias, dg, dgw, dgb;
+    DBuf<int> derr;
+    int r;
+    if ((r = dx.ensure(nx)) || (r = dy.ensure(ny)) || (r = dwt.ensure(nw)) || (r = dbias.ensure(Cout)) ||
+        (r = derr.ensure(1)) || (dpre && ((r = dg.ensure(ny)) || (r = dgw.ensure(nw)) || (r = dgb.ensure(Cout)))))
+        return r;
+    auto done = [&](int code) {
+        for (DBuf<float>* b : {&dx, &dy, &dwt, &dbias, &dg, &dgw, &dgb}) b->release();
+        derr.release();
+        return code;
+    };
+    cudaError_t e = cudaSuccess;
+    auto ok = [&](cudaError_t x) { if (e == cudaSuccess) e = x; };
+    ok(cudaMemcpy(dx.p, x, nx * 4, cudaMemcpyHostToDevice));
+    ok(cudaMemcpy(dwt.p, W, nw * 4, cudaMemcpyHostToDevice));
+    ok(cudaMemset(dbias.p, 0, Cout * 4));
+    if (bias) ok(cudaMemcpy(dbias.p, bias, Cout * 4, cudaMemcpyHostToDevice));
+    ok(cudaMemset(derr.p, 0, sizeof(int)));
+    if (e == cudaSuccess)
+        ok(tensor_cores ? launch_lp_conv3_tc(dx.p, B, Cin, H, dwt.p, bias ? dbias.p : nullptr, Cout, relu != 0, dy.p,
+                                             derr.p, 0)
+                        : launch_lp_conv3(dx.p, B, Cin, H, dwt.p, bias ? dbias.p : nullptr, Cout, relu != 0, dy.p, 0));
+    if (dpre && e == cudaSuccess) {
+        ok(cudaMemcpy(dg.p, dpre, ny * 4, cudaMemcpyHostToDevice));
+        ok(cudaMemset(dgw.p, 0, nw * 4));
+        ok(cudaMemset(dgb.p, 0, Cout * 4));
+        if (e == cudaSuccess)
+            ok(tensor_cores ? launch_lp_conv3_wgrad_tc(dx.p, dg.p, B, Cin, H, Cout, dgw.p, dgb.p, derr.p, 0)
+                            : launch_lp_conv3_wgrad(dx.p, dg.p, B, Cin, H, Cout, dgw.p, dgb.p, 0));
+    }
+    ok(cudaDeviceSynchronize());
+    int flag = 0;
+    ok(cudaMemcpy(&flag, derr.p, sizeof(int), cudaMemcpyDeviceToHost));
+    ok(cudaMemcpy(out, dy.p, ny * 4, cudaMemcpyDeviceToHost));
+    if (dpre) {
+        ok(cudaMemcpy(dW, dgw.p, nw * 4, cudaMemcpyDeviceToHost));
+        ok(cudaMemcpy(db, dgb.p, Cout * 4, cudaMemcpyDeviceToHost));
+    }
+    if (e != cudaSuccess) return done(fail(CRYOIM_ERR_CUDA, "%s", cudaGetErrorString(e)));
+    if (flag) return done(fail(CRYOIM_ERR_CUDA, "tensor-core convolution wait timed out"));
+    return done(CRYOIM_OK);
+}
+
+int cryoim_learn_set_conv(void* ctx, int32_t tensor_cores) {
+    Ctx* c = as_ctx(ctx);
+    int r = check_ready(c, false);
+    if (r) return r;
+    if (tensor_cores != 0 && tensor_cores != 1) return fail(CRYOIM_ERR_ARG, "tensor_cores must be 0 or 1");
+    c->lm.conv_tc = tensor_cores != 0;
     return CRYOIM_OK;
 }
 

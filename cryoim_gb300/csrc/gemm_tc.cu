@@ -28,6 +28,7 @@
 
 #include "../../include/cryoim.h"
 #include "kernels.h"
+#include "tc.cuh"
 
 namespace cryoim {
 namespace {
@@ -47,47 +48,15 @@ constexpr uint32_t IDESC_BF16 = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)
                                 ((uint32_t)(GM >> 4) << 24);
 constexpr uint32_t IDESC_E4M3 = (1u << 4) | ((uint32_t)(GN >> 3) << 17) | ((uint32_t)(GM >> 4) << 24);
 
-__device__ __forceinline__ uint32_t su32(const void* p) {
-    return (uint32_t)__cvta_generic_to_shared(p);
-}
-__device__ __forceinline__ uint64_t gtimer() {
-    uint64_t t;
-    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
-    return t;
-}
-__device__ __forceinline__ void mbar_init(uint64_t* b, uint32_t n) {
-    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(su32(b)), "r"(n) : "memory");
-}
-__device__ __forceinline__ bool mbar_try(uint64_t* b, uint32_t par) {
-    uint32_t ok;
-    asm volatile(
-        "{\n\t.reg .pred p;\n\t"
-        "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
-        "selp.u32 %0, 1, 0, p;\n}"
-        : "=r"(ok)
-        : "r"(su32(b)), "r"(par)
-        : "memory");
-    return ok != 0;
-}
-// Bounded wait.  abort_on_err: also give up as soon as another role has failed.
+using tc::su32;
+using tc::mbar_init;
+using tc::mbar_expect_tx;
+using tc::mbar_arrive;
+using tc::sdesc;
+using tc::tmem_ld32;
+// Bounded wait with this kernel's limit (2 s).
 __device__ __forceinline__ bool mbar_wait(uint64_t* b, uint32_t par, int* err, bool abort_on_err) {
-    if (mbar_try(b, par)) return true;
-    const uint64_t t0 = gtimer();
-    while (true) {
-        if (mbar_try(b, par)) return true;
-        if (abort_on_err && *(volatile int*)err) return false;
-        if (gtimer() - t0 > WAIT_NS) {
-            atomicExch(err, 1);
-            return false;
-        }
-    }
-}
-__device__ __forceinline__ void mbar_expect_tx(uint64_t* b, uint32_t bytes) {
-    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(su32(b)), "r"(bytes)
-                 : "memory");
-}
-__device__ __forceinline__ void mbar_arrive(uint64_t* b) {
-    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(su32(b)) : "memory");
+    return tc::mbar_wait(b, par, err, abort_on_err, WAIT_NS);
 }
 __device__ __forceinline__ void tma_load_2d(void* dst, const CUtensorMap* tm, int c0, int c1,
                                             uint64_t* b) {
@@ -97,17 +66,9 @@ __device__ __forceinline__ void tma_load_2d(void* dst, const CUtensorMap* tm, in
         "l"((uint64_t)tm), "r"(c0), "r"(c1), "r"(su32(b))
         : "memory");
 }
-__device__ __forceinline__ void tc_fence_before() {
-    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
-}
-__device__ __forceinline__ void tc_fence_after() {
-    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-}
-__device__ __forceinline__ void tc_commit(uint64_t* b) {
-    asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
-                     su32(b))
-                 : "memory");
-}
+__device__ __forceinline__ void tc_fence_before() { tc::fence_before(); }
+__device__ __forceinline__ void tc_fence_after() { tc::fence_after(); }
+__device__ __forceinline__ void tc_commit(uint64_t* b) { tc::commit(b); }
 template <bool F8>
 __device__ __forceinline__ void tc_mma(uint32_t d, uint64_t a, uint64_t bdesc, uint32_t acc) {
     if constexpr (F8) {
@@ -126,33 +87,6 @@ __device__ __forceinline__ void tc_mma(uint32_t d, uint64_t a, uint64_t bdesc, u
             : "memory");
     }
 }
-// shared-memory matrix descriptor: K-major, 128-byte swizzle, 8-row atoms 1024 B apart
-__device__ __forceinline__ uint64_t sdesc(uint32_t saddr) {
-    uint64_t d = 0;
-    d |= (uint64_t)((saddr & 0x3FFFFu) >> 4);
-    d |= (uint64_t)1 << 16;          // leading byte offset (unused for swizzled K-major)
-    d |= (uint64_t)(1024 >> 4) << 32;  // stride byte offset
-    d |= (uint64_t)1 << 46;          // descriptor version for tcgen05
-    d |= (uint64_t)2 << 61;          // SWIZZLE_128B
-    return d;
-}
-__device__ __forceinline__ void tmem_ld32(uint32_t taddr, float* v) {
-    uint32_t r[32];
-    asm volatile(
-        "tcgen05.ld.sync.aligned.32x32b.x32.b32 "
-        "{%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,"
-        "%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];"
-        : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]),
-          "=r"(r[7]), "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]),
-          "=r"(r[14]), "=r"(r[15]), "=r"(r[16]), "=r"(r[17]), "=r"(r[18]), "=r"(r[19]),
-          "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]), "=r"(r[24]), "=r"(r[25]),
-          "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
-        : "r"(taddr));
-    asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
-#pragma unroll
-    for (int i = 0; i < 32; ++i) v[i] = __uint_as_float(r[i]);
-}
-
 // Tile t of the launch -> its product, tile coordinates and operand rows.
 struct TileAt {
     int mt, nt, a_row, b_row, m_valid, n_valid, n_tiles, topv_off;

@@ -210,6 +210,12 @@ cudaError_t launch_lp_conv3(const float* in, int B, int Cin, int H, const float*
 // accumulates into dW, db (zero them first)
 cudaError_t launch_lp_conv3_wgrad(const float* in, const float* dpre, int B, int Cin, int H, int Cout, float* dW,
                                   float* db, cudaStream_t st);
+// The same two convolutions on the tensor cores (conv_tc.cu, tcgen05 kind::tf32): Cin <= 32
+// (wgrad: 1 or a multiple of 8), Cout 16 or 32; *err is set if a wait timed out.
+cudaError_t launch_lp_conv3_tc(const float* in, int B, int Cin, int H, const float* W, const float* bias, int Cout,
+                               bool relu, float* out, int* err, cudaStream_t st);
+cudaError_t launch_lp_conv3_wgrad_tc(const float* in, const float* dpre, int B, int Cin, int H, int Cout, float* dW,
+                                     float* db, int* err, cudaStream_t st);
 void launch_lp_relu_grad(const float* out, const float* dout, long n, float* dpre, cudaStream_t st);
 void launch_lp_flip(const float* W, int Cout, int Cin, float* Wf, cudaStream_t st);
 void launch_lp_pool(const float* a, int B, int C, int Hout, float* p, cudaStream_t st);

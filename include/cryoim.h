@@ -476,6 +476,17 @@ int cryoim_learn_load(void* ctx, const char* path);
 int cryoim_learn_params(void* ctx, float* get, const float* set, int64_t* n);
 int cryoim_learn_forward(void* ctx, const float* feat, const float* truth, int32_t B, float* scores,
                          float* loss, float* grads);
+/* Arithmetic of the proposer's 3x3 convolutions (training and inference): 1 (default):
+ * tcgen05 tensor cores, operands rounded to TF32 (10 mantissa bits, to nearest, ties
+ * away from zero), FP32 accumulation; 0: FP32 on the CUDA cores. */
+int cryoim_learn_set_conv(void* ctx, int32_t tensor_cores);
+/* Test hook of the convolution kernels on host arrays (current device): x [B][Cin][H][128],
+ * W [Cout][Cin][3][3], bias [Cout] (may be NULL) -> out [B][Cout][H][128] (circular in the
+ * 128 angles, zero-padded in H, ReLU if relu); with dpre [B][Cout][H][128] also the weight
+ * and bias gradients dW, db.  Cin <= 32 (1 or a multiple of 8 with dpre), Cout 16 or 32. */
+int cryoim_conv3_check(int32_t tensor_cores, const float* x, int32_t B, int32_t Cin, int32_t H, const float* W,
+                       const float* bias, int32_t Cout, int32_t relu, float* out, const float* dpre, float* dW,
+                       float* db);
 /* The proposer's training renderer: B particles of the nx^3 map (host) at eul[b] =
  * (theta, phi, omega) with par[b] = (df1, df2, astig, x, y) (CTF if apply_ctf), white
  * noise at snr (0: none) from seed -> imgs [B][nx][nx].  Fourier slices of the twice

@@ -16,11 +16,56 @@ NR, NT, CM, MIXK = 64, 128, 16, 256
 CONV = [(1, 16), (16, 32), (32, 32), (32, 32)]
 
 
-def torch_reference(w, feat, truth, views, sv):
+def tf32_round(t):
+    """FP32 -> TF32 (10 mantissa bits), to nearest with ties away from zero, as
+    cvt.rna.tf32.f32 rounds the tensor-core convolutions' operands."""
+    import torch
+    u = t.detach().to(torch.float32).contiguous().view(torch.int32)
+    return ((u + 0x1000) & -8192).view(torch.float32)
+
+
+def conv_tf32_function():
+    """A 3x3 convolution (circular in angle, zero-padded in radius) whose operands are
+    rounded to TF32 and whose products are summed in FP64, forward and backward, as
+    conv_tc.cu computes it: the data gradient from the rounded output gradient and
+    weights, the weight gradient from the rounded output gradient and inputs, the bias
+    gradient from the unrounded output gradient."""
+    import torch
+    F = torch.nn.functional
+
+    def pad(a):
+        return F.pad(F.pad(a, (1, 1, 0, 0), mode="circular"), (0, 0, 1, 1))
+
+    class ConvTF32(torch.autograd.Function):
+        @staticmethod
+        def forward(ctx, x, W, b):
+            xr, Wr = tf32_round(x).double(), tf32_round(W).double()
+            ctx.save_for_backward(xr, Wr)
+            return (F.conv2d(pad(xr), Wr) + b.double()[None, :, None, None]).float()
+
+        @staticmethod
+        def backward(ctx, gy):
+            xr, Wr = ctx.saved_tensors
+            gr = tf32_round(gy).double()
+            dx = F.conv2d(pad(gr), Wr.flip(2, 3).transpose(0, 1))
+            xp = pad(xr)
+            H, T = xr.shape[2], xr.shape[3]
+            dW = torch.zeros_like(Wr)
+            for dh in range(3):
+                for dt in range(3):
+                    dW[:, :, dh, dt] = torch.einsum("boht,bcht->oc", gr, xp[:, :, dh:dh + H, dt:dt + T])
+            return dx.float(), dW.float(), gy.double().sum((0, 2, 3)).float()
+
+    return ConvTF32.apply
+
+
+def torch_reference(w, feat, truth, views, sv, tf32=False):
     """The network of learn.cu in torch FP32 (CPU): scores, per-particle loss and the
-    gradients of the mean loss, flattened in the library's parameter order."""
+    gradients of the mean loss, flattened in the library's parameter order.  tf32: the
+    convolutions as the tensor-core kernels compute them (conv_tf32_function)."""
     torch = pytest.importorskip("torch")
     F = torch.nn.functional
+    conv_tf32 = conv_tf32_function() if tf32 else None
     wt = torch.tensor(w, dtype=torch.float32, requires_grad=True)
     x = torch.tensor(feat, dtype=torch.float32)[:, None]
     B = x.shape[0]
@@ -35,9 +80,12 @@ def torch_reference(w, feat, truth, views, sv):
     for layer, (ci, co) in enumerate(CONV):
         W = take(co * ci * 9).reshape(co, ci, 3, 3)
         b = take(co)
-        x = F.pad(x, (1, 1, 0, 0), mode="circular")
-        x = F.pad(x, (0, 0, 1, 1))
-        x = F.relu(F.conv2d(x, W, b))
+        if tf32:
+            x = F.relu(conv_tf32(x, W, b))
+        else:
+            x = F.pad(x, (1, 1, 0, 0), mode="circular")
+            x = F.pad(x, (0, 0, 1, 1))
+            x = F.relu(F.conv2d(x, W, b))
         if layer >= 1:
             x = F.avg_pool2d(x, (2, 1))
     W5 = take(CM * MIXK).reshape(CM, MIXK)
@@ -89,8 +137,12 @@ def random_weights(n, V, rng):
     return w
 
 
-def test_forward_backward_match_torch(lctx):
+@pytest.mark.parametrize("tensor_cores", [False, True])
+def test_forward_backward_match_torch(lctx, tensor_cores):
+    """FP32 convolutions against the FP32 restatement; tensor-core convolutions against
+    the restatement whose convolutions round their operands to TF32 the same way."""
     ctx, p = lctx
+    ctx.learn_set_conv(tensor_cores)
     rng = np.random.default_rng(5)
     views = ctx.learn_views()
     V = len(views)
@@ -107,7 +159,9 @@ def test_forward_backward_match_torch(lctx):
                         math.cos(th * d2r)]
         truth[b, 3] = rng.integers(NT)
     sc, loss, gr = ctx.learn_forward(feat, truth, views=V)
-    rsc, rloss, rgr = torch_reference(w, feat, truth, views.astype(np.float64), 2.0 * p.searchstep)
+    rsc, rloss, rgr = torch_reference(w, feat, truth, views.astype(np.float64), 2.0 * p.searchstep,
+                                      tf32=tensor_cores)
+    ctx.learn_set_conv(True)
     assert np.abs(sc - rsc).max() < 1e-4 * np.abs(rsc).max() + 1e-6
     assert np.allclose(loss, rloss, rtol=1e-4, atol=1e-5)
     # gradients, block by block (conv 1-4 weights and biases, mix, templates)
@@ -115,10 +169,15 @@ def test_forward_backward_match_torch(lctx):
     for ci, co in CONV:
         sizes += [co * ci * 9, co]
     sizes += [CM * MIXK, CM, V * CM * NT]
+    # TF32: an activation the kernels and the restatement compute one FP32 ulp apart can
+    # round to TF32 values one TF32 ulp (2^-10 relative) apart; through the backward
+    # pass such flips move a gradient block by a few 1e-3 of its maximum.  The
+    # convolutions' own arithmetic is pinned exactly by tests/test_gpu_conv_tc.py.
+    gtol = 5e-3 if tensor_cores else 2e-3
     off = 0
     for k, sz in enumerate(sizes):
         a, b = gr[off:off + sz], rgr[off:off + sz]
-        assert np.abs(a - b).max() <= 2e-3 * np.abs(b).max() + 1e-7, (k, np.abs(a - b).max(), np.abs(b).max())
+        assert np.abs(a - b).max() <= gtol * np.abs(b).max() + 1e-7, (k, np.abs(a - b).max(), np.abs(b).max())
         off += sz
 
 
