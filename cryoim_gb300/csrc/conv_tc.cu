@@ -119,37 +119,41 @@ __global__ void __launch_bounds__(CT_NT) k_conv3_tc(ConvTcArgs a) {
     const uint32_t tmem = *tslot;
     constexpr uint32_t idesc = idesc_tf32(N);
 
-    // input row hh of sample b -> ring slot; thread t writes angle t's 32 channels
-    auto stage = [&](int slot, int b, int hh) {
-        unsigned char* dst = sX + slot * CT_ROW_BYTES + t * 128;
+    // input row hh of sample b: thread t loads angle t's channels into registers (load),
+    // rounds them to TF32 and writes them to a ring slot (put)
+    float pre[32];
+    const long cs = (long)H * CT_NT;
+    auto load = [&](int b, int hh) {
         const bool ok = hh >= 0 && hh < H;
         const float* src = a.in + ((long)b * Cin * H + (ok ? hh : 0)) * CT_NT + t;
-        const long cs = (long)H * CT_NT;
 #pragma unroll
-        for (int c4 = 0; c4 < 8; ++c4) {
-            float4 v;
-            const int c = 4 * c4;
-            v.x = (ok && c + 0 < Cin) ? tf32r(__ldg(src + (c + 0) * cs)) : 0.f;
-            v.y = (ok && c + 1 < Cin) ? tf32r(__ldg(src + (c + 1) * cs)) : 0.f;
-            v.z = (ok && c + 2 < Cin) ? tf32r(__ldg(src + (c + 2) * cs)) : 0.f;
-            v.w = (ok && c + 3 < Cin) ? tf32r(__ldg(src + (c + 3) * cs)) : 0.f;
-            *(float4*)(dst + ((c4 ^ (t & 7)) << 4)) = v;
-        }
+        for (int c = 0; c < 32; ++c) pre[c] = (ok && c < Cin) ? __ldg(src + c * cs) : 0.f;
+    };
+    auto put = [&](int slot) {
+        unsigned char* dst = sX + slot * CT_ROW_BYTES + t * 128;
+#pragma unroll
+        for (int c4 = 0; c4 < 8; ++c4)
+            *(float4*)(dst + ((c4 ^ (t & 7)) << 4)) = make_float4(tf32r(pre[4 * c4]), tf32r(pre[4 * c4 + 1]),
+                                                                   tf32r(pre[4 * c4 + 2]), tf32r(pre[4 * c4 + 3]));
     };
 
     uint32_t phase = 0;
     int cur_b = -1, prev_h = -2;
-    bool ok = true;
+    bool ok = true, have = false;  // have: pre already holds the row this step stages
     for (long q = q0; q < q1; ++q) {
         const int b = (int)(q / H), h = (int)(q - (long)b * H);
         // ring slot of input row h' is (h' + 1) % 3
         if (b != cur_b || h != prev_h + 1) {
-            stage(h % 3, b, h - 1);
-            stage((h + 1) % 3, b, h);
+            load(b, h - 1);
+            put(h % 3);
+            load(b, h);
+            put((h + 1) % 3);
             cur_b = b;
+            have = false;
         }
         prev_h = h;
-        stage((h + 2) % 3, b, h + 1);
+        if (!have) load(b, h + 1);
+        put((h + 2) % 3);
         tc::fence_proxy_async();
         tc::fence_before();
         __syncthreads();
@@ -164,6 +168,12 @@ __global__ void __launch_bounds__(CT_NT) k_conv3_tc(ConvTcArgs a) {
                     mma_tf32(tmem, tc::sdesc(xa + kk * 32), tc::sdesc(wb + kk * 32), idesc, (dh | kk) != 0);
             }
             tc::commit(bar);
+        }
+        // the row the next step stages is loaded while the MMAs and the epilogue run
+        have = false;
+        if (q + 1 < q1 && h + 1 < H) {
+            load(b, h + 2);
+            have = true;
         }
         const bool got = tc::mbar_wait(bar, phase, a.err, false, CT_WAIT_NS);
         phase ^= 1u;
@@ -273,13 +283,20 @@ __global__ void __launch_bounds__(CT_NT) k_conv3_wgrad_tc(ConvWgTcArgs a) {
     float dbacc[COUT];
 #pragma unroll
     for (int co = 0; co < COUT; ++co) dbacc[co] = 0.f;
-    auto stageA = [&](int b, int h) {
+    // dpre row h (preA: this thread's angle, every co) and input row hh (preB: every ci)
+    // are loaded into registers a step ahead, then rounded and written to shared memory
+    float preA[COUT], preB[32];
+    const long cs = (long)H * CT_NT;
+    auto loadA = [&](int b, int h) {
         const float* src = a.dpre + ((long)b * COUT * H + h) * CT_NT + t;
 #pragma unroll
+        for (int co = 0; co < COUT; ++co) preA[co] = __ldg(src + co * cs);
+    };
+    auto putA = [&]() {
+#pragma unroll
         for (int co = 0; co < COUT; ++co) {
-            const float gv = __ldg(src + (long)co * H * CT_NT);
-            dbacc[co] += gv;
-            const float v = tf32r(gv);
+            dbacc[co] += preA[co];
+            const float v = tf32r(preA[co]);
 #pragma unroll
             for (int dt = 0; dt < 3; ++dt) {
                 const int s = (t + dt - 1) & (CT_NT - 1), m = dt * COUT + co;
@@ -287,29 +304,39 @@ __global__ void __launch_bounds__(CT_NT) k_conv3_wgrad_tc(ConvWgTcArgs a) {
             }
         }
     };
-    auto stageB = [&](int slot, int b, int hh) {
-        unsigned char* dst = sB + slot * g.SLOT + (t >> 5) * g.PB;
+    auto loadB = [&](int b, int hh) {
         const bool ok = hh >= 0 && hh < H;
         const float* src = a.in + ((long)b * Cin * H + (ok ? hh : 0)) * CT_NT + t;
-        for (int ci = 0; ci < Cin; ++ci) {
-            const float v = ok ? tf32r(__ldg(src + (long)ci * H * CT_NT)) : 0.f;
-            *(float*)(dst + tc::swz128_off4(ci, t & 31)) = v;
-        }
+#pragma unroll
+        for (int c = 0; c < 32; ++c) preB[c] = (ok && c < Cin) ? __ldg(src + c * cs) : 0.f;
+    };
+    auto putB = [&](int slot) {
+        unsigned char* dst = sB + slot * g.SLOT + (t >> 5) * g.PB;
+#pragma unroll
+        for (int ci = 0; ci < 32; ++ci)
+            if (ci < Cin) *(float*)(dst + tc::swz128_off4(ci, t & 31)) = tf32r(preB[ci]);
     };
 
     uint32_t phase = 0;
     int cur_b = -1, prev_h = -2;
-    bool ok = true;
+    bool ok = true, have = false;  // have: preA / preB already hold this step's rows
     for (long q = q0; q < q1; ++q) {
         const int b = (int)(q / H), h = (int)(q - (long)b * H);
         if (b != cur_b || h != prev_h + 1) {
-            stageB(h % 3, b, h - 1);
-            stageB((h + 1) % 3, b, h);
+            loadB(b, h - 1);
+            putB(h % 3);
+            loadB(b, h);
+            putB((h + 1) % 3);
             cur_b = b;
+            have = false;
         }
         prev_h = h;
-        stageB((h + 2) % 3, b, h + 1);
-        stageA(b, h);
+        if (!have) {
+            loadB(b, h + 1);
+            loadA(b, h);
+        }
+        putB((h + 2) % 3);
+        putA();
         tc::fence_proxy_async();
         tc::fence_before();
         __syncthreads();
@@ -326,6 +353,13 @@ __global__ void __launch_bounds__(CT_NT) k_conv3_wgrad_tc(ConvWgTcArgs a) {
                 }
             }
             tc::commit(bar);
+        }
+        // the next step's rows are loaded while the MMAs run
+        have = false;
+        if (q + 1 < q1 && h + 1 < H) {
+            loadB(b, h + 2);
+            loadA(b, h + 1);
+            have = true;
         }
         const bool got = tc::mbar_wait(bar, phase, a.err, false, CT_WAIT_NS);
         phase ^= 1u;
