@@ -17,6 +17,7 @@
 #include <map>
 #include <random>
 #include <string>
+#include <thread>
 #include <vector>
 
 #include "../../include/cryoim.h"
@@ -148,11 +149,10 @@ void euler_from(const float* r, float* th, float* ph, float* om) {
 template <class T> struct DBuf {
     T* p = nullptr;
     size_t n = 0;
+    bool own = true;  // false: another context's buffer, used read-only and never freed here
     int ensure(size_t want) {
         if (want <= n) return 0;
-        if (p) cudaFree(p);
-        p = nullptr;
-        n = 0;
+        release();
         cudaError_t e = cudaMalloc(&p, want * sizeof(T));
         if (e != cudaSuccess) {
             p = nullptr;
@@ -162,10 +162,17 @@ template <class T> struct DBuf {
         n = want;
         return 0;
     }
+    void borrow(const DBuf& o) {
+        release();
+        p = o.p;
+        n = o.n;
+        own = false;
+    }
     void release() {
-        if (p) cudaFree(p);
+        if (p && own) cudaFree(p);
         p = nullptr;
         n = 0;
+        own = true;
     }
 };
 
@@ -345,7 +352,12 @@ struct Ctx {
     long long prof_gemm_launches = 0;
     double prof_gemm_flops = 0.0;
 
+    // second pass lane of the contraction search (refresh_lane): its own stream and
+    // per-pass buffers, this context's read-only state borrowed
+    Ctx* lane2 = nullptr;
+
     ~Ctx() {
+        delete lane2;
         cudaSetDevice(device);
         for (auto& kv : plans) cufftDestroy(kv.second);
         ops.release(); tband.release(); tfcut0.release(); tort.release(); d_views.release();
@@ -1419,6 +1431,72 @@ int ensure_bmat8(Ctx* c) {
     return CRYOIM_OK;
 }
 
+// The second pass lane of the contraction search: a context with its own stream, cuFFT
+// plans, per-pass buffers and proposer activations, and c's read-only state borrowed
+// (parameters, templates, search grids, origin grids, reference-map sections, proposer
+// weights).  Refreshed at every multi-pass call, after c's state is complete.
+int refresh_lane(Ctx* c) {
+    if (!c->lane2) {
+        Ctx* h = new (std::nothrow) Ctx();
+        if (!h) return fail(CRYOIM_ERR_NOMEM, "second lane context");
+        h->device = c->device;
+        c->lane2 = h;
+        CK(cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking));
+        h->own_stream = true;
+    }
+    Ctx* h = c->lane2;
+    h->p = c->p;
+    h->have_params = c->have_params;
+    h->bd = c->bd;
+    h->batch = c->batch;
+    h->ops.borrow(c->ops);
+    h->T = c->T;
+    h->tmpl = c->tmpl;
+    h->tband.borrow(c->tband);
+    h->tfcut0.borrow(c->tfcut0);
+    h->tort.borrow(c->tort);
+    h->grid_ready = c->grid_ready;
+    h->nth = c->nth; h->nph = c->nph; h->nom = c->nom; h->V = c->V;
+    h->views = c->views;
+    h->d_views.borrow(c->d_views);
+    h->alpha.borrow(c->alpha);
+    h->mapcube.borrow(c->mapcube);
+    h->map_ready = c->map_ready;
+    h->csamples.borrow(c->csamples);
+    h->cS = c->cS; h->cKpad = c->cKpad;
+    h->bmat.borrow(c->bmat);
+    h->n_orient = c->n_orient;
+    h->bmat_ready = c->bmat_ready; h->bmat_ms = c->bmat_ms;
+    h->bmat8.borrow(c->bmat8);
+    h->bmat8_ready = c->bmat8_ready; h->bmat8_ms = c->bmat8_ms; h->cKpad8 = c->cKpad8;
+    h->mulA.borrow(c->mulA);
+    h->mulB.borrow(c->mulB);
+    h->cgrid = c->cgrid;
+    h->csamples_c.borrow(c->csamples_c);
+    h->cS_c = c->cS_c; h->cKpad_c = c->cKpad_c; h->n_origin_c = c->n_origin_c;
+    h->orig_max_c = c->orig_max_c; h->orig_step_c = c->orig_step_c;
+    h->bmat_c.borrow(c->bmat_c);
+    h->bmat_c_ready = c->bmat_c_ready; h->n_orient_c = c->n_orient_c;
+    h->corigins_c.borrow(c->corigins_c);
+    h->corigins.borrow(c->corigins);
+    h->n_origin = c->n_origin; h->orig_max = c->orig_max; h->orig_step = c->orig_step;
+    h->view_slot = c->view_slot;
+    h->slot_view = c->slot_view;
+    h->num_sms = c->num_sms;
+    h->prof = c->prof;
+    LearnModel& a = h->lm;
+    const LearnModel& b = c->lm;
+    a.ready = b.ready; a.V = b.V; a.sign = b.sign; a.step = b.step; a.nparam = b.nparam;
+    for (int i = 0; i < 5; ++i) { a.oW[i] = b.oW[i]; a.ob[i] = b.ob[i]; }
+    a.oT = b.oT; a.steps = b.steps; a.conv_tc = b.conv_tc;
+    a.w.borrow(b.w);
+    a.vview.borrow(b.vview);
+    int r;
+    if ((r = a.cerr.ensure(1))) return r;
+    CK(cudaMemsetAsync(a.cerr.p, 0, sizeof(int), h->stream));
+    return CRYOIM_OK;
+}
+
 int contract_impl(Ctx* c, const float* imgs, bool on_device, cryoim_particle* parts, int P,
                   const cryoim_contract_opts* opts, float* cands) {
     int r = check_ready(c, false);
@@ -1477,26 +1555,8 @@ int contract_impl(Ctx* c, const float* imgs, bool on_device, cryoim_particle* pa
     const int pb = std::max(1, std::min(PB, 2400 / std::max(O, 1)));
     const int arows = (kc > 0 || kl > 0) ? PB : pb;
     const int ntiles = (int)((c->n_orient + gemm_tile_n() - 1) / gemm_tile_n());
-    if ((r = ensure_batch(c, PB))) return r;
-    if (f8 ? ((r = c->amat8.ensure((size_t)arows * O * c->cKpad8)) || (r = c->fexp.ensure(PB)))
-           : (r = c->amat.ensure((size_t)arows * O * c->cKpad)))
-        return r;
-    if ((r = c->topv.ensure((size_t)arows * O * ntiles)) || (r = c->topi.ensure((size_t)arows * O * ntiles)))
-        return r;
-    if ((r = c->gerr.ensure(1)) || (r = c->pnorm.ensure(PB)) || (r = c->kor.ensure((size_t)PB * k)) ||
-        (r = c->korig.ensure((size_t)PB * k)) || (r = c->kcc.ensure((size_t)PB * k)) ||
-        (r = c->kcand.ensure((size_t)PB * k * 5)) || (r = c->kcc64.ensure((size_t)PB * k)) ||
-        (r = c->kpart.ensure((size_t)cc_fp64_scratch(k, PB))))
-        return r;
     // rescoring set: each selected orientation and its grid neighbours within nbr steps
     const int maxx = nbox * k;
-    if ((r = c->tilev.ensure((size_t)pb * ntiles)) || (r = c->tileo.ensure((size_t)pb * ntiles)) ||
-        (r = c->tileorig.ensure((size_t)pb * ntiles)) || (r = c->xcand.ensure((size_t)PB * maxx * 5)) ||
-        (r = c->xpr.ensure((size_t)PB * maxx)))
-        return r;
-    if (T > 0 && ((r = c->xalpha.ensure((size_t)PB * maxx * T * 60)) || (r = c->sband.ensure((size_t)PB * w2)) ||
-                  (r = c->xcount.ensure(PB)) || (c->p.apply_ctf && (r = c->tbandc.ensure((size_t)PB * T * w2)))))
-        return r;
     if (c->num_sms == 0) CK(cudaDeviceGetAttribute(&c->num_sms, cudaDevAttrMultiProcessorCount, c->device));
     std::vector<int> src(P);
     {
@@ -1506,357 +1566,413 @@ int contract_impl(Ctx* c, const float* imgs, bool on_device, cryoim_particle* pa
             src[i] = cur;
         }
     }
-    std::vector<float> hpar(8 * PB), hcand((size_t)PB * k * 5), hcc((size_t)PB * k);
-    std::vector<int> hor((size_t)PB * k), horig((size_t)PB * k);
-    std::vector<double> hcc64((size_t)PB * k);
     std::vector<float> ohost(2 * (size_t)O);
     CK(cudaMemcpyAsync(ohost.data(), c->corigins.p, sizeof(float) * 2 * O, cudaMemcpyDeviceToHost, c->stream));
-    // profiling: an event pair around every contraction launch of a pass
-    std::vector<cudaEvent_t> gev;
-    auto gmark = [&](size_t i) -> int {
-        while (gev.size() <= i) {
-            cudaEvent_t e;
-            CK(cudaEventCreate(&e));
-            gev.push_back(e);
-        }
-        CK(cudaEventRecord(gev[i], c->stream));
+    const long row_bytes = f8 ? (long)c->cKpad8 : 2L * c->cKpad;
+    // Passes alternate between two lanes (this context and c->lane2, each with its own
+    // stream, per-pass buffers and host thread), so that one lane's host work between
+    // its waits overlaps the other lane's kernels.
+    const int nlanes = P > PB ? 2 : 1;
+    auto alloc = [&](Ctx* L) -> int {
+        int r;
+        if ((r = ensure_batch(L, PB))) return r;
+        if (f8 ? ((r = L->amat8.ensure((size_t)arows * O * L->cKpad8)) || (r = L->fexp.ensure(PB)))
+               : (r = L->amat.ensure((size_t)arows * O * L->cKpad)))
+            return r;
+        if ((r = L->topv.ensure((size_t)arows * O * ntiles)) || (r = L->topi.ensure((size_t)arows * O * ntiles)))
+            return r;
+        if ((r = L->gerr.ensure(1)) || (r = L->pnorm.ensure(PB)) || (r = L->kor.ensure((size_t)PB * k)) ||
+            (r = L->korig.ensure((size_t)PB * k)) || (r = L->kcc.ensure((size_t)PB * k)) ||
+            (r = L->kcand.ensure((size_t)PB * k * 5)) || (r = L->kcc64.ensure((size_t)PB * k)) ||
+            (r = L->kpart.ensure((size_t)cc_fp64_scratch(k, PB))))
+            return r;
+        if ((r = L->tilev.ensure((size_t)pb * ntiles)) || (r = L->tileo.ensure((size_t)pb * ntiles)) ||
+            (r = L->tileorig.ensure((size_t)pb * ntiles)) || (r = L->xcand.ensure((size_t)PB * maxx * 5)) ||
+            (r = L->xpr.ensure((size_t)PB * maxx)))
+            return r;
+        if (T > 0 && ((r = L->xalpha.ensure((size_t)PB * maxx * T * 60)) || (r = L->sband.ensure((size_t)PB * w2)) ||
+                      (r = L->xcount.ensure(PB)) || (L->p.apply_ctf && (r = L->tbandc.ensure((size_t)PB * T * w2)))))
+            return r;
         return CRYOIM_OK;
     };
-    size_t ngev = 0;
-    const long row_bytes = f8 ? (long)c->cKpad8 : 2L * c->cKpad;
-    for (int b0 = 0; b0 < P; b0 += PB) {
-        const int nb = std::min(PB, P - b0);
-        const float* d_src;
-        if (on_device) {
-            d_src = imgs + b0 * nn;
-        } else {
-            CK(cudaMemcpyAsync(c->imgs.p, imgs + b0 * nn, sizeof(float) * nb * nn, cudaMemcpyHostToDevice,
-                               c->stream));
-            d_src = c->imgs.p;
-        }
-        std::fill(hpar.begin(), hpar.end(), 0.0f);
-        for (int i = 0; i < nb; ++i) {
-            const cryoim_particle& q = parts[b0 + i];
-            const cryoim_particle& s = parts[src[b0 + i]];
-            hpar[i] = q.x; hpar[PB + i] = q.y;
-            hpar[4 * PB + 3 * i] = s.df1; hpar[4 * PB + 3 * i + 1] = s.df2; hpar[4 * PB + 3 * i + 2] = s.astigang;
-        }
-        // mask at the input origin as ort_globesearch.f90:50 does; the transform stays unshifted
-        if ((r = transform_batch(c, d_src, nb, PB, hpar, 1, 0, false))) return r;
-        ParView pv = par_view(c, PB);
-        const float* ctfp = nullptr;
-        const float* tfc = c->tfcut0.p;
-        long tfs = 0;
-        if (c->p.apply_ctf) {
-            launch_ctf_band(nb, c->bd, pv.dfs, c->p.apix, c->p.vol, c->p.cs, c->p.ampwg, c->ctf.p, c->stream);
-            ctfp = c->ctf.p;
-            if (T > 0) {
-                launch_tmpl_fcut(c->tband.p, T, c->ctf.p, nb, c->bd, c->tfcut.p, c->stream);
-                tfc = c->tfcut.p;
-                tfs = (long)T * c->bd.nr;
+    auto run = [&](Ctx* L, int lane) -> int {
+        int r;
+        std::vector<float> hpar(8 * PB), hcand((size_t)PB * k * 5), hcc((size_t)PB * k);
+        std::vector<int> hor((size_t)PB * k), horig((size_t)PB * k);
+        std::vector<double> hcc64((size_t)PB * k);
+        // profiling: an event pair around every contraction launch of a pass
+        std::vector<cudaEvent_t> gev;
+        auto gmark = [&](size_t i) -> int {
+            while (gev.size() <= i) {
+                cudaEvent_t e;
+                CK(cudaEventCreate(&e));
+                gev.push_back(e);
             }
-        }
-        launch_particle_norm(c->band.p, ctfp, c->bd, c->csamples.p, c->cS, nb, c->pnorm.p, c->stream);
-        // operand A rows (particle, origin) of particles [s0, s0 + ns) at row (s0 - a0) O
-        auto build_rows = [&](int s0, int ns, int a0) {
-            const float2* bb = c->band.p + (long)s0 * w2;
-            const float* cc = ctfp ? ctfp + (long)s0 * w2 : nullptr;
-            if (f8)
-                launch_build_a8(bb, cc, c->bd, c->csamples.p, c->cS, c->cKpad8, c->corigins.p, O, c->pnorm.p + s0,
-                                c->mulA.p, c->fexp.p + s0, ns, c->amat8.p + (size_t)(s0 - a0) * O * c->cKpad8,
-                                c->stream);
-            else
-                launch_build_a(bb, cc, c->bd, c->csamples.p, c->cS, c->cKpad, c->corigins.p, O, c->pnorm.p + s0, ns,
-                               c->amat.p + (size_t)(s0 - a0) * O * c->cKpad, c->stream);
-        };
-        GemmArgmaxArgs g{};
-        g.topv = c->topv.p;
-        g.topi = c->topi.p;
-        g.cfull = nullptr;
-        g.err = c->gerr.p;
-        CK(cudaMemsetAsync(c->gerr.p, 0, sizeof(int), c->stream));
-        std::vector<std::vector<int>> lists;
-        ngev = 0;
-        if (kc > 0 || kl > 0) {
-            // proposal forms: the coarse contraction or the learned proposer names each
-            // particle's candidate orientations, the fine contraction runs on their
-            // gathered sections only
-            if ((r = kc > 0 ? coarse_lists(c, nb, ctfp, kc, nbf, lists) : learned_lists(c, nb, kl, nbf, lists)))
-                return r;
-            CK(cudaMemsetAsync(c->gerr.p, 0, sizeof(int), c->stream));
-            const void* bsrc = f8 ? (const void*)c->bmat8.p : (const void*)c->bmat.p;
-            const char* abase = f8 ? (const char*)c->amat8.p : (const char*)c->amat.p;
-            build_rows(0, nb, 0);
-            CK(cudaGetLastError());
-            // particles in groups whose gathered sections stay under 8 GB: one gather and one
-            // grouped contraction (each particle's origin rows against its own sections) per
-            // group, then the k distinct best orientations of each particle
-            for (int i0 = 0; i0 < nb;) {
-                int i1 = i0;
-                long rows = 0;
-                while (i1 < nb && (i1 == i0 || (rows + (long)lists[i1].size()) * row_bytes <= (8L << 30)))
-                    rows += (long)lists[i1++].size();
-                std::vector<int> idx;
-                idx.reserve(rows);
-                for (int i = i0; i < i1; ++i) idx.insert(idx.end(), lists[i].begin(), lists[i].end());
-                if ((r = c->gidx.ensure(rows)) || (r = c->bgather.ensure((size_t)rows * row_bytes))) return r;
-                CK(cudaMemcpyAsync(c->gidx.p, idx.data(), sizeof(int) * rows, cudaMemcpyHostToDevice, c->stream));
-                CK(launch_gather_rows(bsrc, row_bytes, c->gidx.p, (int)rows, c->bgather.p, c->stream));
-                std::vector<GemmGroup> hg(i1 - i0);
-                std::vector<int2> seg(i1 - i0);
-                long roff = 0, toff = 0;
-                for (int i = i0; i < i1; ++i) {
-                    const int nl = (int)lists[i].size();
-                    const int ntp = (nl + gemm_tile_n() - 1) / gemm_tile_n();
-                    GemmGroup& q = hg[i - i0];
-                    q.a_row0 = i * O;
-                    q.m_valid = O;
-                    q.b_row0 = (int)roff;
-                    q.n_valid = nl;
-                    q.topv_off = (int)toff;
-                    seg[i - i0] = make_int2((int)toff, ntp);
-                    roff += nl;
-                    toff += (long)O * ntp;
-                    if (c->prof) c->prof_gemm_flops += 2.0 * (double)O * (double)nl * (double)kpad;
-                }
-                if ((r = c->ggroups.ensure(i1 - i0)) || (r = c->gseg.ensure(i1 - i0))) return r;
-                if (c->prof && (r = gmark(ngev++))) return r;
-                CK(launch_gemm_argmax_grouped(abase, (long)nb * O, c->bgather.p, rows, kpad, f8, hg.data(), i1 - i0,
-                                              c->ggroups.p, g, c->num_sms, c->stream));
-                if (c->prof && (r = gmark(ngev++))) return r;
-                CK(cudaMemcpyAsync(c->gseg.p, seg.data(), sizeof(int2) * seg.size(), cudaMemcpyHostToDevice,
-                                   c->stream));
-                launch_select_distinct(c->topv.p, c->topi.p, O, c->gseg.p, i1 - i0, k, c->kor.p + (size_t)i0 * k,
-                                       c->korig.p + (size_t)i0 * k, c->kcc.p + (size_t)i0 * k, c->stream);
-                CK(cudaGetLastError());
-                // the gather buffer is reused by the next group
-                if (i1 < nb) CK(cudaStreamSynchronize(c->stream));
-                i0 = i1;
-            }
-        } else {
-            // exhaustive: sub-batches of pb particles against every section, queued back to back
-            for (int s0 = 0; s0 < nb; s0 += pb) {
-                const int ns = std::min(pb, nb - s0);
-                build_rows(s0, ns, s0);
-                CK(cudaGetLastError());
-                if (c->prof && (r = gmark(ngev++))) return r;
-                if (f8)
-                    CK(launch_gemm_argmax(c->amat8.p, c->bmat8.p, ns * O, (int)c->n_orient, kpad, true, g,
-                                          c->num_sms, c->stream));
-                else
-                    CK(launch_gemm_argmax(c->amat.p, c->bmat.p, ns * O, (int)c->n_orient, kpad, false, g,
-                                          c->num_sms, c->stream));
-                if (c->prof && (r = gmark(ngev++))) return r;
-                launch_select_topk(c->topv.p, c->topi.p, O, ntiles, k, ns, c->tilev.p, c->tileo.p, c->tileorig.p,
-                                   c->kor.p + (size_t)s0 * k, c->korig.p + (size_t)s0 * k,
-                                   c->kcc.p + (size_t)s0 * k, c->stream);
-                CK(cudaGetLastError());
-                if (c->prof) c->prof_gemm_flops += 2.0 * (double)ns * O * (double)c->n_orient * (double)kpad;
-            }
-        }
-        int gerr = 0;
-        CK(cudaMemcpyAsync(&gerr, c->gerr.p, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
-        CK(cudaMemcpyAsync(hor.data(), c->kor.p, sizeof(int) * nb * k, cudaMemcpyDeviceToHost, c->stream));
-        CK(cudaMemcpyAsync(horig.data(), c->korig.p, sizeof(int) * nb * k, cudaMemcpyDeviceToHost, c->stream));
-        CK(cudaMemcpyAsync(hcc.data(), c->kcc.p, sizeof(float) * nb * k, cudaMemcpyDeviceToHost, c->stream));
-        std::vector<int> hfe(nb, 0);
-        if (f8) CK(cudaMemcpyAsync(hfe.data(), c->fexp.p, sizeof(int) * nb, cudaMemcpyDeviceToHost, c->stream));
-        if ((r = check_flag(c))) return r;
-        if (gerr) return fail(CRYOIM_ERR_CUDA, "contraction pipeline wait timed out");
-        if (f8)  // remove the per-particle exponent: the CC of the unit-norm rows
-            for (int i = 0; i < nb * k; ++i) hcc[i] = std::ldexp(hcc[i], -hfe[i / k]);
-        if (kc > 0 || kl > 0)  // gathered column -> fine orientation index
-            for (int i = 0; i < nb * k; ++i)
-                if (hor[i] >= 0) hor[i] = lists[i / k][hor[i]];
-        if (c->prof)
-            for (size_t e = 0; e + 1 < ngev; e += 2) {
-                float ms = 0.f;
-                CK(cudaEventElapsedTime(&ms, gev[e], gev[e + 1]));
-                c->prof_gemm_ms += ms;
-                c->prof_gemm_launches += 1;
-            }
-        // candidates (theta, phi, omega, x, y) of the selected (orientation, origin) pairs
-        for (int i = 0; i < nb * k; ++i) {
-            int n = hor[i] < 0 ? 0 : hor[i];
-            int v = n / c->nom, io = n % c->nom;
-            int o = horig[i];
-            hcand[5 * i] = c->views[4 * v];
-            hcand[5 * i + 1] = c->views[4 * v + 1];
-            hcand[5 * i + 2] = c->p.searchstep * (float)io;
-            hcand[5 * i + 3] = ohost[2 * o];
-            hcand[5 * i + 4] = ohost[2 * o + 1];
-        }
-        CK(cudaMemcpyAsync(c->kcand.p, hcand.data(), sizeof(float) * nb * k * 5, cudaMemcpyHostToDevice,
-                           c->stream));
-        launch_cc_fp64(c->mapcube.p, c->band.p, ctfp, c->bd, c->csamples.p, c->cS, c->kcand.p, k, nb, c->kpart.p,
-                       c->kcc64.p, c->stream);
-        // Phase-residual rescoring at the particle's own origin (ort_globesearch.f90 scores
-        // every view at particle(i)%x, %y) over each selected orientation and its grid
-        // neighbours within nbr steps (all of them, or, with nbr_best = m, only those of
-        // the m candidates of least phase residual, scored first); the result equals the
-        // exhaustive search wherever its minimum lies in the scored set.  Sets are sorted
-        // by orientation index, without repeats.
-        std::vector<std::vector<int>> xs(nb);
-        std::vector<std::vector<float>> xp(nb);
-        const int span = 2 * c->nph + 1;
-        auto neighbourhood = [&](int n, std::vector<int>& lst) {
-            const int v = n / c->nom, io = n % c->nom, slot = c->view_slot[v];
-            const int it = slot / span, ips = slot % span - c->nph;
-            for (int dt = -nbr; dt <= nbr; ++dt)
-                for (int dp = -nbr; dp <= nbr; ++dp) {
-                    const int it2 = it + dt, ips2 = ips + dp;
-                    if (it2 < 0 || it2 > c->nth || ips2 < -c->nph || ips2 > c->nph) continue;
-                    const int v2 = c->slot_view[(size_t)it2 * span + ips2 + c->nph];
-                    if (v2 < 0) continue;
-                    for (int dw = -nbr; dw <= nbr; ++dw)
-                        lst.push_back(v2 * c->nom + ((io + dw) % c->nom + c->nom) % c->nom);
-                }
-        };
-        // phase residuals of per-particle orientation sets (empty sets score nothing)
-        auto score = [&](const std::vector<std::vector<int>>& sets, std::vector<std::vector<float>>& out) -> int {
-            int maxc = 1;
-            for (int i = 0; i < nb; ++i) maxc = std::max(maxc, (int)sets[i].size());
-            if (maxc > maxx) return fail(CRYOIM_ERR_SIZE, "rescoring set of %d orientations", maxc);
-            std::vector<float> hx((size_t)nb * maxc * 5, 0.0f);
-            std::vector<int> hcount(nb);
-            for (int i = 0; i < nb; ++i) {
-                hcount[i] = (int)sets[i].size();
-                for (int j = 0; j < maxc; ++j) {
-                    const int n = sets[i].empty() ? 0 : sets[i][std::min<size_t>(j, sets[i].size() - 1)];
-                    float* o = &hx[((size_t)i * maxc + j) * 5];
-                    o[0] = c->views[4 * (n / c->nom)];
-                    o[1] = c->views[4 * (n / c->nom) + 1];
-                    o[2] = c->p.searchstep * (float)(n % c->nom);
-                    o[3] = parts[b0 + i].x;
-                    o[4] = parts[b0 + i].y;
-                }
-            }
-            CK(cudaMemcpyAsync(c->xcand.p, hx.data(), sizeof(float) * hx.size(), cudaMemcpyHostToDevice,
-                               c->stream));
-            CK(cudaMemcpyAsync(c->xcount.p, hcount.data(), sizeof(int) * nb, cudaMemcpyHostToDevice, c->stream));
-            launch_refine_alpha(c->xcand.p, nb, c->tort.p, T, c->ops.p, c->xalpha.p, c->stream, maxc);
-            // every candidate of a particle sits at the particle's origin: shift its band once
-            CK(launch_shift_band(c->band.p, c->xcand.p, maxc, c->bd, nb, c->sband.p, c->stream));
-            PrSingleArgs a{};
-            a.band = c->band.p; a.fcut0 = c->fcut0.p; a.tband = c->tband.p; a.tfcut = tfc;
-            a.tfcut_pstride = tfs; a.ctf = ctfp; a.cand = c->xcand.p; a.alpha = c->xalpha.p; a.T = T;
-            a.bd = c->bd; a.pr = c->xpr.p; a.ncand = maxc; a.sband = c->sband.p; a.ncount = c->xcount.p;
-            a.tbandc = ctfp ? c->tbandc.p : nullptr;
-            // candidates of a particle sharing a view, in groups (the sets are sorted by
-            // orientation index, so a view's omegas are adjacent)
-            std::vector<int4> grp;
-            const int rg = pr_rescore_group_size();
-            for (int i = 0; i < nb; ++i)
-                for (size_t j = 0; j < sets[i].size();) {
-                    size_t e = j + 1;
-                    while (e < sets[i].size() && (int)(e - j) < rg && sets[i][e] / c->nom == sets[i][j] / c->nom) ++e;
-                    grp.push_back(make_int4(i, (int)j, (int)(e - j), 0));
-                    j = e;
-                }
-            if (!grp.empty()) {
-                if ((r = c->xgroups.ensure(grp.size()))) return r;
-                CK(cudaMemcpyAsync(c->xgroups.p, grp.data(), sizeof(int4) * grp.size(), cudaMemcpyHostToDevice,
-                                   c->stream));
-                CK(launch_pr_rescore_groups(a, c->xgroups.p, (int)grp.size(), c->stream));
-            }
-            std::vector<float> h((size_t)nb * maxc);
-            CK(cudaMemcpyAsync(h.data(), c->xpr.p, sizeof(float) * h.size(), cudaMemcpyDeviceToHost, c->stream));
-            CK(cudaStreamSynchronize(c->stream));
-            out.assign(nb, std::vector<float>());
-            for (int i = 0; i < nb; ++i) out[i].assign(h.begin() + (size_t)i * maxc, h.begin() + (size_t)i * maxc + sets[i].size());
+            CK(cudaEventRecord(gev[i], L->stream));
             return CRYOIM_OK;
         };
-        if (T > 0) {
-            // the templates under each particle's CTF, once per pass
-            if (ctfp) CK(launch_tband_ctf(c->tband.p, T, ctfp, c->bd, nb, c->tbandc.p, c->stream));
-            if (nbest <= 0 || nbest >= k) {
-                for (int i = 0; i < nb; ++i) {
-                    for (int rr = 0; rr < k; ++rr)
-                        if (hor[i * k + rr] >= 0) neighbourhood(hor[i * k + rr], xs[i]);
-                    std::sort(xs[i].begin(), xs[i].end());
-                    xs[i].erase(std::unique(xs[i].begin(), xs[i].end()), xs[i].end());
-                    if (xs[i].empty()) xs[i].push_back(0);
-                }
-                if ((r = score(xs, xp))) return r;
+        size_t ngev = 0;
+        for (int b0 = lane * PB; b0 < P; b0 += nlanes * PB) {
+            const int nb = std::min(PB, P - b0);
+            const float* d_src;
+            if (on_device) {
+                d_src = imgs + b0 * nn;
             } else {
-                // the candidates first, then the neighbourhoods of the nbest best of them
-                std::vector<std::vector<int>> xa(nb), xb(nb);
-                std::vector<std::vector<float>> pa, pb;
-                for (int i = 0; i < nb; ++i) {
-                    for (int rr = 0; rr < k; ++rr)
-                        if (hor[i * k + rr] >= 0) xa[i].push_back(hor[i * k + rr]);
-                    std::sort(xa[i].begin(), xa[i].end());
-                    xa[i].erase(std::unique(xa[i].begin(), xa[i].end()), xa[i].end());
-                    if (xa[i].empty()) xa[i].push_back(0);
+                CK(cudaMemcpyAsync(L->imgs.p, imgs + b0 * nn, sizeof(float) * nb * nn, cudaMemcpyHostToDevice,
+                                   L->stream));
+                d_src = L->imgs.p;
+            }
+            std::fill(hpar.begin(), hpar.end(), 0.0f);
+            for (int i = 0; i < nb; ++i) {
+                const cryoim_particle& q = parts[b0 + i];
+                const cryoim_particle& s = parts[src[b0 + i]];
+                hpar[i] = q.x; hpar[PB + i] = q.y;
+                hpar[4 * PB + 3 * i] = s.df1; hpar[4 * PB + 3 * i + 1] = s.df2; hpar[4 * PB + 3 * i + 2] = s.astigang;
+            }
+            // mask at the input origin as ort_globesearch.f90:50 does; the transform stays unshifted
+            if ((r = transform_batch(L, d_src, nb, PB, hpar, 1, 0, false))) return r;
+            ParView pv = par_view(L, PB);
+            const float* ctfp = nullptr;
+            const float* tfc = L->tfcut0.p;
+            long tfs = 0;
+            if (L->p.apply_ctf) {
+                launch_ctf_band(nb, L->bd, pv.dfs, L->p.apix, L->p.vol, L->p.cs, L->p.ampwg, L->ctf.p, L->stream);
+                ctfp = L->ctf.p;
+                if (T > 0) {
+                    launch_tmpl_fcut(L->tband.p, T, L->ctf.p, nb, L->bd, L->tfcut.p, L->stream);
+                    tfc = L->tfcut.p;
+                    tfs = (long)T * L->bd.nr;
                 }
-                if ((r = score(xa, pa))) return r;
-                for (int i = 0; i < nb; ++i) {
-                    std::vector<int> ord(xa[i].size());
-                    for (size_t j = 0; j < ord.size(); ++j) ord[j] = (int)j;
-                    std::stable_sort(ord.begin(), ord.end(), [&](int x, int y) { return pa[i][x] < pa[i][y]; });
-                    std::vector<int> nb_set;
-                    for (int j = 0; j < std::min<int>(nbest, (int)ord.size()); ++j) neighbourhood(xa[i][ord[j]], nb_set);
-                    std::sort(nb_set.begin(), nb_set.end());
-                    nb_set.erase(std::unique(nb_set.begin(), nb_set.end()), nb_set.end());
-                    std::set_difference(nb_set.begin(), nb_set.end(), xa[i].begin(), xa[i].end(),
-                                        std::back_inserter(xb[i]));
+            }
+            launch_particle_norm(L->band.p, ctfp, L->bd, L->csamples.p, L->cS, nb, L->pnorm.p, L->stream);
+            // operand A rows (particle, origin) of particles [s0, s0 + ns) at row (s0 - a0) O
+            auto build_rows = [&](int s0, int ns, int a0) {
+                const float2* bb = L->band.p + (long)s0 * w2;
+                const float* cc = ctfp ? ctfp + (long)s0 * w2 : nullptr;
+                if (f8)
+                    launch_build_a8(bb, cc, L->bd, L->csamples.p, L->cS, L->cKpad8, L->corigins.p, O, L->pnorm.p + s0,
+                                    L->mulA.p, L->fexp.p + s0, ns, L->amat8.p + (size_t)(s0 - a0) * O * L->cKpad8,
+                                    L->stream);
+                else
+                    launch_build_a(bb, cc, L->bd, L->csamples.p, L->cS, L->cKpad, L->corigins.p, O, L->pnorm.p + s0, ns,
+                                   L->amat.p + (size_t)(s0 - a0) * O * L->cKpad, L->stream);
+            };
+            GemmArgmaxArgs g{};
+            g.topv = L->topv.p;
+            g.topi = L->topi.p;
+            g.cfull = nullptr;
+            g.err = L->gerr.p;
+            CK(cudaMemsetAsync(L->gerr.p, 0, sizeof(int), L->stream));
+            std::vector<std::vector<int>> lists;
+            ngev = 0;
+            if (kc > 0 || kl > 0) {
+                // proposal forms: the coarse contraction or the learned proposer names each
+                // particle's candidate orientations, the fine contraction runs on their
+                // gathered sections only
+                if ((r = kc > 0 ? coarse_lists(L, nb, ctfp, kc, nbf, lists) : learned_lists(L, nb, kl, nbf, lists)))
+                    return r;
+                CK(cudaMemsetAsync(L->gerr.p, 0, sizeof(int), L->stream));
+                const void* bsrc = f8 ? (const void*)L->bmat8.p : (const void*)L->bmat.p;
+                const char* abase = f8 ? (const char*)L->amat8.p : (const char*)L->amat.p;
+                build_rows(0, nb, 0);
+                CK(cudaGetLastError());
+                // particles in groups whose gathered sections stay under 8 GB: one gather and one
+                // grouped contraction (each particle's origin rows against its own sections) per
+                // group, then the k distinct best orientations of each particle
+                for (int i0 = 0; i0 < nb;) {
+                    int i1 = i0;
+                    long rows = 0;
+                    while (i1 < nb && (i1 == i0 || (rows + (long)lists[i1].size()) * row_bytes <= (8L << 30)))
+                        rows += (long)lists[i1++].size();
+                    std::vector<int> idx;
+                    idx.reserve(rows);
+                    for (int i = i0; i < i1; ++i) idx.insert(idx.end(), lists[i].begin(), lists[i].end());
+                    if ((r = L->gidx.ensure(rows)) || (r = L->bgather.ensure((size_t)rows * row_bytes))) return r;
+                    CK(cudaMemcpyAsync(L->gidx.p, idx.data(), sizeof(int) * rows, cudaMemcpyHostToDevice, L->stream));
+                    CK(launch_gather_rows(bsrc, row_bytes, L->gidx.p, (int)rows, L->bgather.p, L->stream));
+                    std::vector<GemmGroup> hg(i1 - i0);
+                    std::vector<int2> seg(i1 - i0);
+                    long roff = 0, toff = 0;
+                    for (int i = i0; i < i1; ++i) {
+                        const int nl = (int)lists[i].size();
+                        const int ntp = (nl + gemm_tile_n() - 1) / gemm_tile_n();
+                        GemmGroup& q = hg[i - i0];
+                        q.a_row0 = i * O;
+                        q.m_valid = O;
+                        q.b_row0 = (int)roff;
+                        q.n_valid = nl;
+                        q.topv_off = (int)toff;
+                        seg[i - i0] = make_int2((int)toff, ntp);
+                        roff += nl;
+                        toff += (long)O * ntp;
+                        if (L->prof) L->prof_gemm_flops += 2.0 * (double)O * (double)nl * (double)kpad;
+                    }
+                    if ((r = L->ggroups.ensure(i1 - i0)) || (r = L->gseg.ensure(i1 - i0))) return r;
+                    if (L->prof && (r = gmark(ngev++))) return r;
+                    CK(launch_gemm_argmax_grouped(abase, (long)nb * O, L->bgather.p, rows, kpad, f8, hg.data(), i1 - i0,
+                                                  L->ggroups.p, g, L->num_sms, L->stream));
+                    if (L->prof && (r = gmark(ngev++))) return r;
+                    CK(cudaMemcpyAsync(L->gseg.p, seg.data(), sizeof(int2) * seg.size(), cudaMemcpyHostToDevice,
+                                       L->stream));
+                    launch_select_distinct(L->topv.p, L->topi.p, O, L->gseg.p, i1 - i0, k, L->kor.p + (size_t)i0 * k,
+                                           L->korig.p + (size_t)i0 * k, L->kcc.p + (size_t)i0 * k, L->stream);
+                    CK(cudaGetLastError());
+                    // the gather buffer is reused by the next group
+                    if (i1 < nb) CK(cudaStreamSynchronize(L->stream));
+                    i0 = i1;
                 }
-                if ((r = score(xb, pb))) return r;
-                for (int i = 0; i < nb; ++i) {  // merge, sorted by orientation index
-                    size_t ia = 0, ib = 0;
-                    while (ia < xa[i].size() || ib < xb[i].size()) {
-                        if (ib >= xb[i].size() || (ia < xa[i].size() && xa[i][ia] < xb[i][ib])) {
-                            xs[i].push_back(xa[i][ia]);
-                            xp[i].push_back(pa[i][ia++]);
-                        } else {
-                            xs[i].push_back(xb[i][ib]);
-                            xp[i].push_back(pb[i][ib++]);
+            } else {
+                // exhaustive: sub-batches of pb particles against every section, queued back to back
+                for (int s0 = 0; s0 < nb; s0 += pb) {
+                    const int ns = std::min(pb, nb - s0);
+                    build_rows(s0, ns, s0);
+                    CK(cudaGetLastError());
+                    if (L->prof && (r = gmark(ngev++))) return r;
+                    if (f8)
+                        CK(launch_gemm_argmax(L->amat8.p, L->bmat8.p, ns * O, (int)L->n_orient, kpad, true, g,
+                                              L->num_sms, L->stream));
+                    else
+                        CK(launch_gemm_argmax(L->amat.p, L->bmat.p, ns * O, (int)L->n_orient, kpad, false, g,
+                                              L->num_sms, L->stream));
+                    if (L->prof && (r = gmark(ngev++))) return r;
+                    launch_select_topk(L->topv.p, L->topi.p, O, ntiles, k, ns, L->tilev.p, L->tileo.p, L->tileorig.p,
+                                       L->kor.p + (size_t)s0 * k, L->korig.p + (size_t)s0 * k,
+                                       L->kcc.p + (size_t)s0 * k, L->stream);
+                    CK(cudaGetLastError());
+                    if (L->prof) L->prof_gemm_flops += 2.0 * (double)ns * O * (double)L->n_orient * (double)kpad;
+                }
+            }
+            int gerr = 0;
+            CK(cudaMemcpyAsync(&gerr, L->gerr.p, sizeof(int), cudaMemcpyDeviceToHost, L->stream));
+            CK(cudaMemcpyAsync(hor.data(), L->kor.p, sizeof(int) * nb * k, cudaMemcpyDeviceToHost, L->stream));
+            CK(cudaMemcpyAsync(horig.data(), L->korig.p, sizeof(int) * nb * k, cudaMemcpyDeviceToHost, L->stream));
+            CK(cudaMemcpyAsync(hcc.data(), L->kcc.p, sizeof(float) * nb * k, cudaMemcpyDeviceToHost, L->stream));
+            std::vector<int> hfe(nb, 0);
+            if (f8) CK(cudaMemcpyAsync(hfe.data(), L->fexp.p, sizeof(int) * nb, cudaMemcpyDeviceToHost, L->stream));
+            if ((r = check_flag(L))) return r;
+            if (gerr) return fail(CRYOIM_ERR_CUDA, "contraction pipeline wait timed out");
+            if (f8)  // remove the per-particle exponent: the CC of the unit-norm rows
+                for (int i = 0; i < nb * k; ++i) hcc[i] = std::ldexp(hcc[i], -hfe[i / k]);
+            if (kc > 0 || kl > 0)  // gathered column -> fine orientation index
+                for (int i = 0; i < nb * k; ++i)
+                    if (hor[i] >= 0) hor[i] = lists[i / k][hor[i]];
+            if (L->prof)
+                for (size_t e = 0; e + 1 < ngev; e += 2) {
+                    float ms = 0.f;
+                    CK(cudaEventElapsedTime(&ms, gev[e], gev[e + 1]));
+                    L->prof_gemm_ms += ms;
+                    L->prof_gemm_launches += 1;
+                }
+            // candidates (theta, phi, omega, x, y) of the selected (orientation, origin) pairs
+            for (int i = 0; i < nb * k; ++i) {
+                int n = hor[i] < 0 ? 0 : hor[i];
+                int v = n / L->nom, io = n % L->nom;
+                int o = horig[i];
+                hcand[5 * i] = L->views[4 * v];
+                hcand[5 * i + 1] = L->views[4 * v + 1];
+                hcand[5 * i + 2] = L->p.searchstep * (float)io;
+                hcand[5 * i + 3] = ohost[2 * o];
+                hcand[5 * i + 4] = ohost[2 * o + 1];
+            }
+            CK(cudaMemcpyAsync(L->kcand.p, hcand.data(), sizeof(float) * nb * k * 5, cudaMemcpyHostToDevice,
+                               L->stream));
+            launch_cc_fp64(L->mapcube.p, L->band.p, ctfp, L->bd, L->csamples.p, L->cS, L->kcand.p, k, nb, L->kpart.p,
+                           L->kcc64.p, L->stream);
+            // Phase-residual rescoring at the particle's own origin (ort_globesearch.f90 scores
+            // every view at particle(i)%x, %y) over each selected orientation and its grid
+            // neighbours within nbr steps (all of them, or, with nbr_best = m, only those of
+            // the m candidates of least phase residual, scored first); the result equals the
+            // exhaustive search wherever its minimum lies in the scored set.  Sets are sorted
+            // by orientation index, without repeats.
+            std::vector<std::vector<int>> xs(nb);
+            std::vector<std::vector<float>> xp(nb);
+            const int span = 2 * L->nph + 1;
+            auto neighbourhood = [&](int n, std::vector<int>& lst) {
+                const int v = n / L->nom, io = n % L->nom, slot = L->view_slot[v];
+                const int it = slot / span, ips = slot % span - L->nph;
+                for (int dt = -nbr; dt <= nbr; ++dt)
+                    for (int dp = -nbr; dp <= nbr; ++dp) {
+                        const int it2 = it + dt, ips2 = ips + dp;
+                        if (it2 < 0 || it2 > L->nth || ips2 < -L->nph || ips2 > L->nph) continue;
+                        const int v2 = L->slot_view[(size_t)it2 * span + ips2 + L->nph];
+                        if (v2 < 0) continue;
+                        for (int dw = -nbr; dw <= nbr; ++dw)
+                            lst.push_back(v2 * L->nom + ((io + dw) % L->nom + L->nom) % L->nom);
+                    }
+            };
+            // phase residuals of per-particle orientation sets (empty sets score nothing)
+            auto score = [&](const std::vector<std::vector<int>>& sets, std::vector<std::vector<float>>& out) -> int {
+                int maxc = 1;
+                for (int i = 0; i < nb; ++i) maxc = std::max(maxc, (int)sets[i].size());
+                if (maxc > maxx) return fail(CRYOIM_ERR_SIZE, "rescoring set of %d orientations", maxc);
+                std::vector<float> hx((size_t)nb * maxc * 5, 0.0f);
+                std::vector<int> hcount(nb);
+                for (int i = 0; i < nb; ++i) {
+                    hcount[i] = (int)sets[i].size();
+                    for (int j = 0; j < maxc; ++j) {
+                        const int n = sets[i].empty() ? 0 : sets[i][std::min<size_t>(j, sets[i].size() - 1)];
+                        float* o = &hx[((size_t)i * maxc + j) * 5];
+                        o[0] = L->views[4 * (n / L->nom)];
+                        o[1] = L->views[4 * (n / L->nom) + 1];
+                        o[2] = L->p.searchstep * (float)(n % L->nom);
+                        o[3] = parts[b0 + i].x;
+                        o[4] = parts[b0 + i].y;
+                    }
+                }
+                CK(cudaMemcpyAsync(L->xcand.p, hx.data(), sizeof(float) * hx.size(), cudaMemcpyHostToDevice,
+                                   L->stream));
+                CK(cudaMemcpyAsync(L->xcount.p, hcount.data(), sizeof(int) * nb, cudaMemcpyHostToDevice, L->stream));
+                launch_refine_alpha(L->xcand.p, nb, L->tort.p, T, L->ops.p, L->xalpha.p, L->stream, maxc);
+                // every candidate of a particle sits at the particle's origin: shift its band once
+                CK(launch_shift_band(L->band.p, L->xcand.p, maxc, L->bd, nb, L->sband.p, L->stream));
+                PrSingleArgs a{};
+                a.band = L->band.p; a.fcut0 = L->fcut0.p; a.tband = L->tband.p; a.tfcut = tfc;
+                a.tfcut_pstride = tfs; a.ctf = ctfp; a.cand = L->xcand.p; a.alpha = L->xalpha.p; a.T = T;
+                a.bd = L->bd; a.pr = L->xpr.p; a.ncand = maxc; a.sband = L->sband.p; a.ncount = L->xcount.p;
+                a.tbandc = ctfp ? L->tbandc.p : nullptr;
+                // candidates of a particle sharing a view, in groups (the sets are sorted by
+                // orientation index, so a view's omegas are adjacent)
+                std::vector<int4> grp;
+                const int rg = pr_rescore_group_size();
+                for (int i = 0; i < nb; ++i)
+                    for (size_t j = 0; j < sets[i].size();) {
+                        size_t e = j + 1;
+                        while (e < sets[i].size() && (int)(e - j) < rg && sets[i][e] / L->nom == sets[i][j] / L->nom) ++e;
+                        grp.push_back(make_int4(i, (int)j, (int)(e - j), 0));
+                        j = e;
+                    }
+                if (!grp.empty()) {
+                    if ((r = L->xgroups.ensure(grp.size()))) return r;
+                    CK(cudaMemcpyAsync(L->xgroups.p, grp.data(), sizeof(int4) * grp.size(), cudaMemcpyHostToDevice,
+                                       L->stream));
+                    CK(launch_pr_rescore_groups(a, L->xgroups.p, (int)grp.size(), L->stream));
+                }
+                std::vector<float> h((size_t)nb * maxc);
+                CK(cudaMemcpyAsync(h.data(), L->xpr.p, sizeof(float) * h.size(), cudaMemcpyDeviceToHost, L->stream));
+                CK(cudaStreamSynchronize(L->stream));
+                out.assign(nb, std::vector<float>());
+                for (int i = 0; i < nb; ++i) out[i].assign(h.begin() + (size_t)i * maxc, h.begin() + (size_t)i * maxc + sets[i].size());
+                return CRYOIM_OK;
+            };
+            if (T > 0) {
+                // the templates under each particle's CTF, once per pass
+                if (ctfp) CK(launch_tband_ctf(L->tband.p, T, ctfp, L->bd, nb, L->tbandc.p, L->stream));
+                if (nbest <= 0 || nbest >= k) {
+                    for (int i = 0; i < nb; ++i) {
+                        for (int rr = 0; rr < k; ++rr)
+                            if (hor[i * k + rr] >= 0) neighbourhood(hor[i * k + rr], xs[i]);
+                        std::sort(xs[i].begin(), xs[i].end());
+                        xs[i].erase(std::unique(xs[i].begin(), xs[i].end()), xs[i].end());
+                        if (xs[i].empty()) xs[i].push_back(0);
+                    }
+                    if ((r = score(xs, xp))) return r;
+                } else {
+                    // the candidates first, then the neighbourhoods of the nbest best of them
+                    std::vector<std::vector<int>> xa(nb), xb(nb);
+                    std::vector<std::vector<float>> pa, pb;
+                    for (int i = 0; i < nb; ++i) {
+                        for (int rr = 0; rr < k; ++rr)
+                            if (hor[i * k + rr] >= 0) xa[i].push_back(hor[i * k + rr]);
+                        std::sort(xa[i].begin(), xa[i].end());
+                        xa[i].erase(std::unique(xa[i].begin(), xa[i].end()), xa[i].end());
+                        if (xa[i].empty()) xa[i].push_back(0);
+                    }
+                    if ((r = score(xa, pa))) return r;
+                    for (int i = 0; i < nb; ++i) {
+                        std::vector<int> ord(xa[i].size());
+                        for (size_t j = 0; j < ord.size(); ++j) ord[j] = (int)j;
+                        std::stable_sort(ord.begin(), ord.end(), [&](int x, int y) { return pa[i][x] < pa[i][y]; });
+                        std::vector<int> nb_set;
+                        for (int j = 0; j < std::min<int>(nbest, (int)ord.size()); ++j) neighbourhood(xa[i][ord[j]], nb_set);
+                        std::sort(nb_set.begin(), nb_set.end());
+                        nb_set.erase(std::unique(nb_set.begin(), nb_set.end()), nb_set.end());
+                        std::set_difference(nb_set.begin(), nb_set.end(), xa[i].begin(), xa[i].end(),
+                                            std::back_inserter(xb[i]));
+                    }
+                    if ((r = score(xb, pb))) return r;
+                    for (int i = 0; i < nb; ++i) {  // merge, sorted by orientation index
+                        size_t ia = 0, ib = 0;
+                        while (ia < xa[i].size() || ib < xb[i].size()) {
+                            if (ib >= xb[i].size() || (ia < xa[i].size() && xa[i][ia] < xb[i][ib])) {
+                                xs[i].push_back(xa[i][ia]);
+                                xp[i].push_back(pa[i][ia++]);
+                            } else {
+                                xs[i].push_back(xb[i][ib]);
+                                xp[i].push_back(pb[i][ib++]);
+                            }
                         }
                     }
                 }
             }
-        }
-        CK(cudaMemcpyAsync(hcc64.data(), c->kcc64.p, sizeof(double) * nb * k, cudaMemcpyDeviceToHost,
-                           c->stream));
-        CK(cudaStreamSynchronize(c->stream));
-        for (int i = 0; i < nb; ++i) {
-            cryoim_particle& q = parts[b0 + i];
-            q.theta0 = q.theta; q.phi0 = q.phi; q.omega0 = q.omega; q.x0 = q.x; q.y0 = q.y; q.pr0 = q.pr;
-            if (opts->pick == 0) {
-                int best = 0;
-                for (int j = 1; j < (int)xs[i].size(); ++j)
-                    if (xp[i][j] < xp[i][best]) best = j;
-                const int n = xs[i][best];
-                q.theta = c->views[4 * (n / c->nom)];
-                q.phi = c->views[4 * (n / c->nom) + 1];
-                q.omega = c->p.searchstep * (float)(n % c->nom);
-                q.pr = xp[i][best];
-            } else {
-                int best = 0;
-                for (int j = 1; j < k; ++j)
-                    if (hcc64[i * k + j] > hcc64[i * k + best]) best = j;
-                const int sidx = i * k + best;
-                q.theta = hcand[5 * sidx]; q.phi = hcand[5 * sidx + 1]; q.omega = hcand[5 * sidx + 2];
-                q.x = hcand[5 * sidx + 3]; q.y = hcand[5 * sidx + 4];
-                q.pr = (float)hcc64[sidx];
-            }
-            q.dtheta = q.theta - q.theta0; q.dphi = q.phi - q.phi0; q.domega = q.omega - q.omega0;
-            q.dx = q.x - q.x0; q.dy = q.y - q.y0; q.dpr = q.pr - q.pr0;
-            if (cands)
-                for (int j = 0; j < k; ++j) {
-                    const int a = i * k + j;
-                    float* o = cands + ((size_t)(b0 + i) * k + j) * 8;
-                    for (int e = 0; e < 5; ++e) o[e] = hcand[5 * a + e];
-                    o[5] = hcc[a];
-                    o[6] = (float)hcc64[a];
-                    o[7] = 0.0f;
-                    if (T > 0)
-                        for (size_t m = 0; m < xs[i].size(); ++m)
-                            if (xs[i][m] == hor[a]) { o[7] = xp[i][m]; break; }
+            CK(cudaMemcpyAsync(hcc64.data(), L->kcc64.p, sizeof(double) * nb * k, cudaMemcpyDeviceToHost,
+                               L->stream));
+            CK(cudaStreamSynchronize(L->stream));
+            for (int i = 0; i < nb; ++i) {
+                cryoim_particle& q = parts[b0 + i];
+                q.theta0 = q.theta; q.phi0 = q.phi; q.omega0 = q.omega; q.x0 = q.x; q.y0 = q.y; q.pr0 = q.pr;
+                if (opts->pick == 0) {
+                    int best = 0;
+                    for (int j = 1; j < (int)xs[i].size(); ++j)
+                        if (xp[i][j] < xp[i][best]) best = j;
+                    const int n = xs[i][best];
+                    q.theta = L->views[4 * (n / L->nom)];
+                    q.phi = L->views[4 * (n / L->nom) + 1];
+                    q.omega = L->p.searchstep * (float)(n % L->nom);
+                    q.pr = xp[i][best];
+                } else {
+                    int best = 0;
+                    for (int j = 1; j < k; ++j)
+                        if (hcc64[i * k + j] > hcc64[i * k + best]) best = j;
+                    const int sidx = i * k + best;
+                    q.theta = hcand[5 * sidx]; q.phi = hcand[5 * sidx + 1]; q.omega = hcand[5 * sidx + 2];
+                    q.x = hcand[5 * sidx + 3]; q.y = hcand[5 * sidx + 4];
+                    q.pr = (float)hcc64[sidx];
                 }
+                q.dtheta = q.theta - q.theta0; q.dphi = q.phi - q.phi0; q.domega = q.omega - q.omega0;
+                q.dx = q.x - q.x0; q.dy = q.y - q.y0; q.dpr = q.pr - q.pr0;
+                if (cands)
+                    for (int j = 0; j < k; ++j) {
+                        const int a = i * k + j;
+                        float* o = cands + ((size_t)(b0 + i) * k + j) * 8;
+                        for (int e = 0; e < 5; ++e) o[e] = hcand[5 * a + e];
+                        o[5] = hcc[a];
+                        o[6] = (float)hcc64[a];
+                        o[7] = 0.0f;
+                        if (T > 0)
+                            for (size_t m = 0; m < xs[i].size(); ++m)
+                                if (xs[i][m] == hor[a]) { o[7] = xp[i][m]; break; }
+                    }
+            }
         }
-    }
-    for (cudaEvent_t e : gev) cudaEventDestroy(e);
+        for (cudaEvent_t e : gev) cudaEventDestroy(e);
+        return CRYOIM_OK;
+    };
+    if ((r = alloc(c))) return r;
+    if (nlanes > 1 && ((r = refresh_lane(c)) || (r = alloc(c->lane2)))) return r;
+    CK(cudaStreamSynchronize(c->stream));  // origins, sections and proposer ready for both lanes
+    if (nlanes == 1) return run(c, 0);
+    Ctx* L2 = c->lane2;
+    L2->prof_gemm_ms = 0.0;
+    L2->prof_gemm_launches = 0;
+    L2->prof_gemm_flops = 0.0;
+    int r2 = CRYOIM_OK;
+    std::string e2;
+    std::thread th([&] {
+        if (cudaSetDevice(L2->device) != cudaSuccess) {
+            r2 = CRYOIM_ERR_CUDA;
+            e2 = "cudaSetDevice failed in the second lane";
+            return;
+        }
+        r2 = run(L2, 1);
+        if (r2) e2 = g_err;
+    });
+    const int r1 = run(c, 0);
+    th.join();
+    c->prof_gemm_ms += L2->prof_gemm_ms;
+    c->prof_gemm_launches += L2->prof_gemm_launches;
+    c->prof_gemm_flops += L2->prof_gemm_flops;
+    if (r1) return r1;
+    if (r2) return fail(r2, "%s", e2.c_str());
     return CRYOIM_OK;
 }
 
