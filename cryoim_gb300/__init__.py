@@ -85,6 +85,10 @@ class Context:
     def set_batch(self, b: int) -> None:
         call("cryoim_ctx_set_batch", self._h, int(b))
 
+    def set_lanes(self, n: int) -> None:
+        """Pass lanes of the contraction search (1..4, default 4)."""
+        call("cryoim_ctx_set_lanes", self._h, int(n))
+
     def set_profiling(self, on: bool) -> None:
         call("cryoim_ctx_set_profiling", self._h, int(bool(on)))
 

@@ -87,6 +87,7 @@ SIGNATURES = {
     "cryoim_ctx_destroy": [_vp],
     "cryoim_ctx_set_stream": [_vp, _vp],
     "cryoim_ctx_set_batch": [_vp, _i32],
+    "cryoim_ctx_set_lanes": [_vp, _i32],
     "cryoim_set_params": [_vp, _pp],
     "cryoim_ctx_set_profiling": [_vp, _i32],
     "cryoim_ctx_kernel_time": [_vp, C.POINTER(C.c_double), C.POINTER(C.c_int64)],

@@ -352,12 +352,14 @@ struct Ctx {
     long long prof_gemm_launches = 0;
     double prof_gemm_flops = 0.0;
 
-    // second pass lane of the contraction search (refresh_lane): its own stream and
-    // per-pass buffers, this context's read-only state borrowed
-    Ctx* lane2 = nullptr;
+    // pass lanes of the contraction search: this context and xlanes (refresh_lane), each
+    // extra lane with its own stream and per-pass buffers, this context's read-only
+    // state borrowed
+    int lanes = 4;
+    std::vector<Ctx*> xlanes;
 
     ~Ctx() {
-        delete lane2;
+        for (Ctx* x : xlanes) delete x;
         cudaSetDevice(device);
         for (auto& kv : plans) cufftDestroy(kv.second);
         ops.release(); tband.release(); tfcut0.release(); tort.release(); d_views.release();
@@ -1431,20 +1433,20 @@ int ensure_bmat8(Ctx* c) {
     return CRYOIM_OK;
 }
 
-// The second pass lane of the contraction search: a context with its own stream, cuFFT
+// Extra pass lane i of the contraction search: a context with its own stream, cuFFT
 // plans, per-pass buffers and proposer activations, and c's read-only state borrowed
 // (parameters, templates, search grids, origin grids, reference-map sections, proposer
 // weights).  Refreshed at every multi-pass call, after c's state is complete.
-int refresh_lane(Ctx* c) {
-    if (!c->lane2) {
+int refresh_lane(Ctx* c, int i) {
+    while ((int)c->xlanes.size() <= i) {
         Ctx* h = new (std::nothrow) Ctx();
-        if (!h) return fail(CRYOIM_ERR_NOMEM, "second lane context");
+        if (!h) return fail(CRYOIM_ERR_NOMEM, "lane context");
         h->device = c->device;
-        c->lane2 = h;
+        c->xlanes.push_back(h);
         CK(cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking));
         h->own_stream = true;
     }
-    Ctx* h = c->lane2;
+    Ctx* h = c->xlanes[i];
     h->p = c->p;
     h->have_params = c->have_params;
     h->bd = c->bd;
@@ -1569,10 +1571,10 @@ int contract_impl(Ctx* c, const float* imgs, bool on_device, cryoim_particle* pa
     std::vector<float> ohost(2 * (size_t)O);
     CK(cudaMemcpyAsync(ohost.data(), c->corigins.p, sizeof(float) * 2 * O, cudaMemcpyDeviceToHost, c->stream));
     const long row_bytes = f8 ? (long)c->cKpad8 : 2L * c->cKpad;
-    // Passes alternate between two lanes (this context and c->lane2, each with its own
+    // Passes are dealt round-robin to lanes (this context and c->xlanes, each with its own
     // stream, per-pass buffers and host thread), so that one lane's host work between
-    // its waits overlaps the other lane's kernels.
-    const int nlanes = P > PB ? 2 : 1;
+    // its waits overlaps the other lanes' kernels.
+    const int nlanes = std::max(1, std::min(c->lanes, (P + PB - 1) / PB));
     auto alloc = [&](Ctx* L) -> int {
         int r;
         if ((r = ensure_batch(L, PB))) return r;
@@ -1948,31 +1950,38 @@ int contract_impl(Ctx* c, const float* imgs, bool on_device, cryoim_particle* pa
         return CRYOIM_OK;
     };
     if ((r = alloc(c))) return r;
-    if (nlanes > 1 && ((r = refresh_lane(c)) || (r = alloc(c->lane2)))) return r;
-    CK(cudaStreamSynchronize(c->stream));  // origins, sections and proposer ready for both lanes
+    for (int i = 0; i + 1 < nlanes; ++i)
+        if ((r = refresh_lane(c, i)) || (r = alloc(c->xlanes[i]))) return r;
+    CK(cudaStreamSynchronize(c->stream));  // origins, sections and proposer ready for every lane
     if (nlanes == 1) return run(c, 0);
-    Ctx* L2 = c->lane2;
-    L2->prof_gemm_ms = 0.0;
-    L2->prof_gemm_launches = 0;
-    L2->prof_gemm_flops = 0.0;
-    int r2 = CRYOIM_OK;
-    std::string e2;
-    std::thread th([&] {
-        if (cudaSetDevice(L2->device) != cudaSuccess) {
-            r2 = CRYOIM_ERR_CUDA;
-            e2 = "cudaSetDevice failed in the second lane";
-            return;
-        }
-        r2 = run(L2, 1);
-        if (r2) e2 = g_err;
-    });
-    const int r1 = run(c, 0);
-    th.join();
-    c->prof_gemm_ms += L2->prof_gemm_ms;
-    c->prof_gemm_launches += L2->prof_gemm_launches;
-    c->prof_gemm_flops += L2->prof_gemm_flops;
-    if (r1) return r1;
-    if (r2) return fail(r2, "%s", e2.c_str());
+    std::vector<int> rx(nlanes - 1, CRYOIM_OK);
+    std::vector<std::string> ex(nlanes - 1);
+    std::vector<std::thread> th;
+    for (int i = 0; i + 1 < nlanes; ++i) {
+        Ctx* X = c->xlanes[i];
+        X->prof_gemm_ms = 0.0;
+        X->prof_gemm_launches = 0;
+        X->prof_gemm_flops = 0.0;
+        th.emplace_back([&, X, i] {
+            if (cudaSetDevice(X->device) != cudaSuccess) {
+                rx[i] = CRYOIM_ERR_CUDA;
+                ex[i] = "cudaSetDevice failed in a pass lane";
+                return;
+            }
+            rx[i] = run(X, i + 1);
+            if (rx[i]) ex[i] = g_err;
+        });
+    }
+    const int r0 = run(c, 0);
+    for (std::thread& t : th) t.join();
+    for (int i = 0; i + 1 < nlanes; ++i) {
+        c->prof_gemm_ms += c->xlanes[i]->prof_gemm_ms;
+        c->prof_gemm_launches += c->xlanes[i]->prof_gemm_launches;
+        c->prof_gemm_flops += c->xlanes[i]->prof_gemm_flops;
+    }
+    if (r0) return r0;
+    for (int i = 0; i + 1 < nlanes; ++i)
+        if (rx[i]) return fail(rx[i], "%s", ex[i].c_str());
     return CRYOIM_OK;
 }
 
@@ -2087,6 +2096,14 @@ int cryoim_ctx_set_batch(void* ctx, int32_t batch) {
     if (!c) return fail(CRYOIM_ERR_ARG, "null context");
     if (batch < 1 || batch > 65535) return fail(CRYOIM_ERR_ARG, "batch %d out of range", batch);
     c->batch = batch;
+    return CRYOIM_OK;
+}
+
+int cryoim_ctx_set_lanes(void* ctx, int32_t lanes) {
+    Ctx* c = as_ctx(ctx);
+    if (!c) return fail(CRYOIM_ERR_ARG, "null context");
+    if (lanes < 1 || lanes > 4) return fail(CRYOIM_ERR_ARG, "lanes %d out of range 1..4", lanes);
+    c->lanes = lanes;
     return CRYOIM_OK;
 }
 

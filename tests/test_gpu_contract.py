@@ -164,3 +164,25 @@ def test_proposal_form_picks_the_exhaustive_orientation(run, built, precision):
         # FP8 scores may place an orientation at a neighbouring 0.5 px origin
         tol = 1e-4 if precision == "bf16" else 5e-3
         assert cp[i, :, 6].max() > cands[i, :, 6].max() - tol, (i, cp[i, :, 6], cands[i, :, 6])
+
+
+@pytest.mark.parametrize("form", [dict(), dict(coarse=8)])
+def test_pass_lanes_give_the_same_results(run, built, form):
+    """Passes dealt to 1, 2 or 3 lanes (own streams, buffers and host threads) return
+    bit-identical orientations, scores and candidates: one particle per pass here, so
+    every lane runs at least one pass."""
+    import cryoim_gb300 as ci
+    (p, vol, tmpl, timgs, imgs, parts, truth), q, cands, stats = run
+    out = []
+    with ci.Context(0, p) as ctx:
+        ctx.load_templates(timgs, tmpl)
+        ctx.set_reference_map(vol)
+        ctx.set_batch(1)
+        for lanes in (1, 2, 3):
+            ctx.set_lanes(lanes)
+            ql = parts.copy()
+            cl = ctx.contract_search(imgs, ql, origin_max=2.0, origin_step=0.5, topk=8, want_cands=True, **form)
+            out.append((ql, cl))
+    for ql, cl in out[1:]:
+        assert np.array_equal(ql, out[0][0])
+        assert np.array_equal(cl, out[0][1])
