@@ -228,7 +228,25 @@ __global__ void k_ctf_band(Band bd, const float* __restrict__ dfs, float apix, f
     ctf[(long)p * W * W + q] = -(sq * sinf(phase) + ampwg * cosf(phase));
 }
 
+// floor(sqrt(v)) and ceil(sqrt(v)) of a non-negative integer, exactly
+__device__ __forceinline__ int isqrt_floor(int v) {
+    int s = (int)sqrtf((float)v);
+    while (s > 0 && s * s > v) --s;
+    while ((s + 1) * (s + 1) <= v) ++s;
+    return s;
+}
+__device__ __forceinline__ int isqrt_ceil(int v) {
+    const int s = isqrt_floor(v);
+    return s * s < v ? s + 1 : s;
+}
+
 // Fcut of (template x CTF): cal_crosslin_PR_omega.f90:34-38, hoisted per particle.
+// Template amplitude cuts under each particle's CTF (FT_amp_expfit.f90 on template x
+// CTF over the ky >= 0 half plane): one block per (template, particle), one warp per
+// ring at a time.  Ring ir holds the pixels with int(|h| + 1/2) = ir, i.e. the integer
+// range ir^2 - ir + 1 <= hx^2 + ky^2 <= ir^2 + ir; lane l takes rows ky = l, l + 32, ...
+// and the ring's hx on them, summing |t c|, the radius and the count in FP64 (then a
+// warp reduction: no atomics, a fixed order).
 __global__ void k_tmpl_fcut(const float2* __restrict__ tband, int T, const float* __restrict__ ctf,
                             Band bd, float* __restrict__ tfcut) {
     extern __shared__ double dsm[];
@@ -237,24 +255,40 @@ __global__ void k_tmpl_fcut(const float2* __restrict__ tband, int T, const float
     double* sres = dsm + nr;
     int* snum = (int*)(dsm + 2 * nr);
     const int i = blockIdx.x, p = blockIdx.y;
-    for (int k = threadIdx.x; k < nr; k += blockDim.x) { sfav[k] = 0; sres[k] = 0; snum[k] = 0; }
-    __syncthreads();
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
     const float2* tb = tband + (long)i * W * W;
     const float* cb = ctf + (long)p * W * W;
-    const int span = 2 * R + 1, cnt = (R + 1) * span;
-    for (int q = threadIdx.x; q < cnt; q += blockDim.x) {
-        int ky = q / span, hx = q % span - R;
-        float rad = sqrtf((float)(hx * hx + ky * ky));
-        int ir = (int)(rad + 0.5f);
-        if (ir >= bd.min_r && ir <= R) {
-            int b = (ky + R) * W + (hx + R);
-            float c = cb[b];
-            float2 t = tb[b];
-            float a2 = t.x * c, b2 = t.y * c;
-            float amp = sqrtf(a2 * a2 + b2 * b2);
-            atomicAdd(&sfav[ir - bd.min_r], (double)amp);
-            atomicAdd(&sres[ir - bd.min_r], (double)rad);
-            atomicAdd(&snum[ir - bd.min_r], 1);
+    for (int ir = bd.min_r + warp; ir <= R; ir += nw) {
+        double fa = 0.0, rs = 0.0;
+        int n = 0;
+        const int lo = ir * ir - ir + 1, hi = ir * ir + ir;
+        for (int ky = lane; ky <= ir; ky += 32) {
+            const int k2 = ky * ky;
+            if (k2 > hi) continue;
+            const int hmax = isqrt_floor(hi - k2);
+            const int hmin = lo - k2 <= 0 ? 0 : isqrt_ceil(lo - k2);
+            for (int hx = hmin; hx <= hmax; ++hx) {
+                const float rad = sqrtf((float)(hx * hx + k2));
+                for (int sgn = (hx == 0 ? 1 : -1); sgn <= 1; sgn += 2) {
+                    const int b = (ky + R) * W + (sgn * hx + R);
+                    const float c = cb[b];
+                    const float2 t = tb[b];
+                    const float a2 = t.x * c, b2 = t.y * c;
+                    fa += (double)sqrtf(a2 * a2 + b2 * b2);
+                    rs += (double)rad;
+                    ++n;
+                }
+            }
+        }
+        for (int o = 16; o > 0; o >>= 1) {
+            fa += __shfl_xor_sync(0xffffffffu, fa, o);
+            rs += __shfl_xor_sync(0xffffffffu, rs, o);
+            n += __shfl_xor_sync(0xffffffffu, n, o);
+        }
+        if (lane == 0) {
+            sfav[ir - bd.min_r] = fa;
+            sres[ir - bd.min_r] = rs;
+            snum[ir - bd.min_r] = n;
         }
     }
     __syncthreads();
@@ -517,7 +551,7 @@ void launch_tmpl_fcut(const float2* tband, int T, const float* ctf, int B, Band 
                       cudaStream_t st) {
     size_t sm = (size_t)bd.nr * (2 * sizeof(double) + sizeof(int)) + 16;
     dim3 g(T, B);
-    k_tmpl_fcut<<<g, 512, sm, st>>>(tband, T, ctf, bd, tfcut);
+    k_tmpl_fcut<<<g, 256, sm, st>>>(tband, T, ctf, bd, tfcut);
 }
 
 void launch_alpha_table(const float* views, int V, const float* tort, int T, const float* ops,
