@@ -439,12 +439,14 @@ ParView par_view(Ctx* c, int B) {
 }
 
 // Mask / checkerboard / FFT / band of nb images already on the device.
+// keep_flag: leave the non-finite-input flag as it is (a caller that checks it once
+// after several batches) instead of clearing it first.
 int transform_batch(Ctx* c, const float* d_src, int nb, int B, const std::vector<float>& hpar,
-                    int use_mask, int normalize, bool shift) {
+                    int use_mask, int normalize, bool shift, bool keep_flag = false) {
     ParView pv = par_view(c, B);
     CK(cudaMemcpyAsync(c->par.p, hpar.data(), sizeof(float) * 8 * B, cudaMemcpyHostToDevice,
                        c->stream));
-    CK(cudaMemsetAsync(c->flag.p, 0, sizeof(int), c->stream));
+    if (!keep_flag) CK(cudaMemsetAsync(c->flag.p, 0, sizeof(int), c->stream));
     launch_prep_images(d_src, nb, c->p.fftsize, pv.ox, pv.oy, use_mask, c->p.imgmask_px, normalize,
                        c->fft.p, c->flag.p, c->stream);
     CK(cudaGetLastError());
@@ -1210,12 +1212,13 @@ int render_cube(Ctx* c, const float* map3d, CubeTexture* ct) {
 }
 
 // mask at (x, y), transform, polar features of nb images on the device -> L.feat
-int learn_features_dev(Ctx* c, const float* d_img, int nb, const float* ox, const float* oy) {
+int learn_features_dev(Ctx* c, const float* d_img, int nb, const float* ox, const float* oy,
+                       bool keep_flag = false) {
     std::vector<float> hpar(8 * (size_t)nb, 0.0f);
     for (int i = 0; i < nb; ++i) { hpar[i] = ox[i]; hpar[nb + i] = oy[i]; }
     int r;
     if ((r = ensure_batch(c, nb))) return r;
-    if ((r = transform_batch(c, d_img, nb, nb, hpar, 1, 0, false))) return r;
+    if ((r = transform_batch(c, d_img, nb, nb, hpar, 1, 0, false, keep_flag))) return r;
     launch_lp_features(c->band.p, c->bd, nb, c->lm.feat.p, c->stream);
     CK(cudaGetLastError());
     return CRYOIM_OK;
@@ -1289,11 +1292,21 @@ int learn_train_impl(Ctx* c, const float* map3d, const cryoim_learn_opts* o, flo
     }
     const int nsteps = o->samples / B;
     std::uniform_real_distribution<float> U(0.0f, 1.0f);
-    std::vector<float> heul(3 * B), hpar(5 * B), htruth(4 * B), hox(B), hoy(B), hl(B);
+    std::vector<float> heul(3 * B), hpar(5 * B), htruth(4 * B), hox(B), hoy(B);
     const float* ops = table_ops();
     const float d2r = host_angles().deg2rad, dw = 180.0f / LP_NT;
-    double tail = 0.0;
-    int ntail = 0;
+    // No host wait inside the loop: the host draws step s + 1's orientations while the
+    // GPU runs step s.  The non-finite-input flag is checked once at the end (cleared
+    // once here, kept by every step) and the losses of the last 10 % of steps land in
+    // pinned host memory, read after the final wait.
+    const int ntail_steps = std::max(1, nsteps / 10);
+    float* hloss = nullptr;
+    CK(cudaHostAlloc((void**)&hloss, sizeof(float) * (size_t)ntail_steps * B, cudaHostAllocDefault));
+    struct PinnedFree {
+        float* p;
+        ~PinnedFree() { if (p) cudaFreeHost(p); }
+    } hloss_free{hloss};
+    CK(cudaMemsetAsync(c->flag.p, 0, sizeof(int), c->stream));
     for (int sidx = 0; sidx < nsteps; ++sidx) {
         for (int b = 0; b < B; ++b) {
             float e[3];
@@ -1322,20 +1335,20 @@ int learn_train_impl(Ctx* c, const float* map3d, const cryoim_learn_opts* o, flo
                               (unsigned long long)o->seed * 1000003ull + (unsigned long long)sidx,
                               c->p.apply_ctf != 0, img.p, ft.p, var.p)))
             return r;
-        if ((r = learn_features_dev(c, img.p, B, hox.data(), hoy.data()))) return r;
+        if ((r = learn_features_dev(c, img.p, B, hox.data(), hoy.data(), true))) return r;
         if ((r = learn_forward(c, B)) || (r = learn_backward(c, B))) return r;
         launch_lp_adam(L.w.p, L.gr.p, L.m.p, L.v.p, L.nparam, o->lr, ++L.steps, c->stream);
         CK(cudaGetLastError());
-        if (sidx >= nsteps - std::max(1, nsteps / 10)) {
-            CK(cudaMemcpyAsync(hl.data(), L.loss.p, sizeof(float) * B, cudaMemcpyDeviceToHost, c->stream));
-            CK(cudaStreamSynchronize(c->stream));
-            for (int b = 0; b < B; ++b) tail += hl[b];
-            ntail += B;
-        }
-        if ((r = check_flag(c))) return r;
+        const int tail_slot = sidx - (nsteps - ntail_steps);
+        if (tail_slot >= 0)
+            CK(cudaMemcpyAsync(hloss + (size_t)tail_slot * B, L.loss.p, sizeof(float) * B, cudaMemcpyDeviceToHost,
+                               c->stream));
     }
     CK(cudaStreamSynchronize(c->stream));
-    if ((r = learn_conv_status(c))) return r;
+    if ((r = check_flag(c)) || (r = learn_conv_status(c))) return r;
+    double tail = 0.0;
+    const int ntail = ntail_steps * B;
+    for (int q = 0; q < ntail; ++q) tail += hloss[q];
     L.step = c->p.searchstep;
     L.ready = true;
     if (stats) {
