@@ -156,7 +156,8 @@ class Context:
     def contract_search(self, imgs, parts: np.ndarray, origin_max: float = 6.0,
                         origin_step: float = 0.5, topk: int = 16, pick: int = 0,
                         want_cands: bool = False, precision: str = "bf16", nbr: int = 1,
-                        coarse: int = 0, learned: int = 0, nbr_best: int = 0):
+                        coarse: int = 0, learned: int = 0, nbr_best: int = 0,
+                        local_range: float = 0.0, local_step: float = 0.0):
         """Tensor-core cross-correlation search with FP64 / phase-residual rescoring of
         the top-k and their grid neighbours within nbr steps; parts is updated in place.
         precision: "bf16" or "fp8" (e4m3 operands with per-band scales); coarse > 0: the
@@ -164,13 +165,16 @@ class Context:
         only their fine neighbourhoods are correlated); learned > 0: the same with the
         trained proposer's `learned` cells (learn_train / learn_load first); nbr_best > 0:
         only the neighbourhoods of the nbr_best candidates of least phase residual are
-        rescored.  Returns (P, topk, 8) candidates
-        if asked: theta, phi, omega, x, y, CC (contraction), CC (FP64), PR."""
+        rescored; local_range > 0: local grid search of +-local_range degrees at
+        local_step around each particle's own orientation (pick 1, BF16).  Returns (P,
+        topk, 8) candidates if asked: theta, phi, omega, x, y, CC (contraction), CC
+        (FP64), PR."""
         assert parts.dtype == PARTICLE_DTYPE and parts.flags["C_CONTIGUOUS"]
         if precision not in ("bf16", "fp8"):
             raise ValueError("precision must be 'bf16' or 'fp8'")
         o = _abi.ContractOpts(float(origin_max), float(origin_step), int(topk), int(pick),
-                              int(precision == "fp8"), int(nbr), int(coarse), int(learned), int(nbr_best))
+                              int(precision == "fp8"), int(nbr), int(coarse), int(learned), int(nbr_best),
+                              float(local_range), float(local_step))
         out = np.zeros((len(parts), topk, 8), np.float32) if want_cands else None
         if isinstance(imgs, int):
             call("cryoim_contract_search_device", self._h, C.c_void_p(imgs), ptr(parts), len(parts),

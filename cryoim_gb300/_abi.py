@@ -64,7 +64,8 @@ class ContractOpts(C.Structure):
     """cryoim_contract_opts (include/cryoim.h)."""
     _fields_ = [("origin_max", C.c_float), ("origin_step", C.c_float), ("topk", C.c_int32),
                 ("pick", C.c_int32), ("precision", C.c_int32), ("nbr", C.c_int32), ("coarse", C.c_int32),
-                ("learned", C.c_int32), ("nbr_best", C.c_int32)]
+                ("learned", C.c_int32), ("nbr_best", C.c_int32), ("local_range", C.c_float),
+                ("local_step", C.c_float)]
 
 
 class LearnOpts(C.Structure):

@@ -340,6 +340,7 @@ struct Ctx {
     DBuf<double> kpart;
     DBuf<float2> tbandc;
     DBuf<int4> xgroups;
+    DBuf<float> lcentre;  // local form: (theta, phi, omega) grid centre per particle of a group
     DBuf<GemmGroup> ggroups;
     DBuf<int2> gseg;
     LearnModel lm;
@@ -376,7 +377,7 @@ struct Ctx {
         csamples_c.release(); bmat_c.release(); amat_c.release(); corigins_c.release(); topv_c.release();
         tilev_c.release(); kcc_c.release(); topi_c.release(); tileo_c.release(); tileorig_c.release();
         kor_c.release(); korig_c.release(); gidx.release(); pnorm_c.release(); bgather.release();
-        sband.release(); xcount.release(); kpart.release(); ggroups.release(); gseg.release(); tbandc.release(); xgroups.release();
+        sband.release(); xcount.release(); kpart.release(); ggroups.release(); gseg.release(); tbandc.release(); xgroups.release(); lcentre.release();
         lm.release();
         if (pe0) cudaEventDestroy(pe0);
         if (pe1) cudaEventDestroy(pe1);
@@ -1521,8 +1522,6 @@ int contract_impl(Ctx* c, const float* imgs, bool on_device, cryoim_particle* pa
     const int k = opts->topk;
     if (k < 1 || k > 64) return fail(CRYOIM_ERR_ARG, "topk must be 1..64");
     if (!(opts->origin_step > 0) || opts->origin_max < 0) return fail(CRYOIM_ERR_ARG, "bad origin grid");
-    if (opts->pick == 0 && c->T <= 0)
-        return fail(CRYOIM_ERR_STATE, "PR rescoring needs cryoim_load_templates");
     if (opts->precision != 0 && opts->precision != 1) return fail(CRYOIM_ERR_ARG, "precision must be 0 or 1");
     const bool f8 = opts->precision == 1;
     const int nbr = opts->nbr <= 0 ? 1 : opts->nbr;
@@ -1537,8 +1536,23 @@ int contract_impl(Ctx* c, const float* imgs, bool on_device, cryoim_particle* pa
     if (kl < 0 || kl > 64 || (kl > 0 && kc > 0)) return fail(CRYOIM_ERR_ARG, "learned must be 0..64, not with coarse");
     if (kl > 0 && !(c->lm.ready && c->lm.step == c->p.searchstep && c->cgrid.V == c->lm.V))
         return fail(CRYOIM_ERR_STATE, "no trained proposer for this search step (cryoim_learn_train / _load)");
+    // local form: each particle's own grid of (2 lm + 1)^3 orientations, cut from the band
+    // cube per pass instead of gathered from the global sections
+    const bool local = opts->local_range > 0.0f;
+    int lm = 0;
+    long nloc = 0;
+    if (local) {
+        if (!(opts->local_step > 0.0f)) return fail(CRYOIM_ERR_ARG, "local_step must be > 0");
+        lm = (int)std::lround(opts->local_range / opts->local_step);
+        if (lm < 1 || lm > 64) return fail(CRYOIM_ERR_ARG, "local_range / local_step must round to 1..64");
+        if (opts->pick != 1 || f8 || kc > 0 || kl > 0)
+            return fail(CRYOIM_ERR_ARG, "the local form needs pick = 1, BF16, no coarse or learned proposals");
+        nloc = (long)(2 * lm + 1) * (2 * lm + 1) * (2 * lm + 1);
+    } else if (opts->pick == 0 && c->T <= 0) {
+        return fail(CRYOIM_ERR_STATE, "PR rescoring needs cryoim_load_templates");
+    }
     if (P == 0) return CRYOIM_OK;
-    if ((r = f8 ? ensure_bmat8(c) : ensure_bmat(c))) return r;
+    if ((r = local ? ensure_samples(c) : (f8 ? ensure_bmat8(c) : ensure_bmat(c)))) return r;
     if (kc > 0 && (r = ensure_coarse(c, opts->origin_max, opts->origin_step))) return r;
     const int kpad = f8 ? c->cKpad8 : c->cKpad;
     c->last_kpad = kpad;
@@ -1568,8 +1582,15 @@ int contract_impl(Ctx* c, const float* imgs, bool on_device, cryoim_particle* pa
     // grouped launch reads each particle's A against that particle's own few tiles.
     const int PB = std::max(1, c->batch);
     const int pb = std::max(1, std::min(PB, 2400 / std::max(O, 1)));
-    const int arows = (kc > 0 || kl > 0) ? PB : pb;
-    const int ntiles = (int)((c->n_orient + gemm_tile_n() - 1) / gemm_tile_n());
+    const int arows = (kc > 0 || kl > 0 || local) ? PB : pb;
+    const int ntiles = (int)(((local ? nloc : c->n_orient) + gemm_tile_n() - 1) / gemm_tile_n());
+    // the band cube as a filtering texture for the local form's sections (shared by the lanes)
+    struct LocalTexture {
+        cudaArray_t arr = nullptr;
+        cudaTextureObject_t tex = 0;
+        ~LocalTexture() { free_cube_texture(arr, tex); }
+    } ltex;
+    if (local) CK(make_cube_texture(c->mapcube.p, c->p.max_r, c->stream, &ltex.arr, &ltex.tex));
     // rescoring set: each selected orientation and its grid neighbours within nbr steps
     const int maxx = nbox * k;
     if (c->num_sms == 0) CK(cudaDeviceGetAttribute(&c->num_sms, cudaDevAttrMultiProcessorCount, c->device));
@@ -1605,7 +1626,9 @@ int contract_impl(Ctx* c, const float* imgs, bool on_device, cryoim_particle* pa
             (r = L->tileorig.ensure((size_t)pb * ntiles)) || (r = L->xcand.ensure((size_t)PB * maxx * 5)) ||
             (r = L->xpr.ensure((size_t)PB * maxx)))
             return r;
-        if (T > 0 && ((r = L->xalpha.ensure((size_t)PB * maxx * T * 60)) || (r = L->sband.ensure((size_t)PB * w2)) ||
+        if (local && (r = L->lcentre.ensure(3 * (size_t)PB))) return r;
+        if (T > 0 && !local &&
+            ((r = L->xalpha.ensure((size_t)PB * maxx * T * 60)) || (r = L->sband.ensure((size_t)PB * w2)) ||
                       (r = L->xcount.ensure(PB)) || (L->p.apply_ctf && (r = L->tbandc.ensure((size_t)PB * T * w2)))))
             return r;
         return CRYOIM_OK;
@@ -1653,7 +1676,7 @@ int contract_impl(Ctx* c, const float* imgs, bool on_device, cryoim_particle* pa
             if (L->p.apply_ctf) {
                 launch_ctf_band(nb, L->bd, pv.dfs, L->p.apix, L->p.vol, L->p.cs, L->p.ampwg, L->ctf.p, L->stream);
                 ctfp = L->ctf.p;
-                if (T > 0) {
+                if (T > 0 && !local) {
                     launch_tmpl_fcut(L->tband.p, T, L->ctf.p, nb, L->bd, L->tfcut.p, L->stream);
                     tfc = L->tfcut.p;
                     tfs = (long)T * L->bd.nr;
@@ -1680,12 +1703,14 @@ int contract_impl(Ctx* c, const float* imgs, bool on_device, cryoim_particle* pa
             CK(cudaMemsetAsync(L->gerr.p, 0, sizeof(int), L->stream));
             std::vector<std::vector<int>> lists;
             ngev = 0;
-            if (kc > 0 || kl > 0) {
+            if (kc > 0 || kl > 0 || local) {
                 // proposal forms: the coarse contraction or the learned proposer names each
                 // particle's candidate orientations, the fine contraction runs on their
-                // gathered sections only
-                if ((r = kc > 0 ? coarse_lists(L, nb, ctfp, kc, nbf, lists) : learned_lists(L, nb, kl, nbf, lists)))
+                // gathered sections only; the local form cuts each particle's local grid
+                if (!local &&
+                    (r = kc > 0 ? coarse_lists(L, nb, ctfp, kc, nbf, lists) : learned_lists(L, nb, kl, nbf, lists)))
                     return r;
+                auto nrows_of = [&](int i) -> long { return local ? nloc : (long)lists[i].size(); };
                 CK(cudaMemsetAsync(L->gerr.p, 0, sizeof(int), L->stream));
                 const void* bsrc = f8 ? (const void*)L->bmat8.p : (const void*)L->bmat.p;
                 const char* abase = f8 ? (const char*)L->amat8.p : (const char*)L->amat.p;
@@ -1697,19 +1722,34 @@ int contract_impl(Ctx* c, const float* imgs, bool on_device, cryoim_particle* pa
                 for (int i0 = 0; i0 < nb;) {
                     int i1 = i0;
                     long rows = 0;
-                    while (i1 < nb && (i1 == i0 || (rows + (long)lists[i1].size()) * row_bytes <= (8L << 30)))
-                        rows += (long)lists[i1++].size();
-                    std::vector<int> idx;
-                    idx.reserve(rows);
-                    for (int i = i0; i < i1; ++i) idx.insert(idx.end(), lists[i].begin(), lists[i].end());
-                    if ((r = L->gidx.ensure(rows)) || (r = L->bgather.ensure((size_t)rows * row_bytes))) return r;
-                    CK(cudaMemcpyAsync(L->gidx.p, idx.data(), sizeof(int) * rows, cudaMemcpyHostToDevice, L->stream));
-                    CK(launch_gather_rows(bsrc, row_bytes, L->gidx.p, (int)rows, L->bgather.p, L->stream));
+                    while (i1 < nb && (i1 == i0 || (rows + nrows_of(i1)) * row_bytes <= (8L << 30)))
+                        rows += nrows_of(i1++);
+                    if ((r = L->bgather.ensure((size_t)rows * row_bytes))) return r;
+                    if (local) {
+                        std::vector<float> cen(3 * (size_t)(i1 - i0));
+                        for (int i = i0; i < i1; ++i) {
+                            cen[3 * (i - i0)] = parts[b0 + i].theta;
+                            cen[3 * (i - i0) + 1] = parts[b0 + i].phi;
+                            cen[3 * (i - i0) + 2] = parts[b0 + i].omega;
+                        }
+                        CK(cudaMemcpyAsync(L->lcentre.p, cen.data(), sizeof(float) * cen.size(), cudaMemcpyHostToDevice,
+                                           L->stream));
+                        CK(launch_slice_bf16_local(ltex.tex, L->p.max_r, L->csamples.p, L->cS, L->cKpad, L->lcentre.p,
+                                                   lm, opts->local_step, rows, L->bgather.p, L->stream));
+                    } else {
+                        std::vector<int> idx;
+                        idx.reserve(rows);
+                        for (int i = i0; i < i1; ++i) idx.insert(idx.end(), lists[i].begin(), lists[i].end());
+                        if ((r = L->gidx.ensure(rows))) return r;
+                        CK(cudaMemcpyAsync(L->gidx.p, idx.data(), sizeof(int) * rows, cudaMemcpyHostToDevice,
+                                           L->stream));
+                        CK(launch_gather_rows(bsrc, row_bytes, L->gidx.p, (int)rows, L->bgather.p, L->stream));
+                    }
                     std::vector<GemmGroup> hg(i1 - i0);
                     std::vector<int2> seg(i1 - i0);
                     long roff = 0, toff = 0;
                     for (int i = i0; i < i1; ++i) {
-                        const int nl = (int)lists[i].size();
+                        const int nl = (int)nrows_of(i);
                         const int ntp = (nl + gemm_tile_n() - 1) / gemm_tile_n();
                         GemmGroup& q = hg[i - i0];
                         q.a_row0 = i * O;
@@ -1781,11 +1821,19 @@ int contract_impl(Ctx* c, const float* imgs, bool on_device, cryoim_particle* pa
             // candidates (theta, phi, omega, x, y) of the selected (orientation, origin) pairs
             for (int i = 0; i < nb * k; ++i) {
                 int n = hor[i] < 0 ? 0 : hor[i];
-                int v = n / L->nom, io = n % L->nom;
                 int o = horig[i];
-                hcand[5 * i] = L->views[4 * v];
-                hcand[5 * i + 1] = L->views[4 * v + 1];
-                hcand[5 * i + 2] = L->p.searchstep * (float)io;
+                if (local) {  // the local grid index of the particle's own grid, as k_slice_bf16_local
+                    const cryoim_particle& q = parts[b0 + i / k];
+                    const int ln = 2 * lm + 1, li = n / (ln * ln), lj = (n / ln) % ln, lk = n % ln;
+                    hcand[5 * i] = q.theta + opts->local_step * (float)(li - lm);
+                    hcand[5 * i + 1] = q.phi + opts->local_step * (float)(lj - lm);
+                    hcand[5 * i + 2] = q.omega + opts->local_step * (float)(lk - lm);
+                } else {
+                    int v = n / L->nom, io = n % L->nom;
+                    hcand[5 * i] = L->views[4 * v];
+                    hcand[5 * i + 1] = L->views[4 * v + 1];
+                    hcand[5 * i + 2] = L->p.searchstep * (float)io;
+                }
                 hcand[5 * i + 3] = ohost[2 * o];
                 hcand[5 * i + 4] = ohost[2 * o + 1];
             }
@@ -1869,7 +1917,7 @@ int contract_impl(Ctx* c, const float* imgs, bool on_device, cryoim_particle* pa
                 for (int i = 0; i < nb; ++i) out[i].assign(h.begin() + (size_t)i * maxc, h.begin() + (size_t)i * maxc + sets[i].size());
                 return CRYOIM_OK;
             };
-            if (T > 0) {
+            if (T > 0 && !local) {
                 // the templates under each particle's CTF, once per pass
                 if (ctfp) CK(launch_tband_ctf(L->tband.p, T, ctfp, L->bd, nb, L->tbandc.p, L->stream));
                 if (nbest <= 0 || nbest >= k) {

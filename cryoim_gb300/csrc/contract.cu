@@ -102,6 +102,44 @@ __global__ void __launch_bounds__(512) k_slice_bf16(cudaTextureObject_t cube, in
     }
 }
 
+// Local grids: one CTA per (particle p, grid point l) with l = (i * n + j) * n + k,
+// n = 2 m + 1, orientation (theta_p + (i - m) s, phi_p + (j - m) s, omega_p + (k - m) s)
+// from centre[3 p ..]; the row is built exactly as k_slice_bf16 builds it.
+__global__ void __launch_bounds__(512) k_slice_bf16_local(cudaTextureObject_t cube, int R,
+                                                          const int2* __restrict__ samples, int S, int Kpad,
+                                                          const float* __restrict__ centre, int m, float step,
+                                                          float d2r, long n0, __nv_bfloat162* __restrict__ B) {
+    extern __shared__ float2 ssec[];
+    __shared__ double sh[32];
+    __shared__ float rot[9];
+    const int n = 2 * m + 1;
+    const long nloc = (long)n * n * n;
+    const long q = n0 + blockIdx.x;
+    const int p = (int)(q / nloc), l = (int)(q % nloc);
+    const int i = l / (n * n), j = (l / n) % n, k = l % n;
+    if (threadIdx.x == 0)
+        euler_mat(centre[3 * p] + step * (float)(i - m), centre[3 * p + 1] + step * (float)(j - m),
+                  centre[3 * p + 2] + step * (float)(k - m), d2r, rot);
+    __syncthreads();
+    const float off = (float)(R + 1) + 0.5f;
+    float part = 0.0f;
+    for (int t = threadIdx.x; t < S; t += blockDim.x) {
+        const int2 hk = samples[t];
+        const float hx = (float)hk.x, ky = (float)hk.y;
+        const float x = rot[0] * hx + rot[1] * ky, y = rot[3] * hx + rot[4] * ky, z = rot[6] * hx + rot[7] * ky;
+        const float2 val = tex3D<float2>(cube, x + off, y + off, z + off);
+        ssec[t] = val;
+        part += val.x * val.x + val.y * val.y;
+    }
+    const double nrm = block_sum_double((double)part, sh);
+    const float inv = nrm > 0.0 ? (float)(1.0 / sqrt(nrm)) : 0.0f;
+    __nv_bfloat162* row = B + (long)blockIdx.x * (Kpad / 2);
+    for (int t = threadIdx.x; t < Kpad / 2; t += blockDim.x) {
+        float2 val = t < S ? ssec[t] : make_float2(0.f, 0.f);
+        row[t] = __floats2bfloat162_rn(val.x * inv, val.y * inv);
+    }
+}
+
 // FP64 sum over samples of |CTF * P|^2 per particle (the origin shift keeps it).
 __global__ void k_particle_norm(const float2* __restrict__ band, const float* __restrict__ ctf, Band bd,
                                 const int2* __restrict__ samples, int S, double* __restrict__ norm) {
@@ -635,6 +673,21 @@ cudaError_t launch_slice_bf16(cudaTextureObject_t cube, int R, const int2* sampl
         k_slice_bf16<<<(unsigned)nb, 512, sm, st>>>(cube, R, samples, S, Kpad, views, nom, step,
                                                    host_angles().deg2rad, n0 + c0,
                                                    (__nv_bfloat162*)B + c0 * (Kpad / 2));
+    }
+    return cudaGetLastError();
+}
+
+cudaError_t launch_slice_bf16_local(cudaTextureObject_t cube, int R, const int2* samples, int S, int Kpad,
+                                    const float* centre, int m, float step, long count, void* B, cudaStream_t st) {
+    size_t sm = (size_t)S * sizeof(float2);
+    cudaError_t e =
+        cudaFuncSetAttribute(k_slice_bf16_local, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+    if (e != cudaSuccess) return e;
+    for (long c0 = 0; c0 < count; c0 += 65535) {
+        long nb = count - c0 < 65535 ? count - c0 : 65535;
+        k_slice_bf16_local<<<(unsigned)nb, 512, sm, st>>>(cube, R, samples, S, Kpad, centre, m, step,
+                                                         host_angles().deg2rad, c0,
+                                                         (__nv_bfloat162*)B + c0 * (Kpad / 2));
     }
     return cudaGetLastError();
 }

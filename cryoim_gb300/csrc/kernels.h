@@ -174,6 +174,9 @@ void free_cube_texture(cudaArray_t arr, cudaTextureObject_t tex);
 cudaError_t launch_slice_bf16(cudaTextureObject_t cube, int R, const int2* samples, int S, int Kpad,
                               const float* views, int nom, float step, long n0, long count, void* B,
                               cudaStream_t st);
+// Rows of each particle's local grid (k_slice_bf16_local): count = particles x (2 m + 1)^3
+cudaError_t launch_slice_bf16_local(cudaTextureObject_t cube, int R, const int2* samples, int S, int Kpad,
+                                    const float* centre, int m, float step, long count, void* B, cudaStream_t st);
 void launch_particle_norm(const float2* band, const float* ctf, Band bd, const int2* samples, int S,
                           int B, double* norm, cudaStream_t st);
 // Rows (p, o) of A, p < B, o < O; origins: O x 2 (x, y) pixels.

@@ -445,6 +445,17 @@ typedef struct cryoim_contract_opts {
                            all topk candidates.  m > 0: the candidates are scored
                            first, then only the neighbourhoods of the m with the least
                            phase residual                                            */
+    float local_range;  /* 0: global search.  > 0: local search of each particle around
+                           its own (theta, phi, omega): every grid point theta + i s,
+                           phi + j s, omega + k s, |i|, |j|, |k| <= round(local_range / s),
+                           s = local_step (degrees), against every origin; the sections
+                           of these orientations are cut from the map's band cube for
+                           the pass and correlated in BF16 on the tensor cores, the topk
+                           best rescored in FP64 (pick = 1, precision = 0, no coarse or
+                           learned proposals, no templates needed; at most 2,146,689
+                           orientations per particle).  The local form of sub-particle
+                           refinement; no reference counterpart                      */
+    float local_step;
 } cryoim_contract_opts;
 
 /* ---- learned orientation proposer ------------------------------------------- */

@@ -1,0 +1,98 @@
+"""The local form of the contraction search (cryoim_contract_opts.local_range): each
+particle's own grid of orientations around its input (theta, phi, omega), sliced from
+the map's band cube for the pass and correlated against the origin grid on the tensor
+cores (BF16), the top candidates rescored in FP64.  Noise-free particles whose true
+orientation lies on their grid come back within half a grid step of it, at the origin
+next to the truth, from differently centred grids alike; every returned candidate's FP64 correlation equals
+an independent FP64 restatement (oracle central section x oracle-prepared particle, CTF,
+origin shift); passes split across lanes give the same result; bad options are
+refused."""
+import numpy as np
+import pytest
+
+from _data import small_case
+from test_gpu_contract import cc_fp64, map_cube_full
+
+pytestmark = pytest.mark.gpu
+
+STEP, M = 2.0, 3  # local grid: +-3 steps of 2 degrees (343 orientations)
+
+
+@pytest.fixture(scope="module")
+def case(built):
+    return small_case(P=4, T=4, step=4.0)
+
+
+def offsets(P, seed):
+    rng = np.random.default_rng(seed)
+    return rng.integers(-(M - 1), M, size=(P, 3))
+
+
+def run_local(case, off, lanes=4, batch=64, topk=8):
+    import cryoim_gb300 as ci
+    p, vol, tmpl, timgs, imgs, parts, truth = case
+    q = parts.copy()
+    q["theta"] = truth[:, 0] + STEP * off[:, 0]
+    q["phi"] = truth[:, 1] + STEP * off[:, 1]
+    q["omega"] = truth[:, 2] + STEP * off[:, 2]
+    with ci.Context(0, p) as ctx:
+        ctx.set_reference_map(vol)
+        ctx.set_lanes(lanes)
+        ctx.set_batch(batch)
+        cands = ctx.contract_search(imgs, q, origin_max=2.0, origin_step=0.5, topk=topk, pick=1,
+                                    want_cands=True, local_range=M * STEP, local_step=STEP)
+    return q, cands
+
+
+def test_noise_free_particles_land_on_their_true_grid_point(case):
+    from cryoim_gb300 import synth
+    p, vol, tmpl, timgs, imgs, parts, truth = case
+    for seed in (1, 2):
+        q, cands = run_local(case, offsets(len(parts), seed))
+        for i in range(len(parts)):
+            # compared as rotations: near theta = 0 or 180 degrees grid points that shift
+            # phi and omega together lie within a fraction of a step of the truth, and the
+            # best of them can win by interpolation; the search resolves half a step
+            got = tuple(float(q[f][i]) for f in ("theta", "phi", "omega"))
+            err = synth.orientation_error(got, truth[i])
+            assert err < 0.5 * STEP, (i, err, got, truth[i])
+            assert abs(q["x"][i] - parts["x"][i]) <= 0.5 and abs(q["y"][i] - parts["y"][i]) <= 0.5
+            # the pick is the best FP64 CC among the candidates
+            assert q["pr"][i] == pytest.approx(cands[i, :, 6].max(), rel=1e-6)
+
+
+def test_fp64_scores_match_independent_cc(case, orc):
+    p, vol, tmpl, timgs, imgs, parts, truth = case
+    q, cands = run_local(case, offsets(len(parts), 3))
+    vft = map_cube_full(vol)
+    for i in range(len(parts)):
+        for j in range(3):
+            ref = cc_fp64(orc, p, vft, imgs[i], parts[i], cands[i, j, :5].astype(np.float64))
+            assert abs(cands[i, j, 6] - ref) < 1e-6, (i, j, cands[i, j, 6], ref)
+            # the BF16 tensor-core score tracks it
+            assert abs(cands[i, j, 5] - ref) < 2e-2, (i, j, cands[i, j, 5], ref)
+        # candidates lie on the particle's own grid
+        for j in range(cands.shape[1]):
+            d = (cands[i, j, :3] - np.array([q["theta"][i], q["phi"][i], q["omega"][i]])) / STEP
+            assert np.all(np.abs(d - np.round(d)) < 1e-3) and np.all(np.abs(d) <= 2 * M + 1e-3)
+
+
+def test_lanes_and_passes_do_not_change_the_result(case):
+    off = offsets(len(case[5]), 4)
+    q1, c1 = run_local(case, off, lanes=1, batch=64)
+    q4, c4 = run_local(case, off, lanes=3, batch=1)
+    assert np.array_equal(q1, q4)
+    assert np.array_equal(c1, c4)
+
+
+def test_bad_local_options_are_refused(case):
+    import cryoim_gb300 as ci
+    p, vol, tmpl, timgs, imgs, parts, truth = case
+    with ci.Context(0, p) as ctx:
+        ctx.set_reference_map(vol)
+        for kw in (dict(pick=0), dict(pick=1, precision="fp8"), dict(pick=1, local_step=0.0),
+                   dict(pick=1, coarse=4)):
+            args = dict(origin_max=2.0, origin_step=0.5, topk=8, local_range=3.0, local_step=1.0)
+            args.update(kw)
+            with pytest.raises(ci.CryoimError):
+                ctx.contract_search(imgs, parts.copy(), **args)
