@@ -238,8 +238,15 @@ def test_trained_proposer_leads_to_the_exhaustive_pick(built, tmp_path):
         c2.learn_load(path)
         q2 = parts.copy()
         c2b = c2.contract_search(imgs, q2, origin_max=2.0, origin_step=0.5, topk=8, learned=16, want_cands=True)
+        # one particle per pass, dealt to 3 lanes: each lane runs the borrowed proposer
+        c2.set_batch(1)
+        c2.set_lanes(3)
+        q3 = parts.copy()
+        c3 = c2.contract_search(imgs, q3, origin_max=2.0, origin_step=0.5, topk=8, learned=16, want_cands=True)
     assert np.array_equal(q2, ql)
     assert np.array_equal(c2b, cl)
+    assert np.array_equal(q3, ql)
+    assert np.array_equal(c3, cl)
 
 
 def test_learned_form_needs_a_trained_proposer(built):
