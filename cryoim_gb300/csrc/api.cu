@@ -150,6 +150,10 @@ template <class T> struct DBuf {
     T* p = nullptr;
     size_t n = 0;
     bool own = true;  // false: another context's buffer, used read-only and never freed here
+    DBuf() = default;
+    DBuf(const DBuf&) = delete;
+    DBuf& operator=(const DBuf&) = delete;
+    ~DBuf() { release(); }
     int ensure(size_t want) {
         if (want <= n) return 0;
         release();
@@ -386,6 +390,8 @@ struct Ctx {
 };
 
 Ctx* as_ctx(void* c) { return reinterpret_cast<Ctx*>(c); }
+
+int refresh_lane(Ctx* c, int i);
 
 int plan2d(Ctx* c, int nb, cufftHandle* out) {
     auto it = c->plans.find(nb);
@@ -1293,22 +1299,13 @@ int learn_train_impl(Ctx* c, const float* map3d, const cryoim_learn_opts* o, flo
     }
     const int nsteps = o->samples / B;
     std::uniform_real_distribution<float> U(0.0f, 1.0f);
-    std::vector<float> heul(3 * B), hpar(5 * B), htruth(4 * B), hox(B), hoy(B);
+    std::vector<float> heul(3 * B), hpar(5 * B), hox(B), hoy(B);
+    std::vector<float> htruth[2] = {std::vector<float>(4 * B), std::vector<float>(4 * B)};
     const float* ops = table_ops();
     const float d2r = host_angles().deg2rad, dw = 180.0f / LP_NT;
-    // No host wait inside the loop: the host draws step s + 1's orientations while the
-    // GPU runs step s.  The non-finite-input flag is checked once at the end (cleared
-    // once here, kept by every step) and the losses of the last 10 % of steps land in
-    // pinned host memory, read after the final wait.
-    const int ntail_steps = std::max(1, nsteps / 10);
-    float* hloss = nullptr;
-    CK(cudaHostAlloc((void**)&hloss, sizeof(float) * (size_t)ntail_steps * B, cudaHostAllocDefault));
-    struct PinnedFree {
-        float* p;
-        ~PinnedFree() { if (p) cudaFreeHost(p); }
-    } hloss_free{hloss};
-    CK(cudaMemsetAsync(c->flag.p, 0, sizeof(int), c->stream));
-    for (int sidx = 0; sidx < nsteps; ++sidx) {
+    // step s's orientations, CTF and origins (heul, hpar, hox, hoy) and targets (htruth[s & 1])
+    auto draw = [&](int sidx) {
+        std::vector<float>& ht = htruth[sidx & 1];
         for (int b = 0; b < B; ++b) {
             float e[3];
             random_euler(rng, e);
@@ -1322,21 +1319,74 @@ int learn_train_impl(Ctx* c, const float* map3d, const cryoim_learn_opts* o, flo
             hoy[b] = oy;
             float th = e[0], ph = e[1], om = e[2];
             asu_fold(&th, &ph, &om, ops, d2r);
-            htruth[4 * b] = sinf(th * d2r) * cosf(ph * d2r);
-            htruth[4 * b + 1] = sinf(th * d2r) * sinf(ph * d2r);
-            htruth[4 * b + 2] = cosf(th * d2r);
+            ht[4 * b] = sinf(th * d2r) * cosf(ph * d2r);
+            ht[4 * b + 1] = sinf(th * d2r) * sinf(ph * d2r);
+            ht[4 * b + 2] = cosf(th * d2r);
             float wv = std::fmod((float)L.sign * om, 180.0f);
             if (wv < 0.0f) wv += 180.0f;
-            htruth[4 * b + 3] = (float)(((int)std::lround(wv / dw)) % LP_NT);
+            ht[4 * b + 3] = (float)(((int)std::lround(wv / dw)) % LP_NT);
         }
-        CK(cudaMemcpyAsync(deul.p, heul.data(), sizeof(float) * 3 * B, cudaMemcpyHostToDevice, c->stream));
-        CK(cudaMemcpyAsync(dpar.p, hpar.data(), sizeof(float) * 5 * B, cudaMemcpyHostToDevice, c->stream));
-        CK(cudaMemcpyAsync(L.truth.p, htruth.data(), sizeof(float) * 4 * B, cudaMemcpyHostToDevice, c->stream));
-        if ((r = learn_render(c, ct.tex, deul.p, dpar.p, B, o->snr,
-                              (unsigned long long)o->seed * 1000003ull + (unsigned long long)sidx,
-                              c->p.apply_ctf != 0, img.p, ft.p, var.p)))
-            return r;
-        if ((r = learn_features_dev(c, img.p, B, hox.data(), hoy.data(), true))) return r;
+    };
+    // The training data of step s + 1 (projections, transforms, features) are made on a
+    // second lane (its own stream and buffers) while the network runs step s; events order
+    // the hand-over of the features.  No host wait inside the loop: the host draws step
+    // s + 1 while the GPU works.  The non-finite-input flags are checked once at the end
+    // (cleared once here, kept by every step) and the losses of the last 10 % of steps
+    // land in pinned host memory, read after the final wait.
+    if ((r = refresh_lane(c, 0))) return r;
+    Ctx* G = c->xlanes[0];
+    DBuf<float> gimg, gdeul, gdpar, gvar;
+    DBuf<float2> gft;
+    if ((r = gimg.ensure((size_t)B * nn)) || (r = gft.ensure((size_t)B * nn)) || (r = gdeul.ensure(3 * (size_t)B)) ||
+        (r = gdpar.ensure(5 * (size_t)B)) || (r = gvar.ensure(B)) || (r = ensure_batch(G, B)) ||
+        (r = G->lm.feat.ensure((size_t)B * LP_NR * LP_NT)))
+        return r;
+    struct Events {
+        cudaEvent_t ready = nullptr, copied = nullptr;
+        ~Events() {
+            if (ready) cudaEventDestroy(ready);
+            if (copied) cudaEventDestroy(copied);
+        }
+    } ev;
+    CK(cudaEventCreateWithFlags(&ev.ready, cudaEventDisableTiming));
+    CK(cudaEventCreateWithFlags(&ev.copied, cudaEventDisableTiming));
+    const int ntail_steps = std::max(1, nsteps / 10);
+    float* hloss = nullptr;
+    CK(cudaHostAlloc((void**)&hloss, sizeof(float) * (size_t)ntail_steps * B, cudaHostAllocDefault));
+    struct PinnedFree {
+        float* p;
+        ~PinnedFree() { if (p) cudaFreeHost(p); }
+    } hloss_free{hloss};
+    CK(cudaMemsetAsync(c->flag.p, 0, sizeof(int), c->stream));
+    CK(cudaStreamSynchronize(c->stream));  // weights, sign and flag set before the lane starts
+    CK(cudaMemsetAsync(G->flag.p, 0, sizeof(int), G->stream));
+    // step sidx's features into G->lm.feat, once the network has taken the previous ones
+    auto generate = [&](int sidx) -> int {
+        if (sidx > 0) CK(cudaStreamWaitEvent(G->stream, ev.copied, 0));
+        CK(cudaMemcpyAsync(gdeul.p, heul.data(), sizeof(float) * 3 * B, cudaMemcpyHostToDevice, G->stream));
+        CK(cudaMemcpyAsync(gdpar.p, hpar.data(), sizeof(float) * 5 * B, cudaMemcpyHostToDevice, G->stream));
+        int rr;
+        if ((rr = learn_render(G, ct.tex, gdeul.p, gdpar.p, B, o->snr,
+                               (unsigned long long)o->seed * 1000003ull + (unsigned long long)sidx,
+                               G->p.apply_ctf != 0, gimg.p, gft.p, gvar.p)))
+            return rr;
+        if ((rr = learn_features_dev(G, gimg.p, B, hox.data(), hoy.data(), true))) return rr;
+        CK(cudaEventRecord(ev.ready, G->stream));
+        return CRYOIM_OK;
+    };
+    draw(0);
+    if ((r = generate(0))) return r;
+    for (int sidx = 0; sidx < nsteps; ++sidx) {
+        CK(cudaMemcpyAsync(L.truth.p, htruth[sidx & 1].data(), sizeof(float) * 4 * B, cudaMemcpyHostToDevice,
+                           c->stream));
+        CK(cudaStreamWaitEvent(c->stream, ev.ready, 0));
+        CK(cudaMemcpyAsync(L.feat.p, G->lm.feat.p, sizeof(float) * (size_t)B * LP_NR * LP_NT,
+                           cudaMemcpyDeviceToDevice, c->stream));
+        CK(cudaEventRecord(ev.copied, c->stream));
+        if (sidx + 1 < nsteps) {
+            draw(sidx + 1);
+            if ((r = generate(sidx + 1))) return r;
+        }
         if ((r = learn_forward(c, B)) || (r = learn_backward(c, B))) return r;
         launch_lp_adam(L.w.p, L.gr.p, L.m.p, L.v.p, L.nparam, o->lr, ++L.steps, c->stream);
         CK(cudaGetLastError());
@@ -1345,6 +1395,8 @@ int learn_train_impl(Ctx* c, const float* map3d, const cryoim_learn_opts* o, flo
             CK(cudaMemcpyAsync(hloss + (size_t)tail_slot * B, L.loss.p, sizeof(float) * B, cudaMemcpyDeviceToHost,
                                c->stream));
     }
+    CK(cudaStreamSynchronize(G->stream));
+    if ((r = check_flag(G))) return r;
     CK(cudaStreamSynchronize(c->stream));
     if ((r = check_flag(c)) || (r = learn_conv_status(c))) return r;
     double tail = 0.0;
