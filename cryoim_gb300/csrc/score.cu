@@ -384,8 +384,18 @@ __global__ void __launch_bounds__(512) k_pr_rescore(PrSingleArgs a, Consts K) {
     const float* ctfp = a.ctf ? a.ctf + (long)p * W * W : nullptr;
     const int per_t = 60 * nr;
     float f1 = 0.f, f2 = 0.f, k1 = 0.f, k2 = 0.f;
-    for (int q = threadIdx.x; q < T * per_t; q += blockDim.x) {
-        const int i = q / per_t, rem = q - i * per_t, j = rem / nr, iq = rem - j * nr;
+    // (template i, line j, radius iq) of the flat index q = (i * 60 + j) * nr + iq, advanced
+    // by blockDim.x per iteration without integer divisions
+    const int step_j = (int)blockDim.x / nr, step_iq = (int)blockDim.x - step_j * nr;
+    int i = (int)threadIdx.x / per_t, j = ((int)threadIdx.x - i * per_t) / nr;
+    int iq = (int)threadIdx.x - i * per_t - j * nr;
+    auto advance = [&]() {
+        iq += step_iq;
+        j += step_j;
+        if (iq >= nr) { iq -= nr; ++j; }
+        while (j >= 60) { j -= 60; ++i; }
+    };
+    for (int q = threadIdx.x; q < T * per_t; q += blockDim.x, advance()) {
         const int lj = i * 60 + j;
         if (!sval[lj]) continue;
         const float4 cs4 = *reinterpret_cast<const float4*>(scs + 4 * lj);
@@ -474,8 +484,18 @@ __global__ void __launch_bounds__(512) k_pr_rescore_g(PrSingleArgs a, const int4
     float f1[RG], f2[RG], k1[RG], k2[RG];
 #pragma unroll
     for (int g = 0; g < RG; ++g) { f1[g] = 0.f; f2[g] = 0.f; k1[g] = 0.f; k2[g] = 0.f; }
-    for (int q = threadIdx.x; q < T * per_t; q += blockDim.x) {
-        const int i = q / per_t, rem = q - i * per_t, j = rem / nr, iq = rem - j * nr;
+    // (template i, line j, radius iq) of the flat index q = (i * 60 + j) * nr + iq, advanced
+    // by blockDim.x per iteration without integer divisions
+    const int step_j = (int)blockDim.x / nr, step_iq = (int)blockDim.x - step_j * nr;
+    int i = (int)threadIdx.x / per_t, j = ((int)threadIdx.x - i * per_t) / nr;
+    int iq = (int)threadIdx.x - i * per_t - j * nr;
+    auto advance = [&]() {
+        iq += step_iq;
+        j += step_j;
+        if (iq >= nr) { iq -= nr; ++j; }
+        while (j >= 60) { j -= 60; ++i; }
+    };
+    for (int q = threadIdx.x; q < T * per_t; q += blockDim.x, advance()) {
         const int lj = i * 60 + j;
         if (!sval[lj]) continue;
         const float fr = (float)(minR + iq);
