@@ -83,31 +83,38 @@ constexpr int conv_fwd_smem() {
     return 1024 + 3 * CT_ROW_BYTES + 3 * (3 * COUT * 128) + 8 * COUT * 4 + 64;
 }
 
+// 256 threads: warps w and w + 4 share TMEM lanes 32 (w & 3) .. + 31 (angle t); the
+// half h = w >> 2 stages channels 16 h .. 16 h + 15 of angle t and writes the output
+// channels co of its half (COUT / 2 of them) in the epilogue.
+constexpr int CT_FWD_THREADS = 256;
+
 template <int COUT>
-__global__ void __launch_bounds__(CT_NT) k_conv3_tc(ConvTcArgs a) {
+__global__ void __launch_bounds__(CT_FWD_THREADS, 2) k_conv3_tc(ConvTcArgs a) {
     constexpr int N = 3 * COUT;          // product columns (dt, co)
     constexpr int WB = N * 128;          // one dh block of the weight operand
-    constexpr int NP = (N + 31) / 32 * 32;
+    constexpr int CH = COUT / 2;         // output channels per half
     extern __shared__ unsigned char smraw[];
     unsigned char* sm = (unsigned char*)(((uintptr_t)smraw + 1023) & ~(uintptr_t)1023);
     unsigned char* sX = sm;                      // ring of 3 staged input rows
     unsigned char* sWt = sm + 3 * CT_ROW_BYTES;  // 3 dh blocks of N rows
-    float* sEdge = (float*)(sWt + 3 * WB);       // [2][4 warps][COUT]
+    float* sEdge = (float*)(sWt + 3 * WB);       // [2][4 lane quarters][COUT]
     uint64_t* bar = (uint64_t*)(sEdge + 8 * COUT);
     uint32_t* tslot = (uint32_t*)(bar + 1);
-    const int t = threadIdx.x, warp = t >> 5, lane = t & 31;
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    const int quarter = warp & 3, half = warp >> 2;
+    const int t = 32 * quarter + lane;  // the angle (product row, TMEM lane) of this thread
     const int Cin = a.Cin, H = a.H;
     const long q0 = (long)blockIdx.x * a.rows_per_cta;
     const long q1 = min((long)a.B * H, q0 + a.rows_per_cta);
     if (q0 >= q1) return;  // uniform over the block
 
-    if (t == 0) {
+    if (tid == 0) {
         tc::mbar_init(bar, 1);
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
     if (warp == 0) tmem_alloc(tslot);
     // weights: block dh, row n = dt * COUT + co, element ci (zero beyond Cin)
-    for (int i = t; i < 3 * N * 32; i += CT_NT) {
+    for (int i = tid; i < 3 * N * 32; i += CT_FWD_THREADS) {
         const int dh = i / (N * 32), rem = i - dh * N * 32, n = rem >> 5, ci = rem & 31;
         const int dt = n / COUT, co = n - dt * COUT;
         const float v = ci < Cin ? tf32r(__ldg(a.W + ((co * Cin + ci) * 3 + dh) * 3 + dt)) : 0.f;
@@ -119,22 +126,25 @@ __global__ void __launch_bounds__(CT_NT) k_conv3_tc(ConvTcArgs a) {
     const uint32_t tmem = *tslot;
     constexpr uint32_t idesc = idesc_tf32(N);
 
-    // input row hh of sample b: thread t loads angle t's channels into registers (load),
-    // rounds them to TF32 and writes them to a ring slot (put)
-    float pre[32];
+    // input row hh of sample b: this thread loads channels 16 half .. + 15 of angle t into
+    // registers (load), rounds them to TF32 and writes them to a ring slot (put)
+    float pre[16];
     const long cs = (long)H * CT_NT;
+    const int c0 = 16 * half;
     auto load = [&](int b, int hh) {
         const bool ok = hh >= 0 && hh < H;
         const float* src = a.in + ((long)b * Cin * H + (ok ? hh : 0)) * CT_NT + t;
 #pragma unroll
-        for (int c = 0; c < 32; ++c) pre[c] = (ok && c < Cin) ? __ldg(src + c * cs) : 0.f;
+        for (int c = 0; c < 16; ++c) pre[c] = (ok && c0 + c < Cin) ? __ldg(src + (c0 + c) * cs) : 0.f;
     };
     auto put = [&](int slot) {
         unsigned char* dst = sX + slot * CT_ROW_BYTES + t * 128;
 #pragma unroll
-        for (int c4 = 0; c4 < 8; ++c4)
-            *(float4*)(dst + ((c4 ^ (t & 7)) << 4)) = make_float4(tf32r(pre[4 * c4]), tf32r(pre[4 * c4 + 1]),
-                                                                   tf32r(pre[4 * c4 + 2]), tf32r(pre[4 * c4 + 3]));
+        for (int k4 = 0; k4 < 4; ++k4) {
+            const int c4 = 4 * half + k4;
+            *(float4*)(dst + ((c4 ^ (t & 7)) << 4)) = make_float4(tf32r(pre[4 * k4]), tf32r(pre[4 * k4 + 1]),
+                                                                   tf32r(pre[4 * k4 + 2]), tf32r(pre[4 * k4 + 3]));
+        }
     };
 
     uint32_t phase = 0;
@@ -158,7 +168,7 @@ __global__ void __launch_bounds__(CT_NT) k_conv3_tc(ConvTcArgs a) {
         tc::fence_before();
         __syncthreads();
         tc::fence_after();
-        if (t == 0) {
+        if (tid == 0) {
 #pragma unroll
             for (int dh = 0; dh < 3; ++dh) {
                 const uint32_t xa = tc::su32(sX + ((h + dh) % 3) * CT_ROW_BYTES);
@@ -182,35 +192,51 @@ __global__ void __launch_bounds__(CT_NT) k_conv3_tc(ConvTcArgs a) {
             break;
         }
         tc::fence_after();
-        float P[NP];
-        const uint32_t trow = tmem + ((uint32_t)(32 * warp) << 16);
+        // this half's output channels co = CH half .. + CH - 1, each at dt = 0, 1, 2
+        float P0[CH], P1[CH], P2[CH];
+        const uint32_t tlane = tmem + ((uint32_t)(32 * quarter) << 16);
+        if constexpr (CH == 16) {  // columns dt * 32 + 16 half .. + 15
+            tc::tmem_ld16(tlane + 16 * half, P0);
+            tc::tmem_ld16(tlane + 32 + 16 * half, P1);
+            tc::tmem_ld16(tlane + 64 + 16 * half, P2);
+        } else {  // columns dt * 16 .. + 15, of which this half takes 8 half .. + 7
+            float tmp[16];
+            tc::tmem_ld16(tlane, tmp);
 #pragma unroll
-        for (int c = 0; c < NP / 32; ++c) tc::tmem_ld32(trow + c * 32, P + c * 32);
+            for (int c = 0; c < CH; ++c) P0[c] = half ? tmp[CH + c] : tmp[c];
+            tc::tmem_ld16(tlane + 16, tmp);
+#pragma unroll
+            for (int c = 0; c < CH; ++c) P1[c] = half ? tmp[CH + c] : tmp[c];
+            tc::tmem_ld16(tlane + 32, tmp);
+#pragma unroll
+            for (int c = 0; c < CH; ++c) P2[c] = half ? tmp[CH + c] : tmp[c];
+        }
         if (lane == 31) {
 #pragma unroll
-            for (int co = 0; co < COUT; ++co) sEdge[warp * COUT + co] = P[co];
+            for (int c = 0; c < CH; ++c) sEdge[quarter * COUT + CH * half + c] = P0[c];
         }
         if (lane == 0) {
 #pragma unroll
-            for (int co = 0; co < COUT; ++co) sEdge[(4 + warp) * COUT + co] = P[2 * COUT + co];
+            for (int c = 0; c < CH; ++c) sEdge[(4 + quarter) * COUT + CH * half + c] = P2[c];
         }
         tc::fence_before();
         __syncthreads();
-        const int wp = (warp + 3) & 3, wn = (warp + 1) & 3;
+        const int qp = (quarter + 3) & 3, qn = (quarter + 1) & 3;
         float* orow = a.out + ((long)b * COUT * H + h) * CT_NT + t;
 #pragma unroll
-        for (int co = 0; co < COUT; ++co) {
-            float lo = __shfl_up_sync(0xffffffffu, P[co], 1);
-            float hi = __shfl_down_sync(0xffffffffu, P[2 * COUT + co], 1);
-            if (lane == 0) lo = sEdge[wp * COUT + co];
-            if (lane == 31) hi = sEdge[(4 + wn) * COUT + co];
-            float v = lo + P[COUT + co] + hi;
+        for (int c = 0; c < CH; ++c) {
+            const int co = CH * half + c;
+            float lo = __shfl_up_sync(0xffffffffu, P0[c], 1);
+            float hi = __shfl_down_sync(0xffffffffu, P2[c], 1);
+            if (lane == 0) lo = sEdge[qp * COUT + co];
+            if (lane == 31) hi = sEdge[(4 + qn) * COUT + co];
+            float v = lo + P1[c] + hi;
             if (a.bias) v += __ldg(a.bias + co);
             if (a.relu) v = fmaxf(v, 0.f);
             orow[(long)co * H * CT_NT] = v;
         }
     }
-    if (!ok && t == 0) tc::mbar_wait(bar, phase ^ 1u, a.err, false, CT_WAIT_NS);  // MMAs still in flight
+    if (!ok && tid == 0) tc::mbar_wait(bar, phase ^ 1u, a.err, false, CT_WAIT_NS);  // MMAs still in flight
     tc::fence_before();
     __syncthreads();
     if (warp == 0) {
@@ -251,9 +277,14 @@ inline int conv_wgrad_smem(int cout, int cin) {
     return 1024 + g.A_BYTES + 3 * g.SLOT + 64;
 }
 
+// 256 threads: warps w and w + 4 share TMEM lanes 32 (w & 3) .. + 31 (angle t when
+// staging, product row (dt, co) in the epilogue); the half h = w >> 2 stages the output
+// channels co of its half (dpre) and the input channels 16 h .. 16 h + 15, and adds the
+// columns ci of its half to dW at the end.
 template <int COUT>
-__global__ void __launch_bounds__(CT_NT) k_conv3_wgrad_tc(ConvWgTcArgs a) {
+__global__ void __launch_bounds__(CT_FWD_THREADS, 2) k_conv3_wgrad_tc(ConvWgTcArgs a) {
     constexpr int M = 3 * COUT;
+    constexpr int CH = COUT / 2;  // dpre channels per half
     extern __shared__ unsigned char smraw[];
     unsigned char* sm = (unsigned char*)(((uintptr_t)smraw + 1023) & ~(uintptr_t)1023);
     const int Cin = a.Cin, H = a.H;
@@ -262,44 +293,49 @@ __global__ void __launch_bounds__(CT_NT) k_conv3_wgrad_tc(ConvWgTcArgs a) {
     unsigned char* sB = sm + g.A_BYTES;
     uint64_t* bar = (uint64_t*)(sB + 3 * g.SLOT);
     uint32_t* tslot = (uint32_t*)(bar + 1);
-    const int t = threadIdx.x, warp = t >> 5, lane = t & 31;
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    const int quarter = warp & 3, half = warp >> 2;
+    const int t = 32 * quarter + lane;
     const long q0 = (long)blockIdx.x * a.rows_per_cta;
     const long q1 = min((long)a.B * H, q0 + a.rows_per_cta);
     if (q0 >= q1) return;  // uniform over the block
 
-    if (t == 0) {
+    if (tid == 0) {
         tc::mbar_init(bar, 1);
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
     if (warp == 0) tmem_alloc(tslot);
     // rows the MMAs read but whose products are unused start out as zeros
-    for (int i = t; i < (g.A_BYTES + 3 * g.SLOT) / 16; i += CT_NT) ((float4*)sm)[i] = make_float4(0.f, 0.f, 0.f, 0.f);
+    for (int i = tid; i < (g.A_BYTES + 3 * g.SLOT) / 16; i += CT_FWD_THREADS)
+        ((float4*)sm)[i] = make_float4(0.f, 0.f, 0.f, 0.f);
     tc::fence_before();
     __syncthreads();
     tc::fence_after();
     const uint32_t tmem = *tslot;
     const uint32_t idesc = idesc_tf32(g.NB);
 
-    float dbacc[COUT];
+    float dbacc[CH];
 #pragma unroll
-    for (int co = 0; co < COUT; ++co) dbacc[co] = 0.f;
-    // dpre row h (preA: this thread's angle, every co) and input row hh (preB: every ci)
-    // are loaded into registers a step ahead, then rounded and written to shared memory
-    float preA[COUT], preB[32];
+    for (int c = 0; c < CH; ++c) dbacc[c] = 0.f;
+    // dpre row h (preA: this thread's angle, this half's co) and input row hh (preB: this
+    // half's ci) are loaded into registers a step ahead, then rounded and written to
+    // shared memory
+    float preA[CH], preB[16];
     const long cs = (long)H * CT_NT;
+    const int co0 = CH * half, ci0 = 16 * half;
     auto loadA = [&](int b, int h) {
         const float* src = a.dpre + ((long)b * COUT * H + h) * CT_NT + t;
 #pragma unroll
-        for (int co = 0; co < COUT; ++co) preA[co] = __ldg(src + co * cs);
+        for (int c = 0; c < CH; ++c) preA[c] = __ldg(src + (co0 + c) * cs);
     };
     auto putA = [&]() {
 #pragma unroll
-        for (int co = 0; co < COUT; ++co) {
-            dbacc[co] += preA[co];
-            const float v = tf32r(preA[co]);
+        for (int c = 0; c < CH; ++c) {
+            dbacc[c] += preA[c];
+            const float v = tf32r(preA[c]);
 #pragma unroll
             for (int dt = 0; dt < 3; ++dt) {
-                const int s = (t + dt - 1) & (CT_NT - 1), m = dt * COUT + co;
+                const int s = (t + dt - 1) & (CT_NT - 1), m = dt * COUT + co0 + c;
                 *(float*)(sA + (s >> 5) * g.PA + tc::swz128_off4(m, s & 31)) = v;
             }
         }
@@ -308,13 +344,13 @@ __global__ void __launch_bounds__(CT_NT) k_conv3_wgrad_tc(ConvWgTcArgs a) {
         const bool ok = hh >= 0 && hh < H;
         const float* src = a.in + ((long)b * Cin * H + (ok ? hh : 0)) * CT_NT + t;
 #pragma unroll
-        for (int c = 0; c < 32; ++c) preB[c] = (ok && c < Cin) ? __ldg(src + c * cs) : 0.f;
+        for (int c = 0; c < 16; ++c) preB[c] = (ok && ci0 + c < Cin) ? __ldg(src + (ci0 + c) * cs) : 0.f;
     };
     auto putB = [&](int slot) {
         unsigned char* dst = sB + slot * g.SLOT + (t >> 5) * g.PB;
 #pragma unroll
-        for (int ci = 0; ci < 32; ++ci)
-            if (ci < Cin) *(float*)(dst + tc::swz128_off4(ci, t & 31)) = tf32r(preB[ci]);
+        for (int c = 0; c < 16; ++c)
+            if (ci0 + c < Cin) *(float*)(dst + tc::swz128_off4(ci0 + c, t & 31)) = tf32r(preB[c]);
     };
 
     uint32_t phase = 0;
@@ -341,7 +377,7 @@ __global__ void __launch_bounds__(CT_NT) k_conv3_wgrad_tc(ConvWgTcArgs a) {
         tc::fence_before();
         __syncthreads();
         tc::fence_after();
-        if (t == 0) {
+        if (tid == 0) {
             const uint32_t a0 = tc::su32(sA);
             for (int dh = 0; dh < 3; ++dh) {
                 const uint32_t xb = tc::su32(sB + ((h + dh) % 3) * g.SLOT);
@@ -370,23 +406,24 @@ __global__ void __launch_bounds__(CT_NT) k_conv3_wgrad_tc(ConvWgTcArgs a) {
         tc::fence_after();
     }
     if (ok) {
-        float D[96];
-        const uint32_t trow = tmem + ((uint32_t)(32 * warp) << 16);
+        // product row t = (dt, co); this half's columns dh * 32 + 16 half .. + 15 (ci)
+        float D[48];
+        const uint32_t tlane = tmem + ((uint32_t)(32 * quarter) << 16);
 #pragma unroll
-        for (int c = 0; c < 3; ++c) tc::tmem_ld32(trow + c * 32, D + c * 32);
+        for (int dh = 0; dh < 3; ++dh) tc::tmem_ld16(tlane + (uint32_t)(dh * 32 + 16 * half), D + 16 * dh);
         if (t < M) {
             const int dt = t / COUT, co = t - dt * COUT;
             for (int dh = 0; dh < 3; ++dh)
-                for (int ci = 0; ci < Cin; ++ci)
-                    atomicAdd(a.dW + ((co * Cin + ci) * 3 + dh) * 3 + dt, D[dh * 32 + ci]);
+                for (int c = 0; c < 16 && ci0 + c < Cin; ++c)
+                    atomicAdd(a.dW + ((co * Cin + ci0 + c) * 3 + dh) * 3 + dt, D[16 * dh + c]);
         }
 #pragma unroll
-        for (int co = 0; co < COUT; ++co) {
-            float v = dbacc[co];
+        for (int c = 0; c < CH; ++c) {
+            float v = dbacc[c];
             for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
-            if (lane == 0) atomicAdd(a.db + co, v);
+            if (lane == 0) atomicAdd(a.db + co0 + c, v);
         }
-    } else if (t == 0) {
+    } else if (tid == 0) {
         tc::mbar_wait(bar, phase ^ 1u, a.err, false, CT_WAIT_NS);  // MMAs still in flight
     }
     tc::fence_before();
@@ -434,7 +471,7 @@ cudaError_t launch_lp_conv3_tc(const float* in, int B, int Cin, int H, const flo
                 return e;
             set = true;
         }
-        k_conv3_tc<32><<<grid, CT_NT, smem, st>>>(a);
+        k_conv3_tc<32><<<grid, CT_FWD_THREADS, smem, st>>>(a);
     } else {
         constexpr int smem = conv_fwd_smem<16>();
         static bool set = false;
@@ -443,7 +480,7 @@ cudaError_t launch_lp_conv3_tc(const float* in, int B, int Cin, int H, const flo
                 return e;
             set = true;
         }
-        k_conv3_tc<16><<<grid, CT_NT, smem, st>>>(a);
+        k_conv3_tc<16><<<grid, CT_FWD_THREADS, smem, st>>>(a);
     }
     return cudaGetLastError();
 }
@@ -466,7 +503,7 @@ cudaError_t launch_lp_conv3_wgrad_tc(const float* in, const float* dpre, int B, 
                 return e;
             set = true;
         }
-        k_conv3_wgrad_tc<32><<<grid, CT_NT, smem, st>>>(a);
+        k_conv3_wgrad_tc<32><<<grid, CT_FWD_THREADS, smem, st>>>(a);
     } else {
         static bool set = false;
         if (!set) {
@@ -474,7 +511,7 @@ cudaError_t launch_lp_conv3_wgrad_tc(const float* in, const float* dpre, int B, 
                 return e;
             set = true;
         }
-        k_conv3_wgrad_tc<16><<<grid, CT_NT, smem, st>>>(a);
+        k_conv3_wgrad_tc<16><<<grid, CT_FWD_THREADS, smem, st>>>(a);
     }
     return cudaGetLastError();
 }
