@@ -447,9 +447,10 @@ ParView par_view(Ctx* c, int B) {
 
 // Mask / checkerboard / FFT / band of nb images already on the device.
 // keep_flag: leave the non-finite-input flag as it is (a caller that checks it once
-// after several batches) instead of clearing it first.
+// after several batches) instead of clearing it first.  need_fcut = false: the band only,
+// without the particle's amplitude cuts (FT_amp_expfit).
 int transform_batch(Ctx* c, const float* d_src, int nb, int B, const std::vector<float>& hpar,
-                    int use_mask, int normalize, bool shift, bool keep_flag = false) {
+                    int use_mask, int normalize, bool shift, bool keep_flag = false, bool need_fcut = true) {
     ParView pv = par_view(c, B);
     CK(cudaMemcpyAsync(c->par.p, hpar.data(), sizeof(float) * 8 * B, cudaMemcpyHostToDevice,
                        c->stream));
@@ -462,7 +463,7 @@ int transform_batch(Ctx* c, const float* d_src, int nb, int B, const std::vector
     if (r) return r;
     CKF(cufftExecC2C(h, (cufftComplex*)c->fft.p, (cufftComplex*)c->fft.p, CUFFT_FORWARD));
     launch_post_fft(c->fft.p, nb, c->bd, shift ? pv.sx : nullptr, shift ? pv.sy : nullptr,
-                    c->band.p, c->fcut0.p, c->stream);
+                    c->band.p, need_fcut ? c->fcut0.p : nullptr, c->stream);
     CK(cudaGetLastError());
     return CRYOIM_OK;
 }
@@ -1225,7 +1226,7 @@ int learn_features_dev(Ctx* c, const float* d_img, int nb, const float* ox, cons
     for (int i = 0; i < nb; ++i) { hpar[i] = ox[i]; hpar[nb + i] = oy[i]; }
     int r;
     if ((r = ensure_batch(c, nb))) return r;
-    if ((r = transform_batch(c, d_img, nb, nb, hpar, 1, 0, false, keep_flag))) return r;
+    if ((r = transform_batch(c, d_img, nb, nb, hpar, 1, 0, false, keep_flag, false))) return r;
     launch_lp_features(c->band.p, c->bd, nb, c->lm.feat.p, c->stream);
     CK(cudaGetLastError());
     return CRYOIM_OK;

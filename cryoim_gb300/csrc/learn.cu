@@ -472,6 +472,7 @@ __global__ void __launch_bounds__(256) k_mix_dw(const float* __restrict__ x, con
 // 128-point sums against a twiddle table (NT^2 / 2 operations each, a few per particle
 // and view), products over the NT / 2 + 1 frequencies.
 constexpr int NF = NT / 2 + 1;
+constexpr int DR = 8;  // rows per block step of the real transforms
 
 __device__ __forceinline__ void twiddles(float2* tw) {
     for (int k = threadIdx.x; k < NT; k += blockDim.x) {
@@ -485,21 +486,29 @@ __device__ __forceinline__ void twiddles(float2* tw) {
 // rows in a grid-stride loop
 __global__ void __launch_bounds__(NT) k_rdft(const float* __restrict__ x, long n, float2* __restrict__ X) {
     __shared__ float2 tw[NT];
-    __shared__ float sx[NT];
+    __shared__ float sx[DR][NT];
     twiddles(tw);
-    for (long r = blockIdx.x; r < n; r += gridDim.x) {
+    for (long r0 = (long)blockIdx.x * DR; r0 < n; r0 += (long)gridDim.x * DR) {
         __syncthreads();
-        sx[threadIdx.x] = x[r * NT + threadIdx.x];
+#pragma unroll
+        for (int i = 0; i < DR; ++i) sx[i][threadIdx.x] = r0 + i < n ? x[(r0 + i) * NT + threadIdx.x] : 0.f;
         __syncthreads();
         const int f = threadIdx.x;
         if (f < NF) {
-            float re = 0.f, im = 0.f;
+            float re[DR], im[DR];
+#pragma unroll
+            for (int i = 0; i < DR; ++i) re[i] = im[i] = 0.f;
             for (int t = 0; t < NT; ++t) {
                 const float2 w = tw[(f * t) & (NT - 1)];
-                re = fmaf(sx[t], w.x, re);
-                im = fmaf(-sx[t], w.y, im);
+#pragma unroll
+                for (int i = 0; i < DR; ++i) {
+                    re[i] = fmaf(sx[i][t], w.x, re[i]);
+                    im[i] = fmaf(-sx[i][t], w.y, im[i]);
+                }
             }
-            X[r * NF + f] = make_float2(re, im);
+#pragma unroll
+            for (int i = 0; i < DR; ++i)
+                if (r0 + i < n) X[(r0 + i) * NF + f] = make_float2(re[i], im[i]);
         }
     }
 }
@@ -508,22 +517,35 @@ __global__ void __launch_bounds__(NT) k_rdft(const float* __restrict__ x, long n
 // on f = 0 .. NT/2; beta: x = inverse + beta * x (0 or 1)
 __global__ void __launch_bounds__(NT) k_irdft(const float2* __restrict__ X, long n, float* __restrict__ x) {
     __shared__ float2 tw[NT];
-    __shared__ float2 sX[NF];
+    __shared__ float2 sX[DR][NF];
     twiddles(tw);
     const float inv = 1.0f / (float)NT;
-    for (long r = blockIdx.x; r < n; r += gridDim.x) {
+    for (long r0 = (long)blockIdx.x * DR; r0 < n; r0 += (long)gridDim.x * DR) {
         __syncthreads();
-        if (threadIdx.x < NF) sX[threadIdx.x] = X[r * NF + threadIdx.x];
+        if (threadIdx.x < NF) {
+#pragma unroll
+            for (int i = 0; i < DR; ++i)
+                sX[i][threadIdx.x] = r0 + i < n ? X[(r0 + i) * NF + threadIdx.x] : make_float2(0.f, 0.f);
+        }
         __syncthreads();
         const int t = threadIdx.x;
-        float acc = sX[0].x + ((t & 1) ? -sX[NT / 2].x : sX[NT / 2].x);
-        float a2 = 0.f;
+        float acc[DR], a2[DR];
+#pragma unroll
+        for (int i = 0; i < DR; ++i) {
+            acc[i] = sX[i][0].x + ((t & 1) ? -sX[i][NT / 2].x : sX[i][NT / 2].x);
+            a2[i] = 0.f;
+        }
         for (int f = 1; f < NT / 2; ++f) {
             const float2 w = tw[(f * t) & (NT - 1)];
-            a2 = fmaf(sX[f].x, w.x, a2);
-            a2 = fmaf(-sX[f].y, w.y, a2);
+#pragma unroll
+            for (int i = 0; i < DR; ++i) {
+                a2[i] = fmaf(sX[i][f].x, w.x, a2[i]);
+                a2[i] = fmaf(-sX[i][f].y, w.y, a2[i]);
+            }
         }
-        x[r * NT + t] = (acc + 2.0f * a2) * inv;
+#pragma unroll
+        for (int i = 0; i < DR; ++i)
+            if (r0 + i < n) x[(r0 + i) * NT + t] = (acc[i] + 2.0f * a2[i]) * inv;
     }
 }
 
@@ -747,10 +769,10 @@ cudaError_t launch_lp_head(const float* g, const float* T, int B, int V, float* 
     float2* TT = G + (long)B * CM * NF;
     float2* X = TT + (long)V * CM * NF;
     const int gmax = 152 * 16;
-    k_rdft<<<(int)std::min<long>((long)B * CM, gmax), NT, 0, st>>>(g, (long)B * CM, G);
-    k_rdft<<<(int)std::min<long>((long)V * CM, gmax), NT, 0, st>>>(T, (long)V * CM, TT);
+    k_rdft<<<(int)std::min<long>(((long)B * CM + DR - 1) / DR, gmax), NT, 0, st>>>(g, (long)B * CM, G);
+    k_rdft<<<(int)std::min<long>(((long)V * CM + DR - 1) / DR, gmax), NT, 0, st>>>(T, (long)V * CM, TT);
     k_head_prod<<<grid_for((long)B * V * NF, 256), 256, 0, st>>>(G, TT, B, V, X);
-    k_irdft<<<(int)std::min<long>((long)B * V, gmax), NT, 0, st>>>(X, (long)B * V, sc);
+    k_irdft<<<(int)std::min<long>(((long)B * V + DR - 1) / DR, gmax), NT, 0, st>>>(X, (long)B * V, sc);
     return cudaGetLastError();
 }
 void launch_lp_head_grad(const float* g, const float* T, const float* dsc, int B, int V, float* dg, float* dT,
@@ -762,11 +784,11 @@ void launch_lp_head_grad(const float* g, const float* T, const float* dsc, int B
     float2* dTT = D + (long)B * V * NF;
     float2* dG = dTT + (long)V * CM * NF;
     const int gmax = 152 * 16;
-    k_rdft<<<(int)std::min<long>((long)B * V, gmax), NT, 0, st>>>(dsc, (long)B * V, D);
+    k_rdft<<<(int)std::min<long>(((long)B * V + DR - 1) / DR, gmax), NT, 0, st>>>(dsc, (long)B * V, D);
     k_head_dTT<<<grid_for((long)V * CM * NF, 128), 128, 0, st>>>(D, G, B, V, dTT);
     k_head_dG<<<grid_for((long)B * CM * NF, 128), 128, 0, st>>>(D, TT, B, V, dG);
-    k_irdft<<<(int)std::min<long>((long)V * CM, gmax), NT, 0, st>>>(dTT, (long)V * CM, dT);
-    k_irdft<<<(int)std::min<long>((long)B * CM, gmax), NT, 0, st>>>(dG, (long)B * CM, dg);
+    k_irdft<<<(int)std::min<long>(((long)V * CM + DR - 1) / DR, gmax), NT, 0, st>>>(dTT, (long)V * CM, dT);
+    k_irdft<<<(int)std::min<long>(((long)B * CM + DR - 1) / DR, gmax), NT, 0, st>>>(dG, (long)B * CM, dg);
 }
 void launch_lp_loss(const float* sc, int B, int V, const float* vview, const float* truth, float sv, float ss,
                     float* dsc, float* loss, cudaStream_t st) {

@@ -166,7 +166,7 @@ __global__ void k_post_fft(const float2* __restrict__ fft, Band bd, const float*
     for (int k = threadIdx.x; k < nr; k += blockDim.x) { sfav[k] = 0; sres[k] = 0; snum[k] = 0; }
     __syncthreads();
     const float s = (float)nn;
-    const int span = 2 * R + 1, cnt = (R + 1) * span;
+    const int span = 2 * R + 1, cnt = fcut ? (R + 1) * span : 0;  // no amplitude cut asked: band only
     for (int q = threadIdx.x; q < cnt; q += blockDim.x) {
         int ky = q / span, hx = q % span - R;
         float rad = sqrtf((float)(hx * hx + ky * ky));
@@ -181,7 +181,7 @@ __global__ void k_post_fft(const float2* __restrict__ fft, Band bd, const float*
         }
     }
     __syncthreads();
-    if (threadIdx.x == 0) expfit_finish(sfav, sres, snum, nr, fcut + (long)p * nr);
+    if (fcut && threadIdx.x == 0) expfit_finish(sfav, sres, snum, nr, fcut + (long)p * nr);
     const int W = bd.W;
     const bool shift = (sx != nullptr);
     const float xs = shift ? sx[p] + (float)h : 0.f, ys = shift ? sy[p] + (float)h : 0.f;
