@@ -116,6 +116,26 @@ __global__ void k_prep_images(const float* __restrict__ imgs, int nx,
     if (bad) atomicOr(flag, 1);
 }
 
+// floor(sqrt(v)) and ceil(sqrt(v)) of a non-negative integer, exactly
+__device__ __forceinline__ int isqrt_floor(int v) {
+    int s = (int)sqrtf((float)v);
+    while (s > 0 && s * s > v) --s;
+    while ((s + 1) * (s + 1) <= v) ++s;
+    return s;
+}
+__device__ __forceinline__ int isqrt_ceil(int v) {
+    const int s = isqrt_floor(v);
+    return s * s < v ? s + 1 : s;
+}
+
+// h + l += x with Knuth's TwoSum: the pair holds the running sum to ~2^-48 relative in
+// FP32 arithmetic (GB300's FP64 pipe is far slower than its FP32 pipe)
+__device__ __forceinline__ void two_sum_acc(float& h, float& l, float x) {
+    const float s2 = h + x, bb = s2 - h;
+    l += (h - (s2 - bb)) + (x - bb);
+    h = s2;
+}
+
 // FT_amp_expfit.f90:27-46: per-ring means, log, 2x2 least squares, Fcut.
 __device__ void expfit_finish(const double* sfav, const double* sres, const int* snum, int nr,
                               float* out) {
@@ -163,25 +183,45 @@ __global__ void k_post_fft(const float2* __restrict__ fft, Band bd, const float*
     const int p = blockIdx.x;
     const long nn = (long)nx * nx;
     const float2* f = fft + p * nn;
-    for (int k = threadIdx.x; k < nr; k += blockDim.x) { sfav[k] = 0; sres[k] = 0; snum[k] = 0; }
-    __syncthreads();
     const float s = (float)nn;
-    const int span = 2 * R + 1, cnt = fcut ? (R + 1) * span : 0;  // no amplitude cut asked: band only
-    for (int q = threadIdx.x; q < cnt; q += blockDim.x) {
-        int ky = q / span, hx = q % span - R;
-        float rad = sqrtf((float)(hx * hx + ky * ky));
-        int ir = (int)(rad + 0.5f);
-        if (ir >= bd.min_r && ir <= R) {
-            float2 v = f[(long)(ky + h) * nx + (hx + h)];
-            float a = v.x / s, b = -(v.y / s);
-            float amp = sqrtf(a * a + b * b);
-            atomicAdd(&sfav[ir - bd.min_r], (double)amp);
-            atomicAdd(&sres[ir - bd.min_r], (double)rad);
-            atomicAdd(&snum[ir - bd.min_r], 1);
+    if (fcut) {  // (no amplitude cut asked: the band only)
+        // ring sums over the ky >= 0 half plane, one warp per ring as in k_tmpl_fcut
+        const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
+        for (int ir = bd.min_r + warp; ir <= R; ir += nw) {
+            float fh = 0.f, fl = 0.f, rh = 0.f, rl = 0.f;
+            int n = 0;
+            const int lo = ir * ir - ir + 1, hi = ir * ir + ir;
+            for (int ky = lane; ky <= ir; ky += 32) {
+                const int k2 = ky * ky;
+                if (k2 > hi) continue;
+                const int hmax = isqrt_floor(hi - k2);
+                const int hmin = lo - k2 <= 0 ? 0 : isqrt_ceil(lo - k2);
+                for (int hx = hmin; hx <= hmax; ++hx) {
+                    const float rad = sqrtf((float)(hx * hx + k2));
+                    for (int sgn = (hx == 0 ? 1 : -1); sgn <= 1; sgn += 2) {
+                        const float2 v = f[(long)(ky + h) * nx + (sgn * hx + h)];
+                        const float a = v.x / s, b = -(v.y / s);
+                        two_sum_acc(fh, fl, sqrtf(a * a + b * b));
+                        two_sum_acc(rh, rl, rad);
+                        ++n;
+                    }
+                }
+            }
+            double fa = (double)fh + (double)fl, rs = (double)rh + (double)rl;
+            for (int o = 16; o > 0; o >>= 1) {
+                fa += __shfl_xor_sync(0xffffffffu, fa, o);
+                rs += __shfl_xor_sync(0xffffffffu, rs, o);
+                n += __shfl_xor_sync(0xffffffffu, n, o);
+            }
+            if (lane == 0) {
+                sfav[ir - bd.min_r] = fa;
+                sres[ir - bd.min_r] = rs;
+                snum[ir - bd.min_r] = n;
+            }
         }
+        __syncthreads();
+        if (threadIdx.x == 0) expfit_finish(sfav, sres, snum, nr, fcut + (long)p * nr);
     }
-    __syncthreads();
-    if (fcut && threadIdx.x == 0) expfit_finish(sfav, sres, snum, nr, fcut + (long)p * nr);
     const int W = bd.W;
     const bool shift = (sx != nullptr);
     const float xs = shift ? sx[p] + (float)h : 0.f, ys = shift ? sy[p] + (float)h : 0.f;
@@ -228,18 +268,6 @@ __global__ void k_ctf_band(Band bd, const float* __restrict__ dfs, float apix, f
     ctf[(long)p * W * W + q] = -(sq * sinf(phase) + ampwg * cosf(phase));
 }
 
-// floor(sqrt(v)) and ceil(sqrt(v)) of a non-negative integer, exactly
-__device__ __forceinline__ int isqrt_floor(int v) {
-    int s = (int)sqrtf((float)v);
-    while (s > 0 && s * s > v) --s;
-    while ((s + 1) * (s + 1) <= v) ++s;
-    return s;
-}
-__device__ __forceinline__ int isqrt_ceil(int v) {
-    const int s = isqrt_floor(v);
-    return s * s < v ? s + 1 : s;
-}
-
 // Fcut of (template x CTF): cal_crosslin_PR_omega.f90:34-38, hoisted per particle.
 // Template amplitude cuts under each particle's CTF (FT_amp_expfit.f90 on template x
 // CTF over the ky >= 0 half plane): one block per (template, particle), one warp per
@@ -259,7 +287,8 @@ __global__ void k_tmpl_fcut(const float2* __restrict__ tband, int T, const float
     const float2* tb = tband + (long)i * W * W;
     const float* cb = ctf + (long)p * W * W;
     for (int ir = bd.min_r + warp; ir <= R; ir += nw) {
-        double fa = 0.0, rs = 0.0;
+        // per lane an FP32 pair (two_sum_acc), to FP64 once per lane
+        float fh = 0.f, fl = 0.f, rh = 0.f, rl = 0.f;
         int n = 0;
         const int lo = ir * ir - ir + 1, hi = ir * ir + ir;
         for (int ky = lane; ky <= ir; ky += 32) {
@@ -274,12 +303,13 @@ __global__ void k_tmpl_fcut(const float2* __restrict__ tband, int T, const float
                     const float c = cb[b];
                     const float2 t = tb[b];
                     const float a2 = t.x * c, b2 = t.y * c;
-                    fa += (double)sqrtf(a2 * a2 + b2 * b2);
-                    rs += (double)rad;
+                    two_sum_acc(fh, fl, sqrtf(a2 * a2 + b2 * b2));
+                    two_sum_acc(rh, rl, rad);
                     ++n;
                 }
             }
         }
+        double fa = (double)fh + (double)fl, rs = (double)rh + (double)rl;
         for (int o = 16; o > 0; o >>= 1) {
             fa += __shfl_xor_sync(0xffffffffu, fa, o);
             rs += __shfl_xor_sync(0xffffffffu, rs, o);
