@@ -24,6 +24,13 @@ namespace {
 
 inline int cdiv(long a, int b) { return (int)((a + b - 1) / b); }
 
+// h + l += x with Knuth's TwoSum: the pair holds the running sum to ~2^-48 relative
+__device__ __forceinline__ void two_sum_acc(float& h, float& l, float x) {
+    const float s2 = h + x, bb = s2 - h;
+    l += (h - (s2 - bb)) + (x - bb);
+    h = s2;
+}
+
 __device__ double bsum(double v, double* sh) {
     for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
     const int w = threadIdx.x >> 5, l = threadIdx.x & 31, nw = (blockDim.x + 31) >> 5;
@@ -100,16 +107,19 @@ __global__ void k_local_box(const float* __restrict__ imgs, int nx0, const int* 
     const float* a = imgs + (long)blockIdx.x * nn0;
     float avg = 0.f, nd = 1.f;
     if (normalize) {
-        double s = 0;
-        for (long i = threadIdx.x; i < nn0; i += blockDim.x) s += (double)a[i];
-        s = bsum(s, sh);
+        // per thread an FP32 TwoSum pair (exact to ~2^-48), FP64 across the block: GB300's
+        // FP64 pipe is far slower than its FP32 pipe
+        float h = 0.f, l = 0.f;
+        for (long i = threadIdx.x; i < nn0; i += blockDim.x) two_sum_acc(h, l, a[i]);
+        const double s = bsum((double)h + (double)l, sh);
         avg = (float)s / (float)nn0;
-        double s2 = 0;
+        h = 0.f;
+        l = 0.f;
         for (long i = threadIdx.x; i < nn0; i += blockDim.x) {
             const float d = a[i] - avg;
-            s2 += (double)(d * d);
+            two_sum_acc(h, l, d * d);
         }
-        s2 = bsum(s2, sh);
+        const double s2 = bsum((double)h + (double)l, sh);
         nd = sqrtf((float)s2 / (float)nn0);
     }
     const int ix = hk[2 * blockIdx.x], iy = hk[2 * blockIdx.x + 1];

@@ -29,6 +29,13 @@ __device__ __forceinline__ void kahan_add(float& s, float& c, float x) {
     c = (t - s) - y;
     s = t;
 }
+// h + l += x with Knuth's TwoSum: the pair holds the running sum to ~2^-48 relative in
+// FP32 arithmetic (GB300's FP64 pipe is far slower than its FP32 pipe)
+__device__ __forceinline__ void two_sum_acc(float& h, float& l, float x) {
+    const float s2 = h + x, bb = s2 - h;
+    l += (h - (s2 - bb)) + (x - bb);
+    h = s2;
+}
 
 __device__ __forceinline__ float bilerp(float ax, float ay, float v00, float v10, float v01,
                                         float v11) {
@@ -242,6 +249,7 @@ __global__ void __launch_bounds__(512) k_pr_single(PrSingleArgs a, Consts K) {
     const float twopi = __fmul_rn(2.0f, K.pi);
     double p1 = 0.0, p2 = 0.0;
     float f1 = 0.f, f2 = 0.f, k1 = 0.f, k2 = 0.f;
+    float h1 = 0.f, l1 = 0.f, h2 = 0.f, l2 = 0.f;  // unshifted form: TwoSum pairs
     if (SHIFTED)
         for (int q = threadIdx.x; q < nr; q += blockDim.x) sfc[0][q] = fc0[q];
     for (int i = 0; i < a.T; ++i) {
@@ -320,8 +328,8 @@ __global__ void __launch_bounds__(512) k_pr_single(PrSingleArgs a, Consts K) {
                     float d = fabsf(ph2 - ph1);
                     d = fminf(d, K.tpi - d);
                     float w = 0.5f * (amp1 + amp2);
-                    p1 += (double)(d * w);
-                    p2 += (double)w;
+                    two_sum_acc(h1, l1, d * w);
+                    two_sum_acc(h2, l2, w);
                 }
             }
         }
@@ -329,6 +337,9 @@ __global__ void __launch_bounds__(512) k_pr_single(PrSingleArgs a, Consts K) {
     if (SHIFTED) {
         p1 = (double)f1;
         p2 = (double)f2;
+    } else {
+        p1 = (double)h1 + (double)l1;
+        p2 = (double)h2 + (double)l2;
     }
     for (int o = 16; o > 0; o >>= 1) {
         p1 += __shfl_xor_sync(0xffffffffu, p1, o);
