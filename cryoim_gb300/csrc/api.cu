@@ -1892,8 +1892,8 @@ int contract_impl(Ctx* c, const float* imgs, bool on_device, cryoim_particle* pa
             }
             CK(cudaMemcpyAsync(L->kcand.p, hcand.data(), sizeof(float) * nb * k * 5, cudaMemcpyHostToDevice,
                                L->stream));
-            launch_cc_fp64(L->mapcube.p, L->band.p, ctfp, L->bd, L->csamples.p, L->cS, L->kcand.p, k, nb, L->kpart.p,
-                           L->kcc64.p, L->stream);
+            launch_cc_fp64(L->mapcube.p, L->band.p, ctfp, L->bd, L->csamples.p, L->cS, L->kcand.p, k, nb, L->pnorm.p,
+                           L->kpart.p, L->kcc64.p, L->stream);
             // Phase-residual rescoring at the particle's own origin (ort_globesearch.f90 scores
             // every view at particle(i)%x, %y) over each selected orientation and its grid
             // neighbours within nbr steps (all of them, or, with nbr_best = m, only those of

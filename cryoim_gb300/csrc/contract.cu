@@ -402,17 +402,19 @@ __global__ void k_cc_fp64(const float2* __restrict__ cube, const float2* __restr
     __syncthreads();
     const float2* b = band + (long)p * W * W;
     const float* cb = ctf ? ctf + (long)p * W * W : nullptr;
-    double dot = 0, na = 0, nb = 0;
+    double dot = 0, nb = 0;  // the particle's norm is the same for every candidate: k_particle_norm
     const int i0 = (int)((long)S * sp / gridDim.z), i1 = (int)((long)S * (sp + 1) / gridDim.z);
     for (int i = i0 + threadIdx.x; i < i1; i += blockDim.x) {
         const int2 hk = samples[i];
         const double x = rot[0] * hk.x + rot[1] * hk.y, y = rot[3] * hk.x + rot[4] * hk.y,
                      z = rot[6] * hk.x + rot[7] * hk.y;
-        const double fx = floor(x), fy = floor(y), fz = floor(z);
+        // the cube holds FP32 values: its trilinear blend runs in FP32 at the FP64-rotated
+        // coordinates rounded once to FP32 (|x| <= maxR + 1: within 2^-17 px), the products
+        // and sums below in FP64
+        const float xf = (float)x, yf = (float)y, zf = (float)z;
+        const float fx = floorf(xf), fy = floorf(yf), fz = floorf(zf);
         const int ix = (int)fx + off, iy = (int)fy + off, iz = (int)fz + off;
-        // the cube holds FP32 values: its trilinear blend runs in FP32 (exact-geometry
-        // weights rounded once), the products and sums below in FP64
-        const float ax = (float)(x - fx), ay = (float)(y - fy), az = (float)(z - fz);
+        const float ax = xf - fx, ay = yf - fy, az = zf - fz;
         const float2* cb0 = cube + ((long)iz * C + iy) * C + ix;
         float2 r0, r1;
         {
@@ -434,30 +436,31 @@ __global__ void k_cc_fp64(const float2* __restrict__ cube, const float2* __restr
         const double cv = cb ? (double)cb[q] : 1.0;
         const double pr = a2 * cv, pi = -b2 * cv;
         dot += pr * sr + pi * si;
-        na += pr * pr + pi * pi;
         nb += sr * sr + si * si;
     }
     dot = block_sum_double(dot, sh);
-    na = block_sum_double(na, sh);
     nb = block_sum_double(nb, sh);
     if (threadIdx.x == 0) {
         double* o = part + (((long)p * k + c) * gridDim.z + sp) * 3;
         o[0] = dot;
-        o[1] = na;
+        o[1] = 0.0;
         o[2] = nb;
     }
 }
 
 // CC of each (particle, candidate) from its chunks' sums, in chunk order.
-__global__ void k_cc_fp64_finish(const double* __restrict__ part, int n, int ns, double* __restrict__ out) {
+// CC = dot / sqrt(|P|^2 |S|^2): the chunks' dot and section norms, the particle's FP64 norm
+// (sum over the samples of |CTF P|^2, k_particle_norm; the origin phase keeps it)
+__global__ void k_cc_fp64_finish(const double* __restrict__ part, int n, int ns, const double* __restrict__ pnorm,
+                                 int k, double* __restrict__ out) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
-    double dot = 0, na = 0, nb = 0;
+    double dot = 0, nb = 0;
     for (int s = 0; s < ns; ++s) {
         dot += part[((long)i * ns + s) * 3];
-        na += part[((long)i * ns + s) * 3 + 1];
         nb += part[((long)i * ns + s) * 3 + 2];
     }
+    const double na = pnorm[i / k];
     out[i] = (na > 0 && nb > 0) ? dot / sqrt(na * nb) : 0.0;
 }
 
@@ -722,11 +725,12 @@ void launch_select_distinct(float* topv, const int* topi, int O, const int2* seg
 long cc_fp64_scratch(int k, int B) { return (long)k * B * CC_SPLIT * 3; }
 
 void launch_cc_fp64(const float2* cube, const float2* band, const float* ctf, Band bd, const int2* samples,
-                    int S, const float* cand, int k, int B, double* scratch, double* out, cudaStream_t st) {
+                    int S, const float* cand, int k, int B, const double* pnorm, double* scratch, double* out,
+                    cudaStream_t st) {
     dim3 g(k, B, CC_SPLIT);
     const size_t sm = sizeof(double2) * (3 * bd.max_r + 2);
     k_cc_fp64<<<g, 256, sm, st>>>(cube, band, ctf, bd, samples, S, cand, k, scratch);
-    k_cc_fp64_finish<<<(k * B + 127) / 128, 128, 0, st>>>(scratch, k * B, CC_SPLIT, out);
+    k_cc_fp64_finish<<<(k * B + 127) / 128, 128, 0, st>>>(scratch, k * B, CC_SPLIT, pnorm, k, out);
 }
 
 }  // namespace cryoim

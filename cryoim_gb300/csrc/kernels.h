@@ -191,7 +191,8 @@ void launch_select_topk(const float* topv, const int* topi, int O, int ntiles, i
 // scratch: cc_fp64_scratch(k, B) doubles
 long cc_fp64_scratch(int k, int B);
 void launch_cc_fp64(const float2* cube, const float2* band, const float* ctf, Band bd, const int2* samples,
-                    int S, const float* cand, int k, int B, double* scratch, double* out, cudaStream_t st);
+                    int S, const float* cand, int k, int B, const double* pnorm, double* scratch, double* out,
+                    cudaStream_t st);
 
 // ---- learned orientation proposer (learn.cu) ----
 constexpr int LP_NR = 64, LP_NT = 128;   // polar feature: radii over [minR, maxR] x angles over [0, 180)
