@@ -335,6 +335,7 @@ struct Ctx {
     DBuf<float> corigins, topv, kcc, kcand;
     DBuf<int> topi, gerr, kor, korig;
     DBuf<double> pnorm, kcc64;
+    DBuf<double2> pcband;  // per particle of a pass: CTF x (a, b) per band sample, FP64
     int n_origin = 0;
     float orig_max = -1.0f, orig_step = -1.0f;
     DBuf<float> tilev, xcand, xpr;
@@ -1670,7 +1671,8 @@ int contract_impl(Ctx* c, const float* imgs, bool on_device, cryoim_particle* pa
             return r;
         if ((r = L->topv.ensure((size_t)arows * O * ntiles)) || (r = L->topi.ensure((size_t)arows * O * ntiles)))
             return r;
-        if ((r = L->gerr.ensure(1)) || (r = L->pnorm.ensure(PB)) || (r = L->kor.ensure((size_t)PB * k)) ||
+        if ((r = L->gerr.ensure(1)) || (r = L->pnorm.ensure(PB)) || (r = L->pcband.ensure((size_t)PB * L->cS)) ||
+            (r = L->kor.ensure((size_t)PB * k)) ||
             (r = L->korig.ensure((size_t)PB * k)) || (r = L->kcc.ensure((size_t)PB * k)) ||
             (r = L->kcand.ensure((size_t)PB * k * 5)) || (r = L->kcc64.ensure((size_t)PB * k)) ||
             (r = L->kpart.ensure((size_t)cc_fp64_scratch(k, PB))))
@@ -1735,7 +1737,8 @@ int contract_impl(Ctx* c, const float* imgs, bool on_device, cryoim_particle* pa
                     tfs = (long)T * L->bd.nr;
                 }
             }
-            launch_particle_norm(L->band.p, ctfp, L->bd, L->csamples.p, L->cS, nb, L->pnorm.p, L->stream);
+            launch_particle_norm(L->band.p, ctfp, L->bd, L->csamples.p, L->cS, nb, L->pnorm.p, L->stream,
+                                 L->pcband.p);
             // operand A rows (particle, origin) of particles [s0, s0 + ns) at row (s0 - a0) O
             auto build_rows = [&](int s0, int ns, int a0) {
                 const float2* bb = L->band.p + (long)s0 * w2;
@@ -1892,7 +1895,7 @@ int contract_impl(Ctx* c, const float* imgs, bool on_device, cryoim_particle* pa
             }
             CK(cudaMemcpyAsync(L->kcand.p, hcand.data(), sizeof(float) * nb * k * 5, cudaMemcpyHostToDevice,
                                L->stream));
-            launch_cc_fp64(L->mapcube.p, L->band.p, ctfp, L->bd, L->csamples.p, L->cS, L->kcand.p, k, nb, L->pnorm.p,
+            launch_cc_fp64(L->mapcube.p, L->pcband.p, L->bd, L->csamples.p, L->cS, L->kcand.p, k, nb, L->pnorm.p,
                            L->kpart.p, L->kcc64.p, L->stream);
             // Phase-residual rescoring at the particle's own origin (ort_globesearch.f90 scores
             // every view at particle(i)%x, %y) over each selected orientation and its grid

@@ -140,9 +140,11 @@ __global__ void __launch_bounds__(512) k_slice_bf16_local(cudaTextureObject_t cu
     }
 }
 
-// FP64 sum over samples of |CTF * P|^2 per particle (the origin shift keeps it).
+// FP64 sum over samples of |CTF * P|^2 per particle (the origin shift keeps it); with
+// pc, also the samples CTF * (a, b) themselves in FP64, in sample order.
 __global__ void k_particle_norm(const float2* __restrict__ band, const float* __restrict__ ctf, Band bd,
-                                const int2* __restrict__ samples, int S, double* __restrict__ norm) {
+                                const int2* __restrict__ samples, int S, double* __restrict__ norm,
+                                double2* __restrict__ pc) {
     __shared__ double sh[32];
     const int p = blockIdx.x, W = bd.W, R = bd.max_r;
     const float2* b = band + (long)p * W * W;
@@ -154,6 +156,7 @@ __global__ void k_particle_norm(const float2* __restrict__ band, const float* __
         const double cv = c ? (double)c[q] : 1.0;
         const double re = b[q].x * cv, im = b[q].y * cv;
         acc += re * re + im * im;
+        if (pc) pc[(long)p * S + i] = make_double2(re, im);
     }
     acc = block_sum_double(acc, sh);
     if (threadIdx.x == 0) norm[p] = acc;
@@ -372,13 +375,13 @@ __global__ void k_select_distinct(float* __restrict__ v0, const int* __restrict_
 // per-hx and per-ky phasors in double once and multiplies them per sample.
 constexpr int CC_SPLIT = 4;
 
-__global__ void k_cc_fp64(const float2* __restrict__ cube, const float2* __restrict__ band,
-                          const float* __restrict__ ctf, Band bd, const int2* __restrict__ samples, int S,
-                          const float* __restrict__ cand, int k, double* __restrict__ part) {
+__global__ void k_cc_fp64(const float2* __restrict__ cube, const double2* __restrict__ pcband, Band bd,
+                          const int2* __restrict__ samples, int S, const float* __restrict__ cand, int k,
+                          double* __restrict__ part) {
     extern __shared__ double2 ctab[];  // [R + 1] per hx, then [2R + 1] per ky
     __shared__ double sh[32];
     __shared__ double rot[9];
-    const int c = blockIdx.x, p = blockIdx.y, sp = blockIdx.z, W = bd.W, R = bd.max_r, C = 2 * R + 3, off = R + 1;
+    const int c = blockIdx.x, p = blockIdx.y, sp = blockIdx.z, R = bd.max_r, C = 2 * R + 3, off = R + 1;
     const float* cd = cand + ((long)p * k + c) * 5;
     if (threadIdx.x == 0) {
         const double d2r = 3.14159265358979323846 / 180.0;
@@ -400,8 +403,7 @@ __global__ void k_cc_fp64(const float2* __restrict__ cube, const float2* __restr
         ctab[i] = make_double2(cs, sn);
     }
     __syncthreads();
-    const float2* b = band + (long)p * W * W;
-    const float* cb = ctf ? ctf + (long)p * W * W : nullptr;
+    const double2* pcb = pcband + (long)p * S;  // CTF x (a, b) per sample, FP64 (k_particle_norm)
     double dot = 0, nb = 0;  // the particle's norm is the same for every candidate: k_particle_norm
     const int i0 = (int)((long)S * sp / gridDim.z), i1 = (int)((long)S * (sp + 1) / gridDim.z);
     for (int i = i0 + threadIdx.x; i < i1; i += blockDim.x) {
@@ -428,13 +430,12 @@ __global__ void k_cc_fp64(const float2* __restrict__ cube, const float2* __restr
             r1 = make_float2(fmaf(ay, a3.x - a2.x, a2.x), fmaf(ay, a3.y - a2.y, a2.y));
         }
         const double sr = (double)fmaf(az, r1.x - r0.x, r0.x), si = (double)fmaf(az, r1.y - r0.y, r0.y);
-        const int q = (hk.y + R) * W + (hk.x + R);
         // cos/sin of tpn (sx hx + sy ky) from the two tabulated phasors
         const double2 ex = tx[hk.x], ey = ty[hk.y + R];
         const double cs = ex.x * ey.x - ex.y * ey.y, sn = ex.y * ey.x + ex.x * ey.y;
-        const double a2 = b[q].x * cs + b[q].y * sn, b2 = -b[q].x * sn + b[q].y * cs;
-        const double cv = cb ? (double)cb[q] : 1.0;
-        const double pr = a2 * cv, pi = -b2 * cv;
+        // the origin-shifted particle sample (img2d_FT_centshift.f90, b = -Im convention)
+        const double2 pc = pcb[i];
+        const double pr = pc.x * cs + pc.y * sn, pi = pc.x * sn - pc.y * cs;
         dot += pr * sr + pi * si;
         nb += sr * sr + si * si;
     }
@@ -696,8 +697,8 @@ cudaError_t launch_slice_bf16_local(cudaTextureObject_t cube, int R, const int2*
 }
 
 void launch_particle_norm(const float2* band, const float* ctf, Band bd, const int2* samples, int S,
-                          int B, double* norm, cudaStream_t st) {
-    k_particle_norm<<<B, 256, 0, st>>>(band, ctf, bd, samples, S, norm);
+                          int B, double* norm, cudaStream_t st, double2* pc) {
+    k_particle_norm<<<B, 256, 0, st>>>(band, ctf, bd, samples, S, norm, pc);
 }
 
 void launch_build_a(const float2* band, const float* ctf, Band bd, const int2* samples, int S, int Kpad,
@@ -724,12 +725,12 @@ void launch_select_distinct(float* topv, const int* topi, int O, const int2* seg
 
 long cc_fp64_scratch(int k, int B) { return (long)k * B * CC_SPLIT * 3; }
 
-void launch_cc_fp64(const float2* cube, const float2* band, const float* ctf, Band bd, const int2* samples,
-                    int S, const float* cand, int k, int B, const double* pnorm, double* scratch, double* out,
+void launch_cc_fp64(const float2* cube, const double2* pcband, Band bd, const int2* samples, int S,
+                    const float* cand, int k, int B, const double* pnorm, double* scratch, double* out,
                     cudaStream_t st) {
     dim3 g(k, B, CC_SPLIT);
     const size_t sm = sizeof(double2) * (3 * bd.max_r + 2);
-    k_cc_fp64<<<g, 256, sm, st>>>(cube, band, ctf, bd, samples, S, cand, k, scratch);
+    k_cc_fp64<<<g, 256, sm, st>>>(cube, pcband, bd, samples, S, cand, k, scratch);
     k_cc_fp64_finish<<<(k * B + 127) / 128, 128, 0, st>>>(scratch, k * B, CC_SPLIT, pnorm, k, out);
 }
 

@@ -178,7 +178,7 @@ cudaError_t launch_slice_bf16(cudaTextureObject_t cube, int R, const int2* sampl
 cudaError_t launch_slice_bf16_local(cudaTextureObject_t cube, int R, const int2* samples, int S, int Kpad,
                                     const float* centre, int m, float step, long count, void* B, cudaStream_t st);
 void launch_particle_norm(const float2* band, const float* ctf, Band bd, const int2* samples, int S,
-                          int B, double* norm, cudaStream_t st);
+                          int B, double* norm, cudaStream_t st, double2* pc = nullptr);
 // Rows (p, o) of A, p < B, o < O; origins: O x 2 (x, y) pixels.
 void launch_build_a(const float2* band, const float* ctf, Band bd, const int2* samples, int S, int Kpad,
                     const float* origins, int O, const double* norm, int B, void* A, cudaStream_t st);
@@ -190,8 +190,10 @@ void launch_select_topk(const float* topv, const int* topi, int O, int ntiles, i
 // cand: B x k x (theta, phi, omega, x, y); out: B x k FP64 cross-correlations
 // scratch: cc_fp64_scratch(k, B) doubles
 long cc_fp64_scratch(int k, int B);
-void launch_cc_fp64(const float2* cube, const float2* band, const float* ctf, Band bd, const int2* samples,
-                    int S, const float* cand, int k, int B, const double* pnorm, double* scratch, double* out,
+// FP64 CC of k candidates per particle; pcband: each particle's CTF x (a, b) per sample in
+// FP64 and pnorm its FP64 norm (launch_particle_norm)
+void launch_cc_fp64(const float2* cube, const double2* pcband, Band bd, const int2* samples, int S,
+                    const float* cand, int k, int B, const double* pnorm, double* scratch, double* out,
                     cudaStream_t st);
 
 // ---- learned orientation proposer (learn.cu) ----
