@@ -374,22 +374,26 @@ __global__ void k_refine_candidates(float* __restrict__ state, int B, float dang
     }
 }
 
+// One block per candidate row: its Euler matrix and the T template matrices once in shared
+// memory, then crosslin_pair for every (template, operator).
 __global__ void k_refine_alpha(const float* __restrict__ cand, long ncand_rows,
                                const float* __restrict__ tort, int T, const float* __restrict__ ops,
                                float d2r, float r2d, float2* __restrict__ alpha) {
-    long q = (long)blockIdx.x * blockDim.x + threadIdx.x;
-    long total = ncand_rows * T * 60;
-    if (q >= total) return;
-    int j = (int)(q % 60);
-    int i = (int)((q / 60) % T);
-    long pc = q / (60L * T);  // p*11 + c
+    extern __shared__ float em[];  // [9] candidate, then [T][9] templates
+    const long pc = blockIdx.x;    // p * ncand + c
+    if (pc >= ncand_rows) return;
     const float* c = cand + pc * 5;
-    float e1[9], e2[9];
-    euler_mat(c[0], c[1], c[2], d2r, e1);
-    euler_mat(tort[i * 3], tort[i * 3 + 1], tort[i * 3 + 2], d2r, e2);
-    float a1, a2;
-    crosslin_pair(e1, e2, ops + j * 9, r2d, &a1, &a2);
-    alpha[q] = make_float2(a1, a2);
+    if (threadIdx.x == 0) euler_mat(c[0], c[1], c[2], d2r, em);
+    for (int i = threadIdx.x; i < T; i += blockDim.x)
+        euler_mat(tort[i * 3], tort[i * 3 + 1], tort[i * 3 + 2], d2r, em + 9 + 9 * i);
+    __syncthreads();
+    float2* out = alpha + pc * T * 60;
+    for (int q = threadIdx.x; q < T * 60; q += blockDim.x) {
+        const int i = q / 60, j = q - 60 * i;
+        float a1, a2;
+        crosslin_pair(em, em + 9 + 9 * i, ops + j * 9, r2d, &a1, &a2);
+        out[q] = make_float2(a1, a2);
+    }
 }
 
 // ort_refinement.f90:85-91: first minimum of the 11 scores.
@@ -598,10 +602,11 @@ void launch_refine_candidates(float* state, int B, float dang, float dtran, cons
 
 void launch_refine_alpha(const float* cand, int B, const float* tort, int T, const float* ops,
                          float2* alpha, cudaStream_t st, int ncand) {
-    long rows = (long)B * ncand;
-    long total = rows * T * 60;
+    const long rows = (long)B * ncand;
+    const size_t sm = sizeof(float) * 9 * (T + 1);
+    if (sm > 48 * 1024) cudaFuncSetAttribute(k_refine_alpha, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
     HostAngles a = angles();
-    k_refine_alpha<<<cdiv(total, 128), 128, 0, st>>>(cand, rows, tort, T, ops, a.d2r, a.r2d, alpha);
+    k_refine_alpha<<<(unsigned)rows, 256, sm, st>>>(cand, rows, tort, T, ops, a.d2r, a.r2d, alpha);
 }
 
 void launch_refine_select(const float* cand, const float* pr, int B, float* state,
