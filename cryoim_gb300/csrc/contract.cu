@@ -666,6 +666,7 @@ void free_cube_texture(cudaArray_t arr, cudaTextureObject_t tex) {
     if (arr) cudaFreeArray(arr);
 }
 
+constexpr int SLICE_THREADS = 256;  // threads per section row
 cudaError_t launch_slice_bf16(cudaTextureObject_t cube, int R, const int2* samples, int S, int Kpad,
                               const float* views, int nom, float step, long n0, long count, void* B,
                               cudaStream_t st) {
@@ -674,13 +675,16 @@ cudaError_t launch_slice_bf16(cudaTextureObject_t cube, int R, const int2* sampl
     if (e != cudaSuccess) return e;
     for (long c0 = 0; c0 < count; c0 += 65535) {
         long nb = count - c0 < 65535 ? count - c0 : 65535;
-        k_slice_bf16<<<(unsigned)nb, 512, sm, st>>>(cube, R, samples, S, Kpad, views, nom, step,
+        k_slice_bf16<<<(unsigned)nb, SLICE_THREADS, sm, st>>>(cube, R, samples, S, Kpad, views, nom, step,
                                                    host_angles().deg2rad, n0 + c0,
                                                    (__nv_bfloat162*)B + c0 * (Kpad / 2));
     }
     return cudaGetLastError();
 }
 
+// a local grid's rows are short (a few thousand samples at sub-particle sizes): fewer
+// threads per row keep the per-row norm reduction from dominating
+constexpr int LOCAL_SLICE_THREADS = 64;
 cudaError_t launch_slice_bf16_local(cudaTextureObject_t cube, int R, const int2* samples, int S, int Kpad,
                                     const float* centre, int m, float step, long count, void* B, cudaStream_t st) {
     size_t sm = (size_t)S * sizeof(float2);
@@ -689,7 +693,7 @@ cudaError_t launch_slice_bf16_local(cudaTextureObject_t cube, int R, const int2*
     if (e != cudaSuccess) return e;
     for (long c0 = 0; c0 < count; c0 += 65535) {
         long nb = count - c0 < 65535 ? count - c0 : 65535;
-        k_slice_bf16_local<<<(unsigned)nb, 512, sm, st>>>(cube, R, samples, S, Kpad, centre, m, step,
+        k_slice_bf16_local<<<(unsigned)nb, LOCAL_SLICE_THREADS, sm, st>>>(cube, R, samples, S, Kpad, centre, m, step,
                                                          host_angles().deg2rad, c0,
                                                          (__nv_bfloat162*)B + c0 * (Kpad / 2));
     }
