@@ -100,10 +100,12 @@ struct PrSingleArgs {
     Band bd;
     float* pr;               // [B][ncand]
     int ncand = 11;          // 11 for the refinement step (ort_cent_11.f90)
-    const float2* sband = nullptr;  // [B][W*W] band shifted to the candidates' common origin, or nullptr
+    // rescoring by groups (launch_pr_rescore_groups) only:
+    const float2* sband = nullptr;  // [B][W*W] band shifted to the candidates' common origin
     const int* ncount = nullptr;    // [B] candidates in use (later slots are skipped), or nullptr
-    const float2* tbandc = nullptr; // with sband: [B][T][W*W] templates x CTF (launch_tband_ctf), or nullptr
+    const float2* tbandc = nullptr; // [B][T][W*W] templates x CTF (launch_tband_ctf), or nullptr
 };
+// cal_crosslin_PR for each candidate, its origin shift applied to every tap (k_pr_single)
 cudaError_t launch_pr_single(const PrSingleArgs& a, int B, cudaStream_t st);
 // rescoring by groups of candidates sharing a view: groups[g] = (particle, first
 // candidate slot, count <= pr_rescore_group_size(), 0); requires sband

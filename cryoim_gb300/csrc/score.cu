@@ -224,15 +224,10 @@ __global__ void __launch_bounds__(768, 1) k_pr_omega(PrOmegaArgs a, int nomp, Co
 // cal_crosslin_PR.f90:2-71 for the 11 candidates of each particle; the candidate
 // origin shift (img2d_FT_centshift.f90) is applied to each bilinear tap, which is the
 // same per-pixel arithmetic as shifting the whole transform first.
-// SHIFTED (the contraction's rescoring: every candidate at the particle's origin, band
-// pre-shifted) also takes the exhaustive scorer's arithmetic for the phase difference
-// (angle_between) and float Kahan sums per thread, so its values match k_pr_omega's.
-template <bool SHIFTED>
 __global__ void __launch_bounds__(512) k_pr_single(PrSingleArgs a, Consts K) {
     __shared__ double sh[2][32];
     __shared__ float sline[4][60];  // cos, sin of the particle line; cos, sin of the template line
     __shared__ int svalid[60];
-    __shared__ float sfc[2][256];   // SHIFTED: the particle's and the template's amplitude cuts
     const Band bd = a.bd;
     const int W = bd.W, nr = bd.nr, minR = bd.min_r, nx = bd.nx;
     const int c = blockIdx.x, p = blockIdx.y;
@@ -242,22 +237,15 @@ __global__ void __launch_bounds__(512) k_pr_single(PrSingleArgs a, Consts K) {
     const float xs = __fadd_rn(cd[3], nxh), ys = __fadd_rn(cd[4], nxh);
     const int offW = bd.off * W + bd.off;
     const float2* pb = a.band + (long)p * W * W;
-    const float2* sb = SHIFTED ? a.sband + (long)p * W * W : nullptr;
     const float* ctfp = a.ctf ? a.ctf + (long)p * W * W : nullptr;
     const float* fc0 = a.fcut0 + (long)p * nr;
     const float* tfc = a.tfcut + (long)p * a.tfcut_pstride;
     const float twopi = __fmul_rn(2.0f, K.pi);
-    double p1 = 0.0, p2 = 0.0;
-    float f1 = 0.f, f2 = 0.f, k1 = 0.f, k2 = 0.f;
-    float h1 = 0.f, l1 = 0.f, h2 = 0.f, l2 = 0.f;  // unshifted form: TwoSum pairs
-    if (SHIFTED)
-        for (int q = threadIdx.x; q < nr; q += blockDim.x) sfc[0][q] = fc0[q];
+    float h1 = 0.f, l1 = 0.f, h2 = 0.f, l2 = 0.f;  // per-thread sums as TwoSum pairs
     for (int i = 0; i < a.T; ++i) {
         const float2* al = a.alpha + (((long)p * a.ncand + c) * a.T + i) * 60;
         const float2* tb = a.tband + (long)i * W * W;
         const float* fct = tfc + (long)i * nr;
-        // SHIFTED: the templates already multiplied by this particle's CTF
-        const float2* tbc = SHIFTED && a.tbandc ? a.tbandc + ((long)p * a.T + i) * W * W : nullptr;
         // the two in-plane directions of each common line, once per line
         __syncthreads();
         if (threadIdx.x < 60) {
@@ -272,8 +260,6 @@ __global__ void __launch_bounds__(512) k_pr_single(PrSingleArgs a, Consts K) {
                 sline[3][threadIdx.x] = sinf(a2);
             }
         }
-        if (SHIFTED)
-            for (int q = threadIdx.x; q < nr; q += blockDim.x) sfc[1][q] = fct[q];
         __syncthreads();
         for (int q = threadIdx.x; q < 60 * nr; q += blockDim.x) {
             int j = q / nr, iq = q - j * nr;
@@ -285,62 +271,35 @@ __global__ void __launch_bounds__(512) k_pr_single(PrSingleArgs a, Consts K) {
             int lx = (int)x, ly = (int)y;
             float ax = __fsub_rn(x, (float)lx), ay = __fsub_rn(y, (float)ly);
             float tr[4], ti[4];
-            if (SHIFTED) {
 #pragma unroll
-                for (int u = 0; u < 4; ++u) {
-                    const float2 vv = sb[(ly + (u >> 1)) * W + lx + (u & 1) - offW];
-                    tr[u] = vv.x;
-                    ti[u] = vv.y;
-                }
-            } else {
-#pragma unroll
-                for (int u = 0; u < 4; ++u) {
-                    int tx = lx + (u & 1), ty = ly + (u >> 1);
-                    float2 vv = pb[ty * W + tx - offW];
-                    int hx = tx - nx / 2, ky = ty - nx / 2;
-                    float ph = __fdiv_rn(__fmul_rn(twopi, __fadd_rn(__fmul_rn(xs, (float)hx),
-                                                                     __fmul_rn(ys, (float)ky))),
-                                         (float)nx);
-                    float s, co;
-                    sincosf(ph, &s, &co);
-                    tr[u] = __fadd_rn(__fmul_rn(vv.x, co), __fmul_rn(vv.y, s));
-                    ti[u] = __fadd_rn(__fmul_rn(-vv.x, s), __fmul_rn(vv.y, co));
-                }
+            for (int u = 0; u < 4; ++u) {
+                int tx = lx + (u & 1), ty = ly + (u >> 1);
+                float2 vv = pb[ty * W + tx - offW];
+                int hx = tx - nx / 2, ky = ty - nx / 2;
+                float ph = __fdiv_rn(__fmul_rn(twopi, __fadd_rn(__fmul_rn(xs, (float)hx), __fmul_rn(ys, (float)ky))),
+                                     (float)nx);
+                float s, co;
+                sincosf(ph, &s, &co);
+                tr[u] = __fadd_rn(__fmul_rn(vv.x, co), __fmul_rn(vv.y, s));
+                ti[u] = __fadd_rn(__fmul_rn(-vv.x, s), __fmul_rn(vv.y, co));
             }
             float re1 = bilerp(ax, ay, tr[0], tr[1], tr[2], tr[3]);
             float im1 = bilerp(ax, ay, ti[0], ti[1], ti[2], ti[3]);
             float re2, im2;
-            if (tbc)
-                tmpl_sample_cs(tbc, nullptr, W, offW, nxh, sline[2][j], sline[3][j], fr, &re2, &im2);
-            else
-                tmpl_sample_cs(tb, ctfp, W, offW, nxh, sline[2][j], sline[3][j], fr, &re2, &im2);
+            tmpl_sample_cs(tb, ctfp, W, offW, nxh, sline[2][j], sline[3][j], fr, &re2, &im2);
             float amp1 = sqrtf(re1 * re1 + im1 * im1);
             float amp2 = sqrtf(re2 * re2 + im2 * im2);
-            const float cut1 = SHIFTED ? sfc[0][iq] : fc0[iq], cut2 = SHIFTED ? sfc[1][iq] : fct[iq];
-            if (amp1 >= cut1 && amp2 >= cut2) {
-                if (SHIFTED) {
-                    const float d = angle_between(re1 * im2 - im1 * re2, re1 * re2 + im1 * im2, K.pi);
-                    const float w = 0.5f * (amp1 + amp2);
-                    kahan_add(f1, k1, d * w);
-                    kahan_add(f2, k2, w);
-                } else {
-                    float ph1 = atan2f(im1, re1), ph2 = atan2f(im2, re2);
-                    float d = fabsf(ph2 - ph1);
-                    d = fminf(d, K.tpi - d);
-                    float w = 0.5f * (amp1 + amp2);
-                    two_sum_acc(h1, l1, d * w);
-                    two_sum_acc(h2, l2, w);
-                }
+            if (amp1 >= fc0[iq] && amp2 >= fct[iq]) {
+                float ph1 = atan2f(im1, re1), ph2 = atan2f(im2, re2);
+                float d = fabsf(ph2 - ph1);
+                d = fminf(d, K.tpi - d);
+                float w = 0.5f * (amp1 + amp2);
+                two_sum_acc(h1, l1, d * w);
+                two_sum_acc(h2, l2, w);
             }
         }
     }
-    if (SHIFTED) {
-        p1 = (double)f1;
-        p2 = (double)f2;
-    } else {
-        p1 = (double)h1 + (double)l1;
-        p2 = (double)h2 + (double)l2;
-    }
+    double p1 = (double)h1 + (double)l1, p2 = (double)h2 + (double)l2;
     for (int o = 16; o > 0; o >>= 1) {
         p1 += __shfl_xor_sync(0xffffffffu, p1, o);
         p2 += __shfl_xor_sync(0xffffffffu, p2, o);
@@ -356,103 +315,14 @@ __global__ void __launch_bounds__(512) k_pr_single(PrSingleArgs a, Consts K) {
     }
 }
 
-// Rescoring form of k_pr_single<true> (every candidate at the particle's origin, band
-// pre-shifted, templates pre-multiplied by the CTF): the lines of all templates are set
-// up once (directions, validity, cuts in shared memory), then the block's threads run
-// one flat loop over (template, line, radius) with no barrier inside.  Same per-term
-// arithmetic as the exhaustive scorer (angle_between, Kahan sums per thread).
-__global__ void __launch_bounds__(512) k_pr_rescore(PrSingleArgs a, Consts K) {
-    extern __shared__ float rsm[];
-    __shared__ double sh[2][32];
-    const Band bd = a.bd;
-    const int W = bd.W, nr = bd.nr, minR = bd.min_r, nx = bd.nx, T = a.T;
-    const int c = blockIdx.x, p = blockIdx.y;
-    if (a.ncount && c >= a.ncount[p]) return;  // padding slot (whole block)
-    float* scs = rsm;                          // [T][60][4]: cos, sin particle line; cos, sin template line
-    float* sfc = scs + (long)T * 240;          // [T + 1][nr]: template cuts, then the particle's
-    int* sval = reinterpret_cast<int*>(sfc + (long)(T + 1) * nr);  // [T][60]
-    const float2* al0 = a.alpha + ((long)p * a.ncand + c) * T * 60;
-    for (int q = threadIdx.x; q < T * 60; q += blockDim.x) {
-        const float2 aa = al0[q];
-        const bool ok = aa.x < 999.0f && aa.y < 999.0f;
-        sval[q] = ok;
-        if (ok) {
-            const float a1 = __fmul_rn(aa.x, K.d2r), a2 = __fmul_rn(aa.y, K.d2r);
-            scs[4 * q] = cosf(a1);
-            scs[4 * q + 1] = sinf(a1);
-            scs[4 * q + 2] = cosf(a2);
-            scs[4 * q + 3] = sinf(a2);
-        }
-    }
-    const float* tfc = a.tfcut + (long)p * a.tfcut_pstride;
-    for (int q = threadIdx.x; q < T * nr; q += blockDim.x) sfc[q] = tfc[q];
-    for (int q = threadIdx.x; q < nr; q += blockDim.x) sfc[T * nr + q] = a.fcut0[(long)p * nr + q];
-    __syncthreads();
-    const float nxh = (float)(nx / 2);
-    const int offW = bd.off * W + bd.off;
-    const float2* sb = a.sband + (long)p * W * W;
-    const float2* tbc0 = a.tbandc ? a.tbandc + (long)p * T * W * W : nullptr;
-    const float* ctfp = a.ctf ? a.ctf + (long)p * W * W : nullptr;
-    const int per_t = 60 * nr;
-    float f1 = 0.f, f2 = 0.f, k1 = 0.f, k2 = 0.f;
-    // (template i, line j, radius iq) of the flat index q = (i * 60 + j) * nr + iq, advanced
-    // by blockDim.x per iteration without integer divisions
-    const int step_j = (int)blockDim.x / nr, step_iq = (int)blockDim.x - step_j * nr;
-    int i = (int)threadIdx.x / per_t, j = ((int)threadIdx.x - i * per_t) / nr;
-    int iq = (int)threadIdx.x - i * per_t - j * nr;
-    auto advance = [&]() {
-        iq += step_iq;
-        j += step_j;
-        if (iq >= nr) { iq -= nr; ++j; }
-        while (j >= 60) { j -= 60; ++i; }
-    };
-    for (int q = threadIdx.x; q < T * per_t; q += blockDim.x, advance()) {
-        const int lj = i * 60 + j;
-        if (!sval[lj]) continue;
-        const float4 cs4 = *reinterpret_cast<const float4*>(scs + 4 * lj);
-        const float fr = (float)(minR + iq);
-        const float x = __fadd_rn(__fmul_rn(fr, cs4.x), nxh), y = __fadd_rn(__fmul_rn(fr, cs4.y), nxh);
-        const int lx = (int)x, ly = (int)y;
-        const float ax = __fsub_rn(x, (float)lx), ay = __fsub_rn(y, (float)ly);
-        const int b0 = ly * W + lx - offW;
-        const float2 t00 = sb[b0], t10 = sb[b0 + 1], t01 = sb[b0 + W], t11 = sb[b0 + W + 1];
-        const float re1 = bilerp(ax, ay, t00.x, t10.x, t01.x, t11.x);
-        const float im1 = bilerp(ax, ay, t00.y, t10.y, t01.y, t11.y);
-        float re2, im2;
-        if (tbc0)
-            tmpl_sample_cs(tbc0 + (long)i * W * W, nullptr, W, offW, nxh, cs4.z, cs4.w, fr, &re2, &im2);
-        else
-            tmpl_sample_cs(a.tband + (long)i * W * W, ctfp, W, offW, nxh, cs4.z, cs4.w, fr, &re2, &im2);
-        const float amp1 = sqrtf(re1 * re1 + im1 * im1);
-        const float amp2 = sqrtf(re2 * re2 + im2 * im2);
-        if (amp1 >= sfc[T * nr + iq] && amp2 >= sfc[i * nr + iq]) {
-            const float d = angle_between(re1 * im2 - im1 * re2, re1 * re2 + im1 * im2, K.pi);
-            const float w = 0.5f * (amp1 + amp2);
-            kahan_add(f1, k1, d * w);
-            kahan_add(f2, k2, w);
-        }
-    }
-    double p1 = (double)f1, p2 = (double)f2;
-    for (int o = 16; o > 0; o >>= 1) {
-        p1 += __shfl_xor_sync(0xffffffffu, p1, o);
-        p2 += __shfl_xor_sync(0xffffffffu, p2, o);
-    }
-    const int w = threadIdx.x >> 5, l = threadIdx.x & 31, nw = blockDim.x >> 5;
-    if (l == 0) { sh[0][w] = p1; sh[1][w] = p2; }
-    __syncthreads();
-    if (threadIdx.x == 0) {
-        double s1 = 0, s2 = 0;
-        for (int q = 0; q < nw; ++q) { s1 += sh[0][q]; s2 += sh[1][q]; }
-        const float g1 = (float)s1, g2 = (float)s2;
-        a.pr[(long)p * a.ncand + c] = (g2 > 1.0e-10f) ? g1 / g2 * 180.0f / K.pi : 1000.0f;
-    }
-}
-
 // Grouped rescoring: up to RG candidates of one particle that share a view (theta,
 // phi) and differ in omega.  The template side of a term (line direction, taps, cut)
 // does not depend on omega, so each (template, line, radius) sample of the templates
 // is taken once and compared with the RG particle samples.  groups[g] = (particle,
-// first candidate slot, count).  Same per-term arithmetic as k_pr_rescore.
+// first candidate slot, count).  Every candidate sits at the particle's origin (band
+// pre-shifted, templates pre-multiplied by the particle's CTF), and the per-term
+// arithmetic is the exhaustive scorer's (angle_between, Kahan sums per thread), so its
+// values match k_pr_omega's.
 constexpr int RG = 4;
 __global__ void __launch_bounds__(512) k_pr_rescore_g(PrSingleArgs a, const int4* __restrict__ groups, Consts K) {
     extern __shared__ float rsm[];
@@ -708,20 +578,7 @@ cudaError_t launch_tband_ctf(const float2* tband, int T, const float* ctf, const
 
 cudaError_t launch_pr_single(const PrSingleArgs& a, int B, cudaStream_t st) {
     dim3 grid(a.ncand, B);
-    if (a.sband) {
-        // the flat rescoring kernel when its line tables fit in shared memory
-        const size_t sm = sizeof(float) * ((size_t)a.T * 240 + (size_t)(a.T + 1) * a.bd.nr) + sizeof(int) * a.T * 60;
-        if (sm <= 200 * 1024) {
-            cudaError_t e = cudaFuncSetAttribute(k_pr_rescore, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
-            if (e != cudaSuccess) return e;
-            k_pr_rescore<<<grid, 512, sm, st>>>(a, consts());
-            return cudaGetLastError();
-        }
-        if (a.bd.nr > 256) return cudaErrorInvalidValue;
-        k_pr_single<true><<<grid, 512, 0, st>>>(a, consts());
-    } else {
-        k_pr_single<false><<<grid, 512, 0, st>>>(a, consts());
-    }
+    k_pr_single<<<grid, 512, 0, st>>>(a, consts());
     return cudaGetLastError();
 }
 
