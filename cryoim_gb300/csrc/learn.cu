@@ -361,8 +361,8 @@ __global__ void __launch_bounds__(NT) k_conv3_wgrad(const float* __restrict__ in
 }
 
 // dpre = dout where out > 0 (the ReLU gate), else 0
-__global__ void k_relu_grad(const float* __restrict__ out, const float* __restrict__ dout, long n,
-                            float* __restrict__ dpre) {
+// (in place: dout and dpre may be the same buffer)
+__global__ void k_relu_grad(const float* __restrict__ out, const float* dout, long n, float* dpre) {
     for (long q = (long)blockIdx.x * blockDim.x + threadIdx.x; q < n; q += (long)gridDim.x * blockDim.x)
         dpre[q] = out[q] > 0.f ? dout[q] : 0.f;
 }
