@@ -340,7 +340,8 @@ struct Ctx {
     float orig_max = -1.0f, orig_step = -1.0f;
     DBuf<float> tilev, xcand, xpr;
     DBuf<int> tileo, tileorig;
-    DBuf<float2> xalpha, sband;
+    DBuf<float2> xalpha;
+    DBuf<float4> sband;
     DBuf<int> xcount;
     DBuf<double> kpart;
     DBuf<float2> tbandc;

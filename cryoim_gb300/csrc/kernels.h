@@ -101,7 +101,8 @@ struct PrSingleArgs {
     float* pr;               // [B][ncand]
     int ncand = 11;          // 11 for the refinement step (ort_cent_11.f90)
     // rescoring by groups (launch_pr_rescore_groups) only:
-    const float2* sband = nullptr;  // [B][W*W] band shifted to the candidates' common origin
+    const float4* sband = nullptr;  // [B][W*W] band shifted to the candidates' common origin, in
+                                    // (pixel, right neighbour) pairs (launch_shift_band)
     const int* ncount = nullptr;    // [B] candidates in use (later slots are skipped), or nullptr
     const float2* tbandc = nullptr; // [B][T][W*W] templates x CTF (launch_tband_ctf), or nullptr
 };
@@ -113,9 +114,10 @@ cudaError_t launch_pr_rescore_groups(const PrSingleArgs& a, const int4* groups, 
 int pr_rescore_group_size();
 cudaError_t launch_tband_ctf(const float2* tband, int T, const float* ctf, const Band& bd, int B, float2* out,
                              cudaStream_t st);
-// sband for PrSingleArgs: the band of each particle shifted to cand[p][0]'s origin
+// sband for PrSingleArgs: the band of each particle shifted to cand[p][0]'s origin, each
+// pixel stored with its right neighbour
 cudaError_t launch_shift_band(const float2* band, const float* cand, int ncand, const Band& bd, int B,
-                              float2* out, cudaStream_t st);
+                              float4* out, cudaStream_t st);
 
 struct InsertArgs {
     const float2* band;      // [B][W*W] shifted particle FT

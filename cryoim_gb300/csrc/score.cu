@@ -358,7 +358,7 @@ __global__ void __launch_bounds__(512) k_pr_rescore_g(PrSingleArgs a, const int4
     __syncthreads();
     const float nxh = (float)(nx / 2);
     const int offW = bd.off * W + bd.off;
-    const float2* sb = a.sband + (long)p * W * W;
+    const float4* sb = a.sband + (long)p * W * W;
     const float2* tbc0 = a.tbandc ? a.tbandc + (long)p * T * W * W : nullptr;
     const float* ctfp = a.ctf ? a.ctf + (long)p * W * W : nullptr;
     const int per_t = 60 * nr;
@@ -398,7 +398,9 @@ __global__ void __launch_bounds__(512) k_pr_rescore_g(PrSingleArgs a, const int4
             const int lx = (int)x, ly = (int)y;
             const float ax = __fsub_rn(x, (float)lx), ay = __fsub_rn(y, (float)ly);
             const int b0 = ly * W + lx - offW;
-            const float2 t00 = sb[b0], t10 = sb[b0 + 1], t01 = sb[b0 + W], t11 = sb[b0 + W + 1];
+            const float4 r0 = sb[b0], r1 = sb[b0 + W];  // (tap, right tap) of rows y, y + 1
+            const float2 t00 = make_float2(r0.x, r0.y), t10 = make_float2(r0.z, r0.w);
+            const float2 t01 = make_float2(r1.x, r1.y), t11 = make_float2(r1.z, r1.w);
             const float re1 = bilerp(ax, ay, t00.x, t10.x, t01.x, t11.x);
             const float im1 = bilerp(ax, ay, t00.y, t10.y, t01.y, t11.y);
             const float amp1 = sqrtf(re1 * re1 + im1 * im1);
@@ -433,8 +435,22 @@ __global__ void __launch_bounds__(512) k_pr_rescore_g(PrSingleArgs a, const int4
 // The particle transform shifted to the origin its candidates share (cand[p][0][3..4]):
 // per pixel the same phase rotation k_pr_single applies to each bilinear tap
 // (img2d_FT_centshift.f90), computed once per pixel instead of once per tap.
+// Stored as pairs: out[p][m] = (pixel m, its right neighbour m + 1; zero past the row's
+// end), so a bilinear sample reads two aligned 16-byte pairs instead of four taps.
+__device__ __forceinline__ float2 shifted_pixel(const float2* band, int m, int W, int off, int nx, float xs,
+                                                float ys, float twopi) {
+    const int by = m / W, bx = m - by * W;
+    const int hx = bx + off - nx / 2, ky = by + off - nx / 2;
+    const float2 vv = band[m];
+    float ph = __fdiv_rn(__fmul_rn(twopi, __fadd_rn(__fmul_rn(xs, (float)hx), __fmul_rn(ys, (float)ky))),
+                         (float)nx);
+    float s, co;
+    sincosf(ph, &s, &co);
+    return make_float2(__fadd_rn(__fmul_rn(vv.x, co), __fmul_rn(vv.y, s)),
+                       __fadd_rn(__fmul_rn(-vv.x, s), __fmul_rn(vv.y, co)));
+}
 __global__ void k_shift_band(const float2* __restrict__ band, const float* __restrict__ cand, int ncand, Band bd,
-                             Consts K, float2* __restrict__ out) {
+                             Consts K, float4* __restrict__ out) {
     const int W = bd.W, nx = bd.nx, p = blockIdx.y;
     const int m = blockIdx.x * blockDim.x + threadIdx.x;
     if (m >= W * W) return;
@@ -442,15 +458,10 @@ __global__ void k_shift_band(const float2* __restrict__ band, const float* __res
     const float nxh = (float)(nx / 2);
     const float xs = __fadd_rn(cd[3], nxh), ys = __fadd_rn(cd[4], nxh);
     const float twopi = __fmul_rn(2.0f, K.pi);
-    const int by = m / W, bx = m - by * W;
-    const int hx = bx + bd.off - nx / 2, ky = by + bd.off - nx / 2;
-    const float2 vv = band[(long)p * W * W + m];
-    float ph = __fdiv_rn(__fmul_rn(twopi, __fadd_rn(__fmul_rn(xs, (float)hx), __fmul_rn(ys, (float)ky))),
-                         (float)nx);
-    float s, co;
-    sincosf(ph, &s, &co);
-    out[(long)p * W * W + m] = make_float2(__fadd_rn(__fmul_rn(vv.x, co), __fmul_rn(vv.y, s)),
-                                           __fadd_rn(__fmul_rn(-vv.x, s), __fmul_rn(vv.y, co)));
+    const float2* b = band + (long)p * W * W;
+    const float2 v0 = shifted_pixel(b, m, W, bd.off, nx, xs, ys, twopi);
+    const float2 v1 = (m % W) + 1 < W ? shifted_pixel(b, m + 1, W, bd.off, nx, xs, ys, twopi) : make_float2(0.f, 0.f);
+    out[(long)p * W * W + m] = make_float4(v0.x, v0.y, v1.x, v1.y);
 }
 
 // reconstruct.f90:103-145: rotate each half-plane sample, apply the 60 operators,
@@ -549,7 +560,7 @@ cudaError_t launch_pr_omega(const PrOmegaArgs& a, int B, cudaStream_t st) {
 }
 
 cudaError_t launch_shift_band(const float2* band, const float* cand, int ncand, const Band& bd, int B,
-                              float2* out, cudaStream_t st) {
+                              float4* out, cudaStream_t st) {
     const int n = bd.W * bd.W;
     dim3 grid((n + 255) / 256, B);
     k_shift_band<<<grid, 256, 0, st>>>(band, cand, ncand, bd, consts(), out);
