@@ -56,7 +56,7 @@ LAUNCHES_PER_PASS = 29
 # capture at the 2-degree grid (1.483 GB for 31,320 orientations), scaled to the
 # orientation count: operand B streams once per launch.
 GEMM_TRAFFIC_PER_ORIENT = 1.483e9 / 31320
-LANES = 4  # pass lanes of the contraction search (the library's default)
+LANES = 6  # pass lanes of the contraction search (the library's default)
 # dram__bytes_read.sum + dram__bytes_write.sum of one grouped fine-contraction launch over
 # a 64-particle pass of the box-256 workload (ncu capture of --profile-case learned)
 GROUPED_GEMM_TRAFFIC_PER_PASS = 3.802061e9 + 5.544448e6

@@ -86,7 +86,7 @@ class Context:
         call("cryoim_ctx_set_batch", self._h, int(b))
 
     def set_lanes(self, n: int) -> None:
-        """Pass lanes of the contraction search (1..4, default 4)."""
+        """Pass lanes of the contraction search (1..8, default 6)."""
         call("cryoim_ctx_set_lanes", self._h, int(n))
 
     def set_profiling(self, on: bool) -> None:

@@ -362,7 +362,7 @@ struct Ctx {
     // pass lanes of the contraction search: this context and xlanes (refresh_lane), each
     // extra lane with its own stream and per-pass buffers, this context's read-only
     // state borrowed
-    int lanes = 4;
+    int lanes = 6;
     std::vector<Ctx*> xlanes;
 
     ~Ctx() {
@@ -2220,7 +2220,7 @@ int cryoim_ctx_set_batch(void* ctx, int32_t batch) {
 int cryoim_ctx_set_lanes(void* ctx, int32_t lanes) {
     Ctx* c = as_ctx(ctx);
     if (!c) return fail(CRYOIM_ERR_ARG, "null context");
-    if (lanes < 1 || lanes > 4) return fail(CRYOIM_ERR_ARG, "lanes %d out of range 1..4", lanes);
+    if (lanes < 1 || lanes > 8) return fail(CRYOIM_ERR_ARG, "lanes %d out of range 1..8", lanes);
     c->lanes = lanes;
     return CRYOIM_OK;
 }

@@ -116,7 +116,7 @@ int cryoim_set_params(void* ctx, const cryoim_params* p);
 /* Images processed per device batch (default: min(64, 16M / nx^2)).  No reference
  * counterpart: the reference processes one particle at a time. */
 int cryoim_ctx_set_batch(void* ctx, int32_t batch);
-/* Pass lanes of the contraction search (1..4, default 4): passes of `batch` particles are
+/* Pass lanes of the contraction search (1..8, default 6): passes of `batch` particles are
  * dealt round-robin to lanes, each with its own internal stream, device buffers and host
  * thread, so one lane's host work overlaps the others' kernels.  The call stays
  * synchronous: it starts after the work queued on the context's stream and returns when
