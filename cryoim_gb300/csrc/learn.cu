@@ -360,11 +360,14 @@ __global__ void __launch_bounds__(NT) k_conv3_wgrad(const float* __restrict__ in
     }
 }
 
-// dpre = dout where out > 0 (the ReLU gate), else 0
-// (in place: dout and dpre may be the same buffer)
-__global__ void k_relu_grad(const float* __restrict__ out, const float* dout, long n, float* dpre) {
-    for (long q = (long)blockIdx.x * blockDim.x + threadIdx.x; q < n; q += (long)gridDim.x * blockDim.x)
-        dpre[q] = out[q] > 0.f ? dout[q] : 0.f;
+// dpre = dout where out > 0 (the ReLU gate), else 0, four elements per thread step
+// (in place: dout and dpre may be the same buffer; n is a multiple of 4, the buffers 16-byte aligned)
+__global__ void k_relu_grad(const float4* __restrict__ out, const float4* dout, long n4, float4* dpre) {
+    for (long q = (long)blockIdx.x * blockDim.x + threadIdx.x; q < n4; q += (long)gridDim.x * blockDim.x) {
+        const float4 o = out[q], d = dout[q];
+        dpre[q] = make_float4(o.x > 0.f ? d.x : 0.f, o.y > 0.f ? d.y : 0.f, o.z > 0.f ? d.z : 0.f,
+                              o.w > 0.f ? d.w : 0.f);
+    }
 }
 
 // Wf[ci][co][2-dh][2-dt] = W[co][ci][dh][dt]: the data gradient is a k_conv3 with Wf
@@ -375,29 +378,36 @@ __global__ void k_flip(const float* __restrict__ W, int Cout, int Cin, float* __
     Wf[((long)ci * Cout + co) * 9 + (8 - k)] = W[q];
 }
 
-// average of radius pairs: p[b][c][h][t] = (a[..][2h][t] + a[..][2h+1][t]) / 2
-__global__ void k_pool(const float* __restrict__ a, long nout, int Hout, float* __restrict__ p) {
-    for (long q = (long)blockIdx.x * blockDim.x + threadIdx.x; q < nout; q += (long)gridDim.x * blockDim.x) {
-        const int t = (int)(q % NT);
-        const long bch = q / NT;  // (b, c, h)
-        const int h = (int)(bch % Hout);
-        const long bc = bch / Hout;
-        const float* src = a + (bc * 2 * Hout + 2 * h) * NT + t;
-        p[q] = 0.5f * (src[0] + src[NT]);
+// average of radius pairs: p[b][c][h][t] = (a[..][2h][t] + a[..][2h+1][t]) / 2.  Output row
+// (b, c, h) reads input rows 2(b, c, h) and 2(b, c, h) + 1, so no index is split; four
+// angles per thread step (rows of NT floats, 16-byte aligned)
+constexpr int NT4 = NT / 4;
+__global__ void k_pool(const float4* __restrict__ a, long nout4, float4* __restrict__ p) {
+    for (long q = (long)blockIdx.x * blockDim.x + threadIdx.x; q < nout4; q += (long)gridDim.x * blockDim.x) {
+        const long row = q / NT4;
+        const float4* src = a + row * (2 * NT4) + (q - row * NT4);
+        const float4 u = src[0], v = src[NT4];
+        p[q] = make_float4(0.5f * (u.x + v.x), 0.5f * (u.y + v.y), 0.5f * (u.z + v.z), 0.5f * (u.w + v.w));
     }
 }
-// gradient through the pooling and, given the pooled layer's ReLU output a, its gate
-__global__ void k_pool_grad(const float* __restrict__ dp, long nout, int Hout, const float* __restrict__ a,
-                            float* __restrict__ da) {
-    for (long q = (long)blockIdx.x * blockDim.x + threadIdx.x; q < nout; q += (long)gridDim.x * blockDim.x) {
-        const int t = (int)(q % NT);
-        const long bch = q / NT;
-        const int h = (int)(bch % Hout);
-        const long bc = bch / Hout;
-        const long o = (bc * 2 * Hout + 2 * h) * NT + t;
-        const float v = 0.5f * dp[q];
-        da[o] = (!a || a[o] > 0.f) ? v : 0.f;
-        da[o + NT] = (!a || a[o + NT] > 0.f) ? v : 0.f;
+// gradient through the pooling and, given the pooled layer's ReLU output a (or none), its gate
+__global__ void k_pool_grad(const float4* __restrict__ dp, long nout4, const float4* __restrict__ a,
+                            float4* __restrict__ da) {
+    for (long q = (long)blockIdx.x * blockDim.x + threadIdx.x; q < nout4; q += (long)gridDim.x * blockDim.x) {
+        const long row = q / NT4;
+        const long o = row * (2 * NT4) + (q - row * NT4);
+        const float4 g = dp[q];
+        const float4 v = make_float4(0.5f * g.x, 0.5f * g.y, 0.5f * g.z, 0.5f * g.w);
+        if (!a) {
+            da[o] = v;
+            da[o + NT4] = v;
+            continue;
+        }
+        const float4 u0 = a[o], u1 = a[o + NT4];
+        da[o] = make_float4(u0.x > 0.f ? v.x : 0.f, u0.y > 0.f ? v.y : 0.f, u0.z > 0.f ? v.z : 0.f,
+                            u0.w > 0.f ? v.w : 0.f);
+        da[o + NT4] = make_float4(u1.x > 0.f ? v.x : 0.f, u1.y > 0.f ? v.y : 0.f, u1.z > 0.f ? v.z : 0.f,
+                                  u1.w > 0.f ? v.w : 0.f);
     }
 }
 
@@ -739,18 +749,23 @@ cudaError_t launch_lp_conv3_wgrad(const float* in, const float* dpre, int B, int
     return cudaGetLastError();
 }
 void launch_lp_relu_grad(const float* out, const float* dout, long n, float* dpre, cudaStream_t st) {
-    k_relu_grad<<<grid_for(n, 256), 256, 0, st>>>(out, dout, n, dpre);
+    const long n4 = n / 4;  // n = B x C x NR x NT, a multiple of 4
+    k_relu_grad<<<grid_for(n4, 256), 256, 0, st>>>(reinterpret_cast<const float4*>(out),
+                                                   reinterpret_cast<const float4*>(dout), n4,
+                                                   reinterpret_cast<float4*>(dpre));
 }
 void launch_lp_flip(const float* W, int Cout, int Cin, float* Wf, cudaStream_t st) {
     k_flip<<<cdiv((long)Cout * Cin * 9, 256), 256, 0, st>>>(W, Cout, Cin, Wf);
 }
 void launch_lp_pool(const float* a, int B, int C, int Hout, float* p, cudaStream_t st) {
-    const long n = (long)B * C * Hout * NT;
-    k_pool<<<grid_for(n, 256), 256, 0, st>>>(a, n, Hout, p);
+    const long n4 = (long)B * C * Hout * NT4;
+    k_pool<<<grid_for(n4, 256), 256, 0, st>>>(reinterpret_cast<const float4*>(a), n4, reinterpret_cast<float4*>(p));
 }
 void launch_lp_pool_grad(const float* dp, int B, int C, int Hout, const float* a, float* da, cudaStream_t st) {
-    const long n = (long)B * C * Hout * NT;
-    k_pool_grad<<<grid_for(n, 256), 256, 0, st>>>(dp, n, Hout, a, da);
+    const long n4 = (long)B * C * Hout * NT4;
+    k_pool_grad<<<grid_for(n4, 256), 256, 0, st>>>(reinterpret_cast<const float4*>(dp), n4,
+                                                   reinterpret_cast<const float4*>(a),
+                                                   reinterpret_cast<float4*>(da));
 }
 void launch_lp_mix(const float* x, int B, const float* W5, const float* b5, float* g, cudaStream_t st) {
     k_mix<<<B, NT, 0, st>>>(x, W5, b5, g);
