@@ -45,6 +45,18 @@ __device__ double block_sum_d(double v, double* sh) {
 // mask / normalise / checkerboard: img2d_norm.f90:1-22, img2d_mask.f90:2-49,
 // and the (-1)^(hx+ky) multiply of ort_globesearch.f90:51
 // ---------------------------------------------------------------------------
+// h + l += x with Knuth's TwoSum: the pair holds the running sum to ~2^-48 relative in
+// FP32 arithmetic (GB300's FP64 pipe is far slower than its FP32 pipe)
+__device__ __forceinline__ void two_sum_acc(float& h, float& l, float x) {
+    const float s2 = h + x, bb = s2 - h;
+    l += (h - (s2 - bb)) + (x - bb);
+    h = s2;
+}
+
+// One block of 1024 threads per image; warp w walks rows w, w + 32, ..., its lanes the
+// columns, so no pixel index is split by a division.  The image sums the reference takes
+// in FP64 are FP32 TwoSum pairs per thread (exact to far below FP32 rounding), combined
+// in FP64 across the block.
 __global__ void k_prep_images(const float* __restrict__ imgs, int nx,
                               const float* __restrict__ ox, const float* __restrict__ oy,
                               int use_mask, float mask, int normalize, float pi,
@@ -54,64 +66,70 @@ __global__ void k_prep_images(const float* __restrict__ imgs, int nx,
     const long nn = (long)nx * nx;
     const float* img = imgs + p * nn;
     float2* o = out + p * nn;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
     int bad = 0;
     float avg = 0.f, nd = 1.f;
     if (normalize) {
-        double s = 0;
-        for (long i = threadIdx.x; i < nn; i += blockDim.x) s += (double)img[i];
-        s = block_sum_d(s, sh);
+        float h = 0.f, l = 0.f;
+        for (int iy = warp; iy < nx; iy += nw)
+            for (int ix = lane; ix < nx; ix += 32) two_sum_acc(h, l, img[(long)iy * nx + ix]);
+        const double s = block_sum_d((double)h + (double)l, sh);
         avg = (float)s / (float)nn;
-        double s2 = 0;
-        for (long i = threadIdx.x; i < nn; i += blockDim.x) {
-            float d = img[i] - avg;
-            s2 += (double)(d * d);
-        }
-        s2 = block_sum_d(s2, sh);
+        h = 0.f, l = 0.f;
+        for (int iy = warp; iy < nx; iy += nw)
+            for (int ix = lane; ix < nx; ix += 32) {
+                const float d = img[(long)iy * nx + ix] - avg;
+                two_sum_acc(h, l, __fmul_rn(d, d));  // the square rounded to FP32, as the reference
+            }
+        const double s2 = block_sum_d((double)h + (double)l, sh);
         nd = sqrtf((float)s2 / (float)nn);
     }
-    const int h = nx / 2;
+    const int hh = nx / 2;
     float R1 = mask - 3.0f;
     if (R1 <= 0.0f) R1 = 0.0f;
     float R2 = mask + 3.0f;
-    if (R2 > (float)h) R2 = (float)h;
-    const float x0 = ox[p] + (float)h, y0 = oy[p] + (float)h;
+    if (R2 > (float)hh) R2 = (float)hh;
+    const float x0 = ox[p] + (float)hh, y0 = oy[p] + (float)hh;
     double summ = 0;
     if (use_mask) {
-        double s = 0, c = 0;
-        for (long i = threadIdx.x; i < nn; i += blockDim.x) {
-            int iy = (int)(i / nx), ix = (int)(i % nx);
-            float yy = (-y0 + (float)iy) * (-y0 + (float)iy);
-            float xx = (-x0 + (float)ix) * (-x0 + (float)ix);
-            float ra = sqrtf(yy + xx);
-            if (ra > R1 && ra <= R2) {
-                float v = img[i];
-                if (normalize) v = (v - avg) / nd;
-                s += (double)v;
-                c += 1.0;
+        float h = 0.f, l = 0.f;
+        int cnt = 0;
+        for (int iy = warp; iy < nx; iy += nw) {
+            const float yy = (-y0 + (float)iy) * (-y0 + (float)iy);
+            for (int ix = lane; ix < nx; ix += 32) {
+                const float xx = (-x0 + (float)ix) * (-x0 + (float)ix);
+                const float ra = sqrtf(yy + xx);
+                if (ra > R1 && ra <= R2) {
+                    float v = img[(long)iy * nx + ix];
+                    if (normalize) v = (v - avg) / nd;
+                    two_sum_acc(h, l, v);
+                    ++cnt;
+                }
             }
         }
-        s = block_sum_d(s, sh);
-        c = block_sum_d(c, sh);
-        summ = s;
+        summ = block_sum_d((double)h + (double)l, sh);
+        const double c = block_sum_d((double)cnt, sh);
         if (c != 0.0) summ = summ / (double)(float)c;
     }
-    for (long i = threadIdx.x; i < nn; i += blockDim.x) {
-        int iy = (int)(i / nx), ix = (int)(i % nx);
-        float v = img[i];
-        if (!isfinite(v)) bad = 1;
-        if (normalize) v = (v - avg) / nd;
-        if (use_mask) {
-            float yy = (-y0 + (float)iy) * (-y0 + (float)iy);
-            float xx = (-x0 + (float)ix) * (-x0 + (float)ix);
-            float ra = sqrtf(yy + xx);
-            if (ra > R1 && ra <= R2) {
-                float edge = (1.0f + cosf(pi * (ra - R1) / 6.0f)) / 2.0f;
-                v = (float)((double)(v * edge) + (double)(1.0f - edge) * summ);
+    for (int iy = warp; iy < nx; iy += nw) {
+        const float yy = (-y0 + (float)iy) * (-y0 + (float)iy);
+        for (int ix = lane; ix < nx; ix += 32) {
+            const long i = (long)iy * nx + ix;
+            float v = img[i];
+            if (!isfinite(v)) bad = 1;
+            if (normalize) v = (v - avg) / nd;
+            if (use_mask) {
+                const float xx = (-x0 + (float)ix) * (-x0 + (float)ix);
+                const float ra = sqrtf(yy + xx);
+                if (ra > R1 && ra <= R2) {
+                    float edge = (1.0f + cosf(pi * (ra - R1) / 6.0f)) / 2.0f;
+                    v = (float)((double)(v * edge) + (double)(1.0f - edge) * summ);
+                }
+                if (ra > R2) v = (float)summ;
             }
-            if (ra > R2) v = (float)summ;
+            if ((ix + iy) & 1) v = -v;
+            o[i] = make_float2(v, 0.0f);
         }
-        if ((ix + iy) & 1) v = -v;
-        o[i] = make_float2(v, 0.0f);
     }
     if (bad) atomicOr(flag, 1);
 }
@@ -126,14 +144,6 @@ __device__ __forceinline__ int isqrt_floor(int v) {
 __device__ __forceinline__ int isqrt_ceil(int v) {
     const int s = isqrt_floor(v);
     return s * s < v ? s + 1 : s;
-}
-
-// h + l += x with Knuth's TwoSum: the pair holds the running sum to ~2^-48 relative in
-// FP32 arithmetic (GB300's FP64 pipe is far slower than its FP32 pipe)
-__device__ __forceinline__ void two_sum_acc(float& h, float& l, float x) {
-    const float s2 = h + x, bb = s2 - h;
-    l += (h - (s2 - bb)) + (x - bb);
-    h = s2;
 }
 
 // FT_amp_expfit.f90:27-46: per-ring means, log, 2x2 least squares, Fcut.
