@@ -454,9 +454,8 @@ __global__ void __launch_bounds__(256) k_mix_dw(const float* __restrict__ x, con
     float acc[CM], accb[CM];
 #pragma unroll
     for (int o = 0; o < CM; ++o) { acc[o] = 0.f; accb[o] = 0.f; }
-    for (long q = threadIdx.x; q < (long)B * NT; q += blockDim.x) {
-        const long b = q / NT;
-        const int t = (int)(q % NT);
+    const int t = threadIdx.x % NT;  // blockDim is a multiple of NT
+    for (long b = threadIdx.x / NT; b < B; b += blockDim.x / NT) {
         const float v = x[(b * LP_MIXK + k) * NT + t];
 #pragma unroll
         for (int o = 0; o < CM; ++o) {
