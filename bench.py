@@ -23,8 +23,10 @@ on the first 16 particles of the same set, and the two forms' chosen orientation
 compared.
 
 --impl reference times the reference algorithm's CPU restatement (the oracle port of
-the phase-residual search, FP32 in the Fortran's operation order) on all host cores
-over a bounded sample of views of one particle, extrapolated to the full grid.
+the phase-residual search, FP32 in the Fortran's operation order) on every usable host
+core: each step is the complete search of one particle of the same workload (every
+grid view and omega), measured, not extrapolated.  That arm loads no code of this
+package.
 """
 from __future__ import annotations
 
@@ -91,7 +93,7 @@ def _as_tmpl(ci, e):
 
 def make_data(ci, nparticles: int, projector):
     """projector(map, template_records) -> images."""
-    from cryoim_gb300 import synth
+    import synth
     w = WORKLOAD
     rng = np.random.default_rng(w["seed"])
     vol = synth.phantom(w["nx"], w["seed"])
@@ -175,74 +177,149 @@ def asu_views(step: float):
     return np.array(out, np.float32)
 
 
-def cpu_sample(params, tmpl, timgs, img, part, seconds: float = 15.0):
-    """Time the oracle port (FP32) on all host cores over a bounded sample of views of
-    one particle; return particles/s extrapolated to the full view set."""
+def host_cpu() -> dict:
+    """Host cores this process may run on, the machine's count and the CPU model."""
+    try:
+        usable = len(os.sched_getaffinity(0))
+    except Exception:
+        usable = os.cpu_count() or 1
+    model = None
+    try:
+        out = subprocess.run(["lscpu"], capture_output=True, text=True, timeout=10).stdout
+        for line in out.splitlines():
+            if line.split(":")[0].strip() == "Model name":
+                model = line.split(":", 1)[1].strip()
+                break
+    except Exception:
+        pass
+    if model is None:
+        try:
+            for line in open("/proc/cpuinfo"):
+                if line.lower().startswith("model name"):
+                    model = line.split(":", 1)[1].strip()
+                    break
+        except Exception:
+            model = "unknown"
+    return {"threads": usable, "nproc": os.cpu_count(), "cpu_model": model}
+
+
+class CpuSearch:
+    """The reference's global search (ort_globesearch.f90) restated on the CPU: the oracle
+    port in FP32, the Fortran's operation order, one whole particle at a time over every
+    asymmetric-unit view of the grid with OpenMP over views on `threads` host threads,
+    then minloc.  Templates are prepared once (load_template.f90), outside the timing."""
+
+    def __init__(self, pyoracle, params, tmpl, timgs, threads: int):
+        self.orc, self.p, self.tmpl, self.threads = pyoracle, params, tmpl, threads
+        self.tm, self.tf = pyoracle.load_templates(timgs, tmpl, params, "f32")
+        self.views = asu_views(params.searchstep)
+
+    def particle(self, img, part) -> tuple[float, float, float, float]:
+        pr = self.orc.search_views(self.p, self.tm, self.tf, self.tmpl, img, part, self.views,
+                                   nthreads=self.threads, fp="f32")
+        k = int(np.argmin(pr))
+        v, iom = divmod(k, pr.shape[1])
+        return (float(self.views[v, 0]), float(self.views[v, 1]), float(self.p.searchstep * iom),
+                float(pr.flat[k]))
+
+
+def cpu_sample(params, tmpl, timgs, imgs, parts, particles: int = 2):
+    """cpu_baseline of the GPU arm: `particles` whole particles of the same workload
+    searched by the oracle port on every usable host core (about 10-20 s), and one
+    particle on one thread (the reference's own single-threaded execution model)."""
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import pyoracle
-    tm, tf = pyoracle.load_templates(timgs, tmpl, params, "f32")
-    views = asu_views(params.searchstep)
-    nthr = pyoracle.num_threads()
+    host = host_cpu()
+    cs = CpuSearch(pyoracle, params, tmpl, timgs, host["threads"])
+    n = min(particles, len(parts))
     t0 = time.perf_counter()
-    pyoracle.search_views(params, tm, tf, tmpl, img, part, views[:nthr], nthreads=nthr, fp="f32")
-    t1 = time.perf_counter() - t0
-    nv = int(min(len(views), max(nthr, nthr * max(1, int(seconds / max(t1, 1e-3))))))
-    t0 = time.perf_counter()
-    pyoracle.search_views(params, tm, tf, tmpl, img, part, views[:nv], nthreads=nthr, fp="f32")
+    for i in range(n):
+        cs.particle(imgs[i], parts[i])
     dt = time.perf_counter() - t0
-    pps = (nv / len(views)) / dt
-    # the reference's own execution model: one thread
-    n1 = min(len(views), 4)
+    cs1 = CpuSearch(pyoracle, params, tmpl, timgs, 1)
     t0 = time.perf_counter()
-    pyoracle.search_views(params, tm, tf, tmpl, img, part, views[:n1], nthreads=1, fp="f32")
-    pps1 = (n1 / len(views)) / (time.perf_counter() - t0)
-    return pps, {"cores": nthr, "kind": "port", "views": nv, "views_total": len(views), "seconds": dt,
-                 "value_1thread": pps1,
-                 "sample": f"1 particle x {nv}/{len(views)} ASU views (x {len(tmpl)} templates, "
-                           f"Nomega {int(360 / params.searchstep)}) of the phase-residual search, oracle "
-                           f"FP32 port, OpenMP over views on all host cores, extrapolated to the full grid"}
+    cs1.particle(imgs[0], parts[0])
+    dt1 = time.perf_counter() - t0
+    return n / dt, {"cores": host["threads"], "kind": "port", "nproc": host["nproc"],
+                    "cpu_model": host["cpu_model"], "seconds": dt, "value_1thread": 1.0 / dt1,
+                    "sample": f"{n} whole particles of the workload ({len(cs.views)} ASU views x "
+                              f"{int(round(360 / params.searchstep))} omega x {len(tmpl)} templates each), "
+                              f"the oracle's FP32 port of ort_globesearch, OpenMP over views on "
+                              f"{host['threads']} host threads; value_1thread: one particle on one thread"}
 
 
-def config_dict(params, batch, learn_samples=None):
+def config_dict(params):
+    """The workload (identical in both arms): sizes of the box-256 global search."""
     w = WORKLOAD
     return {"workload": "icos global search, box 256, 1-deg ASU grid x 625 origins (10k-particle "
                         "production configuration shapes)",
             "box": w["nx"], "apix": w["apix"], "band_A": [w["min_res"], w["max_res"]],
             "minR": params.min_r, "maxR": params.max_r, "searchstep_deg": w["searchstep"],
-            "origins": f"+-{w['origin']} px @ {w['origin_step']} px", "topk_rescored": w["topk"],
-            "templates": w["ntemplates"], "particles_per_step": batch, "snr": w["snr"],
-            "form": "BF16 contraction over the neighbourhoods (+-2 steps) of the learned proposer's "
-                    f"{w['learned']} cells per particle",
+            "origins": f"+-{w['origin']} px @ {w['origin_step']} px", "templates": w["ntemplates"],
+            "snr": w["snr"], "defocus_um": list(w["df"]), "astigmatism_um": w["astig"]}
+
+
+def form_dict(batch, learn_samples):
+    w = WORKLOAD
+    return {"form": "BF16 contraction over the neighbourhoods (+-2 steps) of the learned proposer's "
+                    f"{w['learned']} cells per particle, top-{w['topk']} rescored (FP64 CC, phase residual)",
+            "particles_per_step": batch,
             "section_build": f"per map, charged pro rata per particle of a {w['cycle_particles']}-particle cycle",
             "learned_proposer": (f"trained on {learn_samples} rendered projections per map, the training time "
-                                 f"charged pro rata per particle of a {w['cycle_particles']}-particle cycle")
-                                if learn_samples else "the reference CPU path has none",
+                                 f"charged pro rata per particle of a {w['cycle_particles']}-particle cycle"),
             "pass_lanes": LANES, "l2": "flushed (256 MiB write) before every timed step"}
 
 
 def run_reference(args):
+    """The reference's CPU path on this host: each step searches one whole particle of
+    the box-256 workload (every grid view and omega, 20 templates) with the oracle's FP32
+    port of ort_globesearch.f90 on every usable host core.  Nothing of this package is
+    imported: parameters and records come from the oracle's restatement, the synthetic
+    data from synth (numpy)."""
     r, w, _ = rank_env()
     if r != 0:
         return 0
-    import cryoim_gb300 as ci
-    from cryoim_gb300 import synth
-    params = make_params(ci)
-    proj = lambda v, t: synth.project_fourier(v, np.stack([t["theta"], t["phi"], t["omega"]], 1))
-    vol, tmpl, timgs, imgs, parts, truth = make_data(ci, 1, proj)
-    vals, info = [], None
-    for k in range(args.warmup + args.steps):
-        pps, info = cpu_sample(params, tmpl, timgs, imgs[0], parts[0], seconds=args.ref_seconds)
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import pyoracle
+    import synth
+    wl = WORKLOAD
+    params = pyoracle.default_params(wl["nx"], apix=wl["apix"], minRes=wl["min_res"], maxRes=wl["max_res"],
+                                     searchstep=wl["searchstep"], ampwg=wl["ampwg"],
+                                     imgmask=(wl["nx"] // 2 - 2) * wl["apix"])
+    ops = pyoracle.icos_ops("f32")
+    nsteps = args.warmup + args.steps
+    rng = np.random.default_rng(wl["seed"])
+    vol = synth.phantom(wl["nx"], wl["seed"], ops)
+    te = synth.random_asu_orientations(wl["ntemplates"], rng)
+    tmpl = np.zeros(wl["ntemplates"], pyoracle.TEMPLATE_DTYPE)
+    tmpl["particle_id"] = np.arange(1, wl["ntemplates"] + 1)
+    tmpl["theta"], tmpl["phi"], tmpl["omega"] = te[:, 0], te[:, 1], te[:, 2]
+    timgs = synth.project_fourier(vol, te)
+    imgs, parts, truth = synth.make_particles(
+        vol, nsteps, wl["seed"] + 1, synth.project_fourier, wl["apix"], dtype=pyoracle.PARTICLE_DTYPE,
+        df_range=wl["df"], astig_max=wl["astig"], origin_max=wl["origin"], snr=wl["snr"], ampwg=wl["ampwg"])
+    host = host_cpu()
+    cs = CpuSearch(pyoracle, params, tmpl, timgs, host["threads"])
+    times = []
+    for k in range(nsteps):
+        t0 = time.perf_counter()
+        cs.particle(imgs[k], parts[k])
         if k >= args.warmup:
-            vals.append(pps)
-    v = float(np.mean(vals))
+            times.append(time.perf_counter() - t0)
+    ms = 1000.0 * float(np.mean(times))
+    v = 1000.0 / ms
+    sample = (f"1 whole particle per step ({len(cs.views)} ASU views x {int(round(360 / params.searchstep))} "
+              f"omega x {wl['ntemplates']} templates), {args.steps} timed particles, the oracle's FP32 port "
+              f"of ort_globesearch, OpenMP over views on {host['threads']} host threads")
     line = {"impl": "reference", "metric": METRIC, "value": v, "unit": "particles/s", "n_gpus": args.gpus,
-            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000.0 / v,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
-            "data": "synthetic", "config": config_dict(params, 1),
-            "cpu_baseline": {"value": v, "unit": "particles/s", "cores": info["cores"], "kind": info["kind"],
-                             "value_1thread": info["value_1thread"],
-                             "sample": info["sample"]},
-            "e2e": {"value": v, "unit": "particles/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+            "data": "synthetic (seeded phantom, CTF, noise)", "config": config_dict(params),
+            "particles_per_step": 1, "form": "the reference's phase-residual global search (CPU)",
+            "cpu_baseline": {"value": v, "unit": "particles/s", "cores": host["threads"], "kind": "port",
+                             "nproc": host["nproc"], "cpu_model": host["cpu_model"], "sample": sample},
+            "e2e": {"value": v, "unit": "particles/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+            "product_modules_loaded": sorted(m for m in sys.modules if m.startswith("cryoim_gb300"))}
     print(json.dumps(line))
     return 0
 
@@ -250,7 +327,7 @@ def run_reference(args):
 def run_ours(args):
     import torch
     import cryoim_gb300 as ci
-    from cryoim_gb300 import synth
+    import synth
     r, world, lr = rank_env()
     dev = lr if torch.cuda.device_count() > 1 else 0
     torch.cuda.set_device(dev)
@@ -494,8 +571,11 @@ def run_ours(args):
     s_ins = sum(1 for ky in range(-R, R + 1) for hx in range(R + 1) if hx * hx + ky * ky <= R * R)
     slice_bytes = st0["orientations"] * st0["kpad"] * 2 + (2 * R + 3) ** 3 * 8 if st0["orientations"] else 0
     ach = gst["gemm_flops"] / max(gst["gemm_ms"], 1e-9) / 1e9  # TFLOP/s of the grouped fine contraction
+    # k_pr_omega: every launch of the npr-particle call summed (a launch covers a batch of
+    # up to 64 particles), so the FLOPs are those of all npr particles
     pr_avg = kms / max(klaunch, 1)
-    pr_achieved = terms * npr * FLOPS_PER_TERM / (pr_avg / 1000.0) / 1e12
+    pr_terms_per_s = terms * npr / (kms / 1000.0)
+    pr_achieved = pr_terms_per_s * FLOPS_PER_TERM / 1e12
 
     def gemm_roofline(g, peak, kernel, src_note):
         a = g["gemm_flops"] / max(g["gemm_ms"], 1e-9) / 1e9
@@ -510,7 +590,7 @@ def run_ours(args):
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_eff / args.steps,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "bf16",
             "data": "synthetic (seeded phantom, CTF, noise; see bench.py docstring)",
-            "config": config_dict(params, B, args.learn_samples),
+            "config": config_dict(params), **form_dict(B, args.learn_samples),
             "e2e": {"value": e2e, "unit": "particles/s", "h2d_bytes_per_step": int(imgs[:B].nbytes + B * 32),
                     "d2h_bytes_per_step": int(B * (w["topk"] * 16 + 8))},
             "gpu_launches": LAUNCHES_PER_PASS * passes * args.steps,
@@ -541,7 +621,9 @@ def run_ours(args):
                           "roofline": {"bound": "fp32", "kernel": "k_pr_omega", "achieved": pr_achieved,
                                        "peak": FP32_PEAK_TFLOPS_NOMINAL, "unit": "TFLOP/s",
                                        "frac": pr_achieved / FP32_PEAK_TFLOPS_NOMINAL,
-                                       "terms_per_particle": terms, "avg_launch_ms": pr_avg,
+                                       "terms_per_particle": terms, "terms_per_s": pr_terms_per_s,
+                                       "avg_launch_ms": pr_avg, "launches": klaunch,
+                                       "kernel_ms_total": kms,
                                        "peak_source": "nominal FP32 FMA rate (no measured non-tensor FP32 peak)"}},
             "bf16_exhaustive_form": {"value": bf_v, "unit": "particles/s",
                                      "identical_orientation_vs_fp32_form": agree(bf_q),
@@ -608,12 +690,10 @@ def run_ours(args):
                                                         "fp32_form": float(np.median(e_p))}},
             "clocks": clk.summary()}
     if not args.no_cpu_baseline:
-        pps, info = cpu_sample(params, tmpl, timgs, imgs[0], parts[0], seconds=args.ref_seconds)
+        pps, info = cpu_sample(params, tmpl, timgs, imgs, parts)
         line["cpu_baseline"] = {"value": pps, "unit": "particles/s", "cores": info["cores"],
-                                "kind": info["kind"], "sample": info["sample"],
-                                "value_1thread": info["value_1thread"],
-                                "note_1thread": "same port on one thread (the reference is single-threaded), "
-                                                "4 views extrapolated"}
+                                "kind": info["kind"], "sample": info["sample"], "nproc": info["nproc"],
+                                "cpu_model": info["cpu_model"], "value_1thread": info["value_1thread"]}
     print(json.dumps(line))
     ctx.close()
     return 0
@@ -665,7 +745,7 @@ def run_precision_report(args):
     drop-in form, itself held to the FP64 oracle by the parity tests) and throughput."""
     import torch
     import cryoim_gb300 as ci
-    from cryoim_gb300 import synth
+    import synth
     r, world, lr = rank_env()
     if r != 0:
         return 0
@@ -757,7 +837,6 @@ def main():
     ap.add_argument("--origin-step", type=float, default=None,
                     help="override the 0.5 px origin step (small cases for profiler captures only)")
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
-    ap.add_argument("--ref-seconds", type=float, default=15.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--profile-case", choices=["learned", "exhaustive-bf16", "exhaustive-fp8", "fp32"],
                     default=None, help="instead of the bench line: a small case for profiler captures")

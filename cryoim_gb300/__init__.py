@@ -356,6 +356,29 @@ class Context:
         call("cryoim_local_refine", self._h, C.byref(lp), ptr(m), ptr(im), ptr(lparts), len(lparts))
 
     # -- mode 3 ---------------------------------------------------------------
+    def local_box_extract(self, imgs, parts: np.ndarray, sym: np.ndarray, loc, apix: float, sub: int,
+                          pr_threshold: float = 90.0, boundx: float = 100.0, d_out: int | None = None,
+                          fftsize: int | None = None):
+        """local_box's sub-image stack mode: (sub images (K, sub, sub) float32 or None when
+        written to the device pointer d_out, sub-particle records (LOCAL_PARTICLE_DTYPE)).
+        imgs: host array (P, n, n) or a device pointer (int, with fftsize)."""
+        p = np.ascontiguousarray(parts, dtype=PARTICLE_DTYPE)
+        s = np.ascontiguousarray(sym, dtype=np.float32).reshape(-1, 3, 3)
+        out = np.zeros(len(p) * len(s), _abi.LOCAL_PARTICLE_DTYPE)
+        n = C.c_int32()
+        if isinstance(imgs, int):
+            assert d_out is not None and fftsize is not None
+            call("cryoim_local_box_extract_device", self._h, C.c_void_p(imgs), ptr(p), len(p), int(fftsize), ptr(s),
+                 len(s), float(loc[0]), float(loc[1]), float(loc[2]), float(apix), int(sub), float(pr_threshold),
+                 float(boundx), C.c_void_p(d_out), ptr(out), C.byref(n))
+            return None, out[: n.value].copy()
+        im = np.ascontiguousarray(imgs, dtype=np.float32)
+        so = np.zeros((len(p) * len(s), sub, sub), np.float32)
+        call("cryoim_local_box_extract", self._h, ptr(im), ptr(p), len(p), im.shape[-1], ptr(s), len(s),
+             float(loc[0]), float(loc[1]), float(loc[2]), float(apix), int(sub), float(pr_threshold), float(boundx),
+             ptr(so), ptr(out), C.byref(n))
+        return so[: n.value].copy(), out[: n.value].copy()
+
     def center(self, imgs, parts: np.ndarray, map3d=None) -> None:
         """Origin centring (calc_center.f90 against map3d, or calc_center_selfrot180.f90
         without); parts is updated in place."""

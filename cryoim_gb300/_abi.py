@@ -137,6 +137,10 @@ SIGNATURES = {
     "cryoim_local_params_default": [_vp, _i32, _i32],
     "cryoim_local_params_derive": [_vp],
     "cryoim_local_refine": [_vp, _vp, _vp, _vp, _vp, _i32],
+    "cryoim_local_box_extract": [_vp, _vp, _vp, _i32, _i32, _vp, _i32, _f32, _f32, _f32, _f32, _i32, _f32, _f32,
+                                 _vp, _vp, _ip],
+    "cryoim_local_box_extract_device": [_vp, _vp, _vp, _i32, _i32, _vp, _i32, _f32, _f32, _f32, _f32, _i32, _f32,
+                                        _f32, _vp, _vp, _ip],
     "cryoim_local_ort_read": [C.c_char_p, _i32, _i32, _vp, _vp, _i32],
     "cryoim_local_ort_write": [C.c_char_p, _vp, _vp, _i32, _i32, _i32, _i32],
     "cryoim_learn_opts_default": [_vp],

@@ -2937,6 +2937,116 @@ static void local_cent11(const float* s, float dang, float dtran, float* c) {
     c[5 * 9 + 2] = s[2] - dang;  c[5 * 10 + 2] = s[2] + dang;
 }
 
+// loc_box.f90:34-91: whole images shifted to centre on the GPU (checkerboard, batched
+// cuFFT, phase ramp, inverse), sub-images cut and normalised by k_lb_cut; the geometry
+// (equivalent orientations, box corners) on the host in the reference's FP32 order.
+static int local_box_extract_impl(Ctx* c, const float* imgs, bool dev_in, const cryoim_particle* parts, int P,
+                                  int nx0, const float* sym, int nsym, float lx, float ly, float lz, float apix,
+                                  int sub, float prt, float bx, float* sub_out, bool dev_out,
+                                  cryoim_local_particle* out, int32_t* nout) {
+    if (!c || !imgs || !parts || !sym || !sub_out || !out || !nout || P < 0)
+        return fail(CRYOIM_ERR_ARG, "null input or negative count");
+    if (nx0 < 8 || (nx0 & 1) || nx0 > 8192 || sub < 2 || sub > nx0 || nsym < 1 || nsym > 4096)
+        return fail(CRYOIM_ERR_SIZE, "fftsize %d, sub_FFTsize %d, nsym %d unsupported", nx0, sub, nsym);
+    *nout = 0;
+    if (P == 0) return CRYOIM_OK;
+    CK(cudaSetDevice(c->device));
+    std::vector<cryoim_local_particle> rec((size_t)P * nsym);
+    std::vector<int> src((size_t)P * nsym);
+    const int K = local_box_stack_geometry(parts, P, sym, nsym, lx, ly, lz, apix, nx0, sub, prt, bx, rec.data(),
+                                           src.data());
+    if (K == 0) return CRYOIM_OK;
+    const long nn0 = (long)nx0 * nx0, ns = (long)sub * sub;
+    // chunks of B selected particles: complex work rows and (host paths) staging within
+    // about 512 MB each
+    const long cap = 512L << 20;
+    const int B = (int)std::max(1L, std::min(64L, std::min(cap / (nn0 * 8), cap / (std::max(1L, ns * nsym) * 4))));
+    DBuf<float2> work;
+    DBuf<float> dimg, dsub, dxy;
+    DBuf<int> dsrc, dhk;
+    int r;
+    if ((r = work.ensure((size_t)B * nn0)) || (r = dxy.ensure(2 * (size_t)B)) || (r = dsrc.ensure(B)) ||
+        (r = dhk.ensure(3 * (size_t)B * nsym)))
+        return r;
+    if (!dev_in && (r = dimg.ensure((size_t)B * nn0))) return r;
+    if (!dev_out && (r = dsub.ensure((size_t)B * nsym * ns))) return r;
+    cufftHandle plan = 0;
+    int plan_n = 0;
+    std::vector<int> hsrc(B), hhk(3 * (size_t)B * nsym);
+    std::vector<float> hxy(2 * (size_t)B);
+    int k = 0;
+    int rc = CRYOIM_OK;
+    while (k < K && rc == CRYOIM_OK) {
+        // the records of the next nb selected particles: k .. k1
+        int nb = 0, k1 = k;
+        while (k1 < K && nb < B) {
+            const int i = src[k1];
+            hsrc[nb] = dev_in ? i : nb;
+            hxy[2 * nb] = -parts[i].x;
+            hxy[2 * nb + 1] = -parts[i].y;
+            for (; k1 < K && src[k1] == i; ++k1) {
+                hhk[3 * (k1 - k)] = rec[k1].local_hx0;
+                hhk[3 * (k1 - k) + 1] = rec[k1].local_ky0;
+                hhk[3 * (k1 - k) + 2] = nb;
+            }
+            if (!dev_in)
+                CK(cudaMemcpyAsync(dimg.p + (size_t)nb * nn0, imgs + (size_t)i * nn0, sizeof(float) * nn0,
+                                   cudaMemcpyHostToDevice, c->stream));
+            ++nb;
+        }
+        const int nk = k1 - k;
+        CK(cudaMemcpyAsync(dsrc.p, hsrc.data(), sizeof(int) * nb, cudaMemcpyHostToDevice, c->stream));
+        CK(cudaMemcpyAsync(dxy.p, hxy.data(), sizeof(float) * 2 * nb, cudaMemcpyHostToDevice, c->stream));
+        CK(cudaMemcpyAsync(dhk.p, hhk.data(), sizeof(int) * 3 * nk, cudaMemcpyHostToDevice, c->stream));
+        if (plan_n != nb) {
+            if (plan) cufftDestroy(plan);
+            plan = 0;
+            int dims[2] = {nx0, nx0};
+            cufftResult fr = cufftPlanMany(&plan, 2, dims, nullptr, 1, 0, nullptr, 1, 0, CUFFT_C2C, nb);
+            if (fr == CUFFT_SUCCESS) fr = cufftSetStream(plan, c->stream);
+            if (fr != CUFFT_SUCCESS) { rc = fail(CRYOIM_ERR_CUDA, "2D FFT plan: cufft %d", (int)fr); break; }
+            plan_n = nb;
+        }
+        launch_lb_checker(dev_in ? imgs : dimg.p, nx0, dsrc.p, nb, work.p, c->stream);
+        cufftResult fr = cufftExecC2C(plan, (cufftComplex*)work.p, (cufftComplex*)work.p, CUFFT_FORWARD);
+        if (fr == CUFFT_SUCCESS) {
+            launch_lb_phase(work.p, nx0, dxy.p, nb, c->stream);
+            fr = cufftExecC2C(plan, (cufftComplex*)work.p, (cufftComplex*)work.p, CUFFT_INVERSE);
+        }
+        if (fr != CUFFT_SUCCESS) { rc = fail(CRYOIM_ERR_CUDA, "2D FFT: cufft %d", (int)fr); break; }
+        float* dst = dev_out ? sub_out + (size_t)k * ns : dsub.p;
+        launch_lb_cut(work.p, nx0, dhk.p, nk, sub, dst, c->stream);
+        cudaError_t e = cudaGetLastError();
+        if (e == cudaSuccess && !dev_out)
+            e = cudaMemcpyAsync(sub_out + (size_t)k * ns, dsub.p, sizeof(float) * nk * ns, cudaMemcpyDeviceToHost,
+                                c->stream);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+        if (e != cudaSuccess) { rc = fail(CRYOIM_ERR_CUDA, "local_box extraction: %s", cudaGetErrorString(e)); break; }
+        k = k1;
+    }
+    if (plan) cufftDestroy(plan);
+    if (rc != CRYOIM_OK) return rc;
+    std::memcpy(out, rec.data(), sizeof(cryoim_local_particle) * K);
+    *nout = K;
+    return CRYOIM_OK;
+}
+
+int cryoim_local_box_extract(void* ctx, const float* imgs, const cryoim_particle* parts, int32_t P, int32_t fftsize,
+                             const float* sym, int32_t nsym, float loc_x, float loc_y, float loc_z, float apix,
+                             int32_t sub_fftsize, float pr_threshold, float boundx, float* sub_imgs,
+                             cryoim_local_particle* out, int32_t* nout) {
+    return local_box_extract_impl(as_ctx(ctx), imgs, false, parts, P, fftsize, sym, nsym, loc_x, loc_y, loc_z,
+                                  apix, sub_fftsize, pr_threshold, boundx, sub_imgs, false, out, nout);
+}
+
+int cryoim_local_box_extract_device(void* ctx, const float* d_imgs, const cryoim_particle* parts, int32_t P,
+                                    int32_t fftsize, const float* sym, int32_t nsym, float loc_x, float loc_y,
+                                    float loc_z, float apix, int32_t sub_fftsize, float pr_threshold, float boundx,
+                                    float* d_sub_imgs, cryoim_local_particle* out, int32_t* nout) {
+    return local_box_extract_impl(as_ctx(ctx), d_imgs, true, parts, P, fftsize, sym, nsym, loc_x, loc_y, loc_z,
+                                  apix, sub_fftsize, pr_threshold, boundx, d_sub_imgs, true, out, nout);
+}
+
 int cryoim_local_refine(void* ctx, const cryoim_local_params* lp, const float* map3d, const float* imgs,
                         cryoim_local_particle* parts, int32_t P) {
     Ctx* c = as_ctx(ctx);

@@ -266,12 +266,13 @@ int cryoim_local_ort_read(const char* path, int32_t first, int32_t last, cryoim_
     return rc;
 }
 
-// format 900 of local_box/SRC/loc_box_coordinate.f90:46 (23 columns) or format 901 of
-// local_refine/SRC/refine_PR.f90:246-253 (28 columns; its PR column is local_PR).
+// format 900 of local_box/SRC/loc_box_coordinate.f90:46 (23 columns), format 901 of
+// local_refine/SRC/refine_PR.f90:246-253 (28 columns; its PR column is local_PR), or
+// format 900 of local_box/SRC/loc_box.f90:93 (14 columns: the sub-image stack mode).
 int cryoim_local_ort_write(const char* path, const cryoim_local_particle* parts, const char* stck,
                            int32_t stck_len, int32_t n, int32_t columns, int32_t append) {
     if (!path || (!parts && n > 0) || n < 0 || (stck && stck_len < 1)) return CRYOIM_ERR_ARG;
-    if (columns != 23 && columns != 28) return CRYOIM_ERR_ARG;
+    if (columns != 23 && columns != 28 && columns != 14) return CRYOIM_ERR_ARG;
     FILE* f = std::fopen(path, append ? "a" : "w");
     if (!f) return CRYOIM_ERR_IO;
     std::string s;
@@ -280,6 +281,18 @@ int cryoim_local_ort_write(const char* path, const cryoim_local_particle* parts,
         const cryoim_local_particle& q = parts[i];
         s.clear();
         put_a(s, stck ? stck + (size_t)i * stck_len : "", 64);
+        if (columns == 14) {  // (a64,i8,f10.4 x 6,i12,i6,f10.4 x 3,f12.4)
+            put_i(s, q.particle_id, 8);
+            for (float v : {q.local_theta0, q.local_phi0, q.local_omega0, q.local_x0, q.local_y0, q.pr})
+                put_f(s, v, 10, 4);
+            put_i(s, q.img_id, 12);
+            put_i(s, q.local_img_id, 6);
+            for (float v : {q.df1, q.df2, q.astigang}) put_f(s, v, 10, 4);
+            put_f(s, q.local_z0, 12, 4);
+            s += '\n';
+            std::fputs(s.c_str(), f);
+            continue;
+        }
         put_i(s, q.particle_id, box ? 8 : 9);
         for (float v : {q.theta, q.phi, q.omega, q.x, q.y}) put_f(s, v, 10, 4);
         put_f(s, box ? q.pr : q.local_pr, 10, 4);

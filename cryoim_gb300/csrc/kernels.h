@@ -14,6 +14,8 @@
 #include <cuda_runtime.h>
 #include <cstdint>
 
+#include "../../include/cryoim.h"
+
 namespace cryoim {
 
 struct Band {
@@ -289,6 +291,18 @@ void launch_norm(float* img, int nx, int B, cudaStream_t st);
 void launch_cross_power(float2* f1, const float2* f2, int nx, long n, cudaStream_t st);
 void launch_rot180(float* a1, float* a2, int nx, long n, cudaStream_t st);
 void launch_peak(const float2* cc, int nx, int B, int half, float* out, cudaStream_t st);
+
+// ---- local.cu: local_box's sub-image stack mode (loc_box.f90) -----------------
+// work[b] = checkerboard x imgs[src[b]] as complex rows (B whole images of nx0^2)
+void launch_lb_checker(const float* imgs, int nx0, const int* src, int B, float2* work, cudaStream_t st);
+// the forward transform's 1/N^2 and the phase ramp of the shift xy[b] = (x, y)
+void launch_lb_phase(float2* work, int nx0, const float* xy, int B, cudaStream_t st);
+// n sub-images: hk[k] = (hx0, ky0, slot of the inverse-transformed image), normalised
+void launch_lb_cut(const float2* work, int nx0, const int* hk, int n, int sub, float* out, cudaStream_t st);
+// host geometry (local_host.cpp): records and source particle per (particle, rotation)
+int local_box_stack_geometry(const cryoim_particle* parts, int P, const float* sym, int nsym, float loc_x,
+                             float loc_y, float loc_z, float apix, int nx0, int sub, float pr_threshold,
+                             float boundx, cryoim_local_particle* out, int* src);
 
 // ---- local.cu: local_refine's sub-particle refinement ------------------------
 cudaError_t launch_local_softmask(float* map, int nx, float mask, double* acc2, cudaStream_t st);

@@ -262,6 +262,68 @@ __global__ void __launch_bounds__(256) k_local_pr(const float* __restrict__ cand
     if (threadIdx.x == 0) out[(long)p * C + c] = s2 > 1.0e-10 ? (float)(s1 / s2) * 180.0f / pi : 1000.0f;
 }
 
+// ---- local_box's sub-image stack mode (loc_box.f90:34-91) ----------------------
+// The whole image with the checkerboard of img2d_centshift.f90, as a complex row.
+__global__ void k_lb_checker(const float* __restrict__ imgs, int nx0, const int* __restrict__ src,
+                             float2* __restrict__ work) {
+    const long nn0 = (long)nx0 * nx0;
+    const long t = (long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= nn0) return;
+    const int ky = (int)(t / nx0), hx = (int)(t - (long)ky * nx0);
+    const float v = imgs[(long)src[blockIdx.y] * nn0 + t];
+    work[(long)blockIdx.y * nn0 + t] = make_float2(((hx + ky) & 1) ? -v : v, 0.0f);
+}
+// img2d_centshift.f90:21-32 on the forward transform: the 1/N^2 of the forward FFT
+// (FFTW.f90:185), then F exp(-i phase), phase = 2 pi (x hx + y ky) / N at the shift
+// (x, y) = (-particle x, -particle y).
+__global__ void k_lb_phase(float2* __restrict__ work, int nx0, const float* __restrict__ xy, float pi) {
+    const long nn0 = (long)nx0 * nx0;
+    const long t = (long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= nn0) return;
+    const int ky = (int)(t / nx0) - nx0 / 2, hx = (int)(t - (long)(t / nx0) * nx0) - nx0 / 2;
+    const float x = xy[2 * blockIdx.y], y = xy[2 * blockIdx.y + 1];
+    const float2 f = work[(long)blockIdx.y * nn0 + t];
+    const float a = f.x / (float)nn0, b = f.y / (float)nn0;
+    const float phase = 2.0f * pi * (x * (float)hx + y * (float)ky) / (float)nx0;
+    const float c = cosf(phase), sn = sinf(phase);
+    work[(long)blockIdx.y * nn0 + t] = make_float2(a * c + b * sn, -a * sn + b * c);
+}
+// loc_box.f90:60-79: one CTA per sub-image, the sub x sub box from pixel (hx0, ky0) of
+// the centred image (the real part of the inverse transform times the checkerboard),
+// wrapped at the edges, then img2d_norm.f90 of the box with FP32 TwoSum sums combined
+// in FP64.  img2d_norm of the whole image before the cut (loc_box.f90:47) is an affine
+// map with positive scale, which the box's own normalisation removes, so it is not
+// applied.  hk[k] = (hx0, ky0, image slot).
+__global__ void k_lb_cut(const float2* __restrict__ work, int nx0, const int* __restrict__ hk, int sub,
+                         float* __restrict__ out) {
+    __shared__ double sh[32];
+    const long nn0 = (long)nx0 * nx0, ns = (long)sub * sub;
+    const int hx0 = hk[3 * blockIdx.x], ky0 = hk[3 * blockIdx.x + 1], slot = hk[3 * blockIdx.x + 2];
+    const float2* w = work + (long)slot * nn0;
+    auto pix = [&](long t) {
+        const int ty = (int)(t / sub);
+        int hx = (int)(t - (long)ty * sub) + hx0, ky = ty + ky0;
+        hx %= nx0;
+        if (hx < 0) hx += nx0;
+        ky %= nx0;
+        if (ky < 0) ky += nx0;
+        const float v = w[(long)ky * nx0 + hx].x;
+        return ((hx + ky) & 1) ? -v : v;
+    };
+    float h = 0.f, l = 0.f;
+    for (long t = threadIdx.x; t < ns; t += blockDim.x) two_sum_acc(h, l, pix(t));
+    const float avg = (float)(bsum((double)h + (double)l, sh) / (double)ns);
+    h = 0.f;
+    l = 0.f;
+    for (long t = threadIdx.x; t < ns; t += blockDim.x) {
+        const float d = pix(t) - avg;
+        two_sum_acc(h, l, d * d);
+    }
+    const float nd = (float)sqrt(bsum((double)h + (double)l, sh) / (double)ns);
+    float* o = out + (long)blockIdx.x * ns;
+    for (long t = threadIdx.x; t < ns; t += blockDim.x) o[t] = (pix(t) - avg) / nd;
+}
+
 }  // namespace
 
 cudaError_t launch_local_softmask(float* map, int nx, float mask, double* acc2, cudaStream_t st) {
@@ -304,6 +366,20 @@ void launch_local_pr(const float* cand, int C, const float* fr, const float* fi,
     dim3 g(C, B);
     const Angles an = host_angles();
     k_local_pr<<<g, 256, 0, st>>>(cand, C, fr, fi, nx, part, ctf, max_r, an.deg2rad, an.pi, out);
+}
+
+void launch_lb_checker(const float* imgs, int nx0, const int* src, int B, float2* work, cudaStream_t st) {
+    dim3 g(cdiv((long)nx0 * nx0, 256), B);
+    k_lb_checker<<<g, 256, 0, st>>>(imgs, nx0, src, work);
+}
+
+void launch_lb_phase(float2* work, int nx0, const float* xy, int B, cudaStream_t st) {
+    dim3 g(cdiv((long)nx0 * nx0, 256), B);
+    k_lb_phase<<<g, 256, 0, st>>>(work, nx0, xy, host_angles().pi);
+}
+
+void launch_lb_cut(const float2* work, int nx0, const int* hk, int n, int sub, float* out, cudaStream_t st) {
+    if (n > 0) k_lb_cut<<<n, 512, 0, st>>>(work, nx0, hk, sub, out);
 }
 
 }  // namespace cryoim

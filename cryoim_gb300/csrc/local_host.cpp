@@ -199,6 +199,78 @@ int cryoim_local_box_coordinates(const cryoim_particle* parts, int32_t P, const 
     return CRYOIM_OK;
 }
 
+}  // extern "C"
+
+namespace cryoim {
+
+// loc_box.f90:43-88 (the sub-image stack mode), geometry only: for every selected
+// particle (load_ort.f90:30-34) and rotation s, the equivalent orientation
+// (equalort.f90), the sub-image centre R^T (loc_x, loc_y, loc_z) split into an integer
+// pixel (truncated) and a fraction, and the box's first pixel hx0 + nx0/2 - sub/2.
+// Records as loc_box.f90:86-88 writes them (particle_id = the running sub-particle
+// count, df as read); src[k] = the whole particle of record k.  Returns the count.
+int local_box_stack_geometry(const cryoim_particle* parts, int P, const float* sym, int nsym, float loc_x,
+                             float loc_y, float loc_z, float apix, int nx0, int sub, float pr_threshold,
+                             float boundx, cryoim_local_particle* out, int* src) {
+    const float r2d = 45.0f / std::atan2(1.0f, 1.0f);
+    const float x0[3] = {loc_x, loc_y, loc_z};
+    int k = 0;
+    for (int i = 0; i < P; ++i) {
+        const cryoim_particle& q = parts[i];
+        if (!(q.pr <= pr_threshold && std::fabs(q.x) <= boundx && std::fabs(q.y) <= boundx)) continue;
+        M3 e;
+        eularmatrix(q.theta, q.phi, q.omega, e);
+        for (int s = 0; s < nsym; ++s) {
+            M3 S, r;
+            std::memcpy(S, sym + 9 * s, sizeof(M3));
+            matmul(S, e, r);
+            float th;
+            if (r[2][2] >= 1.0f) th = 0.0f;
+            else if (r[2][2] < -1.0f) th = 180.0f;
+            else th = std::acos(r[2][2]) * r2d;
+            const float ph = std::atan2(r[1][2], r[0][2]) * r2d;
+            const float om = std::atan2(r[2][1], -r[2][0]) * r2d;
+            M3 rot;
+            eularmatrix(th, ph, om, rot);
+            float c[3];
+            for (int a = 0; a < 3; ++a) {
+                float t = rot[0][a] * x0[0];
+                t = t + rot[1][a] * x0[1];
+                t = t + rot[2][a] * x0[2];
+                c[a] = t;
+            }
+            int hx0 = (int)c[0];
+            const float fx = c[0] - (float)hx0;
+            int ky0 = (int)c[1];
+            const float fy = c[1] - (float)ky0;
+            hx0 = hx0 + nx0 / 2 - sub / 2;
+            ky0 = ky0 + nx0 / 2 - sub / 2;
+            cryoim_local_particle& o = out[k];
+            std::memset(&o, 0, sizeof(o));
+            o.particle_id = k + 1;
+            o.img_id = q.img_id;
+            o.img_particle_id = q.img_particle_id;
+            o.theta = q.theta; o.phi = q.phi; o.omega = q.omega; o.x = q.x; o.y = q.y; o.pr = q.pr;
+            o.df1 = q.df1; o.df2 = q.df2; o.astigang = q.astigang;
+            o.local_img_id = s + 1;
+            o.local_hx0 = hx0;
+            o.local_ky0 = ky0;
+            o.local_theta0 = th; o.local_phi0 = ph; o.local_omega0 = om;
+            o.local_x0 = fx;
+            o.local_y0 = fy;
+            o.local_z0 = c[2] * apix;
+            o.local_pr0 = q.pr;
+            src[k] = i;
+            ++k;
+        }
+    }
+    return k;
+}
+
+}  // namespace cryoim
+
+extern "C" {
+
 int cryoim_local_params_default(cryoim_local_params* p, int32_t fftsize, int32_t fftsize0) {
     if (!p || fftsize < 8 || fftsize0 < fftsize) return CRYOIM_ERR_ARG;
     std::memset(p, 0, sizeof(*p));

@@ -321,6 +321,31 @@ int cryoim_local_box_coordinates(const cryoim_particle* parts, int32_t P, const 
                                  float pr_threshold, float boundx, cryoim_local_particle* out,
                                  int32_t* nout);
 
+/* local_box's sub-image stack mode (local_box/SRC/loc_box.f90:34-91, selected by
+ * local_imgstck=): for each selected particle (PR <= pr_threshold, |x|, |y| <= boundx,
+ * load_ort.f90:30-34) of P whole images (imgs: P x fftsize^2 in record order) the image
+ * is shifted to centre (img2d_centshift.f90 of local_box at (-x, -y)); for each of the
+ * nsym rotations (row-major 3x3) the equivalent orientation (equalort.f90) gives the
+ * sub-image centre R^T (loc_x, loc_y, loc_z), and the sub_fftsize^2 box around it is
+ * cut with periodic wrap and normalised (img2d_norm.f90).  Outputs, nsym per selected
+ * particle in particle order: sub_imgs (room for P x nsym x sub_fftsize^2 floats) and
+ * records as loc_box.f90:86-88 writes them: particle_id = the running sub-particle
+ * count (format 900's Nparticle), local_img_id = the rotation index, local_theta0..
+ * local_omega0 = the equivalent orientation, local_x0 / local_y0 = the fractional part
+ * of the centre, local_z0 = its z times apix, local_hx0 / local_ky0 = the box's first
+ * pixel, df1 / df2 / astigang as read (micrometres, degrees).  *nout = record count.
+ * The whole-image normalisation before the cut (loc_box.f90:47) is not applied: the
+ * sub-image normalisation cancels it exactly. */
+int cryoim_local_box_extract(void* ctx, const float* imgs, const cryoim_particle* parts, int32_t P, int32_t fftsize,
+                             const float* sym, int32_t nsym, float loc_x, float loc_y, float loc_z, float apix,
+                             int32_t sub_fftsize, float pr_threshold, float boundx, float* sub_imgs,
+                             cryoim_local_particle* out, int32_t* nout);
+/* The same with device images in and device sub-images out. */
+int cryoim_local_box_extract_device(void* ctx, const float* d_imgs, const cryoim_particle* parts, int32_t P,
+                                    int32_t fftsize, const float* sym, int32_t nsym, float loc_x, float loc_y,
+                                    float loc_z, float apix, int32_t sub_fftsize, float pr_threshold, float boundx,
+                                    float* d_sub_imgs, cryoim_local_particle* out, int32_t* nout);
+
 /* local_refine parameters (local_refine/SRC/0input_parameters.f90:25-55 defaults,
  * 0calc_initialvalue.f90:65-76 derived values). */
 typedef struct cryoim_local_params {
@@ -353,8 +378,9 @@ int cryoim_local_refine(void* ctx, const cryoim_local_params* p, const float* ma
                         cryoim_local_particle* parts, int32_t P);
 
 /* The local orientation files: 23 list-directed columns in, and out either the 23 of
- * local_box (format 900 of loc_box_coordinate.f90:46, columns = 23) or the 28 of
- * local_refine (format 901 of refine_PR.f90:246-253, columns = 28).  stck as in
+ * local_box (format 900 of loc_box_coordinate.f90:46, columns = 23), the 28 of
+ * local_refine (format 901 of refine_PR.f90:246-253, columns = 28) or the 14 of
+ * local_box's sub-image stack mode (format 900 of loc_box.f90:93, columns = 14).  stck as in
  * cryoim_ort_read (stck_len bytes per record, name width 64 on output). */
 int cryoim_local_ort_read(const char* path, int32_t first, int32_t last, cryoim_local_particle* parts,
                           char* stck, int32_t stck_len);

@@ -1604,6 +1604,101 @@ int local_box_coordinates(const cryoim_particle* parts, int P, const float* sym,
     return k;
 }
 
+/* local_box/SRC/loc_box.f90:34-91, the sub-image stack mode: for every selected particle
+ * (load_ort.f90:30-34) the whole image is shifted to centre (img2d_centshift.f90 of
+ * local_box: checkerboard, forward transform /N^2, the phase ramp of (-x, -y), inverse
+ * transform, checkerboard) and normalised (img2d_norm.f90); for each of the nsym
+ * equivalent orientations (equalort.f90) the sub-image centre R^T (lx, ly, lz) is split
+ * into an integer pixel and a fraction, the sub_FFTsize box around it is cut with
+ * periodic wrap (:60-79) and normalised.  imgs: P whole images of nx0^2 in record order;
+ * out: nsym records per selected particle, sub_out: their sub images (sub^2 each).
+ * Record fields as loc_box.f90:86-88 writes them: local_theta0..omega0 the equivalent
+ * orientation, local_x0/y0 the fractions, local_z0 = z * apix, local_img_id the rotation
+ * index, local_hx0/ky0 the box's first pixel (hx0 + nx0/2 - sub/2), particle_id the
+ * running sub-particle count (format 900's Nparticle), df1/df2/astigang as read (um). */
+template <class R>
+int local_box_extract(const float* imgs, const cryoim_particle* parts, int P, int nx0, const float* sym, int nsym,
+                      R lx, R ly, R lz, R apix, int sub, R prthr, R boundx, float* sub_out,
+                      cryoim_local_particle* out) {
+    const R r2d = R(45) / std::atan2(R(1), R(1));
+    const R pi = R(4) * std::atan2(R(1), R(1));
+    const R x0[3] = {lx, ly, lz};
+    const long nn0 = (long)nx0 * nx0, ns = (long)sub * sub;
+    std::vector<R> a(nn0), b(nn0), cut(ns);
+    int k = 0;
+    for (int i = 0; i < P; ++i) {
+        const cryoim_particle& q = parts[i];
+        if (!((R)q.pr <= prthr && std::fabs((R)q.x) <= boundx && std::fabs((R)q.y) <= boundx)) continue;
+        const float* im = imgs + (long)i * nn0;
+        for (long t = 0; t < nn0; ++t) {
+            const int ky = (int)(t / nx0), hx = (int)(t % nx0);
+            a[t] = (R)im[t] * (((hx + ky) & 1) ? R(-1) : R(1));
+            b[t] = 0;
+        }
+        img2d_fft<R>(a.data(), b.data(), nx0, nx0, 1);
+        const R xs = -(R)q.x, ys = -(R)q.y;
+        for (long t = 0; t < nn0; ++t) {
+            b[t] = -b[t];
+            const int ky = (int)(t / nx0) - nx0 / 2, hx = (int)(t % nx0) - nx0 / 2;
+            const R ph = R(2) * pi * (xs * (R)hx + ys * (R)ky) / (R)(float)nx0;
+            const R c = std::cos(ph), sn = std::sin(ph);
+            const R fr = a[t] * c + b[t] * sn, fi = -a[t] * sn + b[t] * c;
+            a[t] = fr;
+            b[t] = fi;
+        }
+        img2d_fft<R>(a.data(), b.data(), nx0, nx0, -1);
+        for (long t = 0; t < nn0; ++t) {
+            const int ky = (int)(t / nx0), hx = (int)(t % nx0);
+            if ((hx + ky) & 1) a[t] = -a[t];
+        }
+        img2d_norm<R>(a.data(), nx0);
+        R e[9];
+        eularmatrix((R)q.theta, (R)q.phi, (R)q.omega, e);
+        for (int s = 0; s < nsym; ++s) {
+            R r[9];
+            for (int u = 0; u < 3; ++u)
+                for (int v = 0; v < 3; ++v)
+                    r[3 * u + v] = (R)sym[9 * s + 3 * u] * e[v] + (R)sym[9 * s + 3 * u + 1] * e[3 + v] +
+                                   (R)sym[9 * s + 3 * u + 2] * e[6 + v];
+            R th = r[8] >= R(1) ? R(0) : (r[8] < R(-1) ? R(180) : std::acos(r[8]) * r2d);
+            R ph = std::atan2(r[5], r[2]) * r2d, om = std::atan2(r[7], -r[6]) * r2d;
+            R rot[9];
+            eularmatrix(th, ph, om, rot);
+            R c[3];
+            for (int u = 0; u < 3; ++u) c[u] = rot[u] * x0[0] + rot[3 + u] * x0[1] + rot[6 + u] * x0[2];
+            int hx0 = fint(c[0]);
+            const R fx = c[0] - (R)hx0;
+            int ky0 = fint(c[1]);
+            const R fy = c[1] - (R)ky0;
+            hx0 = hx0 + nx0 / 2 - sub / 2;
+            ky0 = ky0 + nx0 / 2 - sub / 2;
+            for (long t = 0; t < ns; ++t) {
+                int ky = (int)(t / sub) + ky0, hx = (int)(t % sub) + hx0;
+                if (hx < 0) hx += nx0;
+                if (hx >= nx0) hx -= nx0;
+                if (ky < 0) ky += nx0;
+                if (ky >= nx0) ky -= nx0;
+                cut[t] = a[(long)ky * nx0 + hx];
+            }
+            img2d_norm<R>(cut.data(), sub);
+            for (long t = 0; t < ns; ++t) sub_out[(long)k * ns + t] = (float)cut[t];
+            cryoim_local_particle& o = out[k];
+            std::memset(&o, 0, sizeof(o));
+            o.particle_id = k + 1;
+            o.img_id = q.img_id; o.img_particle_id = q.img_particle_id;
+            o.theta = q.theta; o.phi = q.phi; o.omega = q.omega; o.x = q.x; o.y = q.y; o.pr = q.pr;
+            o.df1 = q.df1; o.df2 = q.df2; o.astigang = q.astigang;
+            o.local_img_id = s + 1; o.local_hx0 = hx0; o.local_ky0 = ky0;
+            o.local_theta0 = (float)th; o.local_phi0 = (float)ph; o.local_omega0 = (float)om;
+            o.local_x0 = (float)fx; o.local_y0 = (float)fy;
+            o.local_z0 = (float)(c[2] * apix);
+            o.local_pr0 = q.pr;
+            ++k;
+        }
+    }
+    return k;
+}
+
 /* local_refine/SRC/getCTF2d.f90 (defocus already in Angstrom). */
 template <class R> void local_ctf2d(int nx, R df1, R df2, R astig0, R apix, R vol, R cs0, R ampwg, R* ctf) {
     get_ctf2d(nx, df1 / R(1.0e4), df2 / R(1.0e4), astig0, apix, vol, cs0, ampwg, ctf);
@@ -1922,6 +2017,11 @@ template <class R> void transform_ort(int to, R* th, R* ph, R* om, int n) {
                                                   R bx, cryoim_local_particle* out) {                  \
         return local_box_coordinates<R>(pa, P, sym, nsym, lx, ly, lz, apix, nx, prt, bx, out);         \
     }                                                                                                  \
+    extern "C" int orc_local_box_extract_##S(const float* im, const cryoim_particle* pa, int P, int nx0, \
+                                              const float* sym, int nsym, R lx, R ly, R lz, R apix,      \
+                                              int sub, R prt, R bx, float* so, cryoim_local_particle* o) { \
+        return local_box_extract<R>(im, pa, P, nx0, sym, nsym, lx, ly, lz, apix, sub, prt, bx, so, o);   \
+    }                                                                                                  \
     extern "C" int orc_local_refine_##S(const cryoim_local_params* p, const float* map,              \
                                          const float* im, cryoim_local_particle* pa, int P) {          \
         return local_refine<R>(p, map, im, pa, P);                                                     \
@@ -1946,4 +2046,44 @@ extern "C" int orc_num_threads(void) {
 #else
     return 1;
 #endif
+}
+
+/* icosprocess/SRC/0initialvalue.f90:26-45: the code defaults for a stack of nx =
+ * fftsize (the keys 0input_parameters.f90 does not set: mode 0, first 1, applyCTF and
+ * imgmask y, the rest n). */
+extern "C" void orc_params_default(cryoim_params* p, int fftsize) {
+    std::memset(p, 0, sizeof(*p));
+    p->fftsize = fftsize;
+    p->first = 1;
+    p->ncycle = 6;
+    p->apply_ctf = 1;
+    p->use_imgmask = 1;
+    p->imgmask = (float)(fftsize / 2 - 2);
+    p->boundx = (float)(fftsize / 2 - 2);
+    p->pr_threshold = 90.0f;
+    p->vol = 300.0f;
+    p->cs = 2.7f;
+    p->ampwg = 0.1f;
+    p->bfactor = 0.0f;
+    p->min_res = 300.0f;
+    p->max_res = 8.0f;
+    p->apix = 1.0f;
+    p->nsym = 60;
+    p->nlin = 60;
+    p->searchstep = 2.0f;
+    p->maxcentshift = 100.0f;
+}
+
+/* icosprocess/SRC/0calc_initialvalues.f90:4-20 (mode != 6, icosahedral symmetry):
+ * resolutions to radii in FP32, maxR rounded up to even, the mask to pixels, and the
+ * refinement steps. */
+extern "C" void orc_params_derive(cryoim_params* p) {
+    float minres = p->apix * (float)p->fftsize / p->min_res;
+    float maxres = p->apix * (float)p->fftsize / p->max_res;
+    p->min_r = (int)minres;
+    p->max_r = (int)maxres;
+    if (p->max_r % 2 != 0) p->max_r += 1;
+    p->imgmask_px = p->use_imgmask ? p->imgmask / p->apix : p->imgmask;
+    p->delta_angle = 360.0f / (maxres * std::sqrt(5.0f) * 3.14159f);
+    p->delta_trans = (float)p->fftsize / (maxres * std::sqrt(5.0f));
 }

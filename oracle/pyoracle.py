@@ -19,6 +19,49 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 LIB = os.path.join(HERE, "_build", "libcryoim_oracle.so")
 _lib = None
 
+# Records and parameters as laid out in include/cryoim.h (the C oracle compiles against
+# that header); the same layouts as the library's, so arrays of either pass to both.
+_PF = ["theta0", "phi0", "omega0", "x0", "y0", "pr0", "df1", "df2", "astigang",
+       "theta", "phi", "omega", "x", "y", "pr", "dtheta", "dphi", "domega", "dx", "dy", "dpr"]
+PARTICLE_DTYPE = np.dtype([("particle_id", "<i4"), ("img_id", "<i4"), ("img_particle_id", "<i4")]
+                          + [(f, "<f4") for f in _PF])
+TEMPLATE_DTYPE = np.dtype([("particle_id", "<i4"), ("theta", "<f4"), ("phi", "<f4"),
+                           ("omega", "<f4"), ("x", "<f4"), ("y", "<f4")])
+_LI = ["particle_id", "img_id", "img_particle_id", "local_img_id", "local_hx0", "local_ky0"]
+_LF = ["theta", "phi", "omega", "x", "y", "pr", "df1", "df2", "astigang",
+       "local_theta0", "local_phi0", "local_omega0", "local_x0", "local_y0", "local_z0", "local_pr0",
+       "local_theta", "local_phi", "local_omega", "local_x", "local_y", "local_z", "local_pr",
+       "local_dtheta", "local_dphi", "local_domega", "local_dx", "local_dy"]
+LOCAL_PARTICLE_DTYPE = np.dtype([(f, "<i4") for f in _LI] + [(f, "<f4") for f in _LF])
+
+
+class Params(C.Structure):
+    """cryoim_params of include/cryoim.h."""
+    _fields_ = [(n, C.c_int32) for n in (
+        "fftsize", "mode", "first", "last", "ncycle", "apply_ctf", "use_imgmask", "realspaceavg",
+        "subrec", "fsc", "imgstck")] + [(n, C.c_float) for n in (
+        "apix", "min_res", "max_res", "imgmask", "vol", "cs", "ampwg", "bfactor", "pr_threshold",
+        "searchstep", "maxcentshift", "boundx")] + [(n, C.c_int32) for n in (
+        "min_r", "max_r", "nsym", "nlin")] + [(n, C.c_float) for n in (
+        "imgmask_px", "delta_angle", "delta_trans")]
+
+
+def default_params(fftsize: int, **kw) -> Params:
+    """0initialvalue.f90 defaults for nx = fftsize, keyword overrides by icosprocess key
+    name (apix, minRes, maxRes, searchstep, ampwg, imgmask, ...), then the derived values
+    of 0calc_initialvalues.f90 (oracle restatement)."""
+    p = Params()
+    lib().orc_params_default(C.byref(p), C.c_int(int(fftsize)))
+    alias = {"minRes": "min_res", "maxRes": "max_res", "applyCTF": "apply_ctf", "Cs": "cs",
+             "PR_threshold": "pr_threshold", "boundX": "boundx", "Ncycle": "ncycle", "Bfactor": "bfactor"}
+    for k, v in kw.items():
+        k = alias.get(k, k)
+        if not hasattr(p, k):
+            raise KeyError(k)
+        setattr(p, k, v)
+    lib().orc_params_derive(C.byref(p))
+    return p
+
 
 def build() -> None:
     subprocess.run(["make", "-s", "-C", HERE], check=True)
@@ -350,7 +393,6 @@ def gauss_regression(z, fp="f64"):
 
 def local_box_coordinates(parts, sym, loc, apix, fftsize, pr_threshold=90.0, boundx=100.0, fp="f64"):
     """loc_box_coordinate.f90: sub-particle records (LOCAL_PARTICLE_DTYPE)."""
-    from cryoim_gb300._abi import LOCAL_PARTICLE_DTYPE
     p = np.ascontiguousarray(parts)
     s = np.ascontiguousarray(sym, np.float32).reshape(-1, 3, 3)
     out = np.zeros(len(p) * len(s), LOCAL_PARTICLE_DTYPE)
@@ -394,3 +436,19 @@ def grid_sizes(step):
 
 def num_threads():
     return lib().orc_num_threads()
+
+
+def local_box_extract(imgs, parts, sym, loc, apix, sub, pr_threshold=90.0, boundx=100.0, fp="f64"):
+    """loc_box.f90 (sub-image stack mode): (sub images (K, sub, sub) float32, records
+    LOCAL_PARTICLE_DTYPE) for the selected particles x nsym rotations."""
+    im = np.ascontiguousarray(imgs, np.float32)
+    p = np.ascontiguousarray(parts)
+    s = np.ascontiguousarray(sym, np.float32).reshape(-1, 3, 3)
+    nx0 = im.shape[-1]
+    so = np.zeros((len(p) * len(s), sub, sub), np.float32)
+    out = np.zeros(len(p) * len(s), LOCAL_PARTICLE_DTYPE)
+    R = _R(fp)
+    k = _fn("local_box_extract", fp)(_p(im), _p(p), C.c_int(len(p)), C.c_int(nx0), _p(s), C.c_int(len(s)),
+                                     R(loc[0]), R(loc[1]), R(loc[2]), R(apix), C.c_int(sub), R(pr_threshold),
+                                     R(boundx), _p(so), _p(out))
+    return so[:k].copy(), out[:k].copy()

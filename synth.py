@@ -2,7 +2,10 @@
 
 The reference ships no data; its workloads are described by size only.  This module
 builds a phantom (Gaussian blobs placed by the 60 icosahedral rotations plus a solid
-shell), random orientations, CTF-modulated noisy projections and template sets.
+shell), random orientations, CTF-modulated noisy projections and template sets.  It is
+numpy only and imports nothing of the cryoim_gb300 package: the 60 rotations and the
+particle record type are passed in (`ops`, `dtype`), and only when they are not is the
+package asked for its own.  The bench's CPU reference arm passes the oracle's.
 
 Conventions follow icosprocess: ZYZ Euler angles R = Rz(phi) Ry(theta) Rz(omega)
 (euler_mat.f90), a projection samples the map at R*(x, y, z) (project_template2d.f90),
@@ -16,7 +19,12 @@ from __future__ import annotations
 
 import numpy as np
 
-from . import icos_ops
+
+def _ops(ops):
+    if ops is None:
+        import cryoim_gb300
+        ops = cryoim_gb300.icos_ops()
+    return np.asarray(ops).astype(np.float64)
 
 
 def euler_mat(theta, phi, omega) -> np.ndarray:
@@ -76,12 +84,13 @@ def random_asu_orientations(n: int, rng: np.random.Generator) -> np.ndarray:
     return np.array(out)
 
 
-def phantom(n: int, seed: int, nblob_seeds: int = 4) -> np.ndarray:
+def phantom(n: int, seed: int, ops=None, nblob_seeds: int = 4) -> np.ndarray:
     """240 Gaussian blobs (sigma 2.5 px, amplitude U(0.5,1.5) per seed, radius 40-52 px)
-    plus a shell (radius 30-34 px, density 0.3), all scaled by n/128."""
+    plus a shell (radius 30-34 px, density 0.3), all scaled by n/128.  ops: the 60
+    icosahedral rotations (FP32 table, 2-fold frame)."""
     rng = np.random.default_rng(seed)
     s = n / 128.0
-    ops = icos_ops().astype(np.float64)
+    ops = _ops(ops)
     vol = np.zeros((n, n, n), np.float32)
     c = n // 2
     zz, yy, xx = np.meshgrid(np.arange(n) - c, np.arange(n) - c, np.arange(n) - c, indexing="ij")
@@ -183,15 +192,18 @@ def apply_ctf_shift(img: np.ndarray, ctf: np.ndarray | None, x: float, y: float)
 
 def make_particles(map3d: np.ndarray, P: int, seed: int, projector, apix: float,
                    df_range=(1.0, 3.0), astig_max=0.0, origin_max=3.0, snr=0.1,
-                   vol=300.0, cs=2.7, ampwg=0.1, eulers: np.ndarray | None = None):
+                   vol=300.0, cs=2.7, ampwg=0.1, eulers: np.ndarray | None = None, dtype=None):
     """Projections at Haar-random orientations, CTF, origin shift and white noise.
-    Returns (images (P,n,n) float32, particle records (PARTICLE_DTYPE), true eulers)."""
-    from . import particles as _parts
+    Returns (images (P,n,n) float32, particle records (dtype: the cryoim_particle
+    layout), true eulers)."""
+    if dtype is None:
+        import cryoim_gb300
+        dtype = cryoim_gb300.PARTICLE_DTYPE
     rng = np.random.default_rng(seed)
     n = map3d.shape[-1]
     e = random_rotations(P, rng) if eulers is None else np.asarray(eulers, np.float64)
     proj = projector(map3d, e.astype(np.float32))
-    rec = _parts(P)
+    rec = np.zeros(P, dtype)
     imgs = np.empty((P, n, n), np.float32)
     yy, xx = np.meshgrid(np.arange(n) - n // 2, np.arange(n) - n // 2, indexing="ij")
     inside = (xx ** 2 + yy ** 2) <= (0.4 * n) ** 2
@@ -215,9 +227,9 @@ def make_particles(map3d: np.ndarray, P: int, seed: int, projector, apix: float,
     return imgs, rec, e
 
 
-def orientation_error(e1, e2) -> float:
+def orientation_error(e1, e2, ops=None) -> float:
     """Smallest rotation angle (degrees) between e1 and any icosahedral equivalent of e2."""
-    ops = icos_ops().astype(np.float64)
+    ops = _ops(ops)
     R1 = euler_mat(*e1)
     R2 = euler_mat(*e2)
     best = 180.0

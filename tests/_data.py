@@ -7,7 +7,7 @@ import numpy as np
 
 
 def projector(map3d, eulers):
-    from cryoim_gb300 import synth
+    import synth
     return synth.project_numpy(map3d, eulers)
 
 
@@ -15,7 +15,7 @@ def projector(map3d, eulers):
 def small_case(n=64, P=3, T=4, step=4.0, apix=4.0, min_res=60.0, max_res=12.0, snr=0.0, seed=7,
                apply_ctf=1):
     import cryoim_gb300 as ci
-    from cryoim_gb300 import synth
+    import synth
     p = ci.default_params(n, apix=apix, minRes=min_res, maxRes=max_res, searchstep=step,
                           ampwg=0.07, apply_ctf=apply_ctf, imgmask=(n // 2 - 2) * apix)
     vol = synth.phantom(n, seed)

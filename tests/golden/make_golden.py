@@ -1,8 +1,9 @@
 """Generate the golden fixtures under tests/golden/ from the reference sources.
 
-Run in a container where the reference is mounted (read-only) at /root/reference:
+Run where the reference sources are readable, giving their root directory as the
+argument or in the environment variable CRYOIM_REFERENCE:
 
-    python tests/golden/make_golden.py [/root/reference]
+    python tests/golden/make_golden.py <reference root>
 
 Fixtures written:
   icos2f_sym_mat.json -- the 60 rotation matrices, in file order, parsed from
@@ -63,4 +64,7 @@ def main(ref: str) -> None:
 
 
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
+    root = sys.argv[1] if len(sys.argv) > 1 else os.environ.get("CRYOIM_REFERENCE")
+    if not root:
+        sys.exit("usage: make_golden.py <reference root>  (or set CRYOIM_REFERENCE)")
+    main(root)

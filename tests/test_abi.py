@@ -68,3 +68,16 @@ def test_no_cpu_fallback_when_library_missing(tmp_path):
     import cryoim_gb300._abi as abi
     with pytest.raises(ImportError):
         abi.load(str(tmp_path / "absent.so"))
+
+
+def test_oracle_params_and_records_match_the_library(built, orc):
+    """The oracle's restatement of the parameter set-up and its record layouts agree
+    with the library byte for byte, so either side's records pass to the other."""
+    import cryoim_gb300 as ci
+    for n, kw in [(256, dict(apix=1.5, minRes=50.0, maxRes=6.0, searchstep=1.0, ampwg=0.07, imgmask=189.0)),
+                  (128, dict(apix=2.0, minRes=60.0, maxRes=10.0)), (96, dict(apix=3.0, use_imgmask=0)),
+                  (64, {})]:
+        a, b = orc.default_params(n, **kw), ci.default_params(n, **kw)
+        assert C.sizeof(a) == C.sizeof(b)
+        assert C.string_at(C.addressof(a), C.sizeof(a)) == C.string_at(C.addressof(b), C.sizeof(b)), (n, kw)
+    assert orc.PARTICLE_DTYPE == ci.PARTICLE_DTYPE and orc.TEMPLATE_DTYPE == ci.TEMPLATE_DTYPE

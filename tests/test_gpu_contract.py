@@ -112,7 +112,7 @@ def test_pick_matches_exhaustive_pr_search(run, built):
 
 
 def test_noise_free_particles_find_their_orientation(run):
-    from cryoim_gb300 import synth
+    import synth
     (p, vol, tmpl, timgs, imgs, parts, truth), q, cands, stats = run
     for i in range(len(parts)):
         top = cands[i, 0]

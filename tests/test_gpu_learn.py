@@ -266,7 +266,7 @@ def test_render_matches_real_space_projection(built):
     origin shift) against the numpy real-space projector with the same CTF and shift,
     over |h| <= maxR."""
     import cryoim_gb300 as ci
-    from cryoim_gb300 import synth
+    import synth
     p, vol, *_ = small_case()
     n, R = p.fftsize, p.max_r
     rng = np.random.default_rng(9)

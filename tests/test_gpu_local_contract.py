@@ -45,7 +45,7 @@ def run_local(case, off, lanes=4, batch=64, topk=8):
 
 
 def test_noise_free_particles_land_on_their_true_grid_point(case):
-    from cryoim_gb300 import synth
+    import synth
     p, vol, tmpl, timgs, imgs, parts, truth = case
     for seed in (1, 2):
         q, cands = run_local(case, offsets(len(parts), seed))

@@ -1,0 +1,189 @@
+"""Parity at production sizes: the GPU search forms against committed FP64-oracle
+fixtures (tests/golden/<workload>_search.npz, made by tests/golden/make_workload_fixtures.py
+from the same seeded inputs, tests/_workloads.py).
+
+box128 (500 particles of 128^2, 20 templates, 1-degree grid, minR 4 .. maxR 26, SNR 0.1):
+  * FP32 drop-in search (cryoim_globesearch): the PR(omega) row of each of the first 64
+    particles' oracle pick within 1e-4 relative for >= 99.5 % of entries, all entries
+    within the gate-flip bound; every particle's minimum PR within that bound; the same
+    grid orientation as the oracle wherever the oracle's best-two gap exceeds twice the
+    largest observed score error;
+  * the map reconstruct.f90 makes from the FP32 search's picks against the oracle's map
+    from the oracle's picks: FSC >= 0.999 in every shell 1..maxR;
+  * BF16 exhaustive contraction and the learned-proposal form (BF16 contraction over the
+    neighbourhoods of the trained proposer's cells): >= 99 % the oracle's orientation,
+    their maps FSC >= 0.999 against the oracle's map.
+box256 (16 particles of 256^2, 20 templates, 1-degree grid, minR 7 .. maxR 64, SNR 0.05):
+  the same score and orientation checks on every particle; the gate-flip error at this
+  size is measured and bounded (a flip moves a score by about 1 / terms).
+
+A term enters a phase residual only where both amplitudes reach their cuts
+(cal_crosslin_PR_omega.f90:52,56); the particle transform here comes from cuFFT in FP32,
+the oracle's from an FP64 FFT, so a term within rounding of its cut can flip.
+"""
+import json
+import os
+
+import numpy as np
+import pytest
+
+import _workloads as W
+
+pytestmark = pytest.mark.gpu
+HERE = os.path.dirname(os.path.abspath(__file__))
+RTOL = 1e-4
+MIN_FRAC_WITHIN = 0.995
+FSC_MIN = 0.999
+AGREE_MIN = 0.99
+# largest score change one gate flip can make: ~1/terms (box128: ~20k terms per score,
+# box256: ~60k); a score may carry a few flips
+FLIP_TOL = {"box128": 1e-3, "box256": 3e-4}
+REPORT = {}
+
+
+def _fixture(name):
+    path = os.path.join(HERE, "golden", f"{name}_search.npz")
+    return dict(np.load(path))
+
+
+def _report(name, key, value):
+    REPORT.setdefault(name, {})[key] = value
+    out = os.environ.get("CRYOIM_REPORT")
+    if out:
+        with open(out, "w") as f:
+            json.dump(REPORT, f, indent=1)
+
+
+def _inputs(name):
+    fx = _fixture(name)
+    data = W.make(name)
+    p, vol, tmpl, timgs, imgs, parts, truth = data
+    # the regenerated inputs are the ones the fixture was made from
+    np.testing.assert_allclose(W.fingerprint(imgs), fx["fingerprint"], rtol=1e-6, atol=1e-6)
+    np.testing.assert_allclose(W.fingerprint(timgs), fx["tmpl_fingerprint"], rtol=1e-6, atol=1e-6)
+    return data, fx
+
+
+@pytest.fixture(scope="module")
+def box128(built):
+    return _inputs("box128")
+
+
+@pytest.fixture(scope="module")
+def box256(built):
+    return _inputs("box256")
+
+
+def _ctx(data, with_map=False):
+    import cryoim_gb300 as ci
+    p, vol, tmpl, timgs, imgs, parts, truth = data
+    c = ci.Context(0, p)
+    c.load_templates(timgs, tmpl)
+    if with_map:
+        c.set_reference_map(vol)
+    return c
+
+
+def _picks(q):
+    return np.stack([q["theta"], q["phi"], q["omega"]], 1)
+
+
+def _same(q, pick):
+    return np.all(np.abs(_picks(q) - pick) < 1e-3, axis=1)
+
+
+def _fp32_search(name, data, fx):
+    """FP32 search of every particle, the PR array kept for the rows the fixture holds."""
+    p, vol, tmpl, timgs, imgs, parts, truth = data
+    nrow = len(fx["pr_row"])
+    with _ctx(data) as c:
+        qa = parts[:nrow].copy()
+        pra = c.globesearch(imgs[:nrow], qa, want_pr_array=True)
+        qb = parts[nrow:].copy()
+        if len(qb):
+            c.globesearch(imgs[nrow:], qb)
+    q = np.concatenate([qa, qb])
+    it, iph = fx["pick_index"][:nrow, 0], fx["pick_index"][:nrow, 1]
+    rows = pra[np.arange(nrow), it, iph]
+    want = fx["pr_row"]
+    assert np.array_equal(rows >= 999, want >= 999)
+    ok = want < 999
+    rel_rows = np.abs(rows[ok] - want[ok]) / np.abs(want[ok])
+    rel_pick = np.abs(q["pr"] - fx["pr"]) / np.abs(fx["pr"])
+    _report(name, "fp32_rows_frac_within_1e-4", float(np.mean(rel_rows < RTOL)))
+    _report(name, "fp32_rows_max_rel", float(rel_rows.max()))
+    _report(name, "fp32_min_pr_max_rel", float(rel_pick.max()))
+    assert float(np.mean(rel_rows < RTOL)) >= MIN_FRAC_WITHIN, float(np.mean(rel_rows < RTOL))
+    assert float(rel_rows.max()) < FLIP_TOL[name], float(rel_rows.max())
+    assert float(rel_pick.max()) < FLIP_TOL[name], float(rel_pick.max())
+    tol = max(RTOL, float(rel_rows.max()), float(rel_pick.max()))
+    same = _same(q, fx["pick"])
+    decided = fx["gap"] > 2 * tol
+    _report(name, "fp32_identical", float(same.mean()))
+    _report(name, "fp32_decided_particles", int(decided.sum()))
+    assert same[decided].all(), np.nonzero(decided & ~same)[0]
+    return q
+
+
+def _map_fsc(name, data, fx, q):
+    p, vol, tmpl, timgs, imgs, parts, truth = data
+    with _ctx(data) as c:
+        c.rec_begin()
+        c.rec_insert(imgs, q.copy())
+        m = c.rec_finish()
+    coef, shell = W.band_coefficients(m, p.max_r)
+    return W.fsc_shells(coef, fx["map_coef"].astype(np.complex128), shell, p.max_r)
+
+
+def test_box128_fp32_search_and_map_match_oracle(box128):
+    data, fx = box128
+    q = _fp32_search("box128", data, fx)
+    f = _map_fsc("box128", data, fx, q)
+    _report("box128", "fp32_map_fsc_min", float(f.min()))
+    assert f.min() >= FSC_MIN, f
+
+
+@pytest.mark.parametrize("form", ["bf16_exhaustive", "learned"])
+def test_box128_contraction_forms_match_oracle(box128, form):
+    data, fx = box128
+    p, vol, tmpl, timgs, imgs, parts, truth = data
+    s = W.SPECS["box128"]
+    kw = dict(origin_max=4.0, origin_step=0.5, topk=16, pick=0)
+    with _ctx(data, with_map=True) as c:
+        if form == "learned":
+            c.learn_train(vol, samples=16384, batch=256, lr=4e-3, seed=s["seed"], snr=s["snr"],
+                          df_min=s["df"][0], df_max=s["df"][1], astig_max=0.0, origin_max=s["origin"])
+            kw.update(learned=16, nbr_best=4)
+        q = parts.copy()
+        c.contract_search(imgs, q, **kw)
+    same = _same(q, fx["pick"])
+    _report("box128", f"{form}_identical_to_oracle", float(same.mean()))
+    assert same.mean() >= AGREE_MIN, same.mean()
+    f = _map_fsc("box128", data, fx, q)
+    _report("box128", f"{form}_map_fsc_min", float(f.min()))
+    assert f.min() >= FSC_MIN, f
+
+
+def test_box256_fp32_search_matches_oracle(box256):
+    data, fx = box256
+    _fp32_search("box256", data, fx)
+
+
+@pytest.mark.parametrize("form", ["bf16_exhaustive", "learned"])
+def test_box256_contraction_forms_match_oracle(box256, form):
+    data, fx = box256
+    p, vol, tmpl, timgs, imgs, parts, truth = data
+    s = W.SPECS["box256"]
+    kw = dict(origin_max=6.0, origin_step=0.5, topk=16, pick=0)
+    with _ctx(data, with_map=True) as c:
+        if form == "learned":
+            c.learn_train(vol, samples=16384, batch=256, lr=4e-3, seed=s["seed"], snr=s["snr"],
+                          df_min=s["df"][0], df_max=s["df"][1], astig_max=s["astig"], origin_max=s["origin"])
+            kw.update(learned=16, nbr_best=4)
+        q = parts.copy()
+        c.contract_search(imgs, q, **kw)
+    same = _same(q, fx["pick"])
+    _report("box256", f"{form}_identical_to_oracle", float(same.mean()))
+    # every particle whose oracle gap is decisive gets the oracle's orientation
+    decided = fx["gap"] > 2 * FLIP_TOL["box256"]
+    assert same[decided].all(), np.nonzero(decided & ~same)[0]

@@ -146,7 +146,7 @@ def test_proc_icos_transforms_and_random_equivalents(built, orc, tmp_path):
     r = subprocess.run([os.path.join(BIN, "proc_icos"), f"ort0={src}", f"newort={out}", "calc_randort_2f=y",
                         "seed=3"], capture_output=True, text=True)
     assert r.returncode == 0
-    from cryoim_gb300.synth import euler_mat
+    from synth import euler_mat
     ops = orc.icos_ops("f64")
     for row, (t0, p0, o0) in zip(out.read_text().splitlines(), [(70, 10, 33), (85, -20, 120)]):
         e = [float(row[72 + 10 * k:82 + 10 * k]) for k in range(3)]

@@ -110,7 +110,7 @@ def local_case(n=32, n0=48, P=3, seed=11, snr=0.0, sign=1.0):
     sub-particle orientations, centres and origins (noise-free unless snr); the content
     of each window is moved by sign x (local_x0, local_y0)."""
     import cryoim_gb300 as ci
-    from cryoim_gb300 import synth
+    import synth
     rng = np.random.default_rng(seed)
     z, y, x = np.mgrid[0:n, 0:n, 0:n] - n // 2
     vol = np.zeros((n, n, n), np.float32)

@@ -43,7 +43,7 @@ def test_generator_order_is_a_permutation_of_the_table(orc, golden_ops):
 
 @pytest.mark.parametrize("fp", ["f32", "f64"])
 def test_euler_matrix_zyz(orc, fp):
-    from cryoim_gb300.synth import euler_mat
+    from synth import euler_mat
     for th, ph, om in [(0, 0, 0), (30, 40, 50), (90, -45, 270), (123.4, 200.1, -33.3)]:
         m = orc.euler(th, ph, om, fp)
         tol = 1e-6 if fp == "f32" else 1e-13
@@ -53,7 +53,7 @@ def test_euler_matrix_zyz(orc, fp):
 def test_crosslin_angles_define_common_lines(orc):
     """alpha1/alpha2 are the in-plane angles of the shared line v = z1 x S z2: rotating
     (cos a1, sin a1, 0) by R1 and (cos a2, sin a2, 0) by S R2 both give v."""
-    from cryoim_gb300.synth import euler_mat
+    from synth import euler_mat
     o1, o2 = (75.0, 12.0, 40.0), (81.0, -20.0, 200.0)
     a1, a2 = orc.crosslin(o1, o2, "f64")
     ops = orc.icos_ops("f64")
@@ -74,7 +74,7 @@ def test_crosslin_angles_define_common_lines(orc):
 
 
 def test_asu_fold_is_idempotent_and_equivalent(orc):
-    from cryoim_gb300.synth import euler_mat, in_asu
+    from synth import euler_mat, in_asu
     rng = np.random.default_rng(1)
     ops = orc.icos_ops("f64")
     for _ in range(50):
@@ -103,7 +103,7 @@ def test_equalort_and_frame_transforms(orc, built):
     """proc_icos equalort / transform_ort_2fTo5f / 2fTo3f: library (FP32) against the
     oracle (FP32) and against the defining rotation in FP64."""
     import cryoim_gb300 as ci
-    from cryoim_gb300.synth import euler_mat
+    from synth import euler_mat
     e_lib = ci.equalort(70.0, 10.0, 33.0)
     e_orc = orc.equalort(70.0, 10.0, 33.0, "f32")
     assert np.abs(e_lib - e_orc).max() < 1e-3

@@ -8,7 +8,7 @@ from _data import small_case
 
 
 def test_globesearch_recovers_orientation(orc):
-    from cryoim_gb300 import synth
+    import synth
     p, vol, tmpl, timgs, imgs, parts, truth = small_case()
     tm, tf = orc.load_templates(timgs, tmpl, p, "f64")
     q = parts.copy()
@@ -41,7 +41,7 @@ def test_fp32_oracle_agrees_with_fp64(orc):
 
 
 def test_refine_keeps_or_improves(orc):
-    from cryoim_gb300 import synth
+    import synth
     p, vol, tmpl, timgs, imgs, parts, truth = small_case()
     tm, tf = orc.load_templates(timgs, tmpl, p, "f64")
     q = parts.copy()

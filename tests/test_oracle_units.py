@@ -28,7 +28,7 @@ def test_fft3d_matches_numpy(orc):
 
 
 def test_ctf_matches_independent_formula(orc):
-    from cryoim_gb300.synth import ctf2d
+    from synth import ctf2d
     for args in [(1.5, 1.5, 0.0, 2.0), (2.0, 2.1, 37.0, 1.5)]:
         c64 = orc.ctf2d(64, *args, 300.0, 2.7, 0.07, fp="f64")
         ref = ctf2d(64, *args, 300.0, 2.7, 0.07)
