@@ -703,8 +703,9 @@ def run_profile_case(args):
     """Small cases for profiler captures (a few GB on the device, seconds of GPU time):
     learned: 64 particles of the box-256 workload, the headline form with a proposer
     trained on 2,560 projections, 2 calls; exhaustive-bf16 / exhaustive-fp8: 12
-    particles at a 2-degree grid (31,320 orientations), 2 calls; fp32: 4 particles of
-    the FP32 phase-residual form, 2 calls."""
+    particles at a 2-degree grid (31,320 orientations, the section bank built once), 2
+    calls; fp32: 4 particles of the FP32 phase-residual form, 2 calls; insert: 64
+    particles inserted into a fresh reconstruction, 2 calls."""
     import torch
     import cryoim_gb300 as ci
     w = WORKLOAD
@@ -712,7 +713,7 @@ def run_profile_case(args):
     step = 2.0 if case.startswith("exhaustive") else w["searchstep"]
     params = make_params(ci, searchstep=step)
     ctx = ci.Context(0, params)
-    P = {"learned": 64, "exhaustive-bf16": 12, "exhaustive-fp8": 12, "fp32": 4}[case]
+    P = {"learned": 64, "exhaustive-bf16": 12, "exhaustive-fp8": 12, "fp32": 4, "insert": 64}[case]
     vol, tmpl, timgs, imgs, parts, truth = make_data(ci, P, lambda v, t: ctx.project_templates(v, t))
     ctx.load_templates(timgs, tmpl)
     ctx.set_reference_map(vol)
@@ -727,6 +728,11 @@ def run_profile_case(args):
     for _ in range(2):
         if case == "fp32":
             ctx.globesearch(d.data_ptr(), parts.copy())
+        elif case == "insert":
+            q = parts.copy()
+            q["pr"] = 0.0
+            ctx.rec_begin()
+            ctx.rec_insert(d.data_ptr(), q)
         else:
             ctx.contract_search(d.data_ptr(), parts.copy(), **copts)
     torch.cuda.synchronize()
@@ -821,6 +827,112 @@ def run_precision_report(args):
     return 0
 
 
+def run_learned_report(args):
+    """The learned-proposal form evaluated the way its configuration states it, on P
+    particles of the CPU-runnable configuration's generator (box 128, 2.0 A/px, band
+    1/60-1/10 A^-1, defocus 1.0-3.0 um, SNR 0.1, origins within +-3 px; 1-degree grid,
+    origins +-4 px at 0.5 px):
+      * the proposer trained on `--learn-samples` projections the library renders from
+        the map (noisy and noise-free halves are not separated: every render carries
+        noise at the stated SNR);
+      * its cells seed the BF16 fine contraction (pick = 1: best FP64 cross-correlation);
+      * each seed is refined by a local search of +-2 degrees at 0.2 degrees and +-1.5 px
+        at 0.25 px around the particle's own origin (the local form with centred origins);
+      * the judge is the exhaustive BF16 contraction (every grid orientation, pick = 1);
+        a particle whose refined FP64 CC is below the judge's by more than 1e-3 counts as
+        a fallback (the configuration's rule), and the run-time fallback rule of the
+        library (phase residual more than 3 robust standard deviations above the median)
+        is reported beside it, with the agreement of its picks with the exhaustive
+        phase-residual search."""
+    import torch
+    import cryoim_gb300 as ci
+    import synth
+    r, world, lr = rank_env()
+    if r != 0:
+        return 0
+    n, P = 128, args.learned_report
+    seed = 20261204
+    params = ci.default_params(n, apix=2.0, minRes=60.0, maxRes=10.0, searchstep=1.0, ampwg=0.07,
+                               imgmask=(n // 2 - 2) * 2.0)
+    ctx = ci.Context(0, params)
+    rng = np.random.default_rng(seed)
+    vol = synth.phantom(n, seed)
+    te = synth.random_asu_orientations(20, rng)
+    tmpl = _as_tmpl(ci, te)
+    tmpl["particle_id"] = np.arange(1, 21)
+    timgs = ctx.project_templates(vol, tmpl)
+    imgs, parts, truth = synth.make_particles(
+        vol, P, seed + 101, lambda v, e: ctx.project_templates(v, _as_tmpl(ci, e)), 2.0, df_range=(1.0, 3.0),
+        astig_max=0.0, origin_max=3.0, snr=0.1, ampwg=0.07)
+    ctx.load_templates(timgs, tmpl)
+    ctx.set_reference_map(vol)
+    d = torch.from_numpy(imgs).to("cuda:0")
+    g = dict(origin_max=4.0, origin_step=0.5, topk=16)
+    ctx.contract_search(d.data_ptr(), parts[:64].copy(), **g)  # section bank outside the timing
+
+    def timed(fn):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        out = fn()
+        torch.cuda.synchronize()
+        return out, time.perf_counter() - t0
+
+    st, t_train = timed(lambda: ctx.learn_train(vol, samples=args.learn_samples, batch=256, lr=4e-3, seed=seed,
+                                                snr=0.1, df_min=1.0, df_max=3.0, astig_max=0.0, origin_max=3.0))
+    # judge: the exhaustive contraction, best FP64 CC
+    qj = parts.copy()
+    _, t_judge = timed(lambda: ctx.contract_search(d.data_ptr(), qj, pick=1, **g))
+    # the learned form, best FP64 CC among its candidates, then the local search
+    ql = parts.copy()
+    _, t_learn = timed(lambda: ctx.contract_search(d.data_ptr(), ql, pick=1, learned=16, **g))
+    qloc = ql.copy()
+    _, t_local = timed(lambda: ctx.contract_search(d.data_ptr(), qloc, pick=1, origin_max=1.5, origin_step=0.25,
+                                                   topk=16, local_range=2.0, local_step=0.2, centred_origins=True))
+    off = qloc["pr"] < qj["pr"] - 1e-3
+    # the phase-residual forms: exhaustive PR search on the GPU (the drop-in), the learned
+    # form with and without its run-time fallback
+    qpr = parts.copy()
+    _, t_pr = timed(lambda: ctx.globesearch(d.data_ptr(), qpr))
+    qa = parts.copy()
+    _, t_a = timed(lambda: ctx.contract_search(d.data_ptr(), qa, learned=16, nbr_best=4, **g))
+    qf = parts.copy()
+    _, t_f = timed(lambda: ctx.contract_search(d.data_ptr(), qf, learned=16, nbr_best=4, fallback=3.0, **g))
+    nfb = ctx.contract_fallbacks()
+
+    def same(q1, q2):
+        return np.all(np.abs(np.stack([q1["theta"] - q2["theta"], q1["phi"] - q2["phi"],
+                                       q1["omega"] - q2["omega"]], 1)) < 1e-3, axis=1)
+
+    def err(q):
+        return float(np.median([synth.orientation_error((q["theta"][i], q["phi"][i], q["omega"][i]), truth[i])
+                                for i in range(P)]))
+    out = {"report": "learned-proposal form", "particles": P,
+           "config": {"box": n, "apix": 2.0, "band_A": [60.0, 10.0], "searchstep_deg": 1.0,
+                      "origins": "+-4 px @ 0.5 px", "snr": 0.1, "data": "synthetic, seeded"},
+           "proposer": {"training_samples": args.learn_samples, "training_s": t_train, "views": st["views"],
+                        "final_loss": st["loss"]},
+           "cc_form": {"judge": "exhaustive BF16 contraction, best FP64 CC (pick 1)",
+                       "judge_particles_per_s": P / t_judge,
+                       "learned_particles_per_s": P / t_learn,
+                       "local_search": "+-2 deg @ 0.2 deg x +-1.5 px @ 0.25 px around each seed, centred origins",
+                       "local_particles_per_s": P / t_local,
+                       "learned_plus_local_particles_per_s": P / (t_learn + t_local),
+                       "fallbacks_by_the_1e-3_rule": int(off.sum()), "fallback_rate": float(off.mean()),
+                       "learned_identical_to_judge_grid_pick": float(same(ql, qj).mean()),
+                       "cc_gain_of_local_search_median": float(np.median(qloc["pr"] - ql["pr"])),
+                       "median_error_vs_truth_deg": {"judge": err(qj), "learned": err(ql), "learned_plus_local": err(qloc)}},
+           "pr_form": {"fp32_exhaustive_particles_per_s": P / t_pr,
+                       "learned_particles_per_s": P / t_a,
+                       "learned_identical_to_fp32_exhaustive": float(same(qa, qpr).mean()),
+                       "learned_with_fallback_particles_per_s": P / t_f,
+                       "runtime_fallback_rule": "PR above median + 3 x 1.4826 x MAD -> exhaustive contraction",
+                       "runtime_fallbacks": nfb, "runtime_fallback_rate": nfb / P,
+                       "learned_with_fallback_identical_to_fp32_exhaustive": float(same(qf, qpr).mean())}}
+    print(json.dumps(out))
+    ctx.close()
+    return 0
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -838,12 +950,17 @@ def main():
                     help="override the 0.5 px origin step (small cases for profiler captures only)")
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--profile-case", choices=["learned", "exhaustive-bf16", "exhaustive-fp8", "fp32"],
+    ap.add_argument("--profile-case", choices=["learned", "exhaustive-bf16", "exhaustive-fp8", "fp32", "insert"],
                     default=None, help="instead of the bench line: a small case for profiler captures")
     ap.add_argument("--precision-report", type=int, default=0, metavar="P",
                     help="instead of the bench line: BF16 and FP8 contraction against FP64 scores and the "
                          "exhaustive FP32 search on P particles of the box-128 configuration (0.5-degree grid)")
+    ap.add_argument("--learned-report", type=int, default=0, metavar="P",
+                    help="instead of the bench line: the learned-proposal form with local search, judged by the "
+                         "exhaustive contraction on P particles of the box-128 configuration")
     args = ap.parse_args()
+    if args.learned_report:
+        return run_learned_report(args)
     if args.precision_report:
         return run_precision_report(args)
     if args.profile_case:

@@ -157,7 +157,8 @@ class Context:
                         origin_step: float = 0.5, topk: int = 16, pick: int = 0,
                         want_cands: bool = False, precision: str = "bf16", nbr: int = 1,
                         coarse: int = 0, learned: int = 0, nbr_best: int = 0,
-                        local_range: float = 0.0, local_step: float = 0.0):
+                        local_range: float = 0.0, local_step: float = 0.0, fallback: float = 0.0,
+                        centred_origins: bool = False):
         """Tensor-core cross-correlation search with FP64 / phase-residual rescoring of
         the top-k and their grid neighbours within nbr steps; parts is updated in place.
         precision: "bf16" or "fp8" (e4m3 operands with per-band scales); coarse > 0: the
@@ -166,15 +167,18 @@ class Context:
         trained proposer's `learned` cells (learn_train / learn_load first); nbr_best > 0:
         only the neighbourhoods of the nbr_best candidates of least phase residual are
         rescored; local_range > 0: local grid search of +-local_range degrees at
-        local_step around each particle's own orientation (pick 1, BF16).  Returns (P,
-        topk, 8) candidates if asked: theta, phi, omega, x, y, CC (contraction), CC
-        (FP64), PR."""
+        local_step around each particle's own orientation (pick 1, BF16); fallback > 0
+        (learned form): particles whose phase residual lies more than `fallback` robust
+        standard deviations above the call's median are searched again exhaustively
+        (contract_fallbacks() counts them); centred_origins: the origin grid is centred
+        on each particle's own origin.  Returns (P, topk, 8) candidates if asked: theta,
+        phi, omega, x, y, CC (contraction), CC (FP64), PR."""
         assert parts.dtype == PARTICLE_DTYPE and parts.flags["C_CONTIGUOUS"]
         if precision not in ("bf16", "fp8"):
             raise ValueError("precision must be 'bf16' or 'fp8'")
         o = _abi.ContractOpts(float(origin_max), float(origin_step), int(topk), int(pick),
                               int(precision == "fp8"), int(nbr), int(coarse), int(learned), int(nbr_best),
-                              float(local_range), float(local_step))
+                              float(local_range), float(local_step), float(fallback), int(bool(centred_origins)))
         out = np.zeros((len(parts), topk, 8), np.float32) if want_cands else None
         if isinstance(imgs, int):
             call("cryoim_contract_search_device", self._h, C.c_void_p(imgs), ptr(parts), len(parts),
@@ -260,6 +264,16 @@ class Context:
         out = np.zeros((len(parts), 64, 128), np.float32)
         call("cryoim_learn_features", self._h, ptr(im), ptr(parts), len(parts), ptr(out))
         return out
+
+    def set_interpolation(self, kind: str = "trilinear", sigma: float = 0.0) -> None:
+        """Sections of the contraction forms: "trilinear" or "gaussian" (kernel width sigma
+        voxels, 27 taps)."""
+        call("cryoim_set_interpolation", self._h, 1 if kind == "gaussian" else 0, float(sigma))
+
+    def contract_fallbacks(self) -> int:
+        n = C.c_int32()
+        call("cryoim_contract_fallbacks", self._h, C.byref(n))
+        return n.value
 
     def contract_stats(self) -> dict:
         v = np.zeros(6, np.float64)

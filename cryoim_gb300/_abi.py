@@ -65,7 +65,7 @@ class ContractOpts(C.Structure):
     _fields_ = [("origin_max", C.c_float), ("origin_step", C.c_float), ("topk", C.c_int32),
                 ("pick", C.c_int32), ("precision", C.c_int32), ("nbr", C.c_int32), ("coarse", C.c_int32),
                 ("learned", C.c_int32), ("nbr_best", C.c_int32), ("local_range", C.c_float),
-                ("local_step", C.c_float)]
+                ("local_step", C.c_float), ("fallback", C.c_float), ("centred_origins", C.c_int32)]
 
 
 class LearnOpts(C.Structure):
@@ -137,6 +137,9 @@ SIGNATURES = {
     "cryoim_local_params_default": [_vp, _i32, _i32],
     "cryoim_local_params_derive": [_vp],
     "cryoim_local_refine": [_vp, _vp, _vp, _vp, _vp, _i32],
+    "cryoim_contract_fallbacks": [_vp, _ip],
+    "cryoim_gemm_bf16_argmax_withhold": [_vp, _vp, _i32, _i32, _i32, _vp, _vp, _vp, _i32, _i32, _vp],
+    "cryoim_set_interpolation": [_vp, _i32, _f32],
     "cryoim_local_box_extract": [_vp, _vp, _vp, _i32, _i32, _vp, _i32, _f32, _f32, _f32, _f32, _i32, _f32, _f32,
                                  _vp, _vp, _ip],
     "cryoim_local_box_extract_device": [_vp, _vp, _vp, _i32, _i32, _vp, _i32, _f32, _f32, _f32, _f32, _i32, _f32,

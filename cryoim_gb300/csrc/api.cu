@@ -316,6 +316,9 @@ struct Ctx {
     double bmat8_ms = 0.0;
     int cKpad8 = 0, last_kpad = 0;
     double last_slice_ms = 0.0;
+    int last_fallbacks = 0;   // particles of the last contraction call re-searched exhaustively
+    float interp_sigma = 0.0f;  // sections: 0 trilinear, > 0 Gaussian kernel of this width (voxels)
+    DBuf<float> poff;         // per-pass particle origins (x, y) of the centred origin grid
     DBuf<float> mulA, mulB;
     DBuf<unsigned> bandmax;
     DBuf<int> fexp;
@@ -854,7 +857,7 @@ int ensure_bmat(Ctx* c) {
     if (te == cudaSuccess) te = cudaEventRecord(e0, c->stream);
     if (te == cudaSuccess)
         te = launch_slice_bf16(tex, c->p.max_r, c->csamples.p, c->cS, c->cKpad, dv.p, c->nom, c->p.searchstep, 0,
-                               n, c->bmat.p, c->stream);
+                               n, c->bmat.p, c->stream, c->mapcube.p, c->interp_sigma);
     if (te == cudaSuccess) te = cudaEventRecord(e1, c->stream);
     if (te == cudaSuccess) te = cudaEventSynchronize(e1);
     free_cube_texture(arr, tex);
@@ -903,7 +906,7 @@ int ensure_coarse(Ctx* c, float omax, float ostep) {
         cudaError_t te = make_cube_texture(c->mapcube.p, R, c->stream, &arr, &tex);
         if (te == cudaSuccess)
             te = launch_slice_bf16(tex, R, c->csamples_c.p, c->cS_c, c->cKpad_c, dv.p, g.nom, g.step, 0, n,
-                                   c->bmat_c.p, c->stream);
+                                   c->bmat_c.p, c->stream, c->mapcube.p, c->interp_sigma);
         if (te == cudaSuccess) te = cudaStreamSynchronize(c->stream);
         free_cube_texture(arr, tex);
         if (te != cudaSuccess) return fail(CRYOIM_ERR_CUDA, "coarse sections: %s", cudaGetErrorString(te));
@@ -1579,6 +1582,7 @@ int contract_impl(Ctx* c, const float* imgs, bool on_device, cryoim_particle* pa
     if (!(opts->origin_step > 0) || opts->origin_max < 0) return fail(CRYOIM_ERR_ARG, "bad origin grid");
     if (opts->precision != 0 && opts->precision != 1) return fail(CRYOIM_ERR_ARG, "precision must be 0 or 1");
     const bool f8 = opts->precision == 1;
+    const bool centred = opts->centred_origins != 0;
     const int nbr = opts->nbr <= 0 ? 1 : opts->nbr;
     const int nbest = opts->nbr_best;  // 0: neighbourhoods of every candidate
     if (nbest < 0) return fail(CRYOIM_ERR_ARG, "nbr_best must be >= 0");
@@ -1683,6 +1687,7 @@ int contract_impl(Ctx* c, const float* imgs, bool on_device, cryoim_particle* pa
             (r = L->xpr.ensure((size_t)PB * maxx)))
             return r;
         if (local && (r = L->lcentre.ensure(3 * (size_t)PB))) return r;
+        if (centred && (r = L->poff.ensure(2 * (size_t)PB))) return r;
         if (T > 0 && !local &&
             ((r = L->xalpha.ensure((size_t)PB * maxx * T * 60)) || (r = L->sband.ensure((size_t)PB * w2)) ||
                       (r = L->xcount.ensure(PB)) || (L->p.apply_ctf && (r = L->tbandc.ensure((size_t)PB * T * w2)))))
@@ -1740,17 +1745,23 @@ int contract_impl(Ctx* c, const float* imgs, bool on_device, cryoim_particle* pa
             }
             launch_particle_norm(L->band.p, ctfp, L->bd, L->csamples.p, L->cS, nb, L->pnorm.p, L->stream,
                                  L->pcband.p);
+            if (centred) {  // the origin grid around each particle's own origin
+                std::vector<float> po(2 * (size_t)nb);
+                for (int i = 0; i < nb; ++i) { po[2 * i] = parts[b0 + i].x; po[2 * i + 1] = parts[b0 + i].y; }
+                CK(cudaMemcpyAsync(L->poff.p, po.data(), sizeof(float) * po.size(), cudaMemcpyHostToDevice, L->stream));
+            }
             // operand A rows (particle, origin) of particles [s0, s0 + ns) at row (s0 - a0) O
             auto build_rows = [&](int s0, int ns, int a0) {
                 const float2* bb = L->band.p + (long)s0 * w2;
                 const float* cc = ctfp ? ctfp + (long)s0 * w2 : nullptr;
+                const float* po = centred ? L->poff.p + 2 * (size_t)s0 : nullptr;
                 if (f8)
                     launch_build_a8(bb, cc, L->bd, L->csamples.p, L->cS, L->cKpad8, L->corigins.p, O, L->pnorm.p + s0,
                                     L->mulA.p, L->fexp.p + s0, ns, L->amat8.p + (size_t)(s0 - a0) * O * L->cKpad8,
-                                    L->stream);
+                                    L->stream, po);
                 else
                     launch_build_a(bb, cc, L->bd, L->csamples.p, L->cS, L->cKpad, L->corigins.p, O, L->pnorm.p + s0, ns,
-                                   L->amat.p + (size_t)(s0 - a0) * O * L->cKpad, L->stream);
+                                   L->amat.p + (size_t)(s0 - a0) * O * L->cKpad, L->stream, po);
             };
             GemmArgmaxArgs g{};
             g.topv = L->topv.p;
@@ -1792,7 +1803,8 @@ int contract_impl(Ctx* c, const float* imgs, bool on_device, cryoim_particle* pa
                         CK(cudaMemcpyAsync(L->lcentre.p, cen.data(), sizeof(float) * cen.size(), cudaMemcpyHostToDevice,
                                            L->stream));
                         CK(launch_slice_bf16_local(ltex.tex, L->p.max_r, L->csamples.p, L->cS, L->cKpad, L->lcentre.p,
-                                                   lm, opts->local_step, rows, L->bgather.p, L->stream));
+                                                   lm, opts->local_step, rows, L->bgather.p, L->stream,
+                                                   c->mapcube.p, c->interp_sigma));
                     } else {
                         std::vector<int> idx;
                         idx.reserve(rows);
@@ -1891,13 +1903,13 @@ int contract_impl(Ctx* c, const float* imgs, bool on_device, cryoim_particle* pa
                     hcand[5 * i + 1] = L->views[4 * v + 1];
                     hcand[5 * i + 2] = L->p.searchstep * (float)io;
                 }
-                hcand[5 * i + 3] = ohost[2 * o];
-                hcand[5 * i + 4] = ohost[2 * o + 1];
+                hcand[5 * i + 3] = ohost[2 * o] + (centred ? parts[b0 + i / k].x : 0.0f);
+                hcand[5 * i + 4] = ohost[2 * o + 1] + (centred ? parts[b0 + i / k].y : 0.0f);
             }
             CK(cudaMemcpyAsync(L->kcand.p, hcand.data(), sizeof(float) * nb * k * 5, cudaMemcpyHostToDevice,
                                L->stream));
             launch_cc_fp64(L->mapcube.p, L->pcband.p, L->bd, L->csamples.p, L->cS, L->kcand.p, k, nb, L->pnorm.p,
-                           L->kpart.p, L->kcc64.p, L->stream);
+                           L->kpart.p, L->kcc64.p, L->stream, c->interp_sigma);
             // Phase-residual rescoring at the particle's own origin (ort_globesearch.f90 scores
             // every view at particle(i)%x, %y) over each selected orientation and its grid
             // neighbours within nbr steps (all of them, or, with nbr_best = m, only those of
@@ -2100,6 +2112,67 @@ int contract_impl(Ctx* c, const float* imgs, bool on_device, cryoim_particle* pa
     if (r0) return r0;
     for (int i = 0; i + 1 < nlanes; ++i)
         if (rx[i]) return fail(rx[i], "%s", ex[i].c_str());
+    return CRYOIM_OK;
+}
+
+// The learned form with its run-time fallback (cryoim_contract_opts.fallback): the
+// particles whose phase residual lies more than t robust standard deviations above the
+// call's median are searched again by the exhaustive contraction (same options, no
+// proposals) and keep whichever result has the lower phase residual.
+int contract_search_impl(Ctx* c, const float* imgs, bool on_device, cryoim_particle* parts, int P,
+                         const cryoim_contract_opts* opts, float* cands) {
+    if (c) c->last_fallbacks = 0;
+    if (!c || !opts || !(opts->fallback >= 0.0f)) return contract_impl(c, imgs, on_device, parts, P, opts, cands);
+    const bool fb = opts->fallback > 0.0f;
+    if (fb && (opts->learned <= 0 || opts->pick != 0))
+        return fail(CRYOIM_ERR_ARG, "fallback applies to the learned form with pick = 0");
+    if (!fb || !parts || P < 1) return contract_impl(c, imgs, on_device, parts, P, opts, cands);
+    std::vector<cryoim_particle> in(parts, parts + P);
+    int r = contract_impl(c, imgs, on_device, parts, P, opts, cands);
+    if (r) return r;
+    std::vector<float> v(P);
+    for (int i = 0; i < P; ++i) v[i] = parts[i].pr;
+    auto median = [](std::vector<float> x) {
+        const size_t m = x.size() / 2;
+        std::nth_element(x.begin(), x.begin() + m, x.end());
+        return x[m];
+    };
+    const float med = median(v);
+    std::vector<float> dev(P);
+    for (int i = 0; i < P; ++i) dev[i] = std::fabs(v[i] - med);
+    const float thr = med + opts->fallback * 1.4826f * median(dev);
+    std::vector<int> sel;
+    for (int i = 0; i < P; ++i)
+        if (v[i] > thr) sel.push_back(i);
+    if (sel.empty()) return CRYOIM_OK;
+    const int ns = (int)sel.size(), k = opts->topk;
+    const long nn = (long)c->p.fftsize * c->p.fftsize;
+    std::vector<cryoim_particle> sub(ns);
+    for (int j = 0; j < ns; ++j) sub[j] = in[sel[j]];
+    cryoim_contract_opts o2 = *opts;
+    o2.learned = 0;
+    o2.fallback = 0.0f;
+    std::vector<float> c2(cands ? (size_t)ns * k * 8 : 0);
+    if (on_device) {
+        DBuf<float> d;
+        if ((r = d.ensure((size_t)ns * nn))) return r;
+        for (int j = 0; j < ns; ++j)
+            CK(cudaMemcpyAsync(d.p + (size_t)j * nn, imgs + (size_t)sel[j] * nn, sizeof(float) * nn,
+                               cudaMemcpyDeviceToDevice, c->stream));
+        CK(cudaStreamSynchronize(c->stream));
+        r = contract_impl(c, d.p, true, sub.data(), ns, &o2, cands ? c2.data() : nullptr);
+    } else {
+        std::vector<float> h((size_t)ns * nn);
+        for (int j = 0; j < ns; ++j) std::memcpy(&h[(size_t)j * nn], imgs + (size_t)sel[j] * nn, sizeof(float) * nn);
+        r = contract_impl(c, h.data(), false, sub.data(), ns, &o2, cands ? c2.data() : nullptr);
+    }
+    if (r) return r;
+    for (int j = 0; j < ns; ++j)
+        if (sub[j].pr < parts[sel[j]].pr) {
+            parts[sel[j]] = sub[j];
+            if (cands) std::memcpy(cands + (size_t)sel[j] * k * 8, &c2[(size_t)j * k * 8], sizeof(float) * k * 8);
+        }
+    c->last_fallbacks = ns;
     return CRYOIM_OK;
 }
 
@@ -3254,12 +3327,36 @@ int cryoim_set_reference_map(void* ctx, const float* map3d) {
 
 int cryoim_contract_search(void* ctx, const float* imgs, cryoim_particle* parts, int32_t P,
                            const cryoim_contract_opts* opts, float* cands) {
-    return contract_impl(as_ctx(ctx), imgs, false, parts, P, opts, cands);
+    return contract_search_impl(as_ctx(ctx), imgs, false, parts, P, opts, cands);
 }
 
 int cryoim_contract_search_device(void* ctx, const float* d_imgs, cryoim_particle* parts, int32_t P,
                                   const cryoim_contract_opts* opts, float* cands) {
-    return contract_impl(as_ctx(ctx), d_imgs, true, parts, P, opts, cands);
+    return contract_search_impl(as_ctx(ctx), d_imgs, true, parts, P, opts, cands);
+}
+
+int cryoim_set_interpolation(void* ctx, int32_t kind, float sigma) {
+    Ctx* c = as_ctx(ctx);
+    if (!c) return fail(CRYOIM_ERR_ARG, "null context");
+    if (kind == 0) {
+        sigma = 0.0f;
+    } else if (kind != 1 || !(sigma >= 0.25f && sigma <= 2.0f)) {
+        return fail(CRYOIM_ERR_ARG, "interpolation: kind 0 (trilinear) or 1 (Gaussian, sigma 0.25..2 voxels)");
+    }
+    if (sigma != c->interp_sigma) {
+        c->interp_sigma = sigma;
+        c->bmat_ready = false;
+        c->bmat8_ready = false;
+        c->bmat_c_ready = false;
+    }
+    return CRYOIM_OK;
+}
+
+int cryoim_contract_fallbacks(void* ctx, int32_t* n) {
+    Ctx* c = as_ctx(ctx);
+    if (!c || !n) return fail(CRYOIM_ERR_ARG, "null argument");
+    *n = c->last_fallbacks;
+    return CRYOIM_OK;
 }
 
 int cryoim_learn_opts_default(cryoim_learn_opts* o) {

@@ -66,6 +66,37 @@ __global__ void k_map_band(const float2* __restrict__ ft, int nx, int R, float2*
     }
 }
 
+// Gaussian-kernel interpolation of the band cube (C^3 float2, frequency k at index
+// k + off): the 3 x 3 x 3 voxels around the nearest one to (x, y, z), each weighted by
+// exp(-d^2 / (2 sigma^2)) (gk = 1 / (2 sigma^2); the weight is separable in x, y, z),
+// normalised by the weights' sum.  |(x, y, z)| <= maxR keeps every tap inside the cube.
+__device__ __forceinline__ float2 gauss_sample(const float2* __restrict__ cube, int C, int off, float x, float y,
+                                               float z, float gk) {
+    const float rx = rintf(x), ry = rintf(y), rz = rintf(z);
+    float wx[3], wy[3], wz[3];
+#pragma unroll
+    for (int d = 0; d < 3; ++d) {
+        const float ex = x - (rx + (float)(d - 1)), ey = y - (ry + (float)(d - 1)), ez = z - (rz + (float)(d - 1));
+        wx[d] = expf(-gk * ex * ex);
+        wy[d] = expf(-gk * ey * ey);
+        wz[d] = expf(-gk * ez * ez);
+    }
+    const float2* b = cube + ((long)((int)rz + off - 1) * C + ((int)ry + off - 1)) * C + ((int)rx + off - 1);
+    float2 acc = make_float2(0.f, 0.f);
+#pragma unroll
+    for (int dz = 0; dz < 3; ++dz)
+#pragma unroll
+        for (int dy = 0; dy < 3; ++dy) {
+            const float2* r = b + ((long)dz * C + dy) * C;
+            const float w = wz[dz] * wy[dy];
+            const float2 v0 = r[0], v1 = r[1], v2 = r[2];
+            acc.x += w * (wx[0] * v0.x + wx[1] * v1.x + wx[2] * v2.x);
+            acc.y += w * (wx[0] * v0.y + wx[1] * v1.y + wx[2] * v2.y);
+        }
+    const float inv = 1.0f / ((wx[0] + wx[1] + wx[2]) * (wy[0] + wy[1] + wy[2]) * (wz[0] + wz[1] + wz[2]));
+    return make_float2(acc.x * inv, acc.y * inv);
+}
+
 // One CTA per orientation n = view * nomega + iomega: section samples in shared
 // memory, norm (FP32 per thread, FP64 across the block), then the unit-norm row in BF16
 // (Re, Im interleaved, zero pad).  The trilinear interpolation runs on the texture
@@ -75,7 +106,8 @@ __global__ void k_map_band(const float2* __restrict__ ft, int nx, int R, float2*
 __global__ void __launch_bounds__(512) k_slice_bf16(cudaTextureObject_t cube, int R,
                                                     const int2* __restrict__ samples, int S, int Kpad,
                                                     const float* __restrict__ views, int nom, float step,
-                                                    float d2r, long n0, __nv_bfloat162* __restrict__ B) {
+                                                    float d2r, long n0, __nv_bfloat162* __restrict__ B,
+                                                    const float2* __restrict__ lin, float gk) {
     extern __shared__ float2 ssec[];
     __shared__ double sh[32];
     __shared__ float rot[9];
@@ -89,7 +121,8 @@ __global__ void __launch_bounds__(512) k_slice_bf16(cudaTextureObject_t cube, in
         const int2 hk = samples[i];
         const float hx = (float)hk.x, ky = (float)hk.y;
         const float x = rot[0] * hx + rot[1] * ky, y = rot[3] * hx + rot[4] * ky, z = rot[6] * hx + rot[7] * ky;
-        const float2 val = tex3D<float2>(cube, x + off, y + off, z + off);
+        const float2 val = gk > 0.0f ? gauss_sample(lin, 2 * R + 3, R + 1, x, y, z, gk)
+                                     : tex3D<float2>(cube, x + off, y + off, z + off);
         ssec[i] = val;
         part += val.x * val.x + val.y * val.y;
     }
@@ -108,7 +141,8 @@ __global__ void __launch_bounds__(512) k_slice_bf16(cudaTextureObject_t cube, in
 __global__ void __launch_bounds__(512) k_slice_bf16_local(cudaTextureObject_t cube, int R,
                                                           const int2* __restrict__ samples, int S, int Kpad,
                                                           const float* __restrict__ centre, int m, float step,
-                                                          float d2r, long n0, __nv_bfloat162* __restrict__ B) {
+                                                          float d2r, long n0, __nv_bfloat162* __restrict__ B,
+                                                          const float2* __restrict__ lin, float gk) {
     extern __shared__ float2 ssec[];
     __shared__ double sh[32];
     __shared__ float rot[9];
@@ -127,7 +161,8 @@ __global__ void __launch_bounds__(512) k_slice_bf16_local(cudaTextureObject_t cu
         const int2 hk = samples[t];
         const float hx = (float)hk.x, ky = (float)hk.y;
         const float x = rot[0] * hx + rot[1] * ky, y = rot[3] * hx + rot[4] * ky, z = rot[6] * hx + rot[7] * ky;
-        const float2 val = tex3D<float2>(cube, x + off, y + off, z + off);
+        const float2 val = gk > 0.0f ? gauss_sample(lin, 2 * R + 3, R + 1, x, y, z, gk)
+                                     : tex3D<float2>(cube, x + off, y + off, z + off);
         ssec[t] = val;
         part += val.x * val.x + val.y * val.y;
     }
@@ -187,6 +222,7 @@ constexpr int AO = 8;
 __global__ void __launch_bounds__(256) k_build_a(const float2* __restrict__ band, const float* __restrict__ ctf,
                                                  Band bd, const int2* __restrict__ samples, int S, int Kpad,
                                                  const float* __restrict__ origins, int O,
+                                                 const float* __restrict__ poff,
                                                  const double* __restrict__ norm, float two_pi_over_n,
                                                  __nv_bfloat162* __restrict__ A) {
     extern __shared__ float2 ptab[];  // [AO][3 R + 2]
@@ -194,10 +230,12 @@ __global__ void __launch_bounds__(256) k_build_a(const float2* __restrict__ band
     const int no = min(AO, O - o0);
     const float2* b = band + (long)p * W * W;
     const float* c = ctf ? ctf + (long)p * W * W : nullptr;
-    const float h = (float)(bd.nx / 2);
+    // origins relative to the particle's own (poff) or absolute
+    const float hx = (float)(bd.nx / 2) + (poff ? poff[2 * p] : 0.0f);
+    const float hy = (float)(bd.nx / 2) + (poff ? poff[2 * p + 1] : 0.0f);
     const float inv = norm[p] > 0.0 ? (float)(1.0 / sqrt(norm[p])) : 0.0f;
     for (int j = 0; j < no; ++j) {
-        const float sx = origins[2 * (o0 + j)] + h, sy = origins[2 * (o0 + j) + 1] + h;
+        const float sx = origins[2 * (o0 + j)] + hx, sy = origins[2 * (o0 + j) + 1] + hy;
         for (int i = threadIdx.x; i < nt; i += blockDim.x) {
             const float a = i <= R ? two_pi_over_n * (sx * (float)i)
                                    : two_pi_over_n * (sy * (float)(i - 2 * R - 1));
@@ -377,7 +415,7 @@ constexpr int CC_SPLIT = 4;
 
 __global__ void k_cc_fp64(const float2* __restrict__ cube, const double2* __restrict__ pcband, Band bd,
                           const int2* __restrict__ samples, int S, const float* __restrict__ cand, int k,
-                          double* __restrict__ part) {
+                          double* __restrict__ part, double gk) {
     extern __shared__ double2 ctab[];  // [R + 1] per hx, then [2R + 1] per ky
     __shared__ double sh[32];
     __shared__ double rot[9];
@@ -410,26 +448,52 @@ __global__ void k_cc_fp64(const float2* __restrict__ cube, const double2* __rest
         const int2 hk = samples[i];
         const double x = rot[0] * hk.x + rot[1] * hk.y, y = rot[3] * hk.x + rot[4] * hk.y,
                      z = rot[6] * hk.x + rot[7] * hk.y;
-        // the cube holds FP32 values: its trilinear blend runs in FP32 at the FP64-rotated
-        // coordinates rounded once to FP32 (|x| <= maxR + 1: within 2^-17 px), the products
-        // and sums below in FP64
-        const float xf = (float)x, yf = (float)y, zf = (float)z;
-        const float fx = floorf(xf), fy = floorf(yf), fz = floorf(zf);
-        const int ix = (int)fx + off, iy = (int)fy + off, iz = (int)fz + off;
-        const float ax = xf - fx, ay = yf - fy, az = zf - fz;
-        const float2* cb0 = cube + ((long)iz * C + iy) * C + ix;
-        float2 r0, r1;
-        {
-            const float2 v000 = cb0[0], v001 = cb0[1], v010 = cb0[C], v011 = cb0[C + 1];
-            const float2 v100 = cb0[C * C], v101 = cb0[C * C + 1], v110 = cb0[C * C + C], v111 = cb0[C * C + C + 1];
-            const float2 a0 = make_float2(fmaf(ax, v001.x - v000.x, v000.x), fmaf(ax, v001.y - v000.y, v000.y));
-            const float2 a1 = make_float2(fmaf(ax, v011.x - v010.x, v010.x), fmaf(ax, v011.y - v010.y, v010.y));
-            const float2 a2 = make_float2(fmaf(ax, v101.x - v100.x, v100.x), fmaf(ax, v101.y - v100.y, v100.y));
-            const float2 a3 = make_float2(fmaf(ax, v111.x - v110.x, v110.x), fmaf(ax, v111.y - v110.y, v110.y));
-            r0 = make_float2(fmaf(ay, a1.x - a0.x, a0.x), fmaf(ay, a1.y - a0.y, a0.y));
-            r1 = make_float2(fmaf(ay, a3.x - a2.x, a2.x), fmaf(ay, a3.y - a2.y, a2.y));
+        double sr, si;
+        if (gk > 0.0) {
+            // Gaussian kernel in FP64 over the 27 voxels around the nearest one
+            const double rx = rint(x), ry = rint(y), rz = rint(z);
+            double wx[3], wy[3], wz[3];
+            for (int d = 0; d < 3; ++d) {
+                const double ex = x - (rx + (d - 1)), ey = y - (ry + (d - 1)), ez = z - (rz + (d - 1));
+                wx[d] = exp(-gk * ex * ex);
+                wy[d] = exp(-gk * ey * ey);
+                wz[d] = exp(-gk * ez * ez);
+            }
+            const float2* b0 = cube + ((long)((int)rz + off - 1) * C + ((int)ry + off - 1)) * C + ((int)rx + off - 1);
+            double ar = 0.0, ai = 0.0;
+            for (int dz = 0; dz < 3; ++dz)
+                for (int dy = 0; dy < 3; ++dy) {
+                    const float2* rr = b0 + ((long)dz * C + dy) * C;
+                    const double w = wz[dz] * wy[dy];
+                    ar += w * (wx[0] * rr[0].x + wx[1] * rr[1].x + wx[2] * rr[2].x);
+                    ai += w * (wx[0] * rr[0].y + wx[1] * rr[1].y + wx[2] * rr[2].y);
+                }
+            const double inv = 1.0 / ((wx[0] + wx[1] + wx[2]) * (wy[0] + wy[1] + wy[2]) * (wz[0] + wz[1] + wz[2]));
+            sr = ar * inv;
+            si = ai * inv;
+        } else {
+            // the cube holds FP32 values: its trilinear blend runs in FP32 at the FP64-rotated
+            // coordinates rounded once to FP32 (|x| <= maxR + 1: within 2^-17 px), the products
+            // and sums below in FP64
+            const float xf = (float)x, yf = (float)y, zf = (float)z;
+            const float fx = floorf(xf), fy = floorf(yf), fz = floorf(zf);
+            const int ix = (int)fx + off, iy = (int)fy + off, iz = (int)fz + off;
+            const float ax = xf - fx, ay = yf - fy, az = zf - fz;
+            const float2* cb0 = cube + ((long)iz * C + iy) * C + ix;
+            float2 r0, r1;
+            {
+                const float2 v000 = cb0[0], v001 = cb0[1], v010 = cb0[C], v011 = cb0[C + 1];
+                const float2 v100 = cb0[C * C], v101 = cb0[C * C + 1], v110 = cb0[C * C + C], v111 = cb0[C * C + C + 1];
+                const float2 a0 = make_float2(fmaf(ax, v001.x - v000.x, v000.x), fmaf(ax, v001.y - v000.y, v000.y));
+                const float2 a1 = make_float2(fmaf(ax, v011.x - v010.x, v010.x), fmaf(ax, v011.y - v010.y, v010.y));
+                const float2 a2 = make_float2(fmaf(ax, v101.x - v100.x, v100.x), fmaf(ax, v101.y - v100.y, v100.y));
+                const float2 a3 = make_float2(fmaf(ax, v111.x - v110.x, v110.x), fmaf(ax, v111.y - v110.y, v110.y));
+                r0 = make_float2(fmaf(ay, a1.x - a0.x, a0.x), fmaf(ay, a1.y - a0.y, a0.y));
+                r1 = make_float2(fmaf(ay, a3.x - a2.x, a2.x), fmaf(ay, a3.y - a2.y, a2.y));
+            }
+            sr = (double)fmaf(az, r1.x - r0.x, r0.x);
+            si = (double)fmaf(az, r1.y - r0.y, r0.y);
         }
-        const double sr = (double)fmaf(az, r1.x - r0.x, r0.x), si = (double)fmaf(az, r1.y - r0.y, r0.y);
         // cos/sin of tpn (sx hx + sy ky) from the two tabulated phasors
         const double2 ex = tx[hk.x], ey = ty[hk.y + R];
         const double cs = ex.x * ey.x - ex.y * ey.y, sn = ex.y * ey.x + ex.x * ey.y;
@@ -545,6 +609,7 @@ __global__ void k_particle_exp8(const float2* __restrict__ band, const float* __
 __global__ void __launch_bounds__(256) k_build_a8(const float2* __restrict__ band, const float* __restrict__ ctf,
                                                   Band bd, const int2* __restrict__ samples, int S, int Kpad8,
                                                   const float* __restrict__ origins, int O,
+                                                  const float* __restrict__ poff,
                                                   const double* __restrict__ norm, const float* __restrict__ mulA,
                                                   const int* __restrict__ fexp, float two_pi_over_n,
                                                   unsigned short* __restrict__ A8) {
@@ -553,7 +618,8 @@ __global__ void __launch_bounds__(256) k_build_a8(const float2* __restrict__ ban
     const float2* b = band + (long)p * W * W;
     const float* c = ctf ? ctf + (long)p * W * W : nullptr;
     const float h = (float)(bd.nx / 2);
-    const float sx = origins[2 * o] + h, sy = origins[2 * o + 1] + h;
+    const float sx = origins[2 * o] + h + (poff ? poff[2 * p] : 0.0f);
+    const float sy = origins[2 * o + 1] + h + (poff ? poff[2 * p + 1] : 0.0f);
     const float inv = norm[p] > 0.0 ? (float)(1.0 / sqrt(norm[p])) : 0.0f;
     const float pscale = ldexpf(1.0f, fexp[p]);
     unsigned short* row = A8 + ((long)p * O + o) * (Kpad8 / 2);
@@ -617,12 +683,12 @@ cudaError_t launch_b_to_e4m3(const void* B, long n, int Kpad, int S, const float
 
 void launch_build_a8(const float2* band, const float* ctf, Band bd, const int2* samples, int S, int Kpad8,
                      const float* origins, int O, const double* norm, const float* mulA, int* fexp, int B, void* A8,
-                     cudaStream_t st) {
+                     cudaStream_t st, const float* poff) {
     k_particle_exp8<<<B, 256, 0, st>>>(band, ctf, bd, samples, S, norm, mulA, fexp);
     dim3 g(O, B);
     const float tpn = 2.0f * host_angles().pi / (float)bd.nx;
     k_build_a8<<<g, 256, sizeof(float2) * (3 * bd.max_r + 2), st>>>(band, ctf, bd, samples, S, Kpad8, origins, O,
-                                                                     norm, mulA, fexp, tpn,
+                                                                     poff, norm, mulA, fexp, tpn,
                                   (unsigned short*)A8);
 }
 
@@ -669,7 +735,8 @@ void free_cube_texture(cudaArray_t arr, cudaTextureObject_t tex) {
 constexpr int SLICE_THREADS = 256;  // threads per section row
 cudaError_t launch_slice_bf16(cudaTextureObject_t cube, int R, const int2* samples, int S, int Kpad,
                               const float* views, int nom, float step, long n0, long count, void* B,
-                              cudaStream_t st) {
+                              cudaStream_t st, const float2* lin, float sigma) {
+    const float gk = (lin && sigma > 0.0f) ? 1.0f / (2.0f * sigma * sigma) : 0.0f;
     size_t sm = (size_t)S * sizeof(float2);
     cudaError_t e = cudaFuncSetAttribute(k_slice_bf16, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
     if (e != cudaSuccess) return e;
@@ -677,7 +744,7 @@ cudaError_t launch_slice_bf16(cudaTextureObject_t cube, int R, const int2* sampl
         long nb = count - c0 < 65535 ? count - c0 : 65535;
         k_slice_bf16<<<(unsigned)nb, SLICE_THREADS, sm, st>>>(cube, R, samples, S, Kpad, views, nom, step,
                                                    host_angles().deg2rad, n0 + c0,
-                                                   (__nv_bfloat162*)B + c0 * (Kpad / 2));
+                                                   (__nv_bfloat162*)B + c0 * (Kpad / 2), lin, gk);
     }
     return cudaGetLastError();
 }
@@ -686,7 +753,9 @@ cudaError_t launch_slice_bf16(cudaTextureObject_t cube, int R, const int2* sampl
 // threads per row keep the per-row norm reduction from dominating
 constexpr int LOCAL_SLICE_THREADS = 64;
 cudaError_t launch_slice_bf16_local(cudaTextureObject_t cube, int R, const int2* samples, int S, int Kpad,
-                                    const float* centre, int m, float step, long count, void* B, cudaStream_t st) {
+                                    const float* centre, int m, float step, long count, void* B, cudaStream_t st,
+                                    const float2* lin, float sigma) {
+    const float gk = (lin && sigma > 0.0f) ? 1.0f / (2.0f * sigma * sigma) : 0.0f;
     size_t sm = (size_t)S * sizeof(float2);
     cudaError_t e =
         cudaFuncSetAttribute(k_slice_bf16_local, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
@@ -695,7 +764,7 @@ cudaError_t launch_slice_bf16_local(cudaTextureObject_t cube, int R, const int2*
         long nb = count - c0 < 65535 ? count - c0 : 65535;
         k_slice_bf16_local<<<(unsigned)nb, LOCAL_SLICE_THREADS, sm, st>>>(cube, R, samples, S, Kpad, centre, m, step,
                                                          host_angles().deg2rad, c0,
-                                                         (__nv_bfloat162*)B + c0 * (Kpad / 2));
+                                                         (__nv_bfloat162*)B + c0 * (Kpad / 2), lin, gk);
     }
     return cudaGetLastError();
 }
@@ -706,12 +775,14 @@ void launch_particle_norm(const float2* band, const float* ctf, Band bd, const i
 }
 
 void launch_build_a(const float2* band, const float* ctf, Band bd, const int2* samples, int S, int Kpad,
-                    const float* origins, int O, const double* norm, int B, void* A, cudaStream_t st) {
+                    const float* origins, int O, const double* norm, int B, void* A, cudaStream_t st,
+                    const float* poff) {
     const float tpn = 2.0f * host_angles().pi / (float)bd.nx;
     dim3 ga((O + AO - 1) / AO, B);
     const int sm = (int)(sizeof(float2) * AO * (3 * bd.max_r + 2));
     if (sm > 48 * 1024) cudaFuncSetAttribute(k_build_a, cudaFuncAttributeMaxDynamicSharedMemorySize, sm);
-    k_build_a<<<ga, 256, sm, st>>>(band, ctf, bd, samples, S, Kpad, origins, O, norm, tpn, (__nv_bfloat162*)A);
+    k_build_a<<<ga, 256, sm, st>>>(band, ctf, bd, samples, S, Kpad, origins, O, poff, norm, tpn,
+                                   (__nv_bfloat162*)A);
 }
 
 void launch_select_topk(const float* topv, const int* topi, int O, int ntiles, int k, int B,
@@ -731,10 +802,11 @@ long cc_fp64_scratch(int k, int B) { return (long)k * B * CC_SPLIT * 3; }
 
 void launch_cc_fp64(const float2* cube, const double2* pcband, Band bd, const int2* samples, int S,
                     const float* cand, int k, int B, const double* pnorm, double* scratch, double* out,
-                    cudaStream_t st) {
+                    cudaStream_t st, float sigma) {
     dim3 g(k, B, CC_SPLIT);
     const size_t sm = sizeof(double2) * (3 * bd.max_r + 2);
-    k_cc_fp64<<<g, 256, sm, st>>>(cube, pcband, bd, samples, S, cand, k, scratch);
+    const double gk = sigma > 0.0f ? 1.0 / (2.0 * (double)sigma * (double)sigma) : 0.0;
+    k_cc_fp64<<<g, 256, sm, st>>>(cube, pcband, bd, samples, S, cand, k, scratch, gk);
     k_cc_fp64_finish<<<(k * B + 127) / 128, 128, 0, st>>>(scratch, k * B, CC_SPLIT, pnorm, k, out);
 }
 

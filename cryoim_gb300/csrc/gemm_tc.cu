@@ -54,9 +54,10 @@ using tc::mbar_expect_tx;
 using tc::mbar_arrive;
 using tc::sdesc;
 using tc::tmem_ld32;
-// Bounded wait with this kernel's limit (2 s).
-__device__ __forceinline__ bool mbar_wait(uint64_t* b, uint32_t par, int* err, bool abort_on_err) {
-    return tc::mbar_wait(b, par, err, abort_on_err, WAIT_NS);
+// Bounded wait with this kernel's limit (2 s, or the launch's own for the failure-path test).
+__device__ __forceinline__ bool mbar_wait(uint64_t* b, uint32_t par, int* err, bool abort_on_err,
+                                          unsigned long long wait_ns) {
+    return tc::mbar_wait(b, par, err, abort_on_err, wait_ns ? wait_ns : WAIT_NS);
 }
 __device__ __forceinline__ void tma_load_2d(void* dst, const CUtensorMap* tm, int c0, int c1,
                                             uint64_t* b) {
@@ -170,7 +171,12 @@ __global__ void __launch_bounds__(NTHREADS, 1)
             for (int t = blockIdx.x; t < total && ok; t += gridDim.x) {
                 const TileAt ta = tile_at(g, t);
                 for (int kb = 0; kb < g.kblocks; ++kb) {
-                    if (!mbar_wait(empty + s, ph ^ 1u, g.err, true)) { ok = false; break; }
+                    if (!mbar_wait(empty + s, ph ^ 1u, g.err, true, g.wait_ns)) { ok = false; break; }
+                    if (g.withhold && blockIdx.x == 0 && t == 0 && kb == g.withhold - 1) {
+                        // failure-path test: this stage is never loaded and its barrier never completes
+                        if (++s == NSTAGE) { s = 0; ph ^= 1u; }
+                        continue;
+                    }
                     mbar_expect_tx(full + s, STAGE_BYTES);
                     tma_load_2d(sA + s * A_BYTES, &tmA, kb * GK, ta.a_row, full + s);
                     tma_load_2d(sB + s * B_BYTES, &tmB, kb * GK, ta.b_row, full + s);
@@ -181,7 +187,7 @@ __global__ void __launch_bounds__(NTHREADS, 1)
             }
             // every issued copy lands before the CTA can exit
             for (int i = 0; i < NSTAGE; ++i)
-                if (used[i]) mbar_wait(full + i, last_par[i], g.err, false);
+                if (used[i]) mbar_wait(full + i, last_par[i], g.err, false, g.wait_ns);
         }
     } else if (warp == 1) {
         if (lane == 0) {
@@ -191,11 +197,11 @@ __global__ void __launch_bounds__(NTHREADS, 1)
             for (int t = blockIdx.x; t < total && ok; t += gridDim.x, ++lt) {
                 const int b = lt & 1;
                 const uint32_t aph = (uint32_t)(lt >> 1) & 1u;
-                if (!mbar_wait(acce + b, aph ^ 1u, g.err, true)) break;
+                if (!mbar_wait(acce + b, aph ^ 1u, g.err, true, g.wait_ns)) break;
                 tc_fence_after();
                 const uint32_t d = tmem + (uint32_t)(b * GN);
                 for (int kb = 0; kb < g.kblocks; ++kb) {
-                    if (!mbar_wait(full + s, ph, g.err, true)) { ok = false; break; }
+                    if (!mbar_wait(full + s, ph, g.err, true, g.wait_ns)) { ok = false; break; }
                     tc_fence_after();
                     const uint32_t a0 = su32(sA + s * A_BYTES), b0 = su32(sB + s * B_BYTES);
 #pragma unroll
@@ -208,7 +214,7 @@ __global__ void __launch_bounds__(NTHREADS, 1)
             }
             // all issued MMAs complete before TMEM is released
             tc_commit(drain);
-            mbar_wait(drain, 0, g.err, false);
+            mbar_wait(drain, 0, g.err, false, g.wait_ns);
         }
     } else {
         const int q = warp & 3;
@@ -217,7 +223,7 @@ __global__ void __launch_bounds__(NTHREADS, 1)
         for (int t = blockIdx.x; t < total; t += gridDim.x, ++lt) {
             const int b = lt & 1;
             const uint32_t aph = (uint32_t)(lt >> 1) & 1u;
-            if (!mbar_wait(accf + b, aph, g.err, true)) break;
+            if (!mbar_wait(accf + b, aph, g.err, true, g.wait_ns)) break;
             tc_fence_after();
             const TileAt ta = tile_at(g, t);
             const long row = (long)ta.mt * GM + row_in_tile;
@@ -356,7 +362,8 @@ cudaError_t launch_gemm_bf16_argmax(const void* a, const void* b, int M, int N, 
 // Kernel-level test hook (device pointers): C = A B^T with per-(row, 256-column tile)
 // max/argmax, optional full C.  d_err receives 1 if a pipeline wait timed out.
 static int gemm_hook(const void* d_a, const void* d_b, int32_t M, int32_t N, int32_t K, float* d_topv,
-                     int32_t* d_topi, float* d_c, int32_t* d_err, void* stream, bool f8) {
+                     int32_t* d_topi, float* d_c, int32_t* d_err, void* stream, bool f8, int withhold = 0,
+                     unsigned long long wait_ns = 0) {
     const int kq = f8 ? 128 : 64;
     if (!d_a || !d_b || !d_topv || !d_topi || !d_err) return CRYOIM_ERR_ARG;
     if (M < 1 || N < 1 || K < kq || K % kq) return CRYOIM_ERR_SIZE;
@@ -370,6 +377,8 @@ static int gemm_hook(const void* d_a, const void* d_b, int32_t M, int32_t N, int
     g.cfull = d_c;
     g.ldc = N;
     g.err = d_err;
+    g.withhold = withhold;
+    g.wait_ns = wait_ns;
     cudaStream_t st = (cudaStream_t)stream;
     if (cudaMemsetAsync(d_err, 0, sizeof(int), st) != cudaSuccess) return CRYOIM_ERR_CUDA;
     cudaError_t e = cryoim::launch_gemm_argmax(d_a, d_b, M, N, K, f8, g, sms, st);
@@ -386,4 +395,15 @@ extern "C" int cryoim_gemm_e4m3_argmax(const void* d_a, const void* d_b, int32_t
                                        int32_t K, float* d_topv, int32_t* d_topi, float* d_c,
                                        int32_t* d_err, void* stream) {
     return gemm_hook(d_a, d_b, M, N, K, d_topv, d_topi, d_c, d_err, stream, true);
+}
+
+// The failure path of the pipeline: CTA 0 leaves k-stage `stage` of its first tile
+// unloaded and every wait gives up after wait_us microseconds; *d_err comes back 1, the
+// kernel returns, its TMEM is released, and the next launch runs normally.
+extern "C" int cryoim_gemm_bf16_argmax_withhold(const void* d_a, const void* d_b, int32_t M, int32_t N,
+                                                int32_t K, float* d_topv, int32_t* d_topi, int32_t* d_err,
+                                                int32_t stage, int32_t wait_us, void* stream) {
+    if (stage < 0 || stage >= K / 64 || wait_us < 100 || wait_us > 2000000) return CRYOIM_ERR_ARG;
+    return gemm_hook(d_a, d_b, M, N, K, d_topv, d_topi, nullptr, d_err, stream, false, stage + 1,
+                     (unsigned long long)wait_us * 1000ull);
 }

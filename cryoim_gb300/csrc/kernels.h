@@ -152,6 +152,11 @@ struct GemmArgmaxArgs {
     int* err;      // set to 1 when a wait times out (zero it before the launch)
     const GemmGroup* groups = nullptr;  // device array, or nullptr for one product
     int ngroups = 0, total_tiles = 0;   // set by the grouped launcher
+    // tests of the failure path: a wait limit other than the default 2 s, and (withhold
+    // = s + 1) CTA 0's producer leaving k-stage s of its first tile unloaded, so that the
+    // issuer's wait for it runs out
+    unsigned long long wait_ns = 0;
+    int withhold = 0;
 };
 int gemm_tile_n();
 int gemm_tile_m();
@@ -177,17 +182,23 @@ cudaError_t make_cube_texture(const float2* cube, int R, cudaStream_t st, cudaAr
                               cudaTextureObject_t* tex);
 void free_cube_texture(cudaArray_t arr, cudaTextureObject_t tex);
 // Rows n0 .. n0+count-1 of B (orientation n = view * nom + iomega), unit norm, BF16.
+// sigma > 0 (with lin = the band cube in memory): Gaussian-kernel interpolation of
+// width sigma voxels over the 27 voxels around the nearest one instead of the texture's
+// trilinear filtering
 cudaError_t launch_slice_bf16(cudaTextureObject_t cube, int R, const int2* samples, int S, int Kpad,
                               const float* views, int nom, float step, long n0, long count, void* B,
-                              cudaStream_t st);
+                              cudaStream_t st, const float2* lin = nullptr, float sigma = 0.0f);
 // Rows of each particle's local grid (k_slice_bf16_local): count = particles x (2 m + 1)^3
 cudaError_t launch_slice_bf16_local(cudaTextureObject_t cube, int R, const int2* samples, int S, int Kpad,
-                                    const float* centre, int m, float step, long count, void* B, cudaStream_t st);
+                                    const float* centre, int m, float step, long count, void* B, cudaStream_t st,
+                                    const float2* lin = nullptr, float sigma = 0.0f);
 void launch_particle_norm(const float2* band, const float* ctf, Band bd, const int2* samples, int S,
                           int B, double* norm, cudaStream_t st, double2* pc = nullptr);
-// Rows (p, o) of A, p < B, o < O; origins: O x 2 (x, y) pixels.
+// Rows (p, o) of A, p < B, o < O; origins: O x 2 (x, y) pixels, absolute, or relative to
+// each particle's own origin poff[p] = (x, y) when poff is given.
 void launch_build_a(const float2* band, const float* ctf, Band bd, const int2* samples, int S, int Kpad,
-                    const float* origins, int O, const double* norm, int B, void* A, cudaStream_t st);
+                    const float* origins, int O, const double* norm, int B, void* A, cudaStream_t st,
+                    const float* poff = nullptr);
 // Best origin per (particle, tile) (tile_*: B x ntiles scratch), then the k best tiles
 // per particle: distinct orientations with their best origin and CC.
 void launch_select_topk(const float* topv, const int* topi, int O, int ntiles, int k, int B,
@@ -200,7 +211,7 @@ long cc_fp64_scratch(int k, int B);
 // FP64 and pnorm its FP64 norm (launch_particle_norm)
 void launch_cc_fp64(const float2* cube, const double2* pcband, Band bd, const int2* samples, int S,
                     const float* cand, int k, int B, const double* pnorm, double* scratch, double* out,
-                    cudaStream_t st);
+                    cudaStream_t st, float sigma = 0.0f);
 
 // ---- learned orientation proposer (learn.cu) ----
 constexpr int LP_NR = 64, LP_NT = 128;   // polar feature: radii over [minR, maxR] x angles over [0, 180)
@@ -264,7 +275,7 @@ cudaError_t launch_b_to_e4m3(const void* B, long n, int Kpad, int S, const float
                              cudaStream_t st);
 void launch_build_a8(const float2* band, const float* ctf, Band bd, const int2* samples, int S, int Kpad8,
                      const float* origins, int O, const double* norm, const float* mulA, int* fexp, int B, void* A8,
-                     cudaStream_t st);
+                     cudaStream_t st, const float* poff = nullptr);
 
 // ---- fsc.cu: half-map FSC and the FSC-weighted map ---------------------------
 struct FscArgs {

@@ -482,6 +482,17 @@ typedef struct cryoim_contract_opts {
                            orientations per particle).  The local form of sub-particle
                            refinement; no reference counterpart                      */
     float local_step;
+    float fallback;     /* learned form only.  0: off.  t > 0: run-time fallback to the
+                           exhaustive contraction: after the learned form, every
+                           particle whose phase residual exceeds the call's median by
+                           more than t robust standard deviations (1.4826 x the median
+                           absolute deviation) is searched again by the exhaustive
+                           BF16 contraction with the same options, and the result of
+                           lower phase residual is kept (pick = 0).  The count is
+                           returned by cryoim_contract_fallbacks                     */
+    int32_t centred_origins; /* 0: the origin grid is absolute.  1: it is centred on
+                           each particle's own (x, y) (the local form's re-centred
+                           origin search; PR rescoring is unaffected)                */
 } cryoim_contract_opts;
 
 /* ---- learned orientation proposer ------------------------------------------- */
@@ -552,6 +563,16 @@ int cryoim_contract_search(void* ctx, const float* imgs, cryoim_particle* parts,
                            const cryoim_contract_opts* opts, float* cands);
 int cryoim_contract_search_device(void* ctx, const float* d_imgs, cryoim_particle* parts, int32_t P,
                                   const cryoim_contract_opts* opts, float* cands);
+/* Interpolation of the central sections the contraction forms cut from the reference
+ * map (the BF16/FP8 section bank, the local grids and the FP64 rescoring): kind 0
+ * trilinear (the default, as project2d_FT3dTo2d.f90:30-83 interpolates), kind 1 a
+ * Gaussian kernel: the 27 voxels around the nearest one, weighted exp(-d^2/(2 sigma^2)),
+ * normalised by the weights' sum (sigma 0.25..2 voxels).  The reference has trilinear
+ * interpolation only.  Changing it rebuilds the section bank at the next search. */
+int cryoim_set_interpolation(void* ctx, int32_t kind, float sigma);
+/* Particles the last call of a contraction search sent to the exhaustive fallback
+ * (cryoim_contract_opts.fallback). */
+int cryoim_contract_fallbacks(void* ctx, int32_t* n);
 /* out[6]: section build ms, contraction ms and launches since the last call (timed when
  * profiling is on), contraction FLOP, orientations, padded K. Resets the counters. */
 int cryoim_contract_stats(void* ctx, double* out);
@@ -569,6 +590,14 @@ int cryoim_gemm_bf16_argmax(const void* d_a, const void* d_b, int32_t M, int32_t
 int cryoim_gemm_e4m3_argmax(const void* d_a, const void* d_b, int32_t M, int32_t N, int32_t K,
                             float* d_topv, int32_t* d_topi, float* d_c, int32_t* d_err,
                             void* stream);
+/* Test of the contraction kernel's failure path (device pointers as above, no full C):
+ * CTA 0 leaves k-stage `stage` (0 <= stage < K / 64) of its first tile unloaded, so the
+ * MMA issuer's wait for that stage cannot complete; every wait of the launch gives up
+ * after wait_us microseconds (100 .. 2,000,000).  *d_err is 1 afterwards, the kernel has
+ * returned with its TMEM released, and the next launch works.  No reference counterpart. */
+int cryoim_gemm_bf16_argmax_withhold(const void* d_a, const void* d_b, int32_t M, int32_t N, int32_t K,
+                                     float* d_topv, int32_t* d_topi, int32_t* d_err, int32_t stage,
+                                     int32_t wait_us, void* stream);
 
 /* ---- orientation bookkeeping (proc_icos) --------------------------------- */
 

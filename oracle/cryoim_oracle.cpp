@@ -907,6 +907,53 @@ void central_section(const R* fr, const R* fi, int nx, R th, R ph, R om, R* o_re
         }
 }
 
+/* The central section with a Gaussian interpolation kernel instead of the trilinear
+ * one (the reference interpolates trilinearly only; this restates the library's
+ * alternative, cryoim_set_interpolation kind 1): the geometry of central_section, and
+ * per sample the 27 voxels around the nearest one weighted exp(-d^2 / (2 sigma^2)),
+ * normalised by the weights' sum. */
+template <class R>
+void central_section_gauss(const R* fr, const R* fi, int nx, R th, R ph, R om, R sigma, R* o_re, R* o_im) {
+    R rot[9];
+    euler_mat(th, ph, om, rot);
+    long nn = (long)nx * nx;
+    int h = nx / 2;
+    std::fill(o_re, o_re + nn, R(0));
+    std::fill(o_im, o_im + nn, R(0));
+    const R g = R(1) / (R(2) * sigma * sigma);
+    long n = 0;
+    for (int iy = -h; iy <= h - 1; ++iy)
+        for (int ix = -h; ix <= h - 1; ++ix, ++n) {
+            R xp[3] = {(R)ix, (R)iy, R(0)}, xx[3];
+            mv3(rot, xp, xx);
+            if (std::sqrt(xx[0] * xx[0] + xx[1] * xx[1] + xx[2] * xx[2]) > (R)(h - 2)) continue;
+            int c0[3];
+            R w[3][3], ws[3];
+            for (int a = 0; a < 3; ++a) {
+                c0[a] = (int)std::nearbyint(xx[a]);
+                ws[a] = 0;
+                for (int d = 0; d < 3; ++d) {
+                    const R e = xx[a] - (R)(c0[a] + d - 1);
+                    w[a][d] = std::exp(-g * e * e);
+                    ws[a] += w[a][d];
+                }
+            }
+            R sr = 0, si = 0;
+            for (int dz = 0; dz < 3; ++dz)
+                for (int dy = 0; dy < 3; ++dy)
+                    for (int dx = 0; dx < 3; ++dx) {
+                        const long q = (long)(c0[2] + dz - 1 + h) * nn + (long)(c0[1] + dy - 1 + h) * nx +
+                                       (c0[0] + dx - 1 + h);
+                        const R wt = w[0][dx] * w[1][dy] * w[2][dz];
+                        sr += wt * fr[q];
+                        si += wt * fi[q];
+                    }
+            const R inv = R(1) / (ws[0] * ws[1] * ws[2]);
+            o_re[n] = sr * inv;
+            o_im[n] = si * inv;
+        }
+}
+
 /* ------------------------------------------------------------------------ */
 /* reconstruction                                                              */
 /* ------------------------------------------------------------------------ */
@@ -1976,6 +2023,10 @@ template <class R> void transform_ort(int to, R* th, R* ph, R* om, int n) {
     }                                                                                                  \
     extern "C" void orc_project_template2d_##S(const float* map, int nx, R th, R ph, R om, R* o) {  \
         project_template2d<R>(map, nx, th, ph, om, o);                                                 \
+    }                                                                                                  \
+    extern "C" void orc_central_section_gauss_##S(const R* fr, const R* fi, int nx, R th, R ph, R om, R sg,   \
+                                                   R* ore, R* oim) {                                       \
+        central_section_gauss<R>(fr, fi, nx, th, ph, om, sg, ore, oim);                                   \
     }                                                                                                  \
     extern "C" void orc_central_section_##S(const R* fr, const R* fi, int nx, R th, R ph, R om,     \
                                              R* orr, R* oi) {                                          \

@@ -300,6 +300,20 @@ def central_section(fre, fim, theta, phi, omega, fp="f32"):
     return ore, oim
 
 
+def central_section_gauss(fre, fim, theta, phi, omega, sigma, fp="f64"):
+    """The central section with the 27-voxel Gaussian kernel of width sigma voxels."""
+    dt = _dt(fp)
+    fre = np.ascontiguousarray(fre, dt)
+    fim = np.ascontiguousarray(fim, dt)
+    nx = fre.shape[-1]
+    ore = np.zeros((nx, nx), dt)
+    oim = np.zeros((nx, nx), dt)
+    R = _R(fp)
+    _fn("central_section_gauss", fp)(_p(fre), _p(fim), C.c_int(nx), R(theta), R(phi), R(omega), R(sigma),
+                                     _p(ore), _p(oim))
+    return ore, oim
+
+
 def reconstruct(params, imgs, parts, want_acc=False, fp="f64"):
     dt = _dt(fp)
     nx = params.fftsize

@@ -46,7 +46,7 @@ def params(name: str):
 
 def _project_chunk(args):
     vol, eulers = args
-    from cryoim_gb300 import synth
+    import synth
     return synth.project_numpy(vol, eulers)
 
 
@@ -60,7 +60,7 @@ class _PoolProjector:
     def __call__(self, vol, eulers):
         e = np.asarray(eulers)
         if self.workers <= 1 or len(e) < 4:
-            from cryoim_gb300 import synth
+            import synth
             return synth.project_numpy(vol, e)
         chunks = [c for c in np.array_split(e, min(len(e), 4 * self.workers)) if len(c)]
         with mp.get_context("spawn").Pool(self.workers) as pool:
@@ -77,7 +77,7 @@ def make(name: str):
     """(params, vol, tmpl, timgs, imgs, parts, truth) of the named workload (every
     particle of it: the draws of particle i depend on the particle count)."""
     import cryoim_gb300 as ci
-    from cryoim_gb300 import synth
+    import synth
     s = SPECS[name]
     P = s["particles"]
     proj = _PoolProjector(_workers())

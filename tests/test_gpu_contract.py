@@ -186,3 +186,44 @@ def test_pass_lanes_give_the_same_results(run, built, form):
     for ql, cl in out[1:]:
         assert np.array_equal(ql, out[0][0])
         assert np.array_equal(cl, out[0][1])
+
+
+@pytest.mark.parametrize("sigma", [0.5, 0.8])
+def test_gaussian_kernel_sections_match_oracle(run, built, orc, sigma):
+    """cryoim_set_interpolation(kind 1): the section bank, the FP64 rescoring and the
+    pick use the 27-voxel Gaussian kernel.  Every candidate's FP64 CC equals the
+    independent restatement with the oracle's Gaussian central section; the BF16 score of
+    the tensor-core contraction tracks it; noise-free particles still land on their
+    orientation."""
+    import cryoim_gb300 as ci
+    import synth
+    (p, vol, tmpl, timgs, imgs, parts, truth), q, cands, stats = run
+    with ci.Context(0, p) as ctx:
+        ctx.load_templates(timgs, tmpl)
+        ctx.set_reference_map(vol)
+        ctx.set_interpolation("gaussian", sigma)
+        qg = parts.copy()
+        cg = ctx.contract_search(imgs, qg, origin_max=2.0, origin_step=0.5, topk=8, want_cands=True, pick=1)
+        with pytest.raises(ci.CryoimError):
+            ctx.set_interpolation("gaussian", 5.0)
+    vol_ft = map_cube_full(vol)
+    n, R, r0 = p.fftsize, p.max_r, p.min_r
+    h = n // 2
+    ky, hx = np.meshgrid(np.arange(n) - h, np.arange(n) - h, indexing="ij")
+    d2 = hx ** 2 + ky ** 2
+    half = ((hx > 0) | ((hx == 0) & (ky > 0))) & (d2 >= r0 * r0) & (d2 <= R * R)
+    for i in range(len(parts)):
+        a, b, _ = orc.prep_particle(imgs[i], 1, p.imgmask_px, parts["x"][i], parts["y"][i], 0, r0, R, "f64")
+        ctf = orc.ctf2d(n, parts["df1"][i], parts["df2"][i], parts["astigang"][i], p.apix, p.vol, p.cs, p.ampwg,
+                        "f64")
+        for j in range(3):
+            c = cg[i, j].astype(np.float64)
+            sre, sim = orc.central_section_gauss(vol_ft.real, vol_ft.imag, *c[:3], sigma, fp="f64")
+            aa, bb = orc.centshift(a, b, c[3], c[4], "f64")
+            pr, pi = (aa * ctf)[half], (-bb * ctf)[half]
+            qr, qi = sre[half], sim[half]
+            want = np.sum(pr * qr + pi * qi) / np.sqrt(np.sum(pr * pr + pi * pi) * np.sum(qr * qr + qi * qi))
+            assert abs(c[6] - want) < 2e-5, (i, j, c[6], want)
+            assert abs(c[5] - c[6]) < 2e-2, (i, j, c[5], c[6])
+        err = synth.orientation_error((qg["theta"][i], qg["phi"][i], qg["omega"][i]), truth[i])
+        assert err < 1.5 * p.searchstep, (i, err)

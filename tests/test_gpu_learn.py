@@ -289,3 +289,38 @@ def test_render_matches_real_space_projection(built):
         cc = np.real(np.vdot(fa, fb)) / np.sqrt(np.vdot(fa, fa).real * np.vdot(fb, fb).real)
         ratio = np.linalg.norm(fa) / np.linalg.norm(fb)
         assert cc > 0.99 and 0.95 < ratio < 1.05, (i, cc, ratio)
+
+
+def test_learned_form_fallback_to_the_exhaustive_contraction(built):
+    """cryoim_contract_opts.fallback: particles whose phase residual lies more than t
+    robust standard deviations above the call's median are searched again by the
+    exhaustive contraction and keep the lower phase residual.  t = 1e9 sends none and
+    changes nothing; t = 1e-6 sends every particle above the median, each of which ends
+    with min(learned, exhaustive) phase residual and that form's pick."""
+    import cryoim_gb300 as ci
+    p, vol, tmpl, timgs, imgs, parts, truth = small_case(P=8, snr=0.5)
+    kw = dict(origin_max=2.0, origin_step=0.5, topk=8)
+    with ci.Context(0, p) as ctx:
+        ctx.load_templates(timgs, tmpl)
+        ctx.set_reference_map(vol)
+        ctx.learn_train(vol, samples=8192, batch=128, seed=3, snr=0.5, df_min=1.0, df_max=3.0, origin_max=2.0)
+        ql = parts.copy()
+        ctx.contract_search(imgs, ql, learned=16, **kw)
+        assert ctx.contract_fallbacks() == 0
+        qe = parts.copy()
+        ctx.contract_search(imgs, qe, **kw)
+        qn = parts.copy()
+        ctx.contract_search(imgs, qn, learned=16, fallback=1e9, **kw)
+        assert ctx.contract_fallbacks() == 0
+        assert np.array_equal(qn, ql)
+        qf = parts.copy()
+        ctx.contract_search(imgs, qf, learned=16, fallback=1e-6, **kw)
+        nf = ctx.contract_fallbacks()
+        with pytest.raises(ci.CryoimError):
+            ctx.contract_search(imgs, parts.copy(), fallback=1.0, **kw)  # not the learned form
+    sent = ql["pr"] > np.sort(ql["pr"])[len(ql) // 2]  # the library's median: the upper one
+    assert nf == int(sent.sum()) and nf >= 1
+    assert np.array_equal(qf[~sent], ql[~sent])
+    for i in np.nonzero(sent)[0]:
+        want = qe[i] if qe["pr"][i] < ql["pr"][i] else ql[i]
+        assert qf[i] == want, i

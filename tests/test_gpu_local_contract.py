@@ -96,3 +96,33 @@ def test_bad_local_options_are_refused(case):
             args.update(kw)
             with pytest.raises(ci.CryoimError):
                 ctx.contract_search(imgs, parts.copy(), **args)
+
+
+def test_centred_origin_grid_is_a_window_of_the_absolute_one(case):
+    """centred_origins: the origin grid sits around each particle's own (x, y).  With the
+    records' origins on the absolute grid, the centred +-1 px window is a subset of the
+    absolute +-3 px grid: where the absolute pick falls inside the window both forms
+    return the same orientation, origin and FP64 score."""
+    import cryoim_gb300 as ci
+    p, vol, tmpl, timgs, imgs, parts, truth = case
+    off = offsets(len(parts), 5)
+    q0 = parts.copy()
+    q0["theta"] = truth[:, 0] + STEP * off[:, 0]
+    q0["phi"] = truth[:, 1] + STEP * off[:, 1]
+    q0["omega"] = truth[:, 2] + STEP * off[:, 2]
+    q0["x"] = np.round(parts["x"] * 2) / 2 + 0.5
+    q0["y"] = np.round(parts["y"] * 2) / 2 - 0.5
+    kw = dict(origin_step=0.5, topk=8, pick=1, local_range=M * STEP, local_step=STEP)
+    with ci.Context(0, p) as ctx:
+        ctx.set_reference_map(vol)
+        qa = q0.copy()
+        ctx.contract_search(imgs, qa, origin_max=3.0, **kw)
+        qc = q0.copy()
+        cc = ctx.contract_search(imgs, qc, origin_max=1.0, centred_origins=True, want_cands=True, **kw)
+    assert np.all(np.abs(cc[:, :, 3] - q0["x"][:, None]) <= 1.0 + 1e-6)
+    assert np.all(np.abs(cc[:, :, 4] - q0["y"][:, None]) <= 1.0 + 1e-6)
+    inside = (np.abs(qa["x"] - q0["x"]) <= 1.0 + 1e-6) & (np.abs(qa["y"] - q0["y"]) <= 1.0 + 1e-6)
+    assert inside.sum() >= len(parts) // 2
+    for f in ("theta", "phi", "omega", "x", "y"):
+        np.testing.assert_allclose(qc[f][inside], qa[f][inside], atol=1e-5)
+    np.testing.assert_allclose(qc["pr"][inside], qa["pr"][inside], rtol=1e-6)

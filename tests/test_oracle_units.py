@@ -108,3 +108,33 @@ def test_norm(orc):
     img = rng.normal(3.0, 2.0, size=(32, 32))
     o = orc.norm(img, "f64")
     assert abs(o.mean()) < 1e-12 and abs(np.sqrt((o ** 2).mean()) - 1) < 1e-12
+
+
+def test_gaussian_section_known_answers(orc):
+    """The Gaussian-kernel section: a constant map gives the constant inside the cut;
+    at any orientation each sample equals the normalised 27-voxel sum restated in numpy."""
+    n, sig = 32, 0.7
+    c = np.full((n, n, n), 2.5)
+    sr, si = orc.central_section_gauss(c, 0 * c, 17.0, -40.0, 123.0, sig)
+    h = n // 2
+    iy, ix = np.meshgrid(np.arange(n) - h, np.arange(n) - h, indexing="ij")
+    inside = np.hypot(ix, iy) <= h - 2.5
+    assert np.abs(sr[inside] - 2.5).max() < 1e-12 and np.abs(si).max() == 0.0
+    rng = np.random.default_rng(4)
+    fr, fi = rng.normal(size=(2, n, n, n))
+    th, ph, om = 33.0, 71.0, -12.0
+    sr, si = orc.central_section_gauss(fr, fi, th, ph, om, sig)
+    R = orc.euler(th, ph, om, "f64")
+    for (y, x) in [(3, 4), (-7, 2), (0, -9), (10, 1)]:
+        X = R @ np.array([x, y, 0.0])
+        c0 = np.rint(X).astype(int)
+        acc, ws = 0j, 0.0
+        for dz in (-1, 0, 1):
+            for dy in (-1, 0, 1):
+                for dx in (-1, 0, 1):
+                    v = c0 + np.array([dx, dy, dz])
+                    w = np.exp(-np.sum((X - v) ** 2) / (2 * sig * sig))
+                    acc += w * (fr[v[2] + h, v[1] + h, v[0] + h] + 1j * fi[v[2] + h, v[1] + h, v[0] + h])
+                    ws += w
+        k = (y + h) * n + (x + h)
+        assert abs(sr.ravel()[k] - (acc / ws).real) < 1e-12 and abs(si.ravel()[k] - (acc / ws).imag) < 1e-12
