@@ -347,7 +347,7 @@ struct Ctx {
     DBuf<float4> sband;
     DBuf<int> xcount;
     DBuf<double> kpart;
-    DBuf<float2> tbandc;
+    DBuf<float4> tbandc;
     DBuf<int4> xgroups;
     DBuf<float> lcentre;  // local form: (theta, phi, omega) grid centre per particle of a group
     DBuf<GemmGroup> ggroups;
@@ -842,7 +842,12 @@ int ensure_bmat(Ctx* c) {
     if ((r = ensure_samples(c))) return r;
     const long n = (long)c->V * c->nom;
     if (c->bmat_ready && c->n_orient == n) return CRYOIM_OK;
-    if ((r = c->bmat.ensure((size_t)n * c->cKpad))) return r;
+    // rows n .. zrow + 7 are zero: rows zrow + j (j = 0..7) fill empty gather slots of
+    // residue j mod 8 in the proposal forms' slot lists
+    const long zrow = (n + 7) / 8 * 8;
+    if ((r = c->bmat.ensure((size_t)(zrow + 8) * c->cKpad))) return r;
+    CK(cudaMemsetAsync(c->bmat.p + (size_t)n * c->cKpad, 0, sizeof(*c->bmat.p) * (size_t)(zrow + 8 - n) * c->cKpad,
+                       c->stream));
     std::vector<float> v2(2 * (size_t)c->V);
     for (int v = 0; v < c->V; ++v) { v2[2 * v] = c->views[4 * v]; v2[2 * v + 1] = c->views[4 * v + 1]; }
     DBuf<float> dv;
@@ -983,6 +988,7 @@ int coarse_lists(Ctx* c, int nb, const float* ctfp, int kc, int nbf, std::vector
     launch_build_a(c->band.p, ctfp, c->bd, c->csamples_c.p, c->cS_c, c->cKpad_c, c->corigins_c.p, Oc, c->pnorm_c.p,
                    nb, c->amat_c.p, c->stream);
     GemmArgmaxArgs ga{};
+    ga.b_mode = 1;  // the coarse bank's rows are pre-swizzled
     ga.topv = c->topv_c.p;
     ga.topi = c->topi_c.p;
     ga.err = c->gerr.p;
@@ -1464,7 +1470,8 @@ int ensure_bmat8(Ctx* c) {
     if (c->bmat8_ready) return CRYOIM_OK;
     const int S = c->cS, nband = c->p.max_r + 2;
     const long n = c->n_orient;
-    if ((r = c->bmat8.ensure((size_t)n * c->cKpad8)) || (r = c->bandmax.ensure(nband)) ||
+    const long zrow8 = (n + 7) / 8 * 8;
+    if ((r = c->bmat8.ensure((size_t)(zrow8 + 8) * c->cKpad8)) || (r = c->bandmax.ensure(nband)) ||
         (r = c->mulA.ensure(S)) || (r = c->mulB.ensure(S)))
         return r;
     if (c->num_sms == 0) CK(cudaDeviceGetAttribute(&c->num_sms, cudaDevAttrMultiProcessorCount, c->device));
@@ -1494,6 +1501,8 @@ int ensure_bmat8(Ctx* c) {
     CK(cudaMemcpyAsync(c->mulA.p, ma.data(), sizeof(float) * S, cudaMemcpyHostToDevice, c->stream));
     CK(cudaMemcpyAsync(c->mulB.p, mb.data(), sizeof(float) * S, cudaMemcpyHostToDevice, c->stream));
     CK(launch_b_to_e4m3(c->bmat.p, n, c->cKpad, S, c->mulB.p, c->cKpad8, c->bmat8.p, c->stream));
+    CK(cudaMemsetAsync((unsigned char*)c->bmat8.p + (size_t)n * c->cKpad8, 0, (size_t)(zrow8 + 8 - n) * c->cKpad8,
+                       c->stream));
     CK(cudaEventRecord(e1, c->stream));
     CK(cudaEventSynchronize(e1));
     float ms = 0.f;
@@ -1764,12 +1773,13 @@ int contract_impl(Ctx* c, const float* imgs, bool on_device, cryoim_particle* pa
                                    L->amat.p + (size_t)(s0 - a0) * O * L->cKpad, L->stream, po);
             };
             GemmArgmaxArgs g{};
+            g.b_mode = 1;  // section rows are stored pre-swizzled (exhaustive and local tiles)
             g.topv = L->topv.p;
             g.topi = L->topi.p;
             g.cfull = nullptr;
             g.err = L->gerr.p;
             CK(cudaMemsetAsync(L->gerr.p, 0, sizeof(int), L->stream));
-            std::vector<std::vector<int>> lists;
+            std::vector<std::vector<int>> lists, slots;
             ngev = 0;
             if (kc > 0 || kl > 0 || local) {
                 // proposal forms: the coarse contraction or the learned proposer names each
@@ -1778,20 +1788,43 @@ int contract_impl(Ctx* c, const float* imgs, bool on_device, cryoim_particle* pa
                 if (!local &&
                     (r = kc > 0 ? coarse_lists(L, nb, ctfp, kc, nbf, lists) : learned_lists(L, nb, kl, nbf, lists)))
                     return r;
-                auto nrows_of = [&](int i) -> long { return local ? nloc : (long)lists[i].size(); };
                 CK(cudaMemsetAsync(L->gerr.p, 0, sizeof(int), L->stream));
                 const void* bsrc = f8 ? (const void*)L->bmat8.p : (const void*)L->bmat.p;
                 const char* abase = f8 ? (const char*)L->amat8.p : (const char*)L->amat.p;
                 build_rows(0, nb, 0);
                 CK(cudaGetLastError());
-                // particles in groups whose gathered sections stay under 8 GB: one gather and one
-                // grouped contraction (each particle's origin rows against its own sections) per
-                // group, then the k distinct best orientations of each particle
+                // the proposal forms gather their sections from the bank: per particle a slot
+                // list of bank rows, slot s of a tile holding a row of residue s mod 8 (the
+                // rows are stored pre-swizzled, so a row copied to a slot of its own residue
+                // is in the tensor cores' layout), empty slots the bank's zero row of that
+                // residue.  The local form cuts each particle's grid into the pass buffer at a
+                // start that is a multiple of 8.
+                const long zrow = (L->n_orient + 7) / 8 * 8;
+                const long lpitch = (nloc + 7) / 8 * 8;
+                if (!local) {
+                    slots.resize(nb);
+                    for (int i = 0; i < nb; ++i) {
+                        std::vector<int> bucket[8];
+                        for (int n : lists[i]) bucket[n & 7].push_back(n);
+                        size_t mx = 1;
+                        for (auto& bk : bucket) mx = std::max(mx, bk.size());
+                        const int ntp = (int)((mx + 31) / 32);
+                        slots[i].assign((size_t)ntp * 256, 0);
+                        for (int rho = 0; rho < 8; ++rho)
+                            for (int m = 0; m < 32 * ntp; ++m)
+                                slots[i][8 * (size_t)m + rho] =
+                                    m < (int)bucket[rho].size() ? bucket[rho][m] : (int)(zrow + rho);
+                    }
+                }
+                auto rows_of = [&](int i) -> long { return local ? lpitch : (long)slots[i].size(); };
+                // particles in groups whose sections stay under 8 GB: one gather (or cut) and
+                // one grouped contraction (each particle's origin rows against its own
+                // sections) per group, then the k distinct best orientations of each particle
                 for (int i0 = 0; i0 < nb;) {
                     int i1 = i0;
                     long rows = 0;
-                    while (i1 < nb && (i1 == i0 || (rows + nrows_of(i1)) * row_bytes <= (8L << 30)))
-                        rows += nrows_of(i1++);
+                    while (i1 < nb && (i1 == i0 || (rows + rows_of(i1)) * row_bytes <= (8L << 30)))
+                        rows += rows_of(i1++);
                     if ((r = L->bgather.ensure((size_t)rows * row_bytes))) return r;
                     if (local) {
                         std::vector<float> cen(3 * (size_t)(i1 - i0));
@@ -1804,11 +1837,11 @@ int contract_impl(Ctx* c, const float* imgs, bool on_device, cryoim_particle* pa
                                            L->stream));
                         CK(launch_slice_bf16_local(ltex.tex, L->p.max_r, L->csamples.p, L->cS, L->cKpad, L->lcentre.p,
                                                    lm, opts->local_step, rows, L->bgather.p, L->stream,
-                                                   c->mapcube.p, c->interp_sigma));
+                                                   c->mapcube.p, c->interp_sigma, lpitch));
                     } else {
                         std::vector<int> idx;
                         idx.reserve(rows);
-                        for (int i = i0; i < i1; ++i) idx.insert(idx.end(), lists[i].begin(), lists[i].end());
+                        for (int i = i0; i < i1; ++i) idx.insert(idx.end(), slots[i].begin(), slots[i].end());
                         if ((r = L->gidx.ensure(rows))) return r;
                         CK(cudaMemcpyAsync(L->gidx.p, idx.data(), sizeof(int) * rows, cudaMemcpyHostToDevice,
                                            L->stream));
@@ -1818,7 +1851,7 @@ int contract_impl(Ctx* c, const float* imgs, bool on_device, cryoim_particle* pa
                     std::vector<int2> seg(i1 - i0);
                     long roff = 0, toff = 0;
                     for (int i = i0; i < i1; ++i) {
-                        const int nl = (int)nrows_of(i);
+                        const int nl = (int)(local ? nloc : (long)slots[i].size());
                         const int ntp = (nl + gemm_tile_n() - 1) / gemm_tile_n();
                         GemmGroup& q = hg[i - i0];
                         q.a_row0 = i * O;
@@ -1827,9 +1860,12 @@ int contract_impl(Ctx* c, const float* imgs, bool on_device, cryoim_particle* pa
                         q.n_valid = nl;
                         q.topv_off = (int)toff;
                         seg[i - i0] = make_int2((int)toff, ntp);
-                        roff += nl;
+                        roff += local ? lpitch : nl;
                         toff += (long)O * ntp;
-                        if (L->prof) L->prof_gemm_flops += 2.0 * (double)O * (double)nl * (double)kpad;
+                        // the useful work: the particle's listed orientations (not padding slots)
+                        if (L->prof)
+                            L->prof_gemm_flops += 2.0 * (double)O * (double)(local ? nloc : (long)lists[i].size()) *
+                                                  (double)kpad;
                     }
                     if ((r = L->ggroups.ensure(i1 - i0)) || (r = L->gseg.ensure(i1 - i0))) return r;
                     if (L->prof && (r = gmark(ngev++))) return r;
@@ -1877,9 +1913,12 @@ int contract_impl(Ctx* c, const float* imgs, bool on_device, cryoim_particle* pa
             if (gerr) return fail(CRYOIM_ERR_CUDA, "contraction pipeline wait timed out");
             if (f8)  // remove the per-particle exponent: the CC of the unit-norm rows
                 for (int i = 0; i < nb * k; ++i) hcc[i] = std::ldexp(hcc[i], -hfe[i / k]);
-            if (kc > 0 || kl > 0)  // gathered column -> fine orientation index
+            if (kc > 0 || kl > 0)  // gather slot -> fine orientation index (zero rows: none)
                 for (int i = 0; i < nb * k; ++i)
-                    if (hor[i] >= 0) hor[i] = lists[i / k][hor[i]];
+                    if (hor[i] >= 0) {
+                        const int n = slots[i / k][hor[i]];
+                        hor[i] = n < L->n_orient ? n : -1;
+                    }
             if (L->prof)
                 for (size_t e = 0; e + 1 < ngev; e += 2) {
                     float ms = 0.f;

@@ -97,6 +97,20 @@ __device__ __forceinline__ float2 gauss_sample(const float2* __restrict__ cube, 
     return make_float2(acc.x * inv, acc.y * inv);
 }
 
+// Section rows are stored pre-swizzled: within each 128-byte block of K, the 16-byte
+// chunk c of row r sits at chunk c ^ (r & 7), the order in which a TMA load with the
+// 128-byte swizzle would place it in shared memory.  A row copied verbatim into a tile
+// row of the same residue mod 8 (a TMA box without swizzle) is then already in the
+// layout the tensor cores read.  Index of
+// (Re, Im) pair i of row r: BF16 rows hold 32 pairs per block (4 per chunk), FP8 rows 64
+// (8 per chunk).
+__device__ __forceinline__ long bf16_pair_at(long i, long r) {
+    return (i & ~31L) | ((((i >> 2) & 7) ^ (r & 7)) << 2) | (i & 3);
+}
+__device__ __forceinline__ long fp8_pair_at(long i, long r) {
+    return (i & ~63L) | ((((i >> 3) & 7) ^ (r & 7)) << 3) | (i & 7);
+}
+
 // One CTA per orientation n = view * nomega + iomega: section samples in shared
 // memory, norm (FP32 per thread, FP64 across the block), then the unit-norm row in BF16
 // (Re, Im interleaved, zero pad).  The trilinear interpolation runs on the texture
@@ -117,6 +131,8 @@ __global__ void __launch_bounds__(512) k_slice_bf16(cudaTextureObject_t cube, in
     __syncthreads();
     const float off = (float)(R + 1) + 0.5f;
     float part = 0.0f;
+    // four samples per step: their fetches are independent and in flight together
+#pragma unroll 4
     for (int i = threadIdx.x; i < S; i += blockDim.x) {
         const int2 hk = samples[i];
         const float hx = (float)hk.x, ky = (float)hk.y;
@@ -131,25 +147,27 @@ __global__ void __launch_bounds__(512) k_slice_bf16(cudaTextureObject_t cube, in
     __nv_bfloat162* row = B + (long)blockIdx.x * (Kpad / 2);
     for (int i = threadIdx.x; i < Kpad / 2; i += blockDim.x) {
         float2 val = i < S ? ssec[i] : make_float2(0.f, 0.f);
-        row[i] = __floats2bfloat162_rn(val.x * inv, val.y * inv);
+        row[bf16_pair_at(i, n)] = __floats2bfloat162_rn(val.x * inv, val.y * inv);
     }
 }
 
 // Local grids: one CTA per (particle p, grid point l) with l = (i * n + j) * n + k,
 // n = 2 m + 1, orientation (theta_p + (i - m) s, phi_p + (j - m) s, omega_p + (k - m) s)
-// from centre[3 p ..]; the row is built exactly as k_slice_bf16 builds it.
+// from centre[3 p ..]; particle p's rows start at row p * lpitch (lpitch >= n^3); the
+// row is built exactly as k_slice_bf16 builds it.
 __global__ void __launch_bounds__(512) k_slice_bf16_local(cudaTextureObject_t cube, int R,
                                                           const int2* __restrict__ samples, int S, int Kpad,
                                                           const float* __restrict__ centre, int m, float step,
                                                           float d2r, long n0, __nv_bfloat162* __restrict__ B,
-                                                          const float2* __restrict__ lin, float gk) {
+                                                          const float2* __restrict__ lin, float gk, long lpitch) {
     extern __shared__ float2 ssec[];
     __shared__ double sh[32];
     __shared__ float rot[9];
     const int n = 2 * m + 1;
     const long nloc = (long)n * n * n;
     const long q = n0 + blockIdx.x;
-    const int p = (int)(q / nloc), l = (int)(q % nloc);
+    const int p = (int)(q / lpitch), l = (int)(q % lpitch);
+    if (l >= nloc) return;  // padding row between particles' grids (never a valid column)
     const int i = l / (n * n), j = (l / n) % n, k = l % n;
     if (threadIdx.x == 0)
         euler_mat(centre[3 * p] + step * (float)(i - m), centre[3 * p + 1] + step * (float)(j - m),
@@ -157,6 +175,7 @@ __global__ void __launch_bounds__(512) k_slice_bf16_local(cudaTextureObject_t cu
     __syncthreads();
     const float off = (float)(R + 1) + 0.5f;
     float part = 0.0f;
+#pragma unroll 4
     for (int t = threadIdx.x; t < S; t += blockDim.x) {
         const int2 hk = samples[t];
         const float hx = (float)hk.x, ky = (float)hk.y;
@@ -171,7 +190,7 @@ __global__ void __launch_bounds__(512) k_slice_bf16_local(cudaTextureObject_t cu
     __nv_bfloat162* row = B + (long)blockIdx.x * (Kpad / 2);
     for (int t = threadIdx.x; t < Kpad / 2; t += blockDim.x) {
         float2 val = t < S ? ssec[t] : make_float2(0.f, 0.f);
-        row[t] = __floats2bfloat162_rn(val.x * inv, val.y * inv);
+        row[bf16_pair_at(t, q)] = __floats2bfloat162_rn(val.x * inv, val.y * inv);
     }
 }
 
@@ -552,7 +571,7 @@ __global__ void k_band_absmax(const __nv_bfloat162* __restrict__ B, long n, int 
     for (long r = (long)blockIdx.x * stride; r < n; r += (long)gridDim.x * stride) {
         const __nv_bfloat162* row = B + r * (Kpad / 2);
         for (int i = threadIdx.x; i < S; i += blockDim.x) {
-            const float2 v = __bfloat1622float2(row[i]);
+            const float2 v = __bfloat1622float2(row[bf16_pair_at(i, r)]);
             const float m = fmaxf(fabsf(v.x), fabsf(v.y));
             atomicMax(&smax[sample_band(samples[i])], __float_as_uint(m));
         }
@@ -571,11 +590,11 @@ __global__ void k_b_to_e4m3(const __nv_bfloat162* __restrict__ B, int Kpad, int 
     for (int i = threadIdx.x; i < Kpad8 / 2; i += blockDim.x) {
         float2 v = make_float2(0.f, 0.f);
         if (i < S) {
-            v = __bfloat1622float2(row[i]);
+            v = __bfloat1622float2(row[bf16_pair_at(i, r)]);
             v.x *= mulB[i];
             v.y *= mulB[i];
         }
-        out[i] = __nv_cvt_float2_to_fp8x2(v, __NV_SATFINITE, __NV_E4M3);
+        out[fp8_pair_at(i, r)] = __nv_cvt_float2_to_fp8x2(v, __NV_SATFINITE, __NV_E4M3);
     }
 }
 
@@ -754,7 +773,8 @@ cudaError_t launch_slice_bf16(cudaTextureObject_t cube, int R, const int2* sampl
 constexpr int LOCAL_SLICE_THREADS = 64;
 cudaError_t launch_slice_bf16_local(cudaTextureObject_t cube, int R, const int2* samples, int S, int Kpad,
                                     const float* centre, int m, float step, long count, void* B, cudaStream_t st,
-                                    const float2* lin, float sigma) {
+                                    const float2* lin, float sigma, long lpitch) {
+    if (lpitch <= 0) lpitch = (long)(2 * m + 1) * (2 * m + 1) * (2 * m + 1);
     const float gk = (lin && sigma > 0.0f) ? 1.0f / (2.0f * sigma * sigma) : 0.0f;
     size_t sm = (size_t)S * sizeof(float2);
     cudaError_t e =
@@ -764,7 +784,7 @@ cudaError_t launch_slice_bf16_local(cudaTextureObject_t cube, int R, const int2*
         long nb = count - c0 < 65535 ? count - c0 : 65535;
         k_slice_bf16_local<<<(unsigned)nb, LOCAL_SLICE_THREADS, sm, st>>>(cube, R, samples, S, Kpad, centre, m, step,
                                                          host_angles().deg2rad, c0,
-                                                         (__nv_bfloat162*)B + c0 * (Kpad / 2), lin, gk);
+                                                         (__nv_bfloat162*)B + c0 * (Kpad / 2), lin, gk, lpitch);
     }
     return cudaGetLastError();
 }

@@ -275,7 +275,7 @@ PFN_cuTensorMapEncodeTiled_v12000 encode_fn() {
 
 // rows x k elements (BF16, or FP8 as bytes), row-major (k contiguous), box = 128 bytes
 // of k x box_rows, 128-byte swizzle
-bool make_map(CUtensorMap* m, const void* base, long rows, int k, int box_rows, bool f8) {
+bool make_map(CUtensorMap* m, const void* base, long rows, int k, int box_rows, bool f8, bool swizzle = true) {
     auto fn = encode_fn();
     if (!fn) return false;
     const int esz = f8 ? 1 : 2;
@@ -285,7 +285,8 @@ bool make_map(CUtensorMap* m, const void* base, long rows, int k, int box_rows, 
     cuuint32_t es[2] = {1, 1};
     CUresult r = fn(m, f8 ? CU_TENSOR_MAP_DATA_TYPE_UINT8 : CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2,
                     const_cast<void*>(base), dims, strides, box,
-                    es, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B,
+                    es, CU_TENSOR_MAP_INTERLEAVE_NONE,
+                    swizzle ? CU_TENSOR_MAP_SWIZZLE_128B : CU_TENSOR_MAP_SWIZZLE_NONE,
                     CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
     return r == CUDA_SUCCESS;
 }
@@ -301,7 +302,8 @@ cudaError_t launch_gemm_argmax(const void* a, const void* b, int M, int N, int K
     if (K % gk != 0 || M < 1 || N < 1) return cudaErrorInvalidValue;
     if (((uintptr_t)a & 15) || ((uintptr_t)b & 15)) return cudaErrorInvalidValue;
     CUtensorMap ta, tb;
-    if (!make_map(&ta, a, M, K, GM, f8) || !make_map(&tb, b, N, K, GN, f8)) return cudaErrorInvalidValue;
+    if (!make_map(&ta, a, M, K, GM, f8) || !make_map(&tb, b, N, K, GN, f8, in.b_mode == 0))
+        return cudaErrorInvalidValue;
     GemmArgmaxArgs g = in;
     g.m_tiles = (M + GM - 1) / GM;
     g.n_tiles = (N + GN - 1) / GN;
@@ -335,8 +337,12 @@ cudaError_t launch_gemm_argmax_grouped(const void* a, long Mtot, const void* b, 
         total += (long)q.m_tiles * q.n_tiles;
     }
     if (total > (1L << 30)) return cudaErrorInvalidValue;
+    if (in.b_mode == 1)  // pre-swizzled rows: every group's tiles start at a multiple of 8 rows
+        for (int i = 0; i < ngroups; ++i)
+            if (hg[i].b_row0 % 8) return cudaErrorInvalidValue;
     CUtensorMap ta, tb;
-    if (!make_map(&ta, a, Mtot, K, GM, f8) || !make_map(&tb, b, Ntot, K, GN, f8)) return cudaErrorInvalidValue;
+    if (!make_map(&ta, a, Mtot, K, GM, f8) || !make_map(&tb, b, Ntot, K, GN, f8, in.b_mode == 0))
+        return cudaErrorInvalidValue;
     cudaError_t e = cudaMemcpyAsync(dg, hg, sizeof(GemmGroup) * ngroups, cudaMemcpyHostToDevice, st);
     if (e != cudaSuccess) return e;
     GemmArgmaxArgs g = in;

@@ -106,7 +106,8 @@ struct PrSingleArgs {
     const float4* sband = nullptr;  // [B][W*W] band shifted to the candidates' common origin, in
                                     // (pixel, right neighbour) pairs (launch_shift_band)
     const int* ncount = nullptr;    // [B] candidates in use (later slots are skipped), or nullptr
-    const float2* tbandc = nullptr; // [B][T][W*W] templates x CTF (launch_tband_ctf), or nullptr
+    const float4* tbandc = nullptr; // [B][T][W*W] templates x CTF as (pixel, right neighbour) pairs
+                                    // (launch_tband_ctf), or nullptr
 };
 // cal_crosslin_PR for each candidate, its origin shift applied to every tap (k_pr_single)
 cudaError_t launch_pr_single(const PrSingleArgs& a, int B, cudaStream_t st);
@@ -114,7 +115,9 @@ cudaError_t launch_pr_single(const PrSingleArgs& a, int B, cudaStream_t st);
 // candidate slot, count <= pr_rescore_group_size(), 0); requires sband
 cudaError_t launch_pr_rescore_groups(const PrSingleArgs& a, const int4* groups, int ngroups, cudaStream_t st);
 int pr_rescore_group_size();
-cudaError_t launch_tband_ctf(const float2* tband, int T, const float* ctf, const Band& bd, int B, float2* out,
+// the templates x each particle's CTF, each pixel stored with its right neighbour (zero
+// past the row's end), so a bilinear sample reads two 16-byte pairs
+cudaError_t launch_tband_ctf(const float2* tband, int T, const float* ctf, const Band& bd, int B, float4* out,
                              cudaStream_t st);
 // sband for PrSingleArgs: the band of each particle shifted to cand[p][0]'s origin, each
 // pixel stored with its right neighbour
@@ -157,6 +160,10 @@ struct GemmArgmaxArgs {
     // issuer's wait for it runs out
     unsigned long long wait_ns = 0;
     int withhold = 0;
+    // operand B: 0 plain rows (the TMA load applies the 128-byte swizzle); 1 pre-swizzled
+    // rows (contract.cu's section rows) loaded by TMA tiles without swizzle, every tile
+    // starting at a multiple of 8 rows (so a row's residue mod 8 is its slot's)
+    int b_mode = 0;
 };
 int gemm_tile_n();
 int gemm_tile_m();
@@ -191,7 +198,7 @@ cudaError_t launch_slice_bf16(cudaTextureObject_t cube, int R, const int2* sampl
 // Rows of each particle's local grid (k_slice_bf16_local): count = particles x (2 m + 1)^3
 cudaError_t launch_slice_bf16_local(cudaTextureObject_t cube, int R, const int2* samples, int S, int Kpad,
                                     const float* centre, int m, float step, long count, void* B, cudaStream_t st,
-                                    const float2* lin = nullptr, float sigma = 0.0f);
+                                    const float2* lin = nullptr, float sigma = 0.0f, long lpitch = 0);
 void launch_particle_norm(const float2* band, const float* ctf, Band bd, const int2* samples, int S,
                           int B, double* norm, cudaStream_t st, double2* pc = nullptr);
 // Rows (p, o) of A, p < B, o < O; origins: O x 2 (x, y) pixels, absolute, or relative to
@@ -265,10 +272,11 @@ void launch_lp_topk(float* sc, int B, int V, int k, int* cell, float* val, cudaS
 // topv/topi + seg[b].x with distinct columns -> col, origin, cc [B][k]
 void launch_select_distinct(float* topv, const int* topi, int O, const int2* seg, int B, int k, int* col,
                             int* origin, float* cc, cudaStream_t st);
-cudaError_t launch_gather_rows(const void* src, long row_bytes, const int* idx, int n, void* dst, cudaStream_t st);
 // FP8-e4m3 operands (contract.cu): per-band max |B| (R+1 bands, float bits) over every
 // stride-th row; B8 = e4m3(B x mulB) with rows of Kpad8 bytes; A8 rows with mulA and the
 // per-particle exponent fexp (written by launch_build_a8).
+// rows idx[0 .. n) of src (row_bytes each, a multiple of 16) into consecutive rows of dst
+cudaError_t launch_gather_rows(const void* src, long row_bytes, const int* idx, int n, void* dst, cudaStream_t st);
 cudaError_t launch_band_absmax(const void* B, long n, int Kpad, const int2* samples, int S, int nband, int stride,
                                unsigned* out, int sms, cudaStream_t st);
 cudaError_t launch_b_to_e4m3(const void* B, long n, int Kpad, int S, const float* mulB, int Kpad8, void* B8,

@@ -625,9 +625,23 @@ __global__ void __launch_bounds__(256) k_loss(const float* __restrict__ sc, int 
     const float* x = sc + (long)b * n;
     const float* tr = truth + 4 * b;
     const float rad2deg = 57.29577951308232f;
-    float mx = -3.0e38f;
-    for (long q = threadIdx.x; q < n; q += blockDim.x) mx = fmaxf(mx, x[q]);
+    // the target's exponent -(av^2 + as^2) is taken relative to its largest value over the
+    // cells (the normalised target is unchanged), so its sum is >= 1 even for a label far
+    // from every view class (an orientation at an asymmetric-unit edge that no operator
+    // folds inside in FP32)
+    float mx = -3.0e38f, dmin = 3.0e38f;
+    for (long q = threadIdx.x; q < n; q += blockDim.x) {
+        mx = fmaxf(mx, x[q]);
+        const int v = (int)(q / NT), s = (int)(q % NT);
+        const float dot = vview[3 * v] * tr[0] + vview[3 * v + 1] * tr[1] + vview[3 * v + 2] * tr[2];
+        const float av = acosf(fminf(fmaxf(dot, -1.f), 1.f)) * rad2deg / sv;
+        int ds = abs(s - (int)tr[3]) % NT;
+        ds = min(ds, NT - ds);
+        const float as = (float)ds / ss;
+        dmin = fminf(dmin, av * av + as * as);
+    }
     mx = block_max(mx, sh);
+    dmin = -block_max(-dmin, sh);
     float se = 0.f, st = 0.f, stx = 0.f;
     for (long q = threadIdx.x; q < n; q += blockDim.x) {
         const int v = (int)(q / NT), s = (int)(q % NT);
@@ -637,7 +651,7 @@ __global__ void __launch_bounds__(256) k_loss(const float* __restrict__ sc, int 
         int ds = abs(s - (int)tr[3]) % NT;
         ds = min(ds, NT - ds);
         const float as = (float)ds / ss;
-        const float tg = expf(-av * av - as * as);
+        const float tg = expf(dmin - av * av - as * as);
         st += tg;
         stx += tg * (x[q] - mx);
     }
@@ -654,7 +668,7 @@ __global__ void __launch_bounds__(256) k_loss(const float* __restrict__ sc, int 
         int ds = abs(s - (int)tr[3]) % NT;
         ds = min(ds, NT - ds);
         const float as = (float)ds / ss;
-        const float tg = expf(-av * av - as * as);
+        const float tg = expf(dmin - av * av - as * as);
         dsc[(long)b * n + q] = (expf(x[q] - mx) * ise - tg * ist) * ib;
     }
 }

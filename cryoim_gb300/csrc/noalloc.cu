@@ -12,7 +12,9 @@
 // The array lives for the lifetime of the process on every GPU that loads the
 // library.  In host code its name is only a host-side stand-in, so the device address
 // is looked up once per device with cudaGetSymbolAddress (first call on that device,
-// which also copies the 60 symmetry operators into it) and passed to the kernels.
+// which also copies the 60 symmetry operators into it) and passed to the kernels.  That
+// address and table are kept for the life of the process, so the entry point must not
+// be used across a cudaDeviceReset of the device.
 #include <cuda_runtime.h>
 
 #include <cstring>
@@ -97,6 +99,8 @@ extern "C" int cryoim_prscore_noalloc(int32_t nx, int32_t min_r, int32_t max_r,
         return set_error(CRYOIM_ERR_SIZE, "cryoim_prscore_noalloc: K must be 1..CRYOIM_NOALLOC_MAX_CANDIDATES");
     if (max_r - min_r + 1 > kMaxR)
         return set_error(CRYOIM_ERR_SIZE, "cryoim_prscore_noalloc: max_r-min_r+1 exceeds CRYOIM_NOALLOC_MAX_RADII");
+    // errors left pending on this thread by earlier work are not this call's
+    (void)cudaGetLastError();
     int err = CRYOIM_OK;
     float* s = scratch_for_current_device(&err);
     if (!s) return err;
@@ -109,12 +113,18 @@ extern "C" int cryoim_prscore_noalloc(int32_t nx, int32_t min_r, int32_t max_r,
     float2* alpha = reinterpret_cast<float2*>(s + kAlphaOff);
     // every scratch region below is fully rewritten by this call before it is read
     k_pad_candidates<<<1, 64, 0, st>>>(d_cand, K, cand);
-    launch_refine_alpha(cand, 1, d_tmpl_ort, T, ops, alpha, st);
+    cudaError_t e = cudaGetLastError();
+    if (e == cudaSuccess) {
+        launch_refine_alpha(cand, 1, d_tmpl_ort, T, ops, alpha, st);
+        e = cudaGetLastError();
+    }
     const float* tfc = d_tmpl_fcut;
-    if (d_ctf_band) {
+    if (e == cudaSuccess && d_ctf_band) {
         launch_tmpl_fcut(reinterpret_cast<const float2*>(d_tmpl_band), T, d_ctf_band, 1, bd, cuts, st);
+        e = cudaGetLastError();
         tfc = cuts;
     }
+    if (e != cudaSuccess) return set_error(CRYOIM_ERR_CUDA, cudaGetErrorString(e));
     PrSingleArgs a{};
     a.band = reinterpret_cast<const float2*>(d_band);
     a.fcut0 = d_fcut0;
@@ -127,7 +137,7 @@ extern "C" int cryoim_prscore_noalloc(int32_t nx, int32_t min_r, int32_t max_r,
     a.T = T;
     a.bd = bd;
     a.pr = pr;
-    cudaError_t e = launch_pr_single(a, 1, st);
+    e = launch_pr_single(a, 1, st);
     if (e == cudaSuccess)
         e = cudaMemcpyAsync(d_pr, pr, sizeof(float) * K, cudaMemcpyDeviceToDevice, st);
     if (e == cudaSuccess) e = cudaGetLastError();

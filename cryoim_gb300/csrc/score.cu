@@ -67,6 +67,19 @@ __device__ __forceinline__ void tmpl_sample_cs(const float2* __restrict__ tb, co
     *im = bilerp(ax, ay, t00.y, t10.y, t01.y, t11.y);
 }
 
+// The same sample from a band stored as (pixel, right neighbour) pairs: two 16-byte loads
+// carry the four taps, the values and the arithmetic are tmpl_sample_cs's.
+__device__ __forceinline__ void tmpl_sample_pairs(const float4* __restrict__ tb, int W, int offW, float nxh, float cs,
+                                                  float sn, float fr, float* re, float* im) {
+    float x = __fadd_rn(__fmul_rn(fr, cs), nxh), y = __fadd_rn(__fmul_rn(fr, sn), nxh);
+    int lx = (int)x, ly = (int)y;
+    float ax = __fsub_rn(x, (float)lx), ay = __fsub_rn(y, (float)ly);
+    int b0 = ly * W + lx - offW;
+    const float4 r0 = tb[b0], r1 = tb[b0 + W];
+    *re = bilerp(ax, ay, r0.x, r0.z, r1.x, r1.z);
+    *im = bilerp(ax, ay, r0.y, r0.w, r1.y, r1.w);
+}
+
 __device__ __forceinline__ void tmpl_sample(const float2* __restrict__ tb, const float* __restrict__ cb,
                                             int W, int offW, float nxh, float alpha2, float fr,
                                             float d2r, float* re, float* im) {
@@ -320,41 +333,13 @@ __global__ void __launch_bounds__(512) k_pr_single(PrSingleArgs a, Consts K) {
 // does not depend on omega, so each (template, line, radius) sample of the templates
 // is taken once and compared with the RG particle samples.  groups[g] = (particle,
 // first candidate slot, count).  Every candidate sits at the particle's origin (band
-// pre-shifted, templates pre-multiplied by the particle's CTF).
-//
-// One warp per (template, line), lanes over the radii: a line's validity, its template
-// and particle directions and the particle's cuts are warp-uniform or per-lane
-// registers, so a term costs its taps and arithmetic only (no index division, no
-// divergence on invalid lines).  Per term the arithmetic is k_pr_omega's: the template
-// sample bilinear as tmpl_sample_cs, the particle sample as packed (re, im) lerps, the
-// particle amplitude sq * rsqrt(sq), the folded phase difference from the cross and dot
-// products, per-line FP32 sums folded into per-lane Kahan sums, FP64 across the block.
+// pre-shifted, templates pre-multiplied by the particle's CTF), and the per-term
+// arithmetic is the exhaustive scorer's (angle_between, Kahan sums per thread), so its
+// values match k_pr_omega's.
 constexpr int RG = 4;
-constexpr int RW_THREADS = 256;
-
-// angle_between with an approximate reciprocal (rcp.approx: a relative error of about
-// 2^-23 in t, far inside the polynomial's 1.7e-6 rad)
-__device__ __forceinline__ float angle_between_rcp(float cross, float dot, float pi) {
-    const float a = fabsf(cross), b = fabsf(dot);
-    const float mx = fmaxf(a, b), mn = fminf(a, b);
-    float r1;
-    asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r1) : "f"(mx));
-    const float t = mn * r1;
-    const float s = t * t;
-    float p = fmaf(s, -0.011719364672899246f, 0.05264794081449509f);
-    p = fmaf(p, s, -0.11642702668905258f);
-    p = fmaf(p, s, 0.19354058802127838f);
-    p = fmaf(p, s, -0.33262285590171814f);
-    p = fmaf(p, s, 0.9999772310256958f);
-    float r = t * p;
-    r = (a > b) ? 0.5f * pi - r : r;
-    return (dot < 0.0f) ? pi - r : r;
-}
-
-__global__ void __launch_bounds__(RW_THREADS, 3) k_pr_rescore_g(PrSingleArgs a, const int4* __restrict__ groups,
-                                                              Consts K) {
+__global__ void __launch_bounds__(512) k_pr_rescore_g(PrSingleArgs a, const int4* __restrict__ groups, Consts K) {
     extern __shared__ float rsm[];
-    __shared__ double sh[2][RG][RW_THREADS / 32];
+    __shared__ double sh[2][RG][16];
     const Band bd = a.bd;
     const int W = bd.W, nr = bd.nr, minR = bd.min_r, nx = bd.nx, T = a.T;
     const int4 gr = groups[blockIdx.x];
@@ -387,79 +372,67 @@ __global__ void __launch_bounds__(RW_THREADS, 3) k_pr_rescore_g(PrSingleArgs a, 
     const float nxh = (float)(nx / 2);
     const int offW = bd.off * W + bd.off;
     const float4* sb = a.sband + (long)p * W * W;
-    const float2* tbc0 = a.tbandc ? a.tbandc + (long)p * T * W * W : nullptr;
+    const float4* tbc0 = a.tbandc ? a.tbandc + (long)p * T * W * W : nullptr;
     const float* ctfp = a.ctf ? a.ctf + (long)p * W * W : nullptr;
-    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
-    float2 ks[RG], kc[RG];  // per lane: Kahan sums (sum d w, sum w) and their compensations
+    const int per_t = 60 * nr;
+    float f1[RG], f2[RG], k1[RG], k2[RG];
 #pragma unroll
-    for (int g = 0; g < RG; ++g) { ks[g] = make_float2(0.f, 0.f); kc[g] = make_float2(0.f, 0.f); }
-    const float2 m1 = make_float2(-1.f, -1.f);
-    for (int lj = warp; lj < T * 60; lj += nw) {
-        if (!sval[lj]) continue;  // warp-uniform
-        const int i = lj / 60;
-        const float tcs = stl[2 * lj], tsn = stl[2 * lj + 1];
-        float pcs[RG], psn[RG];
+    for (int g = 0; g < RG; ++g) { f1[g] = 0.f; f2[g] = 0.f; k1[g] = 0.f; k2[g] = 0.f; }
+    // (template i, line j, radius iq) of the flat index q = (i * 60 + j) * nr + iq, advanced
+    // by blockDim.x per iteration without integer divisions
+    const int step_j = (int)blockDim.x / nr, step_iq = (int)blockDim.x - step_j * nr;
+    int i = (int)threadIdx.x / per_t, j = ((int)threadIdx.x - i * per_t) / nr;
+    int iq = (int)threadIdx.x - i * per_t - j * nr;
+    auto advance = [&]() {
+        iq += step_iq;
+        j += step_j;
+        if (iq >= nr) { iq -= nr; ++j; }
+        while (j >= 60) { j -= 60; ++i; }
+    };
+    for (int q = threadIdx.x; q < T * per_t; q += blockDim.x, advance()) {
+        const int lj = i * 60 + j;
+        if (!sval[lj]) continue;
+        const float fr = (float)(minR + iq);
+        float re2, im2;
+        if (tbc0)
+            tmpl_sample_pairs(tbc0 + (long)i * W * W, W, offW, nxh, stl[2 * lj], stl[2 * lj + 1], fr, &re2, &im2);
+        else
+            tmpl_sample_cs(a.tband + (long)i * W * W, ctfp, W, offW, nxh, stl[2 * lj], stl[2 * lj + 1], fr, &re2,
+                           &im2);
+        const float amp2 = sqrtf(re2 * re2 + im2 * im2);
+        if (!(amp2 >= sfc[i * nr + iq])) continue;
+        const float cut1 = sfc[T * nr + iq];
 #pragma unroll
         for (int g = 0; g < RG; ++g) {
-            const int q = 2 * (g * T * 60 + lj);
-            pcs[g] = g < m ? spl[q] : 0.f;
-            psn[g] = g < m ? spl[q + 1] : 0.f;
-        }
-        const float2* tb = tbc0 ? tbc0 + (long)i * W * W : a.tband + (long)i * W * W;
-        const float* cb = tbc0 ? nullptr : ctfp;
-        float2 acc[RG];
-#pragma unroll
-        for (int g = 0; g < RG; ++g) acc[g] = make_float2(0.f, 0.f);
-        for (int iq = lane; iq < nr; iq += 32) {
-            const float fr = (float)(minR + iq);
-            float re2, im2;
-            tmpl_sample_cs(tb, cb, W, offW, nxh, tcs, tsn, fr, &re2, &im2);
-            const float amp2 = sqrtf(re2 * re2 + im2 * im2);
-            if (!(amp2 >= sfc[i * nr + iq])) continue;
-            const float cut1 = sfc[T * nr + iq], half2 = 0.5f * amp2;
-#pragma unroll
-            for (int g = 0; g < RG; ++g) {
-                if (g < m) {
-                    const float x = __fadd_rn(__fmul_rn(fr, pcs[g]), nxh), y = __fadd_rn(__fmul_rn(fr, psn[g]), nxh);
-                    const int lx = (int)x, ly = (int)y;
-                    const float2 ax2 = make_float2(__fsub_rn(x, (float)lx), __fsub_rn(x, (float)lx));
-                    const float2 ay2 = make_float2(__fsub_rn(y, (float)ly), __fsub_rn(y, (float)ly));
-                    const int b0 = ly * W + lx - offW;
-                    const float4 r0 = sb[b0], r1 = sb[b0 + W];  // (tap, right tap) of rows y, y + 1
-                    const float2 t00 = make_float2(r0.x, r0.y), t10 = make_float2(r0.z, r0.w);
-                    const float2 t01 = make_float2(r1.x, r1.y), t11 = make_float2(r1.z, r1.w);
-                    const float2 v0 = __ffma2_rn(ax2, __ffma2_rn(t00, m1, t10), t00);
-                    const float2 v1 = __ffma2_rn(ax2, __ffma2_rn(t01, m1, t11), t01);
-                    const float2 z = __ffma2_rn(ay2, __ffma2_rn(v0, m1, v1), v0);
-                    const float2 zz = __fmul2_rn(z, z);
-                    const float sq = zz.x + zz.y;
-                    const float amp1 = sq * rsqrtf(sq);  // NaN for 0: fails the cut
-                    if (amp1 >= cut1) {
-                        const float2 pd = __fmul2_rn(z, make_float2(re2, im2));
-                        const float2 pc = __fmul2_rn(z, make_float2(im2, -re2));
-                        const float d = angle_between_rcp(pc.x + pc.y, pd.x + pd.y, K.pi);
-                        const float w = fmaf(0.5f, amp1, half2);
-                        acc[g] = __ffma2_rn(make_float2(d, 1.0f), make_float2(w, w), acc[g]);
-                    }
-                }
+            if (g >= m) break;
+            const float cs = spl[2 * ((long)g * T * 60 + lj)], sn = spl[2 * ((long)g * T * 60 + lj) + 1];
+            const float x = __fadd_rn(__fmul_rn(fr, cs), nxh), y = __fadd_rn(__fmul_rn(fr, sn), nxh);
+            const int lx = (int)x, ly = (int)y;
+            const float ax = __fsub_rn(x, (float)lx), ay = __fsub_rn(y, (float)ly);
+            const int b0 = ly * W + lx - offW;
+            const float4 r0 = sb[b0], r1 = sb[b0 + W];  // (tap, right tap) of rows y, y + 1
+            const float2 t00 = make_float2(r0.x, r0.y), t10 = make_float2(r0.z, r0.w);
+            const float2 t01 = make_float2(r1.x, r1.y), t11 = make_float2(r1.z, r1.w);
+            const float re1 = bilerp(ax, ay, t00.x, t10.x, t01.x, t11.x);
+            const float im1 = bilerp(ax, ay, t00.y, t10.y, t01.y, t11.y);
+            const float amp1 = sqrtf(re1 * re1 + im1 * im1);
+            if (amp1 >= cut1) {
+                const float d = angle_between(re1 * im2 - im1 * re2, re1 * re2 + im1 * im2, K.pi);
+                const float w = 0.5f * (amp1 + amp2);
+                kahan_add(f1[g], k1[g], d * w);
+                kahan_add(f2[g], k2[g], w);
             }
         }
-#pragma unroll
-        for (int g = 0; g < RG; ++g) {  // Kahan on the pair (sum d w, sum w)
-            const float2 yv = __fadd2_rn(acc[g], make_float2(-kc[g].x, -kc[g].y));
-            const float2 tv = __fadd2_rn(ks[g], yv);
-            kc[g] = __fadd2_rn(__fadd2_rn(tv, make_float2(-ks[g].x, -ks[g].y)), make_float2(-yv.x, -yv.y));
-            ks[g] = tv;
-        }
     }
+    const int w = threadIdx.x >> 5, l = threadIdx.x & 31, nw = blockDim.x >> 5;
 #pragma unroll
     for (int g = 0; g < RG; ++g) {
-        double p1 = (double)ks[g].x, p2 = (double)ks[g].y;
+        double p1 = (double)f1[g], p2 = (double)f2[g];
         for (int o = 16; o > 0; o >>= 1) {
             p1 += __shfl_xor_sync(0xffffffffu, p1, o);
             p2 += __shfl_xor_sync(0xffffffffu, p2, o);
         }
-        if (lane == 0) { sh[0][g][warp] = p1; sh[1][g][warp] = p2; }
+        if (l == 0) { sh[0][g][w] = p1; sh[1][g][w] = p2; }
     }
     __syncthreads();
     if (threadIdx.x < m) {
@@ -505,7 +478,9 @@ __global__ void k_shift_band(const float2* __restrict__ band, const float* __res
 
 // reconstruct.f90:103-145: rotate each half-plane sample, apply the 60 operators,
 // fold to z >= 0 and splat (a*ctf, b*ctf*signz, ctf^2) trilinearly.  One thread per
-// (sample, operator); the three sums of a voxel are one float4 vector atomic.
+// (operator, sample), consecutive threads on consecutive samples of one operator: the
+// samples run along hx, so a warp's splats land on neighbouring voxels and its float4
+// vector reductions share L2 sectors (the three sums of a voxel are one reduction).
 __device__ __forceinline__ void mv3_rn(const float* m, const float* v, float* o) {
     float t0 = __fmul_rn(m[0], v[0]); t0 = __fadd_rn(t0, __fmul_rn(m[1], v[1])); t0 = __fadd_rn(t0, __fmul_rn(m[2], v[2]));
     float t1 = __fmul_rn(m[3], v[0]); t1 = __fadd_rn(t1, __fmul_rn(m[4], v[1])); t1 = __fadd_rn(t1, __fmul_rn(m[5], v[2]));
@@ -518,7 +493,7 @@ __global__ void __launch_bounds__(256) k_insert(InsertArgs a) {
     if (!a.sel[p]) return;
     const long q = (long)blockIdx.x * blockDim.x + threadIdx.x;
     if (q >= (long)a.nsamples * a.nsym) return;
-    const int s = (int)(q / a.nsym), k = (int)(q - (long)s * a.nsym);
+    const int k = (int)(q / a.nsamples), s = (int)(q - (long)k * a.nsamples);
     const Band bd = a.bd;
     const int W = bd.W, R = bd.max_r;
     const int2 hk = a.samples[s];
@@ -607,22 +582,29 @@ cudaError_t launch_shift_band(const float2* band, const float* cand, int ncand, 
 }
 
 // out[p][i] = tband[i] x ctf[p] per band pixel (the products tmpl_sample forms per tap)
-__global__ void k_tband_ctf(const float2* __restrict__ tband, int T, const float* __restrict__ ctf, long w2,
-                            float2* __restrict__ out) {
+__global__ void k_tband_ctf(const float2* __restrict__ tband, int T, const float* __restrict__ ctf, long w2, int W,
+                            float4* __restrict__ out) {
     const int p = blockIdx.y;
     const long n = (long)T * w2;
     for (long q = (long)blockIdx.x * blockDim.x + threadIdx.x; q < n; q += (long)gridDim.x * blockDim.x) {
+        const long m = q % w2;
         const float2 t = tband[q];
-        const float c = ctf[(long)p * w2 + q % w2];
-        out[(long)p * n + q] = make_float2(__fmul_rn(t.x, c), __fmul_rn(t.y, c));
+        const float c = ctf[(long)p * w2 + m];
+        float2 u = make_float2(0.f, 0.f);
+        if ((m % W) + 1 < W) {  // the right neighbour in the same row
+            const float2 t1 = tband[q + 1];
+            const float c1 = ctf[(long)p * w2 + m + 1];
+            u = make_float2(__fmul_rn(t1.x, c1), __fmul_rn(t1.y, c1));
+        }
+        out[(long)p * n + q] = make_float4(__fmul_rn(t.x, c), __fmul_rn(t.y, c), u.x, u.y);
     }
 }
 
-cudaError_t launch_tband_ctf(const float2* tband, int T, const float* ctf, const Band& bd, int B, float2* out,
+cudaError_t launch_tband_ctf(const float2* tband, int T, const float* ctf, const Band& bd, int B, float4* out,
                              cudaStream_t st) {
     const long w2 = (long)bd.W * bd.W;
     dim3 grid((int)std::min<long>((T * w2 + 255) / 256, 4096), B);
-    k_tband_ctf<<<grid, 256, 0, st>>>(tband, T, ctf, w2, out);
+    k_tband_ctf<<<grid, 256, 0, st>>>(tband, T, ctf, w2, bd.W, out);
     return cudaGetLastError();
 }
 
@@ -639,7 +621,7 @@ cudaError_t launch_pr_rescore_groups(const PrSingleArgs& a, const int4* groups, 
     if (sm > 200 * 1024) return cudaErrorInvalidValue;
     cudaError_t e = cudaFuncSetAttribute(k_pr_rescore_g, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
     if (e != cudaSuccess) return e;
-    k_pr_rescore_g<<<ngroups, RW_THREADS, sm, st>>>(a, groups, consts());
+    k_pr_rescore_g<<<ngroups, 512, sm, st>>>(a, groups, consts());
     return cudaGetLastError();
 }
 

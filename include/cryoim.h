@@ -186,8 +186,8 @@ int cryoim_prscore(void* ctx, const float* ft_a, const float* ft_b, const float*
  * pointer and the call runs asynchronously on `stream`; it calls no cudaMalloc,
  * cudaFree or allocating library routine.
  *
- * Computes what cryoim_prscore computes (cal_crosslin_PR.f90) for K <= 11 candidates
- * (theta, phi, omega, x, y) of one particle, from band windows instead of full
+ * Computes what cryoim_prscore computes for K <= 11 candidates (theta, phi, omega,
+ * x, y) of one particle, from band windows instead of full
  * transforms: a band is the (2*max_r+2)^2 float2 (a, b = -Im) window of a centred
  * nx*nx transform starting at pixel (nx/2-max_r, nx/2-max_r).  d_band: unshifted
  * particle FT; d_fcut0: its max_r-min_r+1 amplitude cuts; d_ctf_band: the particle
@@ -201,7 +201,11 @@ int cryoim_prscore(void* ctx, const float* ft_a, const float* ft_b, const float*
  * device (with that device current) looks the array up and fills its operator table,
  * a synchronous step: make that first call before any stream capture.  All calls
  * share the one array, so calls that overlap on the GPU (other streams, other host
- * threads) race; serialise them. */
+ * threads) race; serialise them.  The looked-up address and the operator table are
+ * kept per device for the life of the process: do not use this entry point across a
+ * cudaDeviceReset (or any teardown of the device's primary context).  Errors pending
+ * on the calling thread before the call are cleared on entry; a launch failure of this
+ * call returns CRYOIM_ERR_CUDA. */
 #define CRYOIM_NOALLOC_MAX_TEMPLATES 64
 #define CRYOIM_NOALLOC_MAX_CANDIDATES 11
 #define CRYOIM_NOALLOC_MAX_RADII 256

@@ -5,6 +5,7 @@ production runs the GPU path is built for:
   plus a shell at 30-34 px), 500 particles of 128^2 at 2.0 A/px, defocus U(1.0, 3.0) um
   without astigmatism, origins U(+-3 px), white noise at SNR 0.1, 20 templates at random
   asymmetric-unit orientations, band 1/60-1/10 A^-1 (minR 4, maxR 26), 1-degree grid.
+* box128_fine -- the same data searched on the 0.5-degree grid (the precision form).
 * box256 -- the production shapes: 256^3 phantom (radii x2) at 1.5 A/px, 256^2
   particles, defocus U(0.8, 3.5) um with astigmatism up to 0.1 um at a random angle,
   origins U(+-6 px), SNR 0.05, 20 templates, band 1/50-1/6 A^-1 (minR 7, maxR 64),
@@ -29,6 +30,10 @@ SPECS = {
     "box128": dict(n=128, apix=2.0, min_res=60.0, max_res=10.0, searchstep=1.0, ntemplates=20,
                    particles=500, df=(1.0, 3.0), astig=0.0, origin=3.0, snr=0.1, ampwg=0.07,
                    seed=20261204),
+    # the box128 particles on the 0.5-degree grid (the precision form's search)
+    "box128_fine": dict(n=128, apix=2.0, min_res=60.0, max_res=10.0, searchstep=0.5, ntemplates=20,
+                        particles=500, df=(1.0, 3.0), astig=0.0, origin=3.0, snr=0.1, ampwg=0.07,
+                        seed=20261204),
     "box256": dict(n=256, apix=1.5, min_res=50.0, max_res=6.0, searchstep=1.0, ntemplates=20,
                    particles=16, df=(0.8, 3.5), astig=0.1, origin=6.0, snr=0.05, ampwg=0.07,
                    seed=20261205),
@@ -76,6 +81,8 @@ def _workers() -> int:
 def make(name: str):
     """(params, vol, tmpl, timgs, imgs, parts, truth) of the named workload (every
     particle of it: the draws of particle i depend on the particle count)."""
+    if name == "box128_fine":  # the box128 data, searched on the finer grid
+        return (params(name),) + make("box128")[1:]
     import cryoim_gb300 as ci
     import synth
     s = SPECS[name]

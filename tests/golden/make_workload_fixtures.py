@@ -16,8 +16,9 @@ workloads of tests/_workloads.py and writes, per workload, tests/golden/<name>_s
                map reconstruct.f90 makes from all particles at the oracle's picks
                (tests/_workloads.py band_coefficients), complex64.
 
-Usage: python tests/golden/make_workload_fixtures.py box256 box128   (hours of CPU for
-box128 on a few cores: 500 particles x ~75 core-seconds).
+Usage: python tests/golden/make_workload_fixtures.py box256 box128 box128_fine (hours of
+CPU for box128 on a few cores: 500 particles x ~75 core-seconds; box128_fine searches the
+first 24 of the same particles on the 0.5-degree grid, ~650 core-seconds each).
 """
 from __future__ import annotations
 
@@ -34,7 +35,8 @@ sys.path.insert(0, ROOT)
 sys.path.insert(0, os.path.join(ROOT, "tests"))
 sys.path.insert(0, os.path.join(ROOT, "oracle"))
 
-ROWS = {"box128": 64, "box256": 16}
+ROWS = {"box128": 64, "box256": 16, "box128_fine": 24}
+SEARCHED = {"box128_fine": 24}  # the oracle searches only the first particles of this set
 CHUNK = 40
 
 
@@ -46,7 +48,8 @@ def run(name: str) -> None:
     print(f"{name}: inputs in {time.time() - t0:.0f} s", flush=True)
     tm, tf = pyoracle.load_templates(timgs, tmpl, p, "f64")
     nth, nph, nom = pyoracle.grid_sizes(p.searchstep)
-    P = len(parts)
+    P = SEARCHED.get(name, len(parts))
+    imgs, parts = imgs[:P], parts[:P]
     q = parts.copy()
     pick_index = np.zeros((P, 3), np.int32)
     gap = np.zeros(P)

@@ -159,3 +159,54 @@ def test_merge_finish_and_merge_fsc_match_oracle(built, orc, case):
     f_orc, mf_orc = orc.merge_fsc(p.fftsize, p.max_r, odd, even, p.imgmask_px, "f64")
     assert np.abs(f - f_orc).max() < 1e-5
     assert _rel(mf, mf_orc) < 1e-5, _rel(mf, mf_orc)
+
+
+def test_particle_shards_exchange_tnf_partials(built, case, tmp_path):
+    """Two particle shards, as two ranks of a sharded run would own them (one context
+    each): each inserts its range and writes its tnf partial with the library's writer;
+    the partials read back, summed (the reduction shard.allreduce_partials performs) and
+    added to a fresh accumulation finish to the map of one context that inserted every
+    particle.  reconstruct.f90:92 masks every image at particle(first)'s origin, so the
+    records share one origin here (as merge_icosprocess_subrec's users must)."""
+    import cryoim_gb300 as ci
+    from test_io import lib
+    p, vol, tmpl, timgs, imgs, parts, truth = case
+    q = parts.copy()
+    q["pr"] = 0.0
+    q["x"] = q["y"] = 0.0
+    L = lib()
+    R = p.max_r
+    t = 2 * R + 1
+    ps = ci.Params.from_buffer_copy(p)
+    ps.subrec = 1  # tnf partials: weights start at 0 (reconstruct_substep.f90:25)
+    shards = [slice(0, 1), slice(1, len(q))]
+    got = []
+    for k, sl in enumerate(shards):
+        with ci.Context(0, ps) as c:
+            c.rec_begin()
+            c.rec_insert(imgs[sl], q[sl])
+            fa, fb, wg = c.rec_get_partial()
+        path = str(tmp_path / f"shard{k}.tnf").encode()
+        assert L.cryoim_tnf_write(path, p.fftsize, R, p.apix, p.imgmask, 0, 0, fa.ctypes.data, fb.ctypes.data,
+                                  wg.ctypes.data) == 0
+        ih, fh = np.zeros(4, np.int32), np.zeros(2, np.float32)
+        back = [np.zeros((R + 1, t, t), np.float32) for _ in range(3)]
+        assert L.cryoim_tnf_read(path, ih.ctypes.data, fh.ctypes.data, back[0].ctypes.data, back[1].ctypes.data,
+                                 back[2].ctypes.data) == 0
+        assert all(np.array_equal(a, b) for a, b in zip((fa, fb, wg), back))
+        got.append(back)
+    with ci.Context(0, p) as c:
+        c.rec_begin()
+        for part in got:
+            c.rec_add_partial(*part)
+        merged = c.rec_finish_merge()
+    with ci.Context(0, ps) as c:
+        c.rec_begin()
+        c.rec_insert(imgs, q)
+        whole = c.rec_get_partial()
+    with ci.Context(0, p) as c:
+        c.rec_begin()
+        c.rec_add_partial(*whole)
+        want = c.rec_finish_merge()
+    assert _rel(sum(g[0].astype(np.float64) for g in got), whole[0]) < 1e-5
+    assert _rel(merged, want) < 1e-5

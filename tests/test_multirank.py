@@ -1,6 +1,10 @@
 """Two CPU ranks (gloo): particle shards give the same search results as one process,
 and the all_reduce of partial reconstruction accumulators equals the single-process
-accumulation (the exchange merge_icosprocess_subrec does through tnf files)."""
+accumulation (the exchange merge_icosprocess_subrec does through tnf files).  Each
+rank's partial goes through the library's tnf writer and reader (cryoim_tnf_write /
+cryoim_tnf_read, host code of libcryoim_gb300.so) before the reduction, and the
+merged map of the reduced partial (merge_reconstruct.f90, oracle restatement) equals
+the one of the single-process partial."""
 import os
 import socket
 
@@ -59,8 +63,28 @@ def _worker(rank, world, port, out):
     qq["pr"] = 0.0
     _, acc = pyoracle.reconstruct(pm, imgs[mine], qq[mine], want_acc=True, fp="f64")
     fa, fb, wg = allreduce_partials(acc[0], acc[1], acc[2], wg_init=0.01)
+    # the tnf exchange: this rank's half-box partial (reconstruct_substep.f90) written and
+    # read back by the library, then summed over the ranks
+    import ctypes as C
+    from cryoim_gb300 import load
+    L = load()
+    R = p.max_r
+    t = 2 * R + 1
+    sub = [np.ascontiguousarray(x, np.float32) for x in pyoracle.reconstruct_half(pm, imgs[mine], qq[mine], 0)]
+    sub2 = [np.ascontiguousarray(x, np.float32) for x in pyoracle.reconstruct_half(pm, imgs[mine], qq[mine], 1)]
+    part = [a + b for a, b in zip(sub, sub2)]
+    path = os.path.join(os.path.dirname(out), f"rank{rank}.tnf")
+    assert L.cryoim_tnf_write(path.encode(), p.fftsize, R, p.apix, p.imgmask, 0, 0, part[0].ctypes.data,
+                              part[1].ctypes.data, part[2].ctypes.data) == 0
+    ih, fh = np.zeros(4, np.int32), np.zeros(2, np.float32)
+    back = [np.zeros((R + 1, t, t), np.float32) for _ in range(3)]
+    assert L.cryoim_tnf_read(path.encode(), ih.ctypes.data, fh.ctypes.data, back[0].ctypes.data,
+                             back[1].ctypes.data, back[2].ctypes.data) == 0
+    assert all(np.array_equal(a, b) for a, b in zip(part, back)) and list(ih[:2]) == [p.fftsize, R]
+    tsum = allreduce_partials(*[b.astype(np.float64) for b in back])
     if rank == 0:
-        np.savez(out, fa=fa, fb=fb, wg=wg, res=np.array(sum(got, []), dtype=np.float64))
+        np.savez(out, fa=fa, fb=fb, wg=wg, res=np.array(sum(got, []), dtype=np.float64),
+                 tfa=tsum[0], tfb=tsum[1], twg=tsum[2])
     dist.barrier()
     dist.destroy_process_group()
 
@@ -86,3 +110,11 @@ def test_two_ranks_match_one_process(built, orc, tmp_path):
     _, acc = orc.reconstruct(pm, imgs, qq, want_acc=True, fp="f64")
     for k, a in zip(("fa", "fb", "wg"), acc):
         assert np.allclose(r[k], a, rtol=1e-10, atol=1e-12 * np.abs(a).max())
+    # the tnf partials summed over the ranks = the partial of all particles, and so is
+    # the merged map
+    whole = [a + b for a, b in zip(orc.reconstruct_half(pm, imgs, qq, 0), orc.reconstruct_half(pm, imgs, qq, 1))]
+    for k, a in zip(("tfa", "tfb", "twg"), whole):
+        assert np.allclose(r[k], a, rtol=1e-5, atol=1e-6 * np.abs(a).max())
+    m_ranks = orc.merge_finish(p.fftsize, p.max_r, [r["tfa"], r["tfb"], r["twg"]])
+    m_one = orc.merge_finish(p.fftsize, p.max_r, whole)
+    assert np.linalg.norm(m_ranks - m_one) <= 1e-5 * np.linalg.norm(m_one)

@@ -61,8 +61,29 @@ def test_noalloc_scores_match_prscore(built, orc):
                  C.c_void_p(out.data_ptr()), C.c_void_p(s))
             torch.cuda.synchronize()
             got = out.cpu().numpy()
-            rel = np.abs(got - want) / want
-            assert rel.max() < 1e-4, (call_no, rel.max(), got, want)
+            np.testing.assert_allclose(got, want, rtol=1e-4, err_msg=f"call {call_no}")
+        # without a CTF: the caller's own template cuts (no scratch cuts)
+        i = 2
+        a, b, f = orc.prep_particle(imgs[i], 1, p.imgmask_px, parts["x"][i], parts["y"][i], 0,
+                                    p.min_r, p.max_r, "f64")
+        cand = np.stack([rng.uniform(69, 90, 5), rng.uniform(-30, 30, 5), rng.uniform(0, 360, 5),
+                         rng.uniform(-3, 3, 5), rng.uniform(-3, 3, 5)], 1).astype(np.float32)
+        pn = ci.Params.from_buffer_copy(p)
+        pn.apply_ctf = 0
+        ctx.set_params(pn)
+        ctx.load_templates(timgs, tmpl)
+        want = np.array([ctx.prscore(a, b, f, None, *c) for c in cand], np.float32)
+        band = np.stack([_window(a, n, R), _window(b, n, R)], -1).astype(np.float32)
+        d = {k: torch.from_numpy(np.ascontiguousarray(v, np.float32)).to(dev) for k, v in dict(
+            band=band, fcut0=f, tband=tband, tfcut=tf, tort=tort, cand=cand).items()}
+        out = torch.full((5,), -1.0, device=dev)
+        call("cryoim_prscore_noalloc", n, p.min_r, p.max_r, C.c_void_p(d["band"].data_ptr()),
+             C.c_void_p(d["fcut0"].data_ptr()), None, C.c_void_p(d["tband"].data_ptr()),
+             C.c_void_p(d["tfcut"].data_ptr()), C.c_void_p(d["tort"].data_ptr()), len(tmpl),
+             C.c_void_p(d["cand"].data_ptr()), 5, C.c_void_p(out.data_ptr()),
+             C.c_void_p(torch.cuda.current_stream().cuda_stream))
+        torch.cuda.synchronize()
+        np.testing.assert_allclose(out.cpu().numpy(), want, rtol=1e-4, err_msg="no CTF")
 
 
 def test_noalloc_rejects_sizes_beyond_its_limits(built):
