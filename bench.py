@@ -1051,7 +1051,8 @@ def _rot_angle(Ra, Rb):
 def run_local_report(args):
     """Batched localized refinement from whole particles, the sub-particle configuration's
     pipeline: P particles of 512^2 at 1.0 A/px projected from a 512^3 phantom (the
-    generator's radii x4) in the icosprocess 2-fold frame, CTF 1.0-3.0 um, SNR 0.1, with
+    generator's radii x4) in the icosprocess 2-fold frame, CTF 1.0-3.0 um, noise-free and at
+    SNR 0.1 (the same particles), with
     the signal outside the 12 vertex regions (spheres of radius 56 px) subtracted, as
     localized reconstruction does before it cuts sub-particles;
     orientations taken to the 5-fold frame (proc_icos transform, Ry(v) R); the 12
@@ -1105,10 +1106,14 @@ def run_local_report(args):
     del keep
     p0 = ci.default_params(n0, apix=1.0, minRes=50.0, maxRes=4.0, searchstep=1.0, ampwg=0.07)
     c0 = ci.Context(0, p0)
-    imgs, parts, truth = synth.make_particles(
-        vol, P, seed + 1, lambda v, e: c0.project_templates(v, _as_tmpl(ci, e)), 1.0, df_range=(1.0, 3.0),
-        astig_max=0.0, origin_max=2.0, snr=0.1, ampwg=0.07)
+    # the same particles (orientations, CTF, origins) noise-free and at SNR 0.1
+    sets = {}
+    for snr in (0.0, 0.1):
+        sets[snr] = synth.make_particles(
+            vol, P, seed + 1, lambda v, e: c0.project_templates(v, _as_tmpl(ci, e)), 1.0, df_range=(1.0, 3.0),
+            astig_max=0.0, origin_max=2.0, snr=snr, ampwg=0.07)
     c0.close()
+    _, parts, truth = sets[0.1]
     t5, p5, o5 = ci.transform_ort(5, truth[:, 0], truth[:, 1], truth[:, 2])
     # the local map: 128^3 around (0, 0, zv) in the 5-fold frame, C5 about z
     g = np.arange(n) - n // 2
@@ -1127,57 +1132,63 @@ def run_local_report(args):
     lctx = ci.Context(0, lp)
     lctx.set_lanes(LANES)
     lctx.set_reference_map(lmap)
-    d_imgs = torch.from_numpy(imgs).to("cuda:0")
-    d_sub = torch.empty((P * 12, n, n), device="cuda:0")
-    torch.cuda.synchronize()
-    lctx.local_box_extract(d_imgs.data_ptr(), q[:4], sym, (0.0, 0.0, zv), 1.0, n, d_out=d_sub.data_ptr(), fftsize=n0)
-    torch.cuda.synchronize()
-    te = time.perf_counter()
-    _, rec = lctx.local_box_extract(d_imgs.data_ptr(), q, sym, (0.0, 0.0, zv), 1.0, n, d_out=d_sub.data_ptr(),
-                                    fftsize=n0)
-    torch.cuda.synchronize()
-    t_extract = time.perf_counter() - te
-    K = len(rec)
-    sp = ci.particles(K)
-    sp["particle_id"] = np.arange(1, K + 1)
-    sp["img_id"] = np.arange(1, K + 1)
-    sp["img_particle_id"] = np.arange(1, K + 1)
-    sp["theta"], sp["phi"], sp["omega"] = rec["local_theta0"], rec["local_phi0"], rec["local_omega0"]
-    sp["x"], sp["y"] = rec["local_x0"], rec["local_y0"]
-    sp["df1"], sp["df2"], sp["astigang"] = rec["df1"], rec["df2"], rec["astigang"]
-    kw = dict(origin_max=4.0, origin_step=0.5, topk=16, pick=1, local_range=3.0, local_step=0.25, centred_origins=True)
-    lctx.contract_search(d_sub.data_ptr(), sp[:64].copy(), **kw)  # warm-up (sample lists, texture)
-    torch.cuda.synchronize()
-    ts = time.perf_counter()
-    out = sp.copy()
-    lctx.contract_search(d_sub.data_ptr(), out, **kw)
-    torch.cuda.synchronize()
-    t_search = time.perf_counter() - ts
-    # truth per sub-particle: equalort of the true 5-fold-frame orientation with its rotation
     c5 = [np.array([[np.cos(a), -np.sin(a), 0], [np.sin(a), np.cos(a), 0], [0, 0, 1]])
           for a in np.radians(72.0 * np.arange(5))]
 
-    def err(th, ph, om, i):
+    def err(th, ph, om, i):  # against the sub-particle's true orientation S E5, modulo C5
         Rt = sym[i % 12].astype(np.float64) @ synth.euler_mat(t5[i // 12], p5[i // 12], o5[i // 12])
         R = synth.euler_mat(th, ph, om)
         return min(_rot_angle(R, Z @ Rt) for Z in c5)
-    before = [err(sp["theta"][i], sp["phi"][i], sp["omega"][i], i) for i in range(K)]
-    after = [err(out["theta"][i], out["phi"][i], out["omega"][i], i) for i in range(K)]
-    res = {"report": "batched localized refinement from whole particles", "particles": P, "sub_particles": K,
+
+    kw = dict(origin_max=4.0, origin_step=0.5, topk=16, pick=1, local_range=3.0, local_step=0.25,
+              centred_origins=True)
+    d_sub = torch.empty((P * 12, n, n), device="cuda:0")
+    per_snr = {}
+    for snr, (imgs, _, _) in sets.items():
+        d_imgs = torch.from_numpy(imgs).to("cuda:0")
+        torch.cuda.synchronize()
+        lctx.local_box_extract(d_imgs.data_ptr(), q[:4], sym, (0.0, 0.0, zv), 1.0, n, d_out=d_sub.data_ptr(),
+                               fftsize=n0)
+        torch.cuda.synchronize()
+        te = time.perf_counter()
+        _, rec = lctx.local_box_extract(d_imgs.data_ptr(), q, sym, (0.0, 0.0, zv), 1.0, n, d_out=d_sub.data_ptr(),
+                                        fftsize=n0)
+        torch.cuda.synchronize()
+        t_extract = time.perf_counter() - te
+        K = len(rec)
+        sp = ci.particles(K)
+        sp["particle_id"] = np.arange(1, K + 1)
+        sp["img_id"] = np.arange(1, K + 1)
+        sp["img_particle_id"] = np.arange(1, K + 1)
+        sp["theta"], sp["phi"], sp["omega"] = rec["local_theta0"], rec["local_phi0"], rec["local_omega0"]
+        sp["x"], sp["y"] = rec["local_x0"], rec["local_y0"]
+        sp["df1"], sp["df2"], sp["astigang"] = rec["df1"], rec["df2"], rec["astigang"]
+        lctx.contract_search(d_sub.data_ptr(), sp[:64].copy(), **kw)  # warm-up (sample lists, texture)
+        torch.cuda.synchronize()
+        ts = time.perf_counter()
+        out = sp.copy()
+        lctx.contract_search(d_sub.data_ptr(), out, **kw)
+        torch.cuda.synchronize()
+        t_search = time.perf_counter() - ts
+        before = np.array([err(sp["theta"][i], sp["phi"][i], sp["omega"][i], i) for i in range(K)])
+        after = np.array([err(out["theta"][i], out["phi"][i], out["omega"][i], i) for i in range(K)])
+        per_snr["noise-free" if snr == 0 else f"snr {snr:g}"] = {
+            "extraction": {"entry": "cryoim_local_box_extract_device", "seconds": t_extract,
+                           "sub_particles_per_s": K / t_extract},
+            "local_search": {"entry": "cryoim_contract_search_device (local form, centred origins)",
+                             "seconds": t_search, "sub_particles_per_s": K / t_search},
+            "pipeline_sub_particles_per_s": K / (t_extract + t_search),
+            "median_error_deg_c5": {"before": float(np.median(before)), "after": float(np.median(after))},
+            "fraction_improved": float(np.mean(after < before))}
+        del d_imgs
+    res = {"report": "batched localized refinement from whole particles", "particles": P, "sub_particles": P * 12,
            "config": {"particle_box": n0, "apix": 1.0, "sub_box": n, "vertex_z_px": zv, "vertices": 12,
                       "signal": f"the 12 vertex regions only (spheres of radius {rmask:g} px; the rest subtracted)",
                       "local_map": "128^3 around the vertex, 5-fold frame (C5 about z)",
                       "search": "+-3 deg @ 0.25 deg (15,625 orientations) x origins +-4 px @ 0.5 px (289), "
                                 "centred on each sub-particle's own origin, top 16 rescored in FP64",
-                      "snr": 0.1, "start": "truth + U(+-1 deg) per Euler angle"},
-           "phantom_s": t_phantom,
-           "extraction": {"entry": "cryoim_local_box_extract_device", "seconds": t_extract,
-                          "sub_particles_per_s": K / t_extract},
-           "local_search": {"entry": "cryoim_contract_search_device (local form, centred origins)",
-                            "seconds": t_search, "sub_particles_per_s": K / t_search},
-           "pipeline_sub_particles_per_s": K / (t_extract + t_search),
-           "median_error_deg_c5": {"before": float(np.median(before)), "after": float(np.median(after))},
-           "fraction_improved": float(np.mean(np.array(after) < np.array(before)))}
+                      "ctf": "defocus U(1.0, 3.0) um", "start": "truth + U(+-1 deg) per Euler angle"},
+           "phantom_s": t_phantom, "results": per_snr}
     print(json.dumps(res))
     lctx.close()
     return 0
