@@ -45,15 +45,16 @@ sys.path.insert(0, ROOT)
 
 WORKLOAD = dict(nx=256, apix=1.5, min_res=50.0, max_res=6.0, searchstep=1.0, ntemplates=20,
                 df=(0.8, 3.5), astig=0.1, snr=0.05, origin=6.0, origin_step=0.5, topk=16,
-                ampwg=0.07, seed=20261205, cycle_particles=10000, learned=16, nbr_best=4, learn_lr=4e-3)
+                ampwg=0.07, seed=20261205, cycle_particles=10000, learned=16, nbr_best=4, learn_lr=4e-3,
+                proposal_nbr=1)
 METRIC = "particles/s (box 256), BF16+learned vs plain FP32 GPU at >=99% same orientation"
 FP32_PEAK_TFLOPS_NOMINAL = 152 * 128 * 2 * 2.07e9 / 1e12  # FMA lanes x 2 flop x max SM clock
 FLOPS_PER_TERM = 30.0
 # this library's kernels launched per 64-particle pass of the headline form (ncu launch
 # list): prep, FFT post-processing, CTF, template cuts, norms, features, 4 convolutions,
-# 3 poolings, mix, head, cell top-k, operand A, gather, grouped contraction, distinct
-# selection, FP64 rescoring (2), and two rounds of alpha table, band shift, phase residual
-LAUNCHES_PER_PASS = 29
+# 3 poolings, mix, head, cell top-k, operand A, grouped contraction, distinct selection,
+# FP64 rescoring (2), and two rounds of alpha table, band shift, phase residual
+LAUNCHES_PER_PASS = 28
 # DRAM bytes (read + write) of one GEMM launch (3 particles x 625 origins) from an ncu
 # capture at the 2-degree grid (1.483 GB for 31,320 orientations), scaled to the
 # orientation count: operand B streams once per launch.
@@ -66,8 +67,11 @@ L2_RED_PEAK = 3.779e11
 # sm__pipe_tensor_cycles_active of the FP8 contraction (profiles/k_gemm_argmax_e4m3_box256.md)
 TENSOR_PIPE_ACTIVE_E4M3 = 0.781
 # dram__bytes_read.sum + dram__bytes_write.sum of one grouped fine-contraction launch over
-# a 64-particle pass of the box-256 workload (ncu capture of --profile-case learned)
-GROUPED_GEMM_TRAFFIC_PER_PASS = 3.802061e9 + 5.544448e6
+# a 64-particle pass of the box-256 workload (ncu capture of --profile-case learned: rows
+# copied from the section bank by index, +-1-step proposal neighbourhoods)
+GROUPED_GEMM_TRAFFIC_PER_PASS = 1.783445e9 + 4.284416e6
+# the same for the phase-residual rescoring (mean of the two launches of a pass)
+RESCORE_TRAFFIC_PER_LAUNCH = 0.5 * (0.281961e9 + 3.609344e6 + 0.290479e9 + 3.733504e6)
 
 
 
@@ -267,7 +271,7 @@ def config_dict(params):
 
 def form_dict(batch, learn_samples):
     w = WORKLOAD
-    return {"form": "BF16 contraction over the neighbourhoods (+-2 steps) of the learned proposer's "
+    return {"form": f"BF16 contraction over the neighbourhoods (+-{w['proposal_nbr']} steps) of the learned proposer's "
                     f"{w['learned']} cells per particle, top-{w['topk']} rescored (FP64 CC, phase residual)",
             "particles_per_step": batch,
             "section_build": f"per map, charged pro rata per particle of a {w['cycle_particles']}-particle cycle",
@@ -356,7 +360,7 @@ def run_ours(args):
     h_imgs = torch.from_numpy(imgs[:B]).pin_memory()
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=f"cuda:{dev}")
     copts = dict(origin_max=w["origin"], origin_step=w["origin_step"], topk=w["topk"], pick=0)
-    lopts = dict(copts, learned=w["learned"], nbr_best=w["nbr_best"])
+    lopts = dict(copts, learned=w["learned"], nbr_best=w["nbr_best"], proposal_nbr=w["proposal_nbr"])
     cyc = w["cycle_particles"]
 
     def timed_steps(fn, steps, sampler=None):
@@ -401,6 +405,7 @@ def run_ours(args):
     ms, _ = timed_steps(lambda: search_step(**lopts), args.steps, clk)
     torch.cuda.nvtx.range_pop()
     gst_lanes = ctx.contract_stats()
+    ctx.rescore_stats()  # reset: the rescoring is timed with one lane below
     ctx.set_profiling(False)
     # The timed steps run LANES pass lanes whose kernels overlap, so a launch's event-timed
     # duration there includes other lanes' work: the contraction's roofline is taken from
@@ -411,6 +416,7 @@ def run_ours(args):
         search_step(**lopts)
     torch.cuda.synchronize()
     gst = ctx.contract_stats()
+    rst = ctx.rescore_stats()
     ctx.set_profiling(False)
     ctx.set_lanes(LANES)
     # per-cycle costs charged pro rata: the section build and the proposer's training
@@ -583,12 +589,44 @@ def run_ours(args):
     pr_terms_per_s = terms * npr / (kms / 1000.0)
     pr_achieved = pr_terms_per_s * FLOPS_PER_TERM / 1e12
 
+    # the phase-residual rescoring (k_pr_rescore_s): one term = one (candidate, template,
+    # line, radius) sample pair; a candidate carries the grid's mean terms per orientation
+    # (the FP32 form's exact count over the 1-degree grid / its orientations)
+    terms_per_orient = terms / max(st0["orientations"], 1)
+    rs_terms_per_s = rst["candidates"] * terms_per_orient / max(rst["ms"] / 1000.0, 1e-12)
+    rs_achieved = rs_terms_per_s * FLOPS_PER_TERM / 1e12
+    rescore_roofline = {"bound": "fp32", "kernel": "k_pr_rescore_s", "achieved": rs_achieved,
+                        "peak": FP32_PEAK_TFLOPS_NOMINAL, "unit": "TFLOP/s",
+                        "frac": rs_achieved / FP32_PEAK_TFLOPS_NOMINAL, "terms_per_s": rs_terms_per_s,
+                        "terms_per_candidate": terms_per_orient,
+                        "avg_launch_ms": rst["ms"] / max(rst["launches"], 1), "launches": rst["launches"],
+                        "candidates": rst["candidates"],
+                        "timing": "CUDA events around each launch in 2 one-lane steps of the same workload",
+                        "peak_source": "nominal FP32 FMA rate (no measured non-tensor FP32 peak)",
+                        "traffic": RESCORE_TRAFFIC_PER_LAUNCH,
+                        "traffic_note": "DRAM bytes per launch, ncu capture of --profile-case learned "
+                                        "(mean of the two launches of a 64-particle pass)"}
+
     def gemm_roofline(g, peak, kernel, src_note):
         a = g["gemm_flops"] / max(g["gemm_ms"], 1e-9) / 1e9
         return {"bound": "tensor", "kernel": kernel, "achieved": a, "peak": peak, "unit": "TFLOP/s",
                 "frac": a / peak, "avg_launch_ms": g["gemm_ms"] / max(g["gemm_launches"], 1),
                 "launches": g["gemm_launches"], "orientations": g["orientations"], "kpad": g["kpad"],
                 "peak_source": src_note}
+    contraction_roofline = dict(gemm_roofline(gst, peak_s, "k_gemm_argmax<bf16> (grouped, rows by index)",
+                                f"{src} bf16_tflops_sustained"),
+                                timing="CUDA events around each launch in 2 one-lane steps of the same "
+                                "workload (the kernel alone)",
+                                achieved_in_timed_steps=gst_lanes["gemm_flops"] / max(gst_lanes["gemm_ms"], 1e-9) / 1e9,
+                                achieved_in_timed_steps_note=f"{LANES} lanes: each launch's event time includes the "
+                                "overlapping kernels of the other lanes",
+                                traffic=GROUPED_GEMM_TRAFFIC_PER_PASS * min(1.0, B / 64.0),
+                                traffic_note="DRAM bytes per launch (64-particle pass), ncu capture of a launch "
+                                "of the same shape",
+                                note="the grouped fine contraction of the headline form; its launches are "
+                                "small (each particle's 625 origins x its few hundred listed "
+                                "orientations, copied from the section bank by index), and the step is "
+                                "shared with the rescoring kernels (profiles/ has the launch list)")
     bf_v, bf_st, bf_g, bf_q = forms["bf16"]
     f8_v, f8_st, f8_g, f8_q = forms["fp8"]
     passes = (B + 63) // 64
@@ -607,20 +645,11 @@ def run_ours(args):
                          "final_loss": lst["loss"], "views": lst["views"], "cells_per_particle": w["learned"],
                          "rescoring": f"top-{w['topk']} distinct orientations (FP64 CC), phase residual of "
                                       f"those and of the grid neighbours of the best {w['nbr_best']}"},
-            "roofline": dict(gemm_roofline(gst, peak_s, "k_gemm_argmax<bf16> (grouped, gathered sections)",
-                                           f"{src} bf16_tflops_sustained"),
-                             timing="CUDA events around each launch in 2 one-lane steps of the same "
-                                    "workload (the kernel alone)",
-                             achieved_in_timed_steps=gst_lanes["gemm_flops"] / max(gst_lanes["gemm_ms"], 1e-9) / 1e9,
-                             achieved_in_timed_steps_note=f"{LANES} lanes: each launch's event time includes the "
-                                                          "overlapping kernels of the other lanes",
-                             traffic=GROUPED_GEMM_TRAFFIC_PER_PASS * min(1.0, B / 64.0),
-                             traffic_note="DRAM bytes per launch (64-particle pass), ncu capture of a launch "
-                                          "of the same shape",
-                             note="the grouped fine contraction of the headline form; its launches are "
-                                  "small (each particle's 625 origins x its few thousand gathered "
-                                  "orientations), and the step is shared with the rescoring kernels "
-                                  "(profiles/ has the launch list)"),
+            # the kernel that takes most of the step's GPU time (one lane, kernels alone)
+            "roofline": rescore_roofline if rst["ms"] > gst["gemm_ms"] else contraction_roofline,
+            "roofline_contraction": contraction_roofline,
+            "roofline_rescoring": rescore_roofline,
+            "step_gpu_ms_one_lane": {"contraction": gst["gemm_ms"] / 2, "rescoring": rst["ms"] / 2},
             "section_build_ms": st0["slice_ms"],
             "fp32_form": {"value": fp32_pps, "unit": "particles/s", "particles": npr,
                           "speedup_of_headline": value / fp32_pps,
@@ -731,7 +760,7 @@ def run_profile_case(args):
     if case == "learned":
         ctx.learn_train(vol, samples=2560, batch=256, lr=w["learn_lr"], seed=w["seed"], snr=w["snr"],
                         df_min=w["df"][0], df_max=w["df"][1], astig_max=w["astig"], origin_max=w["origin"])
-        copts.update(learned=w["learned"], nbr_best=w["nbr_best"])
+        copts.update(learned=w["learned"], nbr_best=w["nbr_best"], proposal_nbr=w["proposal_nbr"])
     elif case == "exhaustive-fp8":
         copts.update(precision="fp8")
     for _ in range(2):
@@ -904,6 +933,13 @@ def run_learned_report(args):
     _, t_pr = timed(lambda: ctx.globesearch(d.data_ptr(), qpr))
     qa = parts.copy()
     _, t_a = timed(lambda: ctx.contract_search(d.data_ptr(), qa, learned=16, nbr_best=4, **g))
+    # cells and neighbourhood widths of the proposal lists at this configuration
+    variants = []
+    for kl, pn in ((16, 1), (16, 2), (32, 1), (32, 2)):
+        qv = parts.copy()
+        _, tv = timed(lambda: ctx.contract_search(d.data_ptr(), qv, learned=kl, nbr_best=4, proposal_nbr=pn, **g))
+        variants.append({"learned": kl, "proposal_nbr": pn, "particles_per_s": P / tv,
+                         "identical_to_fp32_exhaustive": None, "_q": qv})
     qf = parts.copy()
     _, t_f = timed(lambda: ctx.contract_search(d.data_ptr(), qf, learned=16, nbr_best=4, fallback=3.0, **g))
     nfb = ctx.contract_fallbacks()
@@ -943,7 +979,10 @@ def run_learned_report(args):
                        "learned_with_fallback_particles_per_s": P / t_f,
                        "runtime_fallback_rule": "PR above median + 3 x 1.4826 x MAD -> exhaustive contraction",
                        "runtime_fallbacks": nfb, "runtime_fallback_rate": nfb / P,
-                       "learned_with_fallback_identical_to_fp32_exhaustive": float(same(qf, qpr).mean())}}
+                       "learned_with_fallback_identical_to_fp32_exhaustive": float(same(qf, qpr).mean()),
+                       "variants": variants}}
+    for v in variants:
+        v["identical_to_fp32_exhaustive"] = float(same(v.pop("_q"), qpr).mean())
     print(json.dumps(out))
     ctx.close()
     return 0
@@ -1017,7 +1056,7 @@ def run_cycle_report(args):
             df_min=w["df"][0], df_max=w["df"][1], astig_max=w["astig"], origin_max=w["origin"]))
         _, st["search_s"] = sync_time(lambda: ctx.contract_search(
             d_imgs.data_ptr(), q, origin_max=w["origin"], origin_step=w["origin_step"], topk=w["topk"],
-            learned=w["learned"], nbr_best=w["nbr_best"]))
+            learned=w["learned"], nbr_best=w["nbr_best"], proposal_nbr=w["proposal_nbr"]))
         _, st["refine_s"] = sync_time(lambda: ctx.refine(d_imgs.data_ptr(), q))
 
         def insert():
@@ -1052,17 +1091,22 @@ def run_local_report(args):
     """Batched localized refinement from whole particles, the sub-particle configuration's
     pipeline: P particles of 512^2 at 1.0 A/px projected from a 512^3 phantom (the
     generator's radii x4) in the icosprocess 2-fold frame, CTF 1.0-3.0 um, noise-free and at
-    SNR 0.1 (the same particles), with
-    the signal outside the 12 vertex regions (spheres of radius 56 px) subtracted, as
-    localized reconstruction does before it cuts sub-particles;
-    orientations taken to the 5-fold frame (proc_icos transform, Ry(v) R); the 12
-    vertex sub-particles of 128^2 per particle cut by local_box's stack mode on the GPU
-    (cryoim_local_box_extract: one rotation of the 5-fold frame's icosahedral set per
-    vertex, vertex at (0, 0, 184 px)); the 128^3 C5 local map cut from the phantom around
-    that vertex; then the contraction search's local form (BF16 on the tensor cores,
-    +-3 degrees at 0.25 degrees x origins +-4 px at 0.5 px around each sub-particle's own
-    origin, top 16 rescored in FP64).  Starting orientations are the truth perturbed by
-    up to 1 degree per Euler angle; errors are measured modulo the local map's C5."""
+    SNR 0.1 (the same particles); orientations taken to the 5-fold frame (proc_icos
+    transform, Ry(v) R); the 12 vertex sub-particles of 128^2 per particle cut by
+    local_box's stack mode on the GPU (cryoim_local_box_extract: one rotation of the 5-fold
+    frame's icosahedral set per vertex, vertex at (0, 0, 184 px)); the 128^3 C5 local map
+    cut from the phantom around that vertex; then the contraction search's local form (BF16
+    on the tensor cores, +-3 degrees at 0.25 degrees x origins +-4 px at 0.5 px around each
+    sub-particle's own origin, top 16 rescored in FP64).  Starting orientations are the
+    truth perturbed by up to 1 degree per Euler angle; errors are measured modulo the
+    local map's C5.
+
+    Signal subtraction, as localized reconstruction does before it cuts a sub-particle:
+    the image a vertex's sub-particle is cut from keeps that vertex's region (a sphere of
+    radius 56 px) and the particle's noise, the projections of the rest of the particle
+    subtracted.  Without it (all 12 vertex regions kept in one image) other vertices that
+    project into the sub-particle's box, and the CTF's delocalisation of their signal, move
+    the correlation's maximum away from the truth; that case is reported beside it."""
     import torch
     import cryoim_gb300 as ci
     import synth
@@ -1090,30 +1134,42 @@ def run_local_report(args):
             sym.append(S)
     sym = np.array(sym, np.float32)
     assert len(sym) == 12
-    # signal subtraction, as localized reconstruction does before cutting sub-particles:
-    # the particles carry only their 12 vertex regions (spheres of radius rmask around the
-    # vertices, in the map's 2-fold frame Ry^T S^T (0, 0, zv))
+    # the vertex regions: spheres of radius rmask around the vertices, in the map's 2-fold
+    # frame Ry^T S^T (0, 0, zv)
     g0 = np.arange(n0, dtype=np.float32) - n0 // 2
-    keep = np.zeros((n0, n0, n0), bool)
-    for S in sym.astype(np.float64):
-        cv = Ry.T @ (S.T @ np.array([0.0, 0.0, zv]))
+
+    def region(S):
+        cv = Ry.T @ (S.astype(np.float64).T @ np.array([0.0, 0.0, zv]))
         lo = np.maximum(np.floor(cv - rmask).astype(int) + n0 // 2, 0)
         hi = np.minimum(np.ceil(cv + rmask).astype(int) + n0 // 2 + 1, n0)
         zs, ys, xs = g0[lo[2]:hi[2]], g0[lo[1]:hi[1]], g0[lo[0]:hi[0]]
         d2 = ((zs[:, None, None] - cv[2]) ** 2 + (ys[None, :, None] - cv[1]) ** 2 + (xs[None, None, :] - cv[0]) ** 2)
-        keep[lo[2]:hi[2], lo[1]:hi[1], lo[0]:hi[0]] |= d2 <= rmask * rmask
-    vol = np.where(keep, vol, np.float32(0.0))
+        return (slice(lo[2], hi[2]), slice(lo[1], hi[1]), slice(lo[0], hi[0])), d2 <= rmask * rmask
+
+    regions = [region(S) for S in sym]
+    keep = np.zeros((n0, n0, n0), bool)
+    for sl, m in regions:
+        keep[sl] |= m
+    vol12 = np.where(keep, vol, np.float32(0.0))
     del keep
     p0 = ci.default_params(n0, apix=1.0, minRes=50.0, maxRes=4.0, searchstep=1.0, ampwg=0.07)
     c0 = ci.Context(0, p0)
-    # the same particles (orientations, CTF, origins) noise-free and at SNR 0.1
-    sets = {}
-    for snr in (0.0, 0.1):
-        sets[snr] = synth.make_particles(
-            vol, P, seed + 1, lambda v, e: c0.project_templates(v, _as_tmpl(ci, e)), 1.0, df_range=(1.0, 3.0),
-            astig_max=0.0, origin_max=2.0, snr=snr, ampwg=0.07)
+
+    def particles(V, snr):  # the same orientations, CTF, origins and noise draws for every V
+        return synth.make_particles(V, P, seed + 1, lambda v_, e: c0.project_templates(v_, _as_tmpl(ci, e)), 1.0,
+                                    df_range=(1.0, 3.0), astig_max=0.0, origin_max=2.0, snr=snr, ampwg=0.07)
+
+    full0, parts, truth = particles(vol12, 0.0)
+    full1 = particles(vol12, 0.1)[0]
+    noise = full1 - full0
+    # per vertex: that vertex's signal alone (+ the particle's noise)
+    vert0 = []
+    for sl, m in regions:
+        vk = np.zeros_like(vol)
+        vk[sl] = np.where(m, vol[sl], np.float32(0.0))
+        vert0.append(particles(vk, 0.0)[0])
+        del vk
     c0.close()
-    _, parts, truth = sets[0.1]
     t5, p5, o5 = ci.transform_ort(5, truth[:, 0], truth[:, 1], truth[:, 2])
     # the local map: 128^3 around (0, 0, zv) in the 5-fold frame, C5 about z
     g = np.arange(n) - n // 2
@@ -1135,27 +1191,34 @@ def run_local_report(args):
     c5 = [np.array([[np.cos(a), -np.sin(a), 0], [np.sin(a), np.cos(a), 0], [0, 0, 1]])
           for a in np.radians(72.0 * np.arange(5))]
 
-    def err(th, ph, om, i):  # against the sub-particle's true orientation S E5, modulo C5
-        Rt = sym[i % 12].astype(np.float64) @ synth.euler_mat(t5[i // 12], p5[i // 12], o5[i // 12])
+    def err(th, ph, om, i, k):  # against the sub-particle's true orientation S E5, modulo C5
+        Rt = sym[k].astype(np.float64) @ synth.euler_mat(t5[i], p5[i], o5[i])
         R = synth.euler_mat(th, ph, om)
         return min(_rot_angle(R, Z @ Rt) for Z in c5)
 
     kw = dict(origin_max=4.0, origin_step=0.5, topk=16, pick=1, local_range=3.0, local_step=0.25,
               centred_origins=True)
     d_sub = torch.empty((P * 12, n, n), device="cuda:0")
-    per_snr = {}
-    for snr, (imgs, _, _) in sets.items():
-        d_imgs = torch.from_numpy(imgs).to("cuda:0")
-        torch.cuda.synchronize()
-        lctx.local_box_extract(d_imgs.data_ptr(), q[:4], sym, (0.0, 0.0, zv), 1.0, n, d_out=d_sub.data_ptr(),
-                               fftsize=n0)
-        torch.cuda.synchronize()
-        te = time.perf_counter()
-        _, rec = lctx.local_box_extract(d_imgs.data_ptr(), q, sym, (0.0, 0.0, zv), 1.0, n, d_out=d_sub.data_ptr(),
-                                        fftsize=n0)
-        torch.cuda.synchronize()
-        t_extract = time.perf_counter() - te
+
+    def run(images_of_vertex):
+        """Extraction (one call per vertex image set, or one call for all 12 vertices) and
+        the local search of every sub-particle; records in the order (vertex, particle)."""
+        recs, t_extract = [], 0.0
+        for k, imgs in images_of_vertex:
+            d_imgs = torch.from_numpy(imgs).to("cuda:0")
+            syms = sym if k is None else sym[k:k + 1]
+            off = sum(len(r_) for r_ in recs)
+            torch.cuda.synchronize()
+            te = time.perf_counter()
+            _, rec = lctx.local_box_extract(d_imgs.data_ptr(), q, syms, (0.0, 0.0, zv), 1.0, n,
+                                            d_out=d_sub.data_ptr() + off * n * n * 4, fftsize=n0)
+            torch.cuda.synchronize()
+            t_extract += time.perf_counter() - te
+            recs.append(rec)
+            del d_imgs
+        rec = np.concatenate(recs)
         K = len(rec)
+        assert K == 12 * P, K  # every particle selected, every vertex inside its image
         sp = ci.particles(K)
         sp["particle_id"] = np.arange(1, K + 1)
         sp["img_id"] = np.arange(1, K + 1)
@@ -1170,20 +1233,33 @@ def run_local_report(args):
         lctx.contract_search(d_sub.data_ptr(), out, **kw)
         torch.cuda.synchronize()
         t_search = time.perf_counter() - ts
-        before = np.array([err(sp["theta"][i], sp["phi"][i], sp["omega"][i], i) for i in range(K)])
-        after = np.array([err(out["theta"][i], out["phi"][i], out["omega"][i], i) for i in range(K)])
-        per_snr["noise-free" if snr == 0 else f"snr {snr:g}"] = {
-            "extraction": {"entry": "cryoim_local_box_extract_device", "seconds": t_extract,
-                           "sub_particles_per_s": K / t_extract},
-            "local_search": {"entry": "cryoim_contract_search_device (local form, centred origins)",
-                             "seconds": t_search, "sub_particles_per_s": K / t_search},
-            "pipeline_sub_particles_per_s": K / (t_extract + t_search),
-            "median_error_deg_c5": {"before": float(np.median(before)), "after": float(np.median(after))},
-            "fraction_improved": float(np.mean(after < before))}
-        del d_imgs
+        # (particle, vertex) of each record: per-vertex calls give P records per vertex;
+        # the all-vertex call gives 12 per particle
+        if len(images_of_vertex) == 1:
+            pi, kk = np.arange(K) // 12, np.arange(K) % 12
+        else:
+            pi, kk = np.tile(np.arange(P), 12), np.repeat(np.arange(12), P)
+        before = np.array([err(sp["theta"][j], sp["phi"][j], sp["omega"][j], pi[j], kk[j]) for j in range(K)])
+        after = np.array([err(out["theta"][j], out["phi"][j], out["omega"][j], pi[j], kk[j]) for j in range(K)])
+        return {"extraction": {"entry": "cryoim_local_box_extract_device", "seconds": t_extract,
+                               "sub_particles_per_s": K / t_extract},
+                "local_search": {"entry": "cryoim_contract_search_device (local form, centred origins)",
+                                 "seconds": t_search, "sub_particles_per_s": K / t_search},
+                "pipeline_sub_particles_per_s": K / (t_extract + t_search),
+                "median_error_deg_c5": {"before": float(np.median(before)), "after": float(np.median(after))},
+                "fraction_improved": float(np.mean(after < before)),
+                "fraction_within_0.5_deg_after": float(np.mean(after < 0.5))}
+
+    per_snr = {}
+    for name, nz in (("noise-free", None), ("snr 0.1", noise)):
+        sub = [(k, vert0[k] + (nz if nz is not None else 0.0)) for k in range(12)]
+        kept = [(None, full0 + (nz if nz is not None else 0.0))]
+        per_snr[name] = {"per-vertex subtraction": run(sub), "12 vertices kept": run(kept)}
     res = {"report": "batched localized refinement from whole particles", "particles": P, "sub_particles": P * 12,
            "config": {"particle_box": n0, "apix": 1.0, "sub_box": n, "vertex_z_px": zv, "vertices": 12,
-                      "signal": f"the 12 vertex regions only (spheres of radius {rmask:g} px; the rest subtracted)",
+                      "signal": (f"per sub-particle: its vertex region (sphere of radius {rmask:g} px) and the "
+                                 "particle's noise, the rest of the particle subtracted; beside it all 12 vertex "
+                                 "regions kept in one image"),
                       "local_map": "128^3 around the vertex, 5-fold frame (C5 about z)",
                       "search": "+-3 deg @ 0.25 deg (15,625 orientations) x origins +-4 px @ 0.5 px (289), "
                                 "centred on each sub-particle's own origin, top 16 rescored in FP64",

@@ -158,7 +158,7 @@ class Context:
                         want_cands: bool = False, precision: str = "bf16", nbr: int = 1,
                         coarse: int = 0, learned: int = 0, nbr_best: int = 0,
                         local_range: float = 0.0, local_step: float = 0.0, fallback: float = 0.0,
-                        centred_origins: bool = False):
+                        centred_origins: bool = False, proposal_nbr: int = 0):
         """Tensor-core cross-correlation search with FP64 / phase-residual rescoring of
         the top-k and their grid neighbours within nbr steps; parts is updated in place.
         precision: "bf16" or "fp8" (e4m3 operands with per-band scales); coarse > 0: the
@@ -171,14 +171,16 @@ class Context:
         (learned form): particles whose phase residual lies more than `fallback` robust
         standard deviations above the call's median are searched again exhaustively
         (contract_fallbacks() counts them); centred_origins: the origin grid is centred
-        on each particle's own origin.  Returns (P, topk, 8) candidates if asked: theta,
+        on each particle's own origin; proposal_nbr: the proposals' fine neighbourhood
+        (+- steps, 0 = 2).  Returns (P, topk, 8) candidates if asked: theta,
         phi, omega, x, y, CC (contraction), CC (FP64), PR."""
         assert parts.dtype == PARTICLE_DTYPE and parts.flags["C_CONTIGUOUS"]
         if precision not in ("bf16", "fp8"):
             raise ValueError("precision must be 'bf16' or 'fp8'")
         o = _abi.ContractOpts(float(origin_max), float(origin_step), int(topk), int(pick),
                               int(precision == "fp8"), int(nbr), int(coarse), int(learned), int(nbr_best),
-                              float(local_range), float(local_step), float(fallback), int(bool(centred_origins)))
+                              float(local_range), float(local_step), float(fallback), int(bool(centred_origins)),
+                              int(proposal_nbr))
         out = np.zeros((len(parts), topk, 8), np.float32) if want_cands else None
         if isinstance(imgs, int):
             call("cryoim_contract_search_device", self._h, C.c_void_p(imgs), ptr(parts), len(parts),
@@ -280,6 +282,13 @@ class Context:
         call("cryoim_contract_stats", self._h, ptr(v))
         return {"slice_ms": v[0], "gemm_ms": v[1], "gemm_launches": int(v[2]), "gemm_flops": v[3],
                 "orientations": int(v[4]), "kpad": int(v[5])}
+
+    def rescore_stats(self) -> dict:
+        """The contraction forms' phase-residual rescoring since the last call (timed
+        while profiling is on): launch ms, launches, candidates scored."""
+        v = np.zeros(3, np.float64)
+        call("cryoim_rescore_stats", self._h, ptr(v))
+        return {"ms": v[0], "launches": int(v[1]), "candidates": v[2]}
 
     # -- mode 5 ---------------------------------------------------------------
     def refine(self, imgs, parts: np.ndarray) -> None:

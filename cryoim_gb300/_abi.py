@@ -65,7 +65,8 @@ class ContractOpts(C.Structure):
     _fields_ = [("origin_max", C.c_float), ("origin_step", C.c_float), ("topk", C.c_int32),
                 ("pick", C.c_int32), ("precision", C.c_int32), ("nbr", C.c_int32), ("coarse", C.c_int32),
                 ("learned", C.c_int32), ("nbr_best", C.c_int32), ("local_range", C.c_float),
-                ("local_step", C.c_float), ("fallback", C.c_float), ("centred_origins", C.c_int32)]
+                ("local_step", C.c_float), ("fallback", C.c_float), ("centred_origins", C.c_int32),
+                ("proposal_nbr", C.c_int32)]
 
 
 class LearnOpts(C.Structure):
@@ -110,6 +111,7 @@ SIGNATURES = {
     "cryoim_contract_search": [_vp, _vp, _vp, _i32, _op, _vp],
     "cryoim_contract_search_device": [_vp, _vp, _vp, _i32, _op, _vp],
     "cryoim_contract_stats": [_vp, _vp],
+    "cryoim_rescore_stats": [_vp, _vp],
     "cryoim_rec_add_partial": [_vp, _vp, _vp, _vp],
     "cryoim_mrc_read_header": [C.c_char_p, _vp],
     "cryoim_mrc_read_sections": [C.c_char_p, _i32, _i32, _vp],

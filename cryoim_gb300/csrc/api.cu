@@ -323,7 +323,8 @@ struct Ctx {
     DBuf<unsigned> bandmax;
     DBuf<int> fexp;
     // coarse-to-fine proposals: a 2x-step grid, the half-radius band, a 2x-step origin
-    // grid; its BF16 sections; per-particle gathered fine rows
+    // grid; its BF16 sections; the proposal forms' per-pass row lists (gidx) and the local
+    // form's cut sections (bgather)
     ViewGrid cgrid;
     DBuf<int2> csamples_c;
     int cS_c = 0, cKpad_c = 0, n_origin_c = 0;
@@ -361,6 +362,10 @@ struct Ctx {
     double prof_gemm_ms = 0.0;
     long long prof_gemm_launches = 0;
     double prof_gemm_flops = 0.0;
+    // phase-residual rescoring launches of the contraction forms (profiling on)
+    double prof_pr_ms = 0.0;
+    long long prof_pr_launches = 0;
+    double prof_pr_cands = 0.0;
 
     // pass lanes of the contraction search: this context and xlanes (refresh_lane), each
     // extra lane with its own stream and per-pass buffers, this context's read-only
@@ -842,12 +847,7 @@ int ensure_bmat(Ctx* c) {
     if ((r = ensure_samples(c))) return r;
     const long n = (long)c->V * c->nom;
     if (c->bmat_ready && c->n_orient == n) return CRYOIM_OK;
-    // rows n .. zrow + 7 are zero: rows zrow + j (j = 0..7) fill empty gather slots of
-    // residue j mod 8 in the proposal forms' slot lists
-    const long zrow = (n + 7) / 8 * 8;
-    if ((r = c->bmat.ensure((size_t)(zrow + 8) * c->cKpad))) return r;
-    CK(cudaMemsetAsync(c->bmat.p + (size_t)n * c->cKpad, 0, sizeof(*c->bmat.p) * (size_t)(zrow + 8 - n) * c->cKpad,
-                       c->stream));
+    if ((r = c->bmat.ensure((size_t)n * c->cKpad))) return r;
     std::vector<float> v2(2 * (size_t)c->V);
     for (int v = 0; v < c->V; ++v) { v2[2 * v] = c->views[4 * v]; v2[2 * v + 1] = c->views[4 * v + 1]; }
     DBuf<float> dv;
@@ -1470,8 +1470,7 @@ int ensure_bmat8(Ctx* c) {
     if (c->bmat8_ready) return CRYOIM_OK;
     const int S = c->cS, nband = c->p.max_r + 2;
     const long n = c->n_orient;
-    const long zrow8 = (n + 7) / 8 * 8;
-    if ((r = c->bmat8.ensure((size_t)(zrow8 + 8) * c->cKpad8)) || (r = c->bandmax.ensure(nband)) ||
+    if ((r = c->bmat8.ensure((size_t)n * c->cKpad8)) || (r = c->bandmax.ensure(nband)) ||
         (r = c->mulA.ensure(S)) || (r = c->mulB.ensure(S)))
         return r;
     if (c->num_sms == 0) CK(cudaDeviceGetAttribute(&c->num_sms, cudaDevAttrMultiProcessorCount, c->device));
@@ -1501,8 +1500,6 @@ int ensure_bmat8(Ctx* c) {
     CK(cudaMemcpyAsync(c->mulA.p, ma.data(), sizeof(float) * S, cudaMemcpyHostToDevice, c->stream));
     CK(cudaMemcpyAsync(c->mulB.p, mb.data(), sizeof(float) * S, cudaMemcpyHostToDevice, c->stream));
     CK(launch_b_to_e4m3(c->bmat.p, n, c->cKpad, S, c->mulB.p, c->cKpad8, c->bmat8.p, c->stream));
-    CK(cudaMemsetAsync((unsigned char*)c->bmat8.p + (size_t)n * c->cKpad8, 0, (size_t)(zrow8 + 8 - n) * c->cKpad8,
-                       c->stream));
     CK(cudaEventRecord(e1, c->stream));
     CK(cudaEventSynchronize(e1));
     float ms = 0.f;
@@ -1598,8 +1595,10 @@ int contract_impl(Ctx* c, const float* imgs, bool on_device, cryoim_particle* pa
     const int nbox = (2 * nbr + 1) * (2 * nbr + 1) * (2 * nbr + 1);
     if (nbr > 3 || (long)nbox * k > 4096) return fail(CRYOIM_ERR_ARG, "(2 nbr + 1)^3 x topk must be <= 4096");
     const int kc = opts->coarse;  // 0: exhaustive; else coarse proposals per particle
-    const int nbf = 2;            // fine neighbourhood of a coarse proposal, in fine steps
+    // fine neighbourhood of a proposal, in fine steps
+    const int nbf = opts->proposal_nbr == 0 ? 2 : opts->proposal_nbr;
     if (kc < 0 || kc > 64) return fail(CRYOIM_ERR_ARG, "coarse must be 0..64");
+    if (nbf < 1 || nbf > 4) return fail(CRYOIM_ERR_ARG, "proposal_nbr must be 0..4");
     const int kl = opts->learned;  // 0: off; else learned proposals per particle
     if (kl < 0 || kl > 64 || (kl > 0 && kc > 0)) return fail(CRYOIM_ERR_ARG, "learned must be 0..64, not with coarse");
     if (kl > 0 && !(c->lm.ready && c->lm.step == c->p.searchstep && c->cgrid.V == c->lm.V))
@@ -1784,7 +1783,7 @@ int contract_impl(Ctx* c, const float* imgs, bool on_device, cryoim_particle* pa
             if (kc > 0 || kl > 0 || local) {
                 // proposal forms: the coarse contraction or the learned proposer names each
                 // particle's candidate orientations, the fine contraction runs on their
-                // gathered sections only; the local form cuts each particle's local grid
+                // sections only; the local form cuts each particle's local grid
                 if (!local &&
                     (r = kc > 0 ? coarse_lists(L, nb, ctfp, kc, nbf, lists) : learned_lists(L, nb, kl, nbf, lists)))
                     return r;
@@ -1793,40 +1792,25 @@ int contract_impl(Ctx* c, const float* imgs, bool on_device, cryoim_particle* pa
                 const char* abase = f8 ? (const char*)L->amat8.p : (const char*)L->amat.p;
                 build_rows(0, nb, 0);
                 CK(cudaGetLastError());
-                // the proposal forms gather their sections from the bank: per particle a slot
-                // list of bank rows, slot s of a tile holding a row of residue s mod 8 (the
-                // rows are stored pre-swizzled, so a row copied to a slot of its own residue
-                // is in the tensor cores' layout), empty slots the bank's zero row of that
-                // residue.  The local form cuts each particle's grid into the pass buffer at a
-                // start that is a multiple of 8.
-                const long zrow = (L->n_orient + 7) / 8 * 8;
+                // the proposal forms read their sections from the bank by index: the
+                // contraction's producer copies each listed row into its tile (the rows are
+                // stored pre-swizzled; the copy re-swizzles a row for its tile row).  The
+                // local form cuts each particle's grid into the pass buffer at a start that
+                // is a multiple of 8.
                 const long lpitch = (nloc + 7) / 8 * 8;
-                if (!local) {
-                    slots.resize(nb);
-                    for (int i = 0; i < nb; ++i) {
-                        std::vector<int> bucket[8];
-                        for (int n : lists[i]) bucket[n & 7].push_back(n);
-                        size_t mx = 1;
-                        for (auto& bk : bucket) mx = std::max(mx, bk.size());
-                        const int ntp = (int)((mx + 31) / 32);
-                        slots[i].assign((size_t)ntp * 256, 0);
-                        for (int rho = 0; rho < 8; ++rho)
-                            for (int m = 0; m < 32 * ntp; ++m)
-                                slots[i][8 * (size_t)m + rho] =
-                                    m < (int)bucket[rho].size() ? bucket[rho][m] : (int)(zrow + rho);
-                    }
-                }
+                if (!local) slots = lists;
                 auto rows_of = [&](int i) -> long { return local ? lpitch : (long)slots[i].size(); };
-                // particles in groups whose sections stay under 8 GB: one gather (or cut) and
-                // one grouped contraction (each particle's origin rows against its own
-                // sections) per group, then the k distinct best orientations of each particle
+                // particles in groups (the local form's cut sections under 8 GB per group): one
+                // grouped contraction per group (each particle's origin rows against its own
+                // sections), then the k distinct best orientations of each particle
                 for (int i0 = 0; i0 < nb;) {
                     int i1 = i0;
                     long rows = 0;
-                    while (i1 < nb && (i1 == i0 || (rows + rows_of(i1)) * row_bytes <= (8L << 30)))
+                    while (i1 < nb && (i1 == i0 || !local || (rows + rows_of(i1)) * row_bytes <= (8L << 30)))
                         rows += rows_of(i1++);
-                    if ((r = L->bgather.ensure((size_t)rows * row_bytes))) return r;
+                    GemmArgmaxArgs gg = g;
                     if (local) {
+                        if ((r = L->bgather.ensure((size_t)rows * row_bytes))) return r;
                         std::vector<float> cen(3 * (size_t)(i1 - i0));
                         for (int i = i0; i < i1; ++i) {
                             cen[3 * (i - i0)] = parts[b0 + i].theta;
@@ -1842,10 +1826,15 @@ int contract_impl(Ctx* c, const float* imgs, bool on_device, cryoim_particle* pa
                         std::vector<int> idx;
                         idx.reserve(rows);
                         for (int i = i0; i < i1; ++i) idx.insert(idx.end(), slots[i].begin(), slots[i].end());
+                        for (int n : idx)
+                            if (n < 0 || n >= L->n_orient) return fail(CRYOIM_ERR_STATE, "proposal row %d", n);
                         if ((r = L->gidx.ensure(rows))) return r;
                         CK(cudaMemcpyAsync(L->gidx.p, idx.data(), sizeof(int) * rows, cudaMemcpyHostToDevice,
                                            L->stream));
-                        CK(launch_gather_rows(bsrc, row_bytes, L->gidx.p, (int)rows, L->bgather.p, L->stream));
+                        gg.b_mode = 2;
+                        gg.b_index = L->gidx.p;
+                        gg.b_rows = (const unsigned char*)bsrc;
+                        gg.b_row_bytes = row_bytes;
                     }
                     std::vector<GemmGroup> hg(i1 - i0);
                     std::vector<int2> seg(i1 - i0);
@@ -1869,15 +1858,16 @@ int contract_impl(Ctx* c, const float* imgs, bool on_device, cryoim_particle* pa
                     }
                     if ((r = L->ggroups.ensure(i1 - i0)) || (r = L->gseg.ensure(i1 - i0))) return r;
                     if (L->prof && (r = gmark(ngev++))) return r;
-                    CK(launch_gemm_argmax_grouped(abase, (long)nb * O, L->bgather.p, rows, kpad, f8, hg.data(), i1 - i0,
-                                                  L->ggroups.p, g, L->num_sms, L->stream));
+                    CK(launch_gemm_argmax_grouped(abase, (long)nb * O, local ? (const void*)L->bgather.p : bsrc, rows,
+                                                  kpad, f8, hg.data(), i1 - i0, L->ggroups.p, gg, L->num_sms,
+                                                  L->stream));
                     if (L->prof && (r = gmark(ngev++))) return r;
                     CK(cudaMemcpyAsync(L->gseg.p, seg.data(), sizeof(int2) * seg.size(), cudaMemcpyHostToDevice,
                                        L->stream));
                     launch_select_distinct(L->topv.p, L->topi.p, O, L->gseg.p, i1 - i0, k, L->kor.p + (size_t)i0 * k,
                                            L->korig.p + (size_t)i0 * k, L->kcc.p + (size_t)i0 * k, L->stream);
                     CK(cudaGetLastError());
-                    // the gather buffer is reused by the next group
+                    // the cut-section buffer and the row lists are reused by the next group
                     if (i1 < nb) CK(cudaStreamSynchronize(L->stream));
                     i0 = i1;
                 }
@@ -1913,12 +1903,9 @@ int contract_impl(Ctx* c, const float* imgs, bool on_device, cryoim_particle* pa
             if (gerr) return fail(CRYOIM_ERR_CUDA, "contraction pipeline wait timed out");
             if (f8)  // remove the per-particle exponent: the CC of the unit-norm rows
                 for (int i = 0; i < nb * k; ++i) hcc[i] = std::ldexp(hcc[i], -hfe[i / k]);
-            if (kc > 0 || kl > 0)  // gather slot -> fine orientation index (zero rows: none)
+            if (kc > 0 || kl > 0)  // list position -> fine orientation index
                 for (int i = 0; i < nb * k; ++i)
-                    if (hor[i] >= 0) {
-                        const int n = slots[i / k][hor[i]];
-                        hor[i] = n < L->n_orient ? n : -1;
-                    }
+                    if (hor[i] >= 0) hor[i] = slots[i / k][hor[i]];
             if (L->prof)
                 for (size_t e = 0; e + 1 < ngev; e += 2) {
                     float ms = 0.f;
@@ -2016,11 +2003,23 @@ int contract_impl(Ctx* c, const float* imgs, bool on_device, cryoim_particle* pa
                     if ((r = L->xgroups.ensure(grp.size()))) return r;
                     CK(cudaMemcpyAsync(L->xgroups.p, grp.data(), sizeof(int4) * grp.size(), cudaMemcpyHostToDevice,
                                        L->stream));
+                    if (L->prof && (r = gmark(ngev++))) return r;
                     CK(launch_pr_rescore_groups(a, L->xgroups.p, (int)grp.size(), L->stream));
+                    if (L->prof) {
+                        if ((r = gmark(ngev++))) return r;
+                        for (int i = 0; i < nb; ++i) L->prof_pr_cands += (double)sets[i].size();
+                    }
                 }
                 std::vector<float> h((size_t)nb * maxc);
                 CK(cudaMemcpyAsync(h.data(), L->xpr.p, sizeof(float) * h.size(), cudaMemcpyDeviceToHost, L->stream));
                 CK(cudaStreamSynchronize(L->stream));
+                if (L->prof && !grp.empty() && ngev >= 2) {
+                    float ms = 0.f;
+                    CK(cudaEventElapsedTime(&ms, gev[ngev - 2], gev[ngev - 1]));
+                    L->prof_pr_ms += ms;
+                    L->prof_pr_launches += 1;
+                    ngev -= 2;
+                }
                 out.assign(nb, std::vector<float>());
                 for (int i = 0; i < nb; ++i) out[i].assign(h.begin() + (size_t)i * maxc, h.begin() + (size_t)i * maxc + sets[i].size());
                 return CRYOIM_OK;
@@ -2131,6 +2130,9 @@ int contract_impl(Ctx* c, const float* imgs, bool on_device, cryoim_particle* pa
         X->prof_gemm_ms = 0.0;
         X->prof_gemm_launches = 0;
         X->prof_gemm_flops = 0.0;
+        X->prof_pr_ms = 0.0;
+        X->prof_pr_launches = 0;
+        X->prof_pr_cands = 0.0;
         th.emplace_back([&, X, i] {
             if (cudaSetDevice(X->device) != cudaSuccess) {
                 rx[i] = CRYOIM_ERR_CUDA;
@@ -2147,6 +2149,9 @@ int contract_impl(Ctx* c, const float* imgs, bool on_device, cryoim_particle* pa
         c->prof_gemm_ms += c->xlanes[i]->prof_gemm_ms;
         c->prof_gemm_launches += c->xlanes[i]->prof_gemm_launches;
         c->prof_gemm_flops += c->xlanes[i]->prof_gemm_flops;
+        c->prof_pr_ms += c->xlanes[i]->prof_pr_ms;
+        c->prof_pr_launches += c->xlanes[i]->prof_pr_launches;
+        c->prof_pr_cands += c->xlanes[i]->prof_pr_cands;
     }
     if (r0) return r0;
     for (int i = 0; i + 1 < nlanes; ++i)
@@ -3663,6 +3668,18 @@ int cryoim_contract_stats(void* ctx, double* out /* 6 */) {
     c->prof_gemm_ms = 0.0;
     c->prof_gemm_launches = 0;
     c->prof_gemm_flops = 0.0;
+    return CRYOIM_OK;
+}
+
+int cryoim_rescore_stats(void* ctx, double* out /* 3 */) {
+    Ctx* c = as_ctx(ctx);
+    if (!c || !out) return fail(CRYOIM_ERR_ARG, "null argument");
+    out[0] = c->prof_pr_ms;
+    out[1] = (double)c->prof_pr_launches;
+    out[2] = c->prof_pr_cands;
+    c->prof_pr_ms = 0.0;
+    c->prof_pr_launches = 0;
+    c->prof_pr_cands = 0.0;
     return CRYOIM_OK;
 }
 

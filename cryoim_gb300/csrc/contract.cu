@@ -101,7 +101,8 @@ __device__ __forceinline__ float2 gauss_sample(const float2* __restrict__ cube, 
 // chunk c of row r sits at chunk c ^ (r & 7), the order in which a TMA load with the
 // 128-byte swizzle would place it in shared memory.  A row copied verbatim into a tile
 // row of the same residue mod 8 (a TMA box without swizzle) is then already in the
-// layout the tensor cores read.  Index of
+// layout the tensor cores read; a row copied by index into any tile row has its chunks
+// re-ordered by the XOR of the two residues (gemm_tc.cu, B rows by index).  Index of
 // (Re, Im) pair i of row r: BF16 rows hold 32 pairs per block (4 per chunk), FP8 rows 64
 // (8 per chunk).
 __device__ __forceinline__ long bf16_pair_at(long i, long r) {
@@ -660,24 +661,9 @@ __global__ void __launch_bounds__(256) k_build_a8(const float2* __restrict__ ban
     }
 }
 
-// One CTA per gathered row: dst[r] = src[idx[r]], rows of row_bytes (a multiple of 16).
-__global__ void k_gather_rows(const uint4* __restrict__ src, long row_vec, const int* __restrict__ idx,
-                              uint4* __restrict__ dst) {
-    const long r = blockIdx.x;
-    const uint4* s = src + (long)idx[r] * row_vec;
-    uint4* d = dst + r * row_vec;
-    for (long i = threadIdx.x; i < row_vec; i += blockDim.x) d[i] = s[i];
-}
-
 inline int cdiv(long a, long b) { return (int)((a + b - 1) / b); }
 
 }  // namespace
-
-cudaError_t launch_gather_rows(const void* src, long row_bytes, const int* idx, int n, void* dst, cudaStream_t st) {
-    if (row_bytes % 16 || n < 1) return cudaErrorInvalidValue;
-    k_gather_rows<<<n, 256, 0, st>>>((const uint4*)src, row_bytes / 16, idx, (uint4*)dst);
-    return cudaGetLastError();
-}
 
 cudaError_t launch_band_absmax(const void* B, long n, int Kpad, const int2* samples, int S, int nband, int stride,
                                unsigned* out, int sms, cudaStream_t st) {

@@ -6,16 +6,19 @@
 // section.  The full C is never stored: each (row, 256-column tile) reduces to
 // (max, argmax).
 //
-// Persistent kernel, one CTA per SM, 192 threads:
+// Persistent kernel, one CTA per SM, 320 threads:
 //   warp 0    : TMA producer (one lane) filling a 4-stage ring of 128-row A and 256-row
 //               B tiles of 128 bytes per row (64 BF16 or 128 FP8 elements, 128-byte
-//               swizzle), mbarrier full/empty handshakes;
+//               swizzle), mbarrier full/empty handshakes (A only when B rows come by
+//               index);
 //   warp 1    : MMA issuer (one lane): 4 x tcgen05.mma (M128 N256, K16 BF16 / K32 FP8,
 //               32 bytes of K each) per stage into one of two TMEM accumulators
 //               (2 x 256 columns), tcgen05.commit frees the stage and, at the end of a
 //               tile, signals the epilogue;
 //   warps 2-5 : epilogue, one TMEM lane (= output row) per thread: tcgen05.ld 32
-//               columns at a time, running max/argmax, then release the accumulator.
+//               columns at a time, running max/argmax, then release the accumulator;
+//   warps 6-9 : with B rows by index (the proposal forms' rows, picked from the section
+//               bank), 64 rows of each B tile each, copied with 16-byte cp.async.
 // Tiles are visited m-fastest so consecutive CTAs share a B tile through L2.
 // Every wait is bounded (2 s of %globaltimer); a timeout sets *err, the issuer drains
 // its MMAs, the producer waits for its copies, and TMEM is freed before exit.
@@ -37,9 +40,11 @@ constexpr int GM = 128, GN = 256, GKB = 128, NSTAGE = 4;  // GKB: bytes of K per
 constexpr int A_BYTES = GM * GKB, B_BYTES = GN * GKB;
 constexpr int STAGE_BYTES = A_BYTES + B_BYTES;
 constexpr int TMEM_COLS = 512;
-constexpr int NTHREADS = 192;
+constexpr int NWARP_CORE = 6, NWARP_B = 4;  // producer, issuer, 4 epilogue; B loaders (b_mode 2)
+constexpr int NTHREADS = 32 * (NWARP_CORE + NWARP_B);
 constexpr unsigned long long WAIT_NS = 2000000000ull;
-constexpr int SMEM_BYTES = NSTAGE * STAGE_BYTES + 1024 + 256;
+// ring, alignment slack, barriers (256 B), the current tile's B row table (b_mode 2)
+constexpr int SMEM_BYTES = NSTAGE * STAGE_BYTES + 1024 + 256 + GN * 8;
 
 // instruction descriptors: D=F32 (bits 4-5), A and B formats at bits 7-9 and 10-12
 // (kind::f16: BF16 = 1; kind::f8f6f4: E4M3 = 0), both K-major (bits 15, 16 = 0),
@@ -66,6 +71,15 @@ __device__ __forceinline__ void tma_load_2d(void* dst, const CUtensorMap* tm, in
         " [%0], [%1, {%2, %3}], [%4];" ::"r"(su32(dst)),
         "l"((uint64_t)tm), "r"(c0), "r"(c1), "r"(su32(b))
         : "memory");
+}
+// 16-byte global -> shared copy through L2 (completes at this thread's next wait_group)
+__device__ __forceinline__ void cp16(uint32_t dst, const void* src) {
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(dst), "l"(src) : "memory");
+}
+__device__ __forceinline__ void cp_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+template <int N>
+__device__ __forceinline__ void cp_wait() {
+    asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory");
 }
 __device__ __forceinline__ void tc_fence_before() { tc::fence_before(); }
 __device__ __forceinline__ void tc_fence_after() { tc::fence_after(); }
@@ -137,15 +151,19 @@ __global__ void __launch_bounds__(NTHREADS, 1)
     uint64_t* acce = accf + 2;
     uint64_t* drain = acce + 2;
     uint32_t* tmem_slot = (uint32_t*)(drain + 1);
+    // b_mode 2: per tile row, the byte offset of its bank row | the bank row's residue
+    unsigned long long* srow = (unsigned long long*)((unsigned char*)bars + 256);
 
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     if (threadIdx.x == 0) {
-        for (int s = 0; s < NSTAGE; ++s) { mbar_init(full + s, 1); mbar_init(empty + s, 1); }
+        // b_mode 2: a stage is full after the A copy's arrival (with its bytes) and each B
+        // loader warp's arrival once its copies have landed
+        for (int s = 0; s < NSTAGE; ++s) { mbar_init(full + s, g.b_mode == 2 ? 1 + NWARP_B : 1); mbar_init(empty + s, 1); }
         for (int b = 0; b < 2; ++b) { mbar_init(accf + b, 1); mbar_init(acce + b, 128); }
         mbar_init(drain, 1);
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
         asm volatile("prefetch.tensormap [%0];" ::"l"((uint64_t)&tmA) : "memory");
-        asm volatile("prefetch.tensormap [%0];" ::"l"((uint64_t)&tmB) : "memory");
+        if (g.b_mode != 2) asm volatile("prefetch.tensormap [%0];" ::"l"((uint64_t)&tmB) : "memory");
     }
     if (warp == 0) {
         asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(
@@ -160,7 +178,62 @@ __global__ void __launch_bounds__(NTHREADS, 1)
     const uint32_t tmem = *tmem_slot;
     const int total = g.groups ? g.total_tiles : g.m_tiles * g.n_tiles;
 
-    if (warp == 0) {
+    if (warp >= NWARP_CORE) {
+        // B rows by index (b_mode 2; idle otherwise): warp w of the NWARP_B loaders copies
+        // tile rows 64 w .. 64 w + 63, lane: 16-byte chunk p = lane % 8 of rows
+        // 64 w + 4 i + lane / 8 (a row's 128 bytes from 8 adjacent lanes), re-swizzled
+        // from the bank row's residue to the tile row's.  A stage's copies are one
+        // cp.async group; two groups stay in flight, then the oldest is waited for, made
+        // visible to the tensor core (proxy fence) and its stage's full barrier receives
+        // the warp's arrival.
+        if (g.b_mode == 2) {
+            const int wb = warp - NWARP_CORE, rq = lane >> 3, p = lane & 7;
+            // this warp's rows of the current tile: byte offset of the bank row | its residue
+            unsigned long long* soff = srow + (size_t)wb * (GN / NWARP_B);
+            int s = 0, npend = 0;
+            uint32_t ph = 0;
+            auto signal_oldest = [&]() {
+                tc::fence_proxy_async();
+                __syncwarp();
+                const int so = (s - npend + NSTAGE) % NSTAGE;
+                if (lane == 0) mbar_arrive(full + so);
+                --npend;
+            };
+            bool ok = true;
+            for (int t = blockIdx.x; t < total && ok; t += gridDim.x) {
+                const TileAt ta = tile_at(g, t);
+                __syncwarp();  // the previous tile's copies are issued (they read soff)
+                for (int j = lane; j < GN / NWARP_B; j += 32) {
+                    const int jt = wb * (GN / NWARP_B) + j;
+                    const int jj = ta.nt * GN + jt < ta.n_valid ? jt : -ta.nt * GN;  // padding: the group's first row
+                    const long n = __ldg(g.b_index + ta.b_row + jj);
+                    soff[j] = (unsigned long long)(n * g.b_row_bytes) | (unsigned long long)(n & 7);
+                }
+                __syncwarp();
+                for (int kb = 0; kb < g.kblocks; ++kb) {
+                    const bool okl = mbar_wait(empty + s, ph ^ 1u, g.err, true, g.wait_ns);
+                    if (!__all_sync(0xffffffffu, okl)) { ok = false; break; }
+                    const uint32_t sb = su32(sB + s * B_BYTES) + (uint32_t)(wb * (GN / NWARP_B) * 128);
+                    const unsigned char* src0 = g.b_rows + (long)kb * GKB + p * 16;
+#pragma unroll
+                    for (int i = 0; i < GN / NWARP_B / 4; ++i) {
+                        const int r = 4 * i + rq;  // row within this warp's 64 (same residue as in the tile)
+                        const unsigned long long v = soff[r];
+                        cp16(sb + r * 128 + ((p ^ (int)(v & 7) ^ (r & 7)) << 4), src0 + (v & ~15ull));
+                    }
+                    cp_commit();
+                    if (++s == NSTAGE) { s = 0; ph ^= 1u; }
+                    if (++npend > 2) {
+                        cp_wait<2>();
+                        signal_oldest();
+                    }
+                }
+            }
+            // every copy lands (and every issued stage is signalled) before the CTA can exit
+            cp_wait<0>();
+            while (npend > 0) signal_oldest();
+        }
+    } else if (warp == 0) {
         if (lane == 0) {
             int s = 0;
             uint32_t ph = 0;
@@ -177,9 +250,9 @@ __global__ void __launch_bounds__(NTHREADS, 1)
                         if (++s == NSTAGE) { s = 0; ph ^= 1u; }
                         continue;
                     }
-                    mbar_expect_tx(full + s, STAGE_BYTES);
+                    mbar_expect_tx(full + s, g.b_mode == 2 ? A_BYTES : STAGE_BYTES);
                     tma_load_2d(sA + s * A_BYTES, &tmA, kb * GK, ta.a_row, full + s);
-                    tma_load_2d(sB + s * B_BYTES, &tmB, kb * GK, ta.b_row, full + s);
+                    if (g.b_mode != 2) tma_load_2d(sB + s * B_BYTES, &tmB, kb * GK, ta.b_row, full + s);
                     used[s] = true;
                     last_par[s] = ph;
                     if (++s == NSTAGE) { s = 0; ph ^= 1u; }
@@ -216,7 +289,7 @@ __global__ void __launch_bounds__(NTHREADS, 1)
             tc_commit(drain);
             mbar_wait(drain, 0, g.err, false, g.wait_ns);
         }
-    } else {
+    } else if (warp >= 2) {
         const int q = warp & 3;
         const int row_in_tile = 32 * q + lane;
         int lt = 0;
@@ -340,8 +413,15 @@ cudaError_t launch_gemm_argmax_grouped(const void* a, long Mtot, const void* b, 
     if (in.b_mode == 1)  // pre-swizzled rows: every group's tiles start at a multiple of 8 rows
         for (int i = 0; i < ngroups; ++i)
             if (hg[i].b_row0 % 8) return cudaErrorInvalidValue;
+    // b_mode 2: b is the bank (in.b_rows), Ntot the length of the index list in.b_index
+    if (in.b_mode == 2 && (!in.b_index || in.b_rows != b || ((uintptr_t)in.b_rows & 15) ||
+                           in.b_row_bytes % 16 || in.b_row_bytes < (long)K * (f8 ? 1 : 2)))
+        return cudaErrorInvalidValue;
     CUtensorMap ta, tb;
-    if (!make_map(&ta, a, Mtot, K, GM, f8) || !make_map(&tb, b, Ntot, K, GN, f8, in.b_mode == 0))
+    if (!make_map(&ta, a, Mtot, K, GM, f8)) return cudaErrorInvalidValue;
+    if (in.b_mode == 2)
+        tb = ta;  // not read
+    else if (!make_map(&tb, b, Ntot, K, GN, f8, in.b_mode == 0))
         return cudaErrorInvalidValue;
     cudaError_t e = cudaMemcpyAsync(dg, hg, sizeof(GemmGroup) * ngroups, cudaMemcpyHostToDevice, st);
     if (e != cudaSuccess) return e;

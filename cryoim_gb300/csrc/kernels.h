@@ -162,8 +162,14 @@ struct GemmArgmaxArgs {
     int withhold = 0;
     // operand B: 0 plain rows (the TMA load applies the 128-byte swizzle); 1 pre-swizzled
     // rows (contract.cu's section rows) loaded by TMA tiles without swizzle, every tile
-    // starting at a multiple of 8 rows (so a row's residue mod 8 is its slot's)
+    // starting at a multiple of 8 rows (so a row's residue mod 8 is its slot's); 2 (grouped
+    // launches only) pre-swizzled rows by index: row j of a group's B is row
+    // b_index[b_row0 + j] of b_rows (b_row_bytes apart), copied into the tile by the
+    // producer warp's 16-byte cp.async with the chunks re-swizzled for the tile row
     int b_mode = 0;
+    const int* b_index = nullptr;
+    const unsigned char* b_rows = nullptr;
+    long b_row_bytes = 0;
 };
 int gemm_tile_n();
 int gemm_tile_m();
@@ -275,8 +281,6 @@ void launch_select_distinct(float* topv, const int* topi, int O, const int2* seg
 // FP8-e4m3 operands (contract.cu): per-band max |B| (R+1 bands, float bits) over every
 // stride-th row; B8 = e4m3(B x mulB) with rows of Kpad8 bytes; A8 rows with mulA and the
 // per-particle exponent fexp (written by launch_build_a8).
-// rows idx[0 .. n) of src (row_bytes each, a multiple of 16) into consecutive rows of dst
-cudaError_t launch_gather_rows(const void* src, long row_bytes, const int* idx, int n, void* dst, cudaStream_t st);
 cudaError_t launch_band_absmax(const void* B, long n, int Kpad, const int2* samples, int S, int nband, int stride,
                                unsigned* out, int sms, cudaStream_t st);
 cudaError_t launch_b_to_e4m3(const void* B, long n, int Kpad, int S, const float* mulB, int Kpad8, void* B8,

@@ -106,6 +106,34 @@ __device__ __forceinline__ float angle_between(float cross, float dot, float pi)
     return (dot < 0.0f) ? pi - r : r;
 }
 
+// angle_between with the hardware reciprocal estimate (relative error ~2^-23, below the
+// polynomial's 1.7e-6 rad) in place of the correctly rounded one.
+__device__ __forceinline__ float angle_between_est(float cross, float dot, float pi) {
+    const float a = fabsf(cross), b = fabsf(dot);
+    const float mx = fmaxf(a, b), mn = fminf(a, b);
+    float rc;
+    asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(rc) : "f"(mx));
+    const float t = mn * rc;
+    const float s = t * t;
+    float p = fmaf(s, -0.011719364672899246f, 0.05264794081449509f);
+    p = fmaf(p, s, -0.11642702668905258f);
+    p = fmaf(p, s, 0.19354058802127838f);
+    p = fmaf(p, s, -0.33262285590171814f);
+    p = fmaf(p, s, 0.9999772310256958f);
+    float r = t * p;
+    r = (a > b) ? 0.5f * pi - r : r;
+    return (dot < 0.0f) ? pi - r : r;
+}
+
+// Kahan summation of the pair (x.x into s.x, x.y into s.y) in packed FP32x2 operations,
+// the same per-component arithmetic as kahan_add.
+__device__ __forceinline__ void kahan_add2(float2& s, float2& c, float2 x) {
+    const float2 y = __fadd2_rn(x, make_float2(-c.x, -c.y));
+    const float2 t = __fadd2_rn(s, y);
+    c = __fadd2_rn(__fadd2_rn(t, make_float2(-s.x, -s.y)), make_float2(-y.x, -y.y));
+    s = t;
+}
+
 __global__ void __launch_bounds__(768, 1) k_pr_omega(PrOmegaArgs a, int nomp, Consts K) {
     extern __shared__ __align__(16) unsigned char smraw[];
     const Band bd = a.bd;
@@ -192,7 +220,7 @@ __global__ void __launch_bounds__(768, 1) k_pr_omega(PrOmegaArgs a, int nomp, Co
                         if (amp1 >= e.w) {
                             const float2 pd = __fmul2_rn(z, make_float2(e.x, e.y));
                             const float2 pc = __fmul2_rn(z, make_float2(e.y, -e.x));
-                            const float d = angle_between(pc.x + pc.y, pd.x + pd.y, K.pi);
+                            const float d = angle_between_est(pc.x + pc.y, pd.x + pd.y, K.pi);
                             const float w = fmaf(0.5f, amp1, e.z);
                             acc = __ffma2_rn(make_float2(d, 1.0f), make_float2(w, w), acc);
                         }
@@ -444,6 +472,143 @@ __global__ void __launch_bounds__(512) k_pr_rescore_g(PrSingleArgs a, const int4
     }
 }
 
+// Grouped rescoring with the particle's shifted band in shared memory.  The groups, the
+// tables and the template side are k_pr_rescore_g's; the particle side reads its four
+// taps from a [W][SP] float2 copy of the band in shared memory (SP = the smallest pitch
+// >= W that is 3 mod 16: 8-byte taps of a line of radii fall on distinct bank pairs
+// for vertical lines and spread over 4-8 for diagonal ones) instead of 16-byte
+// pixel pairs from L1, and its per-term arithmetic is k_pr_omega's in packed FP32x2
+// operations, so a term has the value the exhaustive search gives it.  One block of
+// RS_THREADS threads per SM (the band is 136 KB at W = 130).
+// A two-phase variant (per template: the template samples that pass their cut compacted
+// into a shared-memory list by a block-wide scan, then the candidates over the list with
+// full warps) was built and measured 1.7x slower (4.72 against 2.79 ms for the four
+// launches of the profile case): its four barriers per template leave the template
+// samples' L2 latency exposed with one block per SM, where the flat loop overlaps it.
+constexpr int RS_THREADS = 1024;
+__host__ __device__ inline int rescore_pitch(int W) { return W + ((3 - W % 16) + 16) % 16; }
+__global__ void __launch_bounds__(RS_THREADS, 1) k_pr_rescore_s(PrSingleArgs a, const int4* __restrict__ groups,
+                                                                  Consts K) {
+    extern __shared__ __align__(16) float rsm[];
+    __shared__ double sh[2][RG][RS_THREADS / 32];
+    const Band bd = a.bd;
+    const int W = bd.W, nr = bd.nr, minR = bd.min_r, nx = bd.nx, T = a.T;
+    const int SP = rescore_pitch(W);
+    const int4 gr = groups[blockIdx.x];
+    const int p = gr.x, c0 = gr.y, m = gr.z;
+    float2* sbd = reinterpret_cast<float2*>(rsm);   // [W][SP] shifted particle band
+    float* spl = rsm + 2L * W * SP;                 // [RG][T][60][2]: cos, sin of the particle lines
+    float* stl = spl + (long)RG * T * 120;          // [T][60][2]: cos, sin of the template lines
+    float* sfc = stl + (long)T * 120;               // [T + 1][nr]: template cuts, then the particle's
+    int* sval = reinterpret_cast<int*>(sfc + (long)(T + 1) * nr);  // [T][60]
+    const float4* sb = a.sband + (long)p * W * W;
+    for (int row = threadIdx.x >> 5; row < W; row += RS_THREADS / 32)
+        for (int col = threadIdx.x & 31; col < W; col += 32) {
+            const float4 v = sb[(long)row * W + col];
+            sbd[row * SP + col] = make_float2(v.x, v.y);
+        }
+    for (int q = threadIdx.x; q < T * 60; q += RS_THREADS) {
+        const float2 aa = a.alpha[((long)p * a.ncand + c0) * T * 60 + q];
+        const bool ok = aa.x < 999.0f && aa.y < 999.0f;
+        sval[q] = ok;
+        if (ok) {
+            const float a2 = __fmul_rn(aa.y, K.d2r);
+            stl[2 * q] = cosf(a2);
+            stl[2 * q + 1] = sinf(a2);
+        }
+    }
+    for (int q = threadIdx.x; q < m * T * 60; q += RS_THREADS) {
+        const int g = q / (T * 60), r = q - g * T * 60;
+        const float2 aa = a.alpha[((long)p * a.ncand + c0 + g) * T * 60 + r];
+        const float a1 = __fmul_rn(aa.x, K.d2r);
+        spl[2 * q] = cosf(a1);
+        spl[2 * q + 1] = sinf(a1);
+    }
+    const float* tfc = a.tfcut + (long)p * a.tfcut_pstride;
+    for (int q = threadIdx.x; q < T * nr; q += RS_THREADS) sfc[q] = tfc[q];
+    for (int q = threadIdx.x; q < nr; q += RS_THREADS) sfc[T * nr + q] = a.fcut0[(long)p * nr + q];
+    __syncthreads();
+    const float nxh = (float)(nx / 2);
+    const int offW = bd.off * W + bd.off, offS = bd.off * SP + bd.off;
+    const float4* tbc0 = a.tbandc ? a.tbandc + (long)p * T * W * W : nullptr;
+    const float* ctfp = a.ctf ? a.ctf + (long)p * W * W : nullptr;
+    const int per_t = 60 * nr;
+    float2 fs[RG], fk[RG];  // (PR numerator, weight) sums and their Kahan compensations
+#pragma unroll
+    for (int g = 0; g < RG; ++g) { fs[g] = make_float2(0.f, 0.f); fk[g] = make_float2(0.f, 0.f); }
+    const int step_j = RS_THREADS / nr, step_iq = RS_THREADS - step_j * nr;
+    int i = (int)threadIdx.x / per_t, j = ((int)threadIdx.x - i * per_t) / nr;
+    int iq = (int)threadIdx.x - i * per_t - j * nr;
+    auto advance = [&]() {
+        iq += step_iq;
+        j += step_j;
+        if (iq >= nr) { iq -= nr; ++j; }
+        while (j >= 60) { j -= 60; ++i; }
+    };
+    const float2 nxh2 = make_float2(nxh, nxh);
+    for (int q = threadIdx.x; q < T * per_t; q += RS_THREADS, advance()) {
+        const int lj = i * 60 + j;
+        if (!sval[lj]) continue;
+        const float fr = (float)(minR + iq);
+        float re2, im2;
+        if (tbc0)
+            tmpl_sample_pairs(tbc0 + (long)i * W * W, W, offW, nxh, stl[2 * lj], stl[2 * lj + 1], fr, &re2, &im2);
+        else
+            tmpl_sample_cs(a.tband + (long)i * W * W, ctfp, W, offW, nxh, stl[2 * lj], stl[2 * lj + 1], fr, &re2,
+                           &im2);
+        const float amp2 = sqrtf(re2 * re2 + im2 * im2);
+        if (!(amp2 >= sfc[i * nr + iq])) continue;
+        const float cut1 = sfc[T * nr + iq];
+        const float2 fr2 = make_float2(fr, fr), e2 = make_float2(re2, im2), e2c = make_float2(im2, -re2);
+        const float half2 = 0.5f * amp2;
+        const float2 m1 = make_float2(-1.f, -1.f);
+#pragma unroll
+        for (int g = 0; g < RG; ++g) {
+            if (g >= m) break;
+            // k_pr_omega's per-term arithmetic: position by FMA, bilinear as lerps on
+            // (re, im) pairs, amplitude sq * rsqrt(sq), weight 0.5 amp1 + 0.5 amp2
+            const float2 cs = *reinterpret_cast<const float2*>(&spl[2 * ((long)g * T * 60 + lj)]);
+            const float2 xy = __ffma2_rn(fr2, cs, nxh2);
+            const int lx = (int)xy.x, ly = (int)xy.y;
+            const float2 f = __fadd2_rn(xy, make_float2(-(float)lx, -(float)ly));
+            const float2* tp = sbd + (ly * SP + lx - offS);
+            const float2 t00 = tp[0], t10 = tp[1], t01 = tp[SP], t11 = tp[SP + 1];
+            const float2 ax2 = make_float2(f.x, f.x), ay2 = make_float2(f.y, f.y);
+            const float2 v0 = __ffma2_rn(ax2, __ffma2_rn(t00, m1, t10), t00);
+            const float2 v1 = __ffma2_rn(ax2, __ffma2_rn(t01, m1, t11), t01);
+            const float2 z = __ffma2_rn(ay2, __ffma2_rn(v0, m1, v1), v0);
+            const float2 zz = __fmul2_rn(z, z);
+            const float sq = zz.x + zz.y;
+            const float amp1 = sq * rsqrtf(sq);  // NaN for 0: fails the cut
+            if (amp1 >= cut1) {
+                const float2 pd = __fmul2_rn(z, e2);
+                const float2 pc = __fmul2_rn(z, e2c);
+                const float d = angle_between_est(pc.x + pc.y, pd.x + pd.y, K.pi);
+                const float w = fmaf(0.5f, amp1, half2);
+                kahan_add2(fs[g], fk[g], make_float2(d * w, w));
+            }
+        }
+    }
+    const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
+#pragma unroll
+    for (int g = 0; g < RG; ++g) {
+        double p1 = (double)fs[g].x, p2 = (double)fs[g].y;
+        for (int o = 16; o > 0; o >>= 1) {
+            p1 += __shfl_xor_sync(0xffffffffu, p1, o);
+            p2 += __shfl_xor_sync(0xffffffffu, p2, o);
+        }
+        if (l == 0) { sh[0][g][w] = p1; sh[1][g][w] = p2; }
+    }
+    __syncthreads();
+    if (threadIdx.x < m) {
+        const int g = threadIdx.x;
+        double s1 = 0, s2 = 0;
+        for (int q = 0; q < RS_THREADS / 32; ++q) { s1 += sh[0][g][q]; s2 += sh[1][g][q]; }
+        const float g1 = (float)s1, g2 = (float)s2;
+        a.pr[(long)p * a.ncand + c0 + g] = (g2 > 1.0e-10f) ? g1 / g2 * 180.0f / K.pi : 1000.0f;
+    }
+}
+
 // The particle transform shifted to the origin its candidates share (cand[p][0][3..4]):
 // per pixel the same phase rotation k_pr_single applies to each bilinear tap
 // (img2d_FT_centshift.f90), computed once per pixel instead of once per tap.
@@ -618,6 +783,14 @@ cudaError_t launch_pr_rescore_groups(const PrSingleArgs& a, const int4* groups, 
     if (!a.sband || ngroups < 1) return cudaErrorInvalidValue;
     const size_t sm = sizeof(float) * ((size_t)RG * a.T * 120 + (size_t)a.T * 120 + (size_t)(a.T + 1) * a.bd.nr) +
                       sizeof(int) * a.T * 60;
+    // the band in shared memory where it fits beside the tables (W <= ~140 at T = 20)
+    const size_t sm_s = sm + sizeof(float2) * (size_t)a.bd.W * rescore_pitch(a.bd.W);
+    if (sm_s + sizeof(double) * 2 * RG * (RS_THREADS / 32) <= 227 * 1024) {
+        cudaError_t e = cudaFuncSetAttribute(k_pr_rescore_s, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm_s);
+        if (e != cudaSuccess) return e;
+        k_pr_rescore_s<<<ngroups, RS_THREADS, sm_s, st>>>(a, groups, consts());
+        return cudaGetLastError();
+    }
     if (sm > 200 * 1024) return cudaErrorInvalidValue;
     cudaError_t e = cudaFuncSetAttribute(k_pr_rescore_g, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
     if (e != cudaSuccess) return e;

@@ -464,8 +464,8 @@ typedef struct cryoim_contract_opts {
     int32_t coarse;     /* 0: every grid orientation is correlated.  k > 0 (<= 64):
                            proposal form: a BF16 contraction over half the band, a
                            grid of twice the step and origins at twice the step names
-                           k orientations; only their fine neighbourhoods (+-2 steps)
-                           are correlated at full band                              */
+                           k orientations; only their fine neighbourhoods (+-2 steps,
+                           proposal_nbr) are correlated at full band                */
     int32_t learned;    /* 0: off.  k > 0 (<= 64, not with coarse): the trained
                            proposer (cryoim_learn_train / _load) names k cells (view
                            of the twice-the-step grid, in-plane angle and the angle
@@ -497,6 +497,9 @@ typedef struct cryoim_contract_opts {
     int32_t centred_origins; /* 0: the origin grid is absolute.  1: it is centred on
                            each particle's own (x, y) (the local form's re-centred
                            origin search; PR rescoring is unaffected)                */
+    int32_t proposal_nbr; /* coarse and learned forms: each proposal's fine
+                           neighbourhood, +-proposal_nbr steps in theta, phi and
+                           omega (0 is taken as 2; 1..4)                             */
 } cryoim_contract_opts;
 
 /* ---- learned orientation proposer ------------------------------------------- */
@@ -580,6 +583,9 @@ int cryoim_contract_fallbacks(void* ctx, int32_t* n);
 /* out[6]: section build ms, contraction ms and launches since the last call (timed when
  * profiling is on), contraction FLOP, orientations, padded K. Resets the counters. */
 int cryoim_contract_stats(void* ctx, double* out);
+/* out[3]: the contraction forms' phase-residual rescoring since the last call (timed when
+ * profiling is on): launch ms, launches, candidates scored.  Resets the counters. */
+int cryoim_rescore_stats(void* ctx, double* out);
 
 /* Kernel-level hook of the tensor-core contraction (no reference counterpart: the
  * reference has no cross-correlation search).  Device pointers: A (M x K) and B (N x K)
