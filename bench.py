@@ -537,6 +537,7 @@ def run_ours(args):
     lparts_c["phi"] = ltruth_c[:, 1] + lrng2.uniform(-2.5, 2.5, nlc)
     lparts_c["omega"] = ltruth_c[:, 2] + lrng2.uniform(-2.5, 2.5, nlc)
     lctx.set_reference_map(lvol)
+    lctx.set_interpolation("oversampled")
     d_limg = torch.from_numpy(limg_c).to(f"cuda:{dev}")
     lcopts = dict(origin_max=4.0, origin_step=0.5, topk=16, pick=1, local_range=3.0, local_step=0.25)
     lctx.contract_search(d_limg.data_ptr(), lparts_c[:64].copy(), **lcopts)
@@ -703,8 +704,8 @@ def run_ours(args):
                 "value": 2 * nlc / (lc_ms / 1000.0), "unit": "sub-particles/s", "sub_particles": nlc,
                 "config": "128^2 sub-particles of a 128^3 map at 1 A/px, band 1/50-1/4 A^-1, local grid "
                           "+-3 deg at 0.25 deg (15,625 orientations) x origins +-4 px at 0.5 px (289), "
-                          "top 16 rescored in FP64, SNR %g, starting orientations within 2.5 deg per "
-                          "Euler angle of the truth" % w["snr"],
+                          "top 16 rescored in FP64, sections from the twice-oversampled transform, SNR %g, "
+                          "starting orientations within 2.5 deg per Euler angle of the truth" % w["snr"],
                 "entry": "cryoim_contract_search_device with local_range 3, local_step 0.25",
                 "median_error_vs_truth_deg": {"after": float(np.median(lc_err)), "before": float(np.median(lc_err0))},
                 "roofline": dict(gemm_roofline(lc_g, peak_s, "k_gemm_argmax<bf16> (grouped, local grids)",
@@ -1176,7 +1177,10 @@ def run_local_report(args):
     zz, yy, xx = np.meshgrid(g, g, g, indexing="ij")
     X = np.stack([xx.ravel(), yy.ravel(), zz.ravel() + zv]).astype(np.float64)
     Xm = Ry.T @ X + n0 // 2
-    lmap = map_coordinates(vol, [Xm[2], Xm[1], Xm[0]], order=1, mode="constant").reshape(n, n, n).astype(np.float32)
+    lmap = map_coordinates(vol, [Xm[2], Xm[1], Xm[0]], order=1, mode="constant").reshape(n, n, n)
+    # the local map holds the vertex region the sub-particles keep (a map reconstructed
+    # from the subtracted sub-particles holds no more)
+    lmap = np.where(zz ** 2 + yy ** 2 + xx ** 2 <= rmask * rmask, lmap, 0.0).astype(np.float32)
     # starting orientations in the 5-fold frame, up to 1 degree off per Euler angle
     q = parts.copy()
     q["theta"] = t5 + rng.uniform(-1, 1, P)
@@ -1188,6 +1192,7 @@ def run_local_report(args):
     lctx = ci.Context(0, lp)
     lctx.set_lanes(LANES)
     lctx.set_reference_map(lmap)
+    lctx.set_interpolation("oversampled")
     c5 = [np.array([[np.cos(a), -np.sin(a), 0], [np.sin(a), np.cos(a), 0], [0, 0, 1]])
           for a in np.radians(72.0 * np.arange(5))]
 
@@ -1260,9 +1265,12 @@ def run_local_report(args):
                       "signal": (f"per sub-particle: its vertex region (sphere of radius {rmask:g} px) and the "
                                  "particle's noise, the rest of the particle subtracted; beside it all 12 vertex "
                                  "regions kept in one image"),
-                      "local_map": "128^3 around the vertex, 5-fold frame (C5 about z)",
+                      "local_map": "128^3 around the vertex, 5-fold frame (C5 about z), the vertex region "
+                                   f"(radius {rmask:g} px) only",
                       "search": "+-3 deg @ 0.25 deg (15,625 orientations) x origins +-4 px @ 0.5 px (289), "
-                                "centred on each sub-particle's own origin, top 16 rescored in FP64",
+                                "centred on each sub-particle's own origin, top 16 rescored in FP64; sections "
+                                "from the twice-oversampled transform; score sum Re(P conj(CTF S)) / "
+                                "(|P| |CTF S|)",
                       "ctf": "defocus U(1.0, 3.0) um", "start": "truth + U(+-1 deg) per Euler angle"},
            "phantom_s": t_phantom, "results": per_snr}
     print(json.dumps(res))

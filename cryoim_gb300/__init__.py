@@ -268,9 +268,11 @@ class Context:
         return out
 
     def set_interpolation(self, kind: str = "trilinear", sigma: float = 0.0) -> None:
-        """Sections of the contraction forms: "trilinear" or "gaussian" (kernel width sigma
-        voxels, 27 taps)."""
-        call("cryoim_set_interpolation", self._h, 1 if kind == "gaussian" else 0, float(sigma))
+        """Sections of the contraction forms: "trilinear", "gaussian" (kernel width sigma
+        voxels, 27 taps) or "oversampled" (trilinear on the transform of the map padded to
+        twice its side)."""
+        k = {"trilinear": 0, "gaussian": 1, "oversampled": 2}[kind]
+        call("cryoim_set_interpolation", self._h, k, float(sigma))
 
     def contract_fallbacks(self) -> int:
         n = C.c_int32()

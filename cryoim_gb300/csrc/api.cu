@@ -318,6 +318,11 @@ struct Ctx {
     double last_slice_ms = 0.0;
     int last_fallbacks = 0;   // particles of the last contraction call re-searched exhaustively
     float interp_sigma = 0.0f;  // sections: 0 trilinear, > 0 Gaussian kernel of this width (voxels)
+    // band cube of the reference map: of the map itself (ovs 1) or of the map zero-padded
+    // to twice its side (ovs 2, trilinear on a twice-oversampled transform); its radius
+    // cube_r (side 2 cube_r + 3); the map kept on the device to rebuild it
+    int ovs = 1, cube_r = 0;
+    DBuf<float> mapreal;
     DBuf<float> poff;         // per-pass particle origins (x, y) of the centred origin grid
     DBuf<float> mulA, mulB;
     DBuf<unsigned> bandmax;
@@ -340,6 +345,9 @@ struct Ctx {
     DBuf<int> topi, gerr, kor, korig;
     DBuf<double> pnorm, kcc64;
     DBuf<double2> pcband;  // per particle of a pass: CTF x (a, b) per band sample, FP64
+    // the local form's unbiased score: per particle of a pass sum |P|^2 and the CTF per sample
+    DBuf<double> pnorm0;
+    DBuf<float> pctf;
     int n_origin = 0;
     float orig_max = -1.0f, orig_step = -1.0f;
     DBuf<float> tilev, xcand, xpr;
@@ -382,9 +390,9 @@ struct Ctx {
         tfcut.release(); state.release(); cand.release(); rpr.release(); rot.release();
         prbuf.release(); fft.release(); band.release(); ralpha.release(); best.release();
         flag.release(); sel.release(); acc.release(); samples.release(); vol.release();
-        mapcube.release(); csamples.release(); bmat.release(); amat.release(); corigins.release();
+        mapcube.release(); mapreal.release(); csamples.release(); bmat.release(); amat.release(); corigins.release();
         topv.release(); kcc.release(); kcand.release(); topi.release(); gerr.release();
-        kor.release(); korig.release(); pnorm.release(); kcc64.release();
+        kor.release(); korig.release(); pnorm.release(); kcc64.release(); pnorm0.release(); pctf.release();
         tilev.release(); xcand.release(); xpr.release(); tileo.release(); tileorig.release();
         xalpha.release(); bmat8.release(); amat8.release(); mulA.release(); mulB.release();
         bandmax.release(); fexp.release();
@@ -858,11 +866,11 @@ int ensure_bmat(Ctx* c) {
     CK(cudaEventCreate(&e1));
     cudaArray_t arr = nullptr;
     cudaTextureObject_t tex = 0;
-    cudaError_t te = make_cube_texture(c->mapcube.p, c->p.max_r, c->stream, &arr, &tex);
+    cudaError_t te = make_cube_texture(c->mapcube.p, c->cube_r, c->stream, &arr, &tex);
     if (te == cudaSuccess) te = cudaEventRecord(e0, c->stream);
     if (te == cudaSuccess)
-        te = launch_slice_bf16(tex, c->p.max_r, c->csamples.p, c->cS, c->cKpad, dv.p, c->nom, c->p.searchstep, 0,
-                               n, c->bmat.p, c->stream, c->mapcube.p, c->interp_sigma);
+        te = launch_slice_bf16(tex, c->cube_r, c->csamples.p, c->cS, c->cKpad, dv.p, c->nom, c->p.searchstep, 0,
+                               n, c->bmat.p, c->stream, c->mapcube.p, c->interp_sigma, (float)c->ovs);
     if (te == cudaSuccess) te = cudaEventRecord(e1, c->stream);
     if (te == cudaSuccess) te = cudaEventSynchronize(e1);
     free_cube_texture(arr, tex);
@@ -908,10 +916,10 @@ int ensure_coarse(Ctx* c, float omax, float ostep) {
         CK(cudaMemcpyAsync(dv.p, v2.data(), sizeof(float) * v2.size(), cudaMemcpyHostToDevice, c->stream));
         cudaArray_t arr = nullptr;
         cudaTextureObject_t tex = 0;
-        cudaError_t te = make_cube_texture(c->mapcube.p, R, c->stream, &arr, &tex);
+        cudaError_t te = make_cube_texture(c->mapcube.p, c->cube_r, c->stream, &arr, &tex);
         if (te == cudaSuccess)
-            te = launch_slice_bf16(tex, R, c->csamples_c.p, c->cS_c, c->cKpad_c, dv.p, g.nom, g.step, 0, n,
-                                   c->bmat_c.p, c->stream, c->mapcube.p, c->interp_sigma);
+            te = launch_slice_bf16(tex, c->cube_r, c->csamples_c.p, c->cS_c, c->cKpad_c, dv.p, g.nom, g.step, 0, n,
+                                   c->bmat_c.p, c->stream, c->mapcube.p, c->interp_sigma, (float)c->ovs);
         if (te == cudaSuccess) te = cudaStreamSynchronize(c->stream);
         free_cube_texture(arr, tex);
         if (te != cudaSuccess) return fail(CRYOIM_ERR_CUDA, "coarse sections: %s", cudaGetErrorString(te));
@@ -1542,6 +1550,8 @@ int refresh_lane(Ctx* c, int i) {
     h->alpha.borrow(c->alpha);
     h->mapcube.borrow(c->mapcube);
     h->map_ready = c->map_ready;
+    h->ovs = c->ovs;
+    h->cube_r = c->cube_r;
     h->csamples.borrow(c->csamples);
     h->cS = c->cS; h->cKpad = c->cKpad;
     h->bmat.borrow(c->bmat);
@@ -1657,7 +1667,7 @@ int contract_impl(Ctx* c, const float* imgs, bool on_device, cryoim_particle* pa
         cudaTextureObject_t tex = 0;
         ~LocalTexture() { free_cube_texture(arr, tex); }
     } ltex;
-    if (local) CK(make_cube_texture(c->mapcube.p, c->p.max_r, c->stream, &ltex.arr, &ltex.tex));
+    if (local) CK(make_cube_texture(c->mapcube.p, c->cube_r, c->stream, &ltex.arr, &ltex.tex));
     // rescoring set: each selected orientation and its grid neighbours within nbr steps
     const int maxx = nbox * k;
     if (c->num_sms == 0) CK(cudaDeviceGetAttribute(&c->num_sms, cudaDevAttrMultiProcessorCount, c->device));
@@ -1690,6 +1700,7 @@ int contract_impl(Ctx* c, const float* imgs, bool on_device, cryoim_particle* pa
             (r = L->kcand.ensure((size_t)PB * k * 5)) || (r = L->kcc64.ensure((size_t)PB * k)) ||
             (r = L->kpart.ensure((size_t)cc_fp64_scratch(k, PB))))
             return r;
+        if (local && ((r = L->pnorm0.ensure(PB)) || (r = L->pctf.ensure((size_t)PB * L->cS)))) return r;
         if ((r = L->tilev.ensure((size_t)pb * ntiles)) || (r = L->tileo.ensure((size_t)pb * ntiles)) ||
             (r = L->tileorig.ensure((size_t)pb * ntiles)) || (r = L->xcand.ensure((size_t)PB * maxx * 5)) ||
             (r = L->xpr.ensure((size_t)PB * maxx)))
@@ -1752,7 +1763,7 @@ int contract_impl(Ctx* c, const float* imgs, bool on_device, cryoim_particle* pa
                 }
             }
             launch_particle_norm(L->band.p, ctfp, L->bd, L->csamples.p, L->cS, nb, L->pnorm.p, L->stream,
-                                 L->pcband.p);
+                                 L->pcband.p, local ? L->pnorm0.p : nullptr, local ? L->pctf.p : nullptr);
             if (centred) {  // the origin grid around each particle's own origin
                 std::vector<float> po(2 * (size_t)nb);
                 for (int i = 0; i < nb; ++i) { po[2 * i] = parts[b0 + i].x; po[2 * i + 1] = parts[b0 + i].y; }
@@ -1767,8 +1778,9 @@ int contract_impl(Ctx* c, const float* imgs, bool on_device, cryoim_particle* pa
                     launch_build_a8(bb, cc, L->bd, L->csamples.p, L->cS, L->cKpad8, L->corigins.p, O, L->pnorm.p + s0,
                                     L->mulA.p, L->fexp.p + s0, ns, L->amat8.p + (size_t)(s0 - a0) * O * L->cKpad8,
                                     L->stream, po);
-                else
-                    launch_build_a(bb, cc, L->bd, L->csamples.p, L->cS, L->cKpad, L->corigins.p, O, L->pnorm.p + s0, ns,
+                else  // the local form's rows are normalised by |P| (its sections by |CTF S|)
+                    launch_build_a(bb, cc, L->bd, L->csamples.p, L->cS, L->cKpad, L->corigins.p, O,
+                                   (local ? L->pnorm0.p : L->pnorm.p) + s0, ns,
                                    L->amat.p + (size_t)(s0 - a0) * O * L->cKpad, L->stream, po);
             };
             GemmArgmaxArgs g{};
@@ -1819,9 +1831,10 @@ int contract_impl(Ctx* c, const float* imgs, bool on_device, cryoim_particle* pa
                         }
                         CK(cudaMemcpyAsync(L->lcentre.p, cen.data(), sizeof(float) * cen.size(), cudaMemcpyHostToDevice,
                                            L->stream));
-                        CK(launch_slice_bf16_local(ltex.tex, L->p.max_r, L->csamples.p, L->cS, L->cKpad, L->lcentre.p,
+                        CK(launch_slice_bf16_local(ltex.tex, c->cube_r, L->csamples.p, L->cS, L->cKpad, L->lcentre.p,
                                                    lm, opts->local_step, rows, L->bgather.p, L->stream,
-                                                   c->mapcube.p, c->interp_sigma, lpitch));
+                                                   c->mapcube.p, c->interp_sigma, lpitch,
+                                                   L->pctf.p + (size_t)i0 * L->cS, (float)c->ovs));
                     } else {
                         std::vector<int> idx;
                         idx.reserve(rows);
@@ -1934,8 +1947,13 @@ int contract_impl(Ctx* c, const float* imgs, bool on_device, cryoim_particle* pa
             }
             CK(cudaMemcpyAsync(L->kcand.p, hcand.data(), sizeof(float) * nb * k * 5, cudaMemcpyHostToDevice,
                                L->stream));
-            launch_cc_fp64(L->mapcube.p, L->pcband.p, L->bd, L->csamples.p, L->cS, L->kcand.p, k, nb, L->pnorm.p,
-                           L->kpart.p, L->kcc64.p, L->stream, c->interp_sigma);
+            // the FP64 correlations decide the pick (pick = 1) or are returned with the
+            // candidates; a phase-residual pick without candidate output does not read them
+            const bool need_cc64 = opts->pick != 0 || cands != nullptr;
+            if (need_cc64)
+                launch_cc_fp64(L->mapcube.p, L->pcband.p, L->bd, L->csamples.p, L->cS, L->kcand.p, k, nb,
+                               local ? L->pnorm0.p : L->pnorm.p, L->kpart.p, L->kcc64.p, L->stream, c->interp_sigma,
+                               local ? L->pctf.p : nullptr, c->cube_r, (float)c->ovs);
             // Phase-residual rescoring at the particle's own origin (ort_globesearch.f90 scores
             // every view at particle(i)%x, %y) over each selected orientation and its grid
             // neighbours within nbr steps (all of them, or, with nbr_best = m, only those of
@@ -2074,7 +2092,8 @@ int contract_impl(Ctx* c, const float* imgs, bool on_device, cryoim_particle* pa
                     }
                 }
             }
-            CK(cudaMemcpyAsync(hcc64.data(), L->kcc64.p, sizeof(double) * nb * k, cudaMemcpyDeviceToHost,
+            if (need_cc64)
+                CK(cudaMemcpyAsync(hcc64.data(), L->kcc64.p, sizeof(double) * nb * k, cudaMemcpyDeviceToHost,
                                L->stream));
             CK(cudaStreamSynchronize(L->stream));
             for (int i = 0; i < nb; ++i) {
@@ -3337,36 +3356,54 @@ int cryoim_central_sections(void* ctx, const float* ft_re, const float* ft_im, c
     return CRYOIM_OK;
 }
 
-int cryoim_set_reference_map(void* ctx, const float* map3d) {
-    Ctx* c = as_ctx(ctx);
-    int r = check_ready(c, false);
-    if (r) return r;
-    if (!map3d) return fail(CRYOIM_ERR_ARG, "null map");
-    const int nx = c->p.fftsize, R = c->p.max_r;
-    const long n3 = (long)nx * nx * nx, c3 = (long)(2 * R + 3) * (2 * R + 3) * (2 * R + 3);
-    DBuf<float> dmap;
+// The band cube of c->mapreal: frequencies -(cube_r + 1) .. cube_r + 1 of the map's
+// centred transform (ovs 1), or of the map zero-padded to (2 n)^3 (ovs 2: the samples of
+// a section at frequency h sit at 2 h, cube_r = 2 maxR + 1).  Trilinear interpolation of
+// the twice-oversampled transform matches the map's projections far better (noise-free
+// correlation 0.998 against 0.96 at box 128); it removes the bias the interpolation error
+// puts on the local searches' maxima.
+int build_map_cube(Ctx* c) {
+    const int nx = c->p.fftsize, R = c->p.max_r, ovs = c->ovs, m = ovs * nx;
+    const int Rq = ovs == 1 ? R : 2 * R + 1;
+    const long m3 = (long)m * m * m, c3 = (long)(2 * Rq + 3) * (2 * Rq + 3) * (2 * Rq + 3);
     DBuf<float2> work;
-    if ((r = dmap.ensure(n3)) || (r = work.ensure(n3)) || (r = c->mapcube.ensure(c3))) return r;
-    CK(cudaMemcpyAsync(dmap.p, map3d, sizeof(float) * n3, cudaMemcpyHostToDevice, c->stream));
-    launch_map_checker(dmap.p, nx, work.p, c->stream);
+    int r;
+    if ((r = work.ensure(m3)) || (r = c->mapcube.ensure(c3))) return r;
+    if (ovs == 1)
+        launch_map_checker(c->mapreal.p, nx, work.p, c->stream);
+    else
+        launch_lp_pad_checker(c->mapreal.p, nx, work.p, c->stream);
     CK(cudaGetLastError());
     cufftHandle h;
-    CKF(cufftPlan3d(&h, nx, nx, nx, CUFFT_C2C));
+    CKF(cufftPlan3d(&h, m, m, m, CUFFT_C2C));
     cufftResult fr = cufftSetStream(h, c->stream);
     if (fr == CUFFT_SUCCESS) fr = cufftExecC2C(h, (cufftComplex*)work.p, (cufftComplex*)work.p, CUFFT_FORWARD);
     if (fr != CUFFT_SUCCESS) {
         cufftDestroy(h);
         return fail(CRYOIM_ERR_CUDA, "3D forward FFT failed: cufft %d", (int)fr);
     }
-    launch_map_band(work.p, nx, R, c->mapcube.p, c->stream);
+    launch_map_band(work.p, m, Rq, c->mapcube.p, c->stream);
     cudaError_t e = cudaStreamSynchronize(c->stream);
     cufftDestroy(h);
     if (e != cudaSuccess) return fail(CRYOIM_ERR_CUDA, "reference map: %s", cudaGetErrorString(e));
+    c->cube_r = Rq;
     c->map_ready = true;
     c->bmat_ready = false;
     c->bmat8_ready = false;
     c->bmat_c_ready = false;
     return CRYOIM_OK;
+}
+
+int cryoim_set_reference_map(void* ctx, const float* map3d) {
+    Ctx* c = as_ctx(ctx);
+    int r = check_ready(c, false);
+    if (r) return r;
+    if (!map3d) return fail(CRYOIM_ERR_ARG, "null map");
+    const int nx = c->p.fftsize;
+    const long n3 = (long)nx * nx * nx;
+    if ((r = c->mapreal.ensure(n3))) return r;
+    CK(cudaMemcpyAsync(c->mapreal.p, map3d, sizeof(float) * n3, cudaMemcpyHostToDevice, c->stream));
+    return build_map_cube(c);
 }
 
 int cryoim_contract_search(void* ctx, const float* imgs, cryoim_particle* parts, int32_t P,
@@ -3382,16 +3419,24 @@ int cryoim_contract_search_device(void* ctx, const float* d_imgs, cryoim_particl
 int cryoim_set_interpolation(void* ctx, int32_t kind, float sigma) {
     Ctx* c = as_ctx(ctx);
     if (!c) return fail(CRYOIM_ERR_ARG, "null context");
-    if (kind == 0) {
+    if (kind == 0 || kind == 2) {
         sigma = 0.0f;
     } else if (kind != 1 || !(sigma >= 0.25f && sigma <= 2.0f)) {
-        return fail(CRYOIM_ERR_ARG, "interpolation: kind 0 (trilinear) or 1 (Gaussian, sigma 0.25..2 voxels)");
+        return fail(CRYOIM_ERR_ARG,
+                    "interpolation: kind 0 (trilinear), 1 (Gaussian, sigma 0.25..2 voxels) or 2 (trilinear, "
+                    "twice-oversampled transform)");
     }
-    if (sigma != c->interp_sigma) {
+    const int ovs = kind == 2 ? 2 : 1;
+    if (sigma != c->interp_sigma || ovs != c->ovs) {
         c->interp_sigma = sigma;
         c->bmat_ready = false;
         c->bmat8_ready = false;
         c->bmat_c_ready = false;
+        if (ovs != c->ovs) {
+            c->ovs = ovs;
+            int r;
+            if (c->map_ready && (r = build_map_cube(c))) return r;
+        }
     }
     return CRYOIM_OK;
 }

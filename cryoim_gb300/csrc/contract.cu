@@ -122,13 +122,16 @@ __global__ void __launch_bounds__(512) k_slice_bf16(cudaTextureObject_t cube, in
                                                     const int2* __restrict__ samples, int S, int Kpad,
                                                     const float* __restrict__ views, int nom, float step,
                                                     float d2r, long n0, __nv_bfloat162* __restrict__ B,
-                                                    const float2* __restrict__ lin, float gk) {
+                                                    const float2* __restrict__ lin, float gk, float sc) {
     extern __shared__ float2 ssec[];
     __shared__ double sh[32];
     __shared__ float rot[9];
     const long n = n0 + blockIdx.x;
     const int v = (int)(n / nom), io = (int)(n % nom);
-    if (threadIdx.x == 0) euler_mat(views[2 * v], views[2 * v + 1], step * (float)io, d2r, rot);
+    if (threadIdx.x == 0) {
+        euler_mat(views[2 * v], views[2 * v + 1], step * (float)io, d2r, rot);
+        for (int i = 0; i < 9; ++i) rot[i] *= sc;  // cube voxels per frequency unit
+    }
     __syncthreads();
     const float off = (float)(R + 1) + 0.5f;
     float part = 0.0f;
@@ -156,11 +159,18 @@ __global__ void __launch_bounds__(512) k_slice_bf16(cudaTextureObject_t cube, in
 // n = 2 m + 1, orientation (theta_p + (i - m) s, phi_p + (j - m) s, omega_p + (k - m) s)
 // from centre[3 p ..]; particle p's rows start at row p * lpitch (lpitch >= n^3); the
 // row is built exactly as k_slice_bf16 builds it.
+// With pctf (the CTF of each particle at each sample), a row is normalised by |CTF S|
+// instead of |S|: the particle's own grid, so the contraction's score is the unbiased
+// projection-matching correlation sum Re(P conj(CTF S)) / (|P| |CTF S|) (with A rows
+// normalised by |P|), whose maximum lies at the particle's orientation.  Normalising by
+// |S| (a section shared by every particle, as in the global bank) moves the maximum by
+// a fraction of a degree on whole particles and by degrees on the local maps' sections.
 __global__ void __launch_bounds__(512) k_slice_bf16_local(cudaTextureObject_t cube, int R,
                                                           const int2* __restrict__ samples, int S, int Kpad,
                                                           const float* __restrict__ centre, int m, float step,
                                                           float d2r, long n0, __nv_bfloat162* __restrict__ B,
-                                                          const float2* __restrict__ lin, float gk, long lpitch) {
+                                                          const float2* __restrict__ lin, float gk, long lpitch,
+                                                          const float* __restrict__ pctf, float sc) {
     extern __shared__ float2 ssec[];
     __shared__ double sh[32];
     __shared__ float rot[9];
@@ -170,9 +180,11 @@ __global__ void __launch_bounds__(512) k_slice_bf16_local(cudaTextureObject_t cu
     const int p = (int)(q / lpitch), l = (int)(q % lpitch);
     if (l >= nloc) return;  // padding row between particles' grids (never a valid column)
     const int i = l / (n * n), j = (l / n) % n, k = l % n;
-    if (threadIdx.x == 0)
+    if (threadIdx.x == 0) {
         euler_mat(centre[3 * p] + step * (float)(i - m), centre[3 * p + 1] + step * (float)(j - m),
                   centre[3 * p + 2] + step * (float)(k - m), d2r, rot);
+        for (int e = 0; e < 9; ++e) rot[e] *= sc;  // cube voxels per frequency unit
+    }
     __syncthreads();
     const float off = (float)(R + 1) + 0.5f;
     float part = 0.0f;
@@ -184,7 +196,8 @@ __global__ void __launch_bounds__(512) k_slice_bf16_local(cudaTextureObject_t cu
         const float2 val = gk > 0.0f ? gauss_sample(lin, 2 * R + 3, R + 1, x, y, z, gk)
                                      : tex3D<float2>(cube, x + off, y + off, z + off);
         ssec[t] = val;
-        part += val.x * val.x + val.y * val.y;
+        const float cw = pctf ? pctf[(long)p * S + t] : 1.0f;
+        part += cw * cw * (val.x * val.x + val.y * val.y);
     }
     const double nrm = block_sum_double((double)part, sh);
     const float inv = nrm > 0.0 ? (float)(1.0 / sqrt(nrm)) : 0.0f;
@@ -197,24 +210,31 @@ __global__ void __launch_bounds__(512) k_slice_bf16_local(cudaTextureObject_t cu
 
 // FP64 sum over samples of |CTF * P|^2 per particle (the origin shift keeps it); with
 // pc, also the samples CTF * (a, b) themselves in FP64, in sample order.
+// With norm0, also the sum of |P|^2 without the CTF; with pctf, the CTF at each sample.
 __global__ void k_particle_norm(const float2* __restrict__ band, const float* __restrict__ ctf, Band bd,
                                 const int2* __restrict__ samples, int S, double* __restrict__ norm,
-                                double2* __restrict__ pc) {
+                                double2* __restrict__ pc, double* __restrict__ norm0, float* __restrict__ pctf) {
     __shared__ double sh[32];
     const int p = blockIdx.x, W = bd.W, R = bd.max_r;
     const float2* b = band + (long)p * W * W;
     const float* c = ctf ? ctf + (long)p * W * W : nullptr;
-    double acc = 0.0;
+    double acc = 0.0, acc0 = 0.0;
     for (int i = threadIdx.x; i < S; i += blockDim.x) {
         const int2 hk = samples[i];
         const int q = (hk.y + R) * W + (hk.x + R);
         const double cv = c ? (double)c[q] : 1.0;
         const double re = b[q].x * cv, im = b[q].y * cv;
         acc += re * re + im * im;
+        acc0 += (double)b[q].x * b[q].x + (double)b[q].y * b[q].y;
         if (pc) pc[(long)p * S + i] = make_double2(re, im);
+        if (pctf) pctf[(long)p * S + i] = c ? c[q] : 1.0f;
     }
     acc = block_sum_double(acc, sh);
     if (threadIdx.x == 0) norm[p] = acc;
+    if (norm0) {
+        acc0 = block_sum_double(acc0, sh);
+        if (threadIdx.x == 0) norm0[p] = acc0;
+    }
 }
 
 // The origin phase exp(i 2pi/n (sx hx + sy ky)) of a row of A is separable: the block
@@ -435,11 +455,12 @@ constexpr int CC_SPLIT = 4;
 
 __global__ void k_cc_fp64(const float2* __restrict__ cube, const double2* __restrict__ pcband, Band bd,
                           const int2* __restrict__ samples, int S, const float* __restrict__ cand, int k,
-                          double* __restrict__ part, double gk) {
+                          double* __restrict__ part, double gk, const float* __restrict__ pctf, int Rq, double sc) {
     extern __shared__ double2 ctab[];  // [R + 1] per hx, then [2R + 1] per ky
     __shared__ double sh[32];
     __shared__ double rot[9];
-    const int c = blockIdx.x, p = blockIdx.y, sp = blockIdx.z, R = bd.max_r, C = 2 * R + 3, off = R + 1;
+    // R: the band; Rq: the cube's radius (its side C = 2 Rq + 3), sc cube voxels per frequency
+    const int c = blockIdx.x, p = blockIdx.y, sp = blockIdx.z, R = bd.max_r, C = 2 * Rq + 3, off = Rq + 1;
     const float* cd = cand + ((long)p * k + c) * 5;
     if (threadIdx.x == 0) {
         const double d2r = 3.14159265358979323846 / 180.0;
@@ -448,6 +469,7 @@ __global__ void k_cc_fp64(const float2* __restrict__ cube, const double2* __rest
         rot[0] = c1 * c2 * c3 - s1 * s3; rot[1] = -c1 * c2 * s3 - c3 * s1; rot[2] = c1 * s2;
         rot[3] = c2 * c3 * s1 + c1 * s3; rot[4] = -c2 * s1 * s3 + c1 * c3; rot[5] = s1 * s2;
         rot[6] = -c3 * s2;               rot[7] = s2 * s3;                 rot[8] = c2;
+        for (int i = 0; i < 9; ++i) rot[i] *= sc;
     }
     const double h = (double)(bd.nx / 2), sx = cd[3] + h, sy = cd[4] + h;
     const double tpn = 2.0 * 3.14159265358979323846 / (double)bd.nx;
@@ -521,7 +543,8 @@ __global__ void k_cc_fp64(const float2* __restrict__ cube, const double2* __rest
         const double2 pc = pcb[i];
         const double pr = pc.x * cs + pc.y * sn, pi = pc.x * sn - pc.y * cs;
         dot += pr * sr + pi * si;
-        nb += sr * sr + si * si;
+        const double cw = pctf ? (double)pctf[(long)p * S + i] : 1.0;
+        nb += cw * cw * (sr * sr + si * si);
     }
     dot = block_sum_double(dot, sh);
     nb = block_sum_double(nb, sh);
@@ -740,7 +763,7 @@ void free_cube_texture(cudaArray_t arr, cudaTextureObject_t tex) {
 constexpr int SLICE_THREADS = 256;  // threads per section row
 cudaError_t launch_slice_bf16(cudaTextureObject_t cube, int R, const int2* samples, int S, int Kpad,
                               const float* views, int nom, float step, long n0, long count, void* B,
-                              cudaStream_t st, const float2* lin, float sigma) {
+                              cudaStream_t st, const float2* lin, float sigma, float sc) {
     const float gk = (lin && sigma > 0.0f) ? 1.0f / (2.0f * sigma * sigma) : 0.0f;
     size_t sm = (size_t)S * sizeof(float2);
     cudaError_t e = cudaFuncSetAttribute(k_slice_bf16, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
@@ -749,7 +772,7 @@ cudaError_t launch_slice_bf16(cudaTextureObject_t cube, int R, const int2* sampl
         long nb = count - c0 < 65535 ? count - c0 : 65535;
         k_slice_bf16<<<(unsigned)nb, SLICE_THREADS, sm, st>>>(cube, R, samples, S, Kpad, views, nom, step,
                                                    host_angles().deg2rad, n0 + c0,
-                                                   (__nv_bfloat162*)B + c0 * (Kpad / 2), lin, gk);
+                                                   (__nv_bfloat162*)B + c0 * (Kpad / 2), lin, gk, sc);
     }
     return cudaGetLastError();
 }
@@ -759,7 +782,7 @@ cudaError_t launch_slice_bf16(cudaTextureObject_t cube, int R, const int2* sampl
 constexpr int LOCAL_SLICE_THREADS = 64;
 cudaError_t launch_slice_bf16_local(cudaTextureObject_t cube, int R, const int2* samples, int S, int Kpad,
                                     const float* centre, int m, float step, long count, void* B, cudaStream_t st,
-                                    const float2* lin, float sigma, long lpitch) {
+                                    const float2* lin, float sigma, long lpitch, const float* pctf, float sc) {
     if (lpitch <= 0) lpitch = (long)(2 * m + 1) * (2 * m + 1) * (2 * m + 1);
     const float gk = (lin && sigma > 0.0f) ? 1.0f / (2.0f * sigma * sigma) : 0.0f;
     size_t sm = (size_t)S * sizeof(float2);
@@ -770,14 +793,15 @@ cudaError_t launch_slice_bf16_local(cudaTextureObject_t cube, int R, const int2*
         long nb = count - c0 < 65535 ? count - c0 : 65535;
         k_slice_bf16_local<<<(unsigned)nb, LOCAL_SLICE_THREADS, sm, st>>>(cube, R, samples, S, Kpad, centre, m, step,
                                                          host_angles().deg2rad, c0,
-                                                         (__nv_bfloat162*)B + c0 * (Kpad / 2), lin, gk, lpitch);
+                                                         (__nv_bfloat162*)B + c0 * (Kpad / 2), lin, gk, lpitch,
+                                                         pctf, sc);
     }
     return cudaGetLastError();
 }
 
 void launch_particle_norm(const float2* band, const float* ctf, Band bd, const int2* samples, int S,
-                          int B, double* norm, cudaStream_t st, double2* pc) {
-    k_particle_norm<<<B, 256, 0, st>>>(band, ctf, bd, samples, S, norm, pc);
+                          int B, double* norm, cudaStream_t st, double2* pc, double* norm0, float* pctf) {
+    k_particle_norm<<<B, 256, 0, st>>>(band, ctf, bd, samples, S, norm, pc, norm0, pctf);
 }
 
 void launch_build_a(const float2* band, const float* ctf, Band bd, const int2* samples, int S, int Kpad,
@@ -808,11 +832,12 @@ long cc_fp64_scratch(int k, int B) { return (long)k * B * CC_SPLIT * 3; }
 
 void launch_cc_fp64(const float2* cube, const double2* pcband, Band bd, const int2* samples, int S,
                     const float* cand, int k, int B, const double* pnorm, double* scratch, double* out,
-                    cudaStream_t st, float sigma) {
+                    cudaStream_t st, float sigma, const float* pctf, int cube_r, float sc) {
     dim3 g(k, B, CC_SPLIT);
     const size_t sm = sizeof(double2) * (3 * bd.max_r + 2);
     const double gk = sigma > 0.0f ? 1.0 / (2.0 * (double)sigma * (double)sigma) : 0.0;
-    k_cc_fp64<<<g, 256, sm, st>>>(cube, pcband, bd, samples, S, cand, k, scratch, gk);
+    k_cc_fp64<<<g, 256, sm, st>>>(cube, pcband, bd, samples, S, cand, k, scratch, gk, pctf,
+                                  cube_r < 0 ? bd.max_r : cube_r, (double)sc);
     k_cc_fp64_finish<<<(k * B + 127) / 128, 128, 0, st>>>(scratch, k * B, CC_SPLIT, pnorm, k, out);
 }
 

@@ -200,13 +200,21 @@ void free_cube_texture(cudaArray_t arr, cudaTextureObject_t tex);
 // trilinear filtering
 cudaError_t launch_slice_bf16(cudaTextureObject_t cube, int R, const int2* samples, int S, int Kpad,
                               const float* views, int nom, float step, long n0, long count, void* B,
-                              cudaStream_t st, const float2* lin = nullptr, float sigma = 0.0f);
-// Rows of each particle's local grid (k_slice_bf16_local): count = particles x (2 m + 1)^3
+                              cudaStream_t st, const float2* lin = nullptr, float sigma = 0.0f, float sc = 1.0f);
+// (R: the band cube's radius, its side 2 R + 3; sc: cube voxels per frequency unit, 2 for
+// the cube of the map zero-padded to twice its side)
+// Rows of each particle's local grid (k_slice_bf16_local): count = particles x (2 m + 1)^3;
+// pctf (particles x S, launch_particle_norm): rows normalised by |CTF S| (the unbiased
+// projection-matching score, A rows normalised by |P|), else by |S|
 cudaError_t launch_slice_bf16_local(cudaTextureObject_t cube, int R, const int2* samples, int S, int Kpad,
                                     const float* centre, int m, float step, long count, void* B, cudaStream_t st,
-                                    const float2* lin = nullptr, float sigma = 0.0f, long lpitch = 0);
+                                    const float2* lin = nullptr, float sigma = 0.0f, long lpitch = 0,
+                                    const float* pctf = nullptr, float sc = 1.0f);
+// norm: sum |CTF P|^2 per particle; pc: CTF P per sample (FP64); norm0: sum |P|^2; pctf:
+// the CTF at each sample
 void launch_particle_norm(const float2* band, const float* ctf, Band bd, const int2* samples, int S,
-                          int B, double* norm, cudaStream_t st, double2* pc = nullptr);
+                          int B, double* norm, cudaStream_t st, double2* pc = nullptr, double* norm0 = nullptr,
+                          float* pctf = nullptr);
 // Rows (p, o) of A, p < B, o < O; origins: O x 2 (x, y) pixels, absolute, or relative to
 // each particle's own origin poff[p] = (x, y) when poff is given.
 void launch_build_a(const float2* band, const float* ctf, Band bd, const int2* samples, int S, int Kpad,
@@ -221,10 +229,12 @@ void launch_select_topk(const float* topv, const int* topi, int O, int ntiles, i
 // scratch: cc_fp64_scratch(k, B) doubles
 long cc_fp64_scratch(int k, int B);
 // FP64 CC of k candidates per particle; pcband: each particle's CTF x (a, b) per sample in
-// FP64 and pnorm its FP64 norm (launch_particle_norm)
+// FP64 and pnorm its FP64 norm (launch_particle_norm).  With pctf and pnorm = sum |P|^2
+// (norm0): the unbiased score sum Re(P conj(CTF S)) / (|P| |CTF S|)
 void launch_cc_fp64(const float2* cube, const double2* pcband, Band bd, const int2* samples, int S,
                     const float* cand, int k, int B, const double* pnorm, double* scratch, double* out,
-                    cudaStream_t st, float sigma = 0.0f);
+                    cudaStream_t st, float sigma = 0.0f, const float* pctf = nullptr, int cube_r = -1,
+                    float sc = 1.0f);
 
 // ---- learned orientation proposer (learn.cu) ----
 constexpr int LP_NR = 64, LP_NT = 128;   // polar feature: radii over [minR, maxR] x angles over [0, 180)

@@ -23,7 +23,10 @@ def map_cube_full(vol):
     return ft * sg
 
 
-def cc_fp64(orc, p, vol_ft, img, part, cand):
+def cc_fp64(orc, p, vol_ft, img, part, cand, unbiased=False):
+    """The FP64 score of one candidate: sum Re(CTF P conj S) over the half-plane band,
+    normalised by |CTF P| |S| (the global forms, whose sections are shared by all
+    particles) or, unbiased, by |P| |CTF S| (the local form)."""
     n, R, r0 = p.fftsize, p.max_r, p.min_r
     h = n // 2
     sre, sim = orc.central_section(vol_ft.real, vol_ft.imag, *cand[:3], fp="f64")
@@ -35,6 +38,10 @@ def cc_fp64(orc, p, vol_ft, img, part, cand):
     half = ((hx > 0) | ((hx == 0) & (ky > 0))) & (d2 >= r0 * r0) & (d2 <= R * R)
     pr, pi = (a * ctf)[half], (-b * ctf)[half]
     qr, qi = sre[half], sim[half]
+    if unbiased:
+        c = ctf[half]
+        return float(np.sum(pr * qr + pi * qi) /
+                     np.sqrt(np.sum(a[half] ** 2 + b[half] ** 2) * np.sum(c * c * (qr * qr + qi * qi))))
     return float(np.sum(pr * qr + pi * qi) / np.sqrt(np.sum(pr * pr + pi * pi) * np.sum(qr * qr + qi * qi)))
 
 

@@ -4,8 +4,8 @@ the map's band cube for the pass and correlated against the origin grid on the t
 cores (BF16), the top candidates rescored in FP64.  Noise-free particles whose true
 orientation lies on their grid come back within half a grid step of it, at the origin
 next to the truth, from differently centred grids alike; every returned candidate's FP64 correlation equals
-an independent FP64 restatement (oracle central section x oracle-prepared particle, CTF,
-origin shift); passes split across lanes give the same result; bad options are
+an independent FP64 restatement of the unbiased score sum Re(P conj(CTF S)) / (|P| |CTF S|)
+(oracle central section x oracle-prepared particle, CTF, origin shift); passes split across lanes give the same result; bad options are
 refused."""
 import numpy as np
 import pytest
@@ -67,7 +67,7 @@ def test_fp64_scores_match_independent_cc(case, orc):
     vft = map_cube_full(vol)
     for i in range(len(parts)):
         for j in range(3):
-            ref = cc_fp64(orc, p, vft, imgs[i], parts[i], cands[i, j, :5].astype(np.float64))
+            ref = cc_fp64(orc, p, vft, imgs[i], parts[i], cands[i, j, :5].astype(np.float64), unbiased=True)
             assert abs(cands[i, j, 6] - ref) < 1e-6, (i, j, cands[i, j, 6], ref)
             # the BF16 tensor-core score tracks it
             assert abs(cands[i, j, 5] - ref) < 2e-2, (i, j, cands[i, j, 5], ref)
@@ -126,3 +126,53 @@ def test_centred_origin_grid_is_a_window_of_the_absolute_one(case):
     for f in ("theta", "phi", "omega", "x", "y"):
         np.testing.assert_allclose(qc[f][inside], qa[f][inside], atol=1e-5)
     np.testing.assert_allclose(qc["pr"][inside], qa["pr"][inside], rtol=1e-6)
+
+
+def test_oversampled_sections_score_and_land_on_the_truth(case, orc):
+    """Interpolation kind 2 (trilinear on the transform of the map zero-padded to twice
+    its side): every returned candidate's FP64 score equals an independent FP64
+    restatement on the padded transform (numpy, trilinear), and noise-free particles on a
+    grid of half-degree steps land on their true grid point."""
+    import cryoim_gb300 as ci
+    import synth
+    from scipy.ndimage import map_coordinates
+    p, vol, tmpl, timgs, imgs, parts, truth = case
+    n, R, r0 = p.fftsize, p.max_r, p.min_r
+    step, mm = 0.5, 3
+    rng = np.random.default_rng(11)
+    q = parts.copy()
+    off = rng.integers(-(mm - 1), mm, size=(len(parts), 3))
+    q["theta"] = truth[:, 0] + step * off[:, 0]
+    q["phi"] = truth[:, 1] + step * off[:, 1]
+    q["omega"] = truth[:, 2] + step * off[:, 2]
+    with ci.Context(0, p) as ctx:
+        ctx.set_reference_map(vol)
+        ctx.set_interpolation("oversampled")
+        cands = ctx.contract_search(imgs, q, origin_max=2.0, origin_step=0.5, topk=6, pick=1, want_cands=True,
+                                    local_range=mm * step, local_step=step)
+    m = 2 * n
+    pad = np.zeros((m, m, m))
+    pad[n // 2:n // 2 + n, n // 2:n // 2 + n, n // 2:n // 2 + n] = vol
+    F = np.fft.fftshift(np.fft.fftn(np.fft.ifftshift(pad)))
+    h = n // 2
+    ky, hx = np.meshgrid(np.arange(n) - h, np.arange(n) - h, indexing="ij")
+    d2 = hx ** 2 + ky ** 2
+    half = ((hx > 0) | ((hx == 0) & (ky > 0))) & (d2 >= r0 * r0) & (d2 <= R * R)
+    hs = np.stack([hx[half], ky[half], np.zeros(int(half.sum()))]).astype(np.float64)
+    for i in range(len(parts)):
+        a, b, _ = orc.prep_particle(imgs[i], 1, p.imgmask_px, parts["x"][i], parts["y"][i], 0, r0, R, "f64")
+        ctf = orc.ctf2d(n, parts["df1"][i], parts["df2"][i], parts["astigang"][i], p.apix, p.vol, p.cs, p.ampwg,
+                        "f64")
+        for j in range(3):
+            c = cands[i, j].astype(np.float64)
+            X = 2.0 * (synth.euler_mat(*c[:3]) @ hs) + m // 2
+            s = (map_coordinates(F.real, [X[2], X[1], X[0]], order=1) +
+                 1j * map_coordinates(F.imag, [X[2], X[1], X[0]], order=1))
+            aa, bb = orc.centshift(a, b, c[3], c[4], "f64")
+            pr, pi = (aa * ctf)[half], (-bb * ctf)[half]
+            cw = ctf[half]
+            want = np.sum(pr * s.real + pi * s.imag) / np.sqrt(
+                np.sum(aa[half] ** 2 + bb[half] ** 2) * np.sum(cw * cw * np.abs(s) ** 2))
+            assert abs(c[6] - want) < 2e-5, (i, j, c[6], want)
+        err = synth.orientation_error((q["theta"][i], q["phi"][i], q["omega"][i]), truth[i])
+        assert err < 0.5 * step, (i, err)
