@@ -664,14 +664,18 @@ int globesearch(const cryoim_params* p, const R* tmpl, const R* tfcut, const cry
                 int nthreads) {
     int nx = p->fftsize, minR = p->min_r, maxR = p->max_r, nr = maxR - minR + 1;
     long nn = (long)nx * nx;
-    const R step = (R)p->searchstep, d2r = C<R>::deg2rad();
+    const R step = (R)p->searchstep;
     int nth, nph, nom;
     grid_sizes(p->searchstep, &nth, &nph, &nom);
     long per = (long)nom * (2 * nph + 1) * (nth + 1);
     std::vector<R> tort(T * 3);
     for (int i = 0; i < T; ++i) { tort[i * 3] = t[i].theta; tort[i * 3 + 1] = t[i].phi; tort[i * 3 + 2] = t[i].omega; }
     std::vector<int> src = ctf_source(parts, P);
-    Asu<R> asu;
+    // The view set is the reference's, decided in its single precision (ort_globesearch.f90
+    // declares theta, phi, x, y, z real): at theta = 90 degrees cos() rounds below zero in
+    // FP32 and the equator's views are left out, whatever precision scores the kept views.
+    const Asu<float> asu32;
+    const float step32 = p->searchstep, d2r32 = C<float>::deg2rad();
 #ifdef _OPENMP
     if (nthreads > 0) omp_set_num_threads(nthreads);
 #pragma omp parallel for schedule(dynamic, 1)
@@ -691,13 +695,13 @@ int globesearch(const cryoim_params* p, const R* tmpl, const R* tfcut, const cry
         }
         for (int it = 0; it <= nth; ++it) {
             R theta = R(69.0) + step * (R)it;
-            R tmp = theta * d2r;
-            R z = std::cos(tmp), z0 = std::sin(tmp);
+            const float t32 = (69.0f + step32 * (float)it) * d2r32;
+            const float z = std::cos(t32), z0 = std::sin(t32);
             for (int iph = 0; iph <= nph; ++iph) {
                 R phi = step * (R)iph;
-                tmp = phi * d2r;
-                R x = z0 * std::cos(tmp), y = z0 * std::sin(tmp);
-                if (!asu.inside(x, y, z)) continue;
+                const float p32 = (step32 * (float)iph) * d2r32;
+                const float x = z0 * std::cos(p32), y = z0 * std::sin(p32);
+                if (!asu32.inside(x, y, z)) continue;
                 pr_omega(a.data(), b.data(), fcut0.data(), tmpl, tort.data(), tfcut, ctfp, T, nx,
                          minR, maxR, step, nom, theta, phi, R(0), pro.data());
                 std::copy(pro.begin(), pro.end(), pra.begin() + ((long)it * (2 * nph + 1) + (iph + nph)) * nom);

@@ -15,7 +15,8 @@ Projections are taken by synth.project_numpy (FP64 real-space line integrals wit
 geometry of project_template2d.f90), so the inputs do not depend on the GPU and the
 fixture script (which runs the CPU oracle) and the GPU tests see the same images.  The
 projections are spread over a spawn process pool: no worker is forked from a process
-that has touched the GPU.  `fingerprint()` summarises the inputs so a test can check
+that has touched the GPU.  A spawn worker re-imports the caller's main module, so a
+script that calls make() must keep its work under `if __name__ == "__main__":`.  `fingerprint()` summarises the inputs so a test can check
 that it regenerated exactly the images the fixture was made from.
 """
 from __future__ import annotations

@@ -11,8 +11,8 @@ box128 (500 particles of 128^2, 20 templates, 1-degree grid, minR 4 .. maxR 26, 
   * the map reconstruct.f90 makes from the FP32 search's picks against the oracle's map
     from the oracle's picks: FSC >= 0.999 in every shell 1..maxR;
   * BF16 exhaustive contraction and the learned-proposal form (BF16 contraction over the
-    neighbourhoods of the trained proposer's cells): >= 99 % the oracle's orientation,
-    their maps FSC >= 0.999 against the oracle's map.
+    neighbourhoods of the trained proposer's cells, LEARNED_BOX128): >= 99 % the oracle's
+    orientation, their maps FSC >= 0.999 against the oracle's map.
 box256 (16 particles of 256^2, 20 templates, 1-degree grid, minR 7 .. maxR 64, SNR 0.05):
   the same score and orientation checks on every particle; the gate-flip error at this
   size is measured and bounded (a flip moves a score by about 1 / terms).
@@ -151,6 +151,12 @@ def test_box128_fp32_search_and_map_match_oracle(box128):
     assert f.min() >= FSC_MIN, f
 
 
+# The learned form at this configuration: at a 10 A band and SNR 0.1 the proposer's
+# cells are less sharp than at box 256, so it names more of them and the rescoring takes
+# more candidates (64 cells, +-2-step neighbourhoods, top 32, neighbours of the best 4).
+LEARNED_BOX128 = dict(learned=64, proposal_nbr=2, topk=32, nbr_best=4)
+
+
 @pytest.mark.parametrize("form", ["bf16_exhaustive", "learned"])
 def test_box128_contraction_forms_match_oracle(box128, form):
     data, fx = box128
@@ -161,11 +167,13 @@ def test_box128_contraction_forms_match_oracle(box128, form):
         if form == "learned":
             c.learn_train(vol, samples=16384, batch=256, lr=4e-3, seed=s["seed"], snr=s["snr"],
                           df_min=s["df"][0], df_max=s["df"][1], astig_max=0.0, origin_max=s["origin"])
-            kw.update(learned=16, nbr_best=4)
+            kw.update(LEARNED_BOX128)
         q = parts.copy()
         c.contract_search(imgs, q, **kw)
     same = _same(q, fx["pick"])
+    decided = fx["gap"] > 2 * FLIP_TOL["box128"]
     _report("box128", f"{form}_identical_to_oracle", float(same.mean()))
+    _report("box128", f"{form}_decided_identical", float(same[decided].mean()))
     assert same.mean() >= AGREE_MIN, same.mean()
     f = _map_fsc("box128", data, fx, q)
     _report("box128", f"{form}_map_fsc_min", float(f.min()))
