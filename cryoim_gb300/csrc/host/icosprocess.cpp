@@ -17,9 +17,10 @@
 // neighbourhood in grid steps), nbrbest (rescore only the neighbourhoods of the best k
 // candidates), coarse=k (coarse-contraction proposals), learned=k (proposals of the
 // learned proposer: loaded from learnmodel=file if it exists, else trained on
-// learnsamples projections of model3d and saved there), localrange / localstep (the
-// local form: each particle's own grid around its input orientation, picked by FP64
-// correlation).  Output rows are appended after
+// learnsamples projections of model3d and saved there), proposalnbr (the proposals'
+// fine neighbourhood in grid steps), localrange / localstep (the local form: each
+// particle's own grid around its input orientation, picked by FP64 correlation, on
+// sections of the twice-oversampled transform).  Output rows are appended after
 // every chunk, so a run can resume with first=k as with the reference's per-particle
 // writes.
 #include <algorithm>
@@ -44,7 +45,7 @@ const char* kKeys[] = {"apix",         "minRes",       "maxRes",     "imgmask", 
                        "loc_box",      "check"};
 const char* kExt[] = {"device", "batch", "contract", "originmax", "originstep", "topk", "precision", "nbr",
                       "coarse", "nbrbest", "learned", "learnmodel", "learnsamples", "localrange",
-                      "localstep"};
+                      "localstep", "proposalnbr"};
 
 void usage() {
     std::puts(
@@ -59,7 +60,7 @@ void usage() {
         "  mode=5 local refinement into newortfile (Ncycle, templateort, ...)\n"
         "  common: apix imgmask first last imgstck\n"
         "  GPU extensions: device batch contract=y originmax originstep topk precision=bf16|fp8 nbr nbrbest\n"
-        "                  coarse learned learnmodel learnsamples localrange localstep");
+        "                  coarse learned learnmodel learnsamples proposalnbr localrange localstep");
 }
 
 bool yes(const std::string& v) { return !v.empty() && (v[0] == 'y' || v[0] == 'Y'); }
@@ -258,10 +259,12 @@ int main(int argc, char** argv) {
                                 sval("precision", "bf16") == "fp8" ? 1 : 0, ival("nbr", 1), ival("coarse", 0),
                                 ival("learned", 0), ival("nbrbest", 0), fval("localrange", 0.0f),
                                 fval("localstep", 0.25f)};
+        co.proposal_nbr = ival("proposalnbr", 0);
         if (co.local_range > 0.0f) co.pick = 1;  // the local form picks by FP64 correlation
         if (contract) {
             if (map.empty()) return die("contract=y needs model3d", 2);
             if (cryoim_set_reference_map(ctx, map.data())) return die("reference map", 2);
+            if (co.local_range > 0.0f && cryoim_set_interpolation(ctx, 2, 0.0f)) return die("interpolation", 2);
             if (co.learned > 0) {
                 const std::string model = sval("learnmodel", "proposer.bin");
                 std::FILE* f = std::fopen(model.c_str(), "rb");
