@@ -51,10 +51,13 @@ METRIC = "particles/s (box 256), BF16+learned vs plain FP32 GPU at >=99% same or
 FP32_PEAK_TFLOPS_NOMINAL = 152 * 128 * 2 * 2.07e9 / 1e12  # FMA lanes x 2 flop x max SM clock
 FLOPS_PER_TERM = 30.0
 # this library's kernels launched per 64-particle pass of the headline form (ncu launch
-# list): prep, FFT post-processing, CTF, template cuts, norms, features, 4 convolutions,
-# 3 poolings, mix, head, cell top-k, operand A, grouped contraction, distinct selection,
-# FP64 rescoring (2), and two rounds of alpha table, band shift, phase residual
-LAUNCHES_PER_PASS = 28
+# list, cuFFT's own kernels not counted): prep, FFT post-processing, CTF, template cuts,
+# templates x CTF, particle norms, features, 4 convolutions, 3 poolings, mix, head (2
+# forward real transforms, the product, 1 inverse), cell top-k, operand A, grouped
+# contraction, distinct selection, and two rounds of alpha table, band shift, phase
+# residual (the FP64 correlation is not computed for a phase-residual pick without
+# candidate output)
+LAUNCHES_PER_PASS = 29
 # DRAM bytes (read + write) of one GEMM launch (3 particles x 625 origins) from an ncu
 # capture at the 2-degree grid (1.483 GB for 31,320 orientations), scaled to the
 # orientation count: operand B streams once per launch.

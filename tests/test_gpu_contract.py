@@ -173,6 +173,29 @@ def test_proposal_form_picks_the_exhaustive_orientation(run, built, precision):
         assert cp[i, :, 6].max() > cands[i, :, 6].max() - tol, (i, cp[i, :, 6], cands[i, :, 6])
 
 
+def test_proposal_neighbourhood_width(run, built):
+    """proposal_nbr: the proposals' fine neighbourhood; the widths that cover the coarse
+    grid's gaps (+-2 and +-3 fine steps) give the exhaustive pick on these particles, +-1
+    runs, and widths outside 0..4 are refused."""
+    import cryoim_gb300 as ci
+    (p, vol, tmpl, timgs, imgs, parts, truth), q, cands, stats = run
+    with ci.Context(0, p) as ctx:
+        ctx.load_templates(timgs, tmpl)
+        ctx.set_reference_map(vol)
+        for pn in (2, 3):
+            qp = parts.copy()
+            ctx.contract_search(imgs, qp, origin_max=2.0, origin_step=0.5, topk=8, coarse=8, proposal_nbr=pn)
+            for i in range(len(parts)):
+                assert (qp["theta"][i], qp["phi"][i], qp["omega"][i]) == (q["theta"][i], q["phi"][i], q["omega"][i])
+        qp = parts.copy()
+        ctx.contract_search(imgs, qp, origin_max=2.0, origin_step=0.5, topk=8, coarse=8, proposal_nbr=1)
+        assert np.all(qp["pr"] < 999)
+        for bad in (-1, 5):
+            with pytest.raises(ci.CryoimError):
+                ctx.contract_search(imgs, parts.copy(), origin_max=2.0, origin_step=0.5, topk=8, coarse=8,
+                                    proposal_nbr=bad)
+
+
 @pytest.mark.parametrize("form", [dict(), dict(coarse=8)])
 def test_pass_lanes_give_the_same_results(run, built, form):
     """Passes dealt to 1, 2 or 3 lanes (own streams, buffers and host threads) return
