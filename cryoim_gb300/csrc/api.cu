@@ -2023,6 +2023,10 @@ int contract_impl(Ctx* c, const float* imgs, bool on_device, cryoim_particle* pa
                         grp.push_back(make_int4(i, (int)j, (int)(e - j), 0));
                         j = e;
                     }
+                // larger groups first: a block's time grows with its candidates, so the last
+                // wave of blocks is filled with the short ones (the results do not depend on
+                // the order: each group writes its own candidates' scores)
+                std::stable_sort(grp.begin(), grp.end(), [](const int4& x, const int4& y) { return x.z > y.z; });
                 if (!grp.empty()) {
                     if ((r = L->xgroups.ensure(grp.size()))) return r;
                     CK(cudaMemcpyAsync(L->xgroups.p, grp.data(), sizeof(int4) * grp.size(), cudaMemcpyHostToDevice,

@@ -6,7 +6,7 @@
 // section.  The full C is never stored: each (row, 256-column tile) reduces to
 // (max, argmax).
 //
-// Persistent kernel, one CTA per SM, 448 threads:
+// Persistent kernel, one CTA per SM, 704 threads:
 //   warp 0    : TMA producer (one lane) filling a 4-stage ring of 128-row A and 256-row
 //               B tiles of 128 bytes per row (64 BF16 or 128 FP8 elements, 128-byte
 //               swizzle), mbarrier full/empty handshakes (A only when B rows come by
@@ -17,8 +17,8 @@
 //               tile, signals the epilogue;
 //   warps 2-5 : epilogue, one TMEM lane (= output row) per thread: tcgen05.ld 32
 //               columns at a time, running max/argmax, then release the accumulator;
-//   warps 6-13: with B rows by index (the proposal forms' rows, picked from the section
-//               bank), 32 rows of each B tile each, copied with 16-byte cp.async.
+//   warps 6-21: with B rows by index (the proposal forms' rows, picked from the section
+//               bank), 16 rows of each B tile each, copied with 16-byte cp.async.
 // Tiles are visited m-fastest so consecutive CTAs share a B tile through L2.
 // Every wait is bounded (2 s of %globaltimer); a timeout sets *err, the issuer drains
 // its MMAs, the producer waits for its copies, and TMEM is freed before exit.
@@ -40,7 +40,7 @@ constexpr int GM = 128, GN = 256, GKB = 128, NSTAGE = 4;  // GKB: bytes of K per
 constexpr int A_BYTES = GM * GKB, B_BYTES = GN * GKB;
 constexpr int STAGE_BYTES = A_BYTES + B_BYTES;
 constexpr int TMEM_COLS = 512;
-constexpr int NWARP_CORE = 6, NWARP_B = 8;  // producer, issuer, 4 epilogue; B loaders (b_mode 2)
+constexpr int NWARP_CORE = 6, NWARP_B = 16;  // producer, issuer, 4 epilogue; B loaders (b_mode 2)
 // B loaders: cp.async groups (stages) in flight before the oldest is waited for and
 // signalled.  The signal of stage s follows the issue of stage s + B_LAG, which waits for
 // the issuer to free that slot: NSTAGE - 2 leaves the issuer a stage of slack (NSTAGE - 1
@@ -185,8 +185,8 @@ __global__ void __launch_bounds__(NTHREADS, 1)
 
     if (warp >= NWARP_CORE) {
         // B rows by index (b_mode 2; idle otherwise): warp w of the NWARP_B loaders copies
-        // tile rows 32 w .. 32 w + 31, lane: 16-byte chunk p = lane % 8 of rows
-        // 32 w + 4 i + lane / 8 (a row's 128 bytes from 8 adjacent lanes), re-swizzled
+        // tile rows 16 w .. 16 w + 15, lane: 16-byte chunk p = lane % 8 of rows
+        // 16 w + 4 i + lane / 8 (a row's 128 bytes from 8 adjacent lanes), re-swizzled
         // from the bank row's residue to the tile row's.  A stage's copies are one
         // cp.async group; B_LAG groups stay in flight, then the oldest is waited for, made
         // visible to the tensor core (proxy fence) and its stage's full barrier receives
