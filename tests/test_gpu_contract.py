@@ -257,3 +257,21 @@ def test_gaussian_kernel_sections_match_oracle(run, built, orc, sigma):
             assert abs(c[5] - c[6]) < 2e-2, (i, j, c[5], c[6])
         err = synth.orientation_error((qg["theta"][i], qg["phi"][i], qg["omega"][i]), truth[i])
         assert err < 1.5 * p.searchstep, (i, err)
+
+
+def test_rescoring_stats_count_the_scored_candidates(run, built):
+    """cryoim_rescore_stats: with profiling on, the phase-residual rescoring's launches,
+    their time and the candidates they scored (the candidates and, with nbr = 1, their grid
+    neighbours: at least topk per particle); reset by the read."""
+    import cryoim_gb300 as ci
+    (p, vol, tmpl, timgs, imgs, parts, truth), q, cands, stats = run
+    with ci.Context(0, p) as ctx:
+        ctx.load_templates(timgs, tmpl)
+        ctx.set_reference_map(vol)
+        ctx.set_lanes(1)
+        ctx.set_profiling(True)
+        ctx.contract_search(imgs, parts.copy(), origin_max=2.0, origin_step=0.5, topk=8)
+        st = ctx.rescore_stats()
+        assert st["launches"] >= 1 and st["ms"] > 0.0
+        assert st["candidates"] >= 8 * len(parts)
+        assert ctx.rescore_stats()["launches"] == 0
