@@ -1305,7 +1305,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--batch", type=int, default=1024, help="particles per headline step")
     ap.add_argument("--side-batch", type=int, default=64, help="particles per step of the other forms")
-    ap.add_argument("--pr-particles", type=int, default=192,
+    ap.add_argument("--pr-particles", type=int, default=384,
                     help="particles of the agreement check against the FP32 form")
     ap.add_argument("--learn-samples", type=int, default=16384,
                     help="projections the learned proposer is trained on")

@@ -125,15 +125,6 @@ __device__ __forceinline__ float angle_between_est(float cross, float dot, float
     return (dot < 0.0f) ? pi - r : r;
 }
 
-// Kahan summation of the pair (x.x into s.x, x.y into s.y) in packed FP32x2 operations,
-// the same per-component arithmetic as kahan_add.
-__device__ __forceinline__ void kahan_add2(float2& s, float2& c, float2 x) {
-    const float2 y = __fadd2_rn(x, make_float2(-c.x, -c.y));
-    const float2 t = __fadd2_rn(s, y);
-    c = __fadd2_rn(__fadd2_rn(t, make_float2(-s.x, -s.y)), make_float2(-y.x, -y.y));
-    s = t;
-}
-
 __global__ void __launch_bounds__(768, 1) k_pr_omega(PrOmegaArgs a, int nomp, Consts K) {
     extern __shared__ __align__(16) unsigned char smraw[];
     const Band bd = a.bd;
@@ -533,9 +524,11 @@ __global__ void __launch_bounds__(RS_THREADS, 1) k_pr_rescore_s(PrSingleArgs a, 
     const float4* tbc0 = a.tbandc ? a.tbandc + (long)p * T * W * W : nullptr;
     const float* ctfp = a.ctf ? a.ctf + (long)p * W * W : nullptr;
     const int per_t = 60 * nr;
-    float2 fs[RG], fk[RG];  // (PR numerator, weight) sums and their Kahan compensations
+    // (PR numerator, weight) sums: per thread a plain FP32 pair over its ~40 terms of a
+    // candidate (like k_pr_omega's per-line partials), then FP64 across the block
+    float2 fs[RG];
 #pragma unroll
-    for (int g = 0; g < RG; ++g) { fs[g] = make_float2(0.f, 0.f); fk[g] = make_float2(0.f, 0.f); }
+    for (int g = 0; g < RG; ++g) fs[g] = make_float2(0.f, 0.f);
     const int step_j = RS_THREADS / nr, step_iq = RS_THREADS - step_j * nr;
     int i = (int)threadIdx.x / per_t, j = ((int)threadIdx.x - i * per_t) / nr;
     int iq = (int)threadIdx.x - i * per_t - j * nr;
@@ -585,7 +578,7 @@ __global__ void __launch_bounds__(RS_THREADS, 1) k_pr_rescore_s(PrSingleArgs a, 
                 const float2 pc = __fmul2_rn(z, e2c);
                 const float d = angle_between_est(pc.x + pc.y, pd.x + pd.y, K.pi);
                 const float w = fmaf(0.5f, amp1, half2);
-                kahan_add2(fs[g], fk[g], make_float2(d * w, w));
+                fs[g] = __ffma2_rn(make_float2(d, 1.0f), make_float2(w, w), fs[g]);
             }
         }
     }
