@@ -1213,6 +1213,13 @@ def run_local_report(args):
     lctx.set_lanes(LANES)
     lctx.set_reference_map(lmap)
     lctx.set_interpolation("oversampled")
+    # the noisy set also searched at a band to 8 A (the resolution such data support)
+    lp8 = ci.default_params(n, apix=1.0, minRes=50.0, maxRes=8.0, searchstep=1.0, ampwg=0.07,
+                            imgmask=(n // 2 - 2) * 1.0)
+    lctx8 = ci.Context(0, lp8)
+    lctx8.set_lanes(LANES)
+    lctx8.set_reference_map(lmap)
+    lctx8.set_interpolation("oversampled")
     c5 = [np.array([[np.cos(a), -np.sin(a), 0], [np.sin(a), np.cos(a), 0], [0, 0, 1]])
           for a in np.radians(72.0 * np.arange(5))]
 
@@ -1225,9 +1232,11 @@ def run_local_report(args):
               centred_origins=True)
     d_sub = torch.empty((P * 12, n, n), device="cuda:0")
 
-    def run(images_of_vertex):
+    def run(images_of_vertex, sctx=None):
         """Extraction (one call per vertex image set, or one call for all 12 vertices) and
-        the local search of every sub-particle; records in the order (vertex, particle)."""
+        the local search of every sub-particle (by sctx, else lctx); records in the order
+        (vertex, particle)."""
+        sctx = sctx or lctx
         recs, t_extract = [], 0.0
         for k, imgs in images_of_vertex:
             d_imgs = torch.from_numpy(imgs).to("cuda:0")
@@ -1251,11 +1260,11 @@ def run_local_report(args):
         sp["theta"], sp["phi"], sp["omega"] = rec["local_theta0"], rec["local_phi0"], rec["local_omega0"]
         sp["x"], sp["y"] = rec["local_x0"], rec["local_y0"]
         sp["df1"], sp["df2"], sp["astigang"] = rec["df1"], rec["df2"], rec["astigang"]
-        lctx.contract_search(d_sub.data_ptr(), sp[:64].copy(), **kw)  # warm-up (sample lists, texture)
+        sctx.contract_search(d_sub.data_ptr(), sp[:64].copy(), **kw)  # warm-up (sample lists, texture)
         torch.cuda.synchronize()
         ts = time.perf_counter()
         out = sp.copy()
-        lctx.contract_search(d_sub.data_ptr(), out, **kw)
+        sctx.contract_search(d_sub.data_ptr(), out, **kw)
         torch.cuda.synchronize()
         t_search = time.perf_counter() - ts
         # (particle, vertex) of each record: per-vertex calls give P records per vertex;
@@ -1280,6 +1289,8 @@ def run_local_report(args):
         sub = [(k, vert0[k] + (nz if nz is not None else 0.0)) for k in range(12)]
         kept = [(None, full0 + (nz if nz is not None else 0.0))]
         per_snr[name] = {"per-vertex subtraction": run(sub), "12 vertices kept": run(kept)}
+        if nz is not None:
+            per_snr[name]["per-vertex subtraction, band to 8 A"] = run(sub, lctx8)
     res = {"report": "batched localized refinement from whole particles", "particles": P, "sub_particles": P * 12,
            "config": {"particle_box": n0, "apix": 1.0, "sub_box": n, "vertex_z_px": zv, "vertices": 12,
                       "signal": (f"per sub-particle: its vertex region (sphere of radius {rmask:g} px) and the "
@@ -1295,6 +1306,7 @@ def run_local_report(args):
            "phantom_s": t_phantom, "results": per_snr}
     print(json.dumps(res))
     lctx.close()
+    lctx8.close()
     return 0
 
 
