@@ -45,7 +45,7 @@ sys.path.insert(0, ROOT)
 
 WORKLOAD = dict(nx=256, apix=1.5, min_res=50.0, max_res=6.0, searchstep=1.0, ntemplates=20,
                 df=(0.8, 3.5), astig=0.1, snr=0.05, origin=6.0, origin_step=0.5, topk=16,
-                ampwg=0.07, seed=20261205, cycle_particles=10000, learned=16, nbr_best=4, learn_lr=4e-3,
+                ampwg=0.07, seed=20261205, cycle_particles=10000, learned=24, nbr_best=4, learn_lr=4e-3,
                 proposal_nbr=1)
 METRIC = "particles/s (box 256), BF16+learned vs plain FP32 GPU at >=99% same orientation"
 FP32_PEAK_TFLOPS_NOMINAL = 152 * 128 * 2 * 2.07e9 / 1e12  # FMA lanes x 2 flop x max SM clock
