@@ -54,9 +54,9 @@ FLOPS_PER_TERM = 30.0
 # list, cuFFT's own kernels not counted): prep, FFT post-processing, CTF, template cuts,
 # templates x CTF, particle norms, features, 4 convolutions, 3 poolings, mix, head (2
 # forward real transforms, the product, 1 inverse), cell top-k, operand A, grouped
-# contraction, distinct selection, and two rounds of alpha table, band shift, phase
-# residual (the FP64 correlation is not computed for a phase-residual pick without
-# candidate output)
+# contraction, distinct selection, and two rounds (candidates, neighbours of the best
+# four) of alpha table, band shift, phase residual (the FP64 correlation is not computed
+# for a phase-residual pick without candidate output)
 LAUNCHES_PER_PASS = 29
 # DRAM bytes (read + write) of one GEMM launch (3 particles x 625 origins) from an ncu
 # capture at the 2-degree grid (1.483 GB for 31,320 orientations), scaled to the
