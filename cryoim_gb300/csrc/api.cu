@@ -348,6 +348,7 @@ struct Ctx {
     // the local form's unbiased score: per particle of a pass sum |P|^2 and the CTF per sample
     DBuf<double> pnorm0;
     DBuf<float> pctf;
+    DBuf<int> xorient;  // rescoring: each candidate's grid orientation (view * nom + omega index)
     int n_origin = 0;
     float orig_max = -1.0f, orig_step = -1.0f;
     DBuf<float> tilev, xcand, xpr;
@@ -393,6 +394,7 @@ struct Ctx {
         mapcube.release(); mapreal.release(); csamples.release(); bmat.release(); amat.release(); corigins.release();
         topv.release(); kcc.release(); kcand.release(); topi.release(); gerr.release();
         kor.release(); korig.release(); pnorm.release(); kcc64.release(); pnorm0.release(); pctf.release();
+        xorient.release();
         tilev.release(); xcand.release(); xpr.release(); tileo.release(); tileorig.release();
         xalpha.release(); bmat8.release(); amat8.release(); mulA.release(); mulB.release();
         bandmax.release(); fexp.release();
@@ -2004,7 +2006,21 @@ int contract_impl(Ctx* c, const float* imgs, bool on_device, cryoim_particle* pa
                 CK(cudaMemcpyAsync(L->xcand.p, hx.data(), sizeof(float) * hx.size(), cudaMemcpyHostToDevice,
                                    L->stream));
                 CK(cudaMemcpyAsync(L->xcount.p, hcount.data(), sizeof(int) * nb, cudaMemcpyHostToDevice, L->stream));
-                launch_refine_alpha(L->xcand.p, nb, L->tort.p, T, L->ops.p, L->xalpha.p, L->stream, maxc);
+                // the shared-band kernel takes its line angles from the search grid's view table
+                // (the exhaustive search's own); the other kernel from per-candidate tables
+                const bool shared = pr_rescore_shared_band(L->bd, T);
+                if (shared) {
+                    std::vector<int> ho((size_t)nb * maxc, 0);
+                    for (int i = 0; i < nb; ++i)
+                        for (int j = 0; j < maxc; ++j)
+                            ho[(size_t)i * maxc + j] =
+                                sets[i].empty() ? 0 : sets[i][std::min<size_t>(j, sets[i].size() - 1)];
+                    if ((r = L->xorient.ensure(ho.size()))) return r;
+                    CK(cudaMemcpyAsync(L->xorient.p, ho.data(), sizeof(int) * ho.size(), cudaMemcpyHostToDevice,
+                                       L->stream));
+                } else {
+                    launch_refine_alpha(L->xcand.p, nb, L->tort.p, T, L->ops.p, L->xalpha.p, L->stream, maxc);
+                }
                 // every candidate of a particle sits at the particle's origin: shift its band once
                 CK(launch_shift_band(L->band.p, L->xcand.p, maxc, L->bd, nb, L->sband.p, L->stream));
                 PrSingleArgs a{};
@@ -2012,6 +2028,12 @@ int contract_impl(Ctx* c, const float* imgs, bool on_device, cryoim_particle* pa
                 a.tfcut_pstride = tfs; a.ctf = ctfp; a.cand = L->xcand.p; a.alpha = L->xalpha.p; a.T = T;
                 a.bd = L->bd; a.pr = L->xpr.p; a.ncand = maxc; a.sband = L->sband.p; a.ncount = L->xcount.p;
                 a.tbandc = ctfp ? L->tbandc.p : nullptr;
+                if (shared) {
+                    a.valpha = L->alpha.p;
+                    a.corient = L->xorient.p;
+                    a.nom = L->nom;
+                    a.step = L->p.searchstep;
+                }
                 // candidates of a particle sharing a view, in groups (the sets are sorted by
                 // orientation index, so a view's omegas are adjacent)
                 std::vector<int4> grp;

@@ -108,6 +108,14 @@ struct PrSingleArgs {
     const int* ncount = nullptr;    // [B] candidates in use (later slots are skipped), or nullptr
     const float4* tbandc = nullptr; // [B][T][W*W] templates x CTF as (pixel, right neighbour) pairs
                                     // (launch_tband_ctf), or nullptr
+    // the view table of the search grid ([V][T][60], launch_alpha_table) and each candidate's
+    // grid orientation (view * nom + omega index, [B][ncand]): the shared-band rescoring then
+    // takes its line angles from the table and subtracts omega as k_pr_omega does, so that
+    // its terms are the exhaustive search's (alpha is not read)
+    const float2* valpha = nullptr;
+    const int* corient = nullptr;
+    int nom = 0;
+    float step = 0.0f;
 };
 // cal_crosslin_PR for each candidate, its origin shift applied to every tap (k_pr_single)
 cudaError_t launch_pr_single(const PrSingleArgs& a, int B, cudaStream_t st);
@@ -115,6 +123,9 @@ cudaError_t launch_pr_single(const PrSingleArgs& a, int B, cudaStream_t st);
 // candidate slot, count <= pr_rescore_group_size(), 0); requires sband
 cudaError_t launch_pr_rescore_groups(const PrSingleArgs& a, const int4* groups, int ngroups, cudaStream_t st);
 int pr_rescore_group_size();
+// whether launch_pr_rescore_groups runs the shared-band kernel (which reads valpha and
+// corient) for this band and template count, rather than the one that reads alpha
+bool pr_rescore_shared_band(const Band& bd, int T);
 // the templates x each particle's CTF, each pixel stored with its right neighbour (zero
 // past the row's end), so a bilinear sample reads two 16-byte pairs
 cudaError_t launch_tband_ctf(const float2* tband, int T, const float* ctf, const Band& bd, int B, float4* out,

@@ -498,8 +498,12 @@ __global__ void __launch_bounds__(RS_THREADS, 1) k_pr_rescore_s(PrSingleArgs a, 
             const float4 v = sb[(long)row * W + col];
             sbd[row * SP + col] = make_float2(v.x, v.y);
         }
+    // line directions from the view table, as k_pr_omega computes them: the template's
+    // cos/sin of alpha2, the particle's sincos of (alpha1 - omega) for each candidate
+    const int* co = a.corient + (long)p * a.ncand + c0;
+    const float2* va = a.valpha + (long)(co[0] / a.nom) * T * 60;
     for (int q = threadIdx.x; q < T * 60; q += RS_THREADS) {
-        const float2 aa = a.alpha[((long)p * a.ncand + c0) * T * 60 + q];
+        const float2 aa = va[q];
         const bool ok = aa.x < 999.0f && aa.y < 999.0f;
         sval[q] = ok;
         if (ok) {
@@ -510,10 +514,13 @@ __global__ void __launch_bounds__(RS_THREADS, 1) k_pr_rescore_s(PrSingleArgs a, 
     }
     for (int q = threadIdx.x; q < m * T * 60; q += RS_THREADS) {
         const int g = q / (T * 60), r = q - g * T * 60;
-        const float2 aa = a.alpha[((long)p * a.ncand + c0 + g) * T * 60 + r];
-        const float a1 = __fmul_rn(aa.x, K.d2r);
-        spl[2 * q] = cosf(a1);
-        spl[2 * q + 1] = sinf(a1);
+        const float2 aa = va[r];
+        const float womega = __fmul_rn(a.step, (float)(co[g] % a.nom));
+        const float ang = __fmul_rn(__fsub_rn(aa.x, womega), K.d2r);
+        float sn, cs;
+        sincosf(ang, &sn, &cs);
+        spl[2 * q] = cs;
+        spl[2 * q + 1] = sn;
     }
     const float* tfc = a.tfcut + (long)p * a.tfcut_pstride;
     for (int q = threadIdx.x; q < T * nr; q += RS_THREADS) sfc[q] = tfc[q];
@@ -778,7 +785,8 @@ cudaError_t launch_pr_rescore_groups(const PrSingleArgs& a, const int4* groups, 
                       sizeof(int) * a.T * 60;
     // the band in shared memory where it fits beside the tables (W <= ~140 at T = 20)
     const size_t sm_s = sm + sizeof(float2) * (size_t)a.bd.W * rescore_pitch(a.bd.W);
-    if (sm_s + sizeof(double) * 2 * RG * (RS_THREADS / 32) <= 227 * 1024) {
+    if (pr_rescore_shared_band(a.bd, a.T)) {
+        if (!a.valpha || !a.corient || a.nom < 1) return cudaErrorInvalidValue;
         cudaError_t e = cudaFuncSetAttribute(k_pr_rescore_s, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm_s);
         if (e != cudaSuccess) return e;
         k_pr_rescore_s<<<ngroups, RS_THREADS, sm_s, st>>>(a, groups, consts());
@@ -792,6 +800,13 @@ cudaError_t launch_pr_rescore_groups(const PrSingleArgs& a, const int4* groups, 
 }
 
 int pr_rescore_group_size() { return RG; }
+
+bool pr_rescore_shared_band(const Band& bd, int T) {
+    const size_t sm = sizeof(float) * ((size_t)RG * T * 120 + (size_t)T * 120 + (size_t)(T + 1) * bd.nr) +
+                      sizeof(int) * T * 60;
+    const size_t sm_s = sm + sizeof(float2) * (size_t)bd.W * rescore_pitch(bd.W);
+    return sm_s + sizeof(double) * 2 * RG * (RS_THREADS / 32) <= 227 * 1024;
+}
 
 cudaError_t launch_insert(const InsertArgs& a, int B, cudaStream_t st) {
     long total = (long)a.nsamples * a.nsym;
