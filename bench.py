@@ -747,11 +747,36 @@ def run_profile_case(args):
     trained on 2,560 projections, 2 calls; exhaustive-bf16 / exhaustive-fp8: 12
     particles at a 2-degree grid (31,320 orientations, the section bank built once), 2
     calls; fp32: 4 particles of the FP32 phase-residual form, 2 calls; insert: 64
-    particles inserted into a fresh reconstruction, 2 calls."""
+    particles inserted into a fresh reconstruction, 2 calls; local: 16 sub-particles of
+    the local contraction form (128^2 at 1 A/px, +-3 degrees at 0.25 degrees x origins
+    +-4 px at 0.5 px, oversampled sections), 2 calls."""
     import torch
     import cryoim_gb300 as ci
     w = WORKLOAD
     case = args.profile_case
+    if case == "local":
+        import synth
+        lcp = ci.default_params(128, apix=1.0, minRes=50.0, maxRes=4.0, searchstep=1.0, ampwg=w["ampwg"],
+                                imgmask=62.0)
+        lctx = ci.Context(0, lcp)
+        lvol = synth.phantom(128, w["seed"] + 11)
+        nlc = 16
+        limg_c, lparts_c, ltruth_c = synth.make_particles(
+            lvol, nlc, w["seed"] + 12, lambda v, e: lctx.project_templates(v, _as_tmpl(ci, e)), 1.0,
+            df_range=w["df"], astig_max=w["astig"], origin_max=3.0, snr=w["snr"], ampwg=w["ampwg"])
+        lrng2 = np.random.default_rng(w["seed"] + 13)
+        for k, f in enumerate(("theta", "phi", "omega")):
+            lparts_c[f] = ltruth_c[:, k] + lrng2.uniform(-2.5, 2.5, nlc)
+        lctx.set_reference_map(lvol)
+        lctx.set_interpolation("oversampled")
+        d_limg = torch.from_numpy(limg_c).cuda()
+        for _ in range(2):
+            lctx.contract_search(d_limg.data_ptr(), lparts_c.copy(), origin_max=4.0, origin_step=0.5, topk=16,
+                                 pick=1, local_range=3.0, local_step=0.25)
+        torch.cuda.synchronize()
+        print(json.dumps({"profile_case": case, "particles": nlc, "ok": True}))
+        lctx.close()
+        return 0
     step = 2.0 if case.startswith("exhaustive") else w["searchstep"]
     params = make_params(ci, searchstep=step)
     ctx = ci.Context(0, params)
@@ -1327,7 +1352,7 @@ def main():
                     help="override the 0.5 px origin step (small cases for profiler captures only)")
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--profile-case", choices=["learned", "exhaustive-bf16", "exhaustive-fp8", "fp32", "insert"],
+    ap.add_argument("--profile-case", choices=["learned", "exhaustive-bf16", "exhaustive-fp8", "fp32", "insert", "local"],
                     default=None, help="instead of the bench line: a small case for profiler captures")
     ap.add_argument("--precision-report", type=int, default=0, metavar="P",
                     help="instead of the bench line: BF16 and FP8 contraction against FP64 scores and the "

@@ -17,6 +17,8 @@
 // rounds them (separate multiply and add), so the bilinear taps and weights match it.
 #include <cstdio>
 
+#include <type_traits>
+
 #include "geom.cuh"
 #include "kernels.h"
 
@@ -476,6 +478,12 @@ __global__ void __launch_bounds__(512) k_pr_rescore_g(PrSingleArgs a, const int4
 // full warps) was built and measured 1.7x slower (4.72 against 2.79 ms for the four
 // launches of the profile case): its four barriers per template leave the template
 // samples' L2 latency exposed with one block per SM, where the flat loop overlaps it.
+// Measured alternatives of the flat loop on the same 256-particle workload (rescoring
+// time, one lane): the candidate loop with a run-time count and branches on the cuts
+// 1.12x, a per-warp queue of the samples that pass the template cut (full warps in the
+// candidate loop, but a longer shared-memory dependency chain) 1.36x, the template taps
+// fetched one iteration ahead 1.12x (no gain: not latency-bound), 768 threads 1.07x, 512
+// threads 1.34x, branch-free items or two items per iteration 1.07x.
 constexpr int RS_THREADS = 1024;
 __host__ __device__ inline int rescore_pitch(int W) { return W + ((3 - W % 16) + 16) % 16; }
 __global__ void __launch_bounds__(RS_THREADS, 1) k_pr_rescore_s(PrSingleArgs a, const int4* __restrict__ groups,
@@ -531,11 +539,6 @@ __global__ void __launch_bounds__(RS_THREADS, 1) k_pr_rescore_s(PrSingleArgs a, 
     const float4* tbc0 = a.tbandc ? a.tbandc + (long)p * T * W * W : nullptr;
     const float* ctfp = a.ctf ? a.ctf + (long)p * W * W : nullptr;
     const int per_t = 60 * nr;
-    // (PR numerator, weight) sums: per thread a plain FP32 pair over its ~40 terms of a
-    // candidate (like k_pr_omega's per-line partials), then FP64 across the block
-    float2 fs[RG];
-#pragma unroll
-    for (int g = 0; g < RG; ++g) fs[g] = make_float2(0.f, 0.f);
     const int step_j = RS_THREADS / nr, step_iq = RS_THREADS - step_j * nr;
     int i = (int)threadIdx.x / per_t, j = ((int)threadIdx.x - i * per_t) / nr;
     int iq = (int)threadIdx.x - i * per_t - j * nr;
@@ -546,58 +549,78 @@ __global__ void __launch_bounds__(RS_THREADS, 1) k_pr_rescore_s(PrSingleArgs a, 
         while (j >= 60) { j -= 60; ++i; }
     };
     const float2 nxh2 = make_float2(nxh, nxh);
-    for (int q = threadIdx.x; q < T * per_t; q += RS_THREADS, advance()) {
-        const int lj = i * 60 + j;
-        if (!sval[lj]) continue;
-        const float fr = (float)(minR + iq);
-        float re2, im2;
-        if (tbc0)
-            tmpl_sample_pairs(tbc0 + (long)i * W * W, W, offW, nxh, stl[2 * lj], stl[2 * lj + 1], fr, &re2, &im2);
-        else
-            tmpl_sample_cs(a.tband + (long)i * W * W, ctfp, W, offW, nxh, stl[2 * lj], stl[2 * lj + 1], fr, &re2,
-                           &im2);
-        const float amp2 = sqrtf(re2 * re2 + im2 * im2);
-        if (!(amp2 >= sfc[i * nr + iq])) continue;
-        const float cut1 = sfc[T * nr + iq];
-        const float2 fr2 = make_float2(fr, fr), e2 = make_float2(re2, im2), e2c = make_float2(im2, -re2);
-        const float half2 = 0.5f * amp2;
-        const float2 m1 = make_float2(-1.f, -1.f);
+    const int wi = threadIdx.x >> 5, l = threadIdx.x & 31;
+    // The group's candidate count M is a compile-time constant of each instance of the
+    // loop, so the M candidates' terms of one template sample are independent chains that
+    // the compiler interleaves; the two amplitude cuts are selects, not branches (with
+    // ~70 % of the samples passing each cut, a warp runs both sides of such a branch
+    // anyway).  A term that fails a cut leaves the sums unchanged.
+    auto run = [&](auto mc) {
+        constexpr int M = decltype(mc)::value;
+        // (PR numerator, weight) sums: per thread a plain FP32 pair over its ~40 terms of a
+        // candidate (like k_pr_omega's per-line partials), then FP64 across the block
+        float2 fs[M];
 #pragma unroll
-        for (int g = 0; g < RG; ++g) {
-            if (g >= m) break;
-            // k_pr_omega's per-term arithmetic: position by FMA, bilinear as lerps on
-            // (re, im) pairs, amplitude sq * rsqrt(sq), weight 0.5 amp1 + 0.5 amp2
-            const float2 cs = *reinterpret_cast<const float2*>(&spl[2 * ((long)g * T * 60 + lj)]);
-            const float2 xy = __ffma2_rn(fr2, cs, nxh2);
-            const int lx = (int)xy.x, ly = (int)xy.y;
-            const float2 f = __fadd2_rn(xy, make_float2(-(float)lx, -(float)ly));
-            const float2* tp = sbd + (ly * SP + lx - offS);
-            const float2 t00 = tp[0], t10 = tp[1], t01 = tp[SP], t11 = tp[SP + 1];
-            const float2 ax2 = make_float2(f.x, f.x), ay2 = make_float2(f.y, f.y);
-            const float2 v0 = __ffma2_rn(ax2, __ffma2_rn(t00, m1, t10), t00);
-            const float2 v1 = __ffma2_rn(ax2, __ffma2_rn(t01, m1, t11), t01);
-            const float2 z = __ffma2_rn(ay2, __ffma2_rn(v0, m1, v1), v0);
-            const float2 zz = __fmul2_rn(z, z);
-            const float sq = zz.x + zz.y;
-            const float amp1 = sq * rsqrtf(sq);  // NaN for 0: fails the cut
-            if (amp1 >= cut1) {
+        for (int g = 0; g < M; ++g) fs[g] = make_float2(0.f, 0.f);
+        for (int q = threadIdx.x; q < T * per_t; q += RS_THREADS, advance()) {
+            const int lj = i * 60 + j;
+            if (!sval[lj]) continue;
+            const float fr = (float)(minR + iq);
+            float re2, im2;
+            if (tbc0)
+                tmpl_sample_pairs(tbc0 + (long)i * W * W, W, offW, nxh, stl[2 * lj], stl[2 * lj + 1], fr, &re2,
+                                  &im2);
+            else
+                tmpl_sample_cs(a.tband + (long)i * W * W, ctfp, W, offW, nxh, stl[2 * lj], stl[2 * lj + 1], fr,
+                               &re2, &im2);
+            const float amp2 = sqrtf(re2 * re2 + im2 * im2);
+            const bool ok2 = amp2 >= sfc[i * nr + iq];
+            const float cut1 = sfc[T * nr + iq];
+            const float2 fr2 = make_float2(fr, fr), e2 = make_float2(re2, im2), e2c = make_float2(im2, -re2);
+            const float half2 = 0.5f * amp2;
+            const float2 m1 = make_float2(-1.f, -1.f);
+#pragma unroll
+            for (int g = 0; g < M; ++g) {
+                // k_pr_omega's per-term arithmetic: position by FMA, bilinear as lerps on
+                // (re, im) pairs, amplitude sq * rsqrt(sq), weight 0.5 amp1 + 0.5 amp2
+                const float2 cs = *reinterpret_cast<const float2*>(&spl[2 * ((long)g * T * 60 + lj)]);
+                const float2 xy = __ffma2_rn(fr2, cs, nxh2);
+                const int lx = (int)xy.x, ly = (int)xy.y;
+                const float2 f = __fadd2_rn(xy, make_float2(-(float)lx, -(float)ly));
+                const float2* tp = sbd + (ly * SP + lx - offS);
+                const float2 t00 = tp[0], t10 = tp[1], t01 = tp[SP], t11 = tp[SP + 1];
+                const float2 ax2 = make_float2(f.x, f.x), ay2 = make_float2(f.y, f.y);
+                const float2 v0 = __ffma2_rn(ax2, __ffma2_rn(t00, m1, t10), t00);
+                const float2 v1 = __ffma2_rn(ax2, __ffma2_rn(t01, m1, t11), t01);
+                const float2 z = __ffma2_rn(ay2, __ffma2_rn(v0, m1, v1), v0);
+                const float2 zz = __fmul2_rn(z, z);
+                const float sq = zz.x + zz.y;
+                const float amp1 = sq * rsqrtf(sq);  // NaN for 0: fails the cut
                 const float2 pd = __fmul2_rn(z, e2);
                 const float2 pc = __fmul2_rn(z, e2c);
                 const float d = angle_between_est(pc.x + pc.y, pd.x + pd.y, K.pi);
                 const float w = fmaf(0.5f, amp1, half2);
-                fs[g] = __ffma2_rn(make_float2(d, 1.0f), make_float2(w, w), fs[g]);
+                const float2 nf = __ffma2_rn(make_float2(d, 1.0f), make_float2(w, w), fs[g]);
+                const bool ok = ok2 && amp1 >= cut1;
+                fs[g].x = ok ? nf.x : fs[g].x;
+                fs[g].y = ok ? nf.y : fs[g].y;
             }
         }
-    }
-    const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
 #pragma unroll
-    for (int g = 0; g < RG; ++g) {
-        double p1 = (double)fs[g].x, p2 = (double)fs[g].y;
-        for (int o = 16; o > 0; o >>= 1) {
-            p1 += __shfl_xor_sync(0xffffffffu, p1, o);
-            p2 += __shfl_xor_sync(0xffffffffu, p2, o);
+        for (int g = 0; g < M; ++g) {
+            double p1 = (double)fs[g].x, p2 = (double)fs[g].y;
+            for (int o = 16; o > 0; o >>= 1) {
+                p1 += __shfl_xor_sync(0xffffffffu, p1, o);
+                p2 += __shfl_xor_sync(0xffffffffu, p2, o);
+            }
+            if (l == 0) { sh[0][g][wi] = p1; sh[1][g][wi] = p2; }
         }
-        if (l == 0) { sh[0][g][w] = p1; sh[1][g][w] = p2; }
+    };
+    switch (m) {
+        case 1: run(std::integral_constant<int, 1>()); break;
+        case 2: run(std::integral_constant<int, 2>()); break;
+        case 3: run(std::integral_constant<int, 3>()); break;
+        default: run(std::integral_constant<int, RG>()); break;
     }
     __syncthreads();
     if (threadIdx.x < m) {
