@@ -529,7 +529,10 @@ def run_ours(args):
     lcp = ci.default_params(128, apix=1.0, minRes=50.0, maxRes=4.0, searchstep=1.0, ampwg=w["ampwg"],
                             imgmask=62.0)
     lctx = ci.Context(dev, lcp)
-    lctx.set_lanes(LANES)
+    # one pass lane: each grid's row-line slicer CTAs share texture-cache lines between
+    # neighbouring omegas, which other lanes' grids on the same SMs would evict (measured
+    # 3,295 sub-particles/s with one lane, 2,480-2,704 with six)
+    lctx.set_lanes(1)
     lvol = synth.phantom(128, w["seed"] + 11)
     nlc = 128
     limg_c, lparts_c, ltruth_c = synth.make_particles(
@@ -710,6 +713,7 @@ def run_ours(args):
                           "top 16 rescored in FP64, sections from the twice-oversampled transform, SNR %g, "
                           "starting orientations within 2.5 deg per Euler angle of the truth" % w["snr"],
                 "entry": "cryoim_contract_search_device with local_range 3, local_step 0.25",
+                "pass_lanes": 1,
                 "median_error_vs_truth_deg": {"after": float(np.median(lc_err)), "before": float(np.median(lc_err0))},
                 "roofline": dict(gemm_roofline(lc_g, peak_s, "k_gemm_argmax<bf16> (grouped, local grids)",
                                                f"{src} bf16_tflops_sustained; one-lane call, kernel alone"),

@@ -208,6 +208,81 @@ __global__ void __launch_bounds__(512) k_slice_bf16_local(cudaTextureObject_t cu
     }
 }
 
+// The same rows, one CTA per (particle p, i, j) cutting the n rows k = 0 .. n - 1 (the
+// omega steps) in turn: a thread holds its samples (h, k, CTF^2) in registers across the
+// rows and a row's values in registers until its norm is known, so the CTA needs no
+// shared-memory row and the SM's L1 stays large for the texture fetches, which
+// neighbouring omegas share (0.25 degrees moves a sample by a fraction of a voxel).
+// Each row's values, norm and BF16 row are k_slice_bf16_local's; the norm's FP32
+// per-thread partials cover fewer samples (it agrees to FP32 rounding).
+constexpr int LSR_THREADS = 256, LSR_SPT = 8;  // rows of up to 2,048 samples (pairs)
+__global__ void __launch_bounds__(LSR_THREADS) k_slice_bf16_local_rows(
+    cudaTextureObject_t cube, int R, const int2* __restrict__ samples, int S, int Kpad,
+    const float* __restrict__ centre, int m, float step, float d2r, __nv_bfloat162* __restrict__ B,
+    const float2* __restrict__ lin, float gk, long lpitch, const float* __restrict__ pctf, float sc) {
+    extern __shared__ float rots[];  // [n][9]
+    __shared__ double wsum[2][LSR_THREADS / 32];
+    const int n = 2 * m + 1;
+    const int p = blockIdx.y, ij = blockIdx.x;
+    const int i = ij / n, j = ij % n;
+    for (int k = threadIdx.x; k < n; k += LSR_THREADS) {
+        float* rot = rots + 9 * k;
+        euler_mat(centre[3 * p] + step * (float)(i - m), centre[3 * p + 1] + step * (float)(j - m),
+                  centre[3 * p + 2] + step * (float)(k - m), d2r, rot);
+        for (int e = 0; e < 9; ++e) rot[e] *= sc;  // cube voxels per frequency unit
+    }
+    float hx[LSR_SPT], ky[LSR_SPT], cw2[LSR_SPT];
+#pragma unroll
+    for (int s = 0; s < LSR_SPT; ++s) {
+        const int t = threadIdx.x + s * LSR_THREADS;
+        hx[s] = 0.0f;
+        ky[s] = 0.0f;
+        cw2[s] = 0.0f;
+        if (t < S) {
+            const int2 hk = samples[t];
+            hx[s] = (float)hk.x;
+            ky[s] = (float)hk.y;
+            const float cw = pctf ? pctf[(long)p * S + t] : 1.0f;
+            cw2[s] = cw * cw;
+        }
+    }
+    __syncthreads();
+    const float off = (float)(R + 1) + 0.5f;
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    for (int k = 0; k < n; ++k) {
+        const float* rot = rots + 9 * k;
+        const float r0 = rot[0], r1 = rot[1], r3 = rot[3], r4 = rot[4], r6 = rot[6], r7 = rot[7];
+        float2 val[LSR_SPT];
+        float part = 0.0f;
+#pragma unroll
+        for (int s = 0; s < LSR_SPT; ++s) {
+            val[s] = make_float2(0.f, 0.f);
+            if (threadIdx.x + s * LSR_THREADS < S) {
+                const float x = r0 * hx[s] + r1 * ky[s], y = r3 * hx[s] + r4 * ky[s], z = r6 * hx[s] + r7 * ky[s];
+                val[s] = gk > 0.0f ? gauss_sample(lin, 2 * R + 3, R + 1, x, y, z, gk)
+                                   : tex3D<float2>(cube, x + off, y + off, z + off);
+                part += cw2[s] * (val[s].x * val[s].x + val[s].y * val[s].y);
+            }
+        }
+        // norm: FP64 across the block in a fixed order (warps, then the warps' sums)
+        double d = (double)part;
+        for (int o = 16; o > 0; o >>= 1) d += __shfl_xor_sync(0xffffffffu, d, o);
+        if (lane == 0) wsum[k & 1][wid] = d;
+        __syncthreads();  // also orders this row's reads of wsum[k & 1] before row k + 2 writes it
+        double nrm = 0.0;
+#pragma unroll
+        for (int w = 0; w < LSR_THREADS / 32; ++w) nrm += wsum[k & 1][w];
+        const float inv = nrm > 0.0 ? (float)(1.0 / sqrt(nrm)) : 0.0f;
+        const long q = (long)p * lpitch + (long)ij * n + k;
+        __nv_bfloat162* row = B + q * (Kpad / 2);
+#pragma unroll
+        for (int s = 0; s < LSR_SPT; ++s) {
+            const int t = threadIdx.x + s * LSR_THREADS;
+            if (t < Kpad / 2) row[bf16_pair_at(t, q)] = __floats2bfloat162_rn(val[s].x * inv, val[s].y * inv);
+        }
+    }
+}
+
 // FP64 sum over samples of |CTF * P|^2 per particle (the origin shift keeps it); with
 // pc, also the samples CTF * (a, b) themselves in FP64, in sample order.
 // With norm0, also the sum of |P|^2 without the CTF; with pctf, the CTF at each sample.
@@ -785,6 +860,15 @@ cudaError_t launch_slice_bf16_local(cudaTextureObject_t cube, int R, const int2*
                                     const float2* lin, float sigma, long lpitch, const float* pctf, float sc) {
     if (lpitch <= 0) lpitch = (long)(2 * m + 1) * (2 * m + 1) * (2 * m + 1);
     const float gk = (lin && sigma > 0.0f) ? 1.0f / (2.0f * sigma * sigma) : 0.0f;
+    const long n = 2L * m + 1;
+    if (Kpad / 2 <= LSR_THREADS * LSR_SPT && count % lpitch == 0 && n * n <= 65535 && count / lpitch <= 65535) {
+        // the whole grid of each of count / lpitch particles: rows by (p, i, j) lines of omegas
+        dim3 grid((unsigned)(n * n), (unsigned)(count / lpitch));
+        k_slice_bf16_local_rows<<<grid, LSR_THREADS, sizeof(float) * 9 * (size_t)n, st>>>(
+            cube, R, samples, S, Kpad, centre, m, step, host_angles().deg2rad, (__nv_bfloat162*)B, lin, gk, lpitch,
+            pctf, sc);
+        return cudaGetLastError();
+    }
     size_t sm = (size_t)S * sizeof(float2);
     cudaError_t e =
         cudaFuncSetAttribute(k_slice_bf16_local, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
