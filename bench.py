@@ -73,8 +73,9 @@ TENSOR_PIPE_ACTIVE_E4M3 = 0.781
 # a 64-particle pass of the box-256 workload (ncu capture of --profile-case learned: rows
 # copied from the section bank by index, +-1-step proposal neighbourhoods)
 GROUPED_GEMM_TRAFFIC_PER_PASS = 1.783445e9 + 4.284416e6
-# the same for the phase-residual rescoring (mean of the two launches of a pass)
-RESCORE_TRAFFIC_PER_LAUNCH = 0.5 * (0.281961e9 + 3.609344e6 + 0.290479e9 + 3.733504e6)
+# the same for the phase-residual rescoring (mean of the two launches of a pass,
+# profiles/k_pr_rescore_s_box256.md)
+RESCORE_TRAFFIC_PER_LAUNCH = 0.5 * (585.458432e6 + 3.246592e6 + 769.335296e6 + 3.527936e6)
 
 
 
