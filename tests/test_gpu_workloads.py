@@ -158,8 +158,9 @@ def test_box128_fp32_search_and_map_match_oracle(box128):
 
 # The learned form at this configuration: at a 10 A band and SNR 0.1 the proposer's
 # cells are less sharp than at box 256, so it names more of them and the rescoring takes
-# more candidates (64 cells, +-2-step neighbourhoods, top 32, neighbours of the best 4).
-LEARNED_BOX128 = dict(learned=64, proposal_nbr=2, topk=32, nbr_best=4)
+# more candidates (64 cells, +-3-step neighbourhoods, top 32, neighbours of the best 8:
+# 99.4-99.8 % over three training seeds, against 98.8-99.2 % with +-2 steps and the best 4).
+LEARNED_BOX128 = dict(learned=64, proposal_nbr=3, topk=32, nbr_best=8)
 
 
 @pytest.mark.parametrize("form", ["bf16_exhaustive", "learned"])
