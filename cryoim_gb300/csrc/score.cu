@@ -189,7 +189,7 @@ __global__ void __launch_bounds__(768, 1) k_pr_omega(PrOmegaArgs a, int nomp, Co
                     const float2 csn = make_float2(cs, sn), half2c = make_float2(nxh, nxh);
                     const float4* sl = sline + j * nr;
                     float2 acc = make_float2(0.f, 0.f);  // (sum diff*w, sum w) of this line
-#pragma unroll 4
+#pragma unroll 8
                     for (int iq = 0; iq < nr; ++iq) {
                         const float4 e = sl[iq];
                         if (e.z < 0.0f) continue;
