@@ -76,6 +76,8 @@ GROUPED_GEMM_TRAFFIC_PER_PASS = 1.783445e9 + 4.284416e6
 # the same for the phase-residual rescoring (mean of the two launches of a pass,
 # profiles/k_pr_rescore_s_box256.md)
 RESCORE_TRAFFIC_PER_LAUNCH = 0.5 * (585.458432e6 + 3.246592e6 + 769.335296e6 + 3.527936e6)
+# l1tex__throughput (pct of peak, active) of the same capture: the rescoring's limiter
+RESCORE_L1_ACTIVE = 0.5 * (0.806 + 0.824)
 
 
 
@@ -613,7 +615,12 @@ def run_ours(args):
                         "peak_source": "nominal FP32 FMA rate (no measured non-tensor FP32 peak)",
                         "traffic": RESCORE_TRAFFIC_PER_LAUNCH,
                         "traffic_note": "DRAM bytes per launch, ncu capture of --profile-case learned "
-                                        "(mean of the two launches of a 64-particle pass)"}
+                                        "(mean of the two launches of a 64-particle pass)",
+                        "limiter": {"unit": "l1tex__throughput (L1 / shared-memory data pipe)",
+                                    "active_frac": RESCORE_L1_ACTIVE,
+                                    "note": "ncu, profiles/k_pr_rescore_s_box256.md: the four shared-memory "
+                                            "taps of each term and the template pairs from L1 keep the "
+                                            "data pipe busy; the FP32 pipe is not the bound"}}
 
     def gemm_roofline(g, peak, kernel, src_note):
         a = g["gemm_flops"] / max(g["gemm_ms"], 1e-9) / 1e9
