@@ -124,21 +124,23 @@ def make_data(ci, nparticles: int, projector):
 
 
 class ClockSampler:
-    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+    """nvidia-smi clocks and throttle reasons sampled every 100 ms.  The sampler is started
+    ahead of the timed region (nvidia-smi takes a moment to come up) and summary() keeps
+    the samples that arrived between begin() and end(): the timed region itself."""
 
     Q = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
          "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
          "clocks_event_reasons.sw_power_cap")
 
-    def __init__(self, index: int):
+    def __init__(self, index: int, cmd=None):
         self.index, self.rows, self.proc = index, [], None
+        self.cmd = cmd or ["nvidia-smi", "-i", str(index), f"--query-gpu={self.Q}",
+                           "--format=csv,noheader,nounits", "-lms", "100"]
+        self.t0 = self.t1 = None
 
-    def __enter__(self):
+    def start(self):
         try:
-            self.proc = subprocess.Popen(
-                ["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.Q}",
-                 "--format=csv,noheader,nounits", "-lms", "200"],
-                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.proc = subprocess.Popen(self.cmd, stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
             self.t = threading.Thread(target=self._read, daemon=True)
             self.t.start()
         except Exception:
@@ -149,26 +151,36 @@ class ClockSampler:
         for line in self.proc.stdout:
             parts = [x.strip() for x in line.split(",")]
             if len(parts) >= 7:
-                self.rows.append(parts)
+                self.rows.append((time.perf_counter(), parts))
 
-    def __exit__(self, *exc):
+    def begin(self):
+        self.t0 = time.perf_counter()
+
+    def end(self):
+        self.t1 = time.perf_counter()
+
+    def stop(self):
         if self.proc:
             self.proc.terminate()
             try:
                 self.proc.wait(timeout=5)
             except Exception:
                 self.proc.kill()
+            self.t.join(timeout=5)
 
     def summary(self):
-        if not self.rows:
-            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unavailable"]}
+        t0 = self.t0 if self.t0 is not None else -float("inf")
+        t1 = self.t1 if self.t1 is not None else float("inf")
+        rows = [r for (t, r) in self.rows if t0 <= t <= t1]
+        if not rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unavailable"], "samples": 0}
         num = lambda s: s.replace(".", "", 1).isdigit()
-        sm = [float(r[0]) for r in self.rows if num(r[0])]
-        mx = [float(r[1]) for r in self.rows if num(r[1])]
+        sm = [float(r[0]) for r in rows if num(r[0])]
+        mx = [float(r[1]) for r in rows if num(r[1])]
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
-        reasons = sorted({names[k] for r in self.rows for k in range(4) if r[3 + k].lower() == "active"})
+        reasons = sorted({names[k] for r in rows for k in range(4) if r[3 + k].lower() == "active"})
         return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": max(mx) if mx else None,
-                "reasons": reasons, "samples": len(self.rows)}
+                "reasons": reasons, "samples": len(rows)}
 
 
 def asu_views(step: float):
@@ -375,7 +387,7 @@ def run_ours(args):
             torch.distributed.barrier()
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         if sampler is not None:
-            sampler.__enter__()
+            sampler.begin()
         e0.record(stream)
         out = None
         for _ in range(steps):
@@ -383,7 +395,7 @@ def run_ours(args):
         e1.record(stream)
         torch.cuda.synchronize()
         if sampler is not None:
-            sampler.__exit__(None, None, None)
+            sampler.end()
         return e0.elapsed_time(e1), out
 
     def search_step(dev_ptr=True, n=B, **kw):
@@ -402,14 +414,15 @@ def run_ours(args):
     train_ms = lst["seconds"] * 1000.0
 
     # ---- headline: BF16 contraction on the learned proposer's neighbourhoods ----
+    clk = ClockSampler(dev).start()  # running before the timed region begins
     for _ in range(args.warmup):
         search_step(**lopts)
     st0 = ctx.contract_stats()  # section build time (first call) and reset
     ctx.set_profiling(True)
-    clk = ClockSampler(dev)
     torch.cuda.nvtx.range_push("headline")
     ms, _ = timed_steps(lambda: search_step(**lopts), args.steps, clk)
     torch.cuda.nvtx.range_pop()
+    clk.stop()
     gst_lanes = ctx.contract_stats()
     ctx.rescore_stats()  # reset: the rescoring is timed with one lane below
     ctx.set_profiling(False)
