@@ -70,3 +70,26 @@ def test_reconstruction_correlates_with_phantom(orc):
     band = np.sqrt(x ** 2 + y ** 2 + z ** 2) <= p.max_r - 2
     c = np.abs(np.vdot(F1[band], F2[band])) / np.linalg.norm(F1[band]) / np.linalg.norm(F2[band])
     assert c > 0.5, c
+
+
+def test_view_set_is_decided_in_fp32(orc):
+    """ort_globesearch.f90:7-8,70-78 tests the asymmetric unit in `real`: at theta = 90
+    degrees cos rounds to -4.4e-8 in FP32, so the equator's views are never searched.
+    The FP64 oracle makes the same decision in FP32: the views it searches are exactly
+    those of an independent numpy restatement of the FP32 test (bench.asu_views)."""
+    import os
+    import sys
+    sys.path.insert(0, os.path.dirname(os.path.dirname(os.path.abspath(__file__))))
+    import bench
+    step = 3.0  # 69 + 7 x 3 = 90: the equator is on this grid
+    p, vol, tmpl, timgs, imgs, parts, truth = small_case(P=1, step=step)
+    tm, tf = orc.load_templates(timgs, tmpl, p, "f64")
+    pra = orc.globesearch(p, tm, tf, tmpl, imgs, parts.copy(), want_pr_array=True, fp="f64")[0]
+    searched = pra.min(axis=-1) < 999.0
+    nph = (searched.shape[1] - 1) // 2
+    want = np.zeros_like(searched)
+    for th, ph in bench.asu_views(step):
+        want[int(round((th - 69.0) / step)), int(round(ph / step)) + nph] = True
+    assert np.array_equal(searched, want)
+    assert not searched[int(round((90.0 - 69.0) / step))].any()
+    assert searched.sum() > 0
