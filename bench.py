@@ -55,9 +55,10 @@ FLOPS_PER_TERM = 30.0
 # templates x CTF, particle norms, features, 4 convolutions, 3 poolings, mix, head (2
 # forward real transforms, the product, 1 inverse), cell top-k, operand A, grouped
 # contraction, distinct selection, and two rounds (candidates, neighbours of the best
-# four) of alpha table, band shift, phase residual (the FP64 correlation is not computed
-# for a phase-residual pick without candidate output)
-LAUNCHES_PER_PASS = 29
+# four) of band shift and phase residual (the line angles come from the grid's view
+# table, built once per template set; the FP64 correlation is not computed for a
+# phase-residual pick without candidate output)
+LAUNCHES_PER_PASS = 27
 # DRAM bytes (read + write) of one GEMM launch (3 particles x 625 origins) from an ncu
 # capture at the 2-degree grid (1.483 GB for 31,320 orientations), scaled to the
 # orientation count: operand B streams once per launch.
