@@ -82,6 +82,17 @@ RESCORE_L1_ACTIVE = 0.5 * (0.806 + 0.824)
 
 
 
+def grouped_algorithmic_bytes(g, origins, particles=64):
+    """Algorithmic bytes of one grouped-contraction launch from the library's counters
+    (cryoim_contract_stats): operand A of the pass (particles x origins BF16 rows) plus
+    each listed bank row once, the listed rows from the counted FLOPs
+    (2 x origins x rows x K per particle).  None without a launch."""
+    if not g.get("gemm_launches") or not g.get("kpad"):
+        return None
+    rows = g["gemm_flops"] / g["gemm_launches"] / (2.0 * origins * g["kpad"])
+    return (float(particles) * origins + rows) * g["kpad"] * 2.0
+
+
 def rank_env():
     return (int(os.environ.get("RANK", "0")), int(os.environ.get("WORLD_SIZE", "1")),
             int(os.environ.get("LOCAL_RANK", "0")))
@@ -650,8 +661,11 @@ def run_ours(args):
                                 achieved_in_timed_steps_note=f"{LANES} lanes: each launch's event time includes the "
                                 "overlapping kernels of the other lanes",
                                 traffic=GROUPED_GEMM_TRAFFIC_PER_PASS * min(1.0, B / 64.0),
-                                traffic_note="DRAM bytes per launch (64-particle pass), ncu capture of a launch "
-                                "of the same shape",
+                                traffic_note="DRAM bytes of one launch (64-particle pass) from an ncu capture of "
+                                "--profile-case learned with 16 learned cells, whose lists hold fewer rows "
+                                "than this run's 24-cell lists (algorithmic_bytes_per_launch is this run's)",
+                                algorithmic_bytes_per_launch=grouped_algorithmic_bytes(
+                                    gst, (int(round(2 * w["origin"] / w["origin_step"])) + 1) ** 2),
                                 note="the grouped fine contraction of the headline form; its launches are "
                                 "small (each particle's 625 origins x its few hundred listed "
                                 "orientations, copied from the section bank by index), and the step is "

@@ -1,5 +1,7 @@
-"""The bench's clock sampler keeps the samples of the timed window only (CPU: injected
-samples and a fake sampler command stand in for nvidia-smi)."""
+"""Host-side pieces of bench.py on the CPU: the clock sampler keeps the samples of the
+timed window only (injected samples and a fake sampler command stand in for
+nvidia-smi), and the grouped contraction's algorithmic bytes follow from the library's
+counters."""
 import os
 import sys
 import time
@@ -46,3 +48,11 @@ def test_summary_without_a_sampler_says_so():
     clk.stop()
     s = clk.summary()
     assert s["samples"] == 0 and s["reasons"] == ["unavailable"]
+
+
+def test_grouped_algorithmic_bytes():
+    # 64 particles x 625 origins against 900 listed rows each, K = 12,736, two launches
+    g = {"gemm_launches": 2, "kpad": 12736, "gemm_flops": 2 * (64 * 2.0 * 625 * 900 * 12736)}
+    want = (64 * 625 + 64 * 900) * 12736 * 2.0
+    assert abs(bench.grouped_algorithmic_bytes(g, 625) - want) < 1e-6 * want
+    assert bench.grouped_algorithmic_bytes({"gemm_launches": 0, "kpad": 0, "gemm_flops": 0.0}, 625) is None
