@@ -10,17 +10,20 @@ Synthetic and seeded: a phantom of Gaussian blobs placed by the 60 icosahedral
 rotations plus a shell (the reference map), projected at random orientations; the
 reference names no public dataset.
 
-A step is one call of cryoim_contract_search_device over one batch of particles:
-particle transforms, CTF and origin ramps, the BF16 contraction against every
-orientation's central section with a fused argmax, top-16 selection, FP64 and
-phase-residual rescoring.  The central sections (operand B) are built once per map and
-reused by every particle of a refinement cycle; each step is charged its pro-rata share
-of that build for a 10,000-particle cycle.  `value` = particles/s with images resident
-in HBM; `e2e` = the same call with pinned host images, host->device copies in the timed
-region.  The L2 is flushed (256 MiB write) before every timed step.  The FP32 form
-(cryoim_globesearch_device, the drop-in replacement of ort_globesearch.f90) is timed
-on the first 16 particles of the same set, and the two forms' chosen orientations are
-compared.
+A step is one call of cryoim_contract_search_device over a batch of 1,024 particles in
+the headline form: particle transforms, CTF and origin ramps, the learned proposer's 24
+best cells per particle, the BF16 contraction of their +-1-step grid neighbourhoods
+(section rows read by index from the bank) with a fused argmax, the top-16 distinct
+orientations and the grid neighbours of the best 4 rescored by phase residual.  The
+central sections (operand B) are built once per map and the proposer is trained once per
+map; each step is charged its pro-rata share of both for a 10,000-particle cycle.
+`value` = particles/s with images resident in HBM; `e2e` = the same call with pinned host
+images, host->device copies in the timed region.  The L2 is flushed (256 MiB write)
+before every timed step.  The FP32 form (cryoim_globesearch_device, the drop-in
+replacement of ort_globesearch.f90) is timed on 384 particles of the same set, the
+exhaustive BF16 and FP8 contraction forms and the other proposal forms on smaller
+batches (--side-batch), and every form's chosen orientations are compared with the FP32
+form's on those 384 particles.
 
 --impl reference times the reference algorithm's CPU restatement (the oracle port of
 the phase-residual search, FP32 in the Fortran's operation order) on every usable host
